@@ -1,0 +1,357 @@
+#!/usr/bin/env python3
+"""Pressure-correction PCG benchmark on GB300.
+
+Workload (one step = one solve to 1e-8 relative residual):
+  256^3 hex box (16,777,216 cells, 7-point CSR, 117,047,296 nnz),
+  variable-coefficient Poisson: k_c = exp(N(0,1)) per cell (seed 42),
+  harmonic-averaged to faces through aP = 1/k, Dirichlet p' = 0 on x = 0
+  (PressureOutlet), walls elsewhere, rhs N(0,1) in FP64.  The matrix is
+  assembled on the device by the library's face-loop assembly.
+  value  = time of one mixed-precision (FP32 inner, FP64 residual /
+           reductions / x) Jacobi-PCG solve, inputs resident in HBM;
+  fp64   = time of the plain FP64 Jacobi-PCG solve of the same system;
+  e2e    = the mixed solve through the C ABI with host buffers
+           (ILinearSolver::solve(A, b, x) semantics: CSR + b copied in,
+           preconditioner set up, x copied out).
+Every matrix and vector is far larger than the 129 MB L2, so no flush is
+needed between steps.
+
+`--impl reference` times the reference CG (CGSolver::solve,
+src/solver/LinearSolvers.cpp:420-451) on the host: the compiled reference
+when oracle/_ref exists, otherwise the oracle's C restatement of it, on a
+bounded number of iterations of the same system, scaled to the iteration
+count of the full solve.
+"""
+from __future__ import annotations
+
+import argparse
+import csv
+import io
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "PCG time to 1e-8 rel-res, mixed vs plain FP64 on 1 GB300; SpMV HBM GB/s"
+SEED = 42
+# FP64 Jacobi-PCG iteration count of the seeded system above, by side length
+# (the device FP64 solve reproduces CGSolver's count; recorded from this
+# benchmark's own FP64 leg).  The reference leg scales its bounded sample by it.
+FP64_ITERATIONS = {}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256, help="box side (cells per direction)")
+    ap.add_argument("--tol", type=float, default=1e-8)
+    ap.add_argument("--max-iterations", type=int, default=50000)
+    ap.add_argument("--fp64-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work per baseline sample")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def rank_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                         stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.3)
+        self.proc.terminate()
+        try:
+            self.proc.wait(5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r for r in csv.reader(io.StringIO(self.f.read())) if len(r) >= 9]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx = float(r[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+# ------------------------------------------------------------------ CPU baseline (oracle / compiled reference)
+def cpu_cg_sample(rp, ci, v, b, seconds: float, use_ref: bool):
+    """Time the reference CG on a bounded number of iterations; returns
+    (seconds per iteration, iterations run, kind)."""
+    from oracle import oracle as O
+
+    if use_ref and O.RefLib.available():
+        R = O.RefLib()
+        run = lambda k: R.cg(rp, ci, v, b, 0, 0.0, k)  # noqa: E731
+        kind = "reference"
+    else:
+        run = lambda k: O.cg(rp, ci, v, b, 0, 0.0, k)  # noqa: E731
+        kind = "port"
+    t = time.perf_counter()
+    run(2)
+    t2 = (time.perf_counter() - t) / 2.0
+    k = int(max(3, min(2000, seconds / max(t2, 1e-6))))
+    t = time.perf_counter()
+    run(k)
+    el = time.perf_counter() - t
+    return el / k, k, kind
+
+
+# ------------------------------------------------------------------ workload
+def build_workload(n: int, ctx):
+    import simall_gb300 as sg
+    from simall_gb300 import workloads as W
+
+    mesh = sg.cartesian(n, n, n)
+    aP, phi, rhs = W.varcoef_inputs(mesh, seed=SEED)
+    ps = sg.PressureSystem(mesh, W.X0_OUTLET, ctx=ctx)
+    ps.assemble(1.0, aP, phi)
+    ctx.synchronize()
+    return mesh, ps, rhs
+
+
+def solver_for(sg, ctx, ps, precision, tol, maxit):
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                tolerance=tol, maxIterations=maxit)
+    s = sg.GpuCGSolver(cfg, precision=precision, ctx=ctx)
+    from simall_gb300._lib import check
+    check(s.L.simall_solver_use_pressure_system(s.handle, ps.handle), ctx.handle)
+    return s
+
+
+def time_kernel(s, k, reps=20):
+    import ctypes as C
+    from simall_gb300._lib import check
+    ms = C.c_double()
+    by = C.c_double()
+    check(s.L.simall_solver_time_kernel(s.handle, k, reps, C.byref(ms), C.byref(by)), s.ctx.handle)
+    return ms.value, by.value
+
+
+def run_ours(a, rank, world, local):
+    import torch
+
+    import simall_gb300 as sg
+
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ctx = sg.Context(local)
+    t0 = time.perf_counter()
+    mesh, ps, rhs = build_workload(a.n, ctx)
+    setup_s = time.perf_counter() - t0
+    dev = torch.device("cuda", local)
+    b = torch.from_numpy(rhs).to(dev)
+    x = torch.empty_like(b)
+    xm = torch.empty_like(b)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    s64 = solver_for(sg, ctx, ps, sg.Precision.FP64, a.tol, a.max_iterations)
+    smx = solver_for(sg, ctx, ps, sg.Precision.MIXED, a.tol, a.max_iterations)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(solver, out, steps):
+        barrier()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        l0 = ctx.kernel_launches
+        e0.record(stream)
+        for _ in range(steps):
+            solver.solve_into(b, out)
+        e1.record(stream)
+        e1.synchronize()
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if world > 1:
+            tt = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+            ms = float(tt.item())
+        return ms, ctx.kernel_launches - l0
+
+    # warm-up: W mixed solves, one FP64 solve
+    for _ in range(a.warmup):
+        smx.solve_into(b, xm)
+    s64.solve_into(b, x)
+    clk = ClockSampler(local)
+    clk.start()
+    mixed_ms, launches = timed(smx, xm, a.steps)
+    st_mx = smx.stats
+    mx_iters, mx_updates, mx_true = st_mx.iterations, st_mx.reliable_updates, st_mx.true_residual
+    fp64_ms, _ = timed(s64, x, a.fp64_steps)
+    clocks = clk.stop()
+    fp64_iters, fp64_res = s64.stats.iterations, s64.stats.true_residual
+    xmn, x64 = xm.double().cpu().numpy(), x.cpu().numpy()
+    err_vs_fp64 = float(np.linalg.norm(xmn - x64) / np.linalg.norm(x64))
+
+    # per-kernel CUDA-event timings (roofline)
+    peak, peak_kind = measured_peaks()
+    kern = {}
+    for name, solver, k in [("mixed_spmv_pq", smx, 4), ("mixed_update", smx, 5), ("mixed_dir", smx, 6),
+                            ("fp64_spmv", s64, 0), ("fp64_spmv_pap", s64, 1), ("fp64_update", s64, 2),
+                            ("fp64_dir", s64, 3)]:
+        ms, by = time_kernel(solver, k)
+        kern[name] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6}
+    # dominant kernel of the mixed solve: largest time per iteration
+    dom = max(("mixed_spmv_pq", "mixed_update", "mixed_dir"), key=lambda k: kern[k]["ms"])
+    rl = {"bound": "hbm", "kernel": dom, "achieved": round(kern[dom]["gbs"], 1), "peak": peak,
+          "unit": "GB/s", "frac": round(kern[dom]["gbs"] / peak, 4), "traffic": None,
+          "peak_source": f"{peak_kind} hbm_gbs"}
+
+    # e2e: C ABI with host buffers (matrix + b in, x out, setup inside)
+    rp, ci = ps.pattern()
+    vals, _ = ps.download()
+    e2e_solver = sg.GpuCGSolver(sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG,
+                                                      preconditioner=sg.PreconditionerKind.Jacobi,
+                                                      tolerance=a.tol, maxIterations=a.max_iterations),
+                                precision=sg.Precision.MIXED, ctx=ctx)
+    A = sg.CSRMatrix(rp, ci, vals)
+    xh = np.zeros(len(rhs))
+    e2e_solver.solve(A, rhs, xh)  # warm
+    barrier()
+    t = time.perf_counter()
+    for _ in range(a.e2e_steps):
+        e2e_solver.solve(A, rhs, xh)
+    e2e_s = (time.perf_counter() - t) / a.e2e_steps
+    h2d = rp.nbytes + ci.nbytes + vals.nbytes + rhs.nbytes
+    d2h = xh.nbytes
+
+    out = {
+        "metric": METRIC, "value": round(mixed_ms / 1e3, 6), "unit": "s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": round(mixed_ms, 3), "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
+        "config": {"workload": f"varcoef Poisson {a.n}^3 (k=exp(N(0,1)) harmonic faces, Dirichlet x=0), "
+                               f"Jacobi-PCG to {a.tol:g}", "cells": int(mesh.n_cells), "nnz": int(ps.nnz),
+                   "seed": SEED, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
+        "fp64": {"value": round(fp64_ms / 1e3, 6), "unit": "s", "iterations": int(fp64_iters),
+                 "true_residual": fp64_res},
+        "mixed": {"iterations": int(mx_iters), "reliable_updates": int(mx_updates), "true_residual": mx_true,
+                  "rel_diff_vs_fp64": err_vs_fp64},
+        "speedup_vs_fp64": round(fp64_ms / mixed_ms, 3),
+        "spmv_gbs": {"fp64_csr": round(kern["fp64_spmv"]["gbs"], 1), "fp32_inner": round(kern["mixed_spmv_pq"]["gbs"], 1)},
+        "kernels": {k: {"ms": round(v["ms"], 4), "gbs": round(v["gbs"], 1)} for k, v in kern.items()},
+        "roofline": rl,
+        "e2e": {"value": round(e2e_s, 6), "unit": "s", "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": int(launches),
+        "clocks": clocks,
+        "setup_seconds": round(setup_s, 2),
+    }
+    if rank == 0 and world == 1 and not a.no_cpu_baseline:
+        per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
+        out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,
+                               "sample": f"{k} FP64 Jacobi-CG iterations of this {a.n}^3 system on 1 host core "
+                                         f"({per_it * 1e3:.1f} ms/iteration), scaled to the {fp64_iters} iterations "
+                                         f"of the full solve"}
+    if rank == 0:
+        print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def run_reference(a, rank, world):
+    """The reference CG on the host: compiled reference if present, else the
+    oracle's restatement; bounded samples scaled to the full iteration count."""
+    if rank != 0:
+        return
+    from oracle import oracle as O
+    from simall_gb300 import workloads as W
+
+    # input system: the oracle's own mesh, sparsity and assembly
+    m = O.cartesian_mesh(a.n, a.n, a.n)
+    rng = np.random.default_rng(SEED + 2)
+    k = np.exp(rng.standard_normal(m.nC))
+    rhs = rng.standard_normal(m.nC)
+    rp, ci = O.build_sparsity(m)
+    v, _, _ = O.assemble(m, rp, ci, [1], 1.0, 1.0 / k, np.zeros(m.nF))
+    del m
+    iters = FP64_ITERATIONS.get(a.n)
+    per = []
+    kind = "port"
+    for i in range(a.warmup + a.steps):
+        t, kk, kind = cpu_cg_sample(rp, ci, v, rhs, a.cpu_seconds / 2, use_ref=True)
+        if i >= a.warmup:
+            per.append(t)
+    per_it = float(np.mean(per))
+    scale = iters if iters else 1
+    val = per_it * scale
+    sample = (f"{kk} FP64 Jacobi-CG iterations per step on 1 host core ({per_it * 1e3:.1f} ms/iteration), "
+              + (f"scaled to the {iters} iterations of the full solve" if iters else "not scaled (per iteration)"))
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "s", "n_gpus": world,
+                      "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(per_it * kk * 1e3, 1),
+                      "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                      "data": "synthetic (seeded)",
+                      "config": {"workload": f"varcoef Poisson {a.n}^3, Jacobi-PCG to {a.tol:g}", "seed": SEED},
+                      "cpu_baseline": {"value": round(val, 3), "unit": "s", "cores": 1, "kind": kind,
+                                       "sample": sample},
+                      "e2e": {"value": round(val, 3), "unit": "s", "h2d_bytes_per_step": 0,
+                              "d2h_bytes_per_step": 0}}), flush=True)
+
+
+def main():
+    a = parse()
+    rank, world, local = rank_info()
+    if a.impl == "reference":
+        run_reference(a, rank, world)
+    else:
+        run_ours(a, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

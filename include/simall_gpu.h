@@ -1,0 +1,264 @@
+/*
+ * simall_gpu.h -- C ABI of the GB300 (sm_103a) pressure-correction library.
+ *
+ * One shared library, libsimall_gpu.so, replaces SimAll's pressure-correction
+ * hot path: the face-loop assembly of the pressure-correction Laplacian into
+ * the solver's CSR matrix and the preconditioned CG solve on it.  Every entry
+ * point is extern "C", takes plain pointers and sizes, returns an int status
+ * (SIMALL_OK == 0) and never lets an exception cross the boundary.  Each
+ * declaration names the reference interface it replaces (file:line inside the
+ * SimAll source tree).
+ *
+ * Memory: arguments tagged `mem` are host pointers when mem ==
+ * SIMALL_MEM_HOST (the call copies them host<->device on the context stream
+ * and returns after the result is back on the host) and device pointers when
+ * mem == SIMALL_MEM_DEVICE (no copies; the call returns once the result is
+ * final in device memory).  Device pointers must be 16-byte aligned.
+ *
+ * Threading: an object is used by one host thread at a time (as
+ * solver::ILinearSolver, src/solver/Solver.hpp:92-100).  All GPU work of a
+ * context is ordered on its stream.
+ */
+#ifndef SIMALL_GPU_H
+#define SIMALL_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ------------------------------------------------------------------ status */
+enum simall_status {
+    SIMALL_OK = 0,
+    SIMALL_ERR_INVALID_ARGUMENT = 1, /* null pointer, negative size, bad enum */
+    SIMALL_ERR_CUDA = 2,             /* a CUDA runtime call failed; see last_error */
+    SIMALL_ERR_OUT_OF_MEMORY = 3,
+    SIMALL_ERR_UNSORTED_CSR = 4,     /* a CSR row is not strictly ascending / rowPtr not monotone */
+    SIMALL_ERR_MISSING_DIAGONAL = 5, /* a row has no diagonal entry where the method needs one */
+    SIMALL_ERR_NON_FINITE = 6,       /* NaN or Inf in an input array */
+    SIMALL_ERR_NOT_POSITIVE = 7,     /* non-positive diagonal (mixed precision needs D > 0) */
+    SIMALL_ERR_SIZE_MISMATCH = 8,
+    SIMALL_ERR_BREAKDOWN = 9,        /* p.Ap == 0 (the reference returns early the same way) */
+    SIMALL_ERR_TIMEOUT = 10,         /* a bounded device-side wait ran out */
+    SIMALL_ERR_UNSUPPORTED = 11,
+    SIMALL_ERR_NO_DEVICE = 12,
+    SIMALL_ERR_INDEX_RANGE = 13      /* a column / cell / face index outside [0, n) */
+};
+
+enum simall_memory { SIMALL_MEM_HOST = 0, SIMALL_MEM_DEVICE = 1 };
+
+/* PreconditionerKind ordinals (src/solver/Solver.hpp:75-82).  SSOR and AMG are
+ * not on this path and are rejected with SIMALL_ERR_UNSUPPORTED; None maps to
+ * Jacobi, as make_preconditioner's default branch does
+ * (src/solver/LinearSolvers.cpp:240-254). */
+enum simall_preconditioner {
+    SIMALL_PRECOND_JACOBI = 0,
+    SIMALL_PRECOND_ILU0 = 1,
+    SIMALL_PRECOND_SSOR = 2,
+    SIMALL_PRECOND_AMG = 3,
+    SIMALL_PRECOND_NONE = 4
+};
+
+enum simall_precision {
+    SIMALL_PRECISION_FP64 = 0, /* the reference CG, FP64 throughout */
+    SIMALL_PRECISION_MIXED = 1 /* FP32 inner CG, FP64 true residual, reductions and x (Jacobi only) */
+};
+
+/* BCType ordinals (src/solver/Solver.hpp:105-123) used by the assembly. */
+enum simall_bc_type {
+    SIMALL_BC_WALL = 0,
+    SIMALL_BC_NO_SLIP_WALL = 1,
+    SIMALL_BC_MOVING_WALL = 2,
+    SIMALL_BC_SLIP_WALL = 3,
+    SIMALL_BC_VELOCITY_INLET = 4,
+    SIMALL_BC_PRESSURE_INLET = 5,
+    SIMALL_BC_MASS_FLOW_INLET = 6,
+    SIMALL_BC_PRESSURE_OUTLET = 7,
+    SIMALL_BC_OUTFLOW = 8,
+    SIMALL_BC_SYMMETRY = 9,
+    SIMALL_BC_AXISYMMETRIC = 10,
+    SIMALL_BC_PERIODIC = 11
+};
+
+const char *simall_status_string(int status);
+/* Library version string, e.g. "simall_gb300 0.1.0 sm_103a". */
+const char *simall_version(void);
+
+/* ------------------------------------------------------------------ context */
+/* Replaces gpu::CudaContext (src/gpu/CudaContext.cpp:83-258): a device, a
+ * stream and the library's device-resident scratch.  stream == NULL creates a
+ * private non-blocking stream; otherwise the caller's cudaStream_t is used. */
+typedef struct simall_context simall_context;
+int simall_context_create(int device, void *stream, simall_context **out);
+int simall_context_destroy(simall_context *ctx);
+/* Message of the last failure on this context ("" if none). */
+const char *simall_context_last_error(const simall_context *ctx);
+int simall_context_synchronize(simall_context *ctx);
+/* The cudaStream_t the context orders its work on. */
+void *simall_context_stream(const simall_context *ctx);
+/* Number of kernels this library launched on the context so far. */
+int64_t simall_context_kernel_launches(const simall_context *ctx);
+
+/* ------------------------------------------------------------------ PCG solver */
+/* Replaces solver::ILinearSolver / CGSolver (src/solver/Solver.hpp:92-100,
+ * src/solver/LinearSolvers.cpp:415-459) and gpu::CgGpu
+ * (src/gpu/CgGpu.hpp:87-124). */
+typedef struct simall_solver_config {
+    int preconditioner;    /* simall_preconditioner; default Jacobi */
+    double tolerance;      /* stop when ||r||/max(||b||,1e-30) < tolerance; default 1e-8 */
+    int max_iterations;    /* default 1000 (LinearSolverConfig, Solver.hpp:83-90) */
+    int precision;         /* simall_precision; default FP64 */
+    double reliable_delta; /* mixed: iterated-residual drop that triggers an FP64 update; default 0.1 */
+    int check_interval;    /* iterations between host polls of the device stop flag; 0 = automatic */
+} simall_solver_config;
+
+typedef struct simall_solver_stats {
+    int iterations;          /* as CGSolver::solve returns: it+1 at convergence, maxIterations otherwise */
+    int converged;           /* 1 when final_residual < tolerance */
+    int status;              /* SIMALL_OK or SIMALL_ERR_BREAKDOWN */
+    int reliable_updates;    /* mixed precision: FP64 residual replacements performed */
+    double final_residual;   /* ||r||/max(||b||,1e-30) at exit (last_residual()) */
+    double true_residual;    /* ||b - A x||/max(||b||,1e-30) recomputed in FP64 from the returned x */
+    double b_norm;           /* ||b||_2 */
+    double seconds;          /* wall time of the solve call */
+} simall_solver_stats;
+
+typedef struct simall_solver simall_solver;
+void simall_solver_config_default(simall_solver_config *cfg);
+int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, simall_solver **out);
+int simall_solver_destroy(simall_solver *s);
+/* CSR with int32 rowPtr[n+1], colIdx[nnz] (columns strictly ascending per row,
+ * diagonal present) and FP64 values[nnz] (src/solver/CSRMatrix.hpp:16-22).
+ * Copies host arrays to the device (mem == HOST) or references the caller's
+ * device arrays (mem == DEVICE; they must stay alive and unchanged until the
+ * next set_matrix or destroy).  Runs the preconditioner setup on the device. */
+int simall_solver_set_matrix(simall_solver *s, int64_t n, int64_t nnz, const int32_t *rowPtr,
+                             const int32_t *colIdx, const double *values, int mem);
+/* Re-reads the values of the current pattern (same n, nnz, rowPtr, colIdx) and
+ * redoes the preconditioner setup, as CGSolver::solve does on every call. */
+int simall_solver_update_values(simall_solver *s, const double *values, int mem);
+/* Solves A x = b from x = 0 (CGSolver semantics: the incoming x is ignored). */
+int simall_solver_solve(simall_solver *s, const double *b, double *x, int mem, simall_solver_stats *stats);
+/* y = A x with the solver's current FP64 matrix (the staged SpMV kernel the
+ * solve uses; bit-identical to CSRMatrix::spmv, src/solver/CSRMatrix.hpp:24-35). */
+int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem);
+/* Times `reps` back-to-back launches of one kernel of the solve on the
+ * current matrix, bracketed by CUDA events on the context stream; *ms
+ * receives the average duration of one launch and *bytes the algorithmic
+ * bytes one launch moves (each array counted once per use, ideal reuse of
+ * gathered vectors).  kernel: 0 FP64 CSR SpMV, 1 FP64 SpMV + p.Ap,
+ * 2 FP64 Jacobi update (x, r, z, norms), 3 FP64 direction update,
+ * 4 mixed FP32 SpMV + p.q, 5 mixed update, 6 mixed direction update.
+ * Kernels 4-6 need precision MIXED.  The solver's iteration state is left
+ * undefined; the next solve starts from scratch. */
+int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms, double *bytes);
+/* ILinearSolver::last_residual(). */
+double simall_solver_last_residual(const simall_solver *s);
+/* ILinearSolver::solve(A, b, x) in one call: set_matrix + solve on host arrays. */
+int simall_solver_solve_csr(simall_solver *s, int64_t n, int64_t nnz, const int32_t *rowPtr,
+                            const int32_t *colIdx, const double *values, const double *b, double *x,
+                            simall_solver_stats *stats);
+
+/* ------------------------------------------------------------------ pressure-correction system */
+/* The reference mesh SoA (src/meshing/MeshStorage.hpp:37-105); owner/neighbor
+ * and cell_face_indices are u64 ids, neighbor == UINT64_MAX on boundary faces
+ * (kBoundaryCell). */
+typedef struct simall_mesh_view {
+    int64_t n_cells;
+    int64_t n_faces;
+    const uint64_t *owner;
+    const uint64_t *neighbor;
+    const double *area_x, *area_y, *area_z;
+    const double *centroid_x, *centroid_y, *centroid_z; /* face centroids */
+    const uint32_t *boundary_zone;                      /* 0 = interior */
+    const double *cell_centroid_x, *cell_centroid_y, *cell_centroid_z;
+    const int32_t *cell_face_offsets; /* [n_cells+1] */
+    const uint64_t *cell_face_indices;
+} simall_mesh_view;
+
+typedef struct simall_boundary {
+    uint32_t zone;
+    int type; /* simall_bc_type */
+} simall_boundary;
+
+/* Replaces SimpleAlgorithm::build_sparsity + assemble_pressure_correction
+ * (src/solver/SimpleAlgorithm.cpp:49-98, :358-447) for the SIMPLE variant
+ * without periodic twins.  create() builds the CSR pattern (bit-exact with
+ * build_sparsity), uploads the mesh and precomputes per-face |A|^2 and |d.A|
+ * on the device. */
+typedef struct simall_pressure_system simall_pressure_system;
+int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *mesh, const simall_boundary *bcs,
+                                  int n_bcs, simall_pressure_system **out);
+int simall_pressure_system_destroy(simall_pressure_system *ps);
+/* Sizes, and (when the arrays are non-NULL) host copies of the pattern. */
+int simall_pressure_system_pattern(const simall_pressure_system *ps, int64_t *n, int64_t *nnz, int32_t *rowPtr,
+                                   int32_t *colIdx);
+/* Device pointers of the system's CSR (rowPtr, colIdx, values) and rhs. */
+int simall_pressure_system_device_arrays(const simall_pressure_system *ps, const int32_t **rowPtr,
+                                         const int32_t **colIdx, double **values, double **rhs);
+/* assemble_pressure_correction: values and rhs from aP[n_cells] and
+ * phi[n_faces] (mem says where aP/phi live).  any_dirichlet (optional)
+ * receives 1 when a pressure boundary anchors the system (no cell-0 pin). */
+int simall_assemble_pressure_correction(simall_pressure_system *ps, double rho, const double *aP,
+                                        const double *phi, int mem, int *any_dirichlet);
+/* Host copies of the assembled values[nnz] and rhs[n]. */
+int simall_pressure_system_download(const simall_pressure_system *ps, double *values, double *rhs);
+/* Points the solver at the system's device CSR (no copy) and runs the
+ * preconditioner setup. */
+int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *ps);
+/* Solves the assembled system for p' (x = 0 start) into x (mem). */
+int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,
+                                 simall_solver_stats *stats);
+
+/* ------------------------------------------------------------------ reference GPU facade */
+/* One-for-one replacements of src/gpu/GpuKernels.hpp:48-108 on device
+ * pointers (stream == NULL: the legacy default stream).  dot and nrm2 block
+ * the host, as documented there. */
+int simall_gpu_axpy(double alpha, const double *x, double *y, size_t n, void *stream);
+int simall_gpu_scal(double alpha, double *x, size_t n, void *stream);
+int simall_gpu_copy(const double *src, double *dst, size_t n, void *stream);
+int simall_gpu_dot(const double *x, const double *y, size_t n, void *stream, double *result);
+int simall_gpu_nrm2(const double *x, size_t n, void *stream, double *result);
+int simall_gpu_axpby(double a, const double *x, double b, double *y, size_t n, void *stream);
+int simall_gpu_xpby(const double *x, double beta, double *y, size_t n, void *stream);
+int simall_gpu_spmv_csr(size_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                        const double *x, double *y, void *stream);
+/* z[i] = r[i] / diag[i]  (GpuKernels.hpp:87) */
+int simall_gpu_jacobi_apply(const double *diag, const double *r, double *z, size_t n, void *stream);
+/* In-place ILU(0) of device CSR values (GpuKernels.hpp:89-97); *ok = 0 on a
+ * zero pivot.  Level-scheduled on the device; the factor equals
+ * ILU0Preconditioner::setup's bit for bit. */
+int simall_gpu_ilu0_factor_inplace(size_t n, const int32_t *rowPtr, const int32_t *colIdx, double *values,
+                                   void *stream, int *ok);
+/* z = U^-1 L^-1 r with the factor above (GpuKernels.hpp:99-108). */
+int simall_gpu_ilu0_apply(size_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                          const double *r, double *z, void *stream);
+
+/* ------------------------------------------------------------------ host preprocessing */
+/* Structured n_x*n_y*n_z hex box [0,e_x]x[0,e_y]x[0,e_z] as an unstructured
+ * SoA mesh, identical to CartesianMesher::generate + ConnectivityBuilder::build
+ * + Mesh::compute_geometry (src/meshing/CartesianMesher.cpp:13-101,
+ * Connectivity.cpp:45-115, MeshStorage.cpp:21-97), with an optional
+ * per-node displacement (dx,dy,dz may be NULL) applied before the geometry.
+ * Sizes: n_cells = nx*ny*nz, n_faces = (nx+1)ny nz + nx(ny+1)nz + nx ny(nz+1),
+ * cell_face_indices 6*n_cells.  All output arrays are caller-allocated. */
+int simall_mesh_cartesian(int nx, int ny, int nz, double ex, double ey, double ez, const double *dx,
+                          const double *dy, const double *dz, uint64_t *owner, uint64_t *neighbor,
+                          double *area_x, double *area_y, double *area_z, double *centroid_x,
+                          double *centroid_y, double *centroid_z, uint32_t *boundary_zone, double *volume,
+                          double *cell_centroid_x, double *cell_centroid_y, double *cell_centroid_z,
+                          int32_t *cell_face_offsets, uint64_t *cell_face_indices);
+/* Reverse Cuthill-McKee in place, as renumber_cells_cuthill_mckee
+ * (src/meshing/MeshOps.cpp:547-676).  stats (optional, 3 entries) receives
+ * bandwidth before, after and cells permuted. */
+int simall_mesh_rcm(int64_t n_cells, int64_t n_faces, uint64_t *owner, uint64_t *neighbor, double *volume,
+                    double *cell_centroid_x, double *cell_centroid_y, double *cell_centroid_z,
+                    int32_t *cell_face_offsets, uint64_t *cell_face_indices, int64_t *stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SIMALL_GPU_H */

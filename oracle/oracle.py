@@ -1,0 +1,461 @@
+"""ctypes wrapper over oracle/lib/liboracle.so -- TEST INFRASTRUCTURE.
+
+The C restatement of the SimAll reference algorithms (oracle/simall_oracle.c)
+exposed to numpy.  Only tests/, __graft_entry__.smoke() and bench.py's
+CPU-baseline leg import this module; the product never does.
+
+`RefLib` wraps oracle/_ref/libsimall_ref.so, the reference's own sources
+compiled by oracle/build_ref.sh; it exists only where the reference tree was
+present at build time.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libsimall_ref.so")
+
+_P = C.c_void_p
+_I64 = C.c_int64
+_I32 = C.c_int32
+_D = C.c_double
+
+
+def build_oracle() -> str:
+    """Compile liboracle.so (make -C oracle)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+    return LIB_PATH
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(_P)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build_oracle()
+        L = C.CDLL(LIB_PATH)
+        L.orc_cartesian_topology.restype = _I64
+        L.orc_cartesian_topology.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D] + [_P] * 9
+        L.orc_compute_geometry.restype = None
+        L.orc_compute_geometry.argtypes = [_I64, _I64] + [_P] * 18
+        L.orc_classify_zones.restype = None
+        L.orc_classify_zones.argtypes = [_I64, _P, _P, _P, _P, _D, _D, _D, _P]
+        L.orc_rcm.restype = None
+        L.orc_rcm.argtypes = [_I64, _I64] + [_P] * 10
+        L.orc_build_sparsity.restype = _I64
+        L.orc_build_sparsity.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
+        L.orc_assemble.restype = C.c_int
+        L.orc_assemble.argtypes = [_I64, _I64] + [_P] * 13 + [C.c_int, _D] + [_P] * 6
+        L.orc_dot.restype = _D
+        L.orc_dot.argtypes = [_I64, _P, _P]
+        L.orc_spmv.restype = None
+        L.orc_spmv.argtypes = [_I64, _P, _P, _P, _P, _P]
+        L.orc_jacobi_setup.restype = None
+        L.orc_jacobi_setup.argtypes = [_I64, _P, _P, _P, _P]
+        L.orc_ilu0_setup.restype = None
+        L.orc_ilu0_setup.argtypes = [_I64, _P, _P, _P, _P, _P]
+        L.orc_ilu0_apply.restype = None
+        L.orc_ilu0_apply.argtypes = [_I64, _P, _P, _P, _P, _P, _P, _P]
+        L.orc_cg.restype = C.c_int
+        L.orc_cg.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P, _P]
+        L.orc_assemble_face_k.restype = None
+        L.orc_assemble_face_k.argtypes = [_I64, _I64] + [_P] * 12 + [_D] + [_P] * 8
+        L.orc_face_k_gradient.restype = None
+        L.orc_face_k_gradient.argtypes = [_I64] + [_P] * 10
+        _lib = L
+    return _lib
+
+
+# ---------------------------------------------------------------- mesh
+
+
+@dataclass
+class Mesh:
+    """SoA mesh in the layout of meshing::Mesh (src/meshing/MeshStorage.hpp:37-105);
+    neighbor == -1 marks a boundary face."""
+
+    nC: int
+    nF: int
+    extent: tuple
+    nx: np.ndarray
+    ny: np.ndarray
+    nz: np.ndarray
+    fnOff: np.ndarray
+    fnIdx: np.ndarray
+    owner: np.ndarray
+    neighbor: np.ndarray
+    cfOff: np.ndarray
+    cfIdx: np.ndarray
+    ax: np.ndarray = field(default=None)
+    ay: np.ndarray = field(default=None)
+    az: np.ndarray = field(default=None)
+    fcx: np.ndarray = field(default=None)
+    fcy: np.ndarray = field(default=None)
+    fcz: np.ndarray = field(default=None)
+    zone: np.ndarray = field(default=None)
+    vol: np.ndarray = field(default=None)
+    ccx: np.ndarray = field(default=None)
+    ccy: np.ndarray = field(default=None)
+    ccz: np.ndarray = field(default=None)
+
+
+def cartesian_mesh(Nx, Ny, Nz, ex=1.0, ey=1.0, ez=1.0, node_shift=None) -> Mesh:
+    """CartesianMesher + ConnectivityBuilder + compute_geometry + zones.
+
+    node_shift: optional (3, nNodes) array added to the node coordinates
+    before the geometry is computed (the perturbation of a distorted mesh).
+    """
+    L = lib()
+    nC = Nx * Ny * Nz
+    nN = (Nx + 1) * (Ny + 1) * (Nz + 1)
+    maxF = 6 * nC
+    nx = np.empty(nN)
+    ny = np.empty(nN)
+    nz = np.empty(nN)
+    fnOff = np.empty(maxF + 1, np.int32)
+    fnIdx = np.empty(4 * maxF, np.int64)
+    owner = np.empty(maxF, np.int64)
+    neighbor = np.empty(maxF, np.int64)
+    cfOff = np.empty(nC + 1, np.int32)
+    cfIdx = np.empty(6 * nC, np.int64)
+    nF = L.orc_cartesian_topology(Nx, Ny, Nz, ex, ey, ez, _ptr(nx), _ptr(ny), _ptr(nz), _ptr(fnOff),
+                                  _ptr(fnIdx), _ptr(owner), _ptr(neighbor), _ptr(cfOff), _ptr(cfIdx))
+    m = Mesh(nC, int(nF), (ex, ey, ez), nx, ny, nz, fnOff[: nF + 1].copy(), fnIdx[: 4 * nF].copy(),
+             owner[:nF].copy(), neighbor[:nF].copy(), cfOff, cfIdx)
+    if node_shift is not None:
+        m.nx = m.nx + node_shift[0]
+        m.ny = m.ny + node_shift[1]
+        m.nz = m.nz + node_shift[2]
+    # Zones are classified on the unperturbed geometry, as CartesianMesher does
+    # before any node edit; boundary nodes are never shifted, so the boundary
+    # face centroids are the same either way.
+    compute_geometry(m)
+    m.zone = np.empty(m.nF, np.uint32)
+    L.orc_classify_zones(m.nF, _ptr(m.neighbor), _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), ex, ey, ez,
+                         _ptr(m.zone))
+    return m
+
+
+def compute_geometry(m: Mesh) -> None:
+    L = lib()
+    for k in ("ax", "ay", "az", "fcx", "fcy", "fcz"):
+        setattr(m, k, np.empty(m.nF))
+    for k in ("vol", "ccx", "ccy", "ccz"):
+        setattr(m, k, np.empty(m.nC))
+    L.orc_compute_geometry(m.nC, m.nF, _ptr(m.nx), _ptr(m.ny), _ptr(m.nz), _ptr(m.fnOff), _ptr(m.fnIdx),
+                           _ptr(m.owner), _ptr(m.cfOff), _ptr(m.cfIdx), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                           _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.vol), _ptr(m.ccx), _ptr(m.ccy),
+                           _ptr(m.ccz))
+
+
+def rcm(m: Mesh):
+    """In-place reverse Cuthill-McKee; returns (newPos, (bwBefore, bwAfter, permuted))."""
+    L = lib()
+    newPos = np.empty(m.nC, np.int64)
+    stats = np.zeros(3, np.int64)
+    L.orc_rcm(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.vol), _ptr(m.ccx), _ptr(m.ccy),
+              _ptr(m.ccz), _ptr(m.cfOff), _ptr(m.cfIdx), _ptr(newPos), _ptr(stats))
+    return newPos, tuple(int(s) for s in stats)
+
+
+def build_sparsity(m: Mesh):
+    L = lib()
+    rowPtr = np.empty(m.nC + 1, np.int32)
+    nnz = L.orc_build_sparsity(m.nC, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.cfOff), _ptr(m.cfIdx),
+                               _ptr(rowPtr), None)
+    colIdx = np.empty(nnz, np.int32)
+    L.orc_build_sparsity(m.nC, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.cfOff), _ptr(m.cfIdx), _ptr(rowPtr),
+                         _ptr(colIdx))
+    return rowPtr, colIdx
+
+
+def assemble(m: Mesh, rowPtr, colIdx, pressure_zones, rho, aP, phi):
+    """assemble_pressure_correction; pressure_zones = zone ids with a
+    PressureOutlet/PressureInlet condition.  Returns (values, rhs, anyDirichlet)."""
+    L = lib()
+    nZ = int(max([7] + [z + 1 for z in pressure_zones]))
+    isP = np.zeros(nZ, np.uint8)
+    for z in pressure_zones:
+        isP[z] = 1
+    values = np.empty(len(colIdx))
+    rhs = np.empty(m.nC)
+    aP = np.ascontiguousarray(aP, np.float64)
+    phi = np.ascontiguousarray(phi, np.float64)
+    anyD = L.orc_assemble(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                          _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.zone), _ptr(m.ccx), _ptr(m.ccy),
+                          _ptr(m.ccz), _ptr(isP), nZ, rho, _ptr(aP), _ptr(phi), _ptr(rowPtr), _ptr(colIdx),
+                          _ptr(values), _ptr(rhs))
+    return values, rhs, bool(anyD)
+
+
+def assemble_face_k(m: Mesh, rowPtr, colIdx, is_dirichlet_face, rho, k, pb, src):
+    L = lib()
+    values = np.empty(len(colIdx))
+    rhs = np.empty(m.nC)
+    g = np.empty(m.nF)
+    isD = np.ascontiguousarray(is_dirichlet_face, np.uint8)
+    k = np.ascontiguousarray(k, np.float64)
+    pb = np.ascontiguousarray(pb, np.float64)
+    src = np.ascontiguousarray(src, np.float64)
+    L.orc_assemble_face_k(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                          _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz),
+                          _ptr(isD), rho, _ptr(k), _ptr(pb), _ptr(src), _ptr(rowPtr), _ptr(colIdx),
+                          _ptr(values), _ptr(rhs), _ptr(g))
+    return values, rhs, g
+
+
+def face_k_gradient(m: Mesh, is_dirichlet_face, g, k, pb, x, lam):
+    L = lib()
+    dk = np.empty(m.nF)
+    dpb = np.empty(m.nF)
+    isD = np.ascontiguousarray(is_dirichlet_face, np.uint8)
+    L.orc_face_k_gradient(m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(isD), _ptr(g), _ptr(k), _ptr(pb),
+                          _ptr(x), _ptr(lam), _ptr(dk), _ptr(dpb))
+    return dk, dpb
+
+
+# ---------------------------------------------------------------- linear algebra
+
+
+def spmv(rowPtr, colIdx, values, x):
+    n = len(rowPtr) - 1
+    y = np.empty(n)
+    x = np.ascontiguousarray(x, np.float64)
+    lib().orc_spmv(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(x), _ptr(y))
+    return y
+
+
+def dot(a, b):
+    a = np.ascontiguousarray(a, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    return lib().orc_dot(len(a), _ptr(a), _ptr(b))
+
+
+def jacobi_setup(rowPtr, colIdx, values):
+    n = len(rowPtr) - 1
+    inv = np.empty(n)
+    lib().orc_jacobi_setup(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(inv))
+    return inv
+
+
+def ilu0_setup(rowPtr, colIdx, values):
+    n = len(rowPtr) - 1
+    lu = np.empty(len(values))
+    dp = np.empty(n, np.int32)
+    lib().orc_ilu0_setup(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(lu), _ptr(dp))
+    return lu, dp
+
+
+def ilu0_apply(rowPtr, colIdx, lu, diagPtr, r):
+    n = len(rowPtr) - 1
+    z = np.empty(n)
+    y = np.empty(n)
+    r = np.ascontiguousarray(r, np.float64)
+    lib().orc_ilu0_apply(n, _ptr(rowPtr), _ptr(colIdx), _ptr(lu), _ptr(diagPtr), _ptr(r), _ptr(z), _ptr(y))
+    return z
+
+
+def cg(rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000, history=False):
+    """CGSolver::solve.  Returns (x, iterations, last_residual[, history])."""
+    n = len(rowPtr) - 1
+    x = np.empty(n)
+    last = C.c_double(0.0)
+    hist = np.zeros(max_it) if history else None
+    b = np.ascontiguousarray(b, np.float64)
+    it = lib().orc_cg(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(b), int(precond), float(tol),
+                      int(max_it), _ptr(x), C.byref(last), _ptr(hist))
+    if history:
+        return x, it, last.value, hist[:max(it, 0)]
+    return x, it, last.value
+
+
+# ---------------------------------------------------------------- compiled reference
+
+
+class RefLib:
+    """The reference's own code (oracle/_ref/libsimall_ref.so)."""
+
+    def __init__(self, path: str = REF_PATH):
+        L = C.CDLL(path)
+        L.ref_mesh_cartesian.restype = _P
+        L.ref_mesh_cartesian.argtypes = [C.c_int, C.c_int, C.c_int, _D, _D, _D]
+        L.ref_mesh_free.argtypes = [_P]
+        L.ref_mesh_sizes.argtypes = [_P, _P]
+        L.ref_mesh_get_nodes.argtypes = [_P] * 4
+        L.ref_mesh_set_nodes.argtypes = [_P] * 4
+        L.ref_mesh_get_faces.argtypes = [_P] * 10
+        L.ref_mesh_get_face_nodes.argtypes = [_P] * 3
+        L.ref_mesh_get_cells.argtypes = [_P] * 7
+        L.ref_mesh_rcm.argtypes = [_P, _P]
+        L.ref_sparsity_nnz.restype = _I64
+        L.ref_sparsity_nnz.argtypes = [_P]
+        L.ref_assemble.restype = C.c_int
+        L.ref_assemble.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 6
+        L.ref_cg.restype = C.c_int
+        L.ref_cg.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P, _P]
+        L.ref_precond_apply.argtypes = [C.c_int, C.c_int] + [_P] * 5
+        L.ref_spmv.argtypes = [C.c_int] + [_P] * 5
+        L.ref_cavity_run.restype = C.c_int
+        L.ref_cavity_run.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P]
+        L.ref_cavity_fetch.argtypes = [_P] * 9
+        L.ref_discrete_adjoint.restype = C.c_int
+        L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 12
+        self.L = L
+
+    @staticmethod
+    def available(path: str = REF_PATH) -> bool:
+        return os.path.exists(path)
+
+    # -- mesh
+    def cartesian_mesh(self, Nx, Ny, Nz, ex=1.0, ey=1.0, ez=1.0, node_shift=None, do_rcm=False):
+        L = self.L
+        h = L.ref_mesh_cartesian(Nx, Ny, Nz, ex, ey, ez)
+        try:
+            s = np.zeros(5, np.int64)
+            L.ref_mesh_sizes(h, _ptr(s))
+            nC, nF, nN, ncf, nfn = (int(v) for v in s)
+            if node_shift is not None:
+                nx = np.empty(nN)
+                ny = np.empty(nN)
+                nz = np.empty(nN)
+                L.ref_mesh_get_nodes(h, _ptr(nx), _ptr(ny), _ptr(nz))
+                nx = nx + node_shift[0]
+                ny = ny + node_shift[1]
+                nz = nz + node_shift[2]
+                L.ref_mesh_set_nodes(h, _ptr(nx), _ptr(ny), _ptr(nz))
+            stats = None
+            if do_rcm:
+                st = np.zeros(3, np.int64)
+                L.ref_mesh_rcm(h, _ptr(st))
+                stats = tuple(int(v) for v in st)
+            out = self._fetch(h, nC, nF, nN, ncf, nfn)
+            out["rcm_stats"] = stats
+            out["handle"] = h
+            return out
+        except Exception:
+            L.ref_mesh_free(h)
+            raise
+
+    def _fetch(self, h, nC, nF, nN, ncf, nfn):
+        L = self.L
+        d = {"nC": nC, "nF": nF}
+        d["nx"], d["ny"], d["nz"] = np.empty(nN), np.empty(nN), np.empty(nN)
+        L.ref_mesh_get_nodes(h, _ptr(d["nx"]), _ptr(d["ny"]), _ptr(d["nz"]))
+        own = np.empty(nF, np.uint64)
+        nb = np.empty(nF, np.uint64)
+        for k in ("ax", "ay", "az", "fcx", "fcy", "fcz"):
+            d[k] = np.empty(nF)
+        d["zone"] = np.empty(nF, np.uint32)
+        L.ref_mesh_get_faces(h, _ptr(own), _ptr(nb), _ptr(d["ax"]), _ptr(d["ay"]), _ptr(d["az"]),
+                             _ptr(d["fcx"]), _ptr(d["fcy"]), _ptr(d["fcz"]), _ptr(d["zone"]))
+        d["owner"] = own.view(np.int64).copy()
+        d["neighbor"] = nb.view(np.int64).copy()
+        d["fnOff"] = np.empty(nF + 1, np.int32)
+        fn = np.empty(nfn, np.uint64)
+        L.ref_mesh_get_face_nodes(h, _ptr(d["fnOff"]), _ptr(fn))
+        d["fnIdx"] = fn.view(np.int64).copy()
+        for k in ("vol", "ccx", "ccy", "ccz"):
+            d[k] = np.empty(nC)
+        d["cfOff"] = np.empty(nC + 1, np.int32)
+        cf = np.empty(ncf, np.uint64)
+        L.ref_mesh_get_cells(h, _ptr(d["vol"]), _ptr(d["ccx"]), _ptr(d["ccy"]), _ptr(d["ccz"]),
+                             _ptr(d["cfOff"]), _ptr(cf))
+        d["cfIdx"] = cf.view(np.int64).copy()
+        return d
+
+    def free_mesh(self, mesh_dict):
+        if mesh_dict.get("handle"):
+            self.L.ref_mesh_free(mesh_dict["handle"])
+            mesh_dict["handle"] = None
+
+    def assemble(self, mesh_dict, bcs, rho, aP, phi):
+        """bcs: list of (zone, BCType ordinal).  Returns rowPtr, colIdx, values, rhs."""
+        L = self.L
+        h = mesh_dict["handle"]
+        nnz = L.ref_sparsity_nnz(h)
+        nC = mesh_dict["nC"]
+        zones = np.array([z for z, _ in bcs] or [0], np.uint32)
+        types = np.array([t for _, t in bcs] or [0], np.int32)
+        rowPtr = np.empty(nC + 1, np.int32)
+        colIdx = np.empty(nnz, np.int32)
+        values = np.empty(nnz)
+        rhs = np.empty(nC)
+        aP = np.ascontiguousarray(aP, np.float64)
+        phi = np.ascontiguousarray(phi, np.float64)
+        L.ref_assemble(h, len(bcs), _ptr(zones), _ptr(types), rho, _ptr(aP), _ptr(phi), _ptr(rowPtr),
+                       _ptr(colIdx), _ptr(values), _ptr(rhs))
+        return rowPtr, colIdx, values, rhs
+
+    # -- solvers
+    def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):
+        n = len(rowPtr) - 1
+        x = np.empty(n)
+        last = C.c_double(0)
+        secs = C.c_double(0)
+        b = np.ascontiguousarray(b, np.float64)
+        it = self.L.ref_cg(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(b), int(precond), float(tol),
+                           int(max_it), _ptr(x), C.byref(last), C.byref(secs))
+        return x, it, last.value, secs.value
+
+    def precond_apply(self, kind, rowPtr, colIdx, values, r):
+        n = len(rowPtr) - 1
+        z = np.empty(n)
+        r = np.ascontiguousarray(r, np.float64)
+        self.L.ref_precond_apply(int(kind), n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(r), _ptr(z))
+        return z
+
+    def spmv(self, rowPtr, colIdx, values, x):
+        n = len(rowPtr) - 1
+        y = np.empty(n)
+        x = np.ascontiguousarray(x, np.float64)
+        self.L.ref_spmv(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(x), _ptr(y))
+        return y
+
+    def cavity(self, N, mu=0.01, n_outer=3, n_record=3, precond=0, tol=1e-8, max_it=1000):
+        """SIMPLE lid-driven cavity; records the first n_record pressure systems."""
+        L = self.L
+        sizes = np.zeros(5, np.int64)
+        secs = C.c_double(0)
+        L.ref_cavity_run(N, mu, n_outer, n_record, precond, tol, max_it, _ptr(sizes), C.byref(secs))
+        nC, nnz, nF, nSolve, nRec = (int(v) for v in sizes)
+        out = {
+            "rowPtr": np.empty(nC + 1, np.int32), "colIdx": np.empty(nnz, np.int32),
+            "values": np.empty((nRec, nnz)), "rhs": np.empty((nRec, nC)), "x": np.empty((nRec, nC)),
+            "aP": np.empty((nRec, nC)), "phi": np.empty((nRec, nF)), "iters": np.empty(nSolve, np.int32),
+            "res": np.empty(nSolve),
+        }
+        L.ref_cavity_fetch(*(_ptr(out[k]) for k in ("rowPtr", "colIdx", "values", "rhs", "x", "aP", "phi",
+                                                      "iters", "res")))
+        out["p_solve_seconds"] = secs.value
+        return out
+
+    def discrete_adjoint(self, rowPtr, colIdx, values, dJdQ, owner, neighbor, is_dirichlet, g, k, pb, x,
+                         tol=1e-10, max_iter=500, restart=30):
+        n = len(rowPtr) - 1
+        nF = len(owner)
+        nD = int(np.count_nonzero(is_dirichlet))
+        psi = np.empty(n)
+        grad = np.empty(nF + nD)
+        its = C.c_int64(0)
+        res = C.c_double(0)
+        arr = [np.ascontiguousarray(a, t) for a, t in ((dJdQ, np.float64), (owner, np.int64),
+                                                        (neighbor, np.int64), (is_dirichlet, np.int32),
+                                                        (g, np.float64), (k, np.float64), (pb, np.float64),
+                                                        (x, np.float64))]
+        rc = self.L.ref_discrete_adjoint(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(arr[0]), tol,
+                                         max_iter, restart, nF, _ptr(arr[1]), _ptr(arr[2]), _ptr(arr[3]),
+                                         _ptr(arr[4]), _ptr(arr[5]), _ptr(arr[6]), _ptr(arr[7]), _ptr(psi),
+                                         _ptr(grad), C.byref(its), C.byref(res))
+        return psi, grad, int(its.value), res.value, rc

@@ -1,0 +1,421 @@
+// Test infrastructure only: a C-callable driver over the SimAll reference
+// sources, compiled together with them by oracle/build_ref.sh into
+// oracle/_ref/libsimall_ref.so.  Nothing in the product links or loads it;
+// the tests and the golden-fixture script use it to pin the C restatement in
+// oracle/simall_oracle.c against the reference's own code.
+//
+// Every entry point calls the reference's public (or subclass-visible) API:
+//   meshing::CartesianMesher::generate      src/meshing/CartesianMesher.cpp:13
+//   meshing::Mesh::compute_geometry         src/meshing/MeshStorage.cpp:21
+//   meshing::ops::renumber_cells_cuthill_mckee  src/meshing/MeshOps.cpp:547
+//   SimpleAlgorithm::build_sparsity         src/solver/SimpleAlgorithm.cpp:49
+//   SimpleAlgorithm::assemble_pressure_correction  src/solver/SimpleAlgorithm.cpp:358
+//   SimpleAlgorithm::iterate                src/solver/SimpleAlgorithm.cpp:522
+//   make_cg / make_gmres / make_preconditioner     src/solver/LinearSolvers.cpp:240,462
+//   adjoint::solve_discrete_adjoint         src/adjoint/DiscreteAdjoint.cpp:150
+#include "adjoint/DiscreteAdjoint.hpp"
+#include "meshing/CartesianMesher.hpp"
+#include "meshing/MeshOps.hpp"
+#include "meshing/MeshStorage.hpp"
+#include "solver/FieldRegistry.hpp"
+#include "solver/LinearSolvers.hpp"
+#include "solver/SimpleAlgorithm.hpp"
+
+#include <algorithm>
+#include <chrono>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+namespace S = simall::solver;
+namespace M = simall::meshing;
+using Vec = simall::util::aligned_vector<double>;
+
+namespace
+{
+
+struct RefMesh
+{
+    M::Mesh mesh;
+};
+
+// Exposes the protected assembly hooks of SimpleAlgorithm so the driver can
+// feed aP_ / phiFlux_ directly and read A_p_ / rhs_ back.
+class AssemblyProbe : public S::SimpleAlgorithm
+{
+public:
+    using S::SimpleAlgorithm::SimpleAlgorithm;
+    void sparsity() { build_sparsity(); }
+    void assemble(const double* aP, const double* phi)
+    {
+        build_sparsity();
+        const std::size_t nC = mesh_.cells().size(), nF = mesh_.faces().size();
+        aP_.assign(aP, aP + nC);
+        phiFlux_.assign(phi, phi + nF);
+        assemble_pressure_correction();
+    }
+    const S::CSRMatrix& Ap() const { return A_p_; }
+    const Vec& rhs() const { return rhs_; }
+    const Vec& aP() const { return aP_; }
+    const Vec& phi() const { return phiFlux_; }
+};
+
+std::vector<S::BoundarySpec> make_bcs(int nbc, const std::uint32_t* zones, const int* types)
+{
+    std::vector<S::BoundarySpec> b;
+    for (int i = 0; i < nbc; ++i)
+        b.push_back(S::BoundarySpec{zones[i], static_cast<S::BCType>(types[i]), 0.0, {0, 0, 0}, ""});
+    return b;
+}
+
+S::CSRMatrix make_csr(int n, const int* rowPtr, const int* colIdx, const double* values)
+{
+    S::CSRMatrix A;
+    A.rowPtr.assign(rowPtr, rowPtr + n + 1);
+    const int nnz = rowPtr[n];
+    A.colIdx.assign(colIdx, colIdx + nnz);
+    A.values.assign(values, values + nnz);
+    return A;
+}
+
+// Pressure solver that records each system it is handed (A_p_, rhs_) and the
+// assembly inputs (aP_, phiFlux_) visible at that moment, then solves it with
+// the reference CG.
+class RecordingSolver final : public S::ILinearSolver
+{
+public:
+    RecordingSolver(S::LinearSolverConfig c) : inner_(S::make_cg(c)) {}
+    int solve(const S::CSRMatrix& A, const Vec& b, Vec& x) override
+    {
+        const bool rec = static_cast<int>(iters.size()) < nRecord;
+        if (rec) {
+            if (rowPtr.empty()) {
+                rowPtr.assign(A.rowPtr.begin(), A.rowPtr.end());
+                colIdx.assign(A.colIdx.begin(), A.colIdx.end());
+            }
+            values.insert(values.end(), A.values.begin(), A.values.end());
+            rhs.insert(rhs.end(), b.begin(), b.end());
+            if (probe) {
+                aP.insert(aP.end(), probe->aP().begin(), probe->aP().end());
+                phi.insert(phi.end(), probe->phi().begin(), probe->phi().end());
+            }
+        }
+        const auto t0 = std::chrono::steady_clock::now();
+        const int it = inner_->solve(A, b, x);
+        seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        if (rec)
+            xs.insert(xs.end(), x.begin(), x.end());
+        iters.push_back(it);
+        res.push_back(inner_->last_residual());
+        return it;
+    }
+    double last_residual() const override { return inner_->last_residual(); }
+
+    int nRecord = 0;
+    const AssemblyProbe* probe = nullptr;
+    std::vector<int> rowPtr, colIdx, iters;
+    std::vector<double> values, rhs, xs, aP, phi, res;
+    double seconds = 0.0;
+
+private:
+    std::unique_ptr<S::ILinearSolver> inner_;
+};
+
+RecordingSolver* g_last_cavity = nullptr;
+
+} // namespace
+
+extern "C" {
+
+// ------------------------------------------------------------------ mesh
+void* ref_mesh_cartesian(int nx, int ny, int nz, double ex, double ey, double ez)
+{
+    auto* m = new RefMesh;
+    M::CartesianGridSpec gs{{0, 0, 0}, {ex, ey, ez}, nx, ny, nz};
+    M::CartesianMesher(gs).generate(m->mesh);
+    return m;
+}
+
+void ref_mesh_free(void* h) { delete static_cast<RefMesh*>(h); }
+
+void ref_mesh_sizes(void* h, std::int64_t* out)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    out[0] = static_cast<std::int64_t>(m.cells().size());
+    out[1] = static_cast<std::int64_t>(m.faces().size());
+    out[2] = static_cast<std::int64_t>(m.nodes().size());
+    out[3] = static_cast<std::int64_t>(m.cells().faceIndices.size());
+    out[4] = static_cast<std::int64_t>(m.faces().nodeIndices.size());
+}
+
+void ref_mesh_get_nodes(void* h, double* x, double* y, double* z)
+{
+    auto& N = static_cast<RefMesh*>(h)->mesh.nodes();
+    std::copy(N.x.begin(), N.x.end(), x);
+    std::copy(N.y.begin(), N.y.end(), y);
+    std::copy(N.z.begin(), N.z.end(), z);
+}
+
+// Overwrite node coordinates and recompute face/cell geometry.
+void ref_mesh_set_nodes(void* h, const double* x, const double* y, const double* z)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    auto& N = m.nodes();
+    const std::size_t nN = N.size();
+    std::copy(x, x + nN, N.x.begin());
+    std::copy(y, y + nN, N.y.begin());
+    std::copy(z, z + nN, N.z.begin());
+    m.compute_geometry();
+}
+
+void ref_mesh_get_faces(void* h, std::uint64_t* owner, std::uint64_t* neighbor, double* ax, double* ay,
+                        double* az, double* cx, double* cy, double* cz, std::uint32_t* zone)
+{
+    auto& F = static_cast<RefMesh*>(h)->mesh.faces();
+    std::copy(F.owner.begin(), F.owner.end(), owner);
+    std::copy(F.neighbor.begin(), F.neighbor.end(), neighbor);
+    std::copy(F.areaX.begin(), F.areaX.end(), ax);
+    std::copy(F.areaY.begin(), F.areaY.end(), ay);
+    std::copy(F.areaZ.begin(), F.areaZ.end(), az);
+    std::copy(F.centroidX.begin(), F.centroidX.end(), cx);
+    std::copy(F.centroidY.begin(), F.centroidY.end(), cy);
+    std::copy(F.centroidZ.begin(), F.centroidZ.end(), cz);
+    std::copy(F.boundaryZone.begin(), F.boundaryZone.end(), zone);
+}
+
+void ref_mesh_get_face_nodes(void* h, std::int32_t* nodeOffsets, std::uint64_t* nodeIndices)
+{
+    auto& F = static_cast<RefMesh*>(h)->mesh.faces();
+    std::copy(F.nodeOffsets.begin(), F.nodeOffsets.end(), nodeOffsets);
+    std::copy(F.nodeIndices.begin(), F.nodeIndices.end(), nodeIndices);
+}
+
+void ref_mesh_get_cells(void* h, double* vol, double* cx, double* cy, double* cz,
+                        std::int32_t* faceOffsets, std::uint64_t* faceIndices)
+{
+    auto& C = static_cast<RefMesh*>(h)->mesh.cells();
+    std::copy(C.volume.begin(), C.volume.end(), vol);
+    std::copy(C.centroidX.begin(), C.centroidX.end(), cx);
+    std::copy(C.centroidY.begin(), C.centroidY.end(), cy);
+    std::copy(C.centroidZ.begin(), C.centroidZ.end(), cz);
+    std::copy(C.faceOffsets.begin(), C.faceOffsets.end(), faceOffsets);
+    std::copy(C.faceIndices.begin(), C.faceIndices.end(), faceIndices);
+}
+
+void ref_mesh_rcm(void* h, std::int64_t* out)
+{
+    auto st = M::ops::renumber_cells_cuthill_mckee(static_cast<RefMesh*>(h)->mesh);
+    out[0] = static_cast<std::int64_t>(st.bandwidthBefore);
+    out[1] = static_cast<std::int64_t>(st.bandwidthAfter);
+    out[2] = static_cast<std::int64_t>(st.cellsPermuted);
+}
+
+// ------------------------------------------------------------------ assembly
+std::int64_t ref_sparsity_nnz(void* h)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    std::vector<S::BoundarySpec> bcs;
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    AssemblyProbe p(m, f, bcs, *s1, *s2, S::SimpleOptions{});
+    p.sparsity();
+    return static_cast<std::int64_t>(p.Ap().colIdx.size());
+}
+
+int ref_assemble(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, double rho,
+                 const double* aP, const double* phi, std::int32_t* rowPtr, std::int32_t* colIdx,
+                 double* values, double* rhs)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    auto bcs = make_bcs(nbc, bcZones, bcTypes);
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    S::SimpleOptions o;
+    o.rho = rho;
+    AssemblyProbe p(m, f, bcs, *s1, *s2, o);
+    p.assemble(aP, phi);
+    const auto& A = p.Ap();
+    std::copy(A.rowPtr.begin(), A.rowPtr.end(), rowPtr);
+    std::copy(A.colIdx.begin(), A.colIdx.end(), colIdx);
+    std::copy(A.values.begin(), A.values.end(), values);
+    std::copy(p.rhs().begin(), p.rhs().end(), rhs);
+    return 0;
+}
+
+// ------------------------------------------------------------------ solvers
+// CGSolver::solve (LinearSolvers.cpp:420) with the given preconditioner
+// (PreconditionerKind ordinal).  Returns the iteration count.
+int ref_cg(int n, const int* rowPtr, const int* colIdx, const double* values, const double* b,
+           int precond, double tol, int maxit, double* x, double* lastRes, double* seconds)
+{
+    auto A = make_csr(n, rowPtr, colIdx, values);
+    S::LinearSolverConfig c;
+    c.kind = S::LinearSolverKind::CG;
+    c.preconditioner = static_cast<S::PreconditionerKind>(precond);
+    c.tolerance = tol;
+    c.maxIterations = maxit;
+    auto cg = S::make_cg(c);
+    Vec bb(b, b + n), xx(n, 0.0);
+    const auto t0 = std::chrono::steady_clock::now();
+    const int it = cg->solve(A, bb, xx);
+    if (seconds)
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::copy(xx.begin(), xx.end(), x);
+    *lastRes = cg->last_residual();
+    return it;
+}
+
+// IPreconditioner::setup + apply for one r.
+void ref_precond_apply(int kind, int n, const int* rowPtr, const int* colIdx, const double* values,
+                       const double* r, double* z)
+{
+    auto A = make_csr(n, rowPtr, colIdx, values);
+    auto M = S::make_preconditioner(static_cast<S::PreconditionerKind>(kind));
+    M->setup(A);
+    Vec rr(r, r + n), zz;
+    M->apply(rr, zz);
+    std::copy(zz.begin(), zz.end(), z);
+}
+
+void ref_spmv(int n, const int* rowPtr, const int* colIdx, const double* values, const double* x,
+              double* y)
+{
+    auto A = make_csr(n, rowPtr, colIdx, values);
+    Vec xx(x, x + n), yy;
+    A.spmv(xx, yy);
+    std::copy(yy.begin(), yy.end(), y);
+}
+
+// ------------------------------------------------------------------ cavity SIMPLE
+// Runs nOuter SIMPLE iterations of the lid-driven cavity on an N x N x 1 grid
+// (extent 1 x 1 x 1/N; zones 1,2,3,5,6 NoSlipWall, zone 4 MovingWall (1,0,0))
+// with momentum GMRES(30)+ILU (tol 1e-6, 200 it) and pressure CG with the
+// given preconditioner.  The first nRecord pressure systems are recorded;
+// fetch them with ref_cavity_fetch.
+int ref_cavity_run(int N, double mu, int nOuter, int nRecord, int precond, double tol, int maxit,
+                   std::int64_t* sizes, double* pSolveSeconds)
+{
+    M::Mesh mesh;
+    M::CartesianGridSpec gs{{0, 0, 0}, {1.0, 1.0, 1.0 / N}, N, N, 1};
+    M::CartesianMesher(gs).generate(mesh);
+    const std::size_t nC = mesh.cells().size();
+    S::FieldRegistry fields;
+    fields.scalar("p", nC);
+    fields.vector("U", nC);
+    std::vector<S::BoundarySpec> bcs;
+    for (std::uint32_t z : {1u, 2u, 3u, 5u, 6u})
+        bcs.push_back(S::BoundarySpec{z, S::BCType::NoSlipWall, 0.0, {0, 0, 0}, ""});
+    bcs.push_back(S::BoundarySpec{4u, S::BCType::MovingWall, 0.0, {1.0, 0, 0}, ""});
+
+    S::LinearSolverConfig mc;
+    mc.kind = S::LinearSolverKind::GMRES;
+    mc.preconditioner = S::PreconditionerKind::ILU;
+    mc.tolerance = 1e-6;
+    mc.maxIterations = 200;
+    mc.restart = 30;
+    auto mom = S::make_gmres(mc);
+    S::LinearSolverConfig pc;
+    pc.kind = S::LinearSolverKind::CG;
+    pc.preconditioner = static_cast<S::PreconditionerKind>(precond);
+    pc.tolerance = tol;
+    pc.maxIterations = maxit;
+    delete g_last_cavity;
+    g_last_cavity = new RecordingSolver(pc);
+    g_last_cavity->nRecord = nRecord;
+    S::SimpleOptions o;
+    o.urfU = 0.7;
+    o.urfP = 0.3;
+    o.rho = 1.0;
+    o.mu = mu;
+    AssemblyProbe simple(mesh, fields, bcs, *mom, *g_last_cavity, o);
+    g_last_cavity->probe = &simple;
+    for (int i = 0; i < nOuter; ++i)
+        simple.iterate();
+    g_last_cavity->probe = nullptr;
+    sizes[0] = static_cast<std::int64_t>(nC);
+    sizes[1] = static_cast<std::int64_t>(g_last_cavity->colIdx.size());
+    sizes[2] = static_cast<std::int64_t>(mesh.faces().size());
+    sizes[3] = static_cast<std::int64_t>(g_last_cavity->iters.size());
+    sizes[4] = static_cast<std::int64_t>(std::min<std::size_t>(nRecord, g_last_cavity->iters.size()));
+    if (pSolveSeconds)
+        *pSolveSeconds = g_last_cavity->seconds;
+    return 0;
+}
+
+void ref_cavity_fetch(std::int32_t* rowPtr, std::int32_t* colIdx, double* values, double* rhs, double* x,
+                      double* aP, double* phi, std::int32_t* iters, double* res)
+{
+    auto* r = g_last_cavity;
+    std::copy(r->rowPtr.begin(), r->rowPtr.end(), rowPtr);
+    std::copy(r->colIdx.begin(), r->colIdx.end(), colIdx);
+    std::copy(r->values.begin(), r->values.end(), values);
+    std::copy(r->rhs.begin(), r->rhs.end(), rhs);
+    std::copy(r->xs.begin(), r->xs.end(), x);
+    std::copy(r->aP.begin(), r->aP.end(), aP);
+    std::copy(r->phi.begin(), r->phi.end(), phi);
+    std::copy(r->iters.begin(), r->iters.end(), iters);
+    std::copy(r->res.begin(), r->res.end(), res);
+}
+
+// ------------------------------------------------------------------ adjoint
+// solve_discrete_adjoint on the given CSR (size_t CSR copy) with a
+// dRdAlphaTransposeTimes callback for per-face conductances k_f and
+// Dirichlet values p_b of the face-conductance Poisson problem:
+//   interior face f (o,n):  (dR/dk_f)^T psi = g_f (psi_o - psi_n)(x_o - x_n)
+//   Dirichlet face f (o):   (dR/dk_f)^T psi = g_f psi_o (x_o - pb_f)
+//   and for its value pb_f: (dR/dpb_f)^T psi = -k_f g_f psi_o
+// Design variables: [k_0..k_{nF-1}, pb over the Dirichlet faces in face order].
+int ref_discrete_adjoint(int n, const int* rowPtr, const int* colIdx, const double* values,
+                         const double* dJdQ, double tol, int maxIter, int restart, int nF,
+                         const std::int64_t* owner, const std::int64_t* neighbor, const int* isDirichlet,
+                         const double* g, const double* k, const double* pb, const double* x,
+                         double* psiOut, double* gradOut, std::int64_t* itersOut, double* resOut)
+{
+    simall::adjoint::CsrMatrix A;
+    A.n = static_cast<std::size_t>(n);
+    A.rowPtr.assign(rowPtr, rowPtr + n + 1);
+    A.colIdx.assign(colIdx, colIdx + rowPtr[n]);
+    A.values.assign(values, values + rowPtr[n]);
+    simall::adjoint::DiscreteAdjointInputs in;
+    in.A = &A;
+    in.dJdQ.assign(dJdQ, dJdQ + n);
+    int nD = 0;
+    for (int f = 0; f < nF; ++f)
+        nD += isDirichlet[f] ? 1 : 0;
+    const std::size_t nDV = static_cast<std::size_t>(nF + nD);
+    simall::adjoint::DiscreteAdjointOptions opt;
+    opt.tol = tol;
+    opt.maxIter = static_cast<std::size_t>(maxIter);
+    opt.restart = static_cast<std::size_t>(restart);
+    // solve_discrete_adjoint calls the callback without handing it psi, so
+    // psi is taken from a first run without the callback; the second run is
+    // deterministic and reproduces the same psi before calling back.
+    auto r1 = simall::adjoint::solve_discrete_adjoint(in, nDV, opt);
+    const std::vector<double> psi = r1.psi;
+    in.dRdAlphaTransposeTimes = [&](std::vector<double>& out) {
+        int d = 0;
+        for (int f = 0; f < nF; ++f) {
+            const std::int64_t o = owner[f], nb = neighbor[f];
+            if (nb >= 0) {
+                out[f] = g[f] * (psi[o] - psi[nb]) * (x[o] - x[nb]);
+            } else if (isDirichlet[f]) {
+                out[f] = g[f] * psi[o] * (x[o] - pb[f]);
+                out[nF + d] = -k[f] * g[f] * psi[o];
+                ++d;
+            } else {
+                out[f] = 0.0;
+            }
+        }
+    };
+    auto r2 = simall::adjoint::solve_discrete_adjoint(in, nDV, opt);
+    std::copy(r2.psi.begin(), r2.psi.end(), psiOut);
+    std::copy(r2.gradient.begin(), r2.gradient.end(), gradOut);
+    *itersOut = static_cast<std::int64_t>(r2.iterations);
+    *resOut = r2.residual;
+    return r2.ok ? 0 : 1;
+}
+
+} // extern "C"

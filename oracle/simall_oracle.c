@@ -1,0 +1,844 @@
+/*
+ * simall_oracle.c -- TEST INFRASTRUCTURE, not product code.
+ *
+ * A plain-C, serial restatement of the SimAll reference algorithms on the
+ * pressure-correction path.  It is the checker the CUDA library is compared
+ * against: only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline
+ * leg may load it.  Parity of this restatement with the reference itself is
+ * pinned by tests/test_oracle_vs_reference.py (live, where the reference
+ * compiles) and tests/test_oracle_golden.py (committed fixtures made by
+ * tests/golden/make_golden.py from the compiled reference).
+ *
+ * Floating-point operations are written in the same order as the reference
+ * and the file is compiled with -ffp-contract=off, so results are bit-exact
+ * with the reference on any IEEE-754 host (x86_64 without FMA, aarch64 with
+ * contraction off).
+ *
+ * Index conventions: cell ids are int64, a boundary face has neighbor == -1
+ * (the reference's kBoundaryCell = ~0ull, src/meshing/MeshStorage.hpp:35).
+ */
+#include <math.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define ORC_BOUNDARY (-1)
+
+/* std::max(a, b) as the reference evaluates it: (a < b) ? b : a */
+#define STD_MAX(a, b) (((a) < (b)) ? (b) : (a))
+
+/* ------------------------------------------------------------------ helpers */
+
+static void *xmalloc(size_t n)
+{
+    void *p = malloc(n ? n : 1);
+    if (!p)
+        abort();
+    return p;
+}
+
+static void sort4(int64_t *k)
+{
+    for (int i = 1; i < 4; ++i) {
+        int64_t v = k[i];
+        int j = i - 1;
+        while (j >= 0 && k[j] > v) {
+            k[j + 1] = k[j];
+            --j;
+        }
+        k[j + 1] = v;
+    }
+}
+
+/* ------------------------------------------------------------------ mesh topology */
+
+/*
+ * Structured hex grid as an unstructured SoA mesh.
+ * Follows CartesianMesher::generate (src/meshing/CartesianMesher.cpp:13-58):
+ * node (i,j,k) at origin + (i*dx, j*dy, k*dz), node id ((k*Py)+j)*Px+i; cell
+ * faces in the order -Z{n0,n3,n2,n1}, +Z{n4,n5,n6,n7}, -Y{n0,n1,n5,n4},
+ * +Y{n3,n7,n6,n2}, -X{n0,n4,n7,n3}, +X{n1,n2,n6,n5}.
+ * Then ConnectivityBuilder::build (src/meshing/Connectivity.cpp:45-115): a
+ * face is keyed by its sorted node tuple; the first cell to list it creates it
+ * (owner = that cell, nodes in that cell's order), the second sets neighbor;
+ * each cell's face list keeps its descriptor order.  The lookup here is an
+ * open-addressing table keyed by the sorted tuple.
+ *
+ * Outputs (caller-allocated): nodes x/y/z [nNodes]; fnOff [nF+1]; fnIdx [4nF];
+ * owner/neighbor [nF]; cfOff [nC+1]; cfIdx [6nC].  Returns nF.
+ */
+int64_t orc_cartesian_topology(int Nx, int Ny, int Nz, double ex, double ey, double ez, double *nx,
+                               double *ny, double *nz, int32_t *fnOff, int64_t *fnIdx, int64_t *owner,
+                               int64_t *neighbor, int32_t *cfOff, int64_t *cfIdx)
+{
+    const double dx = ex / Nx, dy = ey / Ny, dz = ez / Nz;
+    const int64_t Px = Nx + 1, Py = Ny + 1, Pz = Nz + 1;
+    int64_t p = 0;
+    for (int64_t k = 0; k < Pz; ++k)
+        for (int64_t j = 0; j < Py; ++j)
+            for (int64_t i = 0; i < Px; ++i) {
+                nx[p] = 0.0 + (double)(int)i * dx;
+                ny[p] = 0.0 + (double)(int)j * dy;
+                nz[p] = 0.0 + (double)(int)k * dz;
+                ++p;
+            }
+    const int64_t nC = (int64_t)Nx * Ny * Nz;
+    const int64_t maxF = 6 * nC;
+    /* hash table of face ids keyed by the face's sorted node tuple (the key
+     * of a stored face is recomputed from its node list) */
+    int64_t cap = 1;
+    while (cap < 2 * maxF)
+        cap <<= 1;
+    int64_t *hval = (int64_t *)xmalloc((size_t)cap * sizeof(int64_t));
+    for (int64_t s = 0; s < cap; ++s)
+        hval[s] = -1;
+    int64_t nF = 0, ncf = 0;
+    int64_t c = 0;
+    cfOff[0] = 0;
+    for (int64_t k = 0; k < Nz; ++k)
+        for (int64_t j = 0; j < Ny; ++j)
+            for (int64_t i = 0; i < Nx; ++i, ++c) {
+#define PID(a, b, d) ((((d) * Py) + (b)) * Px + (a))
+                const int64_t n0 = PID(i, j, k), n1 = PID(i + 1, j, k), n2 = PID(i + 1, j + 1, k),
+                              n3 = PID(i, j + 1, k), n4 = PID(i, j, k + 1), n5 = PID(i + 1, j, k + 1),
+                              n6 = PID(i + 1, j + 1, k + 1), n7 = PID(i, j + 1, k + 1);
+#undef PID
+                const int64_t fv[6][4] = {{n0, n3, n2, n1}, {n4, n5, n6, n7}, {n0, n1, n5, n4},
+                                          {n3, n7, n6, n2}, {n0, n4, n7, n3}, {n1, n2, n6, n5}};
+                for (int q = 0; q < 6; ++q) {
+                    int64_t key[4] = {fv[q][0], fv[q][1], fv[q][2], fv[q][3]};
+                    sort4(key);
+                    uint64_t h = 1469598103934665603ull;
+                    for (int t = 0; t < 4; ++t)
+                        h = (h ^ (uint64_t)key[t]) * 1099511628211ull;
+                    int64_t s = (int64_t)(h & (uint64_t)(cap - 1));
+                    for (;;) {
+                        const int64_t cand = hval[s];
+                        if (cand < 0) {
+                            /* new face */
+                            const int64_t fid = nF++;
+                            hval[s] = fid;
+                            fnOff[fid] = (int32_t)(4 * fid);
+                            for (int t = 0; t < 4; ++t)
+                                fnIdx[4 * fid + t] = fv[q][t];
+                            owner[fid] = c;
+                            neighbor[fid] = ORC_BOUNDARY;
+                            cfIdx[ncf++] = fid;
+                            break;
+                        }
+                        int64_t ck[4] = {fnIdx[4 * cand], fnIdx[4 * cand + 1], fnIdx[4 * cand + 2],
+                                         fnIdx[4 * cand + 3]};
+                        sort4(ck);
+                        if (memcmp(ck, key, sizeof(key)) == 0) {
+                            neighbor[cand] = c;
+                            cfIdx[ncf++] = cand;
+                            break;
+                        }
+                        s = (s + 1) & (cap - 1);
+                    }
+                }
+                cfOff[c + 1] = (int32_t)ncf;
+            }
+    fnOff[nF] = (int32_t)(4 * nF);
+    free(hval);
+    return nF;
+}
+
+/*
+ * Face areas/centroids and cell volumes/centroids.
+ * Follows Mesh::compute_geometry (src/meshing/MeshStorage.cpp:21-97):
+ * face centroid = node average (sum then * 1/n); area = sum over the fan of
+ * 0.5 * (pa-c) x (pb-c); V = sum sgn*(xf.af)/3; C = sum xf*dv*(3/4) / V.
+ */
+void orc_compute_geometry(int64_t nC, int64_t nF, const double *nx, const double *ny, const double *nz,
+                          const int32_t *fnOff, const int64_t *fnIdx, const int64_t *owner,
+                          const int32_t *cfOff, const int64_t *cfIdx, double *ax, double *ay, double *az,
+                          double *fcx, double *fcy, double *fcz, double *vol, double *ccx, double *ccy,
+                          double *ccz)
+{
+    for (int64_t f = 0; f < nF; ++f) {
+        ax[f] = ay[f] = az[f] = 0.0;
+        fcx[f] = fcy[f] = fcz[f] = 0.0;
+        const int32_t s = fnOff[f], e = fnOff[f + 1];
+        if (e - s < 3)
+            continue;
+        double cx = 0.0, cy = 0.0, cz = 0.0;
+        for (int32_t i = s; i < e; ++i) {
+            const int64_t n = fnIdx[i];
+            cx += nx[n];
+            cy += ny[n];
+            cz += nz[n];
+        }
+        const double inv = 1.0 / (double)(e - s);
+        cx *= inv;
+        cy *= inv;
+        cz *= inv;
+        fcx[f] = cx;
+        fcy[f] = cy;
+        fcz[f] = cz;
+        double sx = 0.0, sy = 0.0, sz = 0.0;
+        for (int32_t i = s; i < e; ++i) {
+            const int64_t a = fnIdx[i];
+            const int64_t b = fnIdx[(i + 1 < e) ? i + 1 : s];
+            const double pax = nx[a] - cx, pay = ny[a] - cy, paz = nz[a] - cz;
+            const double pbx = nx[b] - cx, pby = ny[b] - cy, pbz = nz[b] - cz;
+            const double crx = pay * pbz - paz * pby;
+            const double cry = paz * pbx - pax * pbz;
+            const double crz = pax * pby - pay * pbx;
+            sx = sx + crx * 0.5;
+            sy = sy + cry * 0.5;
+            sz = sz + crz * 0.5;
+        }
+        ax[f] = sx;
+        ay[f] = sy;
+        az[f] = sz;
+    }
+    for (int64_t c = 0; c < nC; ++c) {
+        double V = 0.0, wx = 0.0, wy = 0.0, wz = 0.0;
+        for (int32_t i = cfOff[c]; i < cfOff[c + 1]; ++i) {
+            const int64_t f = cfIdx[i];
+            const double sgn = (owner[f] == c) ? 1.0 : -1.0;
+            const double d = fcx[f] * ax[f] + fcy[f] * ay[f] + fcz[f] * az[f];
+            const double dv = sgn * d / 3.0;
+            V += dv;
+            wx = wx + fcx[f] * dv * (3.0 / 4.0);
+            wy = wy + fcy[f] * dv * (3.0 / 4.0);
+            wz = wz + fcz[f] * dv * (3.0 / 4.0);
+        }
+        vol[c] = V;
+        ccx[c] = ccy[c] = ccz[c] = 0.0;
+        if (V != 0.0) {
+            ccx[c] = wx / V;
+            ccy[c] = wy / V;
+            ccz[c] = wz / V;
+        }
+    }
+}
+
+/*
+ * Boundary zones by face centroid, tol 1e-9, origin 0.
+ * Follows CartesianMesher::generate (src/meshing/CartesianMesher.cpp:60-89):
+ * interior faces 0; xMin=1 xMax=2 yMin=3 yMax=4 zMin=5 zMax=6; a boundary
+ * face matching none keeps the ConnectivityBuilder default 1
+ * (src/meshing/Connectivity.cpp:108-110).
+ */
+void orc_classify_zones(int64_t nF, const int64_t *neighbor, const double *fcx, const double *fcy,
+                        const double *fcz, double ex, double ey, double ez, uint32_t *zone)
+{
+    const double tol = 1e-9;
+    for (int64_t f = 0; f < nF; ++f) {
+        if (neighbor[f] != ORC_BOUNDARY) {
+            zone[f] = 0;
+            continue;
+        }
+        const double cx = fcx[f], cy = fcy[f], cz = fcz[f];
+        uint32_t z = 1;
+        if (fabs(cx - 0.0) < tol)
+            z = 1;
+        else if (fabs(cx - (0.0 + ex)) < tol)
+            z = 2;
+        else if (fabs(cy - 0.0) < tol)
+            z = 3;
+        else if (fabs(cy - (0.0 + ey)) < tol)
+            z = 4;
+        else if (fabs(cz - 0.0) < tol)
+            z = 5;
+        else if (fabs(cz - (0.0 + ez)) < tol)
+            z = 6;
+        zone[f] = z;
+    }
+}
+
+/* ------------------------------------------------------------------ RCM */
+
+static int64_t bandwidth(int64_t nF, const int64_t *owner, const int64_t *neighbor)
+{
+    int64_t bw = 0;
+    for (int64_t f = 0; f < nF; ++f) {
+        if (neighbor[f] == ORC_BOUNDARY)
+            continue;
+        const int64_t d = owner[f] > neighbor[f] ? owner[f] - neighbor[f] : neighbor[f] - owner[f];
+        if (d > bw)
+            bw = d;
+    }
+    return bw;
+}
+
+static int cmp_i64(const void *a, const void *b)
+{
+    const int64_t x = *(const int64_t *)a, y = *(const int64_t *)b;
+    return (x > y) - (x < y);
+}
+
+/*
+ * Reverse Cuthill-McKee renumbering, in place.
+ * Follows renumber_cells_cuthill_mckee (src/meshing/MeshOps.cpp:547-676):
+ * adjacency from interior faces (sorted, unique); repeatedly seed BFS at the
+ * lowest-index unvisited cell of minimum degree; enqueue unvisited
+ * neighbours in ascending id, then stably ordered by ascending degree (the
+ * reference's std::sort on <=16 elements is an insertion sort, hence
+ * stable); reverse the visit order; permute cell volume/centroids and the
+ * cell->face CSR; remap face owner/neighbor.  Face arrays keep their order.
+ * Writes newPos[old] = new and stats {bwBefore, bwAfter, permuted}.
+ */
+void orc_rcm(int64_t nC, int64_t nF, int64_t *owner, int64_t *neighbor, double *vol, double *ccx,
+             double *ccy, double *ccz, int32_t *cfOff, int64_t *cfIdx, int64_t *newPos, int64_t *stats)
+{
+    stats[0] = bandwidth(nF, owner, neighbor);
+    if (nC == 0) {
+        stats[1] = stats[2] = 0;
+        return;
+    }
+    int64_t *deg = (int64_t *)calloc((size_t)nC + 1, sizeof(int64_t));
+    for (int64_t f = 0; f < nF; ++f) {
+        if (neighbor[f] == ORC_BOUNDARY)
+            continue;
+        const int64_t a = owner[f], b = neighbor[f];
+        if (a >= nC || b >= nC)
+            continue;
+        deg[a]++;
+        deg[b]++;
+    }
+    int64_t *aoff = (int64_t *)xmalloc(((size_t)nC + 1) * sizeof(int64_t));
+    aoff[0] = 0;
+    for (int64_t c = 0; c < nC; ++c)
+        aoff[c + 1] = aoff[c] + deg[c];
+    int64_t *adj = (int64_t *)xmalloc((size_t)(aoff[nC] ? aoff[nC] : 1) * sizeof(int64_t));
+    int64_t *fill = (int64_t *)calloc((size_t)nC, sizeof(int64_t));
+    for (int64_t f = 0; f < nF; ++f) {
+        if (neighbor[f] == ORC_BOUNDARY)
+            continue;
+        const int64_t a = owner[f], b = neighbor[f];
+        if (a >= nC || b >= nC)
+            continue;
+        adj[aoff[a] + fill[a]++] = b;
+        adj[aoff[b] + fill[b]++] = a;
+    }
+    /* sort + unique per cell; degree = unique count */
+    for (int64_t c = 0; c < nC; ++c) {
+        int64_t *v = adj + aoff[c];
+        const int64_t m = fill[c];
+        qsort(v, (size_t)m, sizeof(int64_t), cmp_i64);
+        int64_t u = 0;
+        for (int64_t t = 0; t < m; ++t)
+            if (u == 0 || v[u - 1] != v[t])
+                v[u++] = v[t];
+        deg[c] = u;
+    }
+    uint8_t *seen = (uint8_t *)calloc((size_t)nC, 1);
+    int64_t *order = (int64_t *)xmalloc((size_t)nC * sizeof(int64_t));
+    int64_t *queue = (int64_t *)xmalloc((size_t)nC * sizeof(int64_t));
+    int64_t *nb = (int64_t *)xmalloc(((size_t)nC + 1) * sizeof(int64_t));
+    int64_t no = 0;
+    while (no < nC) {
+        int64_t seed = -1;
+        for (int64_t c = 0; c < nC; ++c) {
+            if (seen[c])
+                continue;
+            if (seed < 0 || deg[c] < deg[seed])
+                seed = c;
+        }
+        if (seed < 0)
+            break;
+        int64_t qh = 0, qt = 0;
+        queue[qt++] = seed;
+        seen[seed] = 1;
+        while (qh < qt) {
+            const int64_t c = queue[qh++];
+            order[no++] = c;
+            int64_t m = 0;
+            for (int64_t t = 0; t < deg[c]; ++t) {
+                const int64_t n = adj[aoff[c] + t];
+                if (!seen[n]) {
+                    nb[m++] = n;
+                    seen[n] = 1;
+                }
+            }
+            for (int64_t t = 1; t < m; ++t) { /* stable insertion sort by degree */
+                const int64_t v = nb[t];
+                int64_t s = t - 1;
+                while (s >= 0 && deg[nb[s]] > deg[v]) {
+                    nb[s + 1] = nb[s];
+                    --s;
+                }
+                nb[s + 1] = v;
+            }
+            for (int64_t t = 0; t < m; ++t)
+                queue[qt++] = nb[t];
+        }
+    }
+    for (int64_t a = 0, b = no - 1; a < b; ++a, --b) {
+        const int64_t t = order[a];
+        order[a] = order[b];
+        order[b] = t;
+    }
+    for (int64_t c = 0; c < nC; ++c)
+        newPos[c] = -1;
+    for (int64_t k = 0; k < no; ++k)
+        newPos[order[k]] = k;
+    for (int64_t c = 0; c < nC; ++c)
+        if (newPos[c] < 0)
+            newPos[c] = c;
+    double *tmp = (double *)xmalloc((size_t)nC * sizeof(double));
+    double *arrs[4] = {vol, ccx, ccy, ccz};
+    for (int a = 0; a < 4; ++a) {
+        for (int64_t c = 0; c < nC; ++c)
+            tmp[newPos[c]] = arrs[a][c];
+        memcpy(arrs[a], tmp, (size_t)nC * sizeof(double));
+    }
+    free(tmp);
+    const int64_t ncf = cfOff[nC];
+    int32_t *offNew = (int32_t *)xmalloc(((size_t)nC + 1) * sizeof(int32_t));
+    int64_t *idxNew = (int64_t *)xmalloc((size_t)(ncf ? ncf : 1) * sizeof(int64_t));
+    int64_t w = 0;
+    offNew[0] = 0;
+    for (int64_t q = 0; q < nC; ++q) {
+        const int64_t c = order[q];
+        for (int32_t t = cfOff[c]; t < cfOff[c + 1]; ++t)
+            idxNew[w++] = cfIdx[t];
+        offNew[q + 1] = (int32_t)w;
+    }
+    memcpy(cfOff, offNew, ((size_t)nC + 1) * sizeof(int32_t));
+    memcpy(cfIdx, idxNew, (size_t)ncf * sizeof(int64_t));
+    free(offNew);
+    free(idxNew);
+    for (int64_t f = 0; f < nF; ++f) {
+        owner[f] = newPos[owner[f]];
+        if (neighbor[f] != ORC_BOUNDARY)
+            neighbor[f] = newPos[neighbor[f]];
+    }
+    stats[1] = bandwidth(nF, owner, neighbor);
+    stats[2] = no;
+    free(deg);
+    free(aoff);
+    free(adj);
+    free(fill);
+    free(seen);
+    free(order);
+    free(queue);
+    free(nb);
+}
+
+/* ------------------------------------------------------------------ sparsity + assembly */
+
+/*
+ * CSR pattern of the pressure-correction matrix.
+ * Follows SimpleAlgorithm::build_sparsity (src/solver/SimpleAlgorithm.cpp:49-98)
+ * without periodic twins: row c = sorted unique {c} U {other cell of each of
+ * c's faces that is not a boundary}.  With colIdx == NULL only rowPtr is
+ * filled; returns nnz.
+ */
+int64_t orc_build_sparsity(int64_t nC, const int64_t *owner, const int64_t *neighbor,
+                           const int32_t *cfOff, const int64_t *cfIdx, int32_t *rowPtr, int32_t *colIdx)
+{
+    int64_t nnz = 0;
+    int64_t buf[64];
+    rowPtr[0] = 0;
+    for (int64_t c = 0; c < nC; ++c) {
+        int m = 0;
+        buf[m++] = c;
+        for (int32_t t = cfOff[c]; t < cfOff[c + 1]; ++t) {
+            const int64_t f = cfIdx[t];
+            const int64_t oth = (owner[f] == c) ? neighbor[f] : owner[f];
+            if (oth != ORC_BOUNDARY && m < 64)
+                buf[m++] = oth;
+        }
+        for (int i = 1; i < m; ++i) {
+            const int64_t v = buf[i];
+            int j = i - 1;
+            while (j >= 0 && buf[j] > v) {
+                buf[j + 1] = buf[j];
+                --j;
+            }
+            buf[j + 1] = v;
+        }
+        int u = 0;
+        for (int i = 0; i < m; ++i)
+            if (u == 0 || buf[u - 1] != buf[i])
+                buf[u++] = buf[i];
+        if (colIdx)
+            for (int i = 0; i < u; ++i)
+                colIdx[nnz + i] = (int32_t)buf[i];
+        nnz += u;
+        rowPtr[c + 1] = (int32_t)nnz;
+    }
+    return nnz;
+}
+
+/* find_col (src/solver/SimpleAlgorithm.cpp:23-29) */
+static int32_t find_col(const int32_t *rowPtr, const int32_t *colIdx, int64_t row, int64_t col)
+{
+    for (int32_t k = rowPtr[row]; k < rowPtr[row + 1]; ++k)
+        if (colIdx[k] == col)
+            return k;
+    return -1;
+}
+
+/* add_at (src/solver/SimpleAlgorithm.cpp:30-35) */
+static void add_at(const int32_t *rowPtr, const int32_t *colIdx, double *values, int64_t row, int64_t col,
+                   double v)
+{
+    const int32_t k = find_col(rowPtr, colIdx, row, col);
+    if (k >= 0)
+        values[k] += v;
+}
+
+/*
+ * Pressure-correction Laplacian, SIMPLE variant, no periodic twins.
+ * Follows SimpleAlgorithm::assemble_pressure_correction
+ * (src/solver/SimpleAlgorithm.cpp:358-447):
+ *   interior face: coef = rho*|A|^2 / max(0.5*(max(aP_o,1e-30)+max(aP_n,1e-30))*|d.A|, 1e-30),
+ *                  d = C_n - C_o, added +oo, -on, +nn, -no;
+ *   boundary face in a pressure zone (isPressure[zone] != 0, i.e. PressureOutlet
+ *                  or PressureInlet): coef = rho*|A|^2 / max(max(aP_o,1e-30)*|d.A|, 1e-30),
+ *                  d = face centroid - C_o, added +oo, anyDirichlet = 1;
+ *   every face: rhs_o -= phi_f, rhs_n += phi_f (interior);
+ *   no Dirichlet face: A[0,0] *= 1e6 and rhs[0] = 0.
+ * values/rhs are overwritten.  Returns anyDirichlet.
+ */
+int orc_assemble(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                 const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
+                 const uint32_t *zone, const double *ccx, const double *ccy, const double *ccz,
+                 const uint8_t *isPressure, int nZones, double rho, const double *aP, const double *phi,
+                 const int32_t *rowPtr, const int32_t *colIdx, double *values, double *rhs)
+{
+    const int64_t nnz = rowPtr[nC];
+    for (int64_t k = 0; k < nnz; ++k)
+        values[k] = 0.0;
+    for (int64_t c = 0; c < nC; ++c)
+        rhs[c] = 0.0;
+    int anyDirichlet = 0;
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        const double Ax = ax[f], Ay = ay[f], Az = az[f];
+        const double Amag2 = Ax * Ax + Ay * Ay + Az * Az;
+        if (n != ORC_BOUNDARY) {
+            const double dx = ccx[n] - ccx[o];
+            const double dy = ccy[n] - ccy[o];
+            const double dz = ccz[n] - ccz[o];
+            const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+            const double dOwn = STD_MAX(aP[o], 1e-30), dNbr = STD_MAX(aP[n], 1e-30);
+            const double aPf = 0.5 * (dOwn + dNbr);
+            const double den = aPf * ddotA;
+            const double coef = rho * Amag2 / STD_MAX(den, 1e-30);
+            add_at(rowPtr, colIdx, values, o, o, coef);
+            add_at(rowPtr, colIdx, values, o, n, -coef);
+            add_at(rowPtr, colIdx, values, n, n, coef);
+            add_at(rowPtr, colIdx, values, n, o, -coef);
+        } else {
+            const uint32_t zz = zone[f];
+            if ((int)zz < nZones && isPressure[zz]) {
+                const double dx = fcx[f] - ccx[o];
+                const double dy = fcy[f] - ccy[o];
+                const double dz = fcz[f] - ccz[o];
+                const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+                const double den = STD_MAX(aP[o], 1e-30) * ddotA;
+                const double coef = rho * Amag2 / STD_MAX(den, 1e-30);
+                add_at(rowPtr, colIdx, values, o, o, coef);
+                anyDirichlet = 1;
+            }
+        }
+        rhs[o] -= phi[f];
+        if (n != ORC_BOUNDARY)
+            rhs[n] += phi[f];
+    }
+    if (!anyDirichlet && nC > 0) {
+        const int32_t kd = find_col(rowPtr, colIdx, 0, 0);
+        if (kd >= 0)
+            values[kd] *= 1.0e6;
+        rhs[0] = 0.0;
+    }
+    return anyDirichlet;
+}
+
+/* ------------------------------------------------------------------ BLAS-1 + SpMV */
+
+/* dot / norm2 / axpy (src/solver/LinearSolvers.cpp:25-43) */
+double orc_dot(int64_t n, const double *a, const double *b)
+{
+    double s = 0;
+    for (int64_t i = 0; i < n; ++i)
+        s += a[i] * b[i];
+    return s;
+}
+
+static double norm2(int64_t n, const double *a) { return sqrt(orc_dot(n, a, a)); }
+
+static void axpy(int64_t n, double alpha, const double *x, double *y)
+{
+    for (int64_t i = 0; i < n; ++i)
+        y[i] += alpha * x[i];
+}
+
+/* CSRMatrix::spmv (src/solver/CSRMatrix.hpp:24-35) */
+void orc_spmv(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *x,
+              double *y)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double s = 0.0;
+        for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            s += values[k] * x[colIdx[k]];
+        y[i] = s;
+    }
+}
+
+/* ------------------------------------------------------------------ preconditioners */
+
+/* JacobiPreconditioner::setup (src/solver/LinearSolvers.cpp:54-65): first
+ * diagonal entry of each row, 1/a_ii, or 1.0 when zero or missing. */
+void orc_jacobi_setup(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                      double *invDiag)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        invDiag[i] = 1.0;
+        for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                invDiag[i] = (values[k] != 0.0) ? 1.0 / values[k] : 1.0;
+                break;
+            }
+    }
+}
+
+/* ILU0Preconditioner::setup (src/solver/LinearSolvers.cpp:81-122): IKJ
+ * in-place ILU(0) on the pattern; rows below a missing diagonal or a zero
+ * pivot are skipped for that k.  lu and diagPtr are outputs. */
+void orc_ilu0_setup(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, double *lu,
+                    int32_t *diagPtr)
+{
+    memcpy(lu, values, (size_t)rowPtr[n] * sizeof(double));
+    for (int64_t i = 0; i < n; ++i) {
+        diagPtr[i] = -1;
+        for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                diagPtr[i] = k;
+                break;
+            }
+    }
+    for (int64_t i = 1; i < n; ++i) {
+        for (int32_t kp = rowPtr[i]; kp < rowPtr[i + 1]; ++kp) {
+            const int32_t k = colIdx[kp];
+            if (k >= i)
+                break;
+            if (diagPtr[k] < 0)
+                continue;
+            const double piv = lu[diagPtr[k]];
+            if (piv == 0.0)
+                continue;
+            const double m = lu[kp] / piv;
+            lu[kp] = m;
+            for (int32_t jp = diagPtr[k] + 1; jp < rowPtr[k + 1]; ++jp) {
+                const int32_t j = colIdx[jp];
+                for (int32_t qp = kp + 1; qp < rowPtr[i + 1]; ++qp) {
+                    if (colIdx[qp] == j) {
+                        lu[qp] -= m * lu[jp];
+                        break;
+                    }
+                    if (colIdx[qp] > j)
+                        break;
+                }
+            }
+        }
+    }
+}
+
+/* ILU0Preconditioner::apply (src/solver/LinearSolvers.cpp:123-151): forward
+ * unit-lower sweep, then backward sweep z_i = s/u_ii (or s when u_ii is
+ * zero or missing).  y is caller scratch of length n. */
+void orc_ilu0_apply(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *lu,
+                    const int32_t *diagPtr, const double *r, double *z, double *y)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        double s = r[i];
+        for (int32_t kp = rowPtr[i]; kp < rowPtr[i + 1]; ++kp) {
+            const int32_t j = colIdx[kp];
+            if (j >= i)
+                break;
+            s -= lu[kp] * y[j];
+        }
+        y[i] = s;
+    }
+    for (int64_t i = 0; i < n; ++i)
+        z[i] = 0.0;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        double s = y[i];
+        const int32_t kd = diagPtr[i];
+        for (int32_t kp = kd + 1; kp < rowPtr[i + 1]; ++kp)
+            s -= lu[kp] * z[colIdx[kp]];
+        z[i] = (kd >= 0 && lu[kd] != 0.0) ? s / lu[kd] : s;
+    }
+}
+
+/* ------------------------------------------------------------------ CG */
+
+/*
+ * Preconditioned CG.  Follows CGSolver::solve (src/solver/LinearSolvers.cpp:420-451):
+ * setup M; x = 0; r = b; z = M r; p = z; rz = r.z; bnorm = max(|b|,1e-30);
+ * loop { Ap; pAp; if pAp == 0 -> last = sqrt(rz)/bnorm, return it;
+ *        alpha = rz/pAp; x += alpha p; r -= alpha Ap; last = |r|/bnorm;
+ *        if last < tol return it+1; z = M r; rzNew = r.z; beta = rzNew/rz;
+ *        p = z + beta p; rz = rzNew }  return maxIt.
+ * precond: 0 Jacobi, 1 ILU0; any other value is Jacobi (make_preconditioner's
+ * default branch, LinearSolvers.cpp:240-254).  hist (optional, maxIt long)
+ * receives last after each iteration.
+ */
+int orc_cg(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,
+           int precond, double tol, int maxIt, double *x, double *lastRes, double *hist)
+{
+    const int ilu = (precond == 1);
+    double *r = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *z = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *p = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *Ap = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *invD = NULL, *lu = NULL;
+    int32_t *diagPtr = NULL;
+    if (ilu) {
+        lu = (double *)xmalloc((size_t)rowPtr[n] * sizeof(double) + 8);
+        diagPtr = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
+        orc_ilu0_setup(n, rowPtr, colIdx, values, lu, diagPtr);
+    } else {
+        invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_jacobi_setup(n, rowPtr, colIdx, values, invD);
+    }
+#define APPLY_M()                                                                                             \
+    do {                                                                                                      \
+        if (ilu)                                                                                              \
+            orc_ilu0_apply(n, rowPtr, colIdx, lu, diagPtr, r, z, y);                                          \
+        else                                                                                                  \
+            for (int64_t i = 0; i < n; ++i)                                                                   \
+                z[i] = invD[i] * r[i];                                                                        \
+    } while (0)
+    for (int64_t i = 0; i < n; ++i) {
+        x[i] = 0.0;
+        r[i] = b[i];
+    }
+    APPLY_M();
+    memcpy(p, z, (size_t)n * sizeof(double));
+    double rz = orc_dot(n, r, z);
+    const double bn = norm2(n, b);
+    const double bnorm = STD_MAX(bn, 1e-30);
+    int ret = maxIt;
+    double last = 0.0;
+    for (int it = 0; it < maxIt; ++it) {
+        orc_spmv(n, rowPtr, colIdx, values, p, Ap);
+        const double pAp = orc_dot(n, p, Ap);
+        if (pAp == 0) {
+            last = sqrt(rz) / bnorm;
+            ret = it;
+            break;
+        }
+        const double alpha = rz / pAp;
+        axpy(n, alpha, p, x);
+        axpy(n, -alpha, Ap, r);
+        const double rn = norm2(n, r);
+        last = rn / bnorm;
+        if (hist)
+            hist[it] = last;
+        if (last < tol) {
+            ret = it + 1;
+            break;
+        }
+        APPLY_M();
+        const double rzNew = orc_dot(n, r, z);
+        const double beta = rzNew / rz;
+        for (int64_t i = 0; i < n; ++i)
+            p[i] = z[i] + beta * p[i];
+        rz = rzNew;
+    }
+#undef APPLY_M
+    *lastRes = last;
+    free(r);
+    free(z);
+    free(p);
+    free(Ap);
+    free(y);
+    free(invD);
+    free(lu);
+    free(diagPtr);
+    return ret;
+}
+
+/* ------------------------------------------------------------------ face-conductance extension */
+
+/*
+ * Face-conductance Poisson operator (an extension; the reference cannot
+ * express per-face k or non-zero Dirichlet values).  It restates the
+ * reference face coefficient (src/solver/SimpleAlgorithm.cpp:391-393, :417,
+ * :427) with k_f in place of 1/aP_f:
+ *   g_f    = rho*|A|^2 / max(|d.A|, 1e-30)   (d as in orc_assemble)
+ *   coef_f = k_f * g_f
+ * interior faces add +oo,-on,+nn,-no; a Dirichlet face (isDirichlet[f])
+ * adds +oo and rhs_o += coef_f * pb_f.  rhs starts from src (cell source).
+ * No pin is applied.  g receives g_f (0 for Neumann boundary faces).
+ */
+void orc_assemble_face_k(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor,
+                         const double *ax, const double *ay, const double *az, const double *fcx,
+                         const double *fcy, const double *fcz, const double *ccx, const double *ccy,
+                         const double *ccz, const uint8_t *isDirichlet, double rho, const double *k,
+                         const double *pb, const double *src, const int32_t *rowPtr, const int32_t *colIdx,
+                         double *values, double *rhs, double *g)
+{
+    const int64_t nnz = rowPtr[nC];
+    for (int64_t q = 0; q < nnz; ++q)
+        values[q] = 0.0;
+    for (int64_t c = 0; c < nC; ++c)
+        rhs[c] = src[c];
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        const double Ax = ax[f], Ay = ay[f], Az = az[f];
+        const double Amag2 = Ax * Ax + Ay * Ay + Az * Az;
+        double dx, dy, dz;
+        g[f] = 0.0;
+        if (n != ORC_BOUNDARY) {
+            dx = ccx[n] - ccx[o];
+            dy = ccy[n] - ccy[o];
+            dz = ccz[n] - ccz[o];
+        } else if (isDirichlet[f]) {
+            dx = fcx[f] - ccx[o];
+            dy = fcy[f] - ccy[o];
+            dz = fcz[f] - ccz[o];
+        } else {
+            continue;
+        }
+        const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+        const double gf = rho * Amag2 / STD_MAX(ddotA, 1e-30);
+        const double coef = k[f] * gf;
+        g[f] = gf;
+        if (n != ORC_BOUNDARY) {
+            add_at(rowPtr, colIdx, values, o, o, coef);
+            add_at(rowPtr, colIdx, values, o, n, -coef);
+            add_at(rowPtr, colIdx, values, n, n, coef);
+            add_at(rowPtr, colIdx, values, n, o, -coef);
+        } else {
+            add_at(rowPtr, colIdx, values, o, o, coef);
+            rhs[o] += coef * pb[f];
+        }
+    }
+}
+
+/*
+ * Adjoint gradient of L(x) with A(k) x = b(k, pb), given x and the adjoint
+ * lambda = A^-T dL/dx:
+ *   interior f:  dL/dk_f  = -g_f (lambda_o - lambda_n)(x_o - x_n)
+ *   Dirichlet f: dL/dk_f  = -g_f lambda_o (x_o - pb_f)
+ *                dL/dpb_f =  k_f g_f lambda_o
+ * Neumann boundary faces get 0.  This is -(dR/dalpha)^T lambda of
+ * solve_discrete_adjoint (src/adjoint/DiscreteAdjoint.cpp:170-182) for
+ * R = A(k) x - b(k, pb).
+ */
+void orc_face_k_gradient(int64_t nF, const int64_t *owner, const int64_t *neighbor, const uint8_t *isDirichlet,
+                         const double *g, const double *k, const double *pb, const double *x,
+                         const double *lambda, double *dk, double *dpb)
+{
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        dk[f] = 0.0;
+        dpb[f] = 0.0;
+        if (n != ORC_BOUNDARY) {
+            dk[f] = -g[f] * (lambda[o] - lambda[n]) * (x[o] - x[n]);
+        } else if (isDirichlet[f]) {
+            dk[f] = -g[f] * lambda[o] * (x[o] - pb[f]);
+            dpb[f] = k[f] * g[f] * lambda[o];
+        }
+    }
+}

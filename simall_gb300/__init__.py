@@ -1,0 +1,16 @@
+"""GB300 (sm_103a) pressure-correction path for SimAll.
+
+The face-loop assembly of the pressure-correction Laplacian and the
+preconditioned CG solve on it, as hand-written CUDA kernels behind a C ABI
+(include/simall_gpu.h, libsimall_gpu.so).  This package is the Python-side
+mirror of the reference's solver interface plus the mesh/assembly wrappers.
+"""
+from . import build
+from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
+from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
+from .solver import (Context, CSRMatrix, GpuCGSolver, LinearSolverConfig, LinearSolverKind, Precision,
+                     PreconditionerKind, default_context, make_cg, make_linear_solver)
+
+__all__ = ["build", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
+           "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
+           "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver"]

@@ -1,0 +1,457 @@
+// Pressure-correction assembly on the device: the GB300 replacement of
+// SimpleAlgorithm::build_sparsity + assemble_pressure_correction
+// (src/solver/SimpleAlgorithm.cpp:49-98, :358-447), SIMPLE variant, no
+// periodic twins.
+//
+// The reference walks the faces once and scatters each coefficient into four
+// CSR slots through a linear column search (find_col/add_at, :23-35).  Here:
+//   create()  builds the CSR pattern on the host exactly as build_sparsity
+//             does, lists every cell's faces in ascending face id together
+//             with the CSR slot of the neighbour column, and precomputes the
+//             static face geometry |A|^2 and |d.A| on the device from the
+//             mesh SoA (same operation order, no FMA contraction);
+//   assemble  k_face_coef  one thread per face: coef_f from aP (gathered);
+//             k_cell_rows  one thread per cell: writes its whole CSR row and
+//                          rhs entry, summing its faces' contributions in
+//                          ascending face id -- the order in which the
+//                          reference's face loop adds them -- so values and
+//                          rhs are bit-identical to the reference and no
+//                          atomics are needed.
+#include "device.cuh"
+#include "solver.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+struct simall_pressure_system {
+    simall_context *ctx = nullptr;
+    int64_t nC = 0, nF = 0, nnz = 0;
+    std::vector<int32_t> h_rowPtr, h_colIdx;
+    simall::DevBuf<int32_t> rowPtr, colIdx;
+    simall::DevBuf<double> values, rhs;
+    // faces
+    simall::DevBuf<int32_t> owner, neighbor;  // neighbor -1 on boundary faces
+    simall::DevBuf<double> amag2, ddotA;
+    simall::DevBuf<uint8_t> kind;  // 0 interior, 1 pressure boundary, 2 other boundary
+    simall::DevBuf<double> coef;
+    // cells: faces in ascending id; entry = face id | (cell is the neighbour) << 31;
+    // slot = CSR position of the other cell in the row (-1: none)
+    simall::DevBuf<int32_t> cfOff, cfEnt, cfSlot, diagSlot;
+    int anyDirichlet = 0;
+    simall::DevBuf<double> aP, phi;  // staging for host inputs
+};
+
+namespace simall {
+
+namespace {
+
+constexpr uint8_t kInterior = 0, kPressure = 1, kOtherBoundary = 2;
+
+// |A|^2 and |d.A| with the reference's operation order (SimpleAlgorithm.cpp:371-378, :417-420).
+__global__ void __launch_bounds__(kBlock) k_face_geometry(int64_t nF, const int32_t *__restrict__ owner,
+                                                          const int32_t *__restrict__ neighbor,
+                                                          const uint8_t *__restrict__ kind,
+                                                          const double *__restrict__ ax, const double *__restrict__ ay,
+                                                          const double *__restrict__ az, const double *__restrict__ fx,
+                                                          const double *__restrict__ fy, const double *__restrict__ fz,
+                                                          const double *__restrict__ cx, const double *__restrict__ cy,
+                                                          const double *__restrict__ cz, double *__restrict__ amag2,
+                                                          double *__restrict__ ddotA)
+{
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nF; f += (int64_t)gridDim.x * blockDim.x) {
+        const double Ax = ax[f], Ay = ay[f], Az = az[f];
+        amag2[f] = __dadd_rn(__dadd_rn(__dmul_rn(Ax, Ax), __dmul_rn(Ay, Ay)), __dmul_rn(Az, Az));
+        const int o = owner[f], n = neighbor[f];
+        double dx = 0.0, dy = 0.0, dz = 0.0;
+        if (n >= 0) {
+            dx = __dsub_rn(cx[n], cx[o]);
+            dy = __dsub_rn(cy[n], cy[o]);
+            dz = __dsub_rn(cz[n], cz[o]);
+        } else if (kind[f] == kPressure) {
+            dx = __dsub_rn(fx[f], cx[o]);
+            dy = __dsub_rn(fy[f], cy[o]);
+            dz = __dsub_rn(fz[f], cz[o]);
+        }
+        ddotA[f] = fabs(__dadd_rn(__dadd_rn(__dmul_rn(dx, Ax), __dmul_rn(dy, Ay)), __dmul_rn(dz, Az)));
+    }
+}
+
+// coef_f = rho |A|^2 / max(aPf |d.A|, 1e-30)   (SimpleAlgorithm.cpp:379-393, :421-428)
+__global__ void __launch_bounds__(kBlock) k_face_coef(int64_t nF, double rho, const int32_t *__restrict__ owner,
+                                                      const int32_t *__restrict__ neighbor,
+                                                      const uint8_t *__restrict__ kind,
+                                                      const double *__restrict__ amag2,
+                                                      const double *__restrict__ ddotA, const double *__restrict__ aP,
+                                                      double *__restrict__ coef)
+{
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nF; f += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t k = kind[f];
+        double c = 0.0;
+        if (k != kOtherBoundary) {
+            const int o = owner[f];
+            double den;
+            if (k == kInterior) {
+                const double dOwn = std_max(__ldg(aP + o), 1e-30);
+                const double dNbr = std_max(__ldg(aP + neighbor[f]), 1e-30);
+                const double aPf = __dmul_rn(0.5, __dadd_rn(dOwn, dNbr));
+                den = __dmul_rn(aPf, ddotA[f]);
+            } else {
+                den = __dmul_rn(std_max(__ldg(aP + o), 1e-30), ddotA[f]);
+            }
+            c = __ddiv_rn(__dmul_rn(rho, amag2[f]), std_max(den, 1e-30));
+        }
+        coef[f] = c;
+    }
+}
+
+// One CSR row and one rhs entry per thread, faces in ascending id.
+__global__ void __launch_bounds__(kBlock) k_cell_rows(int64_t nC, const int32_t *__restrict__ rowPtr,
+                                                      const int32_t *__restrict__ cfOff,
+                                                      const int32_t *__restrict__ cfEnt,
+                                                      const int32_t *__restrict__ cfSlot,
+                                                      const int32_t *__restrict__ diagSlot,
+                                                      const uint8_t *__restrict__ kind,
+                                                      const double *__restrict__ coef, const double *__restrict__ phi,
+                                                      int anyDirichlet, double *__restrict__ values,
+                                                      double *__restrict__ rhs)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nC; c += (int64_t)gridDim.x * blockDim.x) {
+        const int r0 = rowPtr[c], r1 = rowPtr[c + 1];
+        for (int k = r0; k < r1; ++k)
+            values[k] = 0.0;
+        double diag = 0.0, b = 0.0;
+        for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) {
+            const int ent = cfEnt[e];
+            const int f = ent & 0x7fffffff;
+            const bool isNbr = ent < 0;
+            const double cf = __ldg(coef + f);
+            const uint8_t k = kind[f];
+            if (k != kOtherBoundary)
+                diag = __dadd_rn(diag, cf);
+            if (k == kInterior) {
+                const int slot = cfSlot[e];
+                if (slot >= 0)
+                    values[slot] = __dadd_rn(values[slot], -cf);
+            }
+            const double ph = __ldg(phi + f);
+            b = isNbr ? __dadd_rn(b, ph) : __dsub_rn(b, ph);
+        }
+        const int kd = diagSlot[c];
+        if (!anyDirichlet && c == 0) {
+            diag = __dmul_rn(diag, 1.0e6);
+            b = 0.0;
+        }
+        values[kd] = diag;
+        rhs[c] = b;
+    }
+}
+
+}  // namespace
+
+}  // namespace simall
+
+using namespace simall;
+
+extern "C" {
+
+int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m, const simall_boundary *bcs,
+                                  int n_bcs, simall_pressure_system **out)
+{
+    if (!ctx || !m || !out || (n_bcs > 0 && !bcs) || n_bcs < 0)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    const int64_t nC = m->n_cells, nF = m->n_faces;
+    if (nC <= 0 || nF <= 0 || nC > INT32_MAX - 1 || nF > INT32_MAX - 1)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mesh sizes out of range");
+    if (!m->owner || !m->neighbor || !m->area_x || !m->area_y || !m->area_z || !m->centroid_x || !m->centroid_y ||
+        !m->centroid_z || !m->boundary_zone || !m->cell_centroid_x || !m->cell_centroid_y || !m->cell_centroid_z ||
+        !m->cell_face_offsets || !m->cell_face_indices)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mesh view has a null array");
+    for (int i = 0; i < n_bcs; ++i)
+        if (bcs[i].type == SIMALL_BC_PERIODIC)
+            return fail(ctx, SIMALL_ERR_UNSUPPORTED, "periodic boundaries are not supported by the device assembly");
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const uint64_t kB = ~0ull;
+    // ---- validate ids, classify faces
+    std::vector<int32_t> own(static_cast<size_t>(nF)), nbr(static_cast<size_t>(nF));
+    std::vector<uint8_t> kind(static_cast<size_t>(nF));
+    int anyD = 0;
+    for (int64_t f = 0; f < nF; ++f) {
+        const uint64_t o = m->owner[f], n = m->neighbor[f];
+        if (o >= static_cast<uint64_t>(nC) || (n != kB && n >= static_cast<uint64_t>(nC)))
+            return fail(ctx, SIMALL_ERR_INDEX_RANGE, "face %lld: owner/neighbor out of range",
+                        static_cast<long long>(f));
+        own[f] = static_cast<int32_t>(o);
+        nbr[f] = n == kB ? -1 : static_cast<int32_t>(n);
+        if (n != kB) {
+            kind[f] = kInterior;
+        } else {
+            // find_bc: first spec of the zone (SimpleAlgorithm.cpp:191-197)
+            int type = -1;
+            for (int i = 0; i < n_bcs; ++i)
+                if (bcs[i].zone == m->boundary_zone[f]) {
+                    type = bcs[i].type;
+                    break;
+                }
+            const bool p = (type == SIMALL_BC_PRESSURE_OUTLET || type == SIMALL_BC_PRESSURE_INLET);
+            kind[f] = p ? kPressure : kOtherBoundary;
+            anyD |= p ? 1 : 0;
+        }
+    }
+    if (m->cell_face_offsets[0] != 0)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "cell_face_offsets[0] != 0");
+    for (int64_t c = 0; c < nC; ++c)
+        if (m->cell_face_offsets[c + 1] < m->cell_face_offsets[c])
+            return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "cell_face_offsets not monotone at %lld",
+                        static_cast<long long>(c));
+    const int64_t ncf = m->cell_face_offsets[nC];
+    for (int64_t e = 0; e < ncf; ++e)
+        if (m->cell_face_indices[e] >= static_cast<uint64_t>(nF))
+            return fail(ctx, SIMALL_ERR_INDEX_RANGE, "cell face index out of range");
+    auto *ps = new (std::nothrow) simall_pressure_system;
+    if (!ps)
+        return SIMALL_ERR_OUT_OF_MEMORY;
+    ps->ctx = ctx;
+    ps->nC = nC;
+    ps->nF = nF;
+    ps->anyDirichlet = anyD;
+    // ---- sparsity (build_sparsity :62-82): {c} U other cells of c's faces, sorted, unique
+    ps->h_rowPtr.assign(static_cast<size_t>(nC) + 1, 0);
+    ps->h_colIdx.reserve(static_cast<size_t>(ncf) + static_cast<size_t>(nC));
+    std::vector<int32_t> diagSlot(static_cast<size_t>(nC));
+    {
+        std::vector<int32_t> nb;
+        for (int64_t c = 0; c < nC; ++c) {
+            nb.clear();
+            nb.push_back(static_cast<int32_t>(c));
+            for (int32_t e = m->cell_face_offsets[c]; e < m->cell_face_offsets[c + 1]; ++e) {
+                const int32_t f = static_cast<int32_t>(m->cell_face_indices[e]);
+                const int32_t oth = (own[f] == c) ? nbr[f] : own[f];
+                if (oth >= 0)
+                    nb.push_back(oth);
+            }
+            std::sort(nb.begin(), nb.end());
+            nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
+            const int32_t base = static_cast<int32_t>(ps->h_colIdx.size());
+            for (size_t t = 0; t < nb.size(); ++t) {
+                if (nb[t] == c)
+                    diagSlot[c] = base + static_cast<int32_t>(t);
+                ps->h_colIdx.push_back(nb[t]);
+            }
+            ps->h_rowPtr[c + 1] = static_cast<int32_t>(ps->h_colIdx.size());
+        }
+    }
+    // ---- per-cell face entries as the reference face loop (:366-440) sees them:
+    // every face touches its owner and, if interior, its neighbour; visiting
+    // faces in ascending id lists each cell's faces in that order.  The slot
+    // is the CSR position of the other cell in the cell's row, or -1 where
+    // add_at would find no column.
+    std::vector<int32_t> cfOff(static_cast<size_t>(nC) + 1, 0);
+    for (int64_t f = 0; f < nF; ++f) {
+        cfOff[own[f] + 1]++;
+        if (nbr[f] >= 0)
+            cfOff[nbr[f] + 1]++;
+    }
+    for (int64_t c = 0; c < nC; ++c)
+        cfOff[c + 1] += cfOff[c];
+    std::vector<int32_t> cfEnt(static_cast<size_t>(cfOff[nC])), cfSlot(static_cast<size_t>(cfOff[nC]));
+    {
+        std::vector<int32_t> fill(cfOff.begin(), cfOff.end() - 1);
+        auto slot_of = [&](int32_t row, int32_t col) -> int32_t {
+            const int32_t *b0 = ps->h_colIdx.data() + ps->h_rowPtr[row];
+            const int32_t *b1 = ps->h_colIdx.data() + ps->h_rowPtr[row + 1];
+            const int32_t *it = std::lower_bound(b0, b1, col);
+            return (it != b1 && *it == col) ? static_cast<int32_t>(it - ps->h_colIdx.data()) : -1;
+        };
+        for (int64_t f = 0; f < nF; ++f) {
+            const int32_t o = own[f], n = nbr[f];
+            int32_t w = fill[o]++;
+            cfEnt[w] = static_cast<int32_t>(f);
+            cfSlot[w] = n >= 0 ? slot_of(o, n) : -1;
+            if (n >= 0) {
+                w = fill[n]++;
+                cfEnt[w] = static_cast<int32_t>(static_cast<uint32_t>(f) | 0x80000000u);
+                cfSlot[w] = slot_of(n, o);
+            }
+        }
+    }
+    ps->nnz = static_cast<int64_t>(ps->h_colIdx.size());
+    // ---- upload
+    cudaStream_t st = ctx->stream;
+    const size_t nEnt = cfEnt.size();
+    auto up = [&](void *dst, const void *src, size_t bytes) {
+        return cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, st);
+    };
+    int rc = SIMALL_OK;
+#define PS_TRY(call)                                                                                                    \
+    do {                                                                                                                \
+        cudaError_t e_ = (call);                                                                                        \
+        if (e_ != cudaSuccess) {                                                                                        \
+            rc = cuda_fail(ctx, e_, #call, __FILE__, __LINE__);                                                         \
+            goto fail_out;                                                                                              \
+        }                                                                                                               \
+    } while (0)
+    {
+        PS_TRY(ps->rowPtr.alloc(nC + 1));
+        PS_TRY(ps->colIdx.alloc(ps->nnz));
+        PS_TRY(ps->values.alloc(ps->nnz + 2));
+        PS_TRY(ps->rhs.alloc(nC + 2));
+        PS_TRY(ps->owner.alloc(nF));
+        PS_TRY(ps->neighbor.alloc(nF));
+        PS_TRY(ps->amag2.alloc(nF));
+        PS_TRY(ps->ddotA.alloc(nF));
+        PS_TRY(ps->kind.alloc(nF));
+        PS_TRY(ps->coef.alloc(nF));
+        PS_TRY(ps->cfOff.alloc(nC + 1));
+        PS_TRY(ps->cfEnt.alloc(nEnt ? nEnt : 1));
+        PS_TRY(ps->cfSlot.alloc(nEnt ? nEnt : 1));
+        PS_TRY(ps->diagSlot.alloc(nC));
+        PS_TRY(up(ps->rowPtr.p, ps->h_rowPtr.data(), (nC + 1) * sizeof(int32_t)));
+        PS_TRY(up(ps->colIdx.p, ps->h_colIdx.data(), ps->nnz * sizeof(int32_t)));
+        PS_TRY(up(ps->owner.p, own.data(), nF * sizeof(int32_t)));
+        PS_TRY(up(ps->neighbor.p, nbr.data(), nF * sizeof(int32_t)));
+        PS_TRY(up(ps->kind.p, kind.data(), nF));
+        PS_TRY(up(ps->cfOff.p, cfOff.data(), (nC + 1) * sizeof(int32_t)));
+        if (nEnt) {
+            PS_TRY(up(ps->cfEnt.p, cfEnt.data(), nEnt * sizeof(int32_t)));
+            PS_TRY(up(ps->cfSlot.p, cfSlot.data(), nEnt * sizeof(int32_t)));
+        }
+        PS_TRY(up(ps->diagSlot.p, diagSlot.data(), nC * sizeof(int32_t)));
+        // geometry (temporary device copies of the SoA arrays the kernel reads)
+        DevBuf<double> g[9];
+        const double *src[9] = {m->area_x,     m->area_y,     m->area_z,          m->centroid_x,     m->centroid_y,
+                                m->centroid_z, m->cell_centroid_x, m->cell_centroid_y, m->cell_centroid_z};
+        for (int i = 0; i < 9; ++i) {
+            const int64_t cnt = i < 6 ? nF : nC;
+            PS_TRY(g[i].alloc(cnt));
+            PS_TRY(up(g[i].p, src[i], cnt * sizeof(double)));
+        }
+        const int64_t gg = std::min<int64_t>((nF + kBlock - 1) / kBlock, grid_size_streaming(ctx));
+        k_face_geometry<<<static_cast<int>(gg), kBlock, 0, st>>>(nF, ps->owner.p, ps->neighbor.p, ps->kind.p, g[0].p,
+                                                                 g[1].p, g[2].p, g[3].p, g[4].p, g[5].p, g[6].p, g[7].p,
+                                                                 g[8].p, ps->amag2.p, ps->ddotA.p);
+        ctx->launches.fetch_add(1, std::memory_order_relaxed);
+        PS_TRY(cudaGetLastError());
+        PS_TRY(cudaStreamSynchronize(st));  // host vectors and temporaries die at scope exit
+    }
+#undef PS_TRY
+    *out = ps;
+    return SIMALL_OK;
+fail_out:
+    delete ps;
+    return rc;
+}
+
+int simall_pressure_system_destroy(simall_pressure_system *ps)
+{
+    if (!ps)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(ps->ctx->stream);
+    delete ps;
+    return SIMALL_OK;
+}
+
+int simall_pressure_system_pattern(const simall_pressure_system *ps, int64_t *n, int64_t *nnz, int32_t *rowPtr,
+                                   int32_t *colIdx)
+{
+    if (!ps)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (n)
+        *n = ps->nC;
+    if (nnz)
+        *nnz = ps->nnz;
+    if (rowPtr)
+        std::memcpy(rowPtr, ps->h_rowPtr.data(), (ps->nC + 1) * sizeof(int32_t));
+    if (colIdx)
+        std::memcpy(colIdx, ps->h_colIdx.data(), ps->nnz * sizeof(int32_t));
+    return SIMALL_OK;
+}
+
+int simall_pressure_system_device_arrays(const simall_pressure_system *ps, const int32_t **rowPtr,
+                                         const int32_t **colIdx, double **values, double **rhs)
+{
+    if (!ps)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (rowPtr)
+        *rowPtr = ps->rowPtr.p;
+    if (colIdx)
+        *colIdx = ps->colIdx.p;
+    if (values)
+        *values = ps->values.p;
+    if (rhs)
+        *rhs = ps->rhs.p;
+    return SIMALL_OK;
+}
+
+int simall_assemble_pressure_correction(simall_pressure_system *ps, double rho, const double *aP, const double *phi,
+                                        int mem, int *any_dirichlet)
+{
+    if (!ps || !aP || !phi)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = ps->ctx;
+    if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "assemble: bad memory kind %d", mem);
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const double *dA = aP, *dPhi = phi;
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, ps->aP.alloc(ps->nC));
+        SIMALL_CUDA_TRY(ctx, ps->phi.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(ps->aP.p, aP, ps->nC * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(ps->phi.p, phi, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        dA = ps->aP.p;
+        dPhi = ps->phi.p;
+    }
+    const int gf = static_cast<int>(std::min<int64_t>((ps->nF + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    const int gc = static_cast<int>(std::min<int64_t>((ps->nC + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    k_face_coef<<<gf, kBlock, 0, st>>>(ps->nF, rho, ps->owner.p, ps->neighbor.p, ps->kind.p, ps->amag2.p, ps->ddotA.p,
+                                       dA, ps->coef.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_cell_rows<<<gc, kBlock, 0, st>>>(ps->nC, ps->rowPtr.p, ps->cfOff.p, ps->cfEnt.p, ps->cfSlot.p, ps->diagSlot.p,
+                                       ps->kind.p, ps->coef.p, dPhi, ps->anyDirichlet, ps->values.p, ps->rhs.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (mem == SIMALL_MEM_HOST)
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // staging buffers are reused by the next call
+    if (any_dirichlet)
+        *any_dirichlet = ps->anyDirichlet;
+    return SIMALL_OK;
+}
+
+int simall_pressure_system_download(const simall_pressure_system *ps, double *values, double *rhs)
+{
+    if (!ps)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = ps->ctx;
+    if (values)
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(values, ps->values.p, ps->nnz * sizeof(double), cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+    if (rhs)
+        SIMALL_CUDA_TRY(ctx,
+                        cudaMemcpyAsync(rhs, ps->rhs.p, ps->nC * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return SIMALL_OK;
+}
+
+int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *ps)
+{
+    if (!s || !ps)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (s->ready && s->n == ps->nC && s->nnz == ps->nnz && s->rowPtr == ps->rowPtr.p && s->values == ps->values.p)
+        return simall_solver_update_values(s, ps->values.p, SIMALL_MEM_DEVICE);
+    return simall_solver_set_matrix(s, ps->nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->values.p, SIMALL_MEM_DEVICE);
+}
+
+int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,
+                                 simall_solver_stats *stats)
+{
+    if (!ps || !s || !x)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    int st = simall_solver_use_pressure_system(s, ps);
+    if (st)
+        return st;
+    return solver_solve_impl(s, ps->rhs.p, SIMALL_MEM_DEVICE, x, mem, stats);
+}
+
+}  // extern "C"

@@ -1,0 +1,122 @@
+// Device helpers: deterministic block/grid reductions and the staged CSR
+// row-block SpMV shared by the solver kernels.
+#pragma once
+
+#include "internal.hpp"
+
+#include <cuda_runtime.h>
+
+namespace simall {
+
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;  // valid in lane 0
+}
+
+// Sum of NV values over the block in a fixed tree; the result is valid in
+// thread 0.  Every thread of the block must call it.
+template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV])
+{
+    __shared__ double red[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        v[k] = warp_sum(v[k]);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            red[k][wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            v[k] = warp_sum(lane < nw ? red[k][lane] : 0.0);
+    }
+    __syncthreads();
+}
+
+// Grid-wide sum: every block deposits its block sum in partials[k*gridDim.x+b]
+// and takes a ticket; the last block to arrive sums the partials in index
+// order (fixed for a fixed grid, so the result is reproducible run to run),
+// resets the ticket and returns true with the totals in thread 0's v.
+template <int NV> __device__ __forceinline__ bool grid_sum_last(double (&v)[NV], double *partials, unsigned *ticket)
+{
+    __shared__ unsigned s_last;
+    block_sum<NV>(v);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            partials[k * gridDim.x + blockIdx.x] = v[k];
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last)
+        return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        acc[k] = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+            acc[k] += __ldcg(&partials[k * gridDim.x + b]);
+    }
+    block_sum<NV>(acc);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            v[k] = acc[k];
+        *ticket = 0u;
+    }
+    return true;
+}
+
+// y-rows of A x for the row-blocks this CTA owns (blockIdx.x, +gridDim.x, ...).
+// Each product a_ij*x_j is rounded once into shared memory and every row is
+// summed from 0.0 in column order with separate roundings, the same operation
+// sequence as CSRMatrix::spmv (src/solver/CSRMatrix.hpp:24-35), so the result
+// is bit-identical to it.  epi(row, y_row) consumes each row.
+template <class Epi>
+__device__ __forceinline__ void spmv_rowblocks(const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
+                                               const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                               int nRB, const double *__restrict__ x, Epi &epi)
+{
+    __shared__ double prod[kSpmvNnzCap];
+    for (int b = blockIdx.x; b < nRB; b += gridDim.x) {
+        const int r0 = __ldg(rb + b), r1 = __ldg(rb + b + 1);
+        const int base = __ldg(rowPtr + r0);
+        const int cnt = __ldg(rowPtr + r1) - base;
+        if (cnt <= kSpmvNnzCap) {
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+                prod[k] = __dmul_rn(__ldg(val + base + k), __ldg(x + __ldg(colIdx + base + k)));
+            __syncthreads();
+            for (int row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
+                const int k0 = __ldg(rowPtr + row) - base, k1 = __ldg(rowPtr + row + 1) - base;
+                double s = 0.0;
+                for (int k = k0; k < k1; ++k)
+                    s = __dadd_rn(s, prod[k]);
+                epi(row, s);
+            }
+            __syncthreads();
+        } else {
+            // one row longer than the staging buffer: block-strided sum
+            double s[1] = {0.0};
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+                s[0] += __ldg(val + base + k) * __ldg(x + __ldg(colIdx + base + k));
+            block_sum<1>(s);
+            if (threadIdx.x == 0)
+                epi(r0, s[0]);
+            __syncthreads();
+        }
+    }
+}
+
+// std::max(a, b) as the reference evaluates it.
+__device__ __forceinline__ double std_max(double a, double b) { return (a < b) ? b : a; }
+
+}  // namespace simall

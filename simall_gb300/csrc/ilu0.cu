@@ -1,0 +1,363 @@
+// Level-scheduled ILU(0) on the device.
+//
+// ILU0Preconditioner::setup (src/solver/LinearSolvers.cpp:81-122) factors row
+// i using only rows k < i of its own lower pattern, each already final, and
+// the triangular sweeps of ILU0Preconditioner::apply (:123-151) have the same
+// dependency structure.  Grouping rows into dependency levels (row i's level
+// is one more than the deepest row it reads) lets every row of a level run in
+// parallel while each row keeps the reference's exact sequence of operations:
+// products and differences are rounded separately (__dmul_rn/__dsub_rn) and
+// in column order, so the factor and both sweeps are bit-identical to the
+// reference.  Multicolouring would be faster but changes the factor.
+#include "device.cuh"
+#include "solver.hpp"
+
+#include <algorithm>
+#include <new>
+
+namespace simall {
+
+namespace {
+
+// One level of the IKJ factorisation, one thread per row.
+__global__ void __launch_bounds__(kBlock) k_ilu_factor_level(const int32_t *__restrict__ rows, int cnt,
+                                                             const int32_t *__restrict__ rowPtr,
+                                                             const int32_t *__restrict__ colIdx,
+                                                             const int32_t *__restrict__ diagPtr, double *lu)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt)
+        return;
+    const int i = rows[t];
+    const int end = rowPtr[i + 1];
+    for (int kp = rowPtr[i]; kp < end; ++kp) {
+        const int k = colIdx[kp];
+        if (k >= i)
+            break;
+        const int dk = diagPtr[k];
+        if (dk < 0)
+            continue;
+        const double piv = lu[dk];
+        if (piv == 0.0)
+            continue;
+        const double m = __ddiv_rn(lu[kp], piv);
+        lu[kp] = m;
+        const int kend = rowPtr[k + 1];
+        for (int jp = dk + 1; jp < kend; ++jp) {
+            const int j = colIdx[jp];
+            for (int qp = kp + 1; qp < end; ++qp) {
+                const int c = colIdx[qp];
+                if (c == j) {
+                    lu[qp] = __dsub_rn(lu[qp], __dmul_rn(m, lu[jp]));
+                    break;
+                }
+                if (c > j)
+                    break;
+            }
+        }
+    }
+}
+
+// Forward sweep of one level: y_i = r_i - sum_{j<i} l_ij y_j.
+__global__ void __launch_bounds__(kBlock) k_ilu_fwd_level(const int32_t *__restrict__ rows, int cnt,
+                                                          const int32_t *__restrict__ rowPtr,
+                                                          const int32_t *__restrict__ colIdx,
+                                                          const double *__restrict__ lu, const double *__restrict__ r,
+                                                          double *y)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt)
+        return;
+    const int i = rows[t];
+    double s = r[i];
+    for (int kp = rowPtr[i]; kp < rowPtr[i + 1]; ++kp) {
+        const int j = colIdx[kp];
+        if (j >= i)
+            break;
+        s = __dsub_rn(s, __dmul_rn(lu[kp], __ldcg(y + j)));
+    }
+    y[i] = s;
+}
+
+// Backward sweep of one level: z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii.
+__global__ void __launch_bounds__(kBlock) k_ilu_bwd_level(const int32_t *__restrict__ rows, int cnt,
+                                                          const int32_t *__restrict__ rowPtr,
+                                                          const int32_t *__restrict__ colIdx,
+                                                          const int32_t *__restrict__ diagPtr,
+                                                          const double *__restrict__ lu, const double *__restrict__ y,
+                                                          double *z)
+{
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= cnt)
+        return;
+    const int i = rows[t];
+    double s = y[i];
+    const int kd = diagPtr[i];
+    for (int kp = kd + 1; kp < rowPtr[i + 1]; ++kp)
+        s = __dsub_rn(s, __dmul_rn(lu[kp], __ldcg(z + colIdx[kp])));
+    z[i] = (kd >= 0 && lu[kd] != 0.0) ? __ddiv_rn(s, lu[kd]) : s;
+}
+
+__global__ void k_zero_pivot_check(int n, const int32_t *__restrict__ diagPtr, const double *__restrict__ lu, int *flag)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int d = diagPtr[i];
+        if (d < 0 || lu[d] == 0.0)
+            atomicOr(flag, 1);
+    }
+}
+
+// Rows grouped by level; `lower` selects the forward (j < i) or backward
+// (j > i) dependency structure.
+void levels(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const std::vector<int32_t> &diagPtr, bool lower,
+            std::vector<int32_t> &rowsOut, std::vector<int32_t> &levelPtr, int &maxRows)
+{
+    std::vector<int32_t> lev(static_cast<size_t>(n), 0);
+    int nlev = 0;
+    if (lower) {
+        for (int64_t i = 0; i < n; ++i) {
+            int l = 0;
+            for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+                const int j = colIdx[k];
+                if (j >= i)
+                    break;
+                l = std::max(l, lev[j] + 1);
+            }
+            lev[i] = l;
+            nlev = std::max(nlev, l + 1);
+        }
+    } else {
+        for (int64_t i = n - 1; i >= 0; --i) {
+            int l = 0;
+            const int kd = diagPtr[i];
+            // the backward sweep reads columns after the diagonal (or the
+            // whole row when the diagonal is missing, as the reference's
+            // kd+1 = 0 start does; such rows are rejected before we get here)
+            for (int k = kd + 1; k < rowPtr[i + 1]; ++k) {
+                const int j = colIdx[k];
+                if (j > i)
+                    l = std::max(l, lev[j] + 1);
+            }
+            lev[i] = l;
+            nlev = std::max(nlev, l + 1);
+        }
+    }
+    levelPtr.assign(static_cast<size_t>(nlev) + 1, 0);
+    for (int64_t i = 0; i < n; ++i)
+        levelPtr[lev[i] + 1]++;
+    maxRows = 0;
+    for (int l = 0; l < nlev; ++l) {
+        maxRows = std::max(maxRows, levelPtr[l + 1]);
+        levelPtr[l + 1] += levelPtr[l];
+    }
+    rowsOut.resize(static_cast<size_t>(n));
+    std::vector<int32_t> fill(levelPtr.begin(), levelPtr.end() - 1);
+    for (int64_t i = 0; i < n; ++i)
+        rowsOut[fill[lev[i]]++] = static_cast<int32_t>(i);
+}
+
+int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, const int32_t *colIdx)
+{
+    d->h_diagPtr.assign(static_cast<size_t>(n), -1);
+    for (int64_t i = 0; i < n; ++i)
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                d->h_diagPtr[i] = k;
+                break;
+            }
+    std::vector<int32_t> fr, br;
+    int m1 = 0, m2 = 0;
+    levels(n, rowPtr, colIdx, d->h_diagPtr, true, fr, d->fwdLevelPtr, m1);
+    levels(n, rowPtr, colIdx, d->h_diagPtr, false, br, d->bwdLevelPtr, m2);
+    d->maxLevelRows = std::max(m1, m2);
+    SIMALL_CUDA_TRY(ctx, d->diagPtr.alloc(n));
+    SIMALL_CUDA_TRY(ctx, d->fwdRows.alloc(n));
+    SIMALL_CUDA_TRY(ctx, d->bwdRows.alloc(n));
+    SIMALL_CUDA_TRY(ctx, d->y.alloc(n));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->diagPtr.p, d->h_diagPtr.data(), n * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->fwdRows.p, fr.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->bwdRows.p, br.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    // the copies above read host vectors that die at return
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    d->analysed = true;
+    return SIMALL_OK;
+}
+
+int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx)
+{
+    const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
+    for (int l = 1; l < nlev; ++l) {  // level 0 rows have no lower entries
+        const int a = d->fwdLevelPtr[l], cnt = d->fwdLevelPtr[l + 1] - a;
+        k_ilu_factor_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->fwdRows.p + a, cnt, rowPtr,
+                                                                                    colIdx, d->diagPtr.p, d->lu.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    return SIMALL_OK;
+}
+
+int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx, const double *lu,
+           const double *r, double *z)
+{
+    const int nf = static_cast<int>(d->fwdLevelPtr.size()) - 1;
+    for (int l = 0; l < nf; ++l) {
+        const int a = d->fwdLevelPtr[l], cnt = d->fwdLevelPtr[l + 1] - a;
+        k_ilu_fwd_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->fwdRows.p + a, cnt, rowPtr,
+                                                                                 colIdx, lu, r, d->y.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    const int nb = static_cast<int>(d->bwdLevelPtr.size()) - 1;
+    for (int l = 0; l < nb; ++l) {
+        const int a = d->bwdLevelPtr[l], cnt = d->bwdLevelPtr[l + 1] - a;
+        k_ilu_bwd_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->bwdRows.p + a, cnt, rowPtr,
+                                                                                 colIdx, d->diagPtr.p, lu, d->y.p, z);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    return SIMALL_OK;
+}
+
+}  // namespace
+
+int ilu_setup(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    if (!s->ilu) {
+        s->ilu = new (std::nothrow) IluData;
+        if (!s->ilu)
+            return SIMALL_ERR_OUT_OF_MEMORY;
+    }
+    IluData *d = s->ilu;
+    if (!d->analysed) {
+        int st = analyse(ctx, d, s->n, s->h_rowPtr.data(), s->h_colIdx.data());
+        if (st)
+            return st;
+    }
+    SIMALL_CUDA_TRY(ctx, d->lu.alloc(s->nnz));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->lu.p, s->values, s->nnz * sizeof(double), cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+    return factor(ctx, d, s->rowPtr, s->colIdx);
+}
+
+int ilu_apply(simall_solver *s, const double *r, double *z)
+{
+    return sweeps(s->ctx, s->ilu, s->rowPtr, s->colIdx, s->ilu->lu.p, r, z);
+}
+
+void ilu_free(simall_solver *s)
+{
+    delete s->ilu;
+    s->ilu = nullptr;
+}
+
+}  // namespace simall
+
+using namespace simall;
+
+// ---------------------------------------------------------------- reference facade (GpuKernels.hpp:89-108)
+namespace {
+struct FacadeIlu {
+    simall_context ctx;
+    IluData d;
+};
+
+int facade_ctx(simall_context &ctx, void *stream)
+{
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess)
+        return SIMALL_ERR_NO_DEVICE;
+    ctx.device = dev;
+    if (cudaDeviceGetAttribute(&ctx.num_sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return SIMALL_ERR_CUDA;
+    ctx.stream = static_cast<cudaStream_t>(stream);
+    return SIMALL_OK;
+}
+
+int facade_pattern(simall_context &ctx, size_t n, const int32_t *rowPtr, const int32_t *colIdx,
+                   std::vector<int32_t> &hr, std::vector<int32_t> &hc)
+{
+    hr.resize(n + 1);
+    SIMALL_CUDA_TRY(&ctx, cudaMemcpyAsync(hr.data(), rowPtr, (n + 1) * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          ctx.stream));
+    SIMALL_CUDA_TRY(&ctx, cudaStreamSynchronize(ctx.stream));
+    hc.resize(static_cast<size_t>(hr[n]));
+    SIMALL_CUDA_TRY(&ctx, cudaMemcpyAsync(hc.data(), colIdx, hc.size() * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                          ctx.stream));
+    SIMALL_CUDA_TRY(&ctx, cudaStreamSynchronize(ctx.stream));
+    return check_csr_host(&ctx, static_cast<int64_t>(n), hr[n], hr.data(), hc.data(), nullptr, false);
+}
+}  // namespace
+
+extern "C" {
+
+int simall_gpu_ilu0_factor_inplace(size_t n, const int32_t *rowPtr, const int32_t *colIdx, double *values,
+                                   void *stream, int *ok)
+{
+    if (!rowPtr || !colIdx || !values || !ok)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    *ok = 0;
+    if (n == 0) {
+        *ok = 1;
+        return SIMALL_OK;
+    }
+    auto *f = new (std::nothrow) FacadeIlu;
+    if (!f)
+        return SIMALL_ERR_OUT_OF_MEMORY;
+    std::vector<int32_t> hr, hc;
+    int st = facade_ctx(f->ctx, stream);
+    if (!st)
+        st = facade_pattern(f->ctx, n, rowPtr, colIdx, hr, hc);
+    if (!st)
+        st = analyse(&f->ctx, &f->d, static_cast<int64_t>(n), hr.data(), hc.data());
+    if (!st) {
+        // factor in place: point lu at the caller's values
+        double *saved = f->d.lu.p;
+        f->d.lu.p = values;
+        st = factor(&f->ctx, &f->d, rowPtr, colIdx);
+        f->d.lu.p = saved;
+    }
+    if (!st) {
+        st = f->d.y.alloc(1) == cudaSuccess ? SIMALL_OK : SIMALL_ERR_OUT_OF_MEMORY;
+        int *flag = reinterpret_cast<int *>(f->d.y.p);
+        if (!st && cudaMemsetAsync(flag, 0, sizeof(int), f->ctx.stream) != cudaSuccess)
+            st = SIMALL_ERR_CUDA;
+        if (!st) {
+            k_zero_pivot_check<<<64, kBlock, 0, f->ctx.stream>>>(static_cast<int>(n), f->d.diagPtr.p, values, flag);
+            int h = 1;
+            if (cudaMemcpyAsync(&h, flag, sizeof(int), cudaMemcpyDeviceToHost, f->ctx.stream) != cudaSuccess ||
+                cudaStreamSynchronize(f->ctx.stream) != cudaSuccess)
+                st = SIMALL_ERR_CUDA;
+            else
+                *ok = h ? 0 : 1;
+        }
+    }
+    delete f;
+    return st;
+}
+
+int simall_gpu_ilu0_apply(size_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                          const double *r, double *z, void *stream)
+{
+    if (!rowPtr || !colIdx || !values || !r || !z)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (n == 0)
+        return SIMALL_OK;
+    auto *f = new (std::nothrow) FacadeIlu;
+    if (!f)
+        return SIMALL_ERR_OUT_OF_MEMORY;
+    std::vector<int32_t> hr, hc;
+    int st = facade_ctx(f->ctx, stream);
+    if (!st)
+        st = facade_pattern(f->ctx, n, rowPtr, colIdx, hr, hc);
+    if (!st)
+        st = analyse(&f->ctx, &f->d, static_cast<int64_t>(n), hr.data(), hc.data());
+    if (!st)
+        st = sweeps(&f->ctx, &f->d, rowPtr, colIdx, values, r, z);
+    if (!st && cudaStreamSynchronize(f->ctx.stream) != cudaSuccess)
+        st = SIMALL_ERR_CUDA;
+    delete f;
+    return st;
+}
+
+}  // extern "C"

@@ -1,0 +1,689 @@
+// Mixed-precision Jacobi-PCG: FP32 inner iteration, FP64 true residual,
+// global reductions and solution.
+//
+// Jacobi PCG on A is plain CG on the scaled matrix S A S (S = D^-1/2, unit
+// diagonal) in the variables y = S^-1 x.  The inner iteration runs that CG in
+// FP32 on an FP32 copy of S A S; its correction accumulates in an FP32 vector
+// that is folded into the FP64 solution x at "reliable updates" (residual
+// replacement, van der Vorst & Ye 2000; Strzodka & Goddeke 2006): whenever the
+// iterated residual has dropped by reliable_delta since the last update, or
+// its estimate says the stop test may hold, x += S xh in FP64, the true
+// residual r = b - A x is recomputed in FP64 with the original CSR, the stop
+// test ||r|| / max(||b||,1e-30) < tol is applied to it, and the FP32 residual
+// is replaced by S r.  The search direction is kept, so the Krylov process is
+// not restarted.  Per-thread partial sums are FP32; every cross-thread and
+// cross-CTA reduction is FP64.
+//
+// Storage of S A S: when A is numerically symmetric and its off-diagonal
+// entries lie on at most kMaxDiags distinct diagonals (every structured grid
+// in natural order), only the upper diagonals are stored, FP32, one array per
+// offset: 4 B per stored diagonal per row and no column indices.  Otherwise
+// the off-diagonal entries are kept as FP32 CSR.
+#include "device.cuh"
+#include "solver.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <new>
+
+namespace simall {
+
+constexpr int kMaxDiags = 8;
+
+struct DiaOffsets {
+    int32_t off[kMaxDiags];
+    int nd;
+};
+
+struct MixedData {
+    bool dia = false;
+    DiaOffsets offs{};
+    DevBuf<float> U;          // [nd][n] upper diagonals of S A S (dia)
+    DevBuf<int32_t> orow;     // off-diagonal CSR rowPtr (csr)
+    DevBuf<int32_t> ocol;
+    DevBuf<float> oval;
+    DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
+    DevBuf<float> xh, rh, ph, qh;
+    int nnzOff = 0;
+    bool patternReady = false;
+    std::vector<int32_t> h_orow, h_ocol, h_opos;  // csr: host pattern and the source position of each entry
+    DevBuf<int32_t> opos;
+};
+
+namespace {
+
+__device__ __forceinline__ int ld_flag(const int *p) { return __ldcg(p); }
+
+// s_i = 1/sqrt(a_ii); flag if a_ii <= 0.
+__global__ void __launch_bounds__(kBlock) k_mx_scale(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                     const int32_t *__restrict__ colIdx, const double *__restrict__ val,
+                                                     double *__restrict__ sc, int *flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = 0.0;
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                d = val[k];
+                break;
+            }
+        if (!(d > 0.0)) {
+            atomicOr(flag, 1);
+            d = 1.0;
+        }
+        sc[i] = 1.0 / sqrt(d);
+    }
+}
+
+// Numerical symmetry: a_ji must exist and equal a_ij bit for bit.
+__global__ void __launch_bounds__(kBlock) k_mx_symcheck(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                        const int32_t *__restrict__ colIdx,
+                                                        const double *__restrict__ val, int *flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int j = colIdx[k];
+            if (j <= i)
+                continue;
+            int lo = rowPtr[j], hi = rowPtr[j + 1] - 1, pos = -1;
+            while (lo <= hi) {
+                const int mid = (lo + hi) >> 1;
+                const int c = colIdx[mid];
+                if (c == i) {
+                    pos = mid;
+                    break;
+                }
+                if (c < i)
+                    lo = mid + 1;
+                else
+                    hi = mid - 1;
+            }
+            if (pos < 0 || val[pos] != val[k])
+                atomicOr(flag, 2);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_build_dia(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                         const int32_t *__restrict__ colIdx,
+                                                         const double *__restrict__ val, const double *__restrict__ sc,
+                                                         DiaOffsets o, float *__restrict__ U)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        float u[kMaxDiags];
+#pragma unroll
+        for (int d = 0; d < kMaxDiags; ++d)
+            u[d] = 0.0f;
+        const double si = sc[i];
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int j = colIdx[k];
+            if (j <= i)
+                continue;
+            const int off = j - static_cast<int>(i);
+#pragma unroll
+            for (int d = 0; d < kMaxDiags; ++d)
+                if (d < o.nd && o.off[d] == off)
+                    u[d] = static_cast<float>(val[k] * si * sc[j]);
+        }
+        for (int d = 0; d < o.nd; ++d)
+            U[d * n + i] = u[d];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_build_csr(int nOff, const int32_t *__restrict__ orowOfEntry,
+                                                         const int32_t *__restrict__ ocol,
+                                                         const int32_t *__restrict__ opos,
+                                                         const double *__restrict__ val, const double *__restrict__ sc,
+                                                         float *__restrict__ oval)
+{
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nOff; e += gridDim.x * blockDim.x)
+        oval[e] = static_cast<float>(val[opos[e]] * sc[orowOfEntry[e]] * sc[ocol[e]]);
+}
+
+// ---------------------------------------------------------------- iteration kernels
+// Init: x = 0, rh = S b, ph = rh, xh = 0; rho = rh.rh, ||b||.
+__global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__restrict__ b,
+                                                    const double *__restrict__ sc, double *__restrict__ x,
+                                                    float *__restrict__ rh, float *__restrict__ ph,
+                                                    float *__restrict__ xh, double *partials, SolveScalars *s)
+{
+    float a0 = 0.0f;
+    double a1 = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double bi = b[i];
+        const float r = static_cast<float>(bi * sc[i]);
+        x[i] = 0.0;
+        rh[i] = r;
+        ph[i] = r;
+        xh[i] = 0.0f;
+        a0 += r * r;
+        a1 += bi * bi;
+    }
+    double acc[2] = {static_cast<double>(a0), a1};
+    if (grid_sum_last<2>(acc, partials, &s->counter[0]) && threadIdx.x == 0) {
+        const double bn = sqrt(acc[1]);
+        s->bnorm = std_max(bn, 1e-30);
+        s->rz = acc[0];
+        s->sigma0 = sqrt(acc[0]);
+        s->rmax = s->sigma0;
+        s->t0 = bn / s->bnorm;
+        s->last = s->t0;
+        s->rr = acc[1];
+        s->iter = 0;
+        s->updates = 0;
+        s->need_update = 0;
+        s->status = SIMALL_OK;
+        s->done = 0;
+        s->result = 0;
+        if (s->t0 < s->tol) {
+            s->done = 1;  // b == 0: x = 0 is exact
+        } else if (s->max_iter <= 0) {
+            s->done = 1;
+            s->result = s->max_iter;
+        }
+    }
+}
+
+// alpha from pq (shared by both storage formats).  Thread 0 of the last CTA.
+__device__ __forceinline__ void mx_alpha(SolveScalars *s, double pq)
+{
+    s->pAp = pq;
+    if (!(pq > 0.0)) {
+        // not SPD in FP32 (or exact breakdown): fold in what we have and stop
+        s->status = SIMALL_ERR_BREAKDOWN;
+        s->need_update = 1;
+        s->alpha = 0.0;
+    } else {
+        s->alpha = s->rz / pq;
+    }
+}
+
+// K1 (dia): qh = (S A S) ph, pq = ph.qh.
+__global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int64_t n, DiaOffsets o, const float *__restrict__ U,
+                                                        const float *__restrict__ ph, float *__restrict__ qh,
+                                                        double *partials, SolveScalars *s)
+{
+    if (ld_flag(&s->done))
+        return;
+    float acc = 0.0f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float pi = __ldg(ph + i);
+        float y = pi;
+#pragma unroll
+        for (int d = 0; d < kMaxDiags; ++d) {
+            if (d >= o.nd)
+                break;
+            const int64_t off = o.off[d];
+            if (i + off < n)
+                y += __ldg(U + d * n + i) * __ldg(ph + i + off);
+            if (i - off >= 0)
+                y += __ldg(U + d * n + i - off) * __ldg(ph + i - off);
+        }
+        qh[i] = y;
+        acc += pi * y;
+    }
+    double v[1] = {static_cast<double>(acc)};
+    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0)
+        mx_alpha(s, v[0]);
+}
+
+// K1 (csr): qh = ph + offdiag(S A S) ph, pq = ph.qh.  Thread per row.
+__global__ void __launch_bounds__(kBlock) k_mx_spmv_csr(int64_t n, const int32_t *__restrict__ orow,
+                                                        const int32_t *__restrict__ ocol,
+                                                        const float *__restrict__ oval, const float *__restrict__ ph,
+                                                        float *__restrict__ qh, double *partials, SolveScalars *s)
+{
+    if (ld_flag(&s->done))
+        return;
+    float acc = 0.0f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float pi = __ldg(ph + i);
+        float y = pi;
+        for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k)
+            y += __ldg(oval + k) * __ldg(ph + __ldg(ocol + k));
+        qh[i] = y;
+        acc += pi * y;
+    }
+    double v[1] = {static_cast<double>(acc)};
+    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0)
+        mx_alpha(s, v[0]);
+}
+
+// K2: xh += alpha ph, rh -= alpha qh, rr = rh.rh; decide on a reliable update.
+__global__ void __launch_bounds__(kBlock) k_mx_update(int64_t n, const float *__restrict__ ph,
+                                                      const float *__restrict__ qh, float *__restrict__ xh,
+                                                      float *__restrict__ rh, double *partials, SolveScalars *s)
+{
+    if (ld_flag(&s->done))
+        return;
+    const float alpha = static_cast<float>(__ldcg(&s->alpha));
+    float acc = 0.0f;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n4 = n >> 2;
+    for (int64_t i = tid; i < n4; i += stride) {
+        const float4 p = reinterpret_cast<const float4 *>(ph)[i];
+        const float4 q = reinterpret_cast<const float4 *>(qh)[i];
+        float4 x = reinterpret_cast<float4 *>(xh)[i];
+        float4 r = reinterpret_cast<float4 *>(rh)[i];
+        x.x += alpha * p.x;
+        x.y += alpha * p.y;
+        x.z += alpha * p.z;
+        x.w += alpha * p.w;
+        r.x -= alpha * q.x;
+        r.y -= alpha * q.y;
+        r.z -= alpha * q.z;
+        r.w -= alpha * q.w;
+        reinterpret_cast<float4 *>(xh)[i] = x;
+        reinterpret_cast<float4 *>(rh)[i] = r;
+        acc += r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w;
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
+        xh[i] += alpha * ph[i];
+        const float r = rh[i] - alpha * qh[i];
+        rh[i] = r;
+        acc += r * r;
+    }
+    double v[1] = {static_cast<double>(acc)};
+    if (grid_sum_last<1>(v, partials, &s->counter[2]) && threadIdx.x == 0) {
+        const double rr = v[0];
+        s->iter += 1;
+        const double sigma = sqrt(rr);
+        const double est = s->t0 * sigma / s->sigma0;
+        s->last = est;
+        if (s->need_update || sigma < s->delta * s->rmax || est < s->tol || s->iter >= s->max_iter) {
+            s->need_update = 1;  // beta is formed after the residual replacement
+        } else {
+            s->beta = rr / s->rz;
+            s->rz = rr;
+            if (sigma > s->rmax)
+                s->rmax = sigma;
+        }
+    }
+}
+
+// U1: x += S xh (FP64), xh = 0.
+__global__ void __launch_bounds__(kBlock) k_mx_fold(int64_t n, const double *__restrict__ sc, float *__restrict__ xh,
+                                                    double *__restrict__ x, const SolveScalars *s)
+{
+    if (!ld_flag(&s->need_update) || ld_flag(&s->done))
+        return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x[i] += sc[i] * static_cast<double>(xh[i]);
+        xh[i] = 0.0f;
+    }
+}
+
+// U2: r = b - A x in FP64 (staged CSR SpMV); stop test on the true residual.
+struct ResEpi {
+    const double *b;
+    double *r;
+    double acc;
+    __device__ __forceinline__ void operator()(int row, double y)
+    {
+        const double v = __ldg(b + row) - y;
+        r[row] = v;
+        acc += v * v;
+    }
+};
+
+__global__ void __launch_bounds__(kBlock) k_mx_true_residual(const int32_t *__restrict__ rowPtr,
+                                                             const int32_t *__restrict__ colIdx,
+                                                             const double *__restrict__ val,
+                                                             const int32_t *__restrict__ rb, int nRB,
+                                                             const double *__restrict__ x, const double *__restrict__ b,
+                                                             double *__restrict__ r, double *partials, SolveScalars *s)
+{
+    if (!ld_flag(&s->need_update) || ld_flag(&s->done))
+        return;
+    ResEpi epi{b, r, 0.0};
+    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
+    double v[1] = {epi.acc};
+    if (grid_sum_last<1>(v, partials, &s->counter[3]) && threadIdx.x == 0) {
+        s->rr = v[0];
+        const double t = sqrt(v[0]) / s->bnorm;
+        s->last = t;
+        s->t0 = t;
+        if (t < s->tol) {
+            s->done = 1;
+            s->result = s->iter;
+        } else if (s->iter >= s->max_iter || s->status == SIMALL_ERR_BREAKDOWN) {
+            s->done = 1;
+            s->result = s->iter >= s->max_iter ? s->max_iter : s->iter;
+        }
+    }
+}
+
+// U3: rh = S r (FP32), rho_new = rh.rh; beta = rho_new / rho; reset the trigger.
+__global__ void __launch_bounds__(kBlock) k_mx_replace(int64_t n, const double *__restrict__ sc,
+                                                       const double *__restrict__ r, float *__restrict__ rh,
+                                                       double *partials, SolveScalars *s)
+{
+    if (!ld_flag(&s->need_update) || ld_flag(&s->done))
+        return;
+    float acc = 0.0f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = static_cast<float>(sc[i] * r[i]);
+        rh[i] = v;
+        acc += v * v;
+    }
+    double a[1] = {static_cast<double>(acc)};
+    if (grid_sum_last<1>(a, partials, &s->counter[4]) && threadIdx.x == 0) {
+        const double rho = a[0];
+        s->beta = rho / s->rz;
+        s->rz = rho;
+        s->sigma0 = sqrt(rho);
+        s->rmax = s->sigma0;
+        s->need_update = 0;
+        s->updates += 1;
+    }
+}
+
+// K3: ph = rh + beta ph.
+__global__ void __launch_bounds__(kBlock) k_mx_pupdate(int64_t n, const float *__restrict__ rh, float *__restrict__ ph,
+                                                       const SolveScalars *s)
+{
+    if (ld_flag(&s->done))
+        return;
+    const float beta = static_cast<float>(__ldcg(&s->beta));
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n4 = n >> 2;
+    for (int64_t i = tid; i < n4; i += stride) {
+        const float4 r = reinterpret_cast<const float4 *>(rh)[i];
+        float4 p = reinterpret_cast<float4 *>(ph)[i];
+        p.x = r.x + beta * p.x;
+        p.y = r.y + beta * p.y;
+        p.z = r.z + beta * p.z;
+        p.w = r.w + beta * p.w;
+        reinterpret_cast<float4 *>(ph)[i] = p;
+    }
+    for (int64_t i = 4 * n4 + tid; i < n; i += stride)
+        ph[i] = rh[i] + beta * ph[i];
+}
+
+int grid_n(simall_context *ctx, int64_t n)
+{
+    const int64_t g = (n + kBlock - 1) / kBlock;
+    const int64_t cap = grid_size_streaming(ctx);
+    return static_cast<int>(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+// Host: choose the storage format from the pattern (dia only if allowed).
+void analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
+{
+    const int64_t n = s->n;
+    const int32_t *rp = s->h_rowPtr.data(), *ci = s->h_colIdx.data();
+    std::vector<int32_t> offs;
+    bool ok = allow_dia;
+    int64_t upper = 0;
+    for (int64_t i = 0; i < n && ok; ++i)
+        for (int k = rp[i]; k < rp[i + 1]; ++k) {
+            const int j = ci[k];
+            if (j <= i)
+                continue;
+            ++upper;
+            const int32_t off = j - static_cast<int32_t>(i);
+            if (std::find(offs.begin(), offs.end(), off) == offs.end()) {
+                if (static_cast<int>(offs.size()) == kMaxDiags) {
+                    ok = false;
+                    break;
+                }
+                offs.push_back(off);
+            }
+        }
+    // dia only pays when the diagonals are nearly full
+    if (ok && !offs.empty() && static_cast<double>(offs.size()) * n > 1.3 * static_cast<double>(upper))
+        ok = false;
+    m->dia = ok && !offs.empty();
+    if (m->dia) {
+        std::sort(offs.begin(), offs.end());
+        m->offs.nd = static_cast<int>(offs.size());
+        for (int d = 0; d < kMaxDiags; ++d)
+            m->offs.off[d] = d < m->offs.nd ? offs[d] : 0;
+    } else {
+        m->h_orow.assign(static_cast<size_t>(n) + 1, 0);
+        m->h_ocol.clear();
+        m->h_opos.clear();
+        for (int64_t i = 0; i < n; ++i) {
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                if (ci[k] != i) {
+                    m->h_ocol.push_back(ci[k]);
+                    m->h_opos.push_back(k);
+                }
+            m->h_orow[i + 1] = static_cast<int32_t>(m->h_ocol.size());
+        }
+        m->nnzOff = static_cast<int>(m->h_ocol.size());
+    }
+    m->patternReady = true;
+}
+
+}  // namespace
+
+int mixed_setup(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    if (!s->mixed) {
+        s->mixed = new (std::nothrow) MixedData;
+        if (!s->mixed)
+            return SIMALL_ERR_OUT_OF_MEMORY;
+    }
+    MixedData *m = s->mixed;
+    const int64_t n = s->n;
+    if (!m->patternReady)
+        analyse_pattern(s, m, true);
+    SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
+    SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, m->rh.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, m->ph.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, m->qh.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
+    const int g = grid_n(ctx, n);
+    k_mx_scale<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, s->flag.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (m->dia) {
+        k_mx_symcheck<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, s->flag.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    int h = 0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, s->flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h & 1)
+        return fail(ctx, SIMALL_ERR_NOT_POSITIVE, "mixed precision needs a positive diagonal");
+    if (m->dia && (h & 2))
+        analyse_pattern(s, m, false);  // not numerically symmetric: keep every off-diagonal entry
+    if (m->dia) {
+        SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * n));
+        k_mx_build_dia<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->offs, m->U.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    } else {
+        const int no = m->nnzOff;
+        SIMALL_CUDA_TRY(ctx, m->orow.alloc(n + 1));
+        SIMALL_CUDA_TRY(ctx, m->ocol.alloc(no > 0 ? no : 1));
+        SIMALL_CUDA_TRY(ctx, m->opos.alloc(no > 0 ? no : 1));
+        SIMALL_CUDA_TRY(ctx, m->oval.alloc(no > 0 ? no : 1));
+        std::vector<int32_t> rowOf(static_cast<size_t>(no));
+        for (int64_t i = 0; i < n; ++i)
+            for (int k = m->h_orow[i]; k < m->h_orow[i + 1]; ++k)
+                rowOf[k] = static_cast<int32_t>(i);
+        DevBuf<int32_t> dRowOf;
+        SIMALL_CUDA_TRY(ctx, dRowOf.alloc(no > 0 ? no : 1));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->orow.p, m->h_orow.data(), (n + 1) * sizeof(int32_t),
+                                             cudaMemcpyHostToDevice, ctx->stream));
+        if (no > 0) {
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->ocol.p, m->h_ocol.data(), no * sizeof(int32_t),
+                                                 cudaMemcpyHostToDevice, ctx->stream));
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->opos.p, m->h_opos.data(), no * sizeof(int32_t),
+                                                 cudaMemcpyHostToDevice, ctx->stream));
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(dRowOf.p, rowOf.data(), no * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                                 ctx->stream));
+            k_mx_build_csr<<<grid_n(ctx, no), kBlock, 0, ctx->stream>>>(no, dRowOf.p, m->ocol.p, m->opos.p, s->values,
+                                                                        m->scale.p, m->oval.p);
+            SIMALL_LAUNCH_CHECK(ctx);
+        }
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // dRowOf and rowOf die here
+    }
+    return SIMALL_OK;
+}
+
+namespace {
+
+int enqueue_mixed_iteration(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    MixedData *m = s->mixed;
+    const int64_t n = s->n;
+    const int g = grid_n(ctx, n);
+    if (m->dia)
+        k_mx_spmv_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->offs, m->U.p, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
+    else
+        k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
+                                                     s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    const int cap = grid_size_streaming(ctx);
+    const int gs = s->nRowBlocks < cap ? s->nRowBlocks : cap;
+    k_mx_true_residual<<<gs < 1 ? 1 : gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p,
+                                                                    s->nRowBlocks, s->x.p, s->b.p, s->r.p,
+                                                                    s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rh.p, s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_mx_pupdate<<<g, kBlock, 0, ctx->stream>>>(n, m->rh.p, m->ph.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+constexpr int kMixedKernelsPerIteration = 6;
+
+int run_mixed_chunk(simall_solver *s, int len)
+{
+    simall_context *ctx = s->ctx;
+    for (auto &gc : s->graphs)
+        if (gc.len == len) {
+            SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(gc.exec, ctx->stream));
+            ctx->launches.fetch_add(static_cast<int64_t>(len) * kMixedKernelsPerIteration, std::memory_order_relaxed);
+            return SIMALL_OK;
+        }
+    cudaGraph_t graph = nullptr;
+    SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int st = SIMALL_OK;
+    for (int i = 0; i < len && st == SIMALL_OK; ++i)
+        st = enqueue_mixed_iteration(s);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (st)
+        return st;
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    GraphChunk gc;
+    gc.len = len;
+    e = cudaGraphInstantiate(&gc.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    s->graphs.push_back(gc);
+    SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(gc.exec, ctx->stream));
+    return SIMALL_OK;
+}
+
+}  // namespace
+
+int mixed_solve(simall_solver *s, simall_solver_stats *st)
+{
+    (void)st;
+    simall_context *ctx = s->ctx;
+    MixedData *m = s->mixed;
+    const int64_t n = s->n;
+    double tol = s->cfg.tolerance, delta = s->cfg.reliable_delta;
+    int maxit = s->cfg.max_iterations;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->tol, &tol, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx,
+                    cudaMemcpyAsync(&s->scal.p->delta, &delta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx,
+                    cudaMemcpyAsync(&s->scal.p->max_iter, &maxit, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rh.p, m->ph.p, m->xh.p,
+                                                          s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    int done_iters = 0;
+    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 16;
+    double prev_last = -1.0;
+    int prev_iter = 0;
+    for (;;) {
+        int e = run_mixed_chunk(s, chunk);
+        if (e)
+            return e;
+        done_iters += chunk;
+        e = solver_fetch_scalars(s);
+        if (e)
+            return e;
+        if (s->h_scal->done)
+            break;
+        if (done_iters > 2 * maxit + 64)
+            return fail(ctx, SIMALL_ERR_CUDA, "mixed solver did not raise its stop flag");
+        if (s->cfg.check_interval <= 0) {
+            const double last = s->h_scal->last;
+            const int it = s->h_scal->iter;
+            int next = 64;
+            if (prev_last > 0.0 && last > 0.0 && last < prev_last && it > prev_iter) {
+                const double rate = std::log(last / prev_last) / (it - prev_iter);
+                const double need = std::log(tol / last) / rate;
+                next = need < 4 ? 4 : (need > 64 ? 64 : static_cast<int>(need) + 1);
+            }
+            prev_last = last;
+            prev_iter = it;
+            chunk = next;
+            // snap to a few captured lengths to bound the number of graphs
+            chunk = chunk <= 4 ? 4 : chunk <= 8 ? 8 : chunk <= 16 ? 16 : chunk <= 32 ? 32 : 64;
+        }
+    }
+    return SIMALL_OK;
+}
+
+int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
+{
+    simall_context *ctx = s->ctx;
+    MixedData *m = s->mixed;
+    const int64_t n = s->n;
+    const int g = grid_n(ctx, n);
+    const double nd = static_cast<double>(n);
+    switch (k) {
+    case 4:
+        if (m->dia) {
+            k_mx_spmv_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->offs, m->U.p, m->ph.p, m->qh.p, s->partials.p,
+                                                         s->scal.p);
+            *bytes = (4.0 * m->offs.nd + 8.0) * nd;  // U once, ph gathered once, qh written
+        } else {
+            k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
+                                                         s->partials.p, s->scal.p);
+            *bytes = 8.0 * m->nnzOff + 12.0 * nd + 4.0;
+        }
+        break;
+    case 5:
+        k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+        *bytes = 24.0 * nd;  // ph, qh, xh, rh read; xh, rh written
+        break;
+    case 6:
+        k_mx_pupdate<<<g, kBlock, 0, ctx->stream>>>(n, m->rh.p, m->ph.p, s->scal.p);
+        *bytes = 12.0 * nd;  // rh, ph read; ph written
+        break;
+    default:
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);
+    }
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+void mixed_invalidate_pattern(simall_solver *s)
+{
+    if (s->mixed)
+        s->mixed->patternReady = false;
+}
+
+void mixed_free(simall_solver *s)
+{
+    delete s->mixed;
+    s->mixed = nullptr;
+}
+
+}  // namespace simall

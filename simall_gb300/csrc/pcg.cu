@@ -1,0 +1,914 @@
+// FP64 preconditioned CG on a device CSR matrix: the GB300 replacement of
+// CGSolver::solve (src/solver/LinearSolvers.cpp:415-459) and gpu::CgGpu
+// (src/gpu/CgGpu.cpp:35-238).
+//
+// One iteration is three kernels with all scalars kept on the device:
+//   K1  Ap = A p (staged row-block SpMV) and p.Ap; the last CTA forms alpha.
+//   K2  x += alpha p, r -= alpha Ap, z = M r, ||r||^2 and r.z; the last CTA
+//       applies the reference stop test and forms beta.
+//   K3  p = z + beta p.
+// (ILU0 splits K2 around the level-scheduled triangular solves.)  Every
+// kernel returns at once when the device stop flag is set, so the host
+// enqueues iterations in chunks (captured as CUDA graphs) and polls the flag
+// between chunks instead of after each reduction.
+#include "device.cuh"
+#include "solver.hpp"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <new>
+
+namespace simall {
+
+namespace {
+
+__device__ __forceinline__ int ld_done(const SolveScalars *s) { return __ldcg(&s->done); }
+
+__global__ void __launch_bounds__(kBlock) k_jacobi_setup(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                         const int32_t *__restrict__ colIdx,
+                                                         const double *__restrict__ val, double *__restrict__ invD)
+{
+    // JacobiPreconditioner::setup (LinearSolvers.cpp:54-65)
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double d = 1.0;
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                const double a = val[k];
+                d = (a != 0.0) ? 1.0 / a : 1.0;
+                break;
+            }
+        invD[i] = d;
+    }
+}
+
+__global__ void __launch_bounds__(kBlock) k_check_finite(int64_t n, const double *__restrict__ v, int *flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        if (!isfinite(v[i]))
+            atomicOr(flag, 1);
+}
+
+// x = 0, r = b, z = invD r, p = z; rz = r.z, bnorm = max(||b||, 1e-30).
+__global__ void __launch_bounds__(kBlock) k_init_jacobi(int64_t n, const double *__restrict__ b,
+                                                        const double *__restrict__ invD, double *__restrict__ x,
+                                                        double *__restrict__ r, double *__restrict__ p,
+                                                        double *partials, SolveScalars *s)
+{
+    double acc[2] = {0.0, 0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n2 = n >> 1;
+    for (int64_t i = tid; i < n2; i += stride) {
+        const double2 bb = reinterpret_cast<const double2 *>(b)[i];
+        const double2 id = reinterpret_cast<const double2 *>(invD)[i];
+        const double2 z = make_double2(id.x * bb.x, id.y * bb.y);
+        reinterpret_cast<double2 *>(x)[i] = make_double2(0.0, 0.0);
+        reinterpret_cast<double2 *>(r)[i] = bb;
+        reinterpret_cast<double2 *>(p)[i] = z;
+        acc[0] += bb.x * z.x + bb.y * z.y;
+        acc[1] += bb.x * bb.x + bb.y * bb.y;
+    }
+    if ((n & 1) && tid == 0) {
+        const int64_t i = n - 1;
+        const double bi = b[i], zi = invD[i] * bi;
+        x[i] = 0.0;
+        r[i] = bi;
+        p[i] = zi;
+        acc[0] += bi * zi;
+        acc[1] += bi * bi;
+    }
+    if (grid_sum_last<2>(acc, partials, &s->counter[0]) && threadIdx.x == 0) {
+        s->rz = acc[0];
+        s->bnorm = std_max(sqrt(acc[1]), 1e-30);
+        s->iter = 0;
+        s->status = SIMALL_OK;
+        if (s->max_iter <= 0) {
+            s->done = 1;
+            s->result = s->max_iter;
+        } else {
+            s->done = 0;
+            s->result = 0;
+        }
+    }
+}
+
+struct PapEpi {
+    double *Ap;
+    const double *p;
+    double acc;
+    __device__ __forceinline__ void operator()(int row, double y)
+    {
+        Ap[row] = y;
+        acc += __ldg(p + row) * y;
+    }
+};
+
+// K1: Ap = A p, pAp = p.Ap, alpha = rz / pAp (CGSolver::solve :431-438).
+__global__ void __launch_bounds__(kBlock) k_spmv_pap(const int32_t *__restrict__ rowPtr,
+                                                     const int32_t *__restrict__ colIdx,
+                                                     const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                     int nRB, const double *__restrict__ p, double *__restrict__ Ap,
+                                                     double *partials, SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    PapEpi epi{Ap, p, 0.0};
+    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, p, epi);
+    double v[1] = {epi.acc};
+    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0) {
+        const double pAp = v[0];
+        s->pAp = pAp;
+        if (pAp == 0.0) {
+            s->last = sqrt(s->rz) / s->bnorm;
+            s->result = s->iter;
+            s->done = 1;
+            s->status = SIMALL_ERR_BREAKDOWN;
+        } else {
+            s->alpha = s->rz / pAp;
+        }
+    }
+}
+
+struct StoreEpi {
+    double *y;
+    __device__ __forceinline__ void operator()(int row, double v) { y[row] = v; }
+};
+
+// y = A x alone (the SpMV whose HBM bandwidth is reported).
+__global__ void __launch_bounds__(kBlock) k_spmv_plain(const int32_t *__restrict__ rowPtr,
+                                                       const int32_t *__restrict__ colIdx,
+                                                       const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                       int nRB, const double *__restrict__ x, double *__restrict__ y)
+{
+    StoreEpi epi{y};
+    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
+}
+
+// Stop test and beta (CGSolver::solve :439-449).  Thread 0 of the last CTA.
+__device__ __forceinline__ void finish_iteration(SolveScalars *s, double rr, double rzNew, bool have_rz)
+{
+    s->rr = rr;
+    const double last = sqrt(rr) / s->bnorm;
+    s->last = last;
+    if (last < s->tol) {
+        s->result = s->iter + 1;
+        s->done = 1;
+        return;
+    }
+    if (have_rz) {
+        s->beta = rzNew / s->rz;
+        s->rz = rzNew;
+        s->iter += 1;
+        if (s->iter >= s->max_iter) {
+            s->result = s->max_iter;
+            s->done = 1;
+        }
+    }
+}
+
+// K2 (Jacobi): x += alpha p, r -= alpha Ap, z = invD r (not stored), ||r||^2, r.z.
+__global__ void __launch_bounds__(kBlock) k_update_jacobi(int64_t n, const double *__restrict__ p,
+                                                          const double *__restrict__ Ap,
+                                                          const double *__restrict__ invD, double *__restrict__ x,
+                                                          double *__restrict__ r, double *partials, SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    const double alpha = __ldcg(&s->alpha);
+    double acc[2] = {0.0, 0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n2 = n >> 1;
+    for (int64_t i = tid; i < n2; i += stride) {
+        const double2 pp = reinterpret_cast<const double2 *>(p)[i];
+        const double2 qq = reinterpret_cast<const double2 *>(Ap)[i];
+        const double2 id = reinterpret_cast<const double2 *>(invD)[i];
+        double2 xx = reinterpret_cast<double2 *>(x)[i];
+        double2 rv = reinterpret_cast<double2 *>(r)[i];
+        xx.x += alpha * pp.x;
+        xx.y += alpha * pp.y;
+        rv.x += -alpha * qq.x;
+        rv.y += -alpha * qq.y;
+        reinterpret_cast<double2 *>(x)[i] = xx;
+        reinterpret_cast<double2 *>(r)[i] = rv;
+        acc[0] += rv.x * rv.x + rv.y * rv.y;
+        acc[1] += rv.x * (id.x * rv.x) + rv.y * (id.y * rv.y);
+    }
+    if ((n & 1) && tid == 0) {
+        const int64_t i = n - 1;
+        x[i] += alpha * p[i];
+        const double ri = r[i] + -alpha * Ap[i];
+        r[i] = ri;
+        acc[0] += ri * ri;
+        acc[1] += ri * (invD[i] * ri);
+    }
+    if (grid_sum_last<2>(acc, partials, &s->counter[2]) && threadIdx.x == 0)
+        finish_iteration(s, acc[0], acc[1], true);
+}
+
+// K3 (Jacobi): p = invD r + beta p.
+__global__ void __launch_bounds__(kBlock) k_pupdate_jacobi(int64_t n, const double *__restrict__ r,
+                                                           const double *__restrict__ invD, double *__restrict__ p,
+                                                           const SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    const double beta = __ldcg(&s->beta);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    const int64_t n2 = n >> 1;
+    for (int64_t i = tid; i < n2; i += stride) {
+        const double2 rv = reinterpret_cast<const double2 *>(r)[i];
+        const double2 id = reinterpret_cast<const double2 *>(invD)[i];
+        double2 pp = reinterpret_cast<double2 *>(p)[i];
+        pp.x = id.x * rv.x + beta * pp.x;
+        pp.y = id.y * rv.y + beta * pp.y;
+        reinterpret_cast<double2 *>(p)[i] = pp;
+    }
+    if ((n & 1) && tid == 0) {
+        const int64_t i = n - 1;
+        p[i] = invD[i] * r[i] + beta * p[i];
+    }
+}
+
+// ---------------------------------------------------------------- ILU0 variant kernels
+// x = 0, r = b, ||b||^2 -> bnorm (z comes from the triangular solves).
+__global__ void __launch_bounds__(kBlock) k_init_plain(int64_t n, const double *__restrict__ b, double *__restrict__ x,
+                                                       double *__restrict__ r, double *partials, SolveScalars *s)
+{
+    double acc[1] = {0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride) {
+        const double bi = b[i];
+        x[i] = 0.0;
+        r[i] = bi;
+        acc[0] += bi * bi;
+    }
+    if (grid_sum_last<1>(acc, partials, &s->counter[0]) && threadIdx.x == 0) {
+        s->bnorm = std_max(sqrt(acc[0]), 1e-30);
+        s->iter = 0;
+        s->status = SIMALL_OK;
+        if (s->max_iter <= 0) {
+            s->done = 1;
+            s->result = s->max_iter;
+        } else {
+            s->done = 0;
+            s->result = 0;
+        }
+    }
+}
+
+// p = z, rz = r.z
+__global__ void __launch_bounds__(kBlock) k_init_p_rz(int64_t n, const double *__restrict__ r,
+                                                      const double *__restrict__ z, double *__restrict__ p,
+                                                      double *partials, SolveScalars *s)
+{
+    double acc[1] = {0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride) {
+        const double zi = z[i];
+        p[i] = zi;
+        acc[0] += r[i] * zi;
+    }
+    if (grid_sum_last<1>(acc, partials, &s->counter[3]) && threadIdx.x == 0)
+        s->rz = acc[0];
+}
+
+// K2a: x += alpha p, r -= alpha Ap, ||r||^2; stop test.
+__global__ void __launch_bounds__(kBlock) k_update_xr(int64_t n, const double *__restrict__ p,
+                                                      const double *__restrict__ Ap, double *__restrict__ x,
+                                                      double *__restrict__ r, double *partials, SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    const double alpha = __ldcg(&s->alpha);
+    double acc[1] = {0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride) {
+        x[i] += alpha * p[i];
+        const double ri = r[i] + -alpha * Ap[i];
+        r[i] = ri;
+        acc[0] += ri * ri;
+    }
+    if (grid_sum_last<1>(acc, partials, &s->counter[2]) && threadIdx.x == 0)
+        finish_iteration(s, acc[0], 0.0, false);
+}
+
+// K2b: rzNew = r.z; beta; iteration count.
+__global__ void __launch_bounds__(kBlock) k_rz_beta(int64_t n, const double *__restrict__ r,
+                                                    const double *__restrict__ z, double *partials, SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    double acc[1] = {0.0};
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride)
+        acc[0] += r[i] * z[i];
+    if (grid_sum_last<1>(acc, partials, &s->counter[3]) && threadIdx.x == 0) {
+        const double rzNew = acc[0];
+        s->beta = rzNew / s->rz;
+        s->rz = rzNew;
+        s->iter += 1;
+        if (s->iter >= s->max_iter) {
+            s->result = s->max_iter;
+            s->done = 1;
+        }
+    }
+}
+
+// K3: p = z + beta p.
+__global__ void __launch_bounds__(kBlock) k_pupdate_z(int64_t n, const double *__restrict__ z, double *__restrict__ p,
+                                                      const SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    const double beta = __ldcg(&s->beta);
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i < n; i += stride)
+        p[i] = z[i] + beta * p[i];
+}
+
+// r = b - A x and ||r||^2 (FP64 true residual).
+struct ResidualEpi {
+    const double *b;
+    double *r;
+    double acc;
+    __device__ __forceinline__ void operator()(int row, double y)
+    {
+        const double v = __ldg(b + row) - y;
+        r[row] = v;
+        acc += v * v;
+    }
+};
+
+__global__ void __launch_bounds__(kBlock) k_residual(const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
+                                                     const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                     int nRB, const double *__restrict__ x, const double *__restrict__ b,
+                                                     double *__restrict__ r, double *partials, unsigned *ticket,
+                                                     double *out)
+{
+    ResidualEpi epi{b, r, 0.0};
+    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
+    double v[1] = {epi.acc};
+    if (grid_sum_last<1>(v, partials, ticket) && threadIdx.x == 0)
+        *out = v[0];
+}
+
+int grid_for(simall_context *ctx, int64_t n)
+{
+    const int64_t g = (n + kBlock - 1) / kBlock;
+    const int64_t cap = grid_size_streaming(ctx);
+    return static_cast<int>(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
+int spmv_grid(simall_context *ctx, int nRB)
+{
+    const int cap = grid_size_streaming(ctx);
+    return nRB < 1 ? 1 : (nRB < cap ? nRB : cap);
+}
+
+int check_device_values(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
+    k_check_finite<<<grid_for(ctx, s->nnz), kBlock, 0, ctx->stream>>>(s->nnz, s->values, s->flag.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    int h = 0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, s->flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h)
+        return fail(ctx, SIMALL_ERR_NON_FINITE, "matrix values contain NaN or Inf");
+    return SIMALL_OK;
+}
+
+// Preconditioner / format setup for the current values.
+int setup_values(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    if (s->cfg.precision == SIMALL_PRECISION_MIXED)
+        return mixed_setup(s);
+    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0)
+        return ilu_setup(s);
+    SIMALL_CUDA_TRY(ctx, s->invDiag.alloc(static_cast<size_t>(s->n)));
+    k_jacobi_setup<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->rowPtr, s->colIdx, s->values,
+                                                                     s->invDiag.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+int alloc_vectors(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    const size_t n = static_cast<size_t>(s->n) + 2;  // +2 keeps double2 tails in bounds
+    SIMALL_CUDA_TRY(ctx, s->x.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->r.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->p.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->Ap.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->b.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->z.alloc(n));
+    SIMALL_CUDA_TRY(ctx, s->partials.alloc(static_cast<size_t>(kMaxReduce) * grid_size_streaming(ctx)));
+    if (!s->scal.p) {
+        SIMALL_CUDA_TRY(ctx, s->scal.alloc(1));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->scal.p, 0, sizeof(SolveScalars), ctx->stream));
+    }
+    if (!s->h_scal)
+        SIMALL_CUDA_TRY(ctx, cudaMallocHost(reinterpret_cast<void **>(&s->h_scal), sizeof(SolveScalars)));
+    return SIMALL_OK;
+}
+
+void drop_graphs(simall_solver *s)
+{
+    for (auto &g : s->graphs)
+        if (g.exec)
+            cudaGraphExecDestroy(g.exec);
+    s->graphs.clear();
+}
+
+// Enqueue one FP64 iteration (Jacobi or ILU0).
+int enqueue_iteration(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    const int g = grid_for(ctx, s->n), gs = spmv_grid(ctx, s->nRowBlocks);
+    k_spmv_pap<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
+                                                 s->p.p, s->Ap.p, s->partials.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+        k_update_xr<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int st = ilu_apply(s, s->r.p, s->z.p);
+        if (st)
+            return st;
+        k_rz_beta<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->z.p, s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        k_pupdate_z<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    } else {
+        k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p,
+                                                       s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        k_pupdate_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->invDiag.p, s->p.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    return SIMALL_OK;
+}
+
+// A chunk of `len` iterations, captured once into a graph and replayed.
+int run_chunk(simall_solver *s, int len)
+{
+    simall_context *ctx = s->ctx;
+    for (auto &g : s->graphs)
+        if (g.len == len) {
+            SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(g.exec, ctx->stream));
+            ctx->launches.fetch_add(static_cast<int64_t>(len) *
+                                        (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 ? 0 : 3),
+                                    std::memory_order_relaxed);
+            return SIMALL_OK;
+        }
+    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+        // ILU0 chunks launch one kernel per level; enqueue them directly.
+        for (int i = 0; i < len; ++i) {
+            int st = enqueue_iteration(s);
+            if (st)
+                return st;
+        }
+        return SIMALL_OK;
+    }
+    cudaGraph_t graph = nullptr;
+    SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
+    int st = SIMALL_OK;
+    for (int i = 0; i < len && st == SIMALL_OK; ++i)
+        st = enqueue_iteration(s);
+    cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
+    if (st)
+        return st;
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaStreamEndCapture", __FILE__, __LINE__);
+    GraphChunk gc;
+    gc.len = len;
+    e = cudaGraphInstantiate(&gc.exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaGraphInstantiate", __FILE__, __LINE__);
+    s->graphs.push_back(gc);
+    SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(gc.exec, ctx->stream));
+    return SIMALL_OK;
+}
+
+int fp64_solve(simall_solver *s, simall_solver_stats *st)
+{
+    simall_context *ctx = s->ctx;
+    const int g = grid_for(ctx, s->n);
+    SolveScalars init{};
+    init.tol = s->cfg.tolerance;
+    init.max_iter = s->cfg.max_iterations;
+    // only the control fields are set from the host; counters stay zero
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->tol, &init.tol, sizeof(double), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->max_iter, &init.max_iter, sizeof(int), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+        k_init_plain<<<g, kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int e = ilu_apply(s, s->r.p, s->z.p);
+        if (e)
+            return e;
+        k_init_p_rz<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->z.p, s->p.p, s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    } else {
+        k_init_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->invDiag.p, s->x.p, s->r.p, s->p.p,
+                                                     s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    int done_iters = 0;
+    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 16;
+    double prev_last = -1.0;
+    int prev_iter = 0;
+    for (;;) {
+        const int remaining = s->cfg.max_iterations - done_iters;
+        int len = chunk < remaining ? chunk : remaining;
+        if (len < 1)
+            len = 1;
+        int e = run_chunk(s, len);
+        if (e)
+            return e;
+        done_iters += len;
+        e = solver_fetch_scalars(s);
+        if (e)
+            return e;
+        if (s->h_scal->done)
+            break;
+        if (done_iters >= s->cfg.max_iterations + 1)
+            return fail(ctx, SIMALL_ERR_CUDA, "solver did not raise its stop flag");
+        if (s->cfg.check_interval <= 0) {
+            // predict the remaining iterations from the observed decay rate
+            const double last = s->h_scal->last;
+            const int it = s->h_scal->iter;
+            int next = 64;
+            if (prev_last > 0.0 && last > 0.0 && last < prev_last && it > prev_iter) {
+                const double rate = std::log(last / prev_last) / (it - prev_iter);
+                const double need = std::log(s->cfg.tolerance / last) / rate;
+                next = need < 4 ? 4 : (need > 64 ? 64 : static_cast<int>(need) + 1);
+            }
+            prev_last = last;
+            prev_iter = it;
+            chunk = next;
+        }
+    }
+    (void)st;
+    return SIMALL_OK;
+}
+
+}  // namespace
+
+int solver_fetch_scalars(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_scal, s->scal.p, sizeof(SolveScalars), cudaMemcpyDeviceToHost,
+                                         ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return SIMALL_OK;
+}
+
+int solver_true_residual(simall_solver *s, const double *x, const double *b, double *r, double *rr)
+{
+    simall_context *ctx = s->ctx;
+    k_residual<<<spmv_grid(ctx, s->nRowBlocks), kBlock, 0, ctx->stream>>>(
+        s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, x, b, r, s->partials.p,
+        &s->scal.p->counter[4], reinterpret_cast<double *>(&s->scal.p->rr));
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (rr) {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(rr, &s->scal.p->rr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return SIMALL_OK;
+}
+
+}  // namespace simall
+
+using namespace simall;
+
+extern "C" {
+
+void simall_solver_config_default(simall_solver_config *cfg)
+{
+    if (!cfg)
+        return;
+    cfg->preconditioner = SIMALL_PRECOND_JACOBI;
+    cfg->tolerance = 1.0e-8;
+    cfg->max_iterations = 1000;
+    cfg->precision = SIMALL_PRECISION_FP64;
+    cfg->reliable_delta = 0.1;
+    cfg->check_interval = 0;
+}
+
+int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, simall_solver **out)
+{
+    if (!ctx || !out)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    simall_solver_config c;
+    simall_solver_config_default(&c);
+    if (cfg)
+        c = *cfg;
+    if (c.preconditioner == SIMALL_PRECOND_NONE)
+        c.preconditioner = SIMALL_PRECOND_JACOBI;
+    if (c.preconditioner != SIMALL_PRECOND_JACOBI && c.preconditioner != SIMALL_PRECOND_ILU0)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "preconditioner %d is not on the pressure path", c.preconditioner);
+    if (c.precision != SIMALL_PRECISION_FP64 && c.precision != SIMALL_PRECISION_MIXED)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "precision %d", c.precision);
+    if (c.precision == SIMALL_PRECISION_MIXED && c.preconditioner != SIMALL_PRECOND_JACOBI)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "mixed precision runs with the Jacobi preconditioner");
+    if (!(c.tolerance >= 0.0) || c.reliable_delta <= 0.0 || c.reliable_delta >= 1.0)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "tolerance / reliable_delta out of range");
+    auto *s = new (std::nothrow) simall_solver;
+    if (!s)
+        return SIMALL_ERR_OUT_OF_MEMORY;
+    s->ctx = ctx;
+    s->cfg = c;
+    *out = s;
+    return SIMALL_OK;
+}
+
+int simall_solver_destroy(simall_solver *s)
+{
+    if (!s)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    cudaStreamSynchronize(s->ctx->stream);
+    drop_graphs(s);
+    ilu_free(s);
+    mixed_free(s);
+    if (s->h_scal)
+        cudaFreeHost(s->h_scal);
+    delete s;
+    return SIMALL_OK;
+}
+
+int simall_solver_set_matrix(simall_solver *s, int64_t n, int64_t nnz, const int32_t *rowPtr, const int32_t *colIdx,
+                             const double *values, int mem)
+{
+    if (!s)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = s->ctx;
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    s->ready = false;
+    if (n <= 0 || nnz <= 0 || !rowPtr || !colIdx || !values)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "set_matrix: empty matrix or null array");
+    if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "set_matrix: bad memory kind %d", mem);
+    const bool same_pattern_size = (n == s->n && nnz == s->nnz);
+    s->h_rowPtr.resize(static_cast<size_t>(n) + 1);
+    s->h_colIdx.resize(static_cast<size_t>(nnz));
+    if (mem == SIMALL_MEM_HOST) {
+        int st = check_csr_host(ctx, n, nnz, rowPtr, colIdx, values, true);
+        if (st)
+            return st;
+        std::memcpy(s->h_rowPtr.data(), rowPtr, (n + 1) * sizeof(int32_t));
+        std::memcpy(s->h_colIdx.data(), colIdx, nnz * sizeof(int32_t));
+        SIMALL_CUDA_TRY(ctx, s->own_rowPtr.alloc(n + 1));
+        SIMALL_CUDA_TRY(ctx, s->own_colIdx.alloc(nnz));
+        SIMALL_CUDA_TRY(ctx, s->own_values.alloc(nnz));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_rowPtr.p, rowPtr, (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_colIdx.p, colIdx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_values.p, values, nnz * sizeof(double), cudaMemcpyHostToDevice,
+                                             ctx->stream));
+        s->rowPtr = s->own_rowPtr.p;
+        s->colIdx = s->own_colIdx.p;
+        s->values = s->own_values.p;
+    } else {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_rowPtr.data(), rowPtr, (n + 1) * sizeof(int32_t),
+                                             cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_colIdx.data(), colIdx, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        s->rowPtr = rowPtr;
+        s->colIdx = colIdx;
+        s->values = values;
+        // pattern checks on the host copy; values are checked on the device
+        int st = check_csr_host(ctx, n, nnz, s->h_rowPtr.data(), s->h_colIdx.data(), nullptr, true);
+        if (st)
+            return st;
+    }
+    s->n = n;
+    s->nnz = nnz;
+    s->solved = false;
+    if (mem == SIMALL_MEM_DEVICE) {
+        int st = check_device_values(s);
+        if (st)
+            return st;
+    }
+    // captured graphs embed the matrix pointers and sizes; the ILU level
+    // schedule depends on the pattern
+    (void)same_pattern_size;
+    drop_graphs(s);
+    if (s->ilu)
+        s->ilu->analysed = false;
+    mixed_invalidate_pattern(s);
+    std::vector<int32_t> rb = make_row_blocks(n, s->h_rowPtr.data());
+    s->nRowBlocks = static_cast<int>(rb.size()) - 1;
+    SIMALL_CUDA_TRY(ctx, s->rowBlocks.alloc(rb.size()));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->rowBlocks.p, rb.data(), rb.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    int st = alloc_vectors(s);
+    if (st)
+        return st;
+    st = setup_values(s);
+    if (st)
+        return st;
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    s->ready = true;
+    return SIMALL_OK;
+}
+
+int simall_solver_update_values(simall_solver *s, const double *values, int mem)
+{
+    if (!s || !values)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = s->ctx;
+    if (!s->ready)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "update_values before set_matrix");
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    if (mem == SIMALL_MEM_HOST) {
+        for (int64_t k = 0; k < s->nnz; ++k)
+            if (!std::isfinite(values[k]))
+                return fail(ctx, SIMALL_ERR_NON_FINITE, "matrix values contain NaN or Inf");
+        if (s->values != s->own_values.p) {
+            SIMALL_CUDA_TRY(ctx, s->own_values.alloc(s->nnz));
+            s->values = s->own_values.p;
+            drop_graphs(s);
+        }
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_values.p, values, s->nnz * sizeof(double), cudaMemcpyHostToDevice,
+                                             ctx->stream));
+    } else {
+        if (values != s->values)
+            drop_graphs(s);
+        s->values = values;
+        int st = check_device_values(s);
+        if (st)
+            return st;
+    }
+    int st = setup_values(s);
+    if (st)
+        return st;
+    return SIMALL_OK;
+}
+
+int simall_solver_solve(simall_solver *s, const double *b, double *x, int mem, simall_solver_stats *stats)
+{
+    return simall::solver_solve_impl(s, b, mem, x, mem, stats);
+}
+
+}  // extern "C"
+
+int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, double *x, int xmem,
+                              simall_solver_stats *stats)
+{
+    if (!s || !b || !x)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = s->ctx;
+    if (!s->ready)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "solve before set_matrix");
+    if ((bmem != SIMALL_MEM_HOST && bmem != SIMALL_MEM_DEVICE) || (xmem != SIMALL_MEM_HOST && xmem != SIMALL_MEM_DEVICE))
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "solve: bad memory kind");
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const auto t0 = std::chrono::steady_clock::now();
+    const size_t bytes = static_cast<size_t>(s->n) * sizeof(double);
+    if (bmem == SIMALL_MEM_HOST) {
+        for (int64_t i = 0; i < s->n; ++i)
+            if (!std::isfinite(b[i]))
+                return fail(ctx, SIMALL_ERR_NON_FINITE, "b contains NaN or Inf");
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, b, bytes, cudaMemcpyHostToDevice, ctx->stream));
+    } else {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
+    simall_solver_stats local{};
+    int st;
+    if (s->cfg.precision == SIMALL_PRECISION_MIXED)
+        st = mixed_solve(s, &local);
+    else
+        st = fp64_solve(s, &local);
+    if (st)
+        return st;
+    // FP64 true residual of the returned x (r buffer is free after the loop)
+    double rr = 0.0;
+    if (s->cfg.precision != SIMALL_PRECISION_MIXED) {
+        st = solver_true_residual(s, s->x.p, s->b.p, s->r.p, &rr);
+        if (st)
+            return st;
+    } else {
+        rr = s->h_scal->rr;
+    }
+    if (xmem == SIMALL_MEM_HOST)
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(x, s->x.p, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+    else
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(x, s->x.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    const SolveScalars &h = *s->h_scal;
+    s->last_residual = h.last;
+    s->solved = true;
+    if (stats) {
+        stats->iterations = h.result;
+        stats->final_residual = h.last;
+        stats->converged = (h.last < s->cfg.tolerance) ? 1 : 0;
+        stats->status = h.status;
+        stats->reliable_updates = h.updates;
+        stats->b_norm = h.bnorm;
+        stats->true_residual = std::sqrt(rr) / h.bnorm;
+        stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return SIMALL_OK;
+}
+
+extern "C" {
+
+double simall_solver_last_residual(const simall_solver *s) { return s ? s->last_residual : 0.0; }
+
+int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms, double *bytes)
+{
+    if (!s || !ms || reps <= 0)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = s->ctx;
+    if (!s->ready || !s->solved)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "time_kernel needs a matrix and one completed solve");
+    const bool mixed = s->cfg.precision == SIMALL_PRECISION_MIXED;
+    if ((kernel >= 4 && !mixed) || (kernel >= 1 && kernel <= 3 && (mixed || s->cfg.preconditioner != SIMALL_PRECOND_JACOBI)) ||
+        kernel < 0 || kernel > 6)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "kernel %d not available for this solver", kernel);
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    // keep every kernel doing full work: never converge, never stop
+    SolveScalars sc{};
+    sc.tol = -1.0;
+    sc.max_iter = 0x7fffffff;
+    sc.delta = 0.0;
+    sc.bnorm = 1.0;
+    sc.rz = 1.0;
+    sc.sigma0 = 1.0;
+    sc.t0 = 1.0;
+    sc.rmax = 1.0;
+    sc.alpha = 1e-3;
+    sc.beta = 0.5;
+    // the vectors keep the data of the last solve (p.Ap != 0 keeps K1 running)
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->scal.p, &sc, sizeof(sc), cudaMemcpyHostToDevice, ctx->stream));
+    const int g = grid_for(ctx, s->n), gs = spmv_grid(ctx, s->nRowBlocks);
+    const double nd = static_cast<double>(s->n), nz = static_cast<double>(s->nnz);
+    double b = 0.0;
+    auto launch = [&]() -> int {
+        switch (kernel) {
+        case 0:
+            k_spmv_plain<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p,
+                                                         s->nRowBlocks, s->p.p, s->Ap.p);
+            b = 12.0 * nz + 20.0 * nd + 4.0;
+            break;
+        case 1:
+            k_spmv_pap<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
+                                                       s->p.p, s->Ap.p, s->partials.p, s->scal.p);
+            b = 12.0 * nz + 20.0 * nd + 4.0;
+            break;
+        case 2:
+            k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p,
+                                                           s->partials.p, s->scal.p);
+            b = 56.0 * nd;  // p, Ap, invD, x, r read; x, r written
+            break;
+        case 3:
+            k_pupdate_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->invDiag.p, s->p.p, s->scal.p);
+            b = 32.0 * nd;  // r, invD, p read; p written
+            break;
+        default:
+            return mixed_enqueue_kernel(s, kernel, &b);
+        }
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    };
+    int st = launch();  // warm-up
+    if (st)
+        return st;
+    cudaEvent_t e0, e1;
+    SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e0));
+    SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e1));
+    SIMALL_CUDA_TRY(ctx, cudaEventRecord(e0, ctx->stream));
+    for (int i = 0; i < reps && st == SIMALL_OK; ++i)
+        st = launch();
+    SIMALL_CUDA_TRY(ctx, cudaEventRecord(e1, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaEventSynchronize(e1));
+    float total = 0.0f;
+    cudaEventElapsedTime(&total, e0, e1);
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st)
+        return st;
+    *ms = static_cast<double>(total) / reps;
+    if (bytes)
+        *bytes = b;
+    return SIMALL_OK;
+}
+
+int simall_solver_solve_csr(simall_solver *s, int64_t n, int64_t nnz, const int32_t *rowPtr, const int32_t *colIdx,
+                            const double *values, const double *b, double *x, simall_solver_stats *stats)
+{
+    int st = simall_solver_set_matrix(s, n, nnz, rowPtr, colIdx, values, SIMALL_MEM_HOST);
+    if (st)
+        return st;
+    return simall_solver_solve(s, b, x, SIMALL_MEM_HOST, stats);
+}
+
+}  // extern "C"

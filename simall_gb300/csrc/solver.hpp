@@ -1,0 +1,76 @@
+// The solver object behind simall_solver_* (shared by pcg.cu, ilu0.cu, mixed.cu).
+#pragma once
+
+#include "internal.hpp"
+
+namespace simall {
+
+// Level-scheduled ILU(0) data (ilu0.cu).
+struct IluData {
+    DevBuf<double> lu;          // factored values on A's pattern
+    DevBuf<int32_t> diagPtr;    // position of the diagonal in each row (-1 if missing)
+    DevBuf<int32_t> fwdRows;    // rows grouped by forward level
+    DevBuf<int32_t> bwdRows;    // rows grouped by backward level
+    DevBuf<double> y;           // forward-sweep scratch
+    std::vector<int32_t> fwdLevelPtr, bwdLevelPtr;  // level boundaries into fwdRows / bwdRows (host)
+    std::vector<int32_t> h_diagPtr;
+    int maxLevelRows = 0;
+    bool analysed = false;
+};
+
+struct MixedData;  // mixed.cu
+
+// Chunk of solver iterations captured as a CUDA graph.
+struct GraphChunk {
+    cudaGraphExec_t exec = nullptr;
+    int len = 0;
+};
+
+}  // namespace simall
+
+struct simall_solver {
+    simall_context *ctx = nullptr;
+    simall_solver_config cfg{};
+    int64_t n = 0, nnz = 0;
+    const int32_t *rowPtr = nullptr;
+    const int32_t *colIdx = nullptr;
+    const double *values = nullptr;
+    simall::DevBuf<int32_t> own_rowPtr, own_colIdx;
+    simall::DevBuf<double> own_values;
+    std::vector<int32_t> h_rowPtr, h_colIdx;
+    simall::DevBuf<int32_t> rowBlocks;
+    int nRowBlocks = 0;
+    simall::DevBuf<double> invDiag, x, r, p, Ap, z, b;
+    simall::DevBuf<double> partials;
+    simall::DevBuf<simall::SolveScalars> scal;
+    simall::SolveScalars *h_scal = nullptr;  // pinned mirror
+    simall::DevBuf<int> flag;               // device check results
+    double last_residual = 0.0;
+    bool ready = false;
+    bool solved = false;  // a solve completed on the current matrix
+    simall::IluData *ilu = nullptr;
+    simall::MixedData *mixed = nullptr;
+    std::vector<simall::GraphChunk> graphs;  // captured iteration chunks
+};
+
+namespace simall {
+
+int ilu_setup(simall_solver *s);
+int ilu_apply(simall_solver *s, const double *r, double *z);
+void ilu_free(simall_solver *s);
+
+int mixed_setup(simall_solver *s);
+void mixed_invalidate_pattern(simall_solver *s);
+int mixed_solve(simall_solver *s, simall_solver_stats *st);
+// Enqueue one launch of mixed kernel k (4..6) and its algorithmic bytes.
+int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes);
+void mixed_free(simall_solver *s);
+
+// simall_solver_solve with separate memory kinds for b and x.
+int solver_solve_impl(simall_solver *s, const double *b, int bmem, double *x, int xmem, simall_solver_stats *stats);
+
+// Shared by the FP64 and mixed paths.
+int solver_true_residual(simall_solver *s, const double *x, const double *b, double *r, double *rr);
+int solver_fetch_scalars(simall_solver *s);
+
+}  // namespace simall

@@ -1,0 +1,188 @@
+"""Mesh SoA, the device pressure-correction system, and boundary types.
+
+`MeshSoA` holds the reference's mesh layout (src/meshing/MeshStorage.hpp:
+37-105): u64 owner/neighbor with UINT64_MAX on boundary faces, FP64 areas and
+centroids, u32 zones, and the cell->face CSR.  `cartesian()` builds the
+structured box through the library's host generator (bit-identical to
+CartesianMesher + ConnectivityBuilder + compute_geometry) and `rcm()` applies
+renumber_cells_cuthill_mckee.  `PressureSystem` wraps the device assembly of
+SimpleAlgorithm::assemble_pressure_correction.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from enum import IntEnum
+
+import numpy as np
+
+from . import _lib
+from ._lib import MEM_DEVICE, MEM_HOST, check
+from .solver import Context, GpuCGSolver, default_context, ptr_and_mem, register_child
+
+BOUNDARY = np.uint64(0xFFFFFFFFFFFFFFFF)
+
+
+class BCType(IntEnum):
+    """BCType (src/solver/Solver.hpp:105-123)."""
+
+    Wall = 0
+    NoSlipWall = 1
+    MovingWall = 2
+    SlipWall = 3
+    VelocityInlet = 4
+    PressureInlet = 5
+    MassFlowInlet = 6
+    PressureOutlet = 7
+    OutFlow = 8
+    Symmetry = 9
+    Axisymmetric = 10
+    Periodic = 11
+
+
+@dataclass
+class MeshSoA:
+    n_cells: int
+    n_faces: int
+    owner: np.ndarray
+    neighbor: np.ndarray
+    area_x: np.ndarray
+    area_y: np.ndarray
+    area_z: np.ndarray
+    centroid_x: np.ndarray
+    centroid_y: np.ndarray
+    centroid_z: np.ndarray
+    boundary_zone: np.ndarray
+    volume: np.ndarray
+    cell_centroid_x: np.ndarray
+    cell_centroid_y: np.ndarray
+    cell_centroid_z: np.ndarray
+    cell_face_offsets: np.ndarray
+    cell_face_indices: np.ndarray
+
+    def interior(self) -> np.ndarray:
+        return self.neighbor != BOUNDARY
+
+    def view(self) -> _lib.MeshView:
+        v = _lib.MeshView()
+        v.n_cells = self.n_cells
+        v.n_faces = self.n_faces
+        for name in ("owner", "neighbor", "area_x", "area_y", "area_z", "centroid_x", "centroid_y", "centroid_z",
+                     "boundary_zone", "cell_centroid_x", "cell_centroid_y", "cell_centroid_z", "cell_face_offsets",
+                     "cell_face_indices"):
+            setattr(v, name, getattr(self, name).ctypes.data)
+        return v
+
+
+def n_faces_box(nx: int, ny: int, nz: int) -> int:
+    return (nx + 1) * ny * nz + nx * (ny + 1) * nz + nx * ny * (nz + 1)
+
+
+def cartesian(nx: int, ny: int, nz: int, ex: float = 1.0, ey: float = 1.0, ez: float = 1.0,
+              node_shift: np.ndarray | None = None) -> MeshSoA:
+    L = _lib.load()
+    nC = nx * ny * nz
+    nF = n_faces_box(nx, ny, nz)
+    f64 = lambda k: np.empty(k, np.float64)  # noqa: E731
+    m = MeshSoA(nC, nF, np.empty(nF, np.uint64), np.empty(nF, np.uint64), f64(nF), f64(nF), f64(nF), f64(nF),
+                f64(nF), f64(nF), np.empty(nF, np.uint32), f64(nC), f64(nC), f64(nC), f64(nC),
+                np.empty(nC + 1, np.int32), np.empty(6 * nC, np.uint64))
+    if node_shift is not None:
+        sh = [np.ascontiguousarray(node_shift[i], np.float64) for i in range(3)]
+        shp = [s.ctypes.data for s in sh]
+    else:
+        shp = [None, None, None]
+    st = L.simall_mesh_cartesian(nx, ny, nz, ex, ey, ez, *shp, m.owner.ctypes.data, m.neighbor.ctypes.data,
+                                 m.area_x.ctypes.data, m.area_y.ctypes.data, m.area_z.ctypes.data,
+                                 m.centroid_x.ctypes.data, m.centroid_y.ctypes.data, m.centroid_z.ctypes.data,
+                                 m.boundary_zone.ctypes.data, m.volume.ctypes.data, m.cell_centroid_x.ctypes.data,
+                                 m.cell_centroid_y.ctypes.data, m.cell_centroid_z.ctypes.data,
+                                 m.cell_face_offsets.ctypes.data, m.cell_face_indices.ctypes.data)
+    check(st)
+    return m
+
+
+def rcm(m: MeshSoA):
+    """renumber_cells_cuthill_mckee in place; returns (bwBefore, bwAfter, permuted)."""
+    L = _lib.load()
+    stats = np.zeros(3, np.int64)
+    check(L.simall_mesh_rcm(m.n_cells, m.n_faces, m.owner.ctypes.data, m.neighbor.ctypes.data, m.volume.ctypes.data,
+                            m.cell_centroid_x.ctypes.data, m.cell_centroid_y.ctypes.data,
+                            m.cell_centroid_z.ctypes.data, m.cell_face_offsets.ctypes.data,
+                            m.cell_face_indices.ctypes.data, stats.ctypes.data))
+    return tuple(int(s) for s in stats)
+
+
+class PressureSystem:
+    """Device pressure-correction system (pattern + assembly + solve)."""
+
+    def __init__(self, mesh: MeshSoA, bcs: list[tuple[int, int]] | None = None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.L = self.ctx.L
+        self.mesh = mesh
+        bcs = bcs or []
+        arr = (_lib.Boundary * max(1, len(bcs)))()
+        for i, (z, t) in enumerate(bcs):
+            arr[i].zone = int(z)
+            arr[i].type = int(t)
+        view = mesh.view()
+        h = C.c_void_p()
+        check(self.L.simall_pressure_system_create(self.ctx.handle, C.byref(view), arr, len(bcs), C.byref(h)),
+              self.ctx.handle)
+        self.handle = h.value
+        register_child(self)
+        self.ctx.children.add(self)
+        n = C.c_int64()
+        nnz = C.c_int64()
+        check(self.L.simall_pressure_system_pattern(self.handle, C.byref(n), C.byref(nnz), None, None))
+        self.n = n.value
+        self.nnz = nnz.value
+        self.any_dirichlet = None
+
+    def pattern(self):
+        rp = np.empty(self.n + 1, np.int32)
+        ci = np.empty(self.nnz, np.int32)
+        check(self.L.simall_pressure_system_pattern(self.handle, None, None, rp.ctypes.data, ci.ctypes.data))
+        return rp, ci
+
+    def device_arrays(self):
+        """Raw device addresses (rowPtr, colIdx, values, rhs)."""
+        a = [C.c_void_p() for _ in range(4)]
+        check(self.L.simall_pressure_system_device_arrays(self.handle, *[C.byref(v) for v in a]))
+        return tuple(v.value for v in a)
+
+    def assemble(self, rho: float, aP, phi):
+        pa, ma = ptr_and_mem(aP)
+        pp, mp = ptr_and_mem(phi)
+        if ma != mp:
+            raise ValueError("aP and phi must live in the same memory")
+        anyD = C.c_int()
+        check(self.L.simall_assemble_pressure_correction(self.handle, float(rho), pa, pp, ma, C.byref(anyD)),
+              self.ctx.handle)
+        self.any_dirichlet = bool(anyD.value)
+
+    def download(self):
+        v = np.empty(self.nnz)
+        r = np.empty(self.n)
+        check(self.L.simall_pressure_system_download(self.handle, v.ctypes.data, r.ctypes.data), self.ctx.handle)
+        return v, r
+
+    def solve(self, solver: GpuCGSolver, x=None):
+        """Solve the assembled system; x: numpy (default) or a CUDA tensor."""
+        if x is None:
+            x = np.empty(self.n)
+        px, mx = ptr_and_mem(x)
+        check(self.L.simall_pressure_system_solve(self.handle, solver.handle, px, mx, C.byref(solver.stats)),
+              self.ctx.handle)
+        return x
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            self.L.simall_pressure_system_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

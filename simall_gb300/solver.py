@@ -1,0 +1,271 @@
+"""Python mirror of SimAll's linear-solver interface for the pressure path.
+
+Same names and semantics as the reference (src/solver/Solver.hpp:67-102,
+src/solver/LinearSolvers.hpp:28-43, src/solver/CSRMatrix.hpp:16-36):
+`LinearSolverConfig`, `PreconditionerKind`, `CSRMatrix`, and an
+`ILinearSolver`-shaped `GpuCGSolver` whose `solve(A, b, x)` overwrites x from
+zero and returns the iteration count exactly as CGSolver::solve does
+(LinearSolvers.cpp:420-451), with `last_residual()` the relative residual.
+Every call goes through libsimall_gpu.so; there is no CPU path.
+"""
+from __future__ import annotations
+
+import atexit
+import ctypes as C
+import weakref
+from dataclasses import dataclass, field
+from enum import IntEnum
+
+import numpy as np
+
+from . import _lib
+from ._lib import MEM_DEVICE, MEM_HOST, SimallError, check
+
+
+class LinearSolverKind(IntEnum):
+    GMRES = 0
+    BiCGSTAB = 1
+    CG = 2
+    TFQMR = 3
+
+
+class PreconditionerKind(IntEnum):
+    Jacobi = 0
+    ILU = 1
+    SSOR = 2
+    AMG = 3
+    None_ = 4
+
+
+class Precision(IntEnum):
+    FP64 = 0
+    MIXED = 1
+
+
+@dataclass
+class LinearSolverConfig:
+    """LinearSolverConfig (src/solver/Solver.hpp:83-90), same defaults."""
+
+    kind: LinearSolverKind = LinearSolverKind.GMRES
+    preconditioner: PreconditionerKind = PreconditionerKind.ILU
+    tolerance: float = 1.0e-8
+    maxIterations: int = 1000
+    restart: int = 30
+
+
+@dataclass
+class CSRMatrix:
+    """CSRMatrix (src/solver/CSRMatrix.hpp:16-36): int32 rowPtr/colIdx, FP64 values."""
+
+    rowPtr: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    colIdx: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    values: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float64))
+
+    def rows(self) -> int:
+        return 0 if len(self.rowPtr) == 0 else len(self.rowPtr) - 1
+
+    def nnz(self) -> int:
+        return len(self.colIdx)
+
+
+def _is_torch(a) -> bool:
+    return type(a).__module__.startswith("torch")
+
+
+def ptr_and_mem(a):
+    """(address, memory kind) of a numpy array or a torch tensor."""
+    if a is None:
+        return None, MEM_HOST
+    if _is_torch(a):
+        if not a.is_contiguous():
+            raise ValueError("tensor must be contiguous")
+        return a.data_ptr(), (MEM_DEVICE if a.is_cuda else MEM_HOST)
+    if not a.flags["C_CONTIGUOUS"]:
+        raise ValueError("array must be C-contiguous")
+    return a.ctypes.data, MEM_HOST
+
+
+# Every live library object, so that interpreter shutdown releases children
+# (solvers, pressure systems) before the contexts they point into, while the
+# CUDA runtime is still up.  Finalizer order at shutdown is otherwise
+# arbitrary.
+_live_children: "weakref.WeakSet" = weakref.WeakSet()
+_live_contexts: "weakref.WeakSet" = weakref.WeakSet()
+
+
+def register_child(obj) -> None:
+    _live_children.add(obj)
+
+
+@atexit.register
+def _release_all() -> None:
+    for o in list(_live_children):
+        try:
+            o.close()
+        except Exception:
+            pass
+    for c in list(_live_contexts):
+        try:
+            c.close()
+        except Exception:
+            pass
+
+
+class Context:
+    """A device + stream (simall_context)."""
+
+    def __init__(self, device: int = 0, stream=None):
+        self.L = _lib.load()
+        h = C.c_void_p()
+        s = None
+        if stream is not None:
+            s = stream.cuda_stream if hasattr(stream, "cuda_stream") else int(stream)
+        st = self.L.simall_context_create(int(device), s, C.byref(h))
+        if st != 0:
+            raise SimallError(st, "simall_context_create")
+        self.handle = h.value
+        self.device = device
+        self.children: "weakref.WeakSet" = weakref.WeakSet()
+        _live_contexts.add(self)
+
+    @property
+    def stream(self) -> int:
+        return self.L.simall_context_stream(self.handle) or 0
+
+    @property
+    def kernel_launches(self) -> int:
+        return int(self.L.simall_context_kernel_launches(self.handle))
+
+    def synchronize(self):
+        check(self.L.simall_context_synchronize(self.handle), self.handle)
+
+    def last_error(self) -> str:
+        return (self.L.simall_context_last_error(self.handle) or b"").decode()
+
+    def close(self):
+        if getattr(self, "handle", None):
+            for ch in list(self.children):
+                ch.close()
+            self.L.simall_context_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default_ctx: Context | None = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class GpuCGSolver:
+    """ILinearSolver (src/solver/Solver.hpp:92-100) backed by the device PCG.
+
+    precision=Precision.MIXED selects the FP32-inner / FP64-refined solver
+    (Jacobi only).  `stats` holds the SolverStats of the last solve.
+    """
+
+    def __init__(self, cfg: LinearSolverConfig | None = None, precision: Precision = Precision.FP64,
+                 ctx: Context | None = None, reliable_delta: float = 0.1, check_interval: int = 0):
+        cfg = cfg or LinearSolverConfig(kind=LinearSolverKind.CG)
+        self.cfg = cfg
+        self.ctx = ctx or default_context()
+        self.L = self.ctx.L
+        c = _lib.SolverConfig()
+        self.L.simall_solver_config_default(C.byref(c))
+        c.preconditioner = int(cfg.preconditioner)
+        c.tolerance = float(cfg.tolerance)
+        c.max_iterations = int(cfg.maxIterations)
+        c.precision = int(precision)
+        c.reliable_delta = float(reliable_delta)
+        c.check_interval = int(check_interval)
+        h = C.c_void_p()
+        check(self.L.simall_solver_create(self.ctx.handle, C.byref(c), C.byref(h)), self.ctx.handle)
+        self.handle = h.value
+        self.stats = _lib.SolverStats()
+        self._keep = None  # device arrays referenced by set_matrix
+        register_child(self)
+        self.ctx.children.add(self)
+
+    # -- ILinearSolver -------------------------------------------------------
+    def solve(self, A: CSRMatrix, b, x) -> int:
+        """CGSolver::solve: preconditioner set up again, x overwritten from 0."""
+        n = A.rows()
+        rp = np.ascontiguousarray(A.rowPtr, np.int32)
+        ci = np.ascontiguousarray(A.colIdx, np.int32)
+        va = np.ascontiguousarray(A.values, np.float64)
+        bb = np.ascontiguousarray(b, np.float64)
+        if len(bb) != n:
+            raise SimallError(8, "b size")
+        out = np.empty(n, np.float64)
+        st = self.L.simall_solver_solve_csr(self.handle, n, len(ci), rp.ctypes.data, ci.ctypes.data,
+                                            va.ctypes.data, bb.ctypes.data, out.ctypes.data, C.byref(self.stats))
+        check(st, self.ctx.handle)
+        if isinstance(x, np.ndarray) and x.shape == out.shape:
+            x[...] = out
+        elif isinstance(x, list):
+            x[:] = out.tolist()
+        return int(self.stats.iterations)
+
+    def last_residual(self) -> float:
+        return float(self.L.simall_solver_last_residual(self.handle))
+
+    # -- device-resident use ---------------------------------------------------
+    def set_matrix(self, rowPtr, colIdx, values):
+        """Upload (numpy) or reference (CUDA tensors) a CSR matrix."""
+        p0, m0 = ptr_and_mem(rowPtr)
+        p1, _ = ptr_and_mem(colIdx)
+        p2, _ = ptr_and_mem(values)
+        n = len(rowPtr) - 1
+        check(self.L.simall_solver_set_matrix(self.handle, n, len(colIdx), p0, p1, p2, m0), self.ctx.handle)
+        self._keep = (rowPtr, colIdx, values) if m0 == MEM_DEVICE else None
+        self.n = n
+
+    def update_values(self, values):
+        p, m = ptr_and_mem(values)
+        check(self.L.simall_solver_update_values(self.handle, p, m), self.ctx.handle)
+
+    def solve_into(self, b, x) -> int:
+        """Solve with the current matrix; b and x both numpy or both CUDA tensors."""
+        pb, mb = ptr_and_mem(b)
+        px, mx = ptr_and_mem(x)
+        if mb != mx:
+            raise ValueError("b and x must live in the same memory")
+        check(self.L.simall_solver_solve(self.handle, pb, px, mb, C.byref(self.stats)), self.ctx.handle)
+        return int(self.stats.iterations)
+
+    def spmv(self, x, y):
+        px, mx = ptr_and_mem(x)
+        py, _ = ptr_and_mem(y)
+        check(self.L.simall_solver_spmv(self.handle, px, py, mx), self.ctx.handle)
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            self.L.simall_solver_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def make_cg(cfg: LinearSolverConfig, **kw) -> GpuCGSolver:
+    return GpuCGSolver(cfg, **kw)
+
+
+def make_linear_solver(cfg: LinearSolverConfig, **kw) -> GpuCGSolver:
+    """make_linear_solver (src/solver/Solver.cpp:25-39) for the pressure path:
+    only the CG branch exists on the device."""
+    if cfg.kind != LinearSolverKind.CG:
+        raise NotImplementedError("only CG (the pressure-correction solver) is provided on the GPU")
+    return GpuCGSolver(cfg, **kw)

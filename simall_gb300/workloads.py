@@ -1,0 +1,99 @@
+"""Seeded synthetic inputs with the shapes of the pressure-path workloads.
+
+All randomness comes from numpy's PCG64 (`np.random.default_rng(seed)`), so
+the same seed gives the same inputs on every host.  These produce input data
+only (node shifts, aP, face fluxes, right-hand sides, conductances); the
+computation under test stays in the library.
+
+Workloads (sizes as named by the pressure-path benchmark set):
+  cavity      2-D lid-driven cavity N x N x 1 (SIMPLE trajectory; the systems
+              themselves come from the SIMPLE loop)
+  poisson3d   N^3 box, interior nodes shifted by U(-0.2,0.2)*h per
+              coordinate, RCM, aP = 1, interior face flux N(0,1), all walls
+              (cell-0 pin)
+  varcoef     N^3 box, k_c = exp(N(0,1)) per cell -> aP = 1/k_c (harmonic
+              face averaging), PressureOutlet (p' = 0) on x = 0, rhs N(0,1)
+  batched     many 2-D cavity-type systems, sides log-uniform in [32, 256],
+              aP = 1, rhs N(0,1) with its mean removed, cell-0 pin
+  facek       N^3 box with face conductances exp(N(0,0.5)) and Dirichlet
+              values N(0,1) on x = 0
+"""
+from __future__ import annotations
+
+import numpy as np
+
+from .mesh import BCType, MeshSoA, cartesian, rcm
+
+DEFAULT_SEED = 42
+ALL_WALLS = [(z, int(BCType.NoSlipWall)) for z in (1, 2, 3, 4, 5, 6)]
+X0_OUTLET = [(1, int(BCType.PressureOutlet))] + [(z, int(BCType.NoSlipWall)) for z in (2, 3, 4, 5, 6)]
+CAVITY = [(z, int(BCType.NoSlipWall)) for z in (1, 2, 3, 5, 6)] + [(4, int(BCType.MovingWall))]
+
+
+def interior_node_shift(nx, ny, nz, ex=1.0, ey=1.0, ez=1.0, amp=0.2, seed=DEFAULT_SEED) -> np.ndarray:
+    """(3, nNodes) displacement: U(-amp, amp) * h per coordinate on nodes
+    strictly inside the box, zero on the boundary."""
+    rng = np.random.default_rng(seed)
+    px, py, pz = nx + 1, ny + 1, nz + 1
+    d = rng.uniform(-amp, amp, size=(3, px * py * pz))
+    i = np.arange(px)
+    j = np.arange(py)
+    k = np.arange(pz)
+    inner = ((k[:, None, None] > 0) & (k[:, None, None] < nz) & (j[None, :, None] > 0) & (j[None, :, None] < ny)
+             & (i[None, None, :] > 0) & (i[None, None, :] < nx)).ravel()
+    d[:, ~inner] = 0.0
+    d[0] *= ex / nx
+    d[1] *= ey / ny
+    d[2] *= ez / nz
+    return d
+
+
+def poisson3d_mesh(n=128, seed=DEFAULT_SEED, amp=0.2, renumber=True) -> tuple[MeshSoA, tuple | None]:
+    m = cartesian(n, n, n, 1.0, 1.0, 1.0, node_shift=interior_node_shift(n, n, n, amp=amp, seed=seed))
+    stats = rcm(m) if renumber else None
+    return m, stats
+
+
+def poisson3d_inputs(m: MeshSoA, seed=DEFAULT_SEED):
+    """aP = 1; phi = N(0,1) on interior faces, 0 on boundary faces."""
+    rng = np.random.default_rng(seed + 1)
+    phi = rng.standard_normal(m.n_faces)
+    phi[~m.interior()] = 0.0
+    return np.ones(m.n_cells), phi
+
+
+def varcoef_mesh(n=256) -> MeshSoA:
+    return cartesian(n, n, n, 1.0, 1.0, 1.0)
+
+
+def varcoef_inputs(m: MeshSoA, seed=DEFAULT_SEED):
+    """aP = 1/k with k = exp(N(0,1)) per cell; phi = 0; rhs N(0,1)."""
+    rng = np.random.default_rng(seed + 2)
+    k = np.exp(rng.standard_normal(m.n_cells))
+    rhs = rng.standard_normal(m.n_cells)
+    return 1.0 / k, np.zeros(m.n_faces), rhs
+
+
+def batched_sides(count=512, lo=32, hi=256, seed=DEFAULT_SEED) -> np.ndarray:
+    rng = np.random.default_rng(seed + 3)
+    return np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), size=count))).astype(np.int64)
+
+
+def batched_rhs(n: int, rng: np.random.Generator) -> np.ndarray:
+    b = rng.standard_normal(n)
+    b -= b.mean()
+    b[0] = 0.0  # the pinned cell
+    return b
+
+
+def facek_inputs(m: MeshSoA, seed=DEFAULT_SEED, sigma=0.5):
+    """k_f = exp(N(0, sigma)) on interior and x=0 faces; pb ~ N(0,1) on x=0
+    faces; cell source N(0,1)."""
+    rng = np.random.default_rng(seed + 4)
+    k = np.exp(sigma * rng.standard_normal(m.n_faces))
+    pb = rng.standard_normal(m.n_faces)
+    dirichlet = (~m.interior()) & (m.boundary_zone == 1)
+    k[(~m.interior()) & ~dirichlet] = 0.0
+    pb[~dirichlet] = 0.0
+    src = rng.standard_normal(m.n_cells)
+    return k, pb, dirichlet.astype(np.uint8), src

@@ -1,0 +1,205 @@
+"""Parity of the device PCG (FP64 Jacobi / ILU0, mixed precision) and the
+device SpMV with the oracle (CGSolver::solve, CSRMatrix::spmv,
+src/solver/LinearSolvers.cpp:420-451, src/solver/CSRMatrix.hpp:24-35)."""
+import numpy as np
+import pytest
+
+from helpers import bits_equal, oracle_system, rel, tridiag
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(sg, pc, tol=1e-8, maxit=1000):
+    return sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=pc, tolerance=tol, maxIterations=maxit)
+
+
+def test_spmv_bit_exact(sg, ctx, oracle):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 12)
+    s = sg.GpuCGSolver(_cfg(sg, sg.PreconditionerKind.Jacobi), ctx=ctx)
+    s.set_matrix(rp, ci, v)
+    x = np.random.default_rng(3).standard_normal(len(rp) - 1)
+    y = np.empty_like(x)
+    s.spmv(x, y)
+    assert bits_equal(y, oracle.spmv(rp, ci, v, x))
+
+
+def test_facade_spmv_and_blas1_known_answers(sg, ctx):
+    """tests/unit/gpu/test_gpu_models.cpp:117-178 re-expressed on the device facade."""
+    torch = pytest.importorskip("torch")
+    L = sg.load()
+    dev = torch.device("cuda:0")
+    x = torch.arange(1, 6, dtype=torch.float64, device=dev)
+    y = torch.ones(5, dtype=torch.float64, device=dev)
+    assert L.simall_gpu_axpy(2.0, x.data_ptr(), y.data_ptr(), 5, None) == 0
+    torch.cuda.synchronize()
+    assert torch.allclose(y.cpu(), 1.0 + 2.0 * torch.arange(1, 6, dtype=torch.float64), atol=1e-12)
+    assert L.simall_gpu_scal(0.5, y.data_ptr(), 5, None) == 0
+    torch.cuda.synchronize()
+    assert abs(y[0].item() - 1.5) < 1e-12
+    import ctypes as C
+    d = C.c_double()
+    assert L.simall_gpu_dot(x.data_ptr(), x.data_ptr(), 5, None, C.byref(d)) == 0
+    assert abs(d.value - 55.0) < 1e-12
+    assert L.simall_gpu_nrm2(x.data_ptr(), 5, None, C.byref(d)) == 0
+    assert abs(d.value - np.sqrt(55.0)) < 1e-12 * np.sqrt(55.0)
+    rp = torch.tensor([0, 2, 5, 8, 10], dtype=torch.int32, device=dev)
+    ci = torch.tensor([0, 1, 0, 1, 2, 1, 2, 3, 2, 3], dtype=torch.int32, device=dev)
+    va = torch.tensor([4, -1, -1, 4, -1, -1, 4, -1, -1, 4], dtype=torch.float64, device=dev)
+    xx = torch.arange(1, 5, dtype=torch.float64, device=dev)
+    yy = torch.empty(4, dtype=torch.float64, device=dev)
+    assert L.simall_gpu_spmv_csr(4, rp.data_ptr(), ci.data_ptr(), va.data_ptr(), xx.data_ptr(), yy.data_ptr(),
+                                 None) == 0
+    torch.cuda.synchronize()
+    assert yy.cpu().tolist() == [2.0, 4.0, 6.0, 13.0]
+
+
+def test_cg_tridiagonal_known_answer(sg, ctx):
+    """tests/unit/gpu/test_gpu_models.cpp:181-235: tridiag(-1,4,-1), n=10,
+    b = e_1 + e_n, Jacobi, tol 1e-10: < 50 iterations, ||b - Ax|| < 1e-8."""
+    rp, ci, va = tridiag(10)
+    b = np.zeros(10)
+    b[0] = b[-1] = 1.0
+    s = sg.GpuCGSolver(_cfg(sg, sg.PreconditionerKind.Jacobi, tol=1e-10, maxit=200), ctx=ctx)
+    x = np.zeros(10)
+    it = s.solve(sg.CSRMatrix(rp, ci, va), b, x)
+    assert it < 50 and s.stats.converged
+    r = b - np.array([sum(va[k] * x[ci[k]] for k in range(rp[i], rp[i + 1])) for i in range(10)])
+    assert np.linalg.norm(r) < 1e-8
+
+
+@pytest.mark.parametrize("pc", [0, 1])
+@pytest.mark.parametrize("zones", [(), (1,)])
+def test_pcg_fp64_matches_oracle(sg, ctx, oracle, pc, zones):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 14, pressure_zones=zones)
+    xo, ito, lasto = oracle.cg(rp, ci, v, rhs, pc, 1e-8, 2000)
+    s = sg.GpuCGSolver(_cfg(sg, pc, maxit=2000), ctx=ctx)
+    x = np.zeros(len(rhs))
+    it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    assert abs(it - ito) <= 1, (it, ito)
+    assert rel(x, xo) <= 1e-10
+    assert s.last_residual() < 1e-8 and abs(s.last_residual() - lasto) <= 0.05 * lasto
+    assert s.stats.true_residual < 2e-8
+
+
+def test_pcg_ilu0_larger_matches_oracle(sg, ctx, oracle):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 24)
+    xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 1, 1e-8, 2000)
+    s = sg.GpuCGSolver(_cfg(sg, 1, maxit=2000), ctx=ctx)
+    x = np.zeros(len(rhs))
+    it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    assert abs(it - ito) <= 1 and rel(x, xo) <= 1e-10
+
+
+def test_ilu0_factor_and_apply_bit_exact(sg, ctx, oracle):
+    torch = pytest.importorskip("torch")
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 10)
+    lu, dp = oracle.ilu0_setup(rp, ci, v)
+    dev = torch.device("cuda:0")
+    trp = torch.from_numpy(rp).to(dev)
+    tci = torch.from_numpy(ci).to(dev)
+    tv = torch.from_numpy(v.copy()).to(dev)
+    import ctypes as C
+    ok = C.c_int()
+    L = sg.load()
+    assert L.simall_gpu_ilu0_factor_inplace(len(rp) - 1, trp.data_ptr(), tci.data_ptr(), tv.data_ptr(), None,
+                                            C.byref(ok)) == 0
+    assert ok.value == 1
+    assert bits_equal(tv.cpu().numpy(), lu)
+    r = np.random.default_rng(5).standard_normal(len(rp) - 1)
+    tr = torch.from_numpy(r).to(dev)
+    tz = torch.empty_like(tr)
+    assert L.simall_gpu_ilu0_apply(len(rp) - 1, trp.data_ptr(), tci.data_ptr(), tv.data_ptr(), tr.data_ptr(),
+                                   tz.data_ptr(), None) == 0
+    torch.cuda.synchronize()
+    assert bits_equal(tz.cpu().numpy(), oracle.ilu0_apply(rp, ci, lu, dp, r))
+
+
+@pytest.mark.parametrize("zones", [(), (1,)])
+def test_mixed_precision_reaches_tolerance(sg, ctx, oracle, zones):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 16, pressure_zones=zones, renumber=False, amp=0.0)
+    xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 0, 1e-12, 5000)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx)
+    x = np.zeros(len(rhs))
+    s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    r = rhs - oracle.spmv(rp, ci, v, x)
+    tr = np.linalg.norm(r) / np.linalg.norm(rhs)
+    assert tr < 1e-8 and s.stats.converged
+    assert abs(s.stats.true_residual - tr) <= 1e-3 * tr + 1e-15
+    assert s.stats.reliable_updates >= 1
+
+
+def test_mixed_precision_unstructured_pattern(sg, ctx, oracle):
+    """RCM-renumbered distorted mesh: no diagonal structure, FP32 CSR storage."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 12)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx)
+    x = np.zeros(len(rhs))
+    s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+    assert tr < 1e-8
+
+
+def test_zero_rhs_returns_zero(sg, ctx, oracle):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 6)
+    for prec in (sg.Precision.FP64, sg.Precision.MIXED):
+        s = sg.GpuCGSolver(_cfg(sg, 0), precision=prec, ctx=ctx)
+        x = np.ones(len(rhs))
+        it = s.solve(sg.CSRMatrix(rp, ci, v), np.zeros(len(rhs)), x)
+        assert it == 0 and not np.any(x)
+
+
+def test_max_iterations_semantics(sg, ctx, oracle):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 10)
+    xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 0, 1e-14, 7)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-14, maxit=7), ctx=ctx)
+    x = np.zeros(len(rhs))
+    it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    assert it == ito == 7 and not s.stats.converged
+    assert rel(x, xo) <= 1e-12
+
+
+@pytest.mark.parametrize("bad", ["nan", "unsorted", "nodiag", "range", "rowptr"])
+def test_input_errors_are_reported(sg, ctx, oracle, bad):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 4)
+    rp, ci, v = rp.copy(), ci.copy(), v.copy()
+    expect = {"nan": 6, "unsorted": 4, "nodiag": 5, "range": 13, "rowptr": 8}[bad]
+    if bad == "nan":
+        v[3] = np.nan
+    elif bad == "unsorted":
+        ci[1], ci[2] = ci[2], ci[1]
+    elif bad == "nodiag":
+        ci[0] = ci[1] - 1 if ci[1] > 1 else 1
+        ci[0], ci[1] = min(ci[0], ci[1]), max(ci[0], ci[1])
+        if ci[0] == ci[1] or 0 in ci[rp[0]:rp[1]]:
+            pytest.skip("could not construct the case")
+    elif bad == "range":
+        ci[-1] = len(rp) + 5
+    elif bad == "rowptr":
+        rp[-1] += 1
+    s = sg.GpuCGSolver(_cfg(sg, 0), ctx=ctx)
+    with pytest.raises(sg.SimallError) as e:
+        s.solve(sg.CSRMatrix(rp, ci, v), rhs, np.zeros(len(rhs)))
+    assert e.value.status == expect
+
+
+def test_nonfinite_rhs_rejected(sg, ctx, oracle):
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 4)
+    b = rhs.copy()
+    b[2] = np.inf
+    s = sg.GpuCGSolver(_cfg(sg, 0), ctx=ctx)
+    with pytest.raises(sg.SimallError) as e:
+        s.solve(sg.CSRMatrix(rp, ci, v), b, np.zeros(len(b)))
+    assert e.value.status == 6
+
+
+def test_device_resident_solve_matches_host(sg, ctx, oracle):
+    torch = pytest.importorskip("torch")
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 10)
+    dev = torch.device("cuda:0")
+    s = sg.GpuCGSolver(_cfg(sg, 0), ctx=ctx)
+    trp, tci, tv = (torch.from_numpy(a).to(dev) for a in (rp, ci, v))
+    s.set_matrix(trp, tci, tv)
+    tb = torch.from_numpy(rhs).to(dev)
+    tx = torch.empty_like(tb)
+    s.solve_into(tb, tx)
+    xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
+    assert rel(tx.cpu().numpy(), xo) <= 1e-10
