@@ -311,7 +311,7 @@ class RefLib:
         L.ref_cavity_run.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P]
         L.ref_cavity_fetch.argtypes = [_P] * 9
         L.ref_discrete_adjoint.restype = C.c_int
-        L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 12
+        L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
 
     @staticmethod

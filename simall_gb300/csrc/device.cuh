@@ -116,6 +116,49 @@ __device__ __forceinline__ void spmv_rowblocks(const int32_t *__restrict__ rowPt
     }
 }
 
+// Same row-blocks, fused multiply-add form: a_ij and j are staged in shared
+// memory with coalesced loads, then each row is accumulated with one FMA per
+// nonzero.  Half the FP64 instructions of the exact form (GB300's FP64 rate
+// is low enough for that to matter); the sum differs from CSRMatrix::spmv
+// only in rounding.
+template <class Epi>
+__device__ __forceinline__ void spmv_rowblocks_fma(const int32_t *__restrict__ rowPtr,
+                                                   const int32_t *__restrict__ colIdx,
+                                                   const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                   int nRB, const double *__restrict__ x, Epi &epi)
+{
+    __shared__ double sv[kSpmvNnzCap];
+    __shared__ int32_t sc[kSpmvNnzCap];
+    for (int b = blockIdx.x; b < nRB; b += gridDim.x) {
+        const int r0 = __ldg(rb + b), r1 = __ldg(rb + b + 1);
+        const int base = __ldg(rowPtr + r0);
+        const int cnt = __ldg(rowPtr + r1) - base;
+        if (cnt <= kSpmvNnzCap) {
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
+                sv[k] = __ldg(val + base + k);
+                sc[k] = __ldg(colIdx + base + k);
+            }
+            __syncthreads();
+            for (int row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
+                const int k0 = __ldg(rowPtr + row) - base, k1 = __ldg(rowPtr + row + 1) - base;
+                double s = 0.0;
+                for (int k = k0; k < k1; ++k)
+                    s = fma(sv[k], __ldg(x + sc[k]), s);
+                epi(row, s);
+            }
+            __syncthreads();
+        } else {
+            double s[1] = {0.0};
+            for (int k = threadIdx.x; k < cnt; k += blockDim.x)
+                s[0] = fma(__ldg(val + base + k), __ldg(x + __ldg(colIdx + base + k)), s[0]);
+            block_sum<1>(s);
+            if (threadIdx.x == 0)
+                epi(r0, s[0]);
+            __syncthreads();
+        }
+    }
+}
+
 // std::max(a, b) as the reference evaluates it.
 __device__ __forceinline__ double std_max(double a, double b) { return (a < b) ? b : a; }
 

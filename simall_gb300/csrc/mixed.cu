@@ -38,7 +38,8 @@ struct DiaOffsets {
 struct MixedData {
     bool dia = false;
     DiaOffsets offs{};
-    DevBuf<float> U;          // [nd][n] upper diagonals of S A S (dia)
+    DevBuf<float> U;          // [nd][ldU] upper diagonals of S A S (dia)
+    int64_t ldU = 0;          // diagonal stride, n rounded up to 4 (16-byte aligned rows)
     DevBuf<int32_t> orow;     // off-diagonal CSR rowPtr (csr)
     DevBuf<int32_t> ocol;
     DevBuf<float> oval;
@@ -103,7 +104,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_symcheck(int64_t n, const int32_t
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_mx_build_dia(int64_t n, const int32_t *__restrict__ rowPtr,
+__global__ void __launch_bounds__(kBlock) k_mx_build_dia(int64_t n, int64_t ldU, const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const double *__restrict__ val, const double *__restrict__ sc,
                                                          DiaOffsets o, float *__restrict__ U)
@@ -125,7 +126,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_dia(int64_t n, const int32_
                     u[d] = static_cast<float>(val[k] * si * sc[j]);
         }
         for (int d = 0; d < o.nd; ++d)
-            U[d * n + i] = u[d];
+            U[d * ldU + i] = u[d];
     }
 }
 
@@ -197,29 +198,79 @@ __device__ __forceinline__ void mx_alpha(SolveScalars *s, double pq)
     }
 }
 
-// K1 (dia): qh = (S A S) ph, pq = ph.qh.
-__global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int64_t n, DiaOffsets o, const float *__restrict__ U,
+// Four consecutive floats starting at p; p is 16-byte aligned when `aligned`.
+__device__ __forceinline__ float4 ld4(const float *__restrict__ p, bool aligned)
+{
+    if (aligned)
+        return __ldg(reinterpret_cast<const float4 *>(p));
+    return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
+}
+
+__device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
+{
+    y[0] += a.x * b.x;
+    y[1] += a.y * b.y;
+    y[2] += a.z * b.z;
+    y[3] += a.w * b.w;
+}
+
+// K1 (dia): qh = (S A S) ph, pq = ph.qh.  ND upper diagonals at ascending
+// offsets; row i reads U_d[i] x_{i+off} and, by symmetry, U_d[i-off] x_{i-off}.
+// One thread per 4 consecutive rows with 128-bit loads of every 16-byte
+// aligned stream; rows within the largest offset of either end of the
+// matrix take the bounds-checked path.
+template <int ND>
+__global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
                                                         const float *__restrict__ ph, float *__restrict__ qh,
                                                         double *partials, SolveScalars *s)
 {
     if (ld_flag(&s->done))
         return;
     float acc = 0.0f;
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float pi = __ldg(ph + i);
-        float y = pi;
+    const int nq = (n + 3) >> 2;
+    const int maxoff = o.off[ND - 1];
+    bool al[ND];
 #pragma unroll
-        for (int d = 0; d < kMaxDiags; ++d) {
-            if (d >= o.nd)
-                break;
-            const int64_t off = o.off[d];
-            if (i + off < n)
-                y += __ldg(U + d * n + i) * __ldg(ph + i + off);
-            if (i - off >= 0)
-                y += __ldg(U + d * n + i - off) * __ldg(ph + i - off);
+    for (int d = 0; d < ND; ++d)
+        al[d] = (o.off[d] & 3) == 0;
+    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+        const int i = q << 2;
+        float y[4];
+        if (i >= maxoff && i + 3 + maxoff < n) {
+            const float4 p4 = __ldg(reinterpret_cast<const float4 *>(ph + i));
+            y[0] = p4.x;
+            y[1] = p4.y;
+            y[2] = p4.z;
+            y[3] = p4.w;
+#pragma unroll
+            for (int d = 0; d < ND; ++d) {
+                const int off = o.off[d];
+                const float *Ud = U + d * ldU;
+                fma4(y, __ldg(reinterpret_cast<const float4 *>(Ud + i)), ld4(ph + i + off, al[d]));
+                fma4(y, ld4(Ud + i - off, al[d]), ld4(ph + i - off, al[d]));
+            }
+            *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
+            acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
+        } else {
+            for (int r = 0; r < 4; ++r) {
+                const int row = i + r;
+                if (row >= n)
+                    break;
+                const float pr = __ldg(ph + row);
+                float v = pr;
+#pragma unroll
+                for (int d = 0; d < ND; ++d) {
+                    const int off = o.off[d];
+                    const float *Ud = U + d * ldU;
+                    if (row + off < n)
+                        v += __ldg(Ud + row) * __ldg(ph + row + off);
+                    if (row - off >= 0)
+                        v += __ldg(Ud + row - off) * __ldg(ph + row - off);
+                }
+                qh[row] = v;
+                acc += pr * v;
+            }
         }
-        qh[i] = y;
-        acc += pi * y;
     }
     double v[1] = {static_cast<double>(acc)};
     if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0)
@@ -399,6 +450,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_pupdate(int64_t n, const float *_
         ph[i] = rh[i] + beta * ph[i];
 }
 
+int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *ph, float *qh, double *partials,
+                    SolveScalars *sc);
+
 int grid_n(simall_context *ctx, int64_t n)
 {
     const int64_t g = (n + kBlock - 1) / kBlock;
@@ -455,6 +509,32 @@ void analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
     m->patternReady = true;
 }
 
+int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *ph, float *qh, double *partials,
+                    SolveScalars *sc)
+{
+    const int g = grid_n(ctx, (n + 3) / 4);
+    const int ni = static_cast<int>(n);
+    switch (m->offs.nd) {
+#define SIMALL_DIA_CASE(ND)                                                                                           \
+    case ND:                                                                                                          \
+        k_mx_spmv_dia<ND><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, ph, qh, partials, sc);          \
+        break;
+        SIMALL_DIA_CASE(1)
+        SIMALL_DIA_CASE(2)
+        SIMALL_DIA_CASE(3)
+        SIMALL_DIA_CASE(4)
+        SIMALL_DIA_CASE(5)
+        SIMALL_DIA_CASE(6)
+        SIMALL_DIA_CASE(7)
+        SIMALL_DIA_CASE(8)
+#undef SIMALL_DIA_CASE
+    default:
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "dia storage with %d diagonals", m->offs.nd);
+    }
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
 }  // namespace
 
 int mixed_setup(simall_solver *s)
@@ -491,8 +571,12 @@ int mixed_setup(simall_solver *s)
     if (m->dia && (h & 2))
         analyse_pattern(s, m, false);  // not numerically symmetric: keep every off-diagonal entry
     if (m->dia) {
-        SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * n));
-        k_mx_build_dia<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->offs, m->U.p);
+        m->ldU = (n + 3) & ~static_cast<int64_t>(3);
+        SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * m->ldU));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(m->U.p, 0, static_cast<size_t>(m->offs.nd) * m->ldU * sizeof(float),
+                                             ctx->stream));
+        k_mx_build_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->ldU, s->rowPtr, s->colIdx, s->values, m->scale.p, m->offs,
+                                                      m->U.p);
         SIMALL_LAUNCH_CHECK(ctx);
     } else {
         const int no = m->nnzOff;
@@ -532,12 +616,15 @@ int enqueue_mixed_iteration(simall_solver *s)
     MixedData *m = s->mixed;
     const int64_t n = s->n;
     const int g = grid_n(ctx, n);
-    if (m->dia)
-        k_mx_spmv_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->offs, m->U.p, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
-    else
+    if (m->dia) {
+        int st = launch_spmv_dia(ctx, m, n, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
+        if (st)
+            return st;
+    } else {
         k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
                                                      s->partials.p, s->scal.p);
-    SIMALL_LAUNCH_CHECK(ctx);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
     k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
@@ -650,9 +737,8 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     switch (k) {
     case 4:
         if (m->dia) {
-            k_mx_spmv_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->offs, m->U.p, m->ph.p, m->qh.p, s->partials.p,
-                                                         s->scal.p);
             *bytes = (4.0 * m->offs.nd + 8.0) * nd;  // U once, ph gathered once, qh written
+            return launch_spmv_dia(ctx, m, n, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
         } else {
             k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
                                                          s->partials.p, s->scal.p);

@@ -113,7 +113,7 @@ __global__ void __launch_bounds__(kBlock) k_spmv_pap(const int32_t *__restrict__
     if (ld_done(s))
         return;
     PapEpi epi{Ap, p, 0.0};
-    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, p, epi);
+    spmv_rowblocks_fma(rowPtr, colIdx, val, rb, nRB, p, epi);
     double v[1] = {epi.acc};
     if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0) {
         const double pAp = v[0];
@@ -166,11 +166,14 @@ __device__ __forceinline__ void finish_iteration(SolveScalars *s, double rr, dou
     }
 }
 
-// K2 (Jacobi): x += alpha p, r -= alpha Ap, z = invD r (not stored), ||r||^2, r.z.
+// K2 (Jacobi): x += alpha p, r -= alpha Ap, z = invD r, ||r||^2, r.z.  z is
+// stored so K3 does not spend an FP64 multiply recomputing it (same bytes:
+// K3 reads z instead of r and invD).
 __global__ void __launch_bounds__(kBlock) k_update_jacobi(int64_t n, const double *__restrict__ p,
                                                           const double *__restrict__ Ap,
                                                           const double *__restrict__ invD, double *__restrict__ x,
-                                                          double *__restrict__ r, double *partials, SolveScalars *s)
+                                                          double *__restrict__ r, double *__restrict__ z,
+                                                          double *partials, SolveScalars *s)
 {
     if (ld_done(s))
         return;
@@ -188,27 +191,30 @@ __global__ void __launch_bounds__(kBlock) k_update_jacobi(int64_t n, const doubl
         xx.y += alpha * pp.y;
         rv.x += -alpha * qq.x;
         rv.y += -alpha * qq.y;
+        const double2 zz = make_double2(id.x * rv.x, id.y * rv.y);
         reinterpret_cast<double2 *>(x)[i] = xx;
         reinterpret_cast<double2 *>(r)[i] = rv;
+        reinterpret_cast<double2 *>(z)[i] = zz;
         acc[0] += rv.x * rv.x + rv.y * rv.y;
-        acc[1] += rv.x * (id.x * rv.x) + rv.y * (id.y * rv.y);
+        acc[1] += rv.x * zz.x + rv.y * zz.y;
     }
     if ((n & 1) && tid == 0) {
         const int64_t i = n - 1;
         x[i] += alpha * p[i];
         const double ri = r[i] + -alpha * Ap[i];
+        const double zi = invD[i] * ri;
         r[i] = ri;
+        z[i] = zi;
         acc[0] += ri * ri;
-        acc[1] += ri * (invD[i] * ri);
+        acc[1] += ri * zi;
     }
     if (grid_sum_last<2>(acc, partials, &s->counter[2]) && threadIdx.x == 0)
         finish_iteration(s, acc[0], acc[1], true);
 }
 
-// K3 (Jacobi): p = invD r + beta p.
-__global__ void __launch_bounds__(kBlock) k_pupdate_jacobi(int64_t n, const double *__restrict__ r,
-                                                           const double *__restrict__ invD, double *__restrict__ p,
-                                                           const SolveScalars *s)
+// K3: p = z + beta p (Jacobi and ILU0 alike).
+__global__ void __launch_bounds__(kBlock) k_pupdate(int64_t n, const double *__restrict__ z, double *__restrict__ p,
+                                                    const SolveScalars *s)
 {
     if (ld_done(s))
         return;
@@ -216,16 +222,15 @@ __global__ void __launch_bounds__(kBlock) k_pupdate_jacobi(int64_t n, const doub
     const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
     const int64_t n2 = n >> 1;
     for (int64_t i = tid; i < n2; i += stride) {
-        const double2 rv = reinterpret_cast<const double2 *>(r)[i];
-        const double2 id = reinterpret_cast<const double2 *>(invD)[i];
+        const double2 zz = reinterpret_cast<const double2 *>(z)[i];
         double2 pp = reinterpret_cast<double2 *>(p)[i];
-        pp.x = id.x * rv.x + beta * pp.x;
-        pp.y = id.y * rv.y + beta * pp.y;
+        pp.x = zz.x + beta * pp.x;
+        pp.y = zz.y + beta * pp.y;
         reinterpret_cast<double2 *>(p)[i] = pp;
     }
     if ((n & 1) && tid == 0) {
         const int64_t i = n - 1;
-        p[i] = invD[i] * r[i] + beta * p[i];
+        p[i] = z[i] + beta * p[i];
     }
 }
 
@@ -312,18 +317,6 @@ __global__ void __launch_bounds__(kBlock) k_rz_beta(int64_t n, const double *__r
             s->done = 1;
         }
     }
-}
-
-// K3: p = z + beta p.
-__global__ void __launch_bounds__(kBlock) k_pupdate_z(int64_t n, const double *__restrict__ z, double *__restrict__ p,
-                                                      const SolveScalars *s)
-{
-    if (ld_done(s))
-        return;
-    const double beta = __ldcg(&s->beta);
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t i = tid; i < n; i += stride)
-        p[i] = z[i] + beta * p[i];
 }
 
 // r = b - A x and ||r||^2 (FP64 true residual).
@@ -439,15 +432,13 @@ int enqueue_iteration(simall_solver *s)
             return st;
         k_rz_beta<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->z.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
-        k_pupdate_z<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
-        SIMALL_LAUNCH_CHECK(ctx);
     } else {
-        k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p,
+        k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p, s->z.p,
                                                        s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
-        k_pupdate_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->invDiag.p, s->p.p, s->scal.p);
-        SIMALL_LAUNCH_CHECK(ctx);
     }
+    k_pupdate<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
+    SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
 
@@ -866,12 +857,12 @@ int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms
             break;
         case 2:
             k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p,
-                                                           s->partials.p, s->scal.p);
-            b = 56.0 * nd;  // p, Ap, invD, x, r read; x, r written
+                                                           s->z.p, s->partials.p, s->scal.p);
+            b = 64.0 * nd;  // p, Ap, invD, x, r read; x, r, z written
             break;
         case 3:
-            k_pupdate_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->invDiag.p, s->p.p, s->scal.p);
-            b = 32.0 * nd;  // r, invD, p read; p written
+            k_pupdate<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
+            b = 24.0 * nd;  // z, p read; p written
             break;
         default:
             return mixed_enqueue_kernel(s, kernel, &b);

@@ -1,0 +1,104 @@
+"""Generate the golden fixtures in tests/golden/ from the reference's own code.
+
+Runs only where the reference tree is available (it needs
+oracle/_ref/libsimall_ref.so, built by oracle/build_ref.sh from the SimAll
+sources).  Every array stored here is an output of the reference's functions
+(CartesianMesher + ConnectivityBuilder + compute_geometry,
+renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
+assemble_pressure_correction, CGSolver::solve with Jacobi and ILU0, the
+preconditioners' apply, the SIMPLE cavity loop, solve_discrete_adjoint);
+inputs are seeded synthetic data.  The fixtures are small (a few hundred KB)
+so that the tests that read them run everywhere, the GPU host included.
+
+Usage:  python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from simall_gb300 import workloads as W  # noqa: E402
+
+R = O.RefLib()
+
+
+def mesh_case(name, dims, seed, amp, renumber, bcs, pressure_zones):
+    nx, ny, nz = dims
+    shift = W.interior_node_shift(nx, ny, nz, amp=amp, seed=seed) if amp else None
+    m = R.cartesian_mesh(nx, ny, nz, node_shift=shift, do_rcm=renumber)
+    rng = np.random.default_rng(seed + 100)
+    aP = rng.uniform(0.5, 2.0, m["nC"])
+    phi = rng.standard_normal(m["nF"])
+    phi[m["neighbor"] < 0] = 0.0
+    rp, ci, v, rhs = R.assemble(m, bcs, 1.0, aP, phi)
+    out = {k: m[k] for k in ("owner", "neighbor", "ax", "ay", "az", "fcx", "fcy", "fcz", "zone", "vol", "ccx", "ccy",
+                             "ccz", "cfOff", "cfIdx")}
+    out.update(dims=np.array(dims), seed=np.array(seed), amp=np.array(amp), renumber=np.array(int(renumber)),
+               pressure_zones=np.array(pressure_zones, np.int64), aP=aP, phi=phi, rowPtr=rp, colIdx=ci, values=v,
+               rhs=rhs)
+    if m["rcm_stats"]:
+        out["rcm_stats"] = np.array(m["rcm_stats"])
+    for pc, tag in ((0, "jacobi"), (1, "ilu0")):
+        x, it, last, _ = R.cg(rp, ci, v, rhs, pc, 1e-8, 2000)
+        out[f"cg_{tag}_x"] = x
+        out[f"cg_{tag}_iters"] = np.array(it)
+        out[f"cg_{tag}_last"] = np.array(last)
+        r = np.random.default_rng(seed + 200).standard_normal(len(rhs))
+        out[f"apply_{tag}_r"] = r
+        out[f"apply_{tag}_z"] = R.precond_apply(pc, rp, ci, v, r)
+    xx = np.random.default_rng(seed + 300).standard_normal(len(rhs))
+    out["spmv_x"] = xx
+    out["spmv_y"] = R.spmv(rp, ci, v, xx)
+    R.free_mesh(m)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+def cavity_case(name, N, n_outer, n_record):
+    c = R.cavity(N, mu=0.01, n_outer=n_outer, n_record=n_record, precond=0, tol=1e-8, max_it=1000)
+    np.savez_compressed(os.path.join(HERE, name), N=np.array(N), n_outer=np.array(n_outer), rowPtr=c["rowPtr"],
+                        colIdx=c["colIdx"], values=c["values"], rhs=c["rhs"], x=c["x"], aP=c["aP"], phi=c["phi"],
+                        iters=c["iters"], res=c["res"])
+
+
+def adjoint_case(name):
+    """solve_discrete_adjoint on a small face-conductance Poisson system."""
+    nx, ny, nz = 5, 4, 3
+    m = O.cartesian_mesh(nx, ny, nz, node_shift=W.interior_node_shift(nx, ny, nz, amp=0.1, seed=9))
+    rp, ci = O.build_sparsity(m)
+    rng = np.random.default_rng(9)
+    dirichlet = ((m.neighbor < 0) & (m.zone == 1)).astype(np.uint8)
+    k = np.exp(0.5 * rng.standard_normal(m.nF))
+    k[(m.neighbor < 0) & (dirichlet == 0)] = 0.0
+    pb = np.where(dirichlet == 1, rng.standard_normal(m.nF), 0.0)
+    src = rng.standard_normal(m.nC)
+    v, rhs, g = O.assemble_face_k(m, rp, ci, dirichlet, 1.0, k, pb, src)
+    x, it, last = O.cg(rp, ci, v, rhs, 0, 1e-14, 5000)
+    xt = rng.standard_normal(m.nC)
+    dJdQ = x - xt
+    psi, grad, its, res, rc = R.discrete_adjoint(rp, ci, v, dJdQ, m.owner, m.neighbor, dirichlet, g, k, pb, x,
+                                                 tol=1e-13, max_iter=2000, restart=30)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array([nx, ny, nz]), k=k, pb=pb, src=src,
+                        dirichlet=dirichlet, xt=xt, rowPtr=rp, colIdx=ci, values=v, rhs=rhs, g=g, x=x, psi=psi,
+                        grad=grad, iters=np.array(its), residual=np.array(res), ok=np.array(rc))
+
+
+def main():
+    mesh_case("box_6x5x4_distorted.npz", (6, 5, 4), 1, 0.2, False, [(z, 1) for z in range(1, 7)], [])
+    mesh_case("box_8x8x8_rcm_walls.npz", (8, 8, 8), 7, 0.2, True, [(z, 1) for z in range(1, 7)], [])
+    mesh_case("box_9x7x5_rcm_outlet.npz", (9, 7, 5), 3, 0.2, True,
+              [(1, 7)] + [(z, 1) for z in range(2, 7)], [1])
+    mesh_case("cavity_16x16x1_mesh.npz", (16, 16, 1), 5, 0.0, False, [(z, 1) for z in range(1, 7)], [])
+    cavity_case("cavity_simple_16.npz", 16, 6, 6)
+    adjoint_case("adjoint_face_k_5x4x3.npz")
+    print("fixtures written to", HERE)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,154 @@
+"""The oracle (oracle/simall_oracle.c) against the golden fixtures made from
+the reference's own code (tests/golden/make_golden.py) and against the
+known-answer tests of the reference's test suite.  Runs on any host."""
+import os
+
+import numpy as np
+import pytest
+
+from helpers import bits_equal, tridiag
+
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+MESH_CASES = ["box_6x5x4_distorted.npz", "box_8x8x8_rcm_walls.npz", "box_9x7x5_rcm_outlet.npz",
+              "cavity_16x16x1_mesh.npz"]
+
+
+def load(name):
+    return np.load(os.path.join(GOLD, name))
+
+
+def oracle_mesh(O, g):
+    from simall_gb300 import workloads as W
+
+    nx, ny, nz = (int(v) for v in g["dims"])
+    amp = float(g["amp"])
+    shift = W.interior_node_shift(nx, ny, nz, amp=amp, seed=int(g["seed"])) if amp else None
+    m = O.cartesian_mesh(nx, ny, nz, node_shift=shift)
+    if int(g["renumber"]):
+        _, st = O.rcm(m)
+        assert st == tuple(int(v) for v in g["rcm_stats"])
+    return m
+
+
+@pytest.mark.parametrize("case", MESH_CASES)
+def test_mesh_geometry_and_rcm_bit_exact(oracle, case):
+    g = load(case)
+    m = oracle_mesh(oracle, g)
+    for mine, ref in [("owner", "owner"), ("neighbor", "neighbor"), ("zone", "zone"), ("cfOff", "cfOff"),
+                      ("cfIdx", "cfIdx")]:
+        assert np.array_equal(getattr(m, mine), g[ref]), mine
+    for k in ("ax", "ay", "az", "fcx", "fcy", "fcz", "vol", "ccx", "ccy", "ccz"):
+        assert bits_equal(getattr(m, k), g[k]), k
+
+
+@pytest.mark.parametrize("case", MESH_CASES)
+def test_sparsity_and_assembly_bit_exact(oracle, case):
+    g = load(case)
+    m = oracle_mesh(oracle, g)
+    rp, ci = oracle.build_sparsity(m)
+    assert np.array_equal(rp, g["rowPtr"]) and np.array_equal(ci, g["colIdx"])
+    v, rhs, anyD = oracle.assemble(m, rp, ci, list(g["pressure_zones"]), 1.0, g["aP"], g["phi"])
+    assert bits_equal(v, g["values"]) and bits_equal(rhs, g["rhs"])
+    assert anyD == (len(g["pressure_zones"]) > 0)
+
+
+@pytest.mark.parametrize("case", MESH_CASES)
+@pytest.mark.parametrize("tag,pc", [("jacobi", 0), ("ilu0", 1)])
+def test_cg_and_preconditioners_bit_exact(oracle, case, tag, pc):
+    g = load(case)
+    rp, ci, v, rhs = g["rowPtr"], g["colIdx"], g["values"], g["rhs"]
+    x, it, last = oracle.cg(rp, ci, v, rhs, pc, 1e-8, 2000)
+    assert it == int(g[f"cg_{tag}_iters"])
+    assert last == float(g[f"cg_{tag}_last"])
+    assert bits_equal(x, g[f"cg_{tag}_x"])
+    r = g[f"apply_{tag}_r"]
+    if pc == 0:
+        z = oracle.jacobi_setup(rp, ci, v) * r
+    else:
+        lu, dp = oracle.ilu0_setup(rp, ci, v)
+        z = oracle.ilu0_apply(rp, ci, lu, dp, r)
+    assert bits_equal(z, g[f"apply_{tag}_z"])
+    assert bits_equal(oracle.spmv(rp, ci, v, g["spmv_x"]), g["spmv_y"])
+
+
+def test_cavity_simple_trajectory_systems(oracle):
+    """Each recorded outer iteration of the SIMPLE cavity (aP, phi -> A_p, b -> p')."""
+    c = load("cavity_simple_16.npz")
+    N = int(c["N"])
+    m = oracle.cartesian_mesh(N, N, 1, 1.0, 1.0, 1.0 / N)
+    rp, ci = oracle.build_sparsity(m)
+    assert np.array_equal(rp, c["rowPtr"]) and np.array_equal(ci, c["colIdx"])
+    for it in range(len(c["values"])):
+        v, rhs, anyD = oracle.assemble(m, rp, ci, [], 1.0, c["aP"][it], c["phi"][it])
+        assert not anyD
+        assert bits_equal(v, c["values"][it]) and bits_equal(rhs, c["rhs"][it])
+        x, its, last = oracle.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
+        assert its == int(c["iters"][it]) and last == float(c["res"][it])
+        assert bits_equal(x, c["x"][it])
+
+
+def test_face_conductance_adjoint_against_reference_gradient(oracle):
+    """Face-conductance assembly reproduced bit for bit; the adjoint gradient
+    (CG on A^T = A, then the scatter) matches solve_discrete_adjoint's."""
+    a = load("adjoint_face_k_5x4x3.npz")
+    from simall_gb300 import workloads as W
+
+    nx, ny, nz = (int(v) for v in a["dims"])
+    m = oracle.cartesian_mesh(nx, ny, nz, node_shift=W.interior_node_shift(nx, ny, nz, amp=0.1, seed=9))
+    rp, ci = oracle.build_sparsity(m)
+    v, rhs, g = oracle.assemble_face_k(m, rp, ci, a["dirichlet"], 1.0, a["k"], a["pb"], a["src"])
+    assert bits_equal(v, a["values"]) and bits_equal(rhs, a["rhs"]) and bits_equal(g, a["g"])
+    x, _, _ = oracle.cg(rp, ci, v, rhs, 0, 1e-14, 5000)
+    lam, _, _ = oracle.cg(rp, ci, v, x - a["xt"], 0, 1e-14, 5000)
+    assert np.linalg.norm(lam - a["psi"]) <= 1e-9 * np.linalg.norm(a["psi"])
+    dk, dpb = oracle.face_k_gradient(m, a["dirichlet"], g, a["k"], a["pb"], x, lam)
+    nF = m.nF
+    ref_dk = a["grad"][:nF]
+    ref_dpb = a["grad"][nF:]
+    assert np.allclose(dk, ref_dk, rtol=1e-7, atol=1e-9 * np.abs(ref_dk).max())
+    assert np.allclose(dpb[a["dirichlet"] == 1], ref_dpb, rtol=1e-7, atol=1e-9 * np.abs(ref_dpb).max())
+
+
+# ---------------------------------------------------------------- known answers of the reference test suite
+
+def test_blas1_known_answers(oracle):
+    """tests/unit/gpu/test_gpu_models.cpp:117-141 (dot(1..5) = 55)."""
+    x = np.arange(1, 6, dtype=np.float64)
+    assert oracle.dot(x, x) == 55.0
+
+
+def test_spmv_4x4_known_answer(oracle):
+    """tests/unit/gpu/test_gpu_models.cpp:144-178."""
+    rp = np.array([0, 2, 5, 8, 10], np.int32)
+    ci = np.array([0, 1, 0, 1, 2, 1, 2, 3, 2, 3], np.int32)
+    va = np.array([4, -1, -1, 4, -1, -1, 4, -1, -1, 4], np.float64)
+    assert oracle.spmv(rp, ci, va, np.arange(1, 5, dtype=np.float64)).tolist() == [2.0, 4.0, 6.0, 13.0]
+
+
+def test_cg_tridiagonal_known_answer(oracle):
+    """tests/unit/gpu/test_gpu_models.cpp:181-235."""
+    rp, ci, va = tridiag(10)
+    b = np.zeros(10)
+    b[0] = b[-1] = 1.0
+    x, it, last = oracle.cg(rp, ci, va, b, 0, 1e-10, 200)
+    assert it < 50 and last < 1e-10
+    assert np.linalg.norm(b - oracle.spmv(rp, ci, va, x)) < 1e-8
+
+
+@pytest.mark.parametrize("pc", [0, 1])
+def test_cg_1d_laplacian(oracle, pc):
+    """tests/unit/solver/test_ssor_preconditioner.cpp:65-88 (1-D Laplacian,
+    n=50, b=1, tol 1e-10), with the preconditioners on this path."""
+    rp, ci, va = tridiag(50, -1.0, 2.0, -1.0)
+    b = np.ones(50)
+    x, it, last = oracle.cg(rp, ci, va, b, pc, 1e-10, 200)
+    assert it > 0 and np.linalg.norm(oracle.spmv(rp, ci, va, x) - b) < 1e-7
+
+
+@pytest.mark.parametrize("dims", [(4, 1, 1), (3, 3, 3)])
+def test_rcm_never_increases_bandwidth(oracle, dims):
+    """tests/unit/meshing/test_mesh_ops.cpp:168-199."""
+    m = oracle.cartesian_mesh(*dims, ex=float(dims[0]), ey=float(dims[1]), ez=float(dims[2]))
+    _, (before, after, permuted) = oracle.rcm(m)
+    assert permuted == m.nC and after <= before
+    assert np.all(m.owner < m.nC) and np.all(m.neighbor < m.nC)

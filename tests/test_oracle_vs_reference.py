@@ -1,0 +1,75 @@
+"""The oracle against the reference's own code, live (oracle/_ref, built from
+the reference sources by oracle/build_ref.sh).  Skipped where the compiled
+reference is absent."""
+import numpy as np
+import pytest
+
+from helpers import bits_equal
+
+
+def _shift(dims, seed, amp):
+    from simall_gb300 import workloads as W
+
+    return W.interior_node_shift(*dims, amp=amp, seed=seed) if amp else None
+
+
+@pytest.mark.parametrize("dims,seed,amp,renumber", [((5, 4, 3), 1, 0.2, False), ((7, 7, 7), 2, 0.2, True),
+                                                    ((12, 5, 9), 3, 0.15, True), ((20, 20, 1), 4, 0.0, False)])
+def test_mesh_rcm_assembly_cg(oracle, ref, dims, seed, amp, renumber):
+    sh = _shift(dims, seed, amp)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        _, st = oracle.rcm(m)
+        assert st == r["rcm_stats"]
+    for k in ("owner", "neighbor", "zone", "cfOff", "cfIdx"):
+        assert np.array_equal(getattr(m, k), r[k]), k
+    for k in ("ax", "ay", "az", "fcx", "fcy", "fcz", "vol", "ccx", "ccy", "ccz"):
+        assert bits_equal(getattr(m, k), r[k]), k
+    rng = np.random.default_rng(seed)
+    aP = rng.uniform(0.3, 3.0, m.nC)
+    phi = rng.standard_normal(m.nF)
+    for bcs, pz in (([], []), ([(1, 7), (2, 5)], [1, 2])):
+        rp, ci, v, rhs = ref.assemble(r, bcs, 1.3, aP, phi)
+        orp, oci = oracle.build_sparsity(m)
+        ov, orhs, _ = oracle.assemble(m, orp, oci, pz, 1.3, aP, phi)
+        assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+        assert bits_equal(v, ov) and bits_equal(rhs, orhs)
+        for pc in (0, 1):
+            x, it, last, _ = ref.cg(rp, ci, v, rhs, pc, 1e-9, 3000)
+            ox, oit, olast = oracle.cg(rp, ci, v, rhs, pc, 1e-9, 3000)
+            assert it == oit and last == olast and bits_equal(x, ox)
+    ref.free_mesh(r)
+
+
+def test_precond_none_maps_to_jacobi(oracle, ref):
+    """make_preconditioner's default branch (LinearSolvers.cpp:240-254)."""
+    r = ref.cartesian_mesh(4, 4, 4)
+    rp, ci, v, rhs = ref.assemble(r, [], 1.0, np.ones(64), np.random.default_rng(0).standard_normal(r["nF"]))
+    z = np.random.default_rng(1).standard_normal(64)
+    assert bits_equal(ref.precond_apply(4, rp, ci, v, z), ref.precond_apply(0, rp, ci, v, z))
+    ref.free_mesh(r)
+
+
+def test_cavity_trajectory_longer(oracle, ref):
+    c = ref.cavity(24, mu=0.01, n_outer=4, n_record=4, precond=1, tol=1e-8, max_it=1000)
+    m = oracle.cartesian_mesh(24, 24, 1, 1.0, 1.0, 1.0 / 24)
+    rp, ci = oracle.build_sparsity(m)
+    for it in range(4):
+        v, rhs, _ = oracle.assemble(m, rp, ci, [], 1.0, c["aP"][it], c["phi"][it])
+        assert bits_equal(v, c["values"][it]) and bits_equal(rhs, c["rhs"][it])
+        x, its, last = oracle.cg(rp, ci, v, rhs, 1, 1e-8, 1000)
+        assert its == c["iters"][it] and bits_equal(x, c["x"][it])
+
+
+def test_discrete_adjoint_2x2_known_answer(ref):
+    """tests/unit/longtail/test_longtail_modules.cpp:32-54: A = [[2,1],[0,3]],
+    dJ/dQ = (1,1) -> psi = (0.5, 1/6)."""
+    rp = np.array([0, 2, 3], np.int32)
+    ci = np.array([0, 1, 1], np.int32)
+    va = np.array([2.0, 1.0, 3.0])
+    psi, grad, its, res, rc = ref.discrete_adjoint(rp, ci, va, np.ones(2), np.zeros(0, np.int64),
+                                                   np.zeros(0, np.int64), np.zeros(0, np.int32), np.zeros(0),
+                                                   np.zeros(0), np.zeros(0), np.zeros(2))
+    assert rc == 0
+    assert abs(psi[0] - 0.5) < 1e-6 and abs(psi[1] - 1.0 / 6.0) < 1e-6
