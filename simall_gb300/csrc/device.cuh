@@ -16,6 +16,14 @@ __device__ __forceinline__ double warp_sum(double v)
     return v;  // valid in lane 0
 }
 
+__device__ __forceinline__ float warp_sum_f(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_down_sync(0xffffffffu, v, o);
+    return v;  // valid in lane 0
+}
+
 // Sum of NV values over the block in a fixed tree; the result is valid in
 // thread 0.  Every thread of the block must call it.
 template <int NV> __device__ __forceinline__ void block_sum(double (&v)[NV])
@@ -76,6 +84,44 @@ template <int NV> __device__ __forceinline__ bool grid_sum_last(double (&v)[NV],
     return true;
 }
 
+// grid_sum_last for FP32 per-thread partials: the 32 lanes of a warp are
+// summed in FP32 (one warp's worth of a partial sum), every sum above the warp
+// -- across warps, CTAs and the grid -- is FP64.  On GB300 a double-precision
+// shuffle tree per thread costs more FP64-pipe time than the FP32 streaming
+// kernels it would finish.
+__device__ __forceinline__ bool grid_sum_last_f(float v, double *partials, unsigned *ticket, double &total)
+{
+    __shared__ double wsum[32];
+    __shared__ unsigned s_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+    v = warp_sum_f(v);
+    if (lane == 0)
+        wsum[wid] = static_cast<double>(v);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double b = 0.0;
+        for (int w = 0; w < nw; ++w)
+            b += wsum[w];
+        partials[blockIdx.x] = b;
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last)
+        return false;
+    __threadfence();
+    double acc[1] = {0.0};
+    for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+        acc[0] += __ldcg(&partials[b]);
+    block_sum<1>(acc);
+    if (threadIdx.x == 0) {
+        total = acc[0];
+        *ticket = 0u;
+    }
+    return true;
+}
+
 // y-rows of A x for the row-blocks this CTA owns (blockIdx.x, +gridDim.x, ...).
 // Each product a_ij*x_j is rounded once into shared memory and every row is
 // summed from 0.0 in column order with separate roundings, the same operation
@@ -92,8 +138,27 @@ __device__ __forceinline__ void spmv_rowblocks(const int32_t *__restrict__ rowPt
         const int base = __ldg(rowPtr + r0);
         const int cnt = __ldg(rowPtr + r1) - base;
         if (cnt <= kSpmvNnzCap) {
-            for (int k = threadIdx.x; k < cnt; k += blockDim.x)
-                prod[k] = __dmul_rn(__ldg(val + base + k), __ldg(x + __ldg(colIdx + base + k)));
+            // every load of this thread's slots is issued before any is used
+            constexpr int J = kSpmvNnzCap / kBlock;
+            int c[J];
+            double a[J], g[J];
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                c[j] = k < cnt ? __ldg(colIdx + base + k) : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                a[j] = k < cnt ? __ldg(val + base + k) : 0.0;
+                g[j] = k < cnt ? __ldg(x + c[j]) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                if (k < cnt)
+                    prod[k] = __dmul_rn(a[j], g[j]);
+            }
             __syncthreads();
             for (int row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
                 const int k0 = __ldg(rowPtr + row) - base, k1 = __ldg(rowPtr + row + 1) - base;
@@ -116,8 +181,8 @@ __device__ __forceinline__ void spmv_rowblocks(const int32_t *__restrict__ rowPt
     }
 }
 
-// Same row-blocks, fused multiply-add form: a_ij and j are staged in shared
-// memory with coalesced loads, then each row is accumulated with one FMA per
+// Same row-blocks, fused multiply-add form: a_ij and the gathered x_j are
+// staged in shared memory, then each row is accumulated with one FMA per
 // nonzero.  Half the FP64 instructions of the exact form (GB300's FP64 rate
 // is low enough for that to matter); the sum differs from CSRMatrix::spmv
 // only in rounding.
@@ -128,22 +193,41 @@ __device__ __forceinline__ void spmv_rowblocks_fma(const int32_t *__restrict__ r
                                                    int nRB, const double *__restrict__ x, Epi &epi)
 {
     __shared__ double sv[kSpmvNnzCap];
-    __shared__ int32_t sc[kSpmvNnzCap];
+    __shared__ double sx[kSpmvNnzCap];
     for (int b = blockIdx.x; b < nRB; b += gridDim.x) {
         const int r0 = __ldg(rb + b), r1 = __ldg(rb + b + 1);
         const int base = __ldg(rowPtr + r0);
         const int cnt = __ldg(rowPtr + r1) - base;
         if (cnt <= kSpmvNnzCap) {
-            for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-                sv[k] = __ldg(val + base + k);
-                sc[k] = __ldg(colIdx + base + k);
+            // stage a_ij and the gathered x_j; all loads issued before use
+            constexpr int J = kSpmvNnzCap / kBlock;
+            int c[J];
+            double a[J], g[J];
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                c[j] = k < cnt ? __ldg(colIdx + base + k) : 0;
+            }
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                a[j] = k < cnt ? __ldg(val + base + k) : 0.0;
+                g[j] = k < cnt ? __ldg(x + c[j]) : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < J; ++j) {
+                const int k = threadIdx.x + j * kBlock;
+                if (k < cnt) {
+                    sv[k] = a[j];
+                    sx[k] = g[j];
+                }
             }
             __syncthreads();
             for (int row = r0 + threadIdx.x; row < r1; row += blockDim.x) {
                 const int k0 = __ldg(rowPtr + row) - base, k1 = __ldg(rowPtr + row + 1) - base;
                 double s = 0.0;
                 for (int k = k0; k < k1; ++k)
-                    s = fma(sv[k], __ldg(x + sc[k]), s);
+                    s = fma(sv[k], sx[k], s);
                 epi(row, s);
             }
             __syncthreads();

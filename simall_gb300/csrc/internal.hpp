@@ -25,7 +25,8 @@ namespace simall {
 
 constexpr int kBlock = 256;        // threads per CTA for the streaming kernels
 constexpr int kSpmvRows = 256;     // max rows of one SpMV row-block
-constexpr int kSpmvNnzCap = 2048;  // max nonzeros staged per row-block (16 KB of FP64 products)
+constexpr int kSpmvNnzCap = 2048;  // max nonzeros staged per row-block (16 KB of FP64 per staged array)
+static_assert(kSpmvNnzCap % kBlock == 0, "row-block staging assumes whole slots per thread");
 constexpr int kMaxReduce = 4;      // values reduced together by one kernel
 
 int fail(simall_context *ctx, int status, const char *fmt, ...);

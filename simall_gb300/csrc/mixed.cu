@@ -216,9 +216,11 @@ __device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
 
 // K1 (dia): qh = (S A S) ph, pq = ph.qh.  ND upper diagonals at ascending
 // offsets; row i reads U_d[i] x_{i+off} and, by symmetry, U_d[i-off] x_{i-off}.
-// One thread per 4 consecutive rows with 128-bit loads of every 16-byte
-// aligned stream; rows within the largest offset of either end of the
-// matrix take the bounds-checked path.
+// One thread per 4 consecutive rows, a warp per 128 consecutive rows, with
+// 128-bit loads of every 16-byte aligned stream.  The unit-offset diagonal
+// (every natural-order grid has one) takes x_{i-1}, x_{i+4} and U_0[i-1] from
+// the neighbouring lanes' registers instead of 12 unaligned loads.  Warps
+// that touch the first or last maxoff rows take the bounds-checked path.
 template <int ND>
 __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
                                                         const float *__restrict__ ph, float *__restrict__ qh,
@@ -229,29 +231,43 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaO
     float acc = 0.0f;
     const int nq = (n + 3) >> 2;
     const int maxoff = o.off[ND - 1];
-    bool al[ND];
-#pragma unroll
-    for (int d = 0; d < ND; ++d)
-        al[d] = (o.off[d] & 3) == 0;
-    for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < nq; q += gridDim.x * blockDim.x) {
+    const int lane = threadIdx.x & 31;
+    const int stride = gridDim.x * blockDim.x;
+    for (int q0 = blockIdx.x * blockDim.x + threadIdx.x - lane; q0 < nq; q0 += stride) {
+        const int q = q0 + lane;
         const int i = q << 2;
-        float y[4];
-        if (i >= maxoff && i + 3 + maxoff < n) {
+        const bool fast = q < nq && i >= maxoff && i + 3 + maxoff < n;
+        if (__all_sync(0xffffffffu, fast)) {
             const float4 p4 = __ldg(reinterpret_cast<const float4 *>(ph + i));
-            y[0] = p4.x;
-            y[1] = p4.y;
-            y[2] = p4.z;
-            y[3] = p4.w;
+            float y[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
             for (int d = 0; d < ND; ++d) {
                 const int off = o.off[d];
                 const float *Ud = U + d * ldU;
-                fma4(y, __ldg(reinterpret_cast<const float4 *>(Ud + i)), ld4(ph + i + off, al[d]));
-                fma4(y, ld4(Ud + i - off, al[d]), ld4(ph + i - off, al[d]));
+                const float4 u = __ldg(reinterpret_cast<const float4 *>(Ud + i));
+                if (off == 1) {
+                    float xn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // x[i+4]
+                    float xp = __shfl_up_sync(0xffffffffu, p4.w, 1);    // x[i-1]
+                    float up = __shfl_up_sync(0xffffffffu, u.w, 1);     // U_0[i-1]
+                    if (lane == 31)
+                        xn = __ldg(ph + i + 4);
+                    if (lane == 0) {
+                        xp = __ldg(ph + i - 1);
+                        up = __ldg(Ud + i - 1);
+                    }
+                    y[0] += u.x * p4.y + up * xp;
+                    y[1] += u.y * p4.z + u.x * p4.x;
+                    y[2] += u.z * p4.w + u.y * p4.y;
+                    y[3] += u.w * xn + u.z * p4.z;
+                } else {
+                    const bool al = (off & 3) == 0;
+                    fma4(y, u, ld4(ph + i + off, al));
+                    fma4(y, ld4(Ud + i - off, al), ld4(ph + i - off, al));
+                }
             }
             *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
             acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
-        } else {
+        } else if (q < nq) {
             for (int r = 0; r < 4; ++r) {
                 const int row = i + r;
                 if (row >= n)
@@ -272,9 +288,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaO
             }
         }
     }
-    double v[1] = {static_cast<double>(acc)};
-    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0)
-        mx_alpha(s, v[0]);
+    double total;
+    if (grid_sum_last_f(acc, partials, &s->counter[1], total) && threadIdx.x == 0)
+        mx_alpha(s, total);
 }
 
 // K1 (csr): qh = ph + offdiag(S A S) ph, pq = ph.qh.  Thread per row.
@@ -294,9 +310,9 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_csr(int64_t n, const int32_t
         qh[i] = y;
         acc += pi * y;
     }
-    double v[1] = {static_cast<double>(acc)};
-    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0)
-        mx_alpha(s, v[0]);
+    double total;
+    if (grid_sum_last_f(acc, partials, &s->counter[1], total) && threadIdx.x == 0)
+        mx_alpha(s, total);
 }
 
 // K2: xh += alpha ph, rh -= alpha qh, rr = rh.rh; decide on a reliable update.
@@ -333,9 +349,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_update(int64_t n, const float *__
         rh[i] = r;
         acc += r * r;
     }
-    double v[1] = {static_cast<double>(acc)};
-    if (grid_sum_last<1>(v, partials, &s->counter[2]) && threadIdx.x == 0) {
-        const double rr = v[0];
+    double rr;
+    if (grid_sum_last_f(acc, partials, &s->counter[2], rr) && threadIdx.x == 0) {
         s->iter += 1;
         const double sigma = sqrt(rr);
         const double est = s->t0 * sigma / s->sigma0;
@@ -416,9 +431,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_replace(int64_t n, const double *
         rh[i] = v;
         acc += v * v;
     }
-    double a[1] = {static_cast<double>(acc)};
-    if (grid_sum_last<1>(a, partials, &s->counter[4]) && threadIdx.x == 0) {
-        const double rho = a[0];
+    double rho;
+    if (grid_sum_last_f(acc, partials, &s->counter[4], rho) && threadIdx.x == 0) {
         s->beta = rho / s->rz;
         s->rz = rho;
         s->sigma0 = sqrt(rho);
