@@ -9,7 +9,8 @@
 #   src/solver/Gradient.cpp, src/meshing/MeshStorage.cpp,
 #   src/meshing/CartesianMesher.cpp, src/meshing/Connectivity.cpp,
 #   src/meshing/MeshOps.cpp, src/meshing/MeshQuality.cpp,
-#   src/adjoint/DiscreteAdjoint.cpp
+#   src/adjoint/DiscreteAdjoint.cpp, src/core/PluginLoader.cpp,
+#   src/core/PluginRegistry.cpp
 #
 # Patch: LinearSolvers.cpp assigns util::aligned_vector<int> to std::vector<int>
 # at :85-86 and :170-171, which g++ 13 rejects.  A scratch copy written into
@@ -42,6 +43,8 @@ $REF/src/meshing/Connectivity.cpp
 $REF/src/meshing/MeshOps.cpp
 $REF/src/meshing/MeshQuality.cpp
 $REF/src/adjoint/DiscreteAdjoint.cpp
+$REF/src/core/PluginLoader.cpp
+$REF/src/core/PluginRegistry.cpp
 $HERE/ref_driver.cpp"
 pids=""
 objs=""
@@ -54,6 +57,6 @@ for s in $SRCS; do
     i=$((i + 1))
 done
 for p in $pids; do wait "$p"; done
-$CXX -shared -o "$OUT/libsimall_ref.so.tmp" $objs -lpthread
+$CXX -shared -o "$OUT/libsimall_ref.so.tmp" $objs -lpthread -ldl
 mv "$OUT/libsimall_ref.so.tmp" "$OUT/libsimall_ref.so"
 echo "built $OUT/libsimall_ref.so"

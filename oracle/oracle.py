@@ -310,6 +310,8 @@ class RefLib:
         L.ref_cavity_run.restype = C.c_int
         L.ref_cavity_run.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P]
         L.ref_cavity_fetch.argtypes = [_P] * 9
+        L.ref_plugin_load.restype = _I64
+        L.ref_plugin_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int)]
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -440,6 +442,14 @@ class RefLib:
                                                       "iters", "res")))
         out["p_solve_seconds"] = secs.value
         return out
+
+    def plugin_load(self, path: str):
+        """core::PluginLoader::load of a plugin library; (cookie, name, version, category)."""
+        name = C.create_string_buffer(256)
+        ver = C.create_string_buffer(64)
+        cat = C.c_int(-1)
+        cookie = self.L.ref_plugin_load(path.encode(), name, 256, ver, 64, C.byref(cat))
+        return int(cookie), name.value.decode(), ver.value.decode(), cat.value
 
     def discrete_adjoint(self, rowPtr, colIdx, values, dJdQ, owner, neighbor, is_dirichlet, g, k, pb, x,
                          tol=1e-10, max_iter=500, restart=30):

@@ -13,7 +13,10 @@
 //   SimpleAlgorithm::iterate                src/solver/SimpleAlgorithm.cpp:522
 //   make_cg / make_gmres / make_preconditioner     src/solver/LinearSolvers.cpp:240,462
 //   adjoint::solve_discrete_adjoint         src/adjoint/DiscreteAdjoint.cpp:150
+//   core::PluginLoader::load / PluginRegistry  src/core/PluginLoader.cpp:68, PluginRegistry.cpp:23
 #include "adjoint/DiscreteAdjoint.hpp"
+#include "core/PluginLoader.hpp"
+#include "core/PluginRegistry.hpp"
 #include "meshing/CartesianMesher.hpp"
 #include "meshing/MeshOps.hpp"
 #include "meshing/MeshStorage.hpp"
@@ -24,6 +27,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <memory>
 #include <vector>
@@ -416,6 +420,30 @@ int ref_discrete_adjoint(int n, const int* rowPtr, const int* colIdx, const doub
     *itersOut = static_cast<std::int64_t>(r2.iterations);
     *resOut = r2.residual;
     return r2.ok ? 0 : 1;
+}
+
+// ------------------------------------------------------------------ plugin ABI
+// Loads a plugin library with the reference's PluginLoader (dlopen, ABI
+// check, CreatePlugin, on_load, PluginRegistry::register_auto).  Returns the
+// loader cookie (0 on failure); name/version/category describe what the
+// registry now holds for it (category -1 if it is in no bucket).
+std::int64_t ref_plugin_load(const char *path, char *name, int nameLen, char *version, int versionLen,
+                             int *category)
+{
+    static simall::core::PluginLoader loader;  // keeps the plugin loaded
+    const std::size_t cookie = loader.load(path);
+    *category = -1;
+    if (!cookie)
+        return 0;
+    auto &reg = simall::core::PluginRegistry::instance();
+    for (int c = 0; c < static_cast<int>(simall::plugins::PluginCategory::_Count); ++c)
+        for (auto *p : reg.by_category(static_cast<simall::plugins::PluginCategory>(c))) {
+            const std::string nm = p->name(), vs = p->version();
+            std::snprintf(name, static_cast<std::size_t>(nameLen), "%s", nm.c_str());
+            std::snprintf(version, static_cast<std::size_t>(versionLen), "%s", vs.c_str());
+            *category = c;
+        }
+    return static_cast<std::int64_t>(cookie);
 }
 
 } // extern "C"

@@ -1,0 +1,38 @@
+"""The drop-in boundary as a SimAll host sees it: the reference's own
+PluginLoader loads libsimall_gpu.so (plugins/IPlugin.hpp ABI v1) and files it
+under the Gpu category, and the header-only ILinearSolver adapter
+(include/simall_gpu_solver.hpp) compiles against SimAll's headers and solves
+through the library."""
+import os
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+REFERENCE_SRC = "/root/reference/src"
+ADAPTER_TEST = os.path.join(ROOT, "tests", "cpp", "adapter_main.cpp")
+
+
+def test_reference_plugin_loader_accepts_library(sg, ref):
+    cookie, name, version, category = ref.plugin_load(sg._lib.lib_path())
+    assert cookie > 0
+    assert name == "simall_gb300_pressure" and version
+    assert category == 23  # PluginCategory::Gpu, plugins/SimAllPluginSdk.hpp:96
+
+
+def test_adapter_compiles_against_reference_headers():
+    if not os.path.isdir(REFERENCE_SRC):
+        pytest.skip("SimAll source tree not present")
+    subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Werror", f"-I{REFERENCE_SRC}",
+                    f"-I{os.path.dirname(REFERENCE_SRC)}", f"-I{ROOT}/include", ADAPTER_TEST], check=True)
+
+
+@pytest.mark.gpu
+def test_adapter_solves_through_the_library(sg, tmp_path):
+    lib = sg._lib.lib_path()
+    exe = str(tmp_path / "adapter_main")
+    subprocess.run(["g++", "-std=c++20", "-O1", f"-I{ROOT}/tests/cpp/standin", f"-I{ROOT}/include", ADAPTER_TEST,
+                    "-o", exe, lib, f"-Wl,-rpath,{os.path.dirname(lib)}"], check=True)
+    r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert r.stdout.count(" ok") == 3
