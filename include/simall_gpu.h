@@ -225,6 +225,19 @@ int simall_gpu_axpby(double a, const double *x, double b, double *y, size_t n, v
 int simall_gpu_xpby(const double *x, double beta, double *y, size_t n, void *stream);
 int simall_gpu_spmv_csr(size_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
                         const double *x, double *y, void *stream);
+/* Dot product that allocates no device memory.  It has no counterpart in the
+ * reference: it exists for callers that must not call cudaMalloc -- code whose
+ * device memory is already fully owned by another allocator, loops that cannot
+ * take cudaMalloc's implicit synchronisation, processes that keep a fixed
+ * device footprint after start-up.  Its reduction scratch is a fixed array
+ * inside this library (reserved on every GPU that loads the library, until the
+ * process exits), which limits n to SIMALL_DOT_NOALLOC_MAX_N; larger n returns
+ * SIMALL_ERR_SIZE_MISMATCH.  The first call on each device looks the array's
+ * address up (cudaGetSymbolAddress); make it before any stream capture.  All
+ * calls share the array, so calls that overlap on the GPU race.  Blocks the
+ * host like simall_gpu_dot. */
+#define SIMALL_DOT_NOALLOC_MAX_N 16777216
+int simall_gpu_dot_noalloc(const double *x, const double *y, size_t n, void *stream, double *result);
 /* z[i] = r[i] / diag[i]  (GpuKernels.hpp:87) */
 int simall_gpu_jacobi_apply(const double *diag, const double *r, double *z, size_t n, void *stream);
 /* In-place ILU(0) of device CSR values (GpuKernels.hpp:89-97); *ok = 0 on a
