@@ -60,6 +60,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-systems", type=int, default=512,
+                    help="systems in the batched leg (0 disables it)")
     return ap.parse_args()
 
 
@@ -181,6 +183,69 @@ def time_kernel(s, k, reps=20):
     return ms.value, by.value
 
 
+def run_batched(a, ctx, sg):
+    """Batched leg: `count` cavity pressure systems (sides log-uniform in
+    [32, 256], rhs N(0,1) with mean removed, one pinned cell) solved in one
+    persistent launch (mixed precision) against a loop of plain FP64
+    Jacobi-PCG solves of the same systems with the matrices resident."""
+    import torch
+    from simall_gb300 import workloads as W
+
+    count = a.batched_systems
+    t0 = time.perf_counter()
+    systems, rhs, sides = W.batched_cavity_systems(count=count, seed=SEED, ctx=ctx)
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                tolerance=a.tol, maxIterations=a.max_iterations)
+    B = sg.BatchedSolver(cfg, ctx=ctx)
+    rows = B.set_systems(systems)
+    b = torch.from_numpy(np.concatenate(rhs)).cuda()
+    x = torch.empty_like(b)
+    setup = time.perf_counter() - t0
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    for _ in range(max(1, a.warmup)):
+        B.solve(b, x, per_system=False)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(a.steps):
+        _, st = B.solve(b, x)
+    e1.record(stream)
+    e1.synchronize()
+    batch_ms = e0.elapsed_time(e1) / a.steps
+    tot = B.total
+    # baseline: one FP64 solver per system, matrix resident, solves in a loop
+    solvers, bs, xs = [], [], []
+    for (rp, ci, va), r in zip(systems, rhs):
+        s = sg.GpuCGSolver(cfg, precision=sg.Precision.FP64, ctx=ctx)
+        s.set_matrix(rp, ci, va)
+        solvers.append(s)
+        bs.append(torch.from_numpy(r).cuda())
+        xs.append(torch.empty_like(bs[-1]))
+    for s, bb, xx in zip(solvers, bs, xs):  # warm (graph capture per solver)
+        s.solve_into(bb, xx)
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    its = 0
+    for s, bb, xx in zip(solvers, bs, xs):
+        its += s.solve_into(bb, xx)
+    torch.cuda.synchronize()
+    loop_s = time.perf_counter() - t
+    xb = x.cpu().numpy()
+    diff = max(float(np.linalg.norm(xb[rows[i]:rows[i + 1]] - xs[i].cpu().numpy()) /
+                     max(np.linalg.norm(xs[i].cpu().numpy()), 1e-30)) for i in range(len(systems)))
+    for s in solvers:
+        s.close()
+    return {"workload": f"{count} cavity pressure systems, sides log-uniform [32,256] (seed {SEED}), "
+                        f"{int(rows[-1])} rows", "value": round(batch_ms / 1e3, 6), "unit": "s",
+            "fp64_loop": {"value": round(loop_s, 4), "unit": "s", "iterations": int(its)},
+            "speedup_vs_fp64_loop": round(loop_s / (batch_ms / 1e3), 2),
+            "converged": int(tot.converged), "systems": int(tot.systems), "max_iterations": int(tot.max_iterations),
+            "total_iterations": int(tot.total_iterations), "worst_true_residual": float(tot.worst_true_residual),
+            "max_rel_diff_vs_fp64": diff, "launch_shape": [int(tot.block_threads), int(tot.ctas_per_sm)],
+            "setup_seconds": round(setup, 2)}
+
+
 def run_ours(a, rank, world, local):
     import torch
 
@@ -295,6 +360,8 @@ def run_ours(a, rank, world, local):
         "clocks": clocks,
         "setup_seconds": round(setup_s, 2),
     }
+    if a.batched_systems > 0:
+        out["batched"] = run_batched(a, ctx, sg)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
         out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,

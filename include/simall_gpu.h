@@ -212,6 +212,51 @@ int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *
 int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,
                                  simall_solver_stats *stats);
 
+/* ------------------------------------------------------------------ batched solves */
+/* Many independent SPD systems of uneven size (e.g. one pressure-correction
+ * system per cavity, block or time level) solved in one persistent launch:
+ * the work loop a caller would write around CGSolver::solve
+ * (src/solver/LinearSolvers.cpp:420-451), with the mixed-precision Jacobi-PCG
+ * of simall_solver (FP32 inner iteration, FP64 true residual, reductions and
+ * x) run by one CTA per system.  Systems are given concatenated: system s owns
+ * rows [row_offsets[s], row_offsets[s+1]) and nonzeros [nnz_offsets[s],
+ * nnz_offsets[s+1]); its rowPtr (local, starting at 0, n_s+1 entries) starts at
+ * rowPtr[row_offsets[s] + s]; colIdx are local.  b and x are concatenated
+ * by rows. */
+typedef struct simall_batch simall_batch;
+typedef struct simall_batch_system_stats {
+    int iterations;
+    int reliable_updates;
+    int converged;
+    int status;
+    double true_residual; /* ||b - A x|| / max(||b||, 1e-30) of the returned x, FP64 */
+    double b_norm;
+} simall_batch_system_stats;
+typedef struct simall_batch_stats {
+    int systems;
+    int converged;
+    int max_iterations;
+    int status;               /* SIMALL_OK, or the status of a system that did not converge */
+    int64_t total_iterations;
+    double worst_true_residual;
+    int block_threads;        /* launch shape in use (autotuned unless set) */
+    int ctas_per_sm;
+    double seconds;
+} simall_batch_stats;
+/* cfg: tolerance, max_iterations, reliable_delta as for simall_solver (Jacobi). */
+int simall_batch_create(simall_context *ctx, const simall_solver_config *cfg, simall_batch **out);
+int simall_batch_destroy(simall_batch *b);
+/* Host arrays; validated, scaled and stored on the device. */
+int simall_batch_set_systems(simall_batch *b, int n_systems, const int64_t *row_offsets, const int64_t *nnz_offsets,
+                             const int32_t *rowPtr, const int32_t *colIdx, const double *values);
+/* Solves every system from x = 0.  per_system (optional) has n_systems entries. */
+int simall_batch_solve(simall_batch *b, const double *rhs, double *x, int mem, simall_batch_system_stats *per_system,
+                       simall_batch_stats *total);
+/* Fixes the launch shape (256/512/1024 threads per CTA, 1-8 CTAs per SM);
+ * block_threads == 0 re-enables the autotuner, which times the candidate
+ * shapes on the batch at its next solve and keeps the fastest. */
+int simall_batch_launch_shape(simall_batch *b, int block_threads, int ctas_per_sm);
+
 /* ------------------------------------------------------------------ reference GPU facade */
 /* One-for-one replacements of src/gpu/GpuKernels.hpp:48-108 on device
  * pointers (stream == NULL: the legacy default stream).  dot and nrm2 block

@@ -6,11 +6,12 @@ preconditioned CG solve on it, as hand-written CUDA kernels behind a C ABI
 mirror of the reference's solver interface plus the mesh/assembly wrappers.
 """
 from . import build
+from .batch import BatchedSolver
 from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
 from .solver import (Context, CSRMatrix, GpuCGSolver, LinearSolverConfig, LinearSolverKind, Precision,
                      PreconditionerKind, default_context, make_cg, make_linear_solver)
 
-__all__ = ["build", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
+__all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver"]

@@ -46,6 +46,17 @@ class MeshView(C.Structure):
                 ("cell_face_offsets", _P), ("cell_face_indices", _P)]
 
 
+class BatchSystemStats(C.Structure):
+    _fields_ = [("iterations", _I), ("reliable_updates", _I), ("converged", _I), ("status", _I),
+                ("true_residual", _D), ("b_norm", _D)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("systems", _I), ("converged", _I), ("max_iterations", _I), ("status", _I),
+                ("total_iterations", _I64), ("worst_true_residual", _D), ("block_threads", _I),
+                ("ctas_per_sm", _I), ("seconds", _D)]
+
+
 class Boundary(C.Structure):
     _fields_ = [("zone", C.c_uint32), ("type", _I)]
 
@@ -78,6 +89,11 @@ SIGNATURES = {
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),
+    "simall_batch_create": (_I, [_P, C.POINTER(SolverConfig), C.POINTER(_P)]),
+    "simall_batch_destroy": (_I, [_P]),
+    "simall_batch_set_systems": (_I, [_P, _I, _P, _P, _P, _P, _P]),
+    "simall_batch_solve": (_I, [_P, _P, _P, _I, _P, C.POINTER(BatchStats)]),
+    "simall_batch_launch_shape": (_I, [_P, _I, _I]),
     "simall_gpu_axpy": (_I, [_D, _P, _P, _SZ, _P]),
     "simall_gpu_scal": (_I, [_D, _P, _SZ, _P]),
     "simall_gpu_copy": (_I, [_P, _P, _SZ, _P]),

@@ -97,3 +97,35 @@ def facek_inputs(m: MeshSoA, seed=DEFAULT_SEED, sigma=0.5):
     pb[~dirichlet] = 0.0
     src = rng.standard_normal(m.n_cells)
     return k, pb, dirichlet.astype(np.uint8), src
+
+
+def cavity_pressure_matrix(side: int, ctx=None):
+    """The pressure-correction matrix of a side x side x 1 lid-driven-cavity
+    grid (extent 1 x 1 x 1/side, all walls, aP = 1, rho = 1) assembled by the
+    library's device assembly; returns (rowPtr, colIdx, values)."""
+    from .mesh import PressureSystem
+
+    m = cartesian(side, side, 1, 1.0, 1.0, 1.0 / side)
+    ps = PressureSystem(m, ALL_WALLS, ctx=ctx)
+    ps.assemble(1.0, np.ones(m.n_cells), np.zeros(m.n_faces))
+    rp, ci = ps.pattern()
+    v, _ = ps.download()
+    ps.close()
+    return rp, ci, v
+
+
+def batched_cavity_systems(count=512, lo=32, hi=256, seed=DEFAULT_SEED, ctx=None):
+    """`count` cavity pressure systems with sides log-uniform in [lo, hi] and
+    rhs N(0,1) with the mean removed and the pinned cell zeroed.
+    Returns (systems, rhs_list, sides)."""
+    sides = batched_sides(count, lo, hi, seed)
+    cache = {}
+    systems, rhs = [], []
+    rng = np.random.default_rng(seed + 5)
+    for s in sides:
+        s = int(s)
+        if s not in cache:
+            cache[s] = cavity_pressure_matrix(s, ctx)
+        systems.append(cache[s])
+        rhs.append(batched_rhs(s * s, rng))
+    return systems, rhs, sides

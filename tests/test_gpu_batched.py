@@ -1,0 +1,89 @@
+"""Batched solves: every system of a batch reaches the FP64 true-residual
+tolerance and matches the oracle's FP64 CG solution of that system."""
+import numpy as np
+import pytest
+
+from helpers import oracle_system
+
+pytestmark = pytest.mark.gpu
+
+
+def _cfg(sg, tol=1e-8, maxit=5000):
+    return sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                 tolerance=tol, maxIterations=maxit)
+
+
+def _check(oracle, systems, rhs, x, stats, tol):
+    for k, ((rp, ci, va), b) in enumerate(zip(systems, rhs)):
+        xs = x[k]
+        r = b - oracle.spmv(rp, ci, va, xs)
+        true_rel = np.linalg.norm(r) / max(np.linalg.norm(b), 1e-30)
+        assert true_rel < tol, (k, true_rel)
+        assert stats["converged"][k] == 1
+        assert abs(stats["true_residual"][k] - true_rel) <= 1e-3 * true_rel + 1e-15
+        xo, _, _ = oracle.cg(rp, ci, va, b, 0, 1e-13, 20000)
+        # both solutions satisfy the same system to their tolerances
+        assert np.linalg.norm(xs - xo) <= 1e-4 * max(np.linalg.norm(xo), 1e-30)
+
+
+def test_batched_cavity_systems(sg, ctx, oracle):
+    from simall_gb300 import workloads as W
+
+    systems, rhs, sides = W.batched_cavity_systems(count=24, lo=4, hi=40, seed=3, ctx=ctx)
+    B = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    rows = B.set_systems(systems)
+    b = np.concatenate(rhs)
+    x, stats = B.solve(b)
+    parts = [x[rows[i]:rows[i + 1]] for i in range(len(systems))]
+    _check(oracle, systems, rhs, parts, stats, 1e-8)
+    assert B.total.converged == len(systems) and B.total.block_threads in (256, 512, 1024)
+    # a second solve reuses the tuned shape and the captured graph
+    x2, stats2 = B.solve(b)
+    assert np.array_equal(x, x2)
+
+
+@pytest.mark.parametrize("shape", [(256, 4), (512, 2), (1024, 1)])
+def test_batched_mixed_storage_and_shapes(sg, ctx, oracle, shape):
+    """Structured (diagonal storage) and RCM-renumbered distorted systems
+    (CSR storage) in one batch, with each fixed launch shape."""
+    systems, rhs = [], []
+    for k, n in enumerate((5, 7, 9)):
+        m, rp, ci, v, b, aP, phi = oracle_system(oracle, n, seed=20 + k)
+        systems.append((rp, ci, v))
+        rhs.append(b)
+    from simall_gb300 import workloads as W
+    for side in (6, 13, 30):
+        rp, ci, v = W.cavity_pressure_matrix(side, ctx)
+        systems.append((rp, ci, v))
+        rhs.append(W.batched_rhs(side * side, np.random.default_rng(side)))
+    B = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    rows = B.set_systems(systems)
+    B.launch_shape(*shape)
+    x, stats = B.solve(np.concatenate(rhs))
+    parts = [x[rows[i]:rows[i + 1]] for i in range(len(systems))]
+    _check(oracle, systems, rhs, parts, stats, 1e-8)
+    assert (B.total.block_threads, B.total.ctas_per_sm) == shape
+
+
+def test_batched_device_memory_and_zero_rhs(sg, ctx, oracle):
+    torch = pytest.importorskip("torch")
+    from simall_gb300 import workloads as W
+    systems = [W.cavity_pressure_matrix(s, ctx) for s in (8, 16)]
+    B = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    rows = B.set_systems(systems)
+    b = np.concatenate([W.batched_rhs(64, np.random.default_rng(1)), np.zeros(256)])
+    tb = torch.from_numpy(b).cuda()
+    tx = torch.empty_like(tb)
+    _, stats = B.solve(tb, tx)
+    x = tx.cpu().numpy()
+    assert stats["converged"].all() and stats["iterations"][1] == 0 and not np.any(x[rows[1]:])
+
+
+def test_batched_rejects_bad_system(sg, ctx):
+    rp = np.array([0, 2, 4], np.int32)
+    ci = np.array([0, 1, 0, 1], np.int32)
+    va = np.array([1.0, 2.0, 2.0, -1.0])  # non-positive diagonal
+    B = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    with pytest.raises(sg.SimallError) as e:
+        B.set_systems([(rp, ci, va)])
+    assert e.value.status == 7
