@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-systems", type=int, default=512,
                     help="systems in the batched leg (0 disables it)")
+    ap.add_argument("--adjoint-n", type=int, default=128, help="box side of the differentiation leg (0 disables it)")
+    ap.add_argument("--fd-faces", type=int, default=64, help="faces checked by central differences")
     return ap.parse_args()
 
 
@@ -246,6 +248,94 @@ def run_batched(a, ctx, sg):
             "setup_seconds": round(setup, 2)}
 
 
+def run_adjoint(a, ctx, sg):
+    """Differentiation leg: N^3 box, face conductances exp(N(0,0.5)) on
+    interior and x=0 faces, Dirichlet values N(0,1) on x=0, cell source
+    N(0,1); L = 0.5 ||x - x_t||^2 with x_t the solution for a second seeded
+    conductance field.  Timed: forward (assembly + mixed solve) and backward
+    (adjoint mixed solve + gradient scatter), both to 1e-10.  Checked: central
+    differences (h = 1e-6, FP64 solves to 1e-13) on seeded faces."""
+    import torch
+    from simall_gb300 import workloads as W
+
+    n = a.adjoint_n
+    m = sg.cartesian(n, n, n)
+    k, pb, dirichlet, src = W.facek_inputs(m, seed=SEED)
+    kt, _, _, _ = W.facek_inputs(m, seed=SEED + 1)
+    bcs = [(1, int(sg.BCType.PressureOutlet))] + [(z, int(sg.BCType.NoSlipWall)) for z in range(2, 7)]
+    ps = sg.PressureSystem(m, bcs, ctx=ctx)
+    mk = lambda tol, prec: sg.GpuCGSolver(sg.LinearSolverConfig(  # noqa: E731
+        kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi, tolerance=tol,
+        maxIterations=a.max_iterations), precision=prec, ctx=ctx)
+    smx = mk(1e-10, sg.Precision.MIXED)
+    s64 = mk(1e-13, sg.Precision.FP64)
+    dev = torch.device("cuda:0")
+    tk, tkt, tpb, tsrc = (torch.from_numpy(v).to(dev) for v in (k, kt, pb, src))
+    x = torch.empty(m.n_cells, dtype=torch.float64, device=dev)
+    xt = torch.empty_like(x)
+    lam, dk, dpb = torch.empty_like(x), torch.empty_like(tk), torch.empty_like(tk)
+    ps.assemble_face_conductance(1.0, tkt, tpb, tsrc)
+    ps.solve(s64, xt)
+
+    def step():
+        ps.assemble_face_conductance(1.0, tk, tpb, tsrc)
+        ps.solve(smx, x)
+        tf = time.perf_counter()
+        ps.adjoint(smx, 1.0, tk, tpb, x, x - xt, lam, dk, dpb)
+        ctx.synchronize()
+        return tf
+
+    for _ in range(max(1, a.warmup)):
+        step()
+    fw, bw = [], []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        tf = step()
+        t1 = time.perf_counter()
+        fw.append(tf - t0)
+        bw.append(t1 - tf)
+    it_fwd = int(smx.stats.iterations)
+    # FP64 reference gradient and central differences
+    ps.assemble_face_conductance(1.0, k, pb, src)
+    x64 = ps.solve(s64)
+    xth = xt.cpu().numpy()
+    lam64, dk64, dpb64 = ps.adjoint(s64, 1.0, k, pb, x64, x64 - xth)
+    g_mx = np.concatenate([dk.cpu().numpy(), dpb.cpu().numpy()])
+    g_64 = np.concatenate([dk64, dpb64])
+    mixed_vs_fp64 = float(np.linalg.norm(g_mx - g_64) / np.linalg.norm(g_64))
+
+    def loss(kk, pp):
+        ps.assemble_face_conductance(1.0, kk, pp, src)
+        xx = ps.solve(s64)
+        return 0.5 * float(np.dot(xx - xth, xx - xth))
+
+    rng = np.random.default_rng(SEED + 7)
+    nd = max(1, a.fd_faces // 8)
+    kf = rng.choice(np.flatnonzero(k > 0), size=a.fd_faces - nd, replace=False)
+    pf = rng.choice(np.flatnonzero(dirichlet), size=nd, replace=False)
+    h = 1e-6
+    errs = []
+    for f in kf:
+        kp, km = k.copy(), k.copy()
+        kp[f] += h
+        km[f] -= h
+        fd = (loss(kp, pb) - loss(km, pb)) / (2 * h)
+        errs.append(abs(fd - dk64[f]) / max(abs(dk64[f]), 1e-12))
+    for f in pf:
+        pp, pm = pb.copy(), pb.copy()
+        pp[f] += h
+        pm[f] -= h
+        fd = (loss(k, pp) - loss(k, pm)) / (2 * h)
+        errs.append(abs(fd - dpb64[f]) / max(abs(dpb64[f]), 1e-12))
+    ps.close()
+    return {"workload": f"face-conductance Poisson {n}^3, k_f=exp(N(0,0.5)), Dirichlet N(0,1) on x=0, "
+                        f"L=0.5|x-x_t|^2", "faces": int(m.n_faces),
+            "forward_s": round(float(np.median(fw)), 5), "backward_s": round(float(np.median(bw)), 5),
+            "forward_iterations": it_fwd, "tolerance": 1e-10,
+            "fd_faces": len(errs), "fd_h": h, "fd_max_rel_err": float(np.max(errs)),
+            "fd_median_rel_err": float(np.median(errs)), "mixed_vs_fp64_gradient_rel": mixed_vs_fp64}
+
+
 def run_ours(a, rank, world, local):
     import torch
 
@@ -362,6 +452,8 @@ def run_ours(a, rank, world, local):
     }
     if a.batched_systems > 0:
         out["batched"] = run_batched(a, ctx, sg)
+    if a.adjoint_n > 0:
+        out["adjoint"] = run_adjoint(a, ctx, sg)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
         out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,

@@ -212,6 +212,34 @@ int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *
 int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,
                                  simall_solver_stats *stats);
 
+/* ------------------------------------------------------------------ differentiation */
+/* Face-conductance Poisson operator (an extension: the reference expresses
+ * neither per-face conductances nor non-zero Dirichlet values).  With
+ * g_f = rho |A_f|^2 / max(|d.A_f|, 1e-30) -- the face coefficient of
+ * SimpleAlgorithm.cpp:391-393 with k_f in place of 1/aP_f -- interior faces add
+ * k_f g_f to (o,o),(n,n) and -k_f g_f to (o,n),(n,o); faces in a
+ * PressureOutlet/PressureInlet zone are Dirichlet faces: they add k_f g_f to
+ * (o,o) and k_f g_f pb_f to rhs_o; rhs starts from src[n_cells].  k and pb
+ * are per face ([n_faces]; pb is read on Dirichlet faces only).  No pin. */
+int simall_assemble_face_conductance(simall_pressure_system *ps, double rho, const double *k, const double *pb,
+                                     const double *src, int mem);
+/* Gradient of a loss L(x) with respect to every face conductance and every
+ * Dirichlet value, given the solution x and the adjoint lambda = A^-T dL/dx:
+ *   interior f: dk_f = -g_f (lambda_o - lambda_n)(x_o - x_n)
+ *   Dirichlet f: dk_f = -g_f lambda_o (x_o - pb_f), dpb_f = k_f g_f lambda_o
+ * (dk = dpb = 0 on other faces).  g_f is recomputed from the geometry, not
+ * stored by the forward pass.  Equals -(dR/dalpha)^T psi of
+ * adjoint::solve_discrete_adjoint (src/adjoint/DiscreteAdjoint.cpp:150-185)
+ * for R(x; k, pb) = A(k) x - b(k, pb). */
+int simall_face_conductance_gradient(simall_pressure_system *ps, double rho, const double *k, const double *pb,
+                                     const double *x, const double *lambda, double *dk, double *dpb, int mem);
+/* The backward pass in one call: lambda = A^-T dLdx with solver s on the
+ * system's current (face-conductance) matrix -- A is symmetric, so this is the
+ * PCG of simall_solver -- then the gradient above. */
+int simall_adjoint_face_conductance(simall_pressure_system *ps, simall_solver *s, double rho, const double *k,
+                                    const double *pb, const double *x, const double *dLdx, double *lambda,
+                                    double *dk, double *dpb, int mem, simall_solver_stats *stats);
+
 /* ------------------------------------------------------------------ batched solves */
 /* Many independent SPD systems of uneven size (e.g. one pressure-correction
  * system per cavity, block or time level) solved in one persistent launch:

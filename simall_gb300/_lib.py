@@ -89,6 +89,9 @@ SIGNATURES = {
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),
+    "simall_assemble_face_conductance": (_I, [_P, _D, _P, _P, _P, _I]),
+    "simall_face_conductance_gradient": (_I, [_P, _D, _P, _P, _P, _P, _P, _P, _I]),
+    "simall_adjoint_face_conductance": (_I, [_P, _P, _D, _P, _P, _P, _P, _P, _P, _P, _I, C.POINTER(SolverStats)]),
     "simall_batch_create": (_I, [_P, C.POINTER(SolverConfig), C.POINTER(_P)]),
     "simall_batch_destroy": (_I, [_P]),
     "simall_batch_set_systems": (_I, [_P, _I, _P, _P, _P, _P, _P]),

@@ -41,6 +41,7 @@ struct simall_pressure_system {
     simall::DevBuf<int32_t> cfOff, cfEnt, cfSlot, diagSlot;
     int anyDirichlet = 0;
     simall::DevBuf<double> aP, phi;  // staging for host inputs
+    simall::DevBuf<double> kf, pbf;  // staging for face-conductance inputs
 };
 
 namespace simall {
@@ -145,6 +146,98 @@ __global__ void __launch_bounds__(kBlock) k_cell_rows(int64_t nC, const int32_t 
         }
         values[kd] = diag;
         rhs[c] = b;
+    }
+}
+
+// ---------------------------------------------------------------- face-conductance operator
+// An extension of the assembly above (the reference cannot express per-face
+// conductances or non-zero Dirichlet values): coef_f = k_f * g_f with
+// g_f = rho |A|^2 / max(|d.A|, 1e-30) -- the reference face coefficient with
+// k_f in place of 1/aP_f -- on interior and pressure-boundary faces; a
+// pressure-boundary face also adds coef_f * pb_f to its cell's rhs, which
+// starts from the cell source.  No pin.
+__device__ __forceinline__ double face_g(double rho, double amag2, double ddotA)
+{
+    return __ddiv_rn(__dmul_rn(rho, amag2), std_max(ddotA, 1e-30));
+}
+
+__global__ void __launch_bounds__(kBlock) k_face_coef_k(int64_t nF, double rho, const uint8_t *__restrict__ kind,
+                                                        const double *__restrict__ amag2,
+                                                        const double *__restrict__ ddotA, const double *__restrict__ k,
+                                                        double *__restrict__ coef)
+{
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nF; f += (int64_t)gridDim.x * blockDim.x)
+        coef[f] = kind[f] == kOtherBoundary ? 0.0 : __dmul_rn(k[f], face_g(rho, amag2[f], ddotA[f]));
+}
+
+__global__ void __launch_bounds__(kBlock) k_cell_rows_k(int64_t nC, const int32_t *__restrict__ rowPtr,
+                                                        const int32_t *__restrict__ cfOff,
+                                                        const int32_t *__restrict__ cfEnt,
+                                                        const int32_t *__restrict__ cfSlot,
+                                                        const int32_t *__restrict__ diagSlot,
+                                                        const uint8_t *__restrict__ kind,
+                                                        const double *__restrict__ coef, const double *__restrict__ pb,
+                                                        const double *__restrict__ src, double *__restrict__ values,
+                                                        double *__restrict__ rhs)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nC; c += (int64_t)gridDim.x * blockDim.x) {
+        const int r0 = rowPtr[c], r1 = rowPtr[c + 1];
+        for (int q = r0; q < r1; ++q)
+            values[q] = 0.0;
+        double diag = 0.0, b = src[c];
+        for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) {
+            const int f = cfEnt[e] & 0x7fffffff;
+            const uint8_t kd = kind[f];
+            if (kd == kOtherBoundary)
+                continue;
+            const double cf = __ldg(coef + f);
+            diag = __dadd_rn(diag, cf);
+            if (kd == kInterior) {
+                const int slot = cfSlot[e];
+                if (slot >= 0)
+                    values[slot] = __dadd_rn(values[slot], -cf);
+            } else {
+                b = __dadd_rn(b, __dmul_rn(cf, __ldg(pb + f)));
+            }
+        }
+        values[diagSlot[c]] = diag;
+        rhs[c] = b;
+    }
+}
+
+// dL/dk_f and dL/dpb_f from x and the adjoint lambda = A^-T dL/dx, recomputing
+// g_f from the stored geometry (no coefficient is kept from the forward pass):
+//   interior f:      dk = -g (lambda_o - lambda_n)(x_o - x_n)
+//   pressure face f: dk = -g lambda_o (x_o - pb_f),  dpb = k_f g lambda_o
+// This is -(dR/dalpha)^T lambda of solve_discrete_adjoint
+// (src/adjoint/DiscreteAdjoint.cpp:170-182) for R = A(k) x - b(k, pb).
+__global__ void __launch_bounds__(kBlock) k_face_k_gradient(int64_t nF, double rho, const int32_t *__restrict__ owner,
+                                                            const int32_t *__restrict__ neighbor,
+                                                            const uint8_t *__restrict__ kind,
+                                                            const double *__restrict__ amag2,
+                                                            const double *__restrict__ ddotA,
+                                                            const double *__restrict__ k, const double *__restrict__ pb,
+                                                            const double *__restrict__ x,
+                                                            const double *__restrict__ lambda, double *__restrict__ dk,
+                                                            double *__restrict__ dpb)
+{
+    for (int64_t f = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; f < nF; f += (int64_t)gridDim.x * blockDim.x) {
+        const uint8_t kd = kind[f];
+        double gk = 0.0, gp = 0.0;
+        if (kd != kOtherBoundary) {
+            const double g = face_g(rho, amag2[f], ddotA[f]);
+            const int o = owner[f];
+            const double lo = __ldg(lambda + o), xo = __ldg(x + o);
+            if (kd == kInterior) {
+                const int n = neighbor[f];
+                gk = __dmul_rn(__dmul_rn(-g, __dsub_rn(lo, __ldg(lambda + n))), __dsub_rn(xo, __ldg(x + n)));
+            } else {
+                gk = __dmul_rn(__dmul_rn(-g, lo), __dsub_rn(xo, __ldg(pb + f)));
+                gp = __dmul_rn(__dmul_rn(k[f], g), lo);
+            }
+        }
+        dk[f] = gk;
+        dpb[f] = gp;
     }
 }
 
@@ -441,6 +534,100 @@ int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *
     if (s->ready && s->n == ps->nC && s->nnz == ps->nnz && s->rowPtr == ps->rowPtr.p && s->values == ps->values.p)
         return simall_solver_update_values(s, ps->values.p, SIMALL_MEM_DEVICE);
     return simall_solver_set_matrix(s, ps->nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->values.p, SIMALL_MEM_DEVICE);
+}
+
+int simall_assemble_face_conductance(simall_pressure_system *ps, double rho, const double *k, const double *pb,
+                                     const double *src, int mem)
+{
+    if (!ps || !k || !pb || !src)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = ps->ctx;
+    if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "assemble: bad memory kind %d", mem);
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const double *dk = k, *dpb = pb, *dsrc = src;
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, ps->kf.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, ps->pbf.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, ps->aP.alloc(ps->nC));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(ps->kf.p, k, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(ps->pbf.p, pb, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(ps->aP.p, src, ps->nC * sizeof(double), cudaMemcpyHostToDevice, st));
+        dk = ps->kf.p;
+        dpb = ps->pbf.p;
+        dsrc = ps->aP.p;
+    }
+    const int gf = static_cast<int>(std::min<int64_t>((ps->nF + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    const int gc = static_cast<int>(std::min<int64_t>((ps->nC + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    k_face_coef_k<<<gf, kBlock, 0, st>>>(ps->nF, rho, ps->kind.p, ps->amag2.p, ps->ddotA.p, dk, ps->coef.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_cell_rows_k<<<gc, kBlock, 0, st>>>(ps->nC, ps->rowPtr.p, ps->cfOff.p, ps->cfEnt.p, ps->cfSlot.p, ps->diagSlot.p,
+                                         ps->kind.p, ps->coef.p, dpb, dsrc, ps->values.p, ps->rhs.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (mem == SIMALL_MEM_HOST)
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return SIMALL_OK;
+}
+
+int simall_face_conductance_gradient(simall_pressure_system *ps, double rho, const double *k, const double *pb,
+                                     const double *x, const double *lambda, double *dk, double *dpb, int mem)
+{
+    if (!ps || !k || !pb || !x || !lambda || !dk || !dpb)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = ps->ctx;
+    if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "gradient: bad memory kind %d", mem);
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const double *d_k = k, *d_pb = pb, *d_x = x, *d_l = lambda;
+    double *d_dk = dk, *d_dpb = dpb;
+    DevBuf<double> tk, tpb, tx, tl, tdk, tdpb;
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, tk.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, tpb.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, tx.alloc(ps->nC));
+        SIMALL_CUDA_TRY(ctx, tl.alloc(ps->nC));
+        SIMALL_CUDA_TRY(ctx, tdk.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, tdpb.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(tk.p, k, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(tpb.p, pb, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(tx.p, x, ps->nC * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(tl.p, lambda, ps->nC * sizeof(double), cudaMemcpyHostToDevice, st));
+        d_k = tk.p;
+        d_pb = tpb.p;
+        d_x = tx.p;
+        d_l = tl.p;
+        d_dk = tdk.p;
+        d_dpb = tdpb.p;
+    }
+    const int gf = static_cast<int>(std::min<int64_t>((ps->nF + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    k_face_k_gradient<<<gf, kBlock, 0, st>>>(ps->nF, rho, ps->owner.p, ps->neighbor.p, ps->kind.p, ps->amag2.p,
+                                             ps->ddotA.p, d_k, d_pb, d_x, d_l, d_dk, d_dpb);
+    SIMALL_LAUNCH_CHECK(ctx);
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(dk, d_dk, ps->nF * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(dpb, d_dpb, ps->nF * sizeof(double), cudaMemcpyDeviceToHost, st));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    }
+    return SIMALL_OK;
+}
+
+int simall_adjoint_face_conductance(simall_pressure_system *ps, simall_solver *s, double rho, const double *k,
+                                    const double *pb, const double *x, const double *dLdx, double *lambda,
+                                    double *dk, double *dpb, int mem, simall_solver_stats *stats)
+{
+    if (!ps || !s || !k || !pb || !x || !dLdx || !lambda || !dk || !dpb)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    // the assembled operator is symmetric, so A^T lambda = dL/dx is solved
+    // with the same PCG on the same device matrix
+    int st = simall_solver_use_pressure_system(s, ps);
+    if (st)
+        return st;
+    st = solver_solve_impl(s, dLdx, mem, lambda, mem, stats);
+    if (st)
+        return st;
+    return simall_face_conductance_gradient(ps, rho, k, pb, x, lambda, dk, dpb, mem);
 }
 
 int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,

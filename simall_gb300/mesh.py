@@ -161,6 +161,42 @@ class PressureSystem:
               self.ctx.handle)
         self.any_dirichlet = bool(anyD.value)
 
+    def assemble_face_conductance(self, rho: float, k, pb, src):
+        """Face-conductance operator: coef_f = k_f g_f, Dirichlet values pb on
+        pressure-boundary faces, rhs from the cell source src."""
+        pk, mk = ptr_and_mem(k)
+        pp, mp = ptr_and_mem(pb)
+        ps_, ms = ptr_and_mem(src)
+        if not (mk == mp == ms):
+            raise ValueError("k, pb and src must live in the same memory")
+        check(self.L.simall_assemble_face_conductance(self.handle, float(rho), pk, pp, ps_, mk), self.ctx.handle)
+
+    def face_conductance_gradient(self, rho: float, k, pb, x, lam, dk=None, dpb=None):
+        if dk is None:
+            dk = np.empty(self.mesh.n_faces)
+            dpb = np.empty(self.mesh.n_faces)
+        args = [ptr_and_mem(a) for a in (k, pb, x, lam, dk, dpb)]
+        mem = args[0][1]
+        if any(m != mem for _, m in args):
+            raise ValueError("all arrays must live in the same memory")
+        check(self.L.simall_face_conductance_gradient(self.handle, float(rho), *[p for p, _ in args], mem),
+              self.ctx.handle)
+        return dk, dpb
+
+    def adjoint(self, solver: GpuCGSolver, rho: float, k, pb, x, dLdx, lam=None, dk=None, dpb=None):
+        """lambda = A^-T dL/dx (PCG), then dL/dk and dL/dpb per face."""
+        if lam is None:
+            lam = np.empty(self.n)
+            dk = np.empty(self.mesh.n_faces)
+            dpb = np.empty(self.mesh.n_faces)
+        args = [ptr_and_mem(a) for a in (k, pb, x, dLdx, lam, dk, dpb)]
+        mem = args[0][1]
+        if any(m != mem for _, m in args):
+            raise ValueError("all arrays must live in the same memory")
+        check(self.L.simall_adjoint_face_conductance(self.handle, solver.handle, float(rho), *[p for p, _ in args],
+                                                     mem, C.byref(solver.stats)), self.ctx.handle)
+        return lam, dk, dpb
+
     def download(self):
         v = np.empty(self.nnz)
         r = np.empty(self.n)
