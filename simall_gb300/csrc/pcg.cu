@@ -442,6 +442,14 @@ int enqueue_iteration(simall_solver *s)
     return SIMALL_OK;
 }
 
+// Kernels one FP64 iteration launches (for the launch counter of graph replays).
+int64_t kernels_per_iteration(const simall_solver *s)
+{
+    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 && s->ilu)
+        return 4 + static_cast<int64_t>(s->ilu->fwdLevelPtr.size() - 1) + static_cast<int64_t>(s->ilu->bwdLevelPtr.size() - 1);
+    return 3;
+}
+
 // A chunk of `len` iterations, captured once into a graph and replayed.
 int run_chunk(simall_solver *s, int len)
 {
@@ -449,20 +457,9 @@ int run_chunk(simall_solver *s, int len)
     for (auto &g : s->graphs)
         if (g.len == len) {
             SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(g.exec, ctx->stream));
-            ctx->launches.fetch_add(static_cast<int64_t>(len) *
-                                        (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 ? 0 : 3),
-                                    std::memory_order_relaxed);
+            ctx->launches.fetch_add(static_cast<int64_t>(len) * kernels_per_iteration(s), std::memory_order_relaxed);
             return SIMALL_OK;
         }
-    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
-        // ILU0 chunks launch one kernel per level; enqueue them directly.
-        for (int i = 0; i < len; ++i) {
-            int st = enqueue_iteration(s);
-            if (st)
-                return st;
-        }
-        return SIMALL_OK;
-    }
     cudaGraph_t graph = nullptr;
     SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int st = SIMALL_OK;
@@ -510,7 +507,9 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
         SIMALL_LAUNCH_CHECK(ctx);
     }
     int done_iters = 0;
-    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 16;
+    const bool ilu = s->cfg.preconditioner == SIMALL_PRECOND_ILU0;
+    const int max_chunk = ilu ? 8 : 64;  // an ILU0 iteration is one graph node per level
+    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : (ilu ? 8 : 16);
     double prev_last = -1.0;
     int prev_iter = 0;
     for (;;) {
@@ -518,6 +517,9 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
         int len = chunk < remaining ? chunk : remaining;
         if (len < 1)
             len = 1;
+        // a few distinct lengths only, so the captured graphs are reused
+        if (s->cfg.check_interval <= 0)
+            len = len <= 4 ? len : len <= 8 ? 8 : len <= 16 ? 16 : len <= 32 ? 32 : 64;
         int e = run_chunk(s, len);
         if (e)
             return e;
@@ -533,11 +535,11 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
             // predict the remaining iterations from the observed decay rate
             const double last = s->h_scal->last;
             const int it = s->h_scal->iter;
-            int next = 64;
+            int next = max_chunk;
             if (prev_last > 0.0 && last > 0.0 && last < prev_last && it > prev_iter) {
                 const double rate = std::log(last / prev_last) / (it - prev_iter);
                 const double need = std::log(s->cfg.tolerance / last) / rate;
-                next = need < 4 ? 4 : (need > 64 ? 64 : static_cast<int>(need) + 1);
+                next = need < 4 ? 4 : (need > max_chunk ? max_chunk : static_cast<int>(need) + 1);
             }
             prev_last = last;
             prev_iter = it;
