@@ -531,8 +531,8 @@ int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *
 {
     if (!s || !ps)
         return SIMALL_ERR_INVALID_ARGUMENT;
-    if (s->ready && s->n == ps->nC && s->nnz == ps->nnz && s->rowPtr == ps->rowPtr.p && s->values == ps->values.p)
-        return simall_solver_update_values(s, ps->values.p, SIMALL_MEM_DEVICE);
+    // set_matrix recognises an unchanged pattern on the device and keeps its
+    // analysis (row-blocks, storage format, ILU0 levels, captured graphs)
     return simall_solver_set_matrix(s, ps->nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->values.p, SIMALL_MEM_DEVICE);
 }
 

@@ -230,6 +230,9 @@ int ilu_setup(simall_solver *s)
     }
     IluData *d = s->ilu;
     if (!d->analysed) {
+        int hp = solver_host_pattern(s);
+        if (hp)
+            return hp;
         int st = analyse(ctx, d, s->n, s->h_rowPtr.data(), s->h_colIdx.data());
         if (st)
             return st;

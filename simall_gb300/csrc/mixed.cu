@@ -23,6 +23,7 @@
 #include "solver.hpp"
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <new>
 
@@ -474,39 +475,123 @@ int grid_n(simall_context *ctx, int64_t n)
     return static_cast<int>(g < 1 ? 1 : (g < cap ? g : cap));
 }
 
-// Host: choose the storage format from the pattern (dia only if allowed).
-void analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
+// Distinct upper-triangle offsets j - i of the pattern (a table of
+// kOffTable slots, empty = INT_MIN), the count of upper entries, and an
+// overflow flag when there are more than kMaxDiags distinct offsets.
+constexpr int kOffTable = 16;
+
+__device__ __forceinline__ bool table_insert(int *tab, int off)
 {
-    const int64_t n = s->n;
-    const int32_t *rp = s->h_rowPtr.data(), *ci = s->h_colIdx.data();
-    std::vector<int32_t> offs;
-    bool ok = allow_dia;
-    int64_t upper = 0;
-    for (int64_t i = 0; i < n && ok; ++i)
-        for (int k = rp[i]; k < rp[i + 1]; ++k) {
-            const int j = ci[k];
+    for (int s = 0; s < kOffTable; ++s) {
+        const int cur = tab[s];
+        if (cur == off)
+            return true;
+        if (cur == INT_MIN) {
+            const int prev = atomicCAS(tab + s, INT_MIN, off);
+            if (prev == INT_MIN || prev == off)
+                return true;
+        }
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_offsets(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                       const int32_t *__restrict__ colIdx, int *table,
+                                                       unsigned long long *upper, int *overflow)
+{
+    __shared__ int stab[kOffTable];
+    __shared__ int sover;
+    __shared__ unsigned long long scount;
+    if (threadIdx.x < kOffTable)
+        stab[threadIdx.x] = INT_MIN;
+    if (threadIdx.x == 0) {
+        sover = 0;
+        scount = 0ull;
+    }
+    __syncthreads();
+    int local[kMaxDiags];
+    int nl = 0;
+    bool over = false;
+    unsigned long long cnt = 0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int j = colIdx[k];
             if (j <= i)
                 continue;
-            ++upper;
-            const int32_t off = j - static_cast<int32_t>(i);
-            if (std::find(offs.begin(), offs.end(), off) == offs.end()) {
-                if (static_cast<int>(offs.size()) == kMaxDiags) {
-                    ok = false;
-                    break;
-                }
-                offs.push_back(off);
+            ++cnt;
+            const int off = j - static_cast<int>(i);
+            bool seen = false;
+            for (int t = 0; t < nl; ++t)
+                seen |= (local[t] == off);
+            if (!seen) {
+                if (nl < kMaxDiags)
+                    local[nl++] = off;
+                else
+                    over = true;
             }
         }
-    // dia only pays when the diagonals are nearly full
-    if (ok && !offs.empty() && static_cast<double>(offs.size()) * n > 1.3 * static_cast<double>(upper))
-        ok = false;
-    m->dia = ok && !offs.empty();
+    for (int t = 0; t < nl; ++t)
+        if (!table_insert(stab, local[t]))
+            over = true;
+    if (over)
+        atomicOr(&sover, 1);
+    atomicAdd(&scount, cnt);
+    __syncthreads();
+    if (threadIdx.x < kOffTable && stab[threadIdx.x] != INT_MIN)
+        if (!table_insert(table, stab[threadIdx.x]))
+            atomicOr(overflow, 1);
+    if (threadIdx.x == 0) {
+        atomicAdd(upper, scount);
+        if (sover)
+            atomicOr(overflow, 1);
+    }
+}
+
+// Choose the storage format of S A S from the pattern (diagonal storage only
+// if allowed).  The diagonal test runs on the device; the CSR fallback is
+// built from a host copy of the pattern.
+int analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
+{
+    simall_context *ctx = s->ctx;
+    const int64_t n = s->n;
+    std::vector<int32_t> offs;
+    bool ok = allow_dia;
+    if (ok) {
+        DevBuf<int> tab;
+        DevBuf<unsigned long long> cnt;
+        SIMALL_CUDA_TRY(ctx, tab.alloc(kOffTable + 1));
+        SIMALL_CUDA_TRY(ctx, cnt.alloc(1));
+        std::vector<int> init(kOffTable + 1, INT_MIN);
+        init[kOffTable] = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(tab.p, init.data(), init.size() * sizeof(int), cudaMemcpyHostToDevice,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(cnt.p, 0, sizeof(unsigned long long), ctx->stream));
+        k_mx_offsets<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, tab.p, cnt.p,
+                                                                 tab.p + kOffTable);
+        SIMALL_LAUNCH_CHECK(ctx);
+        std::vector<int> h(kOffTable + 1);
+        unsigned long long upper = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(h.data(), tab.p, h.size() * sizeof(int), cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&upper, cnt.p, sizeof(upper), cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        for (int t = 0; t < kOffTable; ++t)
+            if (h[t] != INT_MIN)
+                offs.push_back(h[t]);
+        ok = !h[kOffTable] && !offs.empty() && static_cast<int>(offs.size()) <= kMaxDiags &&
+             static_cast<double>(offs.size()) * n <= 1.3 * static_cast<double>(upper);
+    }
+    m->dia = ok;
     if (m->dia) {
         std::sort(offs.begin(), offs.end());
         m->offs.nd = static_cast<int>(offs.size());
         for (int d = 0; d < kMaxDiags; ++d)
             m->offs.off[d] = d < m->offs.nd ? offs[d] : 0;
     } else {
+        int st = solver_host_pattern(s);
+        if (st)
+            return st;
+        const int32_t *rp = s->h_rowPtr.data(), *ci = s->h_colIdx.data();
         m->h_orow.assign(static_cast<size_t>(n) + 1, 0);
         m->h_ocol.clear();
         m->h_opos.clear();
@@ -521,6 +606,7 @@ void analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
         m->nnzOff = static_cast<int>(m->h_ocol.size());
     }
     m->patternReady = true;
+    return SIMALL_OK;
 }
 
 int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *ph, float *qh, double *partials,
@@ -561,8 +647,11 @@ int mixed_setup(simall_solver *s)
     }
     MixedData *m = s->mixed;
     const int64_t n = s->n;
-    if (!m->patternReady)
-        analyse_pattern(s, m, true);
+    if (!m->patternReady) {
+        int st = analyse_pattern(s, m, true);
+        if (st)
+            return st;
+    }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
     SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
     SIMALL_CUDA_TRY(ctx, m->rh.alloc(n + 4));
@@ -582,8 +671,11 @@ int mixed_setup(simall_solver *s)
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (h & 1)
         return fail(ctx, SIMALL_ERR_NOT_POSITIVE, "mixed precision needs a positive diagonal");
-    if (m->dia && (h & 2))
-        analyse_pattern(s, m, false);  // not numerically symmetric: keep every off-diagonal entry
+    if (m->dia && (h & 2)) {
+        int st = analyse_pattern(s, m, false);  // not numerically symmetric: keep every off-diagonal entry
+        if (st)
+            return st;
+    }
     if (m->dia) {
         m->ldU = (n + 3) & ~static_cast<int64_t>(3);
         SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * m->ldU));

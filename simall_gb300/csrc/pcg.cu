@@ -49,6 +49,94 @@ __global__ void __launch_bounds__(kBlock) k_check_finite(int64_t n, const double
             atomicOr(flag, 1);
 }
 
+enum : unsigned {
+    kBadRowPtr = 1u,     // rowPtr not monotone or outside [0, nnz]
+    kBadRange = 2u,      // a column outside [0, n)
+    kUnsorted = 4u,      // columns of a row not strictly ascending
+    kNoDiag = 8u,        // a row without its diagonal
+    kNonFinite = 16u,    // NaN / Inf value
+    kPatternDiff = 32u,  // pattern differs from the solver's current one
+    kBlockTooBig = 64u,  // a 256-row block holds more nonzeros than the staging buffer
+    kBadEnds = 128u      // rowPtr[0] != 0 or rowPtr[n] != nnz
+};
+
+__device__ __forceinline__ void or_flags(unsigned f, unsigned *flags)
+{
+    f = __reduce_or_sync(0xffffffffu, f);
+    if ((threadIdx.x & 31) == 0 && f)
+        atomicOr(flags, f);
+}
+
+// Full CSR validation on the device.  Every row's bounds are checked before
+// its columns are read, so a corrupt rowPtr is reported, not followed.
+__global__ void __launch_bounds__(kBlock) k_validate_csr(int64_t n, int64_t nnz, const int32_t *__restrict__ rowPtr,
+                                                         const int32_t *__restrict__ colIdx,
+                                                         const double *__restrict__ values, unsigned *flags)
+{
+    unsigned f = 0;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    if (tid == 0 && (rowPtr[0] != 0 || rowPtr[n] != nnz))
+        f |= kBadEnds;
+    for (int64_t i = tid; i < n; i += stride) {
+        const int a = rowPtr[i], b = rowPtr[i + 1];
+        if (a < 0 || b < a || b > nnz) {
+            f |= kBadRowPtr;
+            continue;
+        }
+        bool diag = false;
+        int prev = -1;
+        for (int k = a; k < b; ++k) {
+            const int c = colIdx[k];
+            if (c < 0 || c >= n) {
+                f |= kBadRange;
+            } else {
+                if (c <= prev)
+                    f |= kUnsorted;
+                prev = c;
+                diag |= (c == i);
+            }
+            if (values && !isfinite(values[k]))
+                f |= kNonFinite;
+        }
+        if (!diag)
+            f |= kNoDiag;
+    }
+    or_flags(f, flags);
+}
+
+__global__ void __launch_bounds__(kBlock) k_compare_pattern(int64_t n, int64_t nnz, const int32_t *__restrict__ ra,
+                                                            const int32_t *__restrict__ ca,
+                                                            const int32_t *__restrict__ rb,
+                                                            const int32_t *__restrict__ cb, unsigned *flags)
+{
+    unsigned f = 0;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t i = tid; i <= n; i += stride)
+        f |= (ra[i] != rb[i]) ? kPatternDiff : 0u;
+    for (int64_t k = tid; k < nnz; k += stride)
+        f |= (ca[k] != cb[k]) ? kPatternDiff : 0u;
+    or_flags(f, flags);
+}
+
+// Row-blocks of kSpmvRows consecutive rows fit the staging buffer?
+__global__ void __launch_bounds__(kBlock) k_rowblock_fit(int64_t n, int64_t nb, const int32_t *__restrict__ rowPtr,
+                                                         unsigned *flags)
+{
+    unsigned f = 0;
+    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t b = tid; b < nb; b += stride) {
+        const int64_t r0 = b * kSpmvRows, r1 = (r0 + kSpmvRows < n) ? r0 + kSpmvRows : n;
+        f |= (rowPtr[r1] - rowPtr[r0] > kSpmvNnzCap) ? kBlockTooBig : 0u;
+    }
+    or_flags(f, flags);
+}
+
+__global__ void __launch_bounds__(kBlock) k_rowblock_fill(int64_t n, int64_t nb, int32_t *__restrict__ rb)
+{
+    for (int64_t b = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; b <= nb; b += (int64_t)gridDim.x * blockDim.x)
+        rb[b] = static_cast<int32_t>(b * kSpmvRows < n ? b * kSpmvRows : n);
+}
+
 // x = 0, r = b, z = invD r, p = z; rz = r.z, bnorm = max(||b||, 1e-30).
 __global__ void __launch_bounds__(kBlock) k_init_jacobi(int64_t n, const double *__restrict__ b,
                                                         const double *__restrict__ invD, double *__restrict__ x,
@@ -552,6 +640,22 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
 
 }  // namespace
 
+int solver_host_pattern(simall_solver *s)
+{
+    if (s->h_pattern_valid)
+        return SIMALL_OK;
+    simall_context *ctx = s->ctx;
+    s->h_rowPtr.resize(static_cast<size_t>(s->n) + 1);
+    s->h_colIdx.resize(static_cast<size_t>(s->nnz));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_rowPtr.data(), s->own_rowPtr.p, (s->n + 1) * sizeof(int32_t),
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_colIdx.data(), s->own_colIdx.p, s->nnz * sizeof(int32_t),
+                                         cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    s->h_pattern_valid = true;
+    return SIMALL_OK;
+}
+
 int solver_fetch_scalars(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
@@ -645,70 +749,103 @@ int simall_solver_set_matrix(simall_solver *s, int64_t n, int64_t nnz, const int
     s->ready = false;
     if (n <= 0 || nnz <= 0 || !rowPtr || !colIdx || !values)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "set_matrix: empty matrix or null array");
+    if (n > INT32_MAX - 1 || nnz > INT32_MAX)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "set_matrix: sizes exceed int32 indexing");
     if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "set_matrix: bad memory kind %d", mem);
-    const bool same_pattern_size = (n == s->n && nnz == s->nnz);
-    s->h_rowPtr.resize(static_cast<size_t>(n) + 1);
-    s->h_colIdx.resize(static_cast<size_t>(nnz));
+    cudaStream_t st = ctx->stream;
+    const cudaMemcpyKind kind = mem == SIMALL_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice;
+    if (mem == SIMALL_MEM_HOST && (rowPtr[0] != 0 || rowPtr[n] != nnz))
+        return fail(ctx, SIMALL_ERR_SIZE_MISMATCH, "CSR: rowPtr[0]=%d rowPtr[n]=%d, nnz=%lld", rowPtr[0], rowPtr[n],
+                    static_cast<long long>(nnz));
+    // the new pattern goes to the staging pair, the values to their home
+    SIMALL_CUDA_TRY(ctx, s->new_rowPtr.alloc(n + 1));
+    SIMALL_CUDA_TRY(ctx, s->new_colIdx.alloc(nnz));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->new_rowPtr.p, rowPtr, (n + 1) * sizeof(int32_t), kind, st));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->new_colIdx.p, colIdx, nnz * sizeof(int32_t), kind, st));
+    const double *vals = values;
     if (mem == SIMALL_MEM_HOST) {
-        int st = check_csr_host(ctx, n, nnz, rowPtr, colIdx, values, true);
-        if (st)
-            return st;
-        std::memcpy(s->h_rowPtr.data(), rowPtr, (n + 1) * sizeof(int32_t));
-        std::memcpy(s->h_colIdx.data(), colIdx, nnz * sizeof(int32_t));
-        SIMALL_CUDA_TRY(ctx, s->own_rowPtr.alloc(n + 1));
-        SIMALL_CUDA_TRY(ctx, s->own_colIdx.alloc(nnz));
         SIMALL_CUDA_TRY(ctx, s->own_values.alloc(nnz));
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_rowPtr.p, rowPtr, (n + 1) * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                             ctx->stream));
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_colIdx.p, colIdx, nnz * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                             ctx->stream));
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_values.p, values, nnz * sizeof(double), cudaMemcpyHostToDevice,
-                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_values.p, values, nnz * sizeof(double), kind, st));
+        vals = s->own_values.p;
+    }
+    // validation, comparison with the current pattern and the row-block test
+    // run on the device; the host reads one flag word
+    SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
+    unsigned *flags = reinterpret_cast<unsigned *>(s->flag.p);
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(flags, 0, sizeof(unsigned), st));
+    const int g = grid_for(ctx, n);
+    k_validate_csr<<<g, kBlock, 0, st>>>(n, nnz, s->new_rowPtr.p, s->new_colIdx.p, vals, flags);
+    SIMALL_LAUNCH_CHECK(ctx);
+    const bool comparable = s->have_pattern && n == s->n && nnz == s->nnz;
+    if (comparable) {
+        k_compare_pattern<<<grid_for(ctx, nnz), kBlock, 0, st>>>(n, nnz, s->new_rowPtr.p, s->new_colIdx.p,
+                                                                 s->own_rowPtr.p, s->own_colIdx.p, flags);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    const int64_t nb = (n + kSpmvRows - 1) / kSpmvRows;
+    k_rowblock_fit<<<grid_for(ctx, nb), kBlock, 0, st>>>(n, nb, s->new_rowPtr.p, flags);
+    SIMALL_LAUNCH_CHECK(ctx);
+    unsigned h = 0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, st));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    if (h & kBadEnds)
+        return fail(ctx, SIMALL_ERR_SIZE_MISMATCH, "CSR: rowPtr[0] != 0 or rowPtr[n] != nnz (%lld)",
+                    static_cast<long long>(nnz));
+    if (h & kBadRowPtr)
+        return fail(ctx, SIMALL_ERR_UNSORTED_CSR, "CSR: rowPtr decreases or leaves [0, nnz]");
+    if (h & kBadRange)
+        return fail(ctx, SIMALL_ERR_INDEX_RANGE, "CSR: a column index is outside [0, n)");
+    if (h & kUnsorted)
+        return fail(ctx, SIMALL_ERR_UNSORTED_CSR, "CSR: columns of a row are not strictly ascending");
+    if (h & kNoDiag)
+        return fail(ctx, SIMALL_ERR_MISSING_DIAGONAL, "CSR: a row has no diagonal entry");
+    if (h & kNonFinite)
+        return fail(ctx, SIMALL_ERR_NON_FINITE, "matrix values contain NaN or Inf");
+    const bool pattern_changed = !(comparable && !(h & kPatternDiff));
+    if (pattern_changed) {
+        std::swap(s->own_rowPtr.p, s->new_rowPtr.p);
+        std::swap(s->own_rowPtr.n, s->new_rowPtr.n);
+        std::swap(s->own_colIdx.p, s->new_colIdx.p);
+        std::swap(s->own_colIdx.n, s->new_colIdx.n);
+        s->have_pattern = true;
+        s->h_pattern_valid = false;
+        drop_graphs(s);
+        if (s->ilu)
+            s->ilu->analysed = false;
+        mixed_invalidate_pattern(s);
+        s->n = n;
+        s->nnz = nnz;
         s->rowPtr = s->own_rowPtr.p;
         s->colIdx = s->own_colIdx.p;
-        s->values = s->own_values.p;
-    } else {
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_rowPtr.data(), rowPtr, (n + 1) * sizeof(int32_t),
-                                             cudaMemcpyDeviceToHost, ctx->stream));
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->h_colIdx.data(), colIdx, nnz * sizeof(int32_t), cudaMemcpyDeviceToHost,
-                                             ctx->stream));
-        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        s->rowPtr = rowPtr;
-        s->colIdx = colIdx;
-        s->values = values;
-        // pattern checks on the host copy; values are checked on the device
-        int st = check_csr_host(ctx, n, nnz, s->h_rowPtr.data(), s->h_colIdx.data(), nullptr, true);
-        if (st)
-            return st;
+        if (!(h & kBlockTooBig)) {
+            s->nRowBlocks = static_cast<int>(nb);
+            SIMALL_CUDA_TRY(ctx, s->rowBlocks.alloc(nb + 1));
+            k_rowblock_fill<<<grid_for(ctx, nb + 1), kBlock, 0, st>>>(n, nb, s->rowBlocks.p);
+            SIMALL_LAUNCH_CHECK(ctx);
+        } else {
+            int e = solver_host_pattern(s);
+            if (e)
+                return e;
+            std::vector<int32_t> rb = make_row_blocks(n, s->h_rowPtr.data());
+            s->nRowBlocks = static_cast<int>(rb.size()) - 1;
+            SIMALL_CUDA_TRY(ctx, s->rowBlocks.alloc(rb.size()));
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->rowBlocks.p, rb.data(), rb.size() * sizeof(int32_t),
+                                                 cudaMemcpyHostToDevice, st));
+            SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        }
     }
-    s->n = n;
-    s->nnz = nnz;
+    if (vals != s->values)
+        drop_graphs(s);  // captured graphs embed the values pointer
+    s->values = vals;
     s->solved = false;
-    if (mem == SIMALL_MEM_DEVICE) {
-        int st = check_device_values(s);
-        if (st)
-            return st;
-    }
-    // captured graphs embed the matrix pointers and sizes; the ILU level
-    // schedule depends on the pattern
-    (void)same_pattern_size;
-    drop_graphs(s);
-    if (s->ilu)
-        s->ilu->analysed = false;
-    mixed_invalidate_pattern(s);
-    std::vector<int32_t> rb = make_row_blocks(n, s->h_rowPtr.data());
-    s->nRowBlocks = static_cast<int>(rb.size()) - 1;
-    SIMALL_CUDA_TRY(ctx, s->rowBlocks.alloc(rb.size()));
-    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->rowBlocks.p, rb.data(), rb.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                         ctx->stream));
-    int st = alloc_vectors(s);
-    if (st)
-        return st;
-    st = setup_values(s);
-    if (st)
-        return st;
-    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    int e = alloc_vectors(s);
+    if (e)
+        return e;
+    e = setup_values(s);
+    if (e)
+        return e;
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     s->ready = true;
     return SIMALL_OK;
 }
@@ -722,9 +859,6 @@ int simall_solver_update_values(simall_solver *s, const double *values, int mem)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "update_values before set_matrix");
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     if (mem == SIMALL_MEM_HOST) {
-        for (int64_t k = 0; k < s->nnz; ++k)
-            if (!std::isfinite(values[k]))
-                return fail(ctx, SIMALL_ERR_NON_FINITE, "matrix values contain NaN or Inf");
         if (s->values != s->own_values.p) {
             SIMALL_CUDA_TRY(ctx, s->own_values.alloc(s->nnz));
             s->values = s->own_values.p;
@@ -732,6 +866,9 @@ int simall_solver_update_values(simall_solver *s, const double *values, int mem)
         }
         SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->own_values.p, values, s->nnz * sizeof(double), cudaMemcpyHostToDevice,
                                              ctx->stream));
+        int st = check_device_values(s);
+        if (st)
+            return st;
     } else {
         if (values != s->values)
             drop_graphs(s);
@@ -766,13 +903,19 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const auto t0 = std::chrono::steady_clock::now();
     const size_t bytes = static_cast<size_t>(s->n) * sizeof(double);
-    if (bmem == SIMALL_MEM_HOST) {
-        for (int64_t i = 0; i < s->n; ++i)
-            if (!std::isfinite(b[i]))
-                return fail(ctx, SIMALL_ERR_NON_FINITE, "b contains NaN or Inf");
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, b, bytes, cudaMemcpyHostToDevice, ctx->stream));
-    } else {
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, b, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->b.p, b, bytes,
+                                         bmem == SIMALL_MEM_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice,
+                                         ctx->stream));
+    {
+        SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
+        k_check_finite<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->flag.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int h = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, s->flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (h)
+            return fail(ctx, SIMALL_ERR_NON_FINITE, "b contains NaN or Inf");
     }
     simall_solver_stats local{};
     int st;

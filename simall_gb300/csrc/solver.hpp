@@ -35,9 +35,13 @@ struct simall_solver {
     const int32_t *rowPtr = nullptr;
     const int32_t *colIdx = nullptr;
     const double *values = nullptr;
-    simall::DevBuf<int32_t> own_rowPtr, own_colIdx;
+    // the current pattern (always a private device copy) and the staging pair
+    // a new pattern is uploaded into before it is compared with the current one
+    simall::DevBuf<int32_t> own_rowPtr, own_colIdx, new_rowPtr, new_colIdx;
     simall::DevBuf<double> own_values;
-    std::vector<int32_t> h_rowPtr, h_colIdx;
+    std::vector<int32_t> h_rowPtr, h_colIdx;  // host copy of the pattern, filled on demand
+    bool h_pattern_valid = false;
+    bool have_pattern = false;
     simall::DevBuf<int32_t> rowBlocks;
     int nRowBlocks = 0;
     simall::DevBuf<double> invDiag, x, r, p, Ap, z, b;
@@ -68,6 +72,9 @@ void mixed_free(simall_solver *s);
 
 // simall_solver_solve with separate memory kinds for b and x.
 int solver_solve_impl(simall_solver *s, const double *b, int bmem, double *x, int xmem, simall_solver_stats *stats);
+
+// Host copy of the current pattern (ILU0 level analysis, CSR fallbacks).
+int solver_host_pattern(simall_solver *s);
 
 // Shared by the FP64 and mixed paths.
 int solver_true_residual(simall_solver *s, const double *x, const double *b, double *r, double *rr);
