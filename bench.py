@@ -442,13 +442,13 @@ def run_ours(a, rank, world, local):
     # per-kernel CUDA-event timings (roofline)
     peak, peak_kind = measured_peaks()
     kern = {}
-    for name, solver, k in [("mixed_spmv_pq", smx, 4), ("mixed_update", smx, 5), ("mixed_dir", smx, 6),
+    for name, solver, k in [("mixed_spmv_pq", smx, 4), ("mixed_update", smx, 5),
                             ("fp64_spmv", s64, 0), ("fp64_spmv_pap", s64, 1), ("fp64_update", s64, 2),
                             ("fp64_dir", s64, 3)]:
         ms, by = time_kernel(solver, k)
         kern[name] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6}
     # dominant kernel of the mixed solve: largest time per iteration
-    dom = max(("mixed_spmv_pq", "mixed_update", "mixed_dir"), key=lambda k: kern[k]["ms"])
+    dom = max(("mixed_spmv_pq", "mixed_update"), key=lambda k: kern[k]["ms"])
     rl = {"bound": "hbm", "kernel": dom, "achieved": round(kern[dom]["gbs"], 1), "peak": peak,
           "unit": "GB/s", "frac": round(kern[dom]["gbs"] / peak, 4), "traffic": None,
           "peak_source": f"{peak_kind} hbm_gbs"}

@@ -45,7 +45,7 @@ struct MixedData {
     DevBuf<int32_t> ocol;
     DevBuf<float> oval;
     DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
-    DevBuf<float> xh, rh, ph, qh;
+    DevBuf<float> xh, rh, ph, ph2, qh;  // ph / ph2: the direction, double-buffered
     int nnzOff = 0;
     bool patternReady = false;
     std::vector<int32_t> h_orow, h_ocol, h_opos;  // csr: host pattern and the source position of each entry
@@ -142,7 +142,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_csr(int nOff, const int32_t
 }
 
 // ---------------------------------------------------------------- iteration kernels
-// Init: x = 0, rh = S b, ph = rh, xh = 0; rho = rh.rh, ||b||.
+// Init: x = 0, rh = S b, ph = 0, beta = 0, xh = 0; rho = rh.rh, ||b||.
 __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__restrict__ b,
                                                     const double *__restrict__ sc, double *__restrict__ x,
                                                     float *__restrict__ rh, float *__restrict__ ph,
@@ -155,7 +155,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         const float r = static_cast<float>(bi * sc[i]);
         x[i] = 0.0;
         rh[i] = r;
-        ph[i] = r;
+        ph[i] = 0.0f;  // the first SpMV forms p = r + 0 * p
         xh[i] = 0.0f;
         a0 += r * r;
         a1 += bi * bi;
@@ -170,6 +170,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         s->t0 = bn / s->bnorm;
         s->last = s->t0;
         s->rr = acc[1];
+        s->beta = 0.0;
         s->iter = 0;
         s->updates = 0;
         s->need_update = 0;
@@ -215,20 +216,37 @@ __device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
     y[3] += a.w * b.w;
 }
 
-// K1 (dia): qh = (S A S) ph, pq = ph.qh.  ND upper diagonals at ascending
-// offsets; row i reads U_d[i] x_{i+off} and, by symmetry, U_d[i-off] x_{i-off}.
-// One thread per 4 consecutive rows, a warp per 128 consecutive rows, with
-// 128-bit loads of every 16-byte aligned stream.  The unit-offset diagonal
-// (every natural-order grid has one) takes x_{i-1}, x_{i+4} and U_0[i-1] from
-// the neighbouring lanes' registers instead of 12 unaligned loads.  Warps
-// that touch the first or last maxoff rows take the bounds-checked path.
-template <int ND>
+// The direction p = r + beta p_old of the next iteration, formed wherever it
+// is needed with one fused multiply-add, so every thread that forms a given
+// p_i gets the same bits.
+__device__ __forceinline__ float dir(float r, float po, float beta) { return __fmaf_rn(beta, po, r); }
+__device__ __forceinline__ float4 dir4(float4 r, float4 po, float beta)
+{
+    return make_float4(dir(r.x, po.x, beta), dir(r.y, po.y, beta), dir(r.z, po.z, beta), dir(r.w, po.w, beta));
+}
+
+// K1 (dia): p = r + beta p_old (written to p_new), q = (S A S) p, p.q.  ND
+// upper diagonals at ascending offsets; row i reads U_d[i] p_{i+off} and, by
+// symmetry, U_d[i-off] p_{i-off}, each p formed from r and p_old on the fly.
+// One thread per 4 consecutive rows, a warp per 128 consecutive rows, 128-bit
+// loads of every 16-byte aligned stream.  Warps that touch the first or last
+// maxoff rows take the bounds-checked path.
+//
+// GRID (offset 1 is the first diagonal and every other offset is a multiple
+// of 4, as on any natural-order structured grid with a row length divisible
+// by 4): every load of a warp's 128 rows is issued before the first
+// multiply, so one memory round trip covers all diagonals; p_{i-1}, p_{i+4}
+// and U_0[i-1] come from the neighbouring lanes' registers, the warp's two
+// edge lanes load them.  Otherwise each diagonal loads as it goes.
+template <int ND, bool GRID>
 __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
-                                                        const float *__restrict__ ph, float *__restrict__ qh,
+                                                        const float *__restrict__ rh, const float *__restrict__ pold,
+                                                        float *__restrict__ pnew, float *__restrict__ qh,
                                                         double *partials, SolveScalars *s)
 {
     if (ld_flag(&s->done))
         return;
+    const float beta = static_cast<float>(__ldcg(&s->beta));
     float acc = 0.0f;
     const int nq = (n + 3) >> 2;
     const int maxoff = o.off[ND - 1];
@@ -238,33 +256,68 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaO
         const int q = q0 + lane;
         const int i = q << 2;
         const bool fast = q < nq && i >= maxoff && i + 3 + maxoff < n;
-        if (__all_sync(0xffffffffu, fast)) {
-            const float4 p4 = __ldg(reinterpret_cast<const float4 *>(ph + i));
+        if (GRID && __all_sync(0xffffffffu, fast)) {
+            // loads: own rows, every diagonal, the far neighbours, the edge lanes' scalars
+            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(rh + i));
+            const float4 o4 = __ldg(reinterpret_cast<const float4 *>(pold + i));
+            float4 u[ND];
+#pragma unroll
+            for (int d = 0; d < ND; ++d)
+                u[d] = __ldg(reinterpret_cast<const float4 *>(U + d * ldU + i));
+            float4 rp[ND > 1 ? ND - 1 : 1], op[ND > 1 ? ND - 1 : 1], rm[ND > 1 ? ND - 1 : 1],
+                om[ND > 1 ? ND - 1 : 1], um[ND > 1 ? ND - 1 : 1];
+#pragma unroll
+            for (int d = 1; d < ND; ++d) {
+                const int off = o.off[d];
+                rp[d - 1] = __ldg(reinterpret_cast<const float4 *>(rh + i + off));
+                op[d - 1] = __ldg(reinterpret_cast<const float4 *>(pold + i + off));
+                rm[d - 1] = __ldg(reinterpret_cast<const float4 *>(rh + i - off));
+                om[d - 1] = __ldg(reinterpret_cast<const float4 *>(pold + i - off));
+                um[d - 1] = __ldg(reinterpret_cast<const float4 *>(U + d * ldU + i - off));
+            }
+            // lane 0 needs row i-1, lane 31 row i+4 (both inside [0, n) on this path)
+            const int ie = lane == 0 ? i - 1 : i + 4;
+            const float re = __ldg(rh + ie), oe = __ldg(pold + ie), ue = __ldg(U + (i - 1));
+            // compute
+            const float4 p4 = dir4(r4, o4, beta);
+            *reinterpret_cast<float4 *>(pnew + i) = p4;
+            float y[4] = {p4.x, p4.y, p4.z, p4.w};
+            {
+                const float pe = dir(re, oe, beta);
+                float pn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // p[i+4]
+                float pp = __shfl_up_sync(0xffffffffu, p4.w, 1);    // p[i-1]
+                float up = __shfl_up_sync(0xffffffffu, u[0].w, 1);  // U_0[i-1]
+                if (lane == 31)
+                    pn = pe;
+                if (lane == 0) {
+                    pp = pe;
+                    up = ue;
+                }
+                y[0] += u[0].x * p4.y + up * pp;
+                y[1] += u[0].y * p4.z + u[0].x * p4.x;
+                y[2] += u[0].z * p4.w + u[0].y * p4.y;
+                y[3] += u[0].w * pn + u[0].z * p4.z;
+            }
+#pragma unroll
+            for (int d = 1; d < ND; ++d) {
+                fma4(y, u[d], dir4(rp[d - 1], op[d - 1], beta));
+                fma4(y, um[d - 1], dir4(rm[d - 1], om[d - 1], beta));
+            }
+            *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
+            acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
+        } else if (!GRID && __all_sync(0xffffffffu, fast)) {
+            const float4 p4 = dir4(__ldg(reinterpret_cast<const float4 *>(rh + i)),
+                                   __ldg(reinterpret_cast<const float4 *>(pold + i)), beta);
+            *reinterpret_cast<float4 *>(pnew + i) = p4;
             float y[4] = {p4.x, p4.y, p4.z, p4.w};
 #pragma unroll
             for (int d = 0; d < ND; ++d) {
                 const int off = o.off[d];
                 const float *Ud = U + d * ldU;
-                const float4 u = __ldg(reinterpret_cast<const float4 *>(Ud + i));
-                if (off == 1) {
-                    float xn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // x[i+4]
-                    float xp = __shfl_up_sync(0xffffffffu, p4.w, 1);    // x[i-1]
-                    float up = __shfl_up_sync(0xffffffffu, u.w, 1);     // U_0[i-1]
-                    if (lane == 31)
-                        xn = __ldg(ph + i + 4);
-                    if (lane == 0) {
-                        xp = __ldg(ph + i - 1);
-                        up = __ldg(Ud + i - 1);
-                    }
-                    y[0] += u.x * p4.y + up * xp;
-                    y[1] += u.y * p4.z + u.x * p4.x;
-                    y[2] += u.z * p4.w + u.y * p4.y;
-                    y[3] += u.w * xn + u.z * p4.z;
-                } else {
-                    const bool al = (off & 3) == 0;
-                    fma4(y, u, ld4(ph + i + off, al));
-                    fma4(y, ld4(Ud + i - off, al), ld4(ph + i - off, al));
-                }
+                const bool al = (off & 3) == 0;
+                fma4(y, __ldg(reinterpret_cast<const float4 *>(Ud + i)),
+                     dir4(ld4(rh + i + off, al), ld4(pold + i + off, al), beta));
+                fma4(y, ld4(Ud + i - off, al), dir4(ld4(rh + i - off, al), ld4(pold + i - off, al), beta));
             }
             *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
             acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
@@ -273,16 +326,17 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaO
                 const int row = i + r;
                 if (row >= n)
                     break;
-                const float pr = __ldg(ph + row);
+                const float pr = dir(__ldg(rh + row), __ldg(pold + row), beta);
+                pnew[row] = pr;
                 float v = pr;
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
                     const int off = o.off[d];
                     const float *Ud = U + d * ldU;
                     if (row + off < n)
-                        v += __ldg(Ud + row) * __ldg(ph + row + off);
+                        v += __ldg(Ud + row) * dir(__ldg(rh + row + off), __ldg(pold + row + off), beta);
                     if (row - off >= 0)
-                        v += __ldg(Ud + row - off) * __ldg(ph + row - off);
+                        v += __ldg(Ud + row - off) * dir(__ldg(rh + row - off), __ldg(pold + row - off), beta);
                 }
                 qh[row] = v;
                 acc += pr * v;
@@ -294,20 +348,25 @@ __global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaO
         mx_alpha(s, total);
 }
 
-// K1 (csr): qh = ph + offdiag(S A S) ph, pq = ph.qh.  Thread per row.
+// K1 (csr): p = r + beta p_old, q = p + offdiag(S A S) p, p.q.  Thread per row.
 __global__ void __launch_bounds__(kBlock) k_mx_spmv_csr(int64_t n, const int32_t *__restrict__ orow,
                                                         const int32_t *__restrict__ ocol,
-                                                        const float *__restrict__ oval, const float *__restrict__ ph,
+                                                        const float *__restrict__ oval, const float *__restrict__ rh,
+                                                        const float *__restrict__ pold, float *__restrict__ pnew,
                                                         float *__restrict__ qh, double *partials, SolveScalars *s)
 {
     if (ld_flag(&s->done))
         return;
+    const float beta = static_cast<float>(__ldcg(&s->beta));
     float acc = 0.0f;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float pi = __ldg(ph + i);
+        const float pi = dir(__ldg(rh + i), __ldg(pold + i), beta);
+        pnew[i] = pi;
         float y = pi;
-        for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k)
-            y += __ldg(oval + k) * __ldg(ph + __ldg(ocol + k));
+        for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k) {
+            const int j = __ldg(ocol + k);
+            y += __ldg(oval + k) * dir(__ldg(rh + j), __ldg(pold + j), beta);
+        }
         qh[i] = y;
         acc += pi * y;
     }
@@ -442,31 +501,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_replace(int64_t n, const double *
         s->updates += 1;
     }
 }
-
-// K3: ph = rh + beta ph.
-__global__ void __launch_bounds__(kBlock) k_mx_pupdate(int64_t n, const float *__restrict__ rh, float *__restrict__ ph,
-                                                       const SolveScalars *s)
-{
-    if (ld_flag(&s->done))
-        return;
-    const float beta = static_cast<float>(__ldcg(&s->beta));
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t n4 = n >> 2;
-    for (int64_t i = tid; i < n4; i += stride) {
-        const float4 r = reinterpret_cast<const float4 *>(rh)[i];
-        float4 p = reinterpret_cast<float4 *>(ph)[i];
-        p.x = r.x + beta * p.x;
-        p.y = r.y + beta * p.y;
-        p.z = r.z + beta * p.z;
-        p.w = r.w + beta * p.w;
-        reinterpret_cast<float4 *>(ph)[i] = p;
-    }
-    for (int64_t i = 4 * n4 + tid; i < n; i += stride)
-        ph[i] = rh[i] + beta * ph[i];
-}
-
-int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *ph, float *qh, double *partials,
-                    SolveScalars *sc);
 
 int grid_n(simall_context *ctx, int64_t n)
 {
@@ -609,15 +643,23 @@ int analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
     return SIMALL_OK;
 }
 
-int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *ph, float *qh, double *partials,
+int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *pold, float *pnew, double *partials,
                     SolveScalars *sc)
 {
     const int g = grid_n(ctx, (n + 3) / 4);
     const int ni = static_cast<int>(n);
+    bool grid = m->offs.nd >= 1 && m->offs.off[0] == 1;
+    for (int d = 1; d < m->offs.nd; ++d)
+        grid = grid && (m->offs.off[d] & 3) == 0;
     switch (m->offs.nd) {
 #define SIMALL_DIA_CASE(ND)                                                                                           \
     case ND:                                                                                                          \
-        k_mx_spmv_dia<ND><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, ph, qh, partials, sc);          \
+        if (grid)                                                                                                     \
+            k_mx_spmv_dia<ND, true><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew,  \
+                                                                   m->qh.p, partials, sc);                            \
+        else                                                                                                          \
+            k_mx_spmv_dia<ND, false><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew, \
+                                                                    m->qh.p, partials, sc);                           \
         break;
         SIMALL_DIA_CASE(1)
         SIMALL_DIA_CASE(2)
@@ -656,6 +698,7 @@ int mixed_setup(simall_solver *s)
     SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
     SIMALL_CUDA_TRY(ctx, m->rh.alloc(n + 4));
     SIMALL_CUDA_TRY(ctx, m->ph.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, m->ph2.alloc(n + 4));
     SIMALL_CUDA_TRY(ctx, m->qh.alloc(n + 4));
     SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
@@ -716,22 +759,27 @@ int mixed_setup(simall_solver *s)
 
 namespace {
 
-int enqueue_mixed_iteration(simall_solver *s)
+// One iteration; `parity` selects which of ph / ph2 holds the previous
+// direction.  A solve starts at parity 0 (ph = 0) and the captured chunks have
+// even lengths, so every chunk starts at parity 0 too.
+int enqueue_mixed_iteration(simall_solver *s, int parity)
 {
     simall_context *ctx = s->ctx;
     MixedData *m = s->mixed;
     const int64_t n = s->n;
     const int g = grid_n(ctx, n);
+    const float *pold = parity ? m->ph2.p : m->ph.p;
+    float *pnew = parity ? m->ph.p : m->ph2.p;
     if (m->dia) {
-        int st = launch_spmv_dia(ctx, m, n, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
+        int st = launch_spmv_dia(ctx, m, n, pold, pnew, s->partials.p, s->scal.p);
         if (st)
             return st;
     } else {
-        k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
-                                                     s->partials.p, s->scal.p);
+        k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, pold, pnew,
+                                                     m->qh.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
     }
-    k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+    k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, pnew, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
@@ -743,12 +791,10 @@ int enqueue_mixed_iteration(simall_solver *s)
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_mx_pupdate<<<g, kBlock, 0, ctx->stream>>>(n, m->rh.p, m->ph.p, s->scal.p);
-    SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
 
-constexpr int kMixedKernelsPerIteration = 6;
+constexpr int kMixedKernelsPerIteration = 5;
 
 int run_mixed_chunk(simall_solver *s, int len)
 {
@@ -763,7 +809,7 @@ int run_mixed_chunk(simall_solver *s, int len)
     SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
     int st = SIMALL_OK;
     for (int i = 0; i < len && st == SIMALL_OK; ++i)
-        st = enqueue_mixed_iteration(s);
+        st = enqueue_mixed_iteration(s, i & 1);
     cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
     if (st)
         return st;
@@ -799,7 +845,8 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
                                                           s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     int done_iters = 0;
-    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 16;
+    // even chunk lengths keep the direction's double buffer in step
+    int chunk = s->cfg.check_interval > 0 ? (s->cfg.check_interval + 1) & ~1 : 16;
     double prev_last = -1.0;
     int prev_iter = 0;
     for (;;) {
@@ -843,21 +890,18 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     switch (k) {
     case 4:
         if (m->dia) {
-            *bytes = (4.0 * m->offs.nd + 8.0) * nd;  // U once, ph gathered once, qh written
-            return launch_spmv_dia(ctx, m, n, m->ph.p, m->qh.p, s->partials.p, s->scal.p);
+            // U once; rh and p_old gathered once; p_new and qh written
+            *bytes = (4.0 * m->offs.nd + 16.0) * nd;
+            return launch_spmv_dia(ctx, m, n, m->ph.p, m->ph2.p, s->partials.p, s->scal.p);
         } else {
-            k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->ph.p, m->qh.p,
-                                                         s->partials.p, s->scal.p);
-            *bytes = 8.0 * m->nnzOff + 12.0 * nd + 4.0;
+            k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, m->ph.p,
+                                                         m->ph2.p, m->qh.p, s->partials.p, s->scal.p);
+            *bytes = 8.0 * m->nnzOff + 20.0 * nd + 4.0;
         }
         break;
     case 5:
-        k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
-        *bytes = 24.0 * nd;  // ph, qh, xh, rh read; xh, rh written
-        break;
-    case 6:
-        k_mx_pupdate<<<g, kBlock, 0, ctx->stream>>>(n, m->rh.p, m->ph.p, s->scal.p);
-        *bytes = 12.0 * nd;  // rh, ph read; ph written
+        k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph2.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+        *bytes = 24.0 * nd;  // p, qh, xh, rh read; xh, rh written
         break;
     default:
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);

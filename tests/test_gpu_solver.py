@@ -114,9 +114,12 @@ def test_ilu0_factor_and_apply_bit_exact(sg, ctx, oracle):
     assert bits_equal(tz.cpu().numpy(), oracle.ilu0_apply(rp, ci, lu, dp, r))
 
 
-@pytest.mark.parametrize("zones", [(), (1,)])
-def test_mixed_precision_reaches_tolerance(sg, ctx, oracle, zones):
-    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 16, pressure_zones=zones, renumber=False, amp=0.0)
+@pytest.mark.parametrize("zones,dims", [((), (16, 16, 16)), ((1,), (16, 16, 16)), ((1,), (13, 11, 9)),
+                                        ((), (7, 5, 3))])
+def test_mixed_precision_reaches_tolerance(sg, ctx, oracle, zones, dims):
+    """Natural order: diagonal storage.  Row lengths that are multiples of 4
+    take the grid SpMV (all loads first), others the general one."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, pressure_zones=zones, renumber=False, amp=0.0, dims=dims)
     xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 0, 1e-12, 5000)
     s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx)
     x = np.zeros(len(rhs))
