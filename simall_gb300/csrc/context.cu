@@ -85,6 +85,27 @@ int check_csr_host(simall_context *ctx, int64_t n, int64_t nnz, const int32_t *r
 
 int grid_size_streaming(simall_context *ctx) { return ctx->num_sms * (2048 / kBlock); }
 
+int resident_grid(simall_context *ctx, const void *kernel, int64_t items)
+{
+    int per_sm = 0;
+    {
+        std::lock_guard<std::mutex> lock(ctx->occupancy_mu);
+        auto it = ctx->resident_per_sm.find(kernel);
+        if (it != ctx->resident_per_sm.end()) {
+            per_sm = it->second;
+        } else {
+            if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, 0) != cudaSuccess)
+                per_sm = 0;
+            if (per_sm < 1 || per_sm > 2048 / kBlock)
+                per_sm = per_sm < 1 ? 1 : 2048 / kBlock;
+            ctx->resident_per_sm.emplace(kernel, per_sm);
+        }
+    }
+    const int64_t g = (items + kBlock - 1) / kBlock;
+    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * per_sm;
+    return static_cast<int>(g < 1 ? 1 : (g < cap ? g : cap));
+}
+
 }  // namespace simall
 
 extern "C" {

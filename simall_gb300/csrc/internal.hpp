@@ -9,7 +9,9 @@
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
+#include <mutex>
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 struct simall_context {
@@ -19,6 +21,8 @@ struct simall_context {
     bool own_stream = false;
     std::string last_error;
     std::atomic<int64_t> launches{0};
+    std::mutex occupancy_mu;
+    std::unordered_map<const void *, int> resident_per_sm;  // kernel -> resident CTAs of kBlock threads per SM
 };
 
 namespace simall {
@@ -117,5 +121,11 @@ int check_csr_host(simall_context *ctx, int64_t n, int64_t nnz, const int32_t *r
 
 // CTAs of a full-occupancy streaming grid (8 x 256 threads per SM).
 int grid_size_streaming(simall_context *ctx);
+// Grid of a grid-stride kernel launched with kBlock threads: exactly one wave
+// of resident CTAs (SMs x the kernel's resident CTAs per SM, from its register
+// and shared-memory use), or fewer when `items` threads' worth of work is
+// smaller.  A second, partial wave would leave most SMs idle at the end of
+// every launch.  Never larger than grid_size_streaming.
+int resident_grid(simall_context *ctx, const void *kernel, int64_t items);
 
 }  // namespace simall

@@ -646,7 +646,7 @@ int analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
 int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *pold, float *pnew, double *partials,
                     SolveScalars *sc)
 {
-    const int g = grid_n(ctx, (n + 3) / 4);
+    const int64_t quads = (n + 3) / 4;
     const int ni = static_cast<int>(n);
     bool grid = m->offs.nd >= 1 && m->offs.off[0] == 1;
     for (int d = 1; d < m->offs.nd; ++d)
@@ -654,12 +654,15 @@ int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *p
     switch (m->offs.nd) {
 #define SIMALL_DIA_CASE(ND)                                                                                           \
     case ND:                                                                                                          \
-        if (grid)                                                                                                     \
+        if (grid) {                                                                                                   \
+            const int g = resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_dia<ND, true>), quads);         \
             k_mx_spmv_dia<ND, true><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew,  \
                                                                    m->qh.p, partials, sc);                            \
-        else                                                                                                          \
+        } else {                                                                                                      \
+            const int g = resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_dia<ND, false>), quads);        \
             k_mx_spmv_dia<ND, false><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew, \
                                                                     m->qh.p, partials, sc);                           \
+        }                                                                                                             \
         break;
         SIMALL_DIA_CASE(1)
         SIMALL_DIA_CASE(2)
@@ -767,7 +770,6 @@ int enqueue_mixed_iteration(simall_solver *s, int parity)
     simall_context *ctx = s->ctx;
     MixedData *m = s->mixed;
     const int64_t n = s->n;
-    const int g = grid_n(ctx, n);
     const float *pold = parity ? m->ph2.p : m->ph.p;
     float *pnew = parity ? m->ph.p : m->ph2.p;
     if (m->dia) {
@@ -775,19 +777,22 @@ int enqueue_mixed_iteration(simall_solver *s, int parity)
         if (st)
             return st;
     } else {
-        k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, pold, pnew,
-                                                     m->qh.p, s->partials.p, s->scal.p);
+        k_mx_spmv_csr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_csr), n), kBlock, 0,
+                        ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, pold, pnew, m->qh.p,
+                                       s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
     }
-    k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, pnew, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+    k_mx_update<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_update), (n + 3) / 4), kBlock, 0,
+                  ctx->stream>>>(n, pnew, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
+    // the reliable-update kernels return at once unless an update is due
+    const int g = grid_n(ctx, n);
     k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    const int cap = grid_size_streaming(ctx);
-    const int gs = s->nRowBlocks < cap ? s->nRowBlocks : cap;
-    k_mx_true_residual<<<gs < 1 ? 1 : gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p,
-                                                                    s->nRowBlocks, s->x.p, s->b.p, s->r.p,
-                                                                    s->partials.p, s->scal.p);
+    k_mx_true_residual<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_true_residual),
+                                       static_cast<int64_t>(s->nRowBlocks) * kBlock),
+                         kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
+                                                   s->x.p, s->b.p, s->r.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
@@ -885,7 +890,6 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     simall_context *ctx = s->ctx;
     MixedData *m = s->mixed;
     const int64_t n = s->n;
-    const int g = grid_n(ctx, n);
     const double nd = static_cast<double>(n);
     switch (k) {
     case 4:
@@ -894,13 +898,15 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
             *bytes = (4.0 * m->offs.nd + 16.0) * nd;
             return launch_spmv_dia(ctx, m, n, m->ph.p, m->ph2.p, s->partials.p, s->scal.p);
         } else {
-            k_mx_spmv_csr<<<g, kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, m->ph.p,
-                                                         m->ph2.p, m->qh.p, s->partials.p, s->scal.p);
+            k_mx_spmv_csr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_csr), n), kBlock, 0,
+                            ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, m->ph.p, m->ph2.p, m->qh.p,
+                                           s->partials.p, s->scal.p);
             *bytes = 8.0 * m->nnzOff + 20.0 * nd + 4.0;
         }
         break;
     case 5:
-        k_mx_update<<<g, kBlock, 0, ctx->stream>>>(n, m->ph2.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
+        k_mx_update<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_update), (n + 3) / 4), kBlock, 0,
+                      ctx->stream>>>(n, m->ph2.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
         *bytes = 24.0 * nd;  // p, qh, xh, rh read; xh, rh written
         break;
     default:

@@ -508,24 +508,28 @@ void drop_graphs(simall_solver *s)
 int enqueue_iteration(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
-    const int g = grid_for(ctx, s->n), gs = spmv_grid(ctx, s->nRowBlocks);
-    k_spmv_pap<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
-                                                 s->p.p, s->Ap.p, s->partials.p, s->scal.p);
+    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    k_spmv_pap<<<resident_grid(ctx, reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0, ctx->stream>>>(
+        s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
-        k_update_xr<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
+        k_update_xr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_update_xr), n), kBlock, 0, ctx->stream>>>(
+            n, s->p.p, s->Ap.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         int st = ilu_apply(s, s->r.p, s->z.p);
         if (st)
             return st;
-        k_rz_beta<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->z.p, s->partials.p, s->scal.p);
+        k_rz_beta<<<resident_grid(ctx, reinterpret_cast<const void *>(k_rz_beta), n), kBlock, 0, ctx->stream>>>(
+            n, s->r.p, s->z.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
     } else {
-        k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p, s->z.p,
-                                                       s->partials.p, s->scal.p);
+        k_update_jacobi<<<resident_grid(ctx, reinterpret_cast<const void *>(k_update_jacobi), n), kBlock, 0,
+                          ctx->stream>>>(n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p, s->z.p, s->partials.p,
+                                         s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
     }
-    k_pupdate<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
+    k_pupdate<<<resident_grid(ctx, reinterpret_cast<const void *>(k_pupdate), n), kBlock, 0, ctx->stream>>>(
+        n, s->z.p, s->p.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
@@ -985,28 +989,31 @@ int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms
     sc.beta = 0.5;
     // the vectors keep the data of the last solve (p.Ap != 0 keeps K1 running)
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->scal.p, &sc, sizeof(sc), cudaMemcpyHostToDevice, ctx->stream));
-    const int g = grid_for(ctx, s->n), gs = spmv_grid(ctx, s->nRowBlocks);
+    const int64_t rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    auto rg = [&](const void *fn, int64_t items) { return resident_grid(ctx, fn, items); };
     const double nd = static_cast<double>(s->n), nz = static_cast<double>(s->nnz);
     double b = 0.0;
     auto launch = [&]() -> int {
         switch (kernel) {
         case 0:
-            k_spmv_plain<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p,
-                                                         s->nRowBlocks, s->p.p, s->Ap.p);
+            k_spmv_plain<<<rg(reinterpret_cast<const void *>(k_spmv_plain), rbThreads), kBlock, 0, ctx->stream>>>(
+                s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p);
             b = 12.0 * nz + 20.0 * nd + 4.0;
             break;
         case 1:
-            k_spmv_pap<<<gs, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
-                                                       s->p.p, s->Ap.p, s->partials.p, s->scal.p);
+            k_spmv_pap<<<rg(reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0, ctx->stream>>>(
+                s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p, s->partials.p,
+                s->scal.p);
             b = 12.0 * nz + 20.0 * nd + 4.0;
             break;
         case 2:
-            k_update_jacobi<<<g, kBlock, 0, ctx->stream>>>(s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p,
-                                                           s->z.p, s->partials.p, s->scal.p);
+            k_update_jacobi<<<rg(reinterpret_cast<const void *>(k_update_jacobi), s->n), kBlock, 0, ctx->stream>>>(
+                s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p, s->z.p, s->partials.p, s->scal.p);
             b = 64.0 * nd;  // p, Ap, invD, x, r read; x, r, z written
             break;
         case 3:
-            k_pupdate<<<g, kBlock, 0, ctx->stream>>>(s->n, s->z.p, s->p.p, s->scal.p);
+            k_pupdate<<<rg(reinterpret_cast<const void *>(k_pupdate), s->n), kBlock, 0, ctx->stream>>>(
+                s->n, s->z.p, s->p.p, s->scal.p);
             b = 24.0 * nd;  // z, p read; p written
             break;
         default:
