@@ -150,8 +150,8 @@ int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem);
  * bytes one launch moves (each array counted once per use, ideal reuse of
  * gathered vectors).  kernel: 0 FP64 CSR SpMV, 1 FP64 SpMV + p.Ap,
  * 2 FP64 Jacobi update (x, r, z, norms), 3 FP64 direction update,
- * 4 mixed FP32 direction update + SpMV + p.q, 5 mixed update.
- * Kernels 4-5 need precision MIXED.  The solver's iteration state is left
+ * 4 mixed FP32 step (r, x, p updates + SpMV + the step's four sums).
+ * Kernel 4 needs precision MIXED.  The solver's iteration state is left
  * undefined; the next solve starts from scratch. */
 int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms, double *bytes);
 /* ILinearSolver::last_residual(). */

@@ -122,6 +122,55 @@ __device__ __forceinline__ bool grid_sum_last_f(float v, double *partials, unsig
     return true;
 }
 
+// grid_sum_last_f for NV values at once (partials[k*gridDim.x + b]); the
+// totals land in thread 0's `total`.
+template <int NV>
+__device__ __forceinline__ bool grid_sum_last_fv(const float (&v)[NV], double *partials, unsigned *ticket,
+                                                 double (&total)[NV])
+{
+    __shared__ double wsum[NV][32];
+    __shared__ unsigned s_last;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        const float w = warp_sum_f(v[k]);
+        if (lane == 0)
+            wsum[k][wid] = static_cast<double>(w);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k) {
+            double b = 0.0;
+            for (int w = 0; w < nw; ++w)
+                b += wsum[k][w];
+            partials[k * gridDim.x + blockIdx.x] = b;
+        }
+        __threadfence();
+        const unsigned t = atomicAdd(ticket, 1u);
+        s_last = (t == gridDim.x - 1) ? 1u : 0u;
+    }
+    __syncthreads();
+    if (!s_last)
+        return false;
+    __threadfence();
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        acc[k] = 0.0;
+        for (unsigned b = threadIdx.x; b < gridDim.x; b += blockDim.x)
+            acc[k] += __ldcg(&partials[k * gridDim.x + b]);
+    }
+    block_sum<NV>(acc);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            total[k] = acc[k];
+        *ticket = 0u;
+    }
+    return true;
+}
+
 // y-rows of A x for the row-blocks this CTA owns (blockIdx.x, +gridDim.x, ...).
 // Each product a_ij*x_j is rounded once into shared memory and every row is
 // summed from 0.0 in column order with separate roundings, the same operation

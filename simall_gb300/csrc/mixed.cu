@@ -45,9 +45,11 @@ struct MixedData {
     DevBuf<int32_t> ocol;
     DevBuf<float> oval;
     DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
-    DevBuf<float> xh, rh, ph, ph2, qh;  // ph / ph2: the direction, double-buffered
+    DevBuf<float> xh;         // FP32 correction, folded into x at reliable updates
+    DevBuf<float> rv[2], qv[2], pv[2];  // r, q = (S A S) p, p; double-buffered by step parity
     int nnzOff = 0;
     bool patternReady = false;
+    bool noDeviceLoop = false;  // conditional graph nodes unavailable
     std::vector<int32_t> h_orow, h_ocol, h_opos;  // csr: host pattern and the source position of each entry
     DevBuf<int32_t> opos;
 };
@@ -142,10 +144,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_csr(int nOff, const int32_t
 }
 
 // ---------------------------------------------------------------- iteration kernels
-// Init: x = 0, rh = S b, ph = 0, beta = 0, xh = 0; rho = rh.rh, ||b||.
+// Init: x = 0, r = S b (into r[0]), p_old = 0 (p[1]), xh = 0, beta = 0;
+// ||b||.  The first step is a FRESH step of parity 1 (reads r[0] and p[1]).
 __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__restrict__ b,
                                                     const double *__restrict__ sc, double *__restrict__ x,
-                                                    float *__restrict__ rh, float *__restrict__ ph,
+                                                    float *__restrict__ r0, float *__restrict__ p1,
                                                     float *__restrict__ xh, double *partials, SolveScalars *s)
 {
     float a0 = 0.0f;
@@ -154,8 +157,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         const double bi = b[i];
         const float r = static_cast<float>(bi * sc[i]);
         x[i] = 0.0;
-        rh[i] = r;
-        ph[i] = 0.0f;  // the first SpMV forms p = r + 0 * p
+        r0[i] = r;
+        p1[i] = 0.0f;
         xh[i] = 0.0f;
         a0 += r * r;
         a1 += bi * bi;
@@ -170,10 +173,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         s->t0 = bn / s->bnorm;
         s->last = s->t0;
         s->rr = acc[1];
+        s->alpha = 0.0;
         s->beta = 0.0;
         s->iter = 0;
         s->updates = 0;
-        s->need_update = 0;
+        s->need_update = 2;  // run the first (FRESH) step; not counted as an update
         s->status = SIMALL_OK;
         s->done = 0;
         s->result = 0;
@@ -186,20 +190,6 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
     }
 }
 
-// alpha from pq (shared by both storage formats).  Thread 0 of the last CTA.
-__device__ __forceinline__ void mx_alpha(SolveScalars *s, double pq)
-{
-    s->pAp = pq;
-    if (!(pq > 0.0)) {
-        // not SPD in FP32 (or exact breakdown): fold in what we have and stop
-        s->status = SIMALL_ERR_BREAKDOWN;
-        s->need_update = 1;
-        s->alpha = 0.0;
-    } else {
-        s->alpha = s->rz / pq;
-    }
-}
-
 // Four consecutive floats starting at p; p is 16-byte aligned when `aligned`.
 __device__ __forceinline__ float4 ld4(const float *__restrict__ p, bool aligned)
 {
@@ -207,6 +197,8 @@ __device__ __forceinline__ float4 ld4(const float *__restrict__ p, bool aligned)
         return __ldg(reinterpret_cast<const float4 *>(p));
     return make_float4(__ldg(p), __ldg(p + 1), __ldg(p + 2), __ldg(p + 3));
 }
+
+__device__ __forceinline__ float4 ldv4(const float *__restrict__ p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
 __device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
 {
@@ -216,213 +208,350 @@ __device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
     y[3] += a.w * b.w;
 }
 
-// The direction p = r + beta p_old of the next iteration, formed wherever it
-// is needed with one fused multiply-add, so every thread that forms a given
-// p_i gets the same bits.
-__device__ __forceinline__ float dir(float r, float po, float beta) { return __fmaf_rn(beta, po, r); }
-__device__ __forceinline__ float4 dir4(float4 r, float4 po, float beta)
+// ---------------------------------------------------------------- the fused iteration
+// One kernel per CG step.  With the step length alpha and beta of the
+// previous step (device scalars), every row forms
+//     r = r_old - alpha q_old,  p = r + beta p_old,  xh += alpha p_old,
+// then q = (S A S) p and the sums p.q, q.q, r.r, r.q.  A neighbour's p is
+// formed again from its r_old, q_old, p_old with the same two fused
+// multiply-adds, so every thread that forms p_j gets the same bits.  The
+// vectors are double-buffered (read *_in, write *_out); the host alternates
+// the two buffers between launches.
+//
+// FRESH: the step after a residual replacement (and the first step): r is
+// the replaced residual, read from r_out and not rewritten; alpha = 0.
+template <bool FRESH>
+__device__ __forceinline__ float pdir(float r, float q, float p, float alpha, float beta)
 {
-    return make_float4(dir(r.x, po.x, beta), dir(r.y, po.y, beta), dir(r.z, po.z, beta), dir(r.w, po.w, beta));
+    const float rn = FRESH ? r : __fmaf_rn(-alpha, q, r);
+    return __fmaf_rn(beta, p, rn);
 }
 
-// K1 (dia): p = r + beta p_old (written to p_new), q = (S A S) p, p.q.  ND
-// upper diagonals at ascending offsets; row i reads U_d[i] p_{i+off} and, by
-// symmetry, U_d[i-off] p_{i-off}, each p formed from r and p_old on the fly.
-// One thread per 4 consecutive rows, a warp per 128 consecutive rows, 128-bit
-// loads of every 16-byte aligned stream.  Warps that touch the first or last
-// maxoff rows take the bounds-checked path.
+template <bool FRESH>
+__device__ __forceinline__ float4 pdir4(float4 r, float4 q, float4 p, float alpha, float beta)
+{
+    return make_float4(pdir<FRESH>(r.x, q.x, p.x, alpha, beta), pdir<FRESH>(r.y, q.y, p.y, alpha, beta),
+                       pdir<FRESH>(r.z, q.z, p.z, alpha, beta), pdir<FRESH>(r.w, q.w, p.w, alpha, beta));
+}
+
+struct IterVecs {
+    const float *rin, *qin, *pin;  // step k-1
+    float *rout, *qout, *pout;     // step k
+    float *xh;
+};
+
+// Thread 0 of the last CTA: alpha = r.r / p.q and beta of the next step,
+// beta = |r - alpha q|^2 / r.r with |r - alpha q|^2 = rr - 2 alpha rq + alpha^2 qq.
+__device__ __forceinline__ void mx_step(SolveScalars *s, double pq, double qq, double rr, double rq)
+{
+    s->pAp = pq;
+    if (!(pq > 0.0) || !(rr > 0.0)) {
+        // not SPD in FP32, or exact breakdown: fold in what we have and stop
+        s->status = SIMALL_ERR_BREAKDOWN;
+        s->need_update = 1;
+        s->alpha = 0.0;
+        s->beta = 0.0;
+        return;
+    }
+    const double alpha = rr / pq;
+    const double next = rr - 2.0 * alpha * rq + alpha * alpha * qq;
+    s->alpha = alpha;
+    s->beta = (next > 0.0 ? next : 0.0) / rr;
+}
+
+// Thread 0 of the last CTA of a step.
+template <bool FRESH>
+__device__ __forceinline__ void mx_finish(SolveScalars *s, const double (&t)[4])
+{
+    const double pq = t[0], qq = t[1], rr = t[2], rq = t[3];
+    if (FRESH) {
+        // r is the replaced (true) residual; restart the update trigger
+        s->rz = rr;
+        s->sigma0 = sqrt(rr);
+        s->rmax = s->sigma0;
+        if (s->need_update == 1)
+            s->updates += 1;
+        s->need_update = 0;
+        mx_step(s, pq, qq, rr, rq);
+        return;
+    }
+    s->iter += 1;
+    const double sigma = sqrt(rr);
+    const double est = s->t0 * sigma / s->sigma0;
+    s->last = est;
+    if (s->need_update || sigma < s->delta * s->rmax || est < s->tol || s->iter >= s->max_iter) {
+        s->need_update = 1;  // fold, true residual, replacement, then a FRESH step
+        return;
+    }
+    if (sigma > s->rmax)
+        s->rmax = sigma;
+    s->rz = rr;
+    mx_step(s, pq, qq, rr, rq);
+}
+
+// Condition handles of the device-side loop (a graph WHILE node over pairs of
+// steps, each step followed by an IF node holding the reliable-update
+// kernels).  use == 0 outside that graph.
+struct CondHandles {
+    cudaGraphConditionalHandle loop;
+    cudaGraphConditionalHandle branch;
+    int use;
+    int first;  // the body's first step: clears the loop condition at entry
+};
+
+// Whether a step returns at once.  Inside the device loop a step also ends the
+// loop when the solve is done or, as a backstop that the true-residual stop
+// test makes unreachable, when the step count passes max_iter + 4.  The
+// body's first step clears the loop condition before its CTAs take their
+// reduction tickets and only a step's last CTA sets it again, so a body whose
+// steps never reach their last CTA ends the loop.
+template <bool FRESH> __device__ __forceinline__ bool mx_skip(const SolveScalars *s, const CondHandles &c)
+{
+    if (FRESH)
+        return ld_flag(&s->done) || !ld_flag(&s->need_update);
+    if (!c.use)
+        return ld_flag(&s->done);
+    const bool stop = ld_flag(&s->done) || __ldcg(&s->iter) - 4 > __ldcg(&s->max_iter);
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        if (stop)
+            cudaGraphSetConditional(c.branch, 0u);
+        if (stop || c.first)
+            cudaGraphSetConditional(c.loop, 0u);
+    }
+    return stop;
+}
+
+// Thread 0 of the last CTA of a normal step, after mx_finish: run the
+// reliable-update branch when it is due; keep looping.
+__device__ __forceinline__ void mx_signal(const SolveScalars *s, const CondHandles &c)
+{
+    if (c.use) {
+        cudaGraphSetConditional(c.branch, s->need_update ? 1u : 0u);
+        cudaGraphSetConditional(c.loop, 1u);
+    }
+}
+
+// Diagonal storage: ND upper diagonals at ascending offsets; row i reads
+// U_d[i] p_{i+off} and, by symmetry, U_d[i-off] p_{i-off}.  One thread per 4
+// consecutive rows, a warp per 128 consecutive rows, 128-bit loads of every
+// 16-byte aligned stream.  Warps that touch the first or last maxoff rows take
+// the bounds-checked path.
 //
 // GRID (offset 1 is the first diagonal and every other offset is a multiple
 // of 4, as on any natural-order structured grid with a row length divisible
-// by 4): every load of a warp's 128 rows is issued before the first
-// multiply, so one memory round trip covers all diagonals; p_{i-1}, p_{i+4}
-// and U_0[i-1] come from the neighbouring lanes' registers, the warp's two
-// edge lanes load them.  Otherwise each diagonal loads as it goes.
-template <int ND, bool GRID>
-__global__ void __launch_bounds__(kBlock) k_mx_spmv_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
-                                                        const float *__restrict__ rh, const float *__restrict__ pold,
-                                                        float *__restrict__ pnew, float *__restrict__ qh,
-                                                        double *partials, SolveScalars *s)
+// by 4): every load of a warp's 128 rows is issued before the first multiply,
+// so one memory round trip covers all diagonals; p_{i-1}, p_{i+4} and
+// U_0[i-1] come from the neighbouring lanes' registers, the warp's two edge
+// lanes load them.  Otherwise each diagonal loads as it goes.
+template <int ND, bool GRID, bool FRESH>
+__global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
+                                                        IterVecs v, double *partials, SolveScalars *s, CondHandles c)
 {
-    if (ld_flag(&s->done))
+    if (mx_skip<FRESH>(s, c))
         return;
+    const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
-    float acc = 0.0f;
+    const float *__restrict__ rs = FRESH ? v.rout : v.rin;  // where r (before this step's update) lives
+    const float *__restrict__ qs = v.qin;
+    const float *__restrict__ ps = v.pin;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // p.q, q.q, r.r, r.q
     const int nq = (n + 3) >> 2;
     const int maxoff = o.off[ND - 1];
     const int lane = threadIdx.x & 31;
     const int stride = gridDim.x * blockDim.x;
     for (int q0 = blockIdx.x * blockDim.x + threadIdx.x - lane; q0 < nq; q0 += stride) {
-        const int q = q0 + lane;
-        const int i = q << 2;
-        const bool fast = q < nq && i >= maxoff && i + 3 + maxoff < n;
-        if (GRID && __all_sync(0xffffffffu, fast)) {
-            // loads: own rows, every diagonal, the far neighbours, the edge lanes' scalars
-            const float4 r4 = __ldg(reinterpret_cast<const float4 *>(rh + i));
-            const float4 o4 = __ldg(reinterpret_cast<const float4 *>(pold + i));
-            float4 u[ND];
+        const int qd = q0 + lane;
+        const int i = qd << 2;
+        const bool fast = qd < nq && i >= maxoff && i + 3 + maxoff < n;
+        float4 r4, p4;
+        float y[4];
+        if (__all_sync(0xffffffffu, fast)) {
+            if (GRID) {
+                constexpr int NF = ND > 1 ? ND - 1 : 1;
+                const float4 ro = ldv4(rs + i), po = ldv4(ps + i);
+                const float4 qo = FRESH ? make_float4(0.f, 0.f, 0.f, 0.f) : ldv4(qs + i);
+                const float4 xo = FRESH ? make_float4(0.f, 0.f, 0.f, 0.f) : ldv4(v.xh + i);
+                float4 u[ND];
 #pragma unroll
-            for (int d = 0; d < ND; ++d)
-                u[d] = __ldg(reinterpret_cast<const float4 *>(U + d * ldU + i));
-            float4 rp[ND > 1 ? ND - 1 : 1], op[ND > 1 ? ND - 1 : 1], rm[ND > 1 ? ND - 1 : 1],
-                om[ND > 1 ? ND - 1 : 1], um[ND > 1 ? ND - 1 : 1];
+                for (int d = 0; d < ND; ++d)
+                    u[d] = ldv4(U + d * ldU + i);
+                float4 rp[NF], qp[NF], pp[NF], rm[NF], qm[NF], pm[NF], um[NF];
 #pragma unroll
-            for (int d = 1; d < ND; ++d) {
-                const int off = o.off[d];
-                rp[d - 1] = __ldg(reinterpret_cast<const float4 *>(rh + i + off));
-                op[d - 1] = __ldg(reinterpret_cast<const float4 *>(pold + i + off));
-                rm[d - 1] = __ldg(reinterpret_cast<const float4 *>(rh + i - off));
-                om[d - 1] = __ldg(reinterpret_cast<const float4 *>(pold + i - off));
-                um[d - 1] = __ldg(reinterpret_cast<const float4 *>(U + d * ldU + i - off));
-            }
-            // lane 0 needs row i-1, lane 31 row i+4 (both inside [0, n) on this path)
-            const int ie = lane == 0 ? i - 1 : i + 4;
-            const float re = __ldg(rh + ie), oe = __ldg(pold + ie), ue = __ldg(U + (i - 1));
-            // compute
-            const float4 p4 = dir4(r4, o4, beta);
-            *reinterpret_cast<float4 *>(pnew + i) = p4;
-            float y[4] = {p4.x, p4.y, p4.z, p4.w};
-            {
-                const float pe = dir(re, oe, beta);
-                float pn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // p[i+4]
-                float pp = __shfl_up_sync(0xffffffffu, p4.w, 1);    // p[i-1]
-                float up = __shfl_up_sync(0xffffffffu, u[0].w, 1);  // U_0[i-1]
-                if (lane == 31)
-                    pn = pe;
-                if (lane == 0) {
-                    pp = pe;
-                    up = ue;
+                for (int d = 1; d < ND; ++d) {
+                    const int off = o.off[d];
+                    rp[d - 1] = ldv4(rs + i + off);
+                    pp[d - 1] = ldv4(ps + i + off);
+                    rm[d - 1] = ldv4(rs + i - off);
+                    pm[d - 1] = ldv4(ps + i - off);
+                    if (!FRESH) {
+                        qp[d - 1] = ldv4(qs + i + off);
+                        qm[d - 1] = ldv4(qs + i - off);
+                    }
+                    um[d - 1] = ldv4(U + d * ldU + i - off);
                 }
-                y[0] += u[0].x * p4.y + up * pp;
-                y[1] += u[0].y * p4.z + u[0].x * p4.x;
-                y[2] += u[0].z * p4.w + u[0].y * p4.y;
-                y[3] += u[0].w * pn + u[0].z * p4.z;
-            }
+                // lane 0 needs row i-1, lane 31 row i+4 (both inside [0, n) on this path)
+                const int ie = lane == 0 ? i - 1 : i + 4;
+                const float re = __ldg(rs + ie), pe0 = __ldg(ps + ie), ue = __ldg(U + (i - 1));
+                const float qe = FRESH ? 0.0f : __ldg(qs + ie);
+                // own rows
+                r4 = FRESH ? ro
+                           : make_float4(__fmaf_rn(-alpha, qo.x, ro.x), __fmaf_rn(-alpha, qo.y, ro.y),
+                                         __fmaf_rn(-alpha, qo.z, ro.z), __fmaf_rn(-alpha, qo.w, ro.w));
+                p4 = make_float4(__fmaf_rn(beta, po.x, r4.x), __fmaf_rn(beta, po.y, r4.y),
+                                 __fmaf_rn(beta, po.z, r4.z), __fmaf_rn(beta, po.w, r4.w));
+                if (!FRESH) {
+                    *reinterpret_cast<float4 *>(v.rout + i) = r4;
+                    *reinterpret_cast<float4 *>(v.xh + i) =
+                        make_float4(__fmaf_rn(alpha, po.x, xo.x), __fmaf_rn(alpha, po.y, xo.y),
+                                    __fmaf_rn(alpha, po.z, xo.z), __fmaf_rn(alpha, po.w, xo.w));
+                }
+                *reinterpret_cast<float4 *>(v.pout + i) = p4;
+                y[0] = p4.x;
+                y[1] = p4.y;
+                y[2] = p4.z;
+                y[3] = p4.w;
+                {
+                    const float pe = pdir<FRESH>(re, qe, pe0, alpha, beta);
+                    float pn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // p[i+4]
+                    float pl = __shfl_up_sync(0xffffffffu, p4.w, 1);    // p[i-1]
+                    float ul = __shfl_up_sync(0xffffffffu, u[0].w, 1);  // U_0[i-1]
+                    if (lane == 31)
+                        pn = pe;
+                    if (lane == 0) {
+                        pl = pe;
+                        ul = ue;
+                    }
+                    y[0] += u[0].x * p4.y + ul * pl;
+                    y[1] += u[0].y * p4.z + u[0].x * p4.x;
+                    y[2] += u[0].z * p4.w + u[0].y * p4.y;
+                    y[3] += u[0].w * pn + u[0].z * p4.z;
+                }
 #pragma unroll
-            for (int d = 1; d < ND; ++d) {
-                fma4(y, u[d], dir4(rp[d - 1], op[d - 1], beta));
-                fma4(y, um[d - 1], dir4(rm[d - 1], om[d - 1], beta));
-            }
-            *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
-            acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
-        } else if (!GRID && __all_sync(0xffffffffu, fast)) {
-            const float4 p4 = dir4(__ldg(reinterpret_cast<const float4 *>(rh + i)),
-                                   __ldg(reinterpret_cast<const float4 *>(pold + i)), beta);
-            *reinterpret_cast<float4 *>(pnew + i) = p4;
-            float y[4] = {p4.x, p4.y, p4.z, p4.w};
-#pragma unroll
-            for (int d = 0; d < ND; ++d) {
-                const int off = o.off[d];
-                const float *Ud = U + d * ldU;
-                const bool al = (off & 3) == 0;
-                fma4(y, __ldg(reinterpret_cast<const float4 *>(Ud + i)),
-                     dir4(ld4(rh + i + off, al), ld4(pold + i + off, al), beta));
-                fma4(y, ld4(Ud + i - off, al), dir4(ld4(rh + i - off, al), ld4(pold + i - off, al), beta));
-            }
-            *reinterpret_cast<float4 *>(qh + i) = make_float4(y[0], y[1], y[2], y[3]);
-            acc += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
-        } else if (q < nq) {
-            for (int r = 0; r < 4; ++r) {
-                const int row = i + r;
-                if (row >= n)
-                    break;
-                const float pr = dir(__ldg(rh + row), __ldg(pold + row), beta);
-                pnew[row] = pr;
-                float v = pr;
+                for (int d = 1; d < ND; ++d) {
+                    fma4(y, u[d], pdir4<FRESH>(rp[d - 1], FRESH ? rp[d - 1] : qp[d - 1], pp[d - 1], alpha, beta));
+                    fma4(y, um[d - 1], pdir4<FRESH>(rm[d - 1], FRESH ? rm[d - 1] : qm[d - 1], pm[d - 1], alpha, beta));
+                }
+            } else {
+                const float4 ro = ldv4(rs + i), po = ldv4(ps + i);
+                const float4 qo = FRESH ? ro : ldv4(qs + i);
+                r4 = FRESH ? ro
+                           : make_float4(__fmaf_rn(-alpha, qo.x, ro.x), __fmaf_rn(-alpha, qo.y, ro.y),
+                                         __fmaf_rn(-alpha, qo.z, ro.z), __fmaf_rn(-alpha, qo.w, ro.w));
+                p4 = make_float4(__fmaf_rn(beta, po.x, r4.x), __fmaf_rn(beta, po.y, r4.y),
+                                 __fmaf_rn(beta, po.z, r4.z), __fmaf_rn(beta, po.w, r4.w));
+                if (!FRESH) {
+                    const float4 xo = ldv4(v.xh + i);
+                    *reinterpret_cast<float4 *>(v.rout + i) = r4;
+                    *reinterpret_cast<float4 *>(v.xh + i) =
+                        make_float4(__fmaf_rn(alpha, po.x, xo.x), __fmaf_rn(alpha, po.y, xo.y),
+                                    __fmaf_rn(alpha, po.z, xo.z), __fmaf_rn(alpha, po.w, xo.w));
+                }
+                *reinterpret_cast<float4 *>(v.pout + i) = p4;
+                y[0] = p4.x;
+                y[1] = p4.y;
+                y[2] = p4.z;
+                y[3] = p4.w;
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
                     const int off = o.off[d];
                     const float *Ud = U + d * ldU;
-                    if (row + off < n)
-                        v += __ldg(Ud + row) * dir(__ldg(rh + row + off), __ldg(pold + row + off), beta);
-                    if (row - off >= 0)
-                        v += __ldg(Ud + row - off) * dir(__ldg(rh + row - off), __ldg(pold + row - off), beta);
+                    const bool al = (off & 3) == 0;
+                    const float4 rp = ld4(rs + i + off, al), rm = ld4(rs + i - off, al);
+                    const float4 qp = FRESH ? rp : ld4(qs + i + off, al), qm = FRESH ? rm : ld4(qs + i - off, al);
+                    fma4(y, ldv4(Ud + i), pdir4<FRESH>(rp, qp, ld4(ps + i + off, al), alpha, beta));
+                    fma4(y, ld4(Ud + i - off, al), pdir4<FRESH>(rm, qm, ld4(ps + i - off, al), alpha, beta));
                 }
-                qh[row] = v;
-                acc += pr * v;
+            }
+            *reinterpret_cast<float4 *>(v.qout + i) = make_float4(y[0], y[1], y[2], y[3]);
+            acc[0] += p4.x * y[0] + p4.y * y[1] + p4.z * y[2] + p4.w * y[3];
+            acc[1] += y[0] * y[0] + y[1] * y[1] + y[2] * y[2] + y[3] * y[3];
+            acc[2] += r4.x * r4.x + r4.y * r4.y + r4.z * r4.z + r4.w * r4.w;
+            acc[3] += r4.x * y[0] + r4.y * y[1] + r4.z * y[2] + r4.w * y[3];
+        } else if (qd < nq) {
+            for (int k = 0; k < 4; ++k) {
+                const int row = i + k;
+                if (row >= n)
+                    break;
+                const float ro = __ldg(rs + row), po = __ldg(ps + row);
+                const float rk = FRESH ? ro : __fmaf_rn(-alpha, __ldg(qs + row), ro);
+                const float pk = __fmaf_rn(beta, po, rk);
+                if (!FRESH) {
+                    v.rout[row] = rk;
+                    v.xh[row] = __fmaf_rn(alpha, po, v.xh[row]);
+                }
+                v.pout[row] = pk;
+                float yk = pk;
+#pragma unroll
+                for (int d = 0; d < ND; ++d) {
+                    const int off = o.off[d];
+                    const float *Ud = U + d * ldU;
+                    if (row + off < n) {
+                        const int j = row + off;
+                        yk += __ldg(Ud + row) *
+                              pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                    }
+                    if (row - off >= 0) {
+                        const int j = row - off;
+                        yk += __ldg(Ud + j) *
+                              pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                    }
+                }
+                v.qout[row] = yk;
+                acc[0] += pk * yk;
+                acc[1] += yk * yk;
+                acc[2] += rk * rk;
+                acc[3] += rk * yk;
             }
         }
     }
-    double total;
-    if (grid_sum_last_f(acc, partials, &s->counter[1], total) && threadIdx.x == 0)
-        mx_alpha(s, total);
+    double t[4];
+    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
+        mx_finish<FRESH>(s, t);
+        if (!FRESH)
+            mx_signal(s, c);
+    }
 }
 
-// K1 (csr): p = r + beta p_old, q = p + offdiag(S A S) p, p.q.  Thread per row.
-__global__ void __launch_bounds__(kBlock) k_mx_spmv_csr(int64_t n, const int32_t *__restrict__ orow,
+// FP32 CSR storage of the off-diagonal part (unit diagonal).  Thread per row.
+template <bool FRESH>
+__global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t *__restrict__ orow,
                                                         const int32_t *__restrict__ ocol,
-                                                        const float *__restrict__ oval, const float *__restrict__ rh,
-                                                        const float *__restrict__ pold, float *__restrict__ pnew,
-                                                        float *__restrict__ qh, double *partials, SolveScalars *s)
+                                                        const float *__restrict__ oval, IterVecs v, double *partials,
+                                                        SolveScalars *s, CondHandles c)
 {
-    if (ld_flag(&s->done))
+    if (mx_skip<FRESH>(s, c))
         return;
+    const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
-    float acc = 0.0f;
+    const float *__restrict__ rs = FRESH ? v.rout : v.rin;
+    const float *__restrict__ qs = v.qin;
+    const float *__restrict__ ps = v.pin;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float pi = dir(__ldg(rh + i), __ldg(pold + i), beta);
-        pnew[i] = pi;
+        const float ro = __ldg(rs + i), po = __ldg(ps + i);
+        const float ri = FRESH ? ro : __fmaf_rn(-alpha, __ldg(qs + i), ro);
+        const float pi = __fmaf_rn(beta, po, ri);
+        if (!FRESH) {
+            v.rout[i] = ri;
+            v.xh[i] = __fmaf_rn(alpha, po, v.xh[i]);
+        }
+        v.pout[i] = pi;
         float y = pi;
         for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k) {
             const int j = __ldg(ocol + k);
-            y += __ldg(oval + k) * dir(__ldg(rh + j), __ldg(pold + j), beta);
+            y += __ldg(oval + k) * pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
         }
-        qh[i] = y;
-        acc += pi * y;
+        v.qout[i] = y;
+        acc[0] += pi * y;
+        acc[1] += y * y;
+        acc[2] += ri * ri;
+        acc[3] += ri * y;
     }
-    double total;
-    if (grid_sum_last_f(acc, partials, &s->counter[1], total) && threadIdx.x == 0)
-        mx_alpha(s, total);
-}
-
-// K2: xh += alpha ph, rh -= alpha qh, rr = rh.rh; decide on a reliable update.
-__global__ void __launch_bounds__(kBlock) k_mx_update(int64_t n, const float *__restrict__ ph,
-                                                      const float *__restrict__ qh, float *__restrict__ xh,
-                                                      float *__restrict__ rh, double *partials, SolveScalars *s)
-{
-    if (ld_flag(&s->done))
-        return;
-    const float alpha = static_cast<float>(__ldcg(&s->alpha));
-    float acc = 0.0f;
-    const int64_t tid = blockIdx.x * (int64_t)blockDim.x + threadIdx.x, stride = (int64_t)gridDim.x * blockDim.x;
-    const int64_t n4 = n >> 2;
-    for (int64_t i = tid; i < n4; i += stride) {
-        const float4 p = reinterpret_cast<const float4 *>(ph)[i];
-        const float4 q = reinterpret_cast<const float4 *>(qh)[i];
-        float4 x = reinterpret_cast<float4 *>(xh)[i];
-        float4 r = reinterpret_cast<float4 *>(rh)[i];
-        x.x += alpha * p.x;
-        x.y += alpha * p.y;
-        x.z += alpha * p.z;
-        x.w += alpha * p.w;
-        r.x -= alpha * q.x;
-        r.y -= alpha * q.y;
-        r.z -= alpha * q.z;
-        r.w -= alpha * q.w;
-        reinterpret_cast<float4 *>(xh)[i] = x;
-        reinterpret_cast<float4 *>(rh)[i] = r;
-        acc += r.x * r.x + r.y * r.y + r.z * r.z + r.w * r.w;
-    }
-    for (int64_t i = 4 * n4 + tid; i < n; i += stride) {
-        xh[i] += alpha * ph[i];
-        const float r = rh[i] - alpha * qh[i];
-        rh[i] = r;
-        acc += r * r;
-    }
-    double rr;
-    if (grid_sum_last_f(acc, partials, &s->counter[2], rr) && threadIdx.x == 0) {
-        s->iter += 1;
-        const double sigma = sqrt(rr);
-        const double est = s->t0 * sigma / s->sigma0;
-        s->last = est;
-        if (s->need_update || sigma < s->delta * s->rmax || est < s->tol || s->iter >= s->max_iter) {
-            s->need_update = 1;  // beta is formed after the residual replacement
-        } else {
-            s->beta = rr / s->rz;
-            s->rz = rr;
-            if (sigma > s->rmax)
-                s->rmax = sigma;
-        }
+    double t[4];
+    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
+        mx_finish<FRESH>(s, t);
+        if (!FRESH)
+            mx_signal(s, c);
     }
 }
 
@@ -478,9 +607,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_true_residual(const int32_t *__re
     }
 }
 
-// U3: rh = S r (FP32), rho_new = rh.rh; beta = rho_new / rho; reset the trigger.
+// U3: r_out = S r (FP32), beta = |S r|^2 / r.r of the last step; the FRESH
+// step that follows forms p = r_out + beta p_in and resets the trigger.
 __global__ void __launch_bounds__(kBlock) k_mx_replace(int64_t n, const double *__restrict__ sc,
-                                                       const double *__restrict__ r, float *__restrict__ rh,
+                                                       const double *__restrict__ r, float *__restrict__ rout,
                                                        double *partials, SolveScalars *s)
 {
     if (!ld_flag(&s->need_update) || ld_flag(&s->done))
@@ -488,18 +618,12 @@ __global__ void __launch_bounds__(kBlock) k_mx_replace(int64_t n, const double *
     float acc = 0.0f;
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const float v = static_cast<float>(sc[i] * r[i]);
-        rh[i] = v;
+        rout[i] = v;
         acc += v * v;
     }
     double rho;
-    if (grid_sum_last_f(acc, partials, &s->counter[4], rho) && threadIdx.x == 0) {
+    if (grid_sum_last_f(acc, partials, &s->counter[4], rho) && threadIdx.x == 0)
         s->beta = rho / s->rz;
-        s->rz = rho;
-        s->sigma0 = sqrt(rho);
-        s->rmax = s->sigma0;
-        s->need_update = 0;
-        s->updates += 1;
-    }
 }
 
 int grid_n(simall_context *ctx, int64_t n)
@@ -643,9 +767,31 @@ int analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
     return SIMALL_OK;
 }
 
-int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *pold, float *pnew, double *partials,
-                    SolveScalars *sc)
+IterVecs iter_vecs(MixedData *m, int par)
 {
+    IterVecs v;
+    v.rin = m->rv[par].p;
+    v.qin = m->qv[par].p;
+    v.pin = m->pv[par].p;
+    v.rout = m->rv[1 - par].p;
+    v.qout = m->qv[1 - par].p;
+    v.pout = m->pv[1 - par].p;
+    v.xh = m->xh.p;
+    return v;
+}
+
+template <bool FRESH>
+int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, const CondHandles &c)
+{
+    const int64_t n = s->n;
+    const IterVecs v = iter_vecs(m, par);
+    if (!m->dia) {
+        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH>);
+        k_mx_iter_csr<FRESH><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p,
+                                                                                   v, s->partials.p, s->scal.p, c);
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    }
     const int64_t quads = (n + 3) / 4;
     const int ni = static_cast<int>(n);
     bool grid = m->offs.nd >= 1 && m->offs.off[0] == 1;
@@ -655,13 +801,13 @@ int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *p
 #define SIMALL_DIA_CASE(ND)                                                                                           \
     case ND:                                                                                                          \
         if (grid) {                                                                                                   \
-            const int g = resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_dia<ND, true>), quads);         \
-            k_mx_spmv_dia<ND, true><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew,  \
-                                                                   m->qh.p, partials, sc);                            \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, true, FRESH>);                          \
+            k_mx_iter_dia<ND, true, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(                \
+                ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
         } else {                                                                                                      \
-            const int g = resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_dia<ND, false>), quads);        \
-            k_mx_spmv_dia<ND, false><<<g, kBlock, 0, ctx->stream>>>(ni, m->ldU, m->offs, m->U.p, m->rh.p, pold, pnew, \
-                                                                    m->qh.p, partials, sc);                           \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, false, FRESH>);                         \
+            k_mx_iter_dia<ND, false, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(               \
+                ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
         }                                                                                                             \
         break;
         SIMALL_DIA_CASE(1)
@@ -678,6 +824,13 @@ int launch_spmv_dia(simall_context *ctx, MixedData *m, int64_t n, const float *p
     }
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
+}
+
+// One CG step of parity `par` (reads buffers [par], writes [1 - par]).
+int launch_iter(simall_context *ctx, simall_solver *s, int par, bool fresh,
+                const CondHandles &c = CondHandles{0, 0, 0, 0})
+{
+    return fresh ? launch_iter_t<true>(ctx, s, s->mixed, par, c) : launch_iter_t<false>(ctx, s, s->mixed, par, c);
 }
 
 }  // namespace
@@ -699,10 +852,11 @@ int mixed_setup(simall_solver *s)
     }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
     SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
-    SIMALL_CUDA_TRY(ctx, m->rh.alloc(n + 4));
-    SIMALL_CUDA_TRY(ctx, m->ph.alloc(n + 4));
-    SIMALL_CUDA_TRY(ctx, m->ph2.alloc(n + 4));
-    SIMALL_CUDA_TRY(ctx, m->qh.alloc(n + 4));
+    for (int k = 0; k < 2; ++k) {
+        SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
+        SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
+        SIMALL_CUDA_TRY(ctx, m->pv[k].alloc(n + 4));
+    }
     SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
     const int g = grid_n(ctx, n);
@@ -762,30 +916,14 @@ int mixed_setup(simall_solver *s)
 
 namespace {
 
-// One iteration; `parity` selects which of ph / ph2 holds the previous
-// direction.  A solve starts at parity 0 (ph = 0) and the captured chunks have
-// even lengths, so every chunk starts at parity 0 too.
-int enqueue_mixed_iteration(simall_solver *s, int parity)
+// The reliable-update kernels after a step of parity `par`: fold, true
+// residual, replacement, FRESH step.  Each returns at once unless the step
+// raised need_update.
+int enqueue_update_branch(simall_solver *s, int par)
 {
     simall_context *ctx = s->ctx;
     MixedData *m = s->mixed;
     const int64_t n = s->n;
-    const float *pold = parity ? m->ph2.p : m->ph.p;
-    float *pnew = parity ? m->ph.p : m->ph2.p;
-    if (m->dia) {
-        int st = launch_spmv_dia(ctx, m, n, pold, pnew, s->partials.p, s->scal.p);
-        if (st)
-            return st;
-    } else {
-        k_mx_spmv_csr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_csr), n), kBlock, 0,
-                        ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, pold, pnew, m->qh.p,
-                                       s->partials.p, s->scal.p);
-        SIMALL_LAUNCH_CHECK(ctx);
-    }
-    k_mx_update<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_update), (n + 3) / 4), kBlock, 0,
-                  ctx->stream>>>(n, pnew, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
-    SIMALL_LAUNCH_CHECK(ctx);
-    // the reliable-update kernels return at once unless an update is due
     const int g = grid_n(ctx, n);
     k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
@@ -794,12 +932,101 @@ int enqueue_mixed_iteration(simall_solver *s, int parity)
                          kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
                                                    s->x.p, s->b.p, s->r.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rh.p, s->partials.p, s->scal.p);
+    k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rv[1 - par].p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    return SIMALL_OK;
+    return launch_iter(ctx, s, par, true);
+}
+
+// One step of parity `par` followed by its reliable-update kernels.  A
+// solve's first step has parity 1 and every captured chunk has an even
+// length, so every chunk starts at parity 0.
+int enqueue_mixed_iteration(simall_solver *s, int par)
+{
+    int st = launch_iter(s->ctx, s, par, false);
+    return st ? st : enqueue_update_branch(s, par);
 }
 
 constexpr int kMixedKernelsPerIteration = 5;
+constexpr int kDeviceLoop = 0;  // GraphChunk::len of the device-side loop graph
+
+// The whole iteration as one graph: WHILE(loop) { step(0); IF(b0) {update
+// branch(0)}; step(1); IF(b1) {update branch(1)} }.  The steps set the
+// conditions from the device, so a solve is one graph launch with no host
+// round trip until it has finished.
+int build_device_loop(simall_solver *s, cudaGraphExec_t *out)
+{
+    simall_context *ctx = s->ctx;
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e != cudaSuccess)
+        return cuda_fail(ctx, e, "cudaGraphCreate", __FILE__, __LINE__);
+    int st = SIMALL_OK;
+    auto check = [&](cudaError_t err, const char *what) {
+        if (err != cudaSuccess && st == SIMALL_OK)
+            st = cuda_fail(ctx, err, what, __FILE__, __LINE__);
+        return st == SIMALL_OK;
+    };
+    cudaGraphConditionalHandle loop = 0, branch[2] = {0, 0};
+    cudaGraph_t body = nullptr, arm[2] = {nullptr, nullptr};
+    if (check(cudaGraphConditionalHandleCreate(&loop, g, 1u, cudaGraphCondAssignDefault), "loop handle")) {
+        cudaGraphNodeParams wp{};
+        wp.type = cudaGraphNodeTypeConditional;
+        wp.conditional.handle = loop;
+        wp.conditional.type = cudaGraphCondTypeWhile;
+        wp.conditional.size = 1;
+        cudaGraphNode_t wn;
+        if (check(cudaGraphAddNode(&wn, g, nullptr, nullptr, 0, &wp), "while node"))
+            body = wp.conditional.phGraph_out[0];
+    }
+    for (int k = 0; k < 2 && st == SIMALL_OK; ++k)
+        check(cudaGraphConditionalHandleCreate(&branch[k], body, 0u, cudaGraphCondAssignDefault), "branch handle");
+    // the loop body: two steps, each followed by its IF node
+    if (st == SIMALL_OK &&
+        check(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
+              "capture body")) {
+        for (int par = 0; par < 2 && st == SIMALL_OK; ++par) {
+            st = launch_iter(ctx, s, par, false, CondHandles{loop, branch[par], 1, par == 0 ? 1 : 0});
+            if (st)
+                break;
+            cudaStreamCaptureStatus cs;
+            const cudaGraphNode_t *deps = nullptr;
+            size_t nd = 0;
+            if (!check(cudaStreamGetCaptureInfo(ctx->stream, &cs, nullptr, nullptr, &deps, nullptr, &nd), "capture info"))
+                break;
+            cudaGraphNodeParams ip{};
+            ip.type = cudaGraphNodeTypeConditional;
+            ip.conditional.handle = branch[par];
+            ip.conditional.type = cudaGraphCondTypeIf;
+            ip.conditional.size = 1;
+            cudaGraphNode_t in;
+            if (!check(cudaGraphAddNode(&in, body, deps, nullptr, nd, &ip), "if node"))
+                break;
+            arm[par] = ip.conditional.phGraph_out[0];
+            check(cudaStreamUpdateCaptureDependencies(ctx->stream, &in, nullptr, 1, cudaStreamSetCaptureDependencies),
+                  "capture dependencies");
+        }
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(ctx->stream, &captured);
+        check(e, "end body capture");
+    }
+    // the IF arms: the reliable-update kernels of each parity
+    for (int par = 0; par < 2 && st == SIMALL_OK; ++par) {
+        if (!check(cudaStreamBeginCaptureToGraph(ctx->stream, arm[par], nullptr, nullptr, 0,
+                                                 cudaStreamCaptureModeThreadLocal),
+                   "capture arm"))
+            break;
+        const int bst = enqueue_update_branch(s, par);
+        cudaGraph_t captured = nullptr;
+        e = cudaStreamEndCapture(ctx->stream, &captured);
+        if (bst && st == SIMALL_OK)
+            st = bst;
+        check(e, "end arm capture");
+    }
+    if (st == SIMALL_OK)
+        check(cudaGraphInstantiate(out, g, 0), "instantiate device loop");
+    cudaGraphDestroy(g);
+    return st;
+}
 
 int run_mixed_chunk(simall_solver *s, int len)
 {
@@ -846,9 +1073,42 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
                     cudaMemcpyAsync(&s->scal.p->delta, &delta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     SIMALL_CUDA_TRY(ctx,
                     cudaMemcpyAsync(&s->scal.p->max_iter, &maxit, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-    k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rh.p, m->ph.p, m->xh.p,
-                                                          s->partials.p, s->scal.p);
+    k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rv[0].p, m->pv[1].p,
+                                                          m->xh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
+    int first = launch_iter(ctx, s, 1, true);
+    if (first)
+        return first;
+    if (s->cfg.check_interval <= 0 && !m->noDeviceLoop) {
+        cudaGraphExec_t ex = nullptr;
+        for (auto &gc : s->graphs)
+            if (gc.len == kDeviceLoop)
+                ex = gc.exec;
+        if (!ex) {
+            if (build_device_loop(s, &ex) == SIMALL_OK) {
+                GraphChunk gc;
+                gc.len = kDeviceLoop;
+                gc.exec = ex;
+                s->graphs.push_back(gc);
+            } else {
+                m->noDeviceLoop = true;  // no conditional graph nodes here: poll from the host instead
+                ex = nullptr;
+                cudaGetLastError();
+            }
+        }
+        if (ex) {
+            SIMALL_CUDA_TRY(ctx, cudaGraphLaunch(ex, ctx->stream));
+            int e = solver_fetch_scalars(s);
+            if (e)
+                return e;
+            const SolveScalars &h = *s->h_scal;
+            ctx->launches.fetch_add(static_cast<int64_t>(h.iter) + 2 + 4 * (static_cast<int64_t>(h.updates) + 1),
+                                    std::memory_order_relaxed);
+            if (!h.done)
+                return fail(ctx, SIMALL_ERR_CUDA, "device loop ended before the stop test held");
+            return SIMALL_OK;
+        }
+    }
     int done_iters = 0;
     // even chunk lengths keep the direction's double buffer in step
     int chunk = s->cfg.check_interval > 0 ? (s->cfg.check_interval + 1) & ~1 : 16;
@@ -889,31 +1149,13 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
 {
     simall_context *ctx = s->ctx;
     MixedData *m = s->mixed;
-    const int64_t n = s->n;
-    const double nd = static_cast<double>(n);
-    switch (k) {
-    case 4:
-        if (m->dia) {
-            // U once; rh and p_old gathered once; p_new and qh written
-            *bytes = (4.0 * m->offs.nd + 16.0) * nd;
-            return launch_spmv_dia(ctx, m, n, m->ph.p, m->ph2.p, s->partials.p, s->scal.p);
-        } else {
-            k_mx_spmv_csr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_spmv_csr), n), kBlock, 0,
-                            ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p, m->rh.p, m->ph.p, m->ph2.p, m->qh.p,
-                                           s->partials.p, s->scal.p);
-            *bytes = 8.0 * m->nnzOff + 20.0 * nd + 4.0;
-        }
-        break;
-    case 5:
-        k_mx_update<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_update), (n + 3) / 4), kBlock, 0,
-                      ctx->stream>>>(n, m->ph2.p, m->qh.p, m->xh.p, m->rh.p, s->partials.p, s->scal.p);
-        *bytes = 24.0 * nd;  // p, qh, xh, rh read; xh, rh written
-        break;
-    default:
+    const double nd = static_cast<double>(s->n);
+    if (k != 4)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);
-    }
-    SIMALL_LAUNCH_CHECK(ctx);
-    return SIMALL_OK;
+    // r, q, p read at parity 0 and written at parity 1, xh read and written,
+    // plus the matrix (each gathered vector counted once)
+    *bytes = m->dia ? (4.0 * m->offs.nd + 32.0) * nd : 8.0 * m->nnzOff + 36.0 * nd + 4.0;
+    return launch_iter(ctx, s, 0, false);
 }
 
 void mixed_invalidate_pattern(simall_solver *s)

@@ -972,7 +972,7 @@ int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "time_kernel needs a matrix and one completed solve");
     const bool mixed = s->cfg.precision == SIMALL_PRECISION_MIXED;
     if ((kernel >= 4 && !mixed) || (kernel >= 1 && kernel <= 3 && (mixed || s->cfg.preconditioner != SIMALL_PRECOND_JACOBI)) ||
-        kernel < 0 || kernel > 5)
+        kernel < 0 || kernel > 4)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "kernel %d not available for this solver", kernel);
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     // keep every kernel doing full work: never converge, never stop

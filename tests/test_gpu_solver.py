@@ -160,6 +160,38 @@ def test_max_iterations_semantics(sg, ctx, oracle):
     assert rel(x, xo) <= 1e-12
 
 
+@pytest.mark.parametrize("dims,renumber", [((12, 12, 12), False), ((11, 9, 7), False), ((9, 8, 7), True)])
+def test_mixed_device_loop_matches_host_polling(sg, ctx, oracle, dims, renumber):
+    """The device-side loop (conditional graph nodes) and host polling every 6
+    steps launch the same kernels in the same order: identical x, iteration
+    and update counts."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=dims, renumber=renumber, pressure_zones=(1,))
+    out = []
+    for ci_ in (0, 6):
+        s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx,
+                           check_interval=ci_)
+        x = np.zeros(len(rhs))
+        it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+        out.append((it, s.stats.reliable_updates, x))
+        assert s.stats.converged and s.stats.true_residual < 1e-9
+    assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
+    assert bits_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("check_interval", [0, 4])
+def test_mixed_max_iterations(sg, ctx, oracle, check_interval):
+    """max_iterations bounds the device loop: CGSolver's return value is
+    maxIterations and the iterate is the folded FP64 x after that many steps."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 10)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-14, maxit=7), precision=sg.Precision.MIXED, ctx=ctx,
+                       check_interval=check_interval)
+    x = np.zeros(len(rhs))
+    it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    assert it == 7 and not s.stats.converged and s.stats.iterations == 7
+    tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+    assert abs(tr - s.stats.true_residual) <= 1e-6 * tr and tr < 1.0
+
+
 @pytest.mark.parametrize("bad", ["nan", "unsorted", "nodiag", "range", "rowptr"])
 def test_input_errors_are_reported(sg, ctx, oracle, bad):
     m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 4)
