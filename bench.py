@@ -44,7 +44,11 @@ SEED = 42
 # FP64 Jacobi-PCG iteration count of the seeded system above, by side length
 # (the device FP64 solve reproduces CGSolver's count; recorded from this
 # benchmark's own FP64 leg).  The reference leg scales its bounded sample by it.
-FP64_ITERATIONS = {}
+FP64_ITERATIONS = {256: 1865}
+# DRAM bytes (read + write) per row of one launch of the fused mixed step, from
+# one ncu capture at 200^3 (profiles/mixed_step_varcoef200.md: 224.2 MB read +
+# 97.3 MB written for 8,000,000 rows); scaled by the rows of the workload.
+NCU_STEP_DRAM_BYTES_PER_ROW = (224.2432e6 + 97.283328e6) / 8.0e6
 
 
 def parse():
@@ -65,6 +69,9 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=128, help="box side of the differentiation leg (0 disables it)")
     ap.add_argument("--fd-faces", type=int, default=64, help="faces checked by central differences")
     ap.add_argument("--poisson-n", type=int, default=128, help="box side of the Jacobi-vs-ILU0 leg (0 disables it)")
+    ap.add_argument("--check-interval", type=int, default=0,
+                    help="solver check_interval: 0 runs each solve as one device-side graph loop, k > 0 polls the "
+                         "stop flag from the host every k steps (chunks of captured steps)")
     return ap.parse_args()
 
 
@@ -168,10 +175,10 @@ def build_workload(n: int, ctx):
     return mesh, ps, rhs
 
 
-def solver_for(sg, ctx, ps, precision, tol, maxit):
+def solver_for(sg, ctx, ps, precision, tol, maxit, check_interval=0):
     cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
                                 tolerance=tol, maxIterations=maxit)
-    s = sg.GpuCGSolver(cfg, precision=precision, ctx=ctx)
+    s = sg.GpuCGSolver(cfg, precision=precision, ctx=ctx, check_interval=check_interval)
     from simall_gb300._lib import check
     check(s.L.simall_solver_use_pressure_system(s.handle, ps.handle), ctx.handle)
     return s
@@ -397,8 +404,8 @@ def run_ours(a, rank, world, local):
     x = torch.empty_like(b)
     xm = torch.empty_like(b)
     stream = torch.cuda.ExternalStream(ctx.stream)
-    s64 = solver_for(sg, ctx, ps, sg.Precision.FP64, a.tol, a.max_iterations)
-    smx = solver_for(sg, ctx, ps, sg.Precision.MIXED, a.tol, a.max_iterations)
+    s64 = solver_for(sg, ctx, ps, sg.Precision.FP64, a.tol, a.max_iterations, a.check_interval)
+    smx = solver_for(sg, ctx, ps, sg.Precision.MIXED, a.tol, a.max_iterations, a.check_interval)
 
     def barrier():
         torch.cuda.synchronize()
@@ -449,8 +456,11 @@ def run_ours(a, rank, world, local):
         kern[name] = {"ms": ms, "bytes": by, "gbs": by / ms / 1e6}
     # dominant kernel of the mixed solve: largest time per iteration
     dom = max(("mixed_step",), key=lambda k: kern[k]["ms"])
+    traffic = NCU_STEP_DRAM_BYTES_PER_ROW * mesh.n_cells  # natural-order grid: diagonal storage
     rl = {"bound": "hbm", "kernel": dom, "achieved": round(kern[dom]["gbs"], 1), "peak": peak,
-          "unit": "GB/s", "frac": round(kern[dom]["gbs"] / peak, 4), "traffic": None,
+          "unit": "GB/s", "frac": round(kern[dom]["gbs"] / peak, 4),
+          "traffic": round(traffic) if traffic else None, "algorithmic_bytes": round(kern[dom]["bytes"]),
+          "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 200^3 capture scaled by rows",
           "peak_source": f"{peak_kind} hbm_gbs"}
 
     # e2e: C ABI with host buffers (matrix + b in, x out, setup inside)
@@ -479,7 +489,8 @@ def run_ours(a, rank, world, local):
         "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic (seeded)",
         "config": {"workload": f"varcoef Poisson {a.n}^3 (k=exp(N(0,1)) harmonic faces, Dirichlet x=0), "
                                f"Jacobi-PCG to {a.tol:g}", "cells": int(mesh.n_cells), "nnz": int(ps.nnz),
-                   "seed": SEED, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)"},
+                   "seed": SEED, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)",
+                   "loop": "device graph loop" if a.check_interval <= 0 else f"host poll every {a.check_interval}"},
         "fp64": {"value": round(fp64_ms / 1e3, 6), "unit": "s", "iterations": int(fp64_iters),
                  "true_residual": fp64_res},
         "mixed": {"iterations": int(mx_iters), "reliable_updates": int(mx_updates), "true_residual": mx_true,

@@ -291,11 +291,12 @@ __device__ __forceinline__ void mx_finish(SolveScalars *s, const double (&t)[4])
 
 // Condition handles of the device-side loop (a graph WHILE node over pairs of
 // steps, each step followed by an IF node holding the reliable-update
-// kernels).  use == 0 outside that graph.
+// kernels).  Only the LOOP instantiation of a normal step reads them; the
+// other instantiations, identical otherwise, carry no device-side graph call
+// (host-polled chunks, kernel timing, profilers).
 struct CondHandles {
     cudaGraphConditionalHandle loop;
     cudaGraphConditionalHandle branch;
-    int use;
     int first;  // the body's first step: clears the loop condition at entry
 };
 
@@ -305,11 +306,11 @@ struct CondHandles {
 // body's first step clears the loop condition before its CTAs take their
 // reduction tickets and only a step's last CTA sets it again, so a body whose
 // steps never reach their last CTA ends the loop.
-template <bool FRESH> __device__ __forceinline__ bool mx_skip(const SolveScalars *s, const CondHandles &c)
+template <bool FRESH, bool LOOP> __device__ __forceinline__ bool mx_skip(const SolveScalars *s, const CondHandles &c)
 {
     if (FRESH)
         return ld_flag(&s->done) || !ld_flag(&s->need_update);
-    if (!c.use)
+    if (!LOOP)
         return ld_flag(&s->done);
     const bool stop = ld_flag(&s->done) || __ldcg(&s->iter) - 4 > __ldcg(&s->max_iter);
     if (blockIdx.x == 0 && threadIdx.x == 0) {
@@ -323,9 +324,9 @@ template <bool FRESH> __device__ __forceinline__ bool mx_skip(const SolveScalars
 
 // Thread 0 of the last CTA of a normal step, after mx_finish: run the
 // reliable-update branch when it is due; keep looping.
-__device__ __forceinline__ void mx_signal(const SolveScalars *s, const CondHandles &c)
+template <bool LOOP> __device__ __forceinline__ void mx_signal(const SolveScalars *s, const CondHandles &c)
 {
-    if (c.use) {
+    if (LOOP) {
         cudaGraphSetConditional(c.branch, s->need_update ? 1u : 0u);
         cudaGraphSetConditional(c.loop, 1u);
     }
@@ -343,11 +344,11 @@ __device__ __forceinline__ void mx_signal(const SolveScalars *s, const CondHandl
 // so one memory round trip covers all diagonals; p_{i-1}, p_{i+4} and
 // U_0[i-1] come from the neighbouring lanes' registers, the warp's two edge
 // lanes load them.  Otherwise each diagonal loads as it goes.
-template <int ND, bool GRID, bool FRESH>
+template <int ND, bool GRID, bool FRESH, bool LOOP>
 __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
                                                         IterVecs v, double *partials, SolveScalars *s, CondHandles c)
 {
-    if (mx_skip<FRESH>(s, c))
+    if (mx_skip<FRESH, LOOP>(s, c))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
@@ -508,18 +509,18 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
     if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
         mx_finish<FRESH>(s, t);
         if (!FRESH)
-            mx_signal(s, c);
+            mx_signal<LOOP>(s, c);
     }
 }
 
 // FP32 CSR storage of the off-diagonal part (unit diagonal).  Thread per row.
-template <bool FRESH>
+template <bool FRESH, bool LOOP>
 __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t *__restrict__ orow,
                                                         const int32_t *__restrict__ ocol,
                                                         const float *__restrict__ oval, IterVecs v, double *partials,
                                                         SolveScalars *s, CondHandles c)
 {
-    if (mx_skip<FRESH>(s, c))
+    if (mx_skip<FRESH, LOOP>(s, c))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
@@ -551,7 +552,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t
     if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
         mx_finish<FRESH>(s, t);
         if (!FRESH)
-            mx_signal(s, c);
+            mx_signal<LOOP>(s, c);
     }
 }
 
@@ -780,14 +781,14 @@ IterVecs iter_vecs(MixedData *m, int par)
     return v;
 }
 
-template <bool FRESH>
+template <bool FRESH, bool LOOP>
 int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, const CondHandles &c)
 {
     const int64_t n = s->n;
     const IterVecs v = iter_vecs(m, par);
     if (!m->dia) {
-        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH>);
-        k_mx_iter_csr<FRESH><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p,
+        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH, LOOP>);
+        k_mx_iter_csr<FRESH, LOOP><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p,
                                                                                    v, s->partials.p, s->scal.p, c);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
@@ -801,12 +802,12 @@ int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, 
 #define SIMALL_DIA_CASE(ND)                                                                                           \
     case ND:                                                                                                          \
         if (grid) {                                                                                                   \
-            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, true, FRESH>);                          \
-            k_mx_iter_dia<ND, true, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(                \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, true, FRESH, LOOP>);                          \
+            k_mx_iter_dia<ND, true, FRESH, LOOP><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(                \
                 ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
         } else {                                                                                                      \
-            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, false, FRESH>);                         \
-            k_mx_iter_dia<ND, false, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(               \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, false, FRESH, LOOP>);                         \
+            k_mx_iter_dia<ND, false, FRESH, LOOP><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(               \
                 ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
         }                                                                                                             \
         break;
@@ -827,10 +828,17 @@ int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, 
 }
 
 // One CG step of parity `par` (reads buffers [par], writes [1 - par]).
-int launch_iter(simall_context *ctx, simall_solver *s, int par, bool fresh,
-                const CondHandles &c = CondHandles{0, 0, 0, 0})
+int launch_iter(simall_context *ctx, simall_solver *s, int par, bool fresh)
 {
-    return fresh ? launch_iter_t<true>(ctx, s, s->mixed, par, c) : launch_iter_t<false>(ctx, s, s->mixed, par, c);
+    const CondHandles none{0, 0, 0};
+    return fresh ? launch_iter_t<true, false>(ctx, s, s->mixed, par, none)
+                 : launch_iter_t<false, false>(ctx, s, s->mixed, par, none);
+}
+
+// A normal step inside the device-side loop.
+int launch_loop_step(simall_context *ctx, simall_solver *s, int par, const CondHandles &c)
+{
+    return launch_iter_t<false, true>(ctx, s, s->mixed, par, c);
 }
 
 }  // namespace
@@ -985,7 +993,7 @@ int build_device_loop(simall_solver *s, cudaGraphExec_t *out)
         check(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
               "capture body")) {
         for (int par = 0; par < 2 && st == SIMALL_OK; ++par) {
-            st = launch_iter(ctx, s, par, false, CondHandles{loop, branch[par], 1, par == 0 ? 1 : 0});
+            st = launch_loop_step(ctx, s, par, CondHandles{loop, branch[par], par == 0 ? 1 : 0});
             if (st)
                 break;
             cudaStreamCaptureStatus cs;
