@@ -69,6 +69,9 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=128, help="box side of the differentiation leg (0 disables it)")
     ap.add_argument("--fd-faces", type=int, default=64, help="faces checked by central differences")
     ap.add_argument("--poisson-n", type=int, default=128, help="box side of the Jacobi-vs-ILU0 leg (0 disables it)")
+    ap.add_argument("--no-cavity", action="store_true", help="skip the 128x128 cavity pressure-step leg")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
+                    help="skip the error check against a 1e-12 FP64 solve")
     ap.add_argument("--check-interval", type=int, default=0,
                     help="solver check_interval: 0 runs each solve as one device-side graph loop, k > 0 polls the "
                          "stop flag from the host every k steps (chunks of captured steps)")
@@ -386,6 +389,63 @@ def run_poisson3d(a, ctx, sg):
     return res
 
 
+def run_cavity(a, ctx, sg, with_cpu):
+    """2-D lid-driven cavity 128x128 (Re 100, SIMPLE urfP 0.3 / urfU 0.7, 200
+    outer iterations): the pressure step of every outer iteration -- aP and
+    phi from host memory, device assembly, Jacobi-PCG to 1e-8, p' back to host
+    memory.  The systems are the reference SIMPLE loop's first and last ones
+    (tests/golden/cavity_simple_128.npz); outer iteration 0 uses the first,
+    iterations 1..199 the last (the reference's solves take 737, then 775
+    iterations every time)."""
+    from simall_gb300 import workloads as W
+
+    c = np.load(os.path.join(ROOT, "tests", "golden", "cavity_simple_128.npz"))
+    N, n_outer = int(c["N"]), int(c["n_outer"])
+    m = sg.cartesian(N, N, 1, 1.0, 1.0, 1.0 / N)
+    ps = sg.PressureSystem(m, W.CAVITY, ctx=ctx)
+    aP = [np.ascontiguousarray(c["aP"][k]) for k in range(2)]
+    phi = [np.ascontiguousarray(c["phi"][k]) for k in range(2)]
+    x = np.empty(m.n_cells)
+    res = {"workload": f"cavity {N}x{N} SIMPLE pressure steps (host aP, phi in; device assembly + Jacobi-PCG to "
+                       f"1e-8; p' out), {n_outer} outer iterations", "cells": int(m.n_cells), "nnz": int(ps.nnz)}
+    for name, prec in (("fp64", sg.Precision.FP64), ("mixed", sg.Precision.MIXED)):
+        s = sg.GpuCGSolver(sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG,
+                                                 preconditioner=sg.PreconditionerKind.Jacobi, tolerance=1e-8,
+                                                 maxIterations=1000), precision=prec, ctx=ctx)
+        for k in (0, 1):  # warm: setup, graph capture
+            ps.assemble(1.0, aP[k], phi[k])
+            ps.solve(s, x)
+        ctx.synchronize()
+        its, worst = 0, 0.0
+        t0 = time.perf_counter()
+        for i in range(n_outer):
+            k = 0 if i == 0 else 1
+            ps.assemble(1.0, aP[k], phi[k])
+            ps.solve(s, x)
+            its += int(s.stats.iterations)
+            worst = max(worst, float(s.stats.true_residual))
+        ctx.synchronize()
+        res[name] = {"value": round(time.perf_counter() - t0, 4), "unit": "s", "iterations": its,
+                     "worst_true_residual": worst}
+        s.close()
+    ps.close()
+    if with_cpu:
+        # the reference CG (the oracle's bit-identical restatement) on the same two systems, 1 host core
+        from oracle import oracle as O
+        om = O.cartesian_mesh(N, N, 1, 1.0, 1.0, 1.0 / N)
+        rp, ci = O.build_sparsity(om)
+        ts = []
+        for k in (0, 1):
+            v, rhs, _ = O.assemble(om, rp, ci, [], 1.0, aP[k], phi[k])
+            t = time.perf_counter()
+            O.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
+            ts.append(time.perf_counter() - t)
+        res["cpu_baseline"] = {"value": round(ts[0] + (n_outer - 1) * ts[1], 3), "unit": "s", "cores": 1,
+                               "kind": "port", "sample": "one CG solve of each of the two systems on 1 host core, "
+                                                         f"scaled to {n_outer} solves (solve only)"}
+    return res
+
+
 def run_ours(a, rank, world, local):
     import torch
 
@@ -483,6 +543,30 @@ def run_ours(a, rank, world, local):
         h2d = rp.nbytes + ci.nbytes + vals.nbytes + rhs.nbytes
         d2h = xh.nbytes
 
+    # accuracy: against a tight FP64 solve, and the mixed x's residual recomputed on the host (numpy)
+    accuracy = None
+    if a.accuracy:
+        s_tight = solver_for(sg, ctx, ps, sg.Precision.FP64, 1e-12, a.max_iterations)
+        xt = torch.empty_like(b)
+        s_tight.solve_into(b, xt)
+        xtn = xt.cpu().numpy()
+        s10 = solver_for(sg, ctx, ps, sg.Precision.MIXED, 1e-10, a.max_iterations)
+        x10 = torch.empty_like(b)
+        ms10, _ = timed(s10, x10, 1)
+
+        def err(v):
+            return float(np.linalg.norm(v - xtn) / np.linalg.norm(xtn))
+
+        y = np.add.reduceat(vals * xmn[ci], rp[:-1])
+        accuracy = {"reference_solve": f"FP64 Jacobi-PCG to 1e-12 ({int(s_tight.stats.iterations)} it)",
+                    "mixed_error": err(xmn), "fp64_error": err(x64),
+                    "mixed_host_residual": float(np.linalg.norm(rhs - y) / np.linalg.norm(rhs)),
+                    "mixed_1e-10": {"value": round(ms10 / 1e3, 6), "unit": "s",
+                                    "iterations": int(s10.stats.iterations), "error": err(x10.cpu().numpy()),
+                                    "true_residual": float(s10.stats.true_residual)}}
+        s_tight.close()
+        s10.close()
+
     out = {
         "metric": METRIC, "value": round(mixed_ms / 1e3, 6), "unit": "s", "n_gpus": world, "steps": a.steps,
         "warmup": a.warmup, "ms_per_step": round(mixed_ms, 3), "higher_is_better": False, "scaling": "weak",
@@ -504,12 +588,16 @@ def run_ours(a, rank, world, local):
         "clocks": clocks,
         "setup_seconds": round(setup_s, 2),
     }
+    if accuracy:
+        out["accuracy"] = accuracy
     if a.batched_systems > 0:
         out["batched"] = run_batched(a, ctx, sg)
     if a.adjoint_n > 0:
         out["adjoint"] = run_adjoint(a, ctx, sg)
     if a.poisson_n > 0:
         out["poisson3d"] = run_poisson3d(a, ctx, sg)
+    if not a.no_cavity:
+        out["cavity"] = run_cavity(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
         out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,

@@ -308,7 +308,7 @@ class RefLib:
         L.ref_precond_apply.argtypes = [C.c_int, C.c_int] + [_P] * 5
         L.ref_spmv.argtypes = [C.c_int] + [_P] * 5
         L.ref_cavity_run.restype = C.c_int
-        L.ref_cavity_run.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P]
+        L.ref_cavity_run.argtypes = [C.c_int, _D, C.c_int, C.c_int, C.c_int, C.c_int, _D, C.c_int, _P, _P]
         L.ref_cavity_fetch.argtypes = [_P] * 9
         L.ref_plugin_load.restype = _I64
         L.ref_plugin_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int)]
@@ -425,12 +425,13 @@ class RefLib:
         self.L.ref_spmv(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(x), _ptr(y))
         return y
 
-    def cavity(self, N, mu=0.01, n_outer=3, n_record=3, precond=0, tol=1e-8, max_it=1000):
-        """SIMPLE lid-driven cavity; records the first n_record pressure systems."""
+    def cavity(self, N, mu=0.01, n_outer=3, n_record=3, precond=0, tol=1e-8, max_it=1000, record_stride=0):
+        """SIMPLE lid-driven cavity; records the first n_record pressure systems
+        and, with record_stride > 0, every record_stride-th one."""
         L = self.L
         sizes = np.zeros(5, np.int64)
         secs = C.c_double(0)
-        L.ref_cavity_run(N, mu, n_outer, n_record, precond, tol, max_it, _ptr(sizes), C.byref(secs))
+        L.ref_cavity_run(N, mu, n_outer, n_record, record_stride, precond, tol, max_it, _ptr(sizes), C.byref(secs))
         nC, nnz, nF, nSolve, nRec = (int(v) for v in sizes)
         out = {
             "rowPtr": np.empty(nC + 1, np.int32), "colIdx": np.empty(nnz, np.int32),

@@ -92,7 +92,8 @@ public:
     RecordingSolver(S::LinearSolverConfig c) : inner_(S::make_cg(c)) {}
     int solve(const S::CSRMatrix& A, const Vec& b, Vec& x) override
     {
-        const bool rec = static_cast<int>(iters.size()) < nRecord;
+        const int idx = static_cast<int>(iters.size());
+        const bool rec = idx < nRecord || (recordStride > 0 && (idx + 1) % recordStride == 0);
         if (rec) {
             if (rowPtr.empty()) {
                 rowPtr.assign(A.rowPtr.begin(), A.rowPtr.end());
@@ -108,15 +109,19 @@ public:
         const auto t0 = std::chrono::steady_clock::now();
         const int it = inner_->solve(A, b, x);
         seconds += std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (rec)
+        if (rec) {
             xs.insert(xs.end(), x.begin(), x.end());
+            ++nRecorded;
+        }
         iters.push_back(it);
         res.push_back(inner_->last_residual());
         return it;
     }
     double last_residual() const override { return inner_->last_residual(); }
 
-    int nRecord = 0;
+    int nRecord = 0;       // record the first nRecord solves
+    int recordStride = 0;  // and, when > 0, every recordStride-th solve
+    int nRecorded = 0;
     const AssemblyProbe* probe = nullptr;
     std::vector<int> rowPtr, colIdx, iters;
     std::vector<double> values, rhs, xs, aP, phi, res;
@@ -299,7 +304,7 @@ void ref_spmv(int n, const int* rowPtr, const int* colIdx, const double* values,
 // with momentum GMRES(30)+ILU (tol 1e-6, 200 it) and pressure CG with the
 // given preconditioner.  The first nRecord pressure systems are recorded;
 // fetch them with ref_cavity_fetch.
-int ref_cavity_run(int N, double mu, int nOuter, int nRecord, int precond, double tol, int maxit,
+int ref_cavity_run(int N, double mu, int nOuter, int nRecord, int recordStride, int precond, double tol, int maxit,
                    std::int64_t* sizes, double* pSolveSeconds)
 {
     M::Mesh mesh;
@@ -329,6 +334,7 @@ int ref_cavity_run(int N, double mu, int nOuter, int nRecord, int precond, doubl
     delete g_last_cavity;
     g_last_cavity = new RecordingSolver(pc);
     g_last_cavity->nRecord = nRecord;
+    g_last_cavity->recordStride = recordStride;
     S::SimpleOptions o;
     o.urfU = 0.7;
     o.urfP = 0.3;
@@ -343,7 +349,7 @@ int ref_cavity_run(int N, double mu, int nOuter, int nRecord, int precond, doubl
     sizes[1] = static_cast<std::int64_t>(g_last_cavity->colIdx.size());
     sizes[2] = static_cast<std::int64_t>(mesh.faces().size());
     sizes[3] = static_cast<std::int64_t>(g_last_cavity->iters.size());
-    sizes[4] = static_cast<std::int64_t>(std::min<std::size_t>(nRecord, g_last_cavity->iters.size()));
+    sizes[4] = static_cast<std::int64_t>(g_last_cavity->nRecorded);
     if (pSolveSeconds)
         *pSolveSeconds = g_last_cavity->seconds;
     return 0;

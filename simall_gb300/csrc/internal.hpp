@@ -105,7 +105,7 @@ struct SolveScalars {
     int status;     // SIMALL_OK / SIMALL_ERR_BREAKDOWN
     int need_update;  // mixed: a reliable update is due
     int updates;      // mixed: reliable updates performed
-    int pad;
+    int seen;         // mixed device loop: iteration count the last controller saw
     unsigned counter[8];  // last-block tickets, one per kernel kind
 };
 

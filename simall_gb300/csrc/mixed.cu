@@ -19,6 +19,20 @@
 // in natural order), only the upper diagonals are stored, FP32, one array per
 // offset: 4 B per stored diagonal per row and no column indices.  Otherwise
 // the off-diagonal entries are kept as FP32 CSR.
+//
+// Row-sum form of the product.  With N the off-diagonal part of S A S and
+// e_i = 1 + sum_j N_ij (summed in FP64 from A, stored rounded to FP32), the
+// inner SpMV evaluates
+//     q_i = e_i p_i - sum_j N_ij (p_i - p_j)
+// which equals p_i + sum_j N_ij p_j.  For a pressure Laplacian the terms of
+// the plain form cancel on smooth directions (q is far smaller than p), and
+// rounding N to FP32 then moves the smallest eigenvalues of the inner operator
+// by far more than their own size; in the row-sum form the rounding only
+// perturbs the positive couplings of a Laplacian whose row sums stay exact to
+// one FP32 rounding, and the differences p_i - p_j of a smooth direction are
+// small and exact.  On the 128 x 128 cavity's pressure systems (one pinned
+// cell) the FP32 inner CG needs 1075 iterations with the plain form and 776
+// with this one, against 775 for FP64 CG; it costs one 4-byte stream per row.
 #include "device.cuh"
 #include "solver.hpp"
 
@@ -45,6 +59,7 @@ struct MixedData {
     DevBuf<int32_t> ocol;
     DevBuf<float> oval;
     DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
+    DevBuf<float> e;          // e_i = 1 + sum_j (S A S)_ij, summed in FP64 from A, then rounded
     DevBuf<float> xh;         // FP32 correction, folded into x at reliable updates
     DevBuf<float> rv[2], qv[2], pv[2];  // r, q = (S A S) p, p; double-buffered by step parity
     int nnzOff = 0;
@@ -133,6 +148,25 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_dia(int64_t n, int64_t ldU,
     }
 }
 
+// e_i = 1 + sum_{j != i} a_ij s_i s_j in FP64 (column order), rounded once to
+// FP32: the row sum of S A S, exact up to that one rounding.
+__global__ void __launch_bounds__(kBlock) k_mx_row_defect(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                          const int32_t *__restrict__ colIdx,
+                                                          const double *__restrict__ val,
+                                                          const double *__restrict__ sc, float *__restrict__ e)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double si = sc[i];
+        double sum = 1.0;
+        for (int k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {
+            const int j = colIdx[k];
+            if (j != i)
+                sum += val[k] * si * sc[j];
+        }
+        e[i] = static_cast<float>(sum);
+    }
+}
+
 __global__ void __launch_bounds__(kBlock) k_mx_build_csr(int nOff, const int32_t *__restrict__ orowOfEntry,
                                                          const int32_t *__restrict__ ocol,
                                                          const int32_t *__restrict__ opos,
@@ -178,6 +212,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         s->iter = 0;
         s->updates = 0;
         s->need_update = 2;  // run the first (FRESH) step; not counted as an update
+        s->seen = -1;
         s->status = SIMALL_OK;
         s->done = 0;
         s->result = 0;
@@ -200,12 +235,13 @@ __device__ __forceinline__ float4 ld4(const float *__restrict__ p, bool aligned)
 
 __device__ __forceinline__ float4 ldv4(const float *__restrict__ p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-__device__ __forceinline__ void fma4(float (&y)[4], float4 a, float4 b)
+// y -= a (p - pn), componentwise: one off-diagonal of the row-sum form.
+__device__ __forceinline__ void dfma4(float (&y)[4], float4 a, float4 p, float4 pn)
 {
-    y[0] += a.x * b.x;
-    y[1] += a.y * b.y;
-    y[2] += a.z * b.z;
-    y[3] += a.w * b.w;
+    y[0] = __fmaf_rn(-a.x, p.x - pn.x, y[0]);
+    y[1] = __fmaf_rn(-a.y, p.y - pn.y, y[1]);
+    y[2] = __fmaf_rn(-a.z, p.z - pn.z, y[2]);
+    y[3] = __fmaf_rn(-a.w, p.w - pn.w, y[3]);
 }
 
 // ---------------------------------------------------------------- the fused iteration
@@ -289,47 +325,35 @@ __device__ __forceinline__ void mx_finish(SolveScalars *s, const double (&t)[4])
     mx_step(s, pq, qq, rr, rq);
 }
 
-// Condition handles of the device-side loop (a graph WHILE node over pairs of
-// steps, each step followed by an IF node holding the reliable-update
-// kernels).  Only the LOOP instantiation of a normal step reads them; the
-// other instantiations, identical otherwise, carry no device-side graph call
-// (host-polled chunks, kernel timing, profilers).
+template <bool FRESH> __device__ __forceinline__ bool mx_skip(const SolveScalars *s)
+{
+    return ld_flag(&s->done) || (FRESH && !ld_flag(&s->need_update));
+}
+
+// Condition handles of the device-side loop: a graph WHILE node over pairs of
+// steps, each step followed by this controller and an IF node holding the
+// reliable-update kernels.
 struct CondHandles {
     cudaGraphConditionalHandle loop;
     cudaGraphConditionalHandle branch;
-    int first;  // the body's first step: clears the loop condition at entry
 };
 
-// Whether a step returns at once.  Inside the device loop a step also ends the
-// loop when the solve is done or, as a backstop that the true-residual stop
-// test makes unreachable, when the step count passes max_iter + 4.  The
-// body's first step clears the loop condition before its CTAs take their
-// reduction tickets and only a step's last CTA sets it again, so a body whose
-// steps never reach their last CTA ends the loop.
-template <bool FRESH, bool LOOP> __device__ __forceinline__ bool mx_skip(const SolveScalars *s, const CondHandles &c)
+// One thread after each step: run the reliable-update branch when the step
+// asked for it; keep looping unless the solve is done.  The loop also ends
+// when a step made no progress (the iteration count did not move since the
+// previous controller ran -- unreachable, since every step that is not done
+// counts) or the count passed max_iter + 4 (also unreachable: the true-
+// residual stop test ends the solve at max_iter).  Keeping the device-side
+// graph calls out of the step kernel leaves its registers to the step.
+__global__ void k_mx_control(SolveScalars *s, CondHandles c)
 {
-    if (FRESH)
-        return ld_flag(&s->done) || !ld_flag(&s->need_update);
-    if (!LOOP)
-        return ld_flag(&s->done);
-    const bool stop = ld_flag(&s->done) || __ldcg(&s->iter) - 4 > __ldcg(&s->max_iter);
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        if (stop)
-            cudaGraphSetConditional(c.branch, 0u);
-        if (stop || c.first)
-            cudaGraphSetConditional(c.loop, 0u);
-    }
-    return stop;
-}
-
-// Thread 0 of the last CTA of a normal step, after mx_finish: run the
-// reliable-update branch when it is due; keep looping.
-template <bool LOOP> __device__ __forceinline__ void mx_signal(const SolveScalars *s, const CondHandles &c)
-{
-    if (LOOP) {
-        cudaGraphSetConditional(c.branch, s->need_update ? 1u : 0u);
-        cudaGraphSetConditional(c.loop, 1u);
-    }
+    if (threadIdx.x != 0)
+        return;
+    const int iter = ld_flag(&s->iter);
+    const bool stop = ld_flag(&s->done) || iter - 4 > ld_flag(&s->max_iter) || iter == s->seen;
+    s->seen = iter;
+    cudaGraphSetConditional(c.branch, (!stop && ld_flag(&s->need_update)) ? 1u : 0u);
+    cudaGraphSetConditional(c.loop, stop ? 0u : 1u);
 }
 
 // Diagonal storage: ND upper diagonals at ascending offsets; row i reads
@@ -344,11 +368,12 @@ template <bool LOOP> __device__ __forceinline__ void mx_signal(const SolveScalar
 // so one memory round trip covers all diagonals; p_{i-1}, p_{i+4} and
 // U_0[i-1] come from the neighbouring lanes' registers, the warp's two edge
 // lanes load them.  Otherwise each diagonal loads as it goes.
-template <int ND, bool GRID, bool FRESH, bool LOOP>
-__global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
-                                                        IterVecs v, double *partials, SolveScalars *s, CondHandles c)
+template <int ND, bool GRID, bool FRESH>
+__global__ void __launch_bounds__(kBlock, 3) k_mx_iter_dia(int n, int64_t ldU, DiaOffsets o, const float *__restrict__ U,
+                                                        const float *__restrict__ e, IterVecs v, double *partials,
+                                                        SolveScalars *s)
 {
-    if (mx_skip<FRESH, LOOP>(s, c))
+    if (mx_skip<FRESH>(s))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
@@ -369,7 +394,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
         if (__all_sync(0xffffffffu, fast)) {
             if (GRID) {
                 constexpr int NF = ND > 1 ? ND - 1 : 1;
-                const float4 ro = ldv4(rs + i), po = ldv4(ps + i);
+                const float4 ro = ldv4(rs + i), po = ldv4(ps + i), e4 = ldv4(e + i);
                 const float4 qo = FRESH ? make_float4(0.f, 0.f, 0.f, 0.f) : ldv4(qs + i);
                 const float4 xo = FRESH ? make_float4(0.f, 0.f, 0.f, 0.f) : ldv4(v.xh + i);
                 float4 u[ND];
@@ -407,10 +432,10 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
                                     __fmaf_rn(alpha, po.z, xo.z), __fmaf_rn(alpha, po.w, xo.w));
                 }
                 *reinterpret_cast<float4 *>(v.pout + i) = p4;
-                y[0] = p4.x;
-                y[1] = p4.y;
-                y[2] = p4.z;
-                y[3] = p4.w;
+                y[0] = e4.x * p4.x;
+                y[1] = e4.y * p4.y;
+                y[2] = e4.z * p4.z;
+                y[3] = e4.w * p4.w;
                 {
                     const float pe = pdir<FRESH>(re, qe, pe0, alpha, beta);
                     float pn = __shfl_down_sync(0xffffffffu, p4.x, 1);  // p[i+4]
@@ -422,15 +447,14 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
                         pl = pe;
                         ul = ue;
                     }
-                    y[0] += u[0].x * p4.y + ul * pl;
-                    y[1] += u[0].y * p4.z + u[0].x * p4.x;
-                    y[2] += u[0].z * p4.w + u[0].y * p4.y;
-                    y[3] += u[0].w * pn + u[0].z * p4.z;
+                    dfma4(y, u[0], p4, make_float4(p4.y, p4.z, p4.w, pn));
+                    dfma4(y, make_float4(ul, u[0].x, u[0].y, u[0].z), p4, make_float4(pl, p4.x, p4.y, p4.z));
                 }
 #pragma unroll
                 for (int d = 1; d < ND; ++d) {
-                    fma4(y, u[d], pdir4<FRESH>(rp[d - 1], FRESH ? rp[d - 1] : qp[d - 1], pp[d - 1], alpha, beta));
-                    fma4(y, um[d - 1], pdir4<FRESH>(rm[d - 1], FRESH ? rm[d - 1] : qm[d - 1], pm[d - 1], alpha, beta));
+                    dfma4(y, u[d], p4, pdir4<FRESH>(rp[d - 1], FRESH ? rp[d - 1] : qp[d - 1], pp[d - 1], alpha, beta));
+                    dfma4(y, um[d - 1], p4,
+                          pdir4<FRESH>(rm[d - 1], FRESH ? rm[d - 1] : qm[d - 1], pm[d - 1], alpha, beta));
                 }
             } else {
                 const float4 ro = ldv4(rs + i), po = ldv4(ps + i);
@@ -448,10 +472,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
                                     __fmaf_rn(alpha, po.z, xo.z), __fmaf_rn(alpha, po.w, xo.w));
                 }
                 *reinterpret_cast<float4 *>(v.pout + i) = p4;
-                y[0] = p4.x;
-                y[1] = p4.y;
-                y[2] = p4.z;
-                y[3] = p4.w;
+                const float4 e4 = ldv4(e + i);
+                y[0] = e4.x * p4.x;
+                y[1] = e4.y * p4.y;
+                y[2] = e4.z * p4.z;
+                y[3] = e4.w * p4.w;
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
                     const int off = o.off[d];
@@ -459,8 +484,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
                     const bool al = (off & 3) == 0;
                     const float4 rp = ld4(rs + i + off, al), rm = ld4(rs + i - off, al);
                     const float4 qp = FRESH ? rp : ld4(qs + i + off, al), qm = FRESH ? rm : ld4(qs + i - off, al);
-                    fma4(y, ldv4(Ud + i), pdir4<FRESH>(rp, qp, ld4(ps + i + off, al), alpha, beta));
-                    fma4(y, ld4(Ud + i - off, al), pdir4<FRESH>(rm, qm, ld4(ps + i - off, al), alpha, beta));
+                    dfma4(y, ldv4(Ud + i), p4, pdir4<FRESH>(rp, qp, ld4(ps + i + off, al), alpha, beta));
+                    dfma4(y, ld4(Ud + i - off, al), p4, pdir4<FRESH>(rm, qm, ld4(ps + i - off, al), alpha, beta));
                 }
             }
             *reinterpret_cast<float4 *>(v.qout + i) = make_float4(y[0], y[1], y[2], y[3]);
@@ -481,20 +506,22 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
                     v.xh[row] = __fmaf_rn(alpha, po, v.xh[row]);
                 }
                 v.pout[row] = pk;
-                float yk = pk;
+                float yk = __ldg(e + row) * pk;
 #pragma unroll
                 for (int d = 0; d < ND; ++d) {
                     const int off = o.off[d];
                     const float *Ud = U + d * ldU;
                     if (row + off < n) {
                         const int j = row + off;
-                        yk += __ldg(Ud + row) *
-                              pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                        const float pj =
+                            pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                        yk = __fmaf_rn(-__ldg(Ud + row), pk - pj, yk);
                     }
                     if (row - off >= 0) {
                         const int j = row - off;
-                        yk += __ldg(Ud + j) *
-                              pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                        const float pj =
+                            pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+                        yk = __fmaf_rn(-__ldg(Ud + j), pk - pj, yk);
                     }
                 }
                 v.qout[row] = yk;
@@ -506,21 +533,18 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_dia(int n, int64_t ldU, DiaO
         }
     }
     double t[4];
-    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
+    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0)
         mx_finish<FRESH>(s, t);
-        if (!FRESH)
-            mx_signal<LOOP>(s, c);
-    }
 }
 
 // FP32 CSR storage of the off-diagonal part (unit diagonal).  Thread per row.
-template <bool FRESH, bool LOOP>
+template <bool FRESH>
 __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t *__restrict__ orow,
                                                         const int32_t *__restrict__ ocol,
-                                                        const float *__restrict__ oval, IterVecs v, double *partials,
-                                                        SolveScalars *s, CondHandles c)
+                                                        const float *__restrict__ oval, const float *__restrict__ e,
+                                                        IterVecs v, double *partials, SolveScalars *s)
 {
-    if (mx_skip<FRESH, LOOP>(s, c))
+    if (mx_skip<FRESH>(s))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
@@ -537,10 +561,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t
             v.xh[i] = __fmaf_rn(alpha, po, v.xh[i]);
         }
         v.pout[i] = pi;
-        float y = pi;
+        float y = __ldg(e + i) * pi;
         for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k) {
             const int j = __ldg(ocol + k);
-            y += __ldg(oval + k) * pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+            const float pj = pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
+            y = __fmaf_rn(-__ldg(oval + k), pi - pj, y);
         }
         v.qout[i] = y;
         acc[0] += pi * y;
@@ -549,11 +574,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t
         acc[3] += ri * y;
     }
     double t[4];
-    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0) {
+    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0)
         mx_finish<FRESH>(s, t);
-        if (!FRESH)
-            mx_signal<LOOP>(s, c);
-    }
 }
 
 // U1: x += S xh (FP64), xh = 0.
@@ -781,15 +803,14 @@ IterVecs iter_vecs(MixedData *m, int par)
     return v;
 }
 
-template <bool FRESH, bool LOOP>
-int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, const CondHandles &c)
+template <bool FRESH> int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par)
 {
     const int64_t n = s->n;
     const IterVecs v = iter_vecs(m, par);
     if (!m->dia) {
-        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH, LOOP>);
-        k_mx_iter_csr<FRESH, LOOP><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(n, m->orow.p, m->ocol.p, m->oval.p,
-                                                                                   v, s->partials.p, s->scal.p, c);
+        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH>);
+        k_mx_iter_csr<FRESH><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(
+            n, m->orow.p, m->ocol.p, m->oval.p, m->e.p, v, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
@@ -802,13 +823,13 @@ int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, 
 #define SIMALL_DIA_CASE(ND)                                                                                           \
     case ND:                                                                                                          \
         if (grid) {                                                                                                   \
-            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, true, FRESH, LOOP>);                          \
-            k_mx_iter_dia<ND, true, FRESH, LOOP><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(                \
-                ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, true, FRESH>);                          \
+            k_mx_iter_dia<ND, true, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(                \
+                ni, m->ldU, m->offs, m->U.p, m->e.p, v, s->partials.p, s->scal.p);                                    \
         } else {                                                                                                      \
-            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, false, FRESH, LOOP>);                         \
-            k_mx_iter_dia<ND, false, FRESH, LOOP><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(               \
-                ni, m->ldU, m->offs, m->U.p, v, s->partials.p, s->scal.p, c);                                         \
+            const void *fn = reinterpret_cast<const void *>(k_mx_iter_dia<ND, false, FRESH>);                         \
+            k_mx_iter_dia<ND, false, FRESH><<<resident_grid(ctx, fn, quads), kBlock, 0, ctx->stream>>>(               \
+                ni, m->ldU, m->offs, m->U.p, m->e.p, v, s->partials.p, s->scal.p);                                    \
         }                                                                                                             \
         break;
         SIMALL_DIA_CASE(1)
@@ -830,15 +851,7 @@ int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par, 
 // One CG step of parity `par` (reads buffers [par], writes [1 - par]).
 int launch_iter(simall_context *ctx, simall_solver *s, int par, bool fresh)
 {
-    const CondHandles none{0, 0, 0};
-    return fresh ? launch_iter_t<true, false>(ctx, s, s->mixed, par, none)
-                 : launch_iter_t<false, false>(ctx, s, s->mixed, par, none);
-}
-
-// A normal step inside the device-side loop.
-int launch_loop_step(simall_context *ctx, simall_solver *s, int par, const CondHandles &c)
-{
-    return launch_iter_t<false, true>(ctx, s, s->mixed, par, c);
+    return fresh ? launch_iter_t<true>(ctx, s, s->mixed, par) : launch_iter_t<false>(ctx, s, s->mixed, par);
 }
 
 }  // namespace
@@ -860,6 +873,7 @@ int mixed_setup(simall_solver *s)
     }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
     SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
+    SIMALL_CUDA_TRY(ctx, m->e.alloc(n + 4));
     for (int k = 0; k < 2; ++k) {
         SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
         SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
@@ -884,6 +898,8 @@ int mixed_setup(simall_solver *s)
         if (st)
             return st;
     }
+    k_mx_row_defect<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->e.p);
+    SIMALL_LAUNCH_CHECK(ctx);
     if (m->dia) {
         m->ldU = (n + 3) & ~static_cast<int64_t>(3);
         SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * m->ldU));
@@ -957,10 +973,10 @@ int enqueue_mixed_iteration(simall_solver *s, int par)
 constexpr int kMixedKernelsPerIteration = 5;
 constexpr int kDeviceLoop = 0;  // GraphChunk::len of the device-side loop graph
 
-// The whole iteration as one graph: WHILE(loop) { step(0); IF(b0) {update
-// branch(0)}; step(1); IF(b1) {update branch(1)} }.  The steps set the
-// conditions from the device, so a solve is one graph launch with no host
-// round trip until it has finished.
+// The whole iteration as one graph: WHILE(loop) { step(0); control;
+// IF(b0) {update branch(0)}; step(1); control; IF(b1) {update branch(1)} }.
+// The controllers set the conditions from the device, so a solve is one graph
+// launch with no host round trip until it has finished.
 int build_device_loop(simall_solver *s, cudaGraphExec_t *out)
 {
     simall_context *ctx = s->ctx;
@@ -993,8 +1009,12 @@ int build_device_loop(simall_solver *s, cudaGraphExec_t *out)
         check(cudaStreamBeginCaptureToGraph(ctx->stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal),
               "capture body")) {
         for (int par = 0; par < 2 && st == SIMALL_OK; ++par) {
-            st = launch_loop_step(ctx, s, par, CondHandles{loop, branch[par], par == 0 ? 1 : 0});
+            st = launch_iter(ctx, s, par, false);
             if (st)
+                break;
+            k_mx_control<<<1, 32, 0, ctx->stream>>>(s->scal.p, CondHandles{loop, branch[par]});
+            ctx->launches.fetch_add(1, std::memory_order_relaxed);
+            if (!check(cudaGetLastError(), "controller launch"))
                 break;
             cudaStreamCaptureStatus cs;
             const cudaGraphNode_t *deps = nullptr;
@@ -1110,7 +1130,7 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
             if (e)
                 return e;
             const SolveScalars &h = *s->h_scal;
-            ctx->launches.fetch_add(static_cast<int64_t>(h.iter) + 2 + 4 * (static_cast<int64_t>(h.updates) + 1),
+            ctx->launches.fetch_add(2 * (static_cast<int64_t>(h.iter) + 2) + 4 * (static_cast<int64_t>(h.updates) + 1),
                                     std::memory_order_relaxed);
             if (!h.done)
                 return fail(ctx, SIMALL_ERR_CUDA, "device loop ended before the stop test held");
@@ -1161,8 +1181,8 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     if (k != 4)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);
     // r, q, p read at parity 0 and written at parity 1, xh read and written,
-    // plus the matrix (each gathered vector counted once)
-    *bytes = m->dia ? (4.0 * m->offs.nd + 32.0) * nd : 8.0 * m->nnzOff + 36.0 * nd + 4.0;
+    // e read, plus the matrix (each gathered vector counted once)
+    *bytes = m->dia ? (4.0 * m->offs.nd + 36.0) * nd : 8.0 * m->nnzOff + 40.0 * nd + 4.0;
     return launch_iter(ctx, s, 0, false);
 }
 

@@ -7,8 +7,8 @@ sources).  Every array stored here is an output of the reference's functions
 renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction, CGSolver::solve with Jacobi and ILU0, the
 preconditioners' apply, the SIMPLE cavity loop, solve_discrete_adjoint);
-inputs are seeded synthetic data.  The fixtures are small (a few hundred KB)
-so that the tests that read them run everywhere, the GPU host included.
+inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
+all) so that the tests that read them run everywhere, the GPU host included.
 
 Usage:  python tests/golden/make_golden.py
 """
@@ -67,6 +67,25 @@ def cavity_case(name, N, n_outer, n_record):
                         iters=c["iters"], res=c["res"])
 
 
+def cavity_case_full_size(name, N, n_outer):
+    """The SIMPLE cavity at full size: records the first and the last outer
+    iteration's pressure system.  The assembled matrix and rhs are stored as
+    SHA-256 digests of their bytes (the test reassembles them from aP and phi);
+    aP, phi, the reference's p' and every solve's iteration count and residual
+    are stored as arrays."""
+    import hashlib
+
+    c = R.cavity(N, mu=0.01, n_outer=n_outer, n_record=1, precond=0, tol=1e-8, max_it=1000, record_stride=n_outer)
+    digest = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    np.savez_compressed(os.path.join(HERE, name), N=np.array(N), n_outer=np.array(n_outer),
+                        recorded=np.array([0, n_outer - 1]),
+                        pattern_sha256=np.array(digest(c["rowPtr"]) + digest(c["colIdx"])),
+                        values_sha256=np.array([digest(v) for v in c["values"]]),
+                        rhs_sha256=np.array([digest(v) for v in c["rhs"]]),
+                        x=c["x"], aP=c["aP"], phi=c["phi"], iters=c["iters"], res=c["res"],
+                        p_solve_seconds=np.array(c["p_solve_seconds"]))
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -96,6 +115,7 @@ def main():
               [(1, 7)] + [(z, 1) for z in range(2, 7)], [1])
     mesh_case("cavity_16x16x1_mesh.npz", (16, 16, 1), 5, 0.0, False, [(z, 1) for z in range(1, 7)], [])
     cavity_case("cavity_simple_16.npz", 16, 6, 6)
+    cavity_case_full_size("cavity_simple_128.npz", 128, 200)
     adjoint_case("adjoint_face_k_5x4x3.npz")
     print("fixtures written to", HERE)
 

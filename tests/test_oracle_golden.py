@@ -87,6 +87,30 @@ def test_cavity_simple_trajectory_systems(oracle):
         assert bits_equal(x, c["x"][it])
 
 
+def test_cavity_128_full_size_systems(oracle):
+    """The 128x128 SIMPLE cavity (Re 100, urfP 0.3, urfU 0.7, 200 outer
+    iterations): the first and the last pressure system, reassembled by the
+    oracle from the recorded aP and phi, have the reference's bytes (SHA-256),
+    and the oracle's CG returns the reference's p', iteration count and
+    residual bit for bit."""
+    import hashlib
+
+    c = load("cavity_simple_128.npz")
+    digest = lambda a: hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()  # noqa: E731
+    N = int(c["N"])
+    m = oracle.cartesian_mesh(N, N, 1, 1.0, 1.0, 1.0 / N)
+    rp, ci = oracle.build_sparsity(m)
+    assert digest(rp) + digest(ci) == str(c["pattern_sha256"])
+    assert len(c["iters"]) == int(c["n_outer"])
+    for k, it in enumerate(c["recorded"]):
+        v, rhs, anyD = oracle.assemble(m, rp, ci, [], 1.0, c["aP"][k], c["phi"][k])
+        assert not anyD
+        assert digest(v) == str(c["values_sha256"][k]) and digest(rhs) == str(c["rhs_sha256"][k])
+        x, its, last = oracle.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
+        assert its == int(c["iters"][it]) and last == float(c["res"][it])
+        assert bits_equal(x, c["x"][k])
+
+
 def test_face_conductance_adjoint_against_reference_gradient(oracle):
     """Face-conductance assembly reproduced bit for bit; the adjoint gradient
     (CG on A^T = A, then the scatter) matches solve_discrete_adjoint's."""
