@@ -112,7 +112,15 @@ typedef struct simall_solver_config {
     int precision;         /* simall_precision; default FP64 */
     double reliable_delta; /* mixed: iterated-residual drop that triggers an FP64 update; default 0.1 */
     int check_interval;    /* iterations between host polls of the device stop flag; 0 = automatic */
+    int engine;            /* simall_engine: how the iteration runs; default SIMALL_ENGINE_AUTO */
 } simall_solver_config;
+
+/* SIMALL_ENGINE_AUTO: systems of up to 131,072 rows (Jacobi FP64, or mixed
+ * precision in diagonal storage) run the whole solve on one thread-block
+ * cluster; larger ones, and any solver with check_interval > 0, launch kernels
+ * per iteration (mixed precision: one device-side graph loop).
+ * SIMALL_ENGINE_KERNELS: always the per-iteration kernels. */
+enum simall_engine { SIMALL_ENGINE_AUTO = 0, SIMALL_ENGINE_KERNELS = 1 };
 
 typedef struct simall_solver_stats {
     int iterations;          /* as CGSolver::solve returns: it+1 at convergence, maxIterations otherwise */
@@ -123,6 +131,9 @@ typedef struct simall_solver_stats {
     double true_residual;    /* ||b - A x||/max(||b||,1e-30) recomputed in FP64 from the returned x */
     double b_norm;           /* ||b||_2 */
     double seconds;          /* wall time of the solve call */
+    int engine;              /* what ran the iteration: 0 kernels per step (device graph loop or host-polled
+                                chunks), 1 one thread-block cluster for the whole solve */
+    int reserved;
 } simall_solver_stats;
 
 typedef struct simall_solver simall_solver;

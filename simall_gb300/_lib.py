@@ -31,12 +31,13 @@ STATUS_NAMES = {
 
 class SolverConfig(C.Structure):
     _fields_ = [("preconditioner", _I), ("tolerance", _D), ("max_iterations", _I), ("precision", _I),
-                ("reliable_delta", _D), ("check_interval", _I)]
+                ("reliable_delta", _D), ("check_interval", _I), ("engine", _I)]
 
 
 class SolverStats(C.Structure):
     _fields_ = [("iterations", _I), ("converged", _I), ("status", _I), ("reliable_updates", _I),
-                ("final_residual", _D), ("true_residual", _D), ("b_norm", _D), ("seconds", _D)]
+                ("final_residual", _D), ("true_residual", _D), ("b_norm", _D), ("seconds", _D),
+                ("engine", _I), ("reserved", _I)]
 
 
 class MeshView(C.Structure):

@@ -15,7 +15,10 @@
 // Storage per system: S A S as symmetric diagonal storage when the system is
 // numerically symmetric with at most kBatchDiags upper diagonals (every
 // structured grid in natural order), otherwise FP32 CSR of its off-diagonal
-// part; FP32 work vectors xh, rh, ph, qh; FP64 scale, b and x.  The CTA size
+// part; FP32 work vectors xh, rh, ph, qh; FP64 scale, b and x.  The SpMV uses
+// the row-sum form of the single-system mixed solver (per-row e_i summed in
+// FP64), which keeps the FP32 iteration count of pinned pressure systems close
+// to the FP64 one.  The CTA size
 // (threads) and CTAs per SM are picked by a small autotuner that times each
 // candidate on the batch itself the first time a batch shape is solved.
 #include "device.cuh"
@@ -67,6 +70,7 @@ struct simall_batch {
     simall::DevBuf<int32_t> rowPtr, colIdx, orow, ocol;
     simall::DevBuf<double> values, scale, b, x;
     simall::DevBuf<float> U, oval, xh, rh, ph, qh;
+    simall::DevBuf<float> E;  // per row: 1 + sum_j (S A S)_ij, summed in FP64 (row-sum form of the SpMV)
     simall::DevBuf<simall::BatchOut> out;
     std::vector<simall::BatchOut> h_out;
     int block = 0, ctas_per_sm = 0;  // autotuned launch shape
@@ -125,10 +129,13 @@ __device__ __forceinline__ double cta_allreduce_f(float a, double *red)
     return t;
 }
 
-// q = (S A S) p on rows [0, n) of one system; returns this thread's p.q part.
+// q = (S A S) p on rows [0, n) of one system in the row-sum form
+// q_i = e_i p_i - sum_j N_ij (p_i - p_j) (N: off-diagonal part of S A S, e_i
+// its row sum plus one, summed in FP64); returns this thread's p.q part.
 __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__restrict__ U,
                                             const int32_t *__restrict__ orow, const int32_t *__restrict__ ocol,
-                                            const float *__restrict__ oval, const float *p, float *q)
+                                            const float *__restrict__ oval, const float *__restrict__ e,
+                                            const float *p, float *q)
 {
     float acc = 0.0f;
     const int n = S.n;
@@ -136,14 +143,14 @@ __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__re
         const float *Us = U + S.u0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const float pi = p[i];
-            float y = pi;
+            float y = e[i] * pi;
             for (int d = 0; d < S.nd; ++d) {
                 const int off = S.off[d];
                 const float *Ud = Us + static_cast<int64_t>(d) * n;
                 if (i + off < n)
-                    y += Ud[i] * p[i + off];
+                    y = __fmaf_rn(-Ud[i], pi - p[i + off], y);
                 if (i - off >= 0)
-                    y += Ud[i - off] * p[i - off];
+                    y = __fmaf_rn(-Ud[i - off], pi - p[i - off], y);
             }
             q[i] = y;
             acc += pi * y;
@@ -154,9 +161,9 @@ __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__re
         const float *va = oval + S.u0;
         for (int i = threadIdx.x; i < n; i += blockDim.x) {
             const float pi = p[i];
-            float y = pi;
+            float y = e[i] * pi;
             for (int k = rp[i]; k < rp[i + 1]; ++k)
-                y += va[k] * p[ci[k]];
+                y = __fmaf_rn(-va[k], pi - p[ci[k]], y);
             q[i] = y;
             acc += pi * y;
         }
@@ -169,7 +176,7 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
                                 const int32_t *__restrict__ colIdx, const double *__restrict__ values,
                                 const float *__restrict__ U, const int32_t *__restrict__ orow,
                                 const int32_t *__restrict__ ocol, const float *__restrict__ oval,
-                                const double *__restrict__ scale_all, const double *__restrict__ b_all,
+                                const float *__restrict__ e_all, const double *__restrict__ scale_all, const double *__restrict__ b_all,
                                 double *x_all, float *xh_all, float *rh_all, float *ph_all, float *qh_all, double tol,
                                 double delta, int maxit, BatchOut *out, double *red)
 {
@@ -204,7 +211,7 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
     bool done = (t0 < tol) || maxit <= 0;
     while (!done) {
         // q = SAS p, alpha
-        const double pq = cta_allreduce_f(batch_spmv(S, U, orow, ocol, oval, ph, qh), red);
+        const double pq = cta_allreduce_f(batch_spmv(S, U, orow, ocol, oval, e_all + S.row0, ph, qh), red);
         const bool breakdown = !(pq > 0.0);
         const float alpha = breakdown ? 0.0f : static_cast<float>(rho / pq);
         // xh += alpha p, rh -= alpha q (own rows: no barrier needed before)
@@ -281,9 +288,9 @@ __global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict
                               const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
                               const double *__restrict__ values, const float *__restrict__ U,
                               const int32_t *__restrict__ orow, const int32_t *__restrict__ ocol,
-                              const float *__restrict__ oval, const double *__restrict__ scale,
-                              const double *__restrict__ b, double *x, float *xh, float *rh, float *ph, float *qh,
-                              double tol, double delta, int maxit, BatchOut *out)
+                              const float *__restrict__ oval, const float *__restrict__ E,
+                              const double *__restrict__ scale, const double *__restrict__ b, double *x, float *xh,
+                              float *rh, float *ph, float *qh, double tol, double delta, int maxit, BatchOut *out)
 {
     __shared__ double red[64];
     __shared__ int s_next;
@@ -297,7 +304,7 @@ __global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict
             return;
         const int id = order[k];
         const BatchSys S = sys[id];
-        batch_solve_one(S, rowPtr, colIdx, values, U, orow, ocol, oval, scale, b, x, xh, rh, ph, qh, tol, delta,
+        batch_solve_one(S, rowPtr, colIdx, values, U, orow, ocol, oval, E, scale, b, x, xh, rh, ph, qh, tol, delta,
                         maxit, out + id, red);
     }
 }
@@ -312,7 +319,8 @@ int launch_batch(simall_batch *B, int block, int ctas_per_sm, const double *b, d
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(B->queue.p, 0, sizeof(int), ctx->stream));
     const int grid = std::max(1, std::min(B->nsys, ctx->num_sms * ctas_per_sm));
     k_batch_solve<<<grid, block, 0, ctx->stream>>>(B->sys.p, B->order.p, B->nsys, B->queue.p, B->rowPtr.p, B->colIdx.p,
-                                                   B->values.p, B->U.p, B->orow.p, B->ocol.p, B->oval.p, B->scale.p, b,
+                                                   B->values.p, B->U.p, B->orow.p, B->ocol.p, B->oval.p, B->E.p,
+                                                   B->scale.p, b,
                                                    x, B->xh.p, B->rh.p, B->ph.p, B->qh.p, B->cfg.tolerance,
                                                    B->cfg.reliable_delta, B->cfg.max_iterations, B->out.p);
     ctx->launches.fetch_add(1, std::memory_order_relaxed);
@@ -405,6 +413,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
         return fail(ctx, SIMALL_ERR_SIZE_MISMATCH, "batch offsets must start at 0 and grow");
     std::vector<BatchSys> sys(static_cast<size_t>(n_systems));
     std::vector<double> scale(static_cast<size_t>(rows));
+    std::vector<float> E(static_cast<size_t>(rows));
     std::vector<float> U;
     std::vector<int32_t> orow, ocol;
     std::vector<float> oval;
@@ -461,6 +470,13 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             dia = false;
         dia = dia && sym;
         const double *sc = scale.data() + r0;
+        for (int64_t i = 0; i < n; ++i) {
+            double sum = 1.0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                if (ci[k] != i)
+                    sum += va[k] * sc[i] * sc[ci[k]];
+            E[r0 + i] = static_cast<float>(sum);
+        }
         if (dia) {
             std::sort(offs.begin(), offs.end());
             S.nd = static_cast<int>(offs.size());
@@ -511,6 +527,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, B->colIdx.alloc(nnz));
     SIMALL_CUDA_TRY(ctx, B->values.alloc(nnz));
     SIMALL_CUDA_TRY(ctx, B->scale.alloc(rows));
+    SIMALL_CUDA_TRY(ctx, B->E.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->b.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->x.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->xh.alloc(rows));
@@ -528,6 +545,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, up(B->colIdx.p, colIdx, nnz * sizeof(int32_t)));
     SIMALL_CUDA_TRY(ctx, up(B->values.p, values, nnz * sizeof(double)));
     SIMALL_CUDA_TRY(ctx, up(B->scale.p, scale.data(), scale.size() * sizeof(double)));
+    SIMALL_CUDA_TRY(ctx, up(B->E.p, E.data(), E.size() * sizeof(float)));
     if (!U.empty())
         SIMALL_CUDA_TRY(ctx, up(B->U.p, U.data(), U.size() * sizeof(float)));
     if (!orow.empty()) {

@@ -1,0 +1,751 @@
+// Small systems on one thread-block cluster.
+//
+// Below some 10^5 rows a Krylov iteration spread over the whole GPU is bound by
+// launch and grid-synchronisation latency, not by bandwidth: on the 128 x 128
+// cavity (16,384 rows, 2.7 MB per FP64 iteration) the multi-kernel PCG spends
+// ~17 us per iteration.  Here one cluster of up to 16 CTAs (one per SM) runs
+// the whole solve in a single launch.  Each CTA owns a contiguous slice of
+// rows; the vectors that other CTAs read (the preconditioned residual and the
+// double-buffered search direction, and for mixed precision the FP32 residual,
+// product and direction) live in the owners' shared memory and are read by the
+// other CTAs through distributed shared memory; a CTA's private per-row state
+// stays in registers.  Every global sum is one cluster barrier: each CTA
+// publishes its partial sums in shared memory, and after the barrier every
+// warp of every CTA reads all partials in rank order and reduces them with the
+// same butterfly, so all CTAs hold bit-identical totals and take identical
+// decisions without further communication.  The only waits are hardware
+// cluster barriers, reached the same number of times by every CTA (the trip
+// count follows from the identical totals and is bounded by max_iter), so no
+// CTA can wait for one that has left.
+//
+// Two solvers, chosen by the single-system solver when the system fits:
+//   FP64 Jacobi PCG (CGSolver::solve, src/solver/LinearSolvers.cpp:420-451):
+//     per iteration q = A p with p = z + beta p_old formed on the fly, p.q;
+//     x, r, z = D^-1 r, r.r, r.z -- two barriers.
+//   Mixed precision (diagonal storage): the fused FP32 step of mixed.cu (row-
+//     sum form, beta from |r - alpha q|^2) with FP64 reliable updates -- one
+//     barrier per step, three more per reliable update.
+#include "device.cuh"
+#include "solver.hpp"
+
+#include <cooperative_groups.h>
+
+#include <algorithm>
+#include <cmath>
+
+namespace cg = cooperative_groups;
+
+namespace simall {
+
+constexpr int kClThreads = 256;
+constexpr int kClMaxRowsPerCta = 8192;  // FP64: rows per thread <= 32
+constexpr int kClMaxIterations = 200000;  // longer limits take the multi-kernel path
+
+namespace {
+
+__device__ __forceinline__ double warp_allsum(double v)
+{
+    // butterfly: every lane ends with the same bits (each step adds a pair in
+    // both lanes of the pair, and a + b == b + a)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ float warp_sum_fl(float v)
+{
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+        v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+struct ClShared {
+    double part[2][4];   // this CTA's partial sums, two slots used alternately
+    double wsum[4][32];  // per-warp sums
+    double tot[4];       // the cluster totals, broadcast to the CTA
+    double ctl[8];       // scalars derived from the totals by one thread, broadcast
+};
+
+struct NoFinish {
+    __device__ void operator()(const double *, double *) const {}
+};
+
+// Butterfly sums of NV values over groups of 2^LEVELS lanes, level by level
+// so the NV dependent chains overlap; every lane of a group ends with the same
+// bits (each level adds a pair in both lanes of the pair, and a + b == b + a).
+template <int LEVELS, int NV, typename T> __device__ __forceinline__ void butterfly(T (&v)[NV])
+{
+#pragma unroll
+    for (int l = 0; l < LEVELS; ++l) {
+        T o[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            o[k] = __shfl_xor_sync(0xffffffffu, v[k], 1 << l);
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            v[k] += o[k];
+    }
+}
+
+constexpr int kClWarps = kClThreads / 32;
+constexpr int kClWarpLevels = kClWarps <= 1 ? 0 : kClWarps <= 2 ? 1 : kClWarps <= 4 ? 2 : kClWarps <= 8 ? 3 : kClWarps <= 16 ? 4 : 5;
+constexpr int kClMaxCtas = 16;  // cluster sizes up to 16: 4 butterfly levels
+
+// Cluster-wide sum of NV values; every thread of every CTA receives the same
+// totals.  Sums within a CTA run in the values' own type (FP32 for the mixed
+// solver's per-thread partials, FP64 for the FP64 solver); the sum across the
+// CTAs -- the global reduction -- is FP64.  One warp per CTA reads the C
+// partials through the cluster window (every warp reading them serialised on
+// the owners' shared memory and cost ~5 us at 1024 threads).  The butterflies
+// run level by level over all NV values: on GB300's narrow FP64 pipe a chain
+// of FP64 adds costs ~100 cycles per level, so the NV chains must overlap and
+// use no more levels than there are warps or CTAs.  `fin(tot, ctl)` runs in one
+// thread of each CTA before the broadcast: scalar arithmetic done once per CTA
+// instead of once per thread.
+template <int NV, typename T, typename Fin = NoFinish>
+__device__ __forceinline__ void cl_allreduce(const T (&v)[NV], double (&out)[NV], ClShared &sh, int &slot,
+                                             const cg::cluster_group &cl, Fin fin = Fin{})
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    T w[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        w[k] = v[k];
+    butterfly<5>(w);
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            sh.wsum[k][wid] = static_cast<double>(w[k]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+        T c[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            c[k] = lane < kClWarps ? static_cast<T>(sh.wsum[k][lane]) : T(0);
+        butterfly<kClWarpLevels>(c);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                sh.part[slot][k] = static_cast<double>(c[k]);
+        }
+    }
+    cl.sync();
+    if (wid == 0) {
+        const int C = static_cast<int>(cl.num_blocks());
+        double t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            t[k] = lane < C ? *cl.map_shared_rank(&sh.part[slot][k], lane) : 0.0;
+        butterfly<4>(t);
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                sh.tot[k] = t[k];
+            fin(sh.tot, sh.ctl);
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        out[k] = sh.tot[k];
+    slot ^= 1;
+}
+
+// Value at global row j of a shared-memory array distributed by slices of
+// 2^logR rows, read through the cluster window from the owner.
+template <typename T>
+__device__ __forceinline__ T cl_load(const cg::cluster_group &cl, T *local, int logR, int j)
+{
+    return *cl.map_shared_rank(local + (j & ((1 << logR) - 1)), static_cast<unsigned>(j >> logR));
+}
+
+// ---------------------------------------------------------------- FP64 Jacobi PCG
+// CGSolver::solve (src/solver/LinearSolvers.cpp:420-451) with Jacobi: x = 0,
+// r = b, z = D^-1 r, p = z; per iteration q = A p, alpha = r.z / p.q,
+// x += alpha p, r -= alpha q, stop when ||r|| / max(||b||, 1e-30) < tol,
+// z = D^-1 r, beta = r.z' / r.z, p = z + beta p.  The direction is the only
+// vector other CTAs read; it is written after the second sum of an iteration
+// and read after the next barrier.  Per row an iteration issues 12 FP64
+// instructions; alpha, beta and the stop test are computed once per CTA.
+enum ClCtl { kAlpha = 0, kBeta = 1, kLast = 2, kStop = 3, kRz = 4 };
+
+template <int RPT>
+__global__ void __launch_bounds__(kClThreads, 1)
+    k_cl_pcg64(int n, int logR, const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
+               const double *__restrict__ val, const double *__restrict__ invD, const double *__restrict__ b,
+               double *__restrict__ x, SolveScalars *s)
+{
+    const cg::cluster_group cl = cg::this_cluster();
+    const int rank = static_cast<int>(cl.block_rank());
+    extern __shared__ __align__(16) double cl_sm[];
+    double *ps = cl_sm;  // the direction of the owned rows
+    const int R = 1 << logR;
+    __shared__ ClShared sh;
+    const int row0 = rank * R;
+    const int nr = max(0, min(R, n - row0));
+    const double tol = s->tol;
+    const int max_iter = s->max_iter;
+
+    double xr[RPT], rr[RPT], dr[RPT], qr[RPT];
+    double a[2] = {0.0, 0.0};
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int il = threadIdx.x + k * kClThreads;
+        xr[k] = rr[k] = dr[k] = qr[k] = 0.0;
+        if (il < nr) {
+            const int i = row0 + il;
+            const double bi = b[i], d = invD[i], z = d * bi;
+            rr[k] = bi;
+            dr[k] = d;
+            ps[il] = z;
+            a[0] += bi * z;
+            a[1] += bi * bi;
+        }
+    }
+    int slot = 0;
+    double t2[2];
+    cl_allreduce<2>(a, t2, sh, slot, cl, [](const double *t, double *c) {
+        c[kRz] = t[0];
+        c[kLast] = sqrt(t[1]) / std_max(sqrt(t[1]), 1e-30);
+    });
+    double rz = sh.ctl[kRz];
+    const double bnorm = std_max(sqrt(t2[1]), 1e-30);
+    double last = sh.ctl[kLast];
+    int it = 0, result = 0, status = SIMALL_OK;
+    bool run = max_iter > 0;
+    if (!run)
+        result = max_iter;
+    while (run) {
+        cl.sync();  // every CTA's direction is complete
+        double acc[1] = {0.0};
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int il = threadIdx.x + k * kClThreads;
+            if (il < nr) {
+                const int i = row0 + il;
+                double q = 0.0;
+                for (int e = __ldg(rowPtr + i); e < __ldg(rowPtr + i + 1); ++e) {
+                    const int j = __ldg(colIdx + e);
+                    const int jl = j - row0;
+                    const double pj = (jl >= 0 && jl < R) ? ps[jl] : cl_load(cl, ps, logR, j);
+                    q = fma(__ldg(val + e), pj, q);
+                }
+                qr[k] = q;
+                acc[0] += ps[il] * q;
+            }
+        }
+        double pq[1];
+        cl_allreduce<1>(acc, pq, sh, slot, cl, [rz](const double *t, double *c) {
+            c[kAlpha] = t[0] == 0.0 ? 0.0 : rz / t[0];
+        });
+        if (pq[0] == 0.0) {
+            last = sqrt(rz) / bnorm;
+            result = it;
+            status = SIMALL_ERR_BREAKDOWN;
+            break;
+        }
+        const double alpha = sh.ctl[kAlpha];
+        double c[2] = {0.0, 0.0};
+        double zr[RPT];
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int il = threadIdx.x + k * kClThreads;
+            zr[k] = 0.0;
+            if (il < nr) {
+                xr[k] = fma(alpha, ps[il], xr[k]);
+                rr[k] = fma(-alpha, qr[k], rr[k]);
+                zr[k] = dr[k] * rr[k];
+                c[0] += rr[k] * rr[k];
+                c[1] += rr[k] * zr[k];
+            }
+        }
+        double t[2];
+        cl_allreduce<2>(c, t, sh, slot, cl, [rz, bnorm, tol, it, max_iter](const double *tt, double *cc) {
+            const double l = sqrt(tt[0]) / bnorm;
+            cc[kLast] = l;
+            cc[kBeta] = tt[1] / rz;
+            cc[kStop] = l < tol ? 1.0 : (it + 1 >= max_iter ? 2.0 : 0.0);
+        });
+        last = sh.ctl[kLast];
+        const double stop = sh.ctl[kStop];
+        if (stop == 1.0) {
+            result = it + 1;
+            break;
+        }
+        const double beta = sh.ctl[kBeta];
+        rz = t[1];
+        if (stop == 2.0) {
+            it = max_iter;
+            result = max_iter;
+            break;
+        }
+        ++it;
+        // p = z + beta p: read by the other CTAs after the barrier at the top of the loop
+#pragma unroll
+        for (int k = 0; k < RPT; ++k) {
+            const int il = threadIdx.x + k * kClThreads;
+            if (il < nr)
+                ps[il] = fma(beta, ps[il], zr[k]);
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int il = threadIdx.x + k * kClThreads;
+        if (il < nr)
+            x[row0 + il] = xr[k];
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        s->rz = rz;
+        s->bnorm = bnorm;
+        s->last = last;
+        s->iter = it;
+        s->result = result;
+        s->status = status;
+        s->done = 1;
+    }
+    cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+}  // namespace
+
+namespace {
+
+// ---------------------------------------------------------------- mixed precision
+// The mixed solver of mixed.cu on one cluster: FP32 CG on S A S (diagonal
+// storage, row-sum form), one fused step per iteration (r, x, p updates, the
+// product and its four sums; beta from |r - alpha q|^2), FP64 reliable updates
+// (x += S xh, r = b - A x from the FP64 CSR, stop test on it, r = S r, then a
+// FRESH step that forms p from the replaced residual).  r, q and p are
+// double-buffered by step parity in the owners' shared memory; xh stays in
+// registers; x lives in global memory (written at folds, read by the true
+// residual after a barrier).  The scalar state of the iteration is kept by one
+// thread per CTA and broadcast after every sum; all CTAs hold identical state.
+struct ClMixState {
+    double rz, sigma0, rmax, t0, last, alpha, beta, bnorm, rr64;
+    int iter, updates, need, done, result, status;
+};
+
+template <bool FRESH>
+__device__ __forceinline__ float cl_pdir(float r, float q, float p, float alpha, float beta)
+{
+    const float rn = FRESH ? r : __fmaf_rn(-alpha, q, r);
+    return __fmaf_rn(beta, p, rn);
+}
+
+// alpha and beta are used in FP32, so they are divided in FP32 (GB300's FP64
+// divide is a long dependent chain on a narrow pipe, and it sits on the
+// critical path of every step); the cancelling sum |r - alpha q|^2 is formed
+// in FP64.
+__device__ __forceinline__ void clmix_step(ClMixState &st, double pq, double qq, double rr, double rq)
+{
+    if (!(pq > 0.0) || !(rr > 0.0)) {
+        st.status = SIMALL_ERR_BREAKDOWN;
+        st.need = 1;
+        st.alpha = 0.0;
+        st.beta = 0.0;
+        return;
+    }
+    const float alpha = __fdiv_rn(static_cast<float>(rr), static_cast<float>(pq));
+    const double a = alpha;
+    const double next = rr - 2.0 * a * rq + a * a * qq;
+    st.alpha = a;
+    st.beta = __fdiv_rn(static_cast<float>(next > 0.0 ? next : 0.0), static_cast<float>(rr));
+}
+
+// One fused step over the owned rows.  Buffers [par] hold step k-1, [par ^ 1]
+// receive step k; FRESH takes r from rv[par ^ 1] (the replaced residual).
+// Shared layout: r[0] r[1] q[0] q[1] p[0] p[1], R floats each; R = 2^logR, so
+// the owner of row j is j >> logR and its slot j & (R - 1).  Every neighbour is
+// read through the cluster window (the owner may be this CTA), so the 2 ND
+// neighbours' loads carry no branch and issue together; a neighbour outside
+// [0, n) reads the row itself with a zero coefficient.
+template <int ND, int RPT, bool FRESH>
+__device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, int logR, int row0, int nr,
+                                           const ClusterMixedArgs &A, const int (&off)[ND], float *base, int par,
+                                           float alpha, float beta, float (&xh)[RPT], float (&acc)[4])
+{
+    const int R = 1 << logR;
+    const float *rs = base + (FRESH ? par ^ 1 : par) * R;
+    const float *qs = base + (2 + par) * R;
+    const float *ps = base + (4 + par) * R;
+    float *rout = base + (par ^ 1) * R;
+    float *qout = base + (2 + (par ^ 1)) * R;
+    float *pout = base + (4 + (par ^ 1)) * R;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        const int il = threadIdx.x + k * kClThreads;
+        if (il >= nr)
+            continue;
+        const int i = row0 + il;
+        float u[2 * ND], rj[2 * ND], qj[2 * ND], pj[2 * ND];
+#pragma unroll
+        for (int d = 0; d < ND; ++d) {
+#pragma unroll
+            for (int side = 0; side < 2; ++side) {
+                const int t = 2 * d + side;
+                const int j0 = side ? i - off[d] : i + off[d];
+                const bool ok = j0 >= 0 && j0 < n;
+                const int j = ok ? j0 : i;
+                u[t] = ok ? __ldg(A.U + d * A.ldU + (side ? j : i)) : 0.0f;
+                const unsigned owner = static_cast<unsigned>(j >> logR);
+                const int jl = j & (R - 1);
+                rj[t] = *cl.map_shared_rank(rs + jl, owner);
+                qj[t] = FRESH ? 0.0f : *cl.map_shared_rank(qs + jl, owner);
+                pj[t] = *cl.map_shared_rank(ps + jl, owner);
+            }
+        }
+        const float ro = rs[il], po = ps[il], ei = __ldg(A.e + i);
+        const float rk = FRESH ? ro : __fmaf_rn(-alpha, qs[il], ro);
+        const float pk = __fmaf_rn(beta, po, rk);
+        if (!FRESH) {
+            rout[il] = rk;
+            xh[k] = __fmaf_rn(alpha, po, xh[k]);
+        }
+        pout[il] = pk;
+        float y = ei * pk;
+#pragma unroll
+        for (int t = 0; t < 2 * ND; ++t)
+            y = __fmaf_rn(-u[t], pk - cl_pdir<FRESH>(rj[t], qj[t], pj[t], alpha, beta), y);
+        qout[il] = y;
+        acc[0] += pk * y;
+        acc[1] += y * y;
+        acc[2] += rk * rk;
+        acc[3] += rk * y;
+    }
+}
+
+template <int ND, int RPT>
+__global__ void __launch_bounds__(kClThreads, 1)
+    k_cl_mixed(int n, int logR, ClusterMixedArgs A, const int32_t *__restrict__ rowPtr,
+               const int32_t *__restrict__ colIdx, const double *__restrict__ val, const double *__restrict__ b,
+               double *__restrict__ x, SolveScalars *s)
+{
+    const cg::cluster_group cl = cg::this_cluster();
+    const int rank = static_cast<int>(cl.block_rank());
+    extern __shared__ __align__(16) double cl_sm[];
+    const int R = 1 << logR;
+    float *base = reinterpret_cast<float *>(cl_sm);  // r[0] r[1] q[0] q[1] p[0] p[1]
+    int off[ND];
+#pragma unroll
+    for (int d = 0; d < ND; ++d)
+        off[d] = A.off[d];
+    __shared__ ClShared sh;
+    __shared__ ClMixState st_sh;
+    ClMixState &st = st_sh;
+    ClMixState *const stp = &st_sh;
+    const int row0 = rank * R;
+    const int nr = max(0, min(R, n - row0));
+    const double tol = s->tol, delta = s->delta;
+    const int max_iter = s->max_iter;
+
+    // init: x = 0, r = S b (r[0]), p_old = 0 (p[1]), xh = 0
+    float xh[RPT];
+    float a0 = 0.0f;
+    double a1 = 0.0;
+#pragma unroll
+    for (int k = 0; k < RPT; ++k) {
+        xh[k] = 0.0f;
+        const int il = threadIdx.x + k * kClThreads;
+        if (il < nr) {
+            const int i = row0 + il;
+            const double bi = b[i];
+            const float r = static_cast<float>(bi * A.scale[i]);
+            x[i] = 0.0;
+            base[il] = r;          // r[0]
+            base[5 * R + il] = 0.0f;  // p[1]
+            a0 += r * r;
+            a1 += bi * bi;
+        }
+    }
+    int slot = 0;
+    {
+        const double v[2] = {static_cast<double>(a0), a1};
+        double t[2];
+        cl_allreduce<2>(v, t, sh, slot, cl, [stp, tol, max_iter](const double *tt, double *) {
+            const double bn = sqrt(tt[1]);
+            stp->bnorm = std_max(bn, 1e-30);
+            stp->rz = tt[0];
+            stp->sigma0 = sqrt(tt[0]);
+            stp->rmax = stp->sigma0;
+            stp->t0 = bn / stp->bnorm;
+            stp->last = stp->t0;
+            stp->rr64 = tt[1];
+            stp->alpha = 0.0;
+            stp->beta = 0.0;
+            stp->iter = 0;
+            stp->updates = 0;
+            stp->need = 2;
+            stp->status = SIMALL_OK;
+            stp->done = 0;
+            stp->result = 0;
+            if (stp->t0 < tol) {
+                stp->done = 1;
+            } else if (max_iter <= 0) {
+                stp->done = 1;
+                stp->result = max_iter;
+            }
+        });
+    }
+    auto fresh_fin = [stp](const double *t, double *) {
+        stp->rz = t[2];
+        stp->sigma0 = sqrt(t[2]);
+        stp->rmax = stp->sigma0;
+        if (stp->need == 1)
+            stp->updates += 1;
+        stp->need = 0;
+        clmix_step(*stp, t[0], t[1], t[2], t[3]);
+    };
+    int par = 1;
+    if (!st.done) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, static_cast<float>(st.beta), xh,
+                              acc);
+        double t[4];
+        cl_allreduce<4>(acc, t, sh, slot, cl, fresh_fin);
+    }
+    par = 0;
+    while (!st.done) {
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        clmix_rows<ND, RPT, false>(cl, n, logR, row0, nr, A, off, base, par, static_cast<float>(st.alpha),
+                               static_cast<float>(st.beta), xh, acc);
+        double t[4];
+        cl_allreduce<4>(acc, t, sh, slot, cl, [stp, tol, delta, max_iter](const double *tt, double *) {
+            stp->iter += 1;
+            const double sigma = sqrtf(static_cast<float>(tt[2]));  // trigger and estimate: FP32 is plenty
+            const double est = stp->t0 * __fdiv_rn(static_cast<float>(sigma), static_cast<float>(stp->sigma0));
+            stp->last = est;
+            if (stp->need || sigma < delta * stp->rmax || est < tol || stp->iter >= max_iter) {
+                stp->need = 1;
+                return;
+            }
+            if (sigma > stp->rmax)
+                stp->rmax = sigma;
+            stp->rz = tt[2];
+            clmix_step(*stp, tt[0], tt[1], tt[2], tt[3]);
+        });
+        if (st.need) {
+            // reliable update: x += S xh (FP64), r = b - A x, r = S r into r[par ^ 1]
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int il = threadIdx.x + k * kClThreads;
+                if (il < nr) {
+                    const int i = row0 + il;
+                    x[i] += A.scale[i] * static_cast<double>(xh[k]);
+                }
+                xh[k] = 0.0f;
+            }
+            cl.sync();  // x complete in global memory
+            double v[2] = {0.0, 0.0};
+#pragma unroll
+            for (int k = 0; k < RPT; ++k) {
+                const int il = threadIdx.x + k * kClThreads;
+                if (il < nr) {
+                    const int i = row0 + il;
+                    double y = 0.0;
+                    for (int e = __ldg(rowPtr + i); e < __ldg(rowPtr + i + 1); ++e)
+                        y = fma(__ldg(val + e), __ldcg(x + __ldg(colIdx + e)), y);  // other SMs' x: via L2
+                    const double r = b[i] - y;
+                    const float rf = static_cast<float>(A.scale[i] * r);
+                    base[(par ^ 1) * R + il] = rf;
+                    v[0] += r * r;
+                    v[1] += static_cast<double>(rf) * rf;
+                }
+            }
+            double t2[2];
+            cl_allreduce<2>(v, t2, sh, slot, cl, [stp, tol, max_iter](const double *tt, double *) {
+                stp->rr64 = tt[0];
+                const double tr = sqrt(tt[0]) / stp->bnorm;
+                stp->last = tr;
+                stp->t0 = tr;
+                if (tr < tol) {
+                    stp->done = 1;
+                    stp->result = stp->iter;
+                } else if (stp->iter >= max_iter || stp->status == SIMALL_ERR_BREAKDOWN) {
+                    stp->done = 1;
+                    stp->result = stp->iter >= max_iter ? max_iter : stp->iter;
+                } else {
+                    stp->beta = tt[1] / stp->rz;
+                }
+            });
+            if (st.done)
+                break;
+            float acc2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, static_cast<float>(st.beta),
+                                  xh, acc2);
+            double t4[4];
+            cl_allreduce<4>(acc2, t4, sh, slot, cl, fresh_fin);
+        }
+        par ^= 1;
+    }
+    if (rank == 0 && threadIdx.x == 0) {
+        s->bnorm = st.bnorm;
+        s->last = st.last;
+        s->rr = st.rr64;
+        s->iter = st.iter;
+        s->result = st.result;
+        s->status = st.status;
+        s->updates = st.updates;
+        s->done = 1;
+    }
+    cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+}  // namespace
+
+namespace {
+
+// Whether `kernel` can run as one cluster of C CTAs with `smem` bytes of
+// dynamic shared memory each on this device.
+bool cluster_fits(simall_context *ctx, const void *kernel, int C, size_t smem)
+{
+    if (C > 8 && cudaFuncSetAttribute(kernel, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    if (cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)) !=
+        cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kClThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, kernel, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return clusters >= 1;
+}
+
+template <typename K, typename... Args>
+int launch_cluster(simall_context *ctx, K kernel, int C, size_t smem, Args... args)
+{
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(C);
+    cfg.blockDim = dim3(kClThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = ctx->stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SIMALL_CUDA_TRY(ctx, cudaLaunchKernelEx(&cfg, kernel, args...));
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+template <int RPT> int try_pcg64(simall_solver *s, int C, int logR, int *status)
+{
+    simall_context *ctx = s->ctx;
+    const size_t smem = sizeof(double) * (static_cast<size_t>(1) << logR);
+    if (!cluster_fits(ctx, reinterpret_cast<const void *>(k_cl_pcg64<RPT>), C, smem))
+        return 0;
+    const int st = launch_cluster(ctx, k_cl_pcg64<RPT>, C, smem, static_cast<int>(s->n), logR, s->rowPtr, s->colIdx,
+                                  s->values, static_cast<const double *>(s->invDiag.p),
+                                  static_cast<const double *>(s->b.p), s->x.p, s->scal.p);
+    *status = st ? st : solver_fetch_scalars(s);
+    s->engine = 1;
+    return 1;
+}
+
+template <int ND, int RPT> int try_mixed(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int *status)
+{
+    simall_context *ctx = s->ctx;
+    const size_t smem = 6 * sizeof(float) * (static_cast<size_t>(1) << logR);
+    if (!cluster_fits(ctx, reinterpret_cast<const void *>(k_cl_mixed<ND, RPT>), C, smem))
+        return 0;
+    const int st = launch_cluster(ctx, k_cl_mixed<ND, RPT>, C, smem, static_cast<int>(s->n), logR, a, s->rowPtr,
+                                  s->colIdx, s->values, static_cast<const double *>(s->b.p), s->x.p, s->scal.p);
+    *status = st ? st : solver_fetch_scalars(s);
+    s->engine = 1;
+    return 1;
+}
+
+template <int ND> int try_mixed_nd(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int *status)
+{
+    const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
+    return rpt <= 1   ? try_mixed<ND, 1>(s, a, C, logR, status)
+           : rpt <= 2 ? try_mixed<ND, 2>(s, a, C, logR, status)
+           : rpt <= 4 ? try_mixed<ND, 4>(s, a, C, logR, status)
+           : rpt <= 8 ? try_mixed<ND, 8>(s, a, C, logR, status)
+                      : try_mixed<ND, 16>(s, a, C, logR, status);
+}
+
+// Slice length (a power of two, at least 256 rows) and cluster size for n rows
+// on at most maxC CTAs; false when n does not fit.
+bool cluster_shape(int64_t n, int maxC, int *C, int *logR)
+{
+    int lr = 8;
+    while ((static_cast<int64_t>(maxC) << lr) < n)
+        ++lr;
+    if ((1 << lr) > kClMaxRowsPerCta)
+        return false;
+    *logR = lr;
+    *C = static_cast<int>((n + (1 << lr) - 1) >> lr);
+    return *C >= 1 && *C <= maxC;
+}
+
+}  // namespace
+
+// Mixed-precision CG on one cluster (diagonal storage, up to 4 diagonals).
+// Returns 0 (not taken) or 1 with *status set.
+int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status)
+{
+    if (s->n <= 0 || s->n > 16 * kClMaxRowsPerCta || s->cfg.max_iterations > kClMaxIterations || a.nd < 1 ||
+        a.nd > 4)
+        return 0;
+    for (int maxC : {16, 8}) {
+        int C = 0, logR = 0;
+        if (!cluster_shape(s->n, maxC, &C, &logR))
+            continue;
+        const int taken = a.nd == 1   ? try_mixed_nd<1>(s, a, C, logR, status)
+                          : a.nd == 2 ? try_mixed_nd<2>(s, a, C, logR, status)
+                          : a.nd == 3 ? try_mixed_nd<3>(s, a, C, logR, status)
+                                      : try_mixed_nd<4>(s, a, C, logR, status);
+        if (taken)
+            return 1;
+    }
+    return 0;
+}
+
+// FP64 Jacobi PCG on one cluster.  Returns 0 (not taken: the system does not
+// fit, or the device cannot run the cluster) or 1 with *status set.
+int cluster_fp64_solve(simall_solver *s, int *status)
+{
+    // one launch runs the whole solve: keep it short even when it does not converge
+    if (s->n <= 0 || s->n > 16 * kClMaxRowsPerCta || s->nnz > INT32_MAX || s->cfg.max_iterations > kClMaxIterations)
+        return 0;
+    for (int maxC : {16, 8}) {
+        int C = 0, logR = 0;
+        if (!cluster_shape(s->n, maxC, &C, &logR))
+            continue;
+        const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
+        const int taken = rpt <= 1    ? try_pcg64<1>(s, C, logR, status)
+                          : rpt <= 2  ? try_pcg64<2>(s, C, logR, status)
+                          : rpt <= 4  ? try_pcg64<4>(s, C, logR, status)
+                          : rpt <= 8  ? try_pcg64<8>(s, C, logR, status)
+                          : rpt <= 16 ? try_pcg64<16>(s, C, logR, status)
+                                      : 0;
+        if (taken)
+            return 1;
+    }
+    return 0;
+}
+
+}  // namespace simall

@@ -1101,6 +1101,19 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
                     cudaMemcpyAsync(&s->scal.p->delta, &delta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     SIMALL_CUDA_TRY(ctx,
                     cudaMemcpyAsync(&s->scal.p->max_iter, &maxit, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    if (m->dia && s->cfg.check_interval <= 0 && s->cfg.engine == SIMALL_ENGINE_AUTO) {
+        ClusterMixedArgs a{};
+        a.U = m->U.p;
+        a.ldU = m->ldU;
+        a.nd = m->offs.nd;
+        for (int d = 0; d < kMaxDiags && d < 8; ++d)
+            a.off[d] = m->offs.off[d];
+        a.e = m->e.p;
+        a.scale = m->scale.p;
+        int cst = SIMALL_OK;
+        if (cluster_mixed_solve(s, a, &cst))
+            return cst;
+    }
     k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rv[0].p, m->pv[1].p,
                                                           m->xh.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);

@@ -585,6 +585,12 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
                                          ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->max_iter, &init.max_iter, sizeof(int), cudaMemcpyHostToDevice,
                                          ctx->stream));
+    if (s->cfg.preconditioner == SIMALL_PRECOND_JACOBI && s->cfg.check_interval <= 0 &&
+        s->cfg.engine == SIMALL_ENGINE_AUTO) {
+        int cst = SIMALL_OK;
+        if (cluster_fp64_solve(s, &cst))
+            return cst;
+    }
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
         k_init_plain<<<g, kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
@@ -699,6 +705,7 @@ void simall_solver_config_default(simall_solver_config *cfg)
     cfg->precision = SIMALL_PRECISION_FP64;
     cfg->reliable_delta = 0.1;
     cfg->check_interval = 0;
+    cfg->engine = SIMALL_ENGINE_AUTO;
 }
 
 int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, simall_solver **out)
@@ -923,6 +930,7 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
     }
     simall_solver_stats local{};
     int st;
+    s->engine = 0;
     if (s->cfg.precision == SIMALL_PRECISION_MIXED)
         st = mixed_solve(s, &local);
     else
@@ -955,6 +963,8 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
         stats->b_norm = h.bnorm;
         stats->true_residual = std::sqrt(rr) / h.bnorm;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        stats->engine = s->engine;
+        stats->reserved = 0;
     }
     return SIMALL_OK;
 }

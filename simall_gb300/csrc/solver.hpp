@@ -52,6 +52,7 @@ struct simall_solver {
     double last_residual = 0.0;
     bool ready = false;
     bool solved = false;  // a solve completed on the current matrix
+    int engine = 0;       // of the last solve: 0 kernels per step, 1 one cluster
     simall::IluData *ilu = nullptr;
     simall::MixedData *mixed = nullptr;
     std::vector<simall::GraphChunk> graphs;  // captured iteration chunks
@@ -72,6 +73,20 @@ void mixed_free(simall_solver *s);
 
 // simall_solver_solve with separate memory kinds for b and x.
 int solver_solve_impl(simall_solver *s, const double *b, int bmem, double *x, int xmem, simall_solver_stats *stats);
+// Whole-solve FP64 Jacobi PCG on one thread-block cluster for systems that fit
+// (cluster.cu); 0 = not taken, 1 = taken with *status set.
+int cluster_fp64_solve(simall_solver *s, int *status);
+// The mixed solver's FP32 operator in diagonal storage (mixed.cu), for the
+// whole-solve mixed-precision CG on one cluster.
+struct ClusterMixedArgs {
+    const float *U;        // [nd][ldU] upper diagonals of S A S
+    int64_t ldU;
+    int nd;
+    int off[8];            // ascending offsets
+    const float *e;        // 1 + row sums of S A S (row-sum form)
+    const double *scale;   // S = D^-1/2
+};
+int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status);
 
 // Host copy of the current pattern (ILU0 level analysis, CSR fallbacks).
 int solver_host_pattern(simall_solver *s);

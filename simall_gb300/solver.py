@@ -174,7 +174,10 @@ class GpuCGSolver:
     """
 
     def __init__(self, cfg: LinearSolverConfig | None = None, precision: Precision = Precision.FP64,
-                 ctx: Context | None = None, reliable_delta: float = 0.1, check_interval: int = 0):
+                 ctx: Context | None = None, reliable_delta: float = 0.1, check_interval: int = 0,
+                 engine: int = 0):
+        """engine: 0 automatic (one thread-block cluster for systems that fit),
+        1 per-iteration kernels only."""
         cfg = cfg or LinearSolverConfig(kind=LinearSolverKind.CG)
         self.cfg = cfg
         self.ctx = ctx or default_context()
@@ -187,6 +190,7 @@ class GpuCGSolver:
         c.precision = int(precision)
         c.reliable_delta = float(reliable_delta)
         c.check_interval = int(check_interval)
+        c.engine = int(engine)
         h = C.c_void_p()
         check(self.L.simall_solver_create(self.ctx.handle, C.byref(c), C.byref(h)), self.ctx.handle)
         self.handle = h.value

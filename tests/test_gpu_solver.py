@@ -169,13 +169,39 @@ def test_mixed_device_loop_matches_host_polling(sg, ctx, oracle, dims, renumber)
     out = []
     for ci_ in (0, 6):
         s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx,
-                           check_interval=ci_)
+                           check_interval=ci_, engine=1)
         x = np.zeros(len(rhs))
         it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
         out.append((it, s.stats.reliable_updates, x))
-        assert s.stats.converged and s.stats.true_residual < 1e-9
+        assert s.stats.converged and s.stats.true_residual < 1e-9 and s.stats.engine == 0
     assert out[0][0] == out[1][0] and out[0][1] == out[1][1]
     assert bits_equal(out[0][2], out[1][2])
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (24, 20, 1), (13, 11, 9), (30, 40, 50)])
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_cluster_engine_matches_kernels(sg, ctx, oracle, dims, prec):
+    """The one-cluster solve of small systems against the per-iteration
+    kernels: FP64 takes the oracle's iteration count and x within 1e-10;
+    mixed reaches the FP64 true residual with an iteration count close to the
+    kernels' (the sums are taken in a different order)."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=dims, renumber=False, amp=0.0, pressure_zones=(1,))
+    precision = sg.Precision.FP64 if prec == "fp64" else sg.Precision.MIXED
+    res = {}
+    for engine in (0, 1):
+        s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=precision, ctx=ctx, engine=engine)
+        x = np.zeros(len(rhs))
+        it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+        assert s.stats.engine == (1 if engine == 0 else 0)
+        assert s.stats.converged and s.stats.true_residual < 1e-9
+        tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+        assert abs(tr - s.stats.true_residual) <= 1e-6 * tr
+        res[engine] = (it, x)
+    if prec == "fp64":
+        xo, ito, _ = oracle.cg(rp, ci, v, rhs, 0, 1e-9, 5000)
+        assert abs(res[0][0] - ito) <= 1 and rel(res[0][1], xo) <= 1e-10
+    else:
+        assert abs(res[0][0] - res[1][0]) <= 0.1 * res[1][0] + 2
 
 
 @pytest.mark.parametrize("check_interval", [0, 4])
