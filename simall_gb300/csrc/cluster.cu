@@ -62,10 +62,11 @@ __device__ __forceinline__ float warp_sum_fl(float v)
 }
 
 struct ClShared {
-    double part[2][4];   // this CTA's partial sums, two slots used alternately
-    double wsum[4][32];  // per-warp sums
-    double tot[4];       // the cluster totals, broadcast to the CTA
-    double ctl[8];       // scalars derived from the totals by one thread, broadcast
+    double inbox[2][16][4];  // every CTA's partial sums, pushed here by their owners; two slots used alternately
+    double wsum[4][32];      // per-warp sums (FP64 values)
+    float wsumf[4][32];      // per-warp sums (FP32 values)
+    double tot[4];           // the cluster totals, broadcast to the CTA
+    double ctl[8];           // scalars derived from the totals by one thread, broadcast
 };
 
 struct NoFinish {
@@ -96,9 +97,11 @@ constexpr int kClMaxCtas = 16;  // cluster sizes up to 16: 4 butterfly levels
 // Cluster-wide sum of NV values; every thread of every CTA receives the same
 // totals.  Sums within a CTA run in the values' own type (FP32 for the mixed
 // solver's per-thread partials, FP64 for the FP64 solver); the sum across the
-// CTAs -- the global reduction -- is FP64.  One warp per CTA reads the C
-// partials through the cluster window (every warp reading them serialised on
-// the owners' shared memory and cost ~5 us at 1024 threads).  The butterflies
+// CTAs -- the global reduction -- is FP64.  Each CTA pushes its partials into
+// every CTA's shared memory before the barrier (stores through the cluster
+// window, whose latency the barrier absorbs; the kernels start with a cluster
+// barrier so that no CTA writes into one that has not started), so after it
+// the sum reads only local shared memory.  The butterflies
 // run level by level over all NV values: on GB300's narrow FP64 pipe a chain
 // of FP64 adds costs ~100 cycles per level, so the NV chains must overlap and
 // use no more levels than there are warps or CTAs.  `fin(tot, ctl)` runs in one
@@ -116,29 +119,46 @@ __device__ __forceinline__ void cl_allreduce(const T (&v)[NV], double (&out)[NV]
     butterfly<5>(w);
     if (lane == 0) {
 #pragma unroll
-        for (int k = 0; k < NV; ++k)
-            sh.wsum[k][wid] = static_cast<double>(w[k]);
+        for (int k = 0; k < NV; ++k) {
+            if constexpr (sizeof(T) == 4)
+                sh.wsumf[k][wid] = w[k];
+            else
+                sh.wsum[k][wid] = w[k];
+        }
     }
     __syncthreads();
+    const int C = static_cast<int>(cl.num_blocks());
     if (wid == 0) {
         T c[NV];
 #pragma unroll
-        for (int k = 0; k < NV; ++k)
-            c[k] = lane < kClWarps ? static_cast<T>(sh.wsum[k][lane]) : T(0);
+        for (int k = 0; k < NV; ++k) {
+            if constexpr (sizeof(T) == 4)
+                c[k] = lane < kClWarps ? sh.wsumf[k][lane] : 0.0f;
+            else
+                c[k] = lane < kClWarps ? sh.wsum[k][lane] : 0.0;
+        }
         butterfly<kClWarpLevels>(c);
-        if (lane == 0) {
+        // Only lanes 0 .. kClWarps-1 hold the CTA's sum after that butterfly:
+        // take lane 0's before lane L pushes it to rank L.  (Pushing another
+        // lane's value gave the CTAs different totals, different branches,
+        // and CTAs that left while others still used their shared memory.)
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            c[k] = __shfl_sync(0xffffffffu, c[k], 0);
+        // push this CTA's partials into every CTA's inbox (lane L -> rank L)
+        if (lane < C) {
+            double *dst = cl.map_shared_rank(&sh.inbox[slot][cl.block_rank()][0], lane);
 #pragma unroll
             for (int k = 0; k < NV; ++k)
-                sh.part[slot][k] = static_cast<double>(c[k]);
+                dst[k] = static_cast<double>(c[k]);
         }
     }
     cl.sync();
     if (wid == 0) {
-        const int C = static_cast<int>(cl.num_blocks());
         double t[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k)
-            t[k] = lane < C ? *cl.map_shared_rank(&sh.part[slot][k], lane) : 0.0;
+            t[k] = lane < C ? sh.inbox[slot][lane][k] : 0.0;
         butterfly<4>(t);
         if (lane == 0) {
 #pragma unroll
@@ -180,6 +200,7 @@ __global__ void __launch_bounds__(kClThreads, 1)
 {
     const cg::cluster_group cl = cg::this_cluster();
     const int rank = static_cast<int>(cl.block_rank());
+    cl.sync();  // every CTA of the cluster has started before any shared memory is written remotely
     extern __shared__ __align__(16) double cl_sm[];
     double *ps = cl_sm;  // the direction of the owned rows
     const int R = 1 << logR;
@@ -425,6 +446,7 @@ __global__ void __launch_bounds__(kClThreads, 1)
 {
     const cg::cluster_group cl = cg::this_cluster();
     const int rank = static_cast<int>(cl.block_rank());
+    cl.sync();  // every CTA of the cluster has started before any shared memory is written remotely
     extern __shared__ __align__(16) double cl_sm[];
     const int R = 1 << logR;
     float *base = reinterpret_cast<float *>(cl_sm);  // r[0] r[1] q[0] q[1] p[0] p[1]
@@ -513,11 +535,14 @@ __global__ void __launch_bounds__(kClThreads, 1)
                                static_cast<float>(st.beta), xh, acc);
         double t[4];
         cl_allreduce<4>(acc, t, sh, slot, cl, [stp, tol, delta, max_iter](const double *tt, double *) {
+            // the trigger and the estimate in FP32 (one thread; FP64 divides and
+            // square roots are long chains on GB300's narrow FP64 pipe)
             stp->iter += 1;
-            const double sigma = sqrtf(static_cast<float>(tt[2]));  // trigger and estimate: FP32 is plenty
-            const double est = stp->t0 * __fdiv_rn(static_cast<float>(sigma), static_cast<float>(stp->sigma0));
+            const float sigma = sqrtf(static_cast<float>(tt[2]));
+            const float est = static_cast<float>(stp->t0) * __fdiv_rn(sigma, static_cast<float>(stp->sigma0));
             stp->last = est;
-            if (stp->need || sigma < delta * stp->rmax || est < tol || stp->iter >= max_iter) {
+            if (stp->need || sigma < static_cast<float>(delta) * static_cast<float>(stp->rmax) ||
+                est < static_cast<float>(tol) || stp->iter >= max_iter) {
                 stp->need = 1;
                 return;
             }
