@@ -78,8 +78,7 @@ def parse():
     return ap.parse_args()
 
 
-def rank_info():
-    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+from simall_gb300.replicas import max_over_ranks, rank_info, shard_by_cost  # noqa: E402
 
 
 # ------------------------------------------------------------------ clocks
@@ -196,17 +195,23 @@ def time_kernel(s, k, reps=20):
     return ms.value, by.value
 
 
-def run_batched(a, ctx, sg):
+def run_batched(a, ctx, sg, rank=0, world=1):
     """Batched leg: `count` cavity pressure systems (sides log-uniform in
     [32, 256], rhs N(0,1) with mean removed, one pinned cell) solved in one
     persistent launch (mixed precision) against a loop of plain FP64
-    Jacobi-PCG solves of the same systems with the matrices resident."""
+    Jacobi-PCG solves of the same systems with the matrices resident.  With
+    N ranks the systems are shared out by size (no exchange between ranks) and
+    the reported time is the slowest rank's."""
     import torch
     from simall_gb300 import workloads as W
 
     count = a.batched_systems
     t0 = time.perf_counter()
     systems, rhs, sides = W.batched_cavity_systems(count=count, seed=SEED, ctx=ctx)
+    if world > 1:
+        mine = shard_by_cost(np.asarray(sides, np.float64) ** 2, rank, world)
+        systems = [systems[i] for i in mine]
+        rhs = [rhs[i] for i in mine]
     cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
                                 tolerance=a.tol, maxIterations=a.max_iterations)
     B = sg.BatchedSolver(cfg, ctx=ctx)
@@ -225,7 +230,7 @@ def run_batched(a, ctx, sg):
         _, st = B.solve(b, x)
     e1.record(stream)
     e1.synchronize()
-    batch_ms = e0.elapsed_time(e1) / a.steps
+    batch_ms = max_over_ranks(e0.elapsed_time(e1) / a.steps, device=b.device)
     tot = B.total
     # baseline: one FP64 solver per system, matrix resident, solves in a loop
     solvers, bs, xs = [], [], []
@@ -243,7 +248,7 @@ def run_batched(a, ctx, sg):
     for s, bb, xx in zip(solvers, bs, xs):
         its += s.solve_into(bb, xx)
     torch.cuda.synchronize()
-    loop_s = time.perf_counter() - t
+    loop_s = max_over_ranks(time.perf_counter() - t, device=b.device)
     xb = x.cpu().numpy()
     diff = max(float(np.linalg.norm(xb[rows[i]:rows[i + 1]] - xs[i].cpu().numpy()) /
                      max(np.linalg.norm(xs[i].cpu().numpy()), 1e-30)) for i in range(len(systems)))
@@ -256,7 +261,7 @@ def run_batched(a, ctx, sg):
             "converged": int(tot.converged), "systems": int(tot.systems), "max_iterations": int(tot.max_iterations),
             "total_iterations": int(tot.total_iterations), "worst_true_residual": float(tot.worst_true_residual),
             "max_rel_diff_vs_fp64": diff, "launch_shape": [int(tot.block_threads), int(tot.ctas_per_sm)],
-            "setup_seconds": round(setup, 2)}
+            "setup_seconds": round(setup, 2), "ranks": world, "systems_on_rank0": len(systems)}
 
 
 def run_adjoint(a, ctx, sg):
@@ -484,11 +489,7 @@ def run_ours(a, rank, world, local):
         e1.record(stream)
         e1.synchronize()
         barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if world > 1:
-            tt = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-            ms = float(tt.item())
+        ms = max_over_ranks(e0.elapsed_time(e1) / steps, device=dev)
         return ms, ctx.kernel_launches - l0
 
     # warm-up: W mixed solves, one FP64 solve
@@ -591,7 +592,7 @@ def run_ours(a, rank, world, local):
     if accuracy:
         out["accuracy"] = accuracy
     if a.batched_systems > 0:
-        out["batched"] = run_batched(a, ctx, sg)
+        out["batched"] = run_batched(a, ctx, sg, rank, world)
     if a.adjoint_n > 0:
         out["adjoint"] = run_adjoint(a, ctx, sg)
     if a.poisson_n > 0:
