@@ -46,9 +46,9 @@ SEED = 42
 # benchmark's own FP64 leg).  The reference leg scales its bounded sample by it.
 FP64_ITERATIONS = {256: 1865}
 # DRAM bytes (read + write) per row of one launch of the fused mixed step, from
-# one ncu capture at 200^3 (profiles/mixed_step_varcoef200.md: 224.2 MB read +
-# 97.3 MB written for 8,000,000 rows); scaled by the rows of the workload.
-NCU_STEP_DRAM_BYTES_PER_ROW = (224.2432e6 + 97.283328e6) / 8.0e6
+# one ncu capture at 200^3 (profiles/mixed_step_varcoef200.md: 255.99 MB read +
+# 99.92 MB written for 8,000,000 rows); scaled by the rows of the workload.
+NCU_STEP_DRAM_BYTES_PER_ROW = (255.991552e6 + 99.923968e6) / 8.0e6
 
 
 def parse():
