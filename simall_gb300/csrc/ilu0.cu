@@ -9,6 +9,15 @@
 // products and differences are rounded separately (__dmul_rn/__dsub_rn) and
 // in column order, so the factor and both sweeps are bit-identical to the
 // reference.  Multicolouring would be faster but changes the factor.
+//
+// The factorisation (once per solve) launches one kernel per level.  The
+// sweeps (twice per PCG iteration) run as one kernel each without levels
+// between launches: warps take 32 consecutive rows of the level order from an
+// atomic ticket, and a row waits only for the rows it reads, each of which
+// publishes its value and then its "done" mark (release) and is read after the
+// mark (acquire).  Rows are handed out in level order, so every row waited for
+// was handed to a warp that is already running; the wait is bounded and a
+// timeout is reported (it never happens unless a row is never produced).
 #include "device.cuh"
 #include "solver.hpp"
 
@@ -98,6 +107,182 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_level(const int32_t *__restr
     z[i] = (kd >= 0 && lu[kd] != 0.0) ? __ddiv_rn(s, lu[kd]) : s;
 }
 
+__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
+{
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
+{
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr unsigned kSweepMaxSpins = 1u << 20;  // ~0.5 s of polling: far beyond any dependency chain
+
+// Wait until row j carries the current sweep's mark; false on timeout.  The
+// first polls are immediate (the row is usually done or nearly so); later
+// ones back off so that thousands of waiting warps do not flood L2 while the
+// rows they wait for are being computed.
+__device__ __forceinline__ bool wait_row(const unsigned *done, int j, unsigned sweep)
+{
+    unsigned ns = 16;
+    for (unsigned spins = 0; ld_acquire(done + j) != sweep; ++spins) {
+        if (spins >= kSweepMaxSpins)
+            return false;
+        if (spins >= 4) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : 256;
+        }
+    }
+    return true;
+}
+
+// Next sweep: reset the ticket, advance the sweep number.
+__global__ void k_sweep_begin(unsigned *ctl)
+{
+    ctl[0] = 0u;
+    ctl[1] += 1u;
+}
+
+// Waits for up to 4 rows at once (their marks polled together), so a row
+// with several dependencies costs one memory round trip per poll, not one per
+// dependency; false on timeout.
+__device__ __forceinline__ bool wait_rows4(const unsigned *done, const int (&j)[4], int cnt, unsigned sweep)
+{
+    unsigned ns = 16;
+    for (unsigned spins = 0;; ++spins) {
+        bool all = true;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (q < cnt)
+                all = (ld_acquire(done + j[q]) == sweep) && all;
+        if (all)
+            return true;
+        if (spins >= kSweepMaxSpins)
+            return false;
+        if (spins >= 4) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : 256;
+        }
+    }
+}
+
+// Forward sweep y_i = r_i - sum_{j<i} l_ij y_j over rows in level order.
+// Dependencies are taken four at a time: wait for the four marks, load the
+// four values, then apply them in column order (the reference's order).
+__global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *__restrict__ order,
+                                                         const int32_t *__restrict__ rowPtr,
+                                                         const int32_t *__restrict__ colIdx,
+                                                         const double *__restrict__ lu, const double *__restrict__ r,
+                                                         double *y, unsigned *done, unsigned *ctl)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned sweep = __ldcg(ctl + 1);
+    bool ok = true;
+    for (;;) {
+        int base = 0;
+        if (lane == 0)
+            base = static_cast<int>(atomicAdd(ctl, 32u));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int t = base + lane;
+        if (t < n) {
+            const int i = __ldg(order + t);
+            double s = __ldg(r + i);
+            const int end = __ldg(rowPtr + i + 1);
+            for (int kp = __ldg(rowPtr + i); kp < end;) {
+                int j[4];
+                double a[4];
+                int cnt = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const bool in = kp + q < end;
+                    const int jj = in ? __ldg(colIdx + kp + q) : i;
+                    a[q] = in ? __ldg(lu + kp + q) : 0.0;  // the row's own data: loaded before the wait
+                    j[q] = jj < i ? jj : i;
+                    cnt += (jj < i && cnt == q) ? 1 : 0;
+                }
+                if (cnt == 0)
+                    break;
+                ok = wait_rows4(done, j, cnt, sweep) && ok;
+                double v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    v[q] = q < cnt ? __ldcg(y + j[q]) : 0.0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < cnt)
+                        s = __dsub_rn(s, __dmul_rn(a[q], v[q]));
+                kp += cnt;
+                if (cnt < 4)
+                    break;
+            }
+            __stcg(y + i, s);
+            st_release(done + i, sweep);
+        }
+    }
+    if (!ok)
+        atomicOr(ctl + 2, 1u);
+}
+
+// Backward sweep z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii over rows in level order.
+__global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *__restrict__ order,
+                                                         const int32_t *__restrict__ rowPtr,
+                                                         const int32_t *__restrict__ colIdx,
+                                                         const int32_t *__restrict__ diagPtr,
+                                                         const double *__restrict__ lu, const double *__restrict__ y,
+                                                         double *z, unsigned *done, unsigned *ctl)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned sweep = __ldcg(ctl + 1);
+    bool ok = true;
+    for (;;) {
+        int base = 0;
+        if (lane == 0)
+            base = static_cast<int>(atomicAdd(ctl, 32u));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int t = base + lane;
+        if (t < n) {
+            const int i = __ldg(order + t);
+            double s = __ldcg(y + i);
+            const int kd = __ldg(diagPtr + i);
+            const int end = __ldg(rowPtr + i + 1);
+            for (int kp = kd + 1; kp < end;) {
+                int j[4];
+                double a[4];
+                int cnt = 0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const bool in = kp + q < end;
+                    j[q] = in ? __ldg(colIdx + kp + q) : i;
+                    a[q] = in ? __ldg(lu + kp + q) : 0.0;
+                    cnt += in ? 1 : 0;
+                }
+                ok = wait_rows4(done, j, cnt, sweep) && ok;
+                double v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    v[q] = q < cnt ? __ldcg(z + j[q]) : 0.0;
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    if (q < cnt)
+                        s = __dsub_rn(s, __dmul_rn(a[q], v[q]));
+                kp += cnt;
+            }
+            const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
+            __stcg(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
+            st_release(done + i, sweep);
+        }
+    }
+    if (!ok)
+        atomicOr(ctl + 2, 1u);
+}
+
 __global__ void k_zero_pivot_check(int n, const int32_t *__restrict__ diagPtr, const double *__restrict__ lu, int *flag)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -174,6 +359,10 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
     SIMALL_CUDA_TRY(ctx, d->fwdRows.alloc(n));
     SIMALL_CUDA_TRY(ctx, d->bwdRows.alloc(n));
     SIMALL_CUDA_TRY(ctx, d->y.alloc(n));
+    SIMALL_CUDA_TRY(ctx, d->done.alloc(n));
+    SIMALL_CUDA_TRY(ctx, d->sweepCtl.alloc(4));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->done.p, 0, n * sizeof(unsigned), ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->sweepCtl.p, 0, 4 * sizeof(unsigned), ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->diagPtr.p, d->h_diagPtr.data(), n * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->fwdRows.p, fr.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice,
@@ -201,20 +390,18 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
 int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx, const double *lu,
            const double *r, double *z)
 {
-    const int nf = static_cast<int>(d->fwdLevelPtr.size()) - 1;
-    for (int l = 0; l < nf; ++l) {
-        const int a = d->fwdLevelPtr[l], cnt = d->fwdLevelPtr[l + 1] - a;
-        k_ilu_fwd_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->fwdRows.p + a, cnt, rowPtr,
-                                                                                 colIdx, lu, r, d->y.p);
-        SIMALL_LAUNCH_CHECK(ctx);
-    }
-    const int nb = static_cast<int>(d->bwdLevelPtr.size()) - 1;
-    for (int l = 0; l < nb; ++l) {
-        const int a = d->bwdLevelPtr[l], cnt = d->bwdLevelPtr[l + 1] - a;
-        k_ilu_bwd_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->bwdRows.p + a, cnt, rowPtr,
-                                                                                 colIdx, d->diagPtr.p, lu, d->y.p, z);
-        SIMALL_LAUNCH_CHECK(ctx);
-    }
+    const int n = static_cast<int>(d->h_diagPtr.size());
+    const int grid = ctx->num_sms * 4;  // 32 warps per SM take rows; more only add waiting warps
+    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_ilu_fwd_free<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->y.p, d->done.p,
+                                                     d->sweepCtl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    k_ilu_bwd_free<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, z,
+                                                     d->done.p, d->sweepCtl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
 
@@ -247,6 +434,22 @@ int ilu_apply(simall_solver *s, const double *r, double *z)
 {
     return sweeps(s->ctx, s->ilu, s->rowPtr, s->colIdx, s->ilu->lu.p, r, z);
 }
+
+// Whether a sweep gave up waiting for a row (a device-side timeout); clears
+// the flag.
+int ilu_check(simall_context *ctx, IluData *d)
+{
+    unsigned h = 0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, d->sweepCtl.p + 2, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (h) {
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->sweepCtl.p + 2, 0, sizeof(unsigned), ctx->stream));
+        return fail(ctx, SIMALL_ERR_CUDA, "ILU(0) sweep: a row wait timed out");
+    }
+    return SIMALL_OK;
+}
+
+int ilu_check(simall_solver *s) { return s->ilu ? ilu_check(s->ctx, s->ilu) : SIMALL_OK; }
 
 void ilu_free(simall_solver *s)
 {
@@ -359,6 +562,8 @@ int simall_gpu_ilu0_apply(size_t n, const int32_t *rowPtr, const int32_t *colIdx
         st = sweeps(&f->ctx, &f->d, rowPtr, colIdx, values, r, z);
     if (!st && cudaStreamSynchronize(f->ctx.stream) != cudaSuccess)
         st = SIMALL_ERR_CUDA;
+    if (!st)
+        st = ilu_check(&f->ctx, &f->d);
     delete f;
     return st;
 }

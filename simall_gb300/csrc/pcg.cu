@@ -538,7 +538,7 @@ int enqueue_iteration(simall_solver *s)
 int64_t kernels_per_iteration(const simall_solver *s)
 {
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 && s->ilu)
-        return 4 + static_cast<int64_t>(s->ilu->fwdLevelPtr.size() - 1) + static_cast<int64_t>(s->ilu->bwdLevelPtr.size() - 1);
+        return 4 + 4;  // SpMV, x/r update, r.z/beta, direction + two sweeps with their resets
     return 3;
 }
 
@@ -605,9 +605,8 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
         SIMALL_LAUNCH_CHECK(ctx);
     }
     int done_iters = 0;
-    const bool ilu = s->cfg.preconditioner == SIMALL_PRECOND_ILU0;
-    const int max_chunk = ilu ? 8 : 64;  // an ILU0 iteration is one graph node per level
-    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : (ilu ? 8 : 16);
+    const int max_chunk = 64;
+    int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 16;
     double prev_last = -1.0;
     int prev_iter = 0;
     for (;;) {
@@ -935,6 +934,8 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
         st = mixed_solve(s, &local);
     else
         st = fp64_solve(s, &local);
+    if (!st && s->cfg.preconditioner == SIMALL_PRECOND_ILU0)
+        st = ilu_check(s);
     if (st)
         return st;
     // FP64 true residual of the returned x (r buffer is free after the loop)

@@ -12,6 +12,8 @@ struct IluData {
     DevBuf<int32_t> fwdRows;    // rows grouped by forward level
     DevBuf<int32_t> bwdRows;    // rows grouped by backward level
     DevBuf<double> y;           // forward-sweep scratch
+    DevBuf<unsigned> done;      // sweeps: done[i] == sweep number once row i is final
+    DevBuf<unsigned> sweepCtl;  // sweeps: [0] work ticket, [1] sweep number, [2] wait-timeout flag
     std::vector<int32_t> fwdLevelPtr, bwdLevelPtr;  // level boundaries into fwdRows / bwdRows (host)
     std::vector<int32_t> h_diagPtr;
     int maxLevelRows = 0;
@@ -61,6 +63,7 @@ struct simall_solver {
 namespace simall {
 
 int ilu_setup(simall_solver *s);
+int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);
 void ilu_free(simall_solver *s);
 
