@@ -251,6 +251,14 @@ int simall_adjoint_face_conductance(simall_pressure_system *ps, simall_solver *s
                                     const double *pb, const double *x, const double *dLdx, double *lambda,
                                     double *dk, double *dpb, int mem, simall_solver_stats *stats);
 
+/* ------------------------------------------------------------------ diagnostics */
+/* Failure detection without a GPU fault (no reference counterpart): runs one
+ * warp that waits, with the same bounded wait as the ILU(0) sweeps, for a mark
+ * that nothing sets.  *timed_out = 1 when the wait ran out and the kernel
+ * returned on its own (the expected result), *seconds = the wall time of the
+ * call (the bound is about a second).  The context stays usable. */
+int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds);
+
 /* ------------------------------------------------------------------ batched solves */
 /* Many independent SPD systems of uneven size (e.g. one pressure-correction
  * system per cavity, block or time level) solved in one persistent launch:

@@ -22,6 +22,7 @@
 #include "solver.hpp"
 
 #include <algorithm>
+#include <chrono>
 #include <new>
 
 namespace simall {
@@ -283,6 +284,16 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
         atomicOr(ctl + 2, 1u);
 }
 
+// One warp waits for a mark that nothing sets: the bounded wait of the sweeps
+// running out, observed from the host.
+__global__ void k_wait_probe(const unsigned *flag, unsigned *out)
+{
+    const int j[4] = {0, 0, 0, 0};
+    const bool ok = wait_rows4(flag, j, 1, 1u);
+    if (threadIdx.x == 0)
+        out[0] = ok ? 0u : 1u;
+}
+
 __global__ void k_zero_pivot_check(int n, const int32_t *__restrict__ diagPtr, const double *__restrict__ lu, int *flag)
 {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -540,6 +551,26 @@ int simall_gpu_ilu0_factor_inplace(size_t n, const int32_t *rowPtr, const int32_
     }
     delete f;
     return st;
+}
+
+int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds)
+{
+    if (!ctx || !timed_out)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    DevBuf<unsigned> buf;
+    SIMALL_CUDA_TRY(ctx, buf.alloc(2));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(buf.p, 0, 2 * sizeof(unsigned), ctx->stream));
+    const auto t0 = std::chrono::steady_clock::now();
+    k_wait_probe<<<1, 32, 0, ctx->stream>>>(buf.p, buf.p + 1);
+    SIMALL_LAUNCH_CHECK(ctx);
+    unsigned h = 0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, buf.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    *timed_out = static_cast<int>(h);
+    if (seconds)
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return SIMALL_OK;
 }
 
 int simall_gpu_ilu0_apply(size_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
