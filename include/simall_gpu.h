@@ -214,6 +214,14 @@ int simall_pressure_system_device_arrays(const simall_pressure_system *ps, const
  * receives 1 when a pressure boundary anchors the system (no cell-0 pin). */
 int simall_assemble_pressure_correction(simall_pressure_system *ps, double rho, const double *aP,
                                         const double *phi, int mem, int *any_dirichlet);
+/* The same for SIMPLEC (PvCouplingVariant::SIMPLEC): the denominator of every
+ * cell is max(aP_c - sum_{k != c} |a_mom,ck|, 1e-30) instead of max(aP_c, 1e-30)
+ * (SimpleAlgorithm.cpp:380-390, 401-409), with mom_values the momentum matrix
+ * A_mom_ on the pressure system's pattern (build_sparsity gives A_mom_ and A_p_
+ * one pattern; nnz values in its order). */
+int simall_assemble_pressure_correction_simplec(simall_pressure_system *ps, double rho, const double *aP,
+                                                const double *mom_values, const double *phi, int mem,
+                                                int *any_dirichlet);
 /* Host copies of the assembled values[nnz] and rhs[n]. */
 int simall_pressure_system_download(const simall_pressure_system *ps, double *values, double *rhs);
 /* Points the solver at the system's device CSR (no copy) and runs the

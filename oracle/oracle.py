@@ -56,6 +56,8 @@ def lib():
         L.orc_rcm.argtypes = [_I64, _I64] + [_P] * 10
         L.orc_build_sparsity.restype = _I64
         L.orc_build_sparsity.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
+        L.orc_simplec_denominator.restype = None
+        L.orc_simplec_denominator.argtypes = [_I64] + [_P] * 5
         L.orc_assemble.restype = C.c_int
         L.orc_assemble.argtypes = [_I64, _I64] + [_P] * 13 + [C.c_int, _D] + [_P] * 6
         L.orc_dot.restype = _D
@@ -181,6 +183,17 @@ def build_sparsity(m: Mesh):
     return rowPtr, colIdx
 
 
+def simplec_denominator(rowPtr, colIdx, mom, aP):
+    """SIMPLEC per-cell denominator (SimpleAlgorithm.cpp:380-390)."""
+    n = len(rowPtr) - 1
+    den = np.empty(n)
+    lib().orc_simplec_denominator(n, _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+                                  _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                                  _ptr(np.ascontiguousarray(mom, np.float64)),
+                                  _ptr(np.ascontiguousarray(aP, np.float64)), _ptr(den))
+    return den
+
+
 def assemble(m: Mesh, rowPtr, colIdx, pressure_zones, rho, aP, phi):
     """assemble_pressure_correction; pressure_zones = zone ids with a
     PressureOutlet/PressureInlet condition.  Returns (values, rhs, anyDirichlet)."""
@@ -303,6 +316,8 @@ class RefLib:
         L.ref_sparsity_nnz.argtypes = [_P]
         L.ref_assemble.restype = C.c_int
         L.ref_assemble.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 6
+        L.ref_assemble_simplec.restype = C.c_int
+        L.ref_assemble_simplec.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 7
         L.ref_cg.restype = C.c_int
         L.ref_cg.argtypes = [C.c_int, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P, _P]
         L.ref_precond_apply.argtypes = [C.c_int, C.c_int] + [_P] * 5
@@ -398,6 +413,24 @@ class RefLib:
         phi = np.ascontiguousarray(phi, np.float64)
         L.ref_assemble(h, len(bcs), _ptr(zones), _ptr(types), rho, _ptr(aP), _ptr(phi), _ptr(rowPtr),
                        _ptr(colIdx), _ptr(values), _ptr(rhs))
+        return rowPtr, colIdx, values, rhs
+
+    def assemble_simplec(self, mesh_dict, bcs, rho, aP, mom, phi):
+        """assemble_pressure_correction with PvCouplingVariant::SIMPLEC, the
+        momentum matrix A_mom_ given by its values on the shared pattern."""
+        L = self.L
+        h = mesh_dict["handle"]
+        nnz = L.ref_sparsity_nnz(h)
+        nC = mesh_dict["nC"]
+        zones = np.array([z for z, _ in bcs] or [0], np.uint32)
+        types = np.array([t for _, t in bcs] or [0], np.int32)
+        rowPtr = np.empty(nC + 1, np.int32)
+        colIdx = np.empty(nnz, np.int32)
+        values = np.empty(nnz)
+        rhs = np.empty(nC)
+        L.ref_assemble_simplec(h, len(bcs), _ptr(zones), _ptr(types), rho, _ptr(np.ascontiguousarray(aP, np.float64)),
+                               _ptr(np.ascontiguousarray(mom, np.float64)), _ptr(np.ascontiguousarray(phi, np.float64)),
+                               _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(rhs))
         return rowPtr, colIdx, values, rhs
 
     # -- solvers

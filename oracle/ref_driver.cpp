@@ -59,6 +59,16 @@ public:
         phiFlux_.assign(phi, phi + nF);
         assemble_pressure_correction();
     }
+    // SIMPLEC: the momentum matrix's values on the shared pattern
+    void assemble_simplec(const double* aP, const double* mom, const double* phi)
+    {
+        build_sparsity();
+        const std::size_t nC = mesh_.cells().size(), nF = mesh_.faces().size();
+        aP_.assign(aP, aP + nC);
+        phiFlux_.assign(phi, phi + nF);
+        A_mom_.values.assign(mom, mom + A_mom_.colIdx.size());
+        assemble_pressure_correction();
+    }
     const S::CSRMatrix& Ap() const { return A_p_; }
     const Vec& rhs() const { return rhs_; }
     const Vec& aP() const { return aP_; }
@@ -246,6 +256,28 @@ int ref_assemble(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTy
     o.rho = rho;
     AssemblyProbe p(m, f, bcs, *s1, *s2, o);
     p.assemble(aP, phi);
+    const auto& A = p.Ap();
+    std::copy(A.rowPtr.begin(), A.rowPtr.end(), rowPtr);
+    std::copy(A.colIdx.begin(), A.colIdx.end(), colIdx);
+    std::copy(A.values.begin(), A.values.end(), values);
+    std::copy(p.rhs().begin(), p.rhs().end(), rhs);
+    return 0;
+}
+
+int ref_assemble_simplec(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, double rho,
+                         const double* aP, const double* mom, const double* phi, std::int32_t* rowPtr,
+                         std::int32_t* colIdx, double* values, double* rhs)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    auto bcs = make_bcs(nbc, bcZones, bcTypes);
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    S::SimpleOptions o;
+    o.rho = rho;
+    o.algorithm = S::PvCouplingVariant::SIMPLEC;
+    AssemblyProbe p(m, f, bcs, *s1, *s2, o);
+    p.assemble_simplec(aP, mom, phi);
     const auto& A = p.Ap();
     std::copy(A.rowPtr.begin(), A.rowPtr.end(), rowPtr);
     std::copy(A.colIdx.begin(), A.colIdx.end(), colIdx);

@@ -554,6 +554,22 @@ int orc_assemble(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *ne
 /* ------------------------------------------------------------------ BLAS-1 + SpMV */
 
 /* dot / norm2 / axpy (src/solver/LinearSolvers.cpp:25-43) */
+/* SIMPLEC denominator, SimpleAlgorithm.cpp:380-390 and 401-409: per cell
+ * max(aP_c - sum_{k != c} |a_mom,ck|, 1e-30), the sum in column order from
+ * 0.0.  Passing den as aP to orc_assemble gives the SIMPLEC system, because
+ * the assembly's own max(aP, 1e-30) leaves den unchanged. */
+void orc_simplec_denominator(int64_t nC, const int32_t *rowPtr, const int32_t *colIdx, const double *mom,
+                             const double *aP, double *den)
+{
+    for (int64_t c = 0; c < nC; ++c) {
+        double sumOff = 0.0;
+        for (int32_t k = rowPtr[c]; k < rowPtr[c + 1]; ++k)
+            if (colIdx[k] != (int32_t)c)
+                sumOff += fabs(mom[k]);
+        den[c] = STD_MAX(aP[c] - sumOff, 1e-30);
+    }
+}
+
 double orc_dot(int64_t n, const double *a, const double *b)
 {
     double s = 0;

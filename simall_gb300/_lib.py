@@ -88,6 +88,7 @@ SIGNATURES = {
     "simall_pressure_system_pattern": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64), _P, _P]),
     "simall_pressure_system_device_arrays": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "simall_assemble_pressure_correction": (_I, [_P, _D, _P, _P, _I, C.POINTER(_I)]),
+    "simall_assemble_pressure_correction_simplec": (_I, [_P, _D, _P, _P, _P, _I, C.POINTER(_I)]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),

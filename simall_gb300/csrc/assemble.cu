@@ -41,6 +41,7 @@ struct simall_pressure_system {
     simall::DevBuf<int32_t> cfOff, cfEnt, cfSlot, diagSlot;
     int anyDirichlet = 0;
     simall::DevBuf<double> aP, phi;  // staging for host inputs
+    simall::DevBuf<double> den;      // SIMPLEC denominators
     simall::DevBuf<double> kf, pbf;  // staging for face-conductance inputs
 };
 
@@ -246,6 +247,28 @@ __global__ void __launch_bounds__(kBlock) k_face_k_gradient(int64_t nF, double r
 }  // namespace simall
 
 using namespace simall;
+
+namespace simall {
+namespace {
+
+// SIMPLEC denominator (SimpleAlgorithm.cpp:380-390, 401-409):
+// den_c = max(aP_c - sum_{k != c} |a_mom,ck|, 1e-30), the sum in column order.
+__global__ void __launch_bounds__(kBlock) k_simplec_den(int64_t nC, const int32_t *__restrict__ rowPtr,
+                                                        const int32_t *__restrict__ colIdx,
+                                                        const double *__restrict__ mom, const double *__restrict__ aP,
+                                                        double *__restrict__ den)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nC; c += (int64_t)gridDim.x * blockDim.x) {
+        double sumOff = 0.0;
+        for (int k = rowPtr[c]; k < rowPtr[c + 1]; ++k)
+            if (colIdx[k] != c)
+                sumOff = __dadd_rn(sumOff, fabs(mom[k]));
+        den[c] = std_max(__dsub_rn(aP[c], sumOff), 1e-30);
+    }
+}
+
+}  // namespace
+}  // namespace simall
 
 extern "C" {
 
@@ -476,6 +499,42 @@ int simall_pressure_system_device_arrays(const simall_pressure_system *ps, const
     if (rhs)
         *rhs = ps->rhs.p;
     return SIMALL_OK;
+}
+
+int simall_assemble_pressure_correction_simplec(simall_pressure_system *ps, double rho, const double *aP,
+                                                const double *mom_values, const double *phi, int mem,
+                                                int *any_dirichlet)
+{
+    if (!ps || !aP || !mom_values || !phi)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = ps->ctx;
+    if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "assemble: bad memory kind %d", mem);
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t st = ctx->stream;
+    const double *dA = aP, *dM = mom_values, *dPhi = phi;
+    DevBuf<double> stageA, stageM, stageP;
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, stageA.alloc(ps->nC));
+        SIMALL_CUDA_TRY(ctx, stageM.alloc(ps->nnz));
+        SIMALL_CUDA_TRY(ctx, stageP.alloc(ps->nF));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(stageA.p, aP, ps->nC * sizeof(double), cudaMemcpyHostToDevice, st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(stageM.p, mom_values, ps->nnz * sizeof(double), cudaMemcpyHostToDevice,
+                                             st));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(stageP.p, phi, ps->nF * sizeof(double), cudaMemcpyHostToDevice, st));
+        dA = stageA.p;
+        dM = stageM.p;
+        dPhi = stageP.p;
+    }
+    SIMALL_CUDA_TRY(ctx, ps->den.alloc(ps->nC));
+    const int gc = static_cast<int>(std::min<int64_t>((ps->nC + kBlock - 1) / kBlock, grid_size_streaming(ctx)));
+    k_simplec_den<<<gc, kBlock, 0, st>>>(ps->nC, ps->rowPtr.p, ps->colIdx.p, dM, dA, ps->den.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    // max(den, 1e-30) is unchanged by the assembly's own max(., 1e-30)
+    int r = simall_assemble_pressure_correction(ps, rho, ps->den.p, dPhi, SIMALL_MEM_DEVICE, any_dirichlet);
+    if (mem == SIMALL_MEM_HOST)
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // the staging buffers die at return
+    return r;
 }
 
 int simall_assemble_pressure_correction(simall_pressure_system *ps, double rho, const double *aP, const double *phi,

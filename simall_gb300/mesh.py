@@ -161,6 +161,19 @@ class PressureSystem:
               self.ctx.handle)
         self.any_dirichlet = bool(anyD.value)
 
+    def assemble_simplec(self, rho: float, aP, mom_values, phi):
+        """SIMPLEC variant: denominators max(aP - sum|offdiag(A_mom)|, 1e-30),
+        mom_values = the momentum matrix's values on this system's pattern."""
+        pa, ma = ptr_and_mem(aP)
+        pm, mm = ptr_and_mem(mom_values)
+        pp, mp = ptr_and_mem(phi)
+        if not (ma == mm == mp):
+            raise ValueError("aP, mom_values and phi must live in the same memory")
+        anyD = C.c_int()
+        check(self.L.simall_assemble_pressure_correction_simplec(self.handle, float(rho), pa, pm, pp, ma,
+                                                                 C.byref(anyD)), self.ctx.handle)
+        self.any_dirichlet = bool(anyD.value)
+
     def assemble_face_conductance(self, rho: float, k, pb, src):
         """Face-conductance operator: coef_f = k_f g_f, Dirichlet values pb on
         pressure-boundary faces, rhs from the cell source src."""

@@ -86,6 +86,26 @@ def cavity_case_full_size(name, N, n_outer):
                         p_solve_seconds=np.array(c["p_solve_seconds"]))
 
 
+def simplec_case(name):
+    """SIMPLEC assembly (PvCouplingVariant::SIMPLEC) on a distorted 6x5x4 box
+    with an outlet on zone 1, seeded aP, momentum values and fluxes; some
+    cells' off-diagonal sums exceed aP (the 1e-30 clamp)."""
+    dims = (6, 5, 4)
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=11)
+    m = O.cartesian_mesh(*dims, node_shift=shift)
+    rp, ci = O.build_sparsity(m)
+    rng = np.random.default_rng(11)
+    aP = rng.uniform(1.0, 3.0, m.nC)
+    mom = rng.standard_normal(len(ci)) * 0.4
+    phi = rng.standard_normal(m.nF)
+    phi[m.neighbor < 0] = 0.0
+    bcs = [(1, 7)] + [(z, 1) for z in range(2, 7)]
+    rm = R.cartesian_mesh(*dims, node_shift=shift)
+    rrp, rci, rv, rrhs = R.assemble_simplec(rm, bcs, 1.3, aP, mom, phi)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), seed=np.array(11), aP=aP, mom=mom, phi=phi,
+                        rho=np.array(1.3), rowPtr=rrp, colIdx=rci, values=rv, rhs=rrhs)
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -117,6 +137,7 @@ def main():
     cavity_case("cavity_simple_16.npz", 16, 6, 6)
     cavity_case_full_size("cavity_simple_128.npz", 128, 200)
     adjoint_case("adjoint_face_k_5x4x3.npz")
+    simplec_case("simplec_6x5x4_outlet.npz")
     print("fixtures written to", HERE)
 
 

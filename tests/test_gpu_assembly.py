@@ -40,6 +40,30 @@ def test_assembly_device_inputs_and_rho(sg, ctx, oracle):
     assert bits_equal(pv, ov) and bits_equal(prhs, orhs)
 
 
+@pytest.mark.parametrize("on_device", [False, True])
+def test_simplec_assembly_bit_exact(sg, ctx, oracle, on_device):
+    """SIMPLEC on the device against the reference fixture (SimpleAlgorithm
+    with PvCouplingVariant::SIMPLEC, tests/golden/make_golden.py)."""
+    import os
+
+    from simall_gb300 import workloads as W
+
+    g = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "simplec_6x5x4_outlet.npz"))
+    dims = tuple(int(v) for v in g["dims"])
+    m = sg.cartesian(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=int(g["seed"])))
+    bcs = [(1, int(sg.BCType.PressureOutlet))] + [(z, int(sg.BCType.NoSlipWall)) for z in range(2, 7)]
+    ps = sg.PressureSystem(m, bcs, ctx=ctx)
+    args = (g["aP"], g["mom"], g["phi"])
+    if on_device:
+        torch = pytest.importorskip("torch")
+        args = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in args)
+    ps.assemble_simplec(float(g["rho"]), *args)
+    ctx.synchronize()
+    v, rhs = ps.download()
+    assert bits_equal(v, g["values"]) and bits_equal(rhs, g["rhs"]) and ps.any_dirichlet
+    ps.close()
+
+
 def test_assembly_then_device_solve(sg, ctx, oracle):
     m = product_mesh(sg, 12, seed=5)
     om, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 12, seed=5)

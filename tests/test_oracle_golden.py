@@ -111,6 +111,21 @@ def test_cavity_128_full_size_systems(oracle):
         assert bits_equal(x, c["x"][k])
 
 
+def test_simplec_assembly_fixture(oracle):
+    """SIMPLEC denominators + assembly reproduce the reference's bytes."""
+    from simall_gb300 import workloads as W
+
+    g = load("simplec_6x5x4_outlet.npz")
+    dims = tuple(int(v) for v in g["dims"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=int(g["seed"])))
+    rp, ci = oracle.build_sparsity(m)
+    assert np.array_equal(rp, g["rowPtr"]) and np.array_equal(ci, g["colIdx"])
+    den = oracle.simplec_denominator(rp, ci, g["mom"], g["aP"])
+    v, rhs, anyD = oracle.assemble(m, rp, ci, [1], float(g["rho"]), den, g["phi"])
+    assert anyD and bits_equal(v, g["values"]) and bits_equal(rhs, g["rhs"])
+    assert np.count_nonzero(den <= 1e-30) > 0  # the clamp is exercised
+
+
 def test_face_conductance_adjoint_against_reference_gradient(oracle):
     """Face-conductance assembly reproduced bit for bit; the adjoint gradient
     (CG on A^T = A, then the scatter) matches solve_discrete_adjoint's."""

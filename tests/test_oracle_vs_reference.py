@@ -42,6 +42,28 @@ def test_mesh_rcm_assembly_cg(oracle, ref, dims, seed, amp, renumber):
     ref.free_mesh(r)
 
 
+@pytest.mark.parametrize("dims,renumber,bcs,pz", [((7, 7, 7), True, [], []),
+                                                  ((9, 6, 4), False, [(1, 7), (2, 5)], [1, 2])])
+def test_simplec_assembly(oracle, ref, dims, renumber, bcs, pz):
+    """PvCouplingVariant::SIMPLEC: denominators aP - sum|offdiag(A_mom)|."""
+    sh = _shift(dims, 5, 0.2)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    rng = np.random.default_rng(5)
+    rp, ci = oracle.build_sparsity(m)
+    aP = rng.uniform(1.0, 4.0, m.nC)
+    mom = rng.standard_normal(len(ci)) * 0.3
+    phi = rng.standard_normal(m.nF)
+    rrp, rci, rv, rrhs = ref.assemble_simplec(r, bcs, 1.1, aP, mom, phi)
+    den = oracle.simplec_denominator(rp, ci, mom, aP)
+    ov, orhs, _ = oracle.assemble(m, rp, ci, pz, 1.1, den, phi)
+    assert np.array_equal(rrp, rp) and np.array_equal(rci, ci)
+    assert bits_equal(rv, ov) and bits_equal(rrhs, orhs)
+    ref.free_mesh(r)
+
+
 def test_precond_none_maps_to_jacobi(oracle, ref):
     """make_preconditioner's default branch (LinearSolvers.cpp:240-254)."""
     r = ref.cartesian_mesh(4, 4, 4)
