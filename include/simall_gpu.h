@@ -231,6 +231,38 @@ int simall_solver_use_pressure_system(simall_solver *s, simall_pressure_system *
 int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, double *x, int mem,
                                  simall_solver_stats *stats);
 
+/* ------------------------------------------------------------------ the field loops around the solve */
+/* The face loops either side of the pressure solve of SimpleAlgorithm, on the
+ * device and bit-identical to the reference: compute_face_fluxes
+ * (SimpleAlgorithm.cpp:201-237, without periodic faces), the least-squares
+ * gradient (LeastSquaresGradient, Gradient.cpp:17-133) and correct_fields
+ * (SimpleAlgorithm.cpp:450-487).  A GpuSimpleAlgorithm::iterate() override that
+ * keeps U, p, aP, phi and p' in device memory runs the whole pressure step
+ * without a host round trip: fluxes -> assemble -> solve -> correct. */
+typedef struct simall_zone_velocity {
+    uint32_t zone;
+    double u[3]; /* BoundarySpec::vectorValue of a VelocityInlet / MovingWall zone */
+} simall_zone_velocity;
+/* Once per system: face areas, cell volumes (Mesh cells().volume) and the
+ * least-squares geometry (the inverse normal matrix of every cell, as the
+ * gradient's precompute) go to the device.  The boundary kinds of the flux
+ * loop come from the specs given to simall_pressure_system_create; zones of
+ * VelocityInlet / MovingWall specs take their vector from `velocities` (zero
+ * when absent). */
+int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const simall_mesh_view *m,
+                                             const double *cell_volume, const simall_zone_velocity *velocities,
+                                             int n_velocities);
+/* phi[n_faces] = rho (u_f . A_f) from the cell velocities. */
+int simall_compute_face_fluxes(simall_pressure_system *ps, double rho, const double *Ux, const double *Uy,
+                               const double *Uz, double *phi, int mem);
+/* (gx, gy, gz)[n_cells] = least-squares gradient of f[n_cells]. */
+int simall_lsq_gradient(simall_pressure_system *ps, const double *f, double *gx, double *gy, double *gz, int mem);
+/* p += urfP p'; U -= V / max(aP, 1e-30) grad p'; on interior faces
+ * phi += rho |A|^2 / max(0.5 (aP_o + aP_n) |d.A|, 1e-30) (p'_o - p'_n).
+ * p, U and phi are updated in place. */
+int simall_correct_fields(simall_pressure_system *ps, double rho, double urfP, const double *aP, const double *pPrime,
+                          double *p, double *Ux, double *Uy, double *Uz, double *phi, int mem);
+
 /* ------------------------------------------------------------------ differentiation */
 /* Face-conductance Poisson operator (an extension: the reference expresses
  * neither per-face conductances nor non-zero Dirichlet values).  With

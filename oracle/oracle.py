@@ -56,6 +56,14 @@ def lib():
         L.orc_rcm.argtypes = [_I64, _I64] + [_P] * 10
         L.orc_build_sparsity.restype = _I64
         L.orc_build_sparsity.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
+        L.orc_face_fluxes.restype = None
+        L.orc_face_fluxes.argtypes = [_I64] + [_P] * 6 + [_P, _P, C.c_int, _D] + [_P] * 4
+        L.orc_lsq_inverse.restype = None
+        L.orc_lsq_inverse.argtypes = [_I64, _I64] + [_P] * 9
+        L.orc_lsq_gradient.restype = None
+        L.orc_lsq_gradient.argtypes = [_I64, _I64] + [_P] * 13
+        L.orc_correct_fields.restype = None
+        L.orc_correct_fields.argtypes = [_I64, _I64] + [_P] * 12 + [_D, _D] + [_P] * 7
         L.orc_simplec_denominator.restype = None
         L.orc_simplec_denominator.argtypes = [_I64] + [_P] * 5
         L.orc_assemble.restype = C.c_int
@@ -181,6 +189,57 @@ def build_sparsity(m: Mesh):
     L.orc_build_sparsity(m.nC, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.cfOff), _ptr(m.cfIdx), _ptr(rowPtr),
                          _ptr(colIdx))
     return rowPtr, colIdx
+
+
+def _zone_tables(bcs):
+    """bcs: list of (zone, BCType ordinal[, (ux, uy, uz)]) -> per-zone type (first
+    spec wins, as find_bc) and vector tables."""
+    nZ = int(max([7] + [b[0] + 1 for b in bcs]))
+    zt = np.full(nZ, -1, np.int32)
+    zv = np.zeros(3 * nZ)
+    for b in bcs:
+        z = int(b[0])
+        if zt[z] == -1:
+            zt[z] = int(b[1])
+            if len(b) > 2:
+                zv[3 * z:3 * z + 3] = b[2]
+    return nZ, zt, zv
+
+
+def face_fluxes(m: Mesh, bcs, rho, U):
+    """compute_face_fluxes (SimpleAlgorithm.cpp:201-237); U = (Ux, Uy, Uz)."""
+    nZ, zt, zv = _zone_tables(bcs)
+    phi = np.empty(m.nF)
+    Ux, Uy, Uz = (np.ascontiguousarray(u, np.float64) for u in U)
+    lib().orc_face_fluxes(m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az), _ptr(m.zone),
+                          _ptr(zt), _ptr(zv), nZ, float(rho), _ptr(Ux), _ptr(Uy), _ptr(Uz), _ptr(phi))
+    return phi
+
+
+def lsq_gradient(m: Mesh, phi):
+    """LeastSquaresGradient precompute + evaluate (Gradient.cpp:17-133)."""
+    L = lib()
+    mInv = np.empty(6 * m.nC)
+    L.orc_lsq_inverse(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz),
+                      _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz), _ptr(mInv))
+    g = np.empty((3, m.nC))
+    L.orc_lsq_gradient(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz),
+                       _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz), _ptr(mInv),
+                       _ptr(np.ascontiguousarray(phi, np.float64)), _ptr(g[0]), _ptr(g[1]), _ptr(g[2]))
+    return g
+
+
+def correct_fields(m: Mesh, rho, urfP, aP, pPrime, p, U, phi):
+    """correct_fields (SimpleAlgorithm.cpp:450-487); returns (p, (Ux, Uy, Uz), phi), inputs untouched."""
+    p = np.array(p, np.float64)
+    Ux, Uy, Uz = (np.array(u, np.float64) for u in U)
+    phi = np.array(phi, np.float64)
+    lib().orc_correct_fields(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                             _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz),
+                             _ptr(m.vol), float(rho), float(urfP), _ptr(np.ascontiguousarray(aP, np.float64)),
+                             _ptr(np.ascontiguousarray(pPrime, np.float64)), _ptr(p), _ptr(Ux), _ptr(Uy), _ptr(Uz),
+                             _ptr(phi))
+    return p, (Ux, Uy, Uz), phi
 
 
 def simplec_denominator(rowPtr, colIdx, mom, aP):
@@ -316,6 +375,12 @@ class RefLib:
         L.ref_sparsity_nnz.argtypes = [_P]
         L.ref_assemble.restype = C.c_int
         L.ref_assemble.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 6
+        L.ref_face_fluxes.restype = C.c_int
+        L.ref_face_fluxes.argtypes = [_P, C.c_int, _P, _P, _P, _D] + [_P] * 4
+        L.ref_lsq_gradient.restype = C.c_int
+        L.ref_lsq_gradient.argtypes = [_P] * 5
+        L.ref_correct_fields.restype = C.c_int
+        L.ref_correct_fields.argtypes = [_P, _D, _D] + [_P] * 7
         L.ref_assemble_simplec.restype = C.c_int
         L.ref_assemble_simplec.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 7
         L.ref_cg.restype = C.c_int
@@ -414,6 +479,33 @@ class RefLib:
         L.ref_assemble(h, len(bcs), _ptr(zones), _ptr(types), rho, _ptr(aP), _ptr(phi), _ptr(rowPtr),
                        _ptr(colIdx), _ptr(values), _ptr(rhs))
         return rowPtr, colIdx, values, rhs
+
+    def face_fluxes(self, mesh_dict, bcs, rho, U):
+        """bcs: list of (zone, BCType ordinal, (ux, uy, uz))."""
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        vec = np.array([list(b[2]) if len(b) > 2 else [0, 0, 0] for b in bcs] or [[0, 0, 0]], np.float64).ravel()
+        Ux, Uy, Uz = (np.ascontiguousarray(u, np.float64) for u in U)
+        phi = np.empty(mesh_dict["nF"])
+        self.L.ref_face_fluxes(mesh_dict["handle"], len(bcs), _ptr(zones), _ptr(types), _ptr(vec), float(rho),
+                               _ptr(Ux), _ptr(Uy), _ptr(Uz), _ptr(phi))
+        return phi
+
+    def lsq_gradient(self, mesh_dict, phi):
+        g = np.empty((3, mesh_dict["nC"]))
+        self.L.ref_lsq_gradient(mesh_dict["handle"], _ptr(np.ascontiguousarray(phi, np.float64)), _ptr(g[0]),
+                                _ptr(g[1]), _ptr(g[2]))
+        return g
+
+    def correct_fields(self, mesh_dict, rho, urfP, aP, pPrime, p, U, phi):
+        p = np.array(p, np.float64)
+        Ux, Uy, Uz = (np.array(u, np.float64) for u in U)
+        phi = np.array(phi, np.float64)
+        self.L.ref_correct_fields(mesh_dict["handle"], float(rho), float(urfP),
+                                  _ptr(np.ascontiguousarray(aP, np.float64)),
+                                  _ptr(np.ascontiguousarray(pPrime, np.float64)), _ptr(p), _ptr(Ux), _ptr(Uy),
+                                  _ptr(Uz), _ptr(phi))
+        return p, (Ux, Uy, Uz), phi
 
     def assemble_simplec(self, mesh_dict, bcs, rho, aP, mom, phi):
         """assemble_pressure_correction with PvCouplingVariant::SIMPLEC, the

@@ -21,6 +21,7 @@
 #include "meshing/MeshOps.hpp"
 #include "meshing/MeshStorage.hpp"
 #include "solver/FieldRegistry.hpp"
+#include "solver/Gradient.hpp"
 #include "solver/LinearSolvers.hpp"
 #include "solver/SimpleAlgorithm.hpp"
 
@@ -69,6 +70,33 @@ public:
         A_mom_.values.assign(mom, mom + A_mom_.colIdx.size());
         assemble_pressure_correction();
     }
+    // compute_face_fluxes with the given cell velocities
+    void fluxes(const double* Ux, const double* Uy, const double* Uz)
+    {
+        const std::size_t nC = mesh_.cells().size();
+        auto& U = F_.vector("U", nC);
+        U.x.assign(Ux, Ux + nC);
+        U.y.assign(Uy, Uy + nC);
+        U.z.assign(Uz, Uz + nC);
+        compute_face_fluxes();
+    }
+    // correct_fields on the given state; the fields are read back by the caller
+    void correct(const double* aP, const double* pPrime, const double* p, const double* Ux, const double* Uy,
+                 const double* Uz, const double* phi)
+    {
+        const std::size_t nC = mesh_.cells().size(), nF = mesh_.faces().size();
+        auto& U = F_.vector("U", nC);
+        auto& pp = F_.scalar("p", nC);
+        U.x.assign(Ux, Ux + nC);
+        U.y.assign(Uy, Uy + nC);
+        U.z.assign(Uz, Uz + nC);
+        pp.assign(p, p + nC);
+        aP_.assign(aP, aP + nC);
+        pPrime_.assign(pPrime, pPrime + nC);
+        phiFlux_.assign(phi, phi + nF);
+        correct_fields();
+    }
+    S::FieldRegistry& fields() { return F_; }
     const S::CSRMatrix& Ap() const { return A_p_; }
     const Vec& rhs() const { return rhs_; }
     const Vec& aP() const { return aP_; }
@@ -261,6 +289,79 @@ int ref_assemble(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTy
     std::copy(A.colIdx.begin(), A.colIdx.end(), colIdx);
     std::copy(A.values.begin(), A.values.end(), values);
     std::copy(p.rhs().begin(), p.rhs().end(), rhs);
+    return 0;
+}
+
+std::vector<S::BoundarySpec> make_bcs_vec(int nbc, const std::uint32_t* zones, const int* types, const double* vec)
+{
+    std::vector<S::BoundarySpec> b;
+    for (int i = 0; i < nbc; ++i) {
+        S::BoundarySpec s{zones[i], static_cast<S::BCType>(types[i]), 0.0, {0, 0, 0}, ""};
+        if (vec) {
+            s.vectorValue[0] = vec[3 * i];
+            s.vectorValue[1] = vec[3 * i + 1];
+            s.vectorValue[2] = vec[3 * i + 2];
+        }
+        b.push_back(s);
+    }
+    return b;
+}
+
+// SimpleAlgorithm::compute_face_fluxes (SimpleAlgorithm.cpp:201-237).
+int ref_face_fluxes(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, const double* bcVec,
+                    double rho, const double* Ux, const double* Uy, const double* Uz, double* phi)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    auto bcs = make_bcs_vec(nbc, bcZones, bcTypes, bcVec);
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    S::SimpleOptions o;
+    o.rho = rho;
+    AssemblyProbe p(m, f, bcs, *s1, *s2, o);
+    p.fluxes(Ux, Uy, Uz);
+    std::copy(p.phi().begin(), p.phi().end(), phi);
+    return 0;
+}
+
+// LeastSquaresGradient::evaluate (Gradient.cpp:91-133).
+int ref_lsq_gradient(void* h, const double* phi, double* gx, double* gy, double* gz)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::LeastSquaresGradient G(m);
+    S::ScalarField f(phi, phi + nC);
+    S::VectorField g;
+    G.evaluate(f, g);
+    std::copy(g.x.begin(), g.x.end(), gx);
+    std::copy(g.y.begin(), g.y.end(), gy);
+    std::copy(g.z.begin(), g.z.end(), gz);
+    return 0;
+}
+
+// SimpleAlgorithm::correct_fields (SimpleAlgorithm.cpp:450-487); p, U and phi in/out.
+int ref_correct_fields(void* h, double rho, double urfP, const double* aP, const double* pPrime, double* p, double* Ux,
+                       double* Uy, double* Uz, double* phi)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::FieldRegistry f;
+    std::vector<S::BoundarySpec> bcs;
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    S::SimpleOptions o;
+    o.rho = rho;
+    o.urfP = urfP;
+    AssemblyProbe pr(m, f, bcs, *s1, *s2, o);
+    pr.correct(aP, pPrime, p, Ux, Uy, Uz, phi);
+    auto& U = *pr.fields().find_vector("U");
+    auto& pp = *pr.fields().find_scalar("p");
+    std::copy(pp.begin(), pp.end(), p);
+    std::copy(U.x.begin(), U.x.end(), Ux);
+    std::copy(U.y.begin(), U.y.end(), Uy);
+    std::copy(U.z.begin(), U.z.end(), Uz);
+    std::copy(pr.phi().begin(), pr.phi().end(), phi);
+    (void)nC;
     return 0;
 }
 

@@ -553,7 +553,6 @@ int orc_assemble(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *ne
 
 /* ------------------------------------------------------------------ BLAS-1 + SpMV */
 
-/* dot / norm2 / axpy (src/solver/LinearSolvers.cpp:25-43) */
 /* SIMPLEC denominator, SimpleAlgorithm.cpp:380-390 and 401-409: per cell
  * max(aP_c - sum_{k != c} |a_mom,ck|, 1e-30), the sum in column order from
  * 0.0.  Passing den as aP to orc_assemble gives the SIMPLEC system, because
@@ -570,6 +569,7 @@ void orc_simplec_denominator(int64_t nC, const int32_t *rowPtr, const int32_t *c
     }
 }
 
+/* dot / norm2 / axpy (src/solver/LinearSolvers.cpp:25-43) */
 double orc_dot(int64_t n, const double *a, const double *b)
 {
     double s = 0;
@@ -857,4 +857,187 @@ void orc_face_k_gradient(int64_t nF, const int64_t *owner, const int64_t *neighb
             dpb[f] = k[f] * g[f] * lambda[o];
         }
     }
+}
+
+/* ------------------------------------------------------------------ the face loops around the solve */
+
+/* BCType ordinals (src/solver/Solver.hpp:105-121) used by the face loops. */
+enum { ORC_BC_WALL = 0, ORC_BC_NOSLIP = 1, ORC_BC_MOVING = 2, ORC_BC_VELIN = 4, ORC_BC_SYMMETRY = 9 };
+
+/* compute_face_fluxes (src/solver/SimpleAlgorithm.cpp:201-237) without
+ * periodic faces.  zoneType[z] = the BCType ordinal of the first boundary spec
+ * with zone z (find_bc), -1 when there is none; zoneVec[3 z .. 3 z + 2] its
+ * vectorValue.  Face velocity: interior 0.5 (U_o + U_n); VelocityInlet and
+ * MovingWall the zone's vector; NoSlipWall, Wall and Symmetry zero; any other
+ * boundary (or none) the owner's velocity. */
+void orc_face_fluxes(int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax, const double *ay,
+                     const double *az, const uint32_t *zone, const int *zoneType, const double *zoneVec, int nZones,
+                     double rho, const double *Ux, const double *Uy, const double *Uz, double *phi)
+{
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        double ux, uy, uz;
+        if (n != ORC_BOUNDARY) {
+            ux = 0.5 * (Ux[o] + Ux[n]);
+            uy = 0.5 * (Uy[o] + Uy[n]);
+            uz = 0.5 * (Uz[o] + Uz[n]);
+        } else {
+            const uint32_t z = zone[f];
+            const int t = (int)z < nZones ? zoneType[z] : -1;
+            if (t == ORC_BC_VELIN || t == ORC_BC_MOVING) {
+                ux = zoneVec[3 * z];
+                uy = zoneVec[3 * z + 1];
+                uz = zoneVec[3 * z + 2];
+            } else if (t == ORC_BC_NOSLIP || t == ORC_BC_WALL || t == ORC_BC_SYMMETRY) {
+                ux = uy = uz = 0.0;
+            } else {
+                ux = Ux[o];
+                uy = Uy[o];
+                uz = Uz[o];
+            }
+        }
+        phi[f] = rho * (ux * ax[f] + uy * ay[f] + uz * az[f]);
+    }
+}
+
+/* LeastSquaresGradient (src/solver/Gradient.cpp:17-133): the inverse of the
+ * weighted normal matrix per cell (precompute, invert3x3_sym), then the
+ * gradient of phi with the boundary faces' difference taken as zero. */
+static void orc_inv3_sym(double xx, double xy, double xz, double yy, double yz, double zz, double out[6])
+{
+    const double det = xx * (yy * zz - yz * yz) - xy * (xy * zz - yz * xz) + xz * (xy * yz - yy * xz);
+    if (fabs(det) < 1e-30) {
+        out[0] = out[1] = out[2] = out[3] = out[4] = out[5] = 0.0;
+        return;
+    }
+    const double inv = 1.0 / det;
+    out[0] = (yy * zz - yz * yz) * inv;
+    out[1] = -(xy * zz - yz * xz) * inv;
+    out[2] = (xy * yz - yy * xz) * inv;
+    out[3] = (xx * zz - xz * xz) * inv;
+    out[4] = -(xx * yz - xy * xz) * inv;
+    out[5] = (xx * yy - xy * xy) * inv;
+}
+
+void orc_lsq_inverse(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *fcx,
+                     const double *fcy, const double *fcz, const double *ccx, const double *ccy, const double *ccz,
+                     double *mInv /* [6 nC] */)
+{
+    double *A = (double *)calloc((size_t)(6 * nC), sizeof(double));
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        if (o == ORC_BOUNDARY)
+            continue;
+        double d[2][3];
+        int64_t cells[2];
+        int cnt;
+        if (n == ORC_BOUNDARY) {
+            d[0][0] = fcx[f] - ccx[o];
+            d[0][1] = fcy[f] - ccy[o];
+            d[0][2] = fcz[f] - ccz[o];
+            cells[0] = o;
+            cnt = 1;
+        } else {
+            const double dx = ccx[n] - ccx[o], dy = ccy[n] - ccy[o], dz = ccz[n] - ccz[o];
+            d[0][0] = dx;
+            d[0][1] = dy;
+            d[0][2] = dz;
+            d[1][0] = -dx;
+            d[1][1] = -dy;
+            d[1][2] = -dz;
+            cells[0] = o;
+            cells[1] = n;
+            cnt = 2;
+        }
+        for (int k = 0; k < cnt; ++k) {
+            const double dx = d[k][0], dy = d[k][1], dz = d[k][2];
+            const double w2 = 1.0 / (dx * dx + dy * dy + dz * dz + 1e-30);
+            double *a = A + 6 * cells[k];
+            a[0] += w2 * dx * dx;
+            a[1] += w2 * dx * dy;
+            a[2] += w2 * dx * dz;
+            a[3] += w2 * dy * dy;
+            a[4] += w2 * dy * dz;
+            a[5] += w2 * dz * dz;
+        }
+    }
+    for (int64_t c = 0; c < nC; ++c) {
+        const double *a = A + 6 * c;
+        orc_inv3_sym(a[0], a[1], a[2], a[3], a[4], a[5], mInv + 6 * c);
+    }
+    free(A);
+}
+
+void orc_lsq_gradient(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *fcx,
+                      const double *fcy, const double *fcz, const double *ccx, const double *ccy, const double *ccz,
+                      const double *mInv, const double *phi, double *gx, double *gy, double *gz)
+{
+    double *b = (double *)calloc((size_t)(3 * nC), sizeof(double));
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        if (o == ORC_BOUNDARY)
+            continue;
+        if (n == ORC_BOUNDARY) {
+            const double dx = fcx[f] - ccx[o], dy = fcy[f] - ccy[o], dz = fcz[f] - ccz[o];
+            const double w2 = 1.0 / (dx * dx + dy * dy + dz * dz + 1e-30);
+            const double dphi = 0.0;
+            b[3 * o] += w2 * dx * dphi;
+            b[3 * o + 1] += w2 * dy * dphi;
+            b[3 * o + 2] += w2 * dz * dphi;
+        } else {
+            const double dx = ccx[n] - ccx[o], dy = ccy[n] - ccy[o], dz = ccz[n] - ccz[o];
+            const double w2 = 1.0 / (dx * dx + dy * dy + dz * dz + 1e-30);
+            const double dphi = phi[n] - phi[o];
+            b[3 * o] += w2 * dx * dphi;
+            b[3 * o + 1] += w2 * dy * dphi;
+            b[3 * o + 2] += w2 * dz * dphi;
+            b[3 * n] += w2 * dx * -dphi;
+            b[3 * n + 1] += w2 * dy * -dphi;
+            b[3 * n + 2] += w2 * dz * -dphi;
+        }
+    }
+    for (int64_t c = 0; c < nC; ++c) {
+        const double *m = mInv + 6 * c, bx = b[3 * c], by = b[3 * c + 1], bz = b[3 * c + 2];
+        gx[c] = m[0] * bx + m[1] * by + m[2] * bz;
+        gy[c] = m[1] * bx + m[3] * by + m[4] * bz;
+        gz[c] = m[2] * bx + m[4] * by + m[5] * bz;
+    }
+    free(b);
+}
+
+/* correct_fields (src/solver/SimpleAlgorithm.cpp:450-487): p += urfP p';
+ * U -= V / max(aP, 1e-30) grad p' (least-squares gradient); interior faces
+ * phi += rho |A|^2 / max(0.5 (aP_o + aP_n) |d.A|, 1e-30) (p'_o - p'_n). */
+void orc_correct_fields(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                        const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
+                        const double *ccx, const double *ccy, const double *ccz, const double *vol, double rho,
+                        double urfP, const double *aP, const double *pPrime, double *p, double *Ux, double *Uy,
+                        double *Uz, double *phi)
+{
+    for (int64_t c = 0; c < nC; ++c)
+        p[c] += urfP * pPrime[c];
+    double *mInv = (double *)malloc((size_t)(6 * nC) * sizeof(double));
+    double *g = (double *)malloc((size_t)(3 * nC) * sizeof(double));
+    orc_lsq_inverse(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv);
+    orc_lsq_gradient(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv, pPrime, g, g + nC, g + 2 * nC);
+    for (int64_t c = 0; c < nC; ++c) {
+        const double w = vol[c] / STD_MAX(aP[c], 1e-30);
+        Ux[c] -= w * g[c];
+        Uy[c] -= w * g[nC + c];
+        Uz[c] -= w * g[2 * nC + c];
+    }
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        const double Ax = ax[f], Ay = ay[f], Az = az[f];
+        const double Amag2 = Ax * Ax + Ay * Ay + Az * Az;
+        if (n != ORC_BOUNDARY) {
+            const double dx = ccx[n] - ccx[o], dy = ccy[n] - ccy[o], dz = ccz[n] - ccz[o];
+            const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+            const double aPf = 0.5 * (aP[o] + aP[n]);
+            const double coef = rho * Amag2 / STD_MAX(aPf * ddotA, 1e-30);
+            phi[f] += coef * (pPrime[o] - pPrime[n]);
+        }
+    }
+    free(mInv);
+    free(g);
 }

@@ -40,6 +40,10 @@ class SolverStats(C.Structure):
                 ("engine", _I), ("reserved", _I)]
 
 
+class ZoneVelocity(C.Structure):
+    _fields_ = [("zone", C.c_uint32), ("u", _D * 3)]
+
+
 class MeshView(C.Structure):
     _fields_ = [("n_cells", _I64), ("n_faces", _I64), ("owner", _P), ("neighbor", _P), ("area_x", _P),
                 ("area_y", _P), ("area_z", _P), ("centroid_x", _P), ("centroid_y", _P), ("centroid_z", _P),
@@ -89,6 +93,10 @@ SIGNATURES = {
     "simall_pressure_system_device_arrays": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "simall_assemble_pressure_correction": (_I, [_P, _D, _P, _P, _I, C.POINTER(_I)]),
     "simall_assemble_pressure_correction_simplec": (_I, [_P, _D, _P, _P, _P, _I, C.POINTER(_I)]),
+    "simall_pressure_system_setup_field_loops": (_I, [_P, C.POINTER(MeshView), _P, _P, _I]),
+    "simall_compute_face_fluxes": (_I, [_P, _D, _P, _P, _P, _P, _I]),
+    "simall_lsq_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
+    "simall_correct_fields": (_I, [_P, _D, _D, _P, _P, _P, _P, _P, _P, _P, _I]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),

@@ -25,25 +25,7 @@
 #include <cstring>
 #include <new>
 
-struct simall_pressure_system {
-    simall_context *ctx = nullptr;
-    int64_t nC = 0, nF = 0, nnz = 0;
-    std::vector<int32_t> h_rowPtr, h_colIdx;
-    simall::DevBuf<int32_t> rowPtr, colIdx;
-    simall::DevBuf<double> values, rhs;
-    // faces
-    simall::DevBuf<int32_t> owner, neighbor;  // neighbor -1 on boundary faces
-    simall::DevBuf<double> amag2, ddotA;
-    simall::DevBuf<uint8_t> kind;  // 0 interior, 1 pressure boundary, 2 other boundary
-    simall::DevBuf<double> coef;
-    // cells: faces in ascending id; entry = face id | (cell is the neighbour) << 31;
-    // slot = CSR position of the other cell in the row (-1: none)
-    simall::DevBuf<int32_t> cfOff, cfEnt, cfSlot, diagSlot;
-    int anyDirichlet = 0;
-    simall::DevBuf<double> aP, phi;  // staging for host inputs
-    simall::DevBuf<double> den;      // SIMPLEC denominators
-    simall::DevBuf<double> kf, pbf;  // staging for face-conductance inputs
-};
+#include "pressure_system.hpp"
 
 namespace simall {
 
@@ -333,6 +315,7 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
     ps->nC = nC;
     ps->nF = nF;
     ps->anyDirichlet = anyD;
+    ps->h_bcs.assign(bcs, bcs + n_bcs);
     // ---- sparsity (build_sparsity :62-82): {c} U other cells of c's faces, sorted, unique
     ps->h_rowPtr.assign(static_cast<size_t>(nC) + 1, 0);
     ps->h_colIdx.reserve(static_cast<size_t>(ncf) + static_cast<size_t>(nC));

@@ -174,6 +174,48 @@ class PressureSystem:
                                                                  C.byref(anyD)), self.ctx.handle)
         self.any_dirichlet = bool(anyD.value)
 
+    # -- the field loops around the solve ------------------------------------------
+    def setup_field_loops(self, velocities=()):
+        """velocities: (zone, (ux, uy, uz)) of VelocityInlet / MovingWall zones."""
+        arr = (_lib.ZoneVelocity * max(1, len(velocities)))()
+        for i, (z, u) in enumerate(velocities):
+            arr[i].zone = int(z)
+            for k in range(3):
+                arr[i].u[k] = float(u[k])
+        view = self.mesh.view()
+        check(self.L.simall_pressure_system_setup_field_loops(self.handle, C.byref(view), self.mesh.volume.ctypes.data,
+                                                              arr, len(velocities)), self.ctx.handle)
+
+    def face_fluxes(self, rho: float, U, phi=None):
+        """compute_face_fluxes; U = (Ux, Uy, Uz) numpy or CUDA tensors."""
+        ptrs = [ptr_and_mem(u) for u in U]
+        if phi is None:
+            phi = np.empty(self.mesh.n_faces)
+        pp, mp = ptr_and_mem(phi)
+        if any(m != mp for _, m in ptrs):
+            raise ValueError("U and phi must live in the same memory")
+        check(self.L.simall_compute_face_fluxes(self.handle, float(rho), ptrs[0][0], ptrs[1][0], ptrs[2][0], pp, mp),
+              self.ctx.handle)
+        return phi
+
+    def lsq_gradient(self, f):
+        pf, mf = ptr_and_mem(f)
+        if mf != _lib.MEM_HOST:
+            raise ValueError("lsq_gradient: host arrays only from Python")
+        g = np.empty((3, self.mesh.n_cells))
+        check(self.L.simall_lsq_gradient(self.handle, pf, g[0].ctypes.data, g[1].ctypes.data, g[2].ctypes.data, mf),
+              self.ctx.handle)
+        return g
+
+    def correct_fields(self, rho: float, urfP: float, aP, pPrime, p, U, phi):
+        """In place on p, U = (Ux, Uy, Uz) and phi (all numpy, or all CUDA tensors)."""
+        arrs = [aP, pPrime, p, U[0], U[1], U[2], phi]
+        pm = [ptr_and_mem(a) for a in arrs]
+        if len({m for _, m in pm}) != 1:
+            raise ValueError("all arrays must live in the same memory")
+        check(self.L.simall_correct_fields(self.handle, float(rho), float(urfP), *[x for x, _ in pm], pm[0][1]),
+              self.ctx.handle)
+
     def assemble_face_conductance(self, rho: float, k, pb, src):
         """Face-conductance operator: coef_f = k_f g_f, Dirichlet values pb on
         pressure-boundary faces, rhs from the cell source src."""

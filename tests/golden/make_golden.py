@@ -106,6 +106,31 @@ def simplec_case(name):
                         rho=np.array(1.3), rowPtr=rrp, colIdx=rci, values=rv, rhs=rrhs)
 
 
+def field_loops_case(name):
+    """compute_face_fluxes, LeastSquaresGradient::evaluate and correct_fields
+    of the reference on a distorted, RCM-renumbered 7x6x5 box with every
+    boundary treatment of the flux loop."""
+    dims = (7, 6, 5)
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=13)
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=True)
+    rng = np.random.default_rng(13)
+    nC, nF = rm["nC"], rm["nF"]
+    U = [rng.standard_normal(nC) for _ in range(3)]
+    bcs = [(1, 4, (0.7, -0.2, 0.1)), (2, 7), (3, 1), (4, 2, (1.0, 0.0, 0.0)), (5, 9), (6, 3)]
+    phi = R.face_fluxes(rm, bcs, 1.2, U)
+    f = rng.standard_normal(nC)
+    g = R.lsq_gradient(rm, f)
+    aP = rng.uniform(0.5, 2.0, nC)
+    pp = rng.standard_normal(nC) * 1e-2
+    p0 = rng.standard_normal(nC)
+    p1, U1, phi1 = R.correct_fields(rm, 1.2, 0.3, aP, pp, p0, U, phi)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), seed=np.array(13),
+                        bc_zone=np.array([b[0] for b in bcs]), bc_type=np.array([b[1] for b in bcs]),
+                        bc_vec=np.array([list(b[2]) if len(b) > 2 else [0.0, 0.0, 0.0] for b in bcs]),
+                        rho=np.array(1.2), urfP=np.array(0.3), U=np.array(U), phi=phi, f=f, grad=g, aP=aP,
+                        pPrime=pp, p0=p0, p1=p1, U1=np.array(U1), phi1=phi1)
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -138,6 +163,7 @@ def main():
     cavity_case_full_size("cavity_simple_128.npz", 128, 200)
     adjoint_case("adjoint_face_k_5x4x3.npz")
     simplec_case("simplec_6x5x4_outlet.npz")
+    field_loops_case("field_loops_7x6x5_rcm.npz")
     print("fixtures written to", HERE)
 
 

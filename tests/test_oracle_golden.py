@@ -126,6 +126,28 @@ def test_simplec_assembly_fixture(oracle):
     assert np.count_nonzero(den <= 1e-30) > 0  # the clamp is exercised
 
 
+def _field_fixture(oracle):
+    from simall_gb300 import workloads as W
+
+    g = load("field_loops_7x6x5_rcm.npz")
+    dims = tuple(int(v) for v in g["dims"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=int(g["seed"])))
+    oracle.rcm(m)
+    bcs = [(int(z), int(t), tuple(v)) for z, t, v in zip(g["bc_zone"], g["bc_type"], g["bc_vec"])]
+    return g, m, bcs
+
+
+def test_field_loops_fixture(oracle):
+    """compute_face_fluxes, the least-squares gradient and correct_fields
+    reproduce the reference's bytes."""
+    g, m, bcs = _field_fixture(oracle)
+    assert bits_equal(oracle.face_fluxes(m, bcs, float(g["rho"]), g["U"]), g["phi"])
+    assert bits_equal(oracle.lsq_gradient(m, g["f"]), g["grad"])
+    p1, U1, phi1 = oracle.correct_fields(m, float(g["rho"]), float(g["urfP"]), g["aP"], g["pPrime"], g["p0"],
+                                         g["U"], g["phi"])
+    assert bits_equal(p1, g["p1"]) and bits_equal(np.array(U1), g["U1"]) and bits_equal(phi1, g["phi1"])
+
+
 def test_face_conductance_adjoint_against_reference_gradient(oracle):
     """Face-conductance assembly reproduced bit for bit; the adjoint gradient
     (CG on A^T = A, then the scatter) matches solve_discrete_adjoint's."""

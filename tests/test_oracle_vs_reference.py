@@ -64,6 +64,35 @@ def test_simplec_assembly(oracle, ref, dims, renumber, bcs, pz):
     ref.free_mesh(r)
 
 
+@pytest.mark.parametrize("dims,renumber", [((6, 5, 4), False), ((7, 6, 5), True), ((10, 9, 1), False)])
+def test_face_loops_around_the_solve(oracle, ref, dims, renumber):
+    """compute_face_fluxes, LeastSquaresGradient and correct_fields: the
+    oracle reproduces the reference's bytes (distorted mesh, every boundary
+    treatment of the flux loop)."""
+    sh = _shift(dims, 8, 0.2 if dims[2] > 1 else 0.0)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    rng = np.random.default_rng(8)
+    U = [rng.standard_normal(m.nC) for _ in range(3)]
+    bcs = [(1, 4, (0.7, -0.2, 0.1)), (2, 7), (3, 1), (4, 2, (1.0, 0.0, 0.0)), (5, 9), (6, 3)]
+    phi = oracle.face_fluxes(m, bcs, 1.2, U)
+    assert bits_equal(phi, ref.face_fluxes(r, bcs, 1.2, U))
+    f = rng.standard_normal(m.nC)
+    g = oracle.lsq_gradient(m, f)
+    assert bits_equal(g, ref.lsq_gradient(r, f))
+    aP = rng.uniform(0.5, 2.0, m.nC)
+    pp = rng.standard_normal(m.nC) * 1e-2
+    p0 = rng.standard_normal(m.nC)
+    got = oracle.correct_fields(m, 1.2, 0.3, aP, pp, p0, U, phi)
+    want = ref.correct_fields(r, 1.2, 0.3, aP, pp, p0, U, phi)
+    assert bits_equal(got[0], want[0]) and bits_equal(got[2], want[2])
+    for a, b in zip(got[1], want[1]):
+        assert bits_equal(a, b)
+    ref.free_mesh(r)
+
+
 def test_precond_none_maps_to_jacobi(oracle, ref):
     """make_preconditioner's default branch (LinearSolvers.cpp:240-254)."""
     r = ref.cartesian_mesh(4, 4, 4)
