@@ -451,6 +451,66 @@ def run_cavity(a, ctx, sg, with_cpu):
     return res
 
 
+def run_pressure_step(a, ctx, sg, with_cpu):
+    """The device-resident pressure step on the distorted 128^3 box (RCM):
+    compute_face_fluxes -> assembly -> FP64 Jacobi-PCG to 1e-8 ->
+    correct_fields, every field in device memory, each stage timed with CUDA
+    events; the face loops' algorithmic bytes give their GB/s."""
+    import torch
+    from simall_gb300 import workloads as W
+
+    n = a.poisson_n
+    m, _ = W.poisson3d_mesh(n, seed=SEED)
+    ps = sg.PressureSystem(m, W.ALL_WALLS, ctx=ctx)
+    ps.setup_field_loops()
+    rng = np.random.default_rng(SEED + 9)
+    dev = torch.device("cuda")
+    U = [torch.from_numpy(rng.standard_normal(m.n_cells)).to(dev) for _ in range(3)]
+    aP = torch.from_numpy(rng.uniform(0.5, 2.0, m.n_cells)).to(dev)
+    p = torch.zeros(m.n_cells, dtype=torch.float64, device=dev)
+    phi = torch.empty(m.n_faces, dtype=torch.float64, device=dev)
+    pp = torch.empty_like(p)
+    s = sg.GpuCGSolver(sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                             tolerance=a.tol, maxIterations=a.max_iterations), ctx=ctx)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    stages = {"fluxes": lambda: ps.face_fluxes(1.0, U, phi), "assemble": lambda: ps.assemble(1.0, aP, phi),
+              "solve": lambda: ps.solve(s, pp), "correct": lambda: ps.correct_fields(1.0, 0.3, aP, pp, p, U, phi)}
+    for f in stages.values():  # warm
+        f()
+    ms = {}
+    for name, f in stages.items():
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        f()
+        e1.record(stream)
+        e1.synchronize()
+        ms[name] = e0.elapsed_time(e1)
+    nC, nF = m.n_cells, m.n_faces
+    nEnt = int(2 * np.count_nonzero(m.neighbor != sg.mesh.BOUNDARY) + np.count_nonzero(m.neighbor == sg.mesh.BOUNDARY))
+    by = {"fluxes": 41 * nF + 24 * nC,
+          "correct": 4 * nC + 4 * nEnt + 48 * nF + 8 * nC + 48 * nC + 24 * nC + 112 * nC + 40 * nF}
+    res = {"workload": f"poisson3d {n}^3 distorted, RCM: fluxes -> assembly -> Jacobi-PCG to {a.tol:g} -> correction, "
+                       f"fields in device memory", "cells": nC, "faces": nF,
+           "ms": {k: round(v, 3) for k, v in ms.items()}, "iterations": int(s.stats.iterations),
+           "gbs": {k: round(by[k] / (ms[k] * 1e6), 1) for k in by}}
+    if with_cpu:
+        from oracle import oracle as O
+        om = O.cartesian_mesh(n, n, n, node_shift=W.interior_node_shift(n, n, n, amp=0.2, seed=SEED))
+        O.rcm(om)
+        Uh = [u.cpu().numpy() for u in U]
+        t = time.perf_counter()
+        ph = O.face_fluxes(om, [(z, 1) for z in range(1, 7)], 1.0, Uh)
+        t1 = time.perf_counter()
+        O.correct_fields(om, 1.0, 0.3, aP.cpu().numpy(), pp.cpu().numpy(), np.zeros(nC), Uh, ph)
+        t2 = time.perf_counter()
+        res["cpu_baseline"] = {"fluxes_ms": round((t1 - t) * 1e3, 1), "correct_ms": round((t2 - t1) * 1e3, 1),
+                               "cores": 1, "kind": "port"}
+    s.close()
+    ps.close()
+    return res
+
+
 def run_ours(a, rank, world, local):
     import torch
 
@@ -597,6 +657,8 @@ def run_ours(a, rank, world, local):
         out["adjoint"] = run_adjoint(a, ctx, sg)
     if a.poisson_n > 0:
         out["poisson3d"] = run_poisson3d(a, ctx, sg)
+    if a.poisson_n > 0:
+        out["pressure_step"] = run_pressure_step(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if not a.no_cavity:
         out["cavity"] = run_cavity(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
