@@ -84,6 +84,13 @@ def lib():
         L.orc_assemble_face_k.argtypes = [_I64, _I64] + [_P] * 12 + [_D] + [_P] * 8
         L.orc_face_k_gradient.restype = None
         L.orc_face_k_gradient.argtypes = [_I64] + [_P] * 10
+        L.orc_assemble_momentum.restype = None
+        L.orc_assemble_momentum.argtypes = [_I64, _I64] + [_P] * 15 + [C.c_int] + [_P] * 3 + [C.c_int, C.c_int] + \
+            [_P] * 8
+        L.orc_bicgstab.restype = C.c_int
+        L.orc_bicgstab.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
+        L.orc_gmres.restype = C.c_int
+        L.orc_gmres.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, C.c_int, _P, _P]
         _lib = L
     return _lib
 
@@ -301,6 +308,50 @@ def face_k_gradient(m: Mesh, is_dirichlet_face, g, k, pb, x, lam):
 # ---------------------------------------------------------------- linear algebra
 
 
+def assemble_momentum(m: Mesh, rowPtr, colIdx, bcs, opt, comp, phi, gp, Ucomp, Un=None, Unm1=None, bdf2=False):
+    """assemble_momentum (SimpleAlgorithm.cpp:240-355) for component comp;
+    bcs as face_fluxes, opt = (rho, mu, urfU, dt), gp = that component of the
+    pressure gradient.  Returns (values, rhs, relaxed diagonal)."""
+    nZ, zt, zv = _zone_tables(bcs)
+    nnz = int(rowPtr[-1])
+    values = np.empty(nnz)
+    rhs = np.empty(m.nC)
+    aP = np.empty(m.nC)
+    z = np.zeros(m.nC)
+    a = [np.ascontiguousarray(v if v is not None else z, np.float64) for v in (phi, gp, Ucomp, Un, Unm1)]
+    lib().orc_assemble_momentum(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                                _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz),
+                                _ptr(m.vol), _ptr(m.zone), _ptr(zt), _ptr(zv), nZ,
+                                _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+                                _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                                _ptr(np.ascontiguousarray(opt, np.float64)), int(bool(bdf2)), int(comp),
+                                *(_ptr(v) for v in a), _ptr(values), _ptr(rhs), _ptr(aP))
+    return values, rhs, aP
+
+
+def bicgstab(rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):
+    """BiCGSTABSolver::solve (LinearSolvers.cpp:363-405); returns (x, iterations, last)."""
+    n = len(rowPtr) - 1
+    x = np.empty(n)
+    last = C.c_double(0)
+    it = lib().orc_bicgstab(n, _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+                            _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                            _ptr(np.ascontiguousarray(values, np.float64)), _ptr(np.ascontiguousarray(b, np.float64)),
+                            int(precond), float(tol), int(max_it), _ptr(x), C.byref(last))
+    return x, it, last.value
+
+
+def gmres(rowPtr, colIdx, values, b, precond=1, tol=1e-8, max_it=1000, restart=30):
+    """GMRESmSolver::solve (LinearSolvers.cpp:268-343); returns (x, iterations, last)."""
+    n = len(rowPtr) - 1
+    x = np.empty(n)
+    last = C.c_double(0)
+    it = lib().orc_gmres(n, _ptr(np.ascontiguousarray(rowPtr, np.int32)), _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                         _ptr(np.ascontiguousarray(values, np.float64)), _ptr(np.ascontiguousarray(b, np.float64)),
+                         int(precond), float(tol), int(max_it), int(restart), _ptr(x), C.byref(last))
+    return x, it, last.value
+
+
 def spmv(rowPtr, colIdx, values, x):
     n = len(rowPtr) - 1
     y = np.empty(n)
@@ -392,6 +443,10 @@ class RefLib:
         L.ref_cavity_fetch.argtypes = [_P] * 9
         L.ref_plugin_load.restype = _I64
         L.ref_plugin_load.argtypes = [C.c_char_p, C.c_char_p, C.c_int, C.c_char_p, C.c_int, C.POINTER(C.c_int)]
+        L.ref_assemble_momentum.restype = C.c_int
+        L.ref_assemble_momentum.argtypes = [_P, C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int] + [_P] * 8
+        L.ref_krylov.restype = C.c_int
+        L.ref_krylov.argtypes = [C.c_int, C.c_int, _D, C.c_int, C.c_int, C.c_int] + [_P] * 7
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -524,6 +579,42 @@ class RefLib:
                                _ptr(np.ascontiguousarray(mom, np.float64)), _ptr(np.ascontiguousarray(phi, np.float64)),
                                _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(rhs))
         return rowPtr, colIdx, values, rhs
+
+    def assemble_momentum(self, mesh_dict, bcs, opt, comp, U, p, phi, Un=None, Unm1=None, bdf2=False, time_step=0):
+        """SimpleAlgorithm::assemble_momentum(comp); returns (values, rhs, aP_)."""
+        L = self.L
+        h = mesh_dict["handle"]
+        nnz = L.ref_sparsity_nnz(h)
+        nC = mesh_dict["nC"]
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        vec = np.array([list(b[2]) if len(b) > 2 else [0, 0, 0] for b in bcs] or [[0, 0, 0]], np.float64).ravel()
+        U3 = np.ascontiguousarray(np.asarray(U, np.float64).reshape(3, nC))
+        z3 = np.zeros((3, nC))
+        Un3 = np.ascontiguousarray(np.asarray(Un, np.float64).reshape(3, nC)) if Un is not None else z3
+        Unm13 = np.ascontiguousarray(np.asarray(Unm1, np.float64).reshape(3, nC)) if Unm1 is not None else z3
+        values = np.empty(nnz)
+        rhs = np.empty(nC)
+        aP = np.empty(nC)
+        L.ref_assemble_momentum(h, len(bcs), _ptr(zones), _ptr(types), _ptr(vec),
+                                _ptr(np.ascontiguousarray(opt, np.float64)), int(bool(bdf2)), int(time_step),
+                                int(comp), _ptr(U3), _ptr(np.ascontiguousarray(p, np.float64)),
+                                _ptr(np.ascontiguousarray(phi, np.float64)), _ptr(Un3), _ptr(Unm13), _ptr(values),
+                                _ptr(rhs), _ptr(aP))
+        return values, rhs, aP
+
+    def krylov(self, kind, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000, restart=30):
+        """make_gmres / make_bicgstab / make_cg by LinearSolverKind ordinal; (x, it, last, seconds)."""
+        n = len(rowPtr) - 1
+        x = np.empty(n)
+        last = C.c_double(0)
+        secs = C.c_double(0)
+        it = self.L.ref_krylov(int(kind), int(precond), float(tol), int(max_it), int(restart), n,
+                               _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+                               _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                               _ptr(np.ascontiguousarray(values, np.float64)),
+                               _ptr(np.ascontiguousarray(b, np.float64)), _ptr(x), C.byref(last), C.byref(secs))
+        return x, it, last.value, secs.value
 
     # -- solvers
     def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):

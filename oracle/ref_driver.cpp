@@ -96,6 +96,34 @@ public:
         phiFlux_.assign(phi, phi + nF);
         correct_fields();
     }
+    // assemble_momentum(comp) on the given state; opt = {rho, mu, urfU, dt}
+    void momentum(const double* opt, int bdf2, int timeStep, int comp, const double* Ux, const double* Uy,
+                  const double* Uz, const double* p, const double* phi, const double* Un, const double* Unm1)
+    {
+        build_sparsity();
+        const std::size_t nC = mesh_.cells().size(), nF = mesh_.faces().size();
+        auto& U = F_.vector("U", nC);
+        U.x.assign(Ux, Ux + nC);
+        U.y.assign(Uy, Uy + nC);
+        U.z.assign(Uz, Uz + nC);
+        F_.scalar("p", nC).assign(p, p + nC);
+        phiFlux_.assign(phi, phi + nF);
+        aP_.assign(nC, 0.0);
+        opt_.rho = opt[0];
+        opt_.mu = opt[1];
+        opt_.urfU = opt[2];
+        opt_.dt = opt[3];
+        opt_.timeScheme = bdf2 ? S::TemporalScheme::BDF2 : S::TemporalScheme::ImplicitEuler;
+        timeStep_ = timeStep;
+        Ux_n_.assign(Un, Un + nC);
+        Uy_n_.assign(Un + nC, Un + 2 * nC);
+        Uz_n_.assign(Un + 2 * nC, Un + 3 * nC);
+        Ux_nm1_.assign(Unm1, Unm1 + nC);
+        Uy_nm1_.assign(Unm1 + nC, Unm1 + 2 * nC);
+        Uz_nm1_.assign(Unm1 + 2 * nC, Unm1 + 3 * nC);
+        assemble_momentum(comp);
+    }
+    const S::CSRMatrix& Amom() const { return A_mom_; }
     S::FieldRegistry& fields() { return F_; }
     const S::CSRMatrix& Ap() const { return A_p_; }
     const Vec& rhs() const { return rhs_; }
@@ -387,7 +415,57 @@ int ref_assemble_simplec(void* h, int nbc, const std::uint32_t* bcZones, const i
     return 0;
 }
 
+// SimpleAlgorithm::assemble_momentum (SimpleAlgorithm.cpp:240-355), one
+// component.  U, Un, Unm1 are [3][nC]; opt = {rho, mu, urfU, dt}; bdf2 selects
+// TemporalScheme::BDF2 (else ImplicitEuler); aP receives aP_ (written by the
+// reference for component 0 only, zeros otherwise).
+int ref_assemble_momentum(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, const double* bcVec,
+                          const double* opt, int bdf2, int timeStep, int comp, const double* U, const double* p,
+                          const double* phi, const double* Un, const double* Unm1, double* values, double* rhs,
+                          double* aP)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::FieldRegistry f;
+    auto bcs = make_bcs_vec(nbc, bcZones, bcTypes, bcVec);
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    AssemblyProbe pr(m, f, bcs, *s1, *s2, S::SimpleOptions{});
+    pr.momentum(opt, bdf2, timeStep, comp, U, U + nC, U + 2 * nC, p, phi, Un, Unm1);
+    const auto& A = pr.Amom();
+    std::copy(A.values.begin(), A.values.end(), values);
+    std::copy(pr.rhs().begin(), pr.rhs().end(), rhs);
+    std::copy(pr.aP().begin(), pr.aP().end(), aP);
+    return 0;
+}
+
 // ------------------------------------------------------------------ solvers
+// make_gmres / make_bicgstab / make_cg (LinearSolvers.cpp:462-473), as
+// make_linear_solver dispatches them (Solver.cpp:25-39): kind is the
+// LinearSolverKind ordinal (0 GMRES, 1 BiCGSTAB, 2 CG).  Returns the
+// iteration count; x from 0.
+int ref_krylov(int kind, int precond, double tol, int maxit, int restart, int n, const int* rowPtr,
+               const int* colIdx, const double* values, const double* b, double* x, double* lastRes,
+               double* seconds)
+{
+    auto A = make_csr(n, rowPtr, colIdx, values);
+    S::LinearSolverConfig c;
+    c.kind = static_cast<S::LinearSolverKind>(kind);
+    c.preconditioner = static_cast<S::PreconditionerKind>(precond);
+    c.tolerance = tol;
+    c.maxIterations = maxit;
+    c.restart = restart;
+    std::unique_ptr<S::ILinearSolver> sol = kind == 1 ? S::make_bicgstab(c) : kind == 2 ? S::make_cg(c) : S::make_gmres(c);
+    Vec bb(b, b + n), xx(n, 0.0);
+    const auto t0 = std::chrono::steady_clock::now();
+    const int it = sol->solve(A, bb, xx);
+    if (seconds)
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    std::copy(xx.begin(), xx.end(), x);
+    *lastRes = sol->last_residual();
+    return it;
+}
+
 // CGSolver::solve (LinearSolvers.cpp:420) with the given preconditioner
 // (PreconditionerKind ordinal).  Returns the iteration count.
 int ref_cg(int n, const int* rowPtr, const int* colIdx, const double* values, const double* b,

@@ -1041,3 +1041,359 @@ void orc_correct_fields(int64_t nC, int64_t nF, const int64_t *owner, const int6
     free(mInv);
     free(g);
 }
+
+/* ------------------------------------------------------------------ momentum */
+
+/*
+ * assemble_momentum (src/solver/SimpleAlgorithm.cpp:240-355) for one velocity
+ * component, first-order upwind, no periodic faces.  values (on the shared
+ * pattern) and rhs are overwritten.  Face loop in face order with the
+ * reference's add_at scatter:
+ *   F = phi_f, ConvO = max(F, 0), ConvN = max(-F, 0), D = mu |A|^2 / max(|d.A|, 1e-30)
+ *   (d: neighbour centroid - owner centroid, or face centroid - owner
+ *   centroid on a boundary face);
+ *   interior: oo += ConvO + D, on -= ConvN + D, nn += ConvN + D, no -= ConvO + D;
+ *   boundary by the zone's first spec (zoneType[z], -1 when none):
+ *     NoSlipWall / Wall / VelocityInlet / MovingWall: oo += ConvO + D,
+ *       rhs_o += (ConvN + D) Ub, Ub = 0 for the walls, the zone vector's
+ *       component otherwise;  Symmetry: nothing;  any other: oo += ConvO.
+ * Then rhs_c -= gp_c vol_c (gp = the component of the pressure gradient);
+ * transient (dt > 0): Vrho_dt = rho vol_c / dt, BDF2 (useBDF2) adds
+ * 1.5 Vrho_dt to the diagonal and (2 Un - 0.5 Unm1) Vrho_dt to rhs, implicit
+ * Euler Vrho_dt and Un Vrho_dt; then Patankar under-relaxation:
+ * a = diag / urfU, rhs_c += (a - diag) Ucomp_c.  aPout (optional) receives the
+ * relaxed diagonal (the reference captures it for component 0).
+ * opt = {rho, mu, urfU, dt}.
+ */
+void orc_assemble_momentum(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                           const double *ay, const double *az, const double *fcx, const double *fcy,
+                           const double *fcz, const double *ccx, const double *ccy, const double *ccz,
+                           const double *vol, const uint32_t *zone, const int *zoneType, const double *zoneVec,
+                           int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int useBDF2,
+                           int comp, const double *phi, const double *gp, const double *Ucomp, const double *Un,
+                           const double *Unm1, double *values, double *rhs, double *aPout)
+{
+    const double rho = opt[0], mu = opt[1], urfU = opt[2], dt = opt[3];
+    const int64_t nnz = rowPtr[nC];
+    for (int64_t k = 0; k < nnz; ++k)
+        values[k] = 0.0;
+    for (int64_t c = 0; c < nC; ++c)
+        rhs[c] = 0.0;
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        const double Ax = ax[f], Ay = ay[f], Az = az[f];
+        const double Amag2 = Ax * Ax + Ay * Ay + Az * Az;
+        const double Ff = phi[f];
+        const double ConvO = STD_MAX(Ff, 0.0);
+        const double ConvN = STD_MAX(-Ff, 0.0);
+        if (n != ORC_BOUNDARY) {
+            const double dx = ccx[n] - ccx[o], dy = ccy[n] - ccy[o], dz = ccz[n] - ccz[o];
+            const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+            const double D = mu * Amag2 / STD_MAX(ddotA, 1e-30);
+            add_at(rowPtr, colIdx, values, o, o, ConvO + D);
+            add_at(rowPtr, colIdx, values, o, n, -(ConvN + D));
+            add_at(rowPtr, colIdx, values, n, n, ConvN + D);
+            add_at(rowPtr, colIdx, values, n, o, -(ConvO + D));
+        } else {
+            const uint32_t z = zone[f];
+            const int t = (int)z < nZones ? zoneType[z] : -1;
+            const double dx = fcx[f] - ccx[o], dy = fcy[f] - ccy[o], dz = fcz[f] - ccz[o];
+            const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+            const double D = mu * Amag2 / STD_MAX(ddotA, 1e-30);
+            if (t == ORC_BC_NOSLIP || t == ORC_BC_WALL || t == ORC_BC_VELIN || t == ORC_BC_MOVING) {
+                const double Ub = (t == ORC_BC_NOSLIP || t == ORC_BC_WALL) ? 0.0 : zoneVec[3 * z + comp];
+                add_at(rowPtr, colIdx, values, o, o, ConvO + D);
+                rhs[o] += (ConvN + D) * Ub;
+            } else if (t == ORC_BC_SYMMETRY) {
+                /* zero normal gradient: no contribution */
+            } else {
+                add_at(rowPtr, colIdx, values, o, o, ConvO);
+            }
+        }
+    }
+    for (int64_t c = 0; c < nC; ++c)
+        rhs[c] -= gp[c] * vol[c];
+    if (dt > 0.0) {
+        for (int64_t c = 0; c < nC; ++c) {
+            const double Vrho_dt = rho * vol[c] / dt;
+            const int32_t kd = find_col(rowPtr, colIdx, c, c);
+            if (kd < 0)
+                continue;
+            if (useBDF2) {
+                values[kd] += 1.5 * Vrho_dt;
+                rhs[c] += (2.0 * Un[c] - 0.5 * Unm1[c]) * Vrho_dt;
+            } else {
+                values[kd] += Vrho_dt;
+                rhs[c] += Un[c] * Vrho_dt;
+            }
+        }
+    }
+    for (int64_t c = 0; c < nC; ++c) {
+        const int32_t kd = find_col(rowPtr, colIdx, c, c);
+        if (kd < 0)
+            continue;
+        const double aDiag = values[kd];
+        const double scaled = aDiag / urfU;
+        values[kd] = scaled;
+        rhs[c] += (scaled - aDiag) * Ucomp[c];
+    }
+    if (aPout)
+        for (int64_t c = 0; c < nC; ++c) {
+            const int32_t kd = find_col(rowPtr, colIdx, c, c);
+            aPout[c] = kd >= 0 ? values[kd] : 0.0;
+        }
+}
+
+/* ------------------------------------------------------------------ non-symmetric Krylov */
+
+/* make_preconditioner (src/solver/LinearSolvers.cpp:240-254) for the kinds the
+ * device supports: 1 ILU(0), anything else Jacobi. */
+typedef struct {
+    int ilu;
+    int64_t n;
+    const int32_t *rowPtr, *colIdx;
+    double *invD, *lu, *y;
+    int32_t *diagPtr;
+} OrcPrec;
+
+static void prec_setup(OrcPrec *M, int kind, int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
+                       const double *values)
+{
+    memset(M, 0, sizeof(*M));
+    M->ilu = (kind == 1);
+    M->n = n;
+    M->rowPtr = rowPtr;
+    M->colIdx = colIdx;
+    if (M->ilu) {
+        M->lu = (double *)xmalloc((size_t)rowPtr[n] * sizeof(double) + 8);
+        M->diagPtr = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
+        M->y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_ilu0_setup(n, rowPtr, colIdx, values, M->lu, M->diagPtr);
+    } else {
+        M->invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_jacobi_setup(n, rowPtr, colIdx, values, M->invD);
+    }
+}
+
+static void prec_apply(const OrcPrec *M, const double *r, double *z)
+{
+    if (M->ilu)
+        orc_ilu0_apply(M->n, M->rowPtr, M->colIdx, M->lu, M->diagPtr, r, z, M->y);
+    else
+        for (int64_t i = 0; i < M->n; ++i)
+            z[i] = M->invD[i] * r[i];
+}
+
+static void prec_free(OrcPrec *M)
+{
+    free(M->invD);
+    free(M->lu);
+    free(M->y);
+    free(M->diagPtr);
+}
+
+/*
+ * BiCGSTAB (BiCGSTABSolver::solve, src/solver/LinearSolvers.cpp:363-405), x
+ * from 0: r = b - A x, rh = r, rho = alpha = omega = 1, v = 0;
+ * loop { rhoNew = rh.r; if 0 -> last = |r|/bnorm, return it;
+ *        beta = (rhoNew/rho)(alpha/omega); p = r + beta (p - omega v);
+ *        y = M p; v = A y; alpha = rhoNew / rh.v; s = r - alpha v;
+ *        if |s| < tol bnorm -> x += alpha y, last = |s|/bnorm, return it+1;
+ *        z = M s; t = A z; omega = t.s / max(t.t, 1e-30);
+ *        x += alpha y + omega z; r = s - omega t; rho = rhoNew;
+ *        last = |r|/bnorm; if last < tol return it+1 }  return maxIt.
+ */
+int orc_bicgstab(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,
+                 int precond, double tol, int maxIt, double *x, double *lastRes)
+{
+    OrcPrec M;
+    prec_setup(&M, precond, n, rowPtr, colIdx, values);
+    const size_t bytes = (size_t)n * sizeof(double) + 8;
+    double *r = (double *)xmalloc(bytes), *rh = (double *)xmalloc(bytes), *p = (double *)xmalloc(bytes);
+    double *v = (double *)xmalloc(bytes), *s = (double *)xmalloc(bytes), *t = (double *)xmalloc(bytes);
+    double *y = (double *)xmalloc(bytes), *z = (double *)xmalloc(bytes);
+    for (int64_t i = 0; i < n; ++i) {
+        x[i] = 0.0;
+        p[i] = 0.0;
+    }
+    orc_spmv(n, rowPtr, colIdx, values, x, v);
+    for (int64_t i = 0; i < n; ++i)
+        r[i] = b[i] - v[i];
+    memcpy(rh, r, (size_t)n * sizeof(double));
+    double rho = 1.0, alpha = 1.0, omega = 1.0, last = 0.0;
+    const double bn = norm2(n, b);
+    const double bnorm = STD_MAX(bn, 1e-30);
+    for (int64_t i = 0; i < n; ++i)
+        v[i] = 0.0;
+    int ret = maxIt;
+    for (int it = 0; it < maxIt; ++it) {
+        const double rhoNew = orc_dot(n, rh, r);
+        if (rhoNew == 0.0) {
+            last = norm2(n, r) / bnorm;
+            ret = it;
+            goto out;
+        }
+        const double beta = (rhoNew / rho) * (alpha / omega);
+        for (int64_t i = 0; i < n; ++i)
+            p[i] = r[i] + beta * (p[i] - omega * v[i]);
+        prec_apply(&M, p, y);
+        orc_spmv(n, rowPtr, colIdx, values, y, v);
+        alpha = rhoNew / orc_dot(n, rh, v);
+        for (int64_t i = 0; i < n; ++i)
+            s[i] = r[i] - alpha * v[i];
+        if (norm2(n, s) < tol * bnorm) {
+            axpy(n, alpha, y, x);
+            last = norm2(n, s) / bnorm;
+            ret = it + 1;
+            goto out;
+        }
+        prec_apply(&M, s, z);
+        orc_spmv(n, rowPtr, colIdx, values, z, t);
+        {
+            const double tt = orc_dot(n, t, t);
+            omega = orc_dot(n, t, s) / STD_MAX(tt, 1e-30);
+        }
+        for (int64_t i = 0; i < n; ++i) {
+            x[i] += alpha * y[i] + omega * z[i];
+            r[i] = s[i] - omega * t[i];
+        }
+        rho = rhoNew;
+        last = norm2(n, r) / bnorm;
+        if (last < tol) {
+            ret = it + 1;
+            goto out;
+        }
+    }
+out:
+    *lastRes = last;
+    free(r);
+    free(rh);
+    free(p);
+    free(v);
+    free(s);
+    free(t);
+    free(y);
+    free(z);
+    prec_free(&M);
+    return ret;
+}
+
+/*
+ * GMRES(m), left-preconditioned, modified Gram-Schmidt and Givens rotations
+ * (GMRESmSolver::solve, src/solver/LinearSolvers.cpp:268-343), x from 0.
+ * Each cycle: r = b - A x, z = M r, beta = |z|; beta < tol bnorm -> last =
+ * beta/bnorm, return iter.  V0 = z/beta, s = (beta, 0, ...); Arnoldi steps
+ * j = 0.. while j < m and iter < maxIt: z = M A v_j; H_ij = v_i.z, z -= H_ij v_i
+ * (i = 0..j); H_{j+1,j} = |z|; v_{j+1} = z / H_{j+1,j} unless it is 0; apply
+ * the previous rotations to column j, form the new one with hypot, rotate s;
+ * last = |s_{j+1}|/bnorm, stop the cycle when last < tol (j counts the step,
+ * iter does not).  Back-substitute H y = s over the j steps, x += V y; return
+ * iter when last < tol.  The outer loop runs at most maxIt cycles.
+ */
+int orc_gmres(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,
+              int precond, double tol, int maxIt, int restart, double *x, double *lastRes)
+{
+    OrcPrec M;
+    prec_setup(&M, precond, n, rowPtr, colIdx, values);
+    const int m = restart > 1 ? restart : 1;
+    const size_t bytes = (size_t)n * sizeof(double) + 8;
+    double *r = (double *)xmalloc(bytes), *w = (double *)xmalloc(bytes), *z = (double *)xmalloc(bytes);
+    double *V = (double *)xmalloc((size_t)(m + 1) * bytes);
+    double *H = (double *)xmalloc((size_t)(m + 1) * (size_t)m * sizeof(double));
+    double *cs = (double *)xmalloc((size_t)m * sizeof(double)), *sn = (double *)xmalloc((size_t)m * sizeof(double));
+    double *sv = (double *)xmalloc((size_t)(m + 1) * sizeof(double)), *yv = (double *)xmalloc((size_t)m * sizeof(double) + 8);
+#define VV(i) (V + (size_t)(i) * ((size_t)n + 1))
+#define HH(i, j) H[(size_t)(i) * (size_t)m + (size_t)(j)]
+    memset(V, 0, (size_t)(m + 1) * bytes);
+    memset(H, 0, (size_t)(m + 1) * (size_t)m * sizeof(double));
+    memset(cs, 0, (size_t)m * sizeof(double));
+    memset(sn, 0, (size_t)m * sizeof(double));
+    for (int64_t i = 0; i < n; ++i)
+        x[i] = 0.0;
+    const double bn = norm2(n, b);
+    const double bnorm = STD_MAX(bn, 1e-30);
+    double last = 0.0;
+    int iter = 0;
+    int ret = -1;
+    for (int outer = 0; outer < maxIt && ret < 0; ++outer) {
+        orc_spmv(n, rowPtr, colIdx, values, x, w);
+        for (int64_t i = 0; i < n; ++i)
+            r[i] = b[i] - w[i];
+        prec_apply(&M, r, z);
+        const double beta = norm2(n, z);
+        if (beta < tol * bnorm) {
+            last = beta / bnorm;
+            ret = iter;
+            break;
+        }
+        memcpy(VV(0), z, (size_t)n * sizeof(double));
+        {
+            const double sc = 1.0 / beta;
+            for (int64_t i = 0; i < n; ++i)
+                VV(0)[i] *= sc;
+        }
+        for (int i = 0; i <= m; ++i)
+            sv[i] = 0.0;
+        sv[0] = beta;
+        int j;
+        for (j = 0; j < m && iter < maxIt; ++j, ++iter) {
+            orc_spmv(n, rowPtr, colIdx, values, VV(j), w);
+            prec_apply(&M, w, z);
+            for (int i = 0; i <= j; ++i) {
+                HH(i, j) = orc_dot(n, VV(i), z);
+                axpy(n, -HH(i, j), VV(i), z);
+            }
+            HH(j + 1, j) = norm2(n, z);
+            if (HH(j + 1, j) != 0.0) {
+                memcpy(VV(j + 1), z, (size_t)n * sizeof(double));
+                const double sc = 1.0 / HH(j + 1, j);
+                for (int64_t i = 0; i < n; ++i)
+                    VV(j + 1)[i] *= sc;
+            }
+            for (int i = 0; i < j; ++i) {
+                const double t = cs[i] * HH(i, j) + sn[i] * HH(i + 1, j);
+                HH(i + 1, j) = -sn[i] * HH(i, j) + cs[i] * HH(i + 1, j);
+                HH(i, j) = t;
+            }
+            const double dd = hypot(HH(j, j), HH(j + 1, j));
+            cs[j] = HH(j, j) / dd;
+            sn[j] = HH(j + 1, j) / dd;
+            HH(j, j) = dd;
+            HH(j + 1, j) = 0.0;
+            const double t = cs[j] * sv[j];
+            sv[j + 1] = -sn[j] * sv[j];
+            sv[j] = t;
+            last = fabs(sv[j + 1]) / bnorm;
+            if (last < tol) {
+                ++j;
+                break;
+            }
+        }
+        for (int i = j - 1; i >= 0; --i) {
+            double sum = sv[i];
+            for (int k = i + 1; k < j; ++k)
+                sum -= HH(i, k) * yv[k];
+            yv[i] = sum / HH(i, i);
+        }
+        for (int i = 0; i < j; ++i)
+            axpy(n, yv[i], VV(i), x);
+        if (last < tol)
+            ret = iter;
+    }
+#undef VV
+#undef HH
+    if (ret < 0)
+        ret = iter;
+    *lastRes = last;
+    free(r);
+    free(w);
+    free(z);
+    free(V);
+    free(H);
+    free(cs);
+    free(sn);
+    free(sv);
+    free(yv);
+    prec_free(&M);
+    return ret;
+}

@@ -5,7 +5,8 @@ oracle/_ref/libsimall_ref.so, built by oracle/build_ref.sh from the SimAll
 sources).  Every array stored here is an output of the reference's functions
 (CartesianMesher + ConnectivityBuilder + compute_geometry,
 renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
-assemble_pressure_correction, CGSolver::solve with Jacobi and ILU0, the
+assemble_pressure_correction / assemble_momentum, CGSolver::solve with
+Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
 preconditioners' apply, the SIMPLE cavity loop, solve_discrete_adjoint);
 inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
@@ -131,6 +132,42 @@ def field_loops_case(name):
                         pPrime=pp, p0=p0, p1=p1, U1=np.array(U1), phi1=phi1)
 
 
+MOM_BCS = [(1, 4, (0.7, -0.2, 0.1)), (2, 7), (3, 1), (4, 2, (1.0, 0.3, 0.0)), (5, 9), (6, 3)]
+
+
+def momentum_case(name):
+    """assemble_momentum of the reference (three components, BDF2 step) on a
+    distorted, RCM-renumbered 7x6x5 box with every boundary treatment, and the
+    reference's GMRES(5)+ILU(0) and BiCGSTAB+Jacobi solves of the x system."""
+    dims = (7, 6, 5)
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=17)
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=True)
+    rng = np.random.default_rng(17)
+    nC = rm["nC"]
+    U = rng.standard_normal((3, nC))
+    p = rng.standard_normal(nC)
+    Un = rng.standard_normal((3, nC))
+    Unm1 = rng.standard_normal((3, nC))
+    phi = R.face_fluxes(rm, MOM_BCS, 1.1, U)
+    opt = np.array([1.1, 0.013, 0.7, 0.05])
+    vals, rhs = [], []
+    for comp in range(3):
+        v, b, aP = R.assemble_momentum(rm, MOM_BCS, opt, comp, U, p, phi, Un, Unm1, bdf2=True, time_step=1)
+        vals.append(v)
+        rhs.append(b)
+        if comp == 0:
+            aP0 = aP
+    rp, ci, _, _ = R.assemble(rm, [], 1.0, np.ones(nC), np.zeros(rm["nF"]))
+    xg, itg, lg, _ = R.krylov(0, rp, ci, vals[0], rhs[0], 1, 1e-10, 200, 5)
+    xb, itb, lb, _ = R.krylov(1, rp, ci, vals[0], rhs[0], 0, 1e-10, 200)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), seed=np.array(17),
+                        bc_zone=np.array([b[0] for b in MOM_BCS]), bc_type=np.array([b[1] for b in MOM_BCS]),
+                        bc_vec=np.array([list(b[2]) if len(b) > 2 else [0.0, 0.0, 0.0] for b in MOM_BCS]),
+                        opt=opt, U=U, p=p, Un=Un, Unm1=Unm1, phi=phi, rowPtr=rp, colIdx=ci, values=np.array(vals),
+                        rhs=np.array(rhs), aP=aP0, x_gmres=xg, it_gmres=np.array(itg), last_gmres=np.array(lg),
+                        x_bicgstab=xb, it_bicgstab=np.array(itb), last_bicgstab=np.array(lb))
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -164,6 +201,7 @@ def main():
     adjoint_case("adjoint_face_k_5x4x3.npz")
     simplec_case("simplec_6x5x4_outlet.npz")
     field_loops_case("field_loops_7x6x5_rcm.npz")
+    momentum_case("momentum_7x6x5_rcm_bdf2.npz")
     print("fixtures written to", HERE)
 
 

@@ -148,6 +148,43 @@ def test_field_loops_fixture(oracle):
     assert bits_equal(p1, g["p1"]) and bits_equal(np.array(U1), g["U1"]) and bits_equal(phi1, g["phi1"])
 
 
+def momentum_fixture(oracle):
+    from simall_gb300 import workloads as W
+
+    g = load("momentum_7x6x5_rcm_bdf2.npz")
+    dims = tuple(int(v) for v in g["dims"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=int(g["seed"])))
+    oracle.rcm(m)
+    bcs = [(int(z), int(t), tuple(v)) for z, t, v in zip(g["bc_zone"], g["bc_type"], g["bc_vec"])]
+    return g, m, bcs
+
+
+def test_momentum_assembly_fixture(oracle):
+    """assemble_momentum (three components, BDF2) reproduces the reference's
+    values, rhs and aP_ bytes."""
+    g, m, bcs = momentum_fixture(oracle)
+    rp, ci = oracle.build_sparsity(m)
+    assert np.array_equal(rp, g["rowPtr"]) and np.array_equal(ci, g["colIdx"])
+    gp = oracle.lsq_gradient(m, g["p"])
+    for comp in range(3):
+        v, rhs, aP = oracle.assemble_momentum(m, rp, ci, bcs, g["opt"], comp, g["phi"], gp[comp], g["U"][comp],
+                                              g["Un"][comp], g["Unm1"][comp], bdf2=True)
+        assert bits_equal(v, g["values"][comp]) and bits_equal(rhs, g["rhs"][comp])
+        if comp == 0:
+            assert bits_equal(aP, g["aP"])
+
+
+def test_gmres_bicgstab_fixture(oracle):
+    """GMRES(5)+ILU(0) and BiCGSTAB+Jacobi on the reference's momentum system:
+    iteration count, last residual and x bit-identical."""
+    g = load("momentum_7x6x5_rcm_bdf2.npz")
+    args = (g["rowPtr"], g["colIdx"], g["values"][0], g["rhs"][0])
+    x, it, last = oracle.gmres(*args, 1, 1e-10, 200, 5)
+    assert it == int(g["it_gmres"]) and last == float(g["last_gmres"]) and bits_equal(x, g["x_gmres"])
+    x, it, last = oracle.bicgstab(*args, 0, 1e-10, 200)
+    assert it == int(g["it_bicgstab"]) and last == float(g["last_bicgstab"]) and bits_equal(x, g["x_bicgstab"])
+
+
 def test_face_conductance_adjoint_against_reference_gradient(oracle):
     """Face-conductance assembly reproduced bit for bit; the adjoint gradient
     (CG on A^T = A, then the scatter) matches solve_discrete_adjoint's."""

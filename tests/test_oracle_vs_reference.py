@@ -124,3 +124,84 @@ def test_discrete_adjoint_2x2_known_answer(ref):
                                                    np.zeros(0), np.zeros(0), np.zeros(2))
     assert rc == 0
     assert abs(psi[0] - 0.5) < 1e-6 and abs(psi[1] - 1.0 / 6.0) < 1e-6
+
+
+# every boundary treatment of assemble_momentum: VelocityInlet, PressureOutlet
+# (the "other" branch), NoSlipWall, MovingWall, Symmetry, SlipWall (other), and
+# zone 0 of a 2-D mesh's front/back faces without a spec
+MOM_BCS = [(1, 4, (0.7, -0.2, 0.1)), (2, 7), (3, 1), (4, 2, (1.0, 0.3, 0.0)), (5, 9), (6, 3)]
+
+
+@pytest.mark.parametrize("dims,renumber,dt,bdf2", [((6, 5, 4), False, 0.0, False), ((7, 6, 5), True, 0.05, False),
+                                                   ((9, 8, 1), False, 0.02, True), ((5, 5, 5), True, 0.1, True)])
+def test_momentum_assembly(oracle, ref, dims, renumber, dt, bdf2):
+    """assemble_momentum for each component, steady, implicit Euler and BDF2:
+    the oracle reproduces the reference's values, rhs and aP_ bytes."""
+    sh = _shift(dims, 11, 0.2 if dims[2] > 1 else 0.0)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    rp, ci = oracle.build_sparsity(m)
+    rng = np.random.default_rng(12)
+    U = rng.standard_normal((3, m.nC))
+    p = rng.standard_normal(m.nC)
+    phi = oracle.face_fluxes(m, MOM_BCS, 1.1, U)
+    phi[::7] = 0.0
+    phi[3::11] = -0.0
+    Un = rng.standard_normal((3, m.nC))
+    Unm1 = rng.standard_normal((3, m.nC))
+    gp = oracle.lsq_gradient(m, p)
+    opt = (1.1, 0.013, 0.7, dt)
+    for comp in range(3):
+        v, rhs, aP = ref.assemble_momentum(r, MOM_BCS, opt, comp, U, p, phi, Un, Unm1, bdf2=bdf2, time_step=1)
+        ov, orhs, oaP = oracle.assemble_momentum(m, rp, ci, MOM_BCS, opt, comp, phi, gp[comp], U[comp], Un[comp],
+                                                 Unm1[comp], bdf2=bdf2)
+        assert bits_equal(v, ov) and bits_equal(rhs, orhs), comp
+        if comp == 0:
+            assert bits_equal(aP, oaP)
+    ref.free_mesh(r)
+
+
+def _conv_diff(n, pe=5.0):
+    """The non-symmetric 1-D upwind convection-diffusion matrix of
+    tests/unit/solver/test_tfqmr_solver.cpp:43-62."""
+    rp, ci, v = [0], [], []
+    for i in range(n):
+        if i > 0:
+            ci.append(i - 1)
+            v.append(-1.0 - pe)
+        ci.append(i)
+        v.append(2.0 + pe)
+        if i < n - 1:
+            ci.append(i + 1)
+            v.append(-1.0)
+        rp.append(len(ci))
+    return np.array(rp, np.int32), np.array(ci, np.int32), np.array(v)
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("pc", [0, 1])
+def test_nonsymmetric_krylov(oracle, ref, kind, pc):
+    """GMRES(m) and BiCGSTAB with Jacobi and ILU(0): iteration count, last
+    residual and x bit-identical to the reference, on the 1-D
+    convection-diffusion matrix and on a momentum system (restart short
+    enough to cycle)."""
+    systems = []
+    rp, ci, v = _conv_diff(40)
+    systems.append((rp, ci, v, np.ones(40), 1e-8, 500, 30))
+    m = oracle.cartesian_mesh(9, 8, 3, node_shift=_shift((9, 8, 3), 4, 0.2))
+    rp, ci = oracle.build_sparsity(m)
+    rng = np.random.default_rng(5)
+    U = rng.standard_normal((3, m.nC))
+    phi = oracle.face_fluxes(m, MOM_BCS, 1.0, U)
+    gp = oracle.lsq_gradient(m, rng.standard_normal(m.nC))
+    mv, mrhs, _ = oracle.assemble_momentum(m, rp, ci, MOM_BCS, (1.0, 0.01, 0.7, 0.0), 0, phi, gp[0], U[0])
+    systems.append((rp, ci, mv, mrhs, 1e-10, 200, 5))
+    systems.append((rp, ci, mv, mrhs, 1e-12, 7, 3))  # stops on maxIterations mid-cycle
+    for rp, ci, v, b, tol, mx, rs in systems:
+        x, it, last, _ = ref.krylov(kind, rp, ci, v, b, pc, tol, mx, rs)
+        ox, oit, olast = (oracle.gmres(rp, ci, v, b, pc, tol, mx, rs) if kind == 0
+                          else oracle.bicgstab(rp, ci, v, b, pc, tol, mx))
+        assert (it, last) == (oit, olast)
+        assert bits_equal(x, ox)
