@@ -101,10 +101,11 @@ void *simall_context_stream(const simall_context *ctx);
 /* Number of kernels this library launched on the context so far. */
 int64_t simall_context_kernel_launches(const simall_context *ctx);
 
-/* ------------------------------------------------------------------ PCG solver */
+/* ------------------------------------------------------------------ Krylov solver */
 /* Replaces solver::ILinearSolver / CGSolver (src/solver/Solver.hpp:92-100,
  * src/solver/LinearSolvers.cpp:415-459) and gpu::CgGpu
- * (src/gpu/CgGpu.hpp:87-124). */
+ * (src/gpu/CgGpu.hpp:87-124); with `kind` also GMRESmSolver and
+ * BiCGSTABSolver (make_linear_solver, src/solver/Solver.cpp:25-39). */
 typedef struct simall_solver_config {
     int preconditioner;    /* simall_preconditioner; default Jacobi */
     double tolerance;      /* stop when ||r||/max(||b||,1e-30) < tolerance; default 1e-8 */
@@ -113,7 +114,21 @@ typedef struct simall_solver_config {
     double reliable_delta; /* mixed: iterated-residual drop that triggers an FP64 update; default 0.1 */
     int check_interval;    /* iterations between host polls of the device stop flag; 0 = automatic */
     int engine;            /* simall_engine: how the iteration runs; default SIMALL_ENGINE_AUTO */
+    int kind;              /* simall_solver_kind; default SIMALL_SOLVER_CG */
+    int restart;           /* GMRES(m): basis size m (LinearSolverConfig::restart); default 30 */
 } simall_solver_config;
+
+/* LinearSolverKind ordinals (src/solver/Solver.hpp:67-73).  CG is the pressure
+ * path (FP64 or mixed precision); GMRES(m) and BiCGSTAB (FP64, Jacobi or
+ * ILU(0)) follow GMRESmSolver::solve and BiCGSTABSolver::solve
+ * (src/solver/LinearSolvers.cpp:268-343, :363-405) for the momentum systems.
+ * TFQMR is rejected with SIMALL_ERR_UNSUPPORTED. */
+enum simall_solver_kind {
+    SIMALL_SOLVER_GMRES = 0,
+    SIMALL_SOLVER_BICGSTAB = 1,
+    SIMALL_SOLVER_CG = 2,
+    SIMALL_SOLVER_TFQMR = 3
+};
 
 /* SIMALL_ENGINE_AUTO: systems of up to 131,072 rows (Jacobi FP64, or mixed
  * precision in diagonal storage) run the whole solve on one thread-block
@@ -262,6 +277,34 @@ int simall_lsq_gradient(simall_pressure_system *ps, const double *f, double *gx,
  * p, U and phi are updated in place. */
 int simall_correct_fields(simall_pressure_system *ps, double rho, double urfP, const double *aP, const double *pPrime,
                           double *p, double *Ux, double *Uy, double *Uz, double *phi, int mem);
+
+/* ------------------------------------------------------------------ momentum assembly */
+/* Replaces SimpleAlgorithm::assemble_momentum (src/solver/SimpleAlgorithm.cpp:240-355),
+ * first-order upwind, no periodic faces.  The reference assembles one velocity
+ * component per call, but its matrix does not depend on the component; one call
+ * here builds that matrix once on the system's pattern (the pattern the
+ * pressure system shares with the momentum matrix, build_sparsity) and the
+ * three right-hand sides, bit-identical to the reference's three assemblies.
+ * Needs simall_pressure_system_setup_field_loops (geometry, boundary kinds and
+ * zone vectors, the least-squares gradient of p). */
+typedef struct simall_momentum_options {
+    double rho;  /* SimpleOptions::rho */
+    double mu;   /* SimpleOptions::mu */
+    double urfU; /* SimpleOptions::urfU (Patankar under-relaxation) */
+    double dt;   /* SimpleOptions::dt; > 0 adds the transient term */
+    int bdf2;    /* 1: BDF2 (TemporalScheme::BDF2 once timeStep >= 1), 0: implicit Euler */
+    int reserved;
+} simall_momentum_options;
+/* U, Un, Unm1: [3][n_cells] (x, y, z components back to back); p[n_cells];
+ * phi[n_faces].  Un is read when dt > 0, Unm1 when dt > 0 and bdf2.  The
+ * result stays on the device (simall_momentum_device_arrays / _download). */
+int simall_assemble_momentum(simall_pressure_system *ps, const simall_momentum_options *opt, const double *U,
+                             const double *p, const double *phi, const double *Un, const double *Unm1, int mem);
+/* Device arrays of the last momentum assembly: values[nnz] on the system's
+ * pattern, rhs[3][n_cells], aP[n_cells] (the relaxed diagonal, SimpleAlgorithm::aP_). */
+int simall_momentum_device_arrays(const simall_pressure_system *ps, const double **values, const double **rhs,
+                                  const double **aP);
+int simall_momentum_download(const simall_pressure_system *ps, double *values, double *rhs, double *aP);
 
 /* ------------------------------------------------------------------ differentiation */
 /* Face-conductance Poisson operator (an extension: the reference expresses

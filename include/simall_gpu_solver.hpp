@@ -44,6 +44,8 @@ public:
         c.tolerance = cfg.tolerance;
         c.max_iterations = cfg.maxIterations;
         c.precision = precision;
+        c.kind = static_cast<int>(cfg.kind);  // CG, GMRES(restart) or BiCGSTAB, as make_linear_solver
+        c.restart = cfg.restart;
         const int st = simall_solver_create(ctx_, &c, &s_);
         if (st != SIMALL_OK) {
             const std::string msg = simall_context_last_error(ctx_);
@@ -93,5 +95,8 @@ private:
     int status_ = SIMALL_OK;
     int maxIt_ = 1000;
 };
+
+// The same adapter for any LinearSolverKind the device provides.
+using GpuLinearSolver = GpuPcgSolver;
 
 }  // namespace simall::gpu_gb300

@@ -31,7 +31,7 @@ STATUS_NAMES = {
 
 class SolverConfig(C.Structure):
     _fields_ = [("preconditioner", _I), ("tolerance", _D), ("max_iterations", _I), ("precision", _I),
-                ("reliable_delta", _D), ("check_interval", _I), ("engine", _I)]
+                ("reliable_delta", _D), ("check_interval", _I), ("engine", _I), ("kind", _I), ("restart", _I)]
 
 
 class SolverStats(C.Structure):
@@ -42,6 +42,10 @@ class SolverStats(C.Structure):
 
 class ZoneVelocity(C.Structure):
     _fields_ = [("zone", C.c_uint32), ("u", _D * 3)]
+
+
+class MomentumOptions(C.Structure):
+    _fields_ = [("rho", _D), ("mu", _D), ("urfU", _D), ("dt", _D), ("bdf2", _I), ("reserved", _I)]
 
 
 class MeshView(C.Structure):
@@ -97,6 +101,9 @@ SIGNATURES = {
     "simall_compute_face_fluxes": (_I, [_P, _D, _P, _P, _P, _P, _I]),
     "simall_lsq_gradient": (_I, [_P, _P, _P, _P, _P, _I]),
     "simall_correct_fields": (_I, [_P, _D, _D, _P, _P, _P, _P, _P, _P, _P, _I]),
+    "simall_assemble_momentum": (_I, [_P, C.POINTER(MomentumOptions), _P, _P, _P, _P, _P, _I]),
+    "simall_momentum_device_arrays": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "simall_momentum_download": (_I, [_P, _P, _P, _P]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),

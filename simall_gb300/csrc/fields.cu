@@ -14,6 +14,7 @@
 #include "solver.hpp"
 
 #include <algorithm>
+#include <cmath>
 #include <new>
 #include <vector>
 
@@ -217,6 +218,17 @@ bool bad_mem(int mem) { return mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVIC
 
 }  // namespace
 
+int ps_gradient(simall_pressure_system *ps, const double *f, double *g)
+{
+    simall_context *ctx = ps->ctx;
+    const int64_t nC = ps->nC;
+    k_lsq_gradient<<<grid_for_ps(ctx, nC), kBlock, 0, ctx->stream>>>(nC, ps->cfOff.p, ps->cfEnt.p, ps->owner.p,
+                                                                     ps->neighbor.p, ps->gdx.p, ps->gdy.p, ps->gdz.p,
+                                                                     ps->gw2.p, ps->minv.p, f, g, g + nC, g + 2 * nC);
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
 }  // namespace simall
 
 using namespace simall;
@@ -241,6 +253,8 @@ int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const s
     // VelocityInlet / MovingWall -> the zone's vector; NoSlipWall / Wall /
     // Symmetry -> zero; any other spec, or none -> the owner's velocity
     std::vector<uint8_t> fk(static_cast<size_t>(nF));
+    // momentum boundary kinds (assemble_momentum, SimpleAlgorithm.cpp:278-318)
+    std::vector<uint8_t> mk(static_cast<size_t>(nF), kMomInterior);
     std::vector<int32_t> slot(static_cast<size_t>(nF), -1);
     std::vector<double> vx, vy, vz;
     std::vector<std::pair<uint32_t, int32_t>> zoneSlot;  // zone -> slot
@@ -256,6 +270,10 @@ int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const s
                 type = b.type;
                 break;
             }
+        mk[f] = (type == SIMALL_BC_VELOCITY_INLET || type == SIMALL_BC_MOVING_WALL) ? kMomZoneVector
+                : (type == SIMALL_BC_NO_SLIP_WALL || type == SIMALL_BC_WALL)       ? kMomWall
+                : (type == SIMALL_BC_SYMMETRY)                                     ? kMomSymmetry
+                                                                                   : kMomOther;
         if (type == SIMALL_BC_VELOCITY_INLET || type == SIMALL_BC_MOVING_WALL) {
             fk[f] = kFaceZoneVector;
             int32_t sl = -1;
@@ -305,6 +323,7 @@ int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const s
     SIMALL_CUDA_TRY(ctx, ps->minv.alloc(6 * nC));
     SIMALL_CUDA_TRY(ctx, ps->vol.alloc(nC));
     SIMALL_CUDA_TRY(ctx, ps->fkind.alloc(nF));
+    SIMALL_CUDA_TRY(ctx, ps->mkind.alloc(nF));
     SIMALL_CUDA_TRY(ctx, ps->fvslot.alloc(nF));
     SIMALL_CUDA_TRY(ctx, ps->zvec.alloc(zv.size()));
     SIMALL_CUDA_TRY(ctx, ps->grad.alloc(3 * nC));
@@ -313,6 +332,8 @@ int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const s
     SIMALL_CUDA_TRY(ctx, up(ps->az.p, m->area_z, nF * sizeof(double)));
     SIMALL_CUDA_TRY(ctx, up(ps->vol.p, cell_volume, nC * sizeof(double)));
     SIMALL_CUDA_TRY(ctx, up(ps->fkind.p, fk.data(), nF));
+    SIMALL_CUDA_TRY(ctx, up(ps->mkind.p, mk.data(), nF));
+    ps->momMu = std::nan("");  // the momentum face diffusion is recomputed at the next assembly
     SIMALL_CUDA_TRY(ctx, up(ps->fvslot.p, slot.data(), nF * sizeof(int32_t)));
     SIMALL_CUDA_TRY(ctx, up(ps->zvec.p, zv.data(), zv.size() * sizeof(double)));
     {

@@ -498,6 +498,7 @@ int alloc_vectors(simall_solver *s)
 
 void drop_graphs(simall_solver *s)
 {
+    krylov_drop_graphs(s);
     for (auto &g : s->graphs)
         if (g.exec)
             cudaGraphExecDestroy(g.exec);
@@ -705,6 +706,8 @@ void simall_solver_config_default(simall_solver_config *cfg)
     cfg->reliable_delta = 0.1;
     cfg->check_interval = 0;
     cfg->engine = SIMALL_ENGINE_AUTO;
+    cfg->kind = SIMALL_SOLVER_CG;
+    cfg->restart = 30;
 }
 
 int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, simall_solver **out)
@@ -724,6 +727,12 @@ int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, s
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "precision %d", c.precision);
     if (c.precision == SIMALL_PRECISION_MIXED && c.preconditioner != SIMALL_PRECOND_JACOBI)
         return fail(ctx, SIMALL_ERR_UNSUPPORTED, "mixed precision runs with the Jacobi preconditioner");
+    if (c.kind != SIMALL_SOLVER_CG && c.kind != SIMALL_SOLVER_GMRES && c.kind != SIMALL_SOLVER_BICGSTAB)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "solver kind %d is not on this path", c.kind);
+    if (c.kind != SIMALL_SOLVER_CG && c.precision != SIMALL_PRECISION_FP64)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "GMRES and BiCGSTAB run in FP64");
+    if (c.kind == SIMALL_SOLVER_GMRES && c.restart < 1)
+        c.restart = 1;  // std::max(1, restart), LinearSolvers.cpp:273
     if (!(c.tolerance >= 0.0) || c.reliable_delta <= 0.0 || c.reliable_delta >= 1.0)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "tolerance / reliable_delta out of range");
     auto *s = new (std::nothrow) simall_solver;
@@ -743,6 +752,7 @@ int simall_solver_destroy(simall_solver *s)
     drop_graphs(s);
     ilu_free(s);
     mixed_free(s);
+    krylov_free(s);
     if (s->h_scal)
         cudaFreeHost(s->h_scal);
     delete s;
@@ -930,7 +940,9 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
     simall_solver_stats local{};
     int st;
     s->engine = 0;
-    if (s->cfg.precision == SIMALL_PRECISION_MIXED)
+    if (s->cfg.kind != SIMALL_SOLVER_CG)
+        st = krylov_solve(s);
+    else if (s->cfg.precision == SIMALL_PRECISION_MIXED)
         st = mixed_solve(s, &local);
     else
         st = fp64_solve(s, &local);

@@ -38,5 +38,20 @@ struct simall_pressure_system {
     int nslots = 0;
     simall::DevBuf<double> grad;                // [3][nC] scratch gradient
     simall::DevBuf<double> stage;               // staging for host field arrays
+    // momentum assembly (momentum.cu)
+    simall::DevBuf<uint8_t> mkind;              // face: kMom* below
+    simall::DevBuf<double> momD;                // mu |A|^2 / max(|d.A|, 1e-30) per face, for mu == momMu
+    double momMu = 0.0;                         // NaN until the first assembly
+    simall::DevBuf<double> mvalues, mrhs, maP;  // values[nnz] (shared pattern), rhs[3][nC], relaxed diagonal
+    bool momReady = false;
 };
+
+namespace simall {
+// Momentum face kinds: interior; VelocityInlet / MovingWall (the zone's vector);
+// NoSlipWall / Wall (zero); Symmetry (no contribution); any other boundary
+// (upwind outflow).
+constexpr uint8_t kMomInterior = 0, kMomZoneVector = 1, kMomWall = 2, kMomSymmetry = 3, kMomOther = 4;
+// Least-squares gradient of f (device, n_cells) into g[3][n_cells] (fields.cu).
+int ps_gradient(simall_pressure_system *ps, const double *f, double *g);
+}  // namespace simall
 

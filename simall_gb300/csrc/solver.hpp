@@ -21,6 +21,7 @@ struct IluData {
 };
 
 struct MixedData;  // mixed.cu
+struct KrylovData;  // krylov.cu
 
 // Chunk of solver iterations captured as a CUDA graph.
 struct GraphChunk {
@@ -57,6 +58,7 @@ struct simall_solver {
     int engine = 0;       // of the last solve: 0 kernels per step, 1 one cluster
     simall::IluData *ilu = nullptr;
     simall::MixedData *mixed = nullptr;
+    simall::KrylovData *krylov = nullptr;
     std::vector<simall::GraphChunk> graphs;  // captured iteration chunks
 };
 
@@ -90,6 +92,12 @@ struct ClusterMixedArgs {
     const double *scale;   // S = D^-1/2
 };
 int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status);
+
+// GMRES(m) / BiCGSTAB (krylov.cu): solve from x = 0 into s->x; fills the
+// result fields of s->h_scal.
+int krylov_solve(simall_solver *s);
+void krylov_drop_graphs(simall_solver *s);
+void krylov_free(simall_solver *s);
 
 // Host copy of the current pattern (ILU0 level analysis, CSR fallbacks).
 int solver_host_pattern(simall_solver *s);

@@ -216,6 +216,39 @@ class PressureSystem:
         check(self.L.simall_correct_fields(self.handle, float(rho), float(urfP), *[x for x, _ in pm], pm[0][1]),
               self.ctx.handle)
 
+    # -- momentum --------------------------------------------------------------------
+    def assemble_momentum(self, rho: float, mu: float, urfU: float, U, p, phi, dt: float = 0.0, Un=None, Unm1=None,
+                          bdf2: bool = False):
+        """assemble_momentum for all three components at once (one matrix,
+        three right-hand sides).  U, Un, Unm1: (3, n_cells) arrays or CUDA
+        tensors; the result stays on the device (momentum_download)."""
+        o = _lib.MomentumOptions(float(rho), float(mu), float(urfU), float(dt), int(bool(bdf2)), 0)
+        args = [ptr_and_mem(a) for a in (U, p, phi)]
+        mem = args[0][1]
+        extra = [ptr_and_mem(a)[0] if a is not None else None for a in (Un, Unm1)]
+        for a in (Un, Unm1):
+            if a is not None and ptr_and_mem(a)[1] != mem:
+                raise ValueError("all arrays must live in the same memory")
+        if any(m != mem for _, m in args):
+            raise ValueError("all arrays must live in the same memory")
+        check(self.L.simall_assemble_momentum(self.handle, C.byref(o), *[q for q, _ in args], *extra, mem),
+              self.ctx.handle)
+
+    def momentum_download(self):
+        """(values[nnz], rhs[3, n_cells], aP[n_cells]) of the last momentum assembly."""
+        v = np.empty(self.nnz)
+        r = np.empty((3, self.n))
+        a = np.empty(self.n)
+        check(self.L.simall_momentum_download(self.handle, v.ctypes.data, r.ctypes.data, a.ctypes.data),
+              self.ctx.handle)
+        return v, r, a
+
+    def momentum_device_arrays(self):
+        """Raw device addresses (values, rhs[3][n], aP) of the last momentum assembly."""
+        a = [C.c_void_p() for _ in range(3)]
+        check(self.L.simall_momentum_device_arrays(self.handle, *[C.byref(v) for v in a]), self.ctx.handle)
+        return tuple(v.value for v in a)
+
     def assemble_face_conductance(self, rho: float, k, pb, src):
         """Face-conductance operator: coef_f = k_f g_f, Dirichlet values pb on
         pressure-boundary faces, rhs from the cell source src."""

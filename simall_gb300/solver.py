@@ -175,7 +175,7 @@ class GpuCGSolver:
 
     def __init__(self, cfg: LinearSolverConfig | None = None, precision: Precision = Precision.FP64,
                  ctx: Context | None = None, reliable_delta: float = 0.1, check_interval: int = 0,
-                 engine: int = 0):
+                 engine: int = 0, _kind: LinearSolverKind = LinearSolverKind.CG):
         """engine: 0 automatic (one thread-block cluster for systems that fit),
         1 per-iteration kernels only."""
         cfg = cfg or LinearSolverConfig(kind=LinearSolverKind.CG)
@@ -191,6 +191,8 @@ class GpuCGSolver:
         c.reliable_delta = float(reliable_delta)
         c.check_interval = int(check_interval)
         c.engine = int(engine)
+        c.kind = int(_kind)
+        c.restart = int(cfg.restart)
         h = C.c_void_p()
         check(self.L.simall_solver_create(self.ctx.handle, C.byref(c), C.byref(h)), self.ctx.handle)
         self.handle = h.value
@@ -263,13 +265,36 @@ class GpuCGSolver:
             pass
 
 
+class GpuLinearSolver(GpuCGSolver):
+    """ILinearSolver of the kind cfg.kind names: GMRES(cfg.restart) or BiCGSTAB
+    (GMRESmSolver / BiCGSTABSolver, src/solver/LinearSolvers.cpp:268-405) in
+    FP64 with the Jacobi or ILU(0) preconditioner, or CG."""
+
+    def __init__(self, cfg: LinearSolverConfig | None = None, ctx: Context | None = None, check_interval: int = 0,
+                 **kw):
+        cfg = cfg or LinearSolverConfig()
+        if cfg.kind == LinearSolverKind.TFQMR:
+            raise NotImplementedError("TFQMR is not provided on the GPU")
+        super().__init__(cfg, ctx=ctx, check_interval=check_interval, _kind=cfg.kind, **kw)
+
+
 def make_cg(cfg: LinearSolverConfig, **kw) -> GpuCGSolver:
     return GpuCGSolver(cfg, **kw)
 
 
+def make_gmres(cfg: LinearSolverConfig, **kw) -> GpuLinearSolver:
+    return GpuLinearSolver(LinearSolverConfig(LinearSolverKind.GMRES, cfg.preconditioner, cfg.tolerance,
+                                              cfg.maxIterations, cfg.restart), **kw)
+
+
+def make_bicgstab(cfg: LinearSolverConfig, **kw) -> GpuLinearSolver:
+    return GpuLinearSolver(LinearSolverConfig(LinearSolverKind.BiCGSTAB, cfg.preconditioner, cfg.tolerance,
+                                              cfg.maxIterations, cfg.restart), **kw)
+
+
 def make_linear_solver(cfg: LinearSolverConfig, **kw) -> GpuCGSolver:
-    """make_linear_solver (src/solver/Solver.cpp:25-39) for the pressure path:
-    only the CG branch exists on the device."""
-    if cfg.kind != LinearSolverKind.CG:
-        raise NotImplementedError("only CG (the pressure-correction solver) is provided on the GPU")
-    return GpuCGSolver(cfg, **kw)
+    """make_linear_solver (src/solver/Solver.cpp:25-39): CG, GMRES(m) and
+    BiCGSTAB run on the device; TFQMR is not provided."""
+    if cfg.kind == LinearSolverKind.CG:
+        return GpuCGSolver(cfg, **kw)
+    return GpuLinearSolver(cfg, **kw)

@@ -1,7 +1,7 @@
 // GpuPcgSolver through the ILinearSolver interface: the 1-D Laplacian of
 // tests/unit/solver/test_ssor_preconditioner.cpp:65-88 (n = 50, b = 1,
-// tol 1e-10), with Jacobi, ILU0 and mixed precision; exits non-zero on a
-// failure.
+// tol 1e-10), with Jacobi, ILU0 and mixed precision, then GMRES and BiCGSTAB
+// on a convection-diffusion matrix; exits non-zero on a failure.
 #include "simall_gpu_solver.hpp"
 
 #include <cmath>
@@ -56,6 +56,51 @@ int main()
         std::printf("%s: it=%d |b-Ax|=%.3e last_residual=%.3e %s\n", c.name, it, std::sqrt(r2), s->last_residual(),
                     ok ? "ok" : "FAIL");
         failures += ok ? 0 : 1;
+    }
+    // GMRES(30) and BiCGSTAB (make_linear_solver's other kinds) on the
+    // non-symmetric upwind convection-diffusion matrix of
+    // tests/unit/solver/test_tfqmr_solver.cpp:43-62 (Pe = 5, n = 30, b = 1)
+    {
+        const int m = 30;
+        const double Pe = 5.0;
+        solver::CSRMatrix B;
+        B.rowPtr.push_back(0);
+        for (int i = 0; i < m; ++i) {
+            if (i > 0) {
+                B.colIdx.push_back(i - 1);
+                B.values.push_back(-1.0 - Pe);
+            }
+            B.colIdx.push_back(i);
+            B.values.push_back(2.0 + Pe);
+            if (i + 1 < m) {
+                B.colIdx.push_back(i + 1);
+                B.values.push_back(-1.0);
+            }
+            B.rowPtr.push_back(static_cast<int>(B.colIdx.size()));
+        }
+        util::aligned_vector<double> bb(m, 1.0), y;
+        const solver::LinearSolverKind kinds[] = {solver::LinearSolverKind::GMRES, solver::LinearSolverKind::BiCGSTAB};
+        for (auto kind : kinds) {
+            solver::LinearSolverConfig cfg;
+            cfg.kind = kind;
+            cfg.preconditioner = solver::PreconditionerKind::Jacobi;
+            cfg.maxIterations = 500;
+            cfg.tolerance = 1.0e-8;
+            std::unique_ptr<solver::ILinearSolver> s = std::make_unique<gpu_gb300::GpuLinearSolver>(cfg);
+            const int it = s->solve(B, bb, y);
+            double r2 = 0.0;
+            for (int i = 0; i < m; ++i) {
+                double s2 = 0.0;
+                for (int k = B.rowPtr[i]; k < B.rowPtr[i + 1]; ++k)
+                    s2 += B.values[k] * y[B.colIdx[k]];
+                r2 += (s2 - bb[i]) * (s2 - bb[i]);
+            }
+            const bool ok = it > 0 && it < 500 && std::sqrt(r2) < 1.0e-6 && s->last_residual() < 1.0e-8;
+            std::printf("%s: it=%d |b-Ax|=%.3e last_residual=%.3e %s\n",
+                        kind == solver::LinearSolverKind::GMRES ? "gmres" : "bicgstab", it, std::sqrt(r2),
+                        s->last_residual(), ok ? "ok" : "FAIL");
+            failures += ok ? 0 : 1;
+        }
     }
     return failures;
 }

@@ -35,4 +35,4 @@ def test_adapter_solves_through_the_library(sg, tmp_path):
                     "-o", exe, lib, f"-Wl,-rpath,{os.path.dirname(lib)}"], check=True)
     r = subprocess.run([exe], capture_output=True, text=True, timeout=120)
     assert r.returncode == 0, r.stdout + r.stderr
-    assert r.stdout.count(" ok") == 3
+    assert r.stdout.count(" ok") == 5
