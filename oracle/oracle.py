@@ -91,6 +91,9 @@ def lib():
         L.orc_bicgstab.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
         L.orc_gmres.restype = C.c_int
         L.orc_gmres.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, C.c_int, _P, _P]
+        L.orc_simple_iterate.restype = None
+        L.orc_simple_iterate.argtypes = [_I64, _I64] + [_P] * 16 + [C.c_int] + [_P] * 3 + [C.c_int, _P, _D, _P, _D] + \
+            [_P] * 9
         _lib = L
     return _lib
 
@@ -352,6 +355,66 @@ def gmres(rowPtr, colIdx, values, b, precond=1, tol=1e-8, max_it=1000, restart=3
     return x, it, last.value
 
 
+class SimpleOracle:
+    """SimpleAlgorithm::iterate / advance_time_step (SimpleAlgorithm.cpp:522-570)
+    restated: the state (U, p, phi, history) lives here, each outer iteration
+    runs orc_simple_iterate.  bcs as face_fluxes; pressure zones are those
+    with a PressureInlet / PressureOutlet spec; mom_cfg / p_cfg =
+    (kind, precond, tol, maxIt, restart)."""
+
+    def __init__(self, m: Mesh, bcs, rho=1.0, mu=1e-3, urfU=0.7, urfP=0.3, dt=0.0, bdf2=False, simplec=False,
+                 mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30)):
+        self.m = m
+        self.nZ, self.zt, self.zv = _zone_tables(bcs)
+        self.isP = np.zeros(self.nZ, np.uint8)
+        for b in bcs:
+            if int(b[1]) in (5, 7) and self.zt[int(b[0])] == int(b[1]):
+                self.isP[int(b[0])] = 1
+        self.rp, self.ci = build_sparsity(m)
+        self.opt = np.array([rho, mu, urfU, urfP, dt], np.float64)
+        self.bdf2, self.simplec = bool(bdf2), bool(simplec)
+        self.mom_cfg = mom_cfg
+        self.p_cfg = p_cfg
+        self.U = np.zeros((3, m.nC))
+        self.p = np.zeros(m.nC)
+        self.phi = np.zeros(m.nF)
+        self.aP = np.zeros(m.nC)
+        self.pPrime = np.zeros(m.nC)
+        self.Un = np.zeros((3, m.nC))
+        self.Unm1 = np.zeros((3, m.nC))
+        self.time_step = 0
+        self.iters = []  # every iterate()'s four solve counts
+
+    def iterate(self):
+        """One outer iteration; returns (res[4] = mom x, y, z, cont, iters[4])."""
+        m = self.m
+        res = np.zeros(4)
+        its = np.zeros(4, np.int32)
+        mc = np.array([self.mom_cfg[0], self.mom_cfg[1], self.mom_cfg[3], self.mom_cfg[4]], np.int32)
+        pc = np.array([self.p_cfg[0], self.p_cfg[1], self.p_cfg[3], self.p_cfg[4]], np.int32)
+        use_bdf2 = self.opt[4] > 0.0 and self.bdf2 and self.time_step >= 1
+        flags = (1 if use_bdf2 else 0) | (2 if self.simplec else 0)
+        lib().orc_simple_iterate(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                                 _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz),
+                                 _ptr(m.vol), _ptr(m.zone), _ptr(self.zt), _ptr(self.zv), _ptr(self.isP), self.nZ,
+                                 _ptr(self.rp), _ptr(self.ci), _ptr(self.opt), flags, _ptr(mc),
+                                 float(self.mom_cfg[2]), _ptr(pc), float(self.p_cfg[2]), _ptr(self.U), _ptr(self.p),
+                                 _ptr(self.Un), _ptr(self.Unm1), _ptr(self.phi), _ptr(self.aP), _ptr(self.pPrime),
+                                 _ptr(res), _ptr(its))
+        self.iters.append(its)
+        return res, its
+
+    def advance_time_step(self, n_inner=5):
+        if self.time_step >= 1:
+            self.Unm1[...] = self.Un
+        self.Un[...] = self.U
+        out = None
+        for _ in range(max(1, n_inner)):
+            out = self.iterate()
+        self.time_step += 1
+        return out
+
+
 def spmv(rowPtr, colIdx, values, x):
     n = len(rowPtr) - 1
     y = np.empty(n)
@@ -447,6 +510,9 @@ class RefLib:
         L.ref_assemble_momentum.argtypes = [_P, C.c_int, _P, _P, _P, _P, C.c_int, C.c_int, C.c_int] + [_P] * 8
         L.ref_krylov.restype = C.c_int
         L.ref_krylov.argtypes = [C.c_int, C.c_int, _D, C.c_int, C.c_int, C.c_int] + [_P] * 7
+        L.ref_simple_run.restype = C.c_int
+        L.ref_simple_run.argtypes = [_P, C.c_int, _P, _P, _P, _P, C.c_int, _P, _D, _P, _D, C.c_int, C.c_int] + \
+            [_P] * 5 + [C.c_int, _P, _P]
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -615,6 +681,33 @@ class RefLib:
                                _ptr(np.ascontiguousarray(values, np.float64)),
                                _ptr(np.ascontiguousarray(b, np.float64)), _ptr(x), C.byref(last), C.byref(secs))
         return x, it, last.value, secs.value
+
+    def simple_run(self, mesh_dict, bcs, U, p, n_outer, rho=1.0, mu=1e-3, urfU=0.7, urfP=0.3, dt=0.0, bdf2=False,
+                   simplec=False, mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30), n_inner=1):
+        """The reference's SimpleAlgorithm: n_outer iterate() calls (or
+        advance_time_step(n_inner) when dt > 0).  Returns dict U, p, phi, res
+        [n_outer, 4], iters [per iterate: mom x, y, z, p], seconds."""
+        nC, nF = mesh_dict["nC"], mesh_dict["nF"]
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        vec = np.array([list(b[2]) if len(b) > 2 else [0, 0, 0] for b in bcs] or [[0, 0, 0]], np.float64).ravel()
+        U = np.array(U, np.float64).reshape(3, nC).copy()
+        p = np.array(p, np.float64).copy()
+        phi = np.empty(nF)
+        res = np.empty((n_outer, 4))
+        cap = 4 * n_outer * max(1, n_inner) + 8
+        its = np.empty(cap, np.int32)
+        nits = C.c_int(0)
+        secs = C.c_double(0)
+        opt = np.array([rho, mu, urfU, urfP, dt], np.float64)
+        mc = np.array([mom_cfg[0], mom_cfg[1], mom_cfg[3], mom_cfg[4]], np.int32)
+        pc = np.array([p_cfg[0], p_cfg[1], p_cfg[3], p_cfg[4]], np.int32)
+        flags = (1 if bdf2 else 0) | (2 if simplec else 0)
+        self.L.ref_simple_run(mesh_dict["handle"], len(bcs), _ptr(zones), _ptr(types), _ptr(vec), _ptr(opt), flags,
+                              _ptr(mc), float(mom_cfg[2]), _ptr(pc), float(p_cfg[2]), int(n_outer), int(n_inner),
+                              _ptr(U), _ptr(p), _ptr(phi), _ptr(res), _ptr(its), cap, C.byref(nits), C.byref(secs))
+        return {"U": U, "p": p, "phi": phi, "res": res, "iters": its[:nits.value].reshape(-1, 4).copy(),
+                "seconds": secs.value}
 
     # -- solvers
     def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):

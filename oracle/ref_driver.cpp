@@ -509,6 +509,97 @@ void ref_spmv(int n, const int* rowPtr, const int* colIdx, const double* values,
     std::copy(yy.begin(), yy.end(), y);
 }
 
+// ------------------------------------------------------------------ SIMPLE runs
+// An ILinearSolver that records the iteration count of every solve.
+class CountingSolver final : public S::ILinearSolver
+{
+public:
+    explicit CountingSolver(std::unique_ptr<S::ILinearSolver> s) : inner_(std::move(s)) {}
+    int solve(const S::CSRMatrix& A, const Vec& b, Vec& x) override
+    {
+        const int it = inner_->solve(A, b, x);
+        iters.push_back(it);
+        return it;
+    }
+    double last_residual() const override { return inner_->last_residual(); }
+    std::vector<int> iters;
+
+private:
+    std::unique_ptr<S::ILinearSolver> inner_;
+};
+
+std::unique_ptr<S::ILinearSolver> make_kind(const int* cfg, double tol)
+{
+    S::LinearSolverConfig c;
+    c.kind = static_cast<S::LinearSolverKind>(cfg[0]);
+    c.preconditioner = static_cast<S::PreconditionerKind>(cfg[1]);
+    c.maxIterations = cfg[2];
+    c.restart = cfg[3];
+    c.tolerance = tol;
+    return cfg[0] == 1 ? S::make_bicgstab(c) : cfg[0] == 2 ? S::make_cg(c) : S::make_gmres(c);
+}
+
+// SimpleAlgorithm on the given mesh from U (in [3][nC]) and p: nOuter calls of
+// iterate() (dt == 0) or of advance_time_step(nInner) (dt > 0).  opt = {rho,
+// mu, urfU, urfP, dt}; flags bit 0 TemporalScheme::BDF2 (else ImplicitEuler),
+// bit 1 PvCouplingVariant::SIMPLEC.  momCfg / pCfg = {kind, precond, maxIt,
+// restart}.  Out: U, p, phi after the run; res[nOuter][4] the residuals each
+// call returned; iters[...] every linear solve's count in call order (size
+// returned in *nIters, at most maxIters written).
+int ref_simple_run(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, const double* bcVec,
+                   const double* opt, int flags, const int* momCfg, double momTol, const int* pCfg, double pTol,
+                   int nOuter, int nInner, double* U, double* p, double* phi, double* res, int* iters, int maxIters,
+                   int* nIters, double* seconds)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::FieldRegistry f;
+    auto& Uf = f.vector("U", nC);
+    Uf.x.assign(U, U + nC);
+    Uf.y.assign(U + nC, U + 2 * nC);
+    Uf.z.assign(U + 2 * nC, U + 3 * nC);
+    f.scalar("p", nC).assign(p, p + nC);
+    auto bcs = make_bcs_vec(nbc, bcZones, bcTypes, bcVec);
+    CountingSolver mom(make_kind(momCfg, momTol)), pres(make_kind(pCfg, pTol));
+    S::SimpleOptions o;
+    o.rho = opt[0];
+    o.mu = opt[1];
+    o.urfU = opt[2];
+    o.urfP = opt[3];
+    o.dt = opt[4];
+    o.timeScheme = (flags & 1) ? S::TemporalScheme::BDF2 : S::TemporalScheme::ImplicitEuler;
+    o.algorithm = (flags & 2) ? S::PvCouplingVariant::SIMPLEC : S::PvCouplingVariant::SIMPLE;
+    AssemblyProbe simple(m, f, bcs, mom, pres, o);
+    const auto t0 = std::chrono::steady_clock::now();
+    for (int i = 0; i < nOuter; ++i) {
+        const S::SimpleResiduals r = o.dt > 0.0 ? simple.advance_time_step(nInner) : simple.iterate();
+        res[4 * i] = r.mom[0];
+        res[4 * i + 1] = r.mom[1];
+        res[4 * i + 2] = r.mom[2];
+        res[4 * i + 3] = r.cont;
+    }
+    if (seconds)
+        *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    auto& Uo = *f.find_vector("U");
+    std::copy(Uo.x.begin(), Uo.x.end(), U);
+    std::copy(Uo.y.begin(), Uo.y.end(), U + nC);
+    std::copy(Uo.z.begin(), Uo.z.end(), U + 2 * nC);
+    const auto& pp = *f.find_scalar("p");
+    std::copy(pp.begin(), pp.end(), p);
+    std::copy(simple.phi().begin(), simple.phi().end(), phi);
+    // interleave: mom x, y, z then p for every iterate()
+    std::vector<int> all;
+    for (std::size_t k = 0; k < pres.iters.size(); ++k) {
+        for (int c = 0; c < 3; ++c)
+            all.push_back(3 * k + c < mom.iters.size() ? mom.iters[3 * k + c] : -1);
+        all.push_back(pres.iters[k]);
+    }
+    *nIters = static_cast<int>(all.size());
+    for (int i = 0; i < static_cast<int>(all.size()) && i < maxIters; ++i)
+        iters[i] = all[i];
+    return 0;
+}
+
 // ------------------------------------------------------------------ cavity SIMPLE
 // Runs nOuter SIMPLE iterations of the lid-driven cavity on an N x N x 1 grid
 // (extent 1 x 1 x 1/N; zones 1,2,3,5,6 NoSlipWall, zone 4 MovingWall (1,0,0))

@@ -1397,3 +1397,95 @@ int orc_gmres(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const dou
     prec_free(&M);
     return ret;
 }
+
+/* ------------------------------------------------------------------ one SIMPLE outer iteration */
+
+/* make_linear_solver (src/solver/Solver.cpp:25-39) for cfg = {kind, precond,
+ * maxIt, restart}: 0 GMRES, 1 BiCGSTAB, 2 CG. */
+static int orc_linear_solve(const int *cfg, double tol, int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
+                            const double *values, const double *b, double *x, double *last)
+{
+    switch (cfg[0]) {
+    case 1:
+        return orc_bicgstab(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], x, last);
+    case 2:
+        return orc_cg(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], x, last, NULL);
+    default:
+        return orc_gmres(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], cfg[3], x, last);
+    }
+}
+
+/*
+ * SimpleAlgorithm::iterate (src/solver/SimpleAlgorithm.cpp:522-547), no
+ * periodic faces, no halo exchange:
+ *   compute_face_fluxes; for k in x, y, z: assemble_momentum(k), solve it from
+ *   x = 0 into U_k, res.mom[k] = |A U_k - b|; compute_face_fluxes again;
+ *   assemble_pressure_correction (SIMPLEC: the denominator from the momentum
+ *   matrix); solve p' from 0; res.cont = |rhs|; correct_fields.
+ * opt = {rho, mu, urfU, urfP, dt}; flags bit 0 BDF2 (the transient term uses
+ * Un and Unm1), bit 1 SIMPLEC.  momCfg / pCfg = {kind, precond, maxIt,
+ * restart}.  U [3][nC], p [nC] in/out; phi [nF], aP [nC], pPrime [nC] out;
+ * res [4] = mom x, y, z and cont; iters [4] the four solves' counts.
+ * isPressure[z] marks zones with a PressureOutlet / PressureInlet spec.
+ */
+void orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                        const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
+                        const double *ccx, const double *ccy, const double *ccz, const double *vol,
+                        const uint32_t *zone, const int *zoneType, const double *zoneVec, const uint8_t *isPressure,
+                        int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int flags,
+                        const int *momCfg, double momTol, const int *pCfg, double pTol, double *U, double *p,
+                        const double *Un, const double *Unm1, double *phi, double *aP, double *pPrime, double *res,
+                        int *iters)
+{
+    const double rho = opt[0], mu = opt[1], urfU = opt[2], urfP = opt[3], dt = opt[4];
+    const int bdf2 = flags & 1, simplec = (flags >> 1) & 1;
+    const int64_t nnz = rowPtr[nC];
+    double *values = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
+    double *rhs = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    double *Ax = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    double *g = (double *)xmalloc((size_t)(3 * nC) * sizeof(double) + 8);
+    double *mInv = (double *)xmalloc((size_t)(6 * nC) * sizeof(double) + 8);
+    double *den = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    const double momOpt[4] = {rho, mu, urfU, dt};
+    orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC, phi);
+    orc_lsq_inverse(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv);
+    orc_lsq_gradient(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv, p, g, g + nC, g + 2 * nC);
+    for (int k = 0; k < 3; ++k) {
+        orc_assemble_momentum(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, zone, zoneType,
+                              zoneVec, nZones, rowPtr, colIdx, momOpt, bdf2, k, phi, g + k * nC, U + k * nC,
+                              Un ? Un + k * nC : NULL, Unm1 ? Unm1 + k * nC : NULL, values, rhs,
+                              k == 0 ? aP : NULL);
+        double last = 0.0;
+        iters[k] = orc_linear_solve(momCfg, momTol, nC, rowPtr, colIdx, values, rhs, U + k * nC, &last);
+        orc_spmv(nC, rowPtr, colIdx, values, U + k * nC, Ax);
+        double s = 0.0;
+        for (int64_t i = 0; i < nC; ++i) {
+            const double d = Ax[i] - rhs[i];
+            s += d * d;
+        }
+        res[k] = sqrt(s);
+    }
+    orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC, phi);
+    if (simplec)
+        orc_simplec_denominator(nC, rowPtr, colIdx, values, aP, den);
+    double *pvals = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
+    orc_assemble(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, zone, ccx, ccy, ccz, isPressure, nZones, rho,
+                 simplec ? den : aP, phi, rowPtr, colIdx, pvals, rhs);
+    {
+        double last = 0.0;
+        iters[3] = orc_linear_solve(pCfg, pTol, nC, rowPtr, colIdx, pvals, rhs, pPrime, &last);
+        double cs = 0.0;
+        for (int64_t i = 0; i < nC; ++i)
+            cs += rhs[i] * rhs[i];
+        res[3] = sqrt(cs);
+    }
+    orc_correct_fields(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, rho, urfP, aP, pPrime, p,
+                       U, U + nC, U + 2 * nC, phi);
+    free(values);
+    free(rhs);
+    free(Ax);
+    free(g);
+    free(mInv);
+    free(den);
+    free(pvals);
+}

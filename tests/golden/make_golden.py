@@ -7,7 +7,8 @@ sources).  Every array stored here is an output of the reference's functions
 renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction / assemble_momentum, CGSolver::solve with
 Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
-preconditioners' apply, the SIMPLE cavity loop, solve_discrete_adjoint);
+preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
+advance_time_step runs, solve_discrete_adjoint);
 inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
 
@@ -168,6 +169,40 @@ def momentum_case(name):
                         x_bicgstab=xb, it_bicgstab=np.array(itb), last_bicgstab=np.array(lb))
 
 
+CAVITY_BCS = [(z, 1) for z in (1, 2, 3, 5, 6)] + [(4, 2, (1.0, 0.0, 0.0))]
+CHANNEL_BCS = [(1, 4, (1.0, 0.1, 0.0)), (2, 7), (3, 1), (4, 1), (5, 9), (6, 0)]
+# name: dims, node-shift amplitude (seed 31), RCM, boundary specs, SimpleOptions and solver configs, outer calls, inner
+SIMPLE_RUNS = {
+    "simple_cavity_64_gmres_ilu.npz": ((64, 64, 1), 0.0, False, CAVITY_BCS,
+                                       dict(mu=0.01, mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30)),
+                                       20, 1),
+    "simple_channel_8x6x5_simplec.npz": ((8, 6, 5), 0.2, True, CHANNEL_BCS,
+                                         dict(mu=0.1, simplec=True, urfP=0.9, mom_cfg=(1, 0, 1e-8, 200, 30),
+                                              p_cfg=(2, 1, 1e-9, 1000, 30)), 5, 1),
+    "simple_cavity_12_bdf2.npz": ((12, 12, 1), 0.0, False, CAVITY_BCS,
+                                  dict(mu=0.01, dt=0.01, bdf2=True, mom_cfg=(0, 0, 1e-8, 200, 5),
+                                       p_cfg=(2, 0, 1e-9, 1000, 30)), 3, 2),
+}
+
+
+def simple_case(name):
+    """The reference's SimpleAlgorithm from rest: U, p, phi, the residuals of
+    every outer call and every linear solve's iteration count."""
+    import json
+
+    dims, amp, renumber, bcs, kw, n_outer, n_inner = SIMPLE_RUNS[name]
+    shift = W.interior_node_shift(*dims, amp=amp, seed=31) if amp else None
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=renumber)
+    nC = rm["nC"]
+    out = R.simple_run(rm, bcs, np.zeros((3, nC)), np.zeros(nC), n_outer, n_inner=n_inner, **kw)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), amp=np.array(amp),
+                        renumber=np.array(renumber), bc_zone=np.array([b[0] for b in bcs]),
+                        bc_type=np.array([b[1] for b in bcs]),
+                        bc_vec=np.array([list(b[2]) if len(b) > 2 else [0.0, 0.0, 0.0] for b in bcs]),
+                        options=np.array(json.dumps(kw)), n_outer=np.array(n_outer), n_inner=np.array(n_inner),
+                        U=out["U"], p=out["p"], phi=out["phi"], res=out["res"], iters=out["iters"])
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -202,6 +237,8 @@ def main():
     simplec_case("simplec_6x5x4_outlet.npz")
     field_loops_case("field_loops_7x6x5_rcm.npz")
     momentum_case("momentum_7x6x5_rcm_bdf2.npz")
+    for name in SIMPLE_RUNS:
+        simple_case(name)
     print("fixtures written to", HERE)
 
 

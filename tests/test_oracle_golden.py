@@ -250,3 +250,39 @@ def test_rcm_never_increases_bandwidth(oracle, dims):
     _, (before, after, permuted) = oracle.rcm(m)
     assert permuted == m.nC and after <= before
     assert np.all(m.owner < m.nC) and np.all(m.neighbor < m.nC)
+
+
+def simple_fixture(oracle, name):
+    """(fixture, oracle mesh, boundary specs, SimpleOptions/solver kwargs) of a
+    SimpleAlgorithm run recorded from the reference."""
+    import json
+
+    from simall_gb300 import workloads as W
+
+    g = load(name)
+    dims = tuple(int(v) for v in g["dims"])
+    amp = float(g["amp"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=amp, seed=31) if amp else None)
+    if bool(g["renumber"]):
+        oracle.rcm(m)
+    bcs = [(int(z), int(t), tuple(v)) for z, t, v in zip(g["bc_zone"], g["bc_type"], g["bc_vec"])]
+    kw = json.loads(str(g["options"]))
+    for k in ("mom_cfg", "p_cfg"):
+        kw[k] = tuple(kw[k])
+    return g, m, bcs, kw
+
+
+@pytest.mark.parametrize("name", ["simple_cavity_64_gmres_ilu.npz", "simple_channel_8x6x5_simplec.npz",
+                                  "simple_cavity_12_bdf2.npz"])
+def test_simple_runs_fixture(oracle, name):
+    """SimpleAlgorithm::iterate / advance_time_step from rest: U, p, phi,
+    residuals and solve counts bit-identical to the reference's run."""
+    g, m, bcs, kw = simple_fixture(oracle, name)
+    s = oracle.SimpleOracle(m, bcs, **kw)
+    res = []
+    for _ in range(int(g["n_outer"])):
+        out = s.advance_time_step(int(g["n_inner"])) if kw.get("dt", 0.0) > 0 else s.iterate()
+        res.append(out[0])
+    assert np.array_equal(np.array(s.iters), g["iters"])
+    assert bits_equal(np.array(res), g["res"])
+    assert bits_equal(s.U, g["U"]) and bits_equal(s.p, g["p"]) and bits_equal(s.phi, g["phi"])

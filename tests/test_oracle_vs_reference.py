@@ -205,3 +205,42 @@ def test_nonsymmetric_krylov(oracle, ref, kind, pc):
                           else oracle.bicgstab(rp, ci, v, b, pc, tol, mx))
         assert (it, last) == (oit, olast)
         assert bits_equal(x, ox)
+
+
+CAVITY_BCS = [(z, 1) for z in (1, 2, 3, 5, 6)] + [(4, 2, (1.0, 0.0, 0.0))]
+CHANNEL_BCS = [(1, 4, (1.0, 0.1, 0.0)), (2, 7), (3, 1), (4, 1), (5, 9), (6, 0)]
+
+SIMPLE_CASES = {
+    # name: (dims, amp, renumber, bcs, kwargs, n_outer, n_inner)
+    "cavity_gmres_ilu": ((16, 16, 1), 0.0, False, CAVITY_BCS,
+                         dict(mu=0.01, mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30)), 6, 1),
+    "channel_simplec_bicgstab": ((8, 6, 5), 0.2, True, CHANNEL_BCS,
+                                 dict(mu=0.1, simplec=True, urfP=0.9, mom_cfg=(1, 0, 1e-8, 200, 30),
+                                      p_cfg=(2, 1, 1e-9, 1000, 30)), 5, 1),
+    "cavity_bdf2_gmres_jacobi": ((12, 12, 1), 0.0, False, CAVITY_BCS,
+                                 dict(mu=0.01, dt=0.01, bdf2=True, mom_cfg=(0, 0, 1e-8, 200, 5),
+                                      p_cfg=(2, 0, 1e-9, 1000, 30)), 3, 2),
+}
+
+
+@pytest.mark.parametrize("case", sorted(SIMPLE_CASES))
+def test_simple_outer_iterations(oracle, ref, case):
+    """SimpleAlgorithm::iterate / advance_time_step: the oracle's outer
+    iterations reproduce the reference's U, p, phi, residuals and every linear
+    solve's iteration count, bit for bit."""
+    dims, amp, renumber, bcs, kw, n_outer, n_inner = SIMPLE_CASES[case]
+    sh = _shift(dims, 31, amp)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    want = ref.simple_run(r, bcs, np.zeros((3, m.nC)), np.zeros(m.nC), n_outer, n_inner=n_inner, **kw)
+    s = oracle.SimpleOracle(m, bcs, **kw)
+    res, its = [], []
+    for _ in range(n_outer):
+        out = s.advance_time_step(n_inner) if kw.get("dt", 0.0) > 0 else s.iterate()
+        res.append(out[0])
+    assert np.array_equal(np.array(s.iters), want["iters"])
+    assert bits_equal(np.array(res), want["res"])
+    assert bits_equal(s.U, want["U"]) and bits_equal(s.p, want["p"]) and bits_equal(s.phi, want["phi"])
+    ref.free_mesh(r)
