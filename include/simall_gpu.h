@@ -306,6 +306,40 @@ int simall_momentum_device_arrays(const simall_pressure_system *ps, const double
                                   const double **aP);
 int simall_momentum_download(const simall_pressure_system *ps, double *values, double *rhs, double *aP);
 
+/* ------------------------------------------------------------------ SIMPLE outer iteration */
+/* Replaces SimpleAlgorithm::iterate / advance_time_step
+ * (src/solver/SimpleAlgorithm.cpp:522-570) with U, p, phi, aP and p' in device
+ * memory: fluxes -> momentum assembly and three momentum solves -> fluxes ->
+ * pressure-correction assembly (SIMPLE or SIMPLEC) -> pressure solve ->
+ * correct_fields.  The pressure system (with its field loops set up) holds
+ * the mesh; the two solvers are any simall_solver of this context (the
+ * reference takes the momentum and pressure ILinearSolver the same way). */
+typedef struct simall_simple_options {
+    double urfU, urfP, rho, mu; /* SimpleOptions (src/solver/SimpleAlgorithm.hpp:43-57) */
+    double dt;                  /* > 0: transient (advance_time_step) */
+    int bdf2;                   /* TemporalScheme::BDF2 (else implicit Euler) */
+    int simplec;                /* PvCouplingVariant::SIMPLEC (else SIMPLE) */
+} simall_simple_options;
+typedef struct simall_simple_residuals {
+    double mom[3];     /* |A U_k - b| of each momentum solve (SimpleResiduals::mom) */
+    double cont;       /* |rhs| of the pressure-correction system (SimpleResiduals::cont) */
+    int iterations[4]; /* the momentum x, y, z and pressure solves' counts */
+} simall_simple_residuals;
+typedef struct simall_simple simall_simple;
+void simall_simple_options_default(simall_simple_options *o);
+/* U and p start at zero. */
+int simall_simple_create(simall_pressure_system *ps, simall_solver *momentum, simall_solver *pressure,
+                         const simall_simple_options *opt, simall_simple **out);
+int simall_simple_destroy(simall_simple *s);
+/* U [3][n_cells], p [n_cells]; either may be NULL. */
+int simall_simple_set_fields(simall_simple *s, const double *U, const double *p, int mem);
+int simall_simple_get_fields(simall_simple *s, double *U, double *p, double *phi, int mem);
+/* The device arrays the iteration updates in place (valid until destroy). */
+int simall_simple_device_fields(simall_simple *s, double **U, double **p, double **phi);
+int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res);
+/* U^{n-1} <- U^n (from the second step on), U^n <- U, then n_inner iterations. */
+int simall_simple_advance_time_step(simall_simple *s, int n_inner, simall_simple_residuals *res);
+
 /* ------------------------------------------------------------------ differentiation */
 /* Face-conductance Poisson operator (an extension: the reference expresses
  * neither per-face conductances nor non-zero Dirichlet values).  With

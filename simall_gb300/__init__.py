@@ -9,6 +9,7 @@ from . import build
 from .batch import BatchedSolver
 from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
+from .simple import GpuSimpleAlgorithm, SimpleOptions, SimpleResiduals
 from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
                      Precision, PreconditionerKind, default_context, make_bicgstab, make_cg, make_gmres,
                      make_linear_solver)
@@ -16,4 +17,4 @@ from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSol
 __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
-           "make_gmres", "make_bicgstab"]
+           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals"]

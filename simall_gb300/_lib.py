@@ -48,6 +48,14 @@ class MomentumOptions(C.Structure):
     _fields_ = [("rho", _D), ("mu", _D), ("urfU", _D), ("dt", _D), ("bdf2", _I), ("reserved", _I)]
 
 
+class SimpleOptions(C.Structure):
+    _fields_ = [("urfU", _D), ("urfP", _D), ("rho", _D), ("mu", _D), ("dt", _D), ("bdf2", _I), ("simplec", _I)]
+
+
+class SimpleResiduals(C.Structure):
+    _fields_ = [("mom", _D * 3), ("cont", _D), ("iterations", _I * 4)]
+
+
 class MeshView(C.Structure):
     _fields_ = [("n_cells", _I64), ("n_faces", _I64), ("owner", _P), ("neighbor", _P), ("area_x", _P),
                 ("area_y", _P), ("area_z", _P), ("centroid_x", _P), ("centroid_y", _P), ("centroid_z", _P),
@@ -104,6 +112,14 @@ SIGNATURES = {
     "simall_assemble_momentum": (_I, [_P, C.POINTER(MomentumOptions), _P, _P, _P, _P, _P, _I]),
     "simall_momentum_device_arrays": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "simall_momentum_download": (_I, [_P, _P, _P, _P]),
+    "simall_simple_options_default": (None, [C.POINTER(SimpleOptions)]),
+    "simall_simple_create": (_I, [_P, _P, _P, C.POINTER(SimpleOptions), C.POINTER(_P)]),
+    "simall_simple_destroy": (_I, [_P]),
+    "simall_simple_set_fields": (_I, [_P, _P, _P, _I]),
+    "simall_simple_get_fields": (_I, [_P, _P, _P, _P, _I]),
+    "simall_simple_device_fields": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "simall_simple_iterate": (_I, [_P, C.POINTER(SimpleResiduals)]),
+    "simall_simple_advance_time_step": (_I, [_P, _I, C.POINTER(SimpleResiduals)]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),
