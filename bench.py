@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--fd-faces", type=int, default=64, help="faces checked by central differences")
     ap.add_argument("--poisson-n", type=int, default=128, help="box side of the Jacobi-vs-ILU0 leg (0 disables it)")
     ap.add_argument("--no-cavity", action="store_true", help="skip the 128x128 cavity pressure-step leg")
+    ap.add_argument("--simple-iterations", type=int, default=20,
+                    help="outer iterations of the device SIMPLE leg (0 disables it)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the error check against a 1e-12 FP64 solve")
     ap.add_argument("--check-interval", type=int, default=0,
@@ -511,6 +513,85 @@ def run_pressure_step(a, ctx, sg, with_cpu):
     return res
 
 
+CAVITY_SIMPLE_BCS = [(z, 1) for z in (1, 2, 3, 5, 6)] + [(4, 2, (1.0, 0.0, 0.0))]
+
+
+def run_simple(a, ctx, sg, with_cpu):
+    """The whole SIMPLE outer iteration on the device (fluxes, momentum
+    assembly and three momentum solves, fluxes, pressure-correction assembly
+    and solve, correction; U, p, phi resident) on the 128x128 lid-driven
+    cavity (Re 100, urfU 0.7, urfP 0.3) from rest, with the reference's
+    solver settings (GMRES(30)+ILU(0) momentum to 1e-6, FP64 Jacobi-CG
+    pressure to 1e-8) and with GMRES(30)+Jacobi momentum and mixed-precision
+    pressure; seconds per outer iteration over the first `simple_iterations`
+    iterations, against the oracle's restatement of SimpleAlgorithm::iterate
+    on one host core."""
+    from oracle import oracle as O  # the parity check and the CPU baseline only
+
+    N = 128
+    n_it = a.simple_iterations
+    m = sg.cartesian(N, N, 1, 1.0, 1.0, 1.0 / N)
+    configs = {
+        "reference_settings": ((0, 1, 1e-6, 200, 30), (2, 0, 1e-8, 1000, 30), sg.Precision.FP64),
+        "gb300_settings": ((0, 0, 1e-6, 200, 30), (2, 0, 1e-8, 1000, 30), sg.Precision.MIXED),
+    }
+    res = {"workload": f"cavity {N}x{N} SIMPLE outer iterations from rest (Re 100), every field in device memory",
+           "cells": int(m.n_cells), "iterations_timed": n_it}
+
+    def make(cfg):
+        mc, pc, prec = cfg
+        mom = sg.make_linear_solver(sg.LinearSolverConfig(sg.LinearSolverKind(mc[0]), sg.PreconditionerKind(mc[1]),
+                                                          mc[2], mc[3], mc[4]), ctx=ctx)
+        pres = sg.GpuCGSolver(sg.LinearSolverConfig(sg.LinearSolverKind.CG, sg.PreconditionerKind(pc[1]), pc[2],
+                                                    pc[3]), precision=prec, ctx=ctx)
+        alg = sg.GpuSimpleAlgorithm(m, CAVITY_SIMPLE_BCS, mom, pres, sg.SimpleOptions(mu=0.01), ctx=ctx)
+        return alg, mom, pres
+
+    for name, cfg in configs.items():
+        alg, mom, pres = make(cfg)
+        for _ in range(2):  # warm: preconditioner analysis, graph capture
+            alg.iterate()
+        alg.close()
+        alg = sg.GpuSimpleAlgorithm(m, CAVITY_SIMPLE_BCS, mom, pres, sg.SimpleOptions(mu=0.01), ctx=ctx)
+        ctx.synchronize()
+        its = np.zeros(4, np.int64)
+        t0 = time.perf_counter()
+        for _ in range(n_it):
+            r = alg.iterate()
+            its += np.array(r.iterations)
+        ctx.synchronize()
+        sec = (time.perf_counter() - t0) / n_it
+        res[name] = {"value": round(sec, 6), "unit": "s per outer iteration",
+                     "momentum": f"GMRES({cfg[0][4]})+{'ILU(0)' if cfg[0][1] == 1 else 'Jacobi'} to {cfg[0][2]:g}",
+                     "pressure": f"{'mixed' if cfg[2] == sg.Precision.MIXED else 'FP64'} Jacobi-CG to {cfg[1][2]:g}",
+                     "solve_iterations_per_outer": [round(float(v) / n_it, 1) for v in its]}
+        alg.close()
+        mom.close()
+        pres.close()
+    # parity: five iterations from rest against the oracle's (reference settings)
+    alg, mom, pres = make(configs["reference_settings"])
+    om = O.cartesian_mesh(N, N, 1, 1.0, 1.0, 1.0 / N)
+    so = O.SimpleOracle(om, CAVITY_SIMPLE_BCS, mu=0.01, mom_cfg=configs["reference_settings"][0],
+                        p_cfg=configs["reference_settings"][1])
+    t = time.perf_counter()
+    for _ in range(5):
+        alg.iterate()
+    for _ in range(5):
+        so.iterate()
+    cpu_s = (time.perf_counter() - t) / 5
+    U, p, _ = alg.fields()
+    res["parity_5_iterations"] = {"rel_U": float(np.linalg.norm(U - so.U) / np.linalg.norm(so.U)),
+                                  "rel_p": float(np.linalg.norm(p - so.p) / np.linalg.norm(so.p))}
+    if with_cpu:
+        res["cpu_baseline"] = {"value": round(cpu_s, 4), "unit": "s per outer iteration", "cores": 1, "kind": "port",
+                               "sample": "the oracle's SimpleAlgorithm::iterate, reference settings, the first 5 "
+                                         "outer iterations from rest on 1 host core"}
+    alg.close()
+    mom.close()
+    pres.close()
+    return res
+
+
 def run_ours(a, rank, world, local):
     import torch
 
@@ -661,6 +742,8 @@ def run_ours(a, rank, world, local):
         out["pressure_step"] = run_pressure_step(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if not a.no_cavity:
         out["cavity"] = run_cavity(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
+    if a.simple_iterations > 0:
+        out["simple"] = run_simple(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
         out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,

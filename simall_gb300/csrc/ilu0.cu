@@ -10,8 +10,10 @@
 // in column order, so the factor and both sweeps are bit-identical to the
 // reference.  Multicolouring would be faster but changes the factor.
 //
-// The factorisation (once per solve) launches one kernel per level.  The
-// sweeps (twice per PCG iteration) run as one kernel each without levels
+// Systems of up to kIluSmallRows rows factor and sweep in one CTA (below).
+// Larger ones: the factorisation (once per solve) launches one kernel per
+// level, and the sweeps (twice per PCG iteration) run as one kernel each
+// without levels
 // between launches: warps take 32 consecutive rows of the level order from an
 // atomic ticket, and a row waits only for the rows it reads, each of which
 // publishes its value and then its "done" mark (release) and is read after the
@@ -284,6 +286,100 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
         atomicOr(ctl + 2, 1u);
 }
 
+// ---------------------------------------------------------------- one CTA
+// For small systems the dependency chain, not the bandwidth, sets the time:
+// one kernel launch per level or a mark per row cost microseconds per level,
+// while one CTA walking the levels with a block barrier between them pays a
+// barrier and an L2 round trip.  The sweep vector lives in shared memory (the
+// backward sweep overwrites y with z in place: row i reads y_i and the final
+// z_j of rows in earlier backward levels only).  Same per-row operations, so
+// the results are bit-identical to the reference's.
+constexpr int kIluSmallThreads = 1024;
+constexpr int kIluSmallRows = 24576;  // 192 KB of shared memory
+
+__global__ void __launch_bounds__(kIluSmallThreads) k_ilu_factor_small(int nlev, const int32_t *__restrict__ lvl,
+                                                                       const int32_t *__restrict__ rows,
+                                                                       const int32_t *__restrict__ rowPtr,
+                                                                       const int32_t *__restrict__ colIdx,
+                                                                       const int32_t *__restrict__ diagPtr, double *lu)
+{
+    for (int l = 1; l < nlev; ++l) {  // level 0 rows have no lower entries
+        const int a = lvl[l], b = lvl[l + 1];
+        for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
+            const int i = rows[t];
+            const int end = rowPtr[i + 1];
+            for (int kp = rowPtr[i]; kp < end; ++kp) {
+                const int k = colIdx[kp];
+                if (k >= i)
+                    break;
+                const int dk = diagPtr[k];
+                if (dk < 0)
+                    continue;
+                const double piv = lu[dk];
+                if (piv == 0.0)
+                    continue;
+                const double m = __ddiv_rn(lu[kp], piv);
+                lu[kp] = m;
+                const int kend = rowPtr[k + 1];
+                for (int jp = dk + 1; jp < kend; ++jp) {
+                    const int j = colIdx[jp];
+                    for (int qp = kp + 1; qp < end; ++qp) {
+                        const int c = colIdx[qp];
+                        if (c == j) {
+                            lu[qp] = __dsub_rn(lu[qp], __dmul_rn(m, lu[jp]));
+                            break;
+                        }
+                        if (c > j)
+                            break;
+                    }
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(kIluSmallThreads) k_ilu_sweeps_small(
+    int n, int nlevF, const int32_t *__restrict__ lvlF, const int32_t *__restrict__ rowsF, int nlevB,
+    const int32_t *__restrict__ lvlB, const int32_t *__restrict__ rowsB, const int32_t *__restrict__ rowPtr,
+    const int32_t *__restrict__ colIdx, const int32_t *__restrict__ diagPtr, const double *__restrict__ lu,
+    const double *__restrict__ r, double *__restrict__ z)
+{
+    extern __shared__ double ys[];
+    for (int l = 0; l < nlevF; ++l) {
+        const int a = __ldg(lvlF + l), b = __ldg(lvlF + l + 1);
+        for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
+            const int i = __ldg(rowsF + t);
+            double s = __ldg(r + i);
+            const int end = __ldg(rowPtr + i + 1);
+            for (int kp = __ldg(rowPtr + i); kp < end; ++kp) {
+                const int j = __ldg(colIdx + kp);
+                if (j >= i)
+                    break;
+                s = __dsub_rn(s, __dmul_rn(__ldg(lu + kp), ys[j]));
+            }
+            ys[i] = s;
+        }
+        __syncthreads();
+    }
+    for (int l = 0; l < nlevB; ++l) {
+        const int a = __ldg(lvlB + l), b = __ldg(lvlB + l + 1);
+        for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
+            const int i = __ldg(rowsB + t);
+            double s = ys[i];
+            const int kd = __ldg(diagPtr + i);
+            const int end = __ldg(rowPtr + i + 1);
+            for (int kp = kd + 1; kp < end; ++kp)
+                s = __dsub_rn(s, __dmul_rn(__ldg(lu + kp), ys[__ldg(colIdx + kp)]));
+            const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
+            ys[i] = (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s;
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        z[i] = ys[i];
+}
+
 // One warp waits for a mark that nothing sets: the bounded wait of the sweeps
 // running out, observed from the host.
 __global__ void k_wait_probe(const unsigned *flag, unsigned *out)
@@ -380,6 +476,16 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
                                          ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->bwdRows.p, br.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice,
                                          ctx->stream));
+    SIMALL_CUDA_TRY(ctx, d->fwdLvl.alloc(d->fwdLevelPtr.size()));
+    SIMALL_CUDA_TRY(ctx, d->bwdLvl.alloc(d->bwdLevelPtr.size()));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->fwdLvl.p, d->fwdLevelPtr.data(), d->fwdLevelPtr.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->bwdLvl.p, d->bwdLevelPtr.data(), d->bwdLevelPtr.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+    d->small = n <= kIluSmallRows;
+    if (d->small)
+        SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                  static_cast<int>(n * sizeof(double))));
     // the copies above read host vectors that die at return
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     d->analysed = true;
@@ -389,6 +495,12 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
 int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx)
 {
     const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
+    if (d->small) {
+        k_ilu_factor_small<<<1, kIluSmallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
+                                                                   d->diagPtr.p, d->lu.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    }
     for (int l = 1; l < nlev; ++l) {  // level 0 rows have no lower entries
         const int a = d->fwdLevelPtr[l], cnt = d->fwdLevelPtr[l + 1] - a;
         k_ilu_factor_level<<<(cnt + kBlock - 1) / kBlock, kBlock, 0, ctx->stream>>>(d->fwdRows.p + a, cnt, rowPtr,
@@ -402,6 +514,14 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
            const double *r, double *z)
 {
     const int n = static_cast<int>(d->h_diagPtr.size());
+    if (d->small) {
+        k_ilu_sweeps_small<<<1, kIluSmallThreads, n * sizeof(double), ctx->stream>>>(
+            n, static_cast<int>(d->fwdLevelPtr.size()) - 1, d->fwdLvl.p, d->fwdRows.p,
+            static_cast<int>(d->bwdLevelPtr.size()) - 1, d->bwdLvl.p, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu,
+            r, z);
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    }
     const int grid = ctx->num_sms * 4;  // 32 warps per SM take rows; more only add waiting warps
     k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
@@ -461,6 +581,8 @@ int ilu_check(simall_context *ctx, IluData *d)
 }
 
 int ilu_check(simall_solver *s) { return s->ilu ? ilu_check(s->ctx, s->ilu) : SIMALL_OK; }
+
+int ilu_apply_launches(const simall_solver *s) { return (s->ilu && s->ilu->small) ? 1 : 4; }
 
 void ilu_free(simall_solver *s)
 {

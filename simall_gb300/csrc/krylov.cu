@@ -747,7 +747,7 @@ int bicgstab_solve(simall_solver *s)
             d->chunks.push_back(c);
             g = &d->chunks.back();
         } else {
-            per = static_cast<int64_t>(len) * (use_ilu(s) ? 13 : 5);
+            per = static_cast<int64_t>(len) * (use_ilu(s) ? 5 + 2 * ilu_apply_launches(s) : 5);
         }
         int e = replay(ctx, g->exec, per);
         if (e)

@@ -539,7 +539,7 @@ int enqueue_iteration(simall_solver *s)
 int64_t kernels_per_iteration(const simall_solver *s)
 {
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 && s->ilu)
-        return 4 + 4;  // SpMV, x/r update, r.z/beta, direction + two sweeps with their resets
+        return 4 + ilu_apply_launches(s);  // SpMV, x/r update, r.z/beta, direction + the sweeps
     return 3;
 }
 

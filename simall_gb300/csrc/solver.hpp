@@ -15,9 +15,11 @@ struct IluData {
     DevBuf<unsigned> done;      // sweeps: done[i] == sweep number once row i is final
     DevBuf<unsigned> sweepCtl;  // sweeps: [0] work ticket, [1] sweep number, [2] wait-timeout flag
     std::vector<int32_t> fwdLevelPtr, bwdLevelPtr;  // level boundaries into fwdRows / bwdRows (host)
+    DevBuf<int32_t> fwdLvl, bwdLvl;                 // the same on the device (single-CTA path)
     std::vector<int32_t> h_diagPtr;
     int maxLevelRows = 0;
     bool analysed = false;
+    bool small = false;  // factor and sweeps in one CTA, the sweep vector in shared memory
 };
 
 struct MixedData;  // mixed.cu
@@ -67,6 +69,7 @@ namespace simall {
 int ilu_setup(simall_solver *s);
 int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);
+int ilu_apply_launches(const simall_solver *s);  // kernels one ilu_apply enqueues
 void ilu_free(simall_solver *s);
 
 int mixed_setup(simall_solver *s);
