@@ -339,45 +339,154 @@ __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_factor_small(int nlev,
     }
 }
 
-__global__ void __launch_bounds__(kIluSmallThreads) k_ilu_sweeps_small(
-    int n, int nlevF, const int32_t *__restrict__ lvlF, const int32_t *__restrict__ rowsF, int nlevB,
-    const int32_t *__restrict__ lvlB, const int32_t *__restrict__ rowsB, const int32_t *__restrict__ rowPtr,
-    const int32_t *__restrict__ colIdx, const int32_t *__restrict__ diagPtr, const double *__restrict__ lu,
-    const double *__restrict__ r, double *__restrict__ z)
+// Asynchronous global -> shared copies (LDGSTS): a thread issues them and goes
+// on; cp.async.wait_group retires its own groups in order.
+__device__ __forceinline__ void cp_async4(void *smem, const void *gmem)
 {
-    extern __shared__ double ys[];
-    for (int l = 0; l < nlevF; ++l) {
-        const int a = __ldg(lvlF + l), b = __ldg(lvlF + l + 1);
-        for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
-            const int i = __ldg(rowsF + t);
-            double s = __ldg(r + i);
-            const int end = __ldg(rowPtr + i + 1);
-            for (int kp = __ldg(rowPtr + i); kp < end; ++kp) {
-                const int j = __ldg(colIdx + kp);
-                if (j >= i)
-                    break;
-                s = __dsub_rn(s, __dmul_rn(__ldg(lu + kp), ys[j]));
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
+{
+    const unsigned sa = static_cast<unsigned>(__cvta_generic_to_shared(smem));
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(sa), "l"(gmem) : "memory");
+}
+
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+
+constexpr int kIluStages = 6;         // levels in flight: the copy of level l + 5 overlaps the work of level l
+constexpr int kIluSmallMaxLevels = 4096;
+constexpr int kIluSmallMaxK = 8;      // entries per row of one triangle
+constexpr int kIluSmallSmem = 220 * 1024;
+
+__device__ __forceinline__ void cp_async_wait_pipeline()
+{
+    asm volatile("cp.async.wait_group %0;" ::"n"(kIluStages - 2) : "memory");
+}
+
+// One triangle of the packed level-ordered sweep: rows (row | count << 24),
+// their entries' columns and values at a stride of k per row, and (backward)
+// the diagonal.
+struct PackedSweep {
+    const int32_t *row, *col;
+    const double *val, *diag;
+    int nlev, k;
+};
+
+// Shared-memory stage of one level: vals [R k], diag [R], cols [R k], rows [R].
+struct StageView {
+    double *val, *diag;
+    int32_t *col, *row;
+};
+
+__device__ __forceinline__ StageView stage_view(unsigned char *base, int stageBytes, int s, int R, int k)
+{
+    unsigned char *b = base + static_cast<size_t>(s) * stageBytes;
+    StageView v;
+    v.val = reinterpret_cast<double *>(b);
+    v.diag = v.val + static_cast<size_t>(R) * k;
+    v.col = reinterpret_cast<int32_t *>(v.diag + R);
+    v.row = v.col + static_cast<size_t>(R) * k;
+    return v;
+}
+
+__device__ __forceinline__ void issue_level(const PackedSweep &p, const int *lvl, int l, StageView st)
+{
+    if (l < p.nlev) {
+        const int a = lvl[l], cnt = lvl[l + 1] - a, k = p.k;
+        for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
+            cp_async4(st.row + q, p.row + a + q);
+            if (p.diag)
+                cp_async8(st.diag + q, p.diag + a + q);
+        }
+        for (int q = threadIdx.x; q < cnt * k; q += blockDim.x) {
+            cp_async4(st.col + q, p.col + static_cast<size_t>(a) * k + q);
+            cp_async8(st.val + q, p.val + static_cast<size_t>(a) * k + q);
+        }
+    }
+    cp_async_commit();  // one group per level, empty past the end, so the wait count stays uniform
+}
+
+// One triangular sweep in place on ys: forward ys_i -= sum l_ij ys_j, backward
+// the same with u_ij and a final division by the diagonal (when non-zero).
+template <bool BACKWARD>
+__device__ __forceinline__ void sweep_levels(const PackedSweep &p, const int *lvl, double *ys, unsigned char *stages,
+                                             int stageBytes, int R)
+{
+    for (int s = 0; s < kIluStages - 1; ++s)
+        issue_level(p, lvl, s, stage_view(stages, stageBytes, s, R, p.k));
+    for (int l = 0; l < p.nlev; ++l) {
+        cp_async_wait_pipeline();  // this thread's copies of level l have landed
+        __syncthreads();           // everyone's copies of level l, and level l - 1's results, are visible
+        issue_level(p, lvl, l + kIluStages - 1, stage_view(stages, stageBytes, (l + kIluStages - 1) % kIluStages, R, p.k));
+        const StageView st = stage_view(stages, stageBytes, l % kIluStages, R, p.k);
+        const int cnt = lvl[l + 1] - lvl[l], k = p.k;
+        for (int t = threadIdx.x; t < cnt; t += blockDim.x) {
+            const int packed = st.row[t];
+            const int i = packed & 0xffffff, c = packed >> 24;
+            double s = ys[i];
+            for (int q = 0; q < c; ++q)
+                s = __dsub_rn(s, __dmul_rn(st.val[t * k + q], ys[st.col[t * k + q]]));
+            if (BACKWARD) {
+                const double dv = st.diag[t];
+                s = dv != 0.0 ? __ddiv_rn(s, dv) : s;
             }
             ys[i] = s;
         }
-        __syncthreads();
     }
-    for (int l = 0; l < nlevB; ++l) {
-        const int a = __ldg(lvlB + l), b = __ldg(lvlB + l + 1);
-        for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
-            const int i = __ldg(rowsB + t);
-            double s = ys[i];
-            const int kd = __ldg(diagPtr + i);
-            const int end = __ldg(rowPtr + i + 1);
-            for (int kp = kd + 1; kp < end; ++kp)
-                s = __dsub_rn(s, __dmul_rn(__ldg(lu + kp), ys[__ldg(colIdx + kp)]));
-            const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
-            ys[i] = (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s;
-        }
-        __syncthreads();
-    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
+    __syncthreads();
+}
+
+// z = (LU)^-1 r in one CTA: ys = r, forward sweep, backward sweep, z = ys.
+__global__ void __launch_bounds__(kIluSmallThreads) k_ilu_sweeps_small(int n, PackedSweep fwd, PackedSweep bwd,
+                                                                       const int *__restrict__ lvlF,
+                                                                       const int *__restrict__ lvlB, int R,
+                                                                       int stageBytes, const double *__restrict__ r,
+                                                                       double *__restrict__ z)
+{
+    extern __shared__ __align__(16) unsigned char smem[];
+    int *sl = reinterpret_cast<int *>(smem);                           // level pointers of both sweeps
+    int *slF = sl, *slB = sl + fwd.nlev + 1;
+    double *ys = reinterpret_cast<double *>(smem + 8 * ((fwd.nlev + bwd.nlev + 3) / 2 + 1));
+    unsigned char *stages = reinterpret_cast<unsigned char *>(ys + n) + ((16 - ((8 * n) & 15)) & 15);
+    for (int q = threadIdx.x; q <= fwd.nlev; q += blockDim.x)
+        slF[q] = lvlF[q];
+    for (int q = threadIdx.x; q <= bwd.nlev; q += blockDim.x)
+        slB[q] = lvlB[q];
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        ys[i] = r[i];
+    __syncthreads();
+    sweep_levels<false>(fwd, slF, ys, stages, stageBytes, R);
+    sweep_levels<true>(bwd, slB, ys, stages, stageBytes, R);
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         z[i] = ys[i];
+}
+
+// Values of the packed sweeps from the factor: entry e of position t reads
+// lu[pos[t k + e]] (pos -1: padding); the backward diagonal is lu[diagPtr[i]]
+// (0 when the row has none).
+__global__ void __launch_bounds__(kBlock) k_ilu_pack(int n, int kf, int kb, const int32_t *__restrict__ fpos,
+                                                     const int32_t *__restrict__ bpos,
+                                                     const int32_t *__restrict__ brow,
+                                                     const int32_t *__restrict__ diagPtr,
+                                                     const double *__restrict__ lu, double *__restrict__ fval,
+                                                     double *__restrict__ bval, double *__restrict__ bdiag)
+{
+    const int stride = gridDim.x * blockDim.x;
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * kf; e += stride) {
+        const int q = fpos[e];
+        fval[e] = q >= 0 ? lu[q] : 0.0;
+    }
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * kb; e += stride) {
+        const int q = bpos[e];
+        bval[e] = q >= 0 ? lu[q] : 0.0;
+    }
+    for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
+        const int kd = diagPtr[brow[t] & 0xffffff];
+        bdiag[t] = kd >= 0 ? lu[kd] : 0.0;
+    }
 }
 
 // One warp waits for a mark that nothing sets: the bounded wait of the sweeps
@@ -482,10 +591,74 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
                                          cudaMemcpyHostToDevice, ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->bwdLvl.p, d->bwdLevelPtr.data(), d->bwdLevelPtr.size() * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, ctx->stream));
-    d->small = n <= kIluSmallRows;
-    if (d->small)
-        SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                  static_cast<int>(n * sizeof(double))));
+    // the single-CTA path: rows of each sweep in level order with their entries packed at a fixed stride
+    d->small = false;
+    const int nlevF = static_cast<int>(d->fwdLevelPtr.size()) - 1, nlevB = static_cast<int>(d->bwdLevelPtr.size()) - 1;
+    if (n <= kIluSmallRows && nlevF + nlevB + 2 <= 2 * kIluSmallMaxLevels) {
+        int kf = 0, kb = 0;
+        for (int64_t i = 0; i < n; ++i) {
+            int lo = 0;
+            for (int k = rowPtr[i]; k < rowPtr[i + 1] && colIdx[k] < i; ++k)
+                ++lo;
+            kf = std::max(kf, lo);
+            const int kd = d->h_diagPtr[i];
+            kb = std::max(kb, rowPtr[i + 1] - (kd + 1));
+        }
+        kf = std::max(kf, 1);
+        kb = std::max(kb, 1);
+        const int R = std::max(d->maxLevelRows, 1);
+        const int K = std::max(kf, kb);
+        const int stageBytes = (R * K * 8 + R * 8 + R * K * 4 + R * 4 + 15) & ~15;
+        const int64_t smemBytes = 8 * ((nlevF + nlevB + 3) / 2 + 1) + ((8 * n + 15) & ~int64_t(15)) +
+                                  static_cast<int64_t>(kIluStages) * stageBytes;
+        if (K <= kIluSmallMaxK && smemBytes <= kIluSmallSmem) {
+            std::vector<int32_t> frow(n), brow(n), fcol(n * kf, 0), fpos(n * kf, -1), bcol(n * kb, 0),
+                bpos(n * kb, -1);
+            for (int64_t t = 0; t < n; ++t) {
+                const int i = fr[t];
+                int c = 0;
+                for (int k = rowPtr[i]; k < rowPtr[i + 1] && colIdx[k] < i; ++k, ++c) {
+                    fcol[t * kf + c] = colIdx[k];
+                    fpos[t * kf + c] = k;
+                }
+                frow[t] = i | (c << 24);
+                const int j = br[t];
+                const int kd = d->h_diagPtr[j];
+                c = 0;
+                for (int k = kd + 1; k < rowPtr[j + 1]; ++k, ++c) {
+                    bcol[t * kb + c] = colIdx[k];
+                    bpos[t * kb + c] = k;
+                }
+                brow[t] = j | (c << 24);
+            }
+            auto up = [&](DevBuf<int32_t> &dst, const std::vector<int32_t> &src) -> cudaError_t {
+                cudaError_t e = dst.alloc(src.size());
+                if (e == cudaSuccess)
+                    e = cudaMemcpyAsync(dst.p, src.data(), src.size() * sizeof(int32_t), cudaMemcpyHostToDevice,
+                                        ctx->stream);
+                return e;
+            };
+            SIMALL_CUDA_TRY(ctx, up(d->frow, frow));
+            SIMALL_CUDA_TRY(ctx, up(d->brow, brow));
+            SIMALL_CUDA_TRY(ctx, up(d->fcol, fcol));
+            SIMALL_CUDA_TRY(ctx, up(d->fpos, fpos));
+            SIMALL_CUDA_TRY(ctx, up(d->bcol, bcol));
+            SIMALL_CUDA_TRY(ctx, up(d->bpos, bpos));
+            SIMALL_CUDA_TRY(ctx, d->fval.alloc(n * kf));
+            SIMALL_CUDA_TRY(ctx, d->bval.alloc(n * kb));
+            SIMALL_CUDA_TRY(ctx, d->bdiag.alloc(n));
+            SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      static_cast<int>(smemBytes)));
+            // the copies above read host vectors that die at return
+            SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+            d->kf = kf;
+            d->kb = kb;
+            d->stageRows = R;
+            d->stageBytes = stageBytes;
+            d->smallSmem = static_cast<int>(smemBytes);
+            d->small = true;
+        }
+    }
     // the copies above read host vectors that die at return
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     d->analysed = true;
@@ -498,6 +671,11 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
     if (d->small) {
         k_ilu_factor_small<<<1, kIluSmallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
                                                                    d->diagPtr.p, d->lu.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        const int n = static_cast<int>(d->h_diagPtr.size());
+        const int items = n * std::max(d->kf, d->kb);
+        k_ilu_pack<<<std::min((items + kBlock - 1) / kBlock, ctx->num_sms * 8), kBlock, 0, ctx->stream>>>(
+            n, d->kf, d->kb, d->fpos.p, d->bpos.p, d->brow.p, d->diagPtr.p, d->lu.p, d->fval.p, d->bval.p, d->bdiag.p);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
@@ -514,11 +692,11 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
            const double *r, double *z)
 {
     const int n = static_cast<int>(d->h_diagPtr.size());
-    if (d->small) {
-        k_ilu_sweeps_small<<<1, kIluSmallThreads, n * sizeof(double), ctx->stream>>>(
-            n, static_cast<int>(d->fwdLevelPtr.size()) - 1, d->fwdLvl.p, d->fwdRows.p,
-            static_cast<int>(d->bwdLevelPtr.size()) - 1, d->bwdLvl.p, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu,
-            r, z);
+    if (d->small && lu == d->lu.p) {
+        PackedSweep f{d->frow.p, d->fcol.p, d->fval.p, nullptr, static_cast<int>(d->fwdLevelPtr.size()) - 1, d->kf};
+        PackedSweep b{d->brow.p, d->bcol.p, d->bval.p, d->bdiag.p, static_cast<int>(d->bwdLevelPtr.size()) - 1, d->kb};
+        k_ilu_sweeps_small<<<1, kIluSmallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p,
+                                                                               d->stageRows, d->stageBytes, r, z);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }

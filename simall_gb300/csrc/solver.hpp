@@ -19,7 +19,12 @@ struct IluData {
     std::vector<int32_t> h_diagPtr;
     int maxLevelRows = 0;
     bool analysed = false;
-    bool small = false;  // factor and sweeps in one CTA, the sweep vector in shared memory
+    // small systems: factor and sweeps in one CTA (ilu0.cu); the sweeps' rows in
+    // level order, each with its triangle's entries packed at a fixed stride
+    bool small = false;
+    int kf = 0, kb = 0, stageRows = 0, stageBytes = 0, smallSmem = 0;
+    DevBuf<int32_t> frow, brow, fcol, bcol, fpos, bpos;
+    DevBuf<double> fval, bval, bdiag;  // refreshed from lu after every factorisation
 };
 
 struct MixedData;  // mixed.cu
