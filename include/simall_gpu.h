@@ -375,6 +375,12 @@ int simall_adjoint_face_conductance(simall_pressure_system *ps, simall_solver *s
  * returned on its own (the expected result), *seconds = the wall time of the
  * call (the bound is about a second).  The context stays usable. */
 int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds);
+/* The small-system ILU(0) path divides through a correctly rounded reciprocal
+ * (one product and two FMAs, Markstein's correction).  For each i, q_recip[i]
+ * is that quotient a[i] / b[i] and q_div[i] the device's correctly rounded
+ * division; the two must be bit-identical (host arrays, n entries). */
+int simall_diagnose_division(simall_context *ctx, int64_t n, const double *a, const double *b, double *q_recip,
+                             double *q_div);
 
 /* ------------------------------------------------------------------ batched solves */
 /* Many independent SPD systems of uneven size (e.g. one pressure-correction

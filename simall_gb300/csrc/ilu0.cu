@@ -294,6 +294,28 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
 // backward sweep overwrites y with z in place: row i reads y_i and the final
 // z_j of rows in earlier backward levels only).  Same per-row operations, so
 // the results are bit-identical to the reference's.
+// a / b rounded to nearest from rb = RN(1/b) (a correctly rounded reciprocal):
+// q = RN(a rb) is within an ulp of a/b, the remainder r = a - b q is exact
+// with one FMA, and q + r rb rounded once is RN(a/b) (Markstein's theorem,
+// IBM J. Res. Dev. 34(1), 1990; Handbook of Floating-Point Arithmetic,
+// 2nd ed., Thm. 5.9).  Three FP64 operations instead of a full division --
+// GB300's FP64 pipe is narrow enough that the divisions of the backward sweep
+// set its time.  The theorem needs a, b, the quotient and the remainder away
+// from overflow and underflow, and a zero numerator keeps its sign only
+// through the product; outside that range (or when b has no usable
+// reciprocal) the division itself is taken.
+__device__ __forceinline__ double div_rn_by_recip(double a, double b, double rb)
+{
+    const double q = a * rb;
+    const double aq = fabs(q), aa = fabs(a);
+    if (aa >= 0x1p-900 && aa <= 0x1p900 && aq >= 0x1p-900 && aq <= 0x1p900 && fabs(rb) >= 0x1p-900 &&
+        fabs(rb) <= 0x1p900) {
+        const double r = fma(-q, b, a);
+        return fma(r, rb, q);
+    }
+    return __ddiv_rn(a, b);
+}
+
 constexpr int kIluSmallThreads = 1024;
 constexpr int kIluSmallRows = 24576;  // 192 KB of shared memory
 
@@ -301,8 +323,15 @@ __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_factor_small(int nlev,
                                                                        const int32_t *__restrict__ rows,
                                                                        const int32_t *__restrict__ rowPtr,
                                                                        const int32_t *__restrict__ colIdx,
-                                                                       const int32_t *__restrict__ diagPtr, double *lu)
+                                                                       const int32_t *__restrict__ diagPtr, double *lu,
+                                                                       double *rpiv)
 {
+    // level 0 rows keep their diagonal: their pivots' reciprocals first
+    for (int t = lvl[0] + threadIdx.x; t < lvl[nlev > 0 ? 1 : 0]; t += blockDim.x) {
+        const int i = rows[t], di = diagPtr[i];
+        rpiv[i] = (di >= 0 && lu[di] != 0.0) ? __drcp_rn(lu[di]) : 0.0;
+    }
+    __syncthreads();
     for (int l = 1; l < nlev; ++l) {  // level 0 rows have no lower entries
         const int a = lvl[l], b = lvl[l + 1];
         for (int t = a + threadIdx.x; t < b; t += blockDim.x) {
@@ -318,7 +347,7 @@ __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_factor_small(int nlev,
                 const double piv = lu[dk];
                 if (piv == 0.0)
                     continue;
-                const double m = __ddiv_rn(lu[kp], piv);
+                const double m = div_rn_by_recip(lu[kp], piv, rpiv[k]);
                 lu[kp] = m;
                 const int kend = rowPtr[k + 1];
                 for (int jp = dk + 1; jp < kend; ++jp) {
@@ -334,6 +363,8 @@ __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_factor_small(int nlev,
                     }
                 }
             }
+            const int di = diagPtr[i];
+            rpiv[i] = (di >= 0 && lu[di] != 0.0) ? __drcp_rn(lu[di]) : 0.0;
         }
         __syncthreads();
     }
@@ -355,7 +386,7 @@ __device__ __forceinline__ void cp_async8(void *smem, const void *gmem)
 
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
 
-constexpr int kIluStages = 6;         // levels in flight: the copy of level l + 5 overlaps the work of level l
+constexpr int kIluStages = 12;        // levels in flight: the copy of level l + 11 overlaps the work of level l
 constexpr int kIluSmallMaxLevels = 4096;
 constexpr int kIluSmallMaxK = 8;      // entries per row of one triangle
 constexpr int kIluSmallSmem = 220 * 1024;
@@ -370,13 +401,13 @@ __device__ __forceinline__ void cp_async_wait_pipeline()
 // the diagonal.
 struct PackedSweep {
     const int32_t *row, *col;
-    const double *val, *diag;
+    const double *val, *diag, *rdiag;
     int nlev, k;
 };
 
-// Shared-memory stage of one level: vals [R k], diag [R], cols [R k], rows [R].
+// Shared-memory stage of one level: vals [R k], diag [R], rdiag [R], cols [R k], rows [R].
 struct StageView {
-    double *val, *diag;
+    double *val, *diag, *rdiag;
     int32_t *col, *row;
 };
 
@@ -386,7 +417,8 @@ __device__ __forceinline__ StageView stage_view(unsigned char *base, int stageBy
     StageView v;
     v.val = reinterpret_cast<double *>(b);
     v.diag = v.val + static_cast<size_t>(R) * k;
-    v.col = reinterpret_cast<int32_t *>(v.diag + R);
+    v.rdiag = v.diag + R;
+    v.col = reinterpret_cast<int32_t *>(v.rdiag + R);
     v.row = v.col + static_cast<size_t>(R) * k;
     return v;
 }
@@ -397,8 +429,10 @@ __device__ __forceinline__ void issue_level(const PackedSweep &p, const int *lvl
         const int a = lvl[l], cnt = lvl[l + 1] - a, k = p.k;
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
             cp_async4(st.row + q, p.row + a + q);
-            if (p.diag)
+            if (p.diag) {
                 cp_async8(st.diag + q, p.diag + a + q);
+                cp_async8(st.rdiag + q, p.rdiag + a + q);
+            }
         }
         for (int q = threadIdx.x; q < cnt * k; q += blockDim.x) {
             cp_async4(st.col + q, p.col + static_cast<size_t>(a) * k + q);
@@ -430,7 +464,7 @@ __device__ __forceinline__ void sweep_levels(const PackedSweep &p, const int *lv
                 s = __dsub_rn(s, __dmul_rn(st.val[t * k + q], ys[st.col[t * k + q]]));
             if (BACKWARD) {
                 const double dv = st.diag[t];
-                s = dv != 0.0 ? __ddiv_rn(s, dv) : s;
+                s = dv != 0.0 ? div_rn_by_recip(s, dv, st.rdiag[t]) : s;
             }
             ys[i] = s;
         }
@@ -472,7 +506,8 @@ __global__ void __launch_bounds__(kBlock) k_ilu_pack(int n, int kf, int kb, cons
                                                      const int32_t *__restrict__ brow,
                                                      const int32_t *__restrict__ diagPtr,
                                                      const double *__restrict__ lu, double *__restrict__ fval,
-                                                     double *__restrict__ bval, double *__restrict__ bdiag)
+                                                     double *__restrict__ bval, double *__restrict__ bdiag,
+                                                     double *__restrict__ brdiag)
 {
     const int stride = gridDim.x * blockDim.x;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * kf; e += stride) {
@@ -485,7 +520,22 @@ __global__ void __launch_bounds__(kBlock) k_ilu_pack(int n, int kf, int kb, cons
     }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
         const int kd = diagPtr[brow[t] & 0xffffff];
-        bdiag[t] = kd >= 0 ? lu[kd] : 0.0;
+        const double d = kd >= 0 ? lu[kd] : 0.0;
+        bdiag[t] = d;
+        brdiag[t] = d != 0.0 ? __drcp_rn(d) : 0.0;
+    }
+}
+
+// a / b both ways (the division the sweeps take from the reciprocal, and the
+// division itself) for the self-check of the reciprocal form.
+__global__ void __launch_bounds__(kBlock) k_div_check(int n, const double *__restrict__ a,
+                                                     const double *__restrict__ b, double *__restrict__ q1,
+                                                     double *__restrict__ q2)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double bi = b[i];
+        q1[i] = div_rn_by_recip(a[i], bi, bi != 0.0 ? __drcp_rn(bi) : 0.0);
+        q2[i] = __ddiv_rn(a[i], bi);
     }
 }
 
@@ -608,7 +658,7 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
         kb = std::max(kb, 1);
         const int R = std::max(d->maxLevelRows, 1);
         const int K = std::max(kf, kb);
-        const int stageBytes = (R * K * 8 + R * 8 + R * K * 4 + R * 4 + 15) & ~15;
+        const int stageBytes = (R * K * 8 + 2 * R * 8 + R * K * 4 + R * 4 + 15) & ~15;
         const int64_t smemBytes = 8 * ((nlevF + nlevB + 3) / 2 + 1) + ((8 * n + 15) & ~int64_t(15)) +
                                   static_cast<int64_t>(kIluStages) * stageBytes;
         if (K <= kIluSmallMaxK && smemBytes <= kIluSmallSmem) {
@@ -647,6 +697,8 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
             SIMALL_CUDA_TRY(ctx, d->fval.alloc(n * kf));
             SIMALL_CUDA_TRY(ctx, d->bval.alloc(n * kb));
             SIMALL_CUDA_TRY(ctx, d->bdiag.alloc(n));
+            SIMALL_CUDA_TRY(ctx, d->brdiag.alloc(n));
+            SIMALL_CUDA_TRY(ctx, d->rpiv.alloc(n));
             SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                       static_cast<int>(smemBytes)));
             // the copies above read host vectors that die at return
@@ -670,12 +722,13 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
     const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
     if (d->small) {
         k_ilu_factor_small<<<1, kIluSmallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
-                                                                   d->diagPtr.p, d->lu.p);
+                                                                   d->diagPtr.p, d->lu.p, d->rpiv.p);
         SIMALL_LAUNCH_CHECK(ctx);
         const int n = static_cast<int>(d->h_diagPtr.size());
         const int items = n * std::max(d->kf, d->kb);
         k_ilu_pack<<<std::min((items + kBlock - 1) / kBlock, ctx->num_sms * 8), kBlock, 0, ctx->stream>>>(
-            n, d->kf, d->kb, d->fpos.p, d->bpos.p, d->brow.p, d->diagPtr.p, d->lu.p, d->fval.p, d->bval.p, d->bdiag.p);
+            n, d->kf, d->kb, d->fpos.p, d->bpos.p, d->brow.p, d->diagPtr.p, d->lu.p, d->fval.p, d->bval.p, d->bdiag.p,
+            d->brdiag.p);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
@@ -693,8 +746,10 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
 {
     const int n = static_cast<int>(d->h_diagPtr.size());
     if (d->small && lu == d->lu.p) {
-        PackedSweep f{d->frow.p, d->fcol.p, d->fval.p, nullptr, static_cast<int>(d->fwdLevelPtr.size()) - 1, d->kf};
-        PackedSweep b{d->brow.p, d->bcol.p, d->bval.p, d->bdiag.p, static_cast<int>(d->bwdLevelPtr.size()) - 1, d->kb};
+        PackedSweep f{d->frow.p, d->fcol.p, d->fval.p, nullptr, nullptr, static_cast<int>(d->fwdLevelPtr.size()) - 1,
+                      d->kf};
+        PackedSweep b{d->brow.p, d->bcol.p, d->bval.p, d->bdiag.p, d->brdiag.p,
+                      static_cast<int>(d->bwdLevelPtr.size()) - 1, d->kb};
         k_ilu_sweeps_small<<<1, kIluSmallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p,
                                                                                d->stageRows, d->stageBytes, r, z);
         SIMALL_LAUNCH_CHECK(ctx);
@@ -870,6 +925,28 @@ int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *se
     *timed_out = static_cast<int>(h);
     if (seconds)
         *seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    return SIMALL_OK;
+}
+
+int simall_diagnose_division(simall_context *ctx, int64_t n, const double *a, const double *b, double *q_recip,
+                             double *q_div)
+{
+    if (!ctx || n < 0 || (n > 0 && (!a || !b || !q_recip || !q_div)) || n > INT32_MAX)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (n == 0)
+        return SIMALL_OK;
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    DevBuf<double> buf;
+    SIMALL_CUDA_TRY(ctx, buf.alloc(4 * n));
+    cudaStream_t st = ctx->stream;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(buf.p, a, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(buf.p + n, b, n * sizeof(double), cudaMemcpyHostToDevice, st));
+    const int grid = static_cast<int>(std::min<int64_t>((n + kBlock - 1) / kBlock, ctx->num_sms * 8));
+    k_div_check<<<grid, kBlock, 0, st>>>(static_cast<int>(n), buf.p, buf.p + n, buf.p + 2 * n, buf.p + 3 * n);
+    SIMALL_LAUNCH_CHECK(ctx);
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(q_recip, buf.p + 2 * n, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(q_div, buf.p + 3 * n, n * sizeof(double), cudaMemcpyDeviceToHost, st));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     return SIMALL_OK;
 }
 

@@ -24,7 +24,8 @@ struct IluData {
     bool small = false;
     int kf = 0, kb = 0, stageRows = 0, stageBytes = 0, smallSmem = 0;
     DevBuf<int32_t> frow, brow, fcol, bcol, fpos, bpos;
-    DevBuf<double> fval, bval, bdiag;  // refreshed from lu after every factorisation
+    DevBuf<double> fval, bval, bdiag, brdiag;  // refreshed from lu after every factorisation
+    DevBuf<double> rpiv;                        // reciprocals of the pivots (factor)
 };
 
 struct MixedData;  // mixed.cu

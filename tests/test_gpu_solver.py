@@ -264,3 +264,29 @@ def test_device_resident_solve_matches_host(sg, ctx, oracle):
     s.solve_into(tb, tx)
     xo, ito, lasto = oracle.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
     assert rel(tx.cpu().numpy(), xo) <= 1e-10
+
+
+@pytest.mark.gpu
+def test_reciprocal_division_is_correctly_rounded(sg, ctx):
+    """The small-system ILU(0) path's a/b through RN(1/b) and one correction
+    step equals the device's correctly rounded division bit for bit: random
+    mantissas over a wide exponent range, near-ties, signed zeros, tiny and
+    huge operands (the guarded range falls back to the division)."""
+    rng = np.random.default_rng(2024)
+    n = 1 << 22
+    a = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-400, 400, n)) * rng.choice([-1.0, 1.0], n)
+    b = rng.uniform(1.0, 2.0, n) * np.exp2(rng.integers(-400, 400, n)) * rng.choice([-1.0, 1.0], n)
+    # quotients near halfway cases: a = b * (1 + k ulp / 2)
+    m = n // 8
+    b[:m] = rng.uniform(1.0, 2.0, m)
+    a[:m] = b[:m] * (1.0 + rng.integers(-64, 64, m) * 2.0 ** -53)
+    special = np.array([0.0, -0.0, 1e-310, -1e-310, 1e300, -1e300, 5e-324, 1.7e308, 1.0, -1.0, 3.0, 7.0])
+    a[-144:] = np.repeat(special, 12)
+    b[-144:] = np.tile(special, 12)
+    q1 = np.empty(n)
+    q2 = np.empty(n)
+    L = sg.load()
+    assert L.simall_diagnose_division(ctx.handle, n, a.ctypes.data, b.ctypes.data, q1.ctypes.data,
+                                      q2.ctypes.data) == 0
+    same = (q1.view(np.int64) == q2.view(np.int64)) | (np.isnan(q1) & np.isnan(q2))
+    assert same.all(), (a[~same][:5], b[~same][:5])
