@@ -72,6 +72,8 @@ def parse():
     ap.add_argument("--no-cavity", action="store_true", help="skip the 128x128 cavity pressure-step leg")
     ap.add_argument("--simple-iterations", type=int, default=20,
                     help="outer iterations of the device SIMPLE leg (0 disables it)")
+    ap.add_argument("--simple-only", action="store_true",
+                    help="run only the device SIMPLE leg and print its JSON (profiling runs)")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the error check against a 1e-12 FP64 solve")
     ap.add_argument("--check-interval", type=int, default=0,
@@ -594,6 +596,13 @@ def run_simple(a, ctx, sg, with_cpu):
 
 def run_ours(a, rank, world, local):
     import torch
+    if a.simple_only:
+        import simall_gb300 as sg
+        sg.build.build()
+        sg.load()
+        ctx = sg.Context(local)
+        print(json.dumps({"simple": run_simple(a, ctx, sg, not a.no_cpu_baseline)}), flush=True)
+        return
 
     import simall_gb300 as sg
 

@@ -304,12 +304,20 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
 // from overflow and underflow, and a zero numerator keeps its sign only
 // through the product; outside that range (or when b has no usable
 // reciprocal) the division itself is taken.
+// Biased exponent field of x, on the integer pipe (GB300 issues about 1.6 FP64
+// operations per clock per SM, so range tests in FP64 would cost as much as
+// the division they replace).
+__device__ __forceinline__ unsigned biased_exp(double x)
+{
+    return static_cast<unsigned>(__double2hiint(x) >> 20) & 0x7ffu;
+}
+
 __device__ __forceinline__ double div_rn_by_recip(double a, double b, double rb)
 {
     const double q = a * rb;
-    const double aq = fabs(q), aa = fabs(a);
-    if (aa >= 0x1p-900 && aa <= 0x1p900 && aq >= 0x1p-900 && aq <= 0x1p900 && fabs(rb) >= 0x1p-900 &&
-        fabs(rb) <= 0x1p900) {
+    // |a|, |q|, |rb| in [2^-900, 2^901): biased exponents in [123, 1924]
+    const unsigned ea = biased_exp(a) - 123u, eq = biased_exp(q) - 123u, er = biased_exp(rb) - 123u;
+    if ((ea | eq | er) <= 1801u && ea <= 1801u && eq <= 1801u && er <= 1801u) {
         const double r = fma(-q, b, a);
         return fma(r, rb, q);
     }
@@ -708,6 +716,9 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
             d->stageRows = R;
             d->stageBytes = stageBytes;
             d->smallSmem = static_cast<int>(smemBytes);
+            // one thread per row of the widest level: every warp pays each level's barrier and loop
+            // control, so warps beyond the widest level only add work to the chain
+            d->smallThreads = std::min(kIluSmallThreads, std::max(64, (R + 31) & ~31));
             d->small = true;
         }
     }
@@ -721,8 +732,8 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
 {
     const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
     if (d->small) {
-        k_ilu_factor_small<<<1, kIluSmallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
-                                                                   d->diagPtr.p, d->lu.p, d->rpiv.p);
+        k_ilu_factor_small<<<1, d->smallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
+                                                                  d->diagPtr.p, d->lu.p, d->rpiv.p);
         SIMALL_LAUNCH_CHECK(ctx);
         const int n = static_cast<int>(d->h_diagPtr.size());
         const int items = n * std::max(d->kf, d->kb);
@@ -750,8 +761,8 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
                       d->kf};
         PackedSweep b{d->brow.p, d->bcol.p, d->bval.p, d->bdiag.p, d->brdiag.p,
                       static_cast<int>(d->bwdLevelPtr.size()) - 1, d->kb};
-        k_ilu_sweeps_small<<<1, kIluSmallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p,
-                                                                               d->stageRows, d->stageBytes, r, z);
+        k_ilu_sweeps_small<<<1, d->smallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p,
+                                                                              d->stageRows, d->stageBytes, r, z);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }

@@ -22,7 +22,7 @@ struct IluData {
     // small systems: factor and sweeps in one CTA (ilu0.cu); the sweeps' rows in
     // level order, each with its triangle's entries packed at a fixed stride
     bool small = false;
-    int kf = 0, kb = 0, stageRows = 0, stageBytes = 0, smallSmem = 0;
+    int kf = 0, kb = 0, stageRows = 0, stageBytes = 0, smallSmem = 0, smallThreads = 0;
     DevBuf<int32_t> frow, brow, fcol, bcol, fpos, bpos;
     DevBuf<double> fval, bval, bdiag, brdiag;  // refreshed from lu after every factorisation
     DevBuf<double> rpiv;                        // reciprocals of the pivots (factor)
