@@ -44,7 +44,9 @@ enum simall_status {
     SIMALL_ERR_TIMEOUT = 10,         /* a bounded device-side wait ran out */
     SIMALL_ERR_UNSUPPORTED = 11,
     SIMALL_ERR_NO_DEVICE = 12,
-    SIMALL_ERR_INDEX_RANGE = 13      /* a column / cell / face index outside [0, n) */
+    SIMALL_ERR_INDEX_RANGE = 13,     /* a column / cell / face index outside [0, n) */
+    SIMALL_ERR_IO = 14,              /* a file could not be opened, written or renamed */
+    SIMALL_ERR_FORMAT = 15           /* not a checkpoint this library reads (magic, version) or truncated */
 };
 
 enum simall_memory { SIMALL_MEM_HOST = 0, SIMALL_MEM_DEVICE = 1 };
@@ -326,6 +328,7 @@ typedef struct simall_simple_residuals {
     int iterations[4]; /* the momentum x, y, z and pressure solves' counts */
 } simall_simple_residuals;
 typedef struct simall_simple simall_simple;
+typedef struct simall_fields simall_fields; /* the field registry, below */
 void simall_simple_options_default(simall_simple_options *o);
 /* U and p start at zero. */
 int simall_simple_create(simall_pressure_system *ps, simall_solver *momentum, simall_solver *pressure,
@@ -336,6 +339,12 @@ int simall_simple_set_fields(simall_simple *s, const double *U, const double *p,
 int simall_simple_get_fields(simall_simple *s, double *U, double *p, double *phi, int mem);
 /* The device arrays the iteration updates in place (valid until destroy). */
 int simall_simple_device_fields(simall_simple *s, double **U, double **p, double **phi);
+/* Keep U and p in a field registry: the iteration then reads and updates the
+ * registry's vector "U" and scalar "p" (created zeroed with n_cells entries
+ * when absent or of another size; they must keep that size while bound), so a
+ * checkpoint of the registry captures the SIMPLE state and a registry read
+ * back from one resumes it. */
+int simall_simple_bind_fields(simall_simple *s, simall_fields *fields);
 int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res);
 /* U^{n-1} <- U^n (from the second step on), U^n <- U, then n_inner iterations. */
 int simall_simple_advance_time_step(simall_simple *s, int n_inner, simall_simple_residuals *res);
@@ -367,6 +376,64 @@ int simall_face_conductance_gradient(simall_pressure_system *ps, double rho, con
 int simall_adjoint_face_conductance(simall_pressure_system *ps, simall_solver *s, double rho, const double *k,
                                     const double *pb, const double *x, const double *dLdx, double *lambda,
                                     double *dk, double *dpb, int mem, simall_solver_stats *stats);
+
+/* ------------------------------------------------------------------ field registry */
+/* Replaces solver::FieldRegistry (src/solver/FieldRegistry.hpp:30-80) with the
+ * fields in device memory: a scalar field is one FP64 array of n entries, a
+ * vector field one [3][n] array (x, y, z back to back).  scalar() / vector()
+ * return the field, creating it zeroed -- or re-creating it zeroed when its
+ * size differs from n -- as the reference's accessors do; the arrays stay
+ * valid until the field is re-created or the registry destroyed.  Fields are
+ * kept in insertion order. */
+int simall_fields_create(simall_context *ctx, simall_fields **out);
+int simall_fields_destroy(simall_fields *f);
+int simall_fields_scalar(simall_fields *f, const char *name, int64_t n, double **data);
+int simall_fields_vector(simall_fields *f, const char *name, int64_t n, double **x, double **y, double **z);
+/* find_scalar / find_vector (vector != 0): *data = NULL and *n = -1 when absent. */
+int simall_fields_find(simall_fields *f, const char *name, int vector, double **data, int64_t *n);
+int simall_fields_count(const simall_fields *f, int *n_scalars, int *n_vectors);
+/* Name (NUL-terminated, truncated to len - 1) and size of the index-th field. */
+int simall_fields_name(const simall_fields *f, int vector, int index, char *buf, int len, int64_t *n);
+/* Host copies: upload creates / re-sizes the field (vector: host holds [3][n]). */
+int simall_fields_upload(simall_fields *f, const char *name, int vector, const double *host, int64_t n);
+int simall_fields_download(simall_fields *f, const char *name, int vector, double *host);
+
+/* ------------------------------------------------------------------ checkpoint */
+/* Replaces io::Checkpoint (src/io/Checkpoint.hpp:26-58, Checkpoint.cpp:66-227):
+ * the same binary format byte for byte (header "SIMALLCP" v1 with a
+ * timestamp, meta, the mesh SoA, then every scalar and vector field of the
+ * registry), written from and read into device memory through pinned,
+ * double-buffered staging; writes go to "<path>.tmp" and are renamed over
+ * <path> when complete.  CheckpointMeta's layout (int, padding, double,
+ * uint64) is kept. */
+typedef struct simall_checkpoint_meta {
+    int32_t iteration;
+    double time;
+    uint64_t settings_hash;
+} simall_checkpoint_meta;
+/* The mesh SoA of meshing::Mesh (src/meshing/MeshStorage.hpp:37-72): host
+ * arrays; offsets have n + 1 entries (NULL writes an empty array). */
+typedef struct simall_checkpoint_mesh {
+    int64_t n_nodes, n_faces, n_cells, n_face_nodes, n_cell_faces;
+    const double *node_x, *node_y, *node_z;
+    const uint64_t *owner, *neighbor;
+    const double *area_x, *area_y, *area_z;
+    const double *centroid_x, *centroid_y, *centroid_z;
+    const uint32_t *boundary_zone;
+    const int32_t *face_node_offsets;
+    const uint64_t *face_node_indices;
+    const double *volume, *cell_centroid_x, *cell_centroid_y, *cell_centroid_z;
+    const int32_t *cell_face_offsets;
+    const uint64_t *cell_face_indices;
+} simall_checkpoint_mesh;
+int simall_checkpoint_write(const char *path, const simall_checkpoint_mesh *mesh, simall_fields *fields,
+                            const simall_checkpoint_meta *meta);
+/* Reads every field into `fields` (scalar()/vector() semantics), *meta if not
+ * NULL, and the mesh into library-allocated host arrays when mesh_out is not
+ * NULL (release them with simall_checkpoint_mesh_free). */
+int simall_checkpoint_read(const char *path, simall_fields *fields, simall_checkpoint_meta *meta,
+                           simall_checkpoint_mesh *mesh_out);
+void simall_checkpoint_mesh_free(simall_checkpoint_mesh *mesh);
 
 /* ------------------------------------------------------------------ diagnostics */
 /* Failure detection without a GPU fault (no reference counterpart): runs one

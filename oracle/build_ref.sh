@@ -10,7 +10,8 @@
 #   src/meshing/CartesianMesher.cpp, src/meshing/Connectivity.cpp,
 #   src/meshing/MeshOps.cpp, src/meshing/MeshQuality.cpp,
 #   src/adjoint/DiscreteAdjoint.cpp, src/core/PluginLoader.cpp,
-#   src/core/PluginRegistry.cpp
+#   src/core/PluginRegistry.cpp, src/io/Checkpoint.cpp,
+#   src/optimization/SimpTopology.cpp
 #
 # Patch: LinearSolvers.cpp assigns util::aligned_vector<int> to std::vector<int>
 # at :85-86 and :170-171, which g++ 13 rejects.  A scratch copy written into
@@ -45,6 +46,8 @@ $REF/src/meshing/MeshQuality.cpp
 $REF/src/adjoint/DiscreteAdjoint.cpp
 $REF/src/core/PluginLoader.cpp
 $REF/src/core/PluginRegistry.cpp
+$REF/src/io/Checkpoint.cpp
+$REF/src/optimization/SimpTopology.cpp
 $HERE/ref_driver.cpp"
 pids=""
 objs=""

@@ -513,6 +513,12 @@ class RefLib:
         L.ref_simple_run.restype = C.c_int
         L.ref_simple_run.argtypes = [_P, C.c_int, _P, _P, _P, _P, C.c_int, _P, _D, _P, _D, C.c_int, C.c_int] + \
             [_P] * 5 + [C.c_int, _P, _P]
+        L.ref_checkpoint_write.restype = C.c_int
+        L.ref_checkpoint_write.argtypes = [_P, C.c_char_p, C.c_int, _P, _P, _P, _P, C.c_int, _D, C.c_uint64]
+        L.ref_checkpoint_read.restype = _P
+        L.ref_checkpoint_read.argtypes = [C.c_char_p, _P, _P]
+        L.ref_checkpoint_field.restype = _I64
+        L.ref_checkpoint_field.argtypes = [C.c_char_p, C.c_int, _P]
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -708,6 +714,40 @@ class RefLib:
                               _ptr(U), _ptr(p), _ptr(phi), _ptr(res), _ptr(its), cap, C.byref(nits), C.byref(secs))
         return {"U": U, "p": p, "phi": phi, "res": res, "iters": its[:nits.value].reshape(-1, 4).copy(),
                 "seconds": secs.value}
+
+    def checkpoint_write(self, mesh_dict, path, fields, iteration=0, time=0.0, settings_hash=0):
+        """io::Checkpoint::write; fields = [(name, is_vector, array (n,) or (3, n))] in insertion order."""
+        arrs = [np.ascontiguousarray(a, np.float64) for _, _, a in fields]
+        names = (C.c_char_p * max(1, len(fields)))(*[f[0].encode() for f in fields])
+        isv = np.array([int(f[1]) for f in fields] or [0], np.int32)
+        sizes = np.array([a.shape[-1] if f[1] else a.size for f, a in zip(fields, arrs)] or [0], np.int64)
+        ptrs = (C.c_void_p * max(1, len(fields)))(*[a.ctypes.data for a in arrs])
+        return self.L.ref_checkpoint_write(mesh_dict["handle"], path.encode(), len(fields), names, _ptr(isv),
+                                           _ptr(sizes), ptrs, int(iteration), float(time), int(settings_hash))
+
+    def checkpoint_read(self, path):
+        """io::Checkpoint::read; returns (mesh dict with a handle, meta (iteration, time, hash),
+        field getter name, is_vector -> array)."""
+        sizes = np.zeros(5, np.int64)
+        meta = np.zeros(3)
+        h = self.L.ref_checkpoint_read(path.encode(), _ptr(sizes), _ptr(meta))
+        if not h:
+            return None
+        s5 = np.zeros(5, np.int64)
+        self.L.ref_mesh_sizes(h, _ptr(s5))
+        md = self._fetch(h, *(int(v) for v in s5))
+        md["handle"] = h
+        md["n_scalars"], md["n_vectors"] = int(sizes[3]), int(sizes[4])
+
+        def field(name, vector=False):
+            n = self.L.ref_checkpoint_field(name.encode(), int(vector), None)
+            if n < 0:
+                return None
+            out = np.empty((3, n) if vector else n)
+            self.L.ref_checkpoint_field(name.encode(), int(vector), _ptr(out))
+            return out
+
+        return md, (int(meta[0]), float(meta[1]), int(meta[2:3].view(np.uint64)[0])), field
 
     # -- solvers
     def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):

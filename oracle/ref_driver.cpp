@@ -14,9 +14,13 @@
 //   make_cg / make_gmres / make_preconditioner     src/solver/LinearSolvers.cpp:240,462
 //   adjoint::solve_discrete_adjoint         src/adjoint/DiscreteAdjoint.cpp:150
 //   core::PluginLoader::load / PluginRegistry  src/core/PluginLoader.cpp:68, PluginRegistry.cpp:23
+//   io::Checkpoint::write / read            src/io/Checkpoint.cpp:66, :145
+//   optimization::SimpTopology              src/optimization/SimpTopology.cpp:18, :132
 #include "adjoint/DiscreteAdjoint.hpp"
 #include "core/PluginLoader.hpp"
 #include "core/PluginRegistry.hpp"
+#include "io/Checkpoint.hpp"
+#include "optimization/SimpTopology.hpp"
 #include "meshing/CartesianMesher.hpp"
 #include "meshing/MeshOps.hpp"
 #include "meshing/MeshStorage.hpp"
@@ -598,6 +602,85 @@ int ref_simple_run(void* h, int nbc, const std::uint32_t* bcZones, const int* bc
     for (int i = 0; i < static_cast<int>(all.size()) && i < maxIters; ++i)
         iters[i] = all[i];
     return 0;
+}
+
+// ------------------------------------------------------------------ checkpoint
+// io::Checkpoint::write of the given mesh and fields: nf fields in the given
+// insertion order, isVector[i] selects vector (data [3][n]) or scalar (data [n]).
+int ref_checkpoint_write(void* h, const char* path, int nf, const char* const* names, const int* isVector,
+                         const std::int64_t* sizes, const double* const* data, int iteration, double time,
+                         std::uint64_t hash)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    for (int i = 0; i < nf; ++i) {
+        const std::size_t n = static_cast<std::size_t>(sizes[i]);
+        if (isVector[i]) {
+            auto& v = f.vector(names[i], n);
+            std::copy(data[i], data[i] + n, v.x.begin());
+            std::copy(data[i] + n, data[i] + 2 * n, v.y.begin());
+            std::copy(data[i] + 2 * n, data[i] + 3 * n, v.z.begin());
+        } else {
+            auto& s = f.scalar(names[i], n);
+            std::copy(data[i], data[i] + n, s.begin());
+        }
+    }
+    simall::io::CheckpointMeta meta{};
+    meta.iteration = iteration;
+    meta.time = time;
+    meta.settingsHash = hash;
+    return simall::io::Checkpoint::write(path, m, f, meta) ? 0 : 1;
+}
+
+// io::Checkpoint::read: returns a mesh handle (cells, faces, nodes in sizes[0..2])
+// and keeps the fields for ref_checkpoint_field; meta[0] = iteration, [1] = time,
+// [2] = settings hash bits.
+S::FieldRegistry* g_ckpt_fields = nullptr;
+void* ref_checkpoint_read(const char* path, std::int64_t* sizes, double* meta)
+{
+    auto* rm = new RefMesh;
+    delete g_ckpt_fields;
+    g_ckpt_fields = new S::FieldRegistry;
+    simall::io::CheckpointMeta md{};
+    if (!simall::io::Checkpoint::read(path, rm->mesh, *g_ckpt_fields, md)) {
+        delete rm;
+        return nullptr;
+    }
+    sizes[0] = static_cast<std::int64_t>(rm->mesh.cells().size());
+    sizes[1] = static_cast<std::int64_t>(rm->mesh.faces().size());
+    sizes[2] = static_cast<std::int64_t>(rm->mesh.nodes().size());
+    sizes[3] = static_cast<std::int64_t>(g_ckpt_fields->scalars().size());
+    sizes[4] = static_cast<std::int64_t>(g_ckpt_fields->vectors().size());
+    meta[0] = md.iteration;
+    meta[1] = md.time;
+    std::memcpy(&meta[2], &md.settingsHash, 8);
+    return rm;
+}
+
+// A field of the last ref_checkpoint_read: returns its size (-1 if absent);
+// out receives n (scalar) or 3n (vector) values when not null.
+std::int64_t ref_checkpoint_field(const char* name, int isVector, double* out)
+{
+    if (!g_ckpt_fields)
+        return -1;
+    if (isVector) {
+        auto* v = g_ckpt_fields->find_vector(name);
+        if (!v)
+            return -1;
+        const std::size_t n = v->size();
+        if (out) {
+            std::copy(v->x.begin(), v->x.end(), out);
+            std::copy(v->y.begin(), v->y.end(), out + n);
+            std::copy(v->z.begin(), v->z.end(), out + 2 * n);
+        }
+        return static_cast<std::int64_t>(n);
+    }
+    auto* s = g_ckpt_fields->find_scalar(name);
+    if (!s)
+        return -1;
+    if (out)
+        std::copy(s->begin(), s->end(), out);
+    return static_cast<std::int64_t>(s->size());
 }
 
 // ------------------------------------------------------------------ cavity SIMPLE

@@ -8,6 +8,7 @@ mirror of the reference's solver interface plus the mesh/assembly wrappers.
 from . import build
 from .batch import BatchedSolver
 from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
+from .fields import DeviceFieldRegistry, checkpoint_read, checkpoint_write
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
 from .simple import GpuSimpleAlgorithm, SimpleOptions, SimpleResiduals
 from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
@@ -17,4 +18,5 @@ from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSol
 __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
-           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals"]
+           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals",
+           "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write"]

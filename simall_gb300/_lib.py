@@ -25,7 +25,7 @@ STATUS_NAMES = {
     4: "SIMALL_ERR_UNSORTED_CSR", 5: "SIMALL_ERR_MISSING_DIAGONAL", 6: "SIMALL_ERR_NON_FINITE",
     7: "SIMALL_ERR_NOT_POSITIVE", 8: "SIMALL_ERR_SIZE_MISMATCH", 9: "SIMALL_ERR_BREAKDOWN",
     10: "SIMALL_ERR_TIMEOUT", 11: "SIMALL_ERR_UNSUPPORTED", 12: "SIMALL_ERR_NO_DEVICE",
-    13: "SIMALL_ERR_INDEX_RANGE",
+    13: "SIMALL_ERR_INDEX_RANGE", 14: "SIMALL_ERR_IO", 15: "SIMALL_ERR_FORMAT",
 }
 
 
@@ -54,6 +54,23 @@ class SimpleOptions(C.Structure):
 
 class SimpleResiduals(C.Structure):
     _fields_ = [("mom", _D * 3), ("cont", _D), ("iterations", _I * 4)]
+
+
+class CheckpointMeta(C.Structure):
+    _fields_ = [("iteration", C.c_int32), ("time", _D), ("settings_hash", C.c_uint64)]
+
+
+CHECKPOINT_MESH_ARRAYS = [("node_x", "f8"), ("node_y", "f8"), ("node_z", "f8"), ("owner", "u8"), ("neighbor", "u8"),
+                          ("area_x", "f8"), ("area_y", "f8"), ("area_z", "f8"), ("centroid_x", "f8"),
+                          ("centroid_y", "f8"), ("centroid_z", "f8"), ("boundary_zone", "u4"),
+                          ("face_node_offsets", "i4"), ("face_node_indices", "u8"), ("volume", "f8"),
+                          ("cell_centroid_x", "f8"), ("cell_centroid_y", "f8"), ("cell_centroid_z", "f8"),
+                          ("cell_face_offsets", "i4"), ("cell_face_indices", "u8")]
+
+
+class CheckpointMesh(C.Structure):
+    _fields_ = [("n_nodes", _I64), ("n_faces", _I64), ("n_cells", _I64), ("n_face_nodes", _I64),
+                ("n_cell_faces", _I64)] + [(name, _P) for name, _ in CHECKPOINT_MESH_ARRAYS]
 
 
 class MeshView(C.Structure):
@@ -121,6 +138,19 @@ SIGNATURES = {
     "simall_simple_device_fields": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "simall_simple_iterate": (_I, [_P, C.POINTER(SimpleResiduals)]),
     "simall_simple_advance_time_step": (_I, [_P, _I, C.POINTER(SimpleResiduals)]),
+    "simall_fields_create": (_I, [_P, C.POINTER(_P)]),
+    "simall_fields_destroy": (_I, [_P]),
+    "simall_fields_scalar": (_I, [_P, C.c_char_p, _I64, C.POINTER(_P)]),
+    "simall_fields_vector": (_I, [_P, C.c_char_p, _I64, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    "simall_fields_find": (_I, [_P, C.c_char_p, _I, C.POINTER(_P), C.POINTER(_I64)]),
+    "simall_fields_count": (_I, [_P, C.POINTER(_I), C.POINTER(_I)]),
+    "simall_fields_name": (_I, [_P, _I, _I, C.c_char_p, _I, C.POINTER(_I64)]),
+    "simall_fields_upload": (_I, [_P, C.c_char_p, _I, _P, _I64]),
+    "simall_fields_download": (_I, [_P, C.c_char_p, _I, _P]),
+    "simall_checkpoint_write": (_I, [C.c_char_p, C.POINTER(CheckpointMesh), _P, C.POINTER(CheckpointMeta)]),
+    "simall_checkpoint_read": (_I, [C.c_char_p, _P, C.POINTER(CheckpointMeta), C.POINTER(CheckpointMesh)]),
+    "simall_checkpoint_mesh_free": (None, [C.POINTER(CheckpointMesh)]),
+    "simall_simple_bind_fields": (_I, [_P, _P]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),

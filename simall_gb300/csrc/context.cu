@@ -135,6 +135,10 @@ const char *simall_status_string(int s)
         return "CG breakdown (p.Ap == 0)";
     case SIMALL_ERR_TIMEOUT:
         return "bounded device wait expired";
+    case SIMALL_ERR_IO:
+        return "file could not be opened, written or renamed";
+    case SIMALL_ERR_FORMAT:
+        return "not a readable checkpoint (magic, version) or truncated";
     case SIMALL_ERR_UNSUPPORTED:
         return "unsupported option";
     case SIMALL_ERR_NO_DEVICE:

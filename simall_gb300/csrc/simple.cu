@@ -20,6 +20,7 @@
 // The host only sequences launches; the solvers poll their stop flags.
 #include "device.cuh"
 #include "pressure_system.hpp"
+#include "registry.hpp"
 #include "solver.hpp"
 
 #include <new>
@@ -30,7 +31,10 @@ struct simall_simple {
     simall_solver *mom = nullptr, *pres = nullptr;
     simall_simple_options o{};
     simall::DevBuf<double> U, p, phi, pPrime, Un, Unm1;
+    double *uext = nullptr, *pext = nullptr;  // U and p of a bound field registry
     int timeStep = 0;
+    double *Ud() { return uext ? uext : U.p; }
+    double *Pd() { return pext ? pext : p.p; }
 };
 
 using namespace simall;
@@ -112,10 +116,10 @@ int simall_simple_create(simall_pressure_system *ps, simall_solver *momentum, si
         return cuda_fail(ctx, e, "SIMPLE field allocation", __FILE__, __LINE__);
     }
     cudaStream_t st = ctx->stream;
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->U.p, 0, 3 * nC * sizeof(double), st));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->Ud(), 0, 3 * nC * sizeof(double), st));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->Un.p, 0, 3 * nC * sizeof(double), st));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->Unm1.p, 0, 3 * nC * sizeof(double), st));
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->p.p, 0, nC * sizeof(double), st));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->Pd(), 0, nC * sizeof(double), st));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->pPrime.p, 0, nC * sizeof(double), st));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->phi.p, 0, nF * sizeof(double), st));
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
@@ -140,12 +144,12 @@ int simall_simple_set_fields(simall_simple *s, const double *U, const double *p,
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const int64_t nC = s->ps->nC;
     if (U) {
-        int e = copy_in(ctx, s->U.p, U, 3 * nC, mem);
+        int e = copy_in(ctx, s->Ud(), U, 3 * nC, mem);
         if (e)
             return e;
     }
     if (p) {
-        int e = copy_in(ctx, s->p.p, p, nC, mem);
+        int e = copy_in(ctx, s->Pd(), p, nC, mem);
         if (e)
             return e;
     }
@@ -162,9 +166,9 @@ int simall_simple_get_fields(simall_simple *s, double *U, double *p, double *phi
     const int64_t nC = s->ps->nC, nF = s->ps->nF;
     int e = SIMALL_OK;
     if (U && !e)
-        e = copy_out(ctx, U, s->U.p, 3 * nC, mem);
+        e = copy_out(ctx, U, s->Ud(), 3 * nC, mem);
     if (p && !e)
-        e = copy_out(ctx, p, s->p.p, nC, mem);
+        e = copy_out(ctx, p, s->Pd(), nC, mem);
     if (phi && !e)
         e = copy_out(ctx, phi, s->phi.p, nF, mem);
     if (e)
@@ -178,11 +182,28 @@ int simall_simple_device_fields(simall_simple *s, double **U, double **p, double
     if (!s)
         return SIMALL_ERR_INVALID_ARGUMENT;
     if (U)
-        *U = s->U.p;
+        *U = s->Ud();
     if (p)
-        *p = s->p.p;
+        *p = s->Pd();
     if (phi)
         *phi = s->phi.p;
+    return SIMALL_OK;
+}
+
+int simall_simple_bind_fields(simall_simple *s, simall_fields *fields)
+{
+    if (!s || !fields || fields->ctx != s->ctx)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    SIMALL_CUDA_TRY(s->ctx, cudaSetDevice(s->ctx->device));
+    int st = SIMALL_OK;
+    simall_fields::Field *u = registry_get(fields, "U", s->ps->nC, true, &st);
+    if (!u)
+        return st;
+    simall_fields::Field *p = registry_get(fields, "p", s->ps->nC, false, &st);
+    if (!p)
+        return st;
+    s->uext = u->data.p;
+    s->pext = p->data.p;
     return SIMALL_OK;
 }
 
@@ -195,7 +216,7 @@ int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res)
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const int64_t nC = ps->nC;
     const simall_simple_options &o = s->o;
-    double *U = s->U.p;
+    double *U = s->Ud();
     simall_simple_residuals r{};
     int e = simall_compute_face_fluxes(ps, o.rho, U, U + nC, U + 2 * nC, s->phi.p, SIMALL_MEM_DEVICE);
     if (e)
@@ -207,7 +228,7 @@ int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res)
     mo.dt = o.dt;
     mo.bdf2 = (o.dt > 0.0 && o.bdf2 && s->timeStep >= 1) ? 1 : 0;  // BDF2 from the second step (:335)
     mo.reserved = 0;
-    e = simall_assemble_momentum(ps, &mo, U, s->p.p, s->phi.p, s->Un.p, s->Unm1.p, SIMALL_MEM_DEVICE);
+    e = simall_assemble_momentum(ps, &mo, U, s->Pd(), s->phi.p, s->Un.p, s->Unm1.p, SIMALL_MEM_DEVICE);
     if (e)
         return e;
     e = simall_solver_set_matrix(s->mom, nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->mvalues.p, SIMALL_MEM_DEVICE);
@@ -235,7 +256,7 @@ int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res)
         return e;
     r.cont = st.b_norm > 1e-30 ? st.b_norm : 0.0;  // |rhs|; the solver floors its norm at 1e-30
     r.iterations[3] = st.iterations;
-    e = simall_correct_fields(ps, o.rho, o.urfP, ps->maP.p, s->pPrime.p, s->p.p, U, U + nC, U + 2 * nC, s->phi.p,
+    e = simall_correct_fields(ps, o.rho, o.urfP, ps->maP.p, s->pPrime.p, s->Pd(), U, U + nC, U + 2 * nC, s->phi.p,
                               SIMALL_MEM_DEVICE);
     if (e)
         return e;
@@ -254,7 +275,7 @@ int simall_simple_advance_time_step(simall_simple *s, int n_inner, simall_simple
     // roll the history: U^{n-1} <- U^n (from the second step), U^n <- U
     if (s->timeStep >= 1)
         SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->Unm1.p, s->Un.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
-    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->Un.p, s->U.p, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->Un.p, s->Ud(), bytes, cudaMemcpyDeviceToDevice, ctx->stream));
     simall_simple_residuals last{};
     for (int k = 0; k < (n_inner > 1 ? n_inner : 1); ++k) {
         int e = simall_simple_iterate(s, &last);

@@ -65,6 +65,11 @@ class GpuSimpleAlgorithm:
         register_child(self)
         self.ctx.children.add(self)
 
+    def bind_fields(self, registry):
+        """Keep U and p in a DeviceFieldRegistry (vector "U", scalar "p")."""
+        check(self.L.simall_simple_bind_fields(self.handle, registry.handle), self.ctx.handle)
+        self._registry = registry
+
     def set_fields(self, U=None, p=None):
         """U: (3, n_cells), p: (n_cells,) -- numpy or CUDA tensors."""
         pu, mu_ = ptr_and_mem(U) if U is not None else (None, None)

@@ -8,7 +8,7 @@ renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction / assemble_momentum, CGSolver::solve with
 Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
 preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
-advance_time_step runs, solve_discrete_adjoint);
+advance_time_step runs, io::Checkpoint::write, solve_discrete_adjoint);
 inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
 
@@ -203,6 +203,26 @@ def simple_case(name):
                         U=out["U"], p=out["p"], phi=out["phi"], res=out["res"], iters=out["iters"])
 
 
+def checkpoint_case(name):
+    """io::Checkpoint::write of the reference: a distorted 4x3x2 box, scalar
+    fields "p" and "T" and vector field "U" (inserted in that order), meta
+    iteration 17, time 0.125, settings hash 0x123456789abcdef0; the file and,
+    beside it, the arrays it holds."""
+    dims = (4, 3, 2)
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=23)
+    rm = R.cartesian_mesh(*dims, node_shift=shift)
+    rng = np.random.default_rng(23)
+    nC = rm["nC"]
+    p, T, U = rng.standard_normal(nC), rng.standard_normal(nC), rng.standard_normal((3, nC))
+    path = os.path.join(HERE, name + ".simallcp")
+    assert R.checkpoint_write(rm, path, [("p", False, p), ("T", False, T), ("U", True, U)], 17, 0.125,
+                              0x123456789ABCDEF0) == 0
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), dims=np.array(dims), seed=np.array(23), p=p, T=T, U=U,
+                        **{k: rm[k] for k in ("nx", "ny", "nz", "owner", "neighbor", "ax", "ay", "az", "fcx", "fcy",
+                                              "fcz", "zone", "fnOff", "fnIdx", "vol", "ccx", "ccy", "ccz", "cfOff",
+                                              "cfIdx")})
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -239,6 +259,7 @@ def main():
     momentum_case("momentum_7x6x5_rcm_bdf2.npz")
     for name in SIMPLE_RUNS:
         simple_case(name)
+    checkpoint_case("checkpoint_4x3x2")
     print("fixtures written to", HERE)
 
 

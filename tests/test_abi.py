@@ -46,7 +46,7 @@ def test_plugin_abi_version(sg):
 
 def test_status_strings(sg):
     L = sg.load()
-    for code in range(14):
+    for code in range(16):
         assert L.simall_status_string(code) and L.simall_status_string(code) != b"unknown status"
     assert L.simall_version().startswith(b"simall_gb300")
 
