@@ -435,6 +435,32 @@ int simall_checkpoint_read(const char *path, simall_fields *fields, simall_check
                            simall_checkpoint_mesh *mesh_out);
 void simall_checkpoint_mesh_free(simall_checkpoint_mesh *mesh);
 
+/* ------------------------------------------------------------------ SIMP topology optimisation */
+/* Replaces optimization::SimpTopology (src/optimization/SimpTopology.hpp:48-80,
+ * .cpp:18-227) with its fields in a device registry: create() is initialize()
+ * (fields "rho", "rhoTilde", "K_simp", "dC_drho", "dC_drhoTilde" of
+ * n_cells entries, set to volumeFraction, volumeFraction, K_min, 0, 0); each
+ * step() filters rho (Helmholtz, CG + Jacobi on the device), forms
+ * K_simp = K_min + (K_max - K_min) rhoTilde^p, takes the caller's "dC_drho"
+ * through the filter, and runs the optimality-criteria update with bisection
+ * on the volume multiplier; *change = sum |delta rho| / n.  The sensitivity
+ * typically comes from simall_adjoint_face_conductance. */
+typedef struct simall_simp_config {
+    double penalty;         /* SimpConfig::penalty (p) */
+    double K_min, K_max;
+    double filter_radius;   /* 0 disables the Helmholtz filter */
+    double volume_fraction;
+    double move;            /* OC move limit */
+    double damping;         /* OC damping exponent */
+    double rho_min;
+} simall_simp_config;
+typedef struct simall_simp simall_simp;
+void simall_simp_config_default(simall_simp_config *cfg);
+int simall_simp_create(simall_pressure_system *ps, simall_fields *fields, const simall_simp_config *cfg,
+                       simall_simp **out);
+int simall_simp_step(simall_simp *s, double *change);
+int simall_simp_destroy(simall_simp *s);
+
 /* ------------------------------------------------------------------ diagnostics */
 /* Failure detection without a GPU fault (no reference counterpart): runs one
  * warp that waits, with the same bounded wait as the ILU(0) sweeps, for a mark

@@ -94,6 +94,8 @@ def lib():
         L.orc_simple_iterate.restype = None
         L.orc_simple_iterate.argtypes = [_I64, _I64] + [_P] * 16 + [C.c_int] + [_P] * 3 + [C.c_int, _P, _D, _P, _D] + \
             [_P] * 9
+        L.orc_simp_step.restype = _D
+        L.orc_simp_step.argtypes = [_I64, _I64] + [_P] * 17
         _lib = L
     return _lib
 
@@ -355,6 +357,29 @@ def gmres(rowPtr, colIdx, values, b, precond=1, tol=1e-8, max_it=1000, restart=3
     return x, it, last.value
 
 
+class SimpOracle:
+    """SimpTopology (src/optimization/SimpTopology.cpp:18-227) restated:
+    initialize() fields and step() with the caller's dC_drho."""
+
+    def __init__(self, m: Mesh, cfg):
+        self.m = m
+        self.cfg = np.ascontiguousarray(cfg, np.float64)
+        self.rp, self.ci = build_sparsity(m)
+        vf = float(cfg[4])
+        self.rho = np.full(m.nC, vf)
+        self.rhoTilde = np.full(m.nC, vf)
+        self.K_simp = np.full(m.nC, float(cfg[1]))
+        self.dC_drho = np.zeros(m.nC)
+        self.dC_drhoTilde = np.zeros(m.nC)
+
+    def step(self) -> float:
+        m = self.m
+        return lib().orc_simp_step(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+                                   _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz), _ptr(m.vol), _ptr(self.rp), _ptr(self.ci),
+                                   _ptr(self.cfg), _ptr(self.rho), _ptr(self.rhoTilde), _ptr(self.K_simp),
+                                   _ptr(self.dC_drho), _ptr(self.dC_drhoTilde))
+
+
 class SimpleOracle:
     """SimpleAlgorithm::iterate / advance_time_step (SimpleAlgorithm.cpp:522-570)
     restated: the state (U, p, phi, history) lives here, each outer iteration
@@ -519,6 +544,8 @@ class RefLib:
         L.ref_checkpoint_read.argtypes = [C.c_char_p, _P, _P]
         L.ref_checkpoint_field.restype = _I64
         L.ref_checkpoint_field.argtypes = [C.c_char_p, C.c_int, _P]
+        L.ref_simp_run.restype = C.c_int
+        L.ref_simp_run.argtypes = [_P, _P, C.c_int] + [_P] * 6
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -748,6 +775,18 @@ class RefLib:
             return out
 
         return md, (int(meta[0]), float(meta[1]), int(meta[2:3].view(np.uint64)[0])), field
+
+    def simp_run(self, mesh_dict, cfg, dC_steps):
+        """SimpTopology::initialize + one step() per row of dC_steps (stored in
+        "dC_drho" before the step); returns (change[k], rho, rhoTilde, K_simp, dC_drhoTilde)."""
+        nC = mesh_dict["nC"]
+        dC = np.ascontiguousarray(dC_steps, np.float64).reshape(-1, nC)
+        k = dC.shape[0]
+        change = np.empty(k)
+        out = [np.empty(nC) for _ in range(4)]
+        self.L.ref_simp_run(mesh_dict["handle"], _ptr(np.ascontiguousarray(cfg, np.float64)), k, _ptr(dC),
+                            _ptr(change), *(_ptr(o) for o in out))
+        return (change, *out)
 
     # -- solvers
     def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):

@@ -683,6 +683,45 @@ std::int64_t ref_checkpoint_field(const char* name, int isVector, double* out)
     return static_cast<std::int64_t>(s->size());
 }
 
+// ------------------------------------------------------------------ SIMP
+// SimpTopology::initialize + nSteps step() calls on the given mesh; before
+// step k the caller's sensitivity dC[k] (nC values) is stored in "dC_drho".
+// cfg = {penalty, K_min, K_max, filterRadius, volumeFraction, move, damping,
+// rhoMin}.  Out: change[k], and the final rho, rhoTilde, K_simp,
+// dC_drhoTilde.
+int ref_simp_run(void* h, const double* cfg, int nSteps, const double* dC, double* change, double* rho,
+                 double* rhoT, double* kSimp, double* dCt)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::FieldRegistry f;
+    simall::optimization::SimpConfig c;
+    c.penalty = cfg[0];
+    c.K_min = cfg[1];
+    c.K_max = cfg[2];
+    c.filterRadius = cfg[3];
+    c.volumeFraction = cfg[4];
+    c.move = cfg[5];
+    c.damping = cfg[6];
+    c.rhoMin = cfg[7];
+    simall::optimization::SimpTopology simp;
+    simp.initialize(m, f, c);
+    for (int k = 0; k < nSteps; ++k) {
+        auto& d = *f.find_scalar("dC_drho");
+        std::copy(dC + k * nC, dC + (k + 1) * nC, d.begin());
+        change[k] = simp.step(m, f);
+    }
+    auto cp = [&](const char* name, double* out) {
+        const auto& v = *f.find_scalar(name);
+        std::copy(v.begin(), v.end(), out);
+    };
+    cp("rho", rho);
+    cp("rhoTilde", rhoT);
+    cp("K_simp", kSimp);
+    cp("dC_drhoTilde", dCt);
+    return 0;
+}
+
 // ------------------------------------------------------------------ cavity SIMPLE
 // Runs nOuter SIMPLE iterations of the lid-driven cavity on an N x N x 1 grid
 // (extent 1 x 1 x 1/N; zones 1,2,3,5,6 NoSlipWall, zone 4 MovingWall (1,0,0))

@@ -1489,3 +1489,129 @@ void orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int6
     free(den);
     free(pvals);
 }
+
+/* ------------------------------------------------------------------ SIMP topology optimisation */
+
+/*
+ * SimpTopology::apply_helmholtz_filter (src/optimization/SimpTopology.cpp:48-130)
+ * restated on the mesh's CSR pattern (diagonal + interior-face neighbours,
+ * the pattern build_sparsity makes): row c starts with its volume on the
+ * diagonal; every interior face with a = |A| > 0 and d = |C_n - C_o| > 0 adds
+ * coeff = r^2 a / d to both diagonals (face order) and -coeff to both
+ * off-diagonal slots; CG + Jacobi (tol 1e-9, 400 iterations) on b = rho vol;
+ * rhoT = clamp(x, 0, 1).  r == 0 copies rho.
+ */
+static void orc_helmholtz(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                          const double *ay, const double *az, const double *ccx, const double *ccy, const double *ccz,
+                          const double *vol, const int32_t *rowPtr, const int32_t *colIdx, double r, const double *rho,
+                          double *rhoT)
+{
+    if (r <= 0.0) {
+        memcpy(rhoT, rho, (size_t)nC * sizeof(double));
+        return;
+    }
+    const double r2 = r * r;
+    const int64_t nnz = rowPtr[nC];
+    double *values = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
+    for (int64_t k = 0; k < nnz; ++k)
+        values[k] = 0.0;
+    for (int64_t c = 0; c < nC; ++c)
+        values[find_col(rowPtr, colIdx, c, c)] = vol[c];
+    for (int64_t f = 0; f < nF; ++f) {
+        const int64_t o = owner[f], n = neighbor[f];
+        if (n == ORC_BOUNDARY)
+            continue;
+        const double a = sqrt(ax[f] * ax[f] + ay[f] * ay[f] + az[f] * az[f]);
+        const double dx = ccx[n] - ccx[o], dy = ccy[n] - ccy[o], dz = ccz[n] - ccz[o];
+        const double d = sqrt(dx * dx + dy * dy + dz * dz);
+        if (d <= 0 || a <= 0)
+            continue;
+        const double coeff = r2 * a / d;
+        add_at(rowPtr, colIdx, values, o, o, coeff);
+        add_at(rowPtr, colIdx, values, o, n, -coeff);
+        add_at(rowPtr, colIdx, values, n, n, coeff);
+        add_at(rowPtr, colIdx, values, n, o, -coeff);
+    }
+    double *b = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    double *x = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    for (int64_t i = 0; i < nC; ++i)
+        b[i] = rho[i] * vol[i];
+    double last = 0.0;
+    orc_cg(nC, rowPtr, colIdx, values, b, 0, 1e-9, 400, x, &last, NULL);
+    for (int64_t i = 0; i < nC; ++i)
+        rhoT[i] = x[i] < 0.0 ? 0.0 : (1.0 < x[i] ? 1.0 : x[i]);
+    free(values);
+    free(b);
+    free(x);
+}
+
+/*
+ * SimpTopology::step (SimpTopology.cpp:132-227): filter rho -> rhoT;
+ * K = Kmin + (Kmax - Kmin) rhoT^p; the sensitivity through the filter (r > 0:
+ * rho is overwritten with dC and filtered into dCt, as the reference does) or
+ * copied; optimality-criteria update with bisection on the volume
+ * multiplier (at most 64 halvings while (l2 - l1) > 1e-9 (l1 + l2 + 1e-30);
+ * the last halving's candidate is kept).  cfg = {penalty, Kmin, Kmax,
+ * filterRadius, volumeFraction, move, damping, rhoMin}.  Returns
+ * sum |rho_new - rho| / nC (rho as it stands before the update).
+ */
+double orc_simp_step(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                     const double *ay, const double *az, const double *ccx, const double *ccy, const double *ccz,
+                     const double *vol, const int32_t *rowPtr, const int32_t *colIdx, const double *cfg, double *rho,
+                     double *rhoT, double *kSimp, double *dC, double *dCt)
+{
+    const double p = cfg[0], Kmin = cfg[1], Kmax = cfg[2], r = cfg[3], vf = cfg[4], move = cfg[5], damping = cfg[6],
+                 rhoMin = cfg[7];
+    orc_helmholtz(nC, nF, owner, neighbor, ax, ay, az, ccx, ccy, ccz, vol, rowPtr, colIdx, r, rho, rhoT);
+    const double dK = Kmax - Kmin;
+    for (int64_t c = 0; c < nC; ++c)
+        kSimp[c] = Kmin + dK * pow(rhoT[c], p);
+    if (r > 0.0) {
+        for (int64_t c = 0; c < nC; ++c)
+            rho[c] = dC[c];
+        orc_helmholtz(nC, nF, owner, neighbor, ax, ay, az, ccx, ccy, ccz, vol, rowPtr, colIdx, r, rho, rhoT);
+        for (int64_t c = 0; c < nC; ++c)
+            dCt[c] = rhoT[c];
+    } else {
+        for (int64_t c = 0; c < nC; ++c)
+            dCt[c] = dC[c];
+    }
+    double Vtot = 0.0;
+    for (int64_t c = 0; c < nC; ++c)
+        Vtot += vol[c];
+    const double Vtarget = vf * Vtot;
+    double *rhoNew = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    for (int64_t c = 0; c < nC; ++c)
+        rhoNew[c] = 0.0;
+    double l1 = 0.0, l2 = 1e9;
+    for (int it = 0; it < 64 && (l2 - l1) > 1e-9 * (l1 + l2 + 1e-30); ++it) {
+        const double lmid = 0.5 * (l1 + l2);
+        double V = 0.0;
+        for (int64_t c = 0; c < nC; ++c) {
+            const double s = -dCt[c] / STD_MAX(1e-12, lmid);
+            const double bf = pow(STD_MAX(0.0, s), damping);
+            const double old = rho[c];
+            const double lo = STD_MAX(rhoMin, old - move);
+            const double hi = (old + move < 1.0) ? old + move : 1.0; /* std::min(1.0, old + move) */
+            const double t = old * bf;
+            /* std::clamp(t, lo, hi) as the reference's library evaluates it,
+             * min(max(t, lo), hi) -- which also fixes its result when the
+             * move limits cross (lo > hi: hi) */
+            const double mx = t < lo ? lo : t;
+            const double v = hi < mx ? hi : mx;
+            rhoNew[c] = v;
+            V += v * vol[c];
+        }
+        if (V > Vtarget)
+            l1 = lmid;
+        else
+            l2 = lmid;
+    }
+    double change = 0.0;
+    for (int64_t c = 0; c < nC; ++c) {
+        change += fabs(rhoNew[c] - rho[c]);
+        rho[c] = rhoNew[c];
+    }
+    free(rhoNew);
+    return change / (double)nC;
+}

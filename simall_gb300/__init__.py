@@ -11,6 +11,7 @@ from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
 from .fields import DeviceFieldRegistry, checkpoint_read, checkpoint_write
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
 from .simple import GpuSimpleAlgorithm, SimpleOptions, SimpleResiduals
+from .topology import GpuSimpTopology, SimpConfig
 from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
                      Precision, PreconditionerKind, default_context, make_bicgstab, make_cg, make_gmres,
                      make_linear_solver)
@@ -19,4 +20,4 @@ __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallEr
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
            "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals",
-           "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write"]
+           "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write", "GpuSimpTopology", "SimpConfig"]

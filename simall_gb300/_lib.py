@@ -73,6 +73,11 @@ class CheckpointMesh(C.Structure):
                 ("n_cell_faces", _I64)] + [(name, _P) for name, _ in CHECKPOINT_MESH_ARRAYS]
 
 
+class SimpConfig(C.Structure):
+    _fields_ = [("penalty", _D), ("K_min", _D), ("K_max", _D), ("filter_radius", _D), ("volume_fraction", _D),
+                ("move", _D), ("damping", _D), ("rho_min", _D)]
+
+
 class MeshView(C.Structure):
     _fields_ = [("n_cells", _I64), ("n_faces", _I64), ("owner", _P), ("neighbor", _P), ("area_x", _P),
                 ("area_y", _P), ("area_z", _P), ("centroid_x", _P), ("centroid_y", _P), ("centroid_z", _P),
@@ -151,6 +156,10 @@ SIGNATURES = {
     "simall_checkpoint_read": (_I, [C.c_char_p, _P, C.POINTER(CheckpointMeta), C.POINTER(CheckpointMesh)]),
     "simall_checkpoint_mesh_free": (None, [C.POINTER(CheckpointMesh)]),
     "simall_simple_bind_fields": (_I, [_P, _P]),
+    "simall_simp_config_default": (None, [C.POINTER(SimpConfig)]),
+    "simall_simp_create": (_I, [_P, _P, C.POINTER(SimpConfig), C.POINTER(_P)]),
+    "simall_simp_step": (_I, [_P, C.POINTER(_D)]),
+    "simall_simp_destroy": (_I, [_P]),
     "simall_pressure_system_download": (_I, [_P, _P, _P]),
     "simall_solver_use_pressure_system": (_I, [_P, _P]),
     "simall_pressure_system_solve": (_I, [_P, _P, _P, _I, C.POINTER(SolverStats)]),

@@ -8,7 +8,8 @@ renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction / assemble_momentum, CGSolver::solve with
 Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
 preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
-advance_time_step runs, io::Checkpoint::write, solve_discrete_adjoint);
+advance_time_step runs, io::Checkpoint::write, SimpTopology steps,
+solve_discrete_adjoint);
 inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
 
@@ -223,6 +224,24 @@ def checkpoint_case(name):
                                               "cfIdx")})
 
 
+def simp_case(name):
+    """SimpTopology::initialize + three step() calls of the reference on a
+    distorted, RCM-renumbered 7x6x5 box, without and with the Helmholtz filter,
+    for seeded negative sensitivities."""
+    dims = (7, 6, 5)
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=51)
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=True)
+    rng = np.random.default_rng(52)
+    dC = -np.abs(rng.standard_normal((3, rm["nC"]))) * 0.1
+    out = {"dims": np.array(dims), "seed": np.array(51), "dC": dC}
+    for tag, radius in (("r0", 0.0), ("r3", 0.3)):
+        cfg = np.array([3.0, 1e-9, 1.0, radius, 0.4, 0.2, 0.5, 1e-3])
+        ch, rho, rt, K, dct = R.simp_run(rm, cfg, dC)
+        out.update({f"{tag}_cfg": cfg, f"{tag}_change": ch, f"{tag}_rho": rho, f"{tag}_rhoTilde": rt,
+                    f"{tag}_K": K, f"{tag}_dCt": dct})
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -260,6 +279,7 @@ def main():
     for name in SIMPLE_RUNS:
         simple_case(name)
     checkpoint_case("checkpoint_4x3x2")
+    simp_case("simp_7x6x5_rcm.npz")
     print("fixtures written to", HERE)
 
 

@@ -286,3 +286,23 @@ def test_simple_runs_fixture(oracle, name):
     assert np.array_equal(np.array(s.iters), g["iters"])
     assert bits_equal(np.array(res), g["res"])
     assert bits_equal(s.U, g["U"]) and bits_equal(s.p, g["p"]) and bits_equal(s.phi, g["phi"])
+
+
+def test_simp_fixture(oracle):
+    """SimpTopology steps (with and without the filter) reproduce the
+    reference's fields and changes bit for bit."""
+    from simall_gb300 import workloads as W
+
+    g = load("simp_7x6x5_rcm.npz")
+    dims = tuple(int(v) for v in g["dims"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=int(g["seed"])))
+    oracle.rcm(m)
+    for tag in ("r0", "r3"):
+        s = oracle.SimpOracle(m, g[f"{tag}_cfg"])
+        ch = []
+        for k in range(3):
+            s.dC_drho[:] = g["dC"][k]
+            ch.append(s.step())
+        assert bits_equal(np.array(ch), g[f"{tag}_change"])
+        assert bits_equal(s.rho, g[f"{tag}_rho"]) and bits_equal(s.rhoTilde, g[f"{tag}_rhoTilde"])
+        assert bits_equal(s.K_simp, g[f"{tag}_K"]) and bits_equal(s.dC_drhoTilde, g[f"{tag}_dCt"])

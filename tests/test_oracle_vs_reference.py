@@ -244,3 +244,29 @@ def test_simple_outer_iterations(oracle, ref, case):
     assert bits_equal(np.array(res), want["res"])
     assert bits_equal(s.U, want["U"]) and bits_equal(s.p, want["p"]) and bits_equal(s.phi, want["phi"])
     ref.free_mesh(r)
+
+
+@pytest.mark.parametrize("dims,radius,renumber", [((7, 6, 5), 0.0, False), ((7, 6, 5), 0.3, True),
+                                                  ((12, 10, 1), 0.15, False)])
+def test_simp_topology_steps(oracle, ref, dims, radius, renumber):
+    """SimpTopology::initialize + step (filter, penalised property, OC update
+    with bisection): three steps with seeded negative sensitivities, rho,
+    rhoTilde, K_simp, dC_drhoTilde and the change bit-identical."""
+    sh = _shift(dims, 51, 0.2 if dims[2] > 1 else 0.0)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    cfg = (3.0, 1e-9, 1.0, radius, 0.4, 0.2, 0.5, 1e-3)
+    rng = np.random.default_rng(52)
+    dC = -np.abs(rng.standard_normal((3, m.nC))) * 0.1
+    want = ref.simp_run(r, cfg, dC)
+    s = oracle.SimpOracle(m, cfg)
+    changes = []
+    for k in range(3):
+        s.dC_drho[:] = dC[k]
+        changes.append(s.step())
+    assert bits_equal(np.array(changes), want[0])
+    for got, w in zip((s.rho, s.rhoTilde, s.K_simp, s.dC_drhoTilde), want[1:]):
+        assert bits_equal(got, w)
+    ref.free_mesh(r)
