@@ -74,6 +74,8 @@ def parse():
                     help="outer iterations of the device SIMPLE leg (0 disables it)")
     ap.add_argument("--simple-only", action="store_true",
                     help="run only the device SIMPLE leg and print its JSON (profiling runs)")
+    ap.add_argument("--state-only", action="store_true",
+                    help="run only the checkpoint / SIMP leg and print its JSON")
     ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
                     help="skip the error check against a 1e-12 FP64 solve")
     ap.add_argument("--check-interval", type=int, default=0,
@@ -594,14 +596,98 @@ def run_simple(a, ctx, sg, with_cpu):
     return res
 
 
+def run_state(a, ctx, sg, with_cpu):
+    """The device field registry, io::Checkpoint and SIMP on the 128^3 box
+    (RCM): a checkpoint of U (vector) and four scalar fields written from HBM
+    to a file and read back (mesh section without nodes), against writing the
+    same bytes from host memory; one SIMP design step (filter off and on)
+    on the device against the oracle's SimpTopology::step on a 64^3 sample."""
+    import tempfile
+
+    from simall_gb300 import workloads as W
+
+    n = a.poisson_n
+    m, _ = W.poisson3d_mesh(n, seed=SEED)
+    nC = m.n_cells
+    reg = sg.DeviceFieldRegistry(ctx)
+    rng = np.random.default_rng(SEED + 21)
+    reg.upload("U", rng.standard_normal((3, nC)), vector=True)
+    for name in ("p", "T", "k", "rho"):
+        reg.upload(name, rng.standard_normal(nC))
+    mesh = {name: np.zeros(0, dt) for name, dt in sg._lib.CHECKPOINT_MESH_ARRAYS}
+    for k in ("owner", "neighbor", "boundary_zone", "volume", "cell_centroid_x", "cell_centroid_y", "cell_centroid_z",
+              "cell_face_offsets", "cell_face_indices"):
+        mesh[k] = getattr(m, k)
+    for k in ("area_x", "area_y", "area_z", "centroid_x", "centroid_y", "centroid_z"):
+        mesh[k] = getattr(m, k)
+    res = {"workload": f"{n}^3 box: checkpoint of U + 4 scalar fields ({7 * nC * 8 / 1e6:.0f} MB of fields) and the "
+                       "mesh arrays; SIMP design steps", "cells": nC}
+    with tempfile.TemporaryDirectory() as td:
+        path = os.path.join(td, "state.simallcp")
+        sg.checkpoint_write(path, mesh, reg, 1, 0.0, 0)  # warm: page cache, pinned staging
+        t = time.perf_counter()
+        sg.checkpoint_write(path, mesh, reg, 2, 0.0, 0)
+        tw = time.perf_counter() - t
+        size = os.path.getsize(path)
+        reg2 = sg.DeviceFieldRegistry(ctx)
+        sg.checkpoint_read(path, reg2, with_mesh=False)
+        t = time.perf_counter()
+        sg.checkpoint_read(path, reg2, with_mesh=False)
+        tr = time.perf_counter() - t
+        same = bool(np.array_equal(reg2.download("U", vector=True), reg.download("U", vector=True)))
+        reg2.close()
+        host = np.concatenate([reg.download("U", vector=True).ravel()] +
+                              [reg.download(k) for k in ("p", "T", "k", "rho")])
+        t = time.perf_counter()
+        host.tofile(os.path.join(td, "host.bin"))
+        th = time.perf_counter() - t
+    res["checkpoint"] = {"bytes": size, "write_s": round(tw, 4), "write_gbs": round(size / tw / 1e9, 2),
+                         "read_s": round(tr, 4), "read_gbs": round(size / tr / 1e9, 2), "round_trip_exact": same,
+                         "host_fields_write_gbs": round(host.nbytes / th / 1e9, 2)}
+    reg.close()
+    # SIMP design step at 64^3 on the device and in the oracle
+    ns = 64
+    ms, _ = W.poisson3d_mesh(ns, seed=SEED)
+    ps = sg.PressureSystem(ms, W.ALL_WALLS, ctx=ctx)
+    ps.setup_field_loops()
+    dC = -np.abs(rng.standard_normal(ms.n_cells)) * 0.1
+    simp_res = {"cells": int(ms.n_cells)}
+    for tag, radius in (("no_filter", 0.0), ("filter", 1.5 / ns)):
+        r3 = sg.DeviceFieldRegistry(ctx)
+        simp = sg.GpuSimpTopology(ps, r3, sg.SimpConfig(filterRadius=radius))
+        r3.upload("dC_drho", dC)
+        simp.step()  # warm
+        r3.upload("dC_drho", dC)
+        ctx.synchronize()
+        t = time.perf_counter()
+        simp.step()
+        simp_res[tag] = {"value": round(time.perf_counter() - t, 5), "unit": "s per design step"}
+        simp.close()
+        r3.close()
+    ps.close()
+    if with_cpu:
+        from oracle import oracle as O
+        om = O.cartesian_mesh(ns, ns, ns, node_shift=W.interior_node_shift(ns, ns, ns, amp=0.2, seed=SEED))
+        O.rcm(om)
+        so = O.SimpOracle(om, (3.0, 1e-9, 1.0, 0.0, 0.4, 0.2, 0.5, 1e-3))
+        so.dC_drho[:] = dC
+        t = time.perf_counter()
+        so.step()
+        simp_res["cpu_baseline"] = {"value": round(time.perf_counter() - t, 4), "unit": "s per design step",
+                                    "cores": 1, "kind": "port", "sample": "no filter, one step"}
+    res["simp"] = simp_res
+    return res
+
+
 def run_ours(a, rank, world, local):
     import torch
-    if a.simple_only:
+    if a.simple_only or a.state_only:
         import simall_gb300 as sg
         sg.build.build()
         sg.load()
         ctx = sg.Context(local)
-        print(json.dumps({"simple": run_simple(a, ctx, sg, not a.no_cpu_baseline)}), flush=True)
+        leg = ("simple", run_simple) if a.simple_only else ("state", run_state)
+        print(json.dumps({leg[0]: leg[1](a, ctx, sg, not a.no_cpu_baseline)}), flush=True)
         return
 
     import simall_gb300 as sg
@@ -753,6 +839,8 @@ def run_ours(a, rank, world, local):
         out["cavity"] = run_cavity(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if a.simple_iterations > 0:
         out["simple"] = run_simple(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
+    if a.poisson_n > 0:
+        out["state"] = run_state(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
         out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,

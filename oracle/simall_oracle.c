@@ -1534,6 +1534,7 @@ static void orc_helmholtz(int64_t nC, int64_t nF, const int64_t *owner, const in
     }
     double *b = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
     double *x = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
+    memset(b, 0, (size_t)nC * sizeof(double) + 8);
     for (int64_t i = 0; i < nC; ++i)
         b[i] = rho[i] * vol[i];
     double last = 0.0;
