@@ -764,9 +764,19 @@ def run_ours(a, rank, world, local):
           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 200^3 capture scaled by rows",
           "peak_source": f"{peak_kind} hbm_gbs"}
 
-    # e2e: C ABI with host buffers (matrix + b in, x out, setup inside)
-    rp, ci = ps.pattern()
-    vals, _ = ps.download()
+    # e2e: C ABI with host buffers (matrix + b in, x out, setup inside); the
+    # host arrays are pinned, as the contract's end-to-end step asks
+    rp_, ci_ = ps.pattern()
+    vals_, _ = ps.download()
+
+    def pinned(arr):
+        t = torch.empty(arr.shape, dtype=getattr(torch, str(arr.dtype)), pin_memory=True)
+        v = t.numpy()
+        v[...] = arr
+        return v
+
+    rp, ci, vals = pinned(rp_), pinned(ci_), pinned(vals_)
+    rhs = pinned(np.ascontiguousarray(rhs))
     e2e_s, h2d, d2h = None, 0, 0
     if a.e2e_steps > 0:
         e2e_solver = sg.GpuCGSolver(sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG,
@@ -774,7 +784,7 @@ def run_ours(a, rank, world, local):
                                                           tolerance=a.tol, maxIterations=a.max_iterations),
                                     precision=sg.Precision.MIXED, ctx=ctx)
         A = sg.CSRMatrix(rp, ci, vals)
-        xh = np.zeros(len(rhs))
+        xh = pinned(np.zeros(len(rhs)))
         e2e_solver.solve(A, rhs, xh)  # warm
         barrier()
         t = time.perf_counter()
