@@ -211,14 +211,18 @@ class GpuCGSolver:
         bb = np.ascontiguousarray(b, np.float64)
         if len(bb) != n:
             raise SimallError(8, "b size")
-        out = np.empty(n, np.float64)
+        # the library writes x directly when the caller's array can take it (no temporary, no copy)
+        direct = (isinstance(x, np.ndarray) and x.dtype == np.float64 and x.shape == (n,)
+                  and x.flags["C_CONTIGUOUS"] and x.flags["WRITEABLE"])
+        out = x if direct else np.empty(n, np.float64)
         st = self.L.simall_solver_solve_csr(self.handle, n, len(ci), rp.ctypes.data, ci.ctypes.data,
                                             va.ctypes.data, bb.ctypes.data, out.ctypes.data, C.byref(self.stats))
         check(st, self.ctx.handle)
-        if isinstance(x, np.ndarray) and x.shape == out.shape:
-            x[...] = out
-        elif isinstance(x, list):
-            x[:] = out.tolist()
+        if not direct:
+            if isinstance(x, np.ndarray) and x.shape == out.shape:
+                x[...] = out
+            elif isinstance(x, list):
+                x[:] = out.tolist()
         return int(self.stats.iterations)
 
     def last_residual(self) -> float:
