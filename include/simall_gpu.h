@@ -321,11 +321,21 @@ typedef struct simall_simple_options {
     double dt;                  /* > 0: transient (advance_time_step) */
     int bdf2;                   /* TemporalScheme::BDF2 (else implicit Euler) */
     int simplec;                /* PvCouplingVariant::SIMPLEC (else SIMPLE) */
+    /* PisoAlgorithm / PimpleAlgorithm (src/solver/PisoAlgorithm.cpp:27-70,
+     * PimpleAlgorithm.cpp:48-96): the defaults 1, 1, 0, 1, 0, 0 are SIMPLE;
+     * PISO is n_correctors >= 1 with urfU = urfP = 1. */
+    int n_outer_correctors;     /* outer correctors per iterate() */
+    int n_correctors;           /* pressure correctors per outer corrector */
+    int n_non_orth_corr;        /* extra pressure passes per corrector */
+    int momentum_predictor;     /* 0: no momentum solve (needs a previous one's aP) */
+    double tol_u, tol_p;        /* outer-loop early exit when every set tolerance holds (0 disables) */
 } simall_simple_options;
 typedef struct simall_simple_residuals {
     double mom[3];     /* |A U_k - b| of each momentum solve (SimpleResiduals::mom) */
-    double cont;       /* |rhs| of the pressure-correction system (SimpleResiduals::cont) */
-    int iterations[4]; /* the momentum x, y, z and pressure solves' counts */
+    double cont;       /* |rhs| of the last pressure-correction system (SimpleResiduals::cont) */
+    int iterations[4]; /* the last momentum x, y, z and pressure solves' counts */
+    int outer;         /* index of the last outer corrector run (PimpleAlgorithm::last_outer_iters) */
+    int reserved;
 } simall_simple_residuals;
 typedef struct simall_simple simall_simple;
 typedef struct simall_fields simall_fields; /* the field registry, below */

@@ -6,6 +6,7 @@
 # Reference files compiled (paths inside the reference tree):
 #   src/solver/LinearSolvers.cpp   (see the one patch below)
 #   src/solver/AMGPreconditioner.cpp, src/solver/SimpleAlgorithm.cpp,
+#   src/solver/PisoAlgorithm.cpp, src/solver/PimpleAlgorithm.cpp,
 #   src/solver/Gradient.cpp, src/meshing/MeshStorage.cpp,
 #   src/meshing/CartesianMesher.cpp, src/meshing/Connectivity.cpp,
 #   src/meshing/MeshOps.cpp, src/meshing/MeshQuality.cpp,
@@ -37,6 +38,8 @@ FLAGS="-std=c++20 -O3 -fPIC -ffp-contract=off -w -Wno-psabi -I$REF/src -I$REF"
 SRCS="$OUT/LinearSolvers_patched.cpp
 $REF/src/solver/AMGPreconditioner.cpp
 $REF/src/solver/SimpleAlgorithm.cpp
+$REF/src/solver/PisoAlgorithm.cpp
+$REF/src/solver/PimpleAlgorithm.cpp
 $REF/src/solver/Gradient.cpp
 $REF/src/meshing/MeshStorage.cpp
 $REF/src/meshing/CartesianMesher.cpp

@@ -91,9 +91,9 @@ def lib():
         L.orc_bicgstab.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
         L.orc_gmres.restype = C.c_int
         L.orc_gmres.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, C.c_int, _P, _P]
-        L.orc_simple_iterate.restype = None
+        L.orc_simple_iterate.restype = C.c_int
         L.orc_simple_iterate.argtypes = [_I64, _I64] + [_P] * 16 + [C.c_int] + [_P] * 3 + [C.c_int, _P, _D, _P, _D] + \
-            [_P] * 9
+            [_P] * 11
         L.orc_simp_step.restype = _D
         L.orc_simp_step.argtypes = [_I64, _I64] + [_P] * 17
         _lib = L
@@ -388,7 +388,11 @@ class SimpleOracle:
     (kind, precond, tol, maxIt, restart)."""
 
     def __init__(self, m: Mesh, bcs, rho=1.0, mu=1e-3, urfU=0.7, urfP=0.3, dt=0.0, bdf2=False, simplec=False,
-                 mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30)):
+                 mom_cfg=(0, 1, 1e-6, 200, 30), p_cfg=(2, 0, 1e-8, 1000, 30), n_outer_correctors=1, n_correctors=1,
+                 n_non_orth_corr=0, momentum_predictor=True, tol_u=0.0, tol_p=0.0):
+        """SIMPLE by default; PISO: n_correctors >= 1 with urfU = urfP = 1
+        (PisoAlgorithm::to_simple_opts); PIMPLE: n_outer_correctors,
+        n_correctors, momentum_predictor, tol_u / tol_p."""
         self.m = m
         self.nZ, self.zt, self.zv = _zone_tables(bcs)
         self.isP = np.zeros(self.nZ, np.uint8)
@@ -409,6 +413,10 @@ class SimpleOracle:
         self.Unm1 = np.zeros((3, m.nC))
         self.time_step = 0
         self.iters = []  # every iterate()'s four solve counts
+        self.loops = np.array([n_outer_correctors, n_correctors, n_non_orth_corr, int(bool(momentum_predictor))],
+                              np.int32)
+        self.tol_up = np.array([tol_u, tol_p], np.float64)
+        self.last_outer = 0
 
     def iterate(self):
         """One outer iteration; returns (res[4] = mom x, y, z, cont, iters[4])."""
@@ -419,11 +427,12 @@ class SimpleOracle:
         pc = np.array([self.p_cfg[0], self.p_cfg[1], self.p_cfg[3], self.p_cfg[4]], np.int32)
         use_bdf2 = self.opt[4] > 0.0 and self.bdf2 and self.time_step >= 1
         flags = (1 if use_bdf2 else 0) | (2 if self.simplec else 0)
-        lib().orc_simple_iterate(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
+        self.last_outer = lib().orc_simple_iterate(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
                                  _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.ccx), _ptr(m.ccy), _ptr(m.ccz),
                                  _ptr(m.vol), _ptr(m.zone), _ptr(self.zt), _ptr(self.zv), _ptr(self.isP), self.nZ,
                                  _ptr(self.rp), _ptr(self.ci), _ptr(self.opt), flags, _ptr(mc),
-                                 float(self.mom_cfg[2]), _ptr(pc), float(self.p_cfg[2]), _ptr(self.U), _ptr(self.p),
+                                 float(self.mom_cfg[2]), _ptr(pc), float(self.p_cfg[2]), _ptr(self.loops),
+                                 _ptr(self.tol_up), _ptr(self.U), _ptr(self.p),
                                  _ptr(self.Un), _ptr(self.Unm1), _ptr(self.phi), _ptr(self.aP), _ptr(self.pPrime),
                                  _ptr(res), _ptr(its))
         self.iters.append(its)
@@ -546,6 +555,9 @@ class RefLib:
         L.ref_checkpoint_field.argtypes = [C.c_char_p, C.c_int, _P]
         L.ref_simp_run.restype = C.c_int
         L.ref_simp_run.argtypes = [_P, _P, C.c_int] + [_P] * 6
+        L.ref_piso_pimple_run.restype = C.c_int
+        L.ref_piso_pimple_run.argtypes = [_P, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _D, _P, _D,
+                                          C.c_int] + [_P] * 5
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -787,6 +799,29 @@ class RefLib:
         self.L.ref_simp_run(mesh_dict["handle"], _ptr(np.ascontiguousarray(cfg, np.float64)), k, _ptr(dC),
                             _ptr(change), *(_ptr(o) for o in out))
         return (change, *out)
+
+    def piso_pimple_run(self, mesh_dict, variant, bcs, U, p, n_steps, rho=1.0, mu=1e-3, dt=1e-3, urfU=0.7,
+                        urfP=0.3, tol_u=0.0, tol_p=0.0, loops=(2, 2, 0, 1), bdf2=True,
+                        mom_cfg=(0, 0, 1e-9, 200, 30), p_cfg=(2, 0, 1e-9, 1000, 30)):
+        """PisoAlgorithm (variant 1) or PimpleAlgorithm (variant 2):
+        n_steps advance_time_step(1) calls; returns dict U, p, phi, res, last_outer."""
+        nC, nF = mesh_dict["nC"], mesh_dict["nF"]
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        vec = np.array([list(b[2]) if len(b) > 2 else [0, 0, 0] for b in bcs] or [[0, 0, 0]], np.float64).ravel()
+        U = np.array(U, np.float64).reshape(3, nC).copy()
+        p = np.array(p, np.float64).copy()
+        phi = np.empty(nF)
+        res = np.empty((n_steps, 4))
+        lo = np.zeros(n_steps, np.int32)
+        opt = np.array([rho, mu, dt, urfU, urfP, tol_u, tol_p], np.float64)
+        mc = np.array([mom_cfg[0], mom_cfg[1], mom_cfg[3], mom_cfg[4]], np.int32)
+        pc = np.array([p_cfg[0], p_cfg[1], p_cfg[3], p_cfg[4]], np.int32)
+        self.L.ref_piso_pimple_run(mesh_dict["handle"], int(variant), len(bcs), _ptr(zones), _ptr(types), _ptr(vec),
+                                   _ptr(opt), _ptr(np.array(loops, np.int32)), int(bool(bdf2)), _ptr(mc),
+                                   float(mom_cfg[2]), _ptr(pc), float(p_cfg[2]), int(n_steps), _ptr(U), _ptr(p),
+                                   _ptr(phi), _ptr(res), _ptr(lo))
+        return {"U": U, "p": p, "phi": phi, "res": res, "last_outer": lo}
 
     # -- solvers
     def cg(self, rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):

@@ -11,6 +11,7 @@
 //   SimpleAlgorithm::build_sparsity         src/solver/SimpleAlgorithm.cpp:49
 //   SimpleAlgorithm::assemble_pressure_correction  src/solver/SimpleAlgorithm.cpp:358
 //   SimpleAlgorithm::iterate                src/solver/SimpleAlgorithm.cpp:522
+//   PisoAlgorithm::iterate, PimpleAlgorithm::iterate  src/solver/PisoAlgorithm.cpp:27, PimpleAlgorithm.cpp:48
 //   make_cg / make_gmres / make_preconditioner     src/solver/LinearSolvers.cpp:240,462
 //   adjoint::solve_discrete_adjoint         src/adjoint/DiscreteAdjoint.cpp:150
 //   core::PluginLoader::load / PluginRegistry  src/core/PluginLoader.cpp:68, PluginRegistry.cpp:23
@@ -27,6 +28,8 @@
 #include "solver/FieldRegistry.hpp"
 #include "solver/Gradient.hpp"
 #include "solver/LinearSolvers.hpp"
+#include "solver/PimpleAlgorithm.hpp"
+#include "solver/PisoAlgorithm.hpp"
 #include "solver/SimpleAlgorithm.hpp"
 
 #include <algorithm>
@@ -601,6 +604,92 @@ int ref_simple_run(void* h, int nbc, const std::uint32_t* bcZones, const int* bc
     *nIters = static_cast<int>(all.size());
     for (int i = 0; i < static_cast<int>(all.size()) && i < maxIters; ++i)
         iters[i] = all[i];
+    return 0;
+}
+
+// PisoAlgorithm / PimpleAlgorithm with the face fluxes readable.
+class PisoProbe : public S::PisoAlgorithm
+{
+public:
+    using S::PisoAlgorithm::PisoAlgorithm;
+    const Vec& phi() const { return phiFlux_; }
+};
+class PimpleProbe : public S::PimpleAlgorithm
+{
+public:
+    using S::PimpleAlgorithm::PimpleAlgorithm;
+    const Vec& phi() const { return phiFlux_; }
+};
+
+// PisoAlgorithm (variant 1) or PimpleAlgorithm (variant 2) on the given mesh
+// from U, p: nSteps calls of advance_time_step(1).  opt = {rho, mu, dt, urfU,
+// urfP, tolU, tolP}; loops = {nOuterCorrectors, nCorrectors, nNonOrthCorr,
+// momentumPredictor}; flags bit 0 BDF2 (else ImplicitEuler).  Out as
+// ref_simple_run, plus lastOuter[k] (PIMPLE's last_outer_iters after step k).
+int ref_piso_pimple_run(void* h, int variant, int nbc, const std::uint32_t* bcZones, const int* bcTypes,
+                        const double* bcVec, const double* opt, const int* loops, int flags, const int* momCfg,
+                        double momTol, const int* pCfg, double pTol, int nSteps, double* U, double* p, double* phi,
+                        double* res, int* lastOuter)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    const std::size_t nC = m.cells().size();
+    S::FieldRegistry f;
+    auto& Uf = f.vector("U", nC);
+    Uf.x.assign(U, U + nC);
+    Uf.y.assign(U + nC, U + 2 * nC);
+    Uf.z.assign(U + 2 * nC, U + 3 * nC);
+    f.scalar("p", nC).assign(p, p + nC);
+    auto bcs = make_bcs_vec(nbc, bcZones, bcTypes, bcVec);
+    auto mom = make_kind(momCfg, momTol);
+    auto pres = make_kind(pCfg, pTol);
+    const auto scheme = (flags & 1) ? S::TemporalScheme::BDF2 : S::TemporalScheme::ImplicitEuler;
+    std::unique_ptr<S::SimpleAlgorithm> alg;
+    const Vec* phiRef = nullptr;
+    PimpleProbe* pimple = nullptr;
+    if (variant == 1) {
+        S::PisoOptions o;
+        o.nCorrectors = loops[1];
+        o.nNonOrthCorr = loops[2];
+        o.rho = opt[0];
+        o.mu = opt[1];
+        o.dt = opt[2];
+        o.timeScheme = scheme;
+        auto* a = new PisoProbe(m, f, bcs, *mom, *pres, o);
+        phiRef = &a->phi();
+        alg.reset(a);
+    } else {
+        S::PimpleOptions o;
+        o.nOuterCorrectors = loops[0];
+        o.nCorrectors = loops[1];
+        o.nNonOrthCorr = loops[2];
+        o.momentumPredictor = loops[3] != 0;
+        o.urfU = opt[3];
+        o.urfP = opt[4];
+        o.tolU = opt[5];
+        o.tolP = opt[6];
+        o.rho = opt[0];
+        o.mu = opt[1];
+        o.dt = opt[2];
+        o.timeScheme = scheme;
+        pimple = new PimpleProbe(m, f, bcs, *mom, *pres, o);
+        phiRef = &pimple->phi();
+        alg.reset(pimple);
+    }
+    for (int k = 0; k < nSteps; ++k) {
+        const S::SimpleResiduals r = alg->advance_time_step(1);
+        res[4 * k] = r.mom[0];
+        res[4 * k + 1] = r.mom[1];
+        res[4 * k + 2] = r.mom[2];
+        res[4 * k + 3] = r.cont;
+        lastOuter[k] = pimple ? pimple->last_outer_iters() : 0;
+    }
+    auto& Uo = *f.find_vector("U");
+    std::copy(Uo.x.begin(), Uo.x.end(), U);
+    std::copy(Uo.y.begin(), Uo.y.end(), U + nC);
+    std::copy(Uo.z.begin(), Uo.z.end(), U + 2 * nC);
+    const auto& pp = *f.find_scalar("p");
+    std::copy(pp.begin(), pp.end(), p);
+    std::copy(phiRef->begin(), phiRef->end(), phi);
     return 0;
 }
 

@@ -1416,29 +1416,39 @@ static int orc_linear_solve(const int *cfg, double tol, int64_t n, const int32_t
 }
 
 /*
- * SimpleAlgorithm::iterate (src/solver/SimpleAlgorithm.cpp:522-547), no
- * periodic faces, no halo exchange:
- *   compute_face_fluxes; for k in x, y, z: assemble_momentum(k), solve it from
- *   x = 0 into U_k, res.mom[k] = |A U_k - b|; compute_face_fluxes again;
+ * SimpleAlgorithm::iterate (src/solver/SimpleAlgorithm.cpp:522-547) and the
+ * iterate() overrides of PisoAlgorithm (src/solver/PisoAlgorithm.cpp:27-70)
+ * and PimpleAlgorithm (src/solver/PimpleAlgorithm.cpp:48-96), no periodic
+ * faces, no halo exchange.  loops = {nOuterCorrectors, nCorrectors,
+ * nNonOrthCorr, momentumPredictor} (SIMPLE: {1, 1, 0, 1}); tolUP = {tolU,
+ * tolP} (PIMPLE's early exit, 0 disables).  Per outer corrector:
+ *   compute_face_fluxes; if momentumPredictor: for k in x, y, z:
+ *   assemble_momentum(k), solve it from x = 0 into U_k, res.mom[k] = |A U_k - b|;
+ *   nCorrectors times { compute_face_fluxes; nNonOrthCorr + 1 times {
  *   assemble_pressure_correction (SIMPLEC: the denominator from the momentum
- *   matrix); solve p' from 0; res.cont = |rhs|; correct_fields.
+ *   matrix); solve p' from 0; correct_fields; the last pass's |rhs| is
+ *   res.cont } }; then stop when both tolerances that are set hold.
  * opt = {rho, mu, urfU, urfP, dt}; flags bit 0 BDF2 (the transient term uses
  * Un and Unm1), bit 1 SIMPLEC.  momCfg / pCfg = {kind, precond, maxIt,
- * restart}.  U [3][nC], p [nC] in/out; phi [nF], aP [nC], pPrime [nC] out;
- * res [4] = mom x, y, z and cont; iters [4] the four solves' counts.
+ * restart}.  U [3][nC], p [nC] in/out; phi [nF], aP [nC] (in/out: kept from
+ * the last predictor), pPrime [nC] out; res [4] = mom x, y, z and cont;
+ * iters [4] the last momentum solves' and the last pressure solve's counts.
+ * Returns the index of the last outer corrector run.
  * isPressure[z] marks zones with a PressureOutlet / PressureInlet spec.
  */
-void orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
-                        const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
-                        const double *ccx, const double *ccy, const double *ccz, const double *vol,
-                        const uint32_t *zone, const int *zoneType, const double *zoneVec, const uint8_t *isPressure,
-                        int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int flags,
-                        const int *momCfg, double momTol, const int *pCfg, double pTol, double *U, double *p,
-                        const double *Un, const double *Unm1, double *phi, double *aP, double *pPrime, double *res,
-                        int *iters)
+int orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax,
+                       const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
+                       const double *ccx, const double *ccy, const double *ccz, const double *vol,
+                       const uint32_t *zone, const int *zoneType, const double *zoneVec, const uint8_t *isPressure,
+                       int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int flags,
+                       const int *momCfg, double momTol, const int *pCfg, double pTol, const int *loops,
+                       const double *tolUP, double *U, double *p, const double *Un, const double *Unm1, double *phi,
+                       double *aP, double *pPrime, double *res, int *iters)
 {
     const double rho = opt[0], mu = opt[1], urfU = opt[2], urfP = opt[3], dt = opt[4];
     const int bdf2 = flags & 1, simplec = (flags >> 1) & 1;
+    const int nOuter = loops[0] < 1 ? 1 : loops[0], nCorr = loops[1] < 1 ? 1 : loops[1];
+    const int nNonOrth = loops[2] < 0 ? 0 : loops[2], predictor = loops[3];
     const int64_t nnz = rowPtr[nC];
     double *values = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
     double *rhs = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
@@ -1446,41 +1456,66 @@ void orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int6
     double *g = (double *)xmalloc((size_t)(3 * nC) * sizeof(double) + 8);
     double *mInv = (double *)xmalloc((size_t)(6 * nC) * sizeof(double) + 8);
     double *den = (double *)xmalloc((size_t)nC * sizeof(double) + 8);
-    const double momOpt[4] = {rho, mu, urfU, dt};
-    orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC, phi);
-    orc_lsq_inverse(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv);
-    orc_lsq_gradient(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv, p, g, g + nC, g + 2 * nC);
-    for (int k = 0; k < 3; ++k) {
-        orc_assemble_momentum(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, zone, zoneType,
-                              zoneVec, nZones, rowPtr, colIdx, momOpt, bdf2, k, phi, g + k * nC, U + k * nC,
-                              Un ? Un + k * nC : NULL, Unm1 ? Unm1 + k * nC : NULL, values, rhs,
-                              k == 0 ? aP : NULL);
-        double last = 0.0;
-        iters[k] = orc_linear_solve(momCfg, momTol, nC, rowPtr, colIdx, values, rhs, U + k * nC, &last);
-        orc_spmv(nC, rowPtr, colIdx, values, U + k * nC, Ax);
-        double s = 0.0;
-        for (int64_t i = 0; i < nC; ++i) {
-            const double d = Ax[i] - rhs[i];
-            s += d * d;
-        }
-        res[k] = sqrt(s);
-    }
-    orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC, phi);
-    if (simplec)
-        orc_simplec_denominator(nC, rowPtr, colIdx, values, aP, den);
     double *pvals = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
-    orc_assemble(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, zone, ccx, ccy, ccz, isPressure, nZones, rho,
-                 simplec ? den : aP, phi, rowPtr, colIdx, pvals, rhs);
-    {
-        double last = 0.0;
-        iters[3] = orc_linear_solve(pCfg, pTol, nC, rowPtr, colIdx, pvals, rhs, pPrime, &last);
-        double cs = 0.0;
-        for (int64_t i = 0; i < nC; ++i)
-            cs += rhs[i] * rhs[i];
-        res[3] = sqrt(cs);
+    const double momOpt[4] = {rho, mu, urfU, dt};
+    orc_lsq_inverse(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv);
+    for (int k = 0; k < 4; ++k)
+        res[k] = 0.0;
+    int outer;
+    for (outer = 0; outer < nOuter; ++outer) {
+        orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC,
+                        phi);
+        if (predictor) {
+            orc_lsq_gradient(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv, p, g, g + nC, g + 2 * nC);
+            for (int k = 0; k < 3; ++k) {
+                orc_assemble_momentum(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, zone,
+                                      zoneType, zoneVec, nZones, rowPtr, colIdx, momOpt, bdf2, k, phi, g + k * nC,
+                                      U + k * nC, Un ? Un + k * nC : NULL, Unm1 ? Unm1 + k * nC : NULL, values, rhs,
+                                      k == 0 ? aP : NULL);
+                double last = 0.0;
+                iters[k] = orc_linear_solve(momCfg, momTol, nC, rowPtr, colIdx, values, rhs, U + k * nC, &last);
+                orc_spmv(nC, rowPtr, colIdx, values, U + k * nC, Ax);
+                double s = 0.0;
+                for (int64_t i = 0; i < nC; ++i) {
+                    const double d = Ax[i] - rhs[i];
+                    s += d * d;
+                }
+                res[k] = sqrt(s);
+            }
+        }
+        for (int corr = 0; corr < nCorr; ++corr) {
+            orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC,
+                            U + 2 * nC, phi);
+            for (int no = 0; no <= nNonOrth; ++no) {
+                if (simplec)
+                    orc_simplec_denominator(nC, rowPtr, colIdx, values, aP, den);
+                orc_assemble(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, zone, ccx, ccy, ccz, isPressure,
+                             nZones, rho, simplec ? den : aP, phi, rowPtr, colIdx, pvals, rhs);
+                double last = 0.0;
+                iters[3] = orc_linear_solve(pCfg, pTol, nC, rowPtr, colIdx, pvals, rhs, pPrime, &last);
+                double cs = 0.0;
+                for (int64_t i = 0; i < nC; ++i)
+                    cs += rhs[i] * rhs[i];
+                res[3] = sqrt(cs);
+                orc_correct_fields(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, rho, urfP,
+                                   aP, pPrime, p, U, U + nC, U + 2 * nC, phi);
+            }
+        }
+        /* PimpleAlgorithm's converged(): every set tolerance holds */
+        const double tolU = tolUP[0], tolP = tolUP[1];
+        int conv = (tolU > 0.0) || (tolP > 0.0);
+        if (tolU > 0.0) {
+            double mm = fabs(res[0]);
+            mm = STD_MAX(mm, fabs(res[1]));
+            mm = STD_MAX(mm, fabs(res[2]));
+            if (mm > tolU)
+                conv = 0;
+        }
+        if (tolP > 0.0 && fabs(res[3]) > tolP)
+            conv = 0;
+        if (conv)
+            break;
     }
-    orc_correct_fields(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, rho, urfP, aP, pPrime, p,
-                       U, U + nC, U + 2 * nC, phi);
     free(values);
     free(rhs);
     free(Ax);
@@ -1488,6 +1523,7 @@ void orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int6
     free(mInv);
     free(den);
     free(pvals);
+    return outer < nOuter ? outer : nOuter - 1;
 }
 
 /* ------------------------------------------------------------------ SIMP topology optimisation */

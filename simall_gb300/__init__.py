@@ -10,7 +10,7 @@ from .batch import BatchedSolver
 from ._lib import MEM_DEVICE, MEM_HOST, SimallError, load
 from .fields import DeviceFieldRegistry, checkpoint_read, checkpoint_write
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
-from .simple import GpuSimpleAlgorithm, SimpleOptions, SimpleResiduals
+from .simple import GpuSimpleAlgorithm, PimpleOptions, PisoOptions, SimpleOptions, SimpleResiduals
 from .topology import GpuSimpTopology, SimpConfig
 from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
                      Precision, PreconditionerKind, default_context, make_bicgstab, make_cg, make_gmres,
@@ -19,5 +19,6 @@ from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSol
 __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
-           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals",
+           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals", "PisoOptions",
+           "PimpleOptions",
            "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write", "GpuSimpTopology", "SimpConfig"]

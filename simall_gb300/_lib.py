@@ -49,11 +49,13 @@ class MomentumOptions(C.Structure):
 
 
 class SimpleOptions(C.Structure):
-    _fields_ = [("urfU", _D), ("urfP", _D), ("rho", _D), ("mu", _D), ("dt", _D), ("bdf2", _I), ("simplec", _I)]
+    _fields_ = [("urfU", _D), ("urfP", _D), ("rho", _D), ("mu", _D), ("dt", _D), ("bdf2", _I), ("simplec", _I),
+                ("n_outer_correctors", _I), ("n_correctors", _I), ("n_non_orth_corr", _I),
+                ("momentum_predictor", _I), ("tol_u", _D), ("tol_p", _D)]
 
 
 class SimpleResiduals(C.Structure):
-    _fields_ = [("mom", _D * 3), ("cont", _D), ("iterations", _I * 4)]
+    _fields_ = [("mom", _D * 3), ("cont", _D), ("iterations", _I * 4), ("outer", _I), ("reserved", _I)]
 
 
 class CheckpointMeta(C.Structure):

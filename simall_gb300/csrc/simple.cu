@@ -1,7 +1,10 @@
 // One SIMPLE outer iteration with every field in device memory: the GB300
 // replacement of SimpleAlgorithm::iterate and ::advance_time_step
-// (src/solver/SimpleAlgorithm.cpp:522-570), no periodic faces, no halo
-// exchange (one GPU).
+// (src/solver/SimpleAlgorithm.cpp:522-570) and of the PISO and PIMPLE
+// iterate() overrides (src/solver/PisoAlgorithm.cpp:27-70,
+// PimpleAlgorithm.cpp:48-96: outer correctors, pressure correctors,
+// non-orthogonal passes, optional momentum predictor, early exit), no
+// periodic faces, no halo exchange (one GPU).
 //
 //   compute_face_fluxes           simall_compute_face_fluxes
 //   assemble_momentum(x, y, z)    simall_assemble_momentum, all three at once:
@@ -23,6 +26,7 @@
 #include "registry.hpp"
 #include "solver.hpp"
 
+#include <cmath>
 #include <new>
 
 struct simall_simple {
@@ -73,6 +77,12 @@ void simall_simple_options_default(simall_simple_options *o)
     o->dt = 0.0;
     o->bdf2 = 0;
     o->simplec = 0;
+    o->n_outer_correctors = 1;
+    o->n_correctors = 1;
+    o->n_non_orth_corr = 0;
+    o->momentum_predictor = 1;
+    o->tol_u = 0.0;
+    o->tol_p = 0.0;
 }
 
 int simall_simple_create(simall_pressure_system *ps, simall_solver *momentum, simall_solver *pressure,
@@ -92,6 +102,10 @@ int simall_simple_create(simall_pressure_system *ps, simall_solver *momentum, si
         o = *opt;
     if (!(o.urfU != 0.0) || !(o.rho == o.rho) || !(o.dt >= 0.0))
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "SIMPLE: urfU must be non-zero and dt >= 0");
+    // the clamps of PimpleAlgorithm's constructor (PimpleAlgorithm.cpp:23-29)
+    o.n_outer_correctors = o.n_outer_correctors < 1 ? 1 : o.n_outer_correctors;
+    o.n_correctors = o.n_correctors < 1 ? 1 : o.n_correctors;
+    o.n_non_orth_corr = o.n_non_orth_corr < 0 ? 0 : o.n_non_orth_corr;
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     auto *s = new (std::nothrow) simall_simple;
     if (!s)
@@ -218,48 +232,76 @@ int simall_simple_iterate(simall_simple *s, simall_simple_residuals *res)
     const simall_simple_options &o = s->o;
     double *U = s->Ud();
     simall_simple_residuals r{};
-    int e = simall_compute_face_fluxes(ps, o.rho, U, U + nC, U + 2 * nC, s->phi.p, SIMALL_MEM_DEVICE);
-    if (e)
-        return e;
-    simall_momentum_options mo;
-    mo.rho = o.rho;
-    mo.mu = o.mu;
-    mo.urfU = o.urfU;
-    mo.dt = o.dt;
-    mo.bdf2 = (o.dt > 0.0 && o.bdf2 && s->timeStep >= 1) ? 1 : 0;  // BDF2 from the second step (:335)
-    mo.reserved = 0;
-    e = simall_assemble_momentum(ps, &mo, U, s->Pd(), s->phi.p, s->Un.p, s->Unm1.p, SIMALL_MEM_DEVICE);
-    if (e)
-        return e;
-    e = simall_solver_set_matrix(s->mom, nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->mvalues.p, SIMALL_MEM_DEVICE);
-    if (e)
-        return e;
-    for (int k = 0; k < 3; ++k) {
-        simall_solver_stats st{};
-        e = solver_solve_impl(s->mom, ps->mrhs.p + k * nC, SIMALL_MEM_DEVICE, U + k * nC, SIMALL_MEM_DEVICE, &st);
+    int outer = 0;
+    for (outer = 0; outer < o.n_outer_correctors; ++outer) {
+        int e = simall_compute_face_fluxes(ps, o.rho, U, U + nC, U + 2 * nC, s->phi.p, SIMALL_MEM_DEVICE);
         if (e)
             return e;
-        r.mom[k] = st.true_residual * st.b_norm;  // |A U_k - b|
-        r.iterations[k] = st.iterations;
+        if (o.momentum_predictor) {
+            simall_momentum_options mo;
+            mo.rho = o.rho;
+            mo.mu = o.mu;
+            mo.urfU = o.urfU;
+            mo.dt = o.dt;
+            mo.bdf2 = (o.dt > 0.0 && o.bdf2 && s->timeStep >= 1) ? 1 : 0;  // BDF2 from the second step (:335)
+            mo.reserved = 0;
+            e = simall_assemble_momentum(ps, &mo, U, s->Pd(), s->phi.p, s->Un.p, s->Unm1.p, SIMALL_MEM_DEVICE);
+            if (e)
+                return e;
+            e = simall_solver_set_matrix(s->mom, nC, ps->nnz, ps->rowPtr.p, ps->colIdx.p, ps->mvalues.p,
+                                         SIMALL_MEM_DEVICE);
+            if (e)
+                return e;
+            for (int k = 0; k < 3; ++k) {
+                simall_solver_stats st{};
+                e = solver_solve_impl(s->mom, ps->mrhs.p + k * nC, SIMALL_MEM_DEVICE, U + k * nC, SIMALL_MEM_DEVICE,
+                                      &st);
+                if (e)
+                    return e;
+                r.mom[k] = st.true_residual * st.b_norm;  // |A U_k - b|
+                r.iterations[k] = st.iterations;
+            }
+        } else if (!ps->momReady) {
+            return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "SIMPLE: no momentum predictor has run to provide aP");
+        }
+        for (int corr = 0; corr < o.n_correctors; ++corr) {
+            e = simall_compute_face_fluxes(ps, o.rho, U, U + nC, U + 2 * nC, s->phi.p, SIMALL_MEM_DEVICE);
+            if (e)
+                return e;
+            for (int no = 0; no <= o.n_non_orth_corr; ++no) {
+                e = o.simplec ? simall_assemble_pressure_correction_simplec(ps, o.rho, ps->maP.p, ps->mvalues.p,
+                                                                            s->phi.p, SIMALL_MEM_DEVICE, nullptr)
+                              : simall_assemble_pressure_correction(ps, o.rho, ps->maP.p, s->phi.p,
+                                                                    SIMALL_MEM_DEVICE, nullptr);
+                if (e)
+                    return e;
+                simall_solver_stats st{};
+                e = simall_pressure_system_solve(ps, s->pres, s->pPrime.p, SIMALL_MEM_DEVICE, &st);
+                if (e)
+                    return e;
+                r.cont = st.b_norm > 1e-30 ? st.b_norm : 0.0;  // |rhs|; the solver floors its norm at 1e-30
+                r.iterations[3] = st.iterations;
+                e = simall_correct_fields(ps, o.rho, o.urfP, ps->maP.p, s->pPrime.p, s->Pd(), U, U + nC, U + 2 * nC,
+                                          s->phi.p, SIMALL_MEM_DEVICE);
+                if (e)
+                    return e;
+            }
+        }
+        // PimpleAlgorithm's early exit: every tolerance that is set holds
+        bool conv = o.tol_u > 0.0 || o.tol_p > 0.0;
+        if (o.tol_u > 0.0) {
+            double mm = std::fabs(r.mom[0]);
+            mm = (mm < std::fabs(r.mom[1])) ? std::fabs(r.mom[1]) : mm;
+            mm = (mm < std::fabs(r.mom[2])) ? std::fabs(r.mom[2]) : mm;
+            if (mm > o.tol_u)
+                conv = false;
+        }
+        if (o.tol_p > 0.0 && std::fabs(r.cont) > o.tol_p)
+            conv = false;
+        if (conv)
+            break;
     }
-    e = simall_compute_face_fluxes(ps, o.rho, U, U + nC, U + 2 * nC, s->phi.p, SIMALL_MEM_DEVICE);
-    if (e)
-        return e;
-    e = o.simplec ? simall_assemble_pressure_correction_simplec(ps, o.rho, ps->maP.p, ps->mvalues.p, s->phi.p,
-                                                                SIMALL_MEM_DEVICE, nullptr)
-                  : simall_assemble_pressure_correction(ps, o.rho, ps->maP.p, s->phi.p, SIMALL_MEM_DEVICE, nullptr);
-    if (e)
-        return e;
-    simall_solver_stats st{};
-    e = simall_pressure_system_solve(ps, s->pres, s->pPrime.p, SIMALL_MEM_DEVICE, &st);
-    if (e)
-        return e;
-    r.cont = st.b_norm > 1e-30 ? st.b_norm : 0.0;  // |rhs|; the solver floors its norm at 1e-30
-    r.iterations[3] = st.iterations;
-    e = simall_correct_fields(ps, o.rho, o.urfP, ps->maP.p, s->pPrime.p, s->Pd(), U, U + nC, U + 2 * nC, s->phi.p,
-                              SIMALL_MEM_DEVICE);
-    if (e)
-        return e;
+    r.outer = outer < o.n_outer_correctors ? outer : o.n_outer_correctors - 1;
     if (res)
         *res = r;
     return SIMALL_OK;

@@ -1,6 +1,7 @@
-"""Python mirror of SimpleAlgorithm (src/solver/SimpleAlgorithm.hpp:60-170)
-on the device: `GpuSimpleAlgorithm(mesh, bcs, momentum_solver,
-pressure_solver, options)` with `iterate()` and `advance_time_step(n)`
+"""Python mirror of SimpleAlgorithm (src/solver/SimpleAlgorithm.hpp:60-170),
+PisoAlgorithm and PimpleAlgorithm on the device: `GpuSimpleAlgorithm(mesh,
+bcs, momentum_solver, pressure_solver, options)` -- options a SimpleOptions,
+PisoOptions or PimpleOptions -- with `iterate()` and `advance_time_step(n)`
 returning the reference's SimpleResiduals (mom[3], cont).  U, p and phi stay
 in device memory between calls; `fields()` copies them out."""
 from __future__ import annotations
@@ -31,10 +32,44 @@ class SimpleOptions:
 
 
 @dataclass
+class PisoOptions:
+    """PisoOptions (src/solver/PisoAlgorithm.hpp:33-41), same defaults; PISO
+    runs without under-relaxation (PisoAlgorithm::to_simple_opts)."""
+
+    nCorrectors: int = 2
+    nNonOrthCorr: int = 0
+    rho: float = 1.0
+    mu: float = 1.0e-3
+    dt: float = 1.0e-3
+    bdf2: bool = True
+
+
+@dataclass
+class PimpleOptions:
+    """PimpleOptions (src/solver/PimpleAlgorithm.hpp:37-59), same defaults;
+    with one outer corrector the under-relaxation is off, as
+    PimpleAlgorithm::to_simple_opts does."""
+
+    nOuterCorrectors: int = 2
+    nCorrectors: int = 2
+    nNonOrthCorr: int = 0
+    momentumPredictor: bool = True
+    urfU: float = 0.7
+    urfP: float = 0.3
+    tolU: float = 0.0
+    tolP: float = 0.0
+    rho: float = 1.0
+    mu: float = 1.0e-3
+    dt: float = 1.0e-3
+    bdf2: bool = True
+
+
+@dataclass
 class SimpleResiduals:
     mom: tuple
     cont: float
     iterations: tuple
+    outer: int = 0
 
 
 class GpuSimpleAlgorithm:
@@ -55,9 +90,26 @@ class GpuSimpleAlgorithm:
         o = _lib.SimpleOptions()
         self.L.simall_simple_options_default(C.byref(o))
         opt = self.options
-        o.urfU, o.urfP, o.rho, o.mu, o.dt = (float(v) for v in (opt.urfU, opt.urfP, opt.rho, opt.mu, opt.dt))
-        o.bdf2 = int(bool(opt.bdf2))
-        o.simplec = int(bool(opt.simplec))
+        if isinstance(opt, PisoOptions):
+            o.urfU, o.urfP, o.rho, o.mu, o.dt = 1.0, 1.0, float(opt.rho), float(opt.mu), float(opt.dt)
+            o.bdf2 = int(bool(opt.bdf2))
+            o.n_correctors = int(opt.nCorrectors)
+            o.n_non_orth_corr = int(opt.nNonOrthCorr)
+        elif isinstance(opt, PimpleOptions):
+            piso_mode = opt.nOuterCorrectors <= 1
+            o.urfU = 1.0 if piso_mode else float(opt.urfU)
+            o.urfP = 1.0 if piso_mode else float(opt.urfP)
+            o.rho, o.mu, o.dt = float(opt.rho), float(opt.mu), float(opt.dt)
+            o.bdf2 = int(bool(opt.bdf2))
+            o.n_outer_correctors = int(opt.nOuterCorrectors)
+            o.n_correctors = int(opt.nCorrectors)
+            o.n_non_orth_corr = int(opt.nNonOrthCorr)
+            o.momentum_predictor = int(bool(opt.momentumPredictor))
+            o.tol_u, o.tol_p = float(opt.tolU), float(opt.tolP)
+        else:
+            o.urfU, o.urfP, o.rho, o.mu, o.dt = (float(v) for v in (opt.urfU, opt.urfP, opt.rho, opt.mu, opt.dt))
+            o.bdf2 = int(bool(opt.bdf2))
+            o.simplec = int(bool(opt.simplec))
         h = C.c_void_p()
         check(self.L.simall_simple_create(self.system.handle, momentum.handle, pressure.handle, C.byref(o),
                                           C.byref(h)), self.ctx.handle)
@@ -96,7 +148,7 @@ class GpuSimpleAlgorithm:
 
     @staticmethod
     def _res(r) -> SimpleResiduals:
-        return SimpleResiduals(tuple(r.mom), float(r.cont), tuple(r.iterations))
+        return SimpleResiduals(tuple(r.mom), float(r.cont), tuple(r.iterations), int(r.outer))
 
     def iterate(self) -> SimpleResiduals:
         r = _lib.SimpleResiduals()

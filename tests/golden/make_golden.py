@@ -8,7 +8,8 @@ renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction / assemble_momentum, CGSolver::solve with
 Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
 preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
-advance_time_step runs, io::Checkpoint::write, SimpTopology steps,
+advance_time_step runs, PisoAlgorithm / PimpleAlgorithm time steps,
+io::Checkpoint::write, SimpTopology steps,
 solve_discrete_adjoint);
 inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
@@ -242,6 +243,34 @@ def simp_case(name):
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
+PISO_PIMPLE_RUNS = {
+    # name: dims, node-shift amplitude (seed 61), RCM, specs, variant (1 PISO, 2 PIMPLE), loops, options, steps
+    "piso_cavity_12.npz": ((12, 12, 1), 0.0, False, CAVITY_BCS, 1, (1, 2, 1, 1), dict(mu=0.01, dt=0.01), 3),
+    "pimple_channel_8x6x5.npz": ((8, 6, 5), 0.2, True, CHANNEL_BCS, 2, (3, 2, 0, 1),
+                                 dict(mu=0.05, dt=0.02, urfU=0.7, urfP=0.3, tol_u=1e-6, tol_p=0.15), 3),
+}
+
+
+def piso_pimple_case(name):
+    """PisoAlgorithm / PimpleAlgorithm of the reference from rest, BDF2 time
+    steps of advance_time_step(1), GMRES(30)+Jacobi momentum and CG+Jacobi
+    pressure: U, p, phi, residuals and PIMPLE's outer-exit index per step."""
+    import json
+
+    dims, amp, renumber, bcs, variant, loops, kw, steps = PISO_PIMPLE_RUNS[name]
+    shift = W.interior_node_shift(*dims, amp=amp, seed=61) if amp else None
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=renumber)
+    nC = rm["nC"]
+    out = R.piso_pimple_run(rm, variant, bcs, np.zeros((3, nC)), np.zeros(nC), steps, loops=loops, **kw)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), amp=np.array(amp),
+                        renumber=np.array(renumber), bc_zone=np.array([b[0] for b in bcs]),
+                        bc_type=np.array([b[1] for b in bcs]),
+                        bc_vec=np.array([list(b[2]) if len(b) > 2 else [0.0, 0.0, 0.0] for b in bcs]),
+                        variant=np.array(variant), loops=np.array(loops), options=np.array(json.dumps(kw)),
+                        steps=np.array(steps), U=out["U"], p=out["p"], phi=out["phi"], res=out["res"],
+                        last_outer=out["last_outer"])
+
+
 def adjoint_case(name):
     """solve_discrete_adjoint on a small face-conductance Poisson system."""
     nx, ny, nz = 5, 4, 3
@@ -280,6 +309,8 @@ def main():
         simple_case(name)
     checkpoint_case("checkpoint_4x3x2")
     simp_case("simp_7x6x5_rcm.npz")
+    for name in PISO_PIMPLE_RUNS:
+        piso_pimple_case(name)
     print("fixtures written to", HERE)
 
 

@@ -270,3 +270,47 @@ def test_simp_topology_steps(oracle, ref, dims, radius, renumber):
     for got, w in zip((s.rho, s.rhoTilde, s.K_simp, s.dC_drhoTilde), want[1:]):
         assert bits_equal(got, w)
     ref.free_mesh(r)
+
+
+PISO_PIMPLE_CASES = {
+    # name: (dims, amp, renumber, bcs, variant, loops, extra kwargs, steps)
+    "piso_cavity": ((12, 12, 1), 0.0, False, CAVITY_BCS, 1, (1, 2, 1, 1), dict(mu=0.01, dt=0.01), 3),
+    "pimple_channel": ((8, 6, 5), 0.2, True, CHANNEL_BCS, 2, (3, 2, 0, 1),
+                       dict(mu=0.05, dt=0.02, urfU=0.7, urfP=0.3, tol_u=1e-6, tol_p=0.15), 3),  # exits at 2, 1, 0
+    "pimple_as_piso": ((10, 8, 1), 0.0, False, CAVITY_BCS, 2, (1, 2, 0, 1), dict(mu=0.02, dt=0.005), 2),
+}
+
+
+def piso_pimple_oracle(oracle, m, bcs, variant, loops, kw):
+    """The oracle configured as PisoAlgorithm / PimpleAlgorithm configure
+    SimpleAlgorithm (PisoAlgorithm.hpp:63-74, PimpleAlgorithm.hpp:92-105)."""
+    piso_mode = variant == 1 or loops[0] <= 1
+    return oracle.SimpleOracle(m, bcs, rho=kw.get("rho", 1.0), mu=kw["mu"], dt=kw["dt"], bdf2=True,
+                               urfU=1.0 if piso_mode else kw["urfU"], urfP=1.0 if piso_mode else kw["urfP"],
+                               mom_cfg=(0, 0, 1e-9, 200, 30), p_cfg=(2, 0, 1e-9, 1000, 30),
+                               n_outer_correctors=1 if variant == 1 else loops[0], n_correctors=loops[1],
+                               n_non_orth_corr=loops[2], momentum_predictor=bool(loops[3]),
+                               tol_u=kw.get("tol_u", 0.0) if variant == 2 else 0.0,
+                               tol_p=kw.get("tol_p", 0.0) if variant == 2 else 0.0)
+
+
+@pytest.mark.parametrize("case", sorted(PISO_PIMPLE_CASES))
+def test_piso_pimple_time_steps(oracle, ref, case):
+    """PisoAlgorithm / PimpleAlgorithm::iterate under advance_time_step(1):
+    U, p, phi, residuals and PIMPLE's outer-exit index bit-identical."""
+    dims, amp, renumber, bcs, variant, loops, kw, steps = PISO_PIMPLE_CASES[case]
+    sh = _shift(dims, 61, amp)
+    r = ref.cartesian_mesh(*dims, node_shift=sh, do_rcm=renumber)
+    m = oracle.cartesian_mesh(*dims, node_shift=sh)
+    if renumber:
+        oracle.rcm(m)
+    want = ref.piso_pimple_run(r, variant, bcs, np.zeros((3, m.nC)), np.zeros(m.nC), steps, loops=loops, **kw)
+    s = piso_pimple_oracle(oracle, m, bcs, variant, loops, kw)
+    res, last = [], []
+    for _ in range(steps):
+        res.append(s.advance_time_step(1)[0])
+        last.append(s.last_outer if variant == 2 else 0)
+    assert bits_equal(np.array(res), want["res"])
+    assert list(want["last_outer"]) == last
+    assert bits_equal(s.U, want["U"]) and bits_equal(s.p, want["p"]) and bits_equal(s.phi, want["phi"])
+    ref.free_mesh(r)
