@@ -306,3 +306,36 @@ def test_simp_fixture(oracle):
         assert bits_equal(np.array(ch), g[f"{tag}_change"])
         assert bits_equal(s.rho, g[f"{tag}_rho"]) and bits_equal(s.rhoTilde, g[f"{tag}_rhoTilde"])
         assert bits_equal(s.K_simp, g[f"{tag}_K"]) and bits_equal(s.dC_drhoTilde, g[f"{tag}_dCt"])
+
+
+@pytest.mark.parametrize("name", ["piso_cavity_12.npz", "pimple_channel_8x6x5.npz"])
+def test_piso_pimple_fixture(oracle, name):
+    """PisoAlgorithm / PimpleAlgorithm time steps: the oracle reproduces the
+    reference's fields, residuals and PIMPLE's exit index bit for bit."""
+    import json
+
+    from simall_gb300 import workloads as W
+
+    g = load(name)
+    dims = tuple(int(v) for v in g["dims"])
+    amp = float(g["amp"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=amp, seed=61) if amp else None)
+    if bool(g["renumber"]):
+        oracle.rcm(m)
+    bcs = [(int(z), int(t), tuple(v)) for z, t, v in zip(g["bc_zone"], g["bc_type"], g["bc_vec"])]
+    kw = json.loads(str(g["options"]))
+    loops = [int(v) for v in g["loops"]]
+    variant = int(g["variant"])
+    piso_mode = variant == 1 or loops[0] <= 1
+    s = oracle.SimpleOracle(m, bcs, mu=kw["mu"], dt=kw["dt"], bdf2=True,
+                            urfU=1.0 if piso_mode else kw["urfU"], urfP=1.0 if piso_mode else kw["urfP"],
+                            mom_cfg=(0, 0, 1e-9, 200, 30), p_cfg=(2, 0, 1e-9, 1000, 30),
+                            n_outer_correctors=1 if variant == 1 else loops[0], n_correctors=loops[1],
+                            n_non_orth_corr=loops[2], momentum_predictor=bool(loops[3]),
+                            tol_u=kw.get("tol_u", 0.0), tol_p=kw.get("tol_p", 0.0))
+    res, outer = [], []
+    for _ in range(int(g["steps"])):
+        res.append(s.advance_time_step(1)[0])
+        outer.append(s.last_outer if variant == 2 else 0)
+    assert bits_equal(np.array(res), g["res"]) and outer == [int(v) for v in g["last_outer"]]
+    assert bits_equal(s.U, g["U"]) and bits_equal(s.p, g["p"]) and bits_equal(s.phi, g["phi"])
