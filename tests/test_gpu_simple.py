@@ -126,5 +126,7 @@ def test_piso_pimple_against_reference(sg, ctx, name):
     assert outer == [int(v) for v in g["last_outer"]]
     assert rel(U, g["U"]) <= 1e-8 and rel(p, g["p"]) <= 1e-8 and rel(phi, g["phi"]) <= 1e-8
     res = np.array(res)
-    assert np.all(np.abs(res[:, 3] - g["res"][:, 3]) <= 1e-8 * np.abs(g["res"][:, 3]))
+    # the last corrector's continuity residual is ~1e-11 here: what is left of
+    # the solvers' rounding, so it agrees to 1e-6 relative (1e-16 absolute)
+    assert np.all(np.abs(res[:, 3] - g["res"][:, 3]) <= 1e-6 * np.abs(g["res"][:, 3]) + 1e-16)
     alg.close()
