@@ -51,10 +51,11 @@ enum simall_status {
 
 enum simall_memory { SIMALL_MEM_HOST = 0, SIMALL_MEM_DEVICE = 1 };
 
-/* PreconditionerKind ordinals (src/solver/Solver.hpp:75-82).  SSOR and AMG are
- * not on this path and are rejected with SIMALL_ERR_UNSUPPORTED; None maps to
- * Jacobi, as make_preconditioner's default branch does
- * (src/solver/LinearSolvers.cpp:240-254). */
+/* PreconditionerKind ordinals (src/solver/Solver.hpp:75-82).  SSOR is
+ * SsorPreconditioner with make_preconditioner's w = 1
+ * (src/solver/LinearSolvers.cpp:163-231, :247-248), FP64 only; AMG is rejected
+ * with SIMALL_ERR_UNSUPPORTED; None maps to Jacobi, as make_preconditioner's
+ * default branch does (:240-254). */
 enum simall_preconditioner {
     SIMALL_PRECOND_JACOBI = 0,
     SIMALL_PRECOND_ILU0 = 1,
@@ -106,8 +107,8 @@ int64_t simall_context_kernel_launches(const simall_context *ctx);
 /* ------------------------------------------------------------------ Krylov solver */
 /* Replaces solver::ILinearSolver / CGSolver (src/solver/Solver.hpp:92-100,
  * src/solver/LinearSolvers.cpp:415-459) and gpu::CgGpu
- * (src/gpu/CgGpu.hpp:87-124); with `kind` also GMRESmSolver and
- * BiCGSTABSolver (make_linear_solver, src/solver/Solver.cpp:25-39). */
+ * (src/gpu/CgGpu.hpp:87-124); with `kind` also GMRESmSolver, BiCGSTABSolver
+ * and TfqmrSolver (make_linear_solver, src/solver/Solver.cpp:25-39). */
 typedef struct simall_solver_config {
     int preconditioner;    /* simall_preconditioner; default Jacobi */
     double tolerance;      /* stop when ||r||/max(||b||,1e-30) < tolerance; default 1e-8 */
@@ -121,10 +122,10 @@ typedef struct simall_solver_config {
 } simall_solver_config;
 
 /* LinearSolverKind ordinals (src/solver/Solver.hpp:67-73).  CG is the pressure
- * path (FP64 or mixed precision); GMRES(m) and BiCGSTAB (FP64, Jacobi or
- * ILU(0)) follow GMRESmSolver::solve and BiCGSTABSolver::solve
- * (src/solver/LinearSolvers.cpp:268-343, :363-405) for the momentum systems.
- * TFQMR is rejected with SIMALL_ERR_UNSUPPORTED. */
+ * path (FP64 or mixed precision); GMRES(m), BiCGSTAB and TFQMR (FP64, Jacobi,
+ * ILU(0) or SSOR) follow GMRESmSolver::solve, BiCGSTABSolver::solve and
+ * TfqmrSolver::solve (src/solver/LinearSolvers.cpp:268-343, :363-405,
+ * :497-609), including their breakdown exits and return values. */
 enum simall_solver_kind {
     SIMALL_SOLVER_GMRES = 0,
     SIMALL_SOLVER_BICGSTAB = 1,
@@ -172,6 +173,12 @@ int simall_solver_solve(simall_solver *s, const double *b, double *x, int mem, s
 /* y = A x with the solver's current FP64 matrix (the staged SpMV kernel the
  * solve uses; bit-identical to CSRMatrix::spmv, src/solver/CSRMatrix.hpp:24-35). */
 int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem);
+/* z = M^-1 r with the solver's FP64 preconditioner, as set up for its current
+ * matrix: IPreconditioner::apply (src/solver/LinearSolvers.hpp:33-34) of
+ * JacobiPreconditioner, ILU0Preconditioner or SsorPreconditioner
+ * (src/solver/LinearSolvers.cpp:66-71, :127-151, :188-231), bit-identical to
+ * them.  r and z must not alias. */
+int simall_solver_precond_apply(simall_solver *s, const double *r, double *z, int mem);
 /* Times `reps` back-to-back launches of one kernel of the solve on the
  * current matrix, bracketed by CUDA events on the context stream; *ms
  * receives the average duration of one launch and *bytes the algorithmic

@@ -44,7 +44,7 @@ public:
         c.tolerance = cfg.tolerance;
         c.max_iterations = cfg.maxIterations;
         c.precision = precision;
-        c.kind = static_cast<int>(cfg.kind);  // CG, GMRES(restart) or BiCGSTAB, as make_linear_solver
+        c.kind = static_cast<int>(cfg.kind);  // CG, GMRES(restart), BiCGSTAB or TFQMR, as make_linear_solver
         c.restart = cfg.restart;
         const int st = simall_solver_create(ctx_, &c, &s_);
         if (st != SIMALL_OK) {

@@ -90,6 +90,12 @@ def lib():
         L.orc_bicgstab.restype = C.c_int
         L.orc_bicgstab.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
         L.orc_gmres.restype = C.c_int
+        L.orc_tfqmr.restype = C.c_int
+        L.orc_tfqmr.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
+        L.orc_ssor_setup.restype = None
+        L.orc_ssor_setup.argtypes = [_I64, _P, _P, _P, _P, _P]
+        L.orc_ssor_apply.restype = None
+        L.orc_ssor_apply.argtypes = [_I64, _P, _P, _P, _P, _P, _D, _P, _P, _P, _P]
         L.orc_gmres.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, C.c_int, _P, _P]
         L.orc_simple_iterate.restype = C.c_int
         L.orc_simple_iterate.argtypes = [_I64, _I64] + [_P] * 16 + [C.c_int] + [_P] * 3 + [C.c_int, _P, _D, _P, _D] + \
@@ -355,6 +361,31 @@ def gmres(rowPtr, colIdx, values, b, precond=1, tol=1e-8, max_it=1000, restart=3
                          _ptr(np.ascontiguousarray(values, np.float64)), _ptr(np.ascontiguousarray(b, np.float64)),
                          int(precond), float(tol), int(max_it), int(restart), _ptr(x), C.byref(last))
     return x, it, last.value
+
+
+def tfqmr(rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):
+    """TfqmrSolver::solve (LinearSolvers.cpp:497-609); returns (x, iterations, last)."""
+    n = len(rowPtr) - 1
+    x = np.empty(n)
+    last = C.c_double(0)
+    it = lib().orc_tfqmr(n, _ptr(np.ascontiguousarray(rowPtr, np.int32)), _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                         _ptr(np.ascontiguousarray(values, np.float64)), _ptr(np.ascontiguousarray(b, np.float64)),
+                         int(precond), float(tol), int(max_it), _ptr(x), C.byref(last))
+    return x, it, last.value
+
+
+def ssor_apply(rowPtr, colIdx, values, r, omega=1.0):
+    """SsorPreconditioner setup + apply (LinearSolvers.cpp:168-231); returns z."""
+    n = len(rowPtr) - 1
+    rp = np.ascontiguousarray(rowPtr, np.int32)
+    ci = np.ascontiguousarray(colIdx, np.int32)
+    v = np.ascontiguousarray(values, np.float64)
+    diag, inv = np.empty(n), np.empty(n)
+    lib().orc_ssor_setup(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(diag), _ptr(inv))
+    z, y, w = np.empty(n), np.empty(n), np.empty(n)
+    lib().orc_ssor_apply(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(diag), _ptr(inv), float(omega),
+                         _ptr(np.ascontiguousarray(r, np.float64)), _ptr(z), _ptr(y), _ptr(w))
+    return z
 
 
 class SimpOracle:

@@ -447,9 +447,9 @@ int ref_assemble_momentum(void* h, int nbc, const std::uint32_t* bcZones, const 
 }
 
 // ------------------------------------------------------------------ solvers
-// make_gmres / make_bicgstab / make_cg (LinearSolvers.cpp:462-473), as
-// make_linear_solver dispatches them (Solver.cpp:25-39): kind is the
-// LinearSolverKind ordinal (0 GMRES, 1 BiCGSTAB, 2 CG).  Returns the
+// make_gmres / make_bicgstab / make_cg / make_tfqmr (LinearSolvers.cpp:462-473,
+// 616-619), as make_linear_solver dispatches them (Solver.cpp:25-39): kind is
+// the LinearSolverKind ordinal (0 GMRES, 1 BiCGSTAB, 2 CG, 3 TFQMR).  Returns the
 // iteration count; x from 0.
 int ref_krylov(int kind, int precond, double tol, int maxit, int restart, int n, const int* rowPtr,
                const int* colIdx, const double* values, const double* b, double* x, double* lastRes,
@@ -462,7 +462,10 @@ int ref_krylov(int kind, int precond, double tol, int maxit, int restart, int n,
     c.tolerance = tol;
     c.maxIterations = maxit;
     c.restart = restart;
-    std::unique_ptr<S::ILinearSolver> sol = kind == 1 ? S::make_bicgstab(c) : kind == 2 ? S::make_cg(c) : S::make_gmres(c);
+    std::unique_ptr<S::ILinearSolver> sol = kind == 1   ? S::make_bicgstab(c)
+                                            : kind == 2 ? S::make_cg(c)
+                                            : kind == 3 ? S::make_tfqmr(c)
+                                                        : S::make_gmres(c);
     Vec bb(b, b + n), xx(n, 0.0);
     const auto t0 = std::chrono::steady_clock::now();
     const int it = sol->solve(A, bb, xx);
@@ -543,7 +546,10 @@ std::unique_ptr<S::ILinearSolver> make_kind(const int* cfg, double tol)
     c.maxIterations = cfg[2];
     c.restart = cfg[3];
     c.tolerance = tol;
-    return cfg[0] == 1 ? S::make_bicgstab(c) : cfg[0] == 2 ? S::make_cg(c) : S::make_gmres(c);
+    return cfg[0] == 1   ? S::make_bicgstab(c)
+           : cfg[0] == 2 ? S::make_cg(c)
+           : cfg[0] == 3 ? S::make_tfqmr(c)
+                         : S::make_gmres(c);
 }
 
 // SimpleAlgorithm on the given mesh from U (in [3][nC]) and p: nOuter calls of

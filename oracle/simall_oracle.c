@@ -684,6 +684,127 @@ void orc_ilu0_apply(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, con
     }
 }
 
+/* SsorPreconditioner::setup (src/solver/LinearSolvers.cpp:168-186): the first
+ * diagonal entry of each row, diag = a_ii and invDiag = 1/a_ii (1.0 when the
+ * entry is zero); diag = invDiag = 1.0 when the row has none. */
+void orc_ssor_setup(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, double *diag,
+                    double *invDiag)
+{
+    for (int64_t i = 0; i < n; ++i) {
+        diag[i] = 1.0;
+        invDiag[i] = 1.0;
+        for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                diag[i] = values[k];
+                invDiag[i] = (values[k] != 0.0) ? 1.0 / values[k] : 1.0;
+                break;
+            }
+    }
+}
+
+/* SsorPreconditioner::apply (src/solver/LinearSolvers.cpp:188-231):
+ *   forward   y_i = (w r_i - sum_{j<i} (w a_ij) y_j) invDiag_i  (columns
+ *             ascending, stopping at the first j >= i);
+ *   scale     v_i = (diag_i y_i) / w;
+ *   backward  z_i = ((v_i - sum_{j>i} a_ij z_j) w) invDiag_i, rows n-1 .. 0;
+ *   z *= (2 - w).
+ * make_preconditioner builds it with w = 1 (:247-248).  y, v: caller scratch. */
+void orc_ssor_apply(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                    const double *diag, const double *invDiag, double omega, const double *r, double *z, double *y,
+                    double *v)
+{
+    for (int64_t i = 0; i < n; ++i)
+        y[i] = 0.0;
+    for (int64_t i = 0; i < n; ++i) {
+        double s = omega * r[i];
+        for (int32_t kp = rowPtr[i]; kp < rowPtr[i + 1]; ++kp) {
+            const int32_t j = colIdx[kp];
+            if (j >= i)
+                break;
+            s -= omega * values[kp] * y[j];
+        }
+        y[i] = s * invDiag[i];
+    }
+    const double scale = (2.0 - omega);
+    for (int64_t i = 0; i < n; ++i)
+        v[i] = diag[i] * y[i] / omega;
+    for (int64_t i = 0; i < n; ++i)
+        z[i] = 0.0;
+    for (int64_t i = n - 1; i >= 0; --i) {
+        double s = v[i];
+        for (int32_t kp = rowPtr[i]; kp < rowPtr[i + 1]; ++kp) {
+            const int32_t j = colIdx[kp];
+            if (j <= i)
+                continue;
+            s -= values[kp] * z[j];
+        }
+        z[i] = s * omega * invDiag[i];
+    }
+    for (int64_t i = 0; i < n; ++i)
+        z[i] *= scale;
+}
+
+/* ------------------------------------------------------------------ preconditioner objects */
+
+/* make_preconditioner (src/solver/LinearSolvers.cpp:240-254) for the kinds
+ * restated here: 1 ILU(0), 2 SSOR (w = 1), anything else Jacobi (AMG, kind 3,
+ * is not restated; None, kind 4, is the default branch's Jacobi). */
+typedef struct {
+    int kind; /* 0 Jacobi, 1 ILU(0), 2 SSOR */
+    int64_t n;
+    const int32_t *rowPtr, *colIdx;
+    const double *values;
+    double *invD, *lu, *y, *diag, *v;
+    int32_t *diagPtr;
+} OrcPrec;
+
+static void prec_setup(OrcPrec *M, int kind, int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
+                       const double *values)
+{
+    memset(M, 0, sizeof(*M));
+    M->kind = (kind == 1 || kind == 2) ? kind : 0;
+    M->n = n;
+    M->rowPtr = rowPtr;
+    M->colIdx = colIdx;
+    M->values = values;
+    if (M->kind == 2) {
+        M->diag = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        M->invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        M->y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        M->v = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_ssor_setup(n, rowPtr, colIdx, values, M->diag, M->invD);
+    } else if (M->kind == 1) {
+        M->lu = (double *)xmalloc((size_t)rowPtr[n] * sizeof(double) + 8);
+        M->diagPtr = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
+        M->y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_ilu0_setup(n, rowPtr, colIdx, values, M->lu, M->diagPtr);
+    } else {
+        M->invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+        orc_jacobi_setup(n, rowPtr, colIdx, values, M->invD);
+    }
+}
+
+static void prec_apply(const OrcPrec *M, const double *r, double *z)
+{
+    if (M->kind == 1)
+        orc_ilu0_apply(M->n, M->rowPtr, M->colIdx, M->lu, M->diagPtr, r, z, M->y);
+    else if (M->kind == 2)
+        orc_ssor_apply(M->n, M->rowPtr, M->colIdx, M->values, M->diag, M->invD, 1.0, r, z, M->y, M->v);
+    else
+        for (int64_t i = 0; i < M->n; ++i)
+            z[i] = M->invD[i] * r[i];
+}
+
+static void prec_free(OrcPrec *M)
+{
+    free(M->invD);
+    free(M->lu);
+    free(M->y);
+    free(M->diagPtr);
+    free(M->diag);
+    free(M->v);
+}
+
 /* ------------------------------------------------------------------ CG */
 
 /*
@@ -693,37 +814,19 @@ void orc_ilu0_apply(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, con
  *        alpha = rz/pAp; x += alpha p; r -= alpha Ap; last = |r|/bnorm;
  *        if last < tol return it+1; z = M r; rzNew = r.z; beta = rzNew/rz;
  *        p = z + beta p; rz = rzNew }  return maxIt.
- * precond: 0 Jacobi, 1 ILU0; any other value is Jacobi (make_preconditioner's
- * default branch, LinearSolvers.cpp:240-254).  hist (optional, maxIt long)
+ * precond: 0 Jacobi, 1 ILU0, 2 SSOR; any other value is Jacobi (OrcPrec).  hist (optional, maxIt long)
  * receives last after each iteration.
  */
 int orc_cg(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,
            int precond, double tol, int maxIt, double *x, double *lastRes, double *hist)
 {
-    const int ilu = (precond == 1);
+    OrcPrec M;
+    prec_setup(&M, precond, n, rowPtr, colIdx, values);
     double *r = (double *)xmalloc((size_t)n * sizeof(double) + 8);
     double *z = (double *)xmalloc((size_t)n * sizeof(double) + 8);
     double *p = (double *)xmalloc((size_t)n * sizeof(double) + 8);
     double *Ap = (double *)xmalloc((size_t)n * sizeof(double) + 8);
-    double *y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
-    double *invD = NULL, *lu = NULL;
-    int32_t *diagPtr = NULL;
-    if (ilu) {
-        lu = (double *)xmalloc((size_t)rowPtr[n] * sizeof(double) + 8);
-        diagPtr = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
-        orc_ilu0_setup(n, rowPtr, colIdx, values, lu, diagPtr);
-    } else {
-        invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
-        orc_jacobi_setup(n, rowPtr, colIdx, values, invD);
-    }
-#define APPLY_M()                                                                                             \
-    do {                                                                                                      \
-        if (ilu)                                                                                              \
-            orc_ilu0_apply(n, rowPtr, colIdx, lu, diagPtr, r, z, y);                                          \
-        else                                                                                                  \
-            for (int64_t i = 0; i < n; ++i)                                                                   \
-                z[i] = invD[i] * r[i];                                                                        \
-    } while (0)
+#define APPLY_M() prec_apply(&M, r, z)
     for (int64_t i = 0; i < n; ++i) {
         x[i] = 0.0;
         r[i] = b[i];
@@ -767,10 +870,7 @@ int orc_cg(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double
     free(z);
     free(p);
     free(Ap);
-    free(y);
-    free(invD);
-    free(lu);
-    free(diagPtr);
+    prec_free(&M);
     return ret;
 }
 
@@ -1146,52 +1246,6 @@ void orc_assemble_momentum(int64_t nC, int64_t nF, const int64_t *owner, const i
 
 /* ------------------------------------------------------------------ non-symmetric Krylov */
 
-/* make_preconditioner (src/solver/LinearSolvers.cpp:240-254) for the kinds the
- * device supports: 1 ILU(0), anything else Jacobi. */
-typedef struct {
-    int ilu;
-    int64_t n;
-    const int32_t *rowPtr, *colIdx;
-    double *invD, *lu, *y;
-    int32_t *diagPtr;
-} OrcPrec;
-
-static void prec_setup(OrcPrec *M, int kind, int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
-                       const double *values)
-{
-    memset(M, 0, sizeof(*M));
-    M->ilu = (kind == 1);
-    M->n = n;
-    M->rowPtr = rowPtr;
-    M->colIdx = colIdx;
-    if (M->ilu) {
-        M->lu = (double *)xmalloc((size_t)rowPtr[n] * sizeof(double) + 8);
-        M->diagPtr = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
-        M->y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
-        orc_ilu0_setup(n, rowPtr, colIdx, values, M->lu, M->diagPtr);
-    } else {
-        M->invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
-        orc_jacobi_setup(n, rowPtr, colIdx, values, M->invD);
-    }
-}
-
-static void prec_apply(const OrcPrec *M, const double *r, double *z)
-{
-    if (M->ilu)
-        orc_ilu0_apply(M->n, M->rowPtr, M->colIdx, M->lu, M->diagPtr, r, z, M->y);
-    else
-        for (int64_t i = 0; i < M->n; ++i)
-            z[i] = M->invD[i] * r[i];
-}
-
-static void prec_free(OrcPrec *M)
-{
-    free(M->invD);
-    free(M->lu);
-    free(M->y);
-    free(M->diagPtr);
-}
-
 /*
  * BiCGSTAB (BiCGSTABSolver::solve, src/solver/LinearSolvers.cpp:363-405), x
  * from 0: r = b - A x, rh = r, rho = alpha = omega = 1, v = 0;
@@ -1398,10 +1452,136 @@ int orc_gmres(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const dou
     return ret;
 }
 
+/*
+ * TFQMR (TfqmrSolver::solve, src/solver/LinearSolvers.cpp:497-609), x from 0:
+ * r = rh = w = b; u1 = M r; v = Au1 = A u1; tau = |r|; bnorm = max(|b|, 1e-30);
+ * tau/bnorm < tol -> last = tau/bnorm, return 0.  rho = rh.r, theta = eta =
+ * alpha = 0, d = 0.  Each iteration:
+ *   sigma = rh.v; |sigma| < 1e-30 -> last = tau/bnorm, return it;
+ *   alpha = rho/sigma; u2 = u1 - alpha M v; Au2 = A u2;
+ *   two half steps (u = u1, Au1 then u = u2, Au2):
+ *     w -= alpha Au; theta' = |w|/max(tau, 1e-30); c = 1/sqrt(1 + theta'^2);
+ *     tau' = tau theta' c; eta' = c c alpha;
+ *     d = u + (theta theta eta / max(alpha, 1e-30)) d; x += eta' d;
+ *     (tau, theta, eta) = (tau', theta', eta');
+ *   last = tau sqrt(2(it+1) + 1) / bnorm; if last < tol: last = |b - A x|/bnorm
+ *     and return it+1 when that is < tol;
+ *   r -= alpha (Au1 + Au2); rhoNew = rh.r; |rho| < 1e-30 -> last = tau/bnorm,
+ *   return it; beta = rhoNew/rho; u1 = M r + beta (u2 + beta u1); Au1 = A u1;
+ *   v = Au1 + beta (Au2 + beta v); rho = rhoNew.
+ * Returns maxIt when the loop ends; *lastRes is left as it was when nothing
+ * sets it (maxIt <= 0), as the reference leaves its member.
+ */
+int orc_tfqmr(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,
+              int precond, double tol, int maxIt, double *x, double *lastRes)
+{
+    OrcPrec M;
+    prec_setup(&M, precond, n, rowPtr, colIdx, values);
+    const size_t bytes = (size_t)n * sizeof(double) + 8;
+    double *r = (double *)xmalloc(bytes), *rh = (double *)xmalloc(bytes), *w = (double *)xmalloc(bytes);
+    double *d = (double *)xmalloc(bytes), *u1 = (double *)xmalloc(bytes), *u2 = (double *)xmalloc(bytes);
+    double *v = (double *)xmalloc(bytes), *Au1 = (double *)xmalloc(bytes), *Au2 = (double *)xmalloc(bytes);
+    double *z = (double *)xmalloc(bytes);
+    int ret = maxIt;
+    for (int64_t i = 0; i < n; ++i) {
+        x[i] = 0.0;
+        d[i] = 0.0;
+        r[i] = b[i];
+    }
+    memcpy(rh, r, (size_t)n * sizeof(double));
+    memcpy(w, r, (size_t)n * sizeof(double));
+    prec_apply(&M, r, u1);
+    orc_spmv(n, rowPtr, colIdx, values, u1, v);
+    memcpy(Au1, v, (size_t)n * sizeof(double));
+    double tau = norm2(n, r);
+    const double bn = norm2(n, b);
+    const double bnorm = STD_MAX(bn, 1e-30);
+    if (tau / bnorm < tol) {
+        *lastRes = tau / bnorm;
+        ret = 0;
+        goto out;
+    }
+    {
+        double rho = orc_dot(n, rh, r);
+        double theta = 0.0, eta = 0.0, alpha = 0.0;
+        for (int it = 0; it < maxIt; ++it) {
+            const double sigma = orc_dot(n, rh, v);
+            if (fabs(sigma) < 1.0e-30) {
+                *lastRes = tau / bnorm;
+                ret = it;
+                goto out;
+            }
+            alpha = rho / sigma;
+            prec_apply(&M, v, z);
+            for (int64_t i = 0; i < n; ++i)
+                u2[i] = u1[i] - alpha * z[i];
+            orc_spmv(n, rowPtr, colIdx, values, u2, Au2);
+            for (int half = 0; half < 2; ++half) {
+                const double *u = half ? u2 : u1;
+                const double *Au = half ? Au2 : Au1;
+                for (int64_t i = 0; i < n; ++i)
+                    w[i] -= alpha * Au[i];
+                const double theta_new = norm2(n, w) / STD_MAX(tau, 1.0e-30);
+                const double c = 1.0 / sqrt(1.0 + theta_new * theta_new);
+                const double tau_new = tau * theta_new * c;
+                const double eta_new = c * c * alpha;
+                for (int64_t i = 0; i < n; ++i) {
+                    d[i] = u[i] + (theta * theta * eta / STD_MAX(alpha, 1.0e-30)) * d[i];
+                    x[i] += eta_new * d[i];
+                }
+                tau = tau_new;
+                theta = theta_new;
+                eta = eta_new;
+            }
+            const double resBound = tau * sqrt(2.0 * (it + 1) + 1.0);
+            *lastRes = resBound / bnorm;
+            if (*lastRes < tol) {
+                orc_spmv(n, rowPtr, colIdx, values, x, z);
+                for (int64_t i = 0; i < n; ++i)
+                    z[i] = b[i] - z[i];
+                *lastRes = norm2(n, z) / bnorm;
+                if (*lastRes < tol) {
+                    ret = it + 1;
+                    goto out;
+                }
+            }
+            for (int64_t i = 0; i < n; ++i)
+                r[i] -= alpha * (Au1[i] + Au2[i]);
+            const double rhoNew = orc_dot(n, rh, r);
+            if (fabs(rho) < 1.0e-30) {
+                *lastRes = tau / bnorm;
+                ret = it;
+                goto out;
+            }
+            const double beta = rhoNew / rho;
+            prec_apply(&M, r, z);
+            for (int64_t i = 0; i < n; ++i)
+                u1[i] = z[i] + beta * (u2[i] + beta * u1[i]);
+            orc_spmv(n, rowPtr, colIdx, values, u1, Au1);
+            for (int64_t i = 0; i < n; ++i)
+                v[i] = Au1[i] + beta * (Au2[i] + beta * v[i]);
+            rho = rhoNew;
+        }
+    }
+out:
+    free(r);
+    free(rh);
+    free(w);
+    free(d);
+    free(u1);
+    free(u2);
+    free(v);
+    free(Au1);
+    free(Au2);
+    free(z);
+    prec_free(&M);
+    return ret;
+}
+
 /* ------------------------------------------------------------------ one SIMPLE outer iteration */
 
 /* make_linear_solver (src/solver/Solver.cpp:25-39) for cfg = {kind, precond,
- * maxIt, restart}: 0 GMRES, 1 BiCGSTAB, 2 CG. */
+ * maxIt, restart}: 0 GMRES, 1 BiCGSTAB, 2 CG, 3 TFQMR. */
 static int orc_linear_solve(const int *cfg, double tol, int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
                             const double *values, const double *b, double *x, double *last)
 {
@@ -1410,6 +1590,8 @@ static int orc_linear_solve(const int *cfg, double tol, int64_t n, const int32_t
         return orc_bicgstab(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], x, last);
     case 2:
         return orc_cg(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], x, last, NULL);
+    case 3:
+        return orc_tfqmr(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], x, last);
     default:
         return orc_gmres(n, rowPtr, colIdx, values, b, cfg[1], tol, cfg[2], cfg[3], x, last);
     }

@@ -14,11 +14,11 @@ from .simple import GpuSimpleAlgorithm, PimpleOptions, PisoOptions, SimpleOption
 from .topology import GpuSimpTopology, SimpConfig
 from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
                      Precision, PreconditionerKind, default_context, make_bicgstab, make_cg, make_gmres,
-                     make_linear_solver)
+                     make_linear_solver, make_tfqmr)
 
 __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallError", "BCType", "MeshSoA", "PressureSystem",
            "cartesian", "rcm", "Context", "CSRMatrix", "GpuCGSolver", "LinearSolverConfig", "LinearSolverKind",
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
-           "make_gmres", "make_bicgstab", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals", "PisoOptions",
+           "make_gmres", "make_bicgstab", "make_tfqmr", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals", "PisoOptions",
            "PimpleOptions",
            "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write", "GpuSimpTopology", "SimpConfig"]

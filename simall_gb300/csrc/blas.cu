@@ -40,6 +40,13 @@ __global__ void k_jacobi_apply(int64_t n, const double *__restrict__ d, const do
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
         z[i] = r[i] / d[i];
 }
+// z = invD r, JacobiPreconditioner::apply (src/solver/LinearSolvers.cpp:66-71)
+__global__ void k_scale_inv(int64_t n, const double *__restrict__ invD, const double *__restrict__ r,
+                            double *__restrict__ z)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        z[i] = __dmul_rn(invD[i], r[i]);
+}
 __global__ void __launch_bounds__(kBlock) k_dot(int64_t n, const double *__restrict__ x, const double *__restrict__ y,
                                                 double *partials, unsigned *ticket, double *out)
 {
@@ -262,6 +269,39 @@ int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem)
         SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     }
     return SIMALL_OK;
+}
+
+int simall_solver_precond_apply(simall_solver *s, const double *r, double *z, int mem)
+{
+    if (!s || !r || !z)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall_context *ctx = s->ctx;
+    if (!s->ready)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "precond_apply before set_matrix");
+    if (s->cfg.precision != SIMALL_PRECISION_FP64)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "precond_apply: the FP64 preconditioners only");
+    SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+    const size_t bytes = static_cast<size_t>(s->n) * sizeof(double);
+    const double *dr = r;
+    double *dz = z;
+    if (mem == SIMALL_MEM_HOST) {  // the solve's own vectors are free between solves
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->p.p, r, bytes, cudaMemcpyHostToDevice, ctx->stream));
+        dr = s->p.p;
+        dz = s->Ap.p;
+    }
+    if (sweep_preconditioner(s->cfg.preconditioner)) {
+        int e = ilu_apply(s, dr, dz);
+        if (e)
+            return e;
+    } else {
+        k_scale_inv<<<grid1(static_cast<size_t>(s->n)), kBlock, 0, ctx->stream>>>(s->n, s->invDiag.p, dr, dz);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    if (mem == SIMALL_MEM_HOST) {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(z, dz, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    return sweep_preconditioner(s->cfg.preconditioner) ? ilu_check(s) : SIMALL_OK;
 }
 
 }  // extern "C"

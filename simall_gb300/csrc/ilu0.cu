@@ -20,6 +20,13 @@
 // mark (acquire).  Rows are handed out in level order, so every row waited for
 // was handed to a warp that is already running; the wait is bounded and a
 // timeout is reported (it never happens unless a row is never produced).
+//
+// SSOR (SsorPreconditioner, :163-231, with the w = 1 that make_preconditioner
+// gives it) has the same dependency structure and runs on the same schedule
+// with A's own values: forward y_i = (r_i - sum_{j<i} a_ij y_j) invD_i,
+// backward z_i = (a_ii y_i - sum_{j>i} a_ij z_j) invD_i, each product and
+// difference rounded as the reference rounds it (w = 1 and 2 - w = 1 scale
+// exactly).
 #include "device.cuh"
 #include "solver.hpp"
 
@@ -172,14 +179,17 @@ __device__ __forceinline__ bool wait_rows4(const unsigned *done, const int (&j)[
     }
 }
 
-// Forward sweep y_i = r_i - sum_{j<i} l_ij y_j over rows in level order.
+// Forward sweep y_i = r_i - sum_{j<i} l_ij y_j over rows in level order
+// (SSOR: a_ij, and the sum times invD_i).
 // Dependencies are taken four at a time: wait for the four marks, load the
 // four values, then apply them in column order (the reference's order).
+template <bool SSOR>
 __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *__restrict__ order,
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const double *__restrict__ lu, const double *__restrict__ r,
-                                                         double *y, unsigned *done, unsigned *ctl)
+                                                         const double *__restrict__ invD, double *y, unsigned *done,
+                                                         unsigned *ctl)
 {
     const int lane = threadIdx.x & 31;
     const unsigned sweep = __ldcg(ctl + 1);
@@ -223,6 +233,8 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
                 if (cnt < 4)
                     break;
             }
+            if (SSOR)
+                s = __dmul_rn(s, __ldg(invD + i));
             __stcg(y + i, s);
             st_release(done + i, sweep);
         }
@@ -231,13 +243,16 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
         atomicOr(ctl + 2, 1u);
 }
 
-// Backward sweep z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii over rows in level order.
+// Backward sweep z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii over rows in level order
+// (SSOR: (a_ii y_i - sum_{j>i} a_ij z_j) invD_i).
+template <bool SSOR>
 __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *__restrict__ order,
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const int32_t *__restrict__ diagPtr,
                                                          const double *__restrict__ lu, const double *__restrict__ y,
-                                                         double *z, unsigned *done, unsigned *ctl)
+                                                         const double *__restrict__ invD, double *z, unsigned *done,
+                                                         unsigned *ctl)
 {
     const int lane = threadIdx.x & 31;
     const unsigned sweep = __ldcg(ctl + 1);
@@ -252,8 +267,10 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
         const int t = base + lane;
         if (t < n) {
             const int i = __ldg(order + t);
-            double s = __ldcg(y + i);
             const int kd = __ldg(diagPtr + i);
+            double s = __ldcg(y + i);
+            if (SSOR)  // v_i = a_ii y_i (the diagonal is present: the CSR contract)
+                s = __dmul_rn(__ldg(lu + kd), s);
             const int end = __ldg(rowPtr + i + 1);
             for (int kp = kd + 1; kp < end;) {
                 int j[4];
@@ -277,8 +294,12 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
                         s = __dsub_rn(s, __dmul_rn(a[q], v[q]));
                 kp += cnt;
             }
-            const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
-            __stcg(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
+            if (SSOR) {
+                __stcg(z + i, __dmul_rn(s, __ldg(invD + i)));
+            } else {
+                const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
+                __stcg(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
+            }
             st_release(done + i, sweep);
         }
     }
@@ -437,10 +458,10 @@ __device__ __forceinline__ void issue_level(const PackedSweep &p, const int *lvl
         const int a = lvl[l], cnt = lvl[l + 1] - a, k = p.k;
         for (int q = threadIdx.x; q < cnt; q += blockDim.x) {
             cp_async4(st.row + q, p.row + a + q);
-            if (p.diag) {
+            if (p.diag)
                 cp_async8(st.diag + q, p.diag + a + q);
+            if (p.rdiag)
                 cp_async8(st.rdiag + q, p.rdiag + a + q);
-            }
         }
         for (int q = threadIdx.x; q < cnt * k; q += blockDim.x) {
             cp_async4(st.col + q, p.col + static_cast<size_t>(a) * k + q);
@@ -452,7 +473,9 @@ __device__ __forceinline__ void issue_level(const PackedSweep &p, const int *lvl
 
 // One triangular sweep in place on ys: forward ys_i -= sum l_ij ys_j, backward
 // the same with u_ij and a final division by the diagonal (when non-zero).
-template <bool BACKWARD>
+// SSOR: forward (ys_i - sum a_ij ys_j) invD_i, backward (a_ii ys_i - sum a_ij
+// ys_j) invD_i.
+template <bool BACKWARD, bool SSOR>
 __device__ __forceinline__ void sweep_levels(const PackedSweep &p, const int *lvl, double *ys, unsigned char *stages,
                                              int stageBytes, int R)
 {
@@ -468,9 +491,13 @@ __device__ __forceinline__ void sweep_levels(const PackedSweep &p, const int *lv
             const int packed = st.row[t];
             const int i = packed & 0xffffff, c = packed >> 24;
             double s = ys[i];
+            if (SSOR && BACKWARD)
+                s = __dmul_rn(st.diag[t], s);
             for (int q = 0; q < c; ++q)
                 s = __dsub_rn(s, __dmul_rn(st.val[t * k + q], ys[st.col[t * k + q]]));
-            if (BACKWARD) {
+            if (SSOR) {
+                s = __dmul_rn(s, st.rdiag[t]);
+            } else if (BACKWARD) {
                 const double dv = st.diag[t];
                 s = dv != 0.0 ? div_rn_by_recip(s, dv, st.rdiag[t]) : s;
             }
@@ -481,7 +508,9 @@ __device__ __forceinline__ void sweep_levels(const PackedSweep &p, const int *lv
     __syncthreads();
 }
 
-// z = (LU)^-1 r in one CTA: ys = r, forward sweep, backward sweep, z = ys.
+// z = (LU)^-1 r (or SSOR's M^-1 r) in one CTA: ys = r, forward sweep, backward
+// sweep, z = ys.
+template <bool SSOR>
 __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_sweeps_small(int n, PackedSweep fwd, PackedSweep bwd,
                                                                        const int *__restrict__ lvlF,
                                                                        const int *__restrict__ lvlB, int R,
@@ -500,22 +529,25 @@ __global__ void __launch_bounds__(kIluSmallThreads) k_ilu_sweeps_small(int n, Pa
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         ys[i] = r[i];
     __syncthreads();
-    sweep_levels<false>(fwd, slF, ys, stages, stageBytes, R);
-    sweep_levels<true>(bwd, slB, ys, stages, stageBytes, R);
+    sweep_levels<false, SSOR>(fwd, slF, ys, stages, stageBytes, R);
+    sweep_levels<true, SSOR>(bwd, slB, ys, stages, stageBytes, R);
     for (int i = threadIdx.x; i < n; i += blockDim.x)
         z[i] = ys[i];
 }
 
 // Values of the packed sweeps from the factor: entry e of position t reads
 // lu[pos[t k + e]] (pos -1: padding); the backward diagonal is lu[diagPtr[i]]
-// (0 when the row has none).
+// (0 when the row has none).  SSOR (frdiag given): lu holds A, rdiag is the
+// inverse diagonal invD of the row in each sweep's order.
 __global__ void __launch_bounds__(kBlock) k_ilu_pack(int n, int kf, int kb, const int32_t *__restrict__ fpos,
                                                      const int32_t *__restrict__ bpos,
+                                                     const int32_t *__restrict__ frow,
                                                      const int32_t *__restrict__ brow,
                                                      const int32_t *__restrict__ diagPtr,
-                                                     const double *__restrict__ lu, double *__restrict__ fval,
-                                                     double *__restrict__ bval, double *__restrict__ bdiag,
-                                                     double *__restrict__ brdiag)
+                                                     const double *__restrict__ lu, const double *__restrict__ invD,
+                                                     double *__restrict__ fval, double *__restrict__ bval,
+                                                     double *__restrict__ bdiag, double *__restrict__ brdiag,
+                                                     double *__restrict__ frdiag)
 {
     const int stride = gridDim.x * blockDim.x;
     for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < n * kf; e += stride) {
@@ -527,10 +559,16 @@ __global__ void __launch_bounds__(kBlock) k_ilu_pack(int n, int kf, int kb, cons
         bval[e] = q >= 0 ? lu[q] : 0.0;
     }
     for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < n; t += stride) {
-        const int kd = diagPtr[brow[t] & 0xffffff];
+        const int bi = brow[t] & 0xffffff;
+        const int kd = diagPtr[bi];
         const double d = kd >= 0 ? lu[kd] : 0.0;
         bdiag[t] = d;
-        brdiag[t] = d != 0.0 ? __drcp_rn(d) : 0.0;
+        if (frdiag) {
+            brdiag[t] = invD[bi];
+            frdiag[t] = invD[frow[t] & 0xffffff];
+        } else {
+            brdiag[t] = d != 0.0 ? __drcp_rn(d) : 0.0;
+        }
     }
 }
 
@@ -707,7 +745,12 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
             SIMALL_CUDA_TRY(ctx, d->bdiag.alloc(n));
             SIMALL_CUDA_TRY(ctx, d->brdiag.alloc(n));
             SIMALL_CUDA_TRY(ctx, d->rpiv.alloc(n));
-            SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small, cudaFuncAttributeMaxDynamicSharedMemorySize,
+            SIMALL_CUDA_TRY(ctx, d->frdiag.alloc(d->mode == 1 ? n : 1));
+            SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small<false>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                      static_cast<int>(smemBytes)));
+            SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ilu_sweeps_small<true>,
+                                                      cudaFuncAttributeMaxDynamicSharedMemorySize,
                                                       static_cast<int>(smemBytes)));
             // the copies above read host vectors that die at return
             SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -728,6 +771,19 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
     return SIMALL_OK;
 }
 
+// The packed single-CTA sweep values from lu (the factor, or A for SSOR).
+int pack(simall_context *ctx, IluData *d)
+{
+    const int n = static_cast<int>(d->h_diagPtr.size());
+    const int items = n * std::max(d->kf, d->kb);
+    const bool ssor = d->mode == 1;
+    k_ilu_pack<<<std::min((items + kBlock - 1) / kBlock, ctx->num_sms * 8), kBlock, 0, ctx->stream>>>(
+        n, d->kf, d->kb, d->fpos.p, d->bpos.p, d->frow.p, d->brow.p, d->diagPtr.p, d->lu.p, ssor ? d->invD : nullptr,
+        d->fval.p, d->bval.p, d->bdiag.p, d->brdiag.p, ssor ? d->frdiag.p : nullptr);
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
 int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx)
 {
     const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
@@ -735,13 +791,7 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
         k_ilu_factor_small<<<1, d->smallThreads, 0, ctx->stream>>>(nlev, d->fwdLvl.p, d->fwdRows.p, rowPtr, colIdx,
                                                                   d->diagPtr.p, d->lu.p, d->rpiv.p);
         SIMALL_LAUNCH_CHECK(ctx);
-        const int n = static_cast<int>(d->h_diagPtr.size());
-        const int items = n * std::max(d->kf, d->kb);
-        k_ilu_pack<<<std::min((items + kBlock - 1) / kBlock, ctx->num_sms * 8), kBlock, 0, ctx->stream>>>(
-            n, d->kf, d->kb, d->fpos.p, d->bpos.p, d->brow.p, d->diagPtr.p, d->lu.p, d->fval.p, d->bval.p, d->bdiag.p,
-            d->brdiag.p);
-        SIMALL_LAUNCH_CHECK(ctx);
-        return SIMALL_OK;
+        return pack(ctx, d);
     }
     for (int l = 1; l < nlev; ++l) {  // level 0 rows have no lower entries
         const int a = d->fwdLevelPtr[l], cnt = d->fwdLevelPtr[l + 1] - a;
@@ -756,26 +806,30 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
            const double *r, double *z)
 {
     const int n = static_cast<int>(d->h_diagPtr.size());
+    const bool ssor = d->mode == 1;
     if (d->small && lu == d->lu.p) {
-        PackedSweep f{d->frow.p, d->fcol.p, d->fval.p, nullptr, nullptr, static_cast<int>(d->fwdLevelPtr.size()) - 1,
-                      d->kf};
+        PackedSweep f{d->frow.p, d->fcol.p, d->fval.p, nullptr, ssor ? d->frdiag.p : nullptr,
+                      static_cast<int>(d->fwdLevelPtr.size()) - 1, d->kf};
         PackedSweep b{d->brow.p, d->bcol.p, d->bval.p, d->bdiag.p, d->brdiag.p,
                       static_cast<int>(d->bwdLevelPtr.size()) - 1, d->kb};
-        k_ilu_sweeps_small<<<1, d->smallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p,
-                                                                              d->stageRows, d->stageBytes, r, z);
+        auto kern = ssor ? k_ilu_sweeps_small<true> : k_ilu_sweeps_small<false>;
+        kern<<<1, d->smallThreads, d->smallSmem, ctx->stream>>>(n, f, b, d->fwdLvl.p, d->bwdLvl.p, d->stageRows,
+                                                                d->stageBytes, r, z);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
     const int grid = ctx->num_sms * 4;  // 32 warps per SM take rows; more only add waiting warps
     k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_ilu_fwd_free<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->y.p, d->done.p,
-                                                     d->sweepCtl.p);
+    auto fwd = ssor ? k_ilu_fwd_free<true> : k_ilu_fwd_free<false>;
+    fwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->invD, d->y.p, d->done.p,
+                                          d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_ilu_bwd_free<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, z,
-                                                     d->done.p, d->sweepCtl.p);
+    auto bwd = ssor ? k_ilu_bwd_free<true> : k_ilu_bwd_free<false>;
+    bwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, d->invD, z,
+                                          d->done.p, d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
@@ -791,6 +845,8 @@ int ilu_setup(simall_solver *s)
             return SIMALL_ERR_OUT_OF_MEMORY;
     }
     IluData *d = s->ilu;
+    d->mode = s->cfg.preconditioner == SIMALL_PRECOND_SSOR ? 1 : 0;
+    d->invD = s->invDiag.p;  // SSOR: set up by the caller for the current values
     if (!d->analysed) {
         int hp = solver_host_pattern(s);
         if (hp)
@@ -802,6 +858,8 @@ int ilu_setup(simall_solver *s)
     SIMALL_CUDA_TRY(ctx, d->lu.alloc(s->nnz));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->lu.p, s->values, s->nnz * sizeof(double), cudaMemcpyDeviceToDevice,
                                          ctx->stream));
+    if (d->mode == 1)  // SSOR sweeps A itself
+        return d->small ? pack(ctx, d) : SIMALL_OK;
     return factor(ctx, d, s->rowPtr, s->colIdx);
 }
 

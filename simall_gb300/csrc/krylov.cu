@@ -1,6 +1,7 @@
 // The non-symmetric Krylov solvers on the device, FP64: the GB300 replacement
-// of BiCGSTABSolver::solve (src/solver/LinearSolvers.cpp:363-405) and
-// GMRESmSolver::solve (:268-343), with the Jacobi or ILU(0) preconditioner.
+// of BiCGSTABSolver::solve (src/solver/LinearSolvers.cpp:363-405),
+// GMRESmSolver::solve (:268-343) and TfqmrSolver::solve (:497-609), with the
+// Jacobi, ILU(0) or SSOR preconditioner.
 // Both start from x = 0 and follow the reference's recurrences, stop tests and
 // return values step for step; only the order of the FP64 sums inside each dot
 // product differs (grid reductions instead of one serial loop).
@@ -29,6 +30,17 @@
 //         the stop test.
 // Each step is one captured graph; the host polls the cycle's stop flag after
 // every step.  A cycle ends with the triangular solve (one CTA) and x += V y.
+//
+// TFQMR, one iteration (Jacobi: six kernels; ILU(0)/SSOR add two sweep pairs):
+//   T1  u2 = u1 - alpha M v
+//   T2  Au2 = A u2; both half steps' w -= alpha Au and |w|^2 -> theta, c,
+//       tau, eta of each half step, the residual bound and the check flag
+//   T3  d = u + coef d, x += eta d (both half steps); r -= alpha (Au1 + Au2);
+//       rh.r -> beta (or the rho breakdown test)
+//   T4  only when the bound passed: |b - A x| -> stop, or go on as T3 would
+//   T5  u1 = M r + beta (u2 + beta u1)
+//   T6  Au1 = A u1; v = Au1 + beta (Au2 + beta v); rh.v -> the iteration
+//       count, the sigma breakdown test and alpha
 #include "device.cuh"
 #include "solver.hpp"
 
@@ -48,19 +60,24 @@ struct KrylovScalars {
     int jdone;      // GMRES: Arnoldi steps taken in this cycle
     int cycle_stop;
     int cycles;
+    // TFQMR
+    double tau, theta, eta, coef[2], etaStep[2];
+    int check;  // the residual bound passed: T4 takes the true residual
     unsigned counter[8];
 };
 
 struct KrylovData {
     // BiCGSTAB vectors beside the solver's x, r, p, z, b
     DevBuf<double> rh, v, sv, t, y;
+    // TFQMR (beside rh, v and the solver's x, r, z, b)
+    DevBuf<double> tw, td, tu1, tu2, tAu1, tAu2;
     // GMRES
     int m = 0;
     int64_t ldV = 0;
     DevBuf<double> V, w, zb[2], hs;
     DevBuf<KrylovScalars> ks;
     KrylovScalars *h_ks = nullptr;
-    std::vector<GraphChunk> chunks;        // BiCGSTAB iteration chunks
+    std::vector<GraphChunk> chunks;        // BiCGSTAB / TFQMR iteration chunks
     std::vector<cudaGraphExec_t> steps;    // GMRES step j
     std::vector<int64_t> stepKernels;
     cudaGraphExec_t restart = nullptr, finish = nullptr;
@@ -287,6 +304,266 @@ __global__ void __launch_bounds__(kBlock) k_bi_update(int64_t n, double *__restr
             return;
         }
         k->beta = (rhoNew / k->rho) * (k->alpha / k->omega);
+    }
+}
+
+// ---------------------------------------------------------------- TFQMR
+
+// T0: x = 0, d = 0, r = rh = w = b, u1 = invD b (Jacobi); |b| -> tau, bnorm, rho
+__global__ void __launch_bounds__(kBlock) k_tf_init(int64_t n, const double *__restrict__ b, double *__restrict__ x,
+                                                    double *__restrict__ r, double *__restrict__ rh,
+                                                    double *__restrict__ w, double *__restrict__ d,
+                                                    const double *__restrict__ invD, double *__restrict__ u1,
+                                                    double *partials, KrylovScalars *k)
+{
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double bi = b[i];
+        x[i] = 0.0;
+        d[i] = 0.0;
+        r[i] = bi;
+        rh[i] = bi;
+        w[i] = bi;
+        if (invD)
+            u1[i] = invD[i] * bi;
+        acc[0] += bi * bi;
+    }
+    if (grid_sum_last<1>(acc, partials, &k->counter[0]) && threadIdx.x == 0) {
+        const double tau = sqrt(acc[0]);
+        k->tau = tau;
+        k->bnorm = std_max(tau, 1e-30);
+        k->rho = acc[0];  // rh.r with rh = r = b
+        k->theta = k->eta = k->alpha = 0.0;
+        k->iter = 0;
+        k->check = 0;
+        k->status = SIMALL_OK;
+        k->done = 0;
+        k->result = 0;
+        if (tau / k->bnorm < k->tol) {
+            k->last = tau / k->bnorm;
+            k->done = 1;
+        } else if (k->max_iter <= 0) {  // the loop does not run; last_residual is left as it was
+            k->done = 1;
+            k->result = k->max_iter;
+        }
+    }
+}
+
+// The sigma test and alpha, at the top of an iteration (thread 0 of a last CTA).
+__device__ __forceinline__ void tf_top(KrylovScalars *k, double sigma)
+{
+    if (fabs(sigma) < 1.0e-30) {
+        k->last = k->tau / k->bnorm;
+        k->result = k->iter;
+        k->done = 1;
+        return;
+    }
+    k->alpha = k->rho / sigma;
+}
+
+struct TfVEpi {
+    double *Au1, *v;
+    const double *Au2, *rh;
+    double beta, acc;
+    bool first;
+    __device__ __forceinline__ void operator()(int row, double val)
+    {
+        Au1[row] = val;
+        const double vi = first ? val : val + beta * (Au2[row] + beta * v[row]);
+        v[row] = vi;
+        acc += __ldg(rh + row) * vi;
+    }
+};
+
+// T6 (and the start, first = 1): Au1 = A u1, v = Au1 + beta (Au2 + beta v)
+// (v = Au1 at the start), sigma = rh.v; the iteration count, maxIterations,
+// the sigma test and alpha.
+__global__ void __launch_bounds__(kBlock) k_tf_spmv_u1(const int32_t *__restrict__ rowPtr,
+                                                       const int32_t *__restrict__ colIdx,
+                                                       const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                       int nRB, const double *__restrict__ u1, double *__restrict__ Au1,
+                                                       const double *__restrict__ Au2, double *__restrict__ v,
+                                                       const double *__restrict__ rh, double *partials,
+                                                       KrylovScalars *k, int first)
+{
+    if (kdone(k))
+        return;
+    TfVEpi epi{Au1, v, Au2, rh, first ? 0.0 : __ldcg(&k->beta), 0.0, first != 0};
+    spmv_rowblocks_fma(rowPtr, colIdx, val, rb, nRB, u1, epi);
+    double acc[1] = {epi.acc};
+    if (grid_sum_last<1>(acc, partials, &k->counter[4]) && threadIdx.x == 0) {
+        if (!first) {
+            k->rho = k->rhoNew;
+            k->iter += 1;
+            if (k->iter >= k->max_iter) {
+                k->result = k->max_iter;
+                k->done = 1;
+                return;
+            }
+        }
+        tf_top(k, acc[0]);
+    }
+}
+
+// T1: u2 = u1 - alpha z, z = invD v (Jacobi) or the sweeps' M v.
+__global__ void __launch_bounds__(kBlock) k_tf_u2(int64_t n, const double *__restrict__ u1,
+                                                  const double *__restrict__ v, const double *__restrict__ invD,
+                                                  const double *__restrict__ z, double *__restrict__ u2,
+                                                  const KrylovScalars *k)
+{
+    if (kdone(k))
+        return;
+    const double alpha = __ldcg(&k->alpha);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double zi = invD ? invD[i] * v[i] : z[i];
+        u2[i] = u1[i] - alpha * zi;
+    }
+}
+
+struct TfWEpi {
+    double *Au2, *w;
+    const double *Au1;
+    double alpha, ww1, ww2;
+    __device__ __forceinline__ void operator()(int row, double val)
+    {
+        Au2[row] = val;
+        const double w1 = w[row] - alpha * Au1[row];
+        const double w2 = w1 - alpha * val;
+        w[row] = w2;
+        ww1 += w1 * w1;
+        ww2 += w2 * w2;
+    }
+};
+
+// One quasi-minimal-residual half step from |w| (thread 0 of a last CTA).
+__device__ __forceinline__ void tf_half(KrylovScalars *k, int h, double wnorm, double alpha)
+{
+    const double theta_new = wnorm / std_max(k->tau, 1.0e-30);
+    const double c = 1.0 / sqrt(1.0 + theta_new * theta_new);
+    k->coef[h] = k->theta * k->theta * k->eta / std_max(alpha, 1.0e-30);
+    k->etaStep[h] = c * c * alpha;
+    k->tau = k->tau * theta_new * c;
+    k->theta = theta_new;
+    k->eta = k->etaStep[h];
+}
+
+// T2: Au2 = A u2; w -= alpha Au1 and then alpha Au2, the norm after each; the
+// scalars of both half steps and the residual bound.
+__global__ void __launch_bounds__(kBlock) k_tf_spmv_u2(const int32_t *__restrict__ rowPtr,
+                                                       const int32_t *__restrict__ colIdx,
+                                                       const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                       int nRB, const double *__restrict__ u2, double *__restrict__ Au2,
+                                                       const double *__restrict__ Au1, double *__restrict__ w,
+                                                       double *partials, KrylovScalars *k)
+{
+    if (kdone(k))
+        return;
+    const double alpha = __ldcg(&k->alpha);
+    TfWEpi epi{Au2, w, Au1, alpha, 0.0, 0.0};
+    spmv_rowblocks_fma(rowPtr, colIdx, val, rb, nRB, u2, epi);
+    double acc[2] = {epi.ww1, epi.ww2};
+    if (grid_sum_last<2>(acc, partials, &k->counter[1]) && threadIdx.x == 0) {
+        tf_half(k, 0, sqrt(acc[0]), alpha);
+        tf_half(k, 1, sqrt(acc[1]), alpha);
+        const double resBound = k->tau * sqrt(2.0 * (k->iter + 1) + 1.0);
+        k->last = resBound / k->bnorm;
+        k->check = k->last < k->tol ? 1 : 0;
+    }
+}
+
+// After x and r are updated (and the true residual, when taken, failed): the
+// rho test on the previous rho, else beta.
+__device__ __forceinline__ void tf_beta(KrylovScalars *k)
+{
+    if (fabs(k->rho) < 1.0e-30) {
+        k->last = k->tau / k->bnorm;
+        k->result = k->iter;
+        k->done = 1;
+        return;
+    }
+    k->beta = k->rhoNew / k->rho;
+}
+
+// T3: d = u1 + coef0 d, x += eta0 d, d = u2 + coef1 d, x += eta1 d;
+// r -= alpha (Au1 + Au2), rh.r -> rhoNew (and beta unless the check is due).
+__global__ void __launch_bounds__(kBlock) k_tf_update(int64_t n, const double *__restrict__ u1,
+                                                      const double *__restrict__ u2, const double *__restrict__ Au1,
+                                                      const double *__restrict__ Au2, double *__restrict__ d,
+                                                      double *__restrict__ x, double *__restrict__ r,
+                                                      const double *__restrict__ rh, double *partials,
+                                                      KrylovScalars *k)
+{
+    if (kdone(k))
+        return;
+    const double alpha = __ldcg(&k->alpha);
+    const double c0 = __ldcg(&k->coef[0]), c1 = __ldcg(&k->coef[1]);
+    const double e0 = __ldcg(&k->etaStep[0]), e1 = __ldcg(&k->etaStep[1]);
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        double di = u1[i] + c0 * d[i];
+        double xi = x[i] + e0 * di;
+        di = u2[i] + c1 * di;
+        x[i] = xi + e1 * di;
+        d[i] = di;
+        const double ri = r[i] - alpha * (Au1[i] + Au2[i]);
+        r[i] = ri;
+        acc[0] += rh[i] * ri;
+    }
+    if (grid_sum_last<1>(acc, partials, &k->counter[2]) && threadIdx.x == 0) {
+        k->rhoNew = acc[0];
+        if (!k->check)
+            tf_beta(k);
+    }
+}
+
+struct TfResEpi {
+    const double *b;
+    double acc;
+    __device__ __forceinline__ void operator()(int row, double val)
+    {
+        const double ri = __ldg(b + row) - val;
+        acc += ri * ri;
+    }
+};
+
+// T4: when the bound passed, |b - A x| / bnorm is the residual: stop below
+// the tolerance, else the rho test and beta.
+__global__ void __launch_bounds__(kBlock) k_tf_check(const int32_t *__restrict__ rowPtr,
+                                                     const int32_t *__restrict__ colIdx,
+                                                     const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                     int nRB, const double *__restrict__ x,
+                                                     const double *__restrict__ b, double *partials,
+                                                     KrylovScalars *k)
+{
+    if (kdone(k) || !__ldcg(&k->check))
+        return;
+    TfResEpi epi{b, 0.0};
+    spmv_rowblocks_fma(rowPtr, colIdx, val, rb, nRB, x, epi);
+    double acc[1] = {epi.acc};
+    if (grid_sum_last<1>(acc, partials, &k->counter[3]) && threadIdx.x == 0) {
+        k->check = 0;
+        k->last = sqrt(acc[0]) / k->bnorm;
+        if (k->last < k->tol) {
+            k->result = k->iter + 1;
+            k->done = 1;
+            return;
+        }
+        tf_beta(k);
+    }
+}
+
+// T5: u1 = z + beta (u2 + beta u1), z = invD r (Jacobi) or the sweeps' M r.
+__global__ void __launch_bounds__(kBlock) k_tf_u1(int64_t n, const double *__restrict__ r,
+                                                  const double *__restrict__ invD, const double *__restrict__ z,
+                                                  const double *__restrict__ u2, double *__restrict__ u1,
+                                                  const KrylovScalars *k)
+{
+    if (kdone(k))
+        return;
+    const double beta = __ldcg(&k->beta);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double zi = invD ? invD[i] * r[i] : z[i];
+        u1[i] = zi + beta * (u2[i] + beta * u1[i]);
     }
 }
 
@@ -623,6 +900,15 @@ int alloc_data(simall_solver *s)
         SIMALL_CUDA_TRY(ctx, d->sv.alloc(n));
         SIMALL_CUDA_TRY(ctx, d->t.alloc(n));
         SIMALL_CUDA_TRY(ctx, d->y.alloc(n));
+    } else if (s->cfg.kind == SIMALL_SOLVER_TFQMR) {
+        SIMALL_CUDA_TRY(ctx, d->rh.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->v.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->tw.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->td.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->tu1.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->tu2.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->tAu1.alloc(n));
+        SIMALL_CUDA_TRY(ctx, d->tAu2.alloc(n));
     } else {
         const int m = s->cfg.restart > 1 ? s->cfg.restart : 1;
         if (m != d->m || d->ldV < static_cast<int64_t>(n)) {
@@ -642,7 +928,8 @@ int alloc_data(simall_solver *s)
     return SIMALL_OK;
 }
 
-bool use_ilu(const simall_solver *s) { return s->cfg.preconditioner == SIMALL_PRECOND_ILU0; }
+// ILU(0) or SSOR: the preconditioner is applied by the triangular sweeps
+bool use_ilu(const simall_solver *s) { return sweep_preconditioner(s->cfg.preconditioner); }
 
 int enqueue_bicgstab_iteration(simall_solver *s)
 {
@@ -671,6 +958,8 @@ int enqueue_bicgstab_iteration(simall_solver *s)
     KLAUNCH(k_bi_update, n, n, s->x.p, d->y.p, s->z.p, s->r.p, d->sv.p, d->t.p, d->rh.p, s->partials.p, k);
     return SIMALL_OK;
 }
+
+int enqueue_tfqmr_iteration(simall_solver *s);
 
 // Captures what `enqueue` puts on the stream into a graph; *kernels = launches it holds.
 template <class F> int capture(simall_solver *s, F &&enqueue, cudaGraphExec_t *out, int64_t *kernels)
@@ -715,12 +1004,31 @@ int fetch(simall_solver *s)
     return SIMALL_OK;
 }
 
-int bicgstab_solve(simall_solver *s)
+// BiCGSTAB and TFQMR: the start, then chunks of captured iterations until the
+// stop flag is raised.
+int chunked_solve(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
     KrylovData *d = s->krylov;
     const int64_t n = s->n;
-    KLAUNCH(k_bi_init, n, n, s->b.p, s->x.p, s->r.p, d->rh.p, s->p.p, d->v.p, s->partials.p, d->ks.p);
+    const bool tfqmr = s->cfg.kind == SIMALL_SOLVER_TFQMR;
+    if (tfqmr) {
+        const bool ilu = use_ilu(s);
+        KLAUNCH(k_tf_init, n, n, s->b.p, s->x.p, s->r.p, d->rh.p, d->tw.p, d->td.p, ilu ? nullptr : s->invDiag.p,
+                d->tu1.p, s->partials.p, d->ks.p);
+        if (ilu) {
+            int e = ilu_apply(s, s->r.p, d->tu1.p);
+            if (e)
+                return e;
+        }
+        const int64_t rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+        KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu1.p,
+                d->tAu1.p, d->tAu2.p, d->v.p, d->rh.p, s->partials.p, d->ks.p, 1);
+    } else {
+        KLAUNCH(k_bi_init, n, n, s->b.p, s->x.p, s->r.p, d->rh.p, s->p.p, d->v.p, s->partials.p, d->ks.p);
+    }
+    const int perIter = tfqmr ? (use_ilu(s) ? 6 + 2 * ilu_apply_launches(s) : 6)
+                              : (use_ilu(s) ? 5 + 2 * ilu_apply_launches(s) : 5);
     int done_iters = 0;
     int chunk = s->cfg.check_interval > 0 ? s->cfg.check_interval : 8;
     for (;;) {
@@ -738,7 +1046,7 @@ int bicgstab_solve(simall_solver *s)
                 [&]() {
                     int st = SIMALL_OK;
                     for (int i = 0; i < len && st == SIMALL_OK; ++i)
-                        st = enqueue_bicgstab_iteration(s);
+                        st = tfqmr ? enqueue_tfqmr_iteration(s) : enqueue_bicgstab_iteration(s);
                     return st;
                 },
                 &c.exec, &per);
@@ -747,7 +1055,7 @@ int bicgstab_solve(simall_solver *s)
             d->chunks.push_back(c);
             g = &d->chunks.back();
         } else {
-            per = static_cast<int64_t>(len) * (use_ilu(s) ? 5 + 2 * ilu_apply_launches(s) : 5);
+            per = static_cast<int64_t>(len) * perIter;
         }
         int e = replay(ctx, g->exec, per);
         if (e)
@@ -759,10 +1067,41 @@ int bicgstab_solve(simall_solver *s)
         if (d->h_ks->done)
             return SIMALL_OK;
         if (done_iters > s->cfg.max_iterations + 64)
-            return fail(ctx, SIMALL_ERR_CUDA, "BiCGSTAB did not raise its stop flag");
+            return fail(ctx, SIMALL_ERR_CUDA, "%s did not raise its stop flag", tfqmr ? "TFQMR" : "BiCGSTAB");
         if (s->cfg.check_interval <= 0)
             chunk = chunk < 64 ? chunk * 2 : 64;
     }
+}
+
+int enqueue_tfqmr_iteration(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    KrylovData *d = s->krylov;
+    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    const bool ilu = use_ilu(s);
+    const double *invD = ilu ? nullptr : s->invDiag.p;
+    KrylovScalars *k = d->ks.p;
+    if (ilu) {
+        int e = ilu_apply(s, d->v.p, s->z.p);
+        if (e)
+            return e;
+    }
+    KLAUNCH(k_tf_u2, n, n, d->tu1.p, d->v.p, invD, s->z.p, d->tu2.p, k);
+    KLAUNCH(k_tf_spmv_u2, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu2.p,
+            d->tAu2.p, d->tAu1.p, d->tw.p, s->partials.p, k);
+    KLAUNCH(k_tf_update, n, n, d->tu1.p, d->tu2.p, d->tAu1.p, d->tAu2.p, d->td.p, s->x.p, s->r.p, d->rh.p,
+            s->partials.p, k);
+    KLAUNCH(k_tf_check, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->x.p, s->b.p,
+            s->partials.p, k);
+    if (ilu) {
+        int e = ilu_apply(s, s->r.p, s->z.p);
+        if (e)
+            return e;
+    }
+    KLAUNCH(k_tf_u1, n, n, s->r.p, invD, s->z.p, d->tu2.p, d->tu1.p, k);
+    KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu1.p,
+            d->tAu1.p, d->tAu2.p, d->v.p, d->rh.p, s->partials.p, k, 0);
+    return SIMALL_OK;
 }
 
 int enqueue_gmres_restart(simall_solver *s)
@@ -915,7 +1254,8 @@ int krylov_solve(simall_solver *s)
                                          ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&d->ks.p->max_iter, &init.max_iter, sizeof(int), cudaMemcpyHostToDevice,
                                          ctx->stream));
-    e = s->cfg.kind == SIMALL_SOLVER_BICGSTAB ? bicgstab_solve(s) : gmres_solve(s);
+    e = (s->cfg.kind == SIMALL_SOLVER_BICGSTAB || s->cfg.kind == SIMALL_SOLVER_TFQMR) ? chunked_solve(s)
+                                                                                     : gmres_solve(s);
     if (e)
         return e;
     // publish the outcome where the common solve path reads it

@@ -473,6 +473,9 @@ int setup_values(simall_solver *s)
     k_jacobi_setup<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->rowPtr, s->colIdx, s->values,
                                                                      s->invDiag.p);
     SIMALL_LAUNCH_CHECK(ctx);
+    // SSOR's inverse diagonal is Jacobi's (SsorPreconditioner::setup, LinearSolvers.cpp:168-186)
+    if (s->cfg.preconditioner == SIMALL_PRECOND_SSOR)
+        return ilu_setup(s);
     return SIMALL_OK;
 }
 
@@ -513,7 +516,7 @@ int enqueue_iteration(simall_solver *s)
     k_spmv_pap<<<resident_grid(ctx, reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0, ctx->stream>>>(
         s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+    if (sweep_preconditioner(s->cfg.preconditioner)) {
         k_update_xr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_update_xr), n), kBlock, 0, ctx->stream>>>(
             n, s->p.p, s->Ap.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
@@ -538,7 +541,7 @@ int enqueue_iteration(simall_solver *s)
 // Kernels one FP64 iteration launches (for the launch counter of graph replays).
 int64_t kernels_per_iteration(const simall_solver *s)
 {
-    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0 && s->ilu)
+    if (sweep_preconditioner(s->cfg.preconditioner) && s->ilu)
         return 4 + ilu_apply_launches(s);  // SpMV, x/r update, r.z/beta, direction + the sweeps
     return 3;
 }
@@ -592,7 +595,7 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
         if (cluster_fp64_solve(s, &cst))
             return cst;
     }
-    if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+    if (sweep_preconditioner(s->cfg.preconditioner)) {
         k_init_plain<<<g, kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         int e = ilu_apply(s, s->r.p, s->z.p);
@@ -721,16 +724,17 @@ int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, s
         c = *cfg;
     if (c.preconditioner == SIMALL_PRECOND_NONE)
         c.preconditioner = SIMALL_PRECOND_JACOBI;
-    if (c.preconditioner != SIMALL_PRECOND_JACOBI && c.preconditioner != SIMALL_PRECOND_ILU0)
+    if (c.preconditioner != SIMALL_PRECOND_JACOBI && !sweep_preconditioner(c.preconditioner))
         return fail(ctx, SIMALL_ERR_UNSUPPORTED, "preconditioner %d is not on the pressure path", c.preconditioner);
     if (c.precision != SIMALL_PRECISION_FP64 && c.precision != SIMALL_PRECISION_MIXED)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "precision %d", c.precision);
     if (c.precision == SIMALL_PRECISION_MIXED && c.preconditioner != SIMALL_PRECOND_JACOBI)
         return fail(ctx, SIMALL_ERR_UNSUPPORTED, "mixed precision runs with the Jacobi preconditioner");
-    if (c.kind != SIMALL_SOLVER_CG && c.kind != SIMALL_SOLVER_GMRES && c.kind != SIMALL_SOLVER_BICGSTAB)
+    if (c.kind != SIMALL_SOLVER_CG && c.kind != SIMALL_SOLVER_GMRES && c.kind != SIMALL_SOLVER_BICGSTAB &&
+        c.kind != SIMALL_SOLVER_TFQMR)
         return fail(ctx, SIMALL_ERR_UNSUPPORTED, "solver kind %d is not on this path", c.kind);
     if (c.kind != SIMALL_SOLVER_CG && c.precision != SIMALL_PRECISION_FP64)
-        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "GMRES and BiCGSTAB run in FP64");
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "GMRES, BiCGSTAB and TFQMR run in FP64");
     if (c.kind == SIMALL_SOLVER_GMRES && c.restart < 1)
         c.restart = 1;  // std::max(1, restart), LinearSolvers.cpp:273
     if (!(c.tolerance >= 0.0) || c.reliable_delta <= 0.0 || c.reliable_delta >= 1.0)
@@ -946,7 +950,7 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
         st = mixed_solve(s, &local);
     else
         st = fp64_solve(s, &local);
-    if (!st && s->cfg.preconditioner == SIMALL_PRECOND_ILU0)
+    if (!st && sweep_preconditioner(s->cfg.preconditioner))
         st = ilu_check(s);
     if (st)
         return st;

@@ -26,6 +26,11 @@ struct IluData {
     DevBuf<int32_t> frow, brow, fcol, bcol, fpos, bpos;
     DevBuf<double> fval, bval, bdiag, brdiag;  // refreshed from lu after every factorisation
     DevBuf<double> rpiv;                        // reciprocals of the pivots (factor)
+    // SSOR (w = 1) runs on the same level schedule: no factor, lu holds A's
+    // values, the sweeps scale by the inverse diagonal invD (the Jacobi one)
+    int mode = 0;                  // 0 ILU(0), 1 SSOR
+    const double *invD = nullptr;  // SSOR: 1/a_ii (1.0 where a_ii == 0)
+    DevBuf<double> frdiag;         // SSOR, single-CTA path: invD in forward level order
 };
 
 struct MixedData;  // mixed.cu
@@ -72,7 +77,9 @@ struct simall_solver {
 
 namespace simall {
 
-int ilu_setup(simall_solver *s);
+// The preconditioners applied by triangular sweeps: ILU(0) and SSOR.
+inline bool sweep_preconditioner(int pc) { return pc == SIMALL_PRECOND_ILU0 || pc == SIMALL_PRECOND_SSOR; }
+int ilu_setup(simall_solver *s);  // ILU(0) factor, or SSOR's sweep data (cfg.preconditioner)
 int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);
 int ilu_apply_launches(const simall_solver *s);  // kernels one ilu_apply enqueues

@@ -257,6 +257,13 @@ class GpuCGSolver:
         py, _ = ptr_and_mem(y)
         check(self.L.simall_solver_spmv(self.handle, px, py, mx), self.ctx.handle)
 
+    def precond_apply(self, r, z):
+        """z = M^-1 r with the preconditioner set up for the current matrix
+        (IPreconditioner::apply, src/solver/LinearSolvers.hpp:33-34)."""
+        pr, mr = ptr_and_mem(r)
+        pz, _ = ptr_and_mem(z)
+        check(self.L.simall_solver_precond_apply(self.handle, pr, pz, mr), self.ctx.handle)
+
     def close(self):
         if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             self.L.simall_solver_destroy(self.handle)
@@ -270,15 +277,14 @@ class GpuCGSolver:
 
 
 class GpuLinearSolver(GpuCGSolver):
-    """ILinearSolver of the kind cfg.kind names: GMRES(cfg.restart) or BiCGSTAB
-    (GMRESmSolver / BiCGSTABSolver, src/solver/LinearSolvers.cpp:268-405) in
-    FP64 with the Jacobi or ILU(0) preconditioner, or CG."""
+    """ILinearSolver of the kind cfg.kind names: GMRES(cfg.restart), BiCGSTAB
+    or TFQMR (GMRESmSolver / BiCGSTABSolver / TfqmrSolver,
+    src/solver/LinearSolvers.cpp:268-405, :497-609) in FP64 with the Jacobi,
+    ILU(0) or SSOR preconditioner, or CG."""
 
     def __init__(self, cfg: LinearSolverConfig | None = None, ctx: Context | None = None, check_interval: int = 0,
                  **kw):
         cfg = cfg or LinearSolverConfig()
-        if cfg.kind == LinearSolverKind.TFQMR:
-            raise NotImplementedError("TFQMR is not provided on the GPU")
         super().__init__(cfg, ctx=ctx, check_interval=check_interval, _kind=cfg.kind, **kw)
 
 
@@ -296,9 +302,14 @@ def make_bicgstab(cfg: LinearSolverConfig, **kw) -> GpuLinearSolver:
                                               cfg.maxIterations, cfg.restart), **kw)
 
 
+def make_tfqmr(cfg: LinearSolverConfig, **kw) -> GpuLinearSolver:
+    return GpuLinearSolver(LinearSolverConfig(LinearSolverKind.TFQMR, cfg.preconditioner, cfg.tolerance,
+                                              cfg.maxIterations, cfg.restart), **kw)
+
+
 def make_linear_solver(cfg: LinearSolverConfig, **kw) -> GpuCGSolver:
-    """make_linear_solver (src/solver/Solver.cpp:25-39): CG, GMRES(m) and
-    BiCGSTAB run on the device; TFQMR is not provided."""
+    """make_linear_solver (src/solver/Solver.cpp:25-39): CG, GMRES(m),
+    BiCGSTAB and TFQMR all run on the device."""
     if cfg.kind == LinearSolverKind.CG:
         return GpuCGSolver(cfg, **kw)
     return GpuLinearSolver(cfg, **kw)

@@ -1,10 +1,14 @@
-"""GMRES(m) and BiCGSTAB on the device (GMRESmSolver / BiCGSTABSolver,
-src/solver/LinearSolvers.cpp:268-405) against the oracle's restatement and the
-reference's own results (tests/golden/momentum_7x6x5_rcm_bdf2.npz): the same
-iteration count (within one, the FP64 dot products are summed in another
-order), a solution within the solve's own accuracy, and the reference's
-return values on the edge cases (b = 0, maxIterations reached mid-cycle,
-maxIterations = 0)."""
+"""GMRES(m), BiCGSTAB and TFQMR on the device (GMRESmSolver / BiCGSTABSolver /
+TfqmrSolver, src/solver/LinearSolvers.cpp:268-405, :497-609) with Jacobi,
+ILU(0) and SSOR, against the oracle's restatement and the reference's own
+results (tests/golden/momentum_7x6x5_rcm_bdf2.npz): the same iteration count
+(within one, the FP64 dot products are summed in another order), a solution
+within the solve's own accuracy, and the reference's return values on the
+edge cases (b = 0, maxIterations reached mid-cycle, maxIterations = 0).
+
+The reference's TFQMR often breaks down or diverges (Jacobi on the
+convection-diffusion matrix, most momentum systems); the parity cases below
+are the ones where its own run converges."""
 import os
 
 import numpy as np
@@ -56,6 +60,8 @@ def _solver(sg, ctx, kind, pc, tol, maxit, restart=30):
 def _oracle_solve(oracle, kind, rp, ci, v, b, pc, tol, maxit, restart):
     if kind == 0:
         return oracle.gmres(rp, ci, v, b, pc, tol, maxit, restart)
+    if kind == 3:
+        return oracle.tfqmr(rp, ci, v, b, pc, tol, maxit)
     return oracle.bicgstab(rp, ci, v, b, pc, tol, maxit)
 
 
@@ -69,7 +75,7 @@ def _device_solve(sg, ctx, kind, rp, ci, v, b, pc, tol, maxit, restart):
 
 
 @pytest.mark.parametrize("kind", [0, 1])
-@pytest.mark.parametrize("pc", [0, 1])
+@pytest.mark.parametrize("pc", [0, 1, 2])
 @pytest.mark.parametrize("case", ["conv_diff", "momentum_small", "momentum_64"])
 def test_matches_oracle(sg, ctx, oracle, kind, pc, case):
     if case == "conv_diff":
@@ -105,13 +111,37 @@ def test_reference_results_fixture(sg, ctx):
     assert abs(it - int(g["it_bicgstab"])) <= 1 and rel(x, g["x_bicgstab"]) <= 1e-8
 
 
-@pytest.mark.parametrize("kind", [0, 1])
+@pytest.mark.parametrize("case,pc,tol", [("conv_diff", 1, 1e-8), ("momentum_small", 1, 1e-6),
+                                         ("momentum_small", 1, 1e-8), ("momentum_small", 1, 1e-10),
+                                         ("momentum_small", 2, 1e-6), ("momentum_small", 2, 1e-8),
+                                         ("momentum_16", 1, 1e-6)])
+def test_tfqmr_matches_oracle(sg, ctx, oracle, case, pc, tol):
+    """TFQMR with ILU(0) or SSOR where the reference's run converges: its
+    count within one, the true residual below tol (TFQMR stops on it), x
+    within the solve's accuracy."""
+    if case == "conv_diff":
+        rp, ci, v = _conv_diff(40)
+        b = np.ones(40)
+    elif case == "momentum_small":
+        rp, ci, v, b = _momentum_system(oracle, (9, 8, 3))
+    else:
+        rp, ci, v, b = _momentum_system(oracle, (16, 16, 16), mu=0.002)
+    ox, oit, olast = oracle.tfqmr(rp, ci, v, b, pc, tol, 300)
+    assert oit < 300 and olast < tol  # the reference converges here
+    x, it, st = _device_solve(sg, ctx, 3, rp, ci, v, b, pc, tol, 300, 30)
+    assert abs(it - oit) <= 1, (it, oit)
+    assert st.converged and st.final_residual < tol and st.true_residual < tol
+    assert rel(x, ox) <= 1e4 * tol
+
+
+@pytest.mark.parametrize("kind", [0, 1, 3])
 def test_edge_cases(sg, ctx, oracle, kind):
     rp, ci, v = _conv_diff(40)
     # b = 0: no iteration, x = 0
     x, it, st = _device_solve(sg, ctx, kind, rp, ci, v, np.zeros(40), 0, 1e-8, 100, 30)
     assert it == 0 and not np.any(x)
     # maxIterations reached (GMRES: mid-cycle, restart 3): the reference's count and x
+    # (TFQMR: its residual bound is still far above tol after seven steps)
     b = np.linspace(1.0, 2.0, 40)
     ox, oit, olast = _oracle_solve(oracle, kind, rp, ci, v, b, 0, 1e-14, 7, 3)
     x, it, st = _device_solve(sg, ctx, kind, rp, ci, v, b, 0, 1e-14, 7, 3)
@@ -135,7 +165,14 @@ def test_ilu_gmres_one_step_exact(sg, ctx, oracle):
     assert oit == 0 and it == 0 and rel(x, ox) <= 1e-12
 
 
-def test_tfqmr_is_rejected(sg, ctx):
-    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.TFQMR, preconditioner=sg.PreconditionerKind.Jacobi)
-    with pytest.raises(NotImplementedError):
-        sg.make_linear_solver(cfg, ctx=ctx)
+def test_tfqmr_make_linear_solver(sg, ctx, oracle):
+    """make_linear_solver hands TFQMR to the device: the reference's ILU(0)
+    known answer (tests/unit/solver/test_tfqmr_solver.cpp:91-111)."""
+    rp, ci, v = _conv_diff(40)
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.TFQMR, preconditioner=sg.PreconditionerKind.ILU,
+                                tolerance=1e-8, maxIterations=500)
+    s = sg.make_linear_solver(cfg, ctx=ctx)
+    x = np.zeros(40)
+    s.solve(sg.CSRMatrix(rp, ci, v), np.ones(40), x)
+    s.close()
+    assert np.linalg.norm(oracle.spmv(rp, ci, v, x) - 1.0) < 1e-4

@@ -233,14 +233,39 @@ def test_cg_tridiagonal_known_answer(oracle):
     assert np.linalg.norm(b - oracle.spmv(rp, ci, va, x)) < 1e-8
 
 
-@pytest.mark.parametrize("pc", [0, 1])
+@pytest.mark.parametrize("pc", [0, 1, 2])
 def test_cg_1d_laplacian(oracle, pc):
     """tests/unit/solver/test_ssor_preconditioner.cpp:65-88 (1-D Laplacian,
-    n=50, b=1, tol 1e-10), with the preconditioners on this path."""
+    n=50, b=1, tol 1e-10), with Jacobi, ILU(0) and the test's own SSOR."""
     rp, ci, va = tridiag(50, -1.0, 2.0, -1.0)
     b = np.ones(50)
     x, it, last = oracle.cg(rp, ci, va, b, pc, 1e-10, 200)
     assert it > 0 and np.linalg.norm(oracle.spmv(rp, ci, va, x) - b) < 1e-7
+
+
+def test_ssor_identity_known_answer(oracle):
+    """tests/unit/solver/test_ssor_preconditioner.cpp:40-62: SSOR(1) of the
+    5x5 identity returns r."""
+    rp = np.arange(6, dtype=np.int32)
+    ci = np.arange(5, dtype=np.int32)
+    r = np.arange(1.0, 6.0)
+    assert oracle.ssor_apply(rp, ci, np.ones(5), r).tolist() == r.tolist()
+
+
+def test_tfqmr_known_answers(oracle):
+    """tests/unit/solver/test_tfqmr_solver.cpp:91-111: TFQMR + ILU(0) on the
+    40-point upwind convection-diffusion matrix, b = 1, tol 1e-8: |Ax - b| <
+    1e-4.  The same file's TFQMR + Jacobi case on the 30-point Laplacian
+    (:67-89) is not met by the reference's own TfqmrSolver: the compiled
+    reference returns after 88 iterations with a non-finite x, and the oracle
+    reproduces that (test_oracle_vs_reference.py::test_tfqmr_laplacian_jacobi)."""
+    rp, ci, va = tridiag(40, -6.0, 7.0, -1.0)
+    b = np.ones(40)
+    x, it, last = oracle.tfqmr(rp, ci, va, b, 1, 1e-8, 500)
+    assert np.linalg.norm(oracle.spmv(rp, ci, va, x) - b) < 1e-4
+    rp, ci, va = tridiag(30, -1.0, 2.0, -1.0)
+    x, it, last = oracle.tfqmr(rp, ci, va, np.ones(30), 0, 1e-8, 500)
+    assert it == 88 and not np.all(np.isfinite(x))
 
 
 @pytest.mark.parametrize("dims", [(4, 1, 1), (3, 3, 3)])
