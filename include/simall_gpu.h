@@ -53,9 +53,11 @@ enum simall_memory { SIMALL_MEM_HOST = 0, SIMALL_MEM_DEVICE = 1 };
 
 /* PreconditionerKind ordinals (src/solver/Solver.hpp:75-82).  SSOR is
  * SsorPreconditioner with make_preconditioner's w = 1
- * (src/solver/LinearSolvers.cpp:163-231, :247-248), FP64 only; AMG is rejected
- * with SIMALL_ERR_UNSUPPORTED; None maps to Jacobi, as make_preconditioner's
- * default branch does (:240-254). */
+ * (src/solver/LinearSolvers.cpp:163-231, :247-248); AMG is AMGPreconditioner
+ * with its default parameters (src/solver/AMGPreconditioner.cpp; hierarchy
+ * built on the host for each new matrix, V-cycle on the device); both FP64
+ * only.  None maps to Jacobi, as make_preconditioner's default branch does
+ * (:240-254). */
 enum simall_preconditioner {
     SIMALL_PRECOND_JACOBI = 0,
     SIMALL_PRECOND_ILU0 = 1,
@@ -175,10 +177,15 @@ int simall_solver_solve(simall_solver *s, const double *b, double *x, int mem, s
 int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem);
 /* z = M^-1 r with the solver's FP64 preconditioner, as set up for its current
  * matrix: IPreconditioner::apply (src/solver/LinearSolvers.hpp:33-34) of
- * JacobiPreconditioner, ILU0Preconditioner or SsorPreconditioner
- * (src/solver/LinearSolvers.cpp:66-71, :127-151, :188-231), bit-identical to
- * them.  r and z must not alias. */
+ * JacobiPreconditioner, ILU0Preconditioner, SsorPreconditioner
+ * (src/solver/LinearSolvers.cpp:66-71, :127-151, :188-231) or
+ * AMGPreconditioner (src/solver/AMGPreconditioner.cpp:418-427),
+ * bit-identical to them.  r and z must not alias. */
 int simall_solver_precond_apply(simall_solver *s, const double *r, double *z, int mem);
+/* The AMG hierarchy built for the current matrix (preconditioner AMG): the
+ * number of levels and the rows of each (up to max_levels of them).  *nlev is
+ * 0 for the other preconditioners. */
+int simall_solver_amg_levels(const simall_solver *s, int *nlev, int32_t *rows, int max_levels);
 /* Times `reps` back-to-back launches of one kernel of the solve on the
  * current matrix, bracketed by CUDA events on the context stream; *ms
  * receives the average duration of one launch and *bytes the algorithmic

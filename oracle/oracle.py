@@ -92,6 +92,8 @@ def lib():
         L.orc_gmres.restype = C.c_int
         L.orc_tfqmr.restype = C.c_int
         L.orc_tfqmr.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
+        L.orc_amg_probe.restype = None
+        L.orc_amg_probe.argtypes = [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]
         L.orc_ssor_setup.restype = None
         L.orc_ssor_setup.argtypes = [_I64, _P, _P, _P, _P, _P]
         L.orc_ssor_apply.restype = None
@@ -372,6 +374,24 @@ def tfqmr(rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000):
                          _ptr(np.ascontiguousarray(values, np.float64)), _ptr(np.ascontiguousarray(b, np.float64)),
                          int(precond), float(tol), int(max_it), _ptr(x), C.byref(last))
     return x, it, last.value
+
+
+def amg_apply(rowPtr, colIdx, values, r=None):
+    """AMGPreconditioner setup + apply (src/solver/AMGPreconditioner.cpp)
+    with make_preconditioner's defaults.  Returns (z or None, [(rows, nnz) of
+    each level], coarsest size)."""
+    n = len(rowPtr) - 1
+    rp = np.ascontiguousarray(rowPtr, np.int32)
+    ci = np.ascontiguousarray(colIdx, np.int32)
+    v = np.ascontiguousarray(values, np.float64)
+    z = None if r is None else np.empty(n)
+    nlev = C.c_int(0)
+    cn = C.c_int32(0)
+    sizes = np.zeros(10, np.int32)
+    nnzs = np.zeros(10, np.int32)
+    lib().orc_amg_probe(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(None if r is None else np.ascontiguousarray(r, np.float64)),
+                        _ptr(z), C.byref(nlev), _ptr(sizes), _ptr(nnzs), C.byref(cn))
+    return z, [(int(sizes[l]), int(nnzs[l])) for l in range(nlev.value)], int(cn.value)
 
 
 def ssor_apply(rowPtr, colIdx, values, r, omega=1.0):

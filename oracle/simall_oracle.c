@@ -744,13 +744,460 @@ void orc_ssor_apply(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, con
         z[i] *= scale;
 }
 
+/* ------------------------------------------------------------------ AMG */
+
+/*
+ * AMGPreconditioner (src/solver/AMGPreconditioner.cpp), with the defaults
+ * make_preconditioner constructs it with (theta 0.25, 10 levels, one pre- and
+ * one post-sweep, coarse threshold 32; AMGPreconditioner.hpp:39-43).
+ * Ruge-Stueben: strong couplings -a_ij >= theta max_k(-a_ik) (:43-67),
+ * greedy C/F split by the largest lambda = |S_i^T| (+1 for each new F point
+ * that i influences), the smallest index on ties (:69-113), direct
+ * interpolation P_ij = -a_ij / a_ii onto C neighbours (:115-151), R = P^T
+ * (:153-174), Galerkin A_c = R (A P) with each product row accumulated in the
+ * order its terms are met and its columns sorted (:176-246), a dense LU with
+ * partial pivoting of the coarsest operator whose row swaps are not applied to
+ * the right-hand side in the solve, as the reference does (:296-322,
+ * :354-377), and a V-cycle of symmetric Gauss-Seidel sweeps (:326-352,
+ * :379-416) from z = 0 (:418-427).
+ */
+typedef struct {
+    int32_t n;
+    int32_t *rp, *ci;
+    double *v;
+} OrcCsr;
+
+#define ORC_AMG_MAX_LEVELS 10
+
+typedef struct {
+    int nlev;
+    OrcCsr A[ORC_AMG_MAX_LEVELS], P[ORC_AMG_MAX_LEVELS], R[ORC_AMG_MAX_LEVELS];
+    int32_t coarseN;
+    double *lu;
+} OrcAmg;
+
+static double csr_diag(const OrcCsr *A, int32_t i)
+{
+    for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k)
+        if (A->ci[k] == i)
+            return A->v[k];
+    return 0.0;
+}
+
+static void csr_free(OrcCsr *A)
+{
+    free(A->rp);
+    free(A->ci);
+    free(A->v);
+    memset(A, 0, sizeof(*A));
+}
+
+/* strong[i] as a CSR list (sp, sj) */
+static void amg_strong(const OrcCsr *A, double theta, int32_t **sp, int32_t **sj)
+{
+    const int32_t n = A->n;
+    int32_t *p = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    int32_t *j = (int32_t *)xmalloc(((size_t)A->rp[n] + 1) * sizeof(int32_t));
+    p[0] = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        p[i + 1] = p[i];
+        double maxOff = 0.0;
+        for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k) {
+            if (A->ci[k] == i)
+                continue;
+            maxOff = STD_MAX(maxOff, -A->v[k]);
+        }
+        if (maxOff <= 0.0)
+            continue;
+        const double thr = theta * maxOff;
+        for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k) {
+            if (A->ci[k] == i)
+                continue;
+            if (-A->v[k] >= thr)
+                j[p[i + 1]++] = A->ci[k];
+        }
+    }
+    *sp = p;
+    *sj = j;
+}
+
+/* cf[i] = 1 C point, 0 F point; returns the number of C points. */
+static int32_t amg_coarsen(int32_t n, const int32_t *sp, const int32_t *sj, int32_t *cf)
+{
+    /* S^T, rows in ascending i as the reference appends them */
+    int32_t *tp = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    int32_t *tj = (int32_t *)xmalloc(((size_t)sp[n] + 1) * sizeof(int32_t));
+    int32_t *fill = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    int32_t *lambda = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    memset(tp, 0, ((size_t)n + 1) * sizeof(int32_t));
+    for (int32_t q = 0; q < sp[n]; ++q)
+        ++tp[sj[q] + 1];
+    for (int32_t i = 0; i < n; ++i)
+        tp[i + 1] += tp[i];
+    memcpy(fill, tp, (size_t)n * sizeof(int32_t));
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t q = sp[i]; q < sp[i + 1]; ++q)
+            tj[fill[sj[q]]++] = i;
+    for (int32_t i = 0; i < n; ++i) {
+        cf[i] = -1;
+        lambda[i] = tp[i + 1] - tp[i];
+    }
+    for (;;) {
+        int32_t best = -1, bestLam = -1;
+        for (int32_t i = 0; i < n; ++i)
+            if (cf[i] < 0 && lambda[i] > bestLam) {
+                bestLam = lambda[i];
+                best = i;
+            }
+        if (best < 0)
+            break;
+        cf[best] = 1;
+        for (int32_t q = tp[best]; q < tp[best + 1]; ++q) {
+            const int32_t j = tj[q];
+            if (cf[j] < 0) {
+                cf[j] = 0;
+                for (int32_t r = sp[j]; r < sp[j + 1]; ++r)
+                    if (cf[sj[r]] < 0)
+                        ++lambda[sj[r]];
+            }
+        }
+        lambda[best] = -1;
+    }
+    int32_t nc = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        if (cf[i] < 0)
+            cf[i] = 1;
+        nc += cf[i] == 1;
+    }
+    free(tp);
+    free(tj);
+    free(fill);
+    free(lambda);
+    return nc;
+}
+
+static void amg_prolongation(const OrcCsr *A, const int32_t *cf, OrcCsr *P)
+{
+    const int32_t nf = A->n;
+    int32_t *cid = (int32_t *)xmalloc(((size_t)nf + 1) * sizeof(int32_t));
+    int32_t nc = 0;
+    for (int32_t i = 0; i < nf; ++i)
+        cid[i] = cf[i] == 1 ? nc++ : -1;
+    P->n = nf;
+    P->rp = (int32_t *)xmalloc(((size_t)nf + 1) * sizeof(int32_t));
+    P->ci = (int32_t *)xmalloc(((size_t)A->rp[nf] + (size_t)nf + 1) * sizeof(int32_t));
+    P->v = (double *)xmalloc(((size_t)A->rp[nf] + (size_t)nf + 1) * sizeof(double));
+    P->rp[0] = 0;
+    int32_t e = 0;
+    for (int32_t i = 0; i < nf; ++i) {
+        if (cf[i] == 1) {
+            P->ci[e] = cid[i];
+            P->v[e++] = 1.0;
+        } else {
+            const double dii = csr_diag(A, i);
+            const double inv = (fabs(dii) > 1e-30) ? 1.0 / dii : 0.0;
+            for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k) {
+                const int32_t j = A->ci[k];
+                if (j == i || cf[j] != 1)
+                    continue;
+                P->ci[e] = cid[j];
+                P->v[e++] = -A->v[k] * inv;
+            }
+        }
+        P->rp[i + 1] = e;
+    }
+    free(cid);
+}
+
+static void amg_transpose(const OrcCsr *M, int32_t newRows, OrcCsr *T)
+{
+    const int32_t nnz = M->rp[M->n];
+    T->n = newRows;
+    T->rp = (int32_t *)xmalloc(((size_t)newRows + 1) * sizeof(int32_t));
+    T->ci = (int32_t *)xmalloc(((size_t)nnz + 1) * sizeof(int32_t));
+    T->v = (double *)xmalloc(((size_t)nnz + 1) * sizeof(double));
+    memset(T->rp, 0, ((size_t)newRows + 1) * sizeof(int32_t));
+    for (int32_t k = 0; k < nnz; ++k)
+        ++T->rp[M->ci[k] + 1];
+    for (int32_t i = 0; i < newRows; ++i)
+        T->rp[i + 1] += T->rp[i];
+    int32_t *cur = (int32_t *)xmalloc(((size_t)newRows + 1) * sizeof(int32_t));
+    memset(cur, 0, ((size_t)newRows + 1) * sizeof(int32_t));
+    for (int32_t i = 0; i < M->n; ++i)
+        for (int32_t k = M->rp[i]; k < M->rp[i + 1]; ++k) {
+            const int32_t c = M->ci[k];
+            const int32_t dst = T->rp[c] + cur[c]++;
+            T->ci[dst] = i;
+            T->v[dst] = M->v[k];
+        }
+    free(cur);
+}
+
+static int cmp_i32(const void *a, const void *b)
+{
+    const int32_t x = *(const int32_t *)a, y = *(const int32_t *)b;
+    return (x > y) - (x < y);
+}
+
+/* C = L * Rm, each row accumulated in the order its terms are met, columns
+ * sorted; ncols columns. */
+static void amg_matmul(const OrcCsr *L, const OrcCsr *Rm, int32_t ncols, OrcCsr *C)
+{
+    const int32_t n = L->n;
+    double *acc = (double *)xmalloc(((size_t)ncols + 1) * sizeof(double));
+    int32_t *mark = (int32_t *)xmalloc(((size_t)ncols + 1) * sizeof(int32_t));
+    int32_t *cols = (int32_t *)xmalloc(((size_t)ncols + 1) * sizeof(int32_t));
+    for (int32_t c = 0; c < ncols; ++c)
+        mark[c] = -1;
+    size_t cap = (size_t)L->rp[n] * 4 + 16, e = 0;
+    C->n = n;
+    C->rp = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    C->ci = (int32_t *)xmalloc(cap * sizeof(int32_t));
+    C->v = (double *)xmalloc(cap * sizeof(double));
+    C->rp[0] = 0;
+    for (int32_t i = 0; i < n; ++i) {
+        int32_t nc = 0;
+        for (int32_t k = L->rp[i]; k < L->rp[i + 1]; ++k) {
+            const int32_t j = L->ci[k];
+            const double lij = L->v[k];
+            for (int32_t kp = Rm->rp[j]; kp < Rm->rp[j + 1]; ++kp) {
+                const int32_t c = Rm->ci[kp];
+                const double v = lij * Rm->v[kp];
+                if (mark[c] != i) {
+                    mark[c] = i;
+                    acc[c] = v;
+                    cols[nc++] = c;
+                } else {
+                    acc[c] += v;
+                }
+            }
+        }
+        qsort(cols, (size_t)nc, sizeof(int32_t), cmp_i32);
+        if (e + (size_t)nc > cap) {
+            while (e + (size_t)nc > cap)
+                cap *= 2;
+            C->ci = (int32_t *)realloc(C->ci, cap * sizeof(int32_t));
+            C->v = (double *)realloc(C->v, cap * sizeof(double));
+        }
+        for (int32_t q = 0; q < nc; ++q) {
+            C->ci[e] = cols[q];
+            C->v[e++] = acc[cols[q]];
+        }
+        C->rp[i + 1] = (int32_t)e;
+    }
+    free(acc);
+    free(mark);
+    free(cols);
+}
+
+void orc_amg_free(OrcAmg *M)
+{
+    for (int l = 0; l < ORC_AMG_MAX_LEVELS; ++l) {
+        csr_free(&M->A[l]);
+        csr_free(&M->P[l]);
+        csr_free(&M->R[l]);
+    }
+    free(M->lu);
+    M->lu = NULL;
+    M->nlev = 0;
+}
+
+void orc_amg_setup(OrcAmg *M, int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values)
+{
+    const double theta = 0.25;
+    const int maxLevels = ORC_AMG_MAX_LEVELS, coarseThreshold = 32;
+    memset(M, 0, sizeof(*M));
+    OrcCsr *A0 = &M->A[0];
+    A0->n = (int32_t)n;
+    A0->rp = (int32_t *)xmalloc(((size_t)n + 1) * sizeof(int32_t));
+    A0->ci = (int32_t *)xmalloc(((size_t)rowPtr[n] + 1) * sizeof(int32_t));
+    A0->v = (double *)xmalloc(((size_t)rowPtr[n] + 1) * sizeof(double));
+    memcpy(A0->rp, rowPtr, ((size_t)n + 1) * sizeof(int32_t));
+    memcpy(A0->ci, colIdx, (size_t)rowPtr[n] * sizeof(int32_t));
+    memcpy(A0->v, values, (size_t)rowPtr[n] * sizeof(double));
+    M->nlev = 1;
+    for (int lvl = 0; lvl < maxLevels - 1; ++lvl) {
+        OrcCsr *Af = &M->A[M->nlev - 1];
+        const int32_t nf = Af->n;
+        if (nf <= coarseThreshold)
+            break;
+        int32_t *sp, *sj;
+        amg_strong(Af, theta, &sp, &sj);
+        int32_t *cf = (int32_t *)xmalloc(((size_t)nf + 1) * sizeof(int32_t));
+        const int32_t nc = amg_coarsen(nf, sp, sj, cf);
+        free(sp);
+        free(sj);
+        if (nc == 0 || nc >= nf) {
+            free(cf);
+            break;
+        }
+        OrcCsr *P = &M->P[M->nlev - 1], *R = &M->R[M->nlev - 1];
+        amg_prolongation(Af, cf, P);
+        free(cf);
+        amg_transpose(P, nc, R);
+        OrcCsr AP;
+        int32_t ncols = 0;
+        for (int32_t q = 0; q < P->rp[P->n]; ++q)
+            ncols = P->ci[q] + 1 > ncols ? P->ci[q] + 1 : ncols;
+        amg_matmul(Af, P, ncols, &AP);
+        amg_matmul(R, &AP, ncols, &M->A[M->nlev]);
+        csr_free(&AP);
+        M->nlev += 1;
+    }
+    const OrcCsr *Ac = &M->A[M->nlev - 1];
+    const int32_t cn = Ac->n;
+    M->coarseN = cn;
+    M->lu = (double *)xmalloc((size_t)cn * (size_t)cn * sizeof(double) + 8);
+    double *LU = M->lu;
+    memset(LU, 0, (size_t)cn * (size_t)cn * sizeof(double));
+    for (int32_t i = 0; i < cn; ++i)
+        for (int32_t k = Ac->rp[i]; k < Ac->rp[i + 1]; ++k)
+            LU[(size_t)i * cn + Ac->ci[k]] = Ac->v[k];
+    for (int32_t k = 0; k < cn; ++k) {
+        int32_t piv = k;
+        double pivVal = fabs(LU[(size_t)k * cn + k]);
+        for (int32_t i = k + 1; i < cn; ++i) {
+            const double v = fabs(LU[(size_t)i * cn + k]);
+            if (v > pivVal) {
+                pivVal = v;
+                piv = i;
+            }
+        }
+        if (pivVal < 1e-30)
+            continue;
+        if (piv != k)
+            for (int32_t j = 0; j < cn; ++j) {
+                const double t = LU[(size_t)k * cn + j];
+                LU[(size_t)k * cn + j] = LU[(size_t)piv * cn + j];
+                LU[(size_t)piv * cn + j] = t;
+            }
+        const double dinv = 1.0 / LU[(size_t)k * cn + k];
+        for (int32_t i = k + 1; i < cn; ++i) {
+            const double f = LU[(size_t)i * cn + k] * dinv;
+            LU[(size_t)i * cn + k] = f;
+            for (int32_t j = k + 1; j < cn; ++j)
+                LU[(size_t)i * cn + j] -= f * LU[(size_t)k * cn + j];
+        }
+    }
+}
+
+static void amg_sgs(const OrcCsr *A, double *x, const double *b)
+{
+    for (int32_t i = 0; i < A->n; ++i) {
+        double s = b[i], aii = 0.0;
+        for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k) {
+            const int32_t j = A->ci[k];
+            if (j == i)
+                aii = A->v[k];
+            else
+                s -= A->v[k] * x[j];
+        }
+        if (fabs(aii) > 1e-30)
+            x[i] = s / aii;
+    }
+    for (int32_t i = A->n - 1; i >= 0; --i) {
+        double s = b[i], aii = 0.0;
+        for (int32_t k = A->rp[i]; k < A->rp[i + 1]; ++k) {
+            const int32_t j = A->ci[k];
+            if (j == i)
+                aii = A->v[k];
+            else
+                s -= A->v[k] * x[j];
+        }
+        if (fabs(aii) > 1e-30)
+            x[i] = s / aii;
+    }
+}
+
+static void amg_direct(const OrcAmg *M, double *x, const double *b)
+{
+    const int32_t n = M->coarseN;
+    if (n == 0)
+        return;
+    double *y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    for (int32_t i = 0; i < n; ++i) {
+        double s = b[i];
+        for (int32_t j = 0; j < i; ++j)
+            s -= M->lu[(size_t)i * n + j] * y[j];
+        y[i] = s;
+    }
+    for (int32_t i = n - 1; i >= 0; --i) {
+        double s = y[i];
+        for (int32_t j = i + 1; j < n; ++j)
+            s -= M->lu[(size_t)i * n + j] * x[j];
+        const double d = M->lu[(size_t)i * n + i];
+        x[i] = (fabs(d) > 1e-30) ? s / d : 0.0;
+    }
+    free(y);
+}
+
+static void csr_spmv(const OrcCsr *A, const double *x, double *y)
+{
+    orc_spmv(A->n, A->rp, A->ci, A->v, x, y);
+}
+
+static void amg_vcycle(const OrcAmg *M, int lvl, double *x, const double *b)
+{
+    if (lvl == M->nlev - 1) {
+        amg_direct(M, x, b);
+        return;
+    }
+    const OrcCsr *A = &M->A[lvl];
+    const int32_t n = A->n, nc = M->R[lvl].n;
+    amg_sgs(A, x, b);
+    double *r = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    csr_spmv(A, x, r);
+    for (int32_t i = 0; i < n; ++i)
+        r[i] = b[i] - r[i];
+    double *rc = (double *)xmalloc((size_t)nc * sizeof(double) + 8);
+    double *ec = (double *)xmalloc((size_t)nc * sizeof(double) + 8);
+    csr_spmv(&M->R[lvl], r, rc);
+    for (int32_t i = 0; i < nc; ++i)
+        ec[i] = 0.0;
+    amg_vcycle(M, lvl + 1, ec, rc);
+    csr_spmv(&M->P[lvl], ec, r);
+    for (int32_t i = 0; i < n; ++i)
+        x[i] += r[i];
+    amg_sgs(A, x, b);
+    free(r);
+    free(rc);
+    free(ec);
+}
+
+void orc_amg_apply(const OrcAmg *M, const double *r, double *z)
+{
+    const int32_t n = M->A[0].n;
+    for (int32_t i = 0; i < n; ++i)
+        z[i] = 0.0;
+    amg_vcycle(M, 0, z, r);
+}
+
+/* Setup + one apply (test entry point); sizes[l] = rows of level l, nnzs[l]
+ * its entries (up to 10 levels), *nlev and *coarseN out.  z may be NULL. */
+void orc_amg_probe(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *r,
+                   double *z, int *nlev, int32_t *sizes, int32_t *nnzs, int32_t *coarseN)
+{
+    OrcAmg M;
+    orc_amg_setup(&M, n, rowPtr, colIdx, values);
+    *nlev = M.nlev;
+    for (int l = 0; l < M.nlev; ++l) {
+        sizes[l] = M.A[l].n;
+        nnzs[l] = M.A[l].rp[M.A[l].n];
+    }
+    *coarseN = M.coarseN;
+    if (z)
+        orc_amg_apply(&M, r, z);
+    orc_amg_free(&M);
+}
+
 /* ------------------------------------------------------------------ preconditioner objects */
 
-/* make_preconditioner (src/solver/LinearSolvers.cpp:240-254) for the kinds
- * restated here: 1 ILU(0), 2 SSOR (w = 1), anything else Jacobi (AMG, kind 3,
- * is not restated; None, kind 4, is the default branch's Jacobi). */
+/* make_preconditioner (src/solver/LinearSolvers.cpp:240-254): 1 ILU(0),
+ * 2 SSOR (w = 1), 3 AMG (default parameters), anything else Jacobi (None,
+ * kind 4, is the default branch's Jacobi). */
 typedef struct {
-    int kind; /* 0 Jacobi, 1 ILU(0), 2 SSOR */
+    int kind; /* 0 Jacobi, 1 ILU(0), 2 SSOR, 3 AMG */
+    OrcAmg amg;
     int64_t n;
     const int32_t *rowPtr, *colIdx;
     const double *values;
@@ -762,12 +1209,14 @@ static void prec_setup(OrcPrec *M, int kind, int64_t n, const int32_t *rowPtr, c
                        const double *values)
 {
     memset(M, 0, sizeof(*M));
-    M->kind = (kind == 1 || kind == 2) ? kind : 0;
+    M->kind = (kind == 1 || kind == 2 || kind == 3) ? kind : 0;
     M->n = n;
     M->rowPtr = rowPtr;
     M->colIdx = colIdx;
     M->values = values;
-    if (M->kind == 2) {
+    if (M->kind == 3) {
+        orc_amg_setup(&M->amg, n, rowPtr, colIdx, values);
+    } else if (M->kind == 2) {
         M->diag = (double *)xmalloc((size_t)n * sizeof(double) + 8);
         M->invD = (double *)xmalloc((size_t)n * sizeof(double) + 8);
         M->y = (double *)xmalloc((size_t)n * sizeof(double) + 8);
@@ -790,6 +1239,8 @@ static void prec_apply(const OrcPrec *M, const double *r, double *z)
         orc_ilu0_apply(M->n, M->rowPtr, M->colIdx, M->lu, M->diagPtr, r, z, M->y);
     else if (M->kind == 2)
         orc_ssor_apply(M->n, M->rowPtr, M->colIdx, M->values, M->diag, M->invD, 1.0, r, z, M->y, M->v);
+    else if (M->kind == 3)
+        orc_amg_apply(&M->amg, r, z);
     else
         for (int64_t i = 0; i < M->n; ++i)
             z[i] = M->invD[i] * r[i];
@@ -803,6 +1254,8 @@ static void prec_free(OrcPrec *M)
     free(M->diagPtr);
     free(M->diag);
     free(M->v);
+    if (M->kind == 3)
+        orc_amg_free(&M->amg);
 }
 
 /* ------------------------------------------------------------------ CG */
@@ -814,7 +1267,7 @@ static void prec_free(OrcPrec *M)
  *        alpha = rz/pAp; x += alpha p; r -= alpha Ap; last = |r|/bnorm;
  *        if last < tol return it+1; z = M r; rzNew = r.z; beta = rzNew/rz;
  *        p = z + beta p; rz = rzNew }  return maxIt.
- * precond: 0 Jacobi, 1 ILU0, 2 SSOR; any other value is Jacobi (OrcPrec).  hist (optional, maxIt long)
+ * precond: 0 Jacobi, 1 ILU0, 2 SSOR, 3 AMG; any other value is Jacobi (OrcPrec).  hist (optional, maxIt long)
  * receives last after each iteration.
  */
 int orc_cg(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, const double *b,

@@ -1,0 +1,451 @@
+// The AMG preconditioner on the device: AMGPreconditioner::apply
+// (src/solver/AMGPreconditioner.cpp:379-427), one V-cycle from z = 0 with one
+// symmetric Gauss-Seidel sweep before and after the coarse correction and a
+// dense LU solve on the coarsest level.  The hierarchy is built on the host
+// (amg_host.cpp) once per matrix and kept in device memory.
+//
+// Gauss-Seidel is sequential by definition: row i reads the new values of
+// the rows before it and the old values of the rows after it (forward; the
+// other way round backward).  Each sweep here writes a second buffer, so the
+// old values stay readable, and takes its rows in dependency-level order from
+// a ticket, each row waiting (bounded) for the marks of the rows whose new
+// values it reads; every row then does the reference's operations in its
+// column order, products and differences rounded separately and the division
+// correctly rounded.  Residual, restriction and prolongation are row sums in
+// column order.  The whole apply is bit-identical to the reference's.
+//
+// Per level above the coarsest: forward sweep x -> t (the pre-smoothing starts
+// from x = 0, so it reads no x), backward sweep t -> x, r = b - A x into t,
+// b_c = R t; on the way back x += P x_c, forward and backward sweeps.
+#include "amg.hpp"
+#include "device.cuh"
+#include "solver.hpp"
+#include "sweep.cuh"
+
+#include <memory>
+#include <new>
+
+namespace simall {
+
+struct AmgLevelDev {
+    int32_t n = 0, nnz = 0;
+    const int32_t *rp = nullptr, *ci = nullptr;  // level 0: the solver's own arrays
+    const double *v = nullptr;
+    DevBuf<int32_t> rpB, ciB;
+    DevBuf<double> vB;
+    DevBuf<int32_t> Prp, Pci, Rrp, Rci;  // to the next level
+    DevBuf<double> Pv, Rv;
+    int32_t nc = 0;
+    DevBuf<int32_t> fwdOrder, bwdOrder;  // rows in forward / backward dependency-level order
+    DevBuf<unsigned> done, ctl;
+    DevBuf<double> x, b, t;  // x, b: levels below the fine one; t: every level
+};
+
+struct AmgData {
+    std::vector<std::unique_ptr<AmgLevelDev>> lv;
+    int nlev = 0;
+    int32_t coarseN = 0;
+    DevBuf<double> lu, y;
+};
+
+namespace {
+
+// Waits (bounded) for the marks of the up to four rows flagged in dep; false
+// on timeout.
+__device__ __forceinline__ bool wait_deps4(const unsigned *done, const int (&j)[4], const bool (&dep)[4],
+                                           unsigned sweep)
+{
+    unsigned ns = 16;
+    for (unsigned spins = 0;; ++spins) {
+        bool all = true;
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+            if (dep[q])
+                all = (ld_acquire(done + j[q]) == sweep) && all;
+        if (all)
+            return true;
+        if (spins >= kSweepMaxSpins)
+            return false;
+        if (spins >= 4) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : 256;
+        }
+    }
+}
+
+// One Gauss-Seidel sweep over the rows in `order`.  Forward (BWD false): row i
+// reads xout_j (this sweep's values, j < i, after their marks) and xin_j
+// (j > i; ZERO: 0) and writes xout_i = (b_i - sum_{j != i} a_ij x_j) / a_ii, or
+// keeps xin_i when |a_ii| <= 1e-30.  Backward: the same with j > i from xout.
+template <bool BWD, bool ZERO>
+__global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__restrict__ order,
+                                                     const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                                     const double *__restrict__ a, const double *__restrict__ b,
+                                                     const double *__restrict__ xin, double *xout, unsigned *done,
+                                                     unsigned *ctl)
+{
+    const int lane = threadIdx.x & 31;
+    const unsigned sweep = __ldcg(ctl + 1);
+    bool ok = true;
+    for (;;) {
+        int base = 0;
+        if (lane == 0)
+            base = static_cast<int>(atomicAdd(ctl, 32u));
+        base = __shfl_sync(0xffffffffu, base, 0);
+        if (base >= n)
+            break;
+        const int t = base + lane;
+        if (t < n) {
+            const int i = __ldg(order + t);
+            double s = __ldg(b + i), aii = 0.0;
+            const int end = __ldg(rp + i + 1);
+            for (int kp = __ldg(rp + i); kp < end; kp += 4) {
+                int j[4];
+                bool dep[4];
+                double av[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    const bool in = kp + q < end;
+                    j[q] = in ? __ldg(ci + kp + q) : i;  // padding reads as the diagonal: no value, no wait
+                    av[q] = in ? __ldg(a + kp + q) : 0.0;
+                    dep[q] = BWD ? j[q] > i : j[q] < i;
+                }
+                ok = wait_deps4(done, j, dep, sweep) && ok;
+                double v[4];
+#pragma unroll
+                for (int q = 0; q < 4; ++q)
+                    v[q] = j[q] == i ? 0.0 : dep[q] ? __ldcg(xout + j[q]) : ZERO ? 0.0 : __ldg(xin + j[q]);
+#pragma unroll
+                for (int q = 0; q < 4; ++q) {
+                    if (kp + q >= end)
+                        break;
+                    if (j[q] == i)
+                        aii = av[q];
+                    else
+                        s = __dsub_rn(s, __dmul_rn(av[q], v[q]));
+                }
+            }
+            const double keep = ZERO ? 0.0 : __ldg(xin + i);
+            __stcg(xout + i, fabs(aii) > 1e-30 ? __ddiv_rn(s, aii) : keep);
+            st_release(done + i, sweep);
+        }
+    }
+    if (!ok)
+        atomicOr(ctl + 2, 1u);
+}
+
+// Row sum of a CSR row in column order from 0.0 (CSRMatrix::spmv,
+// src/solver/CSRMatrix.hpp:24-35).
+__device__ __forceinline__ double row_sum(const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
+                                          const double *__restrict__ a, const double *__restrict__ x, int i)
+{
+    double s = 0.0;
+    const int end = __ldg(rp + i + 1);
+    for (int k = __ldg(rp + i); k < end; ++k)
+        s = __dadd_rn(s, __dmul_rn(__ldg(a + k), __ldg(x + __ldg(ci + k))));
+    return s;
+}
+
+// r = b - A x
+__global__ void __launch_bounds__(kBlock) k_amg_residual(int n, const int32_t *__restrict__ rp,
+                                                         const int32_t *__restrict__ ci, const double *__restrict__ a,
+                                                         const double *__restrict__ x, const double *__restrict__ b,
+                                                         double *__restrict__ r)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        r[i] = __dsub_rn(__ldg(b + i), row_sum(rp, ci, a, x, i));
+}
+
+// y = M x (restriction: the coarse right-hand side)
+__global__ void __launch_bounds__(kBlock) k_amg_spmv(int n, const int32_t *__restrict__ rp,
+                                                     const int32_t *__restrict__ ci, const double *__restrict__ a,
+                                                     const double *__restrict__ x, double *__restrict__ y)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        y[i] = row_sum(rp, ci, a, x, i);
+}
+
+// x += P x_c
+__global__ void __launch_bounds__(kBlock) k_amg_prolong(int n, const int32_t *__restrict__ rp,
+                                                        const int32_t *__restrict__ ci, const double *__restrict__ a,
+                                                        const double *__restrict__ xc, double *__restrict__ x)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] = __dadd_rn(x[i], row_sum(rp, ci, a, xc, i));
+}
+
+// The coarsest level: the reference's dense forward and back substitution
+// (AMGPreconditioner::direct_solve, :354-377), one warp.  Forward: each row's
+// sum takes y_0, y_1, ... in order as they become final, so the lanes advance
+// all rows together; backward: each row's sum starts with x_{i+1}, a chain,
+// so lane 0 runs it.
+__global__ void k_amg_direct(int n, const double *__restrict__ lu, const double *__restrict__ b, double *y,
+                             double *x)
+{
+    const int lane = threadIdx.x;
+    for (int i = lane; i < n; i += 32)
+        y[i] = b[i];
+    __syncwarp();
+    for (int j = 0; j < n; ++j) {
+        const double yj = y[j];
+        for (int i = j + 1 + lane; i < n; i += 32)
+            y[i] = __dsub_rn(y[i], __dmul_rn(lu[static_cast<size_t>(i) * n + j], yj));
+        __syncwarp();
+    }
+    if (lane == 0) {
+        for (int i = n - 1; i >= 0; --i) {
+            double s = y[i];
+            const double *row = lu + static_cast<size_t>(i) * n;
+            for (int j = i + 1; j < n; ++j)
+                s = __dsub_rn(s, __dmul_rn(row[j], x[j]));
+            const double d = row[i];
+            x[i] = fabs(d) > 1e-30 ? __ddiv_rn(s, d) : 0.0;
+        }
+    }
+}
+
+// Rows ordered by dependency level; lower: row i waits for j < i, else j > i.
+void level_order(const AmgCsr &A, bool lower, std::vector<int32_t> &order)
+{
+    const int32_t n = A.n;
+    std::vector<int32_t> lev(n, 0);
+    int32_t nlev = 0;
+    auto visit = [&](int32_t i) {
+        int32_t l = 0;
+        for (int32_t k = A.rp[i]; k < A.rp[i + 1]; ++k) {
+            const int32_t j = A.ci[k];
+            if (lower ? j < i : j > i)
+                l = std::max(l, lev[j] + 1);
+        }
+        lev[i] = l;
+        nlev = std::max(nlev, l + 1);
+    };
+    if (lower)
+        for (int32_t i = 0; i < n; ++i)
+            visit(i);
+    else
+        for (int32_t i = n - 1; i >= 0; --i)
+            visit(i);
+    std::vector<int32_t> ptr(static_cast<size_t>(nlev) + 1, 0);
+    for (int32_t i = 0; i < n; ++i)
+        ++ptr[lev[i] + 1];
+    for (int32_t l = 0; l < nlev; ++l)
+        ptr[l + 1] += ptr[l];
+    order.resize(n);
+    for (int32_t i = 0; i < n; ++i)
+        order[ptr[lev[i]]++] = i;
+}
+
+template <class T> cudaError_t upload(DevBuf<T> &dst, const std::vector<T> &src, cudaStream_t st)
+{
+    cudaError_t e = dst.alloc(src.size() ? src.size() : 1);
+    if (e == cudaSuccess && !src.empty())
+        e = cudaMemcpyAsync(dst.p, src.data(), src.size() * sizeof(T), cudaMemcpyHostToDevice, st);
+    return e;
+}
+
+int grid_rows(simall_context *ctx, int64_t n)
+{
+    const int64_t g = (n + kBlock - 1) / kBlock;
+    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * 8;
+    return static_cast<int>(g < 1 ? 1 : g < cap ? g : cap);
+}
+
+int grid_sweep(simall_context *ctx, int64_t n)
+{
+    // one warp takes 32 rows per ticket; at most 4 CTAs per SM are resident
+    // with room to spare, so every row waited for is held by a running warp
+    const int64_t g = (n + kBlock - 1) / kBlock;
+    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * 4;
+    return static_cast<int>(g < 1 ? 1 : g < cap ? g : cap);
+}
+
+int sweep(simall_context *ctx, AmgLevelDev &L, bool backward, bool zero, const double *b, const double *xin,
+          double *xout)
+{
+    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(L.ctl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    const int g = grid_sweep(ctx, L.n);
+    const int32_t *order = backward ? L.bwdOrder.p : L.fwdOrder.p;
+    if (backward)
+        k_sgs_free<true, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
+                                                               L.ctl.p);
+    else if (zero)
+        k_sgs_free<false, true><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
+                                                               L.ctl.p);
+    else
+        k_sgs_free<false, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
+                                                                L.ctl.p);
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+}  // namespace
+
+int amg_setup(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    int hp = solver_host_pattern(s);
+    if (hp)
+        return hp;
+    if (!s->amg) {
+        s->amg = new (std::nothrow) AmgData;
+        if (!s->amg)
+            return fail(ctx, SIMALL_ERR_OUT_OF_MEMORY, "AMG state");
+    }
+    AmgData *d = s->amg;
+    cudaStream_t st = ctx->stream;
+    std::vector<double> vals(static_cast<size_t>(s->nnz));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(vals.data(), s->values, vals.size() * sizeof(double), cudaMemcpyDeviceToHost,
+                                         st));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    AmgHierarchy h;
+    amg_build_hierarchy(static_cast<int32_t>(s->n), s->h_rowPtr.data(), s->h_colIdx.data(), vals.data(), AmgParams{},
+                        h);
+    const int nlev = static_cast<int>(h.A.size());
+    while (static_cast<int>(d->lv.size()) < nlev) {
+        d->lv.emplace_back(new (std::nothrow) AmgLevelDev);
+        if (!d->lv.back())
+            return fail(ctx, SIMALL_ERR_OUT_OF_MEMORY, "AMG level");
+    }
+    d->nlev = nlev;
+    std::vector<int32_t> ord;
+    for (int l = 0; l < nlev; ++l) {
+        AmgLevelDev &L = *d->lv[l];
+        const AmgCsr &A = h.A[l];
+        L.n = A.n;
+        L.nnz = A.rp[A.n];
+        if (l == 0) {
+            L.rp = s->rowPtr;
+            L.ci = s->colIdx;
+            L.v = s->values;
+        } else {
+            SIMALL_CUDA_TRY(ctx, upload(L.rpB, A.rp, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.ciB, A.ci, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.vB, A.v, st));
+            L.rp = L.rpB.p;
+            L.ci = L.ciB.p;
+            L.v = L.vB.p;
+            SIMALL_CUDA_TRY(ctx, L.x.alloc(A.n));
+            SIMALL_CUDA_TRY(ctx, L.b.alloc(A.n));
+        }
+        SIMALL_CUDA_TRY(ctx, L.t.alloc(A.n));
+        if (l + 1 < nlev) {
+            SIMALL_CUDA_TRY(ctx, upload(L.Prp, h.P[l].rp, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.Pci, h.P[l].ci, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.Pv, h.P[l].v, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.Rrp, h.R[l].rp, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.Rci, h.R[l].ci, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.Rv, h.R[l].v, st));
+            L.nc = h.R[l].n;
+            // only levels that are smoothed need the sweep schedules
+            level_order(A, true, ord);
+            SIMALL_CUDA_TRY(ctx, upload(L.fwdOrder, ord, st));
+            SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // ord is reused
+            level_order(A, false, ord);
+            SIMALL_CUDA_TRY(ctx, upload(L.bwdOrder, ord, st));
+            SIMALL_CUDA_TRY(ctx, L.done.alloc(A.n));
+            SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(L.done.p, 0, A.n * sizeof(unsigned), st));
+            SIMALL_CUDA_TRY(ctx, L.ctl.alloc(4));
+            SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(L.ctl.p, 0, 4 * sizeof(unsigned), st));
+        }
+        // the host hierarchy dies at return: finish this level's copies first
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    }
+    d->coarseN = h.coarseN;
+    SIMALL_CUDA_TRY(ctx, upload(d->lu, h.lu, st));
+    SIMALL_CUDA_TRY(ctx, d->y.alloc(h.coarseN > 0 ? h.coarseN : 1));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    return SIMALL_OK;
+}
+
+int amg_apply(simall_solver *s, const double *r, double *z)
+{
+    simall_context *ctx = s->ctx;
+    AmgData *d = s->amg;
+    const int L = d->nlev;
+    auto xb = [&](int l, const double **b, double **x) {
+        *b = l == 0 ? r : d->lv[l]->b.p;
+        *x = l == 0 ? z : d->lv[l]->x.p;
+    };
+    for (int l = 0; l + 1 < L; ++l) {
+        AmgLevelDev &Lv = *d->lv[l];
+        const double *b;
+        double *x;
+        xb(l, &b, &x);
+        int e = sweep(ctx, Lv, false, true, b, nullptr, Lv.t.p);
+        if (e)
+            return e;
+        e = sweep(ctx, Lv, true, false, b, Lv.t.p, x);
+        if (e)
+            return e;
+        k_amg_residual<<<grid_rows(ctx, Lv.n), kBlock, 0, ctx->stream>>>(Lv.n, Lv.rp, Lv.ci, Lv.v, x, b, Lv.t.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        k_amg_spmv<<<grid_rows(ctx, Lv.nc), kBlock, 0, ctx->stream>>>(Lv.nc, Lv.Rrp.p, Lv.Rci.p, Lv.Rv.p, Lv.t.p,
+                                                                      d->lv[l + 1]->b.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    {
+        const double *b;
+        double *x;
+        xb(L - 1, &b, &x);
+        k_amg_direct<<<1, 32, 0, ctx->stream>>>(d->coarseN, d->lu.p, b, d->y.p, x);
+        SIMALL_LAUNCH_CHECK(ctx);
+    }
+    for (int l = L - 2; l >= 0; --l) {
+        AmgLevelDev &Lv = *d->lv[l];
+        const double *b;
+        double *x;
+        xb(l, &b, &x);
+        k_amg_prolong<<<grid_rows(ctx, Lv.n), kBlock, 0, ctx->stream>>>(Lv.n, Lv.Prp.p, Lv.Pci.p, Lv.Pv.p,
+                                                                         d->lv[l + 1]->x.p, x);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int e = sweep(ctx, Lv, false, false, b, x, Lv.t.p);
+        if (e)
+            return e;
+        e = sweep(ctx, Lv, true, false, b, Lv.t.p, x);
+        if (e)
+            return e;
+    }
+    return SIMALL_OK;
+}
+
+int amg_apply_launches(const simall_solver *s)
+{
+    const int L = s->amg ? s->amg->nlev : 1;
+    return 11 * (L - 1) + 1;
+}
+
+int amg_check(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    AmgData *d = s->amg;
+    for (int l = 0; l + 1 < d->nlev; ++l) {
+        unsigned h = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, d->lv[l]->ctl.p + 2, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (h) {
+            SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->lv[l]->ctl.p + 2, 0, sizeof(unsigned), ctx->stream));
+            return fail(ctx, SIMALL_ERR_CUDA, "AMG smoother: a row wait timed out on level %d", l);
+        }
+    }
+    return SIMALL_OK;
+}
+
+int amg_levels(const simall_solver *s, int *nlev, int32_t *rows, int max_levels)
+{
+    const AmgData *d = s->amg;
+    *nlev = d ? d->nlev : 0;
+    for (int l = 0; d && l < d->nlev && l < max_levels; ++l)
+        rows[l] = d->lv[l]->n;
+    return SIMALL_OK;
+}
+
+void amg_free(simall_solver *s)
+{
+    delete s->amg;
+    s->amg = nullptr;
+}
+
+}  // namespace simall

@@ -304,4 +304,11 @@ int simall_solver_precond_apply(simall_solver *s, const double *r, double *z, in
     return sweep_preconditioner(s->cfg.preconditioner) ? ilu_check(s) : SIMALL_OK;
 }
 
+int simall_solver_amg_levels(const simall_solver *s, int *nlev, int32_t *rows, int max_levels)
+{
+    if (!s || !nlev || (max_levels > 0 && !rows))
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    return amg_levels(s, nlev, rows, max_levels);
+}
+
 }  // extern "C"

@@ -29,6 +29,7 @@
 // exactly).
 #include "device.cuh"
 #include "solver.hpp"
+#include "sweep.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -115,68 +116,6 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_level(const int32_t *__restr
     for (int kp = kd + 1; kp < rowPtr[i + 1]; ++kp)
         s = __dsub_rn(s, __dmul_rn(lu[kp], __ldcg(z + colIdx[kp])));
     z[i] = (kd >= 0 && lu[kd] != 0.0) ? __ddiv_rn(s, lu[kd]) : s;
-}
-
-__device__ __forceinline__ unsigned ld_acquire(const unsigned *p)
-{
-    unsigned v;
-    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-    return v;
-}
-
-__device__ __forceinline__ void st_release(unsigned *p, unsigned v)
-{
-    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-constexpr unsigned kSweepMaxSpins = 1u << 20;  // ~0.5 s of polling: far beyond any dependency chain
-
-// Wait until row j carries the current sweep's mark; false on timeout.  The
-// first polls are immediate (the row is usually done or nearly so); later
-// ones back off so that thousands of waiting warps do not flood L2 while the
-// rows they wait for are being computed.
-__device__ __forceinline__ bool wait_row(const unsigned *done, int j, unsigned sweep)
-{
-    unsigned ns = 16;
-    for (unsigned spins = 0; ld_acquire(done + j) != sweep; ++spins) {
-        if (spins >= kSweepMaxSpins)
-            return false;
-        if (spins >= 4) {
-            __nanosleep(ns);
-            ns = ns < 256 ? 2 * ns : 256;
-        }
-    }
-    return true;
-}
-
-// Next sweep: reset the ticket, advance the sweep number.
-__global__ void k_sweep_begin(unsigned *ctl)
-{
-    ctl[0] = 0u;
-    ctl[1] += 1u;
-}
-
-// Waits for up to 4 rows at once (their marks polled together), so a row
-// with several dependencies costs one memory round trip per poll, not one per
-// dependency; false on timeout.
-__device__ __forceinline__ bool wait_rows4(const unsigned *done, const int (&j)[4], int cnt, unsigned sweep)
-{
-    unsigned ns = 16;
-    for (unsigned spins = 0;; ++spins) {
-        bool all = true;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (q < cnt)
-                all = (ld_acquire(done + j[q]) == sweep) && all;
-        if (all)
-            return true;
-        if (spins >= kSweepMaxSpins)
-            return false;
-        if (spins >= 4) {
-            __nanosleep(ns);
-            ns = ns < 256 ? 2 * ns : 256;
-        }
-    }
 }
 
 // Forward sweep y_i = r_i - sum_{j<i} l_ij y_j over rows in level order
@@ -838,6 +777,8 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
 
 int ilu_setup(simall_solver *s)
 {
+    if (s->cfg.preconditioner == SIMALL_PRECOND_AMG)
+        return amg_setup(s);
     simall_context *ctx = s->ctx;
     if (!s->ilu) {
         s->ilu = new (std::nothrow) IluData;
@@ -865,6 +806,8 @@ int ilu_setup(simall_solver *s)
 
 int ilu_apply(simall_solver *s, const double *r, double *z)
 {
+    if (s->amg)
+        return amg_apply(s, r, z);
     return sweeps(s->ctx, s->ilu, s->rowPtr, s->colIdx, s->ilu->lu.p, r, z);
 }
 
@@ -882,12 +825,23 @@ int ilu_check(simall_context *ctx, IluData *d)
     return SIMALL_OK;
 }
 
-int ilu_check(simall_solver *s) { return s->ilu ? ilu_check(s->ctx, s->ilu) : SIMALL_OK; }
+int ilu_check(simall_solver *s)
+{
+    if (s->amg)
+        return amg_check(s);
+    return s->ilu ? ilu_check(s->ctx, s->ilu) : SIMALL_OK;
+}
 
-int ilu_apply_launches(const simall_solver *s) { return (s->ilu && s->ilu->small) ? 1 : 4; }
+int ilu_apply_launches(const simall_solver *s)
+{
+    if (s->amg)
+        return amg_apply_launches(s);
+    return (s->ilu && s->ilu->small) ? 1 : 4;
+}
 
 void ilu_free(simall_solver *s)
 {
+    amg_free(s);
     delete s->ilu;
     s->ilu = nullptr;
 }

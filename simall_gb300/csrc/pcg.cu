@@ -461,6 +461,8 @@ int check_device_values(simall_solver *s)
     return SIMALL_OK;
 }
 
+void drop_graphs(simall_solver *s);
+
 // Preconditioner / format setup for the current values.
 int setup_values(simall_solver *s)
 {
@@ -469,6 +471,12 @@ int setup_values(simall_solver *s)
         return mixed_setup(s);
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0)
         return ilu_setup(s);
+    if (s->cfg.preconditioner == SIMALL_PRECOND_AMG) {
+        // a new hierarchy may differ in levels and sizes: the captured
+        // iteration graphs hold its buffers and launch shapes
+        drop_graphs(s);
+        return ilu_setup(s);
+    }
     SIMALL_CUDA_TRY(ctx, s->invDiag.alloc(static_cast<size_t>(s->n)));
     k_jacobi_setup<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->rowPtr, s->colIdx, s->values,
                                                                      s->invDiag.p);
@@ -541,7 +549,7 @@ int enqueue_iteration(simall_solver *s)
 // Kernels one FP64 iteration launches (for the launch counter of graph replays).
 int64_t kernels_per_iteration(const simall_solver *s)
 {
-    if (sweep_preconditioner(s->cfg.preconditioner) && s->ilu)
+    if (sweep_preconditioner(s->cfg.preconditioner) && (s->ilu || s->amg))
         return 4 + ilu_apply_launches(s);  // SpMV, x/r update, r.z/beta, direction + the sweeps
     return 3;
 }

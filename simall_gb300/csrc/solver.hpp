@@ -34,6 +34,7 @@ struct IluData {
 };
 
 struct MixedData;  // mixed.cu
+struct AmgData;    // amg.cu
 struct KrylovData;  // krylov.cu
 
 // Chunk of solver iterations captured as a CUDA graph.
@@ -70,6 +71,7 @@ struct simall_solver {
     bool solved = false;  // a solve completed on the current matrix
     int engine = 0;       // of the last solve: 0 kernels per step, 1 one cluster
     simall::IluData *ilu = nullptr;
+    simall::AmgData *amg = nullptr;
     simall::MixedData *mixed = nullptr;
     simall::KrylovData *krylov = nullptr;
     std::vector<simall::GraphChunk> graphs;  // captured iteration chunks
@@ -77,13 +79,27 @@ struct simall_solver {
 
 namespace simall {
 
-// The preconditioners applied by triangular sweeps: ILU(0) and SSOR.
-inline bool sweep_preconditioner(int pc) { return pc == SIMALL_PRECOND_ILU0 || pc == SIMALL_PRECOND_SSOR; }
-int ilu_setup(simall_solver *s);  // ILU(0) factor, or SSOR's sweep data (cfg.preconditioner)
+// The preconditioners applied by kernels of their own (ILU(0) and SSOR
+// sweeps, the AMG V-cycle) rather than fused into the Krylov updates as
+// Jacobi is.  ilu_setup / ilu_apply / ilu_check / ilu_apply_launches serve
+// all three (AMG through amg_*).
+inline bool sweep_preconditioner(int pc)
+{
+    return pc == SIMALL_PRECOND_ILU0 || pc == SIMALL_PRECOND_SSOR || pc == SIMALL_PRECOND_AMG;
+}
+int ilu_setup(simall_solver *s);  // ILU(0) factor, SSOR's sweep data or the AMG hierarchy (cfg.preconditioner)
 int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);
 int ilu_apply_launches(const simall_solver *s);  // kernels one ilu_apply enqueues
 void ilu_free(simall_solver *s);
+
+// AMG (amg.cu): hierarchy built on the host for the current values, V-cycle on the device.
+int amg_setup(simall_solver *s);
+int amg_apply(simall_solver *s, const double *r, double *z);
+int amg_check(simall_solver *s);
+int amg_apply_launches(const simall_solver *s);
+int amg_levels(const simall_solver *s, int *nlev, int32_t *rows, int max_levels);
+void amg_free(simall_solver *s);
 
 int mixed_setup(simall_solver *s);
 void mixed_invalidate_pattern(simall_solver *s);

@@ -264,6 +264,14 @@ class GpuCGSolver:
         pz, _ = ptr_and_mem(z)
         check(self.L.simall_solver_precond_apply(self.handle, pr, pz, mr), self.ctx.handle)
 
+    def amg_levels(self) -> list[int]:
+        """Rows of each level of the AMG hierarchy of the current matrix."""
+        n = C.c_int(0)
+        rows = np.zeros(16, np.int32)
+        check(self.L.simall_solver_amg_levels(self.handle, C.byref(n), rows.ctypes.data_as(C.c_void_p), 16),
+              self.ctx.handle)
+        return [int(v) for v in rows[:n.value]]
+
     def close(self):
         if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
             self.L.simall_solver_destroy(self.handle)

@@ -35,12 +35,13 @@ def test_mesh_rcm_assembly_cg(oracle, ref, dims, seed, amp, renumber):
         ov, orhs, _ = oracle.assemble(m, orp, oci, pz, 1.3, aP, phi)
         assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
         assert bits_equal(v, ov) and bits_equal(rhs, orhs)
-        for pc in (0, 1, 2):
+        for pc in (0, 1, 2, 3):
             x, it, last, _ = ref.cg(rp, ci, v, rhs, pc, 1e-9, 3000)
             ox, oit, olast = oracle.cg(rp, ci, v, rhs, pc, 1e-9, 3000)
             assert it == oit and last == olast and bits_equal(x, ox)
         z = np.random.default_rng(seed + 1).standard_normal(m.nC)
         assert bits_equal(ref.precond_apply(2, rp, ci, v, z), oracle.ssor_apply(rp, ci, v, z))
+        assert bits_equal(ref.precond_apply(3, rp, ci, v, z), oracle.amg_apply(rp, ci, v, z)[0])
     ref.free_mesh(r)
 
 
@@ -183,9 +184,9 @@ def _conv_diff(n, pe=5.0):
 
 
 @pytest.mark.parametrize("kind", [0, 1, 3])
-@pytest.mark.parametrize("pc", [0, 1, 2])
+@pytest.mark.parametrize("pc", [0, 1, 2, 3])
 def test_nonsymmetric_krylov(oracle, ref, kind, pc):
-    """GMRES(m), BiCGSTAB and TFQMR with Jacobi, ILU(0) and SSOR: iteration
+    """GMRES(m), BiCGSTAB and TFQMR with Jacobi, ILU(0), SSOR and AMG: iteration
     count, last residual and x bit-identical to the reference, on the 1-D
     convection-diffusion matrix and on a momentum system (restart short
     enough to cycle)."""
