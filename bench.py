@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--adjoint-n", type=int, default=128, help="box side of the differentiation leg (0 disables it)")
     ap.add_argument("--fd-faces", type=int, default=64, help="faces checked by central differences")
     ap.add_argument("--poisson-n", type=int, default=128, help="box side of the Jacobi-vs-ILU0 leg (0 disables it)")
+    ap.add_argument("--precond-n", type=int, default=64,
+                    help="box side of the preconditioner / Krylov-kind leg (0 disables it)")
     ap.add_argument("--no-cavity", action="store_true", help="skip the 128x128 cavity pressure-step leg")
     ap.add_argument("--simple-iterations", type=int, default=20,
                     help="outer iterations of the device SIMPLE leg (0 disables it)")
@@ -396,6 +398,75 @@ def run_poisson3d(a, ctx, sg):
         res[name] = {"value": round(e0.elapsed_time(e1) / 1e3, 5), "unit": "s", "iterations": int(s.stats.iterations),
                      "true_residual": float(s.stats.true_residual)}
         s.close()
+    ps.close()
+    return res
+
+
+def run_preconditioners(a, ctx, sg, with_cpu):
+    """Every preconditioner and Krylov kind of make_linear_solver on one
+    system: the N^3 distorted, RCM-renumbered Poisson of the poisson3d leg
+    (FP64, tol 1e-8).  setup = set_matrix with the matrix already in device
+    memory (pattern analysis, ILU(0) factor, SSOR schedules, the AMG
+    hierarchy built on the host), solve = CUDA events around the solve."""
+    import torch
+    from simall_gb300 import workloads as W
+
+    n = a.precond_n
+    m, _ = W.poisson3d_mesh(n, seed=SEED)
+    aP, phi = W.poisson3d_inputs(m, seed=SEED)
+    ps = sg.PressureSystem(m, W.ALL_WALLS, ctx=ctx)
+    ps.assemble(1.0, aP, phi)
+    rp_h, ci_h = ps.pattern()
+    vals_h, rhs_h = ps.download()
+    dev = torch.device("cuda")
+    rp, ci = torch.from_numpy(rp_h).to(dev), torch.from_numpy(ci_h).to(dev)
+    vals, b = torch.from_numpy(vals_h).to(dev), torch.from_numpy(rhs_h).to(dev)
+    x = torch.empty_like(b)
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    K, P = sg.LinearSolverKind, sg.PreconditionerKind
+    cases = [("cg_jacobi", K.CG, P.Jacobi), ("cg_ilu0", K.CG, P.ILU), ("cg_ssor", K.CG, P.SSOR),
+             ("cg_amg", K.CG, P.AMG), ("bicgstab_ssor", K.BiCGSTAB, P.SSOR), ("gmres30_ilu0", K.GMRES, P.ILU),
+             ("tfqmr_ssor", K.TFQMR, P.SSOR), ("bicgstab_amg", K.BiCGSTAB, P.AMG)]
+    res = {"workload": f"poisson3d {n}^3 distorted +-20%, RCM, walls + cell-0 pin, FP64 to {a.tol:g}",
+           "rows": int(m.n_cells), "nnz": int(ps.nnz)}
+    for name, kind, pc in cases:
+        s = sg.make_linear_solver(sg.LinearSolverConfig(kind=kind, preconditioner=pc, tolerance=a.tol,
+                                                        maxIterations=2000, restart=30), ctx=ctx)
+        s.set_matrix(rp, ci, vals)
+        if pc != P.AMG:  # warm: graph capture (an AMG setup drops the graphs: its timed solve recaptures)
+            s.solve_into(b, x)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        s.set_matrix(rp, ci, vals)
+        s.update_values(vals)  # the preconditioner is set up again, as the reference does per solve
+        torch.cuda.synchronize()
+        setup = time.perf_counter() - t0
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        s.solve_into(b, x)
+        e1.record(stream)
+        e1.synchronize()
+        r = {"setup_s": round(setup, 4), "solve_s": round(e0.elapsed_time(e1) / 1e3, 5),
+             "iterations": int(s.stats.iterations), "true_residual": float(s.stats.true_residual),
+             "converged": bool(s.stats.converged)}
+        if pc == P.AMG:
+            r["amg_levels"] = s.amg_levels()
+        res[name] = r
+        s.close()
+    if with_cpu:
+        from oracle import oracle as O
+
+        cpu = {}
+        for name, pc in (("cg_jacobi", 0), ("cg_ilu0", 1), ("cg_ssor", 2)):
+            t = time.perf_counter()
+            _, it, _ = O.cg(rp_h, ci_h, vals_h, rhs_h, pc, a.tol, 2000)
+            cpu[name] = {"value": round(time.perf_counter() - t, 3), "unit": "s", "iterations": int(it)}
+        res["cpu_baseline"] = {"cores": 1, "kind": "port", "solves": cpu,
+                               "sample": "the oracle's CGSolver::solve (setup included) on 1 host core; AMG is not "
+                                         "timed on the CPU: the reference's setup rescans all rows for every C "
+                                         "point (O(n^2))"}
     ps.close()
     return res
 
@@ -847,6 +918,8 @@ def run_ours(a, rank, world, local):
         out["adjoint"] = run_adjoint(a, ctx, sg)
     if a.poisson_n > 0:
         out["poisson3d"] = run_poisson3d(a, ctx, sg)
+    if a.precond_n > 0:
+        out["preconditioners"] = run_preconditioners(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if a.poisson_n > 0:
         out["pressure_step"] = run_pressure_step(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if not a.no_cavity:

@@ -7,11 +7,13 @@
 // Gauss-Seidel is sequential by definition: row i reads the new values of
 // the rows before it and the old values of the rows after it (forward; the
 // other way round backward).  Each sweep here writes a second buffer, so the
-// old values stay readable, and takes its rows in dependency-level order from
-// a ticket, each row waiting (bounded) for the marks of the rows whose new
-// values it reads; every row then does the reference's operations in its
-// column order, products and differences rounded separately and the division
-// correctly rounded.  Residual, restriction and prolongation are row sums in
+// old values stay readable.  Levels of more than 24,576 rows take their rows
+// in dependency-level order from a ticket, each row waiting (bounded) for the
+// marks of the rows whose new values it reads; smaller levels (the dense
+// coarse operators) run in one CTA, dependency level after dependency level,
+// the new values in shared memory.  Every row does the reference's operations
+// in its column order, products and differences rounded separately and the
+// division correctly rounded.  Residual, restriction and prolongation are row sums in
 // column order.  The whole apply is bit-identical to the reference's.
 //
 // Per level above the coarsest: forward sweep x -> t (the pre-smoothing starts
@@ -37,6 +39,9 @@ struct AmgLevelDev {
     DevBuf<double> Pv, Rv;
     int32_t nc = 0;
     DevBuf<int32_t> fwdOrder, bwdOrder;  // rows in forward / backward dependency-level order
+    DevBuf<int32_t> fwdLvl, bwdLvl;      // level boundaries into the orders (single-CTA sweeps)
+    int nlevF = 0, nlevB = 0, smallThreads = 0;
+    bool small = false;                  // sweeps in one CTA, the new values in shared memory
     DevBuf<unsigned> done, ctl;
     DevBuf<double> x, b, t;  // x, b: levels below the fine one; t: every level
 };
@@ -134,6 +139,71 @@ __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__res
         atomicOr(ctl + 2, 1u);
 }
 
+constexpr int kSgsSmallRows = 24576;  // the sweep's new values in shared memory: 192 KB
+constexpr int kSgsSmallThreads = 1024;
+
+// The same sweep in one CTA for levels of up to kSgsSmallRows rows: the
+// dependency levels one after the other with a block barrier between them,
+// this sweep's new values in shared memory, one warp per row.  Coarse AMG
+// operators are dense enough (hundreds of entries per row) that their
+// dependency chains are nearly as long as their row counts, so the time per
+// row is what counts: the lanes load a row's entries and form its products
+// a_ij x_j (each rounded) together, then every lane runs the reference's
+// ordered chain of subtractions over the broadcast products.  The diagonal's
+// product enters the chain as +0.0, which leaves every value unchanged, as
+// skipping it does.
+template <bool BWD, bool ZERO>
+__global__ void __launch_bounds__(kSgsSmallThreads) k_sgs_small(int n, int nlev, const int32_t *__restrict__ lvl,
+                                                                const int32_t *__restrict__ order,
+                                                                const int32_t *__restrict__ rp,
+                                                                const int32_t *__restrict__ ci,
+                                                                const double *__restrict__ a,
+                                                                const double *__restrict__ b,
+                                                                const double *__restrict__ xin,
+                                                                double *__restrict__ xout)
+{
+    extern __shared__ double xs[];
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+    for (int l = 0; l < nlev; ++l) {
+        const int t1 = __ldg(lvl + l + 1);
+        for (int t = __ldg(lvl + l) + warp; t < t1; t += nwarps) {
+            const int i = __ldg(order + t);
+            double s = __ldg(b + i), aii = 0.0;
+            const int beg = __ldg(rp + i), end = __ldg(rp + i + 1);
+            for (int k0 = beg; k0 < end; k0 += 32) {
+                const int k = k0 + lane;
+                double p = 0.0;
+                if (k < end) {
+                    const int j = __ldg(ci + k);
+                    const double av = __ldg(a + k);
+                    if (j == i) {
+                        aii = av;  // this lane's; shared below
+                    } else {
+                        const bool dep = BWD ? j > i : j < i;
+                        const double xv = dep ? xs[j] : ZERO ? 0.0 : __ldg(xin + j);
+                        p = __dmul_rn(av, xv);
+                    }
+                }
+                const int cnt = end - k0 < 32 ? end - k0 : 32;
+                for (int q = 0; q < cnt; ++q)
+                    s = __dsub_rn(s, __shfl_sync(0xffffffffu, p, q));
+            }
+            // the diagonal value from whichever lane held it (at most one entry per column)
+            for (int o = 16; o > 0; o >>= 1) {
+                const double other = __shfl_xor_sync(0xffffffffu, aii, o);
+                aii = aii != 0.0 ? aii : other;
+            }
+            if (lane == 0) {
+                const double keep = ZERO ? 0.0 : __ldg(xin + i);
+                xs[i] = fabs(aii) > 1e-30 ? __ddiv_rn(s, aii) : keep;
+            }
+        }
+        __syncthreads();
+    }
+    for (int i = threadIdx.x; i < n; i += blockDim.x)
+        xout[i] = xs[i];
+}
+
 // Row sum of a CSR row in column order from 0.0 (CSRMatrix::spmv,
 // src/solver/CSRMatrix.hpp:24-35).
 __device__ __forceinline__ double row_sum(const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
@@ -205,7 +275,8 @@ __global__ void k_amg_direct(int n, const double *__restrict__ lu, const double 
 }
 
 // Rows ordered by dependency level; lower: row i waits for j < i, else j > i.
-void level_order(const AmgCsr &A, bool lower, std::vector<int32_t> &order)
+// ptr receives the level boundaries; returns the widest level.
+int32_t level_order(const AmgCsr &A, bool lower, std::vector<int32_t> &order, std::vector<int32_t> &ptr)
 {
     const int32_t n = A.n;
     std::vector<int32_t> lev(n, 0);
@@ -226,14 +297,19 @@ void level_order(const AmgCsr &A, bool lower, std::vector<int32_t> &order)
     else
         for (int32_t i = n - 1; i >= 0; --i)
             visit(i);
-    std::vector<int32_t> ptr(static_cast<size_t>(nlev) + 1, 0);
+    ptr.assign(static_cast<size_t>(nlev) + 1, 0);
     for (int32_t i = 0; i < n; ++i)
         ++ptr[lev[i] + 1];
-    for (int32_t l = 0; l < nlev; ++l)
+    int32_t widest = 0;
+    for (int32_t l = 0; l < nlev; ++l) {
+        widest = std::max(widest, ptr[l + 1]);
         ptr[l + 1] += ptr[l];
+    }
     order.resize(n);
+    std::vector<int32_t> fill(ptr.begin(), ptr.end() - 1);
     for (int32_t i = 0; i < n; ++i)
-        order[ptr[lev[i]]++] = i;
+        order[fill[lev[i]]++] = i;
+    return widest;
 }
 
 template <class T> cudaError_t upload(DevBuf<T> &dst, const std::vector<T> &src, cudaStream_t st)
@@ -263,6 +339,22 @@ int grid_sweep(simall_context *ctx, int64_t n)
 int sweep(simall_context *ctx, AmgLevelDev &L, bool backward, bool zero, const double *b, const double *xin,
           double *xout)
 {
+    if (L.small) {
+        const size_t smem = static_cast<size_t>(L.n) * sizeof(double);
+        const int nl = backward ? L.nlevB : L.nlevF;
+        const int32_t *lvl = backward ? L.bwdLvl.p : L.fwdLvl.p, *order = backward ? L.bwdOrder.p : L.fwdOrder.p;
+        if (backward)
+            k_sgs_small<true, false><<<1, L.smallThreads, smem, ctx->stream>>>(L.n, nl, lvl, order, L.rp, L.ci, L.v,
+                                                                                 b, xin, xout);
+        else if (zero)
+            k_sgs_small<false, true><<<1, L.smallThreads, smem, ctx->stream>>>(L.n, nl, lvl, order, L.rp, L.ci, L.v,
+                                                                                 b, xin, xout);
+        else
+            k_sgs_small<false, false><<<1, L.smallThreads, smem, ctx->stream>>>(L.n, nl, lvl, order, L.rp, L.ci,
+                                                                                  L.v, b, xin, xout);
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    }
     k_sweep_begin<<<1, 1, 0, ctx->stream>>>(L.ctl.p);
     SIMALL_LAUNCH_CHECK(ctx);
     const int g = grid_sweep(ctx, L.n);
@@ -339,11 +431,20 @@ int amg_setup(simall_solver *s)
             SIMALL_CUDA_TRY(ctx, upload(L.Rv, h.R[l].v, st));
             L.nc = h.R[l].n;
             // only levels that are smoothed need the sweep schedules
-            level_order(A, true, ord);
+            std::vector<int32_t> ordB, ptrF, ptrB;
+            const int32_t wF = level_order(A, true, ord, ptrF);
+            const int32_t wB = level_order(A, false, ordB, ptrB);
             SIMALL_CUDA_TRY(ctx, upload(L.fwdOrder, ord, st));
-            SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // ord is reused
-            level_order(A, false, ord);
-            SIMALL_CUDA_TRY(ctx, upload(L.bwdOrder, ord, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.bwdOrder, ordB, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.fwdLvl, ptrF, st));
+            SIMALL_CUDA_TRY(ctx, upload(L.bwdLvl, ptrB, st));
+            L.nlevF = static_cast<int>(ptrF.size()) - 1;
+            L.nlevB = static_cast<int>(ptrB.size()) - 1;
+            L.small = A.n <= kSgsSmallRows;
+            // one warp per row of the widest level: every warp pays each level's barrier
+            const int32_t w = std::max(wF, wB);
+            L.smallThreads = std::min(kSgsSmallThreads, std::max(32, 32 * w));
+            SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // the schedules die at the end of this block
             SIMALL_CUDA_TRY(ctx, L.done.alloc(A.n));
             SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(L.done.p, 0, A.n * sizeof(unsigned), st));
             SIMALL_CUDA_TRY(ctx, L.ctl.alloc(4));
@@ -351,6 +452,15 @@ int amg_setup(simall_solver *s)
         }
         // the host hierarchy dies at return: finish this level's copies first
         SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+    }
+    {
+        const int smem = kSgsSmallRows * static_cast<int>(sizeof(double));
+        SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_sgs_small<false, true>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_sgs_small<false, false>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+        SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(k_sgs_small<true, false>,
+                                                  cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     }
     d->coarseN = h.coarseN;
     SIMALL_CUDA_TRY(ctx, upload(d->lu, h.lu, st));
@@ -412,8 +522,13 @@ int amg_apply(simall_solver *s, const double *r, double *z)
 
 int amg_apply_launches(const simall_solver *s)
 {
-    const int L = s->amg ? s->amg->nlev : 1;
-    return 11 * (L - 1) + 1;
+    const AmgData *d = s->amg;
+    if (!d)
+        return 1;
+    int k = 1;  // the coarsest level's solve
+    for (int l = 0; l + 1 < d->nlev; ++l)
+        k += d->lv[l]->small ? 7 : 11;  // 4 sweeps (+ 4 ticket resets), residual, restriction, prolongation
+    return k;
 }
 
 int amg_check(simall_solver *s)
