@@ -1,0 +1,122 @@
+"""The benchmark's own workload at full size: the 256^3 variable-coefficient
+Poisson system (16,777,216 cells, 117,047,296 nonzeros; k = exp(N(0,1)) per
+cell through aP = 1/k, p' = 0 on x = 0, walls elsewhere, rhs N(0,1), seed 42).
+At this size the oracle cannot run the solves, so parity is checked where it
+still applies and through properties that do not depend on size:
+
+* the device assembly equals the oracle's assembly of the same mesh, bit for
+  bit (values and rhs);
+* the device SpMV equals the oracle's CSRMatrix::spmv bit for bit;
+* the mixed-precision solve stops below 1e-8, and its reported residual is
+  the FP64 residual ||b - A x|| / ||b|| recomputed independently on the host
+  from the downloaded x with the oracle's SpMV;
+* the FP64 Jacobi-PCG drop-in reaches the same tolerance, and the two
+  solutions agree to the accuracy a 1e-8 residual allows on this system.
+"""
+import numpy as np
+import pytest
+
+from helpers import bits_equal
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+SEED = 42
+
+
+@pytest.fixture(scope="module")
+def system(sg, ctx):
+    torch = pytest.importorskip("torch")
+    from simall_gb300 import workloads as W
+
+    mesh = sg.cartesian(N, N, N)
+    aP, phi, rhs = W.varcoef_inputs(mesh, seed=SEED)
+    ps = sg.PressureSystem(mesh, W.X0_OUTLET, ctx=ctx)
+    ps.assemble(1.0, aP, phi)
+    rp, ci = ps.pattern()
+    vals, arhs = ps.download()
+    yield {"torch": torch, "mesh": mesh, "aP": aP, "phi": phi, "b": rhs, "ps": ps, "rp": rp, "ci": ci,
+           "vals": vals, "arhs": arhs}
+    ps.close()
+
+
+def _oracle_spmv(oracle, rp, ci, v, x):
+    import ctypes as C
+
+    y = np.empty(len(rp) - 1)
+    P = C.c_void_p
+    oracle.lib().orc_spmv(len(rp) - 1, rp.ctypes.data_as(P), ci.ctypes.data_as(P), v.ctypes.data_as(P),
+                          x.ctypes.data_as(P), y.ctypes.data_as(P))
+    return y
+
+
+def test_full_size_assembly_bit_exact(system, oracle):
+    m = system["mesh"]
+    assert len(system["rp"]) - 1 == N ** 3 and len(system["ci"]) == 117047296
+    L = oracle.lib()
+    import ctypes as C
+
+    P = C.c_void_p
+    isP = np.zeros(7, np.uint8)
+    isP[1] = 1  # x = 0: PressureOutlet
+    values = np.empty(len(system["ci"]))
+    rhs = np.empty(m.n_cells)
+    own = m.owner.view(np.int64)
+    nb = m.neighbor.view(np.int64)
+    arrs = [own, nb, m.area_x, m.area_y, m.area_z, m.centroid_x, m.centroid_y, m.centroid_z, m.boundary_zone,
+            m.cell_centroid_x, m.cell_centroid_y, m.cell_centroid_z]
+    ptrs = [np.ascontiguousarray(a).ctypes.data_as(P) for a in arrs]
+    L.orc_assemble(m.n_cells, m.n_faces, *ptrs, isP.ctypes.data_as(P), 7, 1.0,
+                   np.ascontiguousarray(system["aP"]).ctypes.data_as(P),
+                   np.ascontiguousarray(system["phi"]).ctypes.data_as(P), system["rp"].ctypes.data_as(P),
+                   system["ci"].ctypes.data_as(P), values.ctypes.data_as(P), rhs.ctypes.data_as(P))
+    assert bits_equal(values, system["vals"])
+    assert bits_equal(rhs, system["arhs"])
+
+
+def _solve(sg, ctx, system, precision):
+    torch = system["torch"]
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                tolerance=1e-8, maxIterations=50000)
+    s = sg.GpuCGSolver(cfg, precision=precision, ctx=ctx)
+    from simall_gb300._lib import check
+
+    check(s.L.simall_solver_use_pressure_system(s.handle, system["ps"].handle), ctx.handle)
+    b = torch.from_numpy(system["b"]).cuda()
+    x = torch.empty_like(b)
+    s.solve_into(b, x)
+    st = s.stats
+    out = {"x": x.cpu().numpy(), "iterations": int(st.iterations), "true_residual": float(st.true_residual),
+           "converged": bool(st.converged), "solver": s}
+    return out
+
+
+def test_full_size_spmv_bit_exact(sg, ctx, system, oracle):
+    torch = system["torch"]
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi)
+    s = sg.GpuCGSolver(cfg, ctx=ctx)
+    from simall_gb300._lib import check
+
+    check(s.L.simall_solver_use_pressure_system(s.handle, system["ps"].handle), ctx.handle)
+    x = np.random.default_rng(3).standard_normal(N ** 3)
+    y = torch.empty(N ** 3, dtype=torch.float64, device="cuda")
+    s.spmv(torch.from_numpy(x).cuda(), y)
+    s.close()
+    assert bits_equal(y.cpu().numpy(), _oracle_spmv(oracle, system["rp"], system["ci"], system["vals"], x))
+
+
+def test_full_size_mixed_and_fp64_solves(sg, ctx, system, oracle):
+    mixed = _solve(sg, ctx, system, sg.Precision.MIXED)
+    fp64 = _solve(sg, ctx, system, sg.Precision.FP64)
+    b = system["b"]
+    for r in (mixed, fp64):
+        assert r["converged"] and r["true_residual"] < 1e-8
+        host = _oracle_spmv(oracle, system["rp"], system["ci"], system["vals"], r["x"])
+        res = np.linalg.norm(b - host) / np.linalg.norm(b)
+        assert res < 1e-8
+        assert abs(res - r["true_residual"]) <= 1e-6 * res
+        r["solver"].close()
+    # both stop at a 1e-8 residual; each is ~1e-7 from the exact solution here
+    # (cond(A) ~ 1e5), so they agree to a few 1e-7
+    assert np.linalg.norm(mixed["x"] - fp64["x"]) / np.linalg.norm(fp64["x"]) < 2e-6
+    assert abs(mixed["iterations"] - fp64["iterations"]) <= 0.1 * fp64["iterations"]
