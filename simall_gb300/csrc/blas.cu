@@ -259,10 +259,11 @@ int simall_solver_spmv(simall_solver *s, const double *x, double *y, int mem)
         dx = s->p.p;
         dy = s->Ap.p;
     }
-    const int cap = grid_size_streaming(ctx);
-    const int g = s->nRowBlocks < cap ? s->nRowBlocks : cap;
+    const int64_t cap = grid_size_streaming(ctx);
+    const int64_t units = spmv_direct(s) ? (s->n + kBlock - 1) / kBlock : s->nRowBlocks;
+    const int g = static_cast<int>(units < cap ? units : cap);
     k_spmv_staged<<<g < 1 ? 1 : g, kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p,
-                                                             s->nRowBlocks, dx, dy);
+                                                             spmv_schedule(s), dx, dy);
     SIMALL_LAUNCH_CHECK(ctx);
     if (mem == SIMALL_MEM_HOST) {
         SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(y, dy, bytes, cudaMemcpyDeviceToHost, ctx->stream));

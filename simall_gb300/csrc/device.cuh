@@ -171,6 +171,74 @@ __device__ __forceinline__ bool grid_sum_last_fv(const float (&v)[NV], double *p
     return true;
 }
 
+// Row schedule of the SpMV helpers below: nRB >= 0 row-blocks listed in rb
+// (staged through shared memory), or nRB < 0 for one thread per row over
+// -nRB rows (matrices whose rows are short; see spmv_schedule).
+//
+// y-rows of A x with one thread per row and no staging: each thread issues
+// the column indices and values of up to 8 of its entries, then their
+// gathers, before any arithmetic, and no barrier separates loads from
+// arithmetic, so resident warps cover one another's latency.  The products
+// are rounded and summed from 0.0 in column order, as in spmv_rowblocks.
+template <class Epi>
+__device__ __forceinline__ void spmv_rows_exact(const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
+                                                const double *__restrict__ val, int64_t n,
+                                                const double *__restrict__ x, Epi &epi)
+{
+    for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < n;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        const int k1 = __ldg(rowPtr + row + 1);
+        double s = 0.0;
+        for (int k0 = __ldg(rowPtr + row); k0 < k1; k0 += 8) {
+            int c[8];
+            double a[8], g[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c[q] = k0 + q < k1 ? __ldg(colIdx + k0 + q) : -1;
+                a[q] = k0 + q < k1 ? __ldg(val + k0 + q) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                g[q] = c[q] >= 0 ? __ldg(x + c[q]) : 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (c[q] >= 0)
+                    s = __dadd_rn(s, __dmul_rn(a[q], g[q]));
+        }
+        epi(static_cast<int>(row), s);
+    }
+}
+
+// The same with one FMA per nonzero, the operations of spmv_rowblocks_fma.
+template <class Epi>
+__device__ __forceinline__ void spmv_rows_fma(const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
+                                              const double *__restrict__ val, int64_t n,
+                                              const double *__restrict__ x, Epi &epi)
+{
+    for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < n;
+         row += (int64_t)gridDim.x * blockDim.x) {
+        const int k1 = __ldg(rowPtr + row + 1);
+        double s = 0.0;
+        for (int k0 = __ldg(rowPtr + row); k0 < k1; k0 += 8) {
+            int c[8];
+            double a[8], g[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c[q] = k0 + q < k1 ? __ldg(colIdx + k0 + q) : -1;
+                a[q] = k0 + q < k1 ? __ldg(val + k0 + q) : 0.0;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                g[q] = c[q] >= 0 ? __ldg(x + c[q]) : 0.0;
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (c[q] >= 0)
+                    s = fma(a[q], g[q], s);
+        }
+        epi(static_cast<int>(row), s);
+    }
+}
+
 // y-rows of A x for the row-blocks this CTA owns (blockIdx.x, +gridDim.x, ...).
 // Each product a_ij*x_j is rounded once into shared memory and every row is
 // summed from 0.0 in column order with separate roundings, the same operation
@@ -181,6 +249,10 @@ __device__ __forceinline__ void spmv_rowblocks(const int32_t *__restrict__ rowPt
                                                const double *__restrict__ val, const int32_t *__restrict__ rb,
                                                int nRB, const double *__restrict__ x, Epi &epi)
 {
+    if (nRB < 0) {
+        spmv_rows_exact(rowPtr, colIdx, val, -static_cast<int64_t>(nRB), x, epi);
+        return;
+    }
     __shared__ double prod[kSpmvNnzCap];
     for (int b = blockIdx.x; b < nRB; b += gridDim.x) {
         const int r0 = __ldg(rb + b), r1 = __ldg(rb + b + 1);
@@ -241,6 +313,10 @@ __device__ __forceinline__ void spmv_rowblocks_fma(const int32_t *__restrict__ r
                                                    const double *__restrict__ val, const int32_t *__restrict__ rb,
                                                    int nRB, const double *__restrict__ x, Epi &epi)
 {
+    if (nRB < 0) {
+        spmv_rows_fma(rowPtr, colIdx, val, -static_cast<int64_t>(nRB), x, epi);
+        return;
+    }
     __shared__ double sv[kSpmvNnzCap];
     __shared__ double sx[kSpmvNnzCap];
     for (int b = blockIdx.x; b < nRB; b += gridDim.x) {

@@ -714,6 +714,17 @@ __global__ void __launch_bounds__(kBlock) k_gm_step(const int32_t *__restrict__ 
     const double *src = stale ? Vj : u;
     __shared__ double prod[kSpmvNnzCap];
     StepEpi epi{src, invD, V0, mul, Vj, out, j == 0, 0.0};
+    if (nRB < 0) {  // one thread per row (the schedule of spmv_rowblocks)
+        const int64_t n = -static_cast<int64_t>(nRB);
+        for (int64_t row = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; row < n;
+             row += (int64_t)gridDim.x * blockDim.x) {
+            const int k1 = __ldg(rowPtr + row + 1);
+            double sacc = 0.0;
+            for (int q = __ldg(rowPtr + row); q < k1; ++q)
+                sacc = __dadd_rn(sacc, __dmul_rn(__ldg(val + q), __dmul_rn(__ldg(src + __ldg(colIdx + q)), mul)));
+            epi(static_cast<int>(row), sacc);
+        }
+    }
     // the staged SpMV with the gathered operand scaled on the fly
     for (int bI = blockIdx.x; bI < nRB; bI += gridDim.x) {
         const int r0 = __ldg(rb + bI), r1 = __ldg(rb + bI + 1);
@@ -935,7 +946,7 @@ int enqueue_bicgstab_iteration(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
     KrylovData *d = s->krylov;
-    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    const int64_t n = s->n, rbThreads = spmv_items(s);
     const bool ilu = use_ilu(s);
     const double *invD = ilu ? nullptr : s->invDiag.p;
     KrylovScalars *k = d->ks.p;
@@ -945,7 +956,7 @@ int enqueue_bicgstab_iteration(simall_solver *s)
         if (e)
             return e;
     }
-    KLAUNCH(k_bi_spmv_v, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->y.p, d->v.p,
+    KLAUNCH(k_bi_spmv_v, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), d->y.p, d->v.p,
             d->rh.p, s->partials.p, k);
     KLAUNCH(k_bi_s, n, n, s->r.p, d->v.p, invD, d->sv.p, s->z.p, s->partials.p, k);
     if (ilu) {
@@ -953,7 +964,7 @@ int enqueue_bicgstab_iteration(simall_solver *s)
         if (e)
             return e;
     }
-    KLAUNCH(k_bi_spmv_t, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->z.p, d->t.p,
+    KLAUNCH(k_bi_spmv_t, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), s->z.p, d->t.p,
             d->sv.p, s->partials.p, k);
     KLAUNCH(k_bi_update, n, n, s->x.p, d->y.p, s->z.p, s->r.p, d->sv.p, d->t.p, d->rh.p, s->partials.p, k);
     return SIMALL_OK;
@@ -1021,8 +1032,8 @@ int chunked_solve(simall_solver *s)
             if (e)
                 return e;
         }
-        const int64_t rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
-        KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu1.p,
+        const int64_t rbThreads = spmv_items(s);
+        KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), d->tu1.p,
                 d->tAu1.p, d->tAu2.p, d->v.p, d->rh.p, s->partials.p, d->ks.p, 1);
     } else {
         KLAUNCH(k_bi_init, n, n, s->b.p, s->x.p, s->r.p, d->rh.p, s->p.p, d->v.p, s->partials.p, d->ks.p);
@@ -1077,7 +1088,7 @@ int enqueue_tfqmr_iteration(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
     KrylovData *d = s->krylov;
-    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    const int64_t n = s->n, rbThreads = spmv_items(s);
     const bool ilu = use_ilu(s);
     const double *invD = ilu ? nullptr : s->invDiag.p;
     KrylovScalars *k = d->ks.p;
@@ -1087,11 +1098,11 @@ int enqueue_tfqmr_iteration(simall_solver *s)
             return e;
     }
     KLAUNCH(k_tf_u2, n, n, d->tu1.p, d->v.p, invD, s->z.p, d->tu2.p, k);
-    KLAUNCH(k_tf_spmv_u2, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu2.p,
+    KLAUNCH(k_tf_spmv_u2, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), d->tu2.p,
             d->tAu2.p, d->tAu1.p, d->tw.p, s->partials.p, k);
     KLAUNCH(k_tf_update, n, n, d->tu1.p, d->tu2.p, d->tAu1.p, d->tAu2.p, d->td.p, s->x.p, s->r.p, d->rh.p,
             s->partials.p, k);
-    KLAUNCH(k_tf_check, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->x.p, s->b.p,
+    KLAUNCH(k_tf_check, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), s->x.p, s->b.p,
             s->partials.p, k);
     if (ilu) {
         int e = ilu_apply(s, s->r.p, s->z.p);
@@ -1099,7 +1110,7 @@ int enqueue_tfqmr_iteration(simall_solver *s)
             return e;
     }
     KLAUNCH(k_tf_u1, n, n, s->r.p, invD, s->z.p, d->tu2.p, d->tu1.p, k);
-    KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, d->tu1.p,
+    KLAUNCH(k_tf_spmv_u1, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), d->tu1.p,
             d->tAu1.p, d->tAu2.p, d->v.p, d->rh.p, s->partials.p, k, 0);
     return SIMALL_OK;
 }
@@ -1108,10 +1119,10 @@ int enqueue_gmres_restart(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
     KrylovData *d = s->krylov;
-    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    const int64_t n = s->n, rbThreads = spmv_items(s);
     const bool ilu = use_ilu(s);
     // the restart's M r goes to zb[1], the buffer step 0 reads its pending vector from
-    KLAUNCH(k_gm_resid, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->x.p, s->b.p,
+    KLAUNCH(k_gm_resid, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), s->x.p, s->b.p,
             ilu ? nullptr : s->invDiag.p, s->r.p, d->zb[1].p, s->partials.p, d->ks.p, d->hs.p, d->m);
     if (ilu) {
         int e = ilu_apply(s, s->r.p, d->zb[1].p);
@@ -1126,13 +1137,13 @@ int enqueue_gmres_step(simall_solver *s, int j)
 {
     simall_context *ctx = s->ctx;
     KrylovData *d = s->krylov;
-    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+    const int64_t n = s->n, rbThreads = spmv_items(s);
     const bool ilu = use_ilu(s);
     const int m = d->m;
     auto Vp = [&](int i) { return d->V.p + static_cast<int64_t>(i) * d->ldV; };
     double *z = d->zb[j & 1].p;
     const double *u = d->zb[(j + 1) & 1].p;  // the previous step's (or the restart's) vector
-    KLAUNCH(k_gm_step, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, u, Vp(j), Vp(0),
+    KLAUNCH(k_gm_step, rbThreads, s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), u, Vp(j), Vp(0),
             ilu ? nullptr : s->invDiag.p, ilu ? d->w.p : z, s->partials.p, d->ks.p, d->hs.p, m, j);
     if (ilu) {
         int e = ilu_apply(s, d->w.p, z);

@@ -952,8 +952,8 @@ int enqueue_update_branch(simall_solver *s, int par)
     k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_true_residual<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_true_residual),
-                                       static_cast<int64_t>(s->nRowBlocks) * kBlock),
-                         kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks,
+                                       spmv_items(s)),
+                         kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s),
                                                    s->x.p, s->b.p, s->r.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rv[1 - par].p, s->partials.p, s->scal.p);

@@ -217,6 +217,32 @@ __global__ void __launch_bounds__(kBlock) k_spmv_pap(const int32_t *__restrict__
     }
 }
 
+// K1 for matrices with short rows: the same, one thread per row (spmv_rows_fma).
+__global__ void __launch_bounds__(kBlock) k_spmv_pap_rows(const int32_t *__restrict__ rowPtr,
+                                                          const int32_t *__restrict__ colIdx,
+                                                          const double *__restrict__ val, int64_t n,
+                                                          const double *__restrict__ p, double *__restrict__ Ap,
+                                                          double *partials, SolveScalars *s)
+{
+    if (ld_done(s))
+        return;
+    PapEpi epi{Ap, p, 0.0};
+    spmv_rows_fma(rowPtr, colIdx, val, n, p, epi);
+    double v[1] = {epi.acc};
+    if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0) {
+        const double pAp = v[0];
+        s->pAp = pAp;
+        if (pAp == 0.0) {
+            s->last = sqrt(s->rz) / s->bnorm;
+            s->result = s->iter;
+            s->done = 1;
+            s->status = SIMALL_ERR_BREAKDOWN;
+        } else {
+            s->alpha = s->rz / pAp;
+        }
+    }
+}
+
 struct StoreEpi {
     double *y;
     __device__ __forceinline__ void operator()(int row, double v) { y[row] = v; }
@@ -516,14 +542,33 @@ void drop_graphs(simall_solver *s)
     s->graphs.clear();
 }
 
+// K1: one thread per row when the rows are short on average (no staging
+// barrier), else the staged row-blocks.
+int enqueue_spmv_pap(simall_solver *s)
+{
+    simall_context *ctx = s->ctx;
+    if (spmv_direct(s)) {
+        k_spmv_pap_rows<<<resident_grid(ctx, reinterpret_cast<const void *>(k_spmv_pap_rows), s->n), kBlock, 0,
+                          ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->n, s->p.p, s->Ap.p, s->partials.p,
+                                         s->scal.p);
+    } else {
+        const int64_t rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
+        k_spmv_pap<<<resident_grid(ctx, reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0,
+                     ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p,
+                                    s->partials.p, s->scal.p);
+    }
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
 // Enqueue one FP64 iteration (Jacobi or ILU0).
 int enqueue_iteration(simall_solver *s)
 {
     simall_context *ctx = s->ctx;
-    const int64_t n = s->n, rbThreads = static_cast<int64_t>(s->nRowBlocks) * kBlock;
-    k_spmv_pap<<<resident_grid(ctx, reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0, ctx->stream>>>(
-        s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p, s->partials.p, s->scal.p);
-    SIMALL_LAUNCH_CHECK(ctx);
+    const int64_t n = s->n;
+    int e0 = enqueue_spmv_pap(s);
+    if (e0)
+        return e0;
     if (sweep_preconditioner(s->cfg.preconditioner)) {
         k_update_xr<<<resident_grid(ctx, reinterpret_cast<const void *>(k_update_xr), n), kBlock, 0, ctx->stream>>>(
             n, s->p.p, s->Ap.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
@@ -689,8 +734,8 @@ int solver_fetch_scalars(simall_solver *s)
 int solver_true_residual(simall_solver *s, const double *x, const double *b, double *r, double *rr)
 {
     simall_context *ctx = s->ctx;
-    k_residual<<<spmv_grid(ctx, s->nRowBlocks), kBlock, 0, ctx->stream>>>(
-        s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, x, b, r, s->partials.p,
+    k_residual<<<spmv_direct(s) ? grid_for(ctx, s->n) : spmv_grid(ctx, s->nRowBlocks), kBlock, 0, ctx->stream>>>(
+        s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), x, b, r, s->partials.p,
         &s->scal.p->counter[4], reinterpret_cast<double *>(&s->scal.p->rr));
     SIMALL_LAUNCH_CHECK(ctx);
     if (rr) {
@@ -1031,16 +1076,18 @@ int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms
     auto launch = [&]() -> int {
         switch (kernel) {
         case 0:
-            k_spmv_plain<<<rg(reinterpret_cast<const void *>(k_spmv_plain), rbThreads), kBlock, 0, ctx->stream>>>(
-                s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p);
+            k_spmv_plain<<<rg(reinterpret_cast<const void *>(k_spmv_plain), spmv_items(s)), kBlock, 0,
+                           ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), s->p.p,
+                                          s->Ap.p);
             b = 12.0 * nz + 20.0 * nd + 4.0;
             break;
-        case 1:
-            k_spmv_pap<<<rg(reinterpret_cast<const void *>(k_spmv_pap), rbThreads), kBlock, 0, ctx->stream>>>(
-                s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, s->nRowBlocks, s->p.p, s->Ap.p, s->partials.p,
-                s->scal.p);
+        case 1: {
+            const int e1 = enqueue_spmv_pap(s);
+            if (e1)
+                return e1;
             b = 12.0 * nz + 20.0 * nd + 4.0;
             break;
+        }
         case 2:
             k_update_jacobi<<<rg(reinterpret_cast<const void *>(k_update_jacobi), s->n), kBlock, 0, ctx->stream>>>(
                 s->n, s->p.p, s->Ap.p, s->invDiag.p, s->x.p, s->r.p, s->z.p, s->partials.p, s->scal.p);

@@ -79,6 +79,20 @@ struct simall_solver {
 
 namespace simall {
 
+// Row schedule passed as nRB to the SpMV helpers of device.cuh: matrices
+// whose rows are short on average (at most 16 nonzeros) run one thread per
+// row without staging (-n), others the staged row-blocks.  spmv_items: the
+// threads the schedule wants, for sizing the grid.
+inline bool spmv_direct(const simall_solver *s) { return s->nnz <= 16 * s->n; }
+inline int spmv_schedule(const simall_solver *s)
+{
+    return spmv_direct(s) ? -static_cast<int>(s->n) : s->nRowBlocks;
+}
+inline int64_t spmv_items(const simall_solver *s)
+{
+    return spmv_direct(s) ? s->n : static_cast<int64_t>(s->nRowBlocks) * kBlock;
+}
+
 // The preconditioners applied by kernels of their own (ILU(0) and SSOR
 // sweeps, the AMG V-cycle) rather than fused into the Krylov updates as
 // Jacobi is.  ilu_setup / ilu_apply / ilu_check / ilu_apply_launches serve
