@@ -8,8 +8,8 @@
 // the rows before it and the old values of the rows after it (forward; the
 // other way round backward).  Each sweep here writes a second buffer, so the
 // old values stay readable.  Levels of more than 24,576 rows take their rows
-// in dependency-level order from a ticket, each row waiting (bounded) for the
-// marks of the rows whose new values it reads; smaller levels (the dense
+// in dependency-level order from a ticket, each row polling (bounded) the new
+// values it reads until they land; smaller levels (the dense
 // coarse operators) run in one CTA, dependency level after dependency level,
 // the new values in shared memory.  Every row does the reference's operations
 // in its column order, products and differences rounded separately and the
@@ -42,7 +42,7 @@ struct AmgLevelDev {
     DevBuf<int32_t> fwdLvl, bwdLvl;      // level boundaries into the orders (single-CTA sweeps)
     int nlevF = 0, nlevB = 0, smallThreads = 0;
     bool small = false;                  // sweeps in one CTA, the new values in shared memory
-    DevBuf<unsigned> done, ctl;
+    DevBuf<unsigned> ctl;  // free-running sweeps: [0] ticket, [2] timeout flag
     DevBuf<double> x, b, t;  // x, b: levels below the fine one; t: every level
 };
 
@@ -55,42 +55,18 @@ struct AmgData {
 
 namespace {
 
-// Waits (bounded) for the marks of the up to four rows flagged in dep; false
-// on timeout.
-__device__ __forceinline__ bool wait_deps4(const unsigned *done, const int (&j)[4], const bool (&dep)[4],
-                                           unsigned sweep)
-{
-    unsigned ns = 16;
-    for (unsigned spins = 0;; ++spins) {
-        bool all = true;
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-            if (dep[q])
-                all = (ld_acquire(done + j[q]) == sweep) && all;
-        if (all)
-            return true;
-        if (spins >= kSweepMaxSpins)
-            return false;
-        if (spins >= 4) {
-            __nanosleep(ns);
-            ns = ns < 256 ? 2 * ns : 256;
-        }
-    }
-}
-
 // One Gauss-Seidel sweep over the rows in `order`.  Forward (BWD false): row i
-// reads xout_j (this sweep's values, j < i, after their marks) and xin_j
-// (j > i; ZERO: 0) and writes xout_i = (b_i - sum_{j != i} a_ij x_j) / a_ii, or
-// keeps xin_i when |a_ii| <= 1e-30.  Backward: the same with j > i from xout.
+// reads xout_j (this sweep's values, j < i, polled until they land; xout holds
+// kPending before) and xin_j (j > i; ZERO: 0) and writes xout_i = (b_i -
+// sum_{j != i} a_ij x_j) / a_ii, or keeps xin_i when |a_ii| <= 1e-30.
+// Backward: the same with j > i from xout.
 template <bool BWD, bool ZERO>
 __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__restrict__ order,
                                                      const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                                                      const double *__restrict__ a, const double *__restrict__ b,
-                                                     const double *__restrict__ xin, double *xout, unsigned *done,
-                                                     unsigned *ctl)
+                                                     const double *__restrict__ xin, double *xout, unsigned *ctl)
 {
     const int lane = threadIdx.x & 31;
-    const unsigned sweep = __ldcg(ctl + 1);
     bool ok = true;
     for (;;) {
         int base = 0;
@@ -115,11 +91,12 @@ __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__res
                     av[q] = in ? __ldg(a + kp + q) : 0.0;
                     dep[q] = BWD ? j[q] > i : j[q] < i;
                 }
-                ok = wait_deps4(done, j, dep, sweep) && ok;
                 double v[4];
+                ok = wait_values4(xout, j, dep, v) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    v[q] = j[q] == i ? 0.0 : dep[q] ? __ldcg(xout + j[q]) : ZERO ? 0.0 : __ldg(xin + j[q]);
+                    if (!dep[q])
+                        v[q] = j[q] == i ? 0.0 : ZERO ? 0.0 : __ldg(xin + j[q]);
 #pragma unroll
                 for (int q = 0; q < 4; ++q) {
                     if (kp + q >= end)
@@ -131,8 +108,7 @@ __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__res
                 }
             }
             const double keep = ZERO ? 0.0 : __ldg(xin + i);
-            __stcg(xout + i, fabs(aii) > 1e-30 ? __ddiv_rn(s, aii) : keep);
-            st_release(done + i, sweep);
+            st_value(xout + i, fabs(aii) > 1e-30 ? __ddiv_rn(s, aii) : keep);
         }
     }
     if (!ok)
@@ -355,19 +331,16 @@ int sweep(simall_context *ctx, AmgLevelDev &L, bool backward, bool zero, const d
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
-    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(L.ctl.p);
+    k_sweep_begin_values<<<grid_rows(ctx, L.n), kBlock, 0, ctx->stream>>>(L.ctl.p, xout, L.n);
     SIMALL_LAUNCH_CHECK(ctx);
     const int g = grid_sweep(ctx, L.n);
     const int32_t *order = backward ? L.bwdOrder.p : L.fwdOrder.p;
     if (backward)
-        k_sgs_free<true, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
-                                                               L.ctl.p);
+        k_sgs_free<true, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
     else if (zero)
-        k_sgs_free<false, true><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
-                                                               L.ctl.p);
+        k_sgs_free<false, true><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
     else
-        k_sgs_free<false, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.done.p,
-                                                                L.ctl.p);
+        k_sgs_free<false, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
@@ -445,8 +418,6 @@ int amg_setup(simall_solver *s)
             const int32_t w = std::max(wF, wB);
             L.smallThreads = std::min(kSgsSmallThreads, std::max(32, 32 * w));
             SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // the schedules die at the end of this block
-            SIMALL_CUDA_TRY(ctx, L.done.alloc(A.n));
-            SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(L.done.p, 0, A.n * sizeof(unsigned), st));
             SIMALL_CUDA_TRY(ctx, L.ctl.alloc(4));
             SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(L.ctl.p, 0, 4 * sizeof(unsigned), st));
         }

@@ -15,11 +15,13 @@
 // level, and the sweeps (twice per PCG iteration) run as one kernel each
 // without levels
 // between launches: warps take 32 consecutive rows of the level order from an
-// atomic ticket, and a row waits only for the rows it reads, each of which
-// publishes its value and then its "done" mark (release) and is read after the
-// mark (acquire).  Rows are handed out in level order, so every row waited for
-// was handed to a warp that is already running; the wait is bounded and a
-// timeout is reported (it never happens unless a row is never produced).
+// atomic ticket, and a row waits only for the rows it reads: the output
+// vector starts the sweep filled with a pending marker (a signalling NaN),
+// each row publishes its value with one relaxed store, and a reader polls the
+// values it needs until none is pending.  Rows are handed out in level order,
+// so every row waited for was handed to a warp that is already running; the
+// wait is bounded and a timeout is reported (it never happens unless a row is
+// never produced).
 //
 // SSOR (SsorPreconditioner, :163-231, with the w = 1 that make_preconditioner
 // gives it) has the same dependency structure and runs on the same schedule
@@ -119,19 +121,17 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_level(const int32_t *__restr
 }
 
 // Forward sweep y_i = r_i - sum_{j<i} l_ij y_j over rows in level order
-// (SSOR: a_ij, and the sum times invD_i).
-// Dependencies are taken four at a time: wait for the four marks, load the
-// four values, then apply them in column order (the reference's order).
+// (SSOR: a_ij, and the sum times invD_i).  y holds kPending until a row's value
+// lands (k_sweep_begin_values).  Dependencies are taken four at a time: poll
+// the four values, then apply them in column order (the reference's order).
 template <bool SSOR>
 __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *__restrict__ order,
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const double *__restrict__ lu, const double *__restrict__ r,
-                                                         const double *__restrict__ invD, double *y, unsigned *done,
-                                                         unsigned *ctl)
+                                                         const double *__restrict__ invD, double *y, unsigned *ctl)
 {
     const int lane = threadIdx.x & 31;
-    const unsigned sweep = __ldcg(ctl + 1);
     bool ok = true;
     for (;;) {
         int base = 0;
@@ -147,6 +147,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
             const int end = __ldg(rowPtr + i + 1);
             for (int kp = __ldg(rowPtr + i); kp < end;) {
                 int j[4];
+                bool dep[4];
                 double a[4];
                 int cnt = 0;
 #pragma unroll
@@ -159,11 +160,11 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
                 }
                 if (cnt == 0)
                     break;
-                ok = wait_rows4(done, j, cnt, sweep) && ok;
-                double v[4];
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
-                    v[q] = q < cnt ? __ldcg(y + j[q]) : 0.0;
+                    dep[q] = q < cnt;
+                double v[4];
+                ok = wait_values4(y, j, dep, v) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (q < cnt)
@@ -174,8 +175,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
             }
             if (SSOR)
                 s = __dmul_rn(s, __ldg(invD + i));
-            __stcg(y + i, s);
-            st_release(done + i, sweep);
+            st_value(y + i, s);
         }
     }
     if (!ok)
@@ -183,18 +183,17 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
 }
 
 // Backward sweep z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii over rows in level order
-// (SSOR: (a_ii y_i - sum_{j>i} a_ij z_j) invD_i).
+// (SSOR: (a_ii y_i - sum_{j>i} a_ij z_j) invD_i); z holds kPending until a
+// row's value lands.
 template <bool SSOR>
 __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *__restrict__ order,
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const int32_t *__restrict__ diagPtr,
                                                          const double *__restrict__ lu, const double *__restrict__ y,
-                                                         const double *__restrict__ invD, double *z, unsigned *done,
-                                                         unsigned *ctl)
+                                                         const double *__restrict__ invD, double *z, unsigned *ctl)
 {
     const int lane = threadIdx.x & 31;
-    const unsigned sweep = __ldcg(ctl + 1);
     bool ok = true;
     for (;;) {
         int base = 0;
@@ -213,6 +212,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
             const int end = __ldg(rowPtr + i + 1);
             for (int kp = kd + 1; kp < end;) {
                 int j[4];
+                bool dep[4];
                 double a[4];
                 int cnt = 0;
 #pragma unroll
@@ -220,13 +220,11 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
                     const bool in = kp + q < end;
                     j[q] = in ? __ldg(colIdx + kp + q) : i;
                     a[q] = in ? __ldg(lu + kp + q) : 0.0;
+                    dep[q] = in;
                     cnt += in ? 1 : 0;
                 }
-                ok = wait_rows4(done, j, cnt, sweep) && ok;
                 double v[4];
-#pragma unroll
-                for (int q = 0; q < 4; ++q)
-                    v[q] = q < cnt ? __ldcg(z + j[q]) : 0.0;
+                ok = wait_values4(z, j, dep, v) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (q < cnt)
@@ -234,12 +232,11 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
                 kp += cnt;
             }
             if (SSOR) {
-                __stcg(z + i, __dmul_rn(s, __ldg(invD + i)));
+                st_value(z + i, __dmul_rn(s, __ldg(invD + i)));
             } else {
                 const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
-                __stcg(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
+                st_value(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
             }
-            st_release(done + i, sweep);
         }
     }
     if (!ok)
@@ -610,9 +607,7 @@ int analyse(simall_context *ctx, IluData *d, int64_t n, const int32_t *rowPtr, c
     SIMALL_CUDA_TRY(ctx, d->fwdRows.alloc(n));
     SIMALL_CUDA_TRY(ctx, d->bwdRows.alloc(n));
     SIMALL_CUDA_TRY(ctx, d->y.alloc(n));
-    SIMALL_CUDA_TRY(ctx, d->done.alloc(n));
     SIMALL_CUDA_TRY(ctx, d->sweepCtl.alloc(4));
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->done.p, 0, n * sizeof(unsigned), ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(d->sweepCtl.p, 0, 4 * sizeof(unsigned), ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d->diagPtr.p, d->h_diagPtr.data(), n * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, ctx->stream));
@@ -758,17 +753,17 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
         return SIMALL_OK;
     }
     const int grid = ctx->num_sms * 4;  // 32 warps per SM take rows; more only add waiting warps
-    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
+    const int fill = std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8);
+    k_sweep_begin_values<<<fill < 1 ? 1 : fill, kBlock, 0, ctx->stream>>>(d->sweepCtl.p, d->y.p, n);
     SIMALL_LAUNCH_CHECK(ctx);
     auto fwd = ssor ? k_ilu_fwd_free<true> : k_ilu_fwd_free<false>;
-    fwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->invD, d->y.p, d->done.p,
-                                          d->sweepCtl.p);
+    fwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->invD, d->y.p, d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_sweep_begin<<<1, 1, 0, ctx->stream>>>(d->sweepCtl.p);
+    k_sweep_begin_values<<<fill < 1 ? 1 : fill, kBlock, 0, ctx->stream>>>(d->sweepCtl.p, z, n);
     SIMALL_LAUNCH_CHECK(ctx);
     auto bwd = ssor ? k_ilu_bwd_free<true> : k_ilu_bwd_free<false>;
     bwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, d->invD, z,
-                                          d->done.p, d->sweepCtl.p);
+                                          d->sweepCtl.p);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }

@@ -12,8 +12,7 @@ struct IluData {
     DevBuf<int32_t> fwdRows;    // rows grouped by forward level
     DevBuf<int32_t> bwdRows;    // rows grouped by backward level
     DevBuf<double> y;           // forward-sweep scratch
-    DevBuf<unsigned> done;      // sweeps: done[i] == sweep number once row i is final
-    DevBuf<unsigned> sweepCtl;  // sweeps: [0] work ticket, [1] sweep number, [2] wait-timeout flag
+    DevBuf<unsigned> sweepCtl;  // sweeps: [0] work ticket, [2] wait-timeout flag
     std::vector<int32_t> fwdLevelPtr, bwdLevelPtr;  // level boundaries into fwdRows / bwdRows (host)
     DevBuf<int32_t> fwdLvl, bwdLvl;                 // the same on the device (single-CTA path)
     std::vector<int32_t> h_diagPtr;

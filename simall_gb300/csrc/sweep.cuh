@@ -1,8 +1,8 @@
-// Row marks for sweeps that run without level barriers (ILU(0)/SSOR in
-// ilu0.cu, the AMG smoother in amg.cu): a row publishes its value, then its
-// mark (release); a reader waits for the marks of the rows it reads (acquire,
-// bounded) before loading their values.  ctl[0] is the work ticket, ctl[1]
-// the sweep number the marks carry, ctl[2] the wait-timeout flag.
+// Waits of the sweeps that run without level barriers (ILU(0)/SSOR in
+// ilu0.cu, the AMG smoother in amg.cu): rows are taken in dependency-level
+// order from a ticket and wait (bounded) for the rows they read.  ctl[0] is
+// the work ticket, ctl[1] a sweep number (row marks), ctl[2] the wait-timeout
+// flag.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -70,6 +70,65 @@ __device__ __forceinline__ bool wait_rows4(const unsigned *done, const int (&j)[
             ns = ns < 256 ? 2 * ns : 256;
         }
     }
+}
+
+// Values published in place of marks: before a sweep its output vector is
+// filled with kPending, a signalling NaN (no arithmetic produces one, and the
+// solver rejects non-finite input), each row publishes its value with one
+// relaxed store, and a reader polls the values it needs until none is pending.
+// One memory round trip less per dependency level than mark-then-value.
+constexpr unsigned long long kPending = 0x7FF4C0DE5EED5A1EULL;
+
+__device__ __forceinline__ double ld_value(const double *p)
+{
+    unsigned long long v;
+    asm volatile("ld.relaxed.gpu.global.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return __longlong_as_double(static_cast<long long>(v));
+}
+
+__device__ __forceinline__ void st_value(double *p, double v)
+{
+    asm volatile("st.relaxed.gpu.global.b64 [%0], %1;" ::"l"(p), "l"(__double_as_longlong(v)) : "memory");
+}
+
+__device__ __forceinline__ bool pending(double v)
+{
+    return static_cast<unsigned long long>(__double_as_longlong(v)) == kPending;
+}
+
+// Polls x[j[q]] for the flagged q until none is pending (bounded, backing off
+// as wait_rows4 does); v receives the values, 0 for the others.  False on
+// timeout.
+__device__ __forceinline__ bool wait_values4(const double *x, const int (&j)[4], const bool (&dep)[4],
+                                             double (&v)[4])
+{
+    unsigned ns = 16;
+    for (unsigned spins = 0;; ++spins) {
+        bool all = true;
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            v[q] = dep[q] ? ld_value(x + j[q]) : 0.0;
+            all = !(dep[q] && pending(v[q])) && all;
+        }
+        if (all)
+            return true;
+        if (spins >= kSweepMaxSpins)
+            return false;
+        if (spins >= 4) {
+            __nanosleep(ns);
+            ns = ns < 256 ? 2 * ns : 256;
+        }
+    }
+}
+
+// Next sweep: the output vector to kPending, the ticket to 0.
+[[maybe_unused]] __global__ void k_sweep_begin_values(unsigned *ctl, double *out, int n)
+{
+    const double p = __longlong_as_double(static_cast<long long>(kPending));
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = p;
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        ctl[0] = 0u;
 }
 
 }  // namespace
