@@ -521,12 +521,14 @@ __global__ void __launch_bounds__(kBlock) k_div_check(int n, const double *__res
     }
 }
 
-// One warp waits for a mark that nothing sets: the bounded wait of the sweeps
-// running out, observed from the host.
-__global__ void k_wait_probe(const unsigned *flag, unsigned *out)
+// One warp waits for a value that nothing publishes (x[0] stays pending): the
+// bounded wait of the sweeps running out, observed from the host.
+__global__ void k_wait_probe(const double *x, unsigned *out)
 {
     const int j[4] = {0, 0, 0, 0};
-    const bool ok = wait_rows4(flag, j, 1, 1u);
+    const bool dep[4] = {true, false, false, false};
+    double v[4];
+    const bool ok = wait_values4(x, j, dep, v);
     if (threadIdx.x == 0)
         out[0] = ok ? 0u : 1u;
 }
@@ -931,14 +933,18 @@ int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *se
     if (!ctx || !timed_out)
         return SIMALL_ERR_INVALID_ARGUMENT;
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
-    DevBuf<unsigned> buf;
-    SIMALL_CUDA_TRY(ctx, buf.alloc(2));
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(buf.p, 0, 2 * sizeof(unsigned), ctx->stream));
+    DevBuf<unsigned> buf;  // [0] ticket of the fill, [2] unused, [4] the probe's result
+    DevBuf<double> val;
+    SIMALL_CUDA_TRY(ctx, buf.alloc(5));
+    SIMALL_CUDA_TRY(ctx, val.alloc(1));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(buf.p, 0, 5 * sizeof(unsigned), ctx->stream));
+    k_sweep_begin_values<<<1, 32, 0, ctx->stream>>>(buf.p, val.p, 1);  // val[0] = pending
+    SIMALL_LAUNCH_CHECK(ctx);
     const auto t0 = std::chrono::steady_clock::now();
-    k_wait_probe<<<1, 32, 0, ctx->stream>>>(buf.p, buf.p + 1);
+    k_wait_probe<<<1, 32, 0, ctx->stream>>>(val.p, buf.p + 4);
     SIMALL_LAUNCH_CHECK(ctx);
     unsigned h = 0;
-    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, buf.p + 1, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, buf.p + 4, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     *timed_out = static_cast<int>(h);
     if (seconds)
