@@ -61,7 +61,7 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-8)
     ap.add_argument("--max-iterations", type=int, default=50000)
     ap.add_argument("--fp64-steps", type=int, default=2)
-    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--cpu-seconds", type=float, default=20.0, help="CPU work per baseline sample")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batched-systems", type=int, default=512,
