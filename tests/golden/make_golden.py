@@ -6,7 +6,7 @@ sources).  Every array stored here is an output of the reference's functions
 (CartesianMesher + ConnectivityBuilder + compute_geometry,
 renumber_cells_cuthill_mckee, SimpleAlgorithm::build_sparsity /
 assemble_pressure_correction / assemble_momentum, CGSolver::solve with
-Jacobi and ILU0, GMRES(m) and BiCGSTAB, the
+Jacobi, ILU0, SSOR and AMG, GMRES(m), BiCGSTAB and TFQMR, the
 preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
 advance_time_step runs, PisoAlgorithm / PimpleAlgorithm time steps,
 io::Checkpoint::write, SimpTopology steps,
@@ -293,6 +293,47 @@ def adjoint_case(name):
                         grad=grad, iters=np.array(its), residual=np.array(res), ok=np.array(rc))
 
 
+def solvers_case(name):
+    """SSOR and AMG (apply, CG), TFQMR, and GMRES/BiCGSTAB with SSOR and AMG
+    on a distorted, RCM-renumbered 7x6x5 pressure system and on the 40-point
+    upwind convection-diffusion matrix of tests/unit/solver/test_tfqmr_solver.cpp."""
+    dims, seed = (7, 6, 5), 71
+    m = R.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=0.2, seed=seed), do_rcm=True)
+    rng = np.random.default_rng(seed)
+    aP = rng.uniform(0.5, 2.0, m["nC"])
+    phi = rng.standard_normal(m["nF"])
+    phi[m["neighbor"] < 0] = 0.0
+    rp, ci, v, rhs = R.assemble(m, [], 1.0, aP, phi)
+    R.free_mesh(m)
+    out = {"rowPtr": rp, "colIdx": ci, "values": v, "rhs": rhs}
+    r = rng.standard_normal(len(rhs))
+    out["apply_r"] = r
+    for pc, tag in ((2, "ssor"), (3, "amg")):
+        out[f"apply_{tag}_z"] = R.precond_apply(pc, rp, ci, v, r)
+        x, it, last, _ = R.cg(rp, ci, v, rhs, pc, 1e-10, 500)
+        out[f"cg_{tag}_x"], out[f"cg_{tag}_iters"], out[f"cg_{tag}_last"] = x, np.array(it), np.array(last)
+    for pc, tag in ((1, "ilu0"), (2, "ssor")):
+        x, it, last, _ = R.krylov(3, rp, ci, v, rhs, pc, 1e-8, 300)
+        out[f"tfqmr_{tag}_x"], out[f"tfqmr_{tag}_iters"], out[f"tfqmr_{tag}_last"] = x, np.array(it), np.array(last)
+    n = 40
+    crp, cci, cv = [0], [], []
+    for i in range(n):
+        for j, a in ((i - 1, -6.0), (i, 7.0), (i + 1, -1.0)):
+            if 0 <= j < n:
+                cci.append(j)
+                cv.append(a)
+        crp.append(len(cci))
+    crp, cci, cv = np.array(crp, np.int32), np.array(cci, np.int32), np.array(cv)
+    cb = np.ones(n)
+    out.update(cd_rowPtr=crp, cd_colIdx=cci, cd_values=cv)
+    for kind, ktag in ((0, "gmres"), (1, "bicgstab")):
+        for pc, tag in ((2, "ssor"), (3, "amg")):
+            x, it, last, _ = R.krylov(kind, crp, cci, cv, cb, pc, 1e-8, 500, 30)
+            key = f"cd_{ktag}_{tag}"
+            out[key + "_x"], out[key + "_iters"], out[key + "_last"] = x, np.array(it), np.array(last)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
 def main():
     mesh_case("box_6x5x4_distorted.npz", (6, 5, 4), 1, 0.2, False, [(z, 1) for z in range(1, 7)], [])
     mesh_case("box_8x8x8_rcm_walls.npz", (8, 8, 8), 7, 0.2, True, [(z, 1) for z in range(1, 7)], [])
@@ -311,6 +352,7 @@ def main():
     simp_case("simp_7x6x5_rcm.npz")
     for name in PISO_PIMPLE_RUNS:
         piso_pimple_case(name)
+    solvers_case("solvers_7x6x5_rcm.npz")
     print("fixtures written to", HERE)
 
 

@@ -84,3 +84,33 @@ def test_cg_ssor_matches_oracle(sg, ctx, oracle, dims):
     assert abs(it - oit) <= 1, (it, oit)
     assert st.converged and st.true_residual < 1e-8
     assert rel(x, ox) <= 1e-10
+
+
+@pytest.mark.parametrize("pc", [1, 2, 3])
+def test_zero_diagonals_and_tiny_systems(sg, ctx, oracle, pc):
+    """Rows whose diagonal entry is an explicit 0 (SSOR: invD = 1 and
+    a_ii y_i = 0; ILU(0): the sweep keeps the sum; AMG: Gauss-Seidel keeps
+    the old value), and systems of 1 and 2 rows: the device apply is the
+    oracle's bit for bit."""
+    rp, ci, va = tridiag(40, -1.0, 2.5, -1.2)
+    va = va.copy()
+    for i in (0, 7, 23):
+        va[rp[i] + (0 if i == 0 else 1)] = 0.0  # the diagonal of rows 0, 7, 23
+    cases = [(rp, ci, va), (np.array([0, 1], np.int32), np.array([0], np.int32), np.array([3.0])),
+             (np.array([0, 2, 4], np.int32), np.array([0, 1, 0, 1], np.int32), np.array([2.0, -1.0, -0.5, 4.0]))]
+    for rp_, ci_, va_ in cases:
+        n = len(rp_) - 1
+        r = np.linspace(-1.0, 1.5, n)
+        s = _solver(sg, ctx, pc)
+        s.set_matrix(rp_, ci_, va_)
+        z = np.empty(n)
+        s.precond_apply(r, z)
+        s.close()
+        if pc == 3:
+            oz = oracle.amg_apply(rp_, ci_, va_, r)[0]
+        elif pc == 1:
+            lu, dp = oracle.ilu0_setup(rp_, ci_, va_)
+            oz = oracle.ilu0_apply(rp_, ci_, lu, dp, r)
+        else:
+            oz = oracle.ssor_apply(rp_, ci_, va_, r)
+        assert bits_equal(z, oz), (pc, n)

@@ -364,3 +364,31 @@ def test_piso_pimple_fixture(oracle, name):
         outer.append(s.last_outer if variant == 2 else 0)
     assert bits_equal(np.array(res), g["res"]) and outer == [int(v) for v in g["last_outer"]]
     assert bits_equal(s.U, g["U"]) and bits_equal(s.p, g["p"]) and bits_equal(s.phi, g["phi"])
+
+
+def test_solvers_fixture(oracle):
+    """SSOR and AMG (apply and CG), TFQMR, GMRES and BiCGSTAB with SSOR and
+    AMG: the oracle reproduces the reference's recorded results bit for bit
+    (tests/golden/solvers_7x6x5_rcm.npz)."""
+    g = load("solvers_7x6x5_rcm.npz")
+    rp, ci, v, rhs = g["rowPtr"], g["colIdx"], g["values"], g["rhs"]
+    r = g["apply_r"]
+    assert bits_equal(oracle.ssor_apply(rp, ci, v, r), g["apply_ssor_z"])
+    assert bits_equal(oracle.amg_apply(rp, ci, v, r)[0], g["apply_amg_z"])
+    for pc, tag in ((2, "ssor"), (3, "amg")):
+        x, it, last = oracle.cg(rp, ci, v, rhs, pc, 1e-10, 500)
+        assert it == int(g[f"cg_{tag}_iters"]) and last == float(g[f"cg_{tag}_last"])
+        assert bits_equal(x, g[f"cg_{tag}_x"])
+    for pc, tag in ((1, "ilu0"), (2, "ssor")):
+        x, it, last = oracle.tfqmr(rp, ci, v, rhs, pc, 1e-8, 300)
+        assert it == int(g[f"tfqmr_{tag}_iters"]) and last == float(g[f"tfqmr_{tag}_last"])
+        assert bits_equal(x, g[f"tfqmr_{tag}_x"])
+    crp, cci, cv = g["cd_rowPtr"], g["cd_colIdx"], g["cd_values"]
+    cb = np.ones(len(crp) - 1)
+    for kind, ktag in ((0, "gmres"), (1, "bicgstab")):
+        for pc, tag in ((2, "ssor"), (3, "amg")):
+            x, it, last = (oracle.gmres(crp, cci, cv, cb, pc, 1e-8, 500, 30) if kind == 0
+                           else oracle.bicgstab(crp, cci, cv, cb, pc, 1e-8, 500))
+            key = f"cd_{ktag}_{tag}"
+            assert it == int(g[key + "_iters"]) and last == float(g[key + "_last"])
+            assert bits_equal(x, g[key + "_x"])
