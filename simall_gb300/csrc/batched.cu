@@ -129,6 +129,12 @@ __device__ __forceinline__ double cta_allreduce_f(float a, double *red)
     return t;
 }
 
+// Rows a thread handles per pass of a loop: it keeps its rows t, t + B,
+// t + 2B, ... in the same order, four at a time with all their loads issued
+// before the arithmetic, so a CTA alone keeps enough memory requests in
+// flight to stream a large system (one CTA per system).
+constexpr int kRowsPerPass = 8;
+
 // q = (S A S) p on rows [0, n) of one system in the row-sum form
 // q_i = e_i p_i - sum_j N_ij (p_i - p_j) (N: off-diagonal part of S A S, e_i
 // its row sum plus one, summed in FP64); returns this thread's p.q part.
@@ -138,28 +144,43 @@ __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__re
                                             const float *p, float *q)
 {
     float acc = 0.0f;
-    const int n = S.n;
+    const int n = S.n, B = blockDim.x;
     if (S.nd > 0) {
         const float *Us = U + S.u0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            const float pi = p[i];
-            float y = e[i] * pi;
+        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * B) {
+            float pi[kRowsPerPass], y[kRowsPerPass];
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * B;
+                pi[u] = i < n ? p[i] : 0.0f;
+                y[u] = i < n ? e[i] * pi[u] : 0.0f;
+            }
             for (int d = 0; d < S.nd; ++d) {
                 const int off = S.off[d];
                 const float *Ud = Us + static_cast<int64_t>(d) * n;
-                if (i + off < n)
-                    y = __fmaf_rn(-Ud[i], pi - p[i + off], y);
-                if (i - off >= 0)
-                    y = __fmaf_rn(-Ud[i - off], pi - p[i - off], y);
+#pragma unroll
+                for (int u = 0; u < kRowsPerPass; ++u) {
+                    const int i = i0 + u * B;
+                    if (i < n && i + off < n)
+                        y[u] = __fmaf_rn(-Ud[i], pi[u] - p[i + off], y[u]);
+                    if (i < n && i - off >= 0)
+                        y[u] = __fmaf_rn(-Ud[i - off], pi[u] - p[i - off], y[u]);
+                }
             }
-            q[i] = y;
-            acc += pi * y;
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * B;
+                if (i < n) {
+                    q[i] = y[u];
+                    acc += pi[u] * y[u];
+                }
+            }
         }
     } else {
         const int32_t *rp = orow + S.orp0;
         const int32_t *ci = ocol + S.u0;
         const float *va = oval + S.u0;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
+        for (int i = threadIdx.x; i < n; i += B) {
             const float pi = p[i];
             float y = e[i] * pi;
             for (int k = rp[i]; k < rp[i + 1]; ++k)
@@ -216,11 +237,26 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
         const float alpha = breakdown ? 0.0f : static_cast<float>(rho / pq);
         // xh += alpha p, rh -= alpha q (own rows: no barrier needed before)
         float rr_t = 0.0f;
-        for (int i = threadIdx.x; i < n; i += blockDim.x) {
-            xh[i] += alpha * ph[i];
-            const float r = rh[i] - alpha * qh[i];
-            rh[i] = r;
-            rr_t += r * r;
+        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * blockDim.x) {
+            float xv[kRowsPerPass], pv[kRowsPerPass], rv[kRowsPerPass], qv[kRowsPerPass];
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * blockDim.x;
+                xv[u] = i < n ? xh[i] : 0.0f;
+                pv[u] = i < n ? ph[i] : 0.0f;
+                rv[u] = i < n ? rh[i] : 0.0f;
+                qv[u] = i < n ? qh[i] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * blockDim.x;
+                if (i < n) {
+                    xh[i] = xv[u] + alpha * pv[u];
+                    const float r = rv[u] - alpha * qv[u];
+                    rh[i] = r;
+                    rr_t += r * r;
+                }
+            }
         }
         const double rr = cta_allreduce_f(rr_t, red);
         ++it;
@@ -269,8 +305,21 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
             last = est;
         }
         const float bf = static_cast<float>(beta);
-        for (int i = threadIdx.x; i < n; i += blockDim.x)
-            ph[i] = rh[i] + bf * ph[i];
+        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * blockDim.x) {
+            float rv[kRowsPerPass], pv[kRowsPerPass];
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * blockDim.x;
+                rv[u] = i < n ? rh[i] : 0.0f;
+                pv[u] = i < n ? ph[i] : 0.0f;
+            }
+#pragma unroll
+            for (int u = 0; u < kRowsPerPass; ++u) {
+                const int i = i0 + u * blockDim.x;
+                if (i < n)
+                    ph[i] = rv[u] + bf * pv[u];
+            }
+        }
         __syncthreads();
     }
     if (threadIdx.x == 0) {
