@@ -371,7 +371,8 @@ def run_adjoint(a, ctx, sg):
 def run_poisson3d(a, ctx, sg):
     """3-D pressure Poisson: N^3 box, interior nodes shifted by U(-0.2,0.2)h,
     RCM renumbering, aP = 1, interior face flux N(0,1), walls (cell-0 pin);
-    FP64 Jacobi-PCG against ILU0-PCG to 1e-8."""
+    FP64 Jacobi-PCG against ILU0-PCG to 1e-8, and the mixed-precision solve
+    (after RCM the matrix has no diagonal structure: FP32 CSR storage)."""
     import torch
     from simall_gb300 import workloads as W
 
@@ -384,9 +385,11 @@ def run_poisson3d(a, ctx, sg):
                        f"walls + cell-0 pin, FP64 PCG to {a.tol:g}", "nnz": int(ps.nnz)}
     stream = torch.cuda.ExternalStream(ctx.stream)
     x = torch.empty(m.n_cells, dtype=torch.float64, device="cuda")
-    for name, pc in (("jacobi", sg.PreconditionerKind.Jacobi), ("ilu0", sg.PreconditionerKind.ILU)):
+    for name, pc, prec in (("jacobi", sg.PreconditionerKind.Jacobi, sg.Precision.FP64),
+                           ("ilu0", sg.PreconditionerKind.ILU, sg.Precision.FP64),
+                           ("mixed_jacobi", sg.PreconditionerKind.Jacobi, sg.Precision.MIXED)):
         s = sg.GpuCGSolver(sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=pc, tolerance=a.tol,
-                                                 maxIterations=a.max_iterations), ctx=ctx)
+                                                 maxIterations=a.max_iterations), precision=prec, ctx=ctx)
         ps.solve(s, x)  # warm: setup, graph capture
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)

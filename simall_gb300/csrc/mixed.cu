@@ -562,10 +562,27 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t
         }
         v.pout[i] = pi;
         float y = __ldg(e + i) * pi;
-        for (int k = __ldg(orow + i); k < __ldg(orow + i + 1); ++k) {
-            const int j = __ldg(ocol + k);
-            const float pj = pdir<FRESH>(__ldg(rs + j), FRESH ? 0.0f : __ldg(qs + j), __ldg(ps + j), alpha, beta);
-            y = __fmaf_rn(-__ldg(oval + k), pi - pj, y);
+        // the row's entries eight at a time: indices and values, then the
+        // gathers, all issued before the arithmetic (column order kept)
+        const int k1 = __ldg(orow + i + 1);
+        for (int k0 = __ldg(orow + i); k0 < k1; k0 += 8) {
+            int c[8];
+            float a[8], gr[8], gq[8], gp[8];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                c[q] = k0 + q < k1 ? __ldg(ocol + k0 + q) : -1;
+                a[q] = k0 + q < k1 ? __ldg(oval + k0 + q) : 0.0f;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q) {
+                gr[q] = c[q] >= 0 ? __ldg(rs + c[q]) : 0.0f;
+                gq[q] = (!FRESH && c[q] >= 0) ? __ldg(qs + c[q]) : 0.0f;
+                gp[q] = c[q] >= 0 ? __ldg(ps + c[q]) : 0.0f;
+            }
+#pragma unroll
+            for (int q = 0; q < 8; ++q)
+                if (c[q] >= 0)
+                    y = __fmaf_rn(-a[q], pi - pdir<FRESH>(gr[q], gq[q], gp[q], alpha, beta), y);
         }
         v.qout[i] = y;
         acc[0] += pi * y;
