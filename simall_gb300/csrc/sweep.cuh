@@ -12,11 +12,14 @@ namespace {
 constexpr unsigned kSweepMaxSpins = 1u << 20;  // ~0.5 s of polling: far beyond any dependency chain
 
 // Values published as they land: before a sweep its output vector is
-// filled with kPending, a signalling NaN (no arithmetic produces one, and the
-// solver rejects non-finite input), each row publishes its value with one
-// relaxed store, and a reader polls the values it needs until none is pending.
-// One memory round trip less per dependency level than a separate "done" mark
-// followed by the value.
+// filled with kPending, a signalling NaN with a fixed payload, each row
+// publishes its value with one relaxed store, and a reader polls the values
+// it needs until none is pending.  One memory round trip less per dependency
+// level than a separate "done" mark followed by the value.  No arithmetic
+// produces a signalling NaN, and the solver rejects non-finite right-hand
+// sides and matrices; a row value that still equalled kPending (only by
+// copying that exact bit pattern in from an input) would make its readers
+// run out their bounded wait and report it, not hang.
 constexpr unsigned long long kPending = 0x7FF4C0DE5EED5A1EULL;
 
 __device__ __forceinline__ double ld_value(const double *p)
