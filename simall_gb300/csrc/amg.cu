@@ -7,7 +7,7 @@
 // Gauss-Seidel is sequential by definition: row i reads the new values of
 // the rows before it and the old values of the rows after it (forward; the
 // other way round backward).  Each sweep here writes a second buffer, so the
-// old values stay readable.  Levels of more than 24,576 rows take their rows
+// old values stay readable.  Levels of more than 4,096 rows take their rows
 // in dependency-level order from a ticket, each row polling (bounded) the new
 // values it reads until they land; smaller levels (the dense
 // coarse operators) run in one CTA, dependency level after dependency level,
@@ -115,7 +115,12 @@ __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__res
         atomicOr(ctl + 2, 1u);
 }
 
-constexpr int kSgsSmallRows = 24576;  // the sweep's new values in shared memory: 192 KB
+// Levels of up to this many rows sweep in one CTA (new values in 32 KB of
+// shared memory).  At 64^3 the V-cycle took 158 / 138 / 146 / 177 ms with the
+// bound at 24,576 / 4,096 / 2,048 / 512 rows: the free-running sweep is the
+// faster one on the sparse-ish upper levels, the one-CTA sweep on the dense
+// coarse ones.
+constexpr int kSgsSmallRows = 4096;
 constexpr int kSgsSmallThreads = 1024;
 
 // The same sweep in one CTA for levels of up to kSgsSmallRows rows: the
