@@ -186,6 +186,16 @@ int simall_solver_precond_apply(simall_solver *s, const double *r, double *z, in
  * number of levels and the rows of each (up to max_levels of them).  *nlev is
  * 0 for the other preconditioners. */
 int simall_solver_amg_levels(const simall_solver *s, int *nlev, int32_t *rows, int max_levels);
+/* Diagnostic, host only (no device is touched): the AMG hierarchy this
+ * library builds for A (host CSR arrays), with make_preconditioner's
+ * parameters: the number of levels, the rows of each (up to max_levels), and
+ * a 64-bit FNV-1a digest over the words of every level's operator, every
+ * prolongation and restriction (rowPtr, colIdx, value bits) and the coarsest
+ * level's dense LU.  It has no counterpart in the reference, whose
+ * AMGPreconditioner keeps its levels private; it lets a test compare the
+ * hierarchy with an independent restatement without a GPU. */
+int simall_amg_hierarchy_digest(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values,
+                                int *nlev, int32_t *rows, int max_levels, uint64_t *digest);
 /* Times `reps` back-to-back launches of one kernel of the solve on the
  * current matrix, bracketed by CUDA events on the context stream; *ms
  * receives the average duration of one launch and *bytes the algorithmic

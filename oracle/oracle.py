@@ -92,6 +92,8 @@ def lib():
         L.orc_gmres.restype = C.c_int
         L.orc_tfqmr.restype = C.c_int
         L.orc_tfqmr.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
+        L.orc_amg_digest.restype = C.c_uint64
+        L.orc_amg_digest.argtypes = [_I64, _P, _P, _P, _P]
         L.orc_amg_probe.restype = None
         L.orc_amg_probe.argtypes = [_I64, _P, _P, _P, _P, _P, _P, _P, _P, _P]
         L.orc_ssor_setup.restype = None
@@ -392,6 +394,16 @@ def amg_apply(rowPtr, colIdx, values, r=None):
     lib().orc_amg_probe(n, _ptr(rp), _ptr(ci), _ptr(v), _ptr(None if r is None else np.ascontiguousarray(r, np.float64)),
                         _ptr(z), C.byref(nlev), _ptr(sizes), _ptr(nnzs), C.byref(cn))
     return z, [(int(sizes[l]), int(nnzs[l])) for l in range(nlev.value)], int(cn.value)
+
+
+def amg_digest(rowPtr, colIdx, values):
+    """(levels, digest) of the restated AMG hierarchy (orc_amg_digest)."""
+    n = len(rowPtr) - 1
+    nlev = C.c_int(0)
+    d = lib().orc_amg_digest(n, _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+                             _ptr(np.ascontiguousarray(colIdx, np.int32)),
+                             _ptr(np.ascontiguousarray(values, np.float64)), C.byref(nlev))
+    return nlev.value, int(d)
 
 
 def ssor_apply(rowPtr, colIdx, values, r, omega=1.0):

@@ -1190,6 +1190,52 @@ void orc_amg_probe(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, cons
     orc_amg_free(&M);
 }
 
+/* The digest simall_amg_hierarchy_digest takes (FNV-1a over 64-bit words of
+ * every level's operator, every P and R, then the dense LU), of the hierarchy
+ * restated here.  Test infrastructure: it compares the library's host setup
+ * with this restatement. */
+static uint64_t fnv_word(uint64_t h, uint64_t w)
+{
+    h ^= w;
+    return h * 0x100000001b3ULL;
+}
+
+static uint64_t fnv_csr(uint64_t h, const OrcCsr *m)
+{
+    for (int32_t i = 0; i <= m->n; ++i)
+        h = fnv_word(h, (uint64_t)(uint32_t)m->rp[i]);
+    for (int32_t k = 0; k < m->rp[m->n]; ++k)
+        h = fnv_word(h, (uint64_t)(uint32_t)m->ci[k]);
+    for (int32_t k = 0; k < m->rp[m->n]; ++k) {
+        uint64_t w;
+        memcpy(&w, &m->v[k], sizeof w);
+        h = fnv_word(h, w);
+    }
+    return h;
+}
+
+uint64_t orc_amg_digest(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double *values, int *nlev)
+{
+    OrcAmg M;
+    orc_amg_setup(&M, n, rowPtr, colIdx, values);
+    uint64_t h = 0xcbf29ce484222325ULL;
+    for (int l = 0; l < M.nlev; ++l) {
+        h = fnv_csr(h, &M.A[l]);
+        if (l + 1 < M.nlev) {
+            h = fnv_csr(h, &M.P[l]);
+            h = fnv_csr(h, &M.R[l]);
+        }
+    }
+    for (size_t q = 0; q < (size_t)M.coarseN * (size_t)M.coarseN; ++q) {
+        uint64_t w;
+        memcpy(&w, &M.lu[q], sizeof w);
+        h = fnv_word(h, w);
+    }
+    *nlev = M.nlev;
+    orc_amg_free(&M);
+    return h;
+}
+
 /* ------------------------------------------------------------------ preconditioner objects */
 
 /* make_preconditioner (src/solver/LinearSolvers.cpp:240-254): 1 ILU(0),

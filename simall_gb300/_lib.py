@@ -123,6 +123,7 @@ SIGNATURES = {
     "simall_solver_spmv": (_I, [_P, _P, _P, _I]),
     "simall_solver_precond_apply": (_I, [_P, _P, _P, _I]),
     "simall_solver_amg_levels": (_I, [_P, _P, _P, _I]),
+    "simall_amg_hierarchy_digest": (_I, [_I64, _P, _P, _P, _P, _P, _I, _P]),
     "simall_solver_last_residual": (_D, [_P]),
     "simall_solver_time_kernel": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D)]),
     "simall_solver_solve_csr": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, C.POINTER(SolverStats)]),

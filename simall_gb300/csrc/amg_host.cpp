@@ -17,6 +17,7 @@
 // a_ii), each Galerkin row summed in the order its products are met with its
 // columns sorted afterwards, the dense LU with partial pivoting.
 #include "amg.hpp"
+#include "simall_gpu.h"
 
 #include <algorithm>
 #include <cmath>
@@ -286,3 +287,62 @@ void amg_build_hierarchy(int32_t n, const int32_t *rp, const int32_t *ci, const 
 }
 
 }  // namespace simall
+
+namespace {
+
+// FNV-1a over 64-bit words: the digest both this library and the oracle take
+// of a hierarchy.
+struct Digest {
+    uint64_t h = 0xcbf29ce484222325ULL;
+    void word(uint64_t w)
+    {
+        h ^= w;
+        h *= 0x100000001b3ULL;
+    }
+    void ints(const std::vector<int32_t> &a)
+    {
+        for (int32_t v : a)
+            word(static_cast<uint64_t>(static_cast<uint32_t>(v)));
+    }
+    void reals(const std::vector<double> &a)
+    {
+        for (double v : a) {
+            uint64_t w;
+            std::memcpy(&w, &v, sizeof w);
+            word(w);
+        }
+    }
+    void csr(const simall::AmgCsr &m)
+    {
+        ints(m.rp);
+        ints(m.ci);
+        reals(m.v);
+    }
+};
+
+}  // namespace
+
+extern "C" int simall_amg_hierarchy_digest(int64_t n, const int32_t *rowPtr, const int32_t *colIdx,
+                                           const double *values, int *nlev, int32_t *rows, int max_levels,
+                                           uint64_t *digest)
+{
+    if (n <= 0 || n > INT32_MAX - 1 || !rowPtr || !colIdx || !values || !nlev || !digest ||
+        (max_levels > 0 && !rows))
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    simall::AmgHierarchy h;
+    simall::amg_build_hierarchy(static_cast<int32_t>(n), rowPtr, colIdx, values, simall::AmgParams{}, h);
+    Digest d;
+    for (size_t l = 0; l < h.A.size(); ++l) {
+        d.csr(h.A[l]);
+        if (l < h.P.size()) {
+            d.csr(h.P[l]);
+            d.csr(h.R[l]);
+        }
+    }
+    d.reals(h.lu);
+    *nlev = static_cast<int>(h.A.size());
+    for (int l = 0; l < *nlev && l < max_levels; ++l)
+        rows[l] = h.A[l].n;
+    *digest = d.h;
+    return SIMALL_OK;
+}
