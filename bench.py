@@ -16,6 +16,14 @@ Workload (one step = one solve to 1e-8 relative residual):
 Every matrix and vector is far larger than the 129 MB L2, so no flush is
 needed between steps.
 
+Further legs in the same JSON line (each can be switched off): batched (512
+cavity systems in one launch), adjoint (128^3 face-conductance gradient),
+poisson3d (128^3 distorted RCM: FP64 Jacobi, ILU(0), mixed), preconditioners
+(64^3: every preconditioner and Krylov kind of make_linear_solver),
+pressure_step, cavity, simple (SIMPLE outer iterations on the device) and
+state (checkpoint, SIMP), each with the oracle's CPU time beside it where
+one is meaningful.
+
 `--impl reference` times the reference CG (CGSolver::solve,
 src/solver/LinearSolvers.cpp:420-451) on the host: the compiled reference
 when oracle/_ref exists, otherwise the oracle's C restatement of it, on a
