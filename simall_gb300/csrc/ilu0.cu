@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
 
 // ---------------------------------------------------------------- one CTA
 // For small systems the dependency chain, not the bandwidth, sets the time:
-// one kernel launch per level or a mark per row cost microseconds per level,
+// one kernel launch per level or a polled value per row cost microseconds per level,
 // while one CTA walking the levels with a block barrier between them pays a
 // barrier and an L2 round trip.  The sweep vector lives in shared memory (the
 // backward sweep overwrites y with z in place: row i reads y_i and the final
