@@ -333,3 +333,21 @@ def test_piso_pimple_time_steps(oracle, ref, case):
     assert list(want["last_outer"]) == last
     assert bits_equal(s.U, want["U"]) and bits_equal(s.p, want["p"]) and bits_equal(s.phi, want["phi"])
     ref.free_mesh(r)
+
+
+@pytest.mark.parametrize("kind", [0, 1, 3])
+def test_krylov_edge_cases(oracle, ref, kind):
+    """b = 0, maxIterations = 0 and maxIterations reached after one step:
+    the reference's return values and last residuals, for GMRES(m),
+    BiCGSTAB and TFQMR."""
+    from helpers import tridiag
+
+    rp, ci, va = tridiag(40, -6.0, 7.0, -1.0)
+    b = np.linspace(1.0, 2.0, 40)
+    for bb, mx in ((np.zeros(40), 100), (b, 0), (b, 1)):
+        x, it, last, _ = ref.krylov(kind, rp, ci, va, bb, 0, 1e-12, mx, 3)
+        ox, oit, olast = (oracle.gmres(rp, ci, va, bb, 0, 1e-12, mx, 3) if kind == 0
+                          else oracle.bicgstab(rp, ci, va, bb, 0, 1e-12, mx) if kind == 1
+                          else oracle.tfqmr(rp, ci, va, bb, 0, 1e-12, mx))
+        assert (it, last) == (oit, olast), (kind, mx)
+        assert bits_equal(x, ox)
