@@ -52,7 +52,7 @@ SEED = 42
 # FP64 Jacobi-PCG iteration count of the seeded system above, by side length
 # (the device FP64 solve reproduces CGSolver's count; recorded from this
 # benchmark's own FP64 leg).  The reference leg scales its bounded sample by it.
-FP64_ITERATIONS = {256: 1865}
+FP64_ITERATIONS = {64: 521, 256: 1865}
 # DRAM bytes (read + write) per row of one launch of the fused mixed step, from
 # one ncu capture at 200^3 (profiles/mixed_step_varcoef200.md: 255.99 MB read +
 # 99.92 MB written for 8,000,000 rows); scaled by the rows of the workload.
