@@ -12,14 +12,20 @@
 #   src/meshing/MeshOps.cpp, src/meshing/MeshQuality.cpp,
 #   src/adjoint/DiscreteAdjoint.cpp, src/core/PluginLoader.cpp,
 #   src/core/PluginRegistry.cpp, src/io/Checkpoint.cpp,
-#   src/optimization/SimpTopology.cpp
+#   src/optimization/SimpTopology.cpp, and the GPU facade's host path (no
+#   SIMALL_HAVE_CUDA): src/gpu/CgGpu.cpp, src/gpu/GpuKernels.cpp,
+#   src/gpu/CudaContext.cpp, src/gpu/DeviceMemoryPool.cpp
 #
 # Patch: LinearSolvers.cpp assigns util::aligned_vector<int> to std::vector<int>
 # at :85-86 and :170-171, which g++ 13 rejects.  A scratch copy written into
 # oracle/_ref/ replaces each of those four assignments with .assign(begin,end);
 # behaviour is unchanged.
 #
-# Usage: sh oracle/build_ref.sh [reference-root]   (default /root/reference)
+# Usage: sh oracle/build_ref.sh [reference-root]
+# The root is the argument, else $SIMALL_REFERENCE, else /root/reference.  Exit
+# status 2 when no reference tree is there (e.g. on the GPU host).  The root
+# compiled is recorded in oracle/_ref/REFERENCE_ROOT for the tests that compile
+# against the reference's headers.
 set -eu
 REF=${1:-${SIMALL_REFERENCE:-/root/reference}}
 HERE=$(cd "$(dirname "$0")" && pwd)
@@ -29,6 +35,7 @@ if [ ! -f "$REF/src/solver/LinearSolvers.cpp" ]; then
     exit 2
 fi
 mkdir -p "$OUT"
+printf '%s\n' "$REF" > "$OUT/REFERENCE_ROOT"
 sed -e 's/^        rowPtr_ = A\.rowPtr;$/        rowPtr_.assign(A.rowPtr.begin(), A.rowPtr.end());/' \
     -e 's/^        colIdx_ = A\.colIdx;$/        colIdx_.assign(A.colIdx.begin(), A.colIdx.end());/' \
     "$REF/src/solver/LinearSolvers.cpp" > "$OUT/LinearSolvers_patched.cpp"
@@ -51,6 +58,10 @@ $REF/src/core/PluginLoader.cpp
 $REF/src/core/PluginRegistry.cpp
 $REF/src/io/Checkpoint.cpp
 $REF/src/optimization/SimpTopology.cpp
+$REF/src/gpu/CgGpu.cpp
+$REF/src/gpu/GpuKernels.cpp
+$REF/src/gpu/CudaContext.cpp
+$REF/src/gpu/DeviceMemoryPool.cpp
 $HERE/ref_driver.cpp"
 pids=""
 objs=""

@@ -9,8 +9,18 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REFERENCE_SRC = "/root/reference/src"
 ADAPTER_TEST = os.path.join(ROOT, "tests", "cpp", "adapter_main.cpp")
+
+
+def _reference_src():
+    """src/ of the reference tree oracle/build_ref.sh compiled (recorded in
+    oracle/_ref/REFERENCE_ROOT), or SIMALL_REFERENCE's; None where neither."""
+    root = os.environ.get("SIMALL_REFERENCE")
+    rec = os.path.join(ROOT, "oracle", "_ref", "REFERENCE_ROOT")
+    if not root and os.path.exists(rec):
+        with open(rec) as f:
+            root = f.read().strip()
+    return os.path.join(root, "src") if root and os.path.isdir(os.path.join(root, "src")) else None
 
 
 def test_reference_plugin_loader_accepts_library(sg, ref):
@@ -21,10 +31,11 @@ def test_reference_plugin_loader_accepts_library(sg, ref):
 
 
 def test_adapter_compiles_against_reference_headers():
-    if not os.path.isdir(REFERENCE_SRC):
+    src = _reference_src()
+    if src is None:
         pytest.skip("SimAll source tree not present")
-    subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Werror", f"-I{REFERENCE_SRC}",
-                    f"-I{os.path.dirname(REFERENCE_SRC)}", f"-I{ROOT}/include", ADAPTER_TEST], check=True)
+    subprocess.run(["g++", "-std=c++20", "-fsyntax-only", "-Wall", "-Werror", f"-I{src}",
+                    f"-I{os.path.dirname(src)}", f"-I{ROOT}/include", ADAPTER_TEST], check=True)
 
 
 @pytest.mark.gpu
