@@ -1,7 +1,11 @@
 """Seeded synthetic inputs with the shapes of the pressure-path workloads.
 
-All randomness comes from numpy's PCG64 (`np.random.default_rng(seed)`), so
-the same seed gives the same inputs on every host.  These produce input data
+All randomness comes from numpy's PCG64 (`np.random.default_rng(seed)`), and
+every value derived from it uses correctly rounded IEEE operations only
+(`portable_exp` instead of np.exp, whose last bits differ between x86_64 and
+aarch64 builds of numpy), so the same seed gives the same inputs bit for bit
+on every host -- the reference's fixtures are made on one machine and checked
+on another.  These produce input data
 only (node shifts, aP, face fluxes, right-hand sides, conductances); the
 computation under test stays in the library.
 
@@ -25,6 +29,30 @@ import numpy as np
 from .mesh import BCType, MeshSoA, cartesian, rcm
 
 DEFAULT_SEED = 42
+
+# Cody-Waite split of ln 2: LN2_HI has 32 significant bits, so k * LN2_HI is
+# exact for |k| < 2^20; INV_LN2 = 1/ln 2 rounded.
+_LN2_HI = float.fromhex("0x1.62e42feep-1")
+_LN2_LO = float.fromhex("0x1.a39ef35793c76p-33")
+_INV_LN2 = float.fromhex("0x1.71547652b82fep+0")
+# 1/n! for n = 2..13 (Taylor series of e^r - 1 - r on |r| <= ln2/2; the first
+# neglected term is below 4e-18)
+_INV_FACT = [1.0 / float(np.prod(np.arange(1, n + 1, dtype=np.float64))) for n in range(2, 14)]
+
+
+def portable_exp(x) -> np.ndarray:
+    """e^x from +, -, *, rint and ldexp alone: x = k ln2 + r with |r| <=
+    ln2/2 (Cody-Waite), e^r by its Taylor polynomial in Horner form, scaled
+    by 2^k.  Within a few ulp of e^x for |x| < 700, and bit-identical on every
+    IEEE host (numpy evaluates each operation separately, correctly rounded)."""
+    x = np.asarray(x, np.float64)
+    k = np.rint(x * _INV_LN2)
+    r = (x - k * _LN2_HI) - k * _LN2_LO
+    q = np.full_like(r, _INV_FACT[-1])
+    for c in reversed(_INV_FACT[:-1]):
+        q = q * r + c
+    e = 1.0 + (r + r * (r * q))
+    return np.ldexp(e, k.astype(np.int64))
 ALL_WALLS = [(z, int(BCType.NoSlipWall)) for z in (1, 2, 3, 4, 5, 6)]
 X0_OUTLET = [(1, int(BCType.PressureOutlet))] + [(z, int(BCType.NoSlipWall)) for z in (2, 3, 4, 5, 6)]
 CAVITY = [(z, int(BCType.NoSlipWall)) for z in (1, 2, 3, 5, 6)] + [(4, int(BCType.MovingWall))]
@@ -69,7 +97,7 @@ def varcoef_mesh(n=256) -> MeshSoA:
 def varcoef_inputs(m: MeshSoA, seed=DEFAULT_SEED):
     """aP = 1/k with k = exp(N(0,1)) per cell; phi = 0; rhs N(0,1)."""
     rng = np.random.default_rng(seed + 2)
-    k = np.exp(rng.standard_normal(m.n_cells))
+    k = portable_exp(rng.standard_normal(m.n_cells))
     rhs = rng.standard_normal(m.n_cells)
     return 1.0 / k, np.zeros(m.n_faces), rhs
 
@@ -90,7 +118,7 @@ def facek_inputs(m: MeshSoA, seed=DEFAULT_SEED, sigma=0.5):
     """k_f = exp(N(0, sigma)) on interior and x=0 faces; pb ~ N(0,1) on x=0
     faces; cell source N(0,1)."""
     rng = np.random.default_rng(seed + 4)
-    k = np.exp(sigma * rng.standard_normal(m.n_faces))
+    k = portable_exp(sigma * rng.standard_normal(m.n_faces))
     pb = rng.standard_normal(m.n_faces)
     dirichlet = (~m.interior()) & (m.boundary_zone == 1)
     k[(~m.interior()) & ~dirichlet] = 0.0

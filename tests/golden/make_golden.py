@@ -11,10 +11,13 @@ preconditioners' apply, the SIMPLE cavity loop, SimpleAlgorithm::iterate /
 advance_time_step runs, PisoAlgorithm / PimpleAlgorithm time steps,
 io::Checkpoint::write, SimpTopology steps,
 solve_discrete_adjoint);
-inputs are seeded synthetic data.  The fixtures are small (about 1.5 MB in
+inputs are seeded synthetic data.  The fixtures are small (about 2 MB in
 all) so that the tests that read them run everywhere, the GPU host included.
 
-Usage:  python tests/golden/make_golden.py
+Usage:  python tests/golden/make_golden.py            (the small fixtures)
+        python tests/golden/make_golden.py NAME.npz   (a benchmark-size one:
+        poisson3d_128_cg, varcoef_256_cg, batched_512_cg, adjoint_face_k_24;
+        minutes of the reference's serial solvers each)
 """
 from __future__ import annotations
 
@@ -334,7 +337,181 @@ def solvers_case(name):
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
+def cggpu_case(name):
+    """gpu::CgGpu::set_matrix + solve (src/gpu/CgGpu.cpp:35-238, the GPU
+    facade's host path) on the cases of tests/helpers.py:cggpu_cases: cold and
+    warm starts, every preconditioner, relativeOrders, b = 0, maxIterations 0
+    and 5, the ILU0 -> Jacobi fall-back and the p.q breakdown.  Stores each
+    case's x and stats."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from helpers import cggpu_cases
+
+    out = {}
+    for cname, rp, ci, v, b, x0, pc, tol, mi, ro in cggpu_cases(O):
+        x, st = R.cggpu(rp, ci, v, b, x0, pc, tol, mi, ro)
+        out[cname + "_x"] = x
+        out[cname + "_stats"] = np.array([st["iterations"], st["final_residual"], st["initial_residual"],
+                                          float(st["converged"]), st["precond_after"], st["last_residual"]])
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+# ---------------------------------------------------------------- benchmark sizes
+# The workloads the benchmark times, solved by the reference itself.  Inputs are
+# regenerated from their seeds by the tests (simall_gb300.workloads), so only
+# digests of the assembled systems and summaries of the solutions are stored:
+# the iteration count, last_residual, ||x||_2, sum(x), x.w for a seeded
+# w ~ N(0,1) and every `stride`-th entry of x.
+
+def _digest(a):
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def _x_summary(x, stride, seed):
+    w = np.random.default_rng(seed).standard_normal(len(x))
+    return {"x_norm": np.array(np.linalg.norm(x)), "x_sum": np.array(x.sum()), "x_dot_w": np.array(x @ w),
+            "x_sample": np.ascontiguousarray(x[::stride]), "x_stride": np.array(stride), "w_seed": np.array(seed)}
+
+
+def poisson3d_full_case(name, n=128, seed=W.DEFAULT_SEED, tol=1e-8, max_it=50000):
+    """The 3-D pressure Poisson of the benchmark: n^3 box, interior nodes shifted
+    by U(-0.2,0.2)h, RCM (the reference's renumber_cells_cuthill_mckee), aP = 1,
+    interior face fluxes N(0,1), all walls (cell-0 pin); CGSolver::solve with
+    Jacobi and with ILU0 to 1e-8."""
+    import time
+
+    shift = W.interior_node_shift(n, n, n, seed=seed)
+    m = R.cartesian_mesh(n, n, n, node_shift=shift, do_rcm=True)
+    rng = np.random.default_rng(seed + 1)  # workloads.poisson3d_inputs
+    phi = rng.standard_normal(m["nF"])
+    phi[m["neighbor"] < 0] = 0.0
+    rp, ci, v, rhs = R.assemble(m, W.ALL_WALLS, 1.0, np.ones(m["nC"]), phi)
+    R.free_mesh(m)
+    out = {"n": np.array(n), "seed": np.array(seed), "tol": np.array(tol), "nnz": np.array(len(ci)),
+           "pattern_sha256": np.array(_digest(rp) + _digest(ci)), "values_sha256": np.array(_digest(v)),
+           "rhs_sha256": np.array(_digest(rhs)), "rcm_stats": np.array(m["rcm_stats"])}
+    for pc, tag in ((0, "jacobi"), (1, "ilu0")):
+        t = time.perf_counter()
+        x, it, last, _ = R.cg(rp, ci, v, rhs, pc, tol, max_it)
+        out[f"{tag}_seconds"] = np.array(time.perf_counter() - t)
+        out[f"{tag}_iters"] = np.array(it)
+        out[f"{tag}_last"] = np.array(last)
+        out.update({f"{tag}_{k}": a for k, a in _x_summary(x, 256, seed + 11).items()})
+        print(f"{name}: {tag} {it} iterations, last {last:.3e}, {out[f'{tag}_seconds']:.1f} s", flush=True)
+    np.savez_compressed(os.path.join(HERE, name), **out)
+
+
+def varcoef_full_case(name, n=256, seed=W.DEFAULT_SEED, tol=1e-8, max_it=50000):
+    """The mixed-versus-FP64 workload: n^3 box, aP = 1/k with k = exp(N(0,1))
+    per cell (harmonic faces), PressureOutlet on x = 0, walls elsewhere, rhs
+    N(0,1); CGSolver::solve with Jacobi to 1e-8 (the FP64 solve the mixed
+    precision error is reported against)."""
+    import time
+
+    m = R.cartesian_mesh(n, n, n)
+    rng = np.random.default_rng(seed + 2)  # workloads.varcoef_inputs
+    k = W.portable_exp(rng.standard_normal(m["nC"]))
+    b = rng.standard_normal(m["nC"])
+    rp, ci, v, rhs = R.assemble(m, W.X0_OUTLET, 1.0, 1.0 / k, np.zeros(m["nF"]))
+    R.free_mesh(m)
+    del m, rhs
+    t = time.perf_counter()
+    x, it, last, _ = R.cg(rp, ci, v, b, 0, tol, max_it)
+    secs = time.perf_counter() - t
+    print(f"{name}: {it} iterations, last {last:.3e}, {secs:.1f} s", flush=True)
+    np.savez_compressed(os.path.join(HERE, name), n=np.array(n), seed=np.array(seed), tol=np.array(tol),
+                        nnz=np.array(len(ci)), pattern_sha256=np.array(_digest(rp) + _digest(ci)),
+                        values_sha256=np.array(_digest(v)), b_sha256=np.array(_digest(b)), jacobi_iters=np.array(it),
+                        jacobi_last=np.array(last), jacobi_seconds=np.array(secs),
+                        **{f"jacobi_{k}": a for k, a in _x_summary(x, 2048, seed + 12).items()})
+
+
+def _batched_one(args):
+    side, b, tol, max_it = args
+    R1 = O.RefLib()
+    m = R1.cartesian_mesh(side, side, 1, 1.0, 1.0, 1.0 / side)
+    rp, ci, v, _ = R1.assemble(m, W.ALL_WALLS, 1.0, np.ones(m["nC"]), np.zeros(m["nF"]))
+    R1.free_mesh(m)
+    x, it, last, _ = R1.cg(rp, ci, v, b, 0, tol, max_it)
+    return _digest(v), it, last, x
+
+
+def batched_full_case(name, count=512, seed=W.DEFAULT_SEED, tol=1e-8, max_it=50000, samples=16):
+    """The batched workload: `count` cavity pressure systems with sides
+    log-uniform in [32, 256] (workloads.batched_cavity_systems: extent
+    1 x 1 x 1/side, all walls, aP = 1), rhs N(0,1) with the mean removed and the
+    pinned cell zeroed; each solved by its own CGSolver::solve with Jacobi to
+    1e-8.  Per system: the values digest, iterations, last_residual, ||x||,
+    x.w (w ~ N(0,1) from seed + 13 + system index) and `samples` entries at a
+    stride of n // samples."""
+    import multiprocessing as mp
+
+    sides = W.batched_sides(count, seed=seed)
+    rng = np.random.default_rng(seed + 5)
+    rhs = [W.batched_rhs(int(s) * int(s), rng) for s in sides]
+    with mp.get_context("spawn").Pool(os.cpu_count()) as pool:
+        res = pool.map(_batched_one, [(int(s), b, tol, max_it) for s, b in zip(sides, rhs)], chunksize=1)
+    xs = [r[3] for r in res]
+    dots = [float(x @ np.random.default_rng(seed + 13 + i).standard_normal(len(x))) for i, x in enumerate(xs)]
+    smp = np.stack([x[::len(x) // samples][:samples] for x in xs])
+    np.savez_compressed(os.path.join(HERE, name), count=np.array(count), seed=np.array(seed), tol=np.array(tol),
+                        sides=sides, values_sha256=np.array([r[0] for r in res]),
+                        iters=np.array([r[1] for r in res]), last=np.array([r[2] for r in res]),
+                        x_norm=np.array([np.linalg.norm(x) for x in xs]), x_dot_w=np.array(dots), x_sample=smp)
+    print(f"{name}: {count} systems, {sum(r[1] for r in res)} iterations in all", flush=True)
+
+
+def adjoint_full_case(name, n=24, seed=W.DEFAULT_SEED):
+    """solve_discrete_adjoint (GMRES(30) on A^T, left Jacobi) on the
+    differentiation workload's face-conductance Poisson at n^3 (undistorted
+    box, k_f = exp(N(0,0.5)) on interior and x = 0 faces, Dirichlet values
+    N(0,1) on x = 0, cell source N(0,1): workloads.facek_inputs), with
+    L = 0.5 |x - x_t|^2, x_t the solution for the conductances of seed + 1.
+    The assembly is the oracle's face-conductance restatement; the adjoint and
+    the gradient contraction are the reference's."""
+    m = O.cartesian_mesh(n, n, n)
+    rp, ci = O.build_sparsity(m)
+
+    def inputs(s):
+        rng = np.random.default_rng(s + 4)  # workloads.facek_inputs on this mesh
+        k = W.portable_exp(0.5 * rng.standard_normal(m.nF))
+        pb = rng.standard_normal(m.nF)
+        dirichlet = (m.neighbor < 0) & (m.zone == 1)
+        k[(m.neighbor < 0) & ~dirichlet] = 0.0
+        pb[~dirichlet] = 0.0
+        return k, pb, dirichlet.astype(np.uint8), rng.standard_normal(m.nC)
+
+    k, pb, dirichlet, src = inputs(seed)
+    kt = inputs(seed + 1)[0]
+    vt, rhst, _ = O.assemble_face_k(m, rp, ci, dirichlet, 1.0, kt, pb, src)
+    xt, _, _ = O.cg(rp, ci, vt, rhst, 0, 1e-14, 20000)
+    v, rhs, g = O.assemble_face_k(m, rp, ci, dirichlet, 1.0, k, pb, src)
+    x, _, _ = O.cg(rp, ci, v, rhs, 0, 1e-14, 20000)
+    psi, grad, its, res, rc = R.discrete_adjoint(rp, ci, v, x - xt, m.owner, m.neighbor, dirichlet, g, k, pb, x,
+                                                 tol=1e-12, max_iter=50000, restart=30)
+    print(f"{name}: GMRES {its} iterations, residual {res:.3e}, rc {rc}", flush=True)
+    np.savez_compressed(os.path.join(HERE, name), n=np.array(n), seed=np.array(seed),
+                        k_sha256=np.array(_digest(k)), pb_sha256=np.array(_digest(pb)),
+                        src_sha256=np.array(_digest(src)), values_sha256=np.array(_digest(v)),
+                        rhs_sha256=np.array(_digest(rhs)), xt=xt, psi=psi, grad=grad, iters=np.array(its),
+                        residual=np.array(res), ok=np.array(rc))
+
+
+FULL_SIZE = {
+    "cggpu_cases.npz": cggpu_case,
+    "poisson3d_128_cg.npz": poisson3d_full_case,
+    "varcoef_256_cg.npz": varcoef_full_case,
+    "batched_512_cg.npz": batched_full_case,
+    "adjoint_face_k_24.npz": adjoint_full_case,
+}
+
+
 def main():
+    if len(sys.argv) > 1:  # named fixtures only (the benchmark-size ones take minutes)
+        for name in sys.argv[1:]:
+            FULL_SIZE[name](name)
+        return
     mesh_case("box_6x5x4_distorted.npz", (6, 5, 4), 1, 0.2, False, [(z, 1) for z in range(1, 7)], [])
     mesh_case("box_8x8x8_rcm_walls.npz", (8, 8, 8), 7, 0.2, True, [(z, 1) for z in range(1, 7)], [])
     mesh_case("box_9x7x5_rcm_outlet.npz", (9, 7, 5), 3, 0.2, True,
@@ -353,6 +530,7 @@ def main():
     for name in PISO_PIMPLE_RUNS:
         piso_pimple_case(name)
     solvers_case("solvers_7x6x5_rcm.npz")
+    cggpu_case("cggpu_cases.npz")
     print("fixtures written to", HERE)
 
 

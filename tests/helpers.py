@@ -63,3 +63,60 @@ def tridiag(n, lo=-1.0, d=4.0, hi=-1.0):
             va.append(hi)
         rp.append(len(ci))
     return np.array(rp, np.int32), np.array(ci, np.int32), np.array(va, np.float64)
+
+
+def digest(a) -> str:
+    import hashlib
+
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def x_summary_error(x, fx, prefix):
+    """Largest relative deviation of x from a solution summary stored by
+    tests/golden/make_golden.py (_x_summary): the strided sample, ||x||_2 and
+    x.w for the seeded w ~ N(0,1).  For x.w the deviation is taken relative to
+    ||x||_2: (x - x_ref).w ~ N(0, ||x - x_ref||^2) for an independent w, so it
+    stays near ||x - x_ref|| / ||x|| (an eighth of the bound leaves 8 sigma)."""
+    stride = int(fx[prefix + "_x_stride"])
+    ref = fx[prefix + "_x_sample"]
+    e_sample = rel(x[::stride], ref)
+    xn = float(fx[prefix + "_x_norm"])
+    e_norm = abs(float(np.linalg.norm(x)) - xn) / xn
+    w = np.random.default_rng(int(fx[prefix + "_w_seed"])).standard_normal(len(x))
+    e_dot = abs(float(x @ w) - float(fx[prefix + "_x_dot_w"])) / xn / 8.0
+    return max(e_sample, e_norm, e_dot)
+
+
+def cggpu_cases(O):
+    """gpu::CgGpu cases shared by the oracle-vs-reference, golden and device
+    tests: (name, rowPtr, colIdx, values, b, x0, precond, tol, maxIt,
+    relativeOrders); precond 0 None, 1 Jacobi, 2 ILU0."""
+    m, rp, ci, v, b, _, _ = oracle_system(O, 8, seed=31)
+    n = len(b)
+    rng = np.random.default_rng(31)
+    x0 = rng.standard_normal(n)
+    xs, _, _ = O.cg(rp, ci, v, b, 0, 1e-15, 5000)
+    cases = [
+        ("jacobi_cold", rp, ci, v, b, np.zeros(n), 1, 1e-8, 1000, 0.0),
+        ("jacobi_warm", rp, ci, v, b, x0, 1, 1e-8, 1000, 0.0),
+        ("ilu0_warm", rp, ci, v, b, x0, 2, 1e-8, 1000, 0.0),
+        ("none_cold", rp, ci, v, b, np.zeros(n), 0, 1e-8, 1000, 0.0),
+        ("relative_orders", rp, ci, v, b, x0, 1, 1e-12, 1000, 3.0),
+        ("tolerance_first", rp, ci, v, b, np.zeros(n), 2, 1e-3, 1000, 9.0),
+        ("x0_exact", rp, ci, v, b, xs, 1, 1e-8, 1000, 0.0),
+        ("b_zero_x0_zero", rp, ci, v, np.zeros(n), np.zeros(n), 1, 1e-8, 1000, 0.0),
+        ("b_zero_x0_nonzero", rp, ci, v, np.zeros(n), x0, 2, 1e-8, 1000, 0.0),
+        ("max_iterations_5", rp, ci, v, b, x0, 1, 1e-8, 5, 0.0),
+        ("max_iterations_0", rp, ci, v, b, x0, 1, 1e-8, 0, 0.0),
+    ]
+    # ILU0 whose factor meets a zero pivot (a_00 = 0, eliminated against by
+    # row 1): CgGpu falls back to Jacobi, which divides row 0 by 1
+    trp, tci, tv = tridiag(40, -1.0, 4.0, -1.0)
+    tv = tv.copy()
+    tv[0] = 0.0
+    tb = np.random.default_rng(32).standard_normal(40)
+    cases.append(("ilu0_zero_pivot_fallback", trp, tci, tv, tb, np.zeros(40), 2, 1e-8, 1000, 0.0))
+    # p.q = 0 at the first iteration: an all-zero matrix (diagonal stored)
+    zrp, zci, zv = tridiag(16, 0.0, 0.0, 0.0)
+    cases.append(("breakdown", zrp, zci, zv, np.ones(16), np.zeros(16), 1, 1e-8, 100, 0.0))
+    return cases

@@ -7,7 +7,7 @@ import os
 import numpy as np
 import pytest
 
-from helpers import bits_equal
+from helpers import bits_equal, digest
 
 pytestmark = pytest.mark.gpu
 GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
@@ -69,6 +69,34 @@ def test_adjoint_matches_reference_discrete_adjoint_gradient(sg, ctx, oracle):
     assert np.max(np.abs(dk - ref_dk)) <= 1e-7 * scale
     assert np.max(np.abs(dpb[a["dirichlet"] == 1] - ref_dpb)) <= 1e-7 * np.abs(ref_dpb).max()
     assert np.linalg.norm(lam - a["psi"]) <= 1e-8 * np.linalg.norm(a["psi"])
+
+
+def test_adjoint_matches_reference_discrete_adjoint_gradient_24(sg, ctx):
+    """The differentiation workload's face-conductance system at 24^3 (13,824
+    cells, 43,200 faces; k_f = exp(N(0,0.5)), Dirichlet N(0,1) on x = 0, seed
+    42) against adjoint::solve_discrete_adjoint run by the reference (GMRES(30)
+    on A^T to 1e-12, tests/golden/adjoint_face_k_24.npz)."""
+    from simall_gb300 import workloads as W
+
+    a = np.load(os.path.join(GOLD, "adjoint_face_k_24.npz"))
+    n, seed = int(a["n"]), int(a["seed"])
+    m = sg.cartesian(n, n, n)
+    k, pb, dirichlet, src = W.facek_inputs(m, seed=seed)
+    assert (digest(k), digest(pb), digest(src)) == (str(a["k_sha256"]), str(a["pb_sha256"]), str(a["src_sha256"]))
+    ps = sg.PressureSystem(m, _bcs(sg), ctx=ctx)
+    ps.assemble_face_conductance(1.0, k, pb, src)
+    v, rhs = ps.download()
+    assert digest(v) == str(a["values_sha256"]) and digest(rhs) == str(a["rhs_sha256"])
+    s = sg.GpuCGSolver(_cfg(sg, 1e-14), ctx=ctx)
+    x = ps.solve(s)
+    lam, dk, dpb = ps.adjoint(s, 1.0, k, pb, x, x - a["xt"])
+    nF = m.n_faces
+    ref_dk, ref_dpb = a["grad"][:nF], a["grad"][nF:]
+    assert np.max(np.abs(dk - ref_dk)) <= 1e-7 * np.abs(ref_dk).max()
+    assert np.max(np.abs(dpb[dirichlet == 1] - ref_dpb)) <= 1e-7 * np.abs(ref_dpb).max()
+    assert np.linalg.norm(lam - a["psi"]) <= 1e-8 * np.linalg.norm(a["psi"])
+    s.close()
+    ps.close()
 
 
 def _loss(sg, ps, s, k, pb, src, xt):

@@ -1,9 +1,13 @@
 """Batched solves: every system of a batch reaches the FP64 true-residual
-tolerance and matches the oracle's FP64 CG solution of that system."""
+tolerance and matches the oracle's FP64 CG solution of that system; the
+benchmark's own batch of 512 cavity systems against the reference's FP64
+CGSolver::solve of each system (tests/golden/batched_512_cg.npz)."""
+import os
+
 import numpy as np
 import pytest
 
-from helpers import oracle_system
+from helpers import digest, oracle_system
 
 pytestmark = pytest.mark.gpu
 
@@ -87,3 +91,52 @@ def test_batched_rejects_bad_system(sg, ctx):
     with pytest.raises(sg.SimallError) as e:
         B.set_systems([(rp, ci, va)])
     assert e.value.status == 7
+
+
+def test_benchmark_batch_against_the_reference(sg, ctx):
+    """The 512 systems of the benchmark (sides log-uniform in [32, 256], seed
+    42): the device assembly gives each system's reference matrix (SHA-256);
+    the batched mixed solve brings every system's FP64 true residual, recomputed
+    on the host, below 1e-8 and lands within the accuracy that residual allows
+    of the reference's solution; the FP64 drop-in solves each system within one
+    iteration of the reference's count with x within 1e-10 of the reference's."""
+    import scipy.sparse as sps
+    from simall_gb300 import workloads as W
+
+    fx = np.load(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "batched_512_cg.npz"))
+    count, seed = int(fx["count"]), int(fx["seed"])
+    systems, rhs, sides = W.batched_cavity_systems(count=count, seed=seed, ctx=ctx)
+    assert np.array_equal(sides, fx["sides"])
+    assert [digest(v) for _, _, v in systems] == [str(d) for d in fx["values_sha256"]]
+    cfg = _cfg(sg, tol=float(fx["tol"]), maxit=50000)
+
+    def summary_err(k, xs):
+        n = len(xs)
+        w = np.random.default_rng(seed + 13 + k).standard_normal(n)
+        xn = float(fx["x_norm"][k])
+        smp = xs[::n // fx["x_sample"].shape[1]][:fx["x_sample"].shape[1]]
+        return max(abs(np.linalg.norm(xs) - xn) / xn, abs(float(xs @ w) - float(fx["x_dot_w"][k])) / xn / 8.0,
+                   np.linalg.norm(smp - fx["x_sample"][k]) / np.linalg.norm(fx["x_sample"][k]))
+
+    B = sg.BatchedSolver(cfg, ctx=ctx)
+    rows = B.set_systems(systems)
+    x, stats = B.solve(np.concatenate(rhs))
+    worst = 0.0
+    for k, ((rp, ci, va), b) in enumerate(zip(systems, rhs)):
+        xs = x[rows[k]:rows[k + 1]]
+        A = sps.csr_matrix((va, ci, rp))
+        assert np.linalg.norm(b - A @ xs) / np.linalg.norm(b) < 1e-8, k
+        worst = max(worst, summary_err(k, xs))
+    assert stats["converged"].all()
+    # the reference stops each system at a 1e-8 residual too; pinned Neumann
+    # systems with cond up to ~1e6 leave the two solutions up to ~1e-5 apart
+    assert worst < 1e-4, worst
+    B.close()
+    s = sg.GpuCGSolver(cfg, precision=sg.Precision.FP64, ctx=ctx)
+    for k, ((rp, ci, va), b) in enumerate(zip(systems, rhs)):
+        s.set_matrix(rp, ci, va)
+        xs = np.empty_like(b)
+        it = s.solve_into(b, xs)
+        assert abs(it - int(fx["iters"][k])) <= 1, (k, it, int(fx["iters"][k]))
+        assert summary_err(k, xs) <= 1e-10, k
+    s.close()

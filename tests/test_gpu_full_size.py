@@ -11,17 +11,26 @@ still applies and through properties that do not depend on size:
   the FP64 residual ||b - A x|| / ||b|| recomputed independently on the host
   from the downloaded x with the oracle's SpMV;
 * the FP64 Jacobi-PCG drop-in reaches the same tolerance, and the two
-  solutions agree to the accuracy a 1e-8 residual allows on this system.
+  solutions agree to the accuracy a 1e-8 residual allows on this system;
+* against the reference's own solve of this system (CGSolver::solve with
+  Jacobi to 1e-8, tests/golden/varcoef_256_cg.npz from
+  tests/golden/make_golden.py): the assembled matrix is the reference's (SHA-256),
+  the FP64 drop-in stops within one iteration of the reference's count with x
+  within 1e-10 of the reference's x, and the mixed-precision x is compared
+  with the reference's FP64 x.
 """
+import os
+
 import numpy as np
 import pytest
 
-from helpers import bits_equal
+from helpers import bits_equal, digest, rel, x_summary_error
 
 pytestmark = pytest.mark.gpu
 
 N = 256
 SEED = 42
+GOLD = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 @pytest.fixture(scope="module")
@@ -120,3 +129,18 @@ def test_full_size_mixed_and_fp64_solves(sg, ctx, system, oracle):
     # (cond(A) ~ 1e5), so they agree to a few 1e-7
     assert np.linalg.norm(mixed["x"] - fp64["x"]) / np.linalg.norm(fp64["x"]) < 2e-6
     assert abs(mixed["iterations"] - fp64["iterations"]) <= 0.1 * fp64["iterations"]
+
+
+def test_full_size_fp64_and_mixed_against_the_reference(sg, ctx, system):
+    fx = np.load(os.path.join(GOLD, "varcoef_256_cg.npz"))
+    assert digest(system["rp"]) + digest(system["ci"]) == str(fx["pattern_sha256"])
+    assert digest(system["vals"]) == str(fx["values_sha256"])
+    assert digest(system["b"]) == str(fx["b_sha256"])
+    fp64 = _solve(sg, ctx, system, sg.Precision.FP64)
+    fp64["solver"].close()
+    assert abs(fp64["iterations"] - int(fx["jacobi_iters"])) <= 1, (fp64["iterations"], int(fx["jacobi_iters"]))
+    assert x_summary_error(fp64["x"], fx, "jacobi") <= 1e-10
+    mixed = _solve(sg, ctx, system, sg.Precision.MIXED)
+    mixed["solver"].close()
+    # both stop at a 1e-8 residual; cond(A) ~ 1e5 leaves them a few 1e-7 apart
+    assert rel(mixed["x"][::int(fx["jacobi_x_stride"])], fx["jacobi_x_sample"]) < 2e-6

@@ -392,3 +392,91 @@ def test_solvers_fixture(oracle):
             key = f"cd_{ktag}_{tag}"
             assert it == int(g[key + "_iters"]) and last == float(g[key + "_last"])
             assert bits_equal(x, g[key + "_x"])
+
+
+# ---------------------------------------------------------------- benchmark sizes
+# Fixtures written by the reference at the benchmark's own sizes; the oracle is
+# checked on the parts that fit a CPU test (the GPU tests pin the device solves
+# against the same files).
+
+def test_poisson3d_128_assembly_is_the_references(oracle):
+    """128^3 distorted box, RCM, walls: the oracle's mesh, renumbering and
+    assembly give the reference's CSR and rhs bit for bit (SHA-256)."""
+    from helpers import digest
+    from simall_gb300 import workloads as W
+
+    fx = load("poisson3d_128_cg.npz")
+    n, seed = int(fx["n"]), int(fx["seed"])
+    m = oracle.cartesian_mesh(n, n, n, node_shift=W.interior_node_shift(n, n, n, seed=seed))
+    _, st = oracle.rcm(m)
+    assert st == tuple(int(v) for v in fx["rcm_stats"])
+    rp, ci = oracle.build_sparsity(m)
+    phi = np.random.default_rng(seed + 1).standard_normal(m.nF)  # workloads.poisson3d_inputs
+    phi[m.neighbor < 0] = 0.0
+    v, rhs, _ = oracle.assemble(m, rp, ci, [], 1.0, np.ones(m.nC), phi)
+    assert digest(rp) + digest(ci) == str(fx["pattern_sha256"])
+    assert digest(v) == str(fx["values_sha256"]) and digest(rhs) == str(fx["rhs_sha256"])
+
+
+def test_batched_512_smallest_systems(oracle):
+    """The eight smallest systems of the benchmark's batch: the oracle's
+    assembly has the reference's values and its CG the reference's iteration
+    count, last residual and solution summary, exactly."""
+    from helpers import digest
+    from simall_gb300 import workloads as W
+
+    fx = load("batched_512_cg.npz")
+    seed = int(fx["seed"])
+    sides = W.batched_sides(int(fx["count"]), seed=seed)
+    assert np.array_equal(sides, fx["sides"])
+    rng = np.random.default_rng(seed + 5)
+    rhs = [W.batched_rhs(int(s) * int(s), rng) for s in sides]
+    for k in np.argsort(sides, kind="stable")[:8]:
+        s = int(sides[k])
+        m = oracle.cartesian_mesh(s, s, 1, 1.0, 1.0, 1.0 / s)
+        rp, ci = oracle.build_sparsity(m)
+        v, _, _ = oracle.assemble(m, rp, ci, [], 1.0, np.ones(m.nC), np.zeros(m.nF))
+        assert digest(v) == str(fx["values_sha256"][k])
+        x, it, last = oracle.cg(rp, ci, v, rhs[k], 0, float(fx["tol"]), 50000)
+        assert it == int(fx["iters"][k]) and last == float(fx["last"][k])
+        assert np.linalg.norm(x) == float(fx["x_norm"][k])
+        w = np.random.default_rng(seed + 13 + int(k)).standard_normal(len(x))
+        assert float(x @ w) == float(fx["x_dot_w"][k])
+
+
+def test_adjoint_24_inputs_and_assembly(oracle):
+    """The 24^3 adjoint fixture's inputs regenerate from their seed and the
+    oracle's face-conductance assembly of them is the one the reference's
+    adjoint ran on."""
+    from helpers import digest
+    from simall_gb300 import workloads as W
+
+    fx = load("adjoint_face_k_24.npz")
+    n, seed = int(fx["n"]), int(fx["seed"])
+    m = oracle.cartesian_mesh(n, n, n)
+    rng = np.random.default_rng(seed + 4)
+    k = W.portable_exp(0.5 * rng.standard_normal(m.nF))
+    pb = rng.standard_normal(m.nF)
+    dirichlet = (m.neighbor < 0) & (m.zone == 1)
+    k[(m.neighbor < 0) & ~dirichlet] = 0.0
+    pb[~dirichlet] = 0.0
+    src = rng.standard_normal(m.nC)
+    assert (digest(k), digest(pb), digest(src)) == (str(fx["k_sha256"]), str(fx["pb_sha256"]), str(fx["src_sha256"]))
+    rp, ci = oracle.build_sparsity(m)
+    v, rhs, _ = oracle.assemble_face_k(m, rp, ci, dirichlet.astype(np.uint8), 1.0, k, pb, src)
+    assert digest(v) == str(fx["values_sha256"]) and digest(rhs) == str(fx["rhs_sha256"])
+    assert int(fx["ok"]) == 0  # the reference GMRES reached its 1e-12 tolerance
+
+
+def test_cggpu_against_reference_fixture(oracle):
+    """The oracle's gpu::CgGpu restatement against the reference's own runs
+    (tests/golden/cggpu_cases.npz), bit for bit."""
+    from helpers import cggpu_cases
+
+    g = load("cggpu_cases.npz")
+    for name, rp, ci, v, b, x0, pc, tol, mi, ro in cggpu_cases(oracle):
+        x, st = oracle.cggpu(rp, ci, v, b, x0, pc, tol, mi, ro)
+        assert bits_equal(x, g[name + "_x"]), name
+        ref = g[name + "_stats"]
+        assert [st["iterations"], st["final_residual"], st["initial_residual"], float(st["converged"]),
+                st["precond_after"], st["last_residual"]] == list(ref), name
