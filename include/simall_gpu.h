@@ -121,7 +121,30 @@ typedef struct simall_solver_config {
     int engine;            /* simall_engine: how the iteration runs; default SIMALL_ENGINE_AUTO */
     int kind;              /* simall_solver_kind; default SIMALL_SOLVER_CG */
     int restart;           /* GMRES(m): basis size m (LinearSolverConfig::restart); default 30 */
+    int semantics;         /* simall_semantics; default SIMALL_SEMANTICS_CGSOLVER */
+    double relative_orders; /* SIMALL_SEMANTICS_CGGPU: also stop once ||r|| <= ||r_0|| 10^-relative_orders
+                               (GpuSolverConfig::relativeOrders, src/gpu/CgGpu.hpp:61-63); 0 = off */
 } simall_solver_config;
+
+/* Which reference solver's conventions a CG solve follows.
+ * SIMALL_SEMANTICS_CGSOLVER: solver::CGSolver::solve (src/solver/LinearSolvers.cpp:
+ *   420-451): x starts from 0; stop when ||r||/max(||b||,1e-30) < tolerance;
+ *   None preconditioner means Jacobi (make_preconditioner); pAp == 0 ends the
+ *   loop returning the iterations done.
+ * SIMALL_SEMANTICS_CGGPU: gpu::CgGpu::solve (src/gpu/CgGpu.cpp:118-238): x is the
+ *   initial guess (r = b - A x0) and the solution; stop when ||r||/bRef <=
+ *   tolerance (bRef = ||b||, or 1 when b = 0) or, with relative_orders > 0,
+ *   ||r|| <= ||r_0|| 10^-relative_orders, whichever comes first, also before the
+ *   first iteration (then iterations = 0); None means no preconditioner (z = r);
+ *   an ILU0 factor that meets a missing diagonal or a zero pivot
+ *   (gpu::ilu0_factor_inplace, src/gpu/GpuKernels.cpp:345-401) makes the solver
+ *   Jacobi from then on, as CgGpu::set_matrix does (CgGpu.cpp:64-82; reported in
+ *   simall_solver_stats.preconditioner); |p.q| < 1e-300 ends the loop with
+ *   iterations = 0, residual_norm = 0, converged = 0 and status
+ *   SIMALL_ERR_BREAKDOWN, the values CgGpu::solve leaves (CgGpu.cpp:190-194).
+ *   FP64 CG only, with Jacobi, ILU0 or None.  Jacobi applies r * (1/d) where
+ *   CgGpu divides r / d: the two differ by at most one rounding per entry. */
+enum simall_semantics { SIMALL_SEMANTICS_CGSOLVER = 0, SIMALL_SEMANTICS_CGGPU = 1 };
 
 /* LinearSolverKind ordinals (src/solver/Solver.hpp:67-73).  CG is the pressure
  * path (FP64 or mixed precision); GMRES(m), BiCGSTAB and TFQMR (FP64, Jacobi,
@@ -153,7 +176,10 @@ typedef struct simall_solver_stats {
     double seconds;          /* wall time of the solve call */
     int engine;              /* what ran the iteration: 0 kernels per step (device graph loop or host-polled
                                 chunks), 1 one thread-block cluster for the whole solve */
-    int reserved;
+    int preconditioner;      /* the preconditioner the solve used (CgGpu semantics: Jacobi after an ILU0
+                                fall-back) */
+    double residual_norm;    /* ||r||_2 of the iterated residual at exit (GpuSolverStats::finalResidual) */
+    double initial_residual; /* CgGpu semantics: ||b - A x0||_2 (GpuSolverStats::initialResidual); else ||b||_2 */
 } simall_solver_stats;
 
 typedef struct simall_solver simall_solver;
@@ -208,6 +234,10 @@ int simall_amg_hierarchy_digest(int64_t n, const int32_t *rowPtr, const int32_t 
 int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms, double *bytes);
 /* ILinearSolver::last_residual(). */
 double simall_solver_last_residual(const simall_solver *s);
+/* The preconditioner the solver holds now: the configured one, or Jacobi after
+ * a CgGpu-semantics ILU0 factor failed (GpuSolverConfig::preconditioner as
+ * CgGpu::config() reports it after set_matrix, src/gpu/CgGpu.cpp:64-82). */
+int simall_solver_preconditioner(const simall_solver *s, int *preconditioner);
 /* ILinearSolver::solve(A, b, x) in one call: set_matrix + solve on host arrays. */
 int simall_solver_solve_csr(simall_solver *s, int64_t n, int64_t nnz, const int32_t *rowPtr,
                             const int32_t *colIdx, const double *values, const double *b, double *x,
@@ -502,6 +532,12 @@ int simall_simp_destroy(simall_simp *s);
  * returned on its own (the expected result), *seconds = the wall time of the
  * call (the bound is about a second).  The context stays usable. */
 int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds);
+/* Latency measurements of the free-running triangular sweeps (ILU(0), SSOR,
+ * the AMG smoother's large levels; no reference counterpart): sets, for the
+ * whole process, the CTAs per SM of their grid (1..8; default 4) and the
+ * longest sleep between two polls of a value not yet published (0..4096 ns,
+ * 0 = spin; default 256).  Results do not depend on either. */
+int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns);
 /* The small-system ILU(0) path divides through a correctly rounded reciprocal
  * (one product and two FMAs, Markstein's correction).  For each i, q_recip[i]
  * is that quotient a[i] / b[i] and q_div[i] the device's correctly rounded
@@ -575,9 +611,11 @@ int simall_gpu_spmv_csr(size_t n, const int32_t *rowPtr, const int32_t *colIdx, 
  * inside this library (reserved on every GPU that loads the library, until the
  * process exits), which limits n to SIMALL_DOT_NOALLOC_MAX_N; larger n returns
  * SIMALL_ERR_SIZE_MISMATCH.  The first call on each device looks the array's
- * address up (cudaGetSymbolAddress); make it before any stream capture.  All
- * calls share the array, so calls that overlap on the GPU race.  Blocks the
- * host like simall_gpu_dot. */
+ * address up (cudaGetSymbolAddress); make it before any stream capture.  The
+ * address is cached for the life of the device's context: do not use this
+ * function on a device after calling cudaDeviceReset on it.  All calls share
+ * the array, so calls that overlap on the GPU race.  Blocks the host like
+ * simall_gpu_dot. */
 #define SIMALL_DOT_NOALLOC_MAX_N 16777216
 int simall_gpu_dot_noalloc(const double *x, const double *y, size_t n, void *stream, double *result);
 /* z[i] = r[i] / diag[i]  (GpuKernels.hpp:87) */

@@ -106,6 +106,10 @@ def lib():
             [_P] * 11
         L.orc_simp_step.restype = _D
         L.orc_simp_step.argtypes = [_I64, _I64] + [_P] * 17
+        L.orc_gpu_ilu0_factor.restype = C.c_int
+        L.orc_gpu_ilu0_factor.argtypes = [_I64, _P, _P, _P]
+        L.orc_cggpu_solve.restype = None
+        L.orc_cggpu_solve.argtypes = [C.c_int, _D, C.c_int, _D, _I64] + [_P] * 8
         _lib = L
     return _lib
 
@@ -564,6 +568,27 @@ def cg(rowPtr, colIdx, values, b, precond=0, tol=1e-8, max_it=1000, history=Fals
     return x, it, last.value
 
 
+def cggpu(rowPtr, colIdx, values, b, x0=None, precond=1, tol=1e-8, max_it=1000, relative_orders=0.0):
+    """gpu::CgGpu::set_matrix + solve (host path).  precond: 0 None, 1 Jacobi,
+    2 ILU0.  Returns (x, stats) with stats = dict(iterations, final_residual,
+    initial_residual, converged, precond_after, last_residual)."""
+    return _cggpu_call(lib().orc_cggpu_solve, rowPtr, colIdx, values, b, x0, precond, tol, max_it, relative_orders)
+
+
+def _cggpu_call(fn, rowPtr, colIdx, values, b, x0, precond, tol, max_it, relative_orders):
+    n = len(rowPtr) - 1
+    x = np.zeros(n) if x0 is None else np.array(x0, np.float64, copy=True)
+    out = np.zeros(4)
+    pa = C.c_int(-1)
+    last = C.c_double(0.0)
+    b = np.ascontiguousarray(b, np.float64)
+    fn(int(precond), float(tol), int(max_it), float(relative_orders), n, _ptr(np.ascontiguousarray(rowPtr, np.int32)),
+       _ptr(np.ascontiguousarray(colIdx, np.int32)), _ptr(np.ascontiguousarray(values, np.float64)), _ptr(b),
+       _ptr(x), _ptr(out), C.byref(pa), C.byref(last))
+    return x, {"iterations": int(out[0]), "final_residual": float(out[1]), "initial_residual": float(out[2]),
+               "converged": bool(out[3]), "precond_after": int(pa.value), "last_residual": float(last.value)}
+
+
 # ---------------------------------------------------------------- compiled reference
 
 
@@ -621,6 +646,8 @@ class RefLib:
         L.ref_piso_pimple_run.restype = C.c_int
         L.ref_piso_pimple_run.argtypes = [_P, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _D, _P, _D,
                                           C.c_int] + [_P] * 5
+        L.ref_cggpu_solve.restype = C.c_int
+        L.ref_cggpu_solve.argtypes = [C.c_int, _D, C.c_int, _D, C.c_int] + [_P] * 8
         L.ref_discrete_adjoint.restype = C.c_int
         L.ref_discrete_adjoint.argtypes = [C.c_int, _P, _P, _P, _P, _D, C.c_int, C.c_int, C.c_int] + [_P] * 11
         self.L = L
@@ -896,6 +923,11 @@ class RefLib:
         it = self.L.ref_cg(n, _ptr(rowPtr), _ptr(colIdx), _ptr(values), _ptr(b), int(precond), float(tol),
                            int(max_it), _ptr(x), C.byref(last), C.byref(secs))
         return x, it, last.value, secs.value
+
+    def cggpu(self, rowPtr, colIdx, values, b, x0=None, precond=1, tol=1e-8, max_it=1000, relative_orders=0.0):
+        """gpu::CgGpu (set_matrix + solve) of the reference, host path."""
+        return _cggpu_call(self.L.ref_cggpu_solve, rowPtr, colIdx, values, b, x0, precond, tol, max_it,
+                           relative_orders)
 
     def precond_apply(self, kind, rowPtr, colIdx, values, r):
         n = len(rowPtr) - 1

@@ -20,6 +20,7 @@
 #include "adjoint/DiscreteAdjoint.hpp"
 #include "core/PluginLoader.hpp"
 #include "core/PluginRegistry.hpp"
+#include "gpu/CgGpu.hpp"
 #include "io/Checkpoint.hpp"
 #include "optimization/SimpTopology.hpp"
 #include "meshing/CartesianMesher.hpp"
@@ -945,6 +946,42 @@ int ref_discrete_adjoint(int n, const int* rowPtr, const int* colIdx, const doub
     *itersOut = static_cast<std::int64_t>(r2.iterations);
     *resOut = r2.residual;
     return r2.ok ? 0 : 1;
+}
+
+// ------------------------------------------------------------------ gpu::CgGpu
+// gpu::CgGpu (src/gpu/CgGpu.hpp:49-124, CgGpu.cpp:35-238) on the facade's host
+// path: set_matrix (Jacobi diagonal; ILU0 factor with the fall-back to Jacobi
+// on a zero pivot), then solve with x as the initial guess.  precond: 0 None,
+// 1 Jacobi, 2 ILU0 (GpuPreconditioner order).  out[0..3]: iterations,
+// finalResidual, initialResidual, converged; *precondAfter: the preconditioner
+// the solver holds afterwards (ILU0 -> Jacobi on a failed factor).
+int ref_cggpu_solve(int precond, double tol, int maxIt, double relativeOrders, int n, const int* rowPtr,
+                    const int* colIdx, const double* values, const double* b, double* x, double* out,
+                    int* precondAfter, double* lastResidual)
+{
+    simall::gpu::GpuSolverConfig cfg;
+    cfg.preconditioner = static_cast<simall::gpu::GpuPreconditioner>(precond);
+    cfg.tolerance = tol;
+    cfg.maxIterations = maxIt;
+    cfg.relativeOrders = relativeOrders;
+    simall::gpu::CgGpu solver(cfg);
+    simall::gpu::HostCsrView A;
+    A.n = static_cast<std::size_t>(n);
+    A.nnz = static_cast<std::size_t>(rowPtr[n]);
+    A.rowPtr = rowPtr;
+    A.colIdx = colIdx;
+    A.values = values;
+    solver.set_matrix(A);
+    std::vector<double> bv(b, b + n), xv(x, x + n);
+    const auto st = solver.solve(bv, xv);
+    std::copy(xv.begin(), xv.end(), x);
+    out[0] = st.iterations;
+    out[1] = st.finalResidual;
+    out[2] = st.initialResidual;
+    out[3] = st.converged ? 1.0 : 0.0;
+    *precondAfter = static_cast<int>(solver.config().preconditioner);
+    *lastResidual = solver.last_residual();
+    return 0;
 }
 
 // ------------------------------------------------------------------ plugin ABI

@@ -1373,6 +1373,186 @@ int orc_cg(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, const double
     return ret;
 }
 
+/* ------------------------------------------------------------------ gpu::CgGpu */
+
+/* gpu::ilu0_factor_inplace (src/gpu/GpuKernels.cpp:345-401): IKJ ILU(0) in
+ * place; 0 when a row has no diagonal entry, a pivot U_kk is zero, or a row
+ * i >= 1 ends with a zero U_ii (values are then partly factored), else 1.  On
+ * success the factor equals ILU0Preconditioner::setup's (orc_ilu0_setup). */
+int orc_gpu_ilu0_factor(int64_t n, const int32_t *rowPtr, const int32_t *colIdx, double *values)
+{
+    int32_t *diagPos = (int32_t *)xmalloc((size_t)n * sizeof(int32_t) + 8);
+    int ok = 1;
+    for (int64_t i = 0; i < n && ok; ++i) {
+        diagPos[i] = -1;
+        for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+            if (colIdx[k] == i) {
+                diagPos[i] = k;
+                break;
+            }
+        if (diagPos[i] < 0)
+            ok = 0;
+    }
+    for (int64_t i = 1; i < n && ok; ++i) {
+        for (int32_t p = rowPtr[i]; p < rowPtr[i + 1] && ok; ++p) {
+            const int32_t k = colIdx[p];
+            if (k >= i)
+                break;
+            const double ukk = values[diagPos[k]];
+            if (ukk == 0.0) {
+                ok = 0;
+                break;
+            }
+            const double lik = values[p] / ukk;
+            values[p] = lik;
+            for (int32_t q = diagPos[k] + 1; q < rowPtr[k + 1]; ++q) {
+                const int32_t j = colIdx[q];
+                for (int32_t r = p + 1; r < rowPtr[i + 1]; ++r)
+                    if (colIdx[r] == j) {
+                        values[r] -= lik * values[q];
+                        break;
+                    }
+            }
+        }
+        if (ok && values[diagPos[i]] == 0.0)
+            ok = 0;
+    }
+    free(diagPos);
+    return ok;
+}
+
+/* gpu::CgGpu::set_matrix + solve (src/gpu/CgGpu.cpp:35-238) on the GPU
+ * facade's host path (src/gpu/GpuKernels.cpp: spmv_csr :196-283, dot :125-145,
+ * nrm2 :147-165, axpy/scal/xpby, jacobi_apply :286-334 z_i = r_i / d_i,
+ * ilu0_apply :403-481).  precond: 0 None (z = r), 1 Jacobi (d_i = the row's
+ * first diagonal entry, 1.0 when missing; divides by 1.0 where d_i = 0), 2
+ * ILU0 (falls back to Jacobi for good when the factor fails: *precondAfter).
+ * x is the initial guess and the solution.  out[0..3]: iterations,
+ * finalResidual ||r||_2 (absolute), initialResidual, converged.  Stop test
+ * ||r|| / bRef <= tol (bRef = ||b||, 1 when b = 0) or, with relativeOrders > 0,
+ * ||r|| <= ||r_0|| 10^-relativeOrders -- first trigger wins; |p.q| < 1e-300
+ * ends the loop leaving iterations and finalResidual at 0 (as the reference
+ * does).  *lastResidual: CgGpu::last_residual(). */
+void orc_cggpu_solve(int precond, double tol, int maxIt, double relativeOrders, int64_t n, const int32_t *rowPtr,
+                     const int32_t *colIdx, const double *values, const double *b, double *x, double *out,
+                     int *precondAfter, double *lastResidual)
+{
+    const int64_t nnz = rowPtr[n];
+    double *d = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *lu = NULL;
+    if (precond == 2) {
+        lu = (double *)xmalloc((size_t)nnz * sizeof(double) + 8);
+        memcpy(lu, values, (size_t)nnz * sizeof(double));
+        if (!orc_gpu_ilu0_factor(n, rowPtr, colIdx, lu)) {
+            precond = 1;
+            free(lu);
+            lu = NULL;
+        }
+    }
+    if (precond == 1)
+        for (int64_t i = 0; i < n; ++i) {
+            d[i] = 1.0;
+            for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k)
+                if (colIdx[k] == i) {
+                    d[i] = values[k];
+                    break;
+                }
+        }
+    *precondAfter = precond;
+    double *r = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *z = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *p = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    double *q = (double *)xmalloc((size_t)n * sizeof(double) + 8);
+    out[0] = 0.0;
+    out[1] = 0.0;
+    out[3] = 0.0;
+#define APPLY_M()                                                                                        \
+    do {                                                                                                 \
+        if (precond == 0) {                                                                              \
+            memcpy(z, r, (size_t)n * sizeof(double));                                                   \
+        } else if (precond == 1) {                                                                       \
+            for (int64_t i = 0; i < n; ++i)                                                              \
+                z[i] = r[i] / (d[i] != 0.0 ? d[i] : 1.0);                                                \
+        } else {                                                                                         \
+            for (int64_t i = 0; i < n; ++i) {                                                            \
+                double s = r[i];                                                                         \
+                for (int32_t k = rowPtr[i]; k < rowPtr[i + 1]; ++k) {                                    \
+                    if (colIdx[k] < i)                                                                   \
+                        s -= lu[k] * z[colIdx[k]];                                                       \
+                    else                                                                                 \
+                        break;                                                                           \
+                }                                                                                        \
+                z[i] = s;                                                                                \
+            }                                                                                            \
+            for (int64_t ii = n - 1; ii >= 0; --ii) {                                                    \
+                double s = z[ii], dg = 1.0;                                                              \
+                for (int32_t k = rowPtr[ii]; k < rowPtr[ii + 1]; ++k) {                                  \
+                    if (colIdx[k] > ii)                                                                  \
+                        s -= lu[k] * z[colIdx[k]];                                                       \
+                    else if (colIdx[k] == ii)                                                            \
+                        dg = lu[k];                                                                      \
+                }                                                                                        \
+                z[ii] = s / (dg != 0.0 ? dg : 1.0);                                                      \
+            }                                                                                            \
+        }                                                                                                \
+    } while (0)
+    /* r = b - A x0: spmv, scal(-1), axpy(1, b) */
+    orc_spmv(n, rowPtr, colIdx, values, x, r);
+    for (int64_t i = 0; i < n; ++i)
+        r[i] = -1.0 * r[i];
+    axpy(n, 1.0, b, r);
+    const double bNorm = norm2(n, b);
+    const double bRef = bNorm > 0.0 ? bNorm : 1.0;
+    double rNorm = norm2(n, r);
+    out[2] = rNorm;
+    if (rNorm / bRef <= tol) {
+        out[0] = 0.0;
+        out[1] = rNorm;
+        out[3] = 1.0;
+        *lastResidual = rNorm;
+    } else {
+        APPLY_M();
+        memcpy(p, z, (size_t)n * sizeof(double));
+        double rhoOld = orc_dot(n, r, z);
+        const double dropTol = relativeOrders > 0.0 ? rNorm * pow(10.0, -relativeOrders) : 0.0;
+        for (int it = 1; it <= maxIt; ++it) {
+            orc_spmv(n, rowPtr, colIdx, values, p, q);
+            const double pq = orc_dot(n, p, q);
+            if (fabs(pq) < 1e-300)
+                break;
+            const double alpha = rhoOld / pq;
+            axpy(n, alpha, p, x);
+            axpy(n, -alpha, q, r);
+            rNorm = norm2(n, r);
+            if (rNorm / bRef <= tol || (dropTol > 0.0 && rNorm <= dropTol)) {
+                out[0] = it;
+                out[1] = rNorm;
+                out[3] = 1.0;
+                break;
+            }
+            APPLY_M();
+            const double rhoNew = orc_dot(n, r, z);
+            const double beta = rhoNew / rhoOld;
+            for (int64_t i = 0; i < n; ++i)
+                p[i] = 1.0 * z[i] + beta * p[i];
+            rhoOld = rhoNew;
+            if (it == maxIt) {
+                out[0] = it;
+                out[1] = rNorm;
+                out[3] = 0.0;
+            }
+        }
+        *lastResidual = out[1];
+    }
+#undef APPLY_M
+    free(r);
+    free(z);
+    free(p);
+    free(q);
+    free(d);
+    free(lu);
+}
+
 /* ------------------------------------------------------------------ face-conductance extension */
 
 /*

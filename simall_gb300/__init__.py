@@ -12,7 +12,7 @@ from .fields import DeviceFieldRegistry, checkpoint_read, checkpoint_write
 from .mesh import BCType, MeshSoA, PressureSystem, cartesian, rcm
 from .simple import GpuSimpleAlgorithm, PimpleOptions, PisoOptions, SimpleOptions, SimpleResiduals
 from .topology import GpuSimpTopology, SimpConfig
-from .solver import (Context, CSRMatrix, GpuCGSolver, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
+from .solver import (CgGpu, Context, CSRMatrix, GpuCGSolver, GpuPreconditioner, GpuSolverConfig, GpuSolverStats, GpuLinearSolver, LinearSolverConfig, LinearSolverKind,
                      Precision, PreconditionerKind, default_context, make_bicgstab, make_cg, make_gmres,
                      make_linear_solver, make_tfqmr)
 
@@ -21,4 +21,5 @@ __all__ = ["build", "BatchedSolver", "load", "MEM_HOST", "MEM_DEVICE", "SimallEr
            "Precision", "PreconditionerKind", "default_context", "make_cg", "make_linear_solver", "GpuLinearSolver",
            "make_gmres", "make_bicgstab", "make_tfqmr", "GpuSimpleAlgorithm", "SimpleOptions", "SimpleResiduals", "PisoOptions",
            "PimpleOptions",
-           "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write", "GpuSimpTopology", "SimpConfig"]
+           "DeviceFieldRegistry", "checkpoint_read", "checkpoint_write", "GpuSimpTopology", "SimpConfig",
+           "CgGpu", "GpuPreconditioner", "GpuSolverConfig", "GpuSolverStats"]

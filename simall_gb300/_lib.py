@@ -31,13 +31,14 @@ STATUS_NAMES = {
 
 class SolverConfig(C.Structure):
     _fields_ = [("preconditioner", _I), ("tolerance", _D), ("max_iterations", _I), ("precision", _I),
-                ("reliable_delta", _D), ("check_interval", _I), ("engine", _I), ("kind", _I), ("restart", _I)]
+                ("reliable_delta", _D), ("check_interval", _I), ("engine", _I), ("kind", _I), ("restart", _I),
+                ("semantics", _I), ("relative_orders", _D)]
 
 
 class SolverStats(C.Structure):
     _fields_ = [("iterations", _I), ("converged", _I), ("status", _I), ("reliable_updates", _I),
                 ("final_residual", _D), ("true_residual", _D), ("b_norm", _D), ("seconds", _D),
-                ("engine", _I), ("reserved", _I)]
+                ("engine", _I), ("preconditioner", _I), ("residual_norm", _D), ("initial_residual", _D)]
 
 
 class ZoneVelocity(C.Structure):
@@ -113,6 +114,7 @@ SIGNATURES = {
     "simall_context_stream": (_P, [_P]),
     "simall_context_kernel_launches": (_I64, [_P]),
     "simall_diagnose_bounded_wait": (_I, [_P, C.POINTER(_I), C.POINTER(_D)]),
+    "simall_diagnose_sweep_params": (_I, [_I, _I]),
     "simall_diagnose_division": (_I, [_P, _I64, _P, _P, _P, _P]),
     "simall_solver_config_default": (None, [C.POINTER(SolverConfig)]),
     "simall_solver_create": (_I, [_P, C.POINTER(SolverConfig), C.POINTER(_P)]),
@@ -125,6 +127,7 @@ SIGNATURES = {
     "simall_solver_amg_levels": (_I, [_P, _P, _P, _I]),
     "simall_amg_hierarchy_digest": (_I, [_I64, _P, _P, _P, _P, _P, _I, _P]),
     "simall_solver_last_residual": (_D, [_P]),
+    "simall_solver_preconditioner": (_I, [_P, _P]),
     "simall_solver_time_kernel": (_I, [_P, _I, _I, C.POINTER(_D), C.POINTER(_D)]),
     "simall_solver_solve_csr": (_I, [_P, _I64, _I64, _P, _P, _P, _P, _P, C.POINTER(SolverStats)]),
     "simall_pressure_system_create": (_I, [_P, C.POINTER(MeshView), C.POINTER(Boundary), _I, C.POINTER(_P)]),

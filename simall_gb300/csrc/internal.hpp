@@ -107,6 +107,13 @@ struct SolveScalars {
     int updates;      // mixed: reliable updates performed
     int seen;         // mixed device loop: iteration count the last controller saw
     unsigned counter[8];  // last-block tickets, one per kernel kind
+    // gpu::CgGpu semantics (SIMALL_SEMANTICS_CGGPU; FP64 CG only)
+    int cggpu;          // 1: x0 honoured, stop test <= tol or the relative drop, |p.q| < 1e-300 break
+    int converged;      // cggpu: set by the stop test that ended the solve
+    double drop_factor; // cggpu: 10^-relativeOrders, 0 when off (set by the host)
+    double drop_tol;    // cggpu: ||r_0|| * drop_factor
+    double rnorm0;      // cggpu: ||b - A x0||
+    double rnorm;       // ||r|| at the last stop test (cggpu: finalResidual)
 };
 
 // CSR row-blocks for the staged SpMV: each block holds <= kSpmvRows rows and

@@ -206,9 +206,12 @@ __global__ void __launch_bounds__(kBlock) k_spmv_pap(const int32_t *__restrict__
     if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0) {
         const double pAp = v[0];
         s->pAp = pAp;
-        if (pAp == 0.0) {
-            s->last = sqrt(s->rz) / s->bnorm;
-            s->result = s->iter;
+        if (s->cggpu ? fabs(pAp) < 1e-300 : pAp == 0.0) {
+            // CGSolver returns the iterations done; CgGpu::solve leaves its
+            // stats at zero (src/gpu/CgGpu.cpp:190-194)
+            s->last = s->cggpu ? 0.0 : sqrt(s->rz) / s->bnorm;
+            s->rnorm = s->cggpu ? 0.0 : s->rnorm;
+            s->result = s->cggpu ? 0 : s->iter;
             s->done = 1;
             s->status = SIMALL_ERR_BREAKDOWN;
         } else {
@@ -232,9 +235,12 @@ __global__ void __launch_bounds__(kBlock) k_spmv_pap_rows(const int32_t *__restr
     if (grid_sum_last<1>(v, partials, &s->counter[1]) && threadIdx.x == 0) {
         const double pAp = v[0];
         s->pAp = pAp;
-        if (pAp == 0.0) {
-            s->last = sqrt(s->rz) / s->bnorm;
-            s->result = s->iter;
+        if (s->cggpu ? fabs(pAp) < 1e-300 : pAp == 0.0) {
+            // CGSolver returns the iterations done; CgGpu::solve leaves its
+            // stats at zero (src/gpu/CgGpu.cpp:190-194)
+            s->last = s->cggpu ? 0.0 : sqrt(s->rz) / s->bnorm;
+            s->rnorm = s->cggpu ? 0.0 : s->rnorm;
+            s->result = s->cggpu ? 0 : s->iter;
             s->done = 1;
             s->status = SIMALL_ERR_BREAKDOWN;
         } else {
@@ -258,14 +264,19 @@ __global__ void __launch_bounds__(kBlock) k_spmv_plain(const int32_t *__restrict
     spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
 }
 
-// Stop test and beta (CGSolver::solve :439-449).  Thread 0 of the last CTA.
+// Stop test and beta (CGSolver::solve :439-449; CgGpu::solve, src/gpu/CgGpu.cpp:
+// 199-205, with <= and the relative drop).  Thread 0 of the last CTA.
 __device__ __forceinline__ void finish_iteration(SolveScalars *s, double rr, double rzNew, bool have_rz)
 {
     s->rr = rr;
-    const double last = sqrt(rr) / s->bnorm;
+    const double rn = sqrt(rr);
+    const double last = rn / s->bnorm;
     s->last = last;
-    if (last < s->tol) {
+    s->rnorm = rn;
+    const bool stop = s->cggpu ? (last <= s->tol || (s->drop_tol > 0.0 && rn <= s->drop_tol)) : last < s->tol;
+    if (stop) {
         s->result = s->iter + 1;
+        s->converged = 1;
         s->done = 1;
         return;
     }
@@ -459,6 +470,103 @@ __global__ void __launch_bounds__(kBlock) k_residual(const int32_t *__restrict__
         *out = v[0];
 }
 
+// CgGpu semantics before the first iteration (CgGpu::solve, src/gpu/CgGpu.cpp:
+// 138-168): r = b - A x0 (the SpMV with the reference's rounding, then -y + b),
+// ||b||, ||r_0||; bRef = ||b||, or 1 when b = 0; converged at once when
+// ||r_0|| / bRef <= tol (0 iterations); dropTol = ||r_0|| 10^-relativeOrders.
+struct InitX0Epi {
+    const double *b;
+    double *r;
+    double rr, bb;
+    __device__ __forceinline__ void operator()(int row, double y)
+    {
+        const double bi = __ldg(b + row);
+        const double v = -y + bi;
+        r[row] = v;
+        rr += v * v;
+        bb += bi * bi;
+    }
+};
+
+__global__ void __launch_bounds__(kBlock) k_init_x0(const int32_t *__restrict__ rowPtr,
+                                                    const int32_t *__restrict__ colIdx,
+                                                    const double *__restrict__ val, const int32_t *__restrict__ rb,
+                                                    int nRB, const double *__restrict__ x,
+                                                    const double *__restrict__ b, double *__restrict__ r,
+                                                    double *partials, SolveScalars *s)
+{
+    InitX0Epi epi{b, r, 0.0, 0.0};
+    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
+    double v[2] = {epi.rr, epi.bb};
+    if (grid_sum_last<2>(v, partials, &s->counter[0]) && threadIdx.x == 0) {
+        const double bn = sqrt(v[1]);
+        const double rn = sqrt(v[0]);
+        s->bnorm = bn > 0.0 ? bn : 1.0;
+        s->rr = v[0];
+        s->rnorm0 = rn;
+        s->rnorm = rn;
+        s->last = rn / s->bnorm;
+        s->drop_tol = s->drop_factor > 0.0 ? rn * s->drop_factor : 0.0;
+        s->iter = 0;
+        s->result = 0;
+        s->status = SIMALL_OK;
+        s->converged = 0;
+        if (rn / s->bnorm <= s->tol) {
+            s->converged = 1;
+            s->done = 1;
+        } else if (s->max_iter <= 0) {  // the loop never runs: stats stay zero
+            s->rnorm = 0.0;
+            s->last = 0.0;
+            s->done = 1;
+        } else {
+            s->done = 0;
+        }
+    }
+}
+
+// z = invD r, p = z, rz = r.z (CgGpu semantics, Jacobi or None: invD = 1).
+__global__ void __launch_bounds__(kBlock) k_init_jz(int64_t n, const double *__restrict__ r,
+                                                    const double *__restrict__ invD, double *__restrict__ z,
+                                                    double *__restrict__ p, double *partials, SolveScalars *s)
+{
+    double acc[1] = {0.0};
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double ri = r[i];
+        const double zi = invD[i] * ri;
+        z[i] = zi;
+        p[i] = zi;
+        acc[0] += ri * zi;
+    }
+    if (grid_sum_last<1>(acc, partials, &s->counter[3]) && threadIdx.x == 0)
+        s->rz = acc[0];
+}
+
+__global__ void __launch_bounds__(kBlock) k_fill(int64_t n, double *__restrict__ v, double value)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        v[i] = value;
+}
+
+// gpu::ilu0_factor_inplace's verdict (src/gpu/GpuKernels.cpp:345-401) read off a
+// finished ILU(0) factor: a missing diagonal, or a zero U_ii of a row i >= 1,
+// or a zero U_00 that a later row eliminates against.  Up to the first such
+// pivot the two factorisations perform the same operations, so the verdicts
+// agree.
+__global__ void __launch_bounds__(kBlock) k_cggpu_pivot_check(int64_t n, const int32_t *__restrict__ rowPtr,
+                                                              const int32_t *__restrict__ colIdx,
+                                                              const int32_t *__restrict__ diagPtr,
+                                                              const double *__restrict__ lu, int *flag)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int d = diagPtr[i];
+        if (d < 0 || (i > 0 && lu[d] == 0.0))
+            atomicOr(flag, 1);
+        const int d0 = diagPtr[0];
+        if (i > 0 && d0 >= 0 && rowPtr[i] < rowPtr[i + 1] && colIdx[rowPtr[i]] == 0 && lu[d0] == 0.0)
+            atomicOr(flag, 1);
+    }
+}
+
 int grid_for(simall_context *ctx, int64_t n)
 {
     const int64_t g = (n + kBlock - 1) / kBlock;
@@ -495,6 +603,33 @@ int setup_values(simall_solver *s)
     simall_context *ctx = s->ctx;
     if (s->cfg.precision == SIMALL_PRECISION_MIXED)
         return mixed_setup(s);
+    const bool cggpu = s->cfg.semantics == SIMALL_SEMANTICS_CGGPU;
+    if (cggpu && s->cfg.preconditioner == SIMALL_PRECOND_ILU0) {
+        // CgGpu::set_matrix (src/gpu/CgGpu.cpp:60-83): a factor that fails
+        // makes the solver Jacobi for good
+        const int st = ilu_setup(s);
+        if (st)
+            return st;
+        SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
+        k_cggpu_pivot_check<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->rowPtr, s->colIdx,
+                                                                             s->ilu->diagPtr.p, s->ilu->lu.p,
+                                                                             s->flag.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int h = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, s->flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!h)
+            return SIMALL_OK;
+        s->cfg.preconditioner = SIMALL_PRECOND_JACOBI;
+        drop_graphs(s);  // the captured iterations hold the ILU(0) sweeps
+    }
+    if (cggpu && s->cfg.preconditioner == SIMALL_PRECOND_NONE) {  // z = r
+        SIMALL_CUDA_TRY(ctx, s->invDiag.alloc(static_cast<size_t>(s->n)));
+        k_fill<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->invDiag.p, 1.0);
+        SIMALL_LAUNCH_CHECK(ctx);
+        return SIMALL_OK;
+    }
     if (s->cfg.preconditioner == SIMALL_PRECOND_ILU0)
         return ilu_setup(s);
     if (s->cfg.preconditioner == SIMALL_PRECOND_AMG) {
@@ -642,13 +777,36 @@ int fp64_solve(simall_solver *s, simall_solver_stats *st)
                                          ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->max_iter, &init.max_iter, sizeof(int), cudaMemcpyHostToDevice,
                                          ctx->stream));
+    const bool cggpu = s->cfg.semantics == SIMALL_SEMANTICS_CGGPU;
+    init.cggpu = cggpu ? 1 : 0;
+    init.drop_factor = cggpu && s->cfg.relative_orders > 0.0 ? std::pow(10.0, -s->cfg.relative_orders) : 0.0;
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->cggpu, &init.cggpu, sizeof(int), cudaMemcpyHostToDevice,
+                                         ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&s->scal.p->drop_factor, &init.drop_factor, sizeof(double),
+                                         cudaMemcpyHostToDevice, ctx->stream));
     if (s->cfg.preconditioner == SIMALL_PRECOND_JACOBI && s->cfg.check_interval <= 0 &&
-        s->cfg.engine == SIMALL_ENGINE_AUTO) {
+        s->cfg.engine == SIMALL_ENGINE_AUTO && !cggpu) {
         int cst = SIMALL_OK;
         if (cluster_fp64_solve(s, &cst))
             return cst;
     }
-    if (sweep_preconditioner(s->cfg.preconditioner)) {
+    if (cggpu) {
+        // x holds x0 (copied in by the solve call)
+        k_init_x0<<<resident_grid(ctx, reinterpret_cast<const void *>(k_init_x0), spmv_items(s)), kBlock, 0,
+                    ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s), s->x.p,
+                                   s->b.p, s->r.p, s->partials.p, s->scal.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        if (sweep_preconditioner(s->cfg.preconditioner)) {
+            int e = ilu_apply(s, s->r.p, s->z.p);
+            if (e)
+                return e;
+            k_init_p_rz<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->z.p, s->p.p, s->partials.p, s->scal.p);
+        } else {
+            k_init_jz<<<g, kBlock, 0, ctx->stream>>>(s->n, s->r.p, s->invDiag.p, s->z.p, s->p.p, s->partials.p,
+                                                     s->scal.p);
+        }
+        SIMALL_LAUNCH_CHECK(ctx);
+    } else if (sweep_preconditioner(s->cfg.preconditioner)) {
         k_init_plain<<<g, kBlock, 0, ctx->stream>>>(s->n, s->b.p, s->x.p, s->r.p, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         int e = ilu_apply(s, s->r.p, s->z.p);
@@ -764,6 +922,8 @@ void simall_solver_config_default(simall_solver_config *cfg)
     cfg->engine = SIMALL_ENGINE_AUTO;
     cfg->kind = SIMALL_SOLVER_CG;
     cfg->restart = 30;
+    cfg->semantics = SIMALL_SEMANTICS_CGSOLVER;
+    cfg->relative_orders = 0.0;
 }
 
 int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, simall_solver **out)
@@ -775,9 +935,20 @@ int simall_solver_create(simall_context *ctx, const simall_solver_config *cfg, s
     simall_solver_config_default(&c);
     if (cfg)
         c = *cfg;
-    if (c.preconditioner == SIMALL_PRECOND_NONE)
-        c.preconditioner = SIMALL_PRECOND_JACOBI;
-    if (c.preconditioner != SIMALL_PRECOND_JACOBI && !sweep_preconditioner(c.preconditioner))
+    if (c.semantics != SIMALL_SEMANTICS_CGSOLVER && c.semantics != SIMALL_SEMANTICS_CGGPU)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "semantics %d", c.semantics);
+    if (c.semantics == SIMALL_SEMANTICS_CGGPU) {
+        if (c.kind != SIMALL_SOLVER_CG || c.precision != SIMALL_PRECISION_FP64 ||
+            (c.preconditioner != SIMALL_PRECOND_JACOBI && c.preconditioner != SIMALL_PRECOND_ILU0 &&
+             c.preconditioner != SIMALL_PRECOND_NONE))
+            return fail(ctx, SIMALL_ERR_UNSUPPORTED, "CgGpu semantics: FP64 CG with Jacobi, ILU0 or None");
+        if (!(c.relative_orders >= 0.0))
+            return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "relative_orders must be >= 0");
+    } else if (c.preconditioner == SIMALL_PRECOND_NONE) {
+        c.preconditioner = SIMALL_PRECOND_JACOBI;  // make_preconditioner (LinearSolvers.cpp:240-254)
+    }
+    if (c.preconditioner != SIMALL_PRECOND_JACOBI && c.preconditioner != SIMALL_PRECOND_NONE &&
+        !sweep_preconditioner(c.preconditioner))
         return fail(ctx, SIMALL_ERR_UNSUPPORTED, "preconditioner %d is not on the pressure path", c.preconditioner);
     if (c.precision != SIMALL_PRECISION_FP64 && c.precision != SIMALL_PRECISION_MIXED)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "precision %d", c.precision);
@@ -994,6 +1165,21 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
         if (h)
             return fail(ctx, SIMALL_ERR_NON_FINITE, "b contains NaN or Inf");
     }
+    if (s->cfg.semantics == SIMALL_SEMANTICS_CGGPU) {
+        // x is the initial guess (CgGpu::solve uploads x0, src/gpu/CgGpu.cpp:133-136)
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(s->x.p, x, bytes,
+                                             xmem == SIMALL_MEM_HOST ? cudaMemcpyHostToDevice
+                                                                     : cudaMemcpyDeviceToDevice,
+                                             ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
+        k_check_finite<<<grid_for(ctx, s->n), kBlock, 0, ctx->stream>>>(s->n, s->x.p, s->flag.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        int h = 0;
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(&h, s->flag.p, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (h)
+            return fail(ctx, SIMALL_ERR_NON_FINITE, "the initial guess x contains NaN or Inf");
+    }
     simall_solver_stats local{};
     int st;
     s->engine = 0;
@@ -1025,16 +1211,19 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
     s->last_residual = h.last;
     s->solved = true;
     if (stats) {
+        const bool cggpu = s->cfg.semantics == SIMALL_SEMANTICS_CGGPU;
         stats->iterations = h.result;
         stats->final_residual = h.last;
-        stats->converged = (h.last < s->cfg.tolerance) ? 1 : 0;
+        stats->converged = cggpu ? h.converged : ((h.last < s->cfg.tolerance) ? 1 : 0);
         stats->status = h.status;
         stats->reliable_updates = h.updates;
         stats->b_norm = h.bnorm;
         stats->true_residual = std::sqrt(rr) / h.bnorm;
         stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         stats->engine = s->engine;
-        stats->reserved = 0;
+        stats->preconditioner = s->cfg.preconditioner;
+        stats->residual_norm = cggpu ? h.rnorm : h.last * h.bnorm;
+        stats->initial_residual = cggpu ? h.rnorm0 : h.bnorm;
     }
     return SIMALL_OK;
 }
@@ -1042,6 +1231,14 @@ int simall::solver_solve_impl(simall_solver *s, const double *b, int bmem, doubl
 extern "C" {
 
 double simall_solver_last_residual(const simall_solver *s) { return s ? s->last_residual : 0.0; }
+
+int simall_solver_preconditioner(const simall_solver *s, int *preconditioner)
+{
+    if (!s || !preconditioner)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    *preconditioner = s->cfg.preconditioner;
+    return SIMALL_OK;
+}
 
 int simall_solver_time_kernel(simall_solver *s, int kernel, int reps, double *ms, double *bytes)
 {

@@ -284,6 +284,120 @@ class GpuCGSolver:
             pass
 
 
+class GpuPreconditioner(IntEnum):
+    """gpu::GpuPreconditioner (src/gpu/CgGpu.hpp:52-57)."""
+    None_ = 0
+    Jacobi = 1
+    ILU0 = 2
+
+
+_GPU_PRECOND_TO_C = {GpuPreconditioner.None_: 4, GpuPreconditioner.Jacobi: 0, GpuPreconditioner.ILU0: 1}
+_C_TO_GPU_PRECOND = {v: k for k, v in _GPU_PRECOND_TO_C.items()}
+
+
+@dataclass
+class GpuSolverConfig:
+    """gpu::GpuSolverConfig (src/gpu/CgGpu.hpp:59-66)."""
+    preconditioner: GpuPreconditioner = GpuPreconditioner.Jacobi
+    tolerance: float = 1.0e-8
+    maxIterations: int = 1000
+    relativeOrders: float = 0.0
+
+
+@dataclass
+class GpuSolverStats:
+    """gpu::GpuSolverStats (src/gpu/CgGpu.hpp:68-75)."""
+    iterations: int = 0
+    finalResidual: float = 0.0
+    initialResidual: float = 0.0
+    converged: bool = False
+    timeSeconds: float = 0.0
+
+
+class CgGpu:
+    """gpu::CgGpu (src/gpu/CgGpu.hpp:49-124) on the device: the FP64 PCG of
+    this library with CgGpu::solve's conventions (SIMALL_SEMANTICS_CGGPU):
+    x is the initial guess and the solution, stop on ||r||/bRef <= tolerance
+    or the relativeOrders drop, None = no preconditioner, ILU0 falls back to
+    Jacobi for good when its factor meets a zero pivot."""
+
+    def __init__(self, cfg: GpuSolverConfig | None = None, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.L = self.ctx.L
+        self._cfg = cfg or GpuSolverConfig()
+        self.handle = None
+        self._make()
+        self._last = 0.0
+        self.n = 0
+        register_child(self)
+        self.ctx.children.add(self)
+
+    def _make(self):
+        if self.handle:
+            self.L.simall_solver_destroy(self.handle)
+        c = _lib.SolverConfig()
+        self.L.simall_solver_config_default(C.byref(c))
+        c.preconditioner = _GPU_PRECOND_TO_C[GpuPreconditioner(self._cfg.preconditioner)]
+        c.tolerance = float(self._cfg.tolerance)
+        c.max_iterations = int(self._cfg.maxIterations)
+        c.semantics = 1
+        c.relative_orders = float(self._cfg.relativeOrders)
+        h = C.c_void_p()
+        check(self.L.simall_solver_create(self.ctx.handle, C.byref(c), C.byref(h)), self.ctx.handle)
+        self.handle = h.value
+
+    def config(self) -> GpuSolverConfig:
+        return self._cfg
+
+    def set_config(self, cfg: GpuSolverConfig):
+        """Takes effect at the next set_matrix, as in the reference (the
+        preconditioner data is built there)."""
+        self._cfg = cfg
+        self._make()
+
+    def set_matrix(self, rowPtr, colIdx, values):
+        p0, m0 = ptr_and_mem(rowPtr)
+        p1, _ = ptr_and_mem(colIdx)
+        p2, _ = ptr_and_mem(values)
+        self.n = len(rowPtr) - 1
+        check(self.L.simall_solver_set_matrix(self.handle, self.n, len(colIdx), p0, p1, p2, m0), self.ctx.handle)
+        # the preconditioner after CgGpu::set_matrix's ILU0 -> Jacobi fall-back
+        self._cfg.preconditioner = self._precond_now()
+
+    def _precond_now(self) -> GpuPreconditioner:
+        pc = C.c_int(-1)
+        check(self.L.simall_solver_preconditioner(self.handle, C.byref(pc)), self.ctx.handle)
+        return _C_TO_GPU_PRECOND[pc.value]
+
+    def solve(self, b, x) -> GpuSolverStats:
+        """Solve A x = b; x (numpy array, or a CUDA tensor with b one too) is
+        the initial guess on entry and the solution on exit."""
+        pb, mb = ptr_and_mem(b)
+        px, mx = ptr_and_mem(x)
+        if mb != mx:
+            raise ValueError("b and x must live in the same memory")
+        st = _lib.SolverStats()
+        check(self.L.simall_solver_solve(self.handle, pb, px, mb, C.byref(st)), self.ctx.handle)
+        self.stats = st
+        self._last = float(st.residual_norm)
+        return GpuSolverStats(int(st.iterations), float(st.residual_norm), float(st.initial_residual),
+                              bool(st.converged), float(st.seconds))
+
+    def last_residual(self) -> float:
+        return self._last
+
+    def close(self):
+        if getattr(self, "handle", None) and getattr(self.ctx, "handle", None):
+            self.L.simall_solver_destroy(self.handle)
+        self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 class GpuLinearSolver(GpuCGSolver):
     """ILinearSolver of the kind cfg.kind names: GMRES(cfg.restart), BiCGSTAB
     or TFQMR (GMRESmSolver / BiCGSTABSolver / TfqmrSolver,

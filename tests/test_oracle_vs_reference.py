@@ -351,3 +351,16 @@ def test_krylov_edge_cases(oracle, ref, kind):
                           else oracle.tfqmr(rp, ci, va, bb, 0, 1e-12, mx))
         assert (it, last) == (oit, olast), (kind, mx)
         assert bits_equal(x, ox)
+
+
+def test_cggpu_cases(oracle, ref):
+    """gpu::CgGpu (set_matrix + solve, the facade's host path) against the
+    oracle's restatement: x and every stat bit for bit, including the ILU0 ->
+    Jacobi fall-back, the p.q breakdown, maxIterations 0 and b = 0."""
+    from helpers import cggpu_cases
+
+    for name, rp, ci, v, b, x0, pc, tol, mi, ro in cggpu_cases(oracle):
+        xr, sr = ref.cggpu(rp, ci, v, b, x0, pc, tol, mi, ro)
+        xo, so = oracle.cggpu(rp, ci, v, b, x0, pc, tol, mi, ro)
+        assert bits_equal(xr, xo), name
+        assert sr == so, (name, sr, so)
