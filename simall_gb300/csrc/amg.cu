@@ -64,7 +64,8 @@ template <bool BWD, bool ZERO>
 __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__restrict__ order,
                                                      const int32_t *__restrict__ rp, const int32_t *__restrict__ ci,
                                                      const double *__restrict__ a, const double *__restrict__ b,
-                                                     const double *__restrict__ xin, double *xout, unsigned *ctl)
+                                                     const double *__restrict__ xin, double *xout, unsigned *ctl,
+                                                     unsigned backoff)
 {
     const int lane = threadIdx.x & 31;
     bool ok = true;
@@ -92,7 +93,7 @@ __global__ void __launch_bounds__(kBlock) k_sgs_free(int n, const int32_t *__res
                     dep[q] = BWD ? j[q] > i : j[q] < i;
                 }
                 double v[4];
-                ok = wait_values4(xout, j, dep, v) && ok;
+                ok = wait_values4(xout, j, dep, v, backoff) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (!dep[q])
@@ -341,11 +342,14 @@ int sweep(simall_context *ctx, AmgLevelDev &L, bool backward, bool zero, const d
     const int g = grid_sweep(ctx, L.n);
     const int32_t *order = backward ? L.bwdOrder.p : L.fwdOrder.p;
     if (backward)
-        k_sgs_free<true, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
+        k_sgs_free<true, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p,
+                                                      g_sweep_backoff_ns);
     else if (zero)
-        k_sgs_free<false, true><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
+        k_sgs_free<false, true><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p,
+                                                      g_sweep_backoff_ns);
     else
-        k_sgs_free<false, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p);
+        k_sgs_free<false, false><<<g, kBlock, 0, ctx->stream>>>(L.n, order, L.rp, L.ci, L.v, b, xin, xout, L.ctl.p,
+                                                      g_sweep_backoff_ns);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }

@@ -39,7 +39,41 @@
 
 namespace simall {
 
+int g_sweep_ctas_per_sm = 4;
+unsigned g_sweep_backoff_ns = 256;
+
 namespace {
+
+// a / b rounded to nearest from rb = RN(1/b) (a correctly rounded reciprocal):
+// q = RN(a rb) is within an ulp of a/b, the remainder r = a - b q is exact
+// with one FMA, and q + r rb rounded once is RN(a/b) (Markstein's theorem,
+// IBM J. Res. Dev. 34(1), 1990; Handbook of Floating-Point Arithmetic,
+// 2nd ed., Thm. 5.9).  Three FP64 operations instead of a full division --
+// GB300's FP64 pipe is narrow enough that the divisions of the backward sweep
+// set its time.  The theorem needs a, b, the quotient and the remainder away
+// from overflow and underflow, and a zero numerator keeps its sign only
+// through the product; outside that range (or when b has no usable
+// reciprocal) the division itself is taken.
+// Biased exponent field of x, on the integer pipe (GB300 issues about 1.6 FP64
+// operations per clock per SM, so range tests in FP64 would cost as much as
+// the division they replace).
+__device__ __forceinline__ unsigned biased_exp(double x)
+{
+    return static_cast<unsigned>(__double2hiint(x) >> 20) & 0x7ffu;
+}
+
+__device__ __forceinline__ double div_rn_by_recip(double a, double b, double rb)
+{
+    const double q = a * rb;
+    // |a|, |q|, |rb| in [2^-900, 2^901): biased exponents in [123, 1924]
+    const unsigned ea = biased_exp(a) - 123u, eq = biased_exp(q) - 123u, er = biased_exp(rb) - 123u;
+    if ((ea | eq | er) <= 1801u && ea <= 1801u && eq <= 1801u && er <= 1801u) {
+        const double r = fma(-q, b, a);
+        return fma(r, rb, q);
+    }
+    return __ddiv_rn(a, b);
+}
+
 
 // One level of the IKJ factorisation, one thread per row.
 __global__ void __launch_bounds__(kBlock) k_ilu_factor_level(const int32_t *__restrict__ rows, int cnt,
@@ -129,7 +163,8 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const double *__restrict__ lu, const double *__restrict__ r,
-                                                         const double *__restrict__ invD, double *y, unsigned *ctl)
+                                                         const double *__restrict__ invD, double *y, unsigned *ctl,
+                                                         unsigned backoff)
 {
     const int lane = threadIdx.x & 31;
     bool ok = true;
@@ -164,7 +199,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
                 for (int q = 0; q < 4; ++q)
                     dep[q] = q < cnt;
                 double v[4];
-                ok = wait_values4(y, j, dep, v) && ok;
+                ok = wait_values4(y, j, dep, v, backoff) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (q < cnt)
@@ -184,14 +219,18 @@ __global__ void __launch_bounds__(kBlock) k_ilu_fwd_free(int n, const int32_t *_
 
 // Backward sweep z_i = (y_i - sum_{j>i} u_ij z_j) / u_ii over rows in level order
 // (SSOR: (a_ii y_i - sum_{j>i} a_ij z_j) invD_i); z holds kPending until a
-// row's value lands.
+// row's value lands.  The division runs through rdiag = RN(1/u_ii) when given
+// (div_rn_by_recip: the same bits as the division, three FP64 operations on
+// the chain instead of a full divide), else as a division.
 template <bool SSOR>
 __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *__restrict__ order,
                                                          const int32_t *__restrict__ rowPtr,
                                                          const int32_t *__restrict__ colIdx,
                                                          const int32_t *__restrict__ diagPtr,
                                                          const double *__restrict__ lu, const double *__restrict__ y,
-                                                         const double *__restrict__ invD, double *z, unsigned *ctl)
+                                                         const double *__restrict__ invD,
+                                                         const double *__restrict__ rdiag, double *z, unsigned *ctl,
+                                                         unsigned backoff)
 {
     const int lane = threadIdx.x & 31;
     bool ok = true;
@@ -224,7 +263,7 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
                     cnt += in ? 1 : 0;
                 }
                 double v[4];
-                ok = wait_values4(z, j, dep, v) && ok;
+                ok = wait_values4(z, j, dep, v, backoff) && ok;
 #pragma unroll
                 for (int q = 0; q < 4; ++q)
                     if (q < cnt)
@@ -235,7 +274,10 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
                 st_value(z + i, __dmul_rn(s, __ldg(invD + i)));
             } else {
                 const double dv = kd >= 0 ? __ldg(lu + kd) : 0.0;
-                st_value(z + i, (kd >= 0 && dv != 0.0) ? __ddiv_rn(s, dv) : s);
+                double zi = s;
+                if (kd >= 0 && dv != 0.0)
+                    zi = rdiag ? div_rn_by_recip(s, dv, __ldg(rdiag + i)) : __ddiv_rn(s, dv);
+                st_value(z + i, zi);
             }
         }
     }
@@ -251,36 +293,6 @@ __global__ void __launch_bounds__(kBlock) k_ilu_bwd_free(int n, const int32_t *_
 // backward sweep overwrites y with z in place: row i reads y_i and the final
 // z_j of rows in earlier backward levels only).  Same per-row operations, so
 // the results are bit-identical to the reference's.
-// a / b rounded to nearest from rb = RN(1/b) (a correctly rounded reciprocal):
-// q = RN(a rb) is within an ulp of a/b, the remainder r = a - b q is exact
-// with one FMA, and q + r rb rounded once is RN(a/b) (Markstein's theorem,
-// IBM J. Res. Dev. 34(1), 1990; Handbook of Floating-Point Arithmetic,
-// 2nd ed., Thm. 5.9).  Three FP64 operations instead of a full division --
-// GB300's FP64 pipe is narrow enough that the divisions of the backward sweep
-// set its time.  The theorem needs a, b, the quotient and the remainder away
-// from overflow and underflow, and a zero numerator keeps its sign only
-// through the product; outside that range (or when b has no usable
-// reciprocal) the division itself is taken.
-// Biased exponent field of x, on the integer pipe (GB300 issues about 1.6 FP64
-// operations per clock per SM, so range tests in FP64 would cost as much as
-// the division they replace).
-__device__ __forceinline__ unsigned biased_exp(double x)
-{
-    return static_cast<unsigned>(__double2hiint(x) >> 20) & 0x7ffu;
-}
-
-__device__ __forceinline__ double div_rn_by_recip(double a, double b, double rb)
-{
-    const double q = a * rb;
-    // |a|, |q|, |rb| in [2^-900, 2^901): biased exponents in [123, 1924]
-    const unsigned ea = biased_exp(a) - 123u, eq = biased_exp(q) - 123u, er = biased_exp(rb) - 123u;
-    if ((ea | eq | er) <= 1801u && ea <= 1801u && eq <= 1801u && er <= 1801u) {
-        const double r = fma(-q, b, a);
-        return fma(r, rb, q);
-    }
-    return __ddiv_rn(a, b);
-}
-
 constexpr int kIluSmallThreads = 1024;
 constexpr int kIluSmallRows = 24576;  // 192 KB of shared memory
 
@@ -720,6 +732,17 @@ int pack(simall_context *ctx, IluData *d)
     return SIMALL_OK;
 }
 
+// rdiag_i = RN(1/u_ii), 0 where the diagonal is missing or zero (the sweep
+// then keeps s, as the reference does).
+__global__ void __launch_bounds__(kBlock) k_ilu_rdiag(int n, const int32_t *__restrict__ diagPtr,
+                                                      const double *__restrict__ lu, double *__restrict__ rdiag)
+{
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const int d = diagPtr[i];
+        rdiag[i] = (d >= 0 && lu[d] != 0.0) ? __drcp_rn(lu[d]) : 0.0;
+    }
+}
+
 int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t *colIdx)
 {
     const int nlev = static_cast<int>(d->fwdLevelPtr.size()) - 1;
@@ -735,6 +758,11 @@ int factor(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
                                                                                     colIdx, d->diagPtr.p, d->lu.p);
         SIMALL_LAUNCH_CHECK(ctx);
     }
+    const int n = static_cast<int>(d->h_diagPtr.size());
+    SIMALL_CUDA_TRY(ctx, d->rdiag.alloc(n));
+    k_ilu_rdiag<<<std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8), kBlock, 0, ctx->stream>>>(n, d->diagPtr.p,
+                                                                                                d->lu.p, d->rdiag.p);
+    SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
 
@@ -754,18 +782,22 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
-    const int grid = ctx->num_sms * 4;  // 32 warps per SM take rows; more only add waiting warps
+    // warps beyond a few levels' rows only add polls: g_sweep_ctas_per_sm (4: 32 warps per SM)
+    const int grid = ctx->num_sms * g_sweep_ctas_per_sm;
+    const unsigned backoff = g_sweep_backoff_ns;
+    const double *rdiag = (!ssor && lu == d->lu.p && d->rdiag.p) ? d->rdiag.p : nullptr;
     const int fill = std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8);
     k_sweep_begin_values<<<fill < 1 ? 1 : fill, kBlock, 0, ctx->stream>>>(d->sweepCtl.p, d->y.p, n);
     SIMALL_LAUNCH_CHECK(ctx);
     auto fwd = ssor ? k_ilu_fwd_free<true> : k_ilu_fwd_free<false>;
-    fwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->invD, d->y.p, d->sweepCtl.p);
+    fwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->fwdRows.p, rowPtr, colIdx, lu, r, d->invD, d->y.p, d->sweepCtl.p,
+                                          backoff);
     SIMALL_LAUNCH_CHECK(ctx);
     k_sweep_begin_values<<<fill < 1 ? 1 : fill, kBlock, 0, ctx->stream>>>(d->sweepCtl.p, z, n);
     SIMALL_LAUNCH_CHECK(ctx);
     auto bwd = ssor ? k_ilu_bwd_free<true> : k_ilu_bwd_free<false>;
-    bwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, d->invD, z,
-                                          d->sweepCtl.p);
+    bwd<<<grid, kBlock, 0, ctx->stream>>>(n, d->bwdRows.p, rowPtr, colIdx, d->diagPtr.p, lu, d->y.p, d->invD, rdiag,
+                                          z, d->sweepCtl.p, backoff);
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
@@ -926,6 +958,15 @@ int simall_gpu_ilu0_factor_inplace(size_t n, const int32_t *rowPtr, const int32_
     }
     delete f;
     return st;
+}
+
+int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns)
+{
+    if (ctas_per_sm < 1 || ctas_per_sm > 8 || backoff_ns < 0 || backoff_ns > 4096)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    g_sweep_ctas_per_sm = ctas_per_sm;
+    g_sweep_backoff_ns = static_cast<unsigned>(backoff_ns);
+    return SIMALL_OK;
 }
 
 int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds)

@@ -25,6 +25,7 @@ struct IluData {
     DevBuf<int32_t> frow, brow, fcol, bcol, fpos, bpos;
     DevBuf<double> fval, bval, bdiag, brdiag;  // refreshed from lu after every factorisation
     DevBuf<double> rpiv;                        // reciprocals of the pivots (factor)
+    DevBuf<double> rdiag;                       // larger systems: RN(1/u_ii) of the factor, for the backward sweep
     // SSOR (w = 1) runs on the same level schedule: no factor, lu holds A's
     // values, the sweeps scale by the inverse diagonal invD (the Jacobi one)
     int mode = 0;                  // 0 ILU(0), 1 SSOR
@@ -100,6 +101,12 @@ inline bool sweep_preconditioner(int pc)
 {
     return pc == SIMALL_PRECOND_ILU0 || pc == SIMALL_PRECOND_SSOR || pc == SIMALL_PRECOND_AMG;
 }
+// Launch shape and polling back-off of the free-running triangular sweeps
+// (ILU(0), SSOR, the AMG smoother's large levels): CTAs per SM of the sweep
+// grid and the longest sleep between polls (ns; 0 = spin).  Process-wide;
+// simall_diagnose_sweep_params changes them for latency measurements.
+extern int g_sweep_ctas_per_sm;
+extern unsigned g_sweep_backoff_ns;
 int ilu_setup(simall_solver *s);  // ILU(0) factor, SSOR's sweep data or the AMG hierarchy (cfg.preconditioner)
 int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);

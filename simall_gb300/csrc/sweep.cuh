@@ -42,11 +42,12 @@ __device__ __forceinline__ bool pending(double v)
 // Polls x[j[q]] for the flagged q until none is pending; v receives the
 // values, 0 for the others.  Bounded: false after kSweepMaxSpins polls.  The
 // first polls are immediate (the rows are usually done or nearly so); later
-// ones back off so that thousands of waiting warps do not flood L2.
+// ones back off, doubling from 16 ns up to max_ns, so that thousands of
+// waiting warps do not flood L2 (max_ns = 0: never sleep).
 __device__ __forceinline__ bool wait_values4(const double *x, const int (&j)[4], const bool (&dep)[4],
-                                             double (&v)[4])
+                                             double (&v)[4], unsigned max_ns = 256)
 {
-    unsigned ns = 16;
+    unsigned ns = 16 < max_ns ? 16 : max_ns;
     for (unsigned spins = 0;; ++spins) {
         bool all = true;
 #pragma unroll
@@ -58,9 +59,9 @@ __device__ __forceinline__ bool wait_values4(const double *x, const int (&j)[4],
             return true;
         if (spins >= kSweepMaxSpins)
             return false;
-        if (spins >= 4) {
+        if (spins >= 4 && max_ns) {
             __nanosleep(ns);
-            ns = ns < 256 ? 2 * ns : 256;
+            ns = 2 * ns < max_ns ? 2 * ns : max_ns;
         }
     }
 }
