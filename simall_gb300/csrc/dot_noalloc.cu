@@ -24,7 +24,12 @@
 //
 // Set-up: the first call on each device, with that device current, looks the
 // array's device address up with cudaGetSymbolAddress and caches it.  Make
-// that first call before any stream capture on the device.
+// that first call before any stream capture on the device.  The cached
+// address lives as long as the device's context: after cudaDeviceReset the
+// library's module is loaded again and the array may move, so a caller that
+// resets a device must not use this function on it afterwards.  A call whose
+// device work fails to start drops the device's cached address, so the next
+// call looks it up again.
 #include "device.cuh"
 
 #include <mutex>
@@ -66,11 +71,12 @@ std::mutex g_setup_mu;
 DotScratch *g_scratch_addr[kMaxDevices] = {};
 
 // Device address of g_dot_scratch on the current device (looked up once).
-int scratch_address(DotScratch **out)
+int scratch_address(DotScratch **out, int *device)
 {
     int dev = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
         return SIMALL_ERR_NO_DEVICE;
+    *device = dev;
     std::lock_guard<std::mutex> lk(g_setup_mu);
     if (!g_scratch_addr[dev]) {
         DotScratch *p = nullptr;
@@ -80,6 +86,13 @@ int scratch_address(DotScratch **out)
     }
     *out = g_scratch_addr[dev];
     return SIMALL_OK;
+}
+
+int drop_scratch_address(int dev)
+{
+    std::lock_guard<std::mutex> lk(g_setup_mu);
+    g_scratch_addr[dev] = nullptr;
+    return SIMALL_ERR_CUDA;
 }
 
 }  // namespace
@@ -95,17 +108,18 @@ extern "C" int simall_gpu_dot_noalloc(const double *x, const double *y, size_t n
         return SIMALL_OK;
     }
     DotScratch *sc = nullptr;
-    const int st = scratch_address(&sc);
+    int dev = 0;
+    const int st = scratch_address(&sc, &dev);
     if (st != SIMALL_OK)
         return st;
     cudaStream_t s = static_cast<cudaStream_t>(stream);
     if (cudaMemsetAsync(&sc->ticket, 0, sizeof(unsigned), s) != cudaSuccess)
-        return SIMALL_ERR_CUDA;
+        return drop_scratch_address(dev);
     const size_t per_block = static_cast<size_t>(simall::kBlock) * kPerThread;
     const int blocks = static_cast<int>((n + per_block - 1) / per_block);
     k_dot_noalloc<<<blocks, simall::kBlock, 0, s>>>(n, x, y, sc);
     if (cudaGetLastError() != cudaSuccess)
-        return SIMALL_ERR_CUDA;
+        return drop_scratch_address(dev);
     if (cudaMemcpyAsync(result, &sc->result, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
         cudaStreamSynchronize(s) != cudaSuccess)
         return SIMALL_ERR_CUDA;

@@ -67,3 +67,31 @@ def test_noalloc_dot_keeps_device_memory_constant_and_rejects_oversize():
     assert free1 == free0
     assert noalloc(x.data_ptr(), x.data_ptr(), MAX_N + 1, None, C.byref(out)) == 8  # SIMALL_ERR_SIZE_MISMATCH
     assert noalloc(x.data_ptr(), x.data_ptr(), 0, None, C.byref(out)) == 0 and out.value == 0.0
+
+
+def test_noalloc_dot_on_a_caller_stream():
+    """The ticket reset, the kernel and the result copy all run on the stream
+    the caller passes: a torch stream other than the default, one call at a
+    time, with the operands written on that stream just before."""
+    torch = pytest.importorskip("torch")
+    import simall_gb300 as sg
+
+    L = sg.load()
+    noalloc = _fn(L)
+    dev = torch.device("cuda:0")
+    side = torch.cuda.Stream(device=dev)
+    n = 3_000_017
+    rng = np.random.default_rng(11)
+    xh, yh = rng.standard_normal(n), rng.standard_normal(n)
+    for k in range(3):
+        with torch.cuda.stream(side):
+            x = torch.from_numpy(xh * (k + 1)).to(dev, non_blocking=False)
+            y = torch.from_numpy(yh).to(dev, non_blocking=False)
+            x.mul_(0.5)  # queued on the side stream right before the call
+        got = C.c_double()
+        assert noalloc(x.data_ptr(), y.data_ptr(), n, C.c_void_p(side.cuda_stream), C.byref(got)) == 0
+        side.synchronize()
+        ref = C.c_double()
+        assert L.simall_gpu_dot(x.data_ptr(), y.data_ptr(), n, None, C.byref(ref)) == 0
+        scale = float(np.abs(0.5 * (k + 1) * xh * yh).sum())
+        assert abs(got.value - ref.value) <= 1e-12 * scale, (k, got.value, ref.value)
