@@ -49,10 +49,26 @@ sys.path.insert(0, ROOT)
 
 METRIC = "PCG time to 1e-8 rel-res, mixed vs plain FP64 on 1 GB300; SpMV HBM GB/s"
 SEED = 42
-# FP64 Jacobi-PCG iteration count of the seeded system above, by side length
-# (the device FP64 solve reproduces CGSolver's count; recorded from this
-# benchmark's own FP64 leg).  The reference leg scales its bounded sample by it.
-FP64_ITERATIONS = {64: 521, 256: 1865}
+
+
+def reference_iterations(n: int):
+    """CGSolver::solve's Jacobi iteration count on the n^3 workload to 1e-8, as
+    the reference itself ran it (tests/golden/varcoef_256_cg.npz, written by
+    tests/golden/make_golden.py from the compiled reference); None for sizes
+    without such a run.  The reference arm scales its bounded sample by it."""
+    try:
+        fx = np.load(os.path.join(ROOT, "tests", "golden", "varcoef_256_cg.npz"))
+    except OSError:
+        return None
+    return int(fx["jacobi_iters"]) if int(fx["n"]) == n else None
+
+
+def host_cores() -> int:
+    try:
+        return len(os.sched_getaffinity(0))
+    except (AttributeError, OSError):
+        return os.cpu_count() or 1
+
 # DRAM bytes (read + write) per row of one launch of the fused mixed step, from
 # one ncu capture at 200^3 (profiles/mixed_step_varcoef200.md: 255.99 MB read +
 # 99.92 MB written for 8,000,000 rows); scaled by the rows of the workload.
@@ -80,7 +96,7 @@ def parse():
     ap.add_argument("--precond-n", type=int, default=64,
                     help="box side of the preconditioner / Krylov-kind leg (0 disables it)")
     ap.add_argument("--no-cavity", action="store_true", help="skip the 128x128 cavity pressure-step leg")
-    ap.add_argument("--simple-iterations", type=int, default=20,
+    ap.add_argument("--simple-iterations", type=int, default=200,
                     help="outer iterations of the device SIMPLE leg (0 disables it)")
     ap.add_argument("--simple-only", action="store_true",
                     help="run only the device SIMPLE leg and print its JSON (profiling runs)")
@@ -474,7 +490,7 @@ def run_preconditioners(a, ctx, sg, with_cpu):
             t = time.perf_counter()
             _, it, _ = O.cg(rp_h, ci_h, vals_h, rhs_h, pc, a.tol, 2000)
             cpu[name] = {"value": round(time.perf_counter() - t, 3), "unit": "s", "iterations": int(it)}
-        res["cpu_baseline"] = {"cores": 1, "kind": "port", "solves": cpu,
+        res["cpu_baseline"] = {"cores": 1, "host_nproc": host_cores(), "kind": "port", "solves": cpu,
                                "sample": "the oracle's CGSolver::solve (setup included) on 1 host core; AMG is not "
                                          "timed on the CPU: the reference's setup rescans all rows for every C "
                                          "point (O(n^2))"}
@@ -533,7 +549,7 @@ def run_cavity(a, ctx, sg, with_cpu):
             t = time.perf_counter()
             O.cg(rp, ci, v, rhs, 0, 1e-8, 1000)
             ts.append(time.perf_counter() - t)
-        res["cpu_baseline"] = {"value": round(ts[0] + (n_outer - 1) * ts[1], 3), "unit": "s", "cores": 1,
+        res["cpu_baseline"] = {"value": round(ts[0] + (n_outer - 1) * ts[1], 3), "unit": "s", "cores": 1, "host_nproc": host_cores(),
                                "kind": "port", "sample": "one CG solve of each of the two systems on 1 host core, "
                                                          f"scaled to {n_outer} solves (solve only)"}
     return res
@@ -593,7 +609,7 @@ def run_pressure_step(a, ctx, sg, with_cpu):
         O.correct_fields(om, 1.0, 0.3, aP.cpu().numpy(), pp.cpu().numpy(), np.zeros(nC), Uh, ph)
         t2 = time.perf_counter()
         res["cpu_baseline"] = {"fluxes_ms": round((t1 - t) * 1e3, 1), "correct_ms": round((t2 - t1) * 1e3, 1),
-                               "cores": 1, "kind": "port"}
+                               "cores": 1, "host_nproc": host_cores(), "kind": "port"}
     s.close()
     ps.close()
     return res
@@ -609,9 +625,11 @@ def run_simple(a, ctx, sg, with_cpu):
     cavity (Re 100, urfU 0.7, urfP 0.3) from rest, with the reference's
     solver settings (GMRES(30)+ILU(0) momentum to 1e-6, FP64 Jacobi-CG
     pressure to 1e-8) and with GMRES(30)+Jacobi momentum and mixed-precision
-    pressure; seconds per outer iteration over the first `simple_iterations`
-    iterations, against the oracle's restatement of SimpleAlgorithm::iterate
-    on one host core."""
+    pressure; seconds per outer iteration over `simple_iterations` outer
+    iterations from rest (default 200: the cavity configuration as written,
+    applications/simall_cavity/main.cpp), against the oracle's restatement of
+    SimpleAlgorithm::iterate run for the same iterations on one host core, and
+    the fields of both device runs against the oracle's after the last one."""
     from oracle import oracle as O  # the parity check and the CPU baseline only
 
     N = 128
@@ -633,6 +651,7 @@ def run_simple(a, ctx, sg, with_cpu):
         alg = sg.GpuSimpleAlgorithm(m, CAVITY_SIMPLE_BCS, mom, pres, sg.SimpleOptions(mu=0.01), ctx=ctx)
         return alg, mom, pres
 
+    fields = {}
     for name, cfg in configs.items():
         alg, mom, pres = make(cfg)
         for _ in range(2):  # warm: preconditioner analysis, graph capture
@@ -647,34 +666,36 @@ def run_simple(a, ctx, sg, with_cpu):
             its += np.array(r.iterations)
         ctx.synchronize()
         sec = (time.perf_counter() - t0) / n_it
-        res[name] = {"value": round(sec, 6), "unit": "s per outer iteration",
+        res[name] = {"value": round(sec, 6), "unit": "s per outer iteration", "total_s": round(sec * n_it, 4),
                      "momentum": f"GMRES({cfg[0][4]})+{'ILU(0)' if cfg[0][1] == 1 else 'Jacobi'} to {cfg[0][2]:g}",
                      "pressure": f"{'mixed' if cfg[2] == sg.Precision.MIXED else 'FP64'} Jacobi-CG to {cfg[1][2]:g}",
                      "solve_iterations_per_outer": [round(float(v) / n_it, 1) for v in its]}
+        fields[name] = alg.fields()
         alg.close()
         mom.close()
         pres.close()
-    # parity: five iterations from rest against the oracle's (reference settings)
-    alg, mom, pres = make(configs["reference_settings"])
+    # parity: the oracle's SimpleAlgorithm::iterate (reference settings) for the
+    # same outer iterations from rest; its time on one host core is the CPU
+    # baseline (the whole run, as the cavity configuration is written)
     om = O.cartesian_mesh(N, N, 1, 1.0, 1.0, 1.0 / N)
     so = O.SimpleOracle(om, CAVITY_SIMPLE_BCS, mu=0.01, mom_cfg=configs["reference_settings"][0],
                         p_cfg=configs["reference_settings"][1])
     t = time.perf_counter()
-    for _ in range(5):
-        alg.iterate()
-    for _ in range(5):
+    for _ in range(n_it):
         so.iterate()
-    cpu_s = (time.perf_counter() - t) / 5
-    U, p, _ = alg.fields()
-    res["parity_5_iterations"] = {"rel_U": float(np.linalg.norm(U - so.U) / np.linalg.norm(so.U)),
-                                  "rel_p": float(np.linalg.norm(p - so.p) / np.linalg.norm(so.p))}
+    cpu_s = (time.perf_counter() - t) / n_it
+    U, p, _ = fields["reference_settings"]
+    Um, pm, _ = fields["gb300_settings"]
+    res[f"parity_{n_it}_iterations"] = {
+        "reference_settings": {"rel_U": float(np.linalg.norm(U - so.U) / np.linalg.norm(so.U)),
+                               "rel_p": float(np.linalg.norm(p - so.p) / np.linalg.norm(so.p))},
+        "gb300_settings": {"rel_U": float(np.linalg.norm(Um - so.U) / np.linalg.norm(so.U)),
+                           "rel_p": float(np.linalg.norm(pm - so.p) / np.linalg.norm(so.p))}}
     if with_cpu:
-        res["cpu_baseline"] = {"value": round(cpu_s, 4), "unit": "s per outer iteration", "cores": 1, "kind": "port",
-                               "sample": "the oracle's SimpleAlgorithm::iterate, reference settings, the first 5 "
+        res["cpu_baseline"] = {"value": round(cpu_s, 4), "unit": "s per outer iteration", "cores": 1,
+                               "host_nproc": host_cores(), "kind": "port", "total_s": round(cpu_s * n_it, 2),
+                               "sample": f"the oracle's SimpleAlgorithm::iterate, reference settings, all {n_it} "
                                          "outer iterations from rest on 1 host core"}
-    alg.close()
-    mom.close()
-    pres.close()
     return res
 
 
@@ -760,7 +781,7 @@ def run_state(a, ctx, sg, with_cpu):
         t = time.perf_counter()
         so.step()
         simp_res["cpu_baseline"] = {"value": round(time.perf_counter() - t, 4), "unit": "s per design step",
-                                    "cores": 1, "kind": "port", "sample": "no filter, one step"}
+                                    "cores": 1, "host_nproc": host_cores(), "kind": "port", "sample": "no filter, one step"}
     res["simp"] = simp_res
     return res
 
@@ -941,10 +962,14 @@ def run_ours(a, rank, world, local):
         out["state"] = run_state(a, ctx, sg, rank == 0 and world == 1 and not a.no_cpu_baseline)
     if rank == 0 and world == 1 and not a.no_cpu_baseline:
         per_it, k, kind = cpu_cg_sample(rp, ci, vals, rhs, a.cpu_seconds, use_ref=True)
-        out["cpu_baseline"] = {"value": round(per_it * fp64_iters, 3), "unit": "s", "cores": 1, "kind": kind,
+        ref_iters = reference_iterations(a.n)
+        iters = ref_iters or int(fp64_iters)
+        out["cpu_baseline"] = {"value": round(per_it * iters, 3), "unit": "s", "cores": 1,
+                               "host_nproc": host_cores(), "kind": kind,
                                "sample": f"{k} FP64 Jacobi-CG iterations of this {a.n}^3 system on 1 host core "
-                                         f"({per_it * 1e3:.1f} ms/iteration), scaled to the {fp64_iters} iterations "
-                                         f"of the full solve"}
+                                         f"({per_it * 1e3:.1f} ms/iteration), scaled to the {iters} iterations "
+                                         + ("of the reference's own full solve of it" if ref_iters else
+                                            "of the device FP64 solve (no reference count at this size)")}
     if rank == 0:
         print(json.dumps(out), flush=True)
     if world > 1:
@@ -952,8 +977,14 @@ def run_ours(a, rank, world, local):
 
 
 def run_reference(a, rank, world):
-    """The reference CG on the host: compiled reference if present, else the
-    oracle's restatement; bounded samples scaled to the full iteration count."""
+    """The reference CG (CGSolver::solve, Jacobi, 1 core -- it is serial) on the
+    host: the compiled reference if present, else the oracle's bit-identical
+    restatement.  Each step times a bounded number of iterations of the same
+    system; the solve time is that per-iteration time times the reference's own
+    iteration count: from its full solve of the 256^3 system
+    (tests/golden/varcoef_256_cg.npz), or, for sides up to 64, from a full CG
+    run here.  For other sizes no solve time is reported (value null), only the
+    per-iteration time."""
     if rank != 0:
         return
     from oracle import oracle as O
@@ -962,12 +993,19 @@ def run_reference(a, rank, world):
     # input system: the oracle's own mesh, sparsity and assembly
     m = O.cartesian_mesh(a.n, a.n, a.n)
     rng = np.random.default_rng(SEED + 2)
-    k = np.exp(rng.standard_normal(m.nC))
+    k = W.portable_exp(rng.standard_normal(m.nC))
     rhs = rng.standard_normal(m.nC)
     rp, ci = O.build_sparsity(m)
     v, _, _ = O.assemble(m, rp, ci, [1], 1.0, 1.0 / k, np.zeros(m.nF))
     del m
-    iters = FP64_ITERATIONS.get(a.n)
+    iters = reference_iterations(a.n)
+    count_source = "the reference's own full solve of this system" if iters else None
+    if iters is None and a.n <= 64:
+        if O.RefLib.available():
+            _, iters, _, _ = O.RefLib().cg(rp, ci, v, rhs, 0, a.tol, a.max_iterations)
+        else:
+            _, iters, _ = O.cg(rp, ci, v, rhs, 0, a.tol, a.max_iterations)
+        count_source = "a full CG run of this system here"
     per = []
     kind = "port"
     for i in range(a.warmup + a.steps):
@@ -975,18 +1013,20 @@ def run_reference(a, rank, world):
         if i >= a.warmup:
             per.append(t)
     per_it = float(np.mean(per))
-    scale = iters if iters else 1
-    val = per_it * scale
+    val = round(per_it * iters, 3) if iters else None
     sample = (f"{kk} FP64 Jacobi-CG iterations per step on 1 host core ({per_it * 1e3:.1f} ms/iteration), "
-              + (f"scaled to the {iters} iterations of the full solve" if iters else "not scaled (per iteration)"))
-    print(json.dumps({"impl": "reference", "metric": METRIC, "value": round(val, 3), "unit": "s", "n_gpus": world,
-                      "steps": a.steps, "warmup": a.warmup, "ms_per_step": round(per_it * kk * 1e3, 1),
+              + (f"scaled to the {iters} iterations of {count_source}" if iters
+                 else "no reference iteration count for this size: per-iteration time only"))
+    print(json.dumps({"impl": "reference", "metric": METRIC, "value": val, "unit": "s", "n_gpus": world,
+                      "steps": a.steps, "warmup": a.warmup,
+                      "ms_per_step": round(per_it * iters * 1e3, 1) if iters else None,
+                      "ms_per_iteration": round(per_it * 1e3, 3), "reference_iterations": iters,
                       "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                       "data": "synthetic (seeded)",
                       "config": {"workload": f"varcoef Poisson {a.n}^3, Jacobi-PCG to {a.tol:g}", "seed": SEED},
-                      "cpu_baseline": {"value": round(val, 3), "unit": "s", "cores": 1, "kind": kind,
-                                       "sample": sample},
-                      "e2e": {"value": round(val, 3), "unit": "s", "h2d_bytes_per_step": 0,
+                      "cpu_baseline": {"value": val, "unit": "s", "cores": 1, "host_nproc": host_cores(),
+                                       "kind": kind, "sample": sample},
+                      "e2e": {"value": val, "unit": "s", "h2d_bytes_per_step": 0,
                               "d2h_bytes_per_step": 0}}), flush=True)
 
 
