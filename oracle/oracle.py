@@ -55,9 +55,9 @@ def lib():
         L.orc_rcm.restype = None
         L.orc_rcm.argtypes = [_I64, _I64] + [_P] * 10
         L.orc_build_sparsity.restype = _I64
-        L.orc_build_sparsity.argtypes = [_I64, _P, _P, _P, _P, _P, _P]
+        L.orc_build_sparsity.argtypes = [_I64, _P, _P, _P, _P, _P, _P, _P]
         L.orc_face_fluxes.restype = None
-        L.orc_face_fluxes.argtypes = [_I64] + [_P] * 6 + [_P, _P, C.c_int, _D] + [_P] * 4
+        L.orc_face_fluxes.argtypes = [_I64] + [_P] * 6 + [_P, _P, C.c_int, _D] + [_P] * 5
         L.orc_lsq_inverse.restype = None
         L.orc_lsq_inverse.argtypes = [_I64, _I64] + [_P] * 9
         L.orc_lsq_gradient.restype = None
@@ -67,7 +67,7 @@ def lib():
         L.orc_simplec_denominator.restype = None
         L.orc_simplec_denominator.argtypes = [_I64] + [_P] * 5
         L.orc_assemble.restype = C.c_int
-        L.orc_assemble.argtypes = [_I64, _I64] + [_P] * 13 + [C.c_int, _D] + [_P] * 6
+        L.orc_assemble.argtypes = [_I64, _I64] + [_P] * 13 + [C.c_int, _D] + [_P] * 7
         L.orc_dot.restype = _D
         L.orc_dot.argtypes = [_I64, _P, _P]
         L.orc_spmv.restype = None
@@ -86,7 +86,7 @@ def lib():
         L.orc_face_k_gradient.argtypes = [_I64] + [_P] * 10
         L.orc_assemble_momentum.restype = None
         L.orc_assemble_momentum.argtypes = [_I64, _I64] + [_P] * 15 + [C.c_int] + [_P] * 3 + [C.c_int, C.c_int] + \
-            [_P] * 8
+            [_P] * 8 + [_P]
         L.orc_bicgstab.restype = C.c_int
         L.orc_bicgstab.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, _P, _P]
         L.orc_gmres.restype = C.c_int
@@ -103,9 +103,11 @@ def lib():
         L.orc_gmres.argtypes = [_I64, _P, _P, _P, _P, C.c_int, _D, C.c_int, C.c_int, _P, _P]
         L.orc_simple_iterate.restype = C.c_int
         L.orc_simple_iterate.argtypes = [_I64, _I64] + [_P] * 16 + [C.c_int] + [_P] * 3 + [C.c_int, _P, _D, _P, _D] + \
-            [_P] * 11
+            [_P] * 11 + [_P]
         L.orc_simp_step.restype = _D
         L.orc_simp_step.argtypes = [_I64, _I64] + [_P] * 17
+        L.orc_periodic_pairs.restype = None
+        L.orc_periodic_pairs.argtypes = [_I64, _P, _P, _P, _P, _P, C.c_int, _P, _P]
         L.orc_gpu_ilu0_factor.restype = C.c_int
         L.orc_gpu_ilu0_factor.argtypes = [_I64, _P, _P, _P]
         L.orc_cggpu_solve.restype = None
@@ -206,14 +208,34 @@ def rcm(m: Mesh):
     return newPos, tuple(int(s) for s in stats)
 
 
-def build_sparsity(m: Mesh):
+PERIODIC = 11  # BCType::Periodic (src/solver/Solver.hpp:105-123)
+
+
+def periodic_pairs(m: Mesh, bcs):
+    """SimpleAlgorithm::build_periodic_pairs (SimpleAlgorithm.cpp:101-186):
+    twin[nF] (-1 where none); the periodic zones are those of the Periodic
+    specs in bcs, in order."""
+    zones = np.array([int(b[0]) for b in bcs if int(b[1]) == PERIODIC] or [0], np.uint32)
+    nP = sum(1 for b in bcs if int(b[1]) == PERIODIC)
+    twin = np.empty(m.nF, np.int32)
+    lib().orc_periodic_pairs(m.nF, _ptr(m.neighbor), _ptr(m.zone), _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), nP,
+                             _ptr(zones), _ptr(twin))
+    return twin
+
+
+def _twin(twin):
+    return None if twin is None else np.ascontiguousarray(twin, np.int32)
+
+
+def build_sparsity(m: Mesh, twin=None):
     L = lib()
     rowPtr = np.empty(m.nC + 1, np.int32)
+    tw = _twin(twin)
     nnz = L.orc_build_sparsity(m.nC, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.cfOff), _ptr(m.cfIdx),
-                               _ptr(rowPtr), None)
+                               _ptr(rowPtr), None, _ptr(tw))
     colIdx = np.empty(nnz, np.int32)
     L.orc_build_sparsity(m.nC, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.cfOff), _ptr(m.cfIdx), _ptr(rowPtr),
-                         _ptr(colIdx))
+                         _ptr(colIdx), _ptr(tw))
     return rowPtr, colIdx
 
 
@@ -232,13 +254,14 @@ def _zone_tables(bcs):
     return nZ, zt, zv
 
 
-def face_fluxes(m: Mesh, bcs, rho, U):
+def face_fluxes(m: Mesh, bcs, rho, U, twin=None):
     """compute_face_fluxes (SimpleAlgorithm.cpp:201-237); U = (Ux, Uy, Uz)."""
     nZ, zt, zv = _zone_tables(bcs)
     phi = np.empty(m.nF)
     Ux, Uy, Uz = (np.ascontiguousarray(u, np.float64) for u in U)
     lib().orc_face_fluxes(m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az), _ptr(m.zone),
-                          _ptr(zt), _ptr(zv), nZ, float(rho), _ptr(Ux), _ptr(Uy), _ptr(Uz), _ptr(phi))
+                          _ptr(zt), _ptr(zv), nZ, float(rho), _ptr(Ux), _ptr(Uy), _ptr(Uz), _ptr(phi),
+                          _ptr(_twin(twin)))
     return phi
 
 
@@ -279,7 +302,7 @@ def simplec_denominator(rowPtr, colIdx, mom, aP):
     return den
 
 
-def assemble(m: Mesh, rowPtr, colIdx, pressure_zones, rho, aP, phi):
+def assemble(m: Mesh, rowPtr, colIdx, pressure_zones, rho, aP, phi, twin=None):
     """assemble_pressure_correction; pressure_zones = zone ids with a
     PressureOutlet/PressureInlet condition.  Returns (values, rhs, anyDirichlet)."""
     L = lib()
@@ -294,7 +317,7 @@ def assemble(m: Mesh, rowPtr, colIdx, pressure_zones, rho, aP, phi):
     anyD = L.orc_assemble(m.nC, m.nF, _ptr(m.owner), _ptr(m.neighbor), _ptr(m.ax), _ptr(m.ay), _ptr(m.az),
                           _ptr(m.fcx), _ptr(m.fcy), _ptr(m.fcz), _ptr(m.zone), _ptr(m.ccx), _ptr(m.ccy),
                           _ptr(m.ccz), _ptr(isP), nZ, rho, _ptr(aP), _ptr(phi), _ptr(rowPtr), _ptr(colIdx),
-                          _ptr(values), _ptr(rhs))
+                          _ptr(values), _ptr(rhs), _ptr(_twin(twin)))
     return values, rhs, bool(anyD)
 
 
@@ -327,7 +350,8 @@ def face_k_gradient(m: Mesh, is_dirichlet_face, g, k, pb, x, lam):
 # ---------------------------------------------------------------- linear algebra
 
 
-def assemble_momentum(m: Mesh, rowPtr, colIdx, bcs, opt, comp, phi, gp, Ucomp, Un=None, Unm1=None, bdf2=False):
+def assemble_momentum(m: Mesh, rowPtr, colIdx, bcs, opt, comp, phi, gp, Ucomp, Un=None, Unm1=None, bdf2=False,
+                      twin=None):
     """assemble_momentum (SimpleAlgorithm.cpp:240-355) for component comp;
     bcs as face_fluxes, opt = (rho, mu, urfU, dt), gp = that component of the
     pressure gradient.  Returns (values, rhs, relaxed diagonal)."""
@@ -344,7 +368,7 @@ def assemble_momentum(m: Mesh, rowPtr, colIdx, bcs, opt, comp, phi, gp, Ucomp, U
                                 _ptr(np.ascontiguousarray(rowPtr, np.int32)),
                                 _ptr(np.ascontiguousarray(colIdx, np.int32)),
                                 _ptr(np.ascontiguousarray(opt, np.float64)), int(bool(bdf2)), int(comp),
-                                *(_ptr(v) for v in a), _ptr(values), _ptr(rhs), _ptr(aP))
+                                *(_ptr(v) for v in a), _ptr(values), _ptr(rhs), _ptr(aP), _ptr(_twin(twin)))
     return values, rhs, aP
 
 
@@ -466,7 +490,9 @@ class SimpleOracle:
         for b in bcs:
             if int(b[1]) in (5, 7) and self.zt[int(b[0])] == int(b[1]):
                 self.isP[int(b[0])] = 1
-        self.rp, self.ci = build_sparsity(m)
+        # periodic twins (build_sparsity pairs them first, SimpleAlgorithm.cpp:54-56)
+        self.twin = periodic_pairs(m, bcs) if any(int(b[1]) == PERIODIC for b in bcs) else None
+        self.rp, self.ci = build_sparsity(m, self.twin)
         self.opt = np.array([rho, mu, urfU, urfP, dt], np.float64)
         self.bdf2, self.simplec = bool(bdf2), bool(simplec)
         self.mom_cfg = mom_cfg
@@ -501,7 +527,7 @@ class SimpleOracle:
                                  float(self.mom_cfg[2]), _ptr(pc), float(self.p_cfg[2]), _ptr(self.loops),
                                  _ptr(self.tol_up), _ptr(self.U), _ptr(self.p),
                                  _ptr(self.Un), _ptr(self.Unm1), _ptr(self.phi), _ptr(self.aP), _ptr(self.pPrime),
-                                 _ptr(res), _ptr(its))
+                                 _ptr(res), _ptr(its), _ptr(self.twin))
         self.iters.append(its)
         return res, its
 
@@ -608,7 +634,7 @@ class RefLib:
         L.ref_mesh_get_cells.argtypes = [_P] * 7
         L.ref_mesh_rcm.argtypes = [_P, _P]
         L.ref_sparsity_nnz.restype = _I64
-        L.ref_sparsity_nnz.argtypes = [_P]
+        L.ref_sparsity_nnz.argtypes = [_P, C.c_int, _P, _P]
         L.ref_assemble.restype = C.c_int
         L.ref_assemble.argtypes = [_P, C.c_int, _P, _P, _D] + [_P] * 6
         L.ref_face_fluxes.restype = C.c_int
@@ -646,6 +672,8 @@ class RefLib:
         L.ref_piso_pimple_run.restype = C.c_int
         L.ref_piso_pimple_run.argtypes = [_P, C.c_int, C.c_int, _P, _P, _P, _P, _P, C.c_int, _P, _D, _P, _D,
                                           C.c_int] + [_P] * 5
+        L.ref_periodic_twins.restype = C.c_int
+        L.ref_periodic_twins.argtypes = [_P, C.c_int, _P, _P, _P]
         L.ref_cggpu_solve.restype = C.c_int
         L.ref_cggpu_solve.argtypes = [C.c_int, _D, C.c_int, _D, C.c_int] + [_P] * 8
         L.ref_discrete_adjoint.restype = C.c_int
@@ -718,14 +746,22 @@ class RefLib:
             self.L.ref_mesh_free(mesh_dict["handle"])
             mesh_dict["handle"] = None
 
+    def periodic_twins(self, mesh_dict, bcs):
+        """build_periodic_pairs' twin table (-1 where none)."""
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        twin = np.empty(mesh_dict["nF"], np.int32)
+        self.L.ref_periodic_twins(mesh_dict["handle"], len(bcs), _ptr(zones), _ptr(types), _ptr(twin))
+        return twin
+
     def assemble(self, mesh_dict, bcs, rho, aP, phi):
         """bcs: list of (zone, BCType ordinal).  Returns rowPtr, colIdx, values, rhs."""
         L = self.L
         h = mesh_dict["handle"]
-        nnz = L.ref_sparsity_nnz(h)
         nC = mesh_dict["nC"]
-        zones = np.array([z for z, _ in bcs] or [0], np.uint32)
-        types = np.array([t for _, t in bcs] or [0], np.int32)
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        nnz = L.ref_sparsity_nnz(h, len(bcs), _ptr(zones), _ptr(types))
         rowPtr = np.empty(nC + 1, np.int32)
         colIdx = np.empty(nnz, np.int32)
         values = np.empty(nnz)
@@ -768,10 +804,10 @@ class RefLib:
         momentum matrix A_mom_ given by its values on the shared pattern."""
         L = self.L
         h = mesh_dict["handle"]
-        nnz = L.ref_sparsity_nnz(h)
         nC = mesh_dict["nC"]
-        zones = np.array([z for z, _ in bcs] or [0], np.uint32)
-        types = np.array([t for _, t in bcs] or [0], np.int32)
+        zones = np.array([b[0] for b in bcs] or [0], np.uint32)
+        types = np.array([b[1] for b in bcs] or [0], np.int32)
+        nnz = L.ref_sparsity_nnz(h, len(bcs), _ptr(zones), _ptr(types))
         rowPtr = np.empty(nC + 1, np.int32)
         colIdx = np.empty(nnz, np.int32)
         values = np.empty(nnz)
@@ -785,10 +821,10 @@ class RefLib:
         """SimpleAlgorithm::assemble_momentum(comp); returns (values, rhs, aP_)."""
         L = self.L
         h = mesh_dict["handle"]
-        nnz = L.ref_sparsity_nnz(h)
         nC = mesh_dict["nC"]
         zones = np.array([b[0] for b in bcs] or [0], np.uint32)
         types = np.array([b[1] for b in bcs] or [0], np.int32)
+        nnz = L.ref_sparsity_nnz(h, len(bcs), _ptr(zones), _ptr(types))
         vec = np.array([list(b[2]) if len(b) > 2 else [0, 0, 0] for b in bcs] or [[0, 0, 0]], np.float64).ravel()
         U3 = np.ascontiguousarray(np.asarray(U, np.float64).reshape(3, nC))
         z3 = np.zeros((3, nC))

@@ -60,6 +60,7 @@ class AssemblyProbe : public S::SimpleAlgorithm
 public:
     using S::SimpleAlgorithm::SimpleAlgorithm;
     void sparsity() { build_sparsity(); }
+    const std::vector<int>& twins() const { return periodicTwin_; }
     void assemble(const double* aP, const double* phi)
     {
         build_sparsity();
@@ -78,9 +79,11 @@ public:
         A_mom_.values.assign(mom, mom + A_mom_.colIdx.size());
         assemble_pressure_correction();
     }
-    // compute_face_fluxes with the given cell velocities
+    // compute_face_fluxes with the given cell velocities (after build_sparsity,
+    // as iterate() runs it first: it also pairs the periodic faces)
     void fluxes(const double* Ux, const double* Uy, const double* Uz)
     {
+        build_sparsity();
         const std::size_t nC = mesh_.cells().size();
         auto& U = F_.vector("U", nC);
         U.x.assign(Ux, Ux + nC);
@@ -295,11 +298,11 @@ void ref_mesh_rcm(void* h, std::int64_t* out)
 }
 
 // ------------------------------------------------------------------ assembly
-std::int64_t ref_sparsity_nnz(void* h)
+std::int64_t ref_sparsity_nnz(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes)
 {
     auto& m = static_cast<RefMesh*>(h)->mesh;
     S::FieldRegistry f;
-    std::vector<S::BoundarySpec> bcs;
+    auto bcs = make_bcs(nbc, bcZones, bcTypes);  // periodic specs add twin columns
     S::LinearSolverConfig c;
     auto s1 = S::make_cg(c), s2 = S::make_cg(c);
     AssemblyProbe p(m, f, bcs, *s1, *s2, S::SimpleOptions{});
@@ -325,6 +328,24 @@ int ref_assemble(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTy
     std::copy(A.colIdx.begin(), A.colIdx.end(), colIdx);
     std::copy(A.values.begin(), A.values.end(), values);
     std::copy(p.rhs().begin(), p.rhs().end(), rhs);
+    return 0;
+}
+
+// SimpleAlgorithm::build_periodic_pairs (SimpleAlgorithm.cpp:101-186) through
+// build_sparsity: twin[nF], -1 where a face has no periodic partner.
+int ref_periodic_twins(void* h, int nbc, const std::uint32_t* bcZones, const int* bcTypes, std::int32_t* twin)
+{
+    auto& m = static_cast<RefMesh*>(h)->mesh;
+    S::FieldRegistry f;
+    auto bcs = make_bcs(nbc, bcZones, bcTypes);
+    S::LinearSolverConfig c;
+    auto s1 = S::make_cg(c), s2 = S::make_cg(c);
+    AssemblyProbe p(m, f, bcs, *s1, *s2, S::SimpleOptions{});
+    p.sparsity();
+    const auto& t = p.twins();
+    const std::size_t nF = m.faces().size();
+    for (std::size_t i = 0; i < nF; ++i)
+        twin[i] = t.empty() ? -1 : t[i];
     return 0;
 }
 

@@ -17,6 +17,7 @@
  * Index conventions: cell ids are int64, a boundary face has neighbor == -1
  * (the reference's kBoundaryCell = ~0ull, src/meshing/MeshStorage.hpp:35).
  */
+#include <float.h>
 #include <math.h>
 #include <stdint.h>
 #include <stdlib.h>
@@ -428,8 +429,92 @@ void orc_rcm(int64_t nC, int64_t nF, int64_t *owner, int64_t *neighbor, double *
  * c's faces that is not a boundary}.  With colIdx == NULL only rowPtr is
  * filled; returns nnz.
  */
+/* SimpleAlgorithm::build_periodic_pairs (src/solver/SimpleAlgorithm.cpp:101-186):
+ * periodicZones[0..nP) are the zones of the Periodic boundary specs in spec
+ * order (duplicates kept; a face joins the first listed entry of its zone).
+ * Boundary faces are grouped by that entry in face order; entries are paired
+ * (0,1), (2,3), ...; the translation is mean(B) - mean(A) of the face
+ * centroids (sums in face order, times 1/size); each face of A, in order,
+ * takes the face of B whose centroid is nearest to its own plus the
+ * translation (squared distance, first minimum in B's order), and
+ * twin[a] = b, twin[b] = a -- a later face of A choosing the same b rewrites
+ * twin[b].  twin[f] = -1 elsewhere (fewer than two periodic entries: all). */
+void orc_periodic_pairs(int64_t nF, const int64_t *neighbor, const uint32_t *zone, const double *fcx,
+                        const double *fcy, const double *fcz, int nP, const uint32_t *periodicZones, int32_t *twin)
+{
+    for (int64_t f = 0; f < nF; ++f)
+        twin[f] = -1;
+    if (nP < 2)
+        return;
+    int64_t *cnt = (int64_t *)calloc((size_t)nP + 1, sizeof(int64_t));
+    int32_t *grp = (int32_t *)xmalloc((size_t)nF * sizeof(int32_t) + 8);
+    for (int64_t f = 0; f < nF; ++f) {
+        grp[f] = -1;
+        if (neighbor[f] != ORC_BOUNDARY)
+            continue;
+        for (int i = 0; i < nP; ++i)
+            if (periodicZones[i] == zone[f]) {
+                grp[f] = i;
+                cnt[i + 1]++;
+                break;
+            }
+    }
+    for (int i = 0; i < nP; ++i)
+        cnt[i + 1] += cnt[i];
+    int64_t *list = (int64_t *)xmalloc((size_t)(cnt[nP] + 1) * sizeof(int64_t));
+    int64_t *fill = (int64_t *)xmalloc((size_t)(nP + 1) * sizeof(int64_t));
+    for (int i = 0; i <= nP; ++i)
+        fill[i] = cnt[i];
+    for (int64_t f = 0; f < nF; ++f)
+        if (grp[f] >= 0)
+            list[fill[grp[f]]++] = f;
+    for (int z = 0; z + 1 < nP; z += 2) {
+        const int64_t *A = list + cnt[z], *B = list + cnt[z + 1];
+        const int64_t nA = cnt[z + 1] - cnt[z], nB = cnt[z + 2] - cnt[z + 1];
+        if (nA == 0 || nB == 0)
+            continue;
+        double Ax = 0, Ay = 0, Az = 0, Bx = 0, By = 0, Bz = 0;
+        for (int64_t i = 0; i < nA; ++i) {
+            Ax += fcx[A[i]];
+            Ay += fcy[A[i]];
+            Az += fcz[A[i]];
+        }
+        for (int64_t i = 0; i < nB; ++i) {
+            Bx += fcx[B[i]];
+            By += fcy[B[i]];
+            Bz += fcz[B[i]];
+        }
+        const double invA = 1.0 / (double)nA, invB = 1.0 / (double)nB;
+        const double tx = Bx * invB - Ax * invA, ty = By * invB - Ay * invA, tz = Bz * invB - Az * invA;
+        for (int64_t i = 0; i < nA; ++i) {
+            const int64_t fa = A[i];
+            int64_t best = -1;
+            double bestd2 = DBL_MAX;
+            const double ax = fcx[fa] + tx, ay = fcy[fa] + ty, az = fcz[fa] + tz;
+            for (int64_t j = 0; j < nB; ++j) {
+                const int64_t fb = B[j];
+                const double d2 = (fcx[fb] - ax) * (fcx[fb] - ax) + (fcy[fb] - ay) * (fcy[fb] - ay) +
+                                  (fcz[fb] - az) * (fcz[fb] - az);
+                if (d2 < bestd2) {
+                    bestd2 = d2;
+                    best = fb;
+                }
+            }
+            if (best >= 0) {
+                twin[fa] = (int32_t)best;
+                twin[best] = (int32_t)fa;
+            }
+        }
+    }
+    free(cnt);
+    free(grp);
+    free(list);
+    free(fill);
+}
+
 int64_t orc_build_sparsity(int64_t nC, const int64_t *owner, const int64_t *neighbor,
-                           const int32_t *cfOff, const int64_t *cfIdx, int32_t *rowPtr, int32_t *colIdx)
+                           const int32_t *cfOff, const int64_t *cfIdx, int32_t *rowPtr, int32_t *colIdx,
+                           const int32_t *twin)
 {
     int64_t nnz = 0;
     int64_t buf[64];
@@ -440,8 +525,12 @@ int64_t orc_build_sparsity(int64_t nC, const int64_t *owner, const int64_t *neig
         for (int32_t t = cfOff[c]; t < cfOff[c + 1]; ++t) {
             const int64_t f = cfIdx[t];
             const int64_t oth = (owner[f] == c) ? neighbor[f] : owner[f];
-            if (oth != ORC_BOUNDARY && m < 64)
-                buf[m++] = oth;
+            if (oth != ORC_BOUNDARY) {
+                if (m < 64)
+                    buf[m++] = oth;
+            } else if (twin && twin[f] >= 0 && m < 64) {  /* periodic: the twin face's owner (:71-72) */
+                buf[m++] = owner[twin[f]];
+            }
         }
         for (int i = 1; i < m; ++i) {
             const int64_t v = buf[i];
@@ -500,7 +589,7 @@ int orc_assemble(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *ne
                  const double *ay, const double *az, const double *fcx, const double *fcy, const double *fcz,
                  const uint32_t *zone, const double *ccx, const double *ccy, const double *ccz,
                  const uint8_t *isPressure, int nZones, double rho, const double *aP, const double *phi,
-                 const int32_t *rowPtr, const int32_t *colIdx, double *values, double *rhs)
+                 const int32_t *rowPtr, const int32_t *colIdx, double *values, double *rhs, const int32_t *twin)
 {
     const int64_t nnz = rowPtr[nC];
     for (int64_t k = 0; k < nnz; ++k)
@@ -527,7 +616,17 @@ int orc_assemble(int64_t nC, int64_t nF, const int64_t *owner, const int64_t *ne
             add_at(rowPtr, colIdx, values, n, o, -coef);
         } else {
             const uint32_t zz = zone[f];
-            if ((int)zz < nZones && isPressure[zz]) {
+            if (twin && twin[f] >= 0) {  /* periodic face (:411-419): owner and the twin face's owner */
+                const int64_t tw = owner[twin[f]];
+                const double dx = fcx[f] - ccx[o];
+                const double dy = fcy[f] - ccy[o];
+                const double dz = fcz[f] - ccz[o];
+                const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
+                const double den = STD_MAX(aP[o], 1e-30) * ddotA;
+                const double coef = rho * Amag2 / STD_MAX(den, 1e-30);
+                add_at(rowPtr, colIdx, values, o, o, coef);
+                add_at(rowPtr, colIdx, values, o, tw, -coef);
+            } else if ((int)zz < nZones && isPressure[zz]) {
                 const double dx = fcx[f] - ccx[o];
                 const double dy = fcy[f] - ccy[o];
                 const double dz = fcz[f] - ccz[o];
@@ -1643,15 +1742,17 @@ void orc_face_k_gradient(int64_t nF, const int64_t *owner, const int64_t *neighb
 /* BCType ordinals (src/solver/Solver.hpp:105-121) used by the face loops. */
 enum { ORC_BC_WALL = 0, ORC_BC_NOSLIP = 1, ORC_BC_MOVING = 2, ORC_BC_VELIN = 4, ORC_BC_SYMMETRY = 9 };
 
-/* compute_face_fluxes (src/solver/SimpleAlgorithm.cpp:201-237) without
- * periodic faces.  zoneType[z] = the BCType ordinal of the first boundary spec
+/* compute_face_fluxes (src/solver/SimpleAlgorithm.cpp:201-237).  A periodic
+ * face (twin[f] >= 0; twin may be NULL) takes 0.5 (U_o + U_t) with t the twin
+ * face's owner (:214-219).  zoneType[z] = the BCType ordinal of the first boundary spec
  * with zone z (find_bc), -1 when there is none; zoneVec[3 z .. 3 z + 2] its
  * vectorValue.  Face velocity: interior 0.5 (U_o + U_n); VelocityInlet and
  * MovingWall the zone's vector; NoSlipWall, Wall and Symmetry zero; any other
  * boundary (or none) the owner's velocity. */
 void orc_face_fluxes(int64_t nF, const int64_t *owner, const int64_t *neighbor, const double *ax, const double *ay,
                      const double *az, const uint32_t *zone, const int *zoneType, const double *zoneVec, int nZones,
-                     double rho, const double *Ux, const double *Uy, const double *Uz, double *phi)
+                     double rho, const double *Ux, const double *Uy, const double *Uz, double *phi,
+                     const int32_t *twin)
 {
     for (int64_t f = 0; f < nF; ++f) {
         const int64_t o = owner[f], n = neighbor[f];
@@ -1660,6 +1761,11 @@ void orc_face_fluxes(int64_t nF, const int64_t *owner, const int64_t *neighbor, 
             ux = 0.5 * (Ux[o] + Ux[n]);
             uy = 0.5 * (Uy[o] + Uy[n]);
             uz = 0.5 * (Uz[o] + Uz[n]);
+        } else if (twin && twin[f] >= 0) {
+            const int64_t tw = owner[twin[f]];
+            ux = 0.5 * (Ux[o] + Ux[tw]);
+            uy = 0.5 * (Uy[o] + Uy[tw]);
+            uz = 0.5 * (Uz[o] + Uz[tw]);
         } else {
             const uint32_t z = zone[f];
             const int t = (int)z < nZones ? zoneType[z] : -1;
@@ -1850,7 +1956,7 @@ void orc_assemble_momentum(int64_t nC, int64_t nF, const int64_t *owner, const i
                            const double *vol, const uint32_t *zone, const int *zoneType, const double *zoneVec,
                            int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int useBDF2,
                            int comp, const double *phi, const double *gp, const double *Ucomp, const double *Un,
-                           const double *Unm1, double *values, double *rhs, double *aPout)
+                           const double *Unm1, double *values, double *rhs, double *aPout, const int32_t *twin)
 {
     const double rho = opt[0], mu = opt[1], urfU = opt[2], dt = opt[3];
     const int64_t nnz = rowPtr[nC];
@@ -1879,7 +1985,11 @@ void orc_assemble_momentum(int64_t nC, int64_t nF, const int64_t *owner, const i
             const double dx = fcx[f] - ccx[o], dy = fcy[f] - ccy[o], dz = fcz[f] - ccz[o];
             const double ddotA = fabs(dx * Ax + dy * Ay + dz * Az);
             const double D = mu * Amag2 / STD_MAX(ddotA, 1e-30);
-            if (t == ORC_BC_NOSLIP || t == ORC_BC_WALL || t == ORC_BC_VELIN || t == ORC_BC_MOVING) {
+            if (twin && twin[f] >= 0) {  /* periodic (:275-282): half an interior face's coupling */
+                const int64_t tw = owner[twin[f]];
+                add_at(rowPtr, colIdx, values, o, o, ConvO + D);
+                add_at(rowPtr, colIdx, values, o, tw, -(ConvN + D));
+            } else if (t == ORC_BC_NOSLIP || t == ORC_BC_WALL || t == ORC_BC_VELIN || t == ORC_BC_MOVING) {
                 const double Ub = (t == ORC_BC_NOSLIP || t == ORC_BC_WALL) ? 0.0 : zoneVec[3 * z + comp];
                 add_at(rowPtr, colIdx, values, o, o, ConvO + D);
                 rhs[o] += (ConvN + D) * Ub;
@@ -2304,7 +2414,7 @@ int orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64
                        int nZones, const int32_t *rowPtr, const int32_t *colIdx, const double *opt, int flags,
                        const int *momCfg, double momTol, const int *pCfg, double pTol, const int *loops,
                        const double *tolUP, double *U, double *p, const double *Un, const double *Unm1, double *phi,
-                       double *aP, double *pPrime, double *res, int *iters)
+                       double *aP, double *pPrime, double *res, int *iters, const int32_t *twin)
 {
     const double rho = opt[0], mu = opt[1], urfU = opt[2], urfP = opt[3], dt = opt[4];
     const int bdf2 = flags & 1, simplec = (flags >> 1) & 1;
@@ -2325,14 +2435,14 @@ int orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64
     int outer;
     for (outer = 0; outer < nOuter; ++outer) {
         orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC, U + 2 * nC,
-                        phi);
+                        phi, twin);
         if (predictor) {
             orc_lsq_gradient(nC, nF, owner, neighbor, fcx, fcy, fcz, ccx, ccy, ccz, mInv, p, g, g + nC, g + 2 * nC);
             for (int k = 0; k < 3; ++k) {
                 orc_assemble_momentum(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, ccx, ccy, ccz, vol, zone,
                                       zoneType, zoneVec, nZones, rowPtr, colIdx, momOpt, bdf2, k, phi, g + k * nC,
                                       U + k * nC, Un ? Un + k * nC : NULL, Unm1 ? Unm1 + k * nC : NULL, values, rhs,
-                                      k == 0 ? aP : NULL);
+                                      k == 0 ? aP : NULL, twin);
                 double last = 0.0;
                 iters[k] = orc_linear_solve(momCfg, momTol, nC, rowPtr, colIdx, values, rhs, U + k * nC, &last);
                 orc_spmv(nC, rowPtr, colIdx, values, U + k * nC, Ax);
@@ -2346,12 +2456,12 @@ int orc_simple_iterate(int64_t nC, int64_t nF, const int64_t *owner, const int64
         }
         for (int corr = 0; corr < nCorr; ++corr) {
             orc_face_fluxes(nF, owner, neighbor, ax, ay, az, zone, zoneType, zoneVec, nZones, rho, U, U + nC,
-                            U + 2 * nC, phi);
+                            U + 2 * nC, phi, twin);
             for (int no = 0; no <= nNonOrth; ++no) {
                 if (simplec)
                     orc_simplec_denominator(nC, rowPtr, colIdx, values, aP, den);
                 orc_assemble(nC, nF, owner, neighbor, ax, ay, az, fcx, fcy, fcz, zone, ccx, ccy, ccz, isPressure,
-                             nZones, rho, simplec ? den : aP, phi, rowPtr, colIdx, pvals, rhs);
+                             nZones, rho, simplec ? den : aP, phi, rowPtr, colIdx, pvals, rhs, twin);
                 double last = 0.0;
                 iters[3] = orc_linear_solve(pCfg, pTol, nC, rowPtr, colIdx, pvals, rhs, pPrime, &last);
                 double cs = 0.0;

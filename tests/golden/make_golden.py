@@ -176,6 +176,8 @@ def momentum_case(name):
 
 CAVITY_BCS = [(z, 1) for z in (1, 2, 3, 5, 6)] + [(4, 2, (1.0, 0.0, 0.0))]
 CHANNEL_BCS = [(1, 4, (1.0, 0.1, 0.0)), (2, 7), (3, 1), (4, 1), (5, 9), (6, 0)]
+# periodic in x (zones 1, 2) and z (5, 6), no-slip floor, lid moving in x
+PERIODIC_BCS = [(1, 11), (2, 11), (3, 1), (4, 2, (1.0, 0.0, 0.0)), (5, 11), (6, 11)]
 # name: dims, node-shift amplitude (seed 31), RCM, boundary specs, SimpleOptions and solver configs, outer calls, inner
 SIMPLE_RUNS = {
     "simple_cavity_64_gmres_ilu.npz": ((64, 64, 1), 0.0, False, CAVITY_BCS,
@@ -187,6 +189,9 @@ SIMPLE_RUNS = {
     "simple_cavity_12_bdf2.npz": ((12, 12, 1), 0.0, False, CAVITY_BCS,
                                   dict(mu=0.01, dt=0.01, bdf2=True, mom_cfg=(0, 0, 1e-8, 200, 5),
                                        p_cfg=(2, 0, 1e-9, 1000, 30)), 3, 2),
+    "simple_periodic_couette_8x6x4.npz": ((8, 6, 4), 0.15, True, PERIODIC_BCS,
+                                          dict(mu=0.05, mom_cfg=(0, 1, 1e-8, 200, 30), p_cfg=(2, 0, 1e-9, 1000, 30)),
+                                          6, 1),
 }
 
 
@@ -337,6 +342,31 @@ def solvers_case(name):
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
+def periodic_case(name):
+    """Periodic faces (SimpleAlgorithm.cpp:101-186 pairing, :71-72 sparsity,
+    :214-219 fluxes, :275-282 momentum, :411-419 pressure assembly) on a
+    distorted, RCM-renumbered 8x6x5 channel periodic in x and z: the
+    reference's twin table, CSR, assembled values and rhs, face fluxes and
+    x-momentum values / rhs / aP."""
+    dims, seed = (8, 6, 5), 41
+    shift = W.interior_node_shift(*dims, amp=0.2, seed=seed)
+    rm = R.cartesian_mesh(*dims, node_shift=shift, do_rcm=True)
+    rng = np.random.default_rng(seed)
+    nC, nF = rm["nC"], rm["nF"]
+    aP = rng.uniform(0.5, 2.0, nC)
+    phi = rng.standard_normal(nF)
+    U = rng.standard_normal((3, nC))
+    p = rng.standard_normal(nC)
+    twin = R.periodic_twins(rm, PERIODIC_BCS)
+    rp, ci, v, rhs = R.assemble(rm, [(b[0], b[1]) for b in PERIODIC_BCS], 1.1, aP, phi)
+    flux = R.face_fluxes(rm, PERIODIC_BCS, 1.2, U)
+    mv, mr, maP = R.assemble_momentum(rm, PERIODIC_BCS, (1.0, 0.02, 0.7, 0.0), 0, U, p, flux)
+    np.savez_compressed(os.path.join(HERE, name), dims=np.array(dims), seed=np.array(seed), amp=np.array(0.2),
+                        bc_zone=np.array([b[0] for b in PERIODIC_BCS]), bc_type=np.array([b[1] for b in PERIODIC_BCS]),
+                        aP=aP, phi=phi, U=U, p=p, twin=twin, rowPtr=rp, colIdx=ci, values=v, rhs=rhs, flux=flux,
+                        mom_values=mv, mom_rhs=mr, mom_aP=maP)
+
+
 def cggpu_case(name):
     """gpu::CgGpu::set_matrix + solve (src/gpu/CgGpu.cpp:35-238, the GPU
     facade's host path) on the cases of tests/helpers.py:cggpu_cases: cold and
@@ -391,14 +421,24 @@ def poisson3d_full_case(name, n=128, seed=W.DEFAULT_SEED, tol=1e-8, max_it=50000
     out = {"n": np.array(n), "seed": np.array(seed), "tol": np.array(tol), "nnz": np.array(len(ci)),
            "pattern_sha256": np.array(_digest(rp) + _digest(ci)), "values_sha256": np.array(_digest(v)),
            "rhs_sha256": np.array(_digest(rhs)), "rcm_stats": np.array(m["rcm_stats"])}
+    xs = {}
     for pc, tag in ((0, "jacobi"), (1, "ilu0")):
         t = time.perf_counter()
         x, it, last, _ = R.cg(rp, ci, v, rhs, pc, tol, max_it)
+        xs[tag] = x
         out[f"{tag}_seconds"] = np.array(time.perf_counter() - t)
         out[f"{tag}_iters"] = np.array(it)
         out[f"{tag}_last"] = np.array(last)
         out.update({f"{tag}_{k}": a for k, a in _x_summary(x, 256, seed + 11).items()})
         print(f"{name}: {tag} {it} iterations, last {last:.3e}, {out[f'{tag}_seconds']:.1f} s", flush=True)
+    # the reference's own tight solve: how far each 1e-8 solution is from it
+    xt, it, last, _ = R.cg(rp, ci, v, rhs, 1, 1e-13, max_it)
+    out.update({f"tight_{k}": a for k, a in _x_summary(xt, 256, seed + 11).items()})
+    out["tight_iters"], out["tight_last"] = np.array(it), np.array(last)
+    for tag in xs:
+        out[f"{tag}_err_vs_tight"] = np.array(np.linalg.norm(xs[tag] - xt) / np.linalg.norm(xt))
+    print(f"{name}: tight ILU0 {it} iterations; errors vs tight: "
+          + ", ".join(f"{t} {float(out[t + '_err_vs_tight']):.2e}" for t in xs), flush=True)
     np.savez_compressed(os.path.join(HERE, name), **out)
 
 
@@ -500,6 +540,8 @@ def adjoint_full_case(name, n=24, seed=W.DEFAULT_SEED):
 
 FULL_SIZE = {
     "cggpu_cases.npz": cggpu_case,
+    "periodic_channel_8x6x5.npz": periodic_case,
+    "simple_periodic_couette_8x6x4.npz": simple_case,
     "poisson3d_128_cg.npz": poisson3d_full_case,
     "varcoef_256_cg.npz": varcoef_full_case,
     "batched_512_cg.npz": batched_full_case,
@@ -531,6 +573,7 @@ def main():
         piso_pimple_case(name)
     solvers_case("solvers_7x6x5_rcm.npz")
     cggpu_case("cggpu_cases.npz")
+    periodic_case("periodic_channel_8x6x5.npz")
     print("fixtures written to", HERE)
 
 

@@ -96,11 +96,15 @@ def cggpu_cases(O):
     rng = np.random.default_rng(31)
     x0 = rng.standard_normal(n)
     xs, _, _ = O.cg(rp, ci, v, b, 0, 1e-15, 5000)
+    # unpreconditioned CG wants a well-conditioned matrix: on the pinned
+    # system above (one row scaled by 1e6) rounding alone moves x by 1e-8
+    trp0, tci0, tv0 = tridiag(60, -1.0, 3.0, -1.0)
+    tb0 = np.random.default_rng(33).standard_normal(60)
     cases = [
         ("jacobi_cold", rp, ci, v, b, np.zeros(n), 1, 1e-8, 1000, 0.0),
         ("jacobi_warm", rp, ci, v, b, x0, 1, 1e-8, 1000, 0.0),
         ("ilu0_warm", rp, ci, v, b, x0, 2, 1e-8, 1000, 0.0),
-        ("none_cold", rp, ci, v, b, np.zeros(n), 0, 1e-8, 1000, 0.0),
+        ("none_cold", trp0, tci0, tv0, tb0, np.zeros(60), 0, 1e-10, 1000, 0.0),
         ("relative_orders", rp, ci, v, b, x0, 1, 1e-12, 1000, 3.0),
         ("tolerance_first", rp, ci, v, b, np.zeros(n), 2, 1e-3, 1000, 9.0),
         ("x0_exact", rp, ci, v, b, xs, 1, 1e-8, 1000, 0.0),

@@ -78,7 +78,7 @@ def test_full_size_assembly_bit_exact(system, oracle):
     L.orc_assemble(m.n_cells, m.n_faces, *ptrs, isP.ctypes.data_as(P), 7, 1.0,
                    np.ascontiguousarray(system["aP"]).ctypes.data_as(P),
                    np.ascontiguousarray(system["phi"]).ctypes.data_as(P), system["rp"].ctypes.data_as(P),
-                   system["ci"].ctypes.data_as(P), values.ctypes.data_as(P), rhs.ctypes.data_as(P))
+                   system["ci"].ctypes.data_as(P), values.ctypes.data_as(P), rhs.ctypes.data_as(P), None)
     assert bits_equal(values, system["vals"])
     assert bits_equal(rhs, system["arhs"])
 

@@ -298,7 +298,7 @@ def simple_fixture(oracle, name):
 
 
 @pytest.mark.parametrize("name", ["simple_cavity_64_gmres_ilu.npz", "simple_channel_8x6x5_simplec.npz",
-                                  "simple_cavity_12_bdf2.npz"])
+                                  "simple_cavity_12_bdf2.npz", "simple_periodic_couette_8x6x4.npz"])
 def test_simple_runs_fixture(oracle, name):
     """SimpleAlgorithm::iterate / advance_time_step from rest: U, p, phi,
     residuals and solve counts bit-identical to the reference's run."""
@@ -480,3 +480,30 @@ def test_cggpu_against_reference_fixture(oracle):
         ref = g[name + "_stats"]
         assert [st["iterations"], st["final_residual"], st["initial_residual"], float(st["converged"]),
                 st["precond_after"], st["last_residual"]] == list(ref), name
+
+
+def test_periodic_channel_fixture(oracle):
+    """Periodic faces against the reference's bytes
+    (tests/golden/periodic_channel_8x6x5.npz): twin table, CSR pattern with the
+    twin columns, assembled values and rhs, face fluxes and x-momentum."""
+    from simall_gb300 import workloads as W
+
+    g = load("periodic_channel_8x6x5.npz")
+    dims = tuple(int(v) for v in g["dims"])
+    m = oracle.cartesian_mesh(*dims, node_shift=W.interior_node_shift(*dims, amp=float(g["amp"]),
+                                                                        seed=int(g["seed"])))
+    oracle.rcm(m)
+    bcs = [(int(z), int(t)) + (((1.0, 0.0, 0.0),) if int(t) == 2 else ()) for z, t in zip(g["bc_zone"],
+                                                                                             g["bc_type"])]
+    twin = oracle.periodic_pairs(m, bcs)
+    assert np.array_equal(twin, g["twin"]) and np.count_nonzero(twin >= 0) == 2 * (6 * 5 + 8 * 6)
+    rp, ci = oracle.build_sparsity(m, twin)
+    assert np.array_equal(rp, g["rowPtr"]) and np.array_equal(ci, g["colIdx"])
+    v, rhs, anyD = oracle.assemble(m, rp, ci, [], 1.1, g["aP"], g["phi"], twin)
+    assert not anyD and bits_equal(v, g["values"]) and bits_equal(rhs, g["rhs"])
+    flux = oracle.face_fluxes(m, bcs, 1.2, g["U"], twin)
+    assert bits_equal(flux, g["flux"])
+    gp = oracle.lsq_gradient(m, g["p"])
+    mv, mr, maP = oracle.assemble_momentum(m, rp, ci, bcs, (1.0, 0.02, 0.7, 0.0), 0, flux, gp[0], g["U"][0],
+                                           twin=twin)
+    assert bits_equal(mv, g["mom_values"]) and bits_equal(mr, g["mom_rhs"]) and bits_equal(maP, g["mom_aP"])

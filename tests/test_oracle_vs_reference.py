@@ -228,6 +228,8 @@ def test_tfqmr_laplacian_jacobi(oracle, ref):
 
 CAVITY_BCS = [(z, 1) for z in (1, 2, 3, 5, 6)] + [(4, 2, (1.0, 0.0, 0.0))]
 CHANNEL_BCS = [(1, 4, (1.0, 0.1, 0.0)), (2, 7), (3, 1), (4, 1), (5, 9), (6, 0)]
+# periodic in x (zones 1, 2) and z (5, 6), no-slip floor, lid moving in x
+PERIODIC_BCS = [(1, 11), (2, 11), (3, 1), (4, 2, (1.0, 0.0, 0.0)), (5, 11), (6, 11)]
 
 SIMPLE_CASES = {
     # name: (dims, amp, renumber, bcs, kwargs, n_outer, n_inner)
@@ -239,6 +241,8 @@ SIMPLE_CASES = {
     "cavity_bdf2_gmres_jacobi": ((12, 12, 1), 0.0, False, CAVITY_BCS,
                                  dict(mu=0.01, dt=0.01, bdf2=True, mom_cfg=(0, 0, 1e-8, 200, 5),
                                       p_cfg=(2, 0, 1e-9, 1000, 30)), 3, 2),
+    "periodic_couette_rcm": ((8, 6, 4), 0.15, True, PERIODIC_BCS,
+                             dict(mu=0.05, mom_cfg=(0, 1, 1e-8, 200, 30), p_cfg=(2, 0, 1e-9, 1000, 30)), 6, 1),
 }
 
 
@@ -364,3 +368,39 @@ def test_cggpu_cases(oracle, ref):
         xo, so = oracle.cggpu(rp, ci, v, b, x0, pc, tol, mi, ro)
         assert bits_equal(xr, xo), name
         assert sr == so, (name, sr, so)
+
+
+def test_periodic_faces(oracle, ref):
+    """Periodic pairing, the twin columns, the pressure assembly, the face
+    fluxes and the momentum assembly of the oracle against the reference, bit
+    for bit, on a distorted channel periodic in x and z and on meshes one cell
+    wide across the periodic pair (each face is its own cell's twin)."""
+    from simall_gb300 import workloads as W
+
+    for dims, amp, bcs in (((8, 6, 5), 0.2, PERIODIC_BCS),
+                           ((7, 5, 1), 0.0, [(1, 1), (2, 1), (3, 1), (4, 2, (1.0, 0.0, 0.0)), (5, 11), (6, 11)]),
+                           ((1, 6, 5), 0.0, [(1, 11), (2, 11), (3, 1), (4, 2, (0.0, 0.0, 1.0)), (5, 1), (6, 1)])):
+        sh = _shift(dims, 5, amp)
+        r = ref.cartesian_mesh(*dims, node_shift=sh)
+        m = oracle.cartesian_mesh(*dims, node_shift=sh)
+        twin = oracle.periodic_pairs(m, bcs)
+        assert np.array_equal(ref.periodic_twins(r, bcs), twin) and np.any(twin >= 0)
+        rng = np.random.default_rng(5)
+        aP = rng.uniform(0.5, 2.0, m.nC)
+        phi = rng.standard_normal(m.nF)
+        rp, ci, v, rhs = ref.assemble(r, [(b[0], b[1]) for b in bcs], 1.1, aP, phi)
+        orp, oci = oracle.build_sparsity(m, twin)
+        ov, orhs, anyD = oracle.assemble(m, orp, oci, [], 1.1, aP, phi, twin)
+        assert np.array_equal(rp, orp) and np.array_equal(ci, oci) and not anyD
+        assert bits_equal(v, ov) and bits_equal(rhs, orhs)
+        U = [rng.standard_normal(m.nC) for _ in range(3)]
+        flux = ref.face_fluxes(r, bcs, 1.2, U)
+        assert bits_equal(flux, oracle.face_fluxes(m, bcs, 1.2, U, twin))
+        p = rng.standard_normal(m.nC)
+        g = oracle.lsq_gradient(m, p)
+        for comp in range(3):
+            vr, rr, aPr = ref.assemble_momentum(r, bcs, (1.0, 0.01, 0.7, 0.0), comp, np.array(U), p, flux)
+            vo, ro, aPo = oracle.assemble_momentum(m, orp, oci, bcs, (1.0, 0.01, 0.7, 0.0), comp, flux, g[comp],
+                                                   U[comp], twin=twin)
+            assert bits_equal(vr, vo) and bits_equal(rr, ro) and (comp > 0 or bits_equal(aPr, aPo))
+        ref.free_mesh(r)
