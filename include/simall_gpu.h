@@ -534,10 +534,13 @@ int simall_simp_destroy(simall_simp *s);
 int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds);
 /* Latency measurements of the free-running triangular sweeps (ILU(0), SSOR,
  * the AMG smoother's large levels; no reference counterpart): sets, for the
- * whole process, the CTAs per SM of their grid (1..8; default 4) and the
- * longest sleep between two polls of a value not yet published (0..4096 ns,
- * 0 = spin; default 256).  Results do not depend on either. */
-int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns);
+ * whole process, the CTAs per SM of their grid (1..8; default 4), the longest
+ * sleep between two polls of a value not yet published (0..4096 ns, 0 = spin;
+ * default 256) and whether the ILU(0) backward sweep divides through the
+ * correctly rounded reciprocal of the pivot (1, default) or by a division (0).
+ * Results do not depend on any of them.  Solvers capture their iteration
+ * graphs at their first solve: set these before creating the solver. */
+int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns, int divide_via_reciprocal);
 /* The small-system ILU(0) path divides through a correctly rounded reciprocal
  * (one product and two FMAs, Markstein's correction).  For each i, q_recip[i]
  * is that quotient a[i] / b[i] and q_div[i] the device's correctly rounded

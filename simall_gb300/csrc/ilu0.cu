@@ -41,6 +41,7 @@ namespace simall {
 
 int g_sweep_ctas_per_sm = 4;
 unsigned g_sweep_backoff_ns = 256;
+bool g_sweep_reciprocal = true;
 
 namespace {
 
@@ -785,7 +786,7 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
     // warps beyond a few levels' rows only add polls: g_sweep_ctas_per_sm (4: 32 warps per SM)
     const int grid = ctx->num_sms * g_sweep_ctas_per_sm;
     const unsigned backoff = g_sweep_backoff_ns;
-    const double *rdiag = (!ssor && lu == d->lu.p && d->rdiag.p) ? d->rdiag.p : nullptr;
+    const double *rdiag = (g_sweep_reciprocal && !ssor && lu == d->lu.p && d->rdiag.p) ? d->rdiag.p : nullptr;
     const int fill = std::min((n + kBlock - 1) / kBlock, ctx->num_sms * 8);
     k_sweep_begin_values<<<fill < 1 ? 1 : fill, kBlock, 0, ctx->stream>>>(d->sweepCtl.p, d->y.p, n);
     SIMALL_LAUNCH_CHECK(ctx);
@@ -960,12 +961,13 @@ int simall_gpu_ilu0_factor_inplace(size_t n, const int32_t *rowPtr, const int32_
     return st;
 }
 
-int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns)
+int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns, int divide_via_reciprocal)
 {
     if (ctas_per_sm < 1 || ctas_per_sm > 8 || backoff_ns < 0 || backoff_ns > 4096)
         return SIMALL_ERR_INVALID_ARGUMENT;
     g_sweep_ctas_per_sm = ctas_per_sm;
     g_sweep_backoff_ns = static_cast<unsigned>(backoff_ns);
+    g_sweep_reciprocal = divide_via_reciprocal != 0;
     return SIMALL_OK;
 }
 

@@ -107,6 +107,7 @@ inline bool sweep_preconditioner(int pc)
 // simall_diagnose_sweep_params changes them for latency measurements.
 extern int g_sweep_ctas_per_sm;
 extern unsigned g_sweep_backoff_ns;
+extern bool g_sweep_reciprocal;  // ILU(0) backward sweep: divide through RN(1/u_ii) (same bits)
 int ilu_setup(simall_solver *s);  // ILU(0) factor, SSOR's sweep data or the AMG hierarchy (cfg.preconditioner)
 int ilu_check(simall_solver *s);  // a sweep wait timed out -> error
 int ilu_apply(simall_solver *s, const double *r, double *z);
