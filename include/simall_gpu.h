@@ -266,10 +266,16 @@ typedef struct simall_boundary {
 } simall_boundary;
 
 /* Replaces SimpleAlgorithm::build_sparsity + assemble_pressure_correction
- * (src/solver/SimpleAlgorithm.cpp:49-98, :358-447) for the SIMPLE variant
- * without periodic twins.  create() builds the CSR pattern (bit-exact with
- * build_sparsity), uploads the mesh and precomputes per-face |A|^2 and |d.A|
- * on the device. */
+ * (src/solver/SimpleAlgorithm.cpp:49-98, :358-447).  create() pairs the
+ * periodic faces as build_periodic_pairs does (:101-186: the zones of the
+ * Periodic specs, in spec order, paired two by two; each face of the first
+ * zone of a pair takes the face of the second whose centroid is nearest to
+ * its own plus the mean translation between the zones), builds the CSR pattern
+ * (bit-exact with build_sparsity, twin columns included), uploads the mesh
+ * and precomputes per-face |A|^2 and |d.A| on the device.  A periodic face
+ * couples its owner with its twin face's owner in the pressure assembly, the
+ * face fluxes and the momentum assembly; it is not a Dirichlet anchor.  The
+ * face-conductance extension below rejects systems with periodic faces. */
 typedef struct simall_pressure_system simall_pressure_system;
 int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *mesh, const simall_boundary *bcs,
                                   int n_bcs, simall_pressure_system **out);
@@ -277,6 +283,9 @@ int simall_pressure_system_destroy(simall_pressure_system *ps);
 /* Sizes, and (when the arrays are non-NULL) host copies of the pattern. */
 int simall_pressure_system_pattern(const simall_pressure_system *ps, int64_t *n, int64_t *nnz, int32_t *rowPtr,
                                    int32_t *colIdx);
+/* The periodic twin of every face (-1 where none), twin[n_faces]: the table
+ * SimpleAlgorithm::build_periodic_pairs builds. */
+int simall_pressure_system_periodic_twins(const simall_pressure_system *ps, int32_t *twin);
 /* Device pointers of the system's CSR (rowPtr, colIdx, values) and rhs. */
 int simall_pressure_system_device_arrays(const simall_pressure_system *ps, const int32_t **rowPtr,
                                          const int32_t **colIdx, double **values, double **rhs);
@@ -305,7 +314,8 @@ int simall_pressure_system_solve(simall_pressure_system *ps, simall_solver *s, d
 /* ------------------------------------------------------------------ the field loops around the solve */
 /* The face loops either side of the pressure solve of SimpleAlgorithm, on the
  * device and bit-identical to the reference: compute_face_fluxes
- * (SimpleAlgorithm.cpp:201-237, without periodic faces), the least-squares
+ * (SimpleAlgorithm.cpp:201-237; a periodic face averages its owner's velocity
+ * with its twin face's owner's, :214-219), the least-squares
  * gradient (LeastSquaresGradient, Gradient.cpp:17-133) and correct_fields
  * (SimpleAlgorithm.cpp:450-487).  A GpuSimpleAlgorithm::iterate() override that
  * keeps U, p, aP, phi and p' in device memory runs the whole pressure step
@@ -336,7 +346,8 @@ int simall_correct_fields(simall_pressure_system *ps, double rho, double urfP, c
 
 /* ------------------------------------------------------------------ momentum assembly */
 /* Replaces SimpleAlgorithm::assemble_momentum (src/solver/SimpleAlgorithm.cpp:240-355),
- * first-order upwind, no periodic faces.  The reference assembles one velocity
+ * first-order upwind (a periodic face couples its owner with its twin face's
+ * owner as half an interior face, :275-282).  The reference assembles one velocity
  * component per call, but its matrix does not depend on the component; one call
  * here builds that matrix once on the system's pattern (the pattern the
  * pressure system shares with the momentum matrix, build_sparsity) and the

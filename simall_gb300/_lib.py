@@ -133,6 +133,7 @@ SIGNATURES = {
     "simall_pressure_system_create": (_I, [_P, C.POINTER(MeshView), C.POINTER(Boundary), _I, C.POINTER(_P)]),
     "simall_pressure_system_destroy": (_I, [_P]),
     "simall_pressure_system_pattern": (_I, [_P, C.POINTER(_I64), C.POINTER(_I64), _P, _P]),
+    "simall_pressure_system_periodic_twins": (_I, [_P, _P]),
     "simall_pressure_system_device_arrays": (_I, [_P, C.POINTER(_P), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     "simall_assemble_pressure_correction": (_I, [_P, _D, _P, _P, _I, C.POINTER(_I)]),
     "simall_assemble_pressure_correction_simplec": (_I, [_P, _D, _P, _P, _P, _I, C.POINTER(_I)]),

@@ -1,7 +1,8 @@
 // Pressure-correction assembly on the device: the GB300 replacement of
 // SimpleAlgorithm::build_sparsity + assemble_pressure_correction
-// (src/solver/SimpleAlgorithm.cpp:49-98, :358-447), SIMPLE variant, no
-// periodic twins.
+// (src/solver/SimpleAlgorithm.cpp:49-98, :358-447), periodic faces included
+// (build_periodic_pairs :101-186, the twin column :71-72, the coupling of a
+// periodic face with its twin face's owner :411-419).
 //
 // The reference walks the faces once and scatters each coefficient into four
 // CSR slots through a linear column search (find_col/add_at, :23-35).  Here:
@@ -21,6 +22,7 @@
 #include "solver.hpp"
 
 #include <algorithm>
+#include <cfloat>
 #include <cmath>
 #include <cstring>
 #include <new>
@@ -31,7 +33,6 @@ namespace simall {
 
 namespace {
 
-constexpr uint8_t kInterior = 0, kPressure = 1, kOtherBoundary = 2;
 
 // |A|^2 and |d.A| with the reference's operation order (SimpleAlgorithm.cpp:371-378, :417-420).
 __global__ void __launch_bounds__(kBlock) k_face_geometry(int64_t nF, const int32_t *__restrict__ owner,
@@ -53,7 +54,7 @@ __global__ void __launch_bounds__(kBlock) k_face_geometry(int64_t nF, const int3
             dx = __dsub_rn(cx[n], cx[o]);
             dy = __dsub_rn(cy[n], cy[o]);
             dz = __dsub_rn(cz[n], cz[o]);
-        } else if (kind[f] == kPressure) {
+        } else if (kind[f] == kPressure || kind[f] == kPeriodic) {
             dx = __dsub_rn(fx[f], cx[o]);
             dy = __dsub_rn(fy[f], cy[o]);
             dz = __dsub_rn(fz[f], cz[o]);
@@ -105,6 +106,7 @@ __global__ void __launch_bounds__(kBlock) k_cell_rows(int64_t nC, const int32_t 
         const int r0 = rowPtr[c], r1 = rowPtr[c + 1];
         for (int k = r0; k < r1; ++k)
             values[k] = 0.0;
+        const int kd = diagSlot[c];
         double diag = 0.0, b = 0.0;
         for (int e = cfOff[c]; e < cfOff[c + 1]; ++e) {
             const int ent = cfEnt[e];
@@ -114,15 +116,19 @@ __global__ void __launch_bounds__(kBlock) k_cell_rows(int64_t nC, const int32_t 
             const uint8_t k = kind[f];
             if (k != kOtherBoundary)
                 diag = __dadd_rn(diag, cf);
-            if (k == kInterior) {
+            if (k == kInterior || k == kPeriodic) {
+                // the other cell's column: the neighbour, or the periodic twin
+                // face's owner -- which is this cell itself on a mesh one cell
+                // wide across the periodic pair: then the diagonal
                 const int slot = cfSlot[e];
-                if (slot >= 0)
+                if (slot == kd)
+                    diag = __dadd_rn(diag, -cf);
+                else if (slot >= 0)
                     values[slot] = __dadd_rn(values[slot], -cf);
             }
             const double ph = __ldg(phi + f);
             b = isNbr ? __dadd_rn(b, ph) : __dsub_rn(b, ph);
         }
-        const int kd = diagSlot[c];
         if (!anyDirichlet && c == 0) {
             diag = __dmul_rn(diag, 1.0e6);
             b = 0.0;
@@ -249,6 +255,125 @@ __global__ void __launch_bounds__(kBlock) k_simplec_den(int64_t nC, const int32_
     }
 }
 
+// Periodic pairing, the search: for each face a of zone group A (centroid plus
+// the group translation, formed on the host), the face of group B whose
+// centroid is nearest, squared distance in the reference's operation order
+// (SimpleAlgorithm.cpp:167-176) and the first minimum in B's order.  B is
+// streamed through shared memory in tiles.
+constexpr int kPairTile = 1024;
+
+__global__ void __launch_bounds__(kBlock) k_periodic_nearest(int nA, const double *__restrict__ ax,
+                                                             const double *__restrict__ ay,
+                                                             const double *__restrict__ az, int nB,
+                                                             const double *__restrict__ bx,
+                                                             const double *__restrict__ by,
+                                                             const double *__restrict__ bz, int *__restrict__ best)
+{
+    __shared__ double tx[kPairTile], ty[kPairTile], tz[kPairTile];
+    const int a = blockIdx.x * blockDim.x + threadIdx.x;
+    const double px = a < nA ? ax[a] : 0.0, py = a < nA ? ay[a] : 0.0, pz = a < nA ? az[a] : 0.0;
+    double bestd2 = DBL_MAX;
+    int bi = -1;
+    for (int t0 = 0; t0 < nB; t0 += kPairTile) {
+        const int cnt = min(kPairTile, nB - t0);
+        __syncthreads();
+        for (int j = threadIdx.x; j < cnt; j += blockDim.x) {
+            tx[j] = bx[t0 + j];
+            ty[j] = by[t0 + j];
+            tz[j] = bz[t0 + j];
+        }
+        __syncthreads();
+        for (int j = 0; j < cnt; ++j) {
+            const double dx = __dsub_rn(tx[j], px), dy = __dsub_rn(ty[j], py), dz = __dsub_rn(tz[j], pz);
+            const double d2 = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+            if (d2 < bestd2) {
+                bestd2 = d2;
+                bi = t0 + j;
+            }
+        }
+    }
+    if (a < nA)
+        best[a] = bi;
+}
+
+// SimpleAlgorithm::build_periodic_pairs (SimpleAlgorithm.cpp:101-186) for the
+// Periodic specs of bcs: twin[nF] (-1 where none).  Groups, translations and
+// the writes of the result follow the reference on the host, face order kept;
+// the O(|A| |B|) nearest-centroid search runs on the device.
+int periodic_pairs(simall_context *ctx, const simall_mesh_view *m, const simall_boundary *bcs, int n_bcs,
+                   std::vector<int32_t> &twin)
+{
+    const int64_t nF = m->n_faces;
+    twin.assign(static_cast<size_t>(nF), -1);
+    std::vector<uint32_t> pz;
+    for (int i = 0; i < n_bcs; ++i)
+        if (bcs[i].type == SIMALL_BC_PERIODIC)
+            pz.push_back(bcs[i].zone);
+    if (pz.size() < 2)
+        return SIMALL_OK;
+    std::vector<std::vector<int32_t>> byZone(pz.size());
+    for (int64_t f = 0; f < nF; ++f) {
+        if (m->neighbor[f] != ~0ull)
+            continue;
+        for (size_t i = 0; i < pz.size(); ++i)
+            if (pz[i] == m->boundary_zone[f]) {
+                byZone[i].push_back(static_cast<int32_t>(f));
+                break;
+            }
+    }
+    cudaStream_t st = ctx->stream;
+    for (size_t z = 0; z + 1 < pz.size(); z += 2) {
+        const auto &A = byZone[z];
+        const auto &B = byZone[z + 1];
+        if (A.empty() || B.empty())
+            continue;
+        double Ax = 0, Ay = 0, Az = 0, Bx = 0, By = 0, Bz = 0;
+        for (int32_t f : A) {
+            Ax += m->centroid_x[f];
+            Ay += m->centroid_y[f];
+            Az += m->centroid_z[f];
+        }
+        for (int32_t f : B) {
+            Bx += m->centroid_x[f];
+            By += m->centroid_y[f];
+            Bz += m->centroid_z[f];
+        }
+        const double invA = 1.0 / static_cast<double>(A.size()), invB = 1.0 / static_cast<double>(B.size());
+        const double tx = Bx * invB - Ax * invA, ty = By * invB - Ay * invA, tz = Bz * invB - Az * invA;
+        const int nA = static_cast<int>(A.size()), nB = static_cast<int>(B.size());
+        std::vector<double> h(static_cast<size_t>(3 * (nA + nB)));
+        for (int i = 0; i < nA; ++i) {
+            h[i] = m->centroid_x[A[i]] + tx;
+            h[nA + i] = m->centroid_y[A[i]] + ty;
+            h[2 * nA + i] = m->centroid_z[A[i]] + tz;
+        }
+        double *hb = h.data() + 3 * nA;
+        for (int j = 0; j < nB; ++j) {
+            hb[j] = m->centroid_x[B[j]];
+            hb[nB + j] = m->centroid_y[B[j]];
+            hb[2 * nB + j] = m->centroid_z[B[j]];
+        }
+        DevBuf<double> d;
+        DevBuf<int> best;
+        SIMALL_CUDA_TRY(ctx, d.alloc(h.size()));
+        SIMALL_CUDA_TRY(ctx, best.alloc(nA));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(d.p, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+        const double *db = d.p + 3 * nA;
+        k_periodic_nearest<<<(nA + kBlock - 1) / kBlock, kBlock, 0, st>>>(nA, d.p, d.p + nA, d.p + 2 * nA, nB, db,
+                                                                          db + nB, db + 2 * nB, best.p);
+        SIMALL_LAUNCH_CHECK(ctx);
+        std::vector<int> hbest(static_cast<size_t>(nA));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(hbest.data(), best.p, nA * sizeof(int), cudaMemcpyDeviceToHost, st));
+        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        for (int i = 0; i < nA; ++i)  // in A's order: a later face choosing the same b rewrites twin[b]
+            if (hbest[i] >= 0) {
+                twin[A[i]] = B[hbest[i]];
+                twin[B[hbest[i]]] = A[i];
+            }
+    }
+    return SIMALL_OK;
+}
+
 }  // namespace
 }  // namespace simall
 
@@ -267,9 +392,6 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
         !m->centroid_z || !m->boundary_zone || !m->cell_centroid_x || !m->cell_centroid_y || !m->cell_centroid_z ||
         !m->cell_face_offsets || !m->cell_face_indices)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mesh view has a null array");
-    for (int i = 0; i < n_bcs; ++i)
-        if (bcs[i].type == SIMALL_BC_PERIODIC)
-            return fail(ctx, SIMALL_ERR_UNSUPPORTED, "periodic boundaries are not supported by the device assembly");
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     const uint64_t kB = ~0ull;
     // ---- validate ids, classify faces
@@ -283,8 +405,20 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
                         static_cast<long long>(f));
         own[f] = static_cast<int32_t>(o);
         nbr[f] = n == kB ? -1 : static_cast<int32_t>(n);
+    }
+    // periodic pairs first: build_sparsity needs the twins (SimpleAlgorithm.cpp:54-56)
+    std::vector<int32_t> twin;
+    {
+        const int pst = periodic_pairs(ctx, m, bcs, n_bcs, twin);
+        if (pst)
+            return pst;
+    }
+    for (int64_t f = 0; f < nF; ++f) {
+        const uint64_t n = m->neighbor[f];
         if (n != kB) {
             kind[f] = kInterior;
+        } else if (twin[f] >= 0) {
+            kind[f] = kPeriodic;  // a periodic twin takes precedence over the zone's spec (:214, :279, :411)
         } else {
             // find_bc: first spec of the zone (SimpleAlgorithm.cpp:191-197)
             int type = -1;
@@ -316,6 +450,8 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
     ps->nF = nF;
     ps->anyDirichlet = anyD;
     ps->h_bcs.assign(bcs, bcs + n_bcs);
+    ps->h_twin = twin;
+    ps->periodic = std::any_of(twin.begin(), twin.end(), [](int32_t t) { return t >= 0; });
     // ---- sparsity (build_sparsity :62-82): {c} U other cells of c's faces, sorted, unique
     ps->h_rowPtr.assign(static_cast<size_t>(nC) + 1, 0);
     ps->h_colIdx.reserve(static_cast<size_t>(ncf) + static_cast<size_t>(nC));
@@ -330,6 +466,8 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
                 const int32_t oth = (own[f] == c) ? nbr[f] : own[f];
                 if (oth >= 0)
                     nb.push_back(oth);
+                else if (twin[f] >= 0)
+                    nb.push_back(own[twin[f]]);
             }
             std::sort(nb.begin(), nb.end());
             nb.erase(std::unique(nb.begin(), nb.end()), nb.end());
@@ -368,7 +506,7 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
             const int32_t o = own[f], n = nbr[f];
             int32_t w = fill[o]++;
             cfEnt[w] = static_cast<int32_t>(f);
-            cfSlot[w] = n >= 0 ? slot_of(o, n) : -1;
+            cfSlot[w] = n >= 0 ? slot_of(o, n) : (twin[f] >= 0 ? slot_of(o, own[twin[f]]) : -1);
             if (n >= 0) {
                 w = fill[n]++;
                 cfEnt[w] = static_cast<int32_t>(static_cast<uint32_t>(f) | 0x80000000u);
@@ -418,6 +556,15 @@ int simall_pressure_system_create(simall_context *ctx, const simall_mesh_view *m
             PS_TRY(up(ps->cfSlot.p, cfSlot.data(), nEnt * sizeof(int32_t)));
         }
         PS_TRY(up(ps->diagSlot.p, diagSlot.data(), nC * sizeof(int32_t)));
+        {
+            std::vector<int32_t> partner(nbr);
+            for (int64_t f = 0; f < nF; ++f)
+                if (partner[f] < 0 && twin[f] >= 0)
+                    partner[f] = own[twin[f]];
+            PS_TRY(ps->fpartner.alloc(nF));
+            PS_TRY(up(ps->fpartner.p, partner.data(), nF * sizeof(int32_t)));
+            PS_TRY(cudaStreamSynchronize(st));  // partner dies at scope exit
+        }
         // geometry (temporary device copies of the SoA arrays the kernel reads)
         DevBuf<double> g[9];
         const double *src[9] = {m->area_x,     m->area_y,     m->area_z,          m->centroid_x,     m->centroid_y,
@@ -465,6 +612,14 @@ int simall_pressure_system_pattern(const simall_pressure_system *ps, int64_t *n,
         std::memcpy(rowPtr, ps->h_rowPtr.data(), (ps->nC + 1) * sizeof(int32_t));
     if (colIdx)
         std::memcpy(colIdx, ps->h_colIdx.data(), ps->nnz * sizeof(int32_t));
+    return SIMALL_OK;
+}
+
+int simall_pressure_system_periodic_twins(const simall_pressure_system *ps, int32_t *twin)
+{
+    if (!ps || !twin)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    std::memcpy(twin, ps->h_twin.data(), ps->nF * sizeof(int32_t));
     return SIMALL_OK;
 }
 
@@ -586,6 +741,8 @@ int simall_assemble_face_conductance(simall_pressure_system *ps, double rho, con
     simall_context *ctx = ps->ctx;
     if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "assemble: bad memory kind %d", mem);
+    if (ps->periodic)  // the face-conductance extension defines no periodic coupling
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "face-conductance assembly: the system has periodic faces");
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     const double *dk = k, *dpb = pb, *dsrc = src;
@@ -620,6 +777,8 @@ int simall_face_conductance_gradient(simall_pressure_system *ps, double rho, con
     simall_context *ctx = ps->ctx;
     if (mem != SIMALL_MEM_HOST && mem != SIMALL_MEM_DEVICE)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "gradient: bad memory kind %d", mem);
+    if (ps->periodic)
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "face-conductance gradient: the system has periodic faces");
     SIMALL_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
     cudaStream_t st = ctx->stream;
     const double *d_k = k, *d_pb = pb, *d_x = x, *d_l = lambda;

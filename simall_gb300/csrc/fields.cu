@@ -133,8 +133,10 @@ __global__ void __launch_bounds__(kBlock) k_lsq_gradient(int64_t nC, const int32
 }
 
 // compute_face_fluxes: phi_f = rho (u . A) with the face velocity of the kind.
+// partner: the neighbour of an interior face, the twin face's owner of a
+// periodic one (both kFaceInterior), -1 elsewhere.
 __global__ void __launch_bounds__(kBlock) k_face_fluxes(int64_t nF, double rho, const int32_t *__restrict__ owner,
-                                                        const int32_t *__restrict__ neighbor,
+                                                        const int32_t *__restrict__ partner,
                                                         const uint8_t *__restrict__ fkind,
                                                         const int32_t *__restrict__ fvslot,
                                                         const double *__restrict__ zvec, int nslots,
@@ -148,7 +150,7 @@ __global__ void __launch_bounds__(kBlock) k_face_fluxes(int64_t nF, double rho, 
         double ux, uy, uz;
         switch (fkind[f]) {
         case kFaceInterior: {
-            const int n = neighbor[f];
+            const int n = partner[f];
             ux = __dmul_rn(0.5, __dadd_rn(Ux[o], Ux[n]));
             uy = __dmul_rn(0.5, __dadd_rn(Uy[o], Uy[n]));
             uz = __dmul_rn(0.5, __dadd_rn(Uz[o], Uz[n]));
@@ -261,6 +263,11 @@ int simall_pressure_system_setup_field_loops(simall_pressure_system *ps, const s
     for (int64_t f = 0; f < nF; ++f) {
         if (m->neighbor[f] != ~0ull) {
             fk[f] = kFaceInterior;
+            continue;
+        }
+        if (ps->h_twin[f] >= 0) {  // periodic: averaged with the twin face's owner (:214-219, :275-282)
+            fk[f] = kFaceInterior;
+            mk[f] = kMomPeriodic;
             continue;
         }
         const uint32_t z = m->boundary_zone[f];
@@ -383,7 +390,7 @@ int simall_compute_face_fluxes(simall_pressure_system *ps, double rho, const dou
         }
         out = ps->stage.p + 3 * nC;
     }
-    k_face_fluxes<<<grid_for_ps(ctx, nF), kBlock, 0, st>>>(nF, rho, ps->owner.p, ps->neighbor.p, ps->fkind.p,
+    k_face_fluxes<<<grid_for_ps(ctx, nF), kBlock, 0, st>>>(nF, rho, ps->owner.p, ps->fpartner.p, ps->fkind.p,
                                                            ps->fvslot.p, ps->zvec.p, ps->nslots, ps->ax.p, ps->ay.p,
                                                            ps->az.p, u[0], u[1], u[2], out);
     SIMALL_LAUNCH_CHECK(ctx);

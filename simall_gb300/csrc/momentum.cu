@@ -1,6 +1,6 @@
 // Momentum assembly on the device: the GB300 replacement of
 // SimpleAlgorithm::assemble_momentum (src/solver/SimpleAlgorithm.cpp:240-355),
-// first-order upwind, no periodic faces.
+// first-order upwind, periodic faces included.
 //
 // The reference assembles each velocity component separately, but the matrix
 // it builds does not depend on the component (convection, diffusion,
@@ -63,6 +63,7 @@ __global__ void __launch_bounds__(kBlock) k_mom_rows(const MomArgs a)
         const int r0 = a.rowPtr[c], r1 = a.rowPtr[c + 1];
         for (int k = r0; k < r1; ++k)
             a.values[k] = 0.0;
+        const int kd = a.diagSlot[c];
         double diag = 0.0, b0 = 0.0, b1 = 0.0, b2 = 0.0;
         for (int e = a.cfOff[c]; e < a.cfOff[c + 1]; ++e) {
             const int ent = a.cfEnt[e];
@@ -93,6 +94,17 @@ __global__ void __launch_bounds__(kBlock) k_mom_rows(const MomArgs a)
                 b0 = __dadd_rn(b0, __dmul_rn(w, u0));
                 b1 = __dadd_rn(b1, __dmul_rn(w, u1));
                 b2 = __dadd_rn(b2, __dmul_rn(w, u2));
+            } else if (k == kMomPeriodic) {
+                // half an interior face (:275-282): oo += ConvO + D, o,twin -= ConvN + D
+                // (the twin face's owner is this cell on a mesh one cell wide
+                // across the pair: then the diagonal, in the same order)
+                diag = __dadd_rn(diag, __dadd_rn(convO, D));
+                const double other = __dadd_rn(convN, D);
+                const int slot = a.cfSlot[e];
+                if (slot == kd)
+                    diag = __dadd_rn(diag, -other);
+                else if (slot >= 0)
+                    a.values[slot] = __dadd_rn(a.values[slot], -other);
             } else if (k == kMomOther) {
                 diag = __dadd_rn(diag, convO);
             }
@@ -126,7 +138,7 @@ __global__ void __launch_bounds__(kBlock) k_mom_rows(const MomArgs a)
 #pragma unroll
         for (int q = 0; q < 3; ++q)
             a.rhs[q * nC + c] = __dadd_rn(bb[q], __dmul_rn(dd, a.U[q * nC + c]));
-        a.values[a.diagSlot[c]] = scaled;
+        a.values[kd] = scaled;
         a.aP[c] = scaled;
     }
 }

@@ -15,7 +15,13 @@ struct simall_pressure_system {
     // faces
     simall::DevBuf<int32_t> owner, neighbor;  // neighbor -1 on boundary faces
     simall::DevBuf<double> amag2, ddotA;
-    simall::DevBuf<uint8_t> kind;  // 0 interior, 1 pressure boundary, 2 other boundary
+    simall::DevBuf<uint8_t> kind;  // 0 interior, 1 pressure boundary, 2 other boundary, 3 periodic
+    // periodic faces (SimpleAlgorithm::build_periodic_pairs): the twin face of
+    // each boundary face (-1: none), and per face the cell a flux averages
+    // with (the neighbour, the twin face's owner, or -1)
+    std::vector<int32_t> h_twin;
+    simall::DevBuf<int32_t> fpartner;
+    bool periodic = false;
     simall::DevBuf<double> coef;
     // cells: faces in ascending id; entry = face id | (cell is the neighbour) << 31;
     // slot = CSR position of the other cell in the row (-1: none)
@@ -50,7 +56,10 @@ namespace simall {
 // Momentum face kinds: interior; VelocityInlet / MovingWall (the zone's vector);
 // NoSlipWall / Wall (zero); Symmetry (no contribution); any other boundary
 // (upwind outflow).
-constexpr uint8_t kMomInterior = 0, kMomZoneVector = 1, kMomWall = 2, kMomSymmetry = 3, kMomOther = 4;
+constexpr uint8_t kMomInterior = 0, kMomZoneVector = 1, kMomWall = 2, kMomSymmetry = 3, kMomOther = 4,
+                  kMomPeriodic = 5;
+// Pressure-system face kinds (assemble.cu).
+constexpr uint8_t kInterior = 0, kPressure = 1, kOtherBoundary = 2, kPeriodic = 3;
 // Least-squares gradient of f (device, n_cells) into g[3][n_cells] (fields.cu).
 int ps_gradient(simall_pressure_system *ps, const double *f, double *g);
 }  // namespace simall

@@ -139,6 +139,12 @@ class PressureSystem:
         self.nnz = nnz.value
         self.any_dirichlet = None
 
+    def periodic_twins(self):
+        """The twin face of every face (-1 where none): build_periodic_pairs' table."""
+        tw = np.empty(self.mesh.n_faces, np.int32)
+        check(self.L.simall_pressure_system_periodic_twins(self.handle, tw.ctypes.data))
+        return tw
+
     def pattern(self):
         rp = np.empty(self.n + 1, np.int32)
         ci = np.empty(self.nnz, np.int32)

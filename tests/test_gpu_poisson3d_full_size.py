@@ -17,7 +17,9 @@ interior face fluxes N(0,1), all walls with the cell-0 pin; 2,097,152 rows,
   from its unperturbed x, and the reference's arithmetic with the dot
   products summed in a tree instead of serially (the one thing a parallel
   reduction cannot reproduce) stops at 522.  So the bar is the count within
-  2% of the reference's and x within 2e-7 of its x;
+  2% of the reference's, and x as accurate as the reference's own: against
+  the reference's solve of the same system to 1e-13, no further than twice
+  the reference's 1e-8 solution is from it (7.9e-7);
 * the mixed-precision solve's FP64 true residual, recomputed on the host with
   the oracle's SpMV, is below 1e-8.
 """
@@ -81,7 +83,8 @@ def test_fp64_pcg_matches_the_reference(sg, ctx, p3d, tag):
         assert err <= 1e-10, err
     else:
         assert abs(it - ref_it) <= 0.02 * ref_it, (it, ref_it)
-        assert err <= 2e-7, err
+        err_tight = x_summary_error(x, fx, "tight")
+        assert err_tight <= 2.0 * float(fx["ilu0_err_vs_tight"]), (err_tight, float(fx["ilu0_err_vs_tight"]))
 
 
 def test_mixed_true_residual_on_the_host(sg, ctx, p3d, oracle):

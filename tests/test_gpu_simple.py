@@ -43,7 +43,7 @@ def _run(alg, kw, n_outer, n_inner):
 
 
 @pytest.mark.parametrize("name", ["simple_cavity_64_gmres_ilu.npz", "simple_channel_8x6x5_simplec.npz",
-                                  "simple_cavity_12_bdf2.npz"])
+                                  "simple_cavity_12_bdf2.npz", "simple_periodic_couette_8x6x4.npz"])
 def test_simple_runs_against_reference(sg, ctx, name):
     from simall_gb300 import workloads as W
 
