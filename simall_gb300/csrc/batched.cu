@@ -15,13 +15,15 @@
 // Storage per system: S A S as symmetric diagonal storage when the system is
 // numerically symmetric with at most kBatchDiags upper diagonals (every
 // structured grid in natural order), otherwise FP32 CSR of its off-diagonal
-// part; FP32 work vectors xh, rh, ph, qh; FP64 scale, b and x.  The SpMV uses
-// the row-sum form of the single-system mixed solver (per-row e_i summed in
-// FP64), which keeps the FP32 iteration count of pinned pressure systems close
-// to the FP64 one.  The CTA size
+// part; FP32 work vectors xh, rh, ph, qh; FP64 scale, b and x.  The entries
+// of S A S carry 8-bit corrections and every row of the SpMV is summed in
+// float-float arithmetic (ffop.cuh): on the pinned cavity systems of a batch
+// that keeps the inner iteration count at the FP64 one, where FP32 entries
+// and sums cost 15-30% more iterations.  The CTA size
 // (threads) and CTAs per SM are picked by a small autotuner that times each
 // candidate on the batch itself the first time a batch shape is solved.
 #include "device.cuh"
+#include "ffop.cuh"
 #include "solver.hpp"
 
 #include <algorithm>
@@ -70,7 +72,7 @@ struct simall_batch {
     simall::DevBuf<int32_t> rowPtr, colIdx, orow, ocol;
     simall::DevBuf<double> values, scale, b, x;
     simall::DevBuf<float> U, oval, xh, rh, ph, qh;
-    simall::DevBuf<float> E;  // per row: 1 + sum_j (S A S)_ij, summed in FP64 (row-sum form of the SpMV)
+    simall::DevBuf<int8_t> Uc, oc;  // 8-bit corrections of U / oval (ffop.cuh)
     simall::DevBuf<simall::BatchOut> out;
     std::vector<simall::BatchOut> h_out;
     int block = 0, ctas_per_sm = 0;  // autotuned launch shape
@@ -135,44 +137,52 @@ __device__ __forceinline__ double cta_allreduce_f(float a, double *red)
 // flight to stream a large system (one CTA per system).
 constexpr int kRowsPerPass = 8;
 
-// q = (S A S) p on rows [0, n) of one system in the row-sum form
-// q_i = e_i p_i - sum_j N_ij (p_i - p_j) (N: off-diagonal part of S A S, e_i
-// its row sum plus one, summed in FP64); returns this thread's p.q part.
+// q = (S A S) p on rows [0, n) of one system: q_i = p_i + sum_j N_ij p_j with
+// N (the off-diagonal part of S A S) as FP32 entries plus their 8-bit
+// corrections, the row summed in float-float (ffop.cuh); returns this thread's
+// p.q part.
 __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__restrict__ U,
-                                            const int32_t *__restrict__ orow, const int32_t *__restrict__ ocol,
-                                            const float *__restrict__ oval, const float *__restrict__ e,
-                                            const float *p, float *q)
+                                            const int8_t *__restrict__ Uc, const int32_t *__restrict__ orow,
+                                            const int32_t *__restrict__ ocol, const float *__restrict__ oval,
+                                            const int8_t *__restrict__ oc, const float *p, float *q)
 {
     float acc = 0.0f;
     const int n = S.n, B = blockDim.x;
     if (S.nd > 0) {
         const float *Us = U + S.u0;
+        const int8_t *Ucs = Uc + S.u0;
         for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * B) {
-            float pi[kRowsPerPass], y[kRowsPerPass];
+            float pi[kRowsPerPass];
+            FFAcc y[kRowsPerPass];
 #pragma unroll
             for (int u = 0; u < kRowsPerPass; ++u) {
                 const int i = i0 + u * B;
                 pi[u] = i < n ? p[i] : 0.0f;
-                y[u] = i < n ? e[i] * pi[u] : 0.0f;
+                y[u] = ff_start(pi[u]);
             }
             for (int d = 0; d < S.nd; ++d) {
                 const int off = S.off[d];
-                const float *Ud = Us + static_cast<int64_t>(d) * n;
+                const int64_t dd = static_cast<int64_t>(d) * n;
 #pragma unroll
                 for (int u = 0; u < kRowsPerPass; ++u) {
                     const int i = i0 + u * B;
-                    if (i < n && i + off < n)
-                        y[u] = __fmaf_rn(-Ud[i], pi[u] - p[i + off], y[u]);
-                    if (i < n && i - off >= 0)
-                        y[u] = __fmaf_rn(-Ud[i - off], pi[u] - p[i - off], y[u]);
+                    if (i < n && i + off < n) {
+                        const float a = Us[dd + i];
+                        ff_add(y[u], a, ff_low(a, Ucs[dd + i]), p[i + off]);
+                    }
+                    if (i < n && i - off >= 0) {
+                        const float a = Us[dd + i - off];
+                        ff_add(y[u], a, ff_low(a, Ucs[dd + i - off]), p[i - off]);
+                    }
                 }
             }
 #pragma unroll
             for (int u = 0; u < kRowsPerPass; ++u) {
                 const int i = i0 + u * B;
                 if (i < n) {
-                    q[i] = y[u];
-                    acc += pi[u] * y[u];
+                    const float qi = ff_value(y[u]);
+                    q[i] = qi;
+                    acc += pi[u] * qi;
                 }
             }
         }
@@ -180,13 +190,15 @@ __device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__re
         const int32_t *rp = orow + S.orp0;
         const int32_t *ci = ocol + S.u0;
         const float *va = oval + S.u0;
+        const int8_t *vc = oc + S.u0;
         for (int i = threadIdx.x; i < n; i += B) {
             const float pi = p[i];
-            float y = e[i] * pi;
+            FFAcc y = ff_start(pi);
             for (int k = rp[i]; k < rp[i + 1]; ++k)
-                y = __fmaf_rn(-va[k], pi - p[ci[k]], y);
-            q[i] = y;
-            acc += pi * y;
+                ff_add(y, va[k], ff_low(va[k], vc[k]), p[ci[k]]);
+            const float qi = ff_value(y);
+            q[i] = qi;
+            acc += pi * qi;
         }
     }
     return acc;
@@ -197,7 +209,8 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
                                 const int32_t *__restrict__ colIdx, const double *__restrict__ values,
                                 const float *__restrict__ U, const int32_t *__restrict__ orow,
                                 const int32_t *__restrict__ ocol, const float *__restrict__ oval,
-                                const float *__restrict__ e_all, const double *__restrict__ scale_all, const double *__restrict__ b_all,
+                                const int8_t *__restrict__ Uc, const int8_t *__restrict__ oc,
+                                const double *__restrict__ scale_all, const double *__restrict__ b_all,
                                 double *x_all, float *xh_all, float *rh_all, float *ph_all, float *qh_all, double tol,
                                 double delta, int maxit, BatchOut *out, double *red)
 {
@@ -232,7 +245,7 @@ __device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ r
     bool done = (t0 < tol) || maxit <= 0;
     while (!done) {
         // q = SAS p, alpha
-        const double pq = cta_allreduce_f(batch_spmv(S, U, orow, ocol, oval, e_all + S.row0, ph, qh), red);
+        const double pq = cta_allreduce_f(batch_spmv(S, U, Uc, orow, ocol, oval, oc, ph, qh), red);
         const bool breakdown = !(pq > 0.0);
         const float alpha = breakdown ? 0.0f : static_cast<float>(rho / pq);
         // xh += alpha p, rh -= alpha q (own rows: no barrier needed before)
@@ -337,7 +350,8 @@ __global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict
                               const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
                               const double *__restrict__ values, const float *__restrict__ U,
                               const int32_t *__restrict__ orow, const int32_t *__restrict__ ocol,
-                              const float *__restrict__ oval, const float *__restrict__ E,
+                              const float *__restrict__ oval, const int8_t *__restrict__ Uc,
+                              const int8_t *__restrict__ oc,
                               const double *__restrict__ scale, const double *__restrict__ b, double *x, float *xh,
                               float *rh, float *ph, float *qh, double tol, double delta, int maxit, BatchOut *out)
 {
@@ -353,7 +367,7 @@ __global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict
             return;
         const int id = order[k];
         const BatchSys S = sys[id];
-        batch_solve_one(S, rowPtr, colIdx, values, U, orow, ocol, oval, E, scale, b, x, xh, rh, ph, qh, tol, delta,
+        batch_solve_one(S, rowPtr, colIdx, values, U, orow, ocol, oval, Uc, oc, scale, b, x, xh, rh, ph, qh, tol, delta,
                         maxit, out + id, red);
     }
 }
@@ -368,7 +382,7 @@ int launch_batch(simall_batch *B, int block, int ctas_per_sm, const double *b, d
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(B->queue.p, 0, sizeof(int), ctx->stream));
     const int grid = std::max(1, std::min(B->nsys, ctx->num_sms * ctas_per_sm));
     k_batch_solve<<<grid, block, 0, ctx->stream>>>(B->sys.p, B->order.p, B->nsys, B->queue.p, B->rowPtr.p, B->colIdx.p,
-                                                   B->values.p, B->U.p, B->orow.p, B->ocol.p, B->oval.p, B->E.p,
+                                                   B->values.p, B->U.p, B->orow.p, B->ocol.p, B->oval.p, B->Uc.p, B->oc.p,
                                                    B->scale.p, b,
                                                    x, B->xh.p, B->rh.p, B->ph.p, B->qh.p, B->cfg.tolerance,
                                                    B->cfg.reliable_delta, B->cfg.max_iterations, B->out.p);
@@ -462,8 +476,8 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
         return fail(ctx, SIMALL_ERR_SIZE_MISMATCH, "batch offsets must start at 0 and grow");
     std::vector<BatchSys> sys(static_cast<size_t>(n_systems));
     std::vector<double> scale(static_cast<size_t>(rows));
-    std::vector<float> E(static_cast<size_t>(rows));
     std::vector<float> U;
+    std::vector<int8_t> Uc, oc;
     std::vector<int32_t> orow, ocol;
     std::vector<float> oval;
     std::vector<int32_t> offs;
@@ -519,13 +533,6 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             dia = false;
         dia = dia && sym;
         const double *sc = scale.data() + r0;
-        for (int64_t i = 0; i < n; ++i) {
-            double sum = 1.0;
-            for (int k = rp[i]; k < rp[i + 1]; ++k)
-                if (ci[k] != i)
-                    sum += va[k] * sc[i] * sc[ci[k]];
-            E[r0 + i] = static_cast<float>(sum);
-        }
         if (dia) {
             std::sort(offs.begin(), offs.end());
             S.nd = static_cast<int>(offs.size());
@@ -534,7 +541,9 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             S.u0 = static_cast<int64_t>(U.size());
             S.orp0 = 0;
             U.resize(U.size() + static_cast<size_t>(S.nd) * n, 0.0f);
+            Uc.resize(U.size(), 0);
             float *Us = U.data() + S.u0;
+            int8_t *Ucs = Uc.data() + S.u0;
             for (int64_t i = 0; i < n; ++i)
                 for (int k = rp[i]; k < rp[i + 1]; ++k) {
                     const int j = ci[k];
@@ -542,7 +551,10 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
                         continue;
                     const int d = static_cast<int>(std::find(offs.begin(), offs.end(), j - static_cast<int>(i)) -
                                                    offs.begin());
-                    Us[static_cast<int64_t>(d) * n + i] = static_cast<float>(va[k] * sc[i] * sc[j]);
+                    const double a = va[k] * sc[i] * sc[j];
+                    const int64_t t = static_cast<int64_t>(d) * n + i;
+                    Us[t] = static_cast<float>(a);
+                    Ucs[t] = ff_correction(a, Us[t]);
                 }
         } else {
             S.nd = 0;
@@ -554,8 +566,10 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             for (int64_t i = 0; i < n; ++i) {
                 for (int k = rp[i]; k < rp[i + 1]; ++k)
                     if (ci[k] != i) {
+                        const double a = va[k] * sc[i] * sc[ci[k]];
                         ocol.push_back(ci[k]);
-                        oval.push_back(static_cast<float>(va[k] * sc[i] * sc[ci[k]]));
+                        oval.push_back(static_cast<float>(a));
+                        oc.push_back(ff_correction(a, oval.back()));
                         ++cnt;
                     }
                 orow.push_back(cnt);
@@ -576,7 +590,6 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, B->colIdx.alloc(nnz));
     SIMALL_CUDA_TRY(ctx, B->values.alloc(nnz));
     SIMALL_CUDA_TRY(ctx, B->scale.alloc(rows));
-    SIMALL_CUDA_TRY(ctx, B->E.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->b.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->x.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->xh.alloc(rows));
@@ -584,6 +597,8 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, B->ph.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->qh.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->U.alloc(std::max<size_t>(U.size(), 1)));
+    SIMALL_CUDA_TRY(ctx, B->Uc.alloc(std::max<size_t>(Uc.size(), 1)));
+    SIMALL_CUDA_TRY(ctx, B->oc.alloc(std::max<size_t>(oc.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->orow.alloc(std::max<size_t>(orow.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->ocol.alloc(std::max<size_t>(ocol.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->oval.alloc(std::max<size_t>(oval.size(), 1)));
@@ -594,14 +609,16 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, up(B->colIdx.p, colIdx, nnz * sizeof(int32_t)));
     SIMALL_CUDA_TRY(ctx, up(B->values.p, values, nnz * sizeof(double)));
     SIMALL_CUDA_TRY(ctx, up(B->scale.p, scale.data(), scale.size() * sizeof(double)));
-    SIMALL_CUDA_TRY(ctx, up(B->E.p, E.data(), E.size() * sizeof(float)));
-    if (!U.empty())
+    if (!U.empty()) {
         SIMALL_CUDA_TRY(ctx, up(B->U.p, U.data(), U.size() * sizeof(float)));
+        SIMALL_CUDA_TRY(ctx, up(B->Uc.p, Uc.data(), Uc.size()));
+    }
     if (!orow.empty()) {
         SIMALL_CUDA_TRY(ctx, up(B->orow.p, orow.data(), orow.size() * sizeof(int32_t)));
         if (!ocol.empty()) {
             SIMALL_CUDA_TRY(ctx, up(B->ocol.p, ocol.data(), ocol.size() * sizeof(int32_t)));
             SIMALL_CUDA_TRY(ctx, up(B->oval.p, oval.data(), oval.size() * sizeof(float)));
+            SIMALL_CUDA_TRY(ctx, up(B->oc.p, oc.data(), oc.size()));
         }
     }
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // host staging vectors die here
