@@ -160,8 +160,11 @@ enum simall_solver_kind {
 
 /* SIMALL_ENGINE_AUTO: systems of up to 131,072 rows (Jacobi FP64, or mixed
  * precision in diagonal storage) run the whole solve on one thread-block
- * cluster; larger ones, and any solver with check_interval > 0, launch kernels
- * per iteration (mixed precision: one device-side graph loop).
+ * cluster; mixed precision in sliced storage (any pattern without diagonal
+ * structure, e.g. RCM-renumbered meshes) runs the whole solve in one
+ * persistent cooperative launch over all SMs; the rest, and any solver with
+ * check_interval > 0, launch kernels per iteration (mixed precision: one
+ * device-side graph loop).
  * SIMALL_ENGINE_KERNELS: always the per-iteration kernels. */
 enum simall_engine { SIMALL_ENGINE_AUTO = 0, SIMALL_ENGINE_KERNELS = 1 };
 
@@ -175,7 +178,8 @@ typedef struct simall_solver_stats {
     double b_norm;           /* ||b||_2 */
     double seconds;          /* wall time of the solve call */
     int engine;              /* what ran the iteration: 0 kernels per step (device graph loop or host-polled
-                                chunks), 1 one thread-block cluster for the whole solve */
+                                chunks), 1 one thread-block cluster for the whole solve, 2 one persistent
+                                cooperative launch for the whole solve */
     int preconditioner;      /* the preconditioner the solve used (CgGpu semantics: Jacobi after an ILU0
                                 fall-back) */
     double residual_norm;    /* ||r||_2 of the iterated residual at exit (GpuSolverStats::finalResidual) */

@@ -22,24 +22,29 @@
 
 #include <cmath>
 #include <cstdint>
+#include <cstring>
 
 namespace simall {
 
 // The 8-bit correction of an FP64 value a against its FP32 rounding u:
-// (a - u) in units of 2^(E(u) - 30), E(u) u's binary exponent; 0 where u is 0
-// or below 2^-96 (the correction would leave FP32's normal range).
-inline int8_t ff_correction(double a, float u)
+// (a - u) in units of 2^(E - 157) = ulp(u) / 128, E u's biased exponent; 0
+// where u is 0, not finite or below 2^-96 (the unit would leave FP32's normal
+// range).  The same operations on the host and the device: an exact FP64
+// difference, a multiplication by a power of two and a round-to-nearest-even.
+__host__ __device__ inline int8_t ff_correction(double a, float u)
 {
-    if (u == 0.0f || !std::isfinite(u) || std::fabs(u) < 1.2621774483536189e-29f)  // 2^-96
+    const float au = u < 0.0f ? -u : u;
+    if (!(au >= 1.2621774483536189e-29f) || !(au <= 3.4028234663852886e38f))  // [2^-96, FLT_MAX]
         return 0;
-    int e = 0;
-    std::frexp(static_cast<double>(u), &e);       // |u| = m 2^e, m in [0.5, 1): ulp(u) = 2^(e - 24)
-    const double unit = std::ldexp(1.0, e - 31);  // ulp(u) / 128
-    const double k = std::nearbyint((a - static_cast<double>(u)) / unit);
+    uint32_t bits = 0;
+    memcpy(&bits, &u, sizeof bits);
+    const int E = static_cast<int>((bits >> 23) & 0xffu);
+    const double k = rint((a - static_cast<double>(u)) * ldexp(1.0, 157 - E));
     return static_cast<int8_t>(k > 127.0 ? 127 : (k < -127.0 ? -127 : k));
 }
 
-// The correction's value, exact in FP32: k 2^(E(u) - 30).
+// The correction's value, exact in FP32: k 2^(E - 157), E u's biased exponent
+// (the float whose exponent field is E - 30).
 __device__ __forceinline__ float ff_low(float u, int8_t k)
 {
     const int ebits = __float_as_int(u) & 0x7f800000;

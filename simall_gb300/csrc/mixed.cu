@@ -18,9 +18,14 @@
 // entries lie on at most kMaxDiags distinct diagonals (every structured grid
 // in natural order), only the upper diagonals are stored, FP32, one array per
 // offset: 4 B per stored diagonal per row and no column indices.  Otherwise
-// the off-diagonal entries are kept as FP32 CSR.
+// the off-diagonal entries are kept in sliced storage (sell.cuh: slices of 32
+// rows, entry-major, 16-bit column offsets where the bandwidth allows, FP32
+// values with 8-bit corrections, 7 B per entry) and the product is the
+// compensated plain form of ffop.cuh.  With the default engine the sliced
+// form runs the whole solve in one persistent cooperative launch
+// (mixed_grid.cu); per-step kernels otherwise.
 //
-// Row-sum form of the product.  With N the off-diagonal part of S A S and
+// Row-sum form of the product (diagonal storage).  With N the off-diagonal part of S A S and
 // e_i = 1 + sum_j N_ij (summed in FP64 from A, stored rounded to FP32), the
 // inner SpMV evaluates
 //     q_i = e_i p_i - sum_j N_ij (p_i - p_j)
@@ -34,6 +39,7 @@
 // cell) the FP32 inner CG needs 1075 iterations with the plain form and 776
 // with this one, against 775 for FP64 CG; it costs one 4-byte stream per row.
 #include "device.cuh"
+#include "sell.cuh"
 #include "solver.hpp"
 
 #include <algorithm>
@@ -55,18 +61,27 @@ struct MixedData {
     DiaOffsets offs{};
     DevBuf<float> U;          // [nd][ldU] upper diagonals of S A S (dia)
     int64_t ldU = 0;          // diagonal stride, n rounded up to 4 (16-byte aligned rows)
-    DevBuf<int32_t> orow;     // off-diagonal CSR rowPtr (csr)
-    DevBuf<int32_t> ocol;
-    DevBuf<float> oval;
+    // sliced storage (sell.cuh) of every other pattern
+    int64_t nslices = 0;
+    int64_t sEntries = 0;      // stored entries, padding included (32 per slice per unit of width)
+    bool sWide = false;        // int32 column offsets
+    DevBuf<int32_t> sptr;      // [nslices + 1]
+    DevBuf<int16_t> soff16;
+    DevBuf<int32_t> soff32;
+    DevBuf<int32_t> spos;      // CSR position of each stored entry, -1 for padding
+    DevBuf<float> sval;
+    DevBuf<int8_t> scor;
+    // the persistent engine's grid reduction buffers and barrier (mixed_grid.cu)
+    DevBuf<double> gpart;
+    DevBuf<unsigned long long> gctr;
+    DevBuf<int> gerr;
+    bool noGrid = false;       // cooperative launch unavailable or refused: per-step kernels
     DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
-    DevBuf<float> e;          // e_i = 1 + sum_j (S A S)_ij, summed in FP64 from A, then rounded
+    DevBuf<float> e;          // dia: e_i = 1 + sum_j (S A S)_ij, summed in FP64 from A, then rounded
     DevBuf<float> xh;         // FP32 correction, folded into x at reliable updates
     DevBuf<float> rv[2], qv[2], pv[2];  // r, q = (S A S) p, p; double-buffered by step parity
-    int nnzOff = 0;
     bool patternReady = false;
     bool noDeviceLoop = false;  // conditional graph nodes unavailable
-    std::vector<int32_t> h_orow, h_ocol, h_opos;  // csr: host pattern and the source position of each entry
-    DevBuf<int32_t> opos;
 };
 
 namespace {
@@ -167,14 +182,34 @@ __global__ void __launch_bounds__(kBlock) k_mx_row_defect(int64_t n, const int32
     }
 }
 
-__global__ void __launch_bounds__(kBlock) k_mx_build_csr(int nOff, const int32_t *__restrict__ orowOfEntry,
-                                                         const int32_t *__restrict__ ocol,
-                                                         const int32_t *__restrict__ opos,
-                                                         const double *__restrict__ val, const double *__restrict__ sc,
-                                                         float *__restrict__ oval)
+// Values of the sliced storage: N_ij = a_ij s_i s_j in FP64 (the product in
+// that order), stored rounded to FP32 with its 8-bit correction; padding
+// entries 0.  One thread per row.
+__global__ void __launch_bounds__(kBlock) k_mx_build_sell(int64_t n, const int32_t *__restrict__ sptr,
+                                                          const int32_t *__restrict__ spos,
+                                                          const int32_t *__restrict__ colIdx,
+                                                          const double *__restrict__ val, const double *__restrict__ sc,
+                                                          float *__restrict__ sval, int8_t *__restrict__ scor)
 {
-    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < nOff; e += gridDim.x * blockDim.x)
-        oval[e] = static_cast<float>(val[opos[e]] * sc[orowOfEntry[e]] * sc[ocol[e]]);
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t sl = i >> 5;
+        const int32_t e0 = sptr[sl];
+        const int w = (sptr[sl + 1] - e0) >> 5;
+        const double si = sc[i];
+        for (int k = 0; k < w; ++k) {
+            const int64_t e = static_cast<int64_t>(e0) + static_cast<int64_t>(k) * 32 + (i & 31);
+            const int pos = spos[e];
+            float u = 0.0f;
+            int8_t c = 0;
+            if (pos >= 0) {
+                const double a = val[pos] * si * sc[colIdx[pos]];
+                u = static_cast<float>(a);
+                c = ff_correction(a, u);
+            }
+            sval[e] = u;
+            scor[e] = c;
+        }
+    }
 }
 
 // ---------------------------------------------------------------- iteration kernels
@@ -256,13 +291,6 @@ __device__ __forceinline__ void dfma4(float (&y)[4], float4 a, float4 p, float4 
 //
 // FRESH: the step after a residual replacement (and the first step): r is
 // the replaced residual, read from r_out and not rewritten; alpha = 0.
-template <bool FRESH>
-__device__ __forceinline__ float pdir(float r, float q, float p, float alpha, float beta)
-{
-    const float rn = FRESH ? r : __fmaf_rn(-alpha, q, r);
-    return __fmaf_rn(beta, p, rn);
-}
-
 template <bool FRESH>
 __device__ __forceinline__ float4 pdir4(float4 r, float4 q, float4 p, float alpha, float beta)
 {
@@ -537,59 +565,20 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_iter_dia(int n, int64_t ldU, D
         mx_finish<FRESH>(s, t);
 }
 
-// FP32 CSR storage of the off-diagonal part (unit diagonal).  Thread per row.
-template <bool FRESH>
-__global__ void __launch_bounds__(kBlock) k_mx_iter_csr(int64_t n, const int32_t *__restrict__ orow,
-                                                        const int32_t *__restrict__ ocol,
-                                                        const float *__restrict__ oval, const float *__restrict__ e,
-                                                        IterVecs v, double *partials, SolveScalars *s)
+// Sliced storage (sell.cuh): a warp per slice of 32 rows, grid-stride over
+// the slices.
+template <bool FRESH, bool WIDE>
+__global__ void __launch_bounds__(kBlock) k_mx_iter_sell(SellOp A, IterVecs v, double *partials, SolveScalars *s)
 {
     if (mx_skip<FRESH>(s))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
-    const float *__restrict__ rs = FRESH ? v.rout : v.rin;
-    const float *__restrict__ qs = v.qin;
-    const float *__restrict__ ps = v.pin;
+    const float *rs = FRESH ? v.rout : v.rin;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-        const float ro = __ldg(rs + i), po = __ldg(ps + i);
-        const float ri = FRESH ? ro : __fmaf_rn(-alpha, __ldg(qs + i), ro);
-        const float pi = __fmaf_rn(beta, po, ri);
-        if (!FRESH) {
-            v.rout[i] = ri;
-            v.xh[i] = __fmaf_rn(alpha, po, v.xh[i]);
-        }
-        v.pout[i] = pi;
-        float y = __ldg(e + i) * pi;
-        // the row's entries eight at a time: indices and values, then the
-        // gathers, all issued before the arithmetic (column order kept)
-        const int k1 = __ldg(orow + i + 1);
-        for (int k0 = __ldg(orow + i); k0 < k1; k0 += 8) {
-            int c[8];
-            float a[8], gr[8], gq[8], gp[8];
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                c[q] = k0 + q < k1 ? __ldg(ocol + k0 + q) : -1;
-                a[q] = k0 + q < k1 ? __ldg(oval + k0 + q) : 0.0f;
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q) {
-                gr[q] = c[q] >= 0 ? __ldg(rs + c[q]) : 0.0f;
-                gq[q] = (!FRESH && c[q] >= 0) ? __ldg(qs + c[q]) : 0.0f;
-                gp[q] = c[q] >= 0 ? __ldg(ps + c[q]) : 0.0f;
-            }
-#pragma unroll
-            for (int q = 0; q < 8; ++q)
-                if (c[q] >= 0)
-                    y = __fmaf_rn(-a[q], pi - pdir<FRESH>(gr[q], gq[q], gp[q], alpha, beta), y);
-        }
-        v.qout[i] = y;
-        acc[0] += pi * y;
-        acc[1] += y * y;
-        acc[2] += ri * ri;
-        acc[3] += ri * y;
-    }
+    const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
+    for (int64_t sl = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; sl < A.nslices; sl += nw)
+        sell_slice<FRESH, WIDE, true>(A, sl, rs, v.qin, v.pin, v.rout, v.qout, v.pout, v.xh, alpha, beta, acc);
     double t[4];
     if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0)
         mx_finish<FRESH>(s, t);
@@ -745,6 +734,88 @@ __global__ void __launch_bounds__(kBlock) k_mx_offsets(int64_t n, const int32_t 
     }
 }
 
+// The sliced storage's pattern from a host copy of A's: slice widths, each
+// stored entry's CSR position (-1 for padding) and column offset, narrow
+// offsets when every |j - i| fits 16 bits.
+int build_sell_pattern(simall_solver *s, MixedData *m)
+{
+    simall_context *ctx = s->ctx;
+    const int64_t n = s->n;
+    int st = solver_host_pattern(s);
+    if (st)
+        return st;
+    const int32_t *rp = s->h_rowPtr.data(), *ci = s->h_colIdx.data();
+    const int64_t ns = (n + 31) / 32;
+    std::vector<int32_t> sptr(static_cast<size_t>(ns) + 1, 0);
+    int64_t total = 0;
+    for (int64_t sl = 0; sl < ns; ++sl) {
+        int w = 0;
+        for (int64_t i = sl * 32; i < std::min(n, sl * 32 + 32); ++i) {
+            int c = 0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                c += ci[k] != i ? 1 : 0;
+            w = std::max(w, c);
+        }
+        sptr[sl] = static_cast<int32_t>(total);
+        total += 32 * static_cast<int64_t>(w);
+        if (total > INT32_MAX)
+            return fail(ctx, SIMALL_ERR_UNSUPPORTED, "mixed precision: sliced storage above 2^31 entries");
+    }
+    sptr[ns] = static_cast<int32_t>(total);
+    std::vector<int32_t> pos(static_cast<size_t>(total), -1), off(static_cast<size_t>(total), 0);
+    int64_t band = 0;
+    for (int64_t i = 0; i < n; ++i) {
+        int64_t e = sptr[i >> 5] + (i & 31);
+        for (int k = rp[i]; k < rp[i + 1]; ++k)
+            if (ci[k] != i) {
+                pos[e] = k;
+                off[e] = static_cast<int32_t>(ci[k] - i);
+                band = std::max<int64_t>(band, std::abs(static_cast<int64_t>(off[e])));
+                e += 32;
+            }
+    }
+    m->nslices = ns;
+    m->sEntries = total;
+    m->sWide = band > 32767;
+    const size_t cap = static_cast<size_t>(std::max<int64_t>(total, 1));
+    SIMALL_CUDA_TRY(ctx, m->sptr.alloc(static_cast<size_t>(ns) + 1));
+    SIMALL_CUDA_TRY(ctx, m->spos.alloc(cap));
+    SIMALL_CUDA_TRY(ctx, m->sval.alloc(cap));
+    SIMALL_CUDA_TRY(ctx, m->scor.alloc(cap));
+    SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->sptr.p, sptr.data(), sptr.size() * sizeof(int32_t),
+                                         cudaMemcpyHostToDevice, ctx->stream));
+    std::vector<int16_t> off16;
+    if (total > 0) {
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->spos.p, pos.data(), pos.size() * sizeof(int32_t),
+                                             cudaMemcpyHostToDevice, ctx->stream));
+        if (m->sWide) {
+            SIMALL_CUDA_TRY(ctx, m->soff32.alloc(cap));
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->soff32.p, off.data(), off.size() * sizeof(int32_t),
+                                                 cudaMemcpyHostToDevice, ctx->stream));
+        } else {
+            off16.assign(off.begin(), off.end());
+            SIMALL_CUDA_TRY(ctx, m->soff16.alloc(cap));
+            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->soff16.p, off16.data(), off16.size() * sizeof(int16_t),
+                                                 cudaMemcpyHostToDevice, ctx->stream));
+        }
+    }
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // the host arrays die here
+    return SIMALL_OK;
+}
+
+SellOp sell_op(const simall_solver *s, const MixedData *m)
+{
+    SellOp A;
+    A.n = s->n;
+    A.nslices = m->nslices;
+    A.sptr = m->sptr.p;
+    A.off16 = m->soff16.p;
+    A.off32 = m->soff32.p;
+    A.val = m->sval.p;
+    A.cor = m->scor.p;
+    return A;
+}
+
 // Choose the storage format of S A S from the pattern (diagonal storage only
 // if allowed).  The diagonal test runs on the device; the CSR fallback is
 // built from a host copy of the pattern.
@@ -786,22 +857,9 @@ int analyse_pattern(simall_solver *s, MixedData *m, bool allow_dia)
         for (int d = 0; d < kMaxDiags; ++d)
             m->offs.off[d] = d < m->offs.nd ? offs[d] : 0;
     } else {
-        int st = solver_host_pattern(s);
+        int st = build_sell_pattern(s, m);
         if (st)
             return st;
-        const int32_t *rp = s->h_rowPtr.data(), *ci = s->h_colIdx.data();
-        m->h_orow.assign(static_cast<size_t>(n) + 1, 0);
-        m->h_ocol.clear();
-        m->h_opos.clear();
-        for (int64_t i = 0; i < n; ++i) {
-            for (int k = rp[i]; k < rp[i + 1]; ++k)
-                if (ci[k] != i) {
-                    m->h_ocol.push_back(ci[k]);
-                    m->h_opos.push_back(k);
-                }
-            m->h_orow[i + 1] = static_cast<int32_t>(m->h_ocol.size());
-        }
-        m->nnzOff = static_cast<int>(m->h_ocol.size());
     }
     m->patternReady = true;
     return SIMALL_OK;
@@ -825,9 +883,14 @@ template <bool FRESH> int launch_iter_t(simall_context *ctx, simall_solver *s, M
     const int64_t n = s->n;
     const IterVecs v = iter_vecs(m, par);
     if (!m->dia) {
-        const void *fn = reinterpret_cast<const void *>(k_mx_iter_csr<FRESH>);
-        k_mx_iter_csr<FRESH><<<resident_grid(ctx, fn, n), kBlock, 0, ctx->stream>>>(
-            n, m->orow.p, m->ocol.p, m->oval.p, m->e.p, v, s->partials.p, s->scal.p);
+        const SellOp A = sell_op(s, m);
+        const void *fn = m->sWide ? reinterpret_cast<const void *>(k_mx_iter_sell<FRESH, true>)
+                                  : reinterpret_cast<const void *>(k_mx_iter_sell<FRESH, false>);
+        const int grid = resident_grid(ctx, fn, m->nslices * 32);
+        if (m->sWide)
+            k_mx_iter_sell<FRESH, true><<<grid, kBlock, 0, ctx->stream>>>(A, v, s->partials.p, s->scal.p);
+        else
+            k_mx_iter_sell<FRESH, false><<<grid, kBlock, 0, ctx->stream>>>(A, v, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
@@ -890,7 +953,6 @@ int mixed_setup(simall_solver *s)
     }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
     SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
-    SIMALL_CUDA_TRY(ctx, m->e.alloc(n + 4));
     for (int k = 0; k < 2; ++k) {
         SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
         SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
@@ -915,9 +977,10 @@ int mixed_setup(simall_solver *s)
         if (st)
             return st;
     }
-    k_mx_row_defect<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->e.p);
-    SIMALL_LAUNCH_CHECK(ctx);
     if (m->dia) {
+        SIMALL_CUDA_TRY(ctx, m->e.alloc(n + 4));
+        k_mx_row_defect<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->e.p);
+        SIMALL_LAUNCH_CHECK(ctx);
         m->ldU = (n + 3) & ~static_cast<int64_t>(3);
         SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * m->ldU));
         SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(m->U.p, 0, static_cast<size_t>(m->offs.nd) * m->ldU * sizeof(float),
@@ -925,32 +988,10 @@ int mixed_setup(simall_solver *s)
         k_mx_build_dia<<<g, kBlock, 0, ctx->stream>>>(n, m->ldU, s->rowPtr, s->colIdx, s->values, m->scale.p, m->offs,
                                                       m->U.p);
         SIMALL_LAUNCH_CHECK(ctx);
-    } else {
-        const int no = m->nnzOff;
-        SIMALL_CUDA_TRY(ctx, m->orow.alloc(n + 1));
-        SIMALL_CUDA_TRY(ctx, m->ocol.alloc(no > 0 ? no : 1));
-        SIMALL_CUDA_TRY(ctx, m->opos.alloc(no > 0 ? no : 1));
-        SIMALL_CUDA_TRY(ctx, m->oval.alloc(no > 0 ? no : 1));
-        std::vector<int32_t> rowOf(static_cast<size_t>(no));
-        for (int64_t i = 0; i < n; ++i)
-            for (int k = m->h_orow[i]; k < m->h_orow[i + 1]; ++k)
-                rowOf[k] = static_cast<int32_t>(i);
-        DevBuf<int32_t> dRowOf;
-        SIMALL_CUDA_TRY(ctx, dRowOf.alloc(no > 0 ? no : 1));
-        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->orow.p, m->h_orow.data(), (n + 1) * sizeof(int32_t),
-                                             cudaMemcpyHostToDevice, ctx->stream));
-        if (no > 0) {
-            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->ocol.p, m->h_ocol.data(), no * sizeof(int32_t),
-                                                 cudaMemcpyHostToDevice, ctx->stream));
-            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->opos.p, m->h_opos.data(), no * sizeof(int32_t),
-                                                 cudaMemcpyHostToDevice, ctx->stream));
-            SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(dRowOf.p, rowOf.data(), no * sizeof(int32_t), cudaMemcpyHostToDevice,
-                                                 ctx->stream));
-            k_mx_build_csr<<<grid_n(ctx, no), kBlock, 0, ctx->stream>>>(no, dRowOf.p, m->ocol.p, m->opos.p, s->values,
-                                                                        m->scale.p, m->oval.p);
-            SIMALL_LAUNCH_CHECK(ctx);
-        }
-        SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // dRowOf and rowOf die here
+    } else if (m->sEntries > 0) {
+        k_mx_build_sell<<<g, kBlock, 0, ctx->stream>>>(n, m->sptr.p, m->spos.p, s->colIdx, s->values, m->scale.p,
+                                                       m->sval.p, m->scor.p);
+        SIMALL_LAUNCH_CHECK(ctx);
     }
     return SIMALL_OK;
 }
@@ -1118,6 +1159,38 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
                     cudaMemcpyAsync(&s->scal.p->delta, &delta, sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
     SIMALL_CUDA_TRY(ctx,
                     cudaMemcpyAsync(&s->scal.p->max_iter, &maxit, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+    if (!m->dia && !m->noGrid && s->cfg.check_interval <= 0 && s->cfg.engine == SIMALL_ENGINE_AUTO) {
+        const size_t cap = static_cast<size_t>(ctx->num_sms) * kGridMaxCtasPerSm * 8;
+        if (m->gpart.n < cap)
+            SIMALL_CUDA_TRY(ctx, m->gpart.alloc(cap));
+        if (!m->gctr.p)
+            SIMALL_CUDA_TRY(ctx, m->gctr.alloc(1));
+        if (!m->gerr.p)
+            SIMALL_CUDA_TRY(ctx, m->gerr.alloc(1));
+        GridMixedArgs a{};
+        a.nslices = m->nslices;
+        a.wide = m->sWide;
+        a.sptr = m->sptr.p;
+        a.off16 = m->soff16.p;
+        a.off32 = m->soff32.p;
+        a.sval = m->sval.p;
+        a.scor = m->scor.p;
+        a.scale = m->scale.p;
+        for (int k = 0; k < 2; ++k) {
+            a.r[k] = m->rv[k].p;
+            a.q[k] = m->qv[k].p;
+            a.p[k] = m->pv[k].p;
+        }
+        a.xh = m->xh.p;
+        a.part = m->gpart.p;
+        a.partCap = m->gpart.n;
+        a.ctr = m->gctr.p;
+        a.err = m->gerr.p;
+        int gst = SIMALL_OK;
+        if (grid_mixed_solve(s, a, &gst))
+            return gst;
+        m->noGrid = true;  // not available on this device: per-step kernels from now on
+    }
     if (m->dia && s->cfg.check_interval <= 0 && s->cfg.engine == SIMALL_ENGINE_AUTO) {
         ClusterMixedArgs a{};
         a.U = m->U.p;
@@ -1210,9 +1283,14 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     const double nd = static_cast<double>(s->n);
     if (k != 4)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);
-    // r, q, p read at parity 0 and written at parity 1, xh read and written,
-    // e read, plus the matrix (each gathered vector counted once)
-    *bytes = m->dia ? (4.0 * m->offs.nd + 36.0) * nd : 8.0 * m->nnzOff + 40.0 * nd + 4.0;
+    // r, q, p read at parity 0 and written at parity 1, xh read and written
+    // (each gathered vector counted once), plus the matrix: diagonal storage
+    // 4 B per stored diagonal per row and e; sliced storage 7 B per stored
+    // entry (9 B with wide offsets: offset, value, correction) and the slice
+    // pointers
+    *bytes = m->dia ? (4.0 * m->offs.nd + 36.0) * nd
+                    : (m->sWide ? 9.0 : 7.0) * static_cast<double>(m->sEntries) + 32.0 * nd +
+                          4.0 * static_cast<double>(m->nslices + 1);
     return launch_iter(ctx, s, 0, false);
 }
 

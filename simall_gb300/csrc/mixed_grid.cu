@@ -1,0 +1,479 @@
+// Mixed-precision CG in one persistent cooperative launch (sliced storage).
+//
+// The per-step kernels of mixed.cu run one launch per CG step inside a
+// device-side graph loop; between two steps the graph pays a controller
+// kernel, a conditional node and the launch latency of the next step, about
+// 7 us on GB300 -- a quarter of a step at 128^3.  Here every CTA stays
+// resident for the whole solve (cudaLaunchCooperativeKernel guarantees that
+// all of them are), and a step ends in one grid barrier:
+//   - each CTA reduces its threads' four FP32 partial sums (FP64 across
+//     warps) and publishes them in slot [epoch & 1][cta] of a double buffer;
+//   - thread 0 releases its CTA's writes and adds one to a 64-bit arrival
+//     counter, then polls it with acquire loads until all gridDim.x CTAs of
+//     this epoch have arrived (bounded: ~4 s by %globaltimer, then the CTA
+//     records a timeout and leaves; every other CTA then times out at its
+//     next barrier, so the launch always ends);
+//   - every CTA reads all partials in the same order and reduces them in the
+//     same tree, so all CTAs hold bit-identical totals and take identical
+//     decisions (step length, reliable update, stop) without another barrier.
+// A CTA can be at most one barrier ahead of any other, so two partial slots
+// suffice.  Vectors written in one step are read by other CTAs in the next:
+// those loads are plain (coherent) loads, ordered by the barrier's acquire;
+// only the matrix goes through the read-only path.
+//
+// The algorithm is the one of mixed.cu step for step (the fused step of
+// sell.cuh, van der Vorst-Ye reliable updates with the same trigger, the FP64
+// true residual r = b - A x from the original CSR, the stop test on it), so
+// iteration counts and results agree with the per-step engine up to the
+// order of the FP32 partial sums.  A reliable update costs two more barriers
+// (after the fold x += S xh, and after the true residual with the FP32
+// replacement r = S (b - A x) written in the same pass).
+#include "device.cuh"
+#include "sell.cuh"
+#include "solver.hpp"
+
+#include <algorithm>
+#include <cmath>
+
+namespace simall {
+
+namespace {
+
+constexpr unsigned long long kGridWaitNs = 4000000000ull;  // one barrier wait gives up after ~4 s
+
+struct GridArgs {
+    SellOp A;
+    const int32_t *rowPtr;
+    const int32_t *colIdx;
+    const double *val;
+    const double *b;
+    const double *sc;
+    double *x;
+    float *r[2], *q[2], *p[2];
+    float *xh;
+    double *part;  // [2][gridDim.x][4]
+    unsigned long long *ctr;
+    int *err;
+    SolveScalars *s;
+    double tol, delta;
+    int max_iter;
+};
+
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p)
+{
+    unsigned long long v;
+    asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ unsigned long long global_ns()
+{
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+// Grid barrier of epoch `epoch` (1, 2, ...): returns false (in every thread of
+// the CTA) when the wait ran out.
+__device__ bool grid_barrier(unsigned long long *ctr, unsigned long long epoch, int *err)
+{
+    __shared__ int ok;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        __threadfence();
+        atomicAdd(ctr, 1ull);
+        const unsigned long long target = epoch * gridDim.x;
+        int good = 1;
+        if (ld_acquire(ctr) < target) {
+            const unsigned long long t0 = global_ns();
+            for (unsigned spins = 1; ld_acquire(ctr) < target; ++spins)
+                if ((spins & 63u) == 0 && global_ns() - t0 > kGridWaitNs) {
+                    good = 0;
+                    atomicExch(err, 1);
+                    break;
+                }
+        }
+        __threadfence();
+        ok = good;
+    }
+    __syncthreads();
+    return ok != 0;
+}
+
+// Sum of NV FP64 values over the grid, the same bits in every CTA: block
+// tree, one slot per CTA, barrier, then every CTA sums all slots in index
+// order and reduces them in the same tree.  Returns false on a barrier
+// timeout.
+template <int NV>
+__device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *ctr, unsigned long long &epoch,
+                            int *err)
+{
+    __shared__ double tot[NV];
+    block_sum<NV>(v);
+    double *slot = part + (epoch & 1ull) * gridDim.x * NV;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            slot[static_cast<int64_t>(blockIdx.x) * NV + k] = v[k];
+    }
+    ++epoch;
+    if (!grid_barrier(ctr, epoch, err))
+        return false;
+    double acc[NV];
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        acc[k] = 0.0;
+    for (unsigned c = threadIdx.x; c < gridDim.x; c += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            acc[k] += __ldcg(slot + static_cast<int64_t>(c) * NV + k);
+    }
+    block_sum<NV>(acc);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            tot[k] = acc[k];
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        v[k] = tot[k];
+    __syncthreads();
+    return true;
+}
+
+// FP32 per-thread partials: lanes summed in FP32, everything above in FP64.
+template <int NV>
+__device__ bool grid_allsum_f(const float (&v)[NV], double (&out)[NV], double *part, unsigned long long *ctr,
+                              unsigned long long &epoch, int *err)
+{
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        float w = v[k];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1)
+            w += __shfl_down_sync(0xffffffffu, w, o);
+        out[k] = (threadIdx.x & 31) == 0 ? static_cast<double>(w) : 0.0;  // block_sum adds lane 0 of each warp
+    }
+    return grid_allsum<NV>(out, part, ctr, epoch, err);
+}
+
+// The solver state and its transitions: mixed.cu's k_mx_init, mx_finish,
+// mx_step and k_mx_true_residual / k_mx_replace, on totals every CTA holds.
+struct GridState {
+    double bnorm, rz, sigma0, rmax, t0, last, rr_true, alpha, beta;
+    float alpha_f, beta_f;  // the step's FP32 coefficients
+    int iter, updates, need, done, result, status, par;
+    bool fresh;   // the next step forms p from a replaced residual
+    bool update;  // the step just finished asks for a reliable update
+
+    __device__ void start(double sbb, double bb, double tol, int max_iter)
+    {
+        const double bn = sqrt(bb);
+        bnorm = bn > 1e-30 ? bn : 1e-30;
+        rz = sbb;
+        sigma0 = sqrt(sbb);
+        rmax = sigma0;
+        t0 = bn / bnorm;
+        last = t0;
+        rr_true = bb;
+        alpha = beta = 0.0;
+        alpha_f = beta_f = 0.0f;
+        iter = updates = result = 0;
+        need = 2;  // the first (FRESH) step is not counted as an update
+        done = 0;
+        status = SIMALL_OK;
+        par = 1;   // the first step forms p = r (beta = 0) at parity 1
+        fresh = true;
+        update = false;
+        if (t0 < tol) {
+            done = 1;  // b == 0: x = 0 is exact
+        } else if (max_iter <= 0) {
+            done = 1;
+            result = max_iter;
+        }
+    }
+
+    __device__ void coefficients(const double (&t)[4])
+    {
+        const double pq = t[0], qq = t[1], rr = t[2], rq = t[3];
+        if (!(pq > 0.0) || !(rr > 0.0)) {  // not SPD in FP32, or exact breakdown
+            status = SIMALL_ERR_BREAKDOWN;
+            need = 1;
+            alpha = beta = 0.0;
+        } else {
+            alpha = rr / pq;
+            const double next = rr - 2.0 * alpha * rq + alpha * alpha * qq;
+            beta = (next > 0.0 ? next : 0.0) / rr;
+        }
+        alpha_f = static_cast<float>(alpha);
+        beta_f = static_cast<float>(beta);
+    }
+
+    __device__ void finish_step(const double (&t)[4], double tol, double delta, int max_iter)
+    {
+        const double rr = t[2];
+        if (fresh) {
+            rz = rr;
+            sigma0 = sqrt(rr);
+            rmax = sigma0;
+            if (need == 1)
+                ++updates;
+            need = 0;
+            coefficients(t);
+            fresh = false;
+            par ^= 1;
+            update = need == 1;
+            return;
+        }
+        ++iter;
+        const double sigma = sqrt(rr);
+        const double est = t0 * sigma / sigma0;
+        last = est;
+        if (need || sigma < delta * rmax || est < tol || iter >= max_iter) {
+            need = 1;  // fold, true residual, replacement, then a FRESH step at this parity
+            update = true;
+            return;
+        }
+        if (sigma > rmax)
+            rmax = sigma;
+        rz = rr;
+        coefficients(t);
+        par ^= 1;
+        update = need == 1;
+    }
+
+    // a = {|b - A x|^2, |S (b - A x)|^2 of the FP32 replacement}
+    __device__ void finish_update(const double (&a)[2], double tol, int max_iter)
+    {
+        rr_true = a[0];
+        const double tt = sqrt(a[0]) / bnorm;
+        last = tt;
+        t0 = tt;
+        update = false;
+        if (tt < tol) {
+            done = 1;
+            result = iter;
+        } else if (iter >= max_iter || status == SIMALL_ERR_BREAKDOWN) {
+            done = 1;
+            result = iter >= max_iter ? max_iter : iter;
+        } else {
+            beta = a[1] / rz;
+            beta_f = static_cast<float>(beta);
+            fresh = true;
+        }
+    }
+
+    __device__ void stop(int why)
+    {
+        status = why;
+        done = 1;
+        result = iter;
+    }
+
+    __device__ void publish(SolveScalars *s, bool ok) const
+    {
+        s->rz = rz;
+        s->alpha = alpha;
+        s->beta = beta;
+        s->rr = rr_true;
+        s->bnorm = bnorm;
+        s->last = last;
+        s->sigma0 = sigma0;
+        s->t0 = t0;
+        s->rmax = rmax;
+        s->iter = iter;
+        s->result = result;
+        s->done = done;
+        s->status = ok ? status : SIMALL_ERR_TIMEOUT;
+        s->need_update = 0;
+        s->updates = updates;
+    }
+};
+
+template <bool WIDE>
+__global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
+{
+    const int64_t n = g.A.n;
+    const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t nthr = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    const int64_t warp = tid >> 5, nwarps = nthr >> 5;
+    unsigned long long epoch = 0;
+    bool ok = true;
+
+    // init: x = 0, r[0] = S b, p[1] = 0, xh = 0; |S b|^2 (FP32 rows), |b|^2
+    double tot[2];
+    {
+        float a0 = 0.0f;
+        double a1 = 0.0;
+        for (int64_t i = tid; i < n; i += nthr) {
+            const double bi = g.b[i];
+            const float r = static_cast<float>(bi * g.sc[i]);
+            g.x[i] = 0.0;
+            g.r[0][i] = r;
+            g.p[1][i] = 0.0f;
+            g.xh[i] = 0.0f;
+            a0 += r * r;
+            a1 += bi * bi;
+        }
+        float f[1] = {a0};
+        double d1[1];
+        ok = grid_allsum_f<1>(f, d1, g.part, g.ctr, epoch, g.err);
+        double d2[1] = {a1};
+        ok = ok && grid_allsum<1>(d2, g.part, g.ctr, epoch, g.err);
+        tot[0] = d1[0];
+        tot[1] = d2[0];
+    }
+    // The solver state: identical in every CTA (it follows from the identical
+    // totals), kept in shared memory and advanced by thread 0 alone after each
+    // grid sum; the other threads read the control values after a block barrier.
+    __shared__ GridState st;
+    if (threadIdx.x == 0)
+        st.start(tot[0], tot[1], g.tol, g.max_iter);
+    __syncthreads();
+    const int64_t trip_cap = 2 * static_cast<int64_t>(g.max_iter > 0 ? g.max_iter : 0) + 16;
+    for (int64_t trips = 0; ok && !st.done; ++trips) {
+        if (trips > trip_cap) {  // unreachable: every normal step counts and max_iter ends the solve
+            if (threadIdx.x == 0)
+                st.stop(SIMALL_ERR_TIMEOUT);
+            break;
+        }
+        // ---- one fused step
+        const int par = st.par;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (st.fresh) {
+            for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
+                sell_slice<true, WIDE, false>(g.A, sl, g.r[1 - par], g.q[par], g.p[par], g.r[1 - par], g.q[1 - par],
+                                              g.p[1 - par], g.xh, 0.0f, st.beta_f, acc);
+        } else {
+            for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
+                sell_slice<false, WIDE, false>(g.A, sl, g.r[par], g.q[par], g.p[par], g.r[1 - par], g.q[1 - par],
+                                               g.p[1 - par], g.xh, st.alpha_f, st.beta_f, acc);
+        }
+        double t[4];
+        if (!(ok = grid_allsum_f<4>(acc, t, g.part, g.ctr, epoch, g.err)))
+            break;
+        if (threadIdx.x == 0)
+            st.finish_step(t, g.tol, g.delta, g.max_iter);
+        __syncthreads();
+        if (!st.update)
+            continue;
+        // ---- reliable update: x += S xh, xh = 0
+        for (int64_t i = tid; i < n; i += nthr) {
+            g.x[i] += g.sc[i] * static_cast<double>(g.xh[i]);
+            g.xh[i] = 0.0f;
+        }
+        ++epoch;
+        if (!(ok = grid_barrier(g.ctr, epoch, g.err)))
+            break;
+        // r = b - A x in FP64; the replacement S r (FP32) into the r slot the
+        // FRESH step reads; |r|^2 and |S r|^2
+        float *rrep = g.r[1 - st.par];
+        double a[2] = {0.0, 0.0};
+        for (int64_t i = tid; i < n; i += nthr) {
+            // products rounded, then summed from 0.0 in column order (the
+            // per-step engine's true residual, spmv_rowblocks)
+            const int k1 = __ldg(g.rowPtr + i + 1);
+            double y = 0.0;
+            for (int k = __ldg(g.rowPtr + i); k < k1; ++k)
+                y = __dadd_rn(y, __dmul_rn(__ldg(g.val + k), g.x[__ldg(g.colIdx + k)]));
+            const double v = g.b[i] - y;
+            const float f = static_cast<float>(g.sc[i] * v);
+            rrep[i] = f;
+            a[0] += v * v;
+            a[1] += static_cast<double>(f) * static_cast<double>(f);
+        }
+        if (!(ok = grid_allsum<2>(a, g.part, g.ctr, epoch, g.err)))
+            break;
+        if (threadIdx.x == 0)
+            st.finish_update(a, g.tol, g.max_iter);
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        st.publish(g.s, ok);
+}
+
+}  // namespace
+
+int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
+{
+    simall_context *ctx = s->ctx;
+    if (s->n <= 0 || s->cfg.check_interval > 0 || s->cfg.engine != SIMALL_ENGINE_AUTO)
+        return 0;
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop)
+        return 0;
+    const void *fn = a.wide ? reinterpret_cast<const void *>(k_mx_grid_solve<true>)
+                            : reinterpret_cast<const void *>(k_mx_grid_solve<false>);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0) != cudaSuccess || per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    // enough warps to cover the slices, never more than are resident
+    const int64_t want = std::max<int64_t>(1, (a.nslices * 32 + kBlock - 1) / kBlock);
+    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * std::min(per_sm, kGridMaxCtasPerSm);
+    const int grid = static_cast<int>(std::min(want, cap));
+    if (static_cast<size_t>(grid) * 8 > a.partCap)
+        return 0;
+    GridArgs g{};
+    g.A.n = s->n;
+    g.A.nslices = a.nslices;
+    g.A.sptr = a.sptr;
+    g.A.off16 = a.off16;
+    g.A.off32 = a.off32;
+    g.A.val = a.sval;
+    g.A.cor = a.scor;
+    g.rowPtr = s->rowPtr;
+    g.colIdx = s->colIdx;
+    g.val = s->values;
+    g.b = s->b.p;
+    g.sc = a.scale;
+    g.x = s->x.p;
+    for (int k = 0; k < 2; ++k) {
+        g.r[k] = a.r[k];
+        g.q[k] = a.q[k];
+        g.p[k] = a.p[k];
+    }
+    g.xh = a.xh;
+    g.part = a.part;
+    g.ctr = a.ctr;
+    g.err = a.err;
+    g.s = s->scal.p;
+    g.tol = s->cfg.tolerance;
+    g.delta = s->cfg.reliable_delta;
+    g.max_iter = s->cfg.max_iterations;
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
+    void *args[] = {&g};
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0, ctx->stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        cudaGetLastError();
+        return 0;
+    }
+    ctx->launches.fetch_add(1, std::memory_order_relaxed);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaLaunchCooperativeKernel", __FILE__, __LINE__);
+        return 1;
+    }
+    int timed_out = 0;
+    e = cudaMemcpyAsync(&timed_out, a.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaMemcpyAsync", __FILE__, __LINE__);
+        return 1;
+    }
+    int st = solver_fetch_scalars(s);  // synchronises the stream
+    if (st) {
+        *status = st;
+        return 1;
+    }
+    s->engine = 2;
+    if (timed_out || s->h_scal->status == SIMALL_ERR_TIMEOUT) {
+        *status = fail(ctx, SIMALL_ERR_TIMEOUT, "mixed precision: a grid barrier of the persistent solve timed out");
+        return 1;
+    }
+    *status = s->h_scal->done ? SIMALL_OK : fail(ctx, SIMALL_ERR_CUDA, "persistent solve ended before its stop test");
+    return 1;
+}
+
+}  // namespace simall

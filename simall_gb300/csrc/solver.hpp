@@ -69,7 +69,7 @@ struct simall_solver {
     double last_residual = 0.0;
     bool ready = false;
     bool solved = false;  // a solve completed on the current matrix
-    int engine = 0;       // of the last solve: 0 kernels per step, 1 one cluster
+    int engine = 0;       // of the last solve: 0 kernels per step, 1 one cluster, 2 one persistent grid
     simall::IluData *ilu = nullptr;
     simall::AmgData *amg = nullptr;
     simall::MixedData *mixed = nullptr;
@@ -145,6 +145,29 @@ struct ClusterMixedArgs {
     const double *scale;   // S = D^-1/2
 };
 int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status);
+
+// The mixed solver's sliced operator (mixed.cu) and work vectors for the
+// whole-solve persistent cooperative kernel (mixed_grid.cu); 0 = not taken
+// (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
+// *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
+constexpr int kGridMaxCtasPerSm = 4;
+struct GridMixedArgs {
+    int64_t nslices;
+    bool wide;
+    const int32_t *sptr;
+    const int16_t *off16;
+    const int32_t *off32;
+    const float *sval;
+    const int8_t *scor;
+    const double *scale;
+    float *r[2], *q[2], *p[2];
+    float *xh;
+    double *part;
+    size_t partCap;
+    unsigned long long *ctr;
+    int *err;
+};
+int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status);
 
 // GMRES(m) / BiCGSTAB (krylov.cu): solve from x = 0 into s->x; fills the
 // result fields of s->h_scal.

@@ -84,8 +84,23 @@ def test_assembly_then_device_solve(sg, ctx, oracle):
     assert np.linalg.norm(x2 - xo2) <= 1e-10 * np.linalg.norm(xo2)
 
 
-def test_periodic_is_rejected(sg, ctx):
-    m = product_mesh(sg, 4)
-    with pytest.raises(sg.SimallError) as e:
-        sg.PressureSystem(m, [(1, int(sg.BCType.Periodic)), (2, int(sg.BCType.Periodic))], ctx=ctx)
-    assert e.value.status == 11
+def test_periodic_distorted_renumbered_box(sg, ctx, oracle):
+    """x-periodic distorted, RCM-renumbered box: twins, pattern, values and
+    rhs against the oracle (the pairing searches nearest centroids after the
+    translation, so distortion and renumbering both reach it)."""
+    dims = (6, 5, 4)
+    bcs = [(1, int(sg.BCType.Periodic)), (2, int(sg.BCType.Periodic))] + [
+        (z, int(sg.BCType.NoSlipWall)) for z in range(3, 7)]
+    m = product_mesh(sg, None, dims=dims, renumber=True, seed=21)
+    om, _, _, _, _, aP, phi = oracle_system(oracle, None, dims=dims, renumber=True, seed=21)
+    ps = sg.PressureSystem(m, bcs, ctx=ctx)
+    twin = oracle.periodic_pairs(om, bcs)
+    assert np.array_equal(ps.periodic_twins(), twin) and np.count_nonzero(twin >= 0) == 2 * dims[1] * dims[2]
+    rp, ci = ps.pattern()
+    orp, oci = oracle.build_sparsity(om, twin)
+    assert np.array_equal(rp, orp) and np.array_equal(ci, oci)
+    ps.assemble(1.0, aP, phi)
+    v, rhs = ps.download()
+    ov, orhs, _ = oracle.assemble(om, orp, oci, [], 1.0, aP, phi, twin)
+    assert bits_equal(v, ov) and bits_equal(rhs, orhs)
+    ps.close()

@@ -132,13 +132,78 @@ def test_mixed_precision_reaches_tolerance(sg, ctx, oracle, zones, dims):
 
 
 def test_mixed_precision_unstructured_pattern(sg, ctx, oracle):
-    """RCM-renumbered distorted mesh: no diagonal structure, FP32 CSR storage."""
+    """RCM-renumbered distorted mesh: no diagonal structure, sliced storage."""
     m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 12)
     s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx)
     x = np.zeros(len(rhs))
     s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
     tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
     assert tr < 1e-8
+
+
+@pytest.mark.parametrize("dims,zones", [((9, 8, 7), ()), ((24, 24, 24), ()), ((40, 30, 20), (1,)),
+                                        ((64, 64, 1), ())])
+def test_persistent_engine_matches_kernels(sg, ctx, oracle, dims, zones):
+    """RCM-renumbered distorted boxes (sliced storage): the default engine runs
+    the whole mixed solve in one persistent cooperative launch (engine 2), the
+    per-step kernels (engine KERNELS) the same algorithm one launch per step.
+    Both reach the FP64 true residual, with iteration counts within a few of
+    each other (their FP32 partial sums are grouped differently) and, with the
+    compensated operator, within 5% + 3 of FP64 CG's on pinned systems."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=dims, pressure_zones=zones)
+    res = {}
+    for engine in (0, 1):
+        s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx, engine=engine)
+        x = np.zeros(len(rhs))
+        it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+        assert s.stats.engine == (2 if engine == 0 else 0)
+        tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+        assert s.stats.converged and tr < 1e-9
+        assert abs(tr - s.stats.true_residual) <= 1e-6 * tr
+        res[engine] = (it, s.stats.reliable_updates, x)
+    assert abs(res[0][0] - res[1][0]) <= 0.02 * res[1][0] + 2
+    _, ito, _ = oracle.cg(rp, ci, v, rhs, 0, 1e-9, 5000)
+    assert res[0][0] <= 1.05 * ito + 3
+    assert rel(res[0][2], res[1][2]) <= 1e-7
+
+
+def test_persistent_engine_repeat_is_reproducible(sg, ctx, oracle):
+    """Two solves of the same system on the persistent engine: the grid, the
+    partial-sum order and every decision are fixed, so the bits are too."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 20)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx)
+    xs = []
+    for _ in range(2):
+        x = np.zeros(len(rhs))
+        xs.append((s.solve(sg.CSRMatrix(rp, ci, v), rhs, x), x))
+    assert s.stats.engine == 2 and xs[0][0] == xs[1][0] and bits_equal(xs[0][1], xs[1][1])
+
+
+def test_sliced_storage_wide_offsets(sg, ctx, oracle):
+    """A randomly permuted 40 x 40 x 30 box (48,000 rows): column offsets past
+    16 bits take the int32 offsets of the sliced storage, on both engines."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=(40, 40, 30), renumber=False, amp=0.1,
+                                                pressure_zones=(1,))
+    n = len(rp) - 1
+    perm = np.random.default_rng(4).permutation(n)  # new row k is old row perm[k]
+    inv = np.empty(n, np.int64)
+    inv[perm] = np.arange(n)
+    rows = np.repeat(np.arange(n), np.diff(rp))
+    nr, nc = inv[rows], inv[ci]
+    order = np.lexsort((nc, nr))
+    prp = np.zeros(n + 1, np.int32)
+    np.add.at(prp, nr + 1, 1)
+    prp = np.cumsum(prp).astype(np.int32)
+    pci = nc[order].astype(np.int32)
+    pv = v[order]
+    prhs = rhs[perm]
+    assert np.max(np.abs(pci - np.repeat(np.arange(n), np.diff(prp)))) > 32767
+    for engine in (0, 1):
+        s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx, engine=engine)
+        x = np.zeros(n)
+        s.solve(sg.CSRMatrix(prp, pci, pv), prhs, x)
+        tr = np.linalg.norm(prhs - oracle.spmv(prp, pci, pv, x)) / np.linalg.norm(prhs)
+        assert s.stats.converged and tr < 1e-9 and s.stats.engine == (2 if engine == 0 else 0)
 
 
 def test_zero_rhs_returns_zero(sg, ctx, oracle):
