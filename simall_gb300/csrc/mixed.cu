@@ -65,6 +65,7 @@ struct MixedData {
     int64_t nslices = 0;
     int64_t sEntries = 0;      // stored entries, padding included (32 per slice per unit of width)
     bool sWide = false;        // int32 column offsets
+    int sMaxW = 0;             // widest slice (entries per row); up to kSellStageMaxW the steps are staged
     DevBuf<int32_t> sptr;      // [nslices + 1]
     DevBuf<int16_t> soff16;
     DevBuf<int32_t> soff32;
@@ -79,7 +80,8 @@ struct MixedData {
     DevBuf<double> scale;     // s_i = 1/sqrt(a_ii)
     DevBuf<float> e;          // dia: e_i = 1 + sum_j (S A S)_ij, summed in FP64 from A, then rounded
     DevBuf<float> xh;         // FP32 correction, folded into x at reliable updates
-    DevBuf<float> rv[2], qv[2], pv[2];  // r, q = (S A S) p, p; double-buffered by step parity
+    DevBuf<float> rv[2], qv[2], pv[2];  // dia: r, q = (S A S) p, p; double-buffered by step parity
+    DevBuf<float4> st[2];               // sliced: (r, q, p, xh) per row, double-buffered (sell.cuh)
     bool patternReady = false;
     bool noDeviceLoop = false;  // conditional graph nodes unavailable
 };
@@ -212,6 +214,35 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_sell(int64_t n, const int32
     }
 }
 
+// Thread 0 of the last CTA of an init: the solve's scalars from |S b|^2
+// (FP32 rows) and |b|^2.
+__device__ void mx_start(SolveScalars *s, double sbb, double bb)
+{
+    const double bn = sqrt(bb);
+    s->bnorm = std_max(bn, 1e-30);
+    s->rz = sbb;
+    s->sigma0 = sqrt(sbb);
+    s->rmax = s->sigma0;
+    s->t0 = bn / s->bnorm;
+    s->last = s->t0;
+    s->rr = bb;
+    s->alpha = 0.0;
+    s->beta = 0.0;
+    s->iter = 0;
+    s->updates = 0;
+    s->need_update = 2;  // run the first (FRESH) step; not counted as an update
+    s->seen = -1;
+    s->status = SIMALL_OK;
+    s->done = 0;
+    s->result = 0;
+    if (s->t0 < s->tol) {
+        s->done = 1;  // b == 0: x = 0 is exact
+    } else if (s->max_iter <= 0) {
+        s->done = 1;
+        s->result = s->max_iter;
+    }
+}
+
 // ---------------------------------------------------------------- iteration kernels
 // Init: x = 0, r = S b (into r[0]), p_old = 0 (p[1]), xh = 0, beta = 0;
 // ||b||.  The first step is a FRESH step of parity 1 (reads r[0] and p[1]).
@@ -233,31 +264,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_init(int64_t n, const double *__r
         a1 += bi * bi;
     }
     double acc[2] = {static_cast<double>(a0), a1};
-    if (grid_sum_last<2>(acc, partials, &s->counter[0]) && threadIdx.x == 0) {
-        const double bn = sqrt(acc[1]);
-        s->bnorm = std_max(bn, 1e-30);
-        s->rz = acc[0];
-        s->sigma0 = sqrt(acc[0]);
-        s->rmax = s->sigma0;
-        s->t0 = bn / s->bnorm;
-        s->last = s->t0;
-        s->rr = acc[1];
-        s->alpha = 0.0;
-        s->beta = 0.0;
-        s->iter = 0;
-        s->updates = 0;
-        s->need_update = 2;  // run the first (FRESH) step; not counted as an update
-        s->seen = -1;
-        s->status = SIMALL_OK;
-        s->done = 0;
-        s->result = 0;
-        if (s->t0 < s->tol) {
-            s->done = 1;  // b == 0: x = 0 is exact
-        } else if (s->max_iter <= 0) {
-            s->done = 1;
-            s->result = s->max_iter;
-        }
-    }
+    if (grid_sum_last<2>(acc, partials, &s->counter[0]) && threadIdx.x == 0)
+        mx_start(s, acc[0], acc[1]);
 }
 
 // Four consecutive floats starting at p; p is 16-byte aligned when `aligned`.
@@ -291,6 +299,13 @@ __device__ __forceinline__ void dfma4(float (&y)[4], float4 a, float4 p, float4 
 //
 // FRESH: the step after a residual replacement (and the first step): r is
 // the replaced residual, read from r_out and not rewritten; alpha = 0.
+template <bool FRESH>
+__device__ __forceinline__ float pdir(float r, float q, float p, float alpha, float beta)
+{
+    const float rn = FRESH ? r : __fmaf_rn(-alpha, q, r);
+    return __fmaf_rn(beta, p, rn);
+}
+
 template <bool FRESH>
 __device__ __forceinline__ float4 pdir4(float4 r, float4 q, float4 p, float alpha, float beta)
 {
@@ -566,22 +581,108 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_iter_dia(int n, int64_t ldU, D
 }
 
 // Sliced storage (sell.cuh): a warp per slice of 32 rows, grid-stride over
-// the slices.
+// the slices; the packed state of step parity par is read from `in`, the
+// next written to `out`.  FRESH (after a replacement): alpha = 0.
 template <bool FRESH, bool WIDE>
-__global__ void __launch_bounds__(kBlock) k_mx_iter_sell(SellOp A, IterVecs v, double *partials, SolveScalars *s)
+__global__ void __launch_bounds__(kBlock) k_mx_iter_sell(SellOp A, const float4 *in, float4 *out, double *partials,
+                                                         SolveScalars *s)
 {
     if (mx_skip<FRESH>(s))
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
-    const float *rs = FRESH ? v.rout : v.rin;
     float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t sl = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; sl < A.nslices; sl += nw)
-        sell_slice<FRESH, WIDE, true>(A, sl, rs, v.qin, v.pin, v.rout, v.qout, v.pout, v.xh, alpha, beta, acc);
+        sell_slice<WIDE, true>(A, sl, in, out, alpha, beta, acc);
     double t[4];
     if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0)
         mx_finish<FRESH>(s, t);
+}
+
+// The same step with the streamed operands staged by bulk copies
+// (sell_step_staged); CTA b owns slices [b nslices / grid, (b + 1) nslices /
+// grid).  A copy that does not complete in time ends the solve with
+// SIMALL_ERR_TIMEOUT.
+template <bool FRESH, bool WIDE>
+__global__ void __launch_bounds__(kBlock) k_mx_iter_sell_staged(SellOp A, const float4 *in, float4 *out,
+                                                                double *partials, SolveScalars *s)
+{
+    extern __shared__ __align__(128) unsigned char sell_smem[];
+    __shared__ uint64_t bars[kSellStages];
+    if (mx_skip<FRESH>(s))
+        return;
+    if (threadIdx.x == 0) {
+        for (int b = 0; b < kSellStages; ++b)
+            mbar_init(bars + b, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
+    const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
+    const float beta = static_cast<float>(__ldcg(&s->beta));
+    const int64_t c0 = blockIdx.x * A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * A.nslices / gridDim.x;
+    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    if (!sell_step_staged<WIDE, true>(A, c0, c1, in, out, alpha, beta, acc, R, false) && threadIdx.x == 0) {
+        atomicExch(&s->status, SIMALL_ERR_TIMEOUT);
+        atomicExch(&s->done, 1);
+    }
+    double t[4];
+    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0 && !ld_flag(&s->done))
+        mx_finish<FRESH>(s, t);
+}
+
+// Sliced storage, packed state: init (x = 0, state[1] = (S b, 0, 0, 0): the
+// first step, a FRESH one at parity 1, forms p = r), and the update kernels:
+// fold x += S xh with the xh the triggering step wrote (state[1 - par]), and
+// the replacement r = S (b - A x), xh = 0 written into state[par], which the
+// FRESH step reads.
+__global__ void __launch_bounds__(kBlock) k_mx_init_packed(int64_t n, const double *__restrict__ b,
+                                                           const double *__restrict__ sc, double *__restrict__ x,
+                                                           float4 *__restrict__ st1, double *partials, SolveScalars *s)
+{
+    float a0 = 0.0f;
+    double a1 = 0.0;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double bi = b[i];
+        const float r = static_cast<float>(bi * sc[i]);
+        x[i] = 0.0;
+        st1[i] = make_float4(r, 0.0f, 0.0f, 0.0f);
+        a0 += r * r;
+        a1 += bi * bi;
+    }
+    double acc[2] = {static_cast<double>(a0), a1};
+    if (grid_sum_last<2>(acc, partials, &s->counter[0]) && threadIdx.x == 0)
+        mx_start(s, acc[0], acc[1]);
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_fold_packed(int64_t n, const double *__restrict__ sc,
+                                                           const float4 *__restrict__ st, double *__restrict__ x,
+                                                           const SolveScalars *s)
+{
+    if (!ld_flag(&s->need_update) || ld_flag(&s->done))
+        return;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+        x[i] += sc[i] * static_cast<double>(st[i].w);
+}
+
+__global__ void __launch_bounds__(kBlock) k_mx_replace_packed(int64_t n, const double *__restrict__ sc,
+                                                              const double *__restrict__ r, float4 *__restrict__ st,
+                                                              double *partials, SolveScalars *s)
+{
+    if (!ld_flag(&s->need_update) || ld_flag(&s->done))
+        return;
+    float acc = 0.0f;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const float v = static_cast<float>(sc[i] * r[i]);
+        float *e = reinterpret_cast<float *>(st + i);
+        e[0] = v;
+        e[3] = 0.0f;
+        acc += v * v;
+    }
+    double rho;
+    if (grid_sum_last_f(acc, partials, &s->counter[4], rho) && threadIdx.x == 0)
+        s->beta = rho / s->rz;
 }
 
 // U1: x += S xh (FP64), xh = 0.
@@ -776,6 +877,9 @@ int build_sell_pattern(simall_solver *s, MixedData *m)
     }
     m->nslices = ns;
     m->sEntries = total;
+    m->sMaxW = 0;
+    for (int64_t sl = 0; sl < ns; ++sl)
+        m->sMaxW = std::max(m->sMaxW, (sptr[sl + 1] - sptr[sl]) >> 5);
     m->sWide = band > 32767;
     const size_t cap = static_cast<size_t>(std::max<int64_t>(total, 1));
     SIMALL_CUDA_TRY(ctx, m->sptr.alloc(static_cast<size_t>(ns) + 1));
@@ -878,22 +982,68 @@ IterVecs iter_vecs(MixedData *m, int par)
     return v;
 }
 
+}  // namespace
+
+// Resident CTAs per SM of a kernel with `smem` bytes of dynamic shared memory
+// (raising its limit first); cached per context and kernel.
+int staged_residency(simall_context *ctx, const void *fn, size_t smem, int *per_sm)
+{
+    std::lock_guard<std::mutex> lock(ctx->occupancy_mu);
+    auto it = ctx->resident_per_sm.find(fn);
+    if (it != ctx->resident_per_sm.end()) {
+        *per_sm = it->second;
+        return SIMALL_OK;
+    }
+    SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int n = 0;
+    SIMALL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kBlock, smem));
+    if (n < 1)
+        return fail(ctx, SIMALL_ERR_CUDA, "a staged kernel does not fit on an SM");
+    ctx->resident_per_sm.emplace(fn, n);
+    *per_sm = n;
+    return SIMALL_OK;
+}
+
+namespace {
+
 template <bool FRESH> int launch_iter_t(simall_context *ctx, simall_solver *s, MixedData *m, int par)
 {
     const int64_t n = s->n;
-    const IterVecs v = iter_vecs(m, par);
     if (!m->dia) {
         const SellOp A = sell_op(s, m);
+        const float4 *in = m->st[par].p;
+        float4 *out = m->st[1 - par].p;
+        if (m->sMaxW <= kSellStageMaxW) {
+            const size_t smem = m->sWide ? sell_stage_smem<true>() : sell_stage_smem<false>();
+            const void *fn = m->sWide ? reinterpret_cast<const void *>(k_mx_iter_sell_staged<FRESH, true>)
+                                      : reinterpret_cast<const void *>(k_mx_iter_sell_staged<FRESH, false>);
+            int per_sm = 0;
+            int st = staged_residency(ctx, fn, smem, &per_sm);
+            if (st)
+                return st;
+            const int64_t stages = (m->nslices + kSellStageSlices - 1) / kSellStageSlices;
+            const int grid = static_cast<int>(std::max<int64_t>(
+                1, std::min<int64_t>(stages, static_cast<int64_t>(ctx->num_sms) * per_sm)));
+            if (m->sWide)
+                k_mx_iter_sell_staged<FRESH, true>
+                    <<<grid, kBlock, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
+            else
+                k_mx_iter_sell_staged<FRESH, false>
+                    <<<grid, kBlock, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
+            SIMALL_LAUNCH_CHECK(ctx);
+            return SIMALL_OK;
+        }
         const void *fn = m->sWide ? reinterpret_cast<const void *>(k_mx_iter_sell<FRESH, true>)
                                   : reinterpret_cast<const void *>(k_mx_iter_sell<FRESH, false>);
         const int grid = resident_grid(ctx, fn, m->nslices * 32);
         if (m->sWide)
-            k_mx_iter_sell<FRESH, true><<<grid, kBlock, 0, ctx->stream>>>(A, v, s->partials.p, s->scal.p);
+            k_mx_iter_sell<FRESH, true><<<grid, kBlock, 0, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
         else
-            k_mx_iter_sell<FRESH, false><<<grid, kBlock, 0, ctx->stream>>>(A, v, s->partials.p, s->scal.p);
+            k_mx_iter_sell<FRESH, false><<<grid, kBlock, 0, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
+    const IterVecs v = iter_vecs(m, par);
     const int64_t quads = (n + 3) / 4;
     const int ni = static_cast<int>(n);
     bool grid = m->offs.nd >= 1 && m->offs.off[0] == 1;
@@ -952,11 +1102,16 @@ int mixed_setup(simall_solver *s)
             return st;
     }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
-    SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
-    for (int k = 0; k < 2; ++k) {
-        SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
-        SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
-        SIMALL_CUDA_TRY(ctx, m->pv[k].alloc(n + 4));
+    if (m->dia) {
+        SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
+        for (int k = 0; k < 2; ++k) {
+            SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
+            SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
+            SIMALL_CUDA_TRY(ctx, m->pv[k].alloc(n + 4));
+        }
+    } else {
+        for (int k = 0; k < 2; ++k)
+            SIMALL_CUDA_TRY(ctx, m->st[k].alloc(n));
     }
     SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
@@ -1007,14 +1162,22 @@ int enqueue_update_branch(simall_solver *s, int par)
     MixedData *m = s->mixed;
     const int64_t n = s->n;
     const int g = grid_n(ctx, n);
-    k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
+    if (m->dia)
+        k_mx_fold<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->xh.p, s->x.p, s->scal.p);
+    else
+        k_mx_fold_packed<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, m->st[1 - par].p, s->x.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     k_mx_true_residual<<<resident_grid(ctx, reinterpret_cast<const void *>(k_mx_true_residual),
                                        spmv_items(s)),
                          kBlock, 0, ctx->stream>>>(s->rowPtr, s->colIdx, s->values, s->rowBlocks.p, spmv_schedule(s),
                                                    s->x.p, s->b.p, s->r.p, s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
-    k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rv[1 - par].p, s->partials.p, s->scal.p);
+    if (m->dia)
+        k_mx_replace<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->rv[1 - par].p, s->partials.p,
+                                                    s->scal.p);
+    else
+        k_mx_replace_packed<<<g, kBlock, 0, ctx->stream>>>(n, m->scale.p, s->r.p, m->st[par].p, s->partials.p,
+                                                           s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     return launch_iter(ctx, s, par, true);
 }
@@ -1170,18 +1333,15 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
         GridMixedArgs a{};
         a.nslices = m->nslices;
         a.wide = m->sWide;
+        a.staged = m->sMaxW <= kSellStageMaxW;
         a.sptr = m->sptr.p;
         a.off16 = m->soff16.p;
         a.off32 = m->soff32.p;
         a.sval = m->sval.p;
         a.scor = m->scor.p;
         a.scale = m->scale.p;
-        for (int k = 0; k < 2; ++k) {
-            a.r[k] = m->rv[k].p;
-            a.q[k] = m->qv[k].p;
-            a.p[k] = m->pv[k].p;
-        }
-        a.xh = m->xh.p;
+        a.st[0] = m->st[0].p;
+        a.st[1] = m->st[1].p;
         a.part = m->gpart.p;
         a.partCap = m->gpart.n;
         a.ctr = m->gctr.p;
@@ -1204,8 +1364,12 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
         if (cluster_mixed_solve(s, a, &cst))
             return cst;
     }
-    k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rv[0].p, m->pv[1].p,
-                                                          m->xh.p, s->partials.p, s->scal.p);
+    if (m->dia)
+        k_mx_init<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->rv[0].p,
+                                                              m->pv[1].p, m->xh.p, s->partials.p, s->scal.p);
+    else
+        k_mx_init_packed<<<grid_n(ctx, n), kBlock, 0, ctx->stream>>>(n, s->b.p, m->scale.p, s->x.p, m->st[1].p,
+                                                                     s->partials.p, s->scal.p);
     SIMALL_LAUNCH_CHECK(ctx);
     int first = launch_iter(ctx, s, 1, true);
     if (first)

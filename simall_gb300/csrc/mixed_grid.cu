@@ -49,8 +49,7 @@ struct GridArgs {
     const double *b;
     const double *sc;
     double *x;
-    float *r[2], *q[2], *p[2];
-    float *xh;
+    float4 *st[2];  // (r, q, p, xh) per row, by step parity (sell.cuh)
     double *part;  // [2][gridDim.x][4]
     unsigned long long *ctr;
     int *err;
@@ -291,9 +290,20 @@ struct GridState {
     }
 };
 
-template <bool WIDE>
+template <bool WIDE, bool STAGED>
 __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
 {
+    extern __shared__ __align__(128) unsigned char sell_smem[];
+    __shared__ uint64_t bars[kSellStages];
+    if (STAGED && threadIdx.x == 0) {
+        for (int b = 0; b < kSellStages; ++b)
+            mbar_init(bars + b, 1);
+        mbar_fence_init();
+    }
+    __syncthreads();
+    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
+    // this CTA's slices of the staged steps
+    const int64_t c0 = blockIdx.x * g.A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * g.A.nslices / gridDim.x;
     const int64_t n = g.A.n;
     const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
     const int64_t nthr = static_cast<int64_t>(gridDim.x) * blockDim.x;
@@ -301,7 +311,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
     unsigned long long epoch = 0;
     bool ok = true;
 
-    // init: x = 0, r[0] = S b, p[1] = 0, xh = 0; |S b|^2 (FP32 rows), |b|^2
+    // init: x = 0, state[1] = (S b, 0, 0, 0); |S b|^2 (FP32 rows), |b|^2
     double tot[2];
     {
         float a0 = 0.0f;
@@ -310,9 +320,7 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
             const double bi = g.b[i];
             const float r = static_cast<float>(bi * g.sc[i]);
             g.x[i] = 0.0;
-            g.r[0][i] = r;
-            g.p[1][i] = 0.0f;
-            g.xh[i] = 0.0f;
+            g.st[1][i] = make_float4(r, 0.0f, 0.0f, 0.0f);
             a0 += r * r;
             a1 += bi * bi;
         }
@@ -340,15 +348,18 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
         }
         // ---- one fused step
         const int par = st.par;
+        const float alpha = st.fresh ? 0.0f : st.alpha_f, beta = st.beta_f;
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        if (st.fresh) {
-            for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
-                sell_slice<true, WIDE, false>(g.A, sl, g.r[1 - par], g.q[par], g.p[par], g.r[1 - par], g.q[1 - par],
-                                              g.p[1 - par], g.xh, 0.0f, st.beta_f, acc);
+        if (STAGED) {
+            if (!sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true)) {
+                if (threadIdx.x == 0)
+                    atomicExch(g.err, 1);
+                ok = false;
+                break;
+            }
         } else {
             for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
-                sell_slice<false, WIDE, false>(g.A, sl, g.r[par], g.q[par], g.p[par], g.r[1 - par], g.q[1 - par],
-                                               g.p[1 - par], g.xh, st.alpha_f, st.beta_f, acc);
+                sell_slice<WIDE, false>(g.A, sl, g.st[par], g.st[1 - par], alpha, beta, acc);
         }
         double t[4];
         if (!(ok = grid_allsum_f<4>(acc, t, g.part, g.ctr, epoch, g.err)))
@@ -358,17 +369,18 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
         __syncthreads();
         if (!st.update)
             continue;
-        // ---- reliable update: x += S xh, xh = 0
-        for (int64_t i = tid; i < n; i += nthr) {
-            g.x[i] += g.sc[i] * static_cast<double>(g.xh[i]);
-            g.xh[i] = 0.0f;
+        // ---- reliable update: x += S xh with the xh the triggering step wrote
+        {
+            const float4 *so = g.st[1 - st.par];
+            for (int64_t i = tid; i < n; i += nthr)
+                g.x[i] += g.sc[i] * static_cast<double>(so[i].w);
         }
         ++epoch;
         if (!(ok = grid_barrier(g.ctr, epoch, g.err)))
             break;
-        // r = b - A x in FP64; the replacement S r (FP32) into the r slot the
-        // FRESH step reads; |r|^2 and |S r|^2
-        float *rrep = g.r[1 - st.par];
+        // r = b - A x in FP64; the replacement S r (FP32), and xh = 0, into the
+        // state the FRESH step reads (its q and p stay); |r|^2 and |S r|^2
+        float4 *srep = g.st[st.par];
         double a[2] = {0.0, 0.0};
         for (int64_t i = tid; i < n; i += nthr) {
             // products rounded, then summed from 0.0 in column order (the
@@ -379,7 +391,9 @@ __global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
                 y = __dadd_rn(y, __dmul_rn(__ldg(g.val + k), g.x[__ldg(g.colIdx + k)]));
             const double v = g.b[i] - y;
             const float f = static_cast<float>(g.sc[i] * v);
-            rrep[i] = f;
+            float *e = reinterpret_cast<float *>(srep + i);
+            e[0] = f;
+            e[3] = 0.0f;
             a[0] += v * v;
             a[1] += static_cast<double>(f) * static_cast<double>(f);
         }
@@ -403,10 +417,13 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     int coop = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop)
         return 0;
-    const void *fn = a.wide ? reinterpret_cast<const void *>(k_mx_grid_solve<true>)
-                            : reinterpret_cast<const void *>(k_mx_grid_solve<false>);
+    const void *fn = a.wide ? (a.staged ? reinterpret_cast<const void *>(k_mx_grid_solve<true, true>)
+                                        : reinterpret_cast<const void *>(k_mx_grid_solve<true, false>))
+                            : (a.staged ? reinterpret_cast<const void *>(k_mx_grid_solve<false, true>)
+                                        : reinterpret_cast<const void *>(k_mx_grid_solve<false, false>));
+    const size_t smem = a.staged ? (a.wide ? sell_stage_smem<true>() : sell_stage_smem<false>()) : 0;
     int per_sm = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kBlock, 0) != cudaSuccess || per_sm < 1) {
+    if (staged_residency(ctx, fn, smem, &per_sm) != SIMALL_OK) {
         cudaGetLastError();
         return 0;
     }
@@ -430,12 +447,8 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     g.b = s->b.p;
     g.sc = a.scale;
     g.x = s->x.p;
-    for (int k = 0; k < 2; ++k) {
-        g.r[k] = a.r[k];
-        g.q[k] = a.q[k];
-        g.p[k] = a.p[k];
-    }
-    g.xh = a.xh;
+    g.st[0] = a.st[0];
+    g.st[1] = a.st[1];
     g.part = a.part;
     g.ctr = a.ctr;
     g.err = a.err;
@@ -446,7 +459,7 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
     void *args[] = {&g};
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, 0, ctx->stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, smem, ctx->stream);
     if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
         cudaGetLastError();
         return 0;

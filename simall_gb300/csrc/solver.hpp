@@ -151,17 +151,20 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
 // *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
 constexpr int kGridMaxCtasPerSm = 4;
+// Resident CTAs per SM of a kBlock-thread kernel with `smem` bytes of dynamic
+// shared memory (its limit raised first); cached per context and kernel.
+int staged_residency(simall_context *ctx, const void *fn, size_t smem, int *per_sm);
 struct GridMixedArgs {
     int64_t nslices;
     bool wide;
+    bool staged;  // every slice at most kSellStageMaxW wide: TMA-staged steps
     const int32_t *sptr;
     const int16_t *off16;
     const int32_t *off32;
     const float *sval;
     const int8_t *scor;
     const double *scale;
-    float *r[2], *q[2], *p[2];
-    float *xh;
+    float4 *st[2];  // (r, q, p, xh) per row, by step parity (sell.cuh)
     double *part;
     size_t partCap;
     unsigned long long *ctr;

@@ -164,7 +164,9 @@ def test_persistent_engine_matches_kernels(sg, ctx, oracle, dims, zones):
     assert abs(res[0][0] - res[1][0]) <= 0.02 * res[1][0] + 2
     _, ito, _ = oracle.cg(rp, ci, v, rhs, 0, 1e-9, 5000)
     assert res[0][0] <= 1.05 * ito + 3
-    assert rel(res[0][2], res[1][2]) <= 1e-7
+    # two solutions with true residuals below 1e-9 of a pinned Neumann system
+    # (condition number ~1e4 at 24^3): their distance is bounded by kappa * 1e-9
+    assert rel(res[0][2], res[1][2]) <= 1e-5
 
 
 def test_persistent_engine_repeat_is_reproducible(sg, ctx, oracle):
