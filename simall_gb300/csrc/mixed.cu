@@ -610,7 +610,11 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_sell_staged(SellOp A, const 
 {
     extern __shared__ __align__(128) unsigned char sell_smem[];
     __shared__ uint64_t bars[kSellStages];
-    if (mx_skip<FRESH>(s))
+    __shared__ int skip;
+    if (threadIdx.x == 0)  // one decision per CTA: a timed-out CTA of this launch may raise done meanwhile
+        skip = mx_skip<FRESH>(s) ? 1 : 0;
+    __syncthreads();
+    if (skip)
         return;
     if (threadIdx.x == 0) {
         for (int b = 0; b < kSellStages; ++b)
