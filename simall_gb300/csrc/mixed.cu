@@ -71,7 +71,6 @@ struct MixedData {
     DevBuf<int32_t> soff32;
     DevBuf<int32_t> spos;      // CSR position of each stored entry, -1 for padding
     DevBuf<float> sval;
-    DevBuf<int8_t> scor;
     // the persistent engine's grid reduction buffers and barrier (mixed_grid.cu)
     DevBuf<double> gpart;
     DevBuf<unsigned long long> gctr;
@@ -185,13 +184,12 @@ __global__ void __launch_bounds__(kBlock) k_mx_row_defect(int64_t n, const int32
 }
 
 // Values of the sliced storage: N_ij = a_ij s_i s_j in FP64 (the product in
-// that order), stored rounded to FP32 with its 8-bit correction; padding
-// entries 0.  One thread per row.
+// that order), stored rounded to FP32; padding entries 0.  One thread per row.
 __global__ void __launch_bounds__(kBlock) k_mx_build_sell(int64_t n, const int32_t *__restrict__ sptr,
                                                           const int32_t *__restrict__ spos,
                                                           const int32_t *__restrict__ colIdx,
                                                           const double *__restrict__ val, const double *__restrict__ sc,
-                                                          float *__restrict__ sval, int8_t *__restrict__ scor)
+                                                          float *__restrict__ sval)
 {
     for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t sl = i >> 5;
@@ -201,15 +199,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_build_sell(int64_t n, const int32
         for (int k = 0; k < w; ++k) {
             const int64_t e = static_cast<int64_t>(e0) + static_cast<int64_t>(k) * 32 + (i & 31);
             const int pos = spos[e];
-            float u = 0.0f;
-            int8_t c = 0;
-            if (pos >= 0) {
-                const double a = val[pos] * si * sc[colIdx[pos]];
-                u = static_cast<float>(a);
-                c = ff_correction(a, u);
-            }
-            sval[e] = u;
-            scor[e] = c;
+            sval[e] = pos >= 0 ? static_cast<float>(val[pos] * si * sc[colIdx[pos]]) : 0.0f;
         }
     }
 }
@@ -889,7 +879,6 @@ int build_sell_pattern(simall_solver *s, MixedData *m)
     SIMALL_CUDA_TRY(ctx, m->sptr.alloc(static_cast<size_t>(ns) + 1));
     SIMALL_CUDA_TRY(ctx, m->spos.alloc(cap));
     SIMALL_CUDA_TRY(ctx, m->sval.alloc(cap));
-    SIMALL_CUDA_TRY(ctx, m->scor.alloc(cap));
     SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(m->sptr.p, sptr.data(), sptr.size() * sizeof(int32_t),
                                          cudaMemcpyHostToDevice, ctx->stream));
     std::vector<int16_t> off16;
@@ -920,7 +909,7 @@ SellOp sell_op(const simall_solver *s, const MixedData *m)
     A.off16 = m->soff16.p;
     A.off32 = m->soff32.p;
     A.val = m->sval.p;
-    A.cor = m->scor.p;
+    A.e = m->e.p;
     return A;
 }
 
@@ -1106,17 +1095,6 @@ int mixed_setup(simall_solver *s)
             return st;
     }
     SIMALL_CUDA_TRY(ctx, m->scale.alloc(n));
-    if (m->dia) {
-        SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
-        for (int k = 0; k < 2; ++k) {
-            SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
-            SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
-            SIMALL_CUDA_TRY(ctx, m->pv[k].alloc(n + 4));
-        }
-    } else {
-        for (int k = 0; k < 2; ++k)
-            SIMALL_CUDA_TRY(ctx, m->st[k].alloc(n));
-    }
     SIMALL_CUDA_TRY(ctx, s->flag.alloc(1));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(s->flag.p, 0, sizeof(int), ctx->stream));
     const int g = grid_n(ctx, n);
@@ -1136,10 +1114,28 @@ int mixed_setup(simall_solver *s)
         if (st)
             return st;
     }
+    // the iteration vectors of the storage the solve will use
     if (m->dia) {
-        SIMALL_CUDA_TRY(ctx, m->e.alloc(n + 4));
+        SIMALL_CUDA_TRY(ctx, m->xh.alloc(n + 4));
+        for (int k = 0; k < 2; ++k) {
+            SIMALL_CUDA_TRY(ctx, m->rv[k].alloc(n + 4));
+            SIMALL_CUDA_TRY(ctx, m->qv[k].alloc(n + 4));
+            SIMALL_CUDA_TRY(ctx, m->pv[k].alloc(n + 4));
+        }
+    } else {
+        for (int k = 0; k < 2; ++k)
+            SIMALL_CUDA_TRY(ctx, m->st[k].alloc(n));
+    }
+    {
+        // diagonal storage: n + 4 (the quad loads); sliced: whole slices, zero past n
+        const int64_t ne = m->dia ? n + 4 : m->nslices * 32;
+        SIMALL_CUDA_TRY(ctx, m->e.alloc(ne));
+        if (!m->dia)
+            SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(m->e.p, 0, ne * sizeof(float), ctx->stream));
         k_mx_row_defect<<<g, kBlock, 0, ctx->stream>>>(n, s->rowPtr, s->colIdx, s->values, m->scale.p, m->e.p);
         SIMALL_LAUNCH_CHECK(ctx);
+    }
+    if (m->dia) {
         m->ldU = (n + 3) & ~static_cast<int64_t>(3);
         SIMALL_CUDA_TRY(ctx, m->U.alloc(static_cast<size_t>(m->offs.nd) * m->ldU));
         SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(m->U.p, 0, static_cast<size_t>(m->offs.nd) * m->ldU * sizeof(float),
@@ -1149,7 +1145,7 @@ int mixed_setup(simall_solver *s)
         SIMALL_LAUNCH_CHECK(ctx);
     } else if (m->sEntries > 0) {
         k_mx_build_sell<<<g, kBlock, 0, ctx->stream>>>(n, m->sptr.p, m->spos.p, s->colIdx, s->values, m->scale.p,
-                                                       m->sval.p, m->scor.p);
+                                                       m->sval.p);
         SIMALL_LAUNCH_CHECK(ctx);
     }
     return SIMALL_OK;
@@ -1342,7 +1338,7 @@ int mixed_solve(simall_solver *s, simall_solver_stats *st)
         a.off16 = m->soff16.p;
         a.off32 = m->soff32.p;
         a.sval = m->sval.p;
-        a.scor = m->scor.p;
+        a.e = m->e.p;
         a.scale = m->scale.p;
         a.st[0] = m->st[0].p;
         a.st[1] = m->st[1].p;
@@ -1452,12 +1448,11 @@ int mixed_enqueue_kernel(simall_solver *s, int k, double *bytes)
     if (k != 4)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "mixed kernel id %d", k);
     // r, q, p read at parity 0 and written at parity 1, xh read and written
-    // (each gathered vector counted once), plus the matrix: diagonal storage
-    // 4 B per stored diagonal per row and e; sliced storage 7 B per stored
-    // entry (9 B with wide offsets: offset, value, correction) and the slice
-    // pointers
+    // (each gathered vector counted once), e, plus the matrix: diagonal
+    // storage 4 B per stored diagonal per row; sliced storage 6 B per stored
+    // entry (8 B with wide offsets: offset and value) and the slice pointers
     *bytes = m->dia ? (4.0 * m->offs.nd + 36.0) * nd
-                    : (m->sWide ? 9.0 : 7.0) * static_cast<double>(m->sEntries) + 32.0 * nd +
+                    : (m->sWide ? 8.0 : 6.0) * static_cast<double>(m->sEntries) + 36.0 * nd +
                           4.0 * static_cast<double>(m->nslices + 1);
     return launch_iter(ctx, s, 0, false);
 }

@@ -291,7 +291,7 @@ struct GridState {
 };
 
 template <bool WIDE, bool STAGED>
-__global__ void __launch_bounds__(kBlock, 3) k_mx_grid_solve(GridArgs g)
+__global__ void __launch_bounds__(kBlock, 4) k_mx_grid_solve(GridArgs g)
 {
     extern __shared__ __align__(128) unsigned char sell_smem[];
     __shared__ uint64_t bars[kSellStages];
@@ -440,7 +440,7 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     g.A.off16 = a.off16;
     g.A.off32 = a.off32;
     g.A.val = a.sval;
-    g.A.cor = a.scor;
+    g.A.e = a.e;
     g.rowPtr = s->rowPtr;
     g.colIdx = s->colIdx;
     g.val = s->values;

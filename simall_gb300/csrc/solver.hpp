@@ -162,7 +162,7 @@ struct GridMixedArgs {
     const int16_t *off16;
     const int32_t *off32;
     const float *sval;
-    const int8_t *scor;
+    const float *e;  // row sums, whole slices
     const double *scale;
     float4 *st[2];  // (r, q, p, xh) per row, by step parity (sell.cuh)
     double *part;
