@@ -595,22 +595,19 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_sell(SellOp A, const float4 
 // grid).  A copy that does not complete in time ends the solve with
 // SIMALL_ERR_TIMEOUT.
 template <bool FRESH, bool WIDE>
-__global__ void __launch_bounds__(kBlock) k_mx_iter_sell_staged(SellOp A, const float4 *in, float4 *out,
-                                                                double *partials, SolveScalars *s)
+__global__ void __launch_bounds__(kSellThreads) k_mx_iter_sell_staged(SellOp A, const float4 *in, float4 *out,
+                                                                      double *partials, SolveScalars *s)
 {
     extern __shared__ __align__(128) unsigned char sell_smem[];
-    __shared__ uint64_t bars[kSellStages];
+    __shared__ uint64_t bars[2 * kSellStages];
     __shared__ int skip;
     if (threadIdx.x == 0)  // one decision per CTA: a timed-out CTA of this launch may raise done meanwhile
         skip = mx_skip<FRESH>(s) ? 1 : 0;
     __syncthreads();
     if (skip)
         return;
-    if (threadIdx.x == 0) {
-        for (int b = 0; b < kSellStages; ++b)
-            mbar_init(bars + b, 1);
-        mbar_fence_init();
-    }
+    if (threadIdx.x == 0)
+        sell_ring_init(bars);
     __syncthreads();
     SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
@@ -977,9 +974,9 @@ IterVecs iter_vecs(MixedData *m, int par)
 
 }  // namespace
 
-// Resident CTAs per SM of a kernel with `smem` bytes of dynamic shared memory
-// (raising its limit first); cached per context and kernel.
-int staged_residency(simall_context *ctx, const void *fn, size_t smem, int *per_sm)
+// Resident CTAs per SM of a kernel of `threads` threads with `smem` bytes of
+// dynamic shared memory (raising its limit first); cached per context and kernel.
+int staged_residency(simall_context *ctx, const void *fn, int threads, size_t smem, int *per_sm)
 {
     std::lock_guard<std::mutex> lock(ctx->occupancy_mu);
     auto it = ctx->resident_per_sm.find(fn);
@@ -989,7 +986,7 @@ int staged_residency(simall_context *ctx, const void *fn, size_t smem, int *per_
     }
     SIMALL_CUDA_TRY(ctx, cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int n = 0;
-    SIMALL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, kBlock, smem));
+    SIMALL_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, fn, threads, smem));
     if (n < 1)
         return fail(ctx, SIMALL_ERR_CUDA, "a staged kernel does not fit on an SM");
     ctx->resident_per_sm.emplace(fn, n);
@@ -1011,7 +1008,7 @@ template <bool FRESH> int launch_iter_t(simall_context *ctx, simall_solver *s, M
             const void *fn = m->sWide ? reinterpret_cast<const void *>(k_mx_iter_sell_staged<FRESH, true>)
                                       : reinterpret_cast<const void *>(k_mx_iter_sell_staged<FRESH, false>);
             int per_sm = 0;
-            int st = staged_residency(ctx, fn, smem, &per_sm);
+            int st = staged_residency(ctx, fn, kSellThreads, smem, &per_sm);
             if (st)
                 return st;
             const int64_t stages = (m->nslices + kSellStageSlices - 1) / kSellStageSlices;
@@ -1019,10 +1016,10 @@ template <bool FRESH> int launch_iter_t(simall_context *ctx, simall_solver *s, M
                 1, std::min<int64_t>(stages, static_cast<int64_t>(ctx->num_sms) * per_sm)));
             if (m->sWide)
                 k_mx_iter_sell_staged<FRESH, true>
-                    <<<grid, kBlock, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
+                    <<<grid, kSellThreads, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
             else
                 k_mx_iter_sell_staged<FRESH, false>
-                    <<<grid, kBlock, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
+                    <<<grid, kSellThreads, smem, ctx->stream>>>(A, in, out, s->partials.p, s->scal.p);
             SIMALL_LAUNCH_CHECK(ctx);
             return SIMALL_OK;
         }

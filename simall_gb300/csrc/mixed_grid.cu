@@ -291,15 +291,12 @@ struct GridState {
 };
 
 template <bool WIDE, bool STAGED>
-__global__ void __launch_bounds__(kBlock, 4) k_mx_grid_solve(GridArgs g)
+__global__ void __launch_bounds__(kSellThreads, 4) k_mx_grid_solve(GridArgs g)
 {
     extern __shared__ __align__(128) unsigned char sell_smem[];
-    __shared__ uint64_t bars[kSellStages];
-    if (STAGED && threadIdx.x == 0) {
-        for (int b = 0; b < kSellStages; ++b)
-            mbar_init(bars + b, 1);
-        mbar_fence_init();
-    }
+    __shared__ uint64_t bars[2 * kSellStages];
+    if (STAGED && threadIdx.x == 0)
+        sell_ring_init(bars);
     __syncthreads();
     SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
     // this CTA's slices of the staged steps
@@ -423,12 +420,12 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
                                         : reinterpret_cast<const void *>(k_mx_grid_solve<false, false>));
     const size_t smem = a.staged ? (a.wide ? sell_stage_smem<true>() : sell_stage_smem<false>()) : 0;
     int per_sm = 0;
-    if (staged_residency(ctx, fn, smem, &per_sm) != SIMALL_OK) {
+    if (staged_residency(ctx, fn, kSellThreads, smem, &per_sm) != SIMALL_OK) {
         cudaGetLastError();
         return 0;
     }
-    // enough warps to cover the slices, never more than are resident
-    const int64_t want = std::max<int64_t>(1, (a.nslices * 32 + kBlock - 1) / kBlock);
+    // a stage of slices per CTA at least, never more CTAs than are resident
+    const int64_t want = std::max<int64_t>(1, (a.nslices + kSellStageSlices - 1) / kSellStageSlices);
     const int64_t cap = static_cast<int64_t>(ctx->num_sms) * std::min(per_sm, kGridMaxCtasPerSm);
     const int grid = static_cast<int>(std::min(want, cap));
     if (static_cast<size_t>(grid) * 8 > a.partCap)
@@ -459,7 +456,7 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
     void *args[] = {&g};
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kBlock), args, smem, ctx->stream);
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kSellThreads), args, smem, ctx->stream);
     if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
         cudaGetLastError();
         return 0;

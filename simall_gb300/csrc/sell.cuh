@@ -153,18 +153,21 @@ __device__ __forceinline__ void sell_slice(const SellOp &A, int64_t sl, const fl
 
 // ---------------------------------------------------------------- staged step
 // The same step with the streamed operands staged through shared memory by
-// bulk copies (TMA).  A CTA owns the contiguous slices [c0, c1) and walks
-// them in stages of 8 slices (one per warp).  For a stage, thread 0 issues
-// four bulk copies -- the rows' packed state and row sums, and the stage's
-// offsets and values, each one contiguous range because slices are stored
-// one after the other -- into one slot of a ring of kSellStages buffers, with
-// an mbarrier counting the bytes; the copies of the next kSellStages - 1
-// stages are in flight while a stage is computed.  The threads then read
-// their row's state and entries from shared memory, and only the neighbours'
-// state is gathered from global memory (L1/L2).  Slices up to kSellStageMaxW
-// entries wide take this path (every hex, tet or prism mesh); wider ones the
-// direct sell_slice.
-constexpr int kSellStageSlices = 8;  // slices per stage: one per warp of a 256-thread CTA
+// bulk copies (TMA).  A CTA of kSellThreads owns the contiguous slices
+// [c0, c1) and walks them in stages of 8 slices: warps 0-7 each compute one
+// slice of a stage, warp 8 produces.  For a stage the producer issues four
+// bulk copies -- the rows' packed state and row sums, and the stage's offsets
+// and values, each one contiguous range because slices are stored one after
+// the other -- into one slot of a ring of kSellStages buffers, announced on
+// the slot's `full` mbarrier; it refills a slot once all 8 compute warps have
+// arrived on its `empty` mbarrier.  A compute warp waits for its slot's copies
+// only, reads its rows' state and entries from shared memory and gathers
+// only the neighbours' state from global memory (L1/L2), so warps run up to
+// kSellStages - 1 stages apart and never wait for one another.  Slices up to
+// kSellStageMaxW entries wide take this path (every hex, tet or prism mesh);
+// wider ones the direct sell_slice.
+constexpr int kSellStageSlices = 8;  // slices per stage: one per compute warp
+constexpr int kSellThreads = 32 * (kSellStageSlices + 1);  // 8 compute warps + the producer warp
 constexpr int kSellStageMaxW = 8;    // widest slice a stage buffer holds
 constexpr int kSellStages = 3;       // ring depth
 constexpr int kSellStageEntries = kSellStageSlices * 32 * kSellStageMaxW;
@@ -178,21 +181,30 @@ template <bool WIDE> struct SellStageBuf {
 
 template <bool WIDE> constexpr size_t sell_stage_smem() { return kSellStages * sizeof(SellStageBuf<WIDE>); }
 
-// The ring of one CTA: kSellStages buffers (dynamic shared memory) and their
-// mbarriers; q counts the stages this CTA has issued, the same value in every
-// thread, so slot and phase parity of every stage follow from it.
+// The ring of one CTA: kSellStages buffers (dynamic shared memory), their
+// full and empty mbarriers (2 kSellStages, initialised by sell_ring_init);
+// q counts the stages this CTA has used, the same value in every thread, so
+// the slot and phase parity of every stage follow from it.
 template <bool WIDE> struct SellRing {
     SellStageBuf<WIDE> *buf;
-    uint64_t *bar;
+    uint64_t *bar;  // [0, kSellStages) full, [kSellStages, 2 kSellStages) empty
     uint32_t q;
 };
 
+// Thread 0, once per launch, before a block barrier.
+__device__ __forceinline__ void sell_ring_init(uint64_t *bar)
+{
+    for (int b = 0; b < kSellStages; ++b) {
+        mbar_init(bar + b, 1);
+        mbar_init(bar + kSellStages + b, kSellStageSlices);
+    }
+    mbar_fence_init();
+}
+
 template <bool WIDE>
 __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, int64_t c1, int s, const float4 *in,
-                                                 SellRing<WIDE> &R, uint32_t gq)
+                                                 SellStageBuf<WIDE> &B, uint64_t *bar)
 {
-    SellStageBuf<WIDE> &B = R.buf[gq % kSellStages];
-    uint64_t *bar = R.bar + gq % kSellStages;
     const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
     const int64_t sb = sa + kSellStageSlices < c1 ? sa + kSellStageSlices : c1;
     const int32_t ea = __ldg(A.sptr + sa), eb = __ldg(A.sptr + sb);
@@ -213,10 +225,11 @@ __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, in
     }
 }
 
-// One step over the CTA's slices [c0, c1), staged.  in_written_here: `in` was
-// written earlier in the same launch (the persistent kernel), so the copies
-// follow a proxy fence.  Returns false -- the same in every thread -- when a
-// copy did not complete in time; the copies still in flight are then waited
+// One step over the CTA's slices [c0, c1), staged; every thread of the CTA
+// calls it.  in_written_here: `in` was written earlier in the same launch (the
+// persistent kernel), so the copies follow a proxy fence.  Returns false --
+// the same in every thread -- when a wait ran out (a copy that did not land,
+// a slot that was not released); the copies still in flight are then waited
 // for (bounded) before returning.
 template <bool WIDE, bool NC>
 __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const float4 *in, float4 *out, float alpha,
@@ -224,49 +237,59 @@ __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const 
 {
     const int nst = static_cast<int>((c1 - c0 + kSellStageSlices - 1) / kSellStageSlices);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) {
-        if (in_written_here)
-            fence_proxy_async_global();
-        fence_proxy_async_shared();
-        for (int s = 0; s < kSellStages - 1 && s < nst; ++s)
-            sell_issue_stage<WIDE>(A, c0, c1, s, in, R, R.q + s);
-    }
+    uint64_t *full = R.bar, *empty = R.bar + kSellStages;
     bool ok = true;
-    int s = 0;
-    for (; s < nst; ++s) {
-        if (threadIdx.x == 0 && s + kSellStages - 1 < nst) {
-            fence_proxy_async_shared();  // the slot was read (generic proxy) in stage s - 1
-            sell_issue_stage<WIDE>(A, c0, c1, s + kSellStages - 1, in, R, R.q + s + kSellStages - 1);
+    if (warp == kSellStageSlices) {
+        // producer
+        if (lane == 0) {
+            if (in_written_here)
+                fence_proxy_async_global();
+            int s = 0;
+            for (; s < nst; ++s) {
+                const uint32_t u = R.q + s;
+                if (u >= static_cast<uint32_t>(kSellStages) &&
+                    !mbar_wait(empty + u % kSellStages, (u / kSellStages - 1) & 1u)) {
+                    ok = false;
+                    break;
+                }
+                fence_proxy_async_shared();  // the slot's previous contents were read through the generic proxy
+                sell_issue_stage<WIDE>(A, c0, c1, s, in, R.buf[u % kSellStages], full + u % kSellStages);
+            }
+            if (!ok) {
+                // the copies issued and not yet consumed: let them land before the CTA can leave
+                for (int t = s - kSellStages < 0 ? 0 : s - kSellStages; t < s; ++t)
+                    mbar_wait(full + (R.q + t) % kSellStages, ((R.q + t) / kSellStages) & 1u);
+            }
         }
-        const uint32_t gq = R.q + s;
-        const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
-        const int64_t sl = sa + warp;
-        const bool has = sl < c1;
-        const int32_t ea = __ldg(A.sptr + sa);
-        const int32_t e0 = has ? __ldg(A.sptr + sl) : ea;
-        const int w = has ? (__ldg(A.sptr + sl + 1) - e0) >> 5 : 0;
-        ok = mbar_wait(R.bar + gq % kSellStages, (gq / kSellStages) & 1u) && ok;
-        const SellStageBuf<WIDE> &B = R.buf[gq % kSellStages];
-        const int64_t i = sl * 32 + lane;
-        if (ok && has && i < A.n) {
-            const int t = warp * 32 + lane;
-            const RowStep rs(B.state[t], alpha, beta);
-            const float y = sell_row_any<NC>(w, B.off, B.val, e0 - ea + lane, static_cast<int32_t>(i), rs.p, B.e[t],
-                                             in, alpha, beta);
-            rs.finish(y, out + i, acc);
+    } else {
+        for (int s = 0; s < nst; ++s) {
+            const uint32_t u = R.q + s;
+            const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
+            const int64_t sl = sa + warp;
+            const bool has = sl < c1;
+            const int32_t ea = __ldg(A.sptr + sa);
+            const int32_t e0 = has ? __ldg(A.sptr + sl) : ea;
+            const int w = has ? (__ldg(A.sptr + sl + 1) - e0) >> 5 : 0;
+            if (!mbar_wait(full + u % kSellStages, (u / kSellStages) & 1u)) {
+                ok = false;
+                break;
+            }
+            const SellStageBuf<WIDE> &B = R.buf[u % kSellStages];
+            const int64_t i = sl * 32 + lane;
+            if (has && i < A.n) {
+                const int t = warp * 32 + lane;
+                const RowStep rs(B.state[t], alpha, beta);
+                const float y = sell_row_any<NC>(w, B.off, B.val, e0 - ea + lane, static_cast<int32_t>(i), rs.p,
+                                                 B.e[t], in, alpha, beta);
+                rs.finish(y, out + i, acc);
+            }
+            __syncwarp();
+            if (lane == 0)
+                mbar_arrive(empty + u % kSellStages);
         }
-        ok = __syncthreads_and(ok) != 0;  // every thread is done with the slot; one verdict for the CTA
-        if (!ok)
-            break;
-    }
-    if (!ok) {
-        // stages s .. the last issued may still be copying into this CTA's shared memory
-        const int issued = nst < s + kSellStages ? nst : s + kSellStages;
-        for (int t = s; t < issued; ++t)
-            mbar_wait(R.bar + (R.q + t) % kSellStages, ((R.q + t) / kSellStages) & 1u);
     }
     R.q += static_cast<uint32_t>(nst);
-    return ok;
+    return __syncthreads_and(ok) != 0;
 }
 
 }  // namespace simall

@@ -151,9 +151,9 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
 // *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
 constexpr int kGridMaxCtasPerSm = 4;
-// Resident CTAs per SM of a kBlock-thread kernel with `smem` bytes of dynamic
-// shared memory (its limit raised first); cached per context and kernel.
-int staged_residency(simall_context *ctx, const void *fn, size_t smem, int *per_sm);
+// Resident CTAs per SM of a kernel of `threads` threads with `smem` bytes of
+// dynamic shared memory (its limit raised first); cached per context and kernel.
+int staged_residency(simall_context *ctx, const void *fn, int threads, size_t smem, int *per_sm);
 struct GridMixedArgs {
     int64_t nslices;
     bool wide;
