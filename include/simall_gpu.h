@@ -549,13 +549,20 @@ int simall_simp_destroy(simall_simp *s);
 int simall_diagnose_bounded_wait(simall_context *ctx, int *timed_out, double *seconds);
 /* Latency measurements of the free-running triangular sweeps (ILU(0), SSOR,
  * the AMG smoother's large levels; no reference counterpart): sets, for the
- * whole process, the CTAs per SM of their grid (1..8; default 4), the longest
+ * whole process, the CTAs per SM of their grid (1..8; default 2), the longest
  * sleep between two polls of a value not yet published (0..4096 ns, 0 = spin;
- * default 256) and whether the ILU(0) backward sweep divides through the
+ * default 0) and whether the ILU(0) backward sweep divides through the
  * correctly rounded reciprocal of the pivot (1, default) or by a division (0).
  * Results do not depend on any of them.  Solvers capture their iteration
  * graphs at their first solve: set these before creating the solver. */
 int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns, int divide_via_reciprocal);
+/* Launch parameters of the mixed-precision solve in sliced storage, for the
+ * whole process: how many stages ahead the staged step prefetches its
+ * operands into L2 (0..64; default 0 = none), and the CTAs per SM of the
+ * persistent whole-solve launch (0..8; default 0 = as many as fit).  Results
+ * do not depend on the first; the second regroups the FP32 partial sums.  Set
+ * them before creating the solver. */
+int simall_diagnose_mixed_params(int prefetch_stages, int grid_ctas_per_sm);
 /* The small-system ILU(0) path divides through a correctly rounded reciprocal
  * (one product and two FMAs, Markstein's correction).  For each i, q_recip[i]
  * is that quotient a[i] / b[i] and q_div[i] the device's correctly rounded

@@ -115,6 +115,7 @@ SIGNATURES = {
     "simall_context_kernel_launches": (_I64, [_P]),
     "simall_diagnose_bounded_wait": (_I, [_P, C.POINTER(_I), C.POINTER(_D)]),
     "simall_diagnose_sweep_params": (_I, [_I, _I, _I]),
+    "simall_diagnose_mixed_params": (_I, [_I, _I]),
     "simall_diagnose_division": (_I, [_P, _I64, _P, _P, _P, _P]),
     "simall_solver_config_default": (None, [C.POINTER(SolverConfig)]),
     "simall_solver_create": (_I, [_P, C.POINTER(SolverConfig), C.POINTER(_P)]),

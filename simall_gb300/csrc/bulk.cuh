@@ -82,6 +82,13 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                  : "memory");
 }
 
+// Prefetch of `bytes` (multiple of 16, 16-byte aligned) from global memory
+// into L2; no completion to wait for.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes)
+{
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // Orders this thread's earlier generic-proxy accesses (and the data it has
 // acquired from other threads) before its later async-proxy accesses: global
 // data written by other CTAs earlier in the same launch, and shared buffers

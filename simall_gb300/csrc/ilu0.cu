@@ -39,8 +39,8 @@
 
 namespace simall {
 
-int g_sweep_ctas_per_sm = 4;
-unsigned g_sweep_backoff_ns = 256;
+int g_sweep_ctas_per_sm = 2;
+unsigned g_sweep_backoff_ns = 0;
 bool g_sweep_reciprocal = true;
 
 namespace {
@@ -783,7 +783,7 @@ int sweeps(simall_context *ctx, IluData *d, const int32_t *rowPtr, const int32_t
         SIMALL_LAUNCH_CHECK(ctx);
         return SIMALL_OK;
     }
-    // warps beyond a few levels' rows only add polls: g_sweep_ctas_per_sm (4: 32 warps per SM)
+    // warps beyond a few levels' rows only add polls: g_sweep_ctas_per_sm (2: 16 warps per SM)
     const int grid = ctx->num_sms * g_sweep_ctas_per_sm;
     const unsigned backoff = g_sweep_backoff_ns;
     const double *rdiag = (g_sweep_reciprocal && !ssor && lu == d->lu.p && d->rdiag.p) ? d->rdiag.p : nullptr;
@@ -968,6 +968,15 @@ int simall_diagnose_sweep_params(int ctas_per_sm, int backoff_ns, int divide_via
     g_sweep_ctas_per_sm = ctas_per_sm;
     g_sweep_backoff_ns = static_cast<unsigned>(backoff_ns);
     g_sweep_reciprocal = divide_via_reciprocal != 0;
+    return SIMALL_OK;
+}
+
+int simall_diagnose_mixed_params(int prefetch_stages, int grid_ctas_per_sm)
+{
+    if (prefetch_stages < 0 || prefetch_stages > 64 || grid_ctas_per_sm < 0 || grid_ctas_per_sm > 8)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    g_sell_prefetch = prefetch_stages;
+    g_grid_ctas_per_sm = grid_ctas_per_sm;
     return SIMALL_OK;
 }
 

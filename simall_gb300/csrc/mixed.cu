@@ -49,6 +49,9 @@
 
 namespace simall {
 
+int g_sell_prefetch = 0;
+int g_grid_ctas_per_sm = 0;
+
 constexpr int kMaxDiags = 8;
 
 struct DiaOffsets {
@@ -907,6 +910,7 @@ SellOp sell_op(const simall_solver *s, const MixedData *m)
     A.off32 = m->soff32.p;
     A.val = m->sval.p;
     A.e = m->e.p;
+    A.prefetch = g_sell_prefetch;
     return A;
 }
 

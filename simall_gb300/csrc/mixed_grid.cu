@@ -426,7 +426,8 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     }
     // a stage of slices per CTA at least, never more CTAs than are resident
     const int64_t want = std::max<int64_t>(1, (a.nslices + kSellStageSlices - 1) / kSellStageSlices);
-    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * std::min(per_sm, kGridMaxCtasPerSm);
+    const int use = g_grid_ctas_per_sm > 0 ? std::min(per_sm, g_grid_ctas_per_sm) : per_sm;
+    const int64_t cap = static_cast<int64_t>(ctx->num_sms) * std::min(use, kGridMaxCtasPerSm);
     const int grid = static_cast<int>(std::min(want, cap));
     if (static_cast<size_t>(grid) * 8 > a.partCap)
         return 0;
@@ -438,6 +439,7 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     g.A.off32 = a.off32;
     g.A.val = a.sval;
     g.A.e = a.e;
+    g.A.prefetch = g_sell_prefetch;
     g.rowPtr = s->rowPtr;
     g.colIdx = s->colIdx;
     g.val = s->values;

@@ -40,6 +40,7 @@ struct SellOp {
     const int32_t *off32 = nullptr; // wide column offsets
     const float *val = nullptr;
     const float *e = nullptr;       // [nslices * 32] row sums, zero past n
+    int prefetch = 0;               // staged steps: stages ahead whose operands are prefetched into L2 (0 = off)
 };
 
 // Vector loads: through the read-only path in per-step kernels (NC), plain
@@ -201,6 +202,26 @@ __device__ __forceinline__ void sell_ring_init(uint64_t *bar)
     mbar_fence_init();
 }
 
+// L2 prefetch of stage s's four ranges (the same ranges sell_issue_stage copies).
+template <bool WIDE>
+__device__ __forceinline__ void sell_prefetch_stage(const SellOp &A, int64_t c0, int64_t c1, int s, const float4 *in)
+{
+    const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
+    const int64_t sb = sa + kSellStageSlices < c1 ? sa + kSellStageSlices : c1;
+    const int32_t ea = __ldg(A.sptr + sa), eb = __ldg(A.sptr + sb);
+    const unsigned ne = static_cast<unsigned>(eb - ea);
+    const int64_t r0 = sa * 32, r1 = sb * 32 < A.n ? sb * 32 : A.n;
+    bulk_prefetch_l2(in + r0, static_cast<unsigned>(r1 - r0) * 16u);
+    bulk_prefetch_l2(A.e + r0, static_cast<unsigned>(sb - sa) * 128u);
+    if (ne) {
+        bulk_prefetch_l2(A.val + ea, ne * 4u);
+        if (WIDE)
+            bulk_prefetch_l2(A.off32 + ea, ne * 4u);
+        else
+            bulk_prefetch_l2(A.off16 + ea, ne * 2u);
+    }
+}
+
 template <bool WIDE>
 __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, int64_t c1, int s, const float4 *in,
                                                  SellStageBuf<WIDE> &B, uint64_t *bar)
@@ -254,6 +275,8 @@ __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const 
                 }
                 fence_proxy_async_shared();  // the slot's previous contents were read through the generic proxy
                 sell_issue_stage<WIDE>(A, c0, c1, s, in, R.buf[u % kSellStages], full + u % kSellStages);
+                if (A.prefetch > 0 && s + A.prefetch < nst)
+                    sell_prefetch_stage<WIDE>(A, c0, c1, s + A.prefetch, in);
             }
             if (!ok) {
                 // the copies issued and not yet consumed: let them land before the CTA can leave

@@ -151,6 +151,11 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
 // *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
 constexpr int kGridMaxCtasPerSm = 4;
+// Mixed precision in sliced storage: stages ahead whose operands the staged
+// steps prefetch into L2 (0 = none), and CTAs per SM of the persistent solve
+// (0 = as many as fit).  Process-wide; simall_diagnose_mixed_params sets them.
+extern int g_sell_prefetch;
+extern int g_grid_ctas_per_sm;
 // Resident CTAs per SM of a kernel of `threads` threads with `smem` bytes of
 // dynamic shared memory (its limit raised first); cached per context and kernel.
 int staged_residency(simall_context *ctx, const void *fn, int threads, size_t smem, int *per_sm);
