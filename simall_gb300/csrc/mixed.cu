@@ -584,12 +584,12 @@ __global__ void __launch_bounds__(kBlock) k_mx_iter_sell(SellOp A, const float4 
         return;
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
-    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
     const int64_t nw = (static_cast<int64_t>(gridDim.x) * blockDim.x) >> 5;
     for (int64_t sl = (blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x) >> 5; sl < A.nslices; sl += nw)
         sell_slice<WIDE, true>(A, sl, in, out, alpha, beta, acc);
     double t[4];
-    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0)
+    if (ff_grid_sum_last<4>(acc, reinterpret_cast<FF *>(partials), &s->counter[1], t) && threadIdx.x == 0)
         mx_finish<FRESH>(s, t);
 }
 
@@ -616,13 +616,14 @@ __global__ void __launch_bounds__(kSellThreads) k_mx_iter_sell_staged(SellOp A, 
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
     const int64_t c0 = blockIdx.x * A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * A.nslices / gridDim.x;
-    float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+    FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
     if (!sell_step_staged<WIDE, true>(A, c0, c1, in, out, alpha, beta, acc, R, false) && threadIdx.x == 0) {
         atomicExch(&s->status, SIMALL_ERR_TIMEOUT);
         atomicExch(&s->done, 1);
     }
     double t[4];
-    if (grid_sum_last_fv<4>(acc, partials, &s->counter[1], t) && threadIdx.x == 0 && !ld_flag(&s->done))
+    if (ff_grid_sum_last<4>(acc, reinterpret_cast<FF *>(partials), &s->counter[1], t) && threadIdx.x == 0 &&
+        !ld_flag(&s->done))
         mx_finish<FRESH>(s, t);
 }
 

@@ -141,6 +141,31 @@ __device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *c
     return true;
 }
 
+// The step's four sums: float-float from the thread up (ffsum.cuh), one
+// float-float slot per CTA, FP64 totals in every thread.  Returns false on a
+// barrier timeout.
+template <int NV>
+__device__ bool ff_grid_allsum(FF (&v)[NV], double *part, unsigned long long *ctr, unsigned long long &epoch, int *err,
+                               double (&total)[NV])
+{
+    ff_block_allsum<NV>(v);
+    FF *slot = reinterpret_cast<FF *>(part) + (epoch & 1ull) * gridDim.x * NV;
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            slot[static_cast<int64_t>(blockIdx.x) * NV + k] = v[k];
+    }
+    ++epoch;
+    if (!grid_barrier(ctr, epoch, err))
+        return false;
+    FF out[NV];
+    ff_sum_slots<NV>(slot, gridDim.x, out);
+#pragma unroll
+    for (int k = 0; k < NV; ++k)
+        total[k] = ff_double(out[k]);
+    return true;
+}
+
 // FP32 per-thread partials: lanes summed in FP32, everything above in FP64.
 template <int NV>
 __device__ bool grid_allsum_f(const float (&v)[NV], double (&out)[NV], double *part, unsigned long long *ctr,
@@ -346,7 +371,7 @@ __global__ void __launch_bounds__(kSellThreads, 4) k_mx_grid_solve(GridArgs g)
         // ---- one fused step
         const int par = st.par;
         const float alpha = st.fresh ? 0.0f : st.alpha_f, beta = st.beta_f;
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
         if (STAGED) {
             if (!sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true)) {
                 if (threadIdx.x == 0)
@@ -359,7 +384,7 @@ __global__ void __launch_bounds__(kSellThreads, 4) k_mx_grid_solve(GridArgs g)
                 sell_slice<WIDE, false>(g.A, sl, g.st[par], g.st[1 - par], alpha, beta, acc);
         }
         double t[4];
-        if (!(ok = grid_allsum_f<4>(acc, t, g.part, g.ctr, epoch, g.err)))
+        if (!(ok = ff_grid_allsum<4>(acc, g.part, g.ctr, epoch, g.err, t)))
             break;
         if (threadIdx.x == 0)
             st.finish_step(t, g.tol, g.delta, g.max_iter);

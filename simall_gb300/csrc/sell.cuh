@@ -26,6 +26,7 @@
 #pragma once
 
 #include "bulk.cuh"
+#include "ffsum.cuh"
 
 #include <cstdint>
 #include <type_traits>
@@ -111,7 +112,8 @@ __device__ __forceinline__ float sell_row_any(int w, const OffT *off, const floa
 
 // The step of one row from its previous state o:
 //     r = r_old - alpha q_old,  p = r + beta p_old,  xh += alpha p_old,
-//     q = (S A S) p,  and the row's shares of p.q, q.q, r.r, r.q.
+//     q = (S A S) p,  and the row's shares of p.q, q.q, r.r, r.q, added to
+// the thread's float-float sums (ffsum.cuh).
 struct RowStep {
     float r, p, xh;
     __device__ __forceinline__ RowStep(const float4 &o, float alpha, float beta)
@@ -120,20 +122,20 @@ struct RowStep {
         p = __fmaf_rn(beta, o.z, r);
         xh = __fmaf_rn(alpha, o.z, o.w);
     }
-    __device__ __forceinline__ void finish(float q, float4 *out, float (&acc)[4]) const
+    __device__ __forceinline__ void finish(float q, float4 *out, FF (&acc)[4]) const
     {
         *out = make_float4(r, q, p, xh);
-        acc[0] += p * q;
-        acc[1] += q * q;
-        acc[2] += r * r;
-        acc[3] += r * q;
+        ff_dot_add(acc[0], p, q);
+        ff_dot_add(acc[1], q, q);
+        ff_dot_add(acc[2], r, r);
+        ff_dot_add(acc[3], r, q);
     }
 };
 
 // One step over slice sl (direct loads; any width).
 template <bool WIDE, bool NC>
 __device__ __forceinline__ void sell_slice(const SellOp &A, int64_t sl, const float4 *in, float4 *out, float alpha,
-                                           float beta, float (&acc)[4])
+                                           float beta, FF (&acc)[4])
 {
     const int lane = threadIdx.x & 31;
     const int64_t i = sl * 32 + lane;
@@ -254,7 +256,7 @@ __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, in
 // for (bounded) before returning.
 template <bool WIDE, bool NC>
 __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const float4 *in, float4 *out, float alpha,
-                                 float beta, float (&acc)[4], SellRing<WIDE> &R, bool in_written_here)
+                                 float beta, FF (&acc)[4], SellRing<WIDE> &R, bool in_written_here)
 {
     const int nst = static_cast<int>((c1 - c0 + kSellStageSlices - 1) / kSellStageSlices);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
