@@ -692,7 +692,8 @@ __global__ void __launch_bounds__(kBlock) k_mx_fold(int64_t n, const double *__r
     }
 }
 
-// U2: r = b - A x in FP64 (staged CSR SpMV); stop test on the true residual.
+// U2: r = b - A x in FP64 (staged CSR SpMV, one FMA per entry); stop test on
+// the true residual.
 struct ResEpi {
     const double *b;
     double *r;
@@ -715,7 +716,7 @@ __global__ void __launch_bounds__(kBlock) k_mx_true_residual(const int32_t *__re
     if (!ld_flag(&s->need_update) || ld_flag(&s->done))
         return;
     ResEpi epi{b, r, 0.0};
-    spmv_rowblocks(rowPtr, colIdx, val, rb, nRB, x, epi);
+    spmv_rowblocks_fma(rowPtr, colIdx, val, rb, nRB, x, epi);  // one FMA per entry: GB300's FP64 pipe is narrow
     double v[1] = {epi.acc};
     if (grid_sum_last<1>(v, partials, &s->counter[3]) && threadIdx.x == 0) {
         s->rr = v[0];

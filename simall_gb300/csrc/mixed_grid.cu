@@ -405,12 +405,12 @@ __global__ void __launch_bounds__(kSellThreads, 4) k_mx_grid_solve(GridArgs g)
         float4 *srep = g.st[st.par];
         double a[2] = {0.0, 0.0};
         for (int64_t i = tid; i < n; i += nthr) {
-            // products rounded, then summed from 0.0 in column order (the
-            // per-step engine's true residual, spmv_rowblocks)
+            // one FMA per entry from 0.0 in column order (the per-step
+            // engine's true residual, spmv_rowblocks_fma)
             const int k1 = __ldg(g.rowPtr + i + 1);
             double y = 0.0;
             for (int k = __ldg(g.rowPtr + i); k < k1; ++k)
-                y = __dadd_rn(y, __dmul_rn(__ldg(g.val + k), g.x[__ldg(g.colIdx + k)]));
+                y = __fma_rn(__ldg(g.val + k), g.x[__ldg(g.colIdx + k)], y);
             const double v = g.b[i] - y;
             const float f = static_cast<float>(g.sc[i] * v);
             float *e = reinterpret_cast<float *>(srep + i);
