@@ -58,16 +58,31 @@ __device__ __forceinline__ bool mbar_test(uint64_t *bar, unsigned parity)
     return done != 0;
 }
 
+// One potentially blocking test: the thread may be suspended in hardware
+// until the phase completes or a system-dependent time limit passes, so a
+// waiting warp takes no issue slots from the warps that compute.
+__device__ __forceinline__ bool mbar_try(uint64_t *bar, unsigned parity)
+{
+    uint32_t done;
+    asm volatile("{\n\t.reg .pred p;\n\t"
+                 "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+                 "selp.u32 %0, 1, 0, p;\n\t}"
+                 : "=r"(done)
+                 : "r"(smem_u32(bar)), "r"(parity)
+                 : "memory");
+    return done != 0;
+}
+
 // Waits for the phase of parity `parity` to complete; false after ~4 s.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity)
 {
-    if (mbar_test(bar, parity))
+    if (mbar_try(bar, parity))
         return true;
     const unsigned long long t0 = globaltimer_ns();
-    for (unsigned spins = 1;; ++spins) {
-        if (mbar_test(bar, parity))
+    for (;;) {
+        if (mbar_try(bar, parity))
             return true;
-        if ((spins & 255u) == 0 && globaltimer_ns() - t0 > kBulkWaitNs)
+        if (globaltimer_ns() - t0 > kBulkWaitNs)
             return false;
     }
 }
