@@ -97,6 +97,27 @@ __device__ __forceinline__ void bulk_load(void *dst, const void *src, unsigned b
                  : "memory");
 }
 
+// An L2 policy that evicts the lines it touches first: for data read once
+// per pass (a matrix streamed every step), so that it does not push data that
+// is read again (the vectors other rows gather) out of L2.
+__device__ __forceinline__ uint64_t l2_evict_first_policy()
+{
+    uint64_t pol;
+    asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(pol));
+    return pol;
+}
+
+// bulk_load with an L2 cache policy.
+__device__ __forceinline__ void bulk_load_hint(void *dst, const void *src, unsigned bytes, uint64_t *bar,
+                                               uint64_t policy)
+{
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes.L2::cache_hint [%0], [%1], %2, [%3], %4;" ::
+            "r"(smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar)), "l"(policy)
+        : "memory");
+}
+
 // Prefetch of `bytes` (multiple of 16, 16-byte aligned) from global memory
 // into L2; no completion to wait for.
 __device__ __forceinline__ void bulk_prefetch_l2(const void *src, unsigned bytes)

@@ -171,7 +171,7 @@ __device__ __forceinline__ void sell_slice(const SellOp &A, int64_t sl, const fl
 // wider ones the direct sell_slice.
 constexpr int kSellStageSlices = 8;  // slices per stage: one per compute warp
 constexpr int kSellThreads = 32 * (kSellStageSlices + 1);  // 8 compute warps + the producer warp
-constexpr int kSellStageMaxW = 8;    // widest slice a stage buffer holds
+constexpr int kSellStageMaxW = 6;    // widest slice a stage buffer holds (hex meshes: 6); less shared memory, more L1
 constexpr int kSellStages = 3;       // ring depth
 constexpr int kSellStageEntries = kSellStageSlices * 32 * kSellStageMaxW;
 
@@ -236,15 +236,18 @@ __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, in
     const unsigned sbytes = static_cast<unsigned>(r1 - r0) * 16u;
     const unsigned ebytes = static_cast<unsigned>(sb - sa) * 128u;  // whole slices: e is padded
     const unsigned ob = WIDE ? 4u : 2u;
+    // the matrix streams are read once per step: evict them first, so the
+    // state the neighbours gather stays in L2 between steps
+    const uint64_t once = l2_evict_first_policy();
     mbar_arrive_expect_tx(bar, sbytes + ebytes + ne * (4u + ob));
     bulk_load(B.state, in + r0, sbytes, bar);
-    bulk_load(B.e, A.e + r0, ebytes, bar);
+    bulk_load_hint(B.e, A.e + r0, ebytes, bar, once);
     if (ne) {
-        bulk_load(B.val, A.val + ea, ne * 4u, bar);
+        bulk_load_hint(B.val, A.val + ea, ne * 4u, bar, once);
         if (WIDE)
-            bulk_load(B.off, A.off32 + ea, ne * 4u, bar);
+            bulk_load_hint(B.off, A.off32 + ea, ne * 4u, bar, once);
         else
-            bulk_load(B.off, A.off16 + ea, ne * 2u, bar);
+            bulk_load_hint(B.off, A.off16 + ea, ne * 2u, bar, once);
     }
 }
 

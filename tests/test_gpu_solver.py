@@ -208,6 +208,39 @@ def test_sliced_storage_wide_offsets(sg, ctx, oracle):
         assert s.stats.converged and tr < 1e-9 and s.stats.engine == (2 if engine == 0 else 0)
 
 
+@pytest.mark.parametrize("engine", [0, 1])
+def test_sliced_storage_long_rows(sg, ctx, oracle, engine):
+    """A random graph Laplacian plus a diagonal shift (rows of up to ~20
+    off-diagonal entries): slices wider than a staged buffer take the direct
+    sliced step, on both engines."""
+    rng = np.random.default_rng(12)
+    n = 6000
+    i = rng.integers(0, n, 5 * n)
+    j = rng.integers(0, n, 5 * n)
+    keep = i != j
+    pairs = np.unique(np.sort(np.stack([i[keep], j[keep]], 1), axis=1), axis=0)
+    w = rng.uniform(0.1, 1.0, len(pairs))
+    r_ = np.concatenate([pairs[:, 0], pairs[:, 1]])
+    c_ = np.concatenate([pairs[:, 1], pairs[:, 0]])
+    v_ = -np.concatenate([w, w])
+    deg = np.bincount(r_, weights=-v_, minlength=n)
+    r_ = np.concatenate([r_, np.arange(n)])
+    c_ = np.concatenate([c_, np.arange(n)])
+    v_ = np.concatenate([v_, deg + 0.05])
+    order = np.lexsort((c_, r_))
+    rp = np.zeros(n + 1, np.int32)
+    np.add.at(rp, r_ + 1, 1)
+    rp = np.cumsum(rp).astype(np.int32)
+    ci, v = c_[order].astype(np.int32), v_[order]
+    assert np.max(np.diff(rp)) - 1 > 6
+    b = rng.standard_normal(n)
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=5000), precision=sg.Precision.MIXED, ctx=ctx, engine=engine)
+    x = np.zeros(n)
+    s.solve(sg.CSRMatrix(rp, ci, v), b, x)
+    tr = np.linalg.norm(b - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(b)
+    assert s.stats.converged and tr < 1e-9 and s.stats.engine == (2 if engine == 0 else 0)
+
+
 def test_zero_rhs_returns_zero(sg, ctx, oracle):
     m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 6)
     for prec in (sg.Precision.FP64, sg.Precision.MIXED):
