@@ -406,11 +406,12 @@ __global__ void __launch_bounds__(kSellThreads, 4) k_mx_grid_solve(GridArgs g)
         double a[2] = {0.0, 0.0};
         for (int64_t i = tid; i < n; i += nthr) {
             // one FMA per entry from 0.0 in column order (the per-step
-            // engine's true residual, spmv_rowblocks_fma)
-            const int k1 = __ldg(g.rowPtr + i + 1);
+            // engine's true residual, spmv_rowblocks_fma); A is streamed with
+            // the evict-first hint (__ldcs) so the iteration state stays in L2
+            const int k1 = __ldcs(g.rowPtr + i + 1);
             double y = 0.0;
-            for (int k = __ldg(g.rowPtr + i); k < k1; ++k)
-                y = __fma_rn(__ldg(g.val + k), g.x[__ldg(g.colIdx + k)], y);
+            for (int k = __ldcs(g.rowPtr + i); k < k1; ++k)
+                y = __fma_rn(__ldcs(g.val + k), g.x[__ldcs(g.colIdx + k)], y);
             const double v = g.b[i] - y;
             const float f = static_cast<float>(g.sc[i] * v);
             float *e = reinterpret_cast<float *>(srep + i);
