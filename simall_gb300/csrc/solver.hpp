@@ -150,7 +150,7 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
 // whole-solve persistent cooperative kernel (mixed_grid.cu); 0 = not taken
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
 // *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
-constexpr int kGridMaxCtasPerSm = 4;
+constexpr int kGridMaxCtasPerSm = 3;  // the persistent mixed solve: 3 of 288 threads per SM measured fastest at 128^3
 // Mixed precision in sliced storage: stages ahead whose operands the staged
 // steps prefetch into L2 (0 = none), and CTAs per SM of the persistent solve
 // (0 = as many as fit).  Process-wide; simall_diagnose_mixed_params sets them.
