@@ -330,8 +330,21 @@ def run_batched(a, ctx, sg, rank=0, world=1, with_cpu=False):
             "speedup_vs_fp64_loop": round(loop_s / (batch_ms / 1e3), 2),
             "converged": int(tot.converged), "systems": int(tot.systems), "max_iterations": int(tot.max_iterations),
             "total_iterations": int(tot.total_iterations), "worst_true_residual": float(tot.worst_true_residual),
-            "max_rel_diff_vs_fp64": diff, "launch_shape": [int(tot.block_threads), int(tot.ctas_per_sm)],
+            "max_rel_diff_vs_fp64": diff,
+            "launch_shape": {"block_threads": int(tot.block_threads), "ctas_per_sm": int(tot.ctas_per_sm),
+                             "rows_per_pass": int(tot.rows_per_pass),
+                             "source": ["set", "timed", "autotuner cache"][int(tot.autotune_source)]},
             "setup_seconds": round(setup, 2), "ranks": world, "systems_on_rank0": len(systems)}
+    # roofline of the fused step: per row and step the packed state is read
+    # and written (2 x 16 B), the row sum read (4 B) and the two stored upper
+    # diagonals of a 5-point system (2 x 4 B): 44 B x rows x steps of each system
+    row_steps = float(sum(int(st["iterations"][i]) * int(rows[i + 1] - rows[i]) for i in range(len(systems))))
+    gbs = 44.0 * row_steps / (batch_ms / 1e3) / 1e9
+    peak, peak_kind = measured_peaks()
+    out["roofline"] = {"bound": "hbm", "bytes_per_row_step": 44, "row_steps": row_steps, "achieved": round(gbs, 1),
+                       "peak": peak, "unit": "GB/s", "frac": round(gbs / peak, 4),
+                       "peak_source": f"{peak_kind} hbm_gbs",
+                       "note": "algorithmic bytes; systems of up to 65,536 rows keep part of their state in L2"}
     if cpu:
         out["cpu_baseline"] = cpu
     return out

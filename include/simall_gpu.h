@@ -600,6 +600,8 @@ typedef struct simall_batch_stats {
     int block_threads;        /* launch shape in use (autotuned unless set) */
     int ctas_per_sm;
     double seconds;
+    int rows_per_pass;        /* rows each thread keeps in flight */
+    int autotune_source;      /* 0 set by simall_batch_launch_shape, 1 timed on this batch, 2 autotuner cache */
 } simall_batch_stats;
 /* cfg: tolerance, max_iterations, reliable_delta as for simall_solver (Jacobi). */
 int simall_batch_create(simall_context *ctx, const simall_solver_config *cfg, simall_batch **out);
@@ -610,10 +612,24 @@ int simall_batch_set_systems(simall_batch *b, int n_systems, const int64_t *row_
 /* Solves every system from x = 0.  per_system (optional) has n_systems entries. */
 int simall_batch_solve(simall_batch *b, const double *rhs, double *x, int mem, simall_batch_system_stats *per_system,
                        simall_batch_stats *total);
-/* Fixes the launch shape (256/512/1024 threads per CTA, 1-8 CTAs per SM);
- * block_threads == 0 re-enables the autotuner, which times the candidate
- * shapes on the batch at its next solve and keeps the fastest. */
+/* Fixes the launch shape (256/512/1024 threads per CTA, 1-8 CTAs per SM, at
+ * most 2048 threads per SM; 2 rows in flight per thread); block_threads == 0
+ * re-enables the autotuner, which at the next solve reads the autotuner cache
+ * or times the candidate shapes (threads per CTA, CTAs per SM, rows in flight
+ * per thread) on the batch and keeps the fastest. */
 int simall_batch_launch_shape(simall_batch *b, int block_threads, int ctas_per_sm);
+/* The autotuner cache file of this batch object (JSON; path NULL or "": no
+ * cache).  The default is SIMALL_AUTOTUNE_CACHE when set ("off": none), else
+ * $XDG_CACHE_HOME/simall_gb300/autotune.json, else
+ * $HOME/.cache/simall_gb300/autotune.json.  Entries are keyed by device name,
+ * SM count, kernel revision and a hash of the batch's system sizes. */
+int simall_batch_autotune_cache(simall_batch *b, const char *path);
+/* The cache itself (host only): values = {block_threads, ctas_per_sm,
+ * rows_per_pass}.  lookup returns SIMALL_OK when the key is present,
+ * SIMALL_ERR_IO when it is not (or the file cannot be read); store replaces or
+ * appends the key and rewrites the file through a rename. */
+int simall_autotune_cache_lookup(const char *path, const char *key, int *values);
+int simall_autotune_cache_store(const char *path, const char *key, const int *values, double ms);
 
 /* ------------------------------------------------------------------ reference GPU facade */
 /* One-for-one replacements of src/gpu/GpuKernels.hpp:48-108 on device

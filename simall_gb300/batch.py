@@ -2,6 +2,8 @@
 
 Many independent SPD systems solved in one persistent launch, each with the
 mixed-precision Jacobi-PCG; the Python side only concatenates the systems.
+The launch shape comes from the autotuner (timed on the batch, or read from
+its JSON cache, autotune_cache_lookup / autotune_cache_store).
 """
 from __future__ import annotations
 
@@ -57,6 +59,10 @@ class BatchedSolver:
     def launch_shape(self, block_threads: int, ctas_per_sm: int = 1):
         check(self.L.simall_batch_launch_shape(self.handle, int(block_threads), int(ctas_per_sm)))
 
+    def autotune_cache(self, path: str | None):
+        """Autotuner cache file of this batch (None or "": none)."""
+        check(self.L.simall_batch_autotune_cache(self.handle, (path or "").encode()))
+
     def solve(self, b, x=None, per_system: bool = True):
         """b: concatenated rhs (numpy, or a CUDA tensor with x also a CUDA tensor)."""
         if x is None:
@@ -82,3 +88,17 @@ class BatchedSolver:
             self.close()
         except Exception:
             pass
+
+
+def autotune_cache_lookup(path: str, key: str):
+    """(block_threads, ctas_per_sm, rows_per_pass) stored under key, or None."""
+    L = _lib.load()
+    v = (C.c_int * 3)()
+    st = L.simall_autotune_cache_lookup(path.encode(), key.encode(), v)
+    return tuple(v) if st == 0 else None
+
+
+def autotune_cache_store(path: str, key: str, values, ms: float = 0.0) -> int:
+    L = _lib.load()
+    v = (C.c_int * 3)(*[int(t) for t in values])
+    return int(L.simall_autotune_cache_store(path.encode(), key.encode(), v, float(ms)))

@@ -23,7 +23,9 @@
 // (threads) and CTAs per SM are picked by a small autotuner that times each
 // candidate on the batch itself the first time a batch shape is solved.
 #include "device.cuh"
-#include "ffop.cuh"
+#include "ffsum.cuh"
+#include "mixed_state.cuh"
+#include "sell.cuh"
 #include "solver.hpp"
 
 #include <algorithm>
@@ -71,18 +73,21 @@ struct simall_batch {
     simall::DevBuf<int> order, queue;
     simall::DevBuf<int32_t> rowPtr, colIdx, orow, ocol;
     simall::DevBuf<double> values, scale, b, x;
-    simall::DevBuf<float> U, oval, xh, rh, ph, qh;
-    simall::DevBuf<int8_t> Uc, oc;  // 8-bit corrections of U / oval (ffop.cuh)
+    simall::DevBuf<float> U, oval, e;
+    simall::DevBuf<float4> st[2];  // (r, q, p, xh) per row, by step parity
     simall::DevBuf<simall::BatchOut> out;
     std::vector<simall::BatchOut> h_out;
-    int block = 0, ctas_per_sm = 0;  // autotuned launch shape
+    int block = 0, ctas_per_sm = 0, rows_per_pass = 0;  // autotuned launch shape
+    int tune_source = 0;             // 0 set by the caller, 1 timed on this batch, 2 read from the cache
+    std::string cache_path;          // autotuner cache (JSON); empty: none
+    std::string shape_key;           // the batch's key in that cache
     bool ready = false;
     // the solve (queue reset + persistent kernel) captured as a graph for the
     // current shape and b/x pointers
     cudaGraphExec_t gexec = nullptr;
     const double *g_b = nullptr;
     double *g_x = nullptr;
-    int g_block = 0, g_ctas = 0;
+    int g_block = 0, g_ctas = 0, g_rpp = 0;
     ~simall_batch()
     {
         if (gexec)
@@ -95,280 +100,184 @@ namespace simall {
 
 namespace {
 
-// Sum over the CTA: FP32 within each warp, FP64 across warps; every thread
-// receives the totals.  red must hold 2*32 doubles.
-__device__ __forceinline__ void cta_allreduce2(float a, double b, double *red, double &sa, double &sb)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    a = warp_sum_f(a);
-    b = warp_sum(b);
-    if (lane == 0) {
-        red[wid] = static_cast<double>(a);
-        red[32 + wid] = b;
-    }
-    __syncthreads();
-    double ta = 0.0, tb = 0.0;
-    for (int w = 0; w < nw; ++w) {  // same order in every thread: identical totals
-        ta += red[w];
-        tb += red[32 + w];
-    }
-    __syncthreads();
-    sa = ta;
-    sb = tb;
-}
+// Everything one launch needs.
+struct BatchArgs {
+    const BatchSys *sys;
+    const int *order;
+    int nsys;
+    int *queue;
+    const int32_t *rowPtr, *colIdx;
+    const double *values;
+    const float *U;  // dia systems: [nd][n] upper diagonals of S A S
+    const int32_t *orow, *ocol;
+    const float *oval;  // csr systems: off-diagonal part of S A S
+    const float *e;     // row sums 1 + sum_j (S A S)_ij, every row
+    const double *scale, *b;
+    double *x;
+    float4 *st[2];  // (r, q, p, xh) per row, by step parity
+    double tol, delta;
+    int maxit;
+    BatchOut *out;
+};
 
-__device__ __forceinline__ double cta_allreduce_f(float a, double *red)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
-    a = warp_sum_f(a);
-    if (lane == 0)
-        red[wid] = static_cast<double>(a);
-    __syncthreads();
-    double t = 0.0;
-    for (int w = 0; w < nw; ++w)
-        t += red[w];
-    __syncthreads();
-    return t;
-}
-
-// Rows a thread handles per pass of a loop: it keeps its rows t, t + B,
-// t + 2B, ... in the same order, four at a time with all their loads issued
-// before the arithmetic, so a CTA alone keeps enough memory requests in
-// flight to stream a large system (one CTA per system).
-constexpr int kRowsPerPass = 8;
-
-// q = (S A S) p on rows [0, n) of one system: q_i = p_i + sum_j N_ij p_j with
-// N (the off-diagonal part of S A S) as FP32 entries plus their 8-bit
-// corrections, the row summed in float-float (ffop.cuh); returns this thread's
-// p.q part.
-__device__ __forceinline__ float batch_spmv(const BatchSys &S, const float *__restrict__ U,
-                                            const int8_t *__restrict__ Uc, const int32_t *__restrict__ orow,
-                                            const int32_t *__restrict__ ocol, const float *__restrict__ oval,
-                                            const int8_t *__restrict__ oc, const float *p, float *q)
-{
-    float acc = 0.0f;
-    const int n = S.n, B = blockDim.x;
-    if (S.nd > 0) {
-        const float *Us = U + S.u0;
-        const int8_t *Ucs = Uc + S.u0;
-        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * B) {
-            float pi[kRowsPerPass];
-            FFAcc y[kRowsPerPass];
-#pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * B;
-                pi[u] = i < n ? p[i] : 0.0f;
-                y[u] = ff_start(pi[u]);
-            }
-            for (int d = 0; d < S.nd; ++d) {
-                const int off = S.off[d];
-                const int64_t dd = static_cast<int64_t>(d) * n;
-#pragma unroll
-                for (int u = 0; u < kRowsPerPass; ++u) {
-                    const int i = i0 + u * B;
-                    if (i < n && i + off < n) {
-                        const float a = Us[dd + i];
-                        ff_add(y[u], a, ff_low(a, Ucs[dd + i]), p[i + off]);
-                    }
-                    if (i < n && i - off >= 0) {
-                        const float a = Us[dd + i - off];
-                        ff_add(y[u], a, ff_low(a, Ucs[dd + i - off]), p[i - off]);
-                    }
-                }
-            }
-#pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * B;
-                if (i < n) {
-                    const float qi = ff_value(y[u]);
-                    q[i] = qi;
-                    acc += pi[u] * qi;
-                }
-            }
-        }
-    } else {
-        const int32_t *rp = orow + S.orp0;
-        const int32_t *ci = ocol + S.u0;
-        const float *va = oval + S.u0;
-        const int8_t *vc = oc + S.u0;
-        for (int i = threadIdx.x; i < n; i += B) {
-            const float pi = p[i];
-            FFAcc y = ff_start(pi);
-            for (int k = rp[i]; k < rp[i + 1]; ++k)
-                ff_add(y, va[k], ff_low(va[k], vc[k]), p[ci[k]]);
-            const float qi = ff_value(y);
-            q[i] = qi;
-            acc += pi * qi;
-        }
-    }
-    return acc;
-}
-
-// One CTA solves one system (mixed precision, reliable updates).
-__device__ void batch_solve_one(const BatchSys &S, const int32_t *__restrict__ rowPtr,
-                                const int32_t *__restrict__ colIdx, const double *__restrict__ values,
-                                const float *__restrict__ U, const int32_t *__restrict__ orow,
-                                const int32_t *__restrict__ ocol, const float *__restrict__ oval,
-                                const int8_t *__restrict__ Uc, const int8_t *__restrict__ oc,
-                                const double *__restrict__ scale_all, const double *__restrict__ b_all,
-                                double *x_all, float *xh_all, float *rh_all, float *ph_all, float *qh_all, double tol,
-                                double delta, int maxit, BatchOut *out, double *red)
+// The row-sum product of row i of one system: e_i p_i - sum_j N_ij (p_i -
+// p_j), N = S A S - I, with p_j formed again from the neighbour's previous
+// state (sell.cuh p_of: the owner's two roundings, the same bits).
+__device__ __forceinline__ float batch_row(const BatchSys &S, const BatchArgs &a, const float4 *in, int i, float pi,
+                                           float alpha, float beta)
 {
     const int n = S.n;
-    const double *sc = scale_all + S.row0;
-    const double *b = b_all + S.row0;
-    double *x = x_all + S.row0;
-    float *xh = xh_all + S.row0, *rh = rh_all + S.row0, *ph = ph_all + S.row0, *qh = qh_all + S.row0;
-    const int32_t *rp = rowPtr + S.rp0;
-    const int32_t *ci = colIdx + S.nz0;
-    const double *va = values + S.nz0;
-
-    // init: x = 0, rh = S b, ph = rh, xh = 0
-    float a0 = 0.0f;
-    double a1 = 0.0;
-    for (int i = threadIdx.x; i < n; i += blockDim.x) {
-        const double bi = b[i];
-        const float r = static_cast<float>(bi * sc[i]);
-        x[i] = 0.0;
-        rh[i] = r;
-        ph[i] = r;
-        xh[i] = 0.0f;
-        a0 += r * r;
-        a1 += bi * bi;
-    }
-    double rho, bb;
-    cta_allreduce2(a0, a1, red, rho, bb);
-    const double bn = sqrt(bb);
-    const double bnorm = std_max(bn, 1e-30);
-    double sigma0 = sqrt(rho), rmax = sigma0, t0 = bn / bnorm, last = t0;
-    int it = 0, updates = 0, status = SIMALL_OK;
-    bool done = (t0 < tol) || maxit <= 0;
-    while (!done) {
-        // q = SAS p, alpha
-        const double pq = cta_allreduce_f(batch_spmv(S, U, Uc, orow, ocol, oval, oc, ph, qh), red);
-        const bool breakdown = !(pq > 0.0);
-        const float alpha = breakdown ? 0.0f : static_cast<float>(rho / pq);
-        // xh += alpha p, rh -= alpha q (own rows: no barrier needed before)
-        float rr_t = 0.0f;
-        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * blockDim.x) {
-            float xv[kRowsPerPass], pv[kRowsPerPass], rv[kRowsPerPass], qv[kRowsPerPass];
+    float y = __ldg(a.e + S.row0 + i) * pi;
+    if (S.nd > 0) {
+        const float *U = a.U + S.u0;
 #pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * blockDim.x;
-                xv[u] = i < n ? xh[i] : 0.0f;
-                pv[u] = i < n ? ph[i] : 0.0f;
-                rv[u] = i < n ? rh[i] : 0.0f;
-                qv[u] = i < n ? qh[i] : 0.0f;
+        for (int d = 0; d < kBatchDiags; ++d) {
+            if (d >= S.nd)
+                break;
+            const int off = S.off[d];
+            const float *Ud = U + static_cast<int64_t>(d) * n;
+            if (i + off < n)
+                y = __fmaf_rn(-__ldg(Ud + i), pi - p_of(in[i + off], alpha, beta), y);
+            if (i - off >= 0)
+                y = __fmaf_rn(-__ldg(Ud + i - off), pi - p_of(in[i - off], alpha, beta), y);
+        }
+    } else {
+        const int32_t *rp = a.orow + S.orp0;
+        const int32_t *cc = a.ocol + S.u0;
+        const float *vv = a.oval + S.u0;
+        for (int k = __ldg(rp + i); k < __ldg(rp + i + 1); ++k)
+            y = __fmaf_rn(-__ldg(vv + k), pi - p_of(in[__ldg(cc + k)], alpha, beta), y);
+    }
+    return y;
+}
+
+// One CTA solves one system: the fused mixed-precision CG step of the sliced
+// engines (sell.cuh: r, p, xh updates and q = (S A S) p in one pass over the
+// packed state, four float-float sums, one block reduction per step), the
+// reliable updates and stop test of MixedState.  Rows t, t + B, ... of the
+// system belong to thread t; RPP of them are in flight at a time.  The
+// state of a step is written by the CTA's own threads in the previous step,
+// so plain loads after the block barrier see it.
+template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const BatchArgs &a, BatchOut *out)
+{
+    __shared__ MixedState ms;
+    const int n = S.n, B = blockDim.x;
+    const double *sc = a.scale + S.row0;
+    const double *b = a.b + S.row0;
+    double *x = a.x + S.row0;
+    float4 *st[2] = {a.st[0] + S.row0, a.st[1] + S.row0};
+    const int32_t *rp = a.rowPtr + S.rp0;
+    const int32_t *ci = a.colIdx + S.nz0;
+    const double *va = a.values + S.nz0;
+
+    // init: x = 0, state[1] = (S b, 0, 0, 0); |S b|^2, |b|^2
+    {
+        FF f[1] = {ff_zero()};
+        double bb[1] = {0.0};
+        for (int i = threadIdx.x; i < n; i += B) {
+            const double bi = b[i];
+            const float r = static_cast<float>(bi * sc[i]);
+            x[i] = 0.0;
+            st[1][i] = make_float4(r, 0.0f, 0.0f, 0.0f);
+            ff_dot_add(f[0], r, r);
+            bb[0] += bi * bi;
+        }
+        ff_block_allsum<1>(f);
+        block_sum<1>(bb);  // thread 0
+        if (threadIdx.x == 0)
+            ms.start(ff_double(f[0]), bb[0], a.tol, a.maxit);
+        __syncthreads();
+    }
+    const int64_t trip_cap = 2 * static_cast<int64_t>(a.maxit > 0 ? a.maxit : 0) + 16;
+    for (int64_t trips = 0; !ms.done; ++trips) {
+        if (trips > trip_cap) {  // unreachable: every normal step counts and max_iter ends the solve
+            __syncthreads();
+            if (threadIdx.x == 0)
+                ms.stop(SIMALL_ERR_TIMEOUT);
+            __syncthreads();
+            break;
+        }
+        const int par = ms.par;
+        const float alpha = ms.fresh ? 0.0f : ms.alpha_f, beta = ms.beta_f;
+        const float4 *in = st[par];
+        float4 *outp = st[1 - par];
+        FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+        for (int i0 = threadIdx.x; i0 < n; i0 += RPP * B) {
+            float4 o[RPP];
+#pragma unroll
+            for (int u = 0; u < RPP; ++u) {
+                const int i = i0 + u * B;
+                o[u] = i < n ? in[i] : make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             }
 #pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * blockDim.x;
+            for (int u = 0; u < RPP; ++u) {
+                const int i = i0 + u * B;
                 if (i < n) {
-                    xh[i] = xv[u] + alpha * pv[u];
-                    const float r = rv[u] - alpha * qv[u];
-                    rh[i] = r;
-                    rr_t += r * r;
+                    const RowStep rs(o[u], alpha, beta);
+                    rs.finish(batch_row(S, a, in, i, rs.p, alpha, beta), outp + i, acc);
                 }
             }
         }
-        const double rr = cta_allreduce_f(rr_t, red);
-        ++it;
-        const double sigma = sqrt(rr);
-        const double est = t0 * sigma / sigma0;
-        double beta;
-        if (breakdown || sigma < delta * rmax || est < tol || it >= maxit) {
-            // reliable update: x += S xh (FP64), r = b - A x, rh = S r
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                x[i] += sc[i] * static_cast<double>(xh[i]);
-                xh[i] = 0.0f;
-            }
-            __syncthreads();
-            float rho_t = 0.0f;
-            double r2_t = 0.0;
-            for (int i = threadIdx.x; i < n; i += blockDim.x) {
-                double s = 0.0;
-                for (int k = rp[i]; k < rp[i + 1]; ++k)
-                    s = fma(va[k], x[ci[k]], s);
-                const double r = b[i] - s;
-                const float rf = static_cast<float>(sc[i] * r);
-                rh[i] = rf;
-                rho_t += rf * rf;
-                r2_t += r * r;
-            }
-            double rho_new, r2;
-            cta_allreduce2(rho_t, r2_t, red, rho_new, r2);
-            ++updates;
-            const double t = sqrt(r2) / bnorm;
-            last = t;
-            if (t < tol || it >= maxit || breakdown) {
-                if (breakdown && !(t < tol))
-                    status = SIMALL_ERR_BREAKDOWN;
-                done = true;
-                break;
-            }
-            beta = rho_new / rho;
-            rho = rho_new;
-            sigma0 = sqrt(rho_new);
-            t0 = t;
-            rmax = sigma0;
-        } else {
-            beta = rr / rho;
-            rho = rr;
-            rmax = sigma > rmax ? sigma : rmax;
-            last = est;
-        }
-        const float bf = static_cast<float>(beta);
-        for (int i0 = threadIdx.x; i0 < n; i0 += kRowsPerPass * blockDim.x) {
-            float rv[kRowsPerPass], pv[kRowsPerPass];
+        double t[4];
+        ff_block_allsum<4>(acc);
 #pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * blockDim.x;
-                rv[u] = i < n ? rh[i] : 0.0f;
-                pv[u] = i < n ? ph[i] : 0.0f;
-            }
-#pragma unroll
-            for (int u = 0; u < kRowsPerPass; ++u) {
-                const int i = i0 + u * blockDim.x;
-                if (i < n)
-                    ph[i] = rv[u] + bf * pv[u];
-            }
+        for (int k = 0; k < 4; ++k)
+            t[k] = ff_double(acc[k]);
+        if (threadIdx.x == 0)
+            ms.finish_step(t, a.tol, a.delta, a.maxit);
+        __syncthreads();
+        if (!ms.update)
+            continue;
+        // reliable update: x += S xh with the xh the triggering step wrote
+        const int upar = ms.par;
+        for (int i = threadIdx.x; i < n; i += B)
+            x[i] += sc[i] * static_cast<double>(st[1 - upar][i].w);
+        __syncthreads();
+        // r = b - A x (FP64, one FMA per entry); the FP32 replacement S r and
+        // xh = 0 into the state the FRESH step reads; |r|^2, |S r|^2
+        double r2[2] = {0.0, 0.0};
+        for (int i = threadIdx.x; i < n; i += B) {
+            double y = 0.0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                y = __fma_rn(va[k], x[ci[k]], y);
+            const double v = b[i] - y;
+            const float f = static_cast<float>(sc[i] * v);
+            float *e = reinterpret_cast<float *>(st[upar] + i);
+            e[0] = f;
+            e[3] = 0.0f;
+            r2[0] += v * v;
+            r2[1] += static_cast<double>(f) * static_cast<double>(f);
         }
+        block_sum<2>(r2);  // thread 0
+        if (threadIdx.x == 0)
+            ms.finish_update(r2, a.tol, a.maxit);
         __syncthreads();
     }
     if (threadIdx.x == 0) {
-        out->iterations = it;
-        out->updates = updates;
-        out->status = status;
-        out->converged = last < tol ? 1 : 0;
-        out->true_residual = last;
-        out->b_norm = bn;
+        out->iterations = ms.iter;
+        out->updates = ms.updates;
+        out->status = ms.status;
+        out->converged = ms.last < a.tol ? 1 : 0;
+        out->true_residual = ms.last;
+        out->b_norm = ms.b_norm;
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict__ sys, const int *__restrict__ order, int nsys, int *queue,
-                              const int32_t *__restrict__ rowPtr, const int32_t *__restrict__ colIdx,
-                              const double *__restrict__ values, const float *__restrict__ U,
-                              const int32_t *__restrict__ orow, const int32_t *__restrict__ ocol,
-                              const float *__restrict__ oval, const int8_t *__restrict__ Uc,
-                              const int8_t *__restrict__ oc,
-                              const double *__restrict__ scale, const double *__restrict__ b, double *x, float *xh,
-                              float *rh, float *ph, float *qh, double tol, double delta, int maxit, BatchOut *out)
+template <int RPP> __global__ void __launch_bounds__(1024) k_batch_solve(BatchArgs a)
 {
-    __shared__ double red[64];
     __shared__ int s_next;
     for (;;) {
         if (threadIdx.x == 0)
-            s_next = atomicAdd(queue, 1);
+            s_next = atomicAdd(a.queue, 1);
         __syncthreads();
         const int k = s_next;
         __syncthreads();
-        if (k >= nsys)
+        if (k >= a.nsys)
             return;
-        const int id = order[k];
-        const BatchSys S = sys[id];
-        batch_solve_one(S, rowPtr, colIdx, values, U, orow, ocol, oval, Uc, oc, scale, b, x, xh, rh, ph, qh, tol, delta,
-                        maxit, out + id, red);
+        const int id = a.order[k];
+        const BatchSys S = a.sys[id];
+        batch_solve_one<RPP>(S, a, a.out + id);
     }
 }
 
@@ -376,35 +285,73 @@ __global__ void __launch_bounds__(1024) k_batch_solve(const BatchSys *__restrict
 
 namespace {
 
-int launch_batch(simall_batch *B, int block, int ctas_per_sm, const double *b, double *x)
+int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const double *b, double *x)
 {
     simall_context *ctx = B->ctx;
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(B->queue.p, 0, sizeof(int), ctx->stream));
     const int grid = std::max(1, std::min(B->nsys, ctx->num_sms * ctas_per_sm));
-    k_batch_solve<<<grid, block, 0, ctx->stream>>>(B->sys.p, B->order.p, B->nsys, B->queue.p, B->rowPtr.p, B->colIdx.p,
-                                                   B->values.p, B->U.p, B->orow.p, B->ocol.p, B->oval.p, B->Uc.p, B->oc.p,
-                                                   B->scale.p, b,
-                                                   x, B->xh.p, B->rh.p, B->ph.p, B->qh.p, B->cfg.tolerance,
-                                                   B->cfg.reliable_delta, B->cfg.max_iterations, B->out.p);
+    BatchArgs a{};
+    a.sys = B->sys.p;
+    a.order = B->order.p;
+    a.nsys = B->nsys;
+    a.queue = B->queue.p;
+    a.rowPtr = B->rowPtr.p;
+    a.colIdx = B->colIdx.p;
+    a.values = B->values.p;
+    a.U = B->U.p;
+    a.orow = B->orow.p;
+    a.ocol = B->ocol.p;
+    a.oval = B->oval.p;
+    a.e = B->e.p;
+    a.scale = B->scale.p;
+    a.b = b;
+    a.x = x;
+    a.st[0] = B->st[0].p;
+    a.st[1] = B->st[1].p;
+    a.tol = B->cfg.tolerance;
+    a.delta = B->cfg.reliable_delta;
+    a.maxit = B->cfg.max_iterations;
+    a.out = B->out.p;
+    if (rpp >= 4)
+        k_batch_solve<4><<<grid, block, 0, ctx->stream>>>(a);
+    else if (rpp == 2)
+        k_batch_solve<2><<<grid, block, 0, ctx->stream>>>(a);
+    else
+        k_batch_solve<1><<<grid, block, 0, ctx->stream>>>(a);
     ctx->launches.fetch_add(1, std::memory_order_relaxed);
     B->kernel_launches += 1;
     SIMALL_CUDA_TRY(ctx, cudaGetLastError());
     return SIMALL_OK;
 }
 
-// Times each launch shape on the batch (device b -> scratch x) and keeps the
-// fastest.  Candidates: CTA sizes 256/512/1024 threads, 1-4 CTAs per SM.
+// Times each launch shape -- threads per CTA, CTAs per SM, rows a thread
+// keeps in flight -- on the batch itself (device b -> scratch x) and keeps
+// the fastest; the choice is stored in the autotuner cache under the batch's
+// key, so the next process with the same batch shape on the same device
+// skips the timing.
 int autotune(simall_batch *B, const double *b)
 {
     simall_context *ctx = B->ctx;
-    const int shapes[][2] = {{256, 4}, {256, 2}, {512, 2}, {512, 1}, {1024, 1}};
+    int cached[3] = {0, 0, 0};
+    if (!B->cache_path.empty() &&
+        simall_autotune_cache_lookup(B->cache_path.c_str(), B->shape_key.c_str(), cached) == SIMALL_OK &&
+        (cached[0] == 256 || cached[0] == 512 || cached[0] == 1024) && cached[1] >= 1 && cached[1] <= 8 &&
+        (cached[2] == 1 || cached[2] == 2 || cached[2] == 4) && cached[0] * cached[1] <= 2048) {
+        B->block = cached[0];
+        B->ctas_per_sm = cached[1];
+        B->rows_per_pass = cached[2];
+        B->tune_source = 2;
+        return SIMALL_OK;
+    }
+    const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1},
+                             {512, 2, 2},  {256, 4, 1},  {256, 4, 2},  {512, 1, 2}};
     cudaEvent_t e0, e1;
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e0));
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e1));
     float best = 1e30f;
     for (const auto &sh : shapes) {
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(e0, ctx->stream));
-        int st = launch_batch(B, sh[0], sh[1], b, B->x.p);
+        int st = launch_batch(B, sh[0], sh[1], sh[2], b, B->x.p);
         if (st)
             return st;
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(e1, ctx->stream));
@@ -415,11 +362,45 @@ int autotune(simall_batch *B, const double *b)
             best = ms;
             B->block = sh[0];
             B->ctas_per_sm = sh[1];
+            B->rows_per_pass = sh[2];
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    B->tune_source = 1;
+    if (!B->cache_path.empty()) {
+        const int v[3] = {B->block, B->ctas_per_sm, B->rows_per_pass};
+        simall_autotune_cache_store(B->cache_path.c_str(), B->shape_key.c_str(), v, best);  // best effort
+    }
     return SIMALL_OK;
+}
+
+// The batch's key in the autotuner cache: device, SM count, kernel revision,
+// and an FNV-1a hash of every system's rows, nonzeros and storage.
+std::string batch_shape_key(simall_batch *B)
+{
+    cudaDeviceProp prop{};
+    cudaGetDeviceProperties(&prop, B->ctx->device);
+    uint64_t h = 1469598103934665603ull;
+    auto mix = [&](uint64_t v) {
+        for (int k = 0; k < 8; ++k) {
+            h ^= (v >> (8 * k)) & 0xffu;
+            h *= 1099511628211ull;
+        }
+    };
+    for (const BatchSys &S : B->h_sys) {
+        mix(static_cast<uint64_t>(S.n));
+        mix(static_cast<uint64_t>(S.nd));
+    }
+    mix(static_cast<uint64_t>(B->nnz));
+    std::string name = prop.name;
+    for (char &c : name)
+        if (c == '"' || c == '\\' || static_cast<unsigned char>(c) < 32)
+            c = '_';
+    char buf[256];
+    snprintf(buf, sizeof buf, "batch-fused-v1|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
+             static_cast<long long>(B->rows), static_cast<unsigned long long>(h));
+    return buf;
 }
 
 }  // namespace
@@ -450,6 +431,7 @@ int simall_batch_create(simall_context *ctx, const simall_solver_config *cfg, si
         return SIMALL_ERR_OUT_OF_MEMORY;
     B->ctx = ctx;
     B->cfg = c;
+    B->cache_path = default_autotune_cache_path();
     *out = B;
     return SIMALL_OK;
 }
@@ -476,8 +458,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
         return fail(ctx, SIMALL_ERR_SIZE_MISMATCH, "batch offsets must start at 0 and grow");
     std::vector<BatchSys> sys(static_cast<size_t>(n_systems));
     std::vector<double> scale(static_cast<size_t>(rows));
-    std::vector<float> U;
-    std::vector<int8_t> Uc, oc;
+    std::vector<float> U, e(static_cast<size_t>(rows));
     std::vector<int32_t> orow, ocol;
     std::vector<float> oval;
     std::vector<int32_t> offs;
@@ -533,6 +514,14 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             dia = false;
         dia = dia && sym;
         const double *sc = scale.data() + r0;
+        // e_i = 1 + sum_{j != i} a_ij s_i s_j in FP64, rounded once (the row-sum form)
+        for (int64_t i = 0; i < n; ++i) {
+            double sum = 1.0;
+            for (int k = rp[i]; k < rp[i + 1]; ++k)
+                if (ci[k] != i)
+                    sum += va[k] * sc[i] * sc[ci[k]];
+            e[r0 + i] = static_cast<float>(sum);
+        }
         if (dia) {
             std::sort(offs.begin(), offs.end());
             S.nd = static_cast<int>(offs.size());
@@ -541,9 +530,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             S.u0 = static_cast<int64_t>(U.size());
             S.orp0 = 0;
             U.resize(U.size() + static_cast<size_t>(S.nd) * n, 0.0f);
-            Uc.resize(U.size(), 0);
             float *Us = U.data() + S.u0;
-            int8_t *Ucs = Uc.data() + S.u0;
             for (int64_t i = 0; i < n; ++i)
                 for (int k = rp[i]; k < rp[i + 1]; ++k) {
                     const int j = ci[k];
@@ -551,10 +538,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
                         continue;
                     const int d = static_cast<int>(std::find(offs.begin(), offs.end(), j - static_cast<int>(i)) -
                                                    offs.begin());
-                    const double a = va[k] * sc[i] * sc[j];
-                    const int64_t t = static_cast<int64_t>(d) * n + i;
-                    Us[t] = static_cast<float>(a);
-                    Ucs[t] = ff_correction(a, Us[t]);
+                    Us[static_cast<int64_t>(d) * n + i] = static_cast<float>(va[k] * sc[i] * sc[j]);
                 }
         } else {
             S.nd = 0;
@@ -566,10 +550,8 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
             for (int64_t i = 0; i < n; ++i) {
                 for (int k = rp[i]; k < rp[i + 1]; ++k)
                     if (ci[k] != i) {
-                        const double a = va[k] * sc[i] * sc[ci[k]];
                         ocol.push_back(ci[k]);
-                        oval.push_back(static_cast<float>(a));
-                        oc.push_back(ff_correction(a, oval.back()));
+                        oval.push_back(static_cast<float>(va[k] * sc[i] * sc[ci[k]]));
                         ++cnt;
                     }
                 orow.push_back(cnt);
@@ -592,13 +574,10 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, B->scale.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->b.alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->x.alloc(rows));
-    SIMALL_CUDA_TRY(ctx, B->xh.alloc(rows));
-    SIMALL_CUDA_TRY(ctx, B->rh.alloc(rows));
-    SIMALL_CUDA_TRY(ctx, B->ph.alloc(rows));
-    SIMALL_CUDA_TRY(ctx, B->qh.alloc(rows));
+    SIMALL_CUDA_TRY(ctx, B->e.alloc(rows));
+    SIMALL_CUDA_TRY(ctx, B->st[0].alloc(rows));
+    SIMALL_CUDA_TRY(ctx, B->st[1].alloc(rows));
     SIMALL_CUDA_TRY(ctx, B->U.alloc(std::max<size_t>(U.size(), 1)));
-    SIMALL_CUDA_TRY(ctx, B->Uc.alloc(std::max<size_t>(Uc.size(), 1)));
-    SIMALL_CUDA_TRY(ctx, B->oc.alloc(std::max<size_t>(oc.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->orow.alloc(std::max<size_t>(orow.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->ocol.alloc(std::max<size_t>(ocol.size(), 1)));
     SIMALL_CUDA_TRY(ctx, B->oval.alloc(std::max<size_t>(oval.size(), 1)));
@@ -609,16 +588,14 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     SIMALL_CUDA_TRY(ctx, up(B->colIdx.p, colIdx, nnz * sizeof(int32_t)));
     SIMALL_CUDA_TRY(ctx, up(B->values.p, values, nnz * sizeof(double)));
     SIMALL_CUDA_TRY(ctx, up(B->scale.p, scale.data(), scale.size() * sizeof(double)));
-    if (!U.empty()) {
+    SIMALL_CUDA_TRY(ctx, up(B->e.p, e.data(), e.size() * sizeof(float)));
+    if (!U.empty())
         SIMALL_CUDA_TRY(ctx, up(B->U.p, U.data(), U.size() * sizeof(float)));
-        SIMALL_CUDA_TRY(ctx, up(B->Uc.p, Uc.data(), Uc.size()));
-    }
     if (!orow.empty()) {
         SIMALL_CUDA_TRY(ctx, up(B->orow.p, orow.data(), orow.size() * sizeof(int32_t)));
         if (!ocol.empty()) {
             SIMALL_CUDA_TRY(ctx, up(B->ocol.p, ocol.data(), ocol.size() * sizeof(int32_t)));
             SIMALL_CUDA_TRY(ctx, up(B->oval.p, oval.data(), oval.size() * sizeof(float)));
-            SIMALL_CUDA_TRY(ctx, up(B->oc.p, oc.data(), oc.size()));
         }
     }
     SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(st));  // host staging vectors die here
@@ -628,7 +605,8 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     B->h_sys = std::move(sys);
     B->h_order = std::move(order);
     B->h_out.assign(static_cast<size_t>(n_systems), BatchOut{});
-    B->block = 0;  // re-tune for the new batch
+    B->block = 0;  // re-tune for the new batch (or read the cache)
+    B->shape_key = batch_shape_key(B);
     B->ready = true;
     return SIMALL_OK;
 }
@@ -660,14 +638,15 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
             return st;
     }
     double *dx = (mem == SIMALL_MEM_HOST) ? B->x.p : x;
-    if (!B->gexec || B->g_b != db || B->g_x != dx || B->g_block != B->block || B->g_ctas != B->ctas_per_sm) {
+    if (!B->gexec || B->g_b != db || B->g_x != dx || B->g_block != B->block || B->g_ctas != B->ctas_per_sm ||
+        B->g_rpp != B->rows_per_pass) {
         if (B->gexec) {
             cudaGraphExecDestroy(B->gexec);
             B->gexec = nullptr;
         }
         cudaGraph_t graph = nullptr;
         SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const int st = launch_batch(B, B->block, B->ctas_per_sm, db, dx);
+        const int st = launch_batch(B, B->block, B->ctas_per_sm, B->rows_per_pass, db, dx);
         const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
         if (st)
             return st;
@@ -681,6 +660,7 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         B->g_x = dx;
         B->g_block = B->block;
         B->g_ctas = B->ctas_per_sm;
+        B->g_rpp = B->rows_per_pass;
     } else {
         ctx->launches.fetch_add(1, std::memory_order_relaxed);
         B->kernel_launches += 1;
@@ -720,6 +700,8 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         total->status = worst_status;
         total->block_threads = B->block;
         total->ctas_per_sm = B->ctas_per_sm;
+        total->rows_per_pass = B->rows_per_pass;
+        total->autotune_source = B->tune_source;
         total->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return SIMALL_OK;
@@ -730,8 +712,20 @@ int simall_batch_launch_shape(simall_batch *B, int block_threads, int ctas_per_s
     if (!B || (block_threads != 0 && block_threads != 256 && block_threads != 512 && block_threads != 1024) ||
         ctas_per_sm < 0 || ctas_per_sm > 8)
         return SIMALL_ERR_INVALID_ARGUMENT;
+    if (block_threads && block_threads * ctas_per_sm > 2048)
+        return SIMALL_ERR_INVALID_ARGUMENT;
     B->block = block_threads;
     B->ctas_per_sm = block_threads ? ctas_per_sm : 0;
+    B->rows_per_pass = block_threads ? 2 : 0;
+    B->tune_source = 0;
+    return SIMALL_OK;
+}
+
+int simall_batch_autotune_cache(simall_batch *B, const char *path)
+{
+    if (!B)
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    B->cache_path = path ? path : "";
     return SIMALL_OK;
 }
 

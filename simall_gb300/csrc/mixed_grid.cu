@@ -29,6 +29,7 @@
 // (after the fold x += S xh, and after the true residual with the FP32
 // replacement r = S (b - A x) written in the same pass).
 #include "device.cuh"
+#include "mixed_state.cuh"
 #include "sell.cuh"
 #include "solver.hpp"
 
@@ -182,139 +183,6 @@ __device__ bool grid_allsum_f(const float (&v)[NV], double (&out)[NV], double *p
     return grid_allsum<NV>(out, part, ctr, epoch, err);
 }
 
-// The solver state and its transitions: mixed.cu's k_mx_init, mx_finish,
-// mx_step and k_mx_true_residual / k_mx_replace, on totals every CTA holds.
-struct GridState {
-    double bnorm, rz, sigma0, rmax, t0, last, rr_true, alpha, beta;
-    float alpha_f, beta_f;  // the step's FP32 coefficients
-    int iter, updates, need, done, result, status, par;
-    bool fresh;   // the next step forms p from a replaced residual
-    bool update;  // the step just finished asks for a reliable update
-
-    __device__ void start(double sbb, double bb, double tol, int max_iter)
-    {
-        const double bn = sqrt(bb);
-        bnorm = bn > 1e-30 ? bn : 1e-30;
-        rz = sbb;
-        sigma0 = sqrt(sbb);
-        rmax = sigma0;
-        t0 = bn / bnorm;
-        last = t0;
-        rr_true = bb;
-        alpha = beta = 0.0;
-        alpha_f = beta_f = 0.0f;
-        iter = updates = result = 0;
-        need = 2;  // the first (FRESH) step is not counted as an update
-        done = 0;
-        status = SIMALL_OK;
-        par = 1;   // the first step forms p = r (beta = 0) at parity 1
-        fresh = true;
-        update = false;
-        if (t0 < tol) {
-            done = 1;  // b == 0: x = 0 is exact
-        } else if (max_iter <= 0) {
-            done = 1;
-            result = max_iter;
-        }
-    }
-
-    __device__ void coefficients(const double (&t)[4])
-    {
-        const double pq = t[0], qq = t[1], rr = t[2], rq = t[3];
-        if (!(pq > 0.0) || !(rr > 0.0)) {  // not SPD in FP32, or exact breakdown
-            status = SIMALL_ERR_BREAKDOWN;
-            need = 1;
-            alpha = beta = 0.0;
-        } else {
-            alpha = rr / pq;
-            const double next = rr - 2.0 * alpha * rq + alpha * alpha * qq;
-            beta = (next > 0.0 ? next : 0.0) / rr;
-        }
-        alpha_f = static_cast<float>(alpha);
-        beta_f = static_cast<float>(beta);
-    }
-
-    __device__ void finish_step(const double (&t)[4], double tol, double delta, int max_iter)
-    {
-        const double rr = t[2];
-        if (fresh) {
-            rz = rr;
-            sigma0 = sqrt(rr);
-            rmax = sigma0;
-            if (need == 1)
-                ++updates;
-            need = 0;
-            coefficients(t);
-            fresh = false;
-            par ^= 1;
-            update = need == 1;
-            return;
-        }
-        ++iter;
-        const double sigma = sqrt(rr);
-        const double est = t0 * sigma / sigma0;
-        last = est;
-        if (need || sigma < delta * rmax || est < tol || iter >= max_iter) {
-            need = 1;  // fold, true residual, replacement, then a FRESH step at this parity
-            update = true;
-            return;
-        }
-        if (sigma > rmax)
-            rmax = sigma;
-        rz = rr;
-        coefficients(t);
-        par ^= 1;
-        update = need == 1;
-    }
-
-    // a = {|b - A x|^2, |S (b - A x)|^2 of the FP32 replacement}
-    __device__ void finish_update(const double (&a)[2], double tol, int max_iter)
-    {
-        rr_true = a[0];
-        const double tt = sqrt(a[0]) / bnorm;
-        last = tt;
-        t0 = tt;
-        update = false;
-        if (tt < tol) {
-            done = 1;
-            result = iter;
-        } else if (iter >= max_iter || status == SIMALL_ERR_BREAKDOWN) {
-            done = 1;
-            result = iter >= max_iter ? max_iter : iter;
-        } else {
-            beta = a[1] / rz;
-            beta_f = static_cast<float>(beta);
-            fresh = true;
-        }
-    }
-
-    __device__ void stop(int why)
-    {
-        status = why;
-        done = 1;
-        result = iter;
-    }
-
-    __device__ void publish(SolveScalars *s, bool ok) const
-    {
-        s->rz = rz;
-        s->alpha = alpha;
-        s->beta = beta;
-        s->rr = rr_true;
-        s->bnorm = bnorm;
-        s->last = last;
-        s->sigma0 = sigma0;
-        s->t0 = t0;
-        s->rmax = rmax;
-        s->iter = iter;
-        s->result = result;
-        s->done = done;
-        s->status = ok ? status : SIMALL_ERR_TIMEOUT;
-        s->need_update = 0;
-        s->updates = updates;
-    }
-};
-
 template <bool WIDE, bool STAGED>
 __global__ void __launch_bounds__(kSellThreads, 3) k_mx_grid_solve(GridArgs g)
 {
@@ -357,7 +225,7 @@ __global__ void __launch_bounds__(kSellThreads, 3) k_mx_grid_solve(GridArgs g)
     // The solver state: identical in every CTA (it follows from the identical
     // totals), kept in shared memory and advanced by thread 0 alone after each
     // grid sum; the other threads read the control values after a block barrier.
-    __shared__ GridState st;
+    __shared__ MixedState st;
     if (threadIdx.x == 0)
         st.start(tot[0], tot[1], g.tol, g.max_iter);
     __syncthreads();

@@ -183,6 +183,9 @@ int krylov_solve(simall_solver *s);
 void krylov_drop_graphs(simall_solver *s);
 void krylov_free(simall_solver *s);
 
+// The autotuner cache's default path (autotune_cache.cpp).
+std::string default_autotune_cache_path();
+
 // Host copy of the current pattern (ILU0 level analysis, CSR fallbacks).
 int solver_host_pattern(simall_solver *s);
 

@@ -7,6 +7,13 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
+# batched solves of the test session keep their autotuner cache in a private
+# temporary file, not in the user's cache directory
+if "SIMALL_AUTOTUNE_CACHE" not in os.environ:
+    import tempfile
+
+    os.environ["SIMALL_AUTOTUNE_CACHE"] = os.path.join(tempfile.mkdtemp(prefix="simall_tests_"), "autotune.json")
+
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (runs the sm_103a kernels)")

@@ -140,3 +140,36 @@ def test_benchmark_batch_against_the_reference(sg, ctx):
         assert abs(it - int(fx["iters"][k])) <= 1, (k, it, int(fx["iters"][k]))
         assert summary_err(k, xs) <= 1e-10, k
     s.close()
+
+
+def test_autotuner_cache_across_batch_objects(sg, ctx, tmp_path):
+    """The first batch object times the candidate launch shapes and stores the
+    winner in the cache file; a second object with the same systems reads it
+    instead of timing (autotune_source 2) and solves to the same bits."""
+    from simall_gb300 import workloads as W
+    from simall_gb300.batch import autotune_cache_lookup
+
+    systems, rhs, sides = W.batched_cavity_systems(count=12, lo=8, hi=48, seed=5, ctx=ctx)
+    b = np.concatenate(rhs)
+    cache = str(tmp_path / "autotune.json")
+    B1 = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    B1.autotune_cache(cache)
+    B1.set_systems(systems)
+    x1, _ = B1.solve(b)
+    assert B1.total.autotune_source == 1
+    shape = (B1.total.block_threads, B1.total.ctas_per_sm, B1.total.rows_per_pass)
+    doc = open(cache).read()
+    assert "batch-fused-v1|" in doc and f'"block_threads": {shape[0]}' in doc
+    B2 = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+    B2.autotune_cache(cache)
+    B2.set_systems(systems)
+    x2, _ = B2.solve(b)
+    assert B2.total.autotune_source == 2
+    assert (B2.total.block_threads, B2.total.ctas_per_sm, B2.total.rows_per_pass) == shape
+    assert np.array_equal(x1, x2)
+    # a fixed shape is not the autotuner's
+    B2.launch_shape(512, 2)
+    B2.solve(b)
+    assert B2.total.autotune_source == 0 and B2.total.block_threads == 512
+    B1.close()
+    B2.close()
