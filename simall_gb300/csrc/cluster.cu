@@ -704,12 +704,15 @@ template <int ND, int RPT> int try_mixed(simall_solver *s, const ClusterMixedArg
 
 template <int ND> int try_mixed_nd(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int *status)
 {
+    // every row of the slice needs a slot: RPT * kClThreads >= 2^logR (up to 8192 rows: 32)
     const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
-    return rpt <= 1   ? try_mixed<ND, 1>(s, a, C, logR, status)
-           : rpt <= 2 ? try_mixed<ND, 2>(s, a, C, logR, status)
-           : rpt <= 4 ? try_mixed<ND, 4>(s, a, C, logR, status)
-           : rpt <= 8 ? try_mixed<ND, 8>(s, a, C, logR, status)
-                      : try_mixed<ND, 16>(s, a, C, logR, status);
+    return rpt <= 1    ? try_mixed<ND, 1>(s, a, C, logR, status)
+           : rpt <= 2  ? try_mixed<ND, 2>(s, a, C, logR, status)
+           : rpt <= 4  ? try_mixed<ND, 4>(s, a, C, logR, status)
+           : rpt <= 8  ? try_mixed<ND, 8>(s, a, C, logR, status)
+           : rpt <= 16 ? try_mixed<ND, 16>(s, a, C, logR, status)
+           : rpt <= 32 ? try_mixed<ND, 32>(s, a, C, logR, status)
+                       : 0;
 }
 
 // Slice length (a power of two, at least 256 rows) and cluster size for n rows

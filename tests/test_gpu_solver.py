@@ -305,6 +305,19 @@ def test_cluster_engine_matches_kernels(sg, ctx, oracle, dims, prec):
         assert abs(res[0][0] - res[1][0]) <= 0.1 * res[1][0] + 2
 
 
+def test_cluster_engine_largest_slices(sg, ctx, oracle):
+    """A 300 x 300 natural-order system (90,000 rows, diagonal storage): the
+    one-cluster mixed solve cuts it into 8192-row slices, 32 rows per thread;
+    every row must be iterated (true residual recomputed on the host)."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=(300, 300, 1), renumber=False, amp=0.0,
+                                                pressure_zones=(1,))
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=20000), precision=sg.Precision.MIXED, ctx=ctx)
+    x = np.zeros(len(rhs))
+    s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+    assert s.stats.engine == 1 and s.stats.converged and tr < 1e-8
+
+
 @pytest.mark.parametrize("check_interval", [0, 4])
 def test_mixed_max_iterations(sg, ctx, oracle, check_interval):
     """max_iterations bounds the device loop: CGSolver's return value is
