@@ -602,6 +602,10 @@ typedef struct simall_batch_stats {
     double seconds;
     int rows_per_pass;        /* rows each thread keeps in flight */
     int autotune_source;      /* 0 set by simall_batch_launch_shape, 1 timed on this batch, 2 autotuner cache */
+    int cluster_rows;         /* systems of at least this many rows (diagonal storage) ran on one
+                                 thread-block cluster each; 0: none */
+    int cluster_ctas;         /* CTAs per such cluster */
+    int cluster_systems;      /* systems that ran on clusters */
 } simall_batch_stats;
 /* cfg: tolerance, max_iterations, reliable_delta as for simall_solver (Jacobi). */
 int simall_batch_create(simall_context *ctx, const simall_solver_config *cfg, simall_batch **out);
@@ -613,11 +617,19 @@ int simall_batch_set_systems(simall_batch *b, int n_systems, const int64_t *row_
 int simall_batch_solve(simall_batch *b, const double *rhs, double *x, int mem, simall_batch_system_stats *per_system,
                        simall_batch_stats *total);
 /* Fixes the launch shape (256/512/1024 threads per CTA, 1-8 CTAs per SM, at
- * most 2048 threads per SM; 2 rows in flight per thread); block_threads == 0
- * re-enables the autotuner, which at the next solve reads the autotuner cache
- * or times the candidate shapes (threads per CTA, CTAs per SM, rows in flight
- * per thread) on the batch and keeps the fastest. */
+ * most 2048 threads per SM; 2 rows in flight per thread; every system on the
+ * one-CTA queue); block_threads == 0 re-enables the autotuner, which at the
+ * next solve reads the autotuner cache or times candidates on the batch and
+ * keeps the fastest: first the one-CTA shape (threads per CTA, CTAs per SM,
+ * rows in flight per thread), then with it which systems run on a
+ * thread-block cluster each instead (a row threshold and the cluster size;
+ * systems in diagonal storage, concurrently with the one-CTA queue). */
 int simall_batch_launch_shape(simall_batch *b, int block_threads, int ctas_per_sm);
+/* Fixes which systems run on a thread-block cluster each: systems in diagonal
+ * storage of at least cluster_rows rows (and at most cluster_ctas x 8192) on
+ * clusters of cluster_ctas CTAs (1-16); cluster_rows == 0: none.  Keeps the
+ * one-CTA shape (1024 threads, 1 CTA per SM, 2 rows in flight unless set). */
+int simall_batch_cluster_route(simall_batch *b, int cluster_rows, int cluster_ctas);
 /* The autotuner cache file of this batch object (JSON; path NULL or "": no
  * cache).  The default is SIMALL_AUTOTUNE_CACHE when set ("off": none), else
  * $XDG_CACHE_HOME/simall_gb300/autotune.json, else
@@ -625,7 +637,7 @@ int simall_batch_launch_shape(simall_batch *b, int block_threads, int ctas_per_s
  * SM count, kernel revision and a hash of the batch's system sizes. */
 int simall_batch_autotune_cache(simall_batch *b, const char *path);
 /* The cache itself (host only): values = {block_threads, ctas_per_sm,
- * rows_per_pass}.  lookup returns SIMALL_OK when the key is present,
+ * rows_per_pass, cluster_rows, cluster_ctas}.  lookup returns SIMALL_OK when the key is present,
  * SIMALL_ERR_IO when it is not (or the file cannot be read); store replaces or
  * appends the key and rewrites the file through a rename. */
 int simall_autotune_cache_lookup(const char *path, const char *key, int *values);

@@ -51,14 +51,7 @@ struct BatchSys {
     int off[kBatchDiags];
 };
 
-struct BatchOut {
-    int iterations;
-    int updates;
-    int status;
-    int converged;
-    double true_residual;
-    double b_norm;
-};
+using BatchOut = ClBatchResult;
 
 }  // namespace simall
 
@@ -78,7 +71,16 @@ struct simall_batch {
     simall::DevBuf<simall::BatchOut> out;
     std::vector<simall::BatchOut> h_out;
     int block = 0, ctas_per_sm = 0, rows_per_pass = 0;  // autotuned launch shape
+    int cluster_rows = 0, cluster_ctas = 0;  // systems of at least cluster_rows rows: one cluster of cluster_ctas CTAs
     int tune_source = 0;             // 0 set by the caller, 1 timed on this batch, 2 read from the cache
+    // the current plan: the systems on clusters, per stored-diagonal count, and the rest
+    int plan_rows = -1, plan_ctas = -1;
+    int nsmall = 0, ncluster = 0;
+    std::vector<simall::ClBatchItem> h_items[5];
+    simall::DevBuf<simall::ClBatchItem> items[5];
+    int items_logR[5] = {0, 0, 0, 0, 0};
+    cudaStream_t side = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
     std::string cache_path;          // autotuner cache (JSON); empty: none
     std::string shape_key;           // the batch's key in that cache
     bool ready = false;
@@ -87,11 +89,17 @@ struct simall_batch {
     cudaGraphExec_t gexec = nullptr;
     const double *g_b = nullptr;
     double *g_x = nullptr;
-    int g_block = 0, g_ctas = 0, g_rpp = 0;
+    int g_block = 0, g_ctas = 0, g_rpp = 0, g_crows = -1, g_cctas = -1;
     ~simall_batch()
     {
         if (gexec)
             cudaGraphExecDestroy(gexec);
+        if (ev_fork)
+            cudaEventDestroy(ev_fork);
+        if (ev_join)
+            cudaEventDestroy(ev_join);
+        if (side)
+            cudaStreamDestroy(side);
     }
     int64_t kernel_launches = 0;
 };
@@ -285,15 +293,82 @@ template <int RPP> __global__ void __launch_bounds__(1024) k_batch_solve(BatchAr
 
 namespace {
 
+// Which systems go to clusters: diagonal storage, at least `rows` rows and at
+// most ctas x 8192, and an iteration limit the cluster engine accepts; the
+// others keep the one-CTA queue (largest first).  rows == 0: none.
+int plan_batch(simall_batch *B, int rows, int ctas)
+{
+    simall_context *ctx = B->ctx;
+    if (B->plan_rows == rows && B->plan_ctas == ctas)
+        return SIMALL_OK;
+    std::vector<int> small;
+    for (auto &v : B->h_items)
+        v.clear();
+    for (int id : B->h_order) {
+        const BatchSys &S = B->h_sys[id];
+        const bool big = rows > 0 && ctas > 0 && S.nd >= 1 && S.n >= rows &&
+                         static_cast<int64_t>(S.n) <= static_cast<int64_t>(ctas) * kClBatchMaxRowsPerCta &&
+                         B->cfg.max_iterations <= 200000;
+        if (!big) {
+            small.push_back(id);
+            continue;
+        }
+        ClBatchItem it{};
+        it.n = S.n;
+        it.row0 = S.row0;
+        it.A.U = B->U.p + S.u0;
+        it.A.ldU = S.n;
+        it.A.nd = S.nd;
+        for (int d = 0; d < 8; ++d)
+            it.A.off[d] = d < S.nd ? S.off[d] : 0;
+        it.A.e = B->e.p + S.row0;
+        it.A.scale = B->scale.p + S.row0;
+        it.rowPtr = B->rowPtr.p + S.rp0;
+        it.colIdx = B->colIdx.p + S.nz0;
+        it.val = B->values.p + S.nz0;
+        it.out = B->out.p + id;
+        B->h_items[S.nd].push_back(it);
+    }
+    B->ncluster = 0;
+    for (int nd = 1; nd <= 4; ++nd) {
+        auto &v = B->h_items[nd];
+        if (v.empty())
+            continue;
+        int lr = 8;  // the slice of the launch: the largest system on `ctas` CTAs
+        int nmax = 0;
+        for (const ClBatchItem &it : v)
+            nmax = std::max(nmax, it.n);
+        while ((static_cast<int64_t>(ctas) << lr) < nmax)
+            ++lr;
+        B->items_logR[nd] = lr;
+        for (ClBatchItem &it : v)
+            it.logR = lr;
+        SIMALL_CUDA_TRY(ctx, B->items[nd].alloc(v.size()));
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(B->items[nd].p, v.data(), v.size() * sizeof(ClBatchItem),
+                                             cudaMemcpyHostToDevice, ctx->stream));
+        B->ncluster += static_cast<int>(v.size());
+    }
+    B->nsmall = static_cast<int>(small.size());
+    if (!small.empty())
+        SIMALL_CUDA_TRY(ctx, cudaMemcpyAsync(B->order.p, small.data(), small.size() * sizeof(int),
+                                             cudaMemcpyHostToDevice, ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // the host lists are reused
+    B->plan_rows = rows;
+    B->plan_ctas = ctas;
+    return SIMALL_OK;
+}
+
 int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const double *b, double *x)
 {
     simall_context *ctx = B->ctx;
+    if (B->nsmall == 0)
+        return SIMALL_OK;
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(B->queue.p, 0, sizeof(int), ctx->stream));
-    const int grid = std::max(1, std::min(B->nsys, ctx->num_sms * ctas_per_sm));
+    const int grid = std::max(1, std::min(B->nsmall, ctx->num_sms * ctas_per_sm));
     BatchArgs a{};
     a.sys = B->sys.p;
     a.order = B->order.p;
-    a.nsys = B->nsys;
+    a.nsys = B->nsmall;
     a.queue = B->queue.p;
     a.rowPtr = B->rowPtr.p;
     a.colIdx = B->colIdx.p;
@@ -324,6 +399,44 @@ int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const dou
     return SIMALL_OK;
 }
 
+// The whole batch: the cluster systems on the side stream (launched first, so
+// their clusters take SMs before the one-CTA queue spreads over the GPU),
+// the rest on the context's stream, joined before returning.  Capturable.
+int launch_all(simall_batch *B, int block, int ctas_per_sm, int rpp, int crows, int cctas, const double *b,
+               double *x)
+{
+    simall_context *ctx = B->ctx;
+    int st = plan_batch(B, crows, cctas);
+    if (st)
+        return st;
+    if (B->ncluster > 0) {
+        if (!B->side) {
+            SIMALL_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&B->side, cudaStreamNonBlocking));
+            SIMALL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&B->ev_fork, cudaEventDisableTiming));
+            SIMALL_CUDA_TRY(ctx, cudaEventCreateWithFlags(&B->ev_join, cudaEventDisableTiming));
+        }
+        SIMALL_CUDA_TRY(ctx, cudaEventRecord(B->ev_fork, ctx->stream));
+        SIMALL_CUDA_TRY(ctx, cudaStreamWaitEvent(B->side, B->ev_fork, 0));
+        for (int nd = 1; nd <= 4; ++nd) {
+            const int cnt = static_cast<int>(B->h_items[nd].size());
+            if (cnt == 0)
+                continue;
+            st = cluster_mixed_batch(ctx, B->side, nd, cctas, B->items_logR[nd], B->items[nd].p, cnt, b, x,
+                                     B->cfg.tolerance, B->cfg.reliable_delta, B->cfg.max_iterations);
+            if (st)
+                return st;
+            B->kernel_launches += 1;
+        }
+        SIMALL_CUDA_TRY(ctx, cudaEventRecord(B->ev_join, B->side));
+    }
+    st = launch_batch(B, block, ctas_per_sm, rpp, b, x);
+    if (st)
+        return st;
+    if (B->ncluster > 0)
+        SIMALL_CUDA_TRY(ctx, cudaStreamWaitEvent(ctx->stream, B->ev_join, 0));
+    return SIMALL_OK;
+}
+
 // Times each launch shape -- threads per CTA, CTAs per SM, rows a thread
 // keeps in flight -- on the batch itself (device b -> scratch x) and keeps
 // the fastest; the choice is stored in the autotuner cache under the batch's
@@ -332,26 +445,31 @@ int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const dou
 int autotune(simall_batch *B, const double *b)
 {
     simall_context *ctx = B->ctx;
-    int cached[3] = {0, 0, 0};
+    int cached[5] = {0, 0, 0, 0, 0};
     if (!B->cache_path.empty() &&
         simall_autotune_cache_lookup(B->cache_path.c_str(), B->shape_key.c_str(), cached) == SIMALL_OK &&
         (cached[0] == 256 || cached[0] == 512 || cached[0] == 1024) && cached[1] >= 1 && cached[1] <= 8 &&
-        (cached[2] == 1 || cached[2] == 2 || cached[2] == 4) && cached[0] * cached[1] <= 2048) {
+        (cached[2] == 1 || cached[2] == 2 || cached[2] == 4) && cached[0] * cached[1] <= 2048 && cached[3] >= 0 &&
+        cached[4] >= 0 && cached[4] <= 16) {
         B->block = cached[0];
         B->ctas_per_sm = cached[1];
         B->rows_per_pass = cached[2];
+        B->cluster_rows = cached[3];
+        B->cluster_ctas = cached[4];
         B->tune_source = 2;
         return SIMALL_OK;
     }
-    const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1},
-                             {512, 2, 2},  {256, 4, 1},  {256, 4, 2},  {512, 1, 2}};
     cudaEvent_t e0, e1;
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e0));
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e1));
     float best = 1e30f;
-    for (const auto &sh : shapes) {
+    auto trial = [&](int blk, int cps, int rpp, int crows, int cctas) -> int {
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(e0, ctx->stream));
-        int st = launch_batch(B, sh[0], sh[1], sh[2], b, B->x.p);
+        int st = launch_all(B, blk, cps, rpp, crows, cctas, b, B->x.p);
+        if (st == SIMALL_ERR_UNSUPPORTED && crows > 0) {  // this cluster shape does not fit here
+            cudaGetLastError();
+            return SIMALL_OK;
+        }
         if (st)
             return st;
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(e1, ctx->stream));
@@ -360,16 +478,40 @@ int autotune(simall_batch *B, const double *b)
         cudaEventElapsedTime(&ms, e0, e1);
         if (ms < best) {
             best = ms;
-            B->block = sh[0];
-            B->ctas_per_sm = sh[1];
-            B->rows_per_pass = sh[2];
+            B->block = blk;
+            B->ctas_per_sm = cps;
+            B->rows_per_pass = rpp;
+            B->cluster_rows = crows;
+            B->cluster_ctas = cctas;
         }
+        return SIMALL_OK;
+    };
+    // 1: the one-CTA shape with every system on the queue
+    const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1},
+                             {512, 2, 2},  {256, 4, 1},  {256, 4, 2},  {512, 1, 2}};
+    for (const auto &sh : shapes) {
+        const int st = trial(sh[0], sh[1], sh[2], 0, 0);
+        if (st)
+            return st;
+    }
+    // 2: with that shape, the largest systems on clusters (threshold, cluster size)
+    const int blk = B->block, cps = B->ctas_per_sm, rpp = B->rows_per_pass;
+    int64_t nmax = 0;
+    for (const BatchSys &S : B->h_sys)
+        nmax = std::max<int64_t>(nmax, S.nd >= 1 ? S.n : 0);
+    const int routes[][2] = {{49152, 16}, {32768, 16}, {32768, 8}, {16384, 8}, {16384, 4}, {8192, 4}};
+    for (const auto &r : routes) {
+        if (nmax < r[0])
+            continue;
+        const int st = trial(blk, cps, rpp, r[0], r[1]);
+        if (st)
+            return st;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     B->tune_source = 1;
     if (!B->cache_path.empty()) {
-        const int v[3] = {B->block, B->ctas_per_sm, B->rows_per_pass};
+        const int v[5] = {B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas};
         simall_autotune_cache_store(B->cache_path.c_str(), B->shape_key.c_str(), v, best);  // best effort
     }
     return SIMALL_OK;
@@ -398,7 +540,7 @@ std::string batch_shape_key(simall_batch *B)
         if (c == '"' || c == '\\' || static_cast<unsigned char>(c) < 32)
             c = '_';
     char buf[256];
-    snprintf(buf, sizeof buf, "batch-fused-v1|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
+    snprintf(buf, sizeof buf, "batch-fused-v2|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
              static_cast<long long>(B->rows), static_cast<unsigned long long>(h));
     return buf;
 }
@@ -606,6 +748,9 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     B->h_order = std::move(order);
     B->h_out.assign(static_cast<size_t>(n_systems), BatchOut{});
     B->block = 0;  // re-tune for the new batch (or read the cache)
+    B->cluster_rows = 0;
+    B->cluster_ctas = 0;
+    B->plan_rows = B->plan_ctas = -1;
     B->shape_key = batch_shape_key(B);
     B->ready = true;
     return SIMALL_OK;
@@ -638,15 +783,20 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
             return st;
     }
     double *dx = (mem == SIMALL_MEM_HOST) ? B->x.p : x;
+    // the plan is made outside the capture (it uploads the item lists)
+    int pst = plan_batch(B, B->cluster_rows, B->cluster_ctas);
+    if (pst)
+        return pst;
     if (!B->gexec || B->g_b != db || B->g_x != dx || B->g_block != B->block || B->g_ctas != B->ctas_per_sm ||
-        B->g_rpp != B->rows_per_pass) {
+        B->g_rpp != B->rows_per_pass || B->g_crows != B->cluster_rows || B->g_cctas != B->cluster_ctas) {
         if (B->gexec) {
             cudaGraphExecDestroy(B->gexec);
             B->gexec = nullptr;
         }
         cudaGraph_t graph = nullptr;
         SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
-        const int st = launch_batch(B, B->block, B->ctas_per_sm, B->rows_per_pass, db, dx);
+        const int st =
+            launch_all(B, B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas, db, dx);
         const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
         if (st)
             return st;
@@ -661,6 +811,8 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         B->g_block = B->block;
         B->g_ctas = B->ctas_per_sm;
         B->g_rpp = B->rows_per_pass;
+        B->g_crows = B->cluster_rows;
+        B->g_cctas = B->cluster_ctas;
     } else {
         ctx->launches.fetch_add(1, std::memory_order_relaxed);
         B->kernel_launches += 1;
@@ -702,6 +854,9 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         total->ctas_per_sm = B->ctas_per_sm;
         total->rows_per_pass = B->rows_per_pass;
         total->autotune_source = B->tune_source;
+        total->cluster_rows = B->cluster_rows;
+        total->cluster_ctas = B->cluster_ctas;
+        total->cluster_systems = B->ncluster;
         total->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return SIMALL_OK;
@@ -717,6 +872,23 @@ int simall_batch_launch_shape(simall_batch *B, int block_threads, int ctas_per_s
     B->block = block_threads;
     B->ctas_per_sm = block_threads ? ctas_per_sm : 0;
     B->rows_per_pass = block_threads ? 2 : 0;
+    B->cluster_rows = 0;  // a fixed shape keeps every system on the one-CTA queue
+    B->cluster_ctas = 0;
+    B->tune_source = 0;
+    return SIMALL_OK;
+}
+
+int simall_batch_cluster_route(simall_batch *B, int cluster_rows, int cluster_ctas)
+{
+    if (!B || cluster_rows < 0 || (cluster_rows > 0 && (cluster_ctas < 1 || cluster_ctas > 16)))
+        return SIMALL_ERR_INVALID_ARGUMENT;
+    if (B->block == 0) {  // a fixed shape for the one-CTA queue as well
+        B->block = 1024;
+        B->ctas_per_sm = 1;
+        B->rows_per_pass = 2;
+    }
+    B->cluster_rows = cluster_rows;
+    B->cluster_ctas = cluster_rows > 0 ? cluster_ctas : 0;
     B->tune_source = 0;
     return SIMALL_OK;
 }

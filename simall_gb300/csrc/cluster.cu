@@ -345,7 +345,7 @@ namespace {
 // residual after a barrier).  The scalar state of the iteration is kept by one
 // thread per CTA and broadcast after every sum; all CTAs hold identical state.
 struct ClMixState {
-    double rz, sigma0, rmax, t0, last, alpha, beta, bnorm, rr64;
+    double rz, sigma0, rmax, t0, last, alpha, beta, bnorm, rr64, b_norm;
     int iter, updates, need, done, result, status;
 };
 
@@ -438,13 +438,17 @@ __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, i
     }
 }
 
+// The whole mixed solve of one system on the calling cluster; returns the
+// final state (identical in every CTA).
 template <int ND, int RPT>
-__global__ void __launch_bounds__(kClThreads, 1)
-    k_cl_mixed(int n, int logR, ClusterMixedArgs A, const int32_t *__restrict__ rowPtr,
-               const int32_t *__restrict__ colIdx, const double *__restrict__ val, const double *__restrict__ b,
-               double *__restrict__ x, SolveScalars *s)
+__device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_group &cl, int n, int logR,
+                                                           const ClusterMixedArgs &A,
+                                                           const int32_t *__restrict__ rowPtr,
+                                                           const int32_t *__restrict__ colIdx,
+                                                           const double *__restrict__ val,
+                                                           const double *__restrict__ b, double *__restrict__ x,
+                                                           double tol, double delta, int max_iter)
 {
-    const cg::cluster_group cl = cg::this_cluster();
     const int rank = static_cast<int>(cl.block_rank());
     cl.sync();  // every CTA of the cluster has started before any shared memory is written remotely
     extern __shared__ __align__(16) double cl_sm[];
@@ -460,8 +464,6 @@ __global__ void __launch_bounds__(kClThreads, 1)
     ClMixState *const stp = &st_sh;
     const int row0 = rank * R;
     const int nr = max(0, min(R, n - row0));
-    const double tol = s->tol, delta = s->delta;
-    const int max_iter = s->max_iter;
 
     // init: x = 0, r = S b (r[0]), p_old = 0 (p[1]), xh = 0
     float xh[RPT];
@@ -488,6 +490,7 @@ __global__ void __launch_bounds__(kClThreads, 1)
         double t[2];
         cl_allreduce<2>(v, t, sh, slot, cl, [stp, tol, max_iter](const double *tt, double *) {
             const double bn = sqrt(tt[1]);
+            stp->b_norm = bn;
             stp->bnorm = std_max(bn, 1e-30);
             stp->rz = tt[0];
             stp->sigma0 = sqrt(tt[0]);
@@ -605,7 +608,20 @@ __global__ void __launch_bounds__(kClThreads, 1)
         }
         par ^= 1;
     }
-    if (rank == 0 && threadIdx.x == 0) {
+    cl.sync();  // no CTA leaves while another may still read its shared memory
+    return st;
+}
+
+template <int ND, int RPT>
+__global__ void __launch_bounds__(kClThreads, 1)
+    k_cl_mixed(int n, int logR, ClusterMixedArgs A, const int32_t *__restrict__ rowPtr,
+               const int32_t *__restrict__ colIdx, const double *__restrict__ val, const double *__restrict__ b,
+               double *__restrict__ x, SolveScalars *s)
+{
+    const cg::cluster_group cl = cg::this_cluster();
+    const ClMixState &st =
+        cl_mixed_body<ND, RPT>(cl, n, logR, A, rowPtr, colIdx, val, b, x, s->tol, s->delta, s->max_iter);
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
         s->bnorm = st.bnorm;
         s->last = st.last;
         s->rr = st.rr64;
@@ -615,7 +631,28 @@ __global__ void __launch_bounds__(kClThreads, 1)
         s->updates = st.updates;
         s->done = 1;
     }
-    cl.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+// Many systems, one per cluster (cluster c solves items[c]); b, x and the
+// results are the batch's, at each item's row offset.
+template <int ND, int RPT>
+__global__ void __launch_bounds__(kClThreads, 1)
+    k_cl_mixed_batch(const ClBatchItem *__restrict__ items, const double *__restrict__ b, double *__restrict__ x,
+                     double tol, double delta, int max_iter)
+{
+    const cg::cluster_group cl = cg::this_cluster();
+    const ClBatchItem it = items[blockIdx.x / cl.num_blocks()];
+    const ClMixState &st = cl_mixed_body<ND, RPT>(cl, it.n, it.logR, it.A, it.rowPtr, it.colIdx, it.val,
+                                                  b + it.row0, x + it.row0, tol, delta, max_iter);
+    if (cl.block_rank() == 0 && threadIdx.x == 0) {
+        ClBatchResult &o = *it.out;
+        o.iterations = st.iter;
+        o.updates = st.updates;
+        o.status = st.status;
+        o.converged = st.last < tol ? 1 : 0;
+        o.true_residual = st.last;
+        o.b_norm = st.b_norm;
+    }
 }
 
 }  // namespace
@@ -750,6 +787,62 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
             return 1;
     }
     return 0;
+}
+
+// The large systems of a batch, one cluster of C CTAs each, rows in slices of
+// 2^logR (every item: n <= C 2^logR); all items store nd diagonals.
+namespace {
+template <int ND, int RPT>
+int launch_mixed_batch(simall_context *ctx, cudaStream_t stream, int C, int logR, const ClBatchItem *items, int count,
+                       const double *b, double *x, double tol, double delta, int max_iter)
+{
+    const size_t smem = 6 * sizeof(float) * (static_cast<size_t>(1) << logR);
+    const void *fn = reinterpret_cast<const void *>(k_cl_mixed_batch<ND, RPT>);
+    if (!cluster_fits(ctx, fn, C, smem))
+        return fail(ctx, SIMALL_ERR_UNSUPPORTED, "a cluster of %d CTAs with %zu bytes each does not fit", C, smem);
+    cudaLaunchConfig_t cfg{};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = C;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(static_cast<unsigned>(C) * static_cast<unsigned>(count));
+    cfg.blockDim = dim3(kClThreads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = stream;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    SIMALL_CUDA_TRY(ctx, cudaLaunchKernelEx(&cfg, k_cl_mixed_batch<ND, RPT>, items, b, x, tol, delta, max_iter));
+    SIMALL_LAUNCH_CHECK(ctx);
+    return SIMALL_OK;
+}
+
+template <int ND>
+int launch_mixed_batch_nd(simall_context *ctx, cudaStream_t stream, int C, int logR, const ClBatchItem *items,
+                          int count, const double *b, double *x, double tol, double delta, int max_iter)
+{
+    const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
+    return rpt <= 4    ? launch_mixed_batch<ND, 4>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
+           : rpt <= 8  ? launch_mixed_batch<ND, 8>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
+           : rpt <= 16 ? launch_mixed_batch<ND, 16>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
+                       : launch_mixed_batch<ND, 32>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+}
+}  // namespace
+
+int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, const ClBatchItem *items,
+                        int count, const double *b, double *x, double tol, double delta, int max_iter)
+{
+    if (count <= 0)
+        return SIMALL_OK;
+    if (nd < 1 || nd > 4 || C < 1 || C > kClMaxCtas || logR < 8 || (1 << logR) > kClMaxRowsPerCta ||
+        max_iter > kClMaxIterations)
+        return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "cluster batch: nd %d, C %d, logR %d", nd, C, logR);
+    switch (nd) {
+    case 1: return launch_mixed_batch_nd<1>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    case 2: return launch_mixed_batch_nd<2>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    case 3: return launch_mixed_batch_nd<3>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    default: return launch_mixed_batch_nd<4>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    }
 }
 
 // FP64 Jacobi PCG on one cluster.  Returns 0 (not taken: the system does not

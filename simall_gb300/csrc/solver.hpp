@@ -146,6 +146,30 @@ struct ClusterMixedArgs {
 };
 int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status);
 
+// Batched solves (batched.cu): the per-system result, and the large systems
+// of a batch solved one per thread-block cluster (cluster.cu).
+struct ClBatchResult {
+    int iterations;
+    int updates;
+    int status;
+    int converged;
+    double true_residual;
+    double b_norm;
+};
+struct ClBatchItem {
+    int n;      // rows
+    int logR;   // slice length 2^logR of this launch
+    int64_t row0;  // first row in the batch's b and x
+    ClusterMixedArgs A;  // the system's S A S (diagonal storage), e and scale
+    const int32_t *rowPtr;  // the system's FP64 CSR (local indices)
+    const int32_t *colIdx;
+    const double *val;
+    ClBatchResult *out;
+};
+constexpr int kClBatchMaxRowsPerCta = 8192;
+int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, const ClBatchItem *items,
+                        int count, const double *b, double *x, double tol, double delta, int max_iter);
+
 // The mixed solver's sliced operator (mixed.cu) and work vectors for the
 // whole-solve persistent cooperative kernel (mixed_grid.cu); 0 = not taken
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
