@@ -333,6 +333,8 @@ def run_batched(a, ctx, sg, rank=0, world=1, with_cpu=False):
             "max_rel_diff_vs_fp64": diff,
             "launch_shape": {"block_threads": int(tot.block_threads), "ctas_per_sm": int(tot.ctas_per_sm),
                              "rows_per_pass": int(tot.rows_per_pass),
+                             "cluster_rows": int(tot.cluster_rows), "cluster_ctas": int(tot.cluster_ctas),
+                             "clusters": int(tot.clusters), "systems_on_clusters": int(tot.cluster_systems),
                              "source": ["set", "timed", "autotuner cache"][int(tot.autotune_source)]},
             "setup_seconds": round(setup, 2), "ranks": world, "systems_on_rank0": len(systems)}
     # roofline of the fused step: per row and step the packed state is read

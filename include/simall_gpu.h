@@ -606,6 +606,7 @@ typedef struct simall_batch_stats {
                                  thread-block cluster each; 0: none */
     int cluster_ctas;         /* CTAs per such cluster */
     int cluster_systems;      /* systems that ran on clusters */
+    int clusters;             /* clusters resident at a time (cluster_ctas x clusters SMs held) */
 } simall_batch_stats;
 /* cfg: tolerance, max_iterations, reliable_delta as for simall_solver (Jacobi). */
 int simall_batch_create(simall_context *ctx, const simall_solver_config *cfg, simall_batch **out);
@@ -627,9 +628,11 @@ int simall_batch_solve(simall_batch *b, const double *rhs, double *x, int mem, s
 int simall_batch_launch_shape(simall_batch *b, int block_threads, int ctas_per_sm);
 /* Fixes which systems run on a thread-block cluster each: systems in diagonal
  * storage of at least cluster_rows rows (and at most cluster_ctas x 8192) on
- * clusters of cluster_ctas CTAs (1-16); cluster_rows == 0: none.  Keeps the
+ * `clusters` clusters of cluster_ctas CTAs (1-16) that take them largest
+ * first, on clusters x cluster_ctas SMs; the one-CTA queue runs the rest on
+ * the other SMs at the same time.  cluster_rows == 0: none.  Keeps the
  * one-CTA shape (1024 threads, 1 CTA per SM, 2 rows in flight unless set). */
-int simall_batch_cluster_route(simall_batch *b, int cluster_rows, int cluster_ctas);
+int simall_batch_cluster_route(simall_batch *b, int cluster_rows, int cluster_ctas, int clusters);
 /* The autotuner cache file of this batch object (JSON; path NULL or "": no
  * cache).  The default is SIMALL_AUTOTUNE_CACHE when set ("off": none), else
  * $XDG_CACHE_HOME/simall_gb300/autotune.json, else
@@ -637,7 +640,7 @@ int simall_batch_cluster_route(simall_batch *b, int cluster_rows, int cluster_ct
  * SM count, kernel revision and a hash of the batch's system sizes. */
 int simall_batch_autotune_cache(simall_batch *b, const char *path);
 /* The cache itself (host only): values = {block_threads, ctas_per_sm,
- * rows_per_pass, cluster_rows, cluster_ctas}.  lookup returns SIMALL_OK when the key is present,
+ * rows_per_pass, cluster_rows, cluster_ctas, clusters}.  lookup returns SIMALL_OK when the key is present,
  * SIMALL_ERR_IO when it is not (or the file cannot be read); store replaces or
  * appends the key and rewrites the file through a rename. */
 int simall_autotune_cache_lookup(const char *path, const char *key, int *values);

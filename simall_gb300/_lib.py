@@ -97,7 +97,7 @@ class BatchStats(C.Structure):
     _fields_ = [("systems", _I), ("converged", _I), ("max_iterations", _I), ("status", _I),
                 ("total_iterations", _I64), ("worst_true_residual", _D), ("block_threads", _I),
                 ("ctas_per_sm", _I), ("seconds", _D), ("rows_per_pass", _I), ("autotune_source", _I),
-                ("cluster_rows", _I), ("cluster_ctas", _I), ("cluster_systems", _I)]
+                ("cluster_rows", _I), ("cluster_ctas", _I), ("cluster_systems", _I), ("clusters", _I)]
 
 
 class Boundary(C.Structure):
@@ -183,7 +183,7 @@ SIGNATURES = {
     "simall_batch_solve": (_I, [_P, _P, _P, _I, _P, C.POINTER(BatchStats)]),
     "simall_batch_launch_shape": (_I, [_P, _I, _I]),
     "simall_batch_autotune_cache": (_I, [_P, C.c_char_p]),
-    "simall_batch_cluster_route": (_I, [_P, _I, _I]),
+    "simall_batch_cluster_route": (_I, [_P, _I, _I, _I]),
     "simall_autotune_cache_lookup": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_I)]),
     "simall_autotune_cache_store": (_I, [C.c_char_p, C.c_char_p, C.POINTER(_I), _D]),
     "simall_gpu_axpy": (_I, [_D, _P, _P, _SZ, _P]),

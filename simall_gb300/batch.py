@@ -59,9 +59,10 @@ class BatchedSolver:
     def launch_shape(self, block_threads: int, ctas_per_sm: int = 1):
         check(self.L.simall_batch_launch_shape(self.handle, int(block_threads), int(ctas_per_sm)))
 
-    def cluster_route(self, cluster_rows: int, cluster_ctas: int = 8):
-        """Systems (diagonal storage) of at least cluster_rows rows on one cluster each (0: none)."""
-        check(self.L.simall_batch_cluster_route(self.handle, int(cluster_rows), int(cluster_ctas)))
+    def cluster_route(self, cluster_rows: int, cluster_ctas: int = 8, clusters: int = 4):
+        """Systems (diagonal storage) of at least cluster_rows rows on one cluster each (0: none), on
+        `clusters` clusters of cluster_ctas CTAs."""
+        check(self.L.simall_batch_cluster_route(self.handle, int(cluster_rows), int(cluster_ctas), int(clusters)))
 
     def autotune_cache(self, path: str | None):
         """Autotuner cache file of this batch (None or "": none)."""
@@ -95,14 +96,14 @@ class BatchedSolver:
 
 
 def autotune_cache_lookup(path: str, key: str):
-    """(block_threads, ctas_per_sm, rows_per_pass, cluster_rows, cluster_ctas) stored under key, or None."""
+    """(block_threads, ctas_per_sm, rows_per_pass, cluster_rows, cluster_ctas, clusters) stored under key, or None."""
     L = _lib.load()
-    v = (C.c_int * 5)()
+    v = (C.c_int * 6)()
     st = L.simall_autotune_cache_lookup(path.encode(), key.encode(), v)
     return tuple(v) if st == 0 else None
 
 
 def autotune_cache_store(path: str, key: str, values, ms: float = 0.0) -> int:
     L = _lib.load()
-    v = (C.c_int * 5)(*[int(t) for t in values])
+    v = (C.c_int * 6)(*[int(t) for t in values])
     return int(L.simall_autotune_cache_store(path.encode(), key.encode(), v, float(ms)))

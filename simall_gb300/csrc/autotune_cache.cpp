@@ -4,7 +4,7 @@
 // Format (one entry per line, written whole by this file only):
 //   {
 //    "<key>": {"block_threads": 1024, "ctas_per_sm": 1, "rows_per_pass": 2, "cluster_rows": 32768,
-//              "cluster_ctas": 16, "ms": 61.234},
+//              "cluster_ctas": 16, "clusters": 2, "ms": 61.234},
 //    ...
 //   }
 // A store reads the file, replaces or appends its key and writes the result
@@ -28,7 +28,7 @@ namespace {
 
 struct Entry {
     std::string key;
-    int v[5];
+    int v[6];
     double ms;
 };
 
@@ -44,8 +44,8 @@ bool parse_line(const std::string &line, Entry &e)
     const char *rest = line.c_str() + q1 + 1;
     return std::sscanf(rest,
                        " : {\"block_threads\": %d, \"ctas_per_sm\": %d, \"rows_per_pass\": %d, \"cluster_rows\": %d, "
-                       "\"cluster_ctas\": %d, \"ms\": %lf}",
-                       &e.v[0], &e.v[1], &e.v[2], &e.v[3], &e.v[4], &e.ms) == 6;
+                       "\"cluster_ctas\": %d, \"clusters\": %d, \"ms\": %lf}",
+                       &e.v[0], &e.v[1], &e.v[2], &e.v[3], &e.v[4], &e.v[5], &e.ms) == 7;
 }
 
 std::vector<Entry> read_entries(const char *path)
@@ -146,8 +146,8 @@ int simall_autotune_cache_store(const char *path, const char *key, const int *va
             char buf[192];
             std::snprintf(buf, sizeof buf,
                           "{\"block_threads\": %d, \"ctas_per_sm\": %d, \"rows_per_pass\": %d, \"cluster_rows\": %d, "
-                          "\"cluster_ctas\": %d, \"ms\": %.3f}",
-                          es[i].v[0], es[i].v[1], es[i].v[2], es[i].v[3], es[i].v[4], es[i].ms);
+                          "\"cluster_ctas\": %d, \"clusters\": %d, \"ms\": %.3f}",
+                          es[i].v[0], es[i].v[1], es[i].v[2], es[i].v[3], es[i].v[4], es[i].v[5], es[i].ms);
             f << " \"" << es[i].key << "\": " << buf << (i + 1 < es.size() ? ",\n" : "\n");
         }
         f << "}\n";

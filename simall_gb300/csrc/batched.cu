@@ -72,6 +72,7 @@ struct simall_batch {
     std::vector<simall::BatchOut> h_out;
     int block = 0, ctas_per_sm = 0, rows_per_pass = 0;  // autotuned launch shape
     int cluster_rows = 0, cluster_ctas = 0;  // systems of at least cluster_rows rows: one cluster of cluster_ctas CTAs
+    int clusters = 0;                        // clusters resident at a time (they stride through those systems)
     int tune_source = 0;             // 0 set by the caller, 1 timed on this batch, 2 read from the cache
     // the current plan: the systems on clusters, per stored-diagonal count, and the rest
     int plan_rows = -1, plan_ctas = -1;
@@ -89,7 +90,7 @@ struct simall_batch {
     cudaGraphExec_t gexec = nullptr;
     const double *g_b = nullptr;
     double *g_x = nullptr;
-    int g_block = 0, g_ctas = 0, g_rpp = 0, g_crows = -1, g_cctas = -1;
+    int g_block = 0, g_ctas = 0, g_rpp = 0, g_crows = -1, g_cctas = -1, g_clusters = -1;
     ~simall_batch()
     {
         if (gexec)
@@ -358,13 +359,15 @@ int plan_batch(simall_batch *B, int rows, int ctas)
     return SIMALL_OK;
 }
 
-int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const double *b, double *x)
+int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, int reserved_sms, const double *b, double *x)
 {
     simall_context *ctx = B->ctx;
     if (B->nsmall == 0)
         return SIMALL_OK;
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(B->queue.p, 0, sizeof(int), ctx->stream));
-    const int grid = std::max(1, std::min(B->nsmall, ctx->num_sms * ctas_per_sm));
+    // the SMs the clusters hold are left to them
+    const int sms = std::max(1, ctx->num_sms - reserved_sms);
+    const int grid = std::max(1, std::min(B->nsmall, sms * ctas_per_sm));
     BatchArgs a{};
     a.sys = B->sys.p;
     a.order = B->order.p;
@@ -399,11 +402,13 @@ int launch_batch(simall_batch *B, int block, int ctas_per_sm, int rpp, const dou
     return SIMALL_OK;
 }
 
-// The whole batch: the cluster systems on the side stream (launched first, so
-// their clusters take SMs before the one-CTA queue spreads over the GPU),
-// the rest on the context's stream, joined before returning.  Capturable.
-int launch_all(simall_batch *B, int block, int ctas_per_sm, int rpp, int crows, int cctas, const double *b,
-               double *x)
+// The whole batch: the cluster systems on the side stream, `clusters`
+// clusters of cctas CTAs striding through them, the rest on the context's
+// stream on the other SMs (a one-CTA-queue CTA of 1024 threads fills an SM's
+// registers, so the two never share an SM), joined before returning.
+// Capturable.
+int launch_all(simall_batch *B, int block, int ctas_per_sm, int rpp, int crows, int cctas, int clusters,
+               const double *b, double *x)
 {
     simall_context *ctx = B->ctx;
     int st = plan_batch(B, crows, cctas);
@@ -421,15 +426,16 @@ int launch_all(simall_batch *B, int block, int ctas_per_sm, int rpp, int crows, 
             const int cnt = static_cast<int>(B->h_items[nd].size());
             if (cnt == 0)
                 continue;
-            st = cluster_mixed_batch(ctx, B->side, nd, cctas, B->items_logR[nd], B->items[nd].p, cnt, b, x,
-                                     B->cfg.tolerance, B->cfg.reliable_delta, B->cfg.max_iterations);
+            st = cluster_mixed_batch(ctx, B->side, nd, cctas, B->items_logR[nd], std::max(1, clusters),
+                                     B->items[nd].p, cnt, b, x, B->cfg.tolerance, B->cfg.reliable_delta,
+                                     B->cfg.max_iterations);
             if (st)
                 return st;
             B->kernel_launches += 1;
         }
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(B->ev_join, B->side));
     }
-    st = launch_batch(B, block, ctas_per_sm, rpp, b, x);
+    st = launch_batch(B, block, ctas_per_sm, rpp, B->ncluster > 0 ? std::max(1, clusters) * cctas : 0, b, x);
     if (st)
         return st;
     if (B->ncluster > 0)
@@ -445,17 +451,18 @@ int launch_all(simall_batch *B, int block, int ctas_per_sm, int rpp, int crows, 
 int autotune(simall_batch *B, const double *b)
 {
     simall_context *ctx = B->ctx;
-    int cached[5] = {0, 0, 0, 0, 0};
+    int cached[6] = {0, 0, 0, 0, 0, 0};
     if (!B->cache_path.empty() &&
         simall_autotune_cache_lookup(B->cache_path.c_str(), B->shape_key.c_str(), cached) == SIMALL_OK &&
         (cached[0] == 256 || cached[0] == 512 || cached[0] == 1024) && cached[1] >= 1 && cached[1] <= 8 &&
         (cached[2] == 1 || cached[2] == 2 || cached[2] == 4) && cached[0] * cached[1] <= 2048 && cached[3] >= 0 &&
-        cached[4] >= 0 && cached[4] <= 16) {
+        cached[4] >= 0 && cached[4] <= 16 && cached[5] >= 0) {
         B->block = cached[0];
         B->ctas_per_sm = cached[1];
         B->rows_per_pass = cached[2];
         B->cluster_rows = cached[3];
         B->cluster_ctas = cached[4];
+        B->clusters = cached[5];
         B->tune_source = 2;
         return SIMALL_OK;
     }
@@ -463,9 +470,9 @@ int autotune(simall_batch *B, const double *b)
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e0));
     SIMALL_CUDA_TRY(ctx, cudaEventCreate(&e1));
     float best = 1e30f;
-    auto trial = [&](int blk, int cps, int rpp, int crows, int cctas) -> int {
+    auto trial = [&](int blk, int cps, int rpp, int crows, int cctas, int ncl) -> int {
         SIMALL_CUDA_TRY(ctx, cudaEventRecord(e0, ctx->stream));
-        int st = launch_all(B, blk, cps, rpp, crows, cctas, b, B->x.p);
+        int st = launch_all(B, blk, cps, rpp, crows, cctas, ncl, b, B->x.p);
         if (st == SIMALL_ERR_UNSUPPORTED && crows > 0) {  // this cluster shape does not fit here
             cudaGetLastError();
             return SIMALL_OK;
@@ -483,6 +490,7 @@ int autotune(simall_batch *B, const double *b)
             B->rows_per_pass = rpp;
             B->cluster_rows = crows;
             B->cluster_ctas = cctas;
+            B->clusters = ncl;
         }
         return SIMALL_OK;
     };
@@ -490,20 +498,23 @@ int autotune(simall_batch *B, const double *b)
     const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1},
                              {512, 2, 2},  {256, 4, 1},  {256, 4, 2},  {512, 1, 2}};
     for (const auto &sh : shapes) {
-        const int st = trial(sh[0], sh[1], sh[2], 0, 0);
+        const int st = trial(sh[0], sh[1], sh[2], 0, 0, 0);
         if (st)
             return st;
     }
-    // 2: with that shape, the largest systems on clusters (threshold, cluster size)
+    // 2: with that shape, the largest systems on clusters (row threshold,
+    // cluster size, SMs the clusters hold -- the rest run the one-CTA queue)
     const int blk = B->block, cps = B->ctas_per_sm, rpp = B->rows_per_pass;
     int64_t nmax = 0;
     for (const BatchSys &S : B->h_sys)
         nmax = std::max<int64_t>(nmax, S.nd >= 1 ? S.n : 0);
-    const int routes[][2] = {{49152, 16}, {32768, 16}, {32768, 8}, {16384, 8}, {16384, 4}, {8192, 4}};
+    const int nsm = ctx->num_sms;
+    const int routes[][3] = {{49152, 16, nsm / 5}, {32768, 16, nsm / 5}, {32768, 16, nsm / 3}, {32768, 8, nsm / 5},
+                             {32768, 8, nsm / 3},  {16384, 8, nsm / 3}, {16384, 8, nsm / 2}, {16384, 4, nsm / 3}};
     for (const auto &r : routes) {
         if (nmax < r[0])
             continue;
-        const int st = trial(blk, cps, rpp, r[0], r[1]);
+        const int st = trial(blk, cps, rpp, r[0], r[1], std::max(1, r[2] / r[1]));
         if (st)
             return st;
     }
@@ -511,7 +522,7 @@ int autotune(simall_batch *B, const double *b)
     cudaEventDestroy(e1);
     B->tune_source = 1;
     if (!B->cache_path.empty()) {
-        const int v[5] = {B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas};
+        const int v[6] = {B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas, B->clusters};
         simall_autotune_cache_store(B->cache_path.c_str(), B->shape_key.c_str(), v, best);  // best effort
     }
     return SIMALL_OK;
@@ -540,7 +551,7 @@ std::string batch_shape_key(simall_batch *B)
         if (c == '"' || c == '\\' || static_cast<unsigned char>(c) < 32)
             c = '_';
     char buf[256];
-    snprintf(buf, sizeof buf, "batch-fused-v2|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
+    snprintf(buf, sizeof buf, "batch-fused-v3|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
              static_cast<long long>(B->rows), static_cast<unsigned long long>(h));
     return buf;
 }
@@ -750,6 +761,7 @@ int simall_batch_set_systems(simall_batch *B, int n_systems, const int64_t *row_
     B->block = 0;  // re-tune for the new batch (or read the cache)
     B->cluster_rows = 0;
     B->cluster_ctas = 0;
+    B->clusters = 0;
     B->plan_rows = B->plan_ctas = -1;
     B->shape_key = batch_shape_key(B);
     B->ready = true;
@@ -788,7 +800,8 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
     if (pst)
         return pst;
     if (!B->gexec || B->g_b != db || B->g_x != dx || B->g_block != B->block || B->g_ctas != B->ctas_per_sm ||
-        B->g_rpp != B->rows_per_pass || B->g_crows != B->cluster_rows || B->g_cctas != B->cluster_ctas) {
+        B->g_rpp != B->rows_per_pass || B->g_crows != B->cluster_rows || B->g_cctas != B->cluster_ctas ||
+        B->g_clusters != B->clusters) {
         if (B->gexec) {
             cudaGraphExecDestroy(B->gexec);
             B->gexec = nullptr;
@@ -796,7 +809,8 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         cudaGraph_t graph = nullptr;
         SIMALL_CUDA_TRY(ctx, cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeThreadLocal));
         const int st =
-            launch_all(B, B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas, db, dx);
+            launch_all(B, B->block, B->ctas_per_sm, B->rows_per_pass, B->cluster_rows, B->cluster_ctas, B->clusters, db,
+                       dx);
         const cudaError_t e = cudaStreamEndCapture(ctx->stream, &graph);
         if (st)
             return st;
@@ -813,6 +827,7 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         B->g_rpp = B->rows_per_pass;
         B->g_crows = B->cluster_rows;
         B->g_cctas = B->cluster_ctas;
+        B->g_clusters = B->clusters;
     } else {
         ctx->launches.fetch_add(1, std::memory_order_relaxed);
         B->kernel_launches += 1;
@@ -857,6 +872,7 @@ int simall_batch_solve(simall_batch *B, const double *b, double *x, int mem, sim
         total->cluster_rows = B->cluster_rows;
         total->cluster_ctas = B->cluster_ctas;
         total->cluster_systems = B->ncluster;
+        total->clusters = B->clusters;
         total->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     }
     return SIMALL_OK;
@@ -874,13 +890,14 @@ int simall_batch_launch_shape(simall_batch *B, int block_threads, int ctas_per_s
     B->rows_per_pass = block_threads ? 2 : 0;
     B->cluster_rows = 0;  // a fixed shape keeps every system on the one-CTA queue
     B->cluster_ctas = 0;
+    B->clusters = 0;
     B->tune_source = 0;
     return SIMALL_OK;
 }
 
-int simall_batch_cluster_route(simall_batch *B, int cluster_rows, int cluster_ctas)
+int simall_batch_cluster_route(simall_batch *B, int cluster_rows, int cluster_ctas, int clusters)
 {
-    if (!B || cluster_rows < 0 || (cluster_rows > 0 && (cluster_ctas < 1 || cluster_ctas > 16)))
+    if (!B || cluster_rows < 0 || (cluster_rows > 0 && (cluster_ctas < 1 || cluster_ctas > 16 || clusters < 1)))
         return SIMALL_ERR_INVALID_ARGUMENT;
     if (B->block == 0) {  // a fixed shape for the one-CTA queue as well
         B->block = 1024;
@@ -889,6 +906,7 @@ int simall_batch_cluster_route(simall_batch *B, int cluster_rows, int cluster_ct
     }
     B->cluster_rows = cluster_rows;
     B->cluster_ctas = cluster_rows > 0 ? cluster_ctas : 0;
+    B->clusters = cluster_rows > 0 ? clusters : 0;
     B->tune_source = 0;
     return SIMALL_OK;
 }

@@ -633,25 +633,31 @@ __global__ void __launch_bounds__(kClThreads, 1)
     }
 }
 
-// Many systems, one per cluster (cluster c solves items[c]); b, x and the
-// results are the batch's, at each item's row offset.
+// Many systems on a fixed set of clusters: cluster c solves items c, c + K,
+// c + 2K, ... (K clusters in the grid; the items are ordered largest first),
+// so the batch decides how many SMs the clusters hold.  b, x and the results
+// are the batch's, at each item's row offset.
 template <int ND, int RPT>
 __global__ void __launch_bounds__(kClThreads, 1)
-    k_cl_mixed_batch(const ClBatchItem *__restrict__ items, const double *__restrict__ b, double *__restrict__ x,
-                     double tol, double delta, int max_iter)
+    k_cl_mixed_batch(const ClBatchItem *__restrict__ items, int count, const double *__restrict__ b,
+                     double *__restrict__ x, double tol, double delta, int max_iter)
 {
     const cg::cluster_group cl = cg::this_cluster();
-    const ClBatchItem it = items[blockIdx.x / cl.num_blocks()];
-    const ClMixState &st = cl_mixed_body<ND, RPT>(cl, it.n, it.logR, it.A, it.rowPtr, it.colIdx, it.val,
-                                                  b + it.row0, x + it.row0, tol, delta, max_iter);
-    if (cl.block_rank() == 0 && threadIdx.x == 0) {
-        ClBatchResult &o = *it.out;
-        o.iterations = st.iter;
-        o.updates = st.updates;
-        o.status = st.status;
-        o.converged = st.last < tol ? 1 : 0;
-        o.true_residual = st.last;
-        o.b_norm = st.b_norm;
+    const int K = static_cast<int>(gridDim.x / cl.num_blocks());
+    for (int c = static_cast<int>(blockIdx.x / cl.num_blocks()); c < count; c += K) {
+        const ClBatchItem it = items[c];
+        const ClMixState &st = cl_mixed_body<ND, RPT>(cl, it.n, it.logR, it.A, it.rowPtr, it.colIdx, it.val,
+                                                      b + it.row0, x + it.row0, tol, delta, max_iter);
+        if (cl.block_rank() == 0 && threadIdx.x == 0) {
+            ClBatchResult &o = *it.out;
+            o.iterations = st.iter;
+            o.updates = st.updates;
+            o.status = st.status;
+            o.converged = st.last < tol ? 1 : 0;
+            o.true_residual = st.last;
+            o.b_norm = st.b_norm;
+        }
+        cl.sync();  // the state of this item is read before the next item's init overwrites it
     }
 }
 
@@ -793,8 +799,8 @@ int cluster_mixed_solve(simall_solver *s, const ClusterMixedArgs &a, int *status
 // 2^logR (every item: n <= C 2^logR); all items store nd diagonals.
 namespace {
 template <int ND, int RPT>
-int launch_mixed_batch(simall_context *ctx, cudaStream_t stream, int C, int logR, const ClBatchItem *items, int count,
-                       const double *b, double *x, double tol, double delta, int max_iter)
+int launch_mixed_batch(simall_context *ctx, cudaStream_t stream, int C, int logR, int clusters, const ClBatchItem *items,
+                       int count, const double *b, double *x, double tol, double delta, int max_iter)
 {
     const size_t smem = 6 * sizeof(float) * (static_cast<size_t>(1) << logR);
     const void *fn = reinterpret_cast<const void *>(k_cl_mixed_batch<ND, RPT>);
@@ -806,42 +812,50 @@ int launch_mixed_batch(simall_context *ctx, cudaStream_t stream, int C, int logR
     attr[0].val.clusterDim.x = C;
     attr[0].val.clusterDim.y = 1;
     attr[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(static_cast<unsigned>(C) * static_cast<unsigned>(count));
+    cfg.gridDim = dim3(static_cast<unsigned>(C) * static_cast<unsigned>(std::min(count, clusters)));
     cfg.blockDim = dim3(kClThreads);
     cfg.dynamicSmemBytes = smem;
     cfg.stream = stream;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    SIMALL_CUDA_TRY(ctx, cudaLaunchKernelEx(&cfg, k_cl_mixed_batch<ND, RPT>, items, b, x, tol, delta, max_iter));
+    SIMALL_CUDA_TRY(ctx,
+                    cudaLaunchKernelEx(&cfg, k_cl_mixed_batch<ND, RPT>, items, count, b, x, tol, delta, max_iter));
     SIMALL_LAUNCH_CHECK(ctx);
     return SIMALL_OK;
 }
 
 template <int ND>
-int launch_mixed_batch_nd(simall_context *ctx, cudaStream_t stream, int C, int logR, const ClBatchItem *items,
-                          int count, const double *b, double *x, double tol, double delta, int max_iter)
+int launch_mixed_batch_nd(simall_context *ctx, cudaStream_t stream, int C, int logR, int clusters,
+                          const ClBatchItem *items, int count, const double *b, double *x, double tol, double delta,
+                          int max_iter)
 {
     const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
-    return rpt <= 4    ? launch_mixed_batch<ND, 4>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
-           : rpt <= 8  ? launch_mixed_batch<ND, 8>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
-           : rpt <= 16 ? launch_mixed_batch<ND, 16>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter)
-                       : launch_mixed_batch<ND, 32>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    return rpt <= 4    ? launch_mixed_batch<ND, 4>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
+                                                 max_iter)
+           : rpt <= 8  ? launch_mixed_batch<ND, 8>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
+                                                 max_iter)
+           : rpt <= 16 ? launch_mixed_batch<ND, 16>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
+                                                  max_iter)
+                       : launch_mixed_batch<ND, 32>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
+                                                  max_iter);
 }
 }  // namespace
 
-int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, const ClBatchItem *items,
-                        int count, const double *b, double *x, double tol, double delta, int max_iter)
+int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, int clusters,
+                        const ClBatchItem *items, int count, const double *b, double *x, double tol, double delta,
+                        int max_iter)
 {
     if (count <= 0)
         return SIMALL_OK;
     if (nd < 1 || nd > 4 || C < 1 || C > kClMaxCtas || logR < 8 || (1 << logR) > kClMaxRowsPerCta ||
-        max_iter > kClMaxIterations)
+        max_iter > kClMaxIterations || clusters < 1)
         return fail(ctx, SIMALL_ERR_INVALID_ARGUMENT, "cluster batch: nd %d, C %d, logR %d", nd, C, logR);
     switch (nd) {
-    case 1: return launch_mixed_batch_nd<1>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
-    case 2: return launch_mixed_batch_nd<2>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
-    case 3: return launch_mixed_batch_nd<3>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
-    default: return launch_mixed_batch_nd<4>(ctx, stream, C, logR, items, count, b, x, tol, delta, max_iter);
+    case 1: return launch_mixed_batch_nd<1>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta, max_iter);
+    case 2: return launch_mixed_batch_nd<2>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta, max_iter);
+    case 3: return launch_mixed_batch_nd<3>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta, max_iter);
+    default: return launch_mixed_batch_nd<4>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
+                                             max_iter);
     }
 }
 

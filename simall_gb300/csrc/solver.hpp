@@ -167,8 +167,10 @@ struct ClBatchItem {
     ClBatchResult *out;
 };
 constexpr int kClBatchMaxRowsPerCta = 8192;
-int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, const ClBatchItem *items,
-                        int count, const double *b, double *x, double tol, double delta, int max_iter);
+// `clusters` clusters of C CTAs stride through the `count` items (largest first).
+int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C, int logR, int clusters,
+                        const ClBatchItem *items, int count, const double *b, double *x, double tol, double delta,
+                        int max_iter);
 
 // The mixed solver's sliced operator (mixed.cu) and work vectors for the
 // whole-solve persistent cooperative kernel (mixed_grid.cu); 0 = not taken

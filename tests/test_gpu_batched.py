@@ -158,16 +158,16 @@ def test_autotuner_cache_across_batch_objects(sg, ctx, tmp_path):
     x1, _ = B1.solve(b)
     assert B1.total.autotune_source == 1
     shape = (B1.total.block_threads, B1.total.ctas_per_sm, B1.total.rows_per_pass, B1.total.cluster_rows,
-             B1.total.cluster_ctas)
+             B1.total.cluster_ctas, B1.total.clusters)
     doc = open(cache).read()
-    assert "batch-fused-v2|" in doc and f'"block_threads": {shape[0]}' in doc
+    assert "batch-fused-v3|" in doc and f'"block_threads": {shape[0]}' in doc
     B2 = sg.BatchedSolver(_cfg(sg), ctx=ctx)
     B2.autotune_cache(cache)
     B2.set_systems(systems)
     x2, _ = B2.solve(b)
     assert B2.total.autotune_source == 2
     assert (B2.total.block_threads, B2.total.ctas_per_sm, B2.total.rows_per_pass, B2.total.cluster_rows,
-            B2.total.cluster_ctas) == shape
+            B2.total.cluster_ctas, B2.total.clusters) == shape
     assert np.array_equal(x1, x2)
     # a fixed shape is not the autotuner's
     B2.launch_shape(512, 2)
@@ -177,8 +177,8 @@ def test_autotuner_cache_across_batch_objects(sg, ctx, tmp_path):
     B2.close()
 
 
-@pytest.mark.parametrize("ctas", [4, 8, 16])
-def test_cluster_route(sg, ctx, oracle, ctas):
+@pytest.mark.parametrize("ctas,clusters", [(4, 1), (8, 2), (16, 3)])
+def test_cluster_route(sg, ctx, oracle, ctas, clusters):
     """The largest systems of a batch on one thread-block cluster each, the
     rest on the one-CTA queue, concurrently: every system reaches the
     tolerance and matches the oracle's solution; the same batch without
@@ -194,10 +194,10 @@ def test_cluster_route(sg, ctx, oracle, ctas):
         rhs.append(r - r.mean())
     B = sg.BatchedSolver(_cfg(sg, tol=1e-9), ctx=ctx)
     rows = B.set_systems(systems)
-    B.cluster_route(4096, ctas)
+    B.cluster_route(4096, ctas, clusters)
     x, stats = B.solve(np.concatenate(rhs))
     assert B.total.cluster_systems == sum(1 for sd in sides if sd * sd >= 4096 and sd * sd <= ctas * 8192)
-    assert B.total.cluster_rows == 4096 and B.total.cluster_ctas == ctas
+    assert B.total.cluster_rows == 4096 and B.total.cluster_ctas == ctas and B.total.clusters == clusters
     parts = [x[rows[i]:rows[i + 1]] for i in range(len(systems))]
     _check(oracle, systems, rhs, parts, stats, 1e-9)
     B.close()
