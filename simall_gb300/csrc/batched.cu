@@ -15,13 +15,22 @@
 // Storage per system: S A S as symmetric diagonal storage when the system is
 // numerically symmetric with at most kBatchDiags upper diagonals (every
 // structured grid in natural order), otherwise FP32 CSR of its off-diagonal
-// part; FP32 work vectors xh, rh, ph, qh; FP64 scale, b and x.  The entries
-// of S A S carry 8-bit corrections and every row of the SpMV is summed in
-// float-float arithmetic (ffop.cuh): on the pinned cavity systems of a batch
-// that keeps the inner iteration count at the FP64 one, where FP32 entries
-// and sums cost 15-30% more iterations.  The CTA size
-// (threads) and CTAs per SM are picked by a small autotuner that times each
-// candidate on the batch itself the first time a batch shape is solved.
+// part; the row sums e_i = 1 + sum_j (S A S)_ij (FP64 sum, one rounding) of
+// the row-sum product; the iteration state packed per row as one float4
+// (r, q, p, xh), double-buffered; FP64 scale, b and x.  Each step is the fused
+// single-pass step of the sliced engines (sell.cuh) with float-float sums and
+// one block reduction.
+//
+// Systems of at least cluster_rows rows in diagonal storage run instead on
+// one thread-block cluster each (cluster.cu, k_cl_mixed_batch: vectors in the
+// cluster's shared memory), a fixed number of clusters striding through them
+// on reserved SMs while the one-CTA queue runs the rest on the other SMs; a
+// single SM streams a 65,025-row system at ~47 GB/s, 0.12 s for its ~2000
+// steps, a 16-CTA cluster solves it in ~15 ms.  The one-CTA shape (threads,
+// CTAs per SM, rows in flight per thread) and the cluster route (row
+// threshold, cluster size, clusters) are picked by an autotuner that times
+// candidates on the batch itself and keeps its choice in a JSON cache
+// (autotune_cache.cpp) keyed by device and batch shape.
 #include "device.cuh"
 #include "ffsum.cuh"
 #include "mixed_state.cuh"

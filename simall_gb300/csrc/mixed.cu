@@ -20,10 +20,11 @@
 // offset: 4 B per stored diagonal per row and no column indices.  Otherwise
 // the off-diagonal entries are kept in sliced storage (sell.cuh: slices of 32
 // rows, entry-major, 16-bit column offsets where the bandwidth allows, FP32
-// values with 8-bit corrections, 7 B per entry) and the product is the
-// compensated plain form of ffop.cuh.  With the default engine the sliced
-// form runs the whole solve in one persistent cooperative launch
-// (mixed_grid.cu); per-step kernels otherwise.
+// values, 6 B per entry) with the iteration state packed per row (r, q, p,
+// xh); its steps stage the streamed operands through shared memory by bulk
+// copies.  With the default engine the sliced form runs the whole solve in
+// one persistent cooperative launch (mixed_grid.cu); per-step kernels
+// otherwise.
 //
 // Row-sum form of the product (diagonal storage).  With N the off-diagonal part of S A S and
 // e_i = 1 + sum_j N_ij (summed in FP64 from A, stored rounded to FP32), the
