@@ -618,7 +618,8 @@ __global__ void __launch_bounds__(kSellThreads) k_mx_iter_sell_staged(SellOp A, 
     const float beta = static_cast<float>(__ldcg(&s->beta));
     const int64_t c0 = blockIdx.x * A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * A.nslices / gridDim.x;
     FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
-    if (!sell_step_staged<WIDE, true>(A, c0, c1, in, out, alpha, beta, acc, R, false) && threadIdx.x == 0) {
+    const bool ok = __syncthreads_and(sell_step_staged<WIDE, true>(A, c0, c1, in, out, alpha, beta, acc, R, false));
+    if (!ok && threadIdx.x == 0) {
         atomicExch(&s->status, SIMALL_ERR_TIMEOUT);
         atomicExch(&s->done, 1);
     }

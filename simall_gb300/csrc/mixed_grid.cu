@@ -93,28 +93,36 @@ __device__ bool grid_barrier(unsigned long long *ctr, unsigned long long epoch, 
                     break;
                 }
         }
-        __threadfence();
+        // the acquire loads order what follows; the block barrier below passes
+        // that on to the other threads
         ok = good;
     }
     __syncthreads();
     return ok != 0;
 }
 
-// Sum of NV FP64 values over the grid, the same bits in every CTA: block
-// tree, one slot per CTA, barrier, then every CTA sums all slots in index
-// order and reduces them in the same tree.  Returns false on a barrier
+// Every grid sum uses slots of kSlot values per CTA in two halves by epoch
+// parity, whatever its number of values: a CTA may still read the half of
+// the previous sum while a faster one writes the other half, so the halves
+// must not overlap for sums of different sizes.
+constexpr int kSlot = 4;
+
+// Sum of NV <= kSlot FP64 values over the grid, the same bits in every CTA:
+// block tree, one slot per CTA, barrier, then every CTA sums all slots in
+// index order and reduces them in the same tree.  Returns false on a barrier
 // timeout.
 template <int NV>
 __device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *ctr, unsigned long long &epoch,
                             int *err)
 {
+    static_assert(NV <= kSlot, "a grid sum holds at most kSlot values per CTA");
     __shared__ double tot[NV];
     block_sum<NV>(v);
-    double *slot = part + (epoch & 1ull) * gridDim.x * NV;
+    double *slot = part + (epoch & 1ull) * gridDim.x * kSlot;
     if (threadIdx.x == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k)
-            slot[static_cast<int64_t>(blockIdx.x) * NV + k] = v[k];
+            slot[static_cast<int64_t>(blockIdx.x) * kSlot + k] = v[k];
     }
     ++epoch;
     if (!grid_barrier(ctr, epoch, err))
@@ -126,7 +134,7 @@ __device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *c
     for (unsigned c = threadIdx.x; c < gridDim.x; c += blockDim.x) {
 #pragma unroll
         for (int k = 0; k < NV; ++k)
-            acc[k] += __ldcg(slot + static_cast<int64_t>(c) * NV + k);
+            acc[k] += __ldcg(slot + static_cast<int64_t>(c) * kSlot + k);
     }
     block_sum<NV>(acc);
     if (threadIdx.x == 0) {
@@ -142,29 +150,78 @@ __device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *c
     return true;
 }
 
-// The step's four sums: float-float from the thread up (ffsum.cuh), one
-// float-float slot per CTA, FP64 totals in every thread.  Returns false on a
-// barrier timeout.
-template <int NV>
-__device__ bool ff_grid_allsum(FF (&v)[NV], double *part, unsigned long long *ctr, unsigned long long &epoch, int *err,
-                               double (&total)[NV])
+// The end of a step with as few block barriers as it can have: each warp
+// sums its threads' float-float values; one block barrier (which also joins
+// the threads' verdicts); warp 0 alone sums the warps, publishes the CTA's
+// slot, arrives at the grid barrier and polls it (lane 0; the other lanes
+// wait at a shuffle), sums every CTA's slot in index order and finishes the
+// step on its lane 0; a second block barrier hands the state to the CTA.
+// Returns false (in every thread) on a timeout or a verdict that failed.
+template <class Finish>
+__device__ bool step_allsum(bool ok_thread, FF (&acc)[4], double *part, unsigned long long *ctr,
+                            unsigned long long &epoch, int *err, Finish fin)
 {
-    ff_block_allsum<NV>(v);
-    FF *slot = reinterpret_cast<FF *>(part) + (epoch & 1ull) * gridDim.x * NV;
-    if (threadIdx.x == 0) {
+    __shared__ FF ws[4][32];
+    __shared__ int s_ok;
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
 #pragma unroll
-        for (int k = 0; k < NV; ++k)
-            slot[static_cast<int64_t>(blockIdx.x) * NV + k] = v[k];
+    for (int k = 0; k < 4; ++k) {
+        const FF w = ff_warp_allsum(acc[k]);
+        if (lane == 0)
+            ws[k][wid] = w;
     }
-    ++epoch;
-    if (!grid_barrier(ctr, epoch, err))
+    if (!__syncthreads_and(ok_thread)) {
+        if (threadIdx.x == 0)
+            atomicExch(err, 1);
         return false;
-    FF out[NV];
-    ff_sum_slots<NV>(slot, gridDim.x, out);
+    }
+    FF *slot = reinterpret_cast<FF *>(part) + (epoch & 1ull) * gridDim.x * kSlot;
+    ++epoch;
+    if (wid == 0) {
+        FF c[4];
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
-        total[k] = ff_double(out[k]);
-    return true;
+        for (int k = 0; k < 4; ++k)
+            c[k] = ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero());
+        int good = 1;
+        if (lane == 0) {
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                slot[static_cast<int64_t>(blockIdx.x) * kSlot + k] = c[k];
+            __threadfence();
+            atomicAdd(ctr, 1ull);
+            const unsigned long long target = epoch * gridDim.x;
+            if (ld_acquire(ctr) < target) {
+                const unsigned long long t0 = global_ns();
+                for (unsigned spins = 1; ld_acquire(ctr) < target; ++spins)
+                    if ((spins & 63u) == 0 && global_ns() - t0 > kGridWaitNs) {
+                        good = 0;
+                        atomicExch(err, 1);
+                        break;
+                    }
+            }
+        }
+        good = __shfl_sync(0xffffffffu, good, 0);
+        if (good) {
+            FF t[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+            for (unsigned cta = lane; cta < gridDim.x; cta += 32) {
+#pragma unroll
+                for (int k = 0; k < 4; ++k) {
+                    const float2 v = __ldcg(reinterpret_cast<const float2 *>(slot) + cta * kSlot + k);
+                    t[k] = ff_add(t[k], FF{v.x, v.y});
+                }
+            }
+            double tot[4];
+#pragma unroll
+            for (int k = 0; k < 4; ++k)
+                tot[k] = ff_double(ff_warp_allsum(t[k]));
+            if (lane == 0)
+                fin(tot);
+        }
+        if (lane == 0)
+            s_ok = good;
+    }
+    __syncthreads();
+    return s_ok != 0;
 }
 
 // FP32 per-thread partials: lanes summed in FP32, everything above in FP64.
@@ -240,23 +297,16 @@ __global__ void __launch_bounds__(kSellThreads, 3) k_mx_grid_solve(GridArgs g)
         const int par = st.par;
         const float alpha = st.fresh ? 0.0f : st.alpha_f, beta = st.beta_f;
         FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+        bool step_ok = true;
         if (STAGED) {
-            if (!sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true)) {
-                if (threadIdx.x == 0)
-                    atomicExch(g.err, 1);
-                ok = false;
-                break;
-            }
+            step_ok = sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true);
         } else {
             for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
                 sell_slice<WIDE, false>(g.A, sl, g.st[par], g.st[1 - par], alpha, beta, acc);
         }
-        double t[4];
-        if (!(ok = ff_grid_allsum<4>(acc, g.part, g.ctr, epoch, g.err, t)))
+        if (!(ok = step_allsum(step_ok, acc, g.part, g.ctr, epoch, g.err,
+                               [&](const double (&t)[4]) { st.finish_step(t, g.tol, g.delta, g.max_iter); })))
             break;
-        if (threadIdx.x == 0)
-            st.finish_step(t, g.tol, g.delta, g.max_iter);
-        __syncthreads();
         if (!st.update)
             continue;
         // ---- reliable update: x += S xh with the xh the triggering step wrote

@@ -47,20 +47,25 @@ struct MixedState {
         }
     }
 
+    // alpha and beta are used in FP32, so they are divided in FP32: GB300's
+    // FP64 divide and square root are long chains on a narrow pipe, and this
+    // runs on the critical path of every step.  |r - alpha q|^2, which
+    // cancels, is formed in FP64 with the FP32 alpha the step will use.
     __device__ void coefficients(const double (&t)[4])
     {
         const double pq = t[0], qq = t[1], rr = t[2], rq = t[3];
         if (!(pq > 0.0) || !(rr > 0.0)) {  // not SPD in FP32, or exact breakdown
             status = SIMALL_ERR_BREAKDOWN;
             need = 1;
-            alpha = beta = 0.0;
+            alpha_f = beta_f = 0.0f;
         } else {
-            alpha = rr / pq;
-            const double next = rr - 2.0 * alpha * rq + alpha * alpha * qq;
-            beta = (next > 0.0 ? next : 0.0) / rr;
+            alpha_f = __fdiv_rn(static_cast<float>(rr), static_cast<float>(pq));
+            const double a = alpha_f;
+            const double next = rr - 2.0 * a * rq + a * a * qq;
+            beta_f = __fdiv_rn(static_cast<float>(next > 0.0 ? next : 0.0), static_cast<float>(rr));
         }
-        alpha_f = static_cast<float>(alpha);
-        beta_f = static_cast<float>(beta);
+        alpha = alpha_f;
+        beta = beta_f;
     }
 
     __device__ void finish_step(const double (&t)[4], double tol, double delta, int max_iter)
@@ -68,7 +73,7 @@ struct MixedState {
         const double rr = t[2];
         if (fresh) {
             rz = rr;
-            sigma0 = sqrt(rr);
+            sigma0 = sqrtf(static_cast<float>(rr));
             rmax = sigma0;
             if (need == 1)
                 ++updates;
@@ -80,10 +85,12 @@ struct MixedState {
             return;
         }
         ++iter;
-        const double sigma = sqrt(rr);
-        const double est = t0 * sigma / sigma0;
+        // the trigger and the estimate in FP32 (the same reason as above)
+        const float sigma = sqrtf(static_cast<float>(rr));
+        const float est = static_cast<float>(t0) * __fdiv_rn(sigma, static_cast<float>(sigma0));
         last = est;
-        if (need || sigma < delta * rmax || est < tol || iter >= max_iter) {
+        if (need || sigma < static_cast<float>(delta) * static_cast<float>(rmax) || est < static_cast<float>(tol) ||
+            iter >= max_iter) {
             need = 1;  // fold, true residual, replacement, then a FRESH step at this parity
             update = true;
             return;

@@ -253,10 +253,11 @@ __device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, in
 
 // One step over the CTA's slices [c0, c1), staged; every thread of the CTA
 // calls it.  in_written_here: `in` was written earlier in the same launch (the
-// persistent kernel), so the copies follow a proxy fence.  Returns false --
-// the same in every thread -- when a wait ran out (a copy that did not land,
-// a slot that was not released); the copies still in flight are then waited
-// for (bounded) before returning.
+// persistent kernel), so the copies follow a proxy fence.  Returns this
+// thread's verdict, false when one of its waits ran out (a copy that did not
+// land, a slot that was not released; the producer then waits, bounded, for
+// the copies still in flight); no block barrier at the end: the caller folds
+// the verdicts into the barrier of its reduction (__syncthreads_and).
 template <bool WIDE, bool NC>
 __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const float4 *in, float4 *out, float alpha,
                                  float beta, FF (&acc)[4], SellRing<WIDE> &R, bool in_written_here)
@@ -317,7 +318,7 @@ __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const 
         }
     }
     R.q += static_cast<uint32_t>(nst);
-    return __syncthreads_and(ok) != 0;
+    return ok;
 }
 
 }  // namespace simall
