@@ -346,7 +346,8 @@ namespace {
 // thread per CTA and broadcast after every sum; all CTAs hold identical state.
 struct ClMixState {
     double rz, sigma0, rmax, t0, last, alpha, beta, bnorm, rr64, b_norm;
-    int iter, updates, need, done, result, status;
+    float smin;  // smallest iterated residual norm since the last update
+    int iter, updates, need, done, result, status, stall;
 };
 
 template <bool FRESH>
@@ -495,6 +496,8 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
             stp->rz = tt[0];
             stp->sigma0 = sqrt(tt[0]);
             stp->rmax = stp->sigma0;
+            stp->smin = static_cast<float>(stp->sigma0);
+            stp->stall = 0;
             stp->t0 = bn / stp->bnorm;
             stp->last = stp->t0;
             stp->rr64 = tt[1];
@@ -518,6 +521,8 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
         stp->rz = t[2];
         stp->sigma0 = sqrt(t[2]);
         stp->rmax = stp->sigma0;
+        stp->smin = static_cast<float>(stp->sigma0);
+        stp->stall = 0;
         if (stp->need == 1)
             stp->updates += 1;
         stp->need = 0;
@@ -544,8 +549,14 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
             const float sigma = sqrtf(static_cast<float>(tt[2]));
             const float est = static_cast<float>(stp->t0) * __fdiv_rn(sigma, static_cast<float>(stp->sigma0));
             stp->last = est;
+            if (sigma < stp->smin) {
+                stp->smin = sigma;
+                stp->stall = 0;
+            } else {
+                stp->stall += 1;
+            }
             if (stp->need || sigma < static_cast<float>(delta) * static_cast<float>(stp->rmax) ||
-                est < static_cast<float>(tol) || stp->iter >= max_iter) {
+                est < static_cast<float>(tol) || stp->iter >= max_iter || stp->stall >= kMixedStallSteps) {
                 stp->need = 1;
                 return;
             }

@@ -32,6 +32,12 @@ constexpr int kSpmvRows = 256;     // max rows of one SpMV row-block
 constexpr int kSpmvNnzCap = 2048;  // max nonzeros staged per row-block (16 KB of FP64 per staged array)
 static_assert(kSpmvNnzCap % kBlock == 0, "row-block staging assumes whole slots per thread");
 constexpr int kMaxReduce = 4;      // values reduced together by one kernel
+// Mixed precision: a reliable update is also due when the iterated residual
+// has not reached a new minimum for this many steps.  An FP32 inner CG on a
+// hard system (a 160^3 distorted Neumann box: 8405 FP64 iterations) can
+// stagnate above the reliable_delta drop that would trigger the update; the
+// replacement restarts its residual from the FP64 one and progress resumes.
+constexpr int kMixedStallSteps = 64;
 
 int fail(simall_context *ctx, int status, const char *fmt, ...);
 int cuda_fail(simall_context *ctx, cudaError_t e, const char *what, const char *file, int line);
@@ -114,6 +120,10 @@ struct SolveScalars {
     double drop_tol;    // cggpu: ||r_0|| * drop_factor
     double rnorm0;      // cggpu: ||b - A x0||
     double rnorm;       // ||r|| at the last stop test (cggpu: finalResidual)
+    // mixed: the smallest iterated residual norm since the last reliable
+    // update, and the steps since it was last lowered (stagnation trigger)
+    double smin;
+    int stall;
 };
 
 // CSR row-blocks for the staged SpMV: each block holds <= kSpmvRows rows and

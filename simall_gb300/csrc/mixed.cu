@@ -217,6 +217,8 @@ __device__ void mx_start(SolveScalars *s, double sbb, double bb)
     s->rz = sbb;
     s->sigma0 = sqrt(sbb);
     s->rmax = s->sigma0;
+    s->smin = s->sigma0;
+    s->stall = 0;
     s->t0 = bn / s->bnorm;
     s->last = s->t0;
     s->rr = bb;
@@ -342,6 +344,8 @@ __device__ __forceinline__ void mx_finish(SolveScalars *s, const double (&t)[4])
         s->rz = rr;
         s->sigma0 = sqrt(rr);
         s->rmax = s->sigma0;
+        s->smin = s->sigma0;
+        s->stall = 0;
         if (s->need_update == 1)
             s->updates += 1;
         s->need_update = 0;
@@ -352,7 +356,14 @@ __device__ __forceinline__ void mx_finish(SolveScalars *s, const double (&t)[4])
     const double sigma = sqrt(rr);
     const double est = s->t0 * sigma / s->sigma0;
     s->last = est;
-    if (s->need_update || sigma < s->delta * s->rmax || est < s->tol || s->iter >= s->max_iter) {
+    if (sigma < s->smin) {
+        s->smin = sigma;
+        s->stall = 0;
+    } else {
+        s->stall += 1;
+    }
+    if (s->need_update || sigma < s->delta * s->rmax || est < s->tol || s->iter >= s->max_iter ||
+        s->stall >= kMixedStallSteps) {
         s->need_update = 1;  // fold, true residual, replacement, then a FRESH step
         return;
     }

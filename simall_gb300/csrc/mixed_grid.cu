@@ -150,13 +150,15 @@ __device__ bool grid_allsum(double (&v)[NV], double *part, unsigned long long *c
     return true;
 }
 
-// The end of a step with as few block barriers as it can have: each warp
-// sums its threads' float-float values; one block barrier (which also joins
-// the threads' verdicts); warp 0 alone sums the warps, publishes the CTA's
-// slot, arrives at the grid barrier and polls it (lane 0; the other lanes
-// wait at a shuffle), sums every CTA's slot in index order and finishes the
-// step on its lane 0; a second block barrier hands the state to the CTA.
-// Returns false (in every thread) on a timeout or a verdict that failed.
+// The end of a step with four block barriers: each warp sums its threads'
+// float-float values; a block barrier (which also joins the threads'
+// verdicts); warp 0 sums the warps, publishes the CTA's slot, arrives at the
+// grid barrier and polls it (lane 0; the other lanes wait at a shuffle); a
+// block barrier; every thread then sums its share of the CTA slots (at most a
+// few, all loads in flight at once), the warps and warp 0 combine them in a
+// fixed order, and lane 0 finishes the step; a last block barrier hands the
+// state to the CTA.  Returns false (in every thread) on a timeout or a failed
+// verdict.
 template <class Finish>
 __device__ bool step_allsum(bool ok_thread, FF (&acc)[4], double *part, unsigned long long *ctr,
                             unsigned long long &epoch, int *err, Finish fin)
@@ -182,8 +184,8 @@ __device__ bool step_allsum(bool ok_thread, FF (&acc)[4], double *part, unsigned
 #pragma unroll
         for (int k = 0; k < 4; ++k)
             c[k] = ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero());
-        int good = 1;
         if (lane == 0) {
+            int good = 1;
 #pragma unroll
             for (int k = 0; k < 4; ++k)
                 slot[static_cast<int64_t>(blockIdx.x) * kSlot + k] = c[k];
@@ -199,29 +201,37 @@ __device__ bool step_allsum(bool ok_thread, FF (&acc)[4], double *part, unsigned
                         break;
                     }
             }
-        }
-        good = __shfl_sync(0xffffffffu, good, 0);
-        if (good) {
-            FF t[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
-            for (unsigned cta = lane; cta < gridDim.x; cta += 32) {
-#pragma unroll
-                for (int k = 0; k < 4; ++k) {
-                    const float2 v = __ldcg(reinterpret_cast<const float2 *>(slot) + cta * kSlot + k);
-                    t[k] = ff_add(t[k], FF{v.x, v.y});
-                }
-            }
-            double tot[4];
-#pragma unroll
-            for (int k = 0; k < 4; ++k)
-                tot[k] = ff_double(ff_warp_allsum(t[k]));
-            if (lane == 0)
-                fin(tot);
-        }
-        if (lane == 0)
             s_ok = good;
+        }
     }
     __syncthreads();
-    return s_ok != 0;
+    if (!s_ok)
+        return false;
+    FF t[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
+    for (unsigned cta = threadIdx.x; cta < gridDim.x; cta += blockDim.x) {
+#pragma unroll
+        for (int k = 0; k < 4; ++k) {
+            const float2 v = __ldcg(reinterpret_cast<const float2 *>(slot) + cta * kSlot + k);
+            t[k] = ff_add(t[k], FF{v.x, v.y});
+        }
+    }
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+        const FF w = ff_warp_allsum(t[k]);
+        if (lane == 0)
+            ws[k][wid] = w;
+    }
+    __syncthreads();
+    if (wid == 0) {
+        double tot[4];
+#pragma unroll
+        for (int k = 0; k < 4; ++k)
+            tot[k] = ff_double(ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero()));
+        if (lane == 0)
+            fin(tot);
+    }
+    __syncthreads();
+    return true;
 }
 
 // FP32 per-thread partials: lanes summed in FP32, everything above in FP64.

@@ -15,6 +15,8 @@ struct MixedState {
     double bnorm;   // max(||b||, 1e-30), the stop test's denominator
     double rz, sigma0, rmax, t0, last, rr_true, alpha, beta;
     float alpha_f, beta_f;  // the step's FP32 coefficients
+    float smin;             // smallest iterated residual norm since the last update
+    int stall;              // steps since smin was last lowered
     int iter, updates, need, done, result, status, par;
     bool fresh;   // the next step forms p from a replaced residual
     bool update;  // the step just finished asks for a reliable update
@@ -27,6 +29,8 @@ struct MixedState {
         rz = sbb;
         sigma0 = sqrt(sbb);
         rmax = sigma0;
+        smin = static_cast<float>(sigma0);
+        stall = 0;
         t0 = bn / bnorm;
         last = t0;
         rr_true = bb;
@@ -75,6 +79,8 @@ struct MixedState {
             rz = rr;
             sigma0 = sqrtf(static_cast<float>(rr));
             rmax = sigma0;
+            smin = static_cast<float>(sigma0);
+            stall = 0;
             if (need == 1)
                 ++updates;
             need = 0;
@@ -89,8 +95,14 @@ struct MixedState {
         const float sigma = sqrtf(static_cast<float>(rr));
         const float est = static_cast<float>(t0) * __fdiv_rn(sigma, static_cast<float>(sigma0));
         last = est;
+        if (sigma < smin) {
+            smin = sigma;
+            stall = 0;
+        } else {
+            ++stall;
+        }
         if (need || sigma < static_cast<float>(delta) * static_cast<float>(rmax) || est < static_cast<float>(tol) ||
-            iter >= max_iter) {
+            iter >= max_iter || stall >= kMixedStallSteps) {
             need = 1;  // fold, true residual, replacement, then a FRESH step at this parity
             update = true;
             return;

@@ -96,3 +96,32 @@ def test_mixed_true_residual_on_the_host(sg, ctx, p3d, oracle):
     # different Krylov paths to a 1e-8 residual of this ill-conditioned pinned
     # Neumann system and end 3.1e-5 apart (measured); a regression bound
     assert rel(x[::int(p3d["fx"]["jacobi_x_stride"])], p3d["fx"]["jacobi_x_sample"]) < 1e-4
+
+
+@pytest.mark.parametrize("engine", [0, 1])
+def test_mixed_converges_on_a_hard_system(sg, ctx, engine):
+    """The 160^3 distorted Neumann box needs 8405 FP64 Jacobi-PCG iterations.
+    Its FP32 inner CG stagnates above the reliable_delta drop that would
+    trigger an update; the stagnation trigger (no new residual minimum for 64
+    steps) forces the replacement.  Both engines must converge, within 2.5x
+    the FP64 count (before the trigger: 60,000 steps without converging)."""
+    torch = pytest.importorskip("torch")
+    from simall_gb300 import workloads as W
+
+    m, _ = W.poisson3d_mesh(160, seed=42)
+    aP, phi = W.poisson3d_inputs(m, seed=42)
+    ps = sg.PressureSystem(m, W.ALL_WALLS, ctx=ctx)
+    ps.assemble(1.0, aP, phi)
+    x = torch.empty(m.n_cells, dtype=torch.float64, device="cuda")
+    cfg = sg.LinearSolverConfig(kind=sg.LinearSolverKind.CG, preconditioner=sg.PreconditionerKind.Jacobi,
+                                tolerance=1e-8, maxIterations=60000)
+    s64 = sg.GpuCGSolver(cfg, precision=sg.Precision.FP64, ctx=ctx)
+    ps.solve(s64, x)
+    it64 = s64.stats.iterations
+    s64.close()
+    s = sg.GpuCGSolver(cfg, precision=sg.Precision.MIXED, ctx=ctx, engine=engine)
+    ps.solve(s, x)
+    assert s.stats.converged and s.stats.true_residual < 1e-8
+    assert s.stats.iterations <= 2.5 * it64, (s.stats.iterations, it64)
+    s.close()
+    ps.close()
