@@ -251,7 +251,7 @@ __device__ bool grid_allsum_f(const float (&v)[NV], double (&out)[NV], double *p
 }
 
 template <bool WIDE, bool STAGED>
-__global__ void __launch_bounds__(kSellThreads, 3) k_mx_grid_solve(GridArgs g)
+__global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
 {
     extern __shared__ __align__(128) unsigned char sell_smem[];
     __shared__ uint64_t bars[2 * kSellStages];

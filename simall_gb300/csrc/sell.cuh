@@ -157,19 +157,19 @@ __device__ __forceinline__ void sell_slice(const SellOp &A, int64_t sl, const fl
 // ---------------------------------------------------------------- staged step
 // The same step with the streamed operands staged through shared memory by
 // bulk copies (TMA).  A CTA of kSellThreads owns the contiguous slices
-// [c0, c1) and walks them in stages of 8 slices: warps 0-7 each compute one
-// slice of a stage, warp 8 produces.  For a stage the producer issues four
+// [c0, c1) and walks them in stages of 24 slices: warps 0-23 each compute one
+// slice of a stage, warp 24 produces.  For a stage the producer issues four
 // bulk copies -- the rows' packed state and row sums, and the stage's offsets
 // and values, each one contiguous range because slices are stored one after
 // the other -- into one slot of a ring of kSellStages buffers, announced on
-// the slot's `full` mbarrier; it refills a slot once all 8 compute warps have
+// the slot's `full` mbarrier; it refills a slot once all 24 compute warps have
 // arrived on its `empty` mbarrier.  A compute warp waits for its slot's copies
 // only, reads its rows' state and entries from shared memory and gathers
 // only the neighbours' state from global memory (L1/L2), so warps run up to
 // kSellStages - 1 stages apart and never wait for one another.  Slices up to
 // kSellStageMaxW entries wide take this path (every hex, tet or prism mesh);
 // wider ones the direct sell_slice.
-constexpr int kSellStageSlices = 8;  // slices per stage: one per compute warp
+constexpr int kSellStageSlices = 24;  // slices per stage: one per compute warp (one 800-thread CTA per SM)
 constexpr int kSellThreads = 32 * (kSellStageSlices + 1);  // 8 compute warps + the producer warp
 constexpr int kSellStageMaxW = 6;    // widest slice a stage buffer holds (hex meshes: 6); less shared memory, more L1
 constexpr int kSellStages = 3;       // ring depth

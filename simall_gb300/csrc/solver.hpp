@@ -176,7 +176,10 @@ int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C,
 // whole-solve persistent cooperative kernel (mixed_grid.cu); 0 = not taken
 // (check_interval > 0, engine KERNELS, no cooperative launch), 1 = taken with
 // *status set.  part holds partCap doubles (8 per CTA), ctr and err one word.
-constexpr int kGridMaxCtasPerSm = 3;  // the persistent mixed solve: 3 of 288 threads per SM measured fastest at 128^3
+// the persistent mixed solve: one CTA of 800 threads (24-slice stages) per SM
+// measured fastest at 128^3 (30.2 us per step, against 31.9 us with three
+// 288-thread CTAs and 34.3 us with two 544-thread ones)
+constexpr int kGridMaxCtasPerSm = 1;
 // Mixed precision in sliced storage: stages ahead whose operands the staged
 // steps prefetch into L2 (0 = none), and CTAs per SM of the persistent solve
 // (0 = as many as fit).  Process-wide; simall_diagnose_mixed_params sets them.
