@@ -40,14 +40,6 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t *bar, unsigned by
                  : "memory");
 }
 
-// Announce `bytes` more for the current phase without arriving: copies issued
-// now, the phase's one arrival to come later (with the rest of its bytes).
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes)
-{
-    asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-}
-
 // A plain arrival (a consumer releasing a buffer).
 __device__ __forceinline__ void mbar_arrive(uint64_t *bar)
 {

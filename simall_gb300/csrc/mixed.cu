@@ -624,7 +624,7 @@ __global__ void __launch_bounds__(kSellThreads) k_mx_iter_sell_staged(SellOp A, 
     if (threadIdx.x == 0)
         sell_ring_init(bars);
     __syncthreads();
-    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0, 0};
+    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
     const float alpha = FRESH ? 0.0f : static_cast<float>(__ldcg(&s->alpha));
     const float beta = static_cast<float>(__ldcg(&s->beta));
     const int64_t c0 = blockIdx.x * A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * A.nslices / gridDim.x;

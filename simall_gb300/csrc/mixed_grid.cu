@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
     if (STAGED && threadIdx.x == 0)
         sell_ring_init(bars);
     __syncthreads();
-    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0, 0};
+    SellRing<WIDE> R{reinterpret_cast<SellStageBuf<WIDE> *>(sell_smem), bars, 0};
     // this CTA's slices of the staged steps
     const int64_t c0 = blockIdx.x * g.A.nslices / gridDim.x, c1 = (blockIdx.x + 1) * g.A.nslices / gridDim.x;
     const int64_t n = g.A.n;
@@ -309,8 +309,7 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
         FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
         bool step_ok = true;
         if (STAGED) {
-            step_ok =
-                sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true, true);
+            step_ok = sell_step_staged<WIDE, false>(g.A, c0, c1, g.st[par], g.st[1 - par], alpha, beta, acc, R, true);
         } else {
             for (int64_t sl = warp; sl < g.A.nslices; sl += nwarps)
                 sell_slice<WIDE, false>(g.A, sl, g.st[par], g.st[1 - par], alpha, beta, acc);
@@ -355,8 +354,6 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
             st.finish_update(a, g.tol, g.max_iter);
         __syncthreads();
     }
-    if (STAGED && threadIdx.x == kSellStageSlices * 32)
-        sell_ring_drain(R);  // the next step's matrix copies, issued for a step that will not run
     if (blockIdx.x == 0 && threadIdx.x == 0)
         st.publish(g.s, ok);
 }

@@ -187,14 +187,11 @@ template <bool WIDE> constexpr size_t sell_stage_smem() { return kSellStages * s
 // The ring of one CTA: kSellStages buffers (dynamic shared memory), their
 // full and empty mbarriers (2 kSellStages, initialised by sell_ring_init);
 // q counts the stages this CTA has used, the same value in every thread, so
-// the slot and phase parity of every stage follow from it.  pre (the
-// producer's copy only): stages of the next step whose matrix part is
-// already issued, their phase still waiting for the state part's arrival.
+// the slot and phase parity of every stage follow from it.
 template <bool WIDE> struct SellRing {
     SellStageBuf<WIDE> *buf;
     uint64_t *bar;  // [0, kSellStages) full, [kSellStages, 2 kSellStages) empty
     uint32_t q;
-    int pre;
 };
 
 // Thread 0, once per launch, before a block barrier.
@@ -227,23 +224,23 @@ __device__ __forceinline__ void sell_prefetch_stage(const SellOp &A, int64_t c0,
     }
 }
 
-// The matrix part of stage s (row sums, values, offsets: constant over the
-// solve) into buffer B, announced on `bar` without an arrival; the matrix
-// streams are read once per step, so they are evicted from L2 first and the
-// state the neighbours gather stays there between steps.
 template <bool WIDE>
-__device__ __forceinline__ void sell_issue_matrix(const SellOp &A, int64_t c0, int64_t c1, int s,
-                                                  SellStageBuf<WIDE> &B, uint64_t *bar)
+__device__ __forceinline__ void sell_issue_stage(const SellOp &A, int64_t c0, int64_t c1, int s, const float4 *in,
+                                                 SellStageBuf<WIDE> &B, uint64_t *bar)
 {
     const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
     const int64_t sb = sa + kSellStageSlices < c1 ? sa + kSellStageSlices : c1;
     const int32_t ea = __ldg(A.sptr + sa), eb = __ldg(A.sptr + sb);
     const unsigned ne = static_cast<unsigned>(eb - ea);  // a multiple of 32
-    const int64_t r0 = sa * 32;
+    const int64_t r0 = sa * 32, r1 = sb * 32 < A.n ? sb * 32 : A.n;
+    const unsigned sbytes = static_cast<unsigned>(r1 - r0) * 16u;
     const unsigned ebytes = static_cast<unsigned>(sb - sa) * 128u;  // whole slices: e is padded
     const unsigned ob = WIDE ? 4u : 2u;
+    // the matrix streams are read once per step: evict them first, so the
+    // state the neighbours gather stays in L2 between steps
     const uint64_t once = l2_evict_first_policy();
-    mbar_expect_tx(bar, ebytes + ne * (4u + ob));
+    mbar_arrive_expect_tx(bar, sbytes + ebytes + ne * (4u + ob));
+    bulk_load(B.state, in + r0, sbytes, bar);
     bulk_load_hint(B.e, A.e + r0, ebytes, bar, once);
     if (ne) {
         bulk_load_hint(B.val, A.val + ea, ne * 4u, bar, once);
@@ -254,49 +251,16 @@ __device__ __forceinline__ void sell_issue_matrix(const SellOp &A, int64_t c0, i
     }
 }
 
-// The state part of stage s (the rows' packed state of the previous step),
-// with the phase's one arrival.
-template <bool WIDE>
-__device__ __forceinline__ void sell_issue_state(const SellOp &A, int64_t c0, int64_t c1, int s, const float4 *in,
-                                                 SellStageBuf<WIDE> &B, uint64_t *bar)
-{
-    const int64_t sa = c0 + static_cast<int64_t>(s) * kSellStageSlices;
-    const int64_t sb = sa + kSellStageSlices < c1 ? sa + kSellStageSlices : c1;
-    const int64_t r0 = sa * 32, r1 = sb * 32 < A.n ? sb * 32 : A.n;
-    const unsigned sbytes = static_cast<unsigned>(r1 - r0) * 16u;
-    mbar_arrive_expect_tx(bar, sbytes);
-    bulk_load(B.state, in + r0, sbytes, bar);
-}
-
-// Lets the matrix copies pre-issued for a step that will not run land (their
-// phases get the arrival they wait for), bounded; the producer calls it
-// before its CTA leaves.
-template <bool WIDE> __device__ __forceinline__ void sell_ring_drain(SellRing<WIDE> &R)
-{
-    for (int t = 0; t < R.pre; ++t) {
-        const uint32_t u = R.q + t;
-        mbar_arrive(R.bar + u % kSellStages);
-        mbar_wait(R.bar + u % kSellStages, (u / kSellStages) & 1u);
-    }
-    R.pre = 0;
-}
-
 // One step over the CTA's slices [c0, c1), staged; every thread of the CTA
 // calls it.  in_written_here: `in` was written earlier in the same launch (the
-// persistent kernel), so the copies follow a proxy fence.  preissue_next
-// (the persistent kernel): once this step's copies are issued, the producer
-// issues the matrix part of the next step's first kSellStages stages into
-// the slots as they are released, so that after the grid barrier only the
-// state (in L2) is still to come; sell_ring_drain settles them if no step
-// follows.  Returns this
+// persistent kernel), so the copies follow a proxy fence.  Returns this
 // thread's verdict, false when one of its waits ran out (a copy that did not
 // land, a slot that was not released; the producer then waits, bounded, for
 // the copies still in flight); no block barrier at the end: the caller folds
 // the verdicts into the barrier of its reduction (__syncthreads_and).
 template <bool WIDE, bool NC>
 __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const float4 *in, float4 *out, float alpha,
-                                 float beta, FF (&acc)[4], SellRing<WIDE> &R, bool in_written_here,
-                                 bool preissue_next = false)
+                                 float beta, FF (&acc)[4], SellRing<WIDE> &R, bool in_written_here)
 {
     const int nst = static_cast<int>((c1 - c0 + kSellStageSlices - 1) / kSellStageSlices);
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -310,39 +274,20 @@ __device__ bool sell_step_staged(const SellOp &A, int64_t c0, int64_t c1, const 
             int s = 0;
             for (; s < nst; ++s) {
                 const uint32_t u = R.q + s;
-                if (s < R.pre) {  // slot reserved and matrix issued at the end of the previous step
-                    sell_issue_state<WIDE>(A, c0, c1, s, in, R.buf[u % kSellStages], full + u % kSellStages);
-                } else {
-                    if (u >= static_cast<uint32_t>(kSellStages) &&
-                        !mbar_wait(empty + u % kSellStages, (u / kSellStages - 1) & 1u)) {
-                        ok = false;
-                        break;
-                    }
-                    fence_proxy_async_shared();  // the slot's previous contents were read through the generic proxy
-                    sell_issue_matrix<WIDE>(A, c0, c1, s, R.buf[u % kSellStages], full + u % kSellStages);
-                    sell_issue_state<WIDE>(A, c0, c1, s, in, R.buf[u % kSellStages], full + u % kSellStages);
+                if (u >= static_cast<uint32_t>(kSellStages) &&
+                    !mbar_wait(empty + u % kSellStages, (u / kSellStages - 1) & 1u)) {
+                    ok = false;
+                    break;
                 }
+                fence_proxy_async_shared();  // the slot's previous contents were read through the generic proxy
+                sell_issue_stage<WIDE>(A, c0, c1, s, in, R.buf[u % kSellStages], full + u % kSellStages);
                 if (A.prefetch > 0 && s + A.prefetch < nst)
                     sell_prefetch_stage<WIDE>(A, c0, c1, s + A.prefetch, in);
             }
-            R.pre = 0;
             if (!ok) {
                 // the copies issued and not yet consumed: let them land before the CTA can leave
                 for (int t = s - kSellStages < 0 ? 0 : s - kSellStages; t < s; ++t)
                     mbar_wait(full + (R.q + t) % kSellStages, ((R.q + t) / kSellStages) & 1u);
-            } else if (preissue_next) {
-                const int np = nst < kSellStages ? nst : kSellStages;  // the next step has the same stages
-                for (int t = 0; t < np; ++t) {
-                    const uint32_t u = R.q + nst + t;
-                    if (u >= static_cast<uint32_t>(kSellStages) &&
-                        !mbar_wait(empty + u % kSellStages, (u / kSellStages - 1) & 1u)) {
-                        ok = false;
-                        break;
-                    }
-                    fence_proxy_async_shared();
-                    sell_issue_matrix<WIDE>(A, c0, c1, t, R.buf[u % kSellStages], full + u % kSellStages);
-                    R.pre = t + 1;
-                }
             }
         }
     } else {
