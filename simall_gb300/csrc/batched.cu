@@ -26,7 +26,7 @@
 // cluster's shared memory), a fixed number of clusters striding through them
 // on reserved SMs while the one-CTA queue runs the rest on the other SMs; a
 // single SM streams a 65,025-row system at ~47 GB/s, 0.12 s for its ~2000
-// steps, a 16-CTA cluster solves it in ~15 ms.  The one-CTA shape (threads,
+// steps, a 16-CTA cluster solves it in ~12 ms.  The one-CTA shape (threads,
 // CTAs per SM, rows in flight per thread) and the cluster route (row
 // threshold, cluster size, clusters) are picked by an autotuner that times
 // candidates on the batch itself and keeps its choice in a JSON cache
@@ -518,11 +518,13 @@ int autotune(simall_batch *B, const double *b)
     for (const BatchSys &S : B->h_sys)
         nmax = std::max<int64_t>(nmax, S.nd >= 1 ? S.n : 0);
     // (rows, cluster CTAs, clusters); on the 512-system cavity batch of
-    // sides 32-256 the first takes 0.134 s against 0.197 s for the queue alone,
+    // sides 32-256 the first takes 0.107 s against 0.188 s for the queue alone,
     // and more clusters than these lose: 16-CTA clusters are placed a GPC
-    // at a time and wait for one another
-    const int routes[][3] = {{49152, 16, 4}, {49152, 16, 3}, {40960, 16, 6}, {49152, 8, 8},
-                             {40960, 8, 12}, {32768, 8, 12}, {16384, 4, 16}};
+    // at a time and wait for one another, and every SM a cluster holds is
+    // one the queue, which streams a system at a third of the SM-time a
+    // cluster spends on it, does not have
+    const int routes[][3] = {{40960, 16, 5}, {40960, 16, 4}, {40960, 16, 6}, {49152, 16, 4}, {49152, 16, 3},
+                             {32768, 16, 5}, {40960, 8, 10}, {40960, 8, 12}, {32768, 8, 12}, {16384, 4, 16}};
     for (const auto &r : routes) {
         if (nmax < r[0] || r[1] * r[2] >= ctx->num_sms)
             continue;
@@ -563,7 +565,7 @@ std::string batch_shape_key(simall_batch *B)
         if (c == '"' || c == '\\' || static_cast<unsigned char>(c) < 32)
             c = '_';
     char buf[256];
-    snprintf(buf, sizeof buf, "batch-fused-v3|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
+    snprintf(buf, sizeof buf, "batch-fused-v4|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
              static_cast<long long>(B->rows), static_cast<unsigned long long>(h));
     return buf;
 }

@@ -10,10 +10,20 @@
 // product and direction) live in the owners' shared memory and are read by the
 // other CTAs through distributed shared memory; a CTA's private per-row state
 // stays in registers.  Every global sum is one cluster barrier: each CTA
-// publishes its partial sums in shared memory, and after the barrier every
-// warp of every CTA reads all partials in rank order and reduces them with the
+// pushes its partial sums into every CTA's shared memory, and after the
+// barrier one warp of every CTA reduces all partials in rank order with the
 // same butterfly, so all CTAs hold bit-identical totals and take identical
-// decisions without further communication.  The only waits are hardware
+// decisions without further communication.
+//
+// 512 threads per CTA (one CTA per SM): 16 warps hide the latency of the
+// neighbour loads that 8 could not (a 65,025-row system on 16 CTAs: 8.0 ->
+// 6.2 us per step).  The row index of a thread is made opaque to the compiler
+// in each step (clmix_rows), so per-row addresses are not hoisted out of the
+// solve loop into registers: that hoisting had held up to 255 registers per
+// thread with spills, and at 512 threads a thread has 128.  A step's scalar
+// work is FP32 (ClMixState): with FP64 state and per-thread conversions of
+// alpha and beta, a step cost 1 us more at every size (3.2 against 2.2 us on
+// 2,025 rows; 6.2 against 5.2 us on 65,025).  The only waits are hardware
 // cluster barriers, reached the same number of times by every CTA (the trip
 // count follows from the identical totals and is bounded by max_iter), so no
 // CTA can wait for one that has left.
@@ -25,7 +35,9 @@
 //   Mixed precision (diagonal storage): the fused FP32 step of mixed.cu (row-
 //     sum form, beta from |r - alpha q|^2) with FP64 reliable updates -- one
 //     barrier per step, three more per reliable update.
+#include "bulk.cuh"
 #include "device.cuh"
+#include "ffsum.cuh"
 #include "solver.hpp"
 
 #include <cooperative_groups.h>
@@ -37,40 +49,25 @@ namespace cg = cooperative_groups;
 
 namespace simall {
 
-constexpr int kClThreads = 256;
-constexpr int kClMaxRowsPerCta = 8192;  // FP64: rows per thread <= 32
+constexpr int kClThreads = 512;
+constexpr int kClMaxRowsPerCta = 8192;  // mixed: 6 FP32 vectors of a slice in shared memory
+constexpr int kClPcg64MaxRowsPerCta = 4096;  // FP64: five FP64 registers per owned row and thread
 constexpr int kClMaxIterations = 200000;  // longer limits take the multi-kernel path
 
 namespace {
 
-__device__ __forceinline__ double warp_allsum(double v)
-{
-    // butterfly: every lane ends with the same bits (each step adds a pair in
-    // both lanes of the pair, and a + b == b + a)
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
-__device__ __forceinline__ float warp_sum_fl(float v)
-{
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1)
-        v += __shfl_xor_sync(0xffffffffu, v, o);
-    return v;
-}
-
 struct ClShared {
     double inbox[2][16][4];  // every CTA's partial sums, pushed here by their owners; two slots used alternately
+    float inboxf[2][16][4];  // the same for FP32 partials (summed in float-float after the barrier)
     double wsum[4][32];      // per-warp sums (FP64 values)
     float wsumf[4][32];      // per-warp sums (FP32 values)
     double tot[4];           // the cluster totals, broadcast to the CTA
+    FF totf[4];              // the same, float-float (FP32 partials)
     double ctl[8];           // scalars derived from the totals by one thread, broadcast
 };
 
 struct NoFinish {
-    __device__ void operator()(const double *, double *) const {}
+    template <typename... Args> __device__ void operator()(Args...) const {}
 };
 
 // Butterfly sums of NV values over groups of 2^LEVELS lanes, level by level
@@ -107,10 +104,11 @@ constexpr int kClMaxCtas = 16;  // cluster sizes up to 16: 4 butterfly levels
 // use no more levels than there are warps or CTAs.  `fin(tot, ctl)` runs in one
 // thread of each CTA before the broadcast: scalar arithmetic done once per CTA
 // instead of once per thread.
-template <int NV, typename T, typename Fin = NoFinish>
-__device__ __forceinline__ void cl_allreduce(const T (&v)[NV], double (&out)[NV], ClShared &sh, int &slot,
+template <int NV, typename T, typename O, typename Fin = NoFinish>
+__device__ __forceinline__ void cl_allreduce(const T (&v)[NV], O (&out)[NV], ClShared &sh, int &slot,
                                              const cg::cluster_group &cl, Fin fin = Fin{})
 {
+    static_assert(sizeof(T) == 4 ? sizeof(O) == sizeof(FF) : sizeof(O) == sizeof(double), "FP32 partials give FF totals");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T w[NV];
 #pragma unroll
@@ -147,30 +145,66 @@ __device__ __forceinline__ void cl_allreduce(const T (&v)[NV], double (&out)[NV]
             c[k] = __shfl_sync(0xffffffffu, c[k], 0);
         // push this CTA's partials into every CTA's inbox (lane L -> rank L)
         if (lane < C) {
-            double *dst = cl.map_shared_rank(&sh.inbox[slot][cl.block_rank()][0], lane);
+            if constexpr (sizeof(T) == 4) {
+                float *dst = cl.map_shared_rank(&sh.inboxf[slot][cl.block_rank()][0], lane);
 #pragma unroll
-            for (int k = 0; k < NV; ++k)
-                dst[k] = static_cast<double>(c[k]);
+                for (int k = 0; k < NV; ++k)
+                    dst[k] = c[k];
+            } else {
+                double *dst = cl.map_shared_rank(&sh.inbox[slot][cl.block_rank()][0], lane);
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    dst[k] = static_cast<double>(c[k]);
+            }
         }
     }
     cl.sync();
     if (wid == 0) {
-        double t[NV];
-#pragma unroll
-        for (int k = 0; k < NV; ++k)
-            t[k] = lane < C ? sh.inbox[slot][lane][k] : 0.0;
-        butterfly<4>(t);
-        if (lane == 0) {
+        if constexpr (sizeof(T) == 4) {
+            // FP32 partials: float-float butterfly on the FP32 pipe (the FP64
+            // butterfly here was the longest part of this warp's section,
+            // which every other warp waits for); FP64 only for the totals
+            FF t[NV];
 #pragma unroll
             for (int k = 0; k < NV; ++k)
-                sh.tot[k] = t[k];
-            fin(sh.tot, sh.ctl);
+                t[k] = FF{lane < C ? sh.inboxf[slot][lane][k] : 0.0f, 0.0f};
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k) {
+                    const FF o{__shfl_xor_sync(0xffffffffu, t[k].hi, 1 << l),
+                               __shfl_xor_sync(0xffffffffu, t[k].lo, 1 << l)};
+                    t[k] = ff_add(t[k], o);
+                }
+            }
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    sh.totf[k] = t[k];
+                fin(sh.totf, sh.ctl);
+            }
+        } else {
+            double t[NV];
+#pragma unroll
+            for (int k = 0; k < NV; ++k)
+                t[k] = lane < C ? sh.inbox[slot][lane][k] : 0.0;
+            butterfly<4>(t);
+            if (lane == 0) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    sh.tot[k] = t[k];
+                fin(sh.tot, sh.ctl);
+            }
         }
     }
     __syncthreads();
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
-        out[k] = sh.tot[k];
+    for (int k = 0; k < NV; ++k) {
+        if constexpr (sizeof(T) == 4)
+            out[k] = sh.totf[k];
+        else
+            out[k] = sh.tot[k];
+    }
     slot ^= 1;
 }
 
@@ -344,11 +378,35 @@ namespace {
 // registers; x lives in global memory (written at folds, read by the true
 // residual after a barrier).  The scalar state of the iteration is kept by one
 // thread per CTA and broadcast after every sum; all CTAs hold identical state.
+// A step's scalars are FP32 and its sums float-float: one thread updates them
+// while every other warp of the CTA waits, and on GB300's narrow FP64 pipe
+// each FP64 operation or conversion there costs tens of cycles.  FP64 is kept
+// for the reliable updates: the true residual, the norms of b.
 struct ClMixState {
-    double rz, sigma0, rmax, t0, last, alpha, beta, bnorm, rr64, b_norm;
+    double last, bnorm, rr64, b_norm;  // true relative residual; |b| (floored), |r|^2, |b|
+    FF rz;                             // r.r of the current step (float-float)
+    float t0, sigma0, rmax, alpha, beta;
     float smin;  // smallest iterated residual norm since the last update
     int iter, updates, need, done, result, status, stall;
 };
+
+// The shared::cluster address of shared address `a` in the CTA of rank `rank`.
+__device__ __forceinline__ uint32_t cl_mapa(uint32_t a, unsigned rank)
+{
+    uint32_t r;
+    asm("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+    return r;
+}
+
+// A load through the cluster's shared window (a shared::cta address names
+// this CTA's own memory).  Volatile: kept in program order with the cluster
+// barriers around the step.
+__device__ __forceinline__ float cl_ld(uint32_t a)
+{
+    float v;
+    asm volatile("ld.shared::cluster.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
 
 template <bool FRESH>
 __device__ __forceinline__ float cl_pdir(float r, float q, float p, float alpha, float beta)
@@ -357,48 +415,67 @@ __device__ __forceinline__ float cl_pdir(float r, float q, float p, float alpha,
     return __fmaf_rn(beta, p, rn);
 }
 
-// alpha and beta are used in FP32, so they are divided in FP32 (GB300's FP64
-// divide is a long dependent chain on a narrow pipe, and it sits on the
-// critical path of every step); the cancelling sum |r - alpha q|^2 is formed
-// in FP64.
-__device__ __forceinline__ void clmix_step(ClMixState &st, double pq, double qq, double rr, double rq)
+// x a for a float a, renormalised (the product's error from an FMA).
+__device__ __forceinline__ FF ff_mul_f(FF x, float a)
 {
-    if (!(pq > 0.0) || !(rr > 0.0)) {
+    const float p = __fmul_rn(x.hi, a);
+    const float e = __fmaf_rn(x.lo, a, __fmaf_rn(x.hi, a, -p));
+    const float hi = __fadd_rn(p, e);
+    return FF{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+// alpha = rr / pq and beta = |r - alpha q|^2 / rr, divided in FP32 (they are
+// used in FP32); the cancelling sum |r - alpha q|^2 = rr + alpha (alpha qq -
+// 2 rq) in float-float.  The totals are renormalised float-float values, so
+// their signs are those of their high parts.
+__device__ __forceinline__ void clmix_step(ClMixState &st, FF pq, FF qq, FF rr, FF rq)
+{
+    if (!(pq.hi > 0.0f) || !(rr.hi > 0.0f)) {
         st.status = SIMALL_ERR_BREAKDOWN;
         st.need = 1;
-        st.alpha = 0.0;
-        st.beta = 0.0;
+        st.alpha = 0.0f;
+        st.beta = 0.0f;
         return;
     }
-    const float alpha = __fdiv_rn(static_cast<float>(rr), static_cast<float>(pq));
-    const double a = alpha;
-    const double next = rr - 2.0 * a * rq + a * a * qq;
-    st.alpha = a;
-    st.beta = __fdiv_rn(static_cast<float>(next > 0.0 ? next : 0.0), static_cast<float>(rr));
+    const float alpha = __fdiv_rn(rr.hi, pq.hi);
+    const FF next = ff_add(rr, ff_mul_f(ff_add(ff_mul_f(qq, alpha), FF{-2.0f * rq.hi, -2.0f * rq.lo}), alpha));
+    st.alpha = alpha;
+    st.beta = __fdiv_rn(next.hi > 0.0f ? next.hi : 0.0f, rr.hi);
 }
 
 // One fused step over the owned rows.  Buffers [par] hold step k-1, [par ^ 1]
 // receive step k; FRESH takes r from rv[par ^ 1] (the replaced residual).
 // Shared layout: r[0] r[1] q[0] q[1] p[0] p[1], R floats each; R = 2^logR, so
-// the owner of row j is j >> logR and its slot j & (R - 1).  Every neighbour is
-// read through the cluster window (the owner may be this CTA), so the 2 ND
-// neighbours' loads carry no branch and issue together; a neighbour outside
-// [0, n) reads the row itself with a zero coefficient.
+// the owner of row j is j >> logR and its slot j & (R - 1).  Neighbours are
+// read with 32-bit shared::cluster addresses: this CTA's own shared address
+// for a row it owns, the owner's mapped address (mapa) for any other.  The
+// address is selected, not branched on, so the 2 ND neighbours' loads issue
+// together.  A neighbour outside [0, n) reads the row itself with a zero
+// coefficient.
 template <int ND, int RPT, bool FRESH>
 __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, int logR, int row0, int nr,
                                            const ClusterMixedArgs &A, const int (&off)[ND], float *base, int par,
                                            float alpha, float beta, float (&xh)[RPT], float (&acc)[4])
 {
     const int R = 1 << logR;
+    const unsigned me = static_cast<unsigned>(row0 >> logR);  // this CTA's rank
+    // the thread's row index, opaque to the compiler: per-row addresses are
+    // formed in every step instead of being hoisted out of the solve loop and
+    // held in registers across it
+    int tx = static_cast<int>(threadIdx.x);
+    asm volatile("" : "+r"(tx));
     const float *rs = base + (FRESH ? par ^ 1 : par) * R;
     const float *qs = base + (2 + par) * R;
     const float *ps = base + (4 + par) * R;
+    // shared-window addresses: r's, and the distances from r's array to q's and p's
+    const uint32_t rs_a = smem_u32(rs);
+    const uint32_t qs_d = smem_u32(qs) - rs_a, ps_d = smem_u32(ps) - rs_a;
     float *rout = base + (par ^ 1) * R;
     float *qout = base + (2 + (par ^ 1)) * R;
     float *pout = base + (4 + (par ^ 1)) * R;
 #pragma unroll
     for (int k = 0; k < RPT; ++k) {
-        const int il = threadIdx.x + k * kClThreads;
+        const int il = tx + k * kClThreads;
         if (il >= nr)
             continue;
         const int i = row0 + il;
@@ -414,9 +491,10 @@ __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, i
                 u[t] = ok ? __ldg(A.U + d * A.ldU + (side ? j : i)) : 0.0f;
                 const unsigned owner = static_cast<unsigned>(j >> logR);
                 const int jl = j & (R - 1);
-                rj[t] = *cl.map_shared_rank(rs + jl, owner);
-                qj[t] = FRESH ? 0.0f : *cl.map_shared_rank(qs + jl, owner);
-                pj[t] = *cl.map_shared_rank(ps + jl, owner);
+                const uint32_t a = owner == me ? rs_a + 4u * jl : cl_mapa(rs_a + 4u * jl, owner);
+                rj[t] = cl_ld(a);
+                qj[t] = FRESH ? 0.0f : cl_ld(a + qs_d);
+                pj[t] = cl_ld(a + ps_d);
             }
         }
         const float ro = rs[il], po = ps[il], ei = __ldg(A.e + i);
@@ -493,23 +571,24 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
             const double bn = sqrt(tt[1]);
             stp->b_norm = bn;
             stp->bnorm = std_max(bn, 1e-30);
-            stp->rz = tt[0];
-            stp->sigma0 = sqrt(tt[0]);
+            stp->rz = FF{static_cast<float>(tt[0]), 0.0f};
+            stp->sigma0 = sqrtf(static_cast<float>(tt[0]));
             stp->rmax = stp->sigma0;
-            stp->smin = static_cast<float>(stp->sigma0);
+            stp->smin = stp->sigma0;
             stp->stall = 0;
-            stp->t0 = bn / stp->bnorm;
-            stp->last = stp->t0;
+            const double t0 = bn / stp->bnorm;
+            stp->t0 = static_cast<float>(t0);
+            stp->last = t0;
             stp->rr64 = tt[1];
-            stp->alpha = 0.0;
-            stp->beta = 0.0;
+            stp->alpha = 0.0f;
+            stp->beta = 0.0f;
             stp->iter = 0;
             stp->updates = 0;
             stp->need = 2;
             stp->status = SIMALL_OK;
             stp->done = 0;
             stp->result = 0;
-            if (stp->t0 < tol) {
+            if (t0 < tol) {
                 stp->done = 1;
             } else if (max_iter <= 0) {
                 stp->done = 1;
@@ -517,46 +596,44 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
             }
         });
     }
-    auto fresh_fin = [stp](const double *t, double *) {
+    auto fresh_fin = [stp](const FF *t, double *) {
         stp->rz = t[2];
-        stp->sigma0 = sqrt(t[2]);
+        stp->sigma0 = sqrtf(t[2].hi);
         stp->rmax = stp->sigma0;
-        stp->smin = static_cast<float>(stp->sigma0);
+        stp->smin = stp->sigma0;
         stp->stall = 0;
         if (stp->need == 1)
             stp->updates += 1;
         stp->need = 0;
         clmix_step(*stp, t[0], t[1], t[2], t[3]);
     };
+    const float tolf = static_cast<float>(tol), deltaf = static_cast<float>(delta);
     int par = 1;
     if (!st.done) {
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, static_cast<float>(st.beta), xh,
-                              acc);
-        double t[4];
+        clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, st.beta, xh, acc);
+        FF t[4];
         cl_allreduce<4>(acc, t, sh, slot, cl, fresh_fin);
     }
     par = 0;
     while (!st.done) {
         float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-        clmix_rows<ND, RPT, false>(cl, n, logR, row0, nr, A, off, base, par, static_cast<float>(st.alpha),
-                               static_cast<float>(st.beta), xh, acc);
-        double t[4];
-        cl_allreduce<4>(acc, t, sh, slot, cl, [stp, tol, delta, max_iter](const double *tt, double *) {
-            // the trigger and the estimate in FP32 (one thread; FP64 divides and
-            // square roots are long chains on GB300's narrow FP64 pipe)
+        clmix_rows<ND, RPT, false>(cl, n, logR, row0, nr, A, off, base, par, st.alpha, st.beta, xh, acc);
+        FF t[4];
+        cl_allreduce<4>(acc, t, sh, slot, cl, [stp, tolf, deltaf, max_iter](const FF *tt, double *) {
+            // the trigger and the estimate in FP32 (the stop test itself is the
+            // FP64 true residual of the reliable update it triggers)
             stp->iter += 1;
-            const float sigma = sqrtf(static_cast<float>(tt[2]));
-            const float est = static_cast<float>(stp->t0) * __fdiv_rn(sigma, static_cast<float>(stp->sigma0));
-            stp->last = est;
+            const float sigma = sqrtf(tt[2].hi);
+            const float est = stp->t0 * __fdiv_rn(sigma, stp->sigma0);
             if (sigma < stp->smin) {
                 stp->smin = sigma;
                 stp->stall = 0;
             } else {
                 stp->stall += 1;
             }
-            if (stp->need || sigma < static_cast<float>(delta) * static_cast<float>(stp->rmax) ||
-                est < static_cast<float>(tol) || stp->iter >= max_iter || stp->stall >= kMixedStallSteps) {
+            if (stp->need || sigma < deltaf * stp->rmax || est < tolf || stp->iter >= max_iter ||
+                stp->stall >= kMixedStallSteps) {
                 stp->need = 1;
                 return;
             }
@@ -598,7 +675,7 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
                 stp->rr64 = tt[0];
                 const double tr = sqrt(tt[0]) / stp->bnorm;
                 stp->last = tr;
-                stp->t0 = tr;
+                stp->t0 = static_cast<float>(tr);
                 if (tr < tol) {
                     stp->done = 1;
                     stp->result = stp->iter;
@@ -606,15 +683,14 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
                     stp->done = 1;
                     stp->result = stp->iter >= max_iter ? max_iter : stp->iter;
                 } else {
-                    stp->beta = tt[1] / stp->rz;
+                    stp->beta = static_cast<float>(tt[1] / ff_double(stp->rz));
                 }
             });
             if (st.done)
                 break;
             float acc2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-            clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, static_cast<float>(st.beta),
-                                  xh, acc2);
-            double t4[4];
+            clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, st.beta, xh, acc2);
+            FF t4[4];
             cl_allreduce<4>(acc2, t4, sh, slot, cl, fresh_fin);
         }
         par ^= 1;
@@ -743,6 +819,16 @@ template <int RPT> int try_pcg64(simall_solver *s, int C, int logR, int *status)
     return 1;
 }
 
+// As try_mixed_rpt, up to kClPcg64MaxRowsPerCta rows.
+template <int RPT> int try_pcg64_rpt(simall_solver *s, int C, int logR, int rpt, int *status)
+{
+    if (rpt <= RPT)
+        return try_pcg64<RPT>(s, C, logR, status);
+    if constexpr (2 * RPT * kClThreads <= kClPcg64MaxRowsPerCta)
+        return try_pcg64_rpt<2 * RPT>(s, C, logR, rpt, status);
+    return 0;
+}
+
 template <int ND, int RPT> int try_mixed(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int *status)
 {
     simall_context *ctx = s->ctx;
@@ -756,17 +842,23 @@ template <int ND, int RPT> int try_mixed(simall_solver *s, const ClusterMixedArg
     return 1;
 }
 
+// The smallest RPT (a power of two, from RPT up) with RPT * kClThreads >= the
+// slice's rows, instantiated only up to kClMaxRowsPerCta rows.
+template <int ND, int RPT>
+int try_mixed_rpt(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int rpt, int *status)
+{
+    if (rpt <= RPT)
+        return try_mixed<ND, RPT>(s, a, C, logR, status);
+    if constexpr (2 * RPT * kClThreads <= kClMaxRowsPerCta)
+        return try_mixed_rpt<ND, 2 * RPT>(s, a, C, logR, rpt, status);
+    return 0;
+}
+
 template <int ND> int try_mixed_nd(simall_solver *s, const ClusterMixedArgs &a, int C, int logR, int *status)
 {
-    // every row of the slice needs a slot: RPT * kClThreads >= 2^logR (up to 8192 rows: 32)
+    // every row of the slice needs a slot: RPT * kClThreads >= 2^logR
     const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
-    return rpt <= 1    ? try_mixed<ND, 1>(s, a, C, logR, status)
-           : rpt <= 2  ? try_mixed<ND, 2>(s, a, C, logR, status)
-           : rpt <= 4  ? try_mixed<ND, 4>(s, a, C, logR, status)
-           : rpt <= 8  ? try_mixed<ND, 8>(s, a, C, logR, status)
-           : rpt <= 16 ? try_mixed<ND, 16>(s, a, C, logR, status)
-           : rpt <= 32 ? try_mixed<ND, 32>(s, a, C, logR, status)
-                       : 0;
+    return try_mixed_rpt<ND, 1>(s, a, C, logR, rpt, status);
 }
 
 // Slice length (a power of two, at least 256 rows) and cluster size for n rows
@@ -835,20 +927,30 @@ int launch_mixed_batch(simall_context *ctx, cudaStream_t stream, int C, int logR
     return SIMALL_OK;
 }
 
+// Smallest RPT (from RPT up, powers of two) that covers the slice; logR is
+// checked against kClMaxRowsPerCta by the caller.
+template <int ND, int RPT>
+int launch_mixed_batch_rpt(simall_context *ctx, cudaStream_t stream, int C, int logR, int rpt, int clusters,
+                           const ClBatchItem *items, int count, const double *b, double *x, double tol, double delta,
+                           int max_iter)
+{
+    if constexpr (2 * RPT * kClThreads <= kClMaxRowsPerCta) {
+        if (rpt > RPT)
+            return launch_mixed_batch_rpt<ND, 2 * RPT>(ctx, stream, C, logR, rpt, clusters, items, count, b, x, tol,
+                                                       delta, max_iter);
+    }
+    return launch_mixed_batch<ND, RPT>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta, max_iter);
+}
+
 template <int ND>
 int launch_mixed_batch_nd(simall_context *ctx, cudaStream_t stream, int C, int logR, int clusters,
                           const ClBatchItem *items, int count, const double *b, double *x, double tol, double delta,
                           int max_iter)
 {
     const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
-    return rpt <= 4    ? launch_mixed_batch<ND, 4>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
-                                                 max_iter)
-           : rpt <= 8  ? launch_mixed_batch<ND, 8>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
-                                                 max_iter)
-           : rpt <= 16 ? launch_mixed_batch<ND, 16>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
-                                                  max_iter)
-                       : launch_mixed_batch<ND, 32>(ctx, stream, C, logR, clusters, items, count, b, x, tol, delta,
-                                                  max_iter);
+    constexpr int kMinRpt = 4 * 256 / kClThreads > 1 ? 4 * 256 / kClThreads : 1;  // slices of >= 1024 rows
+    return launch_mixed_batch_rpt<ND, kMinRpt>(ctx, stream, C, logR, rpt, clusters, items, count, b, x, tol, delta,
+                                               max_iter);
 }
 }  // namespace
 
@@ -875,19 +977,14 @@ int cluster_mixed_batch(simall_context *ctx, cudaStream_t stream, int nd, int C,
 int cluster_fp64_solve(simall_solver *s, int *status)
 {
     // one launch runs the whole solve: keep it short even when it does not converge
-    if (s->n <= 0 || s->n > 16 * kClMaxRowsPerCta || s->nnz > INT32_MAX || s->cfg.max_iterations > kClMaxIterations)
+    if (s->n <= 0 || s->n > 16 * kClPcg64MaxRowsPerCta || s->nnz > INT32_MAX || s->cfg.max_iterations > kClMaxIterations)
         return 0;
     for (int maxC : {16, 8}) {
         int C = 0, logR = 0;
         if (!cluster_shape(s->n, maxC, &C, &logR))
             continue;
         const int rpt = ((1 << logR) + kClThreads - 1) / kClThreads;
-        const int taken = rpt <= 1    ? try_pcg64<1>(s, C, logR, status)
-                          : rpt <= 2  ? try_pcg64<2>(s, C, logR, status)
-                          : rpt <= 4  ? try_pcg64<4>(s, C, logR, status)
-                          : rpt <= 8  ? try_pcg64<8>(s, C, logR, status)
-                          : rpt <= 16 ? try_pcg64<16>(s, C, logR, status)
-                                      : 0;
+        const int taken = try_pcg64_rpt<1>(s, C, logR, rpt, status);
         if (taken)
             return 1;
     }
