@@ -207,6 +207,7 @@ template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const Batc
         __syncthreads();
     }
     const int64_t trip_cap = 2 * static_cast<int64_t>(a.maxit > 0 ? a.maxit : 0) + 16;
+    const float tolf = static_cast<float>(a.tol), deltaf = static_cast<float>(a.delta);
     for (int64_t trips = 0; !ms.done; ++trips) {
         if (trips > trip_cap) {  // unreachable: every normal step counts and max_iter ends the solve
             __syncthreads();
@@ -236,13 +237,9 @@ template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const Batc
                 }
             }
         }
-        double t[4];
         ff_block_allsum<4>(acc);
-#pragma unroll
-        for (int k = 0; k < 4; ++k)
-            t[k] = ff_double(acc[k]);
         if (threadIdx.x == 0)
-            ms.finish_step(t, a.tol, a.delta, a.maxit);
+            ms.finish_step(acc, tolf, deltaf, a.maxit);
         __syncthreads();
         if (!ms.update)
             continue;

@@ -415,15 +415,6 @@ __device__ __forceinline__ float cl_pdir(float r, float q, float p, float alpha,
     return __fmaf_rn(beta, p, rn);
 }
 
-// x a for a float a, renormalised (the product's error from an FMA).
-__device__ __forceinline__ FF ff_mul_f(FF x, float a)
-{
-    const float p = __fmul_rn(x.hi, a);
-    const float e = __fmaf_rn(x.lo, a, __fmaf_rn(x.hi, a, -p));
-    const float hi = __fadd_rn(p, e);
-    return FF{hi, __fsub_rn(e, __fsub_rn(hi, p))};
-}
-
 // alpha = rr / pq and beta = |r - alpha q|^2 / rr, divided in FP32 (they are
 // used in FP32); the cancelling sum |r - alpha q|^2 = rr + alpha (alpha qq -
 // 2 rq) in float-float.  The totals are renormalised float-float values, so
@@ -438,7 +429,7 @@ __device__ __forceinline__ void clmix_step(ClMixState &st, FF pq, FF qq, FF rr, 
         return;
     }
     const float alpha = __fdiv_rn(rr.hi, pq.hi);
-    const FF next = ff_add(rr, ff_mul_f(ff_add(ff_mul_f(qq, alpha), FF{-2.0f * rq.hi, -2.0f * rq.lo}), alpha));
+    const FF next = ff_next_rr(rr, qq, rq, alpha);
     st.alpha = alpha;
     st.beta = __fdiv_rn(next.hi > 0.0f ? next.hi : 0.0f, rr.hi);
 }

@@ -51,6 +51,22 @@ __device__ __forceinline__ FF ff_add(FF a, FF b)
     return FF{hi, __fsub_rn(lo, __fsub_rn(hi, s))};
 }
 
+// x a for a float a, renormalised (the product's error from an FMA).
+__device__ __forceinline__ FF ff_mul_f(FF x, float a)
+{
+    const float p = __fmul_rn(x.hi, a);
+    const float e = __fmaf_rn(x.lo, a, __fmaf_rn(x.hi, a, -p));
+    const float hi = __fadd_rn(p, e);
+    return FF{hi, __fsub_rn(e, __fsub_rn(hi, p))};
+}
+
+// |r - alpha q|^2 = rr + alpha (alpha qq - 2 rq) from renormalised totals: it
+// cancels, so it is formed in float-float; the result's sign is its high part's.
+__device__ __forceinline__ FF ff_next_rr(FF rr, FF qq, FF rq, float alpha)
+{
+    return ff_add(rr, ff_mul_f(ff_add(ff_mul_f(qq, alpha), FF{-2.0f * rq.hi, -2.0f * rq.lo}), alpha));
+}
+
 __device__ __forceinline__ double ff_double(FF a) { return static_cast<double>(a.hi) + static_cast<double>(a.lo); }
 
 // Butterfly over the warp: every lane ends with the same bits (each level adds

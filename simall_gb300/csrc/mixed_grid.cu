@@ -223,10 +223,10 @@ __device__ bool step_allsum(bool ok_thread, FF (&acc)[4], double *part, unsigned
     }
     __syncthreads();
     if (wid == 0) {
-        double tot[4];
+        FF tot[4];
 #pragma unroll
         for (int k = 0; k < 4; ++k)
-            tot[k] = ff_double(ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero()));
+            tot[k] = ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero());
         if (lane == 0)
             fin(tot);
     }
@@ -297,6 +297,7 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
         st.start(tot[0], tot[1], g.tol, g.max_iter);
     __syncthreads();
     const int64_t trip_cap = 2 * static_cast<int64_t>(g.max_iter > 0 ? g.max_iter : 0) + 16;
+    const float tolf = static_cast<float>(g.tol), deltaf = static_cast<float>(g.delta);
     for (int64_t trips = 0; ok && !st.done; ++trips) {
         if (trips > trip_cap) {  // unreachable: every normal step counts and max_iter ends the solve
             if (threadIdx.x == 0)
@@ -315,7 +316,7 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
                 sell_slice<WIDE, false>(g.A, sl, g.st[par], g.st[1 - par], alpha, beta, acc);
         }
         if (!(ok = step_allsum(step_ok, acc, g.part, g.ctr, epoch, g.err,
-                               [&](const double (&t)[4]) { st.finish_step(t, g.tol, g.delta, g.max_iter); })))
+                               [&](const FF (&t)[4]) { st.finish_step(t, tolf, deltaf, g.max_iter); })))
             break;
         if (!st.update)
             continue;

@@ -4,18 +4,29 @@
 // transitions of mixed.cu's k_mx_init / mx_finish / mx_step /
 // k_mx_true_residual, advanced by one thread and read by the others after a
 // barrier.
+//
+// A step's totals arrive as float-float values and its scalars are FP32: the
+// thread that advances the state does it while every other thread of its CTA
+// waits at the next barrier, and on GB300's narrow FP64 pipe each FP64
+// operation or conversion on that path costs tens of cycles (in the cluster
+// engine, which has the same state machine, FP64 state cost 1 us per step).
+// FP64 is kept for the reliable updates: the true residual and the norms of b.
 #pragma once
 
+#include "ffsum.cuh"
 #include "internal.hpp"
 
 namespace simall {
 
 struct MixedState {
-    double b_norm;  // ||b||
-    double bnorm;   // max(||b||, 1e-30), the stop test's denominator
-    double rz, sigma0, rmax, t0, last, rr_true, alpha, beta;
-    float alpha_f, beta_f;  // the step's FP32 coefficients
-    float smin;             // smallest iterated residual norm since the last update
+    double b_norm;   // ||b||
+    double bnorm;    // max(||b||, 1e-30), the stop test's denominator
+    double last;     // the last true relative residual
+    double rr_true;  // |b - A x|^2 at the last reliable update
+    FF rz;           // r.r of the current step
+    float sigma0, rmax, t0;  // iterated residual norm after the last update, its running maximum, true residual then
+    float alpha_f, beta_f;   // the step's FP32 coefficients
+    float smin;              // smallest iterated residual norm since the last update
     int stall;              // steps since smin was last lowered
     int iter, updates, need, done, result, status, par;
     bool fresh;   // the next step forms p from a replaced residual
@@ -26,15 +37,15 @@ struct MixedState {
         const double bn = sqrt(bb);
         b_norm = bn;
         bnorm = bn > 1e-30 ? bn : 1e-30;
-        rz = sbb;
-        sigma0 = sqrt(sbb);
+        rz = FF{static_cast<float>(sbb), 0.0f};
+        sigma0 = sqrtf(static_cast<float>(sbb));
         rmax = sigma0;
-        smin = static_cast<float>(sigma0);
+        smin = sigma0;
         stall = 0;
-        t0 = bn / bnorm;
-        last = t0;
+        const double tr = bn / bnorm;
+        t0 = static_cast<float>(tr);
+        last = tr;
         rr_true = bb;
-        alpha = beta = 0.0;
         alpha_f = beta_f = 0.0f;
         iter = updates = result = 0;
         need = 2;  // the first (FRESH) step is not counted as an update
@@ -43,7 +54,7 @@ struct MixedState {
         par = 1;   // the first step forms p = r (beta = 0) at parity 1
         fresh = true;
         update = false;
-        if (t0 < tol) {
+        if (tr < tol) {
             done = 1;  // b == 0: x = 0 is exact
         } else if (max_iter <= 0) {
             done = 1;
@@ -51,35 +62,32 @@ struct MixedState {
         }
     }
 
-    // alpha and beta are used in FP32, so they are divided in FP32: GB300's
-    // FP64 divide and square root are long chains on a narrow pipe, and this
-    // runs on the critical path of every step.  |r - alpha q|^2, which
-    // cancels, is formed in FP64 with the FP32 alpha the step will use.
-    __device__ void coefficients(const double (&t)[4])
+    // alpha and beta are used in FP32, so they are divided in FP32;
+    // |r - alpha q|^2, which cancels, is formed in float-float with the FP32
+    // alpha the step will use.  t = {p.q, q.q, r.r, r.q}, renormalised.
+    __device__ void coefficients(const FF (&t)[4])
     {
-        const double pq = t[0], qq = t[1], rr = t[2], rq = t[3];
-        if (!(pq > 0.0) || !(rr > 0.0)) {  // not SPD in FP32, or exact breakdown
+        const FF pq = t[0], qq = t[1], rr = t[2], rq = t[3];
+        if (!(pq.hi > 0.0f) || !(rr.hi > 0.0f)) {  // not SPD in FP32, or exact breakdown
             status = SIMALL_ERR_BREAKDOWN;
             need = 1;
             alpha_f = beta_f = 0.0f;
         } else {
-            alpha_f = __fdiv_rn(static_cast<float>(rr), static_cast<float>(pq));
-            const double a = alpha_f;
-            const double next = rr - 2.0 * a * rq + a * a * qq;
-            beta_f = __fdiv_rn(static_cast<float>(next > 0.0 ? next : 0.0), static_cast<float>(rr));
+            alpha_f = __fdiv_rn(rr.hi, pq.hi);
+            const FF next = ff_next_rr(rr, qq, rq, alpha_f);
+            beta_f = __fdiv_rn(next.hi > 0.0f ? next.hi : 0.0f, rr.hi);
         }
-        alpha = alpha_f;
-        beta = beta_f;
     }
 
-    __device__ void finish_step(const double (&t)[4], double tol, double delta, int max_iter)
+    // tolf, deltaf: the tolerance and the update trigger as floats
+    __device__ void finish_step(const FF (&t)[4], float tolf, float deltaf, int max_iter)
     {
-        const double rr = t[2];
+        const FF rr = t[2];
         if (fresh) {
             rz = rr;
-            sigma0 = sqrtf(static_cast<float>(rr));
+            sigma0 = sqrtf(rr.hi);
             rmax = sigma0;
-            smin = static_cast<float>(sigma0);
+            smin = sigma0;
             stall = 0;
             if (need == 1)
                 ++updates;
@@ -91,18 +99,17 @@ struct MixedState {
             return;
         }
         ++iter;
-        // the trigger and the estimate in FP32 (the same reason as above)
-        const float sigma = sqrtf(static_cast<float>(rr));
-        const float est = static_cast<float>(t0) * __fdiv_rn(sigma, static_cast<float>(sigma0));
-        last = est;
+        // the trigger and the estimate (the stop test itself is the FP64 true
+        // residual of the reliable update this asks for)
+        const float sigma = sqrtf(rr.hi);
+        const float est = t0 * __fdiv_rn(sigma, sigma0);
         if (sigma < smin) {
             smin = sigma;
             stall = 0;
         } else {
             ++stall;
         }
-        if (need || sigma < static_cast<float>(delta) * static_cast<float>(rmax) || est < static_cast<float>(tol) ||
-            iter >= max_iter || stall >= kMixedStallSteps) {
+        if (need || sigma < deltaf * rmax || est < tolf || iter >= max_iter || stall >= kMixedStallSteps) {
             need = 1;  // fold, true residual, replacement, then a FRESH step at this parity
             update = true;
             return;
@@ -121,7 +128,7 @@ struct MixedState {
         rr_true = a[0];
         const double tt = sqrt(a[0]) / bnorm;
         last = tt;
-        t0 = tt;
+        t0 = static_cast<float>(tt);
         update = false;
         if (tt < tol) {
             done = 1;
@@ -130,8 +137,7 @@ struct MixedState {
             done = 1;
             result = iter >= max_iter ? max_iter : iter;
         } else {
-            beta = a[1] / rz;
-            beta_f = static_cast<float>(beta);
+            beta_f = static_cast<float>(a[1] / ff_double(rz));
             fresh = true;
         }
     }
@@ -145,9 +151,9 @@ struct MixedState {
 
     __device__ void publish(SolveScalars *s, bool ok) const
     {
-        s->rz = rz;
-        s->alpha = alpha;
-        s->beta = beta;
+        s->rz = ff_double(rz);
+        s->alpha = alpha_f;
+        s->beta = beta_f;
         s->rr = rr_true;
         s->bnorm = bnorm;
         s->last = last;
