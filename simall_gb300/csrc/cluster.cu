@@ -44,6 +44,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 namespace cg = cooperative_groups;
 
@@ -57,13 +58,13 @@ constexpr int kClMaxIterations = 200000;  // longer limits take the multi-kernel
 namespace {
 
 struct ClShared {
-    double inbox[2][16][4];  // every CTA's partial sums, pushed here by their owners; two slots used alternately
-    float inboxf[2][16][4];  // the same for FP32 partials (summed in float-float after the barrier)
-    double wsum[4][32];      // per-warp sums (FP64 values)
-    float wsumf[4][32];      // per-warp sums (FP32 values)
-    double tot[4];           // the cluster totals, broadcast to the CTA
-    FF totf[4];              // the same, float-float (FP32 partials)
-    double ctl[8];           // scalars derived from the totals by one thread, broadcast
+    double inbox[2][16][4];   // every CTA's partial sums, pushed here by their owners; two slots used alternately
+    float2 inboxff[2][16][4]; // the same for float-float partials (hi, lo)
+    double wsum[4][32];       // per-warp sums (FP64 values)
+    FF wsumff[4][32];         // per-warp sums (float-float values)
+    double tot[4];            // the cluster totals, broadcast to the CTA
+    FF totf[4];               // the same, float-float
+    double ctl[8];            // scalars derived from the totals by one thread, broadcast
 };
 
 struct NoFinish {
@@ -92,34 +93,43 @@ constexpr int kClWarpLevels = kClWarps <= 1 ? 0 : kClWarps <= 2 ? 1 : kClWarps <
 constexpr int kClMaxCtas = 16;  // cluster sizes up to 16: 4 butterfly levels
 
 // Cluster-wide sum of NV values; every thread of every CTA receives the same
-// totals.  Sums within a CTA run in the values' own type (FP32 for the mixed
-// solver's per-thread partials, FP64 for the FP64 solver); the sum across the
-// CTAs -- the global reduction -- is FP64.  Each CTA pushes its partials into
-// every CTA's shared memory before the barrier (stores through the cluster
-// window, whose latency the barrier absorbs; the kernels start with a cluster
-// barrier so that no CTA writes into one that has not started), so after it
-// the sum reads only local shared memory.  The butterflies
-// run level by level over all NV values: on GB300's narrow FP64 pipe a chain
-// of FP64 adds costs ~100 cycles per level, so the NV chains must overlap and
-// use no more levels than there are warps or CTAs.  `fin(tot, ctl)` runs in one
-// thread of each CTA before the broadcast: scalar arithmetic done once per CTA
-// instead of once per thread.
-template <int NV, typename T, typename O, typename Fin = NoFinish>
-__device__ __forceinline__ void cl_allreduce(const T (&v)[NV], O (&out)[NV], ClShared &sh, int &slot,
+// totals.  Two kinds of partials: float-float (the mixed solver's per-thread
+// sums of FP32 products, with each product's and each addition's error
+// carried) summed in float-float at every level on the FP32 pipe, and FP64
+// (the FP64 solver, and the mixed solver's FP64 residual sums at reliable
+// updates) summed in FP64.  With plain FP32 sums the mixed solver's step count
+// moved by up to 8% with nothing but the thread count changed (783 against
+// 849 steps on a 128^2 cavity system); in float-float it does not depend on
+// the grouping.  Each CTA pushes its partials into every CTA's shared memory
+// before the barrier (stores through the cluster window, whose latency the
+// barrier absorbs; the kernels start with a cluster barrier so that no CTA
+// writes into one that has not started), so after it the sum reads only local
+// shared memory.  The butterflies run level by level over all NV values, so
+// the NV dependent chains overlap, with no more levels than there are warps or
+// CTAs.  `fin(tot, ctl)` runs in one thread of each CTA before the broadcast:
+// scalar arithmetic done once per CTA instead of once per thread.
+template <int NV, typename T, typename Fin = NoFinish>
+__device__ __forceinline__ void cl_allreduce(const T (&v)[NV], T (&out)[NV], ClShared &sh, int &slot,
                                              const cg::cluster_group &cl, Fin fin = Fin{})
 {
-    static_assert(sizeof(T) == 4 ? sizeof(O) == sizeof(FF) : sizeof(O) == sizeof(double), "FP32 partials give FF totals");
+    constexpr bool kFF = std::is_same<T, FF>::value;
+    static_assert(kFF || std::is_same<T, double>::value, "float-float or FP64 partials");
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     T w[NV];
 #pragma unroll
-    for (int k = 0; k < NV; ++k)
-        w[k] = v[k];
-    butterfly<5>(w);
+    for (int k = 0; k < NV; ++k) {
+        if constexpr (kFF)
+            w[k] = ff_warp_allsum(v[k]);
+        else
+            w[k] = v[k];
+    }
+    if constexpr (!kFF)
+        butterfly<5>(w);
     if (lane == 0) {
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            if constexpr (sizeof(T) == 4)
-                sh.wsumf[k][wid] = w[k];
+            if constexpr (kFF)
+                sh.wsumff[k][wid] = w[k];
             else
                 sh.wsum[k][wid] = w[k];
         }
@@ -130,77 +140,89 @@ __device__ __forceinline__ void cl_allreduce(const T (&v)[NV], O (&out)[NV], ClS
         T c[NV];
 #pragma unroll
         for (int k = 0; k < NV; ++k) {
-            if constexpr (sizeof(T) == 4)
-                c[k] = lane < kClWarps ? sh.wsumf[k][lane] : 0.0f;
+            if constexpr (kFF)
+                c[k] = lane < kClWarps ? sh.wsumff[k][lane] : ff_zero();
             else
                 c[k] = lane < kClWarps ? sh.wsum[k][lane] : 0.0;
         }
-        butterfly<kClWarpLevels>(c);
+        if constexpr (kFF) {
+#pragma unroll
+            for (int l = 0; l < kClWarpLevels; ++l) {
+#pragma unroll
+                for (int k = 0; k < NV; ++k)
+                    c[k] = ff_add(c[k], FF{__shfl_xor_sync(0xffffffffu, c[k].hi, 1 << l),
+                                           __shfl_xor_sync(0xffffffffu, c[k].lo, 1 << l)});
+            }
+        } else {
+            butterfly<kClWarpLevels>(c);
+        }
         // Only lanes 0 .. kClWarps-1 hold the CTA's sum after that butterfly:
         // take lane 0's before lane L pushes it to rank L.  (Pushing another
         // lane's value gave the CTAs different totals, different branches,
         // and CTAs that left while others still used their shared memory.)
 #pragma unroll
-        for (int k = 0; k < NV; ++k)
-            c[k] = __shfl_sync(0xffffffffu, c[k], 0);
+        for (int k = 0; k < NV; ++k) {
+            if constexpr (kFF)
+                c[k] = FF{__shfl_sync(0xffffffffu, c[k].hi, 0), __shfl_sync(0xffffffffu, c[k].lo, 0)};
+            else
+                c[k] = __shfl_sync(0xffffffffu, c[k], 0);
+        }
         // push this CTA's partials into every CTA's inbox (lane L -> rank L)
         if (lane < C) {
-            if constexpr (sizeof(T) == 4) {
-                float *dst = cl.map_shared_rank(&sh.inboxf[slot][cl.block_rank()][0], lane);
+            if constexpr (kFF) {
+                float2 *dst = cl.map_shared_rank(&sh.inboxff[slot][cl.block_rank()][0], lane);
 #pragma unroll
                 for (int k = 0; k < NV; ++k)
-                    dst[k] = c[k];
+                    dst[k] = make_float2(c[k].hi, c[k].lo);
             } else {
                 double *dst = cl.map_shared_rank(&sh.inbox[slot][cl.block_rank()][0], lane);
 #pragma unroll
                 for (int k = 0; k < NV; ++k)
-                    dst[k] = static_cast<double>(c[k]);
+                    dst[k] = c[k];
             }
         }
     }
     cl.sync();
     if (wid == 0) {
-        if constexpr (sizeof(T) == 4) {
-            // FP32 partials: float-float butterfly on the FP32 pipe (the FP64
-            // butterfly here was the longest part of this warp's section,
-            // which every other warp waits for); FP64 only for the totals
-            FF t[NV];
+        T t[NV];
 #pragma unroll
-            for (int k = 0; k < NV; ++k)
-                t[k] = FF{lane < C ? sh.inboxf[slot][lane][k] : 0.0f, 0.0f};
+        for (int k = 0; k < NV; ++k) {
+            if constexpr (kFF) {
+                const float2 e = lane < C ? sh.inboxff[slot][lane][k] : make_float2(0.0f, 0.0f);
+                t[k] = FF{e.x, e.y};
+            } else {
+                t[k] = lane < C ? sh.inbox[slot][lane][k] : 0.0;
+            }
+        }
+        if constexpr (kFF) {
 #pragma unroll
             for (int l = 0; l < 4; ++l) {
 #pragma unroll
-                for (int k = 0; k < NV; ++k) {
-                    const FF o{__shfl_xor_sync(0xffffffffu, t[k].hi, 1 << l),
-                               __shfl_xor_sync(0xffffffffu, t[k].lo, 1 << l)};
-                    t[k] = ff_add(t[k], o);
-                }
-            }
-            if (lane == 0) {
-#pragma unroll
                 for (int k = 0; k < NV; ++k)
-                    sh.totf[k] = t[k];
-                fin(sh.totf, sh.ctl);
+                    t[k] = ff_add(t[k], FF{__shfl_xor_sync(0xffffffffu, t[k].hi, 1 << l),
+                                           __shfl_xor_sync(0xffffffffu, t[k].lo, 1 << l)});
             }
         } else {
-            double t[NV];
-#pragma unroll
-            for (int k = 0; k < NV; ++k)
-                t[k] = lane < C ? sh.inbox[slot][lane][k] : 0.0;
             butterfly<4>(t);
-            if (lane == 0) {
+        }
+        if (lane == 0) {
 #pragma unroll
-                for (int k = 0; k < NV; ++k)
+            for (int k = 0; k < NV; ++k) {
+                if constexpr (kFF)
+                    sh.totf[k] = t[k];
+                else
                     sh.tot[k] = t[k];
-                fin(sh.tot, sh.ctl);
             }
+            if constexpr (kFF)
+                fin(sh.totf, sh.ctl);
+            else
+                fin(sh.tot, sh.ctl);
         }
     }
     __syncthreads();
 #pragma unroll
     for (int k = 0; k < NV; ++k) {
-        if constexpr (sizeof(T) == 4)
+        if constexpr (kFF)
             out[k] = sh.totf[k];
         else
             out[k] = sh.tot[k];
@@ -437,16 +459,17 @@ __device__ __forceinline__ void clmix_step(ClMixState &st, FF pq, FF qq, FF rr, 
 // One fused step over the owned rows.  Buffers [par] hold step k-1, [par ^ 1]
 // receive step k; FRESH takes r from rv[par ^ 1] (the replaced residual).
 // Shared layout: r[0] r[1] q[0] q[1] p[0] p[1], R floats each; R = 2^logR, so
-// the owner of row j is j >> logR and its slot j & (R - 1).  Neighbours are
+// the owner of row j is j >> logR and its slot j & (R - 1).  When both
+// neighbours of a row on a diagonal lie in this CTA's slice (most rows, on
+// most diagonals) they are plain shared-memory loads.  Otherwise they are
 // read with 32-bit shared::cluster addresses: this CTA's own shared address
-// for a row it owns, the owner's mapped address (mapa) for any other.  The
-// address is selected, not branched on, so the 2 ND neighbours' loads issue
-// together.  A neighbour outside [0, n) reads the row itself with a zero
-// coefficient.
+// for a row it owns, the owner's mapped address (mapa) for any other; the
+// address is selected, not branched on, so the loads issue together.  A
+// neighbour outside [0, n) reads the row itself with a zero coefficient.
 template <int ND, int RPT, bool FRESH>
 __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, int logR, int row0, int nr,
                                            const ClusterMixedArgs &A, const int (&off)[ND], float *base, int par,
-                                           float alpha, float beta, float (&xh)[RPT], float (&acc)[4])
+                                           float alpha, float beta, float (&xh)[RPT], FF (&acc)[4])
 {
     const int R = 1 << logR;
     const unsigned me = static_cast<unsigned>(row0 >> logR);  // this CTA's rank
@@ -473,13 +496,29 @@ __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, i
         float u[2 * ND], rj[2 * ND], qj[2 * ND], pj[2 * ND];
 #pragma unroll
         for (int d = 0; d < ND; ++d) {
+            const int od = off[d];
+            const float *Ud = A.U + d * A.ldU;
+            if (ND <= 3 && il >= od && il + od < nr) {
+                // both neighbours on this diagonal in this CTA's slice (so in
+                // [0, n)): plain shared-memory loads, no checks (not with 4
+                // diagonals: the two paths then spill at 128 registers)
+                u[2 * d] = __ldg(Ud + i);
+                u[2 * d + 1] = __ldg(Ud + i - od);
+                rj[2 * d] = rs[il + od];
+                rj[2 * d + 1] = rs[il - od];
+                qj[2 * d] = FRESH ? 0.0f : qs[il + od];
+                qj[2 * d + 1] = FRESH ? 0.0f : qs[il - od];
+                pj[2 * d] = ps[il + od];
+                pj[2 * d + 1] = ps[il - od];
+                continue;
+            }
 #pragma unroll
             for (int side = 0; side < 2; ++side) {
                 const int t = 2 * d + side;
-                const int j0 = side ? i - off[d] : i + off[d];
+                const int j0 = side ? i - od : i + od;
                 const bool ok = j0 >= 0 && j0 < n;
                 const int j = ok ? j0 : i;
-                u[t] = ok ? __ldg(A.U + d * A.ldU + (side ? j : i)) : 0.0f;
+                u[t] = ok ? __ldg(Ud + (side ? j : i)) : 0.0f;
                 const unsigned owner = static_cast<unsigned>(j >> logR);
                 const int jl = j & (R - 1);
                 const uint32_t a = owner == me ? rs_a + 4u * jl : cl_mapa(rs_a + 4u * jl, owner);
@@ -501,10 +540,10 @@ __device__ __forceinline__ void clmix_rows(const cg::cluster_group &cl, int n, i
         for (int t = 0; t < 2 * ND; ++t)
             y = __fmaf_rn(-u[t], pk - cl_pdir<FRESH>(rj[t], qj[t], pj[t], alpha, beta), y);
         qout[il] = y;
-        acc[0] += pk * y;
-        acc[1] += y * y;
-        acc[2] += rk * rk;
-        acc[3] += rk * y;
+        ff_dot_add(acc[0], pk, y);
+        ff_dot_add(acc[1], y, y);
+        ff_dot_add(acc[2], rk, rk);
+        ff_dot_add(acc[3], rk, y);
     }
 }
 
@@ -601,14 +640,14 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
     const float tolf = static_cast<float>(tol), deltaf = static_cast<float>(delta);
     int par = 1;
     if (!st.done) {
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
         clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, st.beta, xh, acc);
         FF t[4];
         cl_allreduce<4>(acc, t, sh, slot, cl, fresh_fin);
     }
     par = 0;
     while (!st.done) {
-        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        FF acc[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
         clmix_rows<ND, RPT, false>(cl, n, logR, row0, nr, A, off, base, par, st.alpha, st.beta, xh, acc);
         FF t[4];
         cl_allreduce<4>(acc, t, sh, slot, cl, [stp, tolf, deltaf, max_iter](const FF *tt, double *) {
@@ -679,7 +718,7 @@ __device__ __forceinline__ const ClMixState &cl_mixed_body(const cg::cluster_gro
             });
             if (st.done)
                 break;
-            float acc2[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+            FF acc2[4] = {ff_zero(), ff_zero(), ff_zero(), ff_zero()};
             clmix_rows<ND, RPT, true>(cl, n, logR, row0, nr, A, off, base, par, 0.0f, st.beta, xh, acc2);
             FF t4[4];
             cl_allreduce<4>(acc2, t4, sh, slot, cl, fresh_fin);
