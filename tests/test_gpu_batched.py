@@ -201,3 +201,37 @@ def test_cluster_route(sg, ctx, oracle, ctas, clusters):
     parts = [x[rows[i]:rows[i + 1]] for i in range(len(systems))]
     _check(oracle, systems, rhs, parts, stats, 1e-9)
     B.close()
+
+
+def test_step_counts_do_not_depend_on_engine_or_route(sg, ctx):
+    """The one-CTA queue and the cluster engine advance the same mixed CG
+    with float-float sums: every system takes the same number of steps
+    whether it runs on one CTA or on a cluster of 4, 8 or 16 CTAs, and the
+    solutions agree to rounding."""
+    from simall_gb300 import workloads as W
+
+    sides = [120, 96, 70, 64, 33]
+    systems = [W.cavity_pressure_matrix(sd, ctx) for sd in sides]
+    rng = np.random.default_rng(23)
+    rhs = []
+    for rp, _, _ in systems:
+        r = rng.standard_normal(len(rp) - 1)
+        rhs.append(r - r.mean())
+    b = np.concatenate(rhs)
+    counts, xs, on_clusters = [], [], []
+    for route in [(0, 8, 1), (4096, 4, 1), (4096, 8, 2), (4096, 16, 3)]:
+        B = sg.BatchedSolver(_cfg(sg), ctx=ctx)
+        B.set_systems(systems)
+        B.launch_shape(1024, 1)
+        B.cluster_route(*route)
+        x, stats = B.solve(b)
+        assert B.total.converged == len(sides)
+        counts.append(stats["iterations"].copy())
+        xs.append(x)
+        on_clusters.append(B.total.cluster_systems)
+        B.close()
+    assert on_clusters[0] == 0 and min(on_clusters[1:]) >= 3
+    for c in counts[1:]:
+        assert np.array_equal(c, counts[0]), (counts[0], c)
+    for x in xs[1:]:
+        assert np.linalg.norm(x - xs[0]) <= 1e-10 * np.linalg.norm(xs[0])
