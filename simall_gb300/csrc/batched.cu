@@ -237,10 +237,7 @@ template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const Batc
                 }
             }
         }
-        ff_block_allsum<4>(acc);
-        if (threadIdx.x == 0)
-            ms.finish_step(acc, tolf, deltaf, a.maxit);
-        __syncthreads();
+        ff_block_finish<4>(acc, [&](const FF (&t)[4]) { ms.finish_step(t, tolf, deltaf, a.maxit); });
         if (!ms.update)
             continue;
         // reliable update: x += S xh with the xh the triggering step wrote

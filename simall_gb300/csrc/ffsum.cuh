@@ -111,6 +111,32 @@ template <int NV> __device__ __forceinline__ void ff_block_allsum(FF (&v)[NV])
     __syncthreads();
 }
 
+// Sum of NV values over the block, handed to `fin(const FF (&tot)[NV])` in
+// thread 0, whose results every thread may read after the return: two block
+// barriers (ff_block_allsum followed by a barrier around thread 0's work
+// takes four).  Every thread must call it.
+template <int NV, class Fin> __device__ __forceinline__ void ff_block_finish(FF (&v)[NV], Fin fin)
+{
+    __shared__ FF ws[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; ++k) {
+        v[k] = ff_warp_allsum(v[k]);
+        if (lane == 0)
+            ws[k][wid] = v[k];
+    }
+    __syncthreads();
+    if (wid == 0) {
+        FF t[NV];
+#pragma unroll
+        for (int k = 0; k < NV; ++k)
+            t[k] = ff_warp_allsum(lane < nw ? ws[k][lane] : ff_zero());
+        if (lane == 0)
+            fin(t);
+    }
+    __syncthreads();
+}
+
 // Sum of the CTA slots part[c * NV + k], c < nslots, in a fixed order; the
 // result is in every thread.  Every thread must call it.
 template <int NV> __device__ __forceinline__ void ff_sum_slots(const FF *part, unsigned nslots, FF (&out)[NV])
