@@ -23,7 +23,10 @@
 // thread with spills, and at 512 threads a thread has 128.  A step's scalar
 // work is FP32 (ClMixState): with FP64 state and per-thread conversions of
 // alpha and beta, a step cost 1 us more at every size (3.2 against 2.2 us on
-// 2,025 rows; 6.2 against 5.2 us on 65,025).  The only waits are hardware
+// 2,025 rows; 6.2 against 5.2 us on 65,025, both with FP32 sums).  The step's
+// sums are float-float (cl_allreduce), at ~0.5 us per step and ~0.2 ns per
+// row of a slice more than FP32 sums (2.7 and 6.7 us on those systems), so
+// that the step count does not depend on the launch shape.  The only waits are hardware
 // cluster barriers, reached the same number of times by every CTA (the trip
 // count follows from the identical totals and is bounded by max_iter), so no
 // CTA can wait for one that has left.
