@@ -29,6 +29,7 @@
 // (after the fold x += S xh, and after the true residual with the FP32
 // replacement r = S (b - A x) written in the same pass).
 #include "device.cuh"
+#include "dia_step.cuh"
 #include "mixed_state.cuh"
 #include "sell.cuh"
 #include "solver.hpp"
@@ -359,6 +360,144 @@ __global__ void __launch_bounds__(kSellThreads, 1) k_mx_grid_solve(GridArgs g)
         st.publish(g.s, ok);
 }
 
+// ---------------------------------------------------------------- diagonal storage
+// The same solve for symmetric diagonal storage: the step of dia_step.cuh
+// (coherent vector loads), one CTA of kGridDiaThreads per SM.  The state is
+// r, q, p by step parity and one xh, as in the per-step engine: the first
+// step (FRESH, parity 1) reads r from r[0] and p_old = 0 from p[1]; after a
+// step of parity P asks for a reliable update, x += S xh, the replacement
+// S (b - A x) goes to r[1 - P] and a FRESH step of parity P follows.
+constexpr int kGridDiaThreads = 512;
+
+struct GridDiaDev {
+    int n;
+    int64_t ldU;
+    DiaOffsets o;
+    const float *U, *e;
+    float *rv[2], *qv[2], *pv[2], *xh;
+    const int32_t *rowPtr;
+    const int32_t *colIdx;
+    const double *val;
+    const double *b;
+    const double *sc;
+    double *x;
+    double *part;
+    unsigned long long *ctr;
+    int *err;
+    SolveScalars *s;
+    double tol, delta;
+    int max_iter;
+};
+
+// The FRESH step (the first one and one after each reliable update) out of
+// line, so that its copy of the step does not add to the registers of the
+// ordinary step's loop.
+template <int ND, bool GRID>
+__device__ __noinline__ void grid_dia_fresh(const GridDiaDev &g, const IterVecs &v, float beta, float (&acc)[4])
+{
+    dia_step<ND, GRID, true, true>(g.n, g.ldU, g.o, g.U, g.e, v, 0.0f, beta, acc);
+}
+
+template <int ND, bool GRID>
+__global__ void __launch_bounds__(kGridDiaThreads, 1) k_mx_grid_dia(GridDiaDev g)
+{
+    const int64_t n = g.n;
+    const int64_t tid = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t nthr = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    unsigned long long epoch = 0;
+    bool ok = true;
+
+    // init: x = 0, r[0] = S b, p[1] = 0, xh = 0; |S b|^2 (FP32 rows), |b|^2
+    double tot[2];
+    {
+        float a0 = 0.0f;
+        double a1 = 0.0;
+        for (int64_t i = tid; i < n; i += nthr) {
+            const double bi = g.b[i];
+            const float r = static_cast<float>(bi * g.sc[i]);
+            g.x[i] = 0.0;
+            g.rv[0][i] = r;
+            g.pv[1][i] = 0.0f;
+            g.xh[i] = 0.0f;
+            a0 += r * r;
+            a1 += bi * bi;
+        }
+        float f[1] = {a0};
+        double d1[1];
+        ok = grid_allsum_f<1>(f, d1, g.part, g.ctr, epoch, g.err);
+        double d2[1] = {a1};
+        ok = ok && grid_allsum<1>(d2, g.part, g.ctr, epoch, g.err);
+        tot[0] = d1[0];
+        tot[1] = d2[0];
+    }
+    __shared__ MixedState st;
+    if (threadIdx.x == 0)
+        st.start(tot[0], tot[1], g.tol, g.max_iter);
+    __syncthreads();
+    const int64_t trip_cap = 2 * static_cast<int64_t>(g.max_iter > 0 ? g.max_iter : 0) + 16;
+    const float tolf = static_cast<float>(g.tol), deltaf = static_cast<float>(g.delta);
+    for (int64_t trips = 0; ok && !st.done; ++trips) {
+        if (trips > trip_cap) {  // unreachable: every normal step counts and max_iter ends the solve
+            if (threadIdx.x == 0)
+                st.stop(SIMALL_ERR_TIMEOUT);
+            break;
+        }
+        // ---- one fused step
+        const int par = st.par;
+        const float alpha = st.fresh ? 0.0f : st.alpha_f, beta = st.beta_f;
+        const IterVecs v{g.rv[par], g.qv[par], g.pv[par], g.rv[1 - par], g.qv[1 - par], g.pv[1 - par], g.xh};
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+        if (st.fresh)
+            grid_dia_fresh<ND, GRID>(g, v, beta, acc);
+        else
+            dia_step<ND, GRID, false, true>(g.n, g.ldU, g.o, g.U, g.e, v, alpha, beta, acc);
+        FF facc[4] = {FF{acc[0], 0.0f}, FF{acc[1], 0.0f}, FF{acc[2], 0.0f}, FF{acc[3], 0.0f}};
+        if (!(ok = step_allsum(true, facc, g.part, g.ctr, epoch, g.err,
+                               [&](const FF (&t)[4]) { st.finish_step(t, tolf, deltaf, g.max_iter); })))
+            break;
+        if (!st.update)
+            continue;
+        // ---- reliable update: x += S xh with the xh the triggering step wrote
+        for (int64_t i = tid; i < n; i += nthr) {
+            g.x[i] += g.sc[i] * static_cast<double>(g.xh[i]);
+            g.xh[i] = 0.0f;
+        }
+        ++epoch;
+        if (!(ok = grid_barrier(g.ctr, epoch, g.err)))
+            break;
+        // r = b - A x in FP64 (one FMA per entry from 0.0 in column order, as
+        // the per-step engine's true residual; A streamed with the evict-first
+        // hint); the replacement S r (FP32) into the r the FRESH step reads;
+        // |r|^2 and |S r|^2
+        float *rrep = g.rv[1 - st.par];
+        double a[2] = {0.0, 0.0};
+        for (int64_t i = tid; i < n; i += nthr) {
+            const int k1 = __ldcs(g.rowPtr + i + 1);
+            double y = 0.0;
+            for (int k = __ldcs(g.rowPtr + i); k < k1; ++k)
+                y = __fma_rn(__ldcs(g.val + k), g.x[__ldcs(g.colIdx + k)], y);
+            const double r = g.b[i] - y;
+            const float f = static_cast<float>(g.sc[i] * r);
+            rrep[i] = f;
+            a[0] += r * r;
+            a[1] += static_cast<double>(f) * static_cast<double>(f);
+        }
+        if (!(ok = grid_allsum<2>(a, g.part, g.ctr, epoch, g.err)))
+            break;
+        if (threadIdx.x == 0)
+            st.finish_update(a, g.tol, g.max_iter);
+        __syncthreads();
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0)
+        st.publish(g.s, ok);
+}
+
+template <int ND> const void *grid_dia_kernel(bool grid)
+{
+    return grid ? reinterpret_cast<const void *>(k_mx_grid_dia<ND, true>)
+                : reinterpret_cast<const void *>(k_mx_grid_dia<ND, false>);
+}
+
 }  // namespace
 
 int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
@@ -414,6 +553,91 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
     void *args[] = {&g};
     cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kSellThreads), args, smem, ctx->stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        cudaGetLastError();
+        return 0;
+    }
+    ctx->launches.fetch_add(1, std::memory_order_relaxed);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaLaunchCooperativeKernel", __FILE__, __LINE__);
+        return 1;
+    }
+    int timed_out = 0;
+    e = cudaMemcpyAsync(&timed_out, a.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaMemcpyAsync", __FILE__, __LINE__);
+        return 1;
+    }
+    int st = solver_fetch_scalars(s);  // synchronises the stream
+    if (st) {
+        *status = st;
+        return 1;
+    }
+    s->engine = 2;
+    if (timed_out || s->h_scal->status == SIMALL_ERR_TIMEOUT) {
+        *status = fail(ctx, SIMALL_ERR_TIMEOUT, "mixed precision: a grid barrier of the persistent solve timed out");
+        return 1;
+    }
+    *status = s->h_scal->done ? SIMALL_OK : fail(ctx, SIMALL_ERR_CUDA, "persistent solve ended before its stop test");
+    return 1;
+}
+
+int grid_dia_solve(simall_solver *s, const GridDiaArgs &a, int *status)
+{
+    simall_context *ctx = s->ctx;
+    if (s->n <= 0 || s->n > INT32_MAX - 8 || s->cfg.check_interval > 0 || s->cfg.engine != SIMALL_ENGINE_AUTO ||
+        a.nd < 1 || a.nd > kGridDiaMaxDiags)
+        return 0;
+    int coop = 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device) != cudaSuccess || !coop)
+        return 0;
+    const void *fn = a.nd == 1   ? grid_dia_kernel<1>(a.grid)
+                     : a.nd == 2 ? grid_dia_kernel<2>(a.grid)
+                     : a.nd == 3 ? grid_dia_kernel<3>(a.grid)
+                                 : grid_dia_kernel<4>(a.grid);
+    int per_sm = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kGridDiaThreads, 0) != cudaSuccess ||
+        per_sm < 1) {
+        cudaGetLastError();
+        return 0;
+    }
+    // one CTA per SM, never more than there are quads of rows for
+    const int64_t quads = (s->n + 3) / 4;
+    const int64_t want = std::max<int64_t>(1, (quads + kGridDiaThreads - 1) / kGridDiaThreads);
+    const int grid = static_cast<int>(std::min<int64_t>(want, ctx->num_sms));
+    if (static_cast<size_t>(grid) * 2 * kSlot > a.partCap)
+        return 0;
+    GridDiaDev g{};
+    g.n = static_cast<int>(s->n);
+    g.ldU = a.ldU;
+    for (int d = 0; d < kMaxDiags; ++d)
+        g.o.off[d] = d < a.nd ? a.off[d] : 0;
+    g.o.nd = a.nd;
+    g.U = a.U;
+    g.e = a.e;
+    for (int k = 0; k < 2; ++k) {
+        g.rv[k] = a.rv[k];
+        g.qv[k] = a.qv[k];
+        g.pv[k] = a.pv[k];
+    }
+    g.xh = a.xh;
+    g.rowPtr = s->rowPtr;
+    g.colIdx = s->colIdx;
+    g.val = s->values;
+    g.b = s->b.p;
+    g.sc = a.scale;
+    g.x = s->x.p;
+    g.part = a.part;
+    g.ctr = a.ctr;
+    g.err = a.err;
+    g.s = s->scal.p;
+    g.tol = s->cfg.tolerance;
+    g.delta = s->cfg.reliable_delta;
+    g.max_iter = s->cfg.max_iterations;
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
+    void *args[] = {&g};
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kGridDiaThreads), args, 0, ctx->stream);
     if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
         cudaGetLastError();
         return 0;

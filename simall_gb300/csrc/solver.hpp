@@ -206,6 +206,27 @@ struct GridMixedArgs {
 };
 int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status);
 
+// The same persistent solve for symmetric diagonal storage (up to
+// kGridDiaMaxDiags upper diagonals), the state in separate r, q, p vectors
+// by step parity and one xh.  Returns 0 (not taken) or 1 with *status set.
+constexpr int kGridDiaMaxDiags = 4;
+struct GridDiaArgs {
+    int nd;
+    bool grid;  // offset 1 first, every other offset a multiple of 4
+    int32_t off[8];
+    int64_t ldU;
+    const float *U;  // [nd][ldU] upper diagonals of S A S
+    const float *e;  // row sums
+    const double *scale;
+    float *rv[2], *qv[2], *pv[2];
+    float *xh;
+    double *part;
+    size_t partCap;
+    unsigned long long *ctr;
+    int *err;
+};
+int grid_dia_solve(simall_solver *s, const GridDiaArgs &a, int *status);
+
 // GMRES(m) / BiCGSTAB (krylov.cu): solve from x = 0 into s->x; fills the
 // result fields of s->h_scal.
 int krylov_solve(simall_solver *s);

@@ -305,6 +305,30 @@ def test_cluster_engine_matches_kernels(sg, ctx, oracle, dims, prec):
         assert abs(res[0][0] - res[1][0]) <= 0.1 * res[1][0] + 2
 
 
+@pytest.mark.parametrize("dims", [(64, 64, 40), (61, 59, 40), (400, 400, 1)])
+def test_persistent_diagonal_engine_matches_kernels(sg, ctx, oracle, dims):
+    """Natural-order systems too large for one cluster (diagonal storage, 3-D
+    with offsets that are multiples of 4 and ones that are not, 2-D): the
+    persistent solve (engine 2) reaches the tolerance, checked by a host
+    residual, in a step count close to the per-step kernels'; the two
+    solutions agree to the tolerance."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=dims, renumber=False, amp=0.0, pressure_zones=(1,))
+    assert len(rhs) > 131072
+    res = {}
+    for engine in (0, 1):
+        s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-9, maxit=20000), precision=sg.Precision.MIXED, ctx=ctx, engine=engine)
+        x = np.zeros(len(rhs))
+        it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+        assert s.stats.engine == (2 if engine == 0 else 0)
+        tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+        assert s.stats.converged and tr < 1e-9
+        assert abs(tr - s.stats.true_residual) <= 1e-6 * tr
+        res[engine] = (it, x)
+        s.close()
+    assert abs(res[0][0] - res[1][0]) <= 0.1 * res[1][0] + 2
+    assert rel(res[0][1], res[1][1]) <= 1e-5
+
+
 def _nine_point(nx, ny, center=8.4):
     """2-D 9-point SPD stencil in natural order: four upper diagonals (1,
     nx - 1, nx, nx + 1), symmetric, diagonally dominant."""
