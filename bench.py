@@ -1013,6 +1013,7 @@ def run_ours(a, rank, world, local):
     mixed_ms, launches = timed(smx, xm, a.steps)
     st_mx = smx.stats
     mx_iters, mx_updates, mx_true = st_mx.iterations, st_mx.reliable_updates, st_mx.true_residual
+    mx_engine = int(st_mx.engine)
     fp64_ms, _ = timed(s64, x, a.fp64_steps)
     clocks = clk.stop()
     fp64_iters, fp64_res = s64.stats.iterations, s64.stats.true_residual
@@ -1058,6 +1059,11 @@ def run_ours(a, rank, world, local):
           "traffic": round(traffic) if traffic else None, "algorithmic_bytes": round(kern[dom]["bytes"]),
           "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum, 200^3 capture scaled by rows",
           "peak_source": f"{peak_kind} hbm_gbs"}
+    if mx_iters > 0:
+        # the same step inside the solve (reliable updates included)
+        us = mixed_ms * 1e3 / mx_iters
+        gbs = kern[dom]["bytes"] / (us * 1e-3) / 1e6
+        rl["in_solve"] = {"us_per_step": round(us, 2), "gbs": round(gbs, 1), "frac": round(gbs / peak, 4)}
 
     # e2e: C ABI with host buffers (matrix + b in, x out, setup inside); the
     # host arrays are pinned, as the contract's end-to-end step asks
@@ -1148,7 +1154,9 @@ def run_ours(a, rank, world, local):
         "config": {"workload": f"varcoef Poisson {a.n}^3 (k=exp(N(0,1)) harmonic faces, Dirichlet x=0), "
                                f"Jacobi-PCG to {a.tol:g}", "cells": int(mesh.n_cells), "nnz": int(ps.nnz),
                    "seed": SEED, "parallelism": f"replicas x{world}", "l2": "inputs larger than L2 (no flush)",
-                   "loop": "device graph loop" if a.check_interval <= 0 else f"host poll every {a.check_interval}"},
+                   "loop": ({2: "one persistent cooperative launch", 1: "one thread-block cluster"}.get(
+                       mx_engine, "device graph loop") if a.check_interval <= 0
+                       else f"host poll every {a.check_interval}")},
         "fp64": {"value": round(fp64_ms / 1e3, 6), "unit": "s", "iterations": int(fp64_iters),
                  "true_residual": fp64_res},
         "mixed": {"iterations": int(mx_iters), "reliable_updates": int(mx_updates), "true_residual": mx_true,

@@ -160,11 +160,12 @@ enum simall_solver_kind {
 
 /* SIMALL_ENGINE_AUTO: systems of up to 131,072 rows (Jacobi FP64, or mixed
  * precision in diagonal storage) run the whole solve on one thread-block
- * cluster; mixed precision in sliced storage (any pattern without diagonal
- * structure, e.g. RCM-renumbered meshes) runs the whole solve in one
- * persistent cooperative launch over all SMs; the rest, and any solver with
- * check_interval > 0, launch kernels per iteration (mixed precision: one
- * device-side graph loop).
+ * cluster; larger mixed-precision solves run the whole solve in one
+ * persistent cooperative launch over all SMs, in sliced storage (any pattern
+ * without diagonal structure, e.g. RCM-renumbered meshes) or in diagonal
+ * storage with up to four upper diagonals (natural-order structured grids);
+ * the rest, and any solver with check_interval > 0, launch kernels per
+ * iteration (mixed precision: one device-side graph loop).
  * SIMALL_ENGINE_KERNELS: always the per-iteration kernels. */
 enum simall_engine { SIMALL_ENGINE_AUTO = 0, SIMALL_ENGINE_KERNELS = 1 };
 
