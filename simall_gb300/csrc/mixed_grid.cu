@@ -1,4 +1,6 @@
-// Mixed-precision CG in one persistent cooperative launch (sliced storage).
+// Mixed-precision CG in one persistent cooperative launch: sliced storage
+// (k_mx_grid_solve, the TMA-staged step of sell.cuh) and symmetric diagonal
+// storage (k_mx_grid_dia, the step of dia_step.cuh).
 //
 // The per-step kernels of mixed.cu run one launch per CG step inside a
 // device-side graph loop; between two steps the graph pays a controller
@@ -22,7 +24,7 @@
 // only the matrix goes through the read-only path.
 //
 // The algorithm is the one of mixed.cu step for step (the fused step of
-// sell.cuh, van der Vorst-Ye reliable updates with the same trigger, the FP64
+// sell.cuh or dia_step.cuh, van der Vorst-Ye reliable updates with the same trigger, the FP64
 // true residual r = b - A x from the original CSR, the stop test on it), so
 // iteration counts and results agree with the per-step engine up to the
 // order of the FP32 partial sums.  A reliable update costs two more barriers
