@@ -8,8 +8,9 @@
 // 7 us on GB300 -- a quarter of a step at 128^3.  Here every CTA stays
 // resident for the whole solve (cudaLaunchCooperativeKernel guarantees that
 // all of them are), and a step ends in one grid barrier:
-//   - each CTA reduces its threads' four FP32 partial sums (FP64 across
-//     warps) and publishes them in slot [epoch & 1][cta] of a double buffer;
+//   - each CTA reduces its threads' four partial sums in float-float
+//     (mixed_state.cuh, ffsum.cuh) and publishes them in slot
+//     [epoch & 1][cta] of a double buffer;
 //   - thread 0 releases its CTA's writes and adds one to a 64-bit arrival
 //     counter, then polls it with acquire loads until all gridDim.x CTAs of
 //     this epoch have arrived (bounded: ~4 s by %globaltimer, then the CTA
@@ -24,10 +25,10 @@
 // only the matrix goes through the read-only path.
 //
 // The algorithm is the one of mixed.cu step for step (the fused step of
-// sell.cuh or dia_step.cuh, van der Vorst-Ye reliable updates with the same trigger, the FP64
-// true residual r = b - A x from the original CSR, the stop test on it), so
-// iteration counts and results agree with the per-step engine up to the
-// order of the FP32 partial sums.  A reliable update costs two more barriers
+// sell.cuh or dia_step.cuh, van der Vorst-Ye reliable updates with the same
+// trigger, the FP64 true residual r = b - A x from the original CSR, the stop
+// test on it), so iteration counts and results agree with the per-step engine
+// up to the order of the partial sums.  A reliable update costs two more barriers
 // (after the fold x += S xh, and after the true residual with the FP32
 // replacement r = S (b - A x) written in the same pass).
 #include "device.cuh"
