@@ -393,6 +393,28 @@ def test_mixed_max_iterations(sg, ctx, oracle, check_interval):
     assert abs(tr - s.stats.true_residual) <= 1e-6 * tr and tr < 1.0
 
 
+def test_persistent_diagonal_engine_limits(sg, ctx, oracle):
+    """The persistent diagonal-storage solve (a natural-order system above
+    the cluster limit): max_iterations bounds it as CGSolver's return value
+    with the folded FP64 x after that many steps; a zero right-hand side
+    returns x = 0 at once."""
+    m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 0, dims=(64, 64, 40), renumber=False, amp=0.0,
+                                                pressure_zones=(1,))
+    s = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-14, maxit=7), precision=sg.Precision.MIXED, ctx=ctx)
+    x = np.zeros(len(rhs))
+    it = s.solve(sg.CSRMatrix(rp, ci, v), rhs, x)
+    assert s.stats.engine == 2
+    assert it == 7 and not s.stats.converged and s.stats.iterations == 7
+    tr = np.linalg.norm(rhs - oracle.spmv(rp, ci, v, x)) / np.linalg.norm(rhs)
+    assert abs(tr - s.stats.true_residual) <= 1e-6 * tr and tr < 1.0
+    z = np.full(len(rhs), 7.0)
+    s2 = sg.GpuCGSolver(_cfg(sg, 0, tol=1e-8, maxit=100), precision=sg.Precision.MIXED, ctx=ctx)
+    it = s2.solve(sg.CSRMatrix(rp, ci, v), np.zeros(len(rhs)), z)
+    assert s2.stats.engine == 2 and it == 0 and s2.stats.converged and not z.any()
+    s.close()
+    s2.close()
+
+
 @pytest.mark.parametrize("bad", ["nan", "unsorted", "nodiag", "range", "rowptr"])
 def test_input_errors_are_reported(sg, ctx, oracle, bad):
     m, rp, ci, v, rhs, aP, phi = oracle_system(oracle, 4)
