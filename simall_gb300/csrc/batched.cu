@@ -140,25 +140,34 @@ struct BatchArgs {
 
 // The row-sum product of row i of one system: e_i p_i - sum_j N_ij (p_i -
 // p_j), N = S A S - I, with p_j formed again from the neighbour's previous
-// state (sell.cuh p_of: the owner's two roundings, the same bits).
+// state (sell.cuh p_of: the owner's two roundings, the same bits).  ND > 0:
+// ND stored diagonals; every coefficient and neighbour is loaded before the
+// first multiply (a neighbour outside [0, n) reads the row itself with a
+// zero coefficient, which adds nothing), so a row waits for one round of
+// loads instead of one per diagonal.  ND == 0: the system's off-diagonal CSR.
+template <int ND>
 __device__ __forceinline__ float batch_row(const BatchSys &S, const BatchArgs &a, const float4 *in, int i, float pi,
                                            float alpha, float beta)
 {
     const int n = S.n;
     float y = __ldg(a.e + S.row0 + i) * pi;
-    if (S.nd > 0) {
+    if constexpr (ND > 0) {
         const float *U = a.U + S.u0;
+        float u[2 * ND];
+        float4 g[2 * ND];
 #pragma unroll
-        for (int d = 0; d < kBatchDiags; ++d) {
-            if (d >= S.nd)
-                break;
+        for (int d = 0; d < ND; ++d) {
             const int off = S.off[d];
             const float *Ud = U + static_cast<int64_t>(d) * n;
-            if (i + off < n)
-                y = __fmaf_rn(-__ldg(Ud + i), pi - p_of(in[i + off], alpha, beta), y);
-            if (i - off >= 0)
-                y = __fmaf_rn(-__ldg(Ud + i - off), pi - p_of(in[i - off], alpha, beta), y);
+            const bool up = i + off < n, dn = i - off >= 0;
+            u[2 * d] = up ? __ldg(Ud + i) : 0.0f;
+            u[2 * d + 1] = dn ? __ldg(Ud + i - off) : 0.0f;
+            g[2 * d] = in[up ? i + off : i];
+            g[2 * d + 1] = in[dn ? i - off : i];
         }
+#pragma unroll
+        for (int t = 0; t < 2 * ND; ++t)
+            y = __fmaf_rn(-u[t], pi - p_of(g[t], alpha, beta), y);
     } else {
         const int32_t *rp = a.orow + S.orp0;
         const int32_t *cc = a.ocol + S.u0;
@@ -176,7 +185,7 @@ __device__ __forceinline__ float batch_row(const BatchSys &S, const BatchArgs &a
 // system belong to thread t; RPP of them are in flight at a time.  The
 // state of a step is written by the CTA's own threads in the previous step,
 // so plain loads after the block barrier see it.
-template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const BatchArgs &a, BatchOut *out)
+template <int RPP, int ND> __device__ void batch_solve_one(const BatchSys &S, const BatchArgs &a, BatchOut *out)
 {
     __shared__ MixedState ms;
     const int n = S.n, B = blockDim.x;
@@ -233,7 +242,7 @@ template <int RPP> __device__ void batch_solve_one(const BatchSys &S, const Batc
                 const int i = i0 + u * B;
                 if (i < n) {
                     const RowStep rs(o[u], alpha, beta);
-                    rs.finish(batch_row(S, a, in, i, rs.p, alpha, beta), outp + i, acc);
+                    rs.finish(batch_row<ND>(S, a, in, i, rs.p, alpha, beta), outp + i, acc);
                 }
             }
         }
@@ -289,7 +298,13 @@ template <int RPP> __global__ void __launch_bounds__(1024) k_batch_solve(BatchAr
             return;
         const int id = a.order[k];
         const BatchSys S = a.sys[id];
-        batch_solve_one<RPP>(S, a, a.out + id);
+        switch (S.nd) {  // the stored diagonals, fixed at compile time in the step
+        case 1: batch_solve_one<RPP, 1>(S, a, a.out + id); break;
+        case 2: batch_solve_one<RPP, 2>(S, a, a.out + id); break;
+        case 3: batch_solve_one<RPP, 3>(S, a, a.out + id); break;
+        case 4: batch_solve_one<RPP, 4>(S, a, a.out + id); break;
+        default: batch_solve_one<RPP, 0>(S, a, a.out + id); break;
+        }
     }
 }
 
