@@ -513,8 +513,8 @@ int autotune(simall_batch *B, const double *b)
         return SIMALL_OK;
     };
     // 1: the one-CTA shape with every system on the queue
-    const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1},
-                             {512, 2, 2},  {256, 4, 1},  {256, 4, 2},  {512, 1, 2}};
+    const int shapes[][3] = {{1024, 1, 1}, {1024, 1, 2}, {1024, 1, 4}, {512, 2, 1}, {512, 2, 2},
+                             {256, 4, 1},  {256, 4, 2},  {512, 1, 2},  {512, 1, 4}};
     for (const auto &sh : shapes) {
         const int st = trial(sh[0], sh[1], sh[2], 0, 0, 0);
         if (st)
@@ -527,13 +527,14 @@ int autotune(simall_batch *B, const double *b)
     for (const BatchSys &S : B->h_sys)
         nmax = std::max<int64_t>(nmax, S.nd >= 1 ? S.n : 0);
     // (rows, cluster CTAs, clusters); on the 512-system cavity batch of
-    // sides 32-256 the first takes 0.107 s against 0.188 s for the queue alone,
+    // sides 32-256 the first takes 0.098 s against 0.188 s for the queue alone,
     // and more clusters than these lose: 16-CTA clusters are placed a GPC
     // at a time and wait for one another, and every SM a cluster holds is
     // one the queue, which streams a system at a third of the SM-time a
     // cluster spends on it, does not have
-    const int routes[][3] = {{40960, 16, 5}, {40960, 16, 4}, {40960, 16, 6}, {49152, 16, 4}, {49152, 16, 3},
-                             {32768, 16, 5}, {40960, 8, 10}, {40960, 8, 12}, {32768, 8, 12}, {16384, 4, 16}};
+    const int routes[][3] = {{49152, 16, 4}, {49152, 16, 3}, {49152, 16, 5}, {57344, 16, 3}, {49152, 8, 8},
+                             {57344, 8, 6},  {40960, 16, 5}, {40960, 16, 4}, {40960, 16, 6}, {32768, 16, 5},
+                             {40960, 8, 10}, {40960, 8, 12}, {32768, 8, 12}, {16384, 4, 16}};
     for (const auto &r : routes) {
         if (nmax < r[0] || r[1] * r[2] >= ctx->num_sms)
             continue;
@@ -574,7 +575,7 @@ std::string batch_shape_key(simall_batch *B)
         if (c == '"' || c == '\\' || static_cast<unsigned char>(c) < 32)
             c = '_';
     char buf[256];
-    snprintf(buf, sizeof buf, "batch-fused-v4|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
+    snprintf(buf, sizeof buf, "batch-fused-v5|%s|sm%d|n%d|rows%lld|%016llx", name.c_str(), B->ctx->num_sms, B->nsys,
              static_cast<long long>(B->rows), static_cast<unsigned long long>(h));
     return buf;
 }

@@ -160,7 +160,7 @@ def test_autotuner_cache_across_batch_objects(sg, ctx, tmp_path):
     shape = (B1.total.block_threads, B1.total.ctas_per_sm, B1.total.rows_per_pass, B1.total.cluster_rows,
              B1.total.cluster_ctas, B1.total.clusters)
     doc = open(cache).read()
-    assert "batch-fused-v4|" in doc and f'"block_threads": {shape[0]}' in doc
+    assert "batch-fused-v5|" in doc and f'"block_threads": {shape[0]}' in doc
     B2 = sg.BatchedSolver(_cfg(sg), ctx=ctx)
     B2.autotune_cache(cache)
     B2.set_systems(systems)
