@@ -19,14 +19,18 @@
 // the row-sum product; the iteration state packed per row as one float4
 // (r, q, p, xh), double-buffered; FP64 scale, b and x.  Each step is the fused
 // single-pass step of the sliced engines (sell.cuh) with float-float sums and
-// one block reduction.
+// one block reduction; a CTA takes the step specialised for its system's
+// number of stored diagonals, so a row's coefficients and neighbours are all
+// loaded before its first multiply (the rows of a CTA's system live in L2,
+// and a row's time is its load latency).
 //
 // Systems of at least cluster_rows rows in diagonal storage run instead on
 // one thread-block cluster each (cluster.cu, k_cl_mixed_batch: vectors in the
 // cluster's shared memory), a fixed number of clusters striding through them
-// on reserved SMs while the one-CTA queue runs the rest on the other SMs; a
-// single SM streams a 65,025-row system at ~47 GB/s, 0.12 s for its ~2000
-// steps, a 16-CTA cluster solves it in ~12 ms.  The one-CTA shape (threads,
+// on reserved SMs while the one-CTA queue runs the rest on the other SMs: one
+// SM took 0.12 s for the ~2000 steps of a 65,025-row system before the
+// specialised step (about 47 GB/s), a 16-CTA cluster takes ~13 ms.  The
+// one-CTA shape (threads,
 // CTAs per SM, rows in flight per thread) and the cluster route (row
 // threshold, cluster size, clusters) are picked by an autotuner that times
 // candidates on the batch itself and keeps its choice in a JSON cache
