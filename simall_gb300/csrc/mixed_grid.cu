@@ -501,6 +501,48 @@ template <int ND> const void *grid_dia_kernel(bool grid)
                 : reinterpret_cast<const void *>(k_mx_grid_dia<ND, false>);
 }
 
+// The cooperative launch of a whole persistent solve and its verdict: 0 when
+// the launch is refused (too large for the device, or no cooperative
+// launch), else 1 with *status: the launch error, a grid barrier's timeout,
+// or whether the solve reached its stop test.  `args` points to the kernel's
+// one argument struct; ctr and err are reset first.
+int launch_persistent(simall_solver *s, const void *fn, int grid, int threads, size_t smem, void *args,
+                      unsigned long long *ctr, int *err, int *status)
+{
+    simall_context *ctx = s->ctx;
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), ctx->stream));
+    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(int), ctx->stream));
+    void *argv[] = {args};
+    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(threads), argv, smem, ctx->stream);
+    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
+        cudaGetLastError();
+        return 0;
+    }
+    ctx->launches.fetch_add(1, std::memory_order_relaxed);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaLaunchCooperativeKernel", __FILE__, __LINE__);
+        return 1;
+    }
+    int timed_out = 0;
+    e = cudaMemcpyAsync(&timed_out, err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e != cudaSuccess) {
+        *status = cuda_fail(ctx, e, "cudaMemcpyAsync", __FILE__, __LINE__);
+        return 1;
+    }
+    int st = solver_fetch_scalars(s);  // synchronises the stream
+    if (st) {
+        *status = st;
+        return 1;
+    }
+    s->engine = 2;
+    if (timed_out || s->h_scal->status == SIMALL_ERR_TIMEOUT) {
+        *status = fail(ctx, SIMALL_ERR_TIMEOUT, "mixed precision: a grid barrier of the persistent solve timed out");
+        return 1;
+    }
+    *status = s->h_scal->done ? SIMALL_OK : fail(ctx, SIMALL_ERR_CUDA, "persistent solve ended before its stop test");
+    return 1;
+}
+
 }  // namespace
 
 int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
@@ -552,37 +594,7 @@ int grid_mixed_solve(simall_solver *s, const GridMixedArgs &a, int *status)
     g.tol = s->cfg.tolerance;
     g.delta = s->cfg.reliable_delta;
     g.max_iter = s->cfg.max_iterations;
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
-    void *args[] = {&g};
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kSellThreads), args, smem, ctx->stream);
-    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
-        cudaGetLastError();
-        return 0;
-    }
-    ctx->launches.fetch_add(1, std::memory_order_relaxed);
-    if (e != cudaSuccess) {
-        *status = cuda_fail(ctx, e, "cudaLaunchCooperativeKernel", __FILE__, __LINE__);
-        return 1;
-    }
-    int timed_out = 0;
-    e = cudaMemcpyAsync(&timed_out, a.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e != cudaSuccess) {
-        *status = cuda_fail(ctx, e, "cudaMemcpyAsync", __FILE__, __LINE__);
-        return 1;
-    }
-    int st = solver_fetch_scalars(s);  // synchronises the stream
-    if (st) {
-        *status = st;
-        return 1;
-    }
-    s->engine = 2;
-    if (timed_out || s->h_scal->status == SIMALL_ERR_TIMEOUT) {
-        *status = fail(ctx, SIMALL_ERR_TIMEOUT, "mixed precision: a grid barrier of the persistent solve timed out");
-        return 1;
-    }
-    *status = s->h_scal->done ? SIMALL_OK : fail(ctx, SIMALL_ERR_CUDA, "persistent solve ended before its stop test");
-    return 1;
+    return launch_persistent(s, fn, grid, kSellThreads, smem, &g, a.ctr, a.err, status);
 }
 
 int grid_dia_solve(simall_solver *s, const GridDiaArgs &a, int *status)
@@ -637,37 +649,7 @@ int grid_dia_solve(simall_solver *s, const GridDiaArgs &a, int *status)
     g.tol = s->cfg.tolerance;
     g.delta = s->cfg.reliable_delta;
     g.max_iter = s->cfg.max_iterations;
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.ctr, 0, sizeof(unsigned long long), ctx->stream));
-    SIMALL_CUDA_TRY(ctx, cudaMemsetAsync(a.err, 0, sizeof(int), ctx->stream));
-    void *args[] = {&g};
-    cudaError_t e = cudaLaunchCooperativeKernel(fn, dim3(grid), dim3(kGridDiaThreads), args, 0, ctx->stream);
-    if (e == cudaErrorCooperativeLaunchTooLarge || e == cudaErrorNotSupported) {
-        cudaGetLastError();
-        return 0;
-    }
-    ctx->launches.fetch_add(1, std::memory_order_relaxed);
-    if (e != cudaSuccess) {
-        *status = cuda_fail(ctx, e, "cudaLaunchCooperativeKernel", __FILE__, __LINE__);
-        return 1;
-    }
-    int timed_out = 0;
-    e = cudaMemcpyAsync(&timed_out, a.err, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
-    if (e != cudaSuccess) {
-        *status = cuda_fail(ctx, e, "cudaMemcpyAsync", __FILE__, __LINE__);
-        return 1;
-    }
-    int st = solver_fetch_scalars(s);  // synchronises the stream
-    if (st) {
-        *status = st;
-        return 1;
-    }
-    s->engine = 2;
-    if (timed_out || s->h_scal->status == SIMALL_ERR_TIMEOUT) {
-        *status = fail(ctx, SIMALL_ERR_TIMEOUT, "mixed precision: a grid barrier of the persistent solve timed out");
-        return 1;
-    }
-    *status = s->h_scal->done ? SIMALL_OK : fail(ctx, SIMALL_ERR_CUDA, "persistent solve ended before its stop test");
-    return 1;
+    return launch_persistent(s, fn, grid, kGridDiaThreads, 0, &g, a.ctr, a.err, status);
 }
 
 }  // namespace simall
